@@ -1,0 +1,425 @@
+#!/usr/bin/env python
+"""Benchmark of the Phase pressure solve on one GB300.
+
+Workload: the 1024x1024 rising-bubble pressure system (1,048,576 cells,
+5,238,784 nonzeros, dt/rho face coefficients with 1000x contrast, p fixed on
+y+ and normal-gradient elsewhere, rhs = src::div(u*) of a seeded divergent
+velocity), solved to ||b - A x||_2/||b||_2 <= 1e-8 in FP64 from a zero guess.
+
+One step = device assembly of fv::laplacian(dt/rho, p) == src::div(u*) +
+hand-over to the solver (value permutation) + ILU(0) factorisation +
+BiCGStab to 1e-8 + true-residual check, inputs resident in HBM.
+`e2e` times the same solve through the reference-facing call sequence of
+FiniteVolumeEquation::solve (setRank, set(rowPtr, colInd, vals) with
+CrsEquation's 5-slot layout, setRhs, solve, x) with host buffers.
+
+--impl reference times the CPU implementation of the same solve (the
+oracle's OpenMP BiCGStab with one ILU(0) subdomain per thread -- Ifpack2
+Schwarz/RILUK as run on that many MPI ranks) on a bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+METRIC = ("ms per pCorr solve to 1e-8 rel. residual: plain FP64 vs "
+          "learned+mixed, GB300")
+WORKLOAD = "rising-bubble pressure system 1024x1024 (1M cells, nnz 5238784)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=1024)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--subdomain-rows", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}",
+                 f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[3:7]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------- CPU solve
+def cpu_solve_sample(rp, ci, v, b, seconds, threads):
+    """Time the oracle's BiCGStab + Schwarz-ILU(0) (one contiguous block per
+    thread) on a bounded sample; returns (ms per solve, info)."""
+    import numpy as np
+    import oracle_bind as ob
+    n = b.size
+    part = (np.arange(n, dtype=np.int64) * threads // n).astype(np.int32)
+    h, ms, sms = ob.bicgstab_history(rp, ci, v, b, 5, part=part,
+                                     threads=threads)
+    per_iter = ms / max(1, len(h) - 1)
+    budget = int(max(20, min(20000, seconds * 1000.0 / max(per_iter, 1e-3))))
+    h, ms, sms = ob.bicgstab_history(rp, ci, v, b, budget, part=part,
+                                     threads=threads)
+    its = len(h) - 1
+    per_iter = ms / max(1, its)
+    hit = np.flatnonzero(h <= 1e-8)
+    if hit.size:
+        need = int(hit[0])
+        how = f"ran to 1e-8 in {need} iterations"
+    else:
+        k0 = its // 2
+        rate = (h[its] / h[k0]) ** (1.0 / max(1, its - k0))
+        need = int(its + math.ceil(math.log(1e-8 / h[its]) / math.log(rate))) \
+            if 0 < rate < 1 else -1
+        how = (f"ran {its} iterations ({h[its]:.2e} rel. residual), "
+               f"extrapolated to 1e-8 at {need} iterations from the "
+               f"residual decay rate {rate:.5f}/iteration")
+    value = sms + per_iter * need if need > 0 else float("nan")
+    return value, dict(iterations=need, ms_per_iter=per_iter, setup_ms=sms,
+                       sample=how)
+
+
+def build_system(nx, want_device=True):
+    import numpy as np
+    import phase_gb300 as pg
+    from phase_gb300 import workloads
+    w = workloads.rising_bubble(nx, nx, seed=3)
+    mesh = pg.Mesh(w["nodes"], w["cptr"], w["cind"])
+    w = workloads.rising_bubble(nx, nx, seed=3, faces=mesh.faces(),
+                                cells=mesh.cells())
+    coeff = mesh.dt_over_rho(w["gamma"], w["rho1"], w["rho2"], w["dt"])
+    return mesh, w, coeff
+
+
+def slots_layout(rp, ci, v):
+    """Expand a compact CSR into CrsEquation's layout: 5 slots per row (more
+    when a row is longer), unused slots with column -1
+    (CrsEquation.cpp:159-164)."""
+    import numpy as np
+    n = len(rp) - 1
+    cnt = np.diff(rp)
+    width = np.maximum(cnt, 5)
+    srp = np.zeros(n + 1, np.int32)
+    np.cumsum(width, out=srp[1:])
+    sci = np.full(srp[-1], -1, np.int32)
+    sv = np.zeros(srp[-1])
+    rows = np.repeat(np.arange(n), cnt)
+    pos = srp[rows] + (np.arange(len(ci)) - rp[rows])
+    sci[pos] = ci
+    sv[pos] = v
+    return srp, sci, sv
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import phase_gb300 as pg
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+
+    nx = args.nx
+    mesh, w, coeff = build_system(nx)
+    n = mesh.n_cells
+    dev = torch.device("cuda", local)
+    d_coeff = torch.from_numpy(coeff).to(dev)
+    d_bv = torch.from_numpy(w["bc_value"]).to(dev)
+    d_u = torch.from_numpy(np.ascontiguousarray(w["u"]).ravel()).to(dev)
+    eqn = pg.Equation(mesh, pg.GAMMA_FACE, w["bc_type"])
+    prec = pg.MIXED if args.precision == "mixed" else pg.FP64
+    solver = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
+                                   precision=prec,
+                                   subdomain_rows=args.subdomain_rows)
+    stream = torch.cuda.ExternalStream(pg.stream_handle(), device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        eqn.assemble_device(gamma_face=d_coeff.data_ptr(),
+                            bc_value=d_bv.data_ptr(), u_face=d_u.data_ptr())
+        solver.set_eqn(eqn)
+        solver.setGuess(None)
+        solver.solve()
+        return solver.stats.as_dict()
+
+    for _ in range(max(3, args.warmup)):
+        st = step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    stats = []
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = pg.kernel_launches()
+    clocks.start()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))          # L2 flush (256 MB > 129 MB L2)
+            ev[k][0].record(stream)
+        stats.append(step())
+        with torch.cuda.stream(stream):
+            ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    launches = pg.kernel_launches() - launches0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t[0])
+
+    # kernel-level roofline on the same system
+    prof = solver.profile(reps=50)
+    a_nnz = int(eqn.nnz)
+    # compulsory bytes per launch
+    b_spmv = 12 * a_nnz + 4 * (n + 1) + 8 * n * 3          # A, x, rhat, v
+    b_prec = 12 * a_nnz + 8 * n + 8 * n + 8 * n * 5        # LU, rp/dg, dinv, r p v in, p z out
+    b_upd = 8 * n * 9                                       # x r ph sh s t rh in; x r out
+    iters = max(1, stats[-1]["iters"])
+    shares = {"spmv": 2 * prof["spmv"], "ilu_apply": 2 * prof["precond"],
+              "update": prof["update"]}
+    dom = max(shares, key=shares.get)
+    bytes_of = {"spmv": b_spmv, "ilu_apply": b_prec, "update": b_upd}
+    ms_of = {"spmv": prof["spmv"], "ilu_apply": prof["precond"],
+             "update": prof["update"]}
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_of[dom] / (ms_of[dom] * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
+                "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "algorithmic_bytes": bytes_of[dom],
+                "launch_ms": round(ms_of[dom], 5),
+                "per_kernel_gbs": {k: round(bytes_of[k] / (ms_of[k] * 1e-3) / 1e9, 1)
+                                   for k in bytes_of},
+                "frac_of_8tbs": round(achieved / 8000.0, 4)}
+
+    # e2e through the reference-facing call sequence with host buffers
+    e2e = None
+    if not args.no_e2e:
+        rp, ci, v, rhs = eqn.export()
+        srp, sci, sv = slots_layout(rp, ci, v)
+        pin = lambda a: torch.from_numpy(a).pin_memory().numpy()
+        srp, sci, sv, b = pin(srp), pin(sci), pin(sv), pin(-rhs)
+        xh = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
+        s2 = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
+                                   precision=prec,
+                                   subdomain_rows=args.subdomain_rows)
+
+        def e2e_step():
+            s2.setRank(n)
+            s2.set(srp, sci, sv)
+            s2.setRhs(b)
+            s2.setGuess(None)
+            s2.solve()
+            xh[:] = s2.x()
+            return s2.stats.as_dict()
+
+        for _ in range(2):
+            e2e_step()
+        times = []
+        for _ in range(max(1, min(args.steps, 3))):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            e2e_st = e2e_step()
+            times.append((time.perf_counter() - t1) * 1e3)
+        e2e = {"value": round(sum(times) / len(times), 3), "unit": "ms",
+               "h2d_bytes_per_step": int(srp.nbytes + sci.nbytes + sv.nbytes
+                                         + b.nbytes),
+               "d2h_bytes_per_step": int(xh.nbytes),
+               "iters": e2e_st["iters"], "rel_residual": e2e_st["rel_residual"],
+               "path": "setRank + set(rowPtr, colInd[-1 slots], vals) + setRhs"
+                       " + solve + x() via the C ABI, pinned host buffers"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rp, ci, v, rhs = eqn.export()
+        threads = len(os.sched_getaffinity(0))
+        val, info = cpu_solve_sample(rp, ci, v, -rhs, args.cpu_seconds,
+                                     threads)
+        cpu = {"value": round(val, 1), "unit": "ms", "cores": threads,
+               "kind": "port",
+               "sample": f"oracle BiCGStab + Schwarz-ILU(0), {threads} "
+                         f"subdomains, FP64, same system, zero guess: "
+                         + info["sample"],
+               "iterations": info["iterations"],
+               "ms_per_iter": round(info["ms_per_iter"], 3)}
+
+    if rank == 0:
+        last = stats[-1]
+        out = {
+            "metric": METRIC, "value": round(ms, 3), "unit": "ms",
+            "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
+            "ms_per_step": round(ms, 3), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype":
+                "f64" if prec == pg.FP64 else "f32-inner/f64-refined",
+            "data": "synthetic (seeded rising-bubble fields, no dataset)",
+            "config": {"workload": WORKLOAD, "n_cells": n, "nnz": a_nnz,
+                       "precision": args.precision,
+                       "preconditioner": "Schwarz ILU(0), "
+                       f"{solver.partition()[1]} subdomains",
+                       "tolerance": 1e-8, "guess": "zero",
+                       "l2": "256 MB flush write before every step; working "
+                             "set > 129 MB L2"},
+            "iters": last["iters"], "rel_residual": last["rel_residual"],
+            "solve_ms": round(last["ms"], 3),
+            "factor_ms": round(last["setup_ms"], 3),
+            "ms_per_iter": round(last["ms"] / iters, 4),
+            "step_ms_all": [round(x, 3) for x in step_ms],
+            "solves_per_s": round(1000.0 / ms * world, 2),
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(launches), "clocks": clk,
+            "wall_s": round(wall, 3),
+        }
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(args):
+    """CPU implementation of the same solve (the oracle), all host threads."""
+    import numpy as np
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle_bind as ob
+    from phase_gb300 import workloads
+    ob.lib()
+    nx = args.nx
+    w = workloads.rising_bubble(nx, nx, seed=3)
+    om = ob.OracleMesh(w["nodes"], w["cptr"], w["cind"])
+    w = workloads.rising_bubble(nx, nx, seed=3, faces=om.faces(),
+                                cells=om.cells())
+    coeff = om.dt_over_rho(w["gamma"], w["rho1"], w["rho2"], w["dt"])
+    rp, ci, v, rhs = om.laplacian(coeff, w["bc_type"], w["bc_value"], w["u"])
+    threads = len(os.sched_getaffinity(0))
+    vals = []
+    info = None
+    per_step_seconds = max(2.0, args.cpu_seconds / max(1, args.steps))
+    for _ in range(args.steps):
+        val, info = cpu_solve_sample(rp, ci, v, -rhs, per_step_seconds, threads)
+        vals.append(val)
+    value = float(np.median(vals))
+    out = {
+        "metric": METRIC, "value": round(value, 1), "unit": "ms",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(value, 1), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded rising-bubble fields, no dataset)",
+        "config": {"workload": WORKLOAD, "n_cells": int(om.n_cells),
+                   "nnz": int(len(ci)), "precision": "fp64",
+                   "preconditioner": f"Schwarz ILU(0), {threads} subdomains",
+                   "tolerance": 1e-8, "guess": "zero"},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(value, 1), "unit": "ms",
+                         "cores": threads, "kind": "port",
+                         "sample": info["sample"]},
+        "e2e": {"value": round(value, 1), "unit": "ms",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,222 @@
+/*
+ * phase_gb300 -- GB300 (sm_103a) pressure assembly + BiCGStab/ILU solve for
+ * the Phase 2D unstructured finite-volume solver.
+ *
+ * C ABI: plain pointers and sizes, opaque handles, int status codes.  No C++
+ * exceptions cross this boundary.  Host buffers are owned by the caller;
+ * device buffers are owned by the library.  A handle is not thread-safe: one
+ * host thread drives it at a time, as Phase's single-threaded ranks do.
+ * All work of the library is issued on one CUDA stream (pg_stream()).
+ *
+ * Reference interfaces each entry point replaces are cited as file:line
+ * within the obrienadam/Phase source tree.
+ */
+#ifndef PHASE_GB300_H
+#define PHASE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define PG_OK 0
+#define PG_MAX_ITERS 1   /* solve stopped at max iterations */
+#define PG_BREAKDOWN 2   /* BiCGStab breakdown (rho or <t,t> = 0) or zero pivot */
+#define PG_NON_FINITE 3  /* NaN/Inf in the inputs or the iteration */
+#define PG_BAD_ARG 4     /* invalid argument / size / handle */
+#define PG_TIMEOUT 5     /* a bounded device wait ran out */
+#define PG_CUDA_ERROR 6  /* a CUDA runtime call failed */
+
+/* where a pointer argument lives */
+#define PG_HOST 0
+#define PG_DEVICE 1
+
+/* boundary types, FiniteVolumeField<T>::BoundaryType
+ * (src/2D/Unstructured/FiniteVolume/Field/FiniteVolumeField.h) */
+#define PG_BC_FIXED 0
+#define PG_BC_NORMAL_GRADIENT 1
+#define PG_BC_SYMMETRY 2
+
+/* which fv::laplacian overload an equation is assembled by */
+#define PG_GAMMA_SCALAR 0 /* fv::laplacian(Scalar, phi)   Laplacian.h:49-83  */
+#define PG_GAMMA_FACE 1   /* fv::laplacian(field, phi)    Laplacian.h:132-167 */
+
+/* preconditioners */
+#define PG_PREC_NONE 0
+#define PG_PREC_JACOBI 1
+#define PG_PREC_ILU0 2 /* additive Schwarz (overlap 0) with ILU(0) blocks, as
+                          Ifpack2 "schwarz" + "RILUK" level-of-fill 0
+                          (TrilinosBelosSparseMatrixSolver.cpp:63-85) */
+
+/* arithmetic of the Krylov iteration */
+#define PG_FP64 0
+#define PG_MIXED 1 /* FP32 inner BiCGStab + ILU inside FP64 refinement */
+
+typedef struct pg_mesh pg_mesh;
+typedef struct pg_eqn pg_eqn;
+typedef struct pg_solver pg_solver;
+
+/* Last error message of the calling thread (never NULL). */
+const char *pg_last_error(void);
+
+/* The CUDA stream (cudaStream_t) all library work is issued on. */
+void *pg_stream(void);
+
+/* Blocks until all library work issued so far has finished. */
+int pg_synchronize(void);
+
+/* ------------------------------------------------------------------------
+ * Mesh.  Replaces FiniteVolumeGrid2D::init(nodes, cptr, cind, origin)
+ * (src/2D/Unstructured/FiniteVolumeGrid2D/FiniteVolumeGrid2D.cpp:20-35),
+ * createCell (:84-114) and the link set-up of init() (:396-450): faces are
+ * numbered in cell order by node-pair de-duplication, the first cell that
+ * meets a face is its lCell, links are kept in face-id order.
+ * nodes_xy[2*n_nodes], cptr[n_cells+1], cind[cptr[n_cells]] (host).
+ * ---------------------------------------------------------------------- */
+int pg_mesh_create(const double *nodes_xy, int64_t n_nodes,
+                   const int64_t *cptr, const int64_t *cind, int64_t n_cells,
+                   pg_mesh **out);
+int pg_mesh_destroy(pg_mesh *m);
+int pg_mesh_sizes(const pg_mesh *m, int64_t *n_cells, int64_t *n_faces,
+                  int64_t *n_interior, int64_t *n_boundary);
+/* Face data (host copies), face-id order: owner/neighbour cells (rcell = -1
+ * on boundary faces), centroid and normal (Face.cpp:9-18). Any may be NULL. */
+int pg_mesh_faces(const pg_mesh *m, int32_t *lcell, int32_t *rcell,
+                  double *fx, double *fy, double *nx, double *ny);
+/* Cell centroids and volumes (Cell.cpp:8-29). Any may be NULL. */
+int pg_mesh_cells(const pg_mesh *m, double *cx, double *cy, double *vol);
+
+/* ------------------------------------------------------------------------
+ * Pressure equation on the device.  A pg_eqn is a FiniteVolumeEquation<Scalar>
+ * (src/2D/Unstructured/FiniteVolume/Equation/FiniteVolumeEquation.h:14-98)
+ * whose CSR lives in HBM.  Its sparsity pattern is that of CrsEquation after
+ * fv::laplacian (CrsEquation.cpp:159-164,263-281): placeholder slots dropped,
+ * entries in order of first addCoeff.  bc_type[n_faces] (host) fixes the
+ * boundary type of each boundary face for the life of the equation.
+ * ---------------------------------------------------------------------- */
+int pg_eqn_create(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
+                  pg_eqn **out);
+int pg_eqn_destroy(pg_eqn *e);
+int pg_eqn_sizes(const pg_eqn *e, int64_t *n_rows, int64_t *nnz);
+
+/* fv::laplacian(gamma, p) == src::div(u) assembled on the device by the
+ * face-coloured kernels.  Replaces Laplacian.h:49-83 (gamma_face == NULL,
+ * scalar gamma) or :132-167 (gamma_face[n_faces]), Source.cpp:5-21
+ * (u_face_xy[2*n_faces], NULL = no divergence source) and
+ * CrsEquation::operator==(Vector) (CrsEquation.cpp:459-461).
+ * bc_value[n_faces] holds phi on FIXED boundary faces (may be NULL when no
+ * face is FIXED).  ptr_kind says where the arrays live. */
+int pg_assemble_laplacian(pg_eqn *e, const double *gamma_face,
+                          double gamma_scalar, const double *bc_value,
+                          const double *u_face_xy, int ptr_kind);
+
+/* Copy the assembled CSR + rhs_ (the equation's own right-hand side; the
+ * solver receives -rhs_, FiniteVolumeEquation.tpp:179) to host buffers.
+ * row_ptr[n+1], col_ind[nnz], vals[nnz], rhs[n]; any may be NULL. */
+int pg_eqn_export(const pg_eqn *e, int32_t *row_ptr, int32_t *col_ind,
+                  double *vals, double *rhs);
+
+/* Face coefficient timeStep / rho_f with rho_f = rho1 + clamp(gamma_f,0,1)
+ * (rho2 - rho1) and gamma_f the distance-weighted face interpolation of the
+ * cell volume fraction (FractionalStepMultiphase.cpp:175-185,
+ * FiniteVolumeField.tpp:130-162, ScalarFiniteVolumeField.cpp:75-86).
+ * Boundary faces take the owner cell's value (normal-gradient gamma).
+ * gamma_cell[n_cells] in, coeff_face[n_faces] out. */
+int pg_face_dt_over_rho(const pg_mesh *m, const double *gamma_cell,
+                        double rho1, double rho2, double dt,
+                        double *coeff_face, int ptr_kind);
+
+/* ScalarGradient::computeFaces + compute(FACE_TO_CELL)
+ * (src/2D/Unstructured/FiniteVolume/Field/ScalarGradient.cpp:34-74).
+ * phi_cell[n_cells], phi_face[n_faces] (boundary values) in;
+ * grad_face[2*n_faces], grad_cell[2*n_cells] out (either may be NULL). */
+int pg_gradient(const pg_mesh *m, const double *phi_cell,
+                const double *phi_face, double *grad_face, double *grad_cell,
+                int ptr_kind);
+
+/* ------------------------------------------------------------------------
+ * Sparse solver.  Replaces the SparseMatrixSolver plugin
+ * (src/Math/SparseMatrixSolver.h:11-62) as driven by
+ * FiniteVolumeEquation<T>::solve (FiniteVolumeEquation.tpp:171-192), with
+ * the semantics of the Belos BiCGStab + Ifpack2 right preconditioner backend
+ * (TrilinosBelosSparseMatrixSolver.cpp:18-99, TrilinosSparseMatrixSolver.cpp
+ * :23-112).
+ * ---------------------------------------------------------------------- */
+typedef struct {
+  double tolerance;   /* ||b - A x||_2 / ||b||_2 target (Belos default 1e-8) */
+  int max_iters;      /* Belos default 500 */
+  int precond;        /* PG_PREC_* */
+  int subdomain_rows; /* target rows per Schwarz subdomain; 0 = default;
+                         -1 = one subdomain (global ILU(0)) */
+  int precision;      /* PG_FP64 | PG_MIXED */
+  int inner_max_iters;     /* PG_MIXED: inner iterations per refinement step */
+  double inner_tolerance;  /* PG_MIXED: inner relative residual target */
+} pg_solver_cfg;
+
+typedef struct {
+  int iters;           /* BiCGStab iterations (inner iterations if mixed) */
+  int outer_iters;     /* refinement steps (mixed) or restarts + 1 */
+  int status;          /* PG_OK, PG_MAX_ITERS, PG_BREAKDOWN, PG_NON_FINITE */
+  double rel_residual; /* true ||b - A x||_2 / ||b||_2 computed in FP64 */
+  double ms;           /* device time of the solve (CUDA events) */
+  double setup_ms;     /* device time of the value permutation + ILU factor */
+} pg_solve_stats;
+
+/* Defaults: tolerance 1e-8, max_iters 500, ILU(0) Schwarz, FP64. */
+void pg_solver_default_cfg(pg_solver_cfg *cfg);
+int pg_solver_create(const pg_solver_cfg *cfg, pg_solver **out);
+int pg_solver_destroy(pg_solver *s);
+
+/* SparseMatrixSolver::setRank(int) (SparseMatrixSolver.h:23). */
+int pg_solver_set_rank(pg_solver *s, int64_t n);
+
+/* SparseMatrixSolver::set(rowPtr, colInds, vals) (SparseMatrixSolver.h
+ * :32-34).  Negative column indices are CrsEquation placeholders and are
+ * skipped; repeated columns in a row are summed.  row_ptr[n+1],
+ * col_ind[row_ptr[n]], vals[row_ptr[n]] in ptr_kind memory.  The sparsity
+ * analysis (Schwarz partition, level schedule) is redone only when the
+ * pattern differs from the previous call's. */
+int pg_solver_set_csr(pg_solver *s, const int32_t *row_ptr,
+                      const int32_t *col_ind, const double *vals,
+                      int ptr_kind);
+
+/* Take the matrix and -rhs_ of a device equation without a host round trip
+ * (the device form of FiniteVolumeEquation::solve's set + setRhs). */
+int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e);
+
+/* SparseMatrixSolver::setRhs (receives the already negated rhs) and
+ * setGuess (SparseMatrixSolver.h:38-40).  rhs[n], x0[n]; x0 == NULL sets a
+ * zero initial guess. */
+int pg_solver_set_rhs(pg_solver *s, const double *rhs, int ptr_kind);
+int pg_solver_set_guess(pg_solver *s, const double *x0, int ptr_kind);
+
+/* SparseMatrixSolver::solve (SparseMatrixSolver.h:42): factor the
+ * preconditioner and iterate from the current guess (the previous solution
+ * unless set_guess was called, as Belos' warm start).  Blocks until done. */
+int pg_solver_solve(pg_solver *s, pg_solve_stats *stats);
+
+/* SparseMatrixSolver::x(i) for all i (SparseMatrixSolver.h:48). x[n]. */
+int pg_solver_get_x(const pg_solver *s, double *x, int ptr_kind);
+
+/* Time the solver's kernels in isolation on its current system: each is
+ * launched `reps` times back to back on the library stream between CUDA
+ * events.  ms[0] SpMV with fused dot, ms[1] ILU(0)/Jacobi apply with fused
+ * update, ms[2] BiCGStab x/r update, ms[3] ILU(0) factorisation; per launch.
+ * Leaves the solution untouched.  (No reference counterpart: measurement.) */
+int pg_solver_profile(pg_solver *s, int reps, double *ms);
+
+/* Number of kernels the library has launched since it was loaded. */
+uint64_t pg_kernel_launches(void);
+
+/* Subdomain id of every row of the last analysed pattern (host, part[n]);
+ * returns the number of subdomains in *n_parts. */
+int pg_solver_partition(const pg_solver *s, int32_t *part, int *n_parts);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

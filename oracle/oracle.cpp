@@ -1,0 +1,865 @@
+// CPU oracle for the Phase pressure-solve path -- TEST INFRASTRUCTURE ONLY.
+// Restates the reference algorithms in plain C++ (no Boost, Eigen or
+// Trilinos).  Only the tests, bench.py's CPU baseline and smoke() use it, as
+// the checker; the product library never links it.
+// Compiled with -ffp-contract=off so that products and sums round exactly as
+// the reference's x86 build does (no fused multiply-add).
+#include "oracle.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <queue>
+#include <utility>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+static double ms_since(Clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+}
+
+struct V2 {
+  double x, y;
+};
+static inline double dot(V2 a, V2 b) { return a.x * b.x + a.y * b.y; }
+static inline double mag_sqr(V2 a) { return a.x * a.x + a.y * a.y; }
+static inline V2 sub(V2 a, V2 b) { return {a.x - b.x, a.y - b.y}; }
+
+}  // namespace
+
+struct or_mesh {
+  std::vector<V2> nodes;
+  std::vector<V2> centroid;
+  std::vector<double> volume;
+  // faces, in creation order (FiniteVolumeGrid2D::createCell)
+  std::vector<int32_t> fl, fr, fln, frn;
+  std::vector<V2> fc, fn;
+  // per-cell link lists: interior links (face, cell) and boundary links
+  // (face), each in face-id order (FiniteVolumeGrid2D::init :405-419)
+  std::vector<std::vector<std::pair<int32_t, int32_t>>> nb;
+  std::vector<std::vector<int32_t>> bd;
+  int64_t n_interior = 0, n_boundary = 0;
+};
+
+// Face::outwardNorm(point) (Face.cpp:48-50)
+static inline V2 outward_norm(const or_mesh &m, int32_t f, V2 p) {
+  V2 n = m.fn[f];
+  return dot(sub(m.fc[f], p), n) > 0. ? n : V2{-n.x, -n.y};
+}
+
+extern "C" or_mesh *or_mesh_create(const double *nodes_xy, int64_t n_nodes,
+                                   const int64_t *cptr, const int64_t *cind,
+                                   int64_t n_cells) {
+  auto *m = new or_mesh();
+  m->nodes.resize(n_nodes);
+  for (int64_t i = 0; i < n_nodes; ++i)
+    m->nodes[i] = {nodes_xy[2 * i], nodes_xy[2 * i + 1]};
+
+  m->centroid.resize(n_cells);
+  m->volume.resize(n_cells);
+  std::map<std::pair<int64_t, int64_t>, int32_t> dir;  // faceDirectory_
+
+  for (int64_t c = 0; c < n_cells; ++c) {
+    const int64_t b = cptr[c], e = cptr[c + 1], k = e - b;
+    // Cell::Cell (Cell.cpp:8-29): polygon area and centroid (shoelace form
+    // of the polygon area/centroid integrals; orientation corrected so the
+    // area is positive).
+    double a2 = 0., sx = 0., sy = 0.;
+    for (int64_t i = 0; i < k; ++i) {
+      V2 p = m->nodes[cind[b + i]], q = m->nodes[cind[b + (i + 1) % k]];
+      double cr = p.x * q.y - q.x * p.y;
+      a2 += cr;
+      sx += (p.x + q.x) * cr;
+      sy += (p.y + q.y) * cr;
+    }
+    m->volume[c] = std::fabs(a2) / 2.;
+    m->centroid[c] = {sx / (3. * a2), sy / (3. * a2)};
+
+    // FiniteVolumeGrid2D::createCell (FiniteVolumeGrid2D.cpp:84-114)
+    for (int64_t i = 0; i < k; ++i) {
+      int64_t n1 = cind[b + i], n2 = cind[b + (i + 1) % k];
+      auto key = n1 < n2 ? std::make_pair(n1, n2) : std::make_pair(n2, n1);
+      auto it = dir.find(key);
+      if (it == dir.end()) {
+        int32_t id = (int32_t)m->fl.size();
+        dir.emplace(key, id);
+        V2 ln = m->nodes[n1], rn = m->nodes[n2];
+        // Face::Face (Face.cpp:9-18): centroid = 0.5*(l+r), normal =
+        // normalVec(r - l) = (t.y, -t.x) (Vector2D.h:26)
+        m->fc.push_back({0.5 * (ln.x + rn.x), 0.5 * (ln.y + rn.y)});
+        V2 t = sub(rn, ln);
+        m->fn.push_back({t.y, -t.x});
+        m->fl.push_back((int32_t)c);
+        m->fr.push_back(-1);
+        m->fln.push_back((int32_t)n1);
+        m->frn.push_back((int32_t)n2);
+      } else {
+        m->fr[it->second] = (int32_t)c;
+      }
+    }
+  }
+
+  // FiniteVolumeGrid2D::init (:405-419): links in face-id order
+  m->nb.resize(n_cells);
+  m->bd.resize(n_cells);
+  for (int32_t f = 0; f < (int32_t)m->fl.size(); ++f) {
+    if (m->fr[f] < 0) {
+      m->bd[m->fl[f]].push_back(f);
+      ++m->n_boundary;
+    } else {
+      m->nb[m->fl[f]].push_back({f, m->fr[f]});
+      m->nb[m->fr[f]].push_back({f, m->fl[f]});
+      ++m->n_interior;
+    }
+  }
+  return m;
+}
+
+extern "C" void or_mesh_destroy(or_mesh *m) { delete m; }
+
+extern "C" void or_mesh_sizes(const or_mesh *m, int64_t *n_cells,
+                              int64_t *n_faces, int64_t *n_interior,
+                              int64_t *n_boundary) {
+  *n_cells = (int64_t)m->centroid.size();
+  *n_faces = (int64_t)m->fl.size();
+  *n_interior = m->n_interior;
+  *n_boundary = m->n_boundary;
+}
+
+extern "C" void or_mesh_cells(const or_mesh *m, double *cx, double *cy,
+                              double *vol) {
+  for (size_t c = 0; c < m->centroid.size(); ++c) {
+    cx[c] = m->centroid[c].x;
+    cy[c] = m->centroid[c].y;
+    vol[c] = m->volume[c];
+  }
+}
+
+extern "C" void or_mesh_faces(const or_mesh *m, int32_t *lcell,
+                              int32_t *rcell, int32_t *lnode, int32_t *rnode,
+                              double *fx, double *fy, double *nx, double *ny) {
+  for (size_t f = 0; f < m->fl.size(); ++f) {
+    lcell[f] = m->fl[f];
+    rcell[f] = m->fr[f];
+    lnode[f] = m->fln[f];
+    rnode[f] = m->frn[f];
+    fx[f] = m->fc[f].x;
+    fy[f] = m->fc[f].y;
+    nx[f] = m->fn[f].x;
+    ny[f] = m->fn[f].y;
+  }
+}
+
+extern "C" int64_t or_mesh_nlinks(const or_mesh *m) {
+  return 2 * m->n_interior + m->n_boundary;
+}
+
+extern "C" void or_mesh_links(const or_mesh *m, int64_t *link_ptr,
+                              int32_t *link_face, int32_t *link_cell) {
+  int64_t k = 0;
+  link_ptr[0] = 0;
+  for (size_t c = 0; c < m->nb.size(); ++c) {
+    for (auto &l : m->nb[c]) {
+      link_face[k] = l.first;
+      link_cell[k++] = l.second;
+    }
+    for (int32_t f : m->bd[c]) {
+      link_face[k] = f;
+      link_cell[k++] = -1;
+    }
+    link_ptr[c + 1] = k;
+  }
+}
+
+// FiniteVolumeField::interpolateFaces(DISTANCE) (FiniteVolumeField.tpp
+// :130-162) with Face::distanceWeight (Face.cpp:60-64), then
+// setBoundaryFaces for NORMAL_GRADIENT patches (:165-183).
+extern "C" void or_interpolate_faces(const or_mesh *m, const double *cv,
+                                     double *fv) {
+  for (size_t f = 0; f < m->fl.size(); ++f) {
+    int32_t l = m->fl[f], r = m->fr[f];
+    if (r < 0) {
+      fv[f] = cv[l];
+      continue;
+    }
+    V2 dr = sub(m->fc[f], m->centroid[r]);
+    V2 dl = sub(m->fc[f], m->centroid[l]);
+    double l1 = std::sqrt(dr.x * dr.x + dr.y * dr.y);
+    double l2 = std::sqrt(dl.x * dl.x + dl.y * dl.y);
+    double g = l1 / (l1 + l2);
+    fv[f] = g * cv[l] + (1. - g) * cv[r];
+  }
+}
+
+extern "C" void or_dt_over_rho_faces(const or_mesh *m, const double *gf,
+                                     double rho1, double rho2, double dt,
+                                     double *out) {
+  for (size_t f = 0; f < m->fl.size(); ++f) {
+    double g = std::min(std::max(gf[f], 0.), 1.);
+    double rho = rho1 + g * (rho2 - rho1);
+    out[f] = dt / rho;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// CrsEquation semantics (CrsEquation.cpp:159-164 ctor with nnz=5 placeholder
+// slots per row, :263-281 addCoeff).  Each row keeps its slots in a vector;
+// an addCoeff that finds no free slot appends at the end of the row, which
+// is where the reference inserts (colInd_.insert at rowPtr_[row+1]).
+struct or_eqn {
+  std::vector<std::vector<std::pair<int32_t, double>>> rows;
+  std::vector<double> rhs;
+};
+
+static void add_coeff(or_eqn &e, int32_t row, int32_t col, double val) {
+  auto &r = e.rows[row];
+  for (auto &s : r) {
+    if (s.first == col) {
+      s.second += val;
+      return;
+    } else if (s.first == -1) {
+      s.first = col;
+      s.second = val;
+      return;
+    }
+  }
+  r.push_back({col, val});
+}
+
+extern "C" or_eqn *or_laplacian(const or_mesh *m, const double *gamma_face,
+                                double gamma_scalar, const int32_t *bc_type,
+                                const double *bc_value,
+                                const double *u_face_xy) {
+  const int64_t n = (int64_t)m->centroid.size();
+  auto *e = new or_eqn();
+  e->rows.assign(n, std::vector<std::pair<int32_t, double>>(5, {-1, 0.}));
+  e->rhs.assign(n, 0.);
+
+  for (int32_t c = 0; c < (int32_t)n; ++c) {
+    const V2 pc = m->centroid[c];
+    for (auto &l : m->nb[c]) {
+      const int32_t f = l.first, nbc = l.second;
+      V2 rc = sub(m->centroid[nbc], pc);     // InteriorLink rCellVec
+      V2 sf = outward_norm(*m, f, pc);       // InteriorLink outwardNorm
+      if (gamma_face) {
+        // Laplacian.h:139-142: diag first, then neighbour
+        double coeff = gamma_face[f] * dot(rc, sf) / mag_sqr(rc);
+        add_coeff(*e, c, c, -coeff);
+        add_coeff(*e, c, nbc, coeff);
+      } else {
+        // Laplacian.h:55-58: neighbour first, then diag
+        double coeff = gamma_scalar * dot(rc, sf) / mag_sqr(rc);
+        add_coeff(*e, c, nbc, coeff);
+        add_coeff(*e, c, c, -coeff);
+      }
+    }
+    for (int32_t f : m->bd[c]) {
+      V2 rf = sub(m->fc[f], pc);             // BoundaryLink rFaceVec
+      V2 sf = outward_norm(*m, f, pc);
+      double g = gamma_face ? gamma_face[f] : gamma_scalar;
+      double coeff = g * dot(rf, sf) / mag_sqr(rf);
+      switch (bc_type[f]) {
+      case OR_FIXED:
+        add_coeff(*e, c, c, -coeff);
+        e->rhs[c] += coeff * bc_value[f];
+        break;
+      default:  // NORMAL_GRADIENT / SYMMETRY: no contribution
+        break;
+      }
+    }
+  }
+
+  if (u_face_xy) {
+    // src::div(u) (Source.cpp:5-21), then operator==(Vector) -> rhs_ -= divU
+    // (CrsEquation.cpp:432-435,459-461)
+    for (int32_t c = 0; c < (int32_t)n; ++c) {
+      const V2 pc = m->centroid[c];
+      double d = 0.;
+      for (auto &l : m->nb[c]) {
+        int32_t f = l.first;
+        V2 u{u_face_xy[2 * f], u_face_xy[2 * f + 1]};
+        d += dot(u, outward_norm(*m, f, pc));
+      }
+      for (int32_t f : m->bd[c]) {
+        V2 u{u_face_xy[2 * f], u_face_xy[2 * f + 1]};
+        d += dot(u, outward_norm(*m, f, pc));
+      }
+      e->rhs[c] -= d;
+    }
+  }
+  return e;
+}
+
+extern "C" void or_eqn_destroy(or_eqn *e) { delete e; }
+
+extern "C" void or_eqn_sizes(const or_eqn *e, int64_t *n, int64_t *n_slots,
+                             int64_t *nnz) {
+  *n = (int64_t)e->rows.size();
+  int64_t s = 0, u = 0;
+  for (auto &r : e->rows) {
+    s += (int64_t)r.size();
+    for (auto &p : r) u += p.first >= 0;
+  }
+  *n_slots = s;
+  *nnz = u;
+}
+
+extern "C" void or_eqn_export_slots(const or_eqn *e, int32_t *row_ptr,
+                                    int32_t *col_ind, double *vals,
+                                    double *rhs) {
+  int64_t k = 0;
+  row_ptr[0] = 0;
+  for (size_t i = 0; i < e->rows.size(); ++i) {
+    for (auto &p : e->rows[i]) {
+      col_ind[k] = p.first;
+      vals[k++] = p.second;
+    }
+    row_ptr[i + 1] = (int32_t)k;
+    rhs[i] = e->rhs[i];
+  }
+}
+
+extern "C" void or_eqn_export_csr(const or_eqn *e, int32_t *row_ptr,
+                                  int32_t *col_ind, double *vals,
+                                  double *rhs) {
+  int64_t k = 0;
+  row_ptr[0] = 0;
+  for (size_t i = 0; i < e->rows.size(); ++i) {
+    for (auto &p : e->rows[i]) {
+      if (p.first < 0) continue;
+      col_ind[k] = p.first;
+      vals[k++] = p.second;
+    }
+    row_ptr[i + 1] = (int32_t)k;
+    rhs[i] = e->rhs[i];
+  }
+}
+
+// ScalarGradient::computeFaces (ScalarGradient.cpp:34-47) and
+// compute(FACE_TO_CELL) (:49-74)
+extern "C" void or_gradient(const or_mesh *m, const double *phi,
+                            const double *phi_face, double *gf,
+                            double *gc) {
+  const size_t nf = m->fl.size();
+  for (size_t f = 0; f < nf; ++f) {
+    int32_t l = m->fl[f], r = m->fr[f];
+    V2 d;
+    double dphi;
+    if (r >= 0) {
+      d = sub(m->centroid[r], m->centroid[l]);
+      dphi = phi[r] - phi[l];
+    } else {
+      d = sub(m->fc[f], m->centroid[l]);
+      dphi = phi_face[f] - phi[l];
+    }
+    double ms = mag_sqr(d);
+    gf[2 * f] = dphi * d.x / ms;
+    gf[2 * f + 1] = dphi * d.y / ms;
+  }
+  for (size_t c = 0; c < m->centroid.size(); ++c) {
+    V2 sum{0., 0.}, tmp{0., 0.};
+    auto acc = [&](int32_t f) {
+      V2 sf = outward_norm(*m, f, m->centroid[c]);
+      sf = {std::fabs(sf.x), std::fabs(sf.y)};
+      tmp.x += gf[2 * f] * sf.x;
+      tmp.y += gf[2 * f + 1] * sf.y;
+      sum.x += sf.x;
+      sum.y += sf.y;
+    };
+    for (auto &l : m->nb[c]) acc(l.first);
+    for (int32_t f : m->bd[c]) acc(f);
+    gc[2 * c] = tmp.x / sum.x;
+    gc[2 * c + 1] = tmp.y / sum.y;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Sparse kernels and Krylov solver
+
+namespace {
+
+struct Csr {
+  int64_t n;
+  const int32_t *rp;
+  const int32_t *ci;
+  const double *v;
+};
+
+static void spmv(const Csr &A, const double *x, double *y) {
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < A.n; ++i) {
+    double s = 0.;
+    for (int32_t j = A.rp[i]; j < A.rp[i + 1]; ++j) s += A.v[j] * x[A.ci[j]];
+    y[i] = s;
+  }
+}
+
+static double vdot(int64_t n, const double *a, const double *b) {
+  double s = 0.;
+#pragma omp parallel for schedule(static) reduction(+ : s)
+  for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+
+// Incomplete LU with zero fill, row-wise IKJ form (Saad, Iterative Methods
+// for Sparse Linear Systems, 2nd ed., Alg. 10.4), restricted to the diagonal
+// blocks of a row partition (Ifpack2 additive Schwarz, overlap 0, with a
+// RILUK(0) subdomain solver).  Columns of each row are visited in increasing
+// order; entries coupling two subdomains are excluded (stored as 0).
+struct Ilu0 {
+  int64_t n = 0;
+  const int32_t *rp = nullptr, *ci = nullptr;
+  std::vector<double> lu;
+  std::vector<int32_t> diag;         // position of the diagonal per row
+  std::vector<std::vector<int32_t>> order;  // per row: entry positions by col
+  std::vector<std::vector<int32_t>> groups; // rows of each subdomain, sorted
+  int status = 0;
+
+  void build(const Csr &A, const int32_t *part, int n_parts) {
+    n = A.n;
+    rp = A.rp;
+    ci = A.ci;
+    lu.assign(A.v, A.v + A.rp[A.n]);
+    diag.assign(n, -1);
+    order.assign(n, {});
+    for (int64_t i = 0; i < n; ++i) {
+      auto &o = order[i];
+      for (int32_t j = rp[i]; j < rp[i + 1]; ++j) {
+        if (part && part[ci[j]] != part[i]) {
+          lu[j] = 0.;
+          continue;
+        }
+        o.push_back(j);
+        if (ci[j] == i) diag[i] = j;
+      }
+      std::sort(o.begin(), o.end(),
+                [&](int32_t a, int32_t b) { return ci[a] < ci[b]; });
+    }
+    if (part) {
+      groups.assign(n_parts, {});
+      for (int64_t i = 0; i < n; ++i) groups[part[i]].push_back((int32_t)i);
+    } else {
+      groups.assign(1, {});
+      groups[0].resize(n);
+      std::iota(groups[0].begin(), groups[0].end(), 0);
+    }
+    int bad = 0;
+#pragma omp parallel
+    {
+      std::vector<int32_t> pos(n, -1);
+#pragma omp for schedule(dynamic, 1) reduction(+ : bad)
+      for (int64_t g = 0; g < (int64_t)groups.size(); ++g) {
+        for (int32_t i : groups[g]) {
+          for (int32_t j : order[i]) pos[ci[j]] = j;
+          for (int32_t j : order[i]) {
+            int32_t k = ci[j];
+            if (k >= i) break;
+            int32_t dk = diag[k];
+            if (dk < 0 || lu[dk] == 0.) {
+              ++bad;
+              continue;
+            }
+            double lik = lu[j] / lu[dk];
+            lu[j] = lik;
+            for (int32_t jj : order[k]) {
+              int32_t c = ci[jj];
+              if (c <= k) continue;
+              int32_t p = pos[c];
+              if (p >= 0) lu[p] -= lik * lu[jj];
+            }
+          }
+          for (int32_t j : order[i]) pos[ci[j]] = -1;
+          if (diag[i] < 0 || lu[diag[i]] == 0. || !std::isfinite(lu[diag[i]]))
+            ++bad;
+        }
+      }
+    }
+    status = bad ? 2 : 0;
+  }
+
+  void apply(const double *r, double *z) const {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t g = 0; g < (int64_t)groups.size(); ++g) {
+      const auto &rows = groups[g];
+      for (int32_t i : rows) {
+        double s = r[i];
+        for (int32_t j : order[i]) {
+          int32_t c = ci[j];
+          if (c >= i) break;
+          s -= lu[j] * z[c];
+        }
+        z[i] = s;
+      }
+      for (auto it = rows.rbegin(); it != rows.rend(); ++it) {
+        int32_t i = *it;
+        double s = z[i];
+        for (auto jt = order[i].rbegin(); jt != order[i].rend(); ++jt) {
+          int32_t c = ci[*jt];
+          if (c <= i) break;
+          s -= lu[*jt] * z[c];
+        }
+        z[i] = s / lu[diag[i]];
+      }
+    }
+  }
+};
+
+// ILUT(p, tau): dual-threshold incomplete LU (Saad, "ILUT: a dual threshold
+// incomplete LU factorization", Numer. Linear Algebra Appl. 1 (1994);
+// Iterative Methods for Sparse Linear Systems, Alg. 10.6).  Row i is
+// eliminated in a dense work row; multipliers and the final row are dropped
+// below tau * ||a_i||_2, and at most p entries are kept in each of the L and
+// U parts of the row (the diagonal is always kept).
+struct Ilut {
+  int64_t n = 0;
+  std::vector<int64_t> lp, up;
+  std::vector<int32_t> lc, uc;  // U rows store the diagonal first
+  std::vector<double> lv, uv;
+  int status = 0;
+
+  void build(const Csr &A, double tau, int p) {
+    n = A.n;
+    lp.assign(1, 0);
+    up.assign(1, 0);
+    lc.clear(); uc.clear(); lv.clear(); uv.clear();
+    std::vector<double> w(n, 0.);
+    std::vector<char> in(n, 0);
+    std::vector<int32_t> nzl, nzu;
+    for (int64_t i = 0; i < n; ++i) {
+      double nrm = 0.;
+      nzl.clear();
+      nzu.clear();
+      bool has_diag = false;
+      for (int32_t j = A.rp[i]; j < A.rp[i + 1]; ++j) {
+        int32_t c = A.ci[j];
+        nrm += A.v[j] * A.v[j];
+        if (!in[c]) {
+          in[c] = 1;
+          (c < i ? nzl : nzu).push_back(c);
+        }
+        w[c] += A.v[j];
+        if (c == i) has_diag = true;
+      }
+      if (!has_diag) {
+        in[i] = 1;
+        nzu.push_back((int32_t)i);
+      }
+      nrm = std::sqrt(nrm);
+      const double tol = tau * nrm;
+      // eliminate lower entries in increasing column order (min-heap)
+      std::priority_queue<int32_t, std::vector<int32_t>, std::greater<int32_t>>
+          heap(nzl.begin(), nzl.end());
+      std::vector<int32_t> kept_l;
+      while (!heap.empty()) {
+        int32_t k = heap.top();
+        heap.pop();
+        double wk = w[k] / uv[up[k]];
+        if (std::fabs(wk) < tol) {
+          w[k] = 0.;
+          continue;
+        }
+        w[k] = wk;
+        kept_l.push_back(k);
+        for (int64_t jj = up[k] + 1; jj < up[k + 1]; ++jj) {
+          int32_t c = uc[jj];
+          if (!in[c]) {
+            in[c] = 1;
+            if (c < i) {
+              nzl.push_back(c);
+              heap.push(c);
+            } else {
+              nzu.push_back(c);
+            }
+          }
+          w[c] -= wk * uv[jj];
+        }
+      }
+      // keep the p largest L multipliers
+      std::sort(kept_l.begin(), kept_l.end(), [&](int32_t a, int32_t b) {
+        return std::fabs(w[a]) > std::fabs(w[b]);
+      });
+      if ((int)kept_l.size() > p) kept_l.resize(p);
+      std::sort(kept_l.begin(), kept_l.end());
+      for (int32_t k : kept_l) {
+        lc.push_back(k);
+        lv.push_back(w[k]);
+      }
+      lp.push_back((int64_t)lc.size());
+      // U part: drop small, keep p largest off-diagonals
+      std::vector<int32_t> ku;
+      for (int32_t c : nzu)
+        if (c != i && std::fabs(w[c]) >= tol) ku.push_back(c);
+      std::sort(ku.begin(), ku.end(), [&](int32_t a, int32_t b) {
+        return std::fabs(w[a]) > std::fabs(w[b]);
+      });
+      if ((int)ku.size() > p) ku.resize(p);
+      std::sort(ku.begin(), ku.end());
+      double d = w[i];
+      if (d == 0.) d = (tol > 0. ? tol : 1e-4);  // zero pivot replacement
+      if (!std::isfinite(d)) status = 3;
+      uc.push_back((int32_t)i);
+      uv.push_back(d);
+      for (int32_t c : ku) {
+        uc.push_back(c);
+        uv.push_back(w[c]);
+      }
+      up.push_back((int64_t)uc.size());
+      for (int32_t c : nzl) { w[c] = 0.; in[c] = 0; }
+      for (int32_t c : nzu) { w[c] = 0.; in[c] = 0; }
+    }
+  }
+
+  void apply(const double *r, double *z) const {
+    for (int64_t i = 0; i < n; ++i) {
+      double s = r[i];
+      for (int64_t j = lp[i]; j < lp[i + 1]; ++j) s -= lv[j] * z[lc[j]];
+      z[i] = s;
+    }
+    for (int64_t i = n - 1; i >= 0; --i) {
+      double s = z[i];
+      for (int64_t j = up[i] + 1; j < up[i + 1]; ++j) s -= uv[j] * z[uc[j]];
+      z[i] = s / uv[up[i]];
+    }
+  }
+};
+
+struct Precond {
+  int kind = OR_PREC_NONE;
+  Ilu0 ilu0;
+  Ilut ilut;
+  std::vector<double> dinv;
+  int status = 0;
+
+  void build(const Csr &A, const or_solver_cfg &cfg) {
+    kind = cfg.precond;
+    if (kind == OR_PREC_ILU0) {
+      ilu0.build(A, cfg.part, cfg.n_parts);
+      status = ilu0.status;
+    } else if (kind == OR_PREC_ILUT) {
+      ilut.build(A, cfg.ilut_drop, cfg.ilut_fill);
+      status = ilut.status;
+    } else if (kind == OR_PREC_JACOBI) {
+      dinv.assign(A.n, 1.);
+      for (int64_t i = 0; i < A.n; ++i)
+        for (int32_t j = A.rp[i]; j < A.rp[i + 1]; ++j)
+          if (A.ci[j] == i && A.v[j] != 0.) dinv[i] = 1. / A.v[j];
+    }
+  }
+  void apply(int64_t n, const double *r, double *z) const {
+    switch (kind) {
+    case OR_PREC_ILU0: ilu0.apply(r, z); break;
+    case OR_PREC_ILUT: ilut.apply(r, z); break;
+    case OR_PREC_JACOBI:
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < n; ++i) z[i] = dinv[i] * r[i];
+      break;
+    default:
+      std::memcpy(z, r, sizeof(double) * n);
+    }
+  }
+};
+
+// BiCGStab (van der Vorst, SIAM J. Sci. Stat. Comput. 13 (1992)) with right
+// preconditioning: A M^-1 y = b, x = M^-1 y.  The stop test is on the
+// recursively updated residual, confirmed with a true residual b - A x; if
+// the true residual has drifted above tol the iteration restarts from it.
+// hist (optional) records ||r_k||/||b|| per iteration.
+static int bicgstab(const Csr &A, const double *b, double *x,
+                    const or_solver_cfg &cfg, or_solver_stats *st,
+                    double *hist, int stop_on_tol) {
+  const int64_t n = A.n;
+  auto t_setup = Clock::now();
+  Precond M;
+  M.build(A, cfg);
+  double setup_ms = ms_since(t_setup);
+  auto t0 = Clock::now();
+
+  std::vector<double> r(n), rh(n), p(n, 0.), v(n, 0.), ph(n), s(n), sh(n),
+      t(n);
+  if (!cfg.use_guess) std::fill(x, x + n, 0.);
+  const double bn = std::sqrt(vdot(n, b, b));
+  auto true_residual = [&]() {
+    spmv(A, x, r.data());
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) r[i] = b[i] - r[i];
+    return std::sqrt(vdot(n, r.data(), r.data()));
+  };
+  int status = 1, it = 0;
+  double rn = true_residual();
+  if (hist) hist[0] = bn > 0 ? rn / bn : 0.;
+  if (bn == 0.) {
+    std::fill(x, x + n, 0.);
+    rn = 0.;
+    status = 0;
+  } else if (rn / bn <= cfg.tol && stop_on_tol) {
+    status = 0;
+  } else if (M.status) {
+    status = M.status;
+  } else {
+    double rho_old = 1., alpha = 1., omega = 1.;
+    rh = r;
+    int restarts = 0;
+    while (it < cfg.max_iters) {
+      double rho = vdot(n, rh.data(), r.data());
+      if (rho == 0.) { status = 2; break; }
+      double beta = (rho / rho_old) * (alpha / omega);
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < n; ++i) p[i] = r[i] + beta * (p[i] - omega * v[i]);
+      M.apply(n, p.data(), ph.data());
+      spmv(A, ph.data(), v.data());
+      double rv = vdot(n, rh.data(), v.data());
+      if (rv == 0.) { status = 2; break; }
+      alpha = rho / rv;
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < n; ++i) s[i] = r[i] - alpha * v[i];
+      M.apply(n, s.data(), sh.data());
+      spmv(A, sh.data(), t.data());
+      double tt = vdot(n, t.data(), t.data());
+      double ts = vdot(n, t.data(), s.data());
+      omega = tt > 0. ? ts / tt : 0.;
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < n; ++i) {
+        x[i] += alpha * ph[i] + omega * sh[i];
+        r[i] = s[i] - omega * t[i];
+      }
+      rho_old = rho;
+      ++it;
+      rn = std::sqrt(vdot(n, r.data(), r.data()));
+      if (hist) hist[it] = rn / bn;
+      if (!std::isfinite(rn)) { status = 3; break; }
+      if (stop_on_tol && rn / bn <= cfg.tol) {
+        rn = true_residual();
+        if (rn / bn <= cfg.tol) { status = 0; break; }
+        if (++restarts > 20) { status = 2; break; }
+        rh = r;
+        std::fill(p.begin(), p.end(), 0.);
+        std::fill(v.begin(), v.end(), 0.);
+        rho_old = alpha = omega = 1.;
+      }
+      if (omega == 0.) { status = 2; break; }
+    }
+  }
+  double ms = ms_since(t0);
+  if (st) {
+    rn = true_residual();
+    st->iters = it;
+    st->status = status;
+    st->rel_residual = bn > 0 ? rn / bn : 0.;
+    st->ms = ms;
+    st->setup_ms = setup_ms;
+  }
+  if (hist && !st) hist[cfg.max_iters + 1] = ms, hist[cfg.max_iters + 2] = setup_ms;
+  return it;
+}
+
+struct ThreadScope {
+  int saved = 0;
+  explicit ThreadScope(int k) {
+#ifdef _OPENMP
+    saved = omp_get_max_threads();
+    if (k > 0) omp_set_num_threads(k);
+#endif
+  }
+  ~ThreadScope() {
+#ifdef _OPENMP
+    omp_set_num_threads(saved);
+#endif
+  }
+};
+
+}  // namespace
+
+extern "C" int or_bicgstab(int64_t n, const int32_t *row_ptr,
+                           const int32_t *col_ind, const double *vals,
+                           const double *b, double *x,
+                           const or_solver_cfg *cfg, or_solver_stats *stats) {
+  ThreadScope ts(cfg->n_threads);
+  Csr A{n, row_ptr, col_ind, vals};
+  or_solver_stats st{};
+  bicgstab(A, b, x, *cfg, &st, nullptr, 1);
+  if (stats) *stats = st;
+  return st.status;
+}
+
+extern "C" int or_bicgstab_history(int64_t n, const int32_t *row_ptr,
+                                   const int32_t *col_ind, const double *vals,
+                                   const double *b, const or_solver_cfg *cfg,
+                                   double *hist, double *ms_out,
+                                   double *setup_ms_out) {
+  ThreadScope ts(cfg->n_threads);
+  Csr A{n, row_ptr, col_ind, vals};
+  std::vector<double> x(n, 0.);
+  or_solver_cfg c = *cfg;
+  c.use_guess = 0;
+  std::vector<double> h(c.max_iters + 3, 0.);
+  int it = bicgstab(A, b, x.data(), c, nullptr, h.data(), 0);
+  for (int i = 0; i <= it; ++i) hist[i] = h[i];
+  *ms_out = h[c.max_iters + 1];
+  *setup_ms_out = h[c.max_iters + 2];
+  return it;
+}
+
+extern "C" int or_ilu0(int64_t n, const int32_t *row_ptr,
+                       const int32_t *col_ind, const double *vals,
+                       const int32_t *part, double *out_vals) {
+  Csr A{n, row_ptr, col_ind, vals};
+  Ilu0 f;
+  int np = 0;
+  if (part)
+    for (int64_t i = 0; i < n; ++i) np = std::max(np, part[i] + 1);
+  f.build(A, part, np);
+  std::copy(f.lu.begin(), f.lu.end(), out_vals);
+  return f.status;
+}
+
+extern "C" void or_ilu0_apply(int64_t n, const int32_t *row_ptr,
+                              const int32_t *col_ind, const double *lu_vals,
+                              const int32_t *part, const double *r,
+                              double *z) {
+  // rebuild the row orders; the factor values are taken as given
+  Csr A{n, row_ptr, col_ind, lu_vals};
+  Ilu0 f;
+  int np = 0;
+  if (part)
+    for (int64_t i = 0; i < n; ++i) np = std::max(np, part[i] + 1);
+  f.n = n;
+  f.rp = row_ptr;
+  f.ci = col_ind;
+  f.lu.assign(lu_vals, lu_vals + row_ptr[n]);
+  f.diag.assign(n, -1);
+  f.order.assign(n, {});
+  for (int64_t i = 0; i < n; ++i) {
+    for (int32_t j = row_ptr[i]; j < row_ptr[i + 1]; ++j) {
+      if (part && part[col_ind[j]] != part[i]) continue;
+      f.order[i].push_back(j);
+      if (col_ind[j] == i) f.diag[i] = j;
+    }
+    std::sort(f.order[i].begin(), f.order[i].end(),
+              [&](int32_t a, int32_t b) { return col_ind[a] < col_ind[b]; });
+  }
+  if (part) {
+    f.groups.assign(np, {});
+    for (int64_t i = 0; i < n; ++i) f.groups[part[i]].push_back((int32_t)i);
+  } else {
+    f.groups.assign(1, std::vector<int32_t>(n));
+    std::iota(f.groups[0].begin(), f.groups[0].end(), 0);
+  }
+  (void)A;
+  f.apply(r, z);
+}
+
+extern "C" void or_spmv(int64_t n, const int32_t *row_ptr,
+                        const int32_t *col_ind, const double *vals,
+                        const double *x, double *y) {
+  Csr A{n, row_ptr, col_ind, vals};
+  spmv(A, x, y);
+}

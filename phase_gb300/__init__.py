@@ -1,0 +1,387 @@
+"""phase_gb300 -- GB300 pressure assembly + BiCGStab/ILU(0) for Phase.
+
+Python host binding over the C ABI of libphase_gb300.so
+(include/phase_gb300.h).  Names mirror the reference interfaces the library
+replaces: ``SparseMatrixSolver`` (src/Math/SparseMatrixSolver.h:11-62) with
+setRank/set/setRhs/setGuess/solve/x/nIters/error, and the device
+``FiniteVolumeEquation`` assembled by ``fv.laplacian(...) == src.div(u)``.
+
+There is no CPU path: every call runs the CUDA library, and loading fails
+loudly when the library has not been built or no GPU is present.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libphase_gb300.so")
+
+PG_OK, PG_MAX_ITERS, PG_BREAKDOWN, PG_NON_FINITE, PG_BAD_ARG, PG_TIMEOUT, \
+    PG_CUDA_ERROR = range(7)
+PG_HOST, PG_DEVICE = 0, 1
+FIXED, NORMAL_GRADIENT, SYMMETRY = 0, 1, 2
+GAMMA_SCALAR, GAMMA_FACE = 0, 1
+PREC_NONE, PREC_JACOBI, PREC_ILU0 = 0, 1, 2
+FP64, MIXED = 0, 1
+
+STATUS_NAMES = {0: "converged", 1: "max_iters", 2: "breakdown",
+                3: "non_finite", 4: "bad_arg", 5: "timeout", 6: "cuda_error"}
+
+
+class PhaseError(RuntimeError):
+    """A library call failed (bad argument or CUDA error)."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{STATUS_NAMES.get(status, status)}] {message}")
+        self.status = status
+
+
+class SolverCfg(ctypes.Structure):
+    _fields_ = [("tolerance", ctypes.c_double), ("max_iters", ctypes.c_int),
+                ("precond", ctypes.c_int), ("subdomain_rows", ctypes.c_int),
+                ("precision", ctypes.c_int), ("inner_max_iters", ctypes.c_int),
+                ("inner_tolerance", ctypes.c_double)]
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [("iters", ctypes.c_int), ("outer_iters", ctypes.c_int),
+                ("status", ctypes.c_int), ("rel_residual", ctypes.c_double),
+                ("ms", ctypes.c_double), ("setup_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_D = ctypes.c_double
+_I = ctypes.c_int
+
+# name -> (restype, argtypes); every entry point of include/phase_gb300.h
+PROTOTYPES = {
+    "pg_last_error": (ctypes.c_char_p, []),
+    "pg_stream": (_P, []),
+    "pg_synchronize": (_I, []),
+    "pg_mesh_create": (_I, [_P, _I64, _P, _P, _I64, ctypes.POINTER(_P)]),
+    "pg_mesh_destroy": (_I, [_P]),
+    "pg_mesh_sizes": (_I, [_P, _P, _P, _P, _P]),
+    "pg_mesh_faces": (_I, [_P, _P, _P, _P, _P, _P, _P]),
+    "pg_mesh_cells": (_I, [_P, _P, _P, _P]),
+    "pg_eqn_create": (_I, [_P, _I, _P, ctypes.POINTER(_P)]),
+    "pg_eqn_destroy": (_I, [_P]),
+    "pg_eqn_sizes": (_I, [_P, _P, _P]),
+    "pg_assemble_laplacian": (_I, [_P, _P, _D, _P, _P, _I]),
+    "pg_eqn_export": (_I, [_P, _P, _P, _P, _P]),
+    "pg_face_dt_over_rho": (_I, [_P, _P, _D, _D, _D, _P, _I]),
+    "pg_gradient": (_I, [_P, _P, _P, _P, _P, _I]),
+    "pg_solver_default_cfg": (None, [ctypes.POINTER(SolverCfg)]),
+    "pg_solver_create": (_I, [ctypes.POINTER(SolverCfg), ctypes.POINTER(_P)]),
+    "pg_solver_destroy": (_I, [_P]),
+    "pg_solver_set_rank": (_I, [_P, _I64]),
+    "pg_solver_set_csr": (_I, [_P, _P, _P, _P, _I]),
+    "pg_solver_set_eqn": (_I, [_P, _P]),
+    "pg_solver_set_rhs": (_I, [_P, _P, _I]),
+    "pg_solver_set_guess": (_I, [_P, _P, _I]),
+    "pg_solver_solve": (_I, [_P, ctypes.POINTER(SolveStats)]),
+    "pg_solver_get_x": (_I, [_P, _P, _I]),
+    "pg_solver_partition": (_I, [_P, _P, ctypes.POINTER(_I)]),
+    "pg_solver_profile": (_I, [_P, _I, _P]),
+    "pg_kernel_launches": (ctypes.c_uint64, []),
+}
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load libphase_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with "
+                "`python -c 'import __graft_entry__ as g; g.build()'`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in PROTOTYPES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc: int, allow=(PG_OK,)):
+    if rc not in allow:
+        raise PhaseError(rc, lib().pg_last_error().decode())
+    return rc
+
+
+def _ptr(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def _f64(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if n is not None and a.size != n:
+        raise ValueError(f"expected {n} values, got {a.size}")
+    return a
+
+
+def _i32(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    if n is not None and a.size != n:
+        raise ValueError(f"expected {n} values, got {a.size}")
+    return a
+
+
+def stream_handle() -> int:
+    """cudaStream_t of the library (for torch.cuda.ExternalStream)."""
+    return int(lib().pg_stream() or 0)
+
+
+def kernel_launches() -> int:
+    """Kernels launched by the library since it was loaded."""
+    return int(lib().pg_kernel_launches())
+
+
+def synchronize():
+    _check(lib().pg_synchronize())
+
+
+class Mesh:
+    """FiniteVolumeGrid2D built on the device from (nodes, cptr, cind)."""
+
+    def __init__(self, nodes_xy, cptr, cind):
+        nodes_xy = _f64(nodes_xy)
+        cptr = np.ascontiguousarray(cptr, dtype=np.int64)
+        cind = np.ascontiguousarray(cind, dtype=np.int64)
+        h = _P()
+        _check(lib().pg_mesh_create(_ptr(nodes_xy), nodes_xy.size // 2,
+                                    _ptr(cptr), _ptr(cind), cptr.size - 1,
+                                    ctypes.byref(h)))
+        self._h = h
+        s = np.zeros(4, np.int64)
+        _check(lib().pg_mesh_sizes(h, _ptr(s[0:1]), _ptr(s[1:2]), _ptr(s[2:3]),
+                                   _ptr(s[3:4])))
+        self.n_cells, self.n_faces, self.n_interior, self.n_boundary = map(int, s)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.pg_mesh_destroy(h)
+            self._h = None
+
+    def faces(self):
+        nf = self.n_faces
+        out = dict(lcell=np.empty(nf, np.int32), rcell=np.empty(nf, np.int32),
+                   fx=np.empty(nf), fy=np.empty(nf), nx=np.empty(nf),
+                   ny=np.empty(nf))
+        _check(lib().pg_mesh_faces(self._h, *(_ptr(out[k]) for k in
+                                              ("lcell", "rcell", "fx", "fy",
+                                               "nx", "ny"))))
+        return out
+
+    def cells(self):
+        n = self.n_cells
+        out = dict(cx=np.empty(n), cy=np.empty(n), vol=np.empty(n))
+        _check(lib().pg_mesh_cells(self._h, _ptr(out["cx"]), _ptr(out["cy"]),
+                                   _ptr(out["vol"])))
+        return out
+
+    def dt_over_rho(self, gamma_cell, rho1, rho2, dt):
+        g = _f64(gamma_cell, self.n_cells)
+        out = np.empty(self.n_faces)
+        _check(lib().pg_face_dt_over_rho(self._h, _ptr(g), rho1, rho2, dt,
+                                         _ptr(out), PG_HOST))
+        return out
+
+    def gradient(self, phi_cell, phi_face):
+        pc = _f64(phi_cell, self.n_cells)
+        pf = _f64(phi_face, self.n_faces)
+        gf = np.empty(2 * self.n_faces)
+        gc = np.empty(2 * self.n_cells)
+        _check(lib().pg_gradient(self._h, _ptr(pc), _ptr(pf), _ptr(gf),
+                                 _ptr(gc), PG_HOST))
+        return gf.reshape(-1, 2), gc.reshape(-1, 2)
+
+
+class Equation:
+    """Device FiniteVolumeEquation<Scalar> for one fv::laplacian overload."""
+
+    def __init__(self, mesh: Mesh, gamma_kind: int, bc_type):
+        self.mesh = mesh
+        bc = _i32(bc_type, mesh.n_faces)
+        h = _P()
+        _check(lib().pg_eqn_create(mesh._h, gamma_kind, _ptr(bc),
+                                   ctypes.byref(h)))
+        self._h = h
+        self.gamma_kind = gamma_kind
+        s = np.zeros(2, np.int64)
+        _check(lib().pg_eqn_sizes(h, _ptr(s[0:1]), _ptr(s[1:2])))
+        self.n, self.nnz = int(s[0]), int(s[1])
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.pg_eqn_destroy(h)
+            self._h = None
+
+    def assemble(self, gamma_face=None, gamma_scalar=0.0, bc_value=None,
+                 u_face=None):
+        nf = self.mesh.n_faces
+        g = None if gamma_face is None else _f64(gamma_face, nf)
+        bv = None if bc_value is None else _f64(bc_value, nf)
+        u = None if u_face is None else _f64(u_face, 2 * nf)
+        _check(lib().pg_assemble_laplacian(self._h, _ptr(g), gamma_scalar,
+                                           _ptr(bv), _ptr(u), PG_HOST))
+        return self
+
+    def assemble_device(self, gamma_face: int = 0, gamma_scalar=0.0,
+                        bc_value: int = 0, u_face: int = 0):
+        """assemble() with device pointers (0 = absent)."""
+        _check(lib().pg_assemble_laplacian(
+            self._h, _P(gamma_face or None), gamma_scalar,
+            _P(bc_value or None), _P(u_face or None), PG_DEVICE))
+        return self
+
+    def export(self):
+        rp = np.empty(self.n + 1, np.int32)
+        ci = np.empty(self.nnz, np.int32)
+        v = np.empty(self.nnz)
+        rhs = np.empty(self.n)
+        _check(lib().pg_eqn_export(self._h, _ptr(rp), _ptr(ci), _ptr(v),
+                                   _ptr(rhs)))
+        return rp, ci, v, rhs
+
+
+def default_cfg(**kw) -> SolverCfg:
+    c = SolverCfg()
+    lib().pg_solver_default_cfg(ctypes.byref(c))
+    for k, v in kw.items():
+        if not hasattr(c, k):
+            raise KeyError(k)
+        setattr(c, k, v)
+    return c
+
+
+class SparseMatrixSolver:
+    """The SparseMatrixSolver plugin backed by the GB300 library.
+
+    Mirrors src/Math/SparseMatrixSolver.h:11-62: setRank, set(rowPtr,
+    colInds, vals) (negative columns are CrsEquation placeholders and are
+    skipped), setGuess, setRhs (already negated rhs), solve, x, nIters,
+    error.  ``set_eqn`` takes a device equation without a host round trip.
+    """
+
+    def __init__(self, **cfg):
+        c = default_cfg(**cfg)
+        h = _P()
+        _check(lib().pg_solver_create(ctypes.byref(c), ctypes.byref(h)))
+        self._h = h
+        self.cfg = c
+        self.n = 0
+        self.stats = SolveStats()
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.pg_solver_destroy(h)
+            self._h = None
+
+    # reference-named API
+    def setRank(self, n: int):
+        _check(lib().pg_solver_set_rank(self._h, int(n)))
+        self.n = int(n)
+
+    def set(self, row_ptr, col_ind, vals):
+        rp = _i32(row_ptr, self.n + 1)
+        ci = _i32(col_ind, int(rp[-1]))
+        v = _f64(vals, int(rp[-1]))
+        _check(lib().pg_solver_set_csr(self._h, _ptr(rp), _ptr(ci), _ptr(v),
+                                       PG_HOST))
+
+    def set_eqn(self, eqn: Equation):
+        _check(lib().pg_solver_set_eqn(self._h, eqn._h))
+        self.n = eqn.n
+
+    def setRhs(self, rhs):
+        r = _f64(rhs, self.n)
+        _check(lib().pg_solver_set_rhs(self._h, _ptr(r), PG_HOST))
+
+    def setGuess(self, x0):
+        """Initial guess for the next solve; None = zero guess."""
+        if x0 is None:
+            _check(lib().pg_solver_set_guess(self._h, None, PG_HOST))
+            return
+        x = _f64(x0, self.n)
+        _check(lib().pg_solver_set_guess(self._h, _ptr(x), PG_HOST))
+
+    def set_device(self, row_ptr: int, col_ind: int, vals: int):
+        """set() with device pointers (e.g. torch.Tensor.data_ptr())."""
+        _check(lib().pg_solver_set_csr(self._h, _P(row_ptr), _P(col_ind),
+                                       _P(vals), PG_DEVICE))
+
+    def x_device(self, out_ptr: int):
+        """Copy the solution into device memory at out_ptr."""
+        _check(lib().pg_solver_get_x(self._h, _P(out_ptr), PG_DEVICE))
+
+    def solve(self) -> float:
+        st = SolveStats()
+        rc = lib().pg_solver_solve(self._h, ctypes.byref(st))
+        _check(rc, allow=(PG_OK, PG_MAX_ITERS, PG_BREAKDOWN, PG_NON_FINITE))
+        self.stats = st
+        return st.rel_residual
+
+    def x(self):
+        out = np.empty(self.n)
+        _check(lib().pg_solver_get_x(self._h, _ptr(out), PG_HOST))
+        return out
+
+    def nIters(self) -> int:
+        return self.stats.iters
+
+    def error(self) -> float:
+        return self.stats.rel_residual
+
+    def partition(self):
+        part = np.empty(self.n, np.int32)
+        k = ctypes.c_int()
+        _check(lib().pg_solver_partition(self._h, _ptr(part), ctypes.byref(k)))
+        return part, k.value
+
+    def profile(self, reps: int = 20):
+        """Per-launch ms of the hot kernels on the current system:
+        spmv, precond apply, update, ilu factor."""
+        ms = np.zeros(4)
+        _check(lib().pg_solver_profile(self._h, int(reps), _ptr(ms)))
+        return dict(spmv=ms[0], precond=ms[1], update=ms[2], factor=ms[3])
+
+    def printStatus(self, msg: str):
+        print(f"{msg} iterations = {self.nIters()}, error = {self.error():f}.")
+
+
+@dataclass
+class _FvNamespace:
+    """fv::laplacian as a function returning a device equation."""
+
+    @staticmethod
+    def laplacian(gamma, mesh: Mesh, bc_type, bc_value=None, div_u=None,
+                  eqn: Equation | None = None) -> Equation:
+        """fv::laplacian(gamma, phi) == src::div(u) on the device.
+
+        gamma: float (Laplacian.h:49-83) or per-face array (:132-167).
+        div_u: face velocities [n_faces, 2] for the src::div right-hand side.
+        """
+        face = not np.isscalar(gamma)
+        kind = GAMMA_FACE if face else GAMMA_SCALAR
+        if eqn is None or eqn.gamma_kind != kind:
+            eqn = Equation(mesh, kind, bc_type)
+        return eqn.assemble(gamma_face=gamma if face else None,
+                            gamma_scalar=0.0 if face else float(gamma),
+                            bc_value=bc_value, u_face=div_u)
+
+
+fv = _FvNamespace()

@@ -1,0 +1,525 @@
+// Host-side set-up of libphase_gb300: mesh construction, the CrsEquation
+// sparsity pattern with its face-coloured scatter schedule, and the sparsity
+// analysis (Schwarz partition + level schedule) of solver matrices.
+// All of it runs once per mesh / per pattern, never per solve.
+// Built with -ffp-contract=off so geometry rounds as the reference's does.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+
+#include "internal.h"
+
+namespace pg {
+
+// ------------------------------------------------------------------ mesh
+// FiniteVolumeGrid2D::init(nodes, cptr, cind) (FiniteVolumeGrid2D.cpp:20-35)
+// and createCell (:84-114).  Faces are de-duplicated on their unordered node
+// pair with a per-node adjacency chain (no ordered map): the first cell that
+// meets a face creates it with (lNode, rNode) in that cell's orientation and
+// becomes its lCell; the second cell makes it interior as rCell.
+int build_host_mesh(const double *nodes_xy, int64_t n_nodes,
+                    const int64_t *cptr, const int64_t *cind, int64_t n_cells,
+                    HostMesh &m) {
+  PG_CHECK_ARG(nodes_xy && cptr && cind, "pg_mesh_create: NULL array");
+  PG_CHECK_ARG(n_nodes > 0 && n_cells > 0, "pg_mesh_create: empty mesh");
+  PG_CHECK_ARG(n_cells < (int64_t)1 << 30, "pg_mesh_create: too many cells");
+  PG_CHECK_ARG(cptr[0] == 0, "pg_mesh_create: cptr[0] must be 0");
+  for (int64_t c = 0; c < n_cells; ++c)
+    PG_CHECK_ARG(cptr[c + 1] - cptr[c] >= 3,
+                 "pg_mesh_create: a cell needs at least 3 nodes");
+  const int64_t n_ent = cptr[n_cells];
+  for (int64_t k = 0; k < n_ent; ++k)
+    PG_CHECK_ARG(cind[k] >= 0 && cind[k] < n_nodes,
+                 "pg_mesh_create: node index out of range");
+
+  m.n_cells = n_cells;
+  m.cx.resize(n_cells);
+  m.cy.resize(n_cells);
+  m.vol.resize(n_cells);
+
+  std::vector<int32_t> head(n_nodes, -1), next, other, fid;
+  next.reserve(n_ent);
+  other.reserve(n_ent);
+  fid.reserve(n_ent);
+  m.fl.reserve(n_ent / 2 + 16);
+
+  for (int64_t c = 0; c < n_cells; ++c) {
+    const int64_t b = cptr[c], k = cptr[c + 1] - b;
+    // Cell::Cell (Cell.cpp:8-29): polygon area and centroid from the
+    // shoelace sums; orientation is corrected so the area is positive.
+    double a2 = 0., sx = 0., sy = 0.;
+    for (int64_t i = 0; i < k; ++i) {
+      const int64_t p = cind[b + i], q = cind[b + (i + 1) % k];
+      const double px = nodes_xy[2 * p], py = nodes_xy[2 * p + 1];
+      const double qx = nodes_xy[2 * q], qy = nodes_xy[2 * q + 1];
+      const double cr = px * qy - qx * py;
+      a2 += cr;
+      sx += (px + qx) * cr;
+      sy += (py + qy) * cr;
+    }
+    PG_CHECK_ARG(a2 != 0., "pg_mesh_create: degenerate (zero-area) cell");
+    m.vol[c] = std::fabs(a2) / 2.;
+    m.cx[c] = sx / (3. * a2);
+    m.cy[c] = sy / (3. * a2);
+
+    for (int64_t i = 0; i < k; ++i) {
+      const int32_t n1 = (int32_t)cind[b + i];
+      const int32_t n2 = (int32_t)cind[b + (i + 1) % k];
+      const int32_t lo = std::min(n1, n2), hi = std::max(n1, n2);
+      int32_t found = -1;
+      for (int32_t e = head[lo]; e >= 0; e = next[e])
+        if (other[e] == hi) {
+          found = fid[e];
+          break;
+        }
+      if (found < 0) {
+        const int32_t f = (int32_t)m.fl.size();
+        next.push_back(head[lo]);
+        other.push_back(hi);
+        fid.push_back(f);
+        head[lo] = (int32_t)next.size() - 1;
+        // Face::Face (Face.cpp:9-18): centroid 0.5*(l + r), tangent r - l,
+        // normal = tangent.normalVec() = (t.y, -t.x) (Vector2D.h:26)
+        const double lx = nodes_xy[2 * n1], ly = nodes_xy[2 * n1 + 1];
+        const double rx = nodes_xy[2 * n2], ry = nodes_xy[2 * n2 + 1];
+        m.fcx.push_back(0.5 * (lx + rx));
+        m.fcy.push_back(0.5 * (ly + ry));
+        m.fnx.push_back(ry - ly);
+        m.fny.push_back(-(rx - lx));
+        m.fl.push_back((int32_t)c);
+        m.fr.push_back(-1);
+      } else {
+        // Face::addCell (Face.cpp:66-81): at most two cells per face
+        PG_CHECK_ARG(m.fr[found] < 0,
+                     "pg_mesh_create: a face is shared by more than two cells");
+        m.fr[found] = (int32_t)c;
+      }
+    }
+  }
+  m.n_faces = (int64_t)m.fl.size();
+
+  // FiniteVolumeGrid2D::init() (:405-419): walk faces in id order; boundary
+  // faces give their lCell a boundary link, interior faces give both cells an
+  // interior link.  Per cell the interior links precede the boundary links.
+  std::vector<int32_t> ni(n_cells, 0), nb(n_cells, 0);
+  for (int64_t f = 0; f < m.n_faces; ++f) {
+    if (m.fr[f] < 0) {
+      ++nb[m.fl[f]];
+      ++m.n_boundary;
+    } else {
+      ++ni[m.fl[f]];
+      ++ni[m.fr[f]];
+      ++m.n_interior;
+    }
+  }
+  m.link_ptr.assign(n_cells + 1, 0);
+  for (int64_t c = 0; c < n_cells; ++c)
+    m.link_ptr[c + 1] = m.link_ptr[c] + ni[c] + nb[c];
+  m.link_face.assign(m.link_ptr[n_cells], -1);
+  m.link_cell.assign(m.link_ptr[n_cells], -1);
+  std::vector<int64_t> pi(n_cells), pb(n_cells);
+  for (int64_t c = 0; c < n_cells; ++c) {
+    pi[c] = m.link_ptr[c];
+    pb[c] = m.link_ptr[c] + ni[c];
+  }
+  for (int32_t f = 0; f < (int32_t)m.n_faces; ++f) {
+    const int32_t l = m.fl[f], r = m.fr[f];
+    if (r < 0) {
+      m.link_face[pb[l]++] = f;
+    } else {
+      m.link_face[pi[l]] = f;
+      m.link_cell[pi[l]++] = r;
+      m.link_face[pi[r]] = f;
+      m.link_cell[pi[r]++] = l;
+    }
+  }
+  m.n_interior_links = std::move(ni);
+  return PG_OK;
+}
+
+// ---------------------------------------------------------------- pattern
+// The pattern CrsEquation holds after fv::laplacian: each row starts with 5
+// placeholder slots (CrsEquation.cpp:159-164) that addCoeff fills in order of
+// first appearance of a column, appending past the fifth (:263-281).  The
+// scalar-gamma overload adds (cell, nb) before (cell, cell) for every
+// interior link (Laplacian.h:55-58); the face-gamma overload adds the
+// diagonal first (:139-142); FIXED boundary links add the diagonal
+// (:66-69, :150-153).  Placeholders that stay empty are dropped.
+int build_pattern(const HostMesh &m, int gamma_kind, const int32_t *bc_type,
+                  EqnPattern &p) {
+  const int64_t n = m.n_cells;
+  p.n = n;
+  p.row_ptr.assign(n + 1, 0);
+  p.col_ind.clear();
+  p.col_ind.reserve(n * 5);
+  p.diag.assign(n, -1);
+  const int64_t nf = m.n_faces;
+  std::vector<int32_t> f_slot_l(nf, -1), f_slot_r(nf, -1), f_diag_l(nf, -1),
+      f_diag_r(nf, -1);
+
+  std::vector<int32_t> row;
+  auto add = [&](int32_t col) -> int32_t {
+    for (size_t k = 0; k < row.size(); ++k)
+      if (row[k] == col) return (int32_t)k;
+    row.push_back(col);
+    return (int32_t)row.size() - 1;
+  };
+  for (int64_t c = 0; c < n; ++c) {
+    row.clear();
+    const int64_t b = m.link_ptr[c], e = m.link_ptr[c + 1];
+    const int64_t base = (int64_t)p.col_ind.size();
+    std::vector<std::pair<int64_t, int32_t>> off_slot, diag_slot;  // link->k
+    for (int64_t k = b; k < e; ++k) {
+      const int32_t f = m.link_face[k], nbc = m.link_cell[k];
+      if (nbc >= 0) {
+        int32_t so, sd;
+        if (gamma_kind == PG_GAMMA_FACE) {
+          sd = add((int32_t)c);
+          so = add(nbc);
+        } else {
+          so = add(nbc);
+          sd = add((int32_t)c);
+        }
+        const bool is_l = m.fl[f] == (int32_t)c;
+        (is_l ? f_slot_l : f_slot_r)[f] = (int32_t)(base + so);
+        (is_l ? f_diag_l : f_diag_r)[f] = (int32_t)(base + sd);
+      } else if (bc_type[f] == PG_BC_FIXED) {
+        f_diag_l[f] = (int32_t)(base + add((int32_t)c));
+      }
+    }
+    for (size_t k = 0; k < row.size(); ++k) {
+      if (row[k] == (int32_t)c) p.diag[c] = (int32_t)(base + k);
+      p.col_ind.push_back(row[k]);
+    }
+    PG_CHECK_ARG(p.col_ind.size() < ((size_t)1 << 31),
+                 "pg_eqn_create: too many matrix entries");
+    p.row_ptr[c + 1] = (int32_t)p.col_ind.size();
+  }
+  p.nnz = (int64_t)p.col_ind.size();
+
+  // Greedy face colouring in face-id order: a face takes the lowest colour
+  // that no other face of its cells has; interior faces use colours
+  // [0, n_interior_colors), boundary faces the colours after them.  Faces of
+  // one colour share no cell, so one launch per colour scatters into the
+  // diagonal and the rhs of both cells without atomics.
+  std::vector<uint64_t> used(n, 0);
+  std::vector<int32_t> color(nf, -1);
+  int max_c = -1;
+  for (int64_t f = 0; f < nf; ++f) {
+    if (m.fr[f] < 0) continue;
+    uint64_t u = used[m.fl[f]] | used[m.fr[f]];
+    PG_CHECK_ARG(~u != 0, "pg_eqn_create: more than 64 face colours");
+    int cidx = __builtin_ctzll(~u);
+    color[f] = cidx;
+    used[m.fl[f]] |= 1ull << cidx;
+    used[m.fr[f]] |= 1ull << cidx;
+    max_c = std::max(max_c, cidx);
+  }
+  p.n_interior_colors = max_c + 1;
+  std::fill(used.begin(), used.end(), 0);
+  int max_b = -1;
+  for (int64_t f = 0; f < nf; ++f) {
+    if (m.fr[f] >= 0) continue;
+    uint64_t u = used[m.fl[f]];
+    PG_CHECK_ARG(~u != 0, "pg_eqn_create: more than 64 boundary face colours");
+    int cidx = __builtin_ctzll(~u);
+    used[m.fl[f]] |= 1ull << cidx;
+    color[f] = p.n_interior_colors + cidx;
+    max_b = std::max(max_b, cidx);
+  }
+  const int n_colors = p.n_interior_colors + max_b + 1;
+  p.color_ptr.assign(n_colors + 1, 0);
+  for (int64_t f = 0; f < nf; ++f) ++p.color_ptr[color[f] + 1];
+  for (int c = 0; c < n_colors; ++c) p.color_ptr[c + 1] += p.color_ptr[c];
+  std::vector<int32_t> fill(p.color_ptr.begin(), p.color_ptr.end() - 1);
+  p.cface.assign(nf, -1);
+  for (int32_t f = 0; f < (int32_t)nf; ++f) p.cface[fill[color[f]]++] = f;
+  p.slot_lr.resize(nf);
+  p.slot_rl.resize(nf);
+  p.diag_l.resize(nf);
+  p.diag_r.resize(nf);
+  for (int64_t k = 0; k < nf; ++k) {
+    const int32_t f = p.cface[k];
+    p.slot_lr[k] = f_slot_l[f];
+    p.slot_rl[k] = f_slot_r[f];
+    p.diag_l[k] = f_diag_l[f];
+    p.diag_r[k] = f_diag_r[f];
+  }
+  return PG_OK;
+}
+
+// --------------------------------------------------------------- analysis
+namespace {
+
+// Recursive graph bisection on the symmetrised pattern.  Each range of
+// vertices is reordered by breadth-first distance from a pseudo-peripheral
+// vertex (two sweeps) and cut so both halves hold whole multiples of the
+// target subdomain size; cuts recurse until a range fits one subdomain.
+// Emission order is left-to-right, so consecutive subdomains are neighbours.
+struct Bisector {
+  int64_t n;
+  const std::vector<int64_t> &ap;
+  const std::vector<int32_t> &aj;
+  std::vector<int32_t> in_range, seen;
+  int32_t range_stamp = 0, seen_stamp = 0;
+  std::vector<int32_t> queue;
+
+  Bisector(int64_t n_, const std::vector<int64_t> &ap_,
+           const std::vector<int32_t> &aj_)
+      : n(n_), ap(ap_), aj(aj_), in_range(n_, 0), seen(n_, 0) {
+    queue.reserve(n_);
+  }
+
+  // BFS over the vertices stamped in_range, starting at s and restarting at
+  // unvisited vertices of `verts` so disconnected ranges are covered.
+  // Returns the last vertex dequeued; the visit order is left in `queue`.
+  int32_t bfs(int32_t s, const int32_t *verts, int64_t cnt) {
+    ++seen_stamp;
+    queue.clear();
+    int64_t head = 0, scan = 0;
+    int32_t last = s;
+    auto push = [&](int32_t v) {
+      seen[v] = seen_stamp;
+      queue.push_back(v);
+    };
+    push(s);
+    while ((int64_t)queue.size() < cnt) {
+      while (head < (int64_t)queue.size()) {
+        int32_t v = queue[head++];
+        last = v;
+        for (int64_t k = ap[v]; k < ap[v + 1]; ++k) {
+          int32_t w = aj[k];
+          if (in_range[w] == range_stamp && seen[w] != seen_stamp) push(w);
+        }
+      }
+      while ((int64_t)queue.size() < cnt && seen[verts[scan]] == seen_stamp)
+        ++scan;
+      if ((int64_t)queue.size() < cnt) push(verts[scan]);
+    }
+    while (head < (int64_t)queue.size()) last = queue[head++];
+    return last;
+  }
+};
+
+}  // namespace
+
+int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
+            int subdomain_rows, Analysis &a) {
+  PG_CHECK_ARG(n > 0 && row_ptr && col_ind, "analyse: empty matrix");
+  PG_CHECK_ARG(row_ptr[0] == 0, "row_ptr[0] must be 0");
+  for (int64_t i = 0; i < n; ++i)
+    PG_CHECK_ARG(row_ptr[i + 1] >= row_ptr[i], "row_ptr must be non-decreasing");
+  const int64_t n_src = row_ptr[n];
+  for (int64_t k = 0; k < n_src; ++k)
+    PG_CHECK_ARG(col_ind[k] < n, "column index out of range");
+
+  a = Analysis();
+  a.n = n;
+  a.n_src = n_src;
+
+  // 1. compact rows: drop placeholders, merge repeated columns
+  std::vector<int64_t> cp(n + 1, 0);
+  std::vector<int32_t> cc, cs;  // column, source index
+  cc.reserve(n_src);
+  cs.reserve(n_src);
+  {
+    std::vector<int32_t> mark(n, -1);
+    for (int64_t i = 0; i < n; ++i) {
+      const int64_t start = (int64_t)cc.size();
+      for (int64_t k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+        const int32_t c = col_ind[k];
+        if (c < 0) continue;
+        if (mark[c] >= start) {  // repeated column: summed later
+          a.dup_src.push_back((int32_t)k);
+          a.dup_dst.push_back(mark[c]);  // compact index, remapped below
+          continue;
+        }
+        mark[c] = (int32_t)cc.size();
+        cc.push_back(c);
+        cs.push_back((int32_t)k);
+      }
+      cp[i + 1] = (int64_t)cc.size();
+    }
+  }
+  a.nnz = (int64_t)cc.size();
+
+  // 2. symmetrised adjacency without the diagonal
+  std::vector<int64_t> ap(n + 1, 0);
+  std::vector<int32_t> aj;
+  {
+    std::vector<int64_t> deg(n, 0);
+    for (int64_t i = 0; i < n; ++i)
+      for (int64_t k = cp[i]; k < cp[i + 1]; ++k)
+        if (cc[k] != i) {
+          ++deg[i];
+          ++deg[cc[k]];
+        }
+    for (int64_t i = 0; i < n; ++i) ap[i + 1] = ap[i] + deg[i];
+    aj.resize(ap[n]);
+    std::vector<int64_t> pos(ap.begin(), ap.end() - 1);
+    for (int64_t i = 0; i < n; ++i)
+      for (int64_t k = cp[i]; k < cp[i + 1]; ++k)
+        if (cc[k] != i) {
+          aj[pos[i]++] = cc[k];
+          aj[pos[cc[k]]++] = (int32_t)i;
+        }
+    // sort + unique each list
+    std::vector<int64_t> np(n + 1, 0);
+    int64_t w = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      std::sort(aj.begin() + ap[i], aj.begin() + ap[i + 1]);
+      int64_t e = std::unique(aj.begin() + ap[i], aj.begin() + ap[i + 1]) -
+                  aj.begin();
+      for (int64_t k = ap[i]; k < e; ++k) aj[w++] = aj[k];
+      np[i + 1] = w;
+    }
+    aj.resize(w);
+    ap.swap(np);
+  }
+
+  // 3. partition
+  int64_t target = subdomain_rows;
+  if (target == 0) target = 1024;
+  std::vector<int32_t> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::vector<std::pair<int64_t, int64_t>> parts;  // ranges of `order`
+  if (target < 0 || n <= target) {
+    parts.push_back({0, n});
+    a.global_ilu = (target < 0) || n <= target;
+  } else {
+    Bisector bs(n, ap, aj);
+    std::vector<std::pair<int64_t, int64_t>> stack{{0, n}};
+    while (!stack.empty()) {
+      auto [lo, hi] = stack.back();
+      stack.pop_back();
+      const int64_t cnt = hi - lo;
+      if (cnt <= target) {
+        parts.push_back({lo, hi});
+        continue;
+      }
+      ++bs.range_stamp;
+      for (int64_t k = lo; k < hi; ++k) bs.in_range[order[k]] = bs.range_stamp;
+      int32_t start = *std::min_element(order.begin() + lo, order.begin() + hi);
+      int32_t far = bs.bfs(start, order.data() + lo, cnt);
+      bs.bfs(far, order.data() + lo, cnt);
+      std::copy(bs.queue.begin(), bs.queue.end(), order.begin() + lo);
+      const int64_t k_parts = (cnt + target - 1) / target;
+      const int64_t left = cnt * (k_parts / 2) / k_parts;
+      stack.push_back({lo + left, hi});
+      stack.push_back({lo, lo + left});
+    }
+  }
+  a.n_sub = (int)parts.size();
+  a.part.assign(n, 0);
+  for (int s = 0; s < a.n_sub; ++s)
+    for (int64_t k = parts[s].first; k < parts[s].second; ++k)
+      a.part[order[k]] = s;
+
+  // 4. levels inside each subdomain (rows visited in increasing original
+  //    index; a row's level is one more than its deepest earlier neighbour
+  //    in the same subdomain) and the level-ordered permutation
+  std::vector<int32_t> level(n, 0);
+  a.perm.resize(n);
+  a.sub_ptr.assign(a.n_sub + 1, 0);
+  a.sub_lvl.assign(a.n_sub + 1, 0);
+  a.lvl_ptr.assign(1, 0);
+  int64_t out = 0;
+  for (int s = 0; s < a.n_sub; ++s) {
+    std::vector<int32_t> rows(order.begin() + parts[s].first,
+                              order.begin() + parts[s].second);
+    std::sort(rows.begin(), rows.end());
+    int32_t nl = 0;
+    for (int32_t i : rows) {
+      int32_t lv = 0;
+      for (int64_t k = ap[i]; k < ap[i + 1]; ++k) {
+        const int32_t j = aj[k];
+        if (j < i && a.part[j] == s) lv = std::max(lv, level[j] + 1);
+      }
+      level[i] = lv;
+      nl = std::max(nl, lv + 1);
+    }
+    std::stable_sort(rows.begin(), rows.end(), [&](int32_t x, int32_t y) {
+      return level[x] < level[y];
+    });
+    a.sub_ptr[s] = (int32_t)out;
+    for (size_t k = 0; k < rows.size(); ++k) {
+      if (k == 0 || level[rows[k]] != level[rows[k - 1]])
+        if (k > 0) a.lvl_ptr.push_back((int32_t)(out + k));
+      a.perm[out + k] = rows[k];
+    }
+    out += (int64_t)rows.size();
+    a.lvl_ptr.push_back((int32_t)out);
+    a.sub_lvl[s + 1] = (int32_t)a.lvl_ptr.size() - 1;
+    a.max_sub_rows = std::max(a.max_sub_rows, (int)rows.size());
+    a.max_levels = std::max(a.max_levels, (int)nl);
+  }
+  a.sub_ptr[a.n_sub] = (int32_t)n;
+  a.iperm.resize(n);
+  for (int64_t k = 0; k < n; ++k) a.iperm[a.perm[k]] = (int32_t)k;
+
+  // 5. permuted CSR, columns sorted
+  a.prp.assign(n + 1, 0);
+  a.pci.resize(a.nnz);
+  a.psrc.resize(a.nnz);
+  std::vector<int32_t> cmap(a.nnz);  // compact index -> permuted index
+  {
+    std::vector<std::pair<int32_t, int32_t>> tmp;
+    int64_t w = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      const int32_t r = a.perm[i];
+      tmp.clear();
+      for (int64_t k = cp[r]; k < cp[r + 1]; ++k)
+        tmp.push_back({a.iperm[cc[k]], (int32_t)k});
+      std::sort(tmp.begin(), tmp.end());
+      for (auto &t : tmp) {
+        a.pci[w] = t.first;
+        a.psrc[w] = cs[t.second];
+        cmap[t.second] = (int32_t)w;
+        ++w;
+      }
+      a.prp[i + 1] = (int32_t)w;
+    }
+  }
+  for (auto &d : a.dup_dst) d = cmap[d];
+
+  // 6. ILU(0) storage: the entries of each row inside its subdomain,
+  //    L (columns before the row), diagonal, U (columns after)
+  a.lrp.assign(n + 1, 0);
+  a.ldg.assign(n, -1);
+  a.lci.clear();
+  a.lsrc.clear();
+  for (int s = 0; s < a.n_sub; ++s) {
+    const int32_t r0 = a.sub_ptr[s], r1 = a.sub_ptr[s + 1];
+    const int64_t e0 = (int64_t)a.lci.size();
+    for (int32_t i = r0; i < r1; ++i) {
+      bool have_diag = false;
+      for (int32_t k = a.prp[i]; k < a.prp[i + 1]; ++k) {
+        const int32_t c = a.pci[k];
+        if (c < r0 || c >= r1) continue;
+        if (c == i) {
+          a.ldg[i] = (int32_t)a.lci.size();
+          have_diag = true;
+        } else if (c > i && !have_diag) {  // structural zero diagonal
+          a.ldg[i] = (int32_t)a.lci.size();
+          a.lci.push_back(i - r0);
+          a.lsrc.push_back(-1);
+          have_diag = true;
+        }
+        a.lci.push_back(c - r0);
+        a.lsrc.push_back(k);
+      }
+      if (!have_diag) {
+        a.ldg[i] = (int32_t)a.lci.size();
+        a.lci.push_back(i - r0);
+        a.lsrc.push_back(-1);
+      }
+      a.lrp[i + 1] = (int32_t)a.lci.size();
+    }
+    a.max_sub_lu = std::max(a.max_sub_lu, (int)((int64_t)a.lci.size() - e0));
+  }
+  return PG_OK;
+}
+
+}  // namespace pg

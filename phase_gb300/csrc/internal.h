@@ -1,0 +1,179 @@
+// Internal declarations shared by the host code and the CUDA kernels of
+// libphase_gb300.  Not part of the public C ABI (include/phase_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/phase_gb300.h"
+
+namespace pg {
+
+// ---------------------------------------------------------------- errors
+void set_error(const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what, const char *file, int line);
+
+#define PG_CUDA(call)                                                      \
+  do {                                                                     \
+    cudaError_t e_ = (call);                                               \
+    if (e_ != cudaSuccess) return ::pg::cuda_fail(e_, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define PG_CHECK_ARG(cond, msg)                                            \
+  do {                                                                     \
+    if (!(cond)) {                                                         \
+      ::pg::set_error(msg);                                                \
+      return PG_BAD_ARG;                                                   \
+    }                                                                      \
+  } while (0)
+
+cudaStream_t stream();
+
+// Device buffer owned by the library (cudaMalloc / cudaFree).
+template <class T> struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  // (re)allocate to hold at least count elements; contents undefined
+  cudaError_t reserve(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    release();
+    size_t bytes = (count ? count : 1) * sizeof(T) + 64;  // tail padding
+    cudaError_t e = cudaMalloc((void **)&p, bytes);
+    if (e == cudaSuccess) n = count;
+    return e;
+  }
+  cudaError_t upload(const T *h, size_t count) {
+    cudaError_t e = reserve(count);
+    if (e != cudaSuccess) return e;
+    if (!count) return cudaSuccess;
+    return cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice,
+                           stream());
+  }
+  cudaError_t upload(const std::vector<T> &v) { return upload(v.data(), v.size()); }
+  cudaError_t zero(size_t count) {
+    cudaError_t e = reserve(count);
+    if (e != cudaSuccess) return e;
+    return cudaMemsetAsync(p, 0, (count ? count : 1) * sizeof(T), stream());
+  }
+};
+
+// Copy count elements from src (host or device per ptr_kind) to dst (device).
+cudaError_t copy_in(void *dst, const void *src, size_t bytes, int ptr_kind);
+cudaError_t copy_out(void *dst, const void *src, size_t bytes, int ptr_kind);
+
+// ------------------------------------------------------------------ mesh
+// Host mesh, built once per pg_mesh_create (FiniteVolumeGrid2D semantics).
+struct HostMesh {
+  int64_t n_cells = 0, n_faces = 0, n_interior = 0, n_boundary = 0;
+  std::vector<double> cx, cy, vol;              // per cell
+  std::vector<int32_t> fl, fr;                  // per face (fr = -1 boundary)
+  std::vector<double> fcx, fcy, fnx, fny;       // per face centroid, normal
+  // per-cell links: interior links then boundary links, each in face order
+  std::vector<int64_t> link_ptr;
+  std::vector<int32_t> link_face, link_cell;    // link_cell = -1 boundary
+  std::vector<int32_t> n_interior_links;        // per cell
+};
+
+int build_host_mesh(const double *nodes_xy, int64_t n_nodes,
+                    const int64_t *cptr, const int64_t *cind, int64_t n_cells,
+                    HostMesh &m);
+
+// Device geometry per face side, precomputed once per mesh so assembly
+// reproduces the reference's arithmetic (coeff = gamma*dot(r,Sf)/|r|^2).
+struct DevMesh {
+  DevBuf<double> cx, cy, vol;
+  DevBuf<int32_t> fl, fr;
+  DevBuf<double> fcx, fcy, fnx, fny;
+  DevBuf<int64_t> link_ptr;
+  DevBuf<int32_t> link_face;
+};
+
+}  // namespace pg
+
+struct pg_mesh {
+  pg::HostMesh h;
+  pg::DevMesh d;
+  // link geometry per face side: dot(r, Sf_out) for the lCell and rCell
+  // links, |r|^2, and the sign that turns the face normal into each side's
+  // outward normal
+  std::vector<double> dot_l, dot_r, msq;
+  std::vector<int8_t> sgn_l, sgn_r;
+};
+
+namespace pg {
+
+// ------------------------------------------------------------- equation
+struct EqnPattern {
+  int64_t n = 0, nnz = 0;
+  std::vector<int32_t> row_ptr, col_ind;
+  std::vector<int32_t> diag;  // position of diagonal per row (-1 if none)
+  // face-coloured scatter schedule: faces permuted so each colour is a
+  // contiguous range; per permuted face: original id and target slots.
+  std::vector<int32_t> color_ptr;       // [n_colors+1]
+  std::vector<int32_t> cface;           // original face id
+  std::vector<int32_t> slot_lr, slot_rl, diag_l, diag_r;  // -1 if unused
+  int n_interior_colors = 0;
+};
+
+int build_pattern(const HostMesh &m, int gamma_kind, const int32_t *bc_type,
+                  EqnPattern &p);
+
+}  // namespace pg
+
+struct pg_eqn {
+  const pg_mesh *mesh = nullptr;
+  int gamma_kind = 0;
+  pg::EqnPattern p;
+  std::vector<int32_t> bc_type;
+  pg::DevBuf<int32_t> row_ptr, col_ind;
+  pg::DevBuf<double> vals, rhs;
+  // colour-ordered face schedule on device
+  pg::DevBuf<int32_t> cface, cl, cr, slot_lr, slot_rl, diag_l, diag_r;
+  pg::DevBuf<int32_t> cbc;  // bc type per colour-ordered face
+  pg::DevBuf<double> cdot_l, cdot_r, cmsq, csfl_x, csfl_y, csfr_x, csfr_y;
+  pg::DevBuf<double> stage_a, stage_b, stage_c;  // host-input staging
+  uint64_t version = 0;  // bumps on every assembly
+  uint64_t pattern_id = 0;
+};
+
+namespace pg {
+
+// --------------------------------------------------------------- analysis
+// Sparsity analysis of a solver matrix: additive-Schwarz partition, level
+// schedule within each subdomain and the permutation that makes every
+// subdomain contiguous and level-ordered.
+struct Analysis {
+  int64_t n = 0;
+  int64_t nnz = 0;        // entries after dropping placeholders/merging
+  int64_t n_src = 0;      // length of the caller's col_ind array
+  int n_sub = 0;
+  int max_sub_rows = 0, max_sub_lu = 0, max_levels = 0;
+  std::vector<int32_t> perm, iperm;        // new->old, old->new
+  std::vector<int32_t> prp, pci, psrc;     // permuted CSR; psrc -> caller idx
+  std::vector<int32_t> dup_dst, dup_src;   // extra summed duplicates
+  std::vector<int32_t> sub_ptr;            // [n_sub+1] permuted row starts
+  std::vector<int32_t> sub_lvl;            // [n_sub+1] index into lvl_ptr
+  std::vector<int32_t> lvl_ptr;            // level row boundaries
+  // ILU(0) storage restricted to subdomains
+  std::vector<int32_t> lrp, ldg, lsrc;     // row ptr, diag pos, -> perm entry
+  std::vector<int32_t> lci;                // subdomain-local column
+  std::vector<int32_t> part;               // subdomain of each original row
+  bool global_ilu = false;                 // one subdomain holding all rows
+};
+
+int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
+            int subdomain_rows, Analysis &a);
+
+}  // namespace pg

@@ -1,0 +1,836 @@
+// CUDA kernels of libphase_gb300, written for sm_103a (GB300).
+//
+// The sparse pressure path is HBM-bandwidth bound and uses no tensor cores.
+//  * Assembly: face-coloured, atomic-free scatter of fv::laplacian + src::div
+//    into the CSR values and rhs (one launch per colour).
+//  * Solver: values are gathered once per solve into a permuted CSR in which
+//    every Schwarz subdomain is a contiguous, level-ordered row range.  ILU(0)
+//    is factorised and applied per subdomain by one CTA that walks the level
+//    schedule with a barrier between levels; the subdomain's factor and
+//    vector are staged in shared memory for the triangular sweeps.
+//  * BiCGStab: every dot product is fused into the kernel that produces its
+//    operands (warp shuffle + block tree + last-block grid reduction in a
+//    fixed order, so results are deterministic) and the scalar recurrences
+//    (alpha, beta, omega, convergence) run on the device in the last block.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+
+#include "../../include/phase_gb300.h"
+#include "kernels.cuh"
+
+namespace pg {
+
+static std::atomic<uint64_t> g_launches{0};
+void count_launches(int k) { g_launches.fetch_add((uint64_t)k, std::memory_order_relaxed); }
+uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
+namespace {
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ bool finite(double v) { return isfinite(v); }
+
+// Block-reduce ND values, store the block partials, and let the last block
+// to finish reduce all partials (fixed order) into tot[].  Returns true in
+// the last block only; tot[] is valid in all its threads.
+template <int ND>
+__device__ bool grid_reduce(double (&v)[ND], const RedWork &w,
+                            double (&tot)[ND]) {
+  __shared__ double sh[ND][kVecBlock / 32];
+  __shared__ bool is_last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < ND; ++k) {
+    double s = warp_sum(v[k]);
+    if (lane == 0) sh[k][warp] = s;
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+      double s = lane < nw ? sh[k][lane] : 0.;
+      s = warp_sum(s);
+      if (lane == 0) w.partials[k * w.grid + blockIdx.x] = s;
+    }
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    unsigned int t = atomicAdd(w.ticket, 1u);
+    is_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!is_last) return false;
+  __threadfence();
+#pragma unroll
+  for (int k = 0; k < ND; ++k) {
+    double s = 0.;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
+      s += __ldcg(&w.partials[k * w.grid + i]);
+    s = warp_sum(s);
+    if (lane == 0) sh[k][warp] = s;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < ND; ++k) {
+    double s = 0.;
+    for (int i = 0; i < nw; ++i) s += sh[k][i];
+    tot[k] = s;
+  }
+  if (threadIdx.x == 0) *w.ticket = 0u;
+  return true;
+}
+
+// ------------------------------------------------------------ assembly
+// One launch per interior colour: no two faces of a colour share a cell,
+// so every += below has a single writer in the launch.  Arithmetic uses
+// explicitly rounded operations in the reference's order:
+// coeff = (gamma * dot(r, Sf)) / |r|^2  (Laplacian.h:139-142, 55-58).
+__global__ void k_assemble_interior(
+    int nf, int off, const int32_t *__restrict__ cface,
+    const int32_t *__restrict__ cl, const int32_t *__restrict__ cr,
+    const double *__restrict__ dot_l, const double *__restrict__ dot_r,
+    const double *__restrict__ msq, const int32_t *__restrict__ slot_lr,
+    const int32_t *__restrict__ slot_rl, const int32_t *__restrict__ diag_l,
+    const int32_t *__restrict__ diag_r, const double *__restrict__ sfl_x,
+    const double *__restrict__ sfl_y, const double *__restrict__ sfr_x,
+    const double *__restrict__ sfr_y, const double *__restrict__ gamma_face,
+    double gamma_scalar, const double *__restrict__ u_face,
+    double *__restrict__ vals, double *__restrict__ rhs) {
+  const int k = off + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= off + nf) return;
+  const int f = cface[k];
+  const int l = cl[k], r = cr[k];
+  const double g = gamma_face ? gamma_face[f] : gamma_scalar;
+  const double m2 = msq[k];
+  const double c_l = __ddiv_rn(__dmul_rn(g, dot_l[k]), m2);
+  const double c_r = __ddiv_rn(__dmul_rn(g, dot_r[k]), m2);
+  vals[slot_lr[k]] = __dadd_rn(vals[slot_lr[k]], c_l);
+  vals[slot_rl[k]] = __dadd_rn(vals[slot_rl[k]], c_r);
+  vals[diag_l[k]] = __dadd_rn(vals[diag_l[k]], -c_l);
+  vals[diag_r[k]] = __dadd_rn(vals[diag_r[k]], -c_r);
+  if (u_face) {
+    // src::div(u): rhs_ -= dot(u_f, Sf_out) for both cells (Source.cpp:11-15)
+    const double ux = u_face[2 * f], uy = u_face[2 * f + 1];
+    const double dl = __dadd_rn(__dmul_rn(ux, sfl_x[k]), __dmul_rn(uy, sfl_y[k]));
+    const double dr = __dadd_rn(__dmul_rn(ux, sfr_x[k]), __dmul_rn(uy, sfr_y[k]));
+    rhs[l] = __dadd_rn(rhs[l], -dl);
+    rhs[r] = __dadd_rn(rhs[r], -dr);
+  }
+}
+
+// Boundary colours: FIXED faces add -coeff to the owner's diagonal and
+// coeff * phi_b to its rhs (Laplacian.h:66-69, 150-153); every boundary face
+// contributes its flux to src::div.
+__global__ void k_assemble_boundary(
+    int nf, int off, const int32_t *__restrict__ cface,
+    const int32_t *__restrict__ cl, const int32_t *__restrict__ bc,
+    const double *__restrict__ dot_l, const double *__restrict__ msq,
+    const int32_t *__restrict__ diag_l, const double *__restrict__ sfl_x,
+    const double *__restrict__ sfl_y, const double *__restrict__ gamma_face,
+    double gamma_scalar, const double *__restrict__ bc_value,
+    const double *__restrict__ u_face, double *__restrict__ vals,
+    double *__restrict__ rhs) {
+  const int k = off + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= off + nf) return;
+  const int f = cface[k];
+  const int l = cl[k];
+  double acc = rhs[l];
+  if (bc[k] == PG_BC_FIXED) {
+    const double g = gamma_face ? gamma_face[f] : gamma_scalar;
+    const double c = __ddiv_rn(__dmul_rn(g, dot_l[k]), msq[k]);
+    vals[diag_l[k]] = __dadd_rn(vals[diag_l[k]], -c);
+    acc = __dadd_rn(acc, __dmul_rn(c, bc_value[f]));
+  }
+  if (u_face) {
+    const double ux = u_face[2 * f], uy = u_face[2 * f + 1];
+    acc = __dadd_rn(acc, -__dadd_rn(__dmul_rn(ux, sfl_x[k]), __dmul_rn(uy, sfl_y[k])));
+  }
+  rhs[l] = acc;
+}
+
+// dt / rho_f (FractionalStepMultiphase.cpp:175-185 with the distance-weighted
+// face interpolation FiniteVolumeField.tpp:130-162, Face.cpp:60-64)
+__global__ void k_dt_over_rho(int nf, const int32_t *__restrict__ fl,
+                              const int32_t *__restrict__ fr,
+                              const double *__restrict__ fcx,
+                              const double *__restrict__ fcy,
+                              const double *__restrict__ cx,
+                              const double *__restrict__ cy,
+                              const double *__restrict__ gc, double rho1,
+                              double rho2, double dt, double *__restrict__ out) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int l = fl[f], r = fr[f];
+  double gf;
+  if (r < 0) {
+    gf = gc[l];
+  } else {
+    const double ax = __dadd_rn(fcx[f], -cx[r]), ay = __dadd_rn(fcy[f], -cy[r]);
+    const double bx = __dadd_rn(fcx[f], -cx[l]), by = __dadd_rn(fcy[f], -cy[l]);
+    const double l1 = __dsqrt_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)));
+    const double l2 = __dsqrt_rn(__dadd_rn(__dmul_rn(bx, bx), __dmul_rn(by, by)));
+    const double w = __ddiv_rn(l1, __dadd_rn(l1, l2));
+    gf = __dadd_rn(__dmul_rn(w, gc[l]), __dmul_rn(__dadd_rn(1., -w), gc[r]));
+  }
+  const double c = fmin(fmax(gf, 0.), 1.);
+  const double rho = __dadd_rn(rho1, __dmul_rn(c, __dadd_rn(rho2, -rho1)));
+  out[f] = __ddiv_rn(dt, rho);
+}
+
+// ScalarGradient::computeFaces (ScalarGradient.cpp:34-47)
+__global__ void k_grad_faces(int nf, const int32_t *__restrict__ fl,
+                             const int32_t *__restrict__ fr,
+                             const double *__restrict__ fcx,
+                             const double *__restrict__ fcy,
+                             const double *__restrict__ cx,
+                             const double *__restrict__ cy,
+                             const double *__restrict__ phi,
+                             const double *__restrict__ phi_face,
+                             double *__restrict__ gf) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int l = fl[f], r = fr[f];
+  double dx, dy, d;
+  if (r >= 0) {
+    dx = __dadd_rn(cx[r], -cx[l]);
+    dy = __dadd_rn(cy[r], -cy[l]);
+    d = __dadd_rn(phi[r], -phi[l]);
+  } else {
+    dx = __dadd_rn(fcx[f], -cx[l]);
+    dy = __dadd_rn(fcy[f], -cy[l]);
+    d = __dadd_rn(phi_face[f], -phi[l]);
+  }
+  const double m2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+  gf[2 * f] = __ddiv_rn(__dmul_rn(d, dx), m2);
+  gf[2 * f + 1] = __ddiv_rn(__dmul_rn(d, dy), m2);
+}
+
+// ScalarGradient::compute(FACE_TO_CELL) (ScalarGradient.cpp:56-73): |Sf|
+// weighted average of the face gradients over the links, in link order.
+__global__ void k_grad_cells(int n, const int64_t *__restrict__ link_ptr,
+                             const int32_t *__restrict__ link_face,
+                             const double *__restrict__ fnx,
+                             const double *__restrict__ fny,
+                             const double *__restrict__ gf,
+                             double *__restrict__ gc) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  double tx = 0., ty = 0., sx = 0., sy = 0.;
+  for (int64_t k = link_ptr[c]; k < link_ptr[c + 1]; ++k) {
+    const int f = link_face[k];
+    const double ax = fabs(fnx[f]), ay = fabs(fny[f]);
+    tx = __dadd_rn(tx, __dmul_rn(gf[2 * f], ax));
+    ty = __dadd_rn(ty, __dmul_rn(gf[2 * f + 1], ay));
+    sx = __dadd_rn(sx, ax);
+    sy = __dadd_rn(sy, ay);
+  }
+  gc[2 * c] = __ddiv_rn(tx, sx);
+  gc[2 * c + 1] = __ddiv_rn(ty, sy);
+}
+
+// --------------------------------------------------------- permutation
+__global__ void k_permute_values(int nnz, const int32_t *__restrict__ psrc,
+                                 const double *__restrict__ src,
+                                 double *__restrict__ dst) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < nnz) dst[j] = src[psrc[j]];
+}
+// Repeated columns of a row are summed in the caller's order by one thread
+// (they only occur in hand-built inputs, never in assembled equations).
+__global__ void k_add_dups(int nd, const int32_t *__restrict__ dd,
+                           const int32_t *__restrict__ ds,
+                           const double *__restrict__ src,
+                           double *__restrict__ dst) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  for (int k = 0; k < nd; ++k) dst[dd[k]] += src[ds[k]];
+}
+__global__ void k_permute_vec(int n, const int32_t *__restrict__ perm,
+                              const double *__restrict__ src, double scale,
+                              double *__restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = scale * src[perm[i]];
+}
+__global__ void k_unpermute_vec(int n, const int32_t *__restrict__ perm,
+                                const double *__restrict__ src,
+                                double *__restrict__ dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[perm[i]] = src[i];
+}
+
+// ------------------------------------------------------------- ILU(0)
+// Row-wise IKJ ILU(0) (Saad, Iterative Methods for Sparse Linear Systems,
+// Alg. 10.4) on the diagonal block of one subdomain.  The CTA walks the
+// level schedule; rows of one level depend only on rows of earlier levels,
+// which the barrier has completed.  Pivots are computed in FP64.
+template <class MT>
+__global__ void k_ilu0_factor(SolverDev d, const double *__restrict__ pvals,
+                              MT *__restrict__ lu, MT *__restrict__ ldinv,
+                              int *__restrict__ bad) {
+  const int s = blockIdx.x;
+  const int r0 = d.sub_ptr[s], r1 = d.sub_ptr[s + 1];
+  const int e0 = d.lrp[r0], e1 = d.lrp[r1];
+  for (int j = e0 + threadIdx.x; j < e1; j += blockDim.x) {
+    const int src = d.lsrc[j];
+    lu[j] = (MT)(src >= 0 ? pvals[src] : 0.);
+  }
+  __syncthreads();
+  const int l0 = d.sub_lvl[s], l1 = d.sub_lvl[s + 1];
+  for (int lv = l0; lv < l1; ++lv) {
+    const int a = d.lvl_ptr[lv], b = d.lvl_ptr[lv + 1];
+    for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
+      const int rb = d.lrp[i], re = d.lrp[i + 1], dg = d.ldg[i];
+      for (int j = rb; j < dg; ++j) {
+        const int k = r0 + d.lci[j];
+        const double ukk = (double)lu[d.ldg[k]];
+        const double lik = (double)lu[j] / ukk;
+        lu[j] = (MT)lik;
+        // a_ic -= l_ik * u_kc for c in U(k) that is also in row i
+        int q = j + 1;
+        const int ke = d.lrp[k + 1];
+        for (int jj = d.ldg[k] + 1; jj < ke; ++jj) {
+          const int c = d.lci[jj];
+          while (q < re && d.lci[q] < c) ++q;
+          if (q >= re) break;
+          if (d.lci[q] == c) lu[q] = (MT)((double)lu[q] - lik * (double)lu[jj]);
+        }
+      }
+      const double piv = (double)lu[dg];
+      if (piv == 0. || !isfinite(piv)) {
+        atomicAdd(bad, 1);
+        ldinv[i] = (MT)0.;
+      } else {
+        ldinv[i] = (MT)(1. / piv);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <class VT>
+__device__ __forceinline__ VT pre_input(int mode, int i, const VT *r, VT *pv,
+                                        const VT *v, const KScalars *sc) {
+  if (mode == 1) {
+    const VT val = (VT)((double)r[i] + sc->beta * ((double)pv[i] - sc->omega * (double)v[i]));
+    pv[i] = val;
+    return val;
+  } else if (mode == 2) {
+    const VT val = (VT)((double)r[i] - sc->alpha * (double)v[i]);
+    pv[i] = val;
+    return val;
+  }
+  return pv[i];
+}
+
+// Forward/backward sweeps of one subdomain with its factor and vector staged
+// in shared memory.  Layout: z[nr] | dinv[nr] | rp[nr+1] | dg[nr] | ci[ne] |
+// lu[ne].
+template <class VT, class MT, int MODE>
+__global__ void k_ilu0_apply_smem(SolverDev d, const MT *__restrict__ lu,
+                                  const MT *__restrict__ ldinv,
+                                  const VT *__restrict__ r, VT *__restrict__ pv,
+                                  const VT *__restrict__ v, VT *__restrict__ z,
+                                  const KScalars *__restrict__ sc) {
+  if (sc && sc->done) return;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int s = blockIdx.x;
+  const int r0 = d.sub_ptr[s], r1 = d.sub_ptr[s + 1], nr = r1 - r0;
+  const int e0 = d.lrp[r0], ne = d.lrp[r1] - e0;
+  VT *zs = reinterpret_cast<VT *>(smem);
+  size_t off = ((size_t)nr * sizeof(VT) + 15) & ~(size_t)15;
+  MT *dis = reinterpret_cast<MT *>(smem + off);
+  off += ((size_t)nr * sizeof(MT) + 15) & ~(size_t)15;
+  int *rps = reinterpret_cast<int *>(smem + off);
+  off += ((size_t)(nr + 1) * sizeof(int) + 15) & ~(size_t)15;
+  int *dgs = reinterpret_cast<int *>(smem + off);
+  off += ((size_t)nr * sizeof(int) + 15) & ~(size_t)15;
+  int *cis = reinterpret_cast<int *>(smem + off);
+  off += ((size_t)ne * sizeof(int) + 15) & ~(size_t)15;
+  MT *lus = reinterpret_cast<MT *>(smem + off);
+
+  for (int j = threadIdx.x; j < ne; j += blockDim.x) {
+    cis[j] = d.lci[e0 + j];
+    lus[j] = lu[e0 + j];
+  }
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+    rps[i] = d.lrp[r0 + i] - e0;
+    dgs[i] = d.ldg[r0 + i] - e0;
+    dis[i] = ldinv[r0 + i];
+    zs[i] = pre_input<VT>(MODE, r0 + i, r, pv, v, sc);
+  }
+  if (threadIdx.x == 0) rps[nr] = ne;
+  __syncthreads();
+
+  const int l0 = d.sub_lvl[s], l1 = d.sub_lvl[s + 1];
+  for (int lv = l0; lv < l1; ++lv) {
+    const int a = d.lvl_ptr[lv] - r0, b = d.lvl_ptr[lv + 1] - r0;
+    for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
+      VT acc = zs[i];
+      for (int j = rps[i]; j < dgs[i]; ++j) acc -= (VT)lus[j] * zs[cis[j]];
+      zs[i] = acc;
+    }
+    __syncthreads();
+  }
+  for (int lv = l1 - 1; lv >= l0; --lv) {
+    const int a = d.lvl_ptr[lv] - r0, b = d.lvl_ptr[lv + 1] - r0;
+    for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
+      VT acc = zs[i];
+      for (int j = dgs[i] + 1; j < rps[i + 1]; ++j) acc -= (VT)lus[j] * zs[cis[j]];
+      zs[i] = acc * (VT)dis[i];
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) z[r0 + i] = zs[i];
+}
+
+// Same sweeps with the vector and factor in global memory, for subdomains
+// too large for shared memory (the single-subdomain global ILU(0)).
+template <class VT, class MT, int MODE>
+__global__ void k_ilu0_apply_global(SolverDev d, const MT *__restrict__ lu,
+                                    const MT *__restrict__ ldinv,
+                                    const VT *__restrict__ r,
+                                    VT *__restrict__ pv, const VT *__restrict__ v,
+                                    VT *__restrict__ z,
+                                    const KScalars *__restrict__ sc) {
+  if (sc && sc->done) return;
+  const int s = blockIdx.x;
+  const int r0 = d.sub_ptr[s], r1 = d.sub_ptr[s + 1];
+  for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
+    z[i] = pre_input<VT>(MODE, i, r, pv, v, sc);
+  __syncthreads();
+  const int l0 = d.sub_lvl[s], l1 = d.sub_lvl[s + 1];
+  for (int lv = l0; lv < l1; ++lv) {
+    const int a = d.lvl_ptr[lv], b = d.lvl_ptr[lv + 1];
+    for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
+      VT acc = z[i];
+      for (int j = d.lrp[i]; j < d.ldg[i]; ++j)
+        acc -= (VT)lu[j] * z[r0 + d.lci[j]];
+      z[i] = acc;
+    }
+    __syncthreads();
+  }
+  for (int lv = l1 - 1; lv >= l0; --lv) {
+    const int a = d.lvl_ptr[lv], b = d.lvl_ptr[lv + 1];
+    for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
+      VT acc = z[i];
+      for (int j = d.ldg[i] + 1; j < d.lrp[i + 1]; ++j)
+        acc -= (VT)lu[j] * z[r0 + d.lci[j]];
+      z[i] = acc * (VT)ldinv[i];
+    }
+    __syncthreads();
+  }
+}
+
+// Jacobi / identity preconditioner with the same fused updates.
+template <class VT, class MT, int MODE>
+__global__ void k_diag_apply(int n, const MT *__restrict__ dinv,
+                             const VT *__restrict__ r, VT *__restrict__ pv,
+                             const VT *__restrict__ v, VT *__restrict__ z,
+                             const KScalars *__restrict__ sc) {
+  if (sc && sc->done) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    const VT x = pre_input<VT>(MODE, i, r, pv, v, sc);
+    z[i] = dinv ? (VT)dinv[i] * x : x;
+  }
+}
+
+__global__ void k_jacobi_diag(int n, const int32_t *__restrict__ prp,
+                              const int32_t *__restrict__ pci,
+                              const double *__restrict__ pv,
+                              double *__restrict__ dinv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double dv = 0.;
+  for (int j = prp[i]; j < prp[i + 1]; ++j)
+    if (pci[j] == i) dv = pv[j];
+  dinv[i] = dv != 0. ? 1. / dv : 1.;
+}
+
+// ------------------------------------------------------ SpMV + Krylov
+template <class VT, class MT>
+__device__ __forceinline__ VT row_dot(const int32_t *__restrict__ rp,
+                                      const int32_t *__restrict__ ci,
+                                      const MT *__restrict__ val,
+                                      const VT *__restrict__ x, int i) {
+  VT s = 0;
+  const int b = rp[i], e = rp[i + 1];
+  for (int j = b; j < e; ++j) s += (VT)val[j] * x[ci[j]];
+  return s;
+}
+
+template <class VT, class MT>
+__global__ void __launch_bounds__(kVecBlock)
+k_krylov_init(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ b,
+              const VT *__restrict__ x, VT *__restrict__ r, VT *__restrict__ rh,
+              VT *__restrict__ p, VT *__restrict__ v, KScalars *sc, RedWork w) {
+  double acc[2] = {0., 0.};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
+       i += gridDim.x * blockDim.x) {
+    const VT ri = b[i] - row_dot<VT, MT>(d.prp, d.pci, val, x, i);
+    r[i] = ri;
+    rh[i] = ri;
+    p[i] = 0;
+    v[i] = 0;
+    acc[0] += (double)ri * (double)ri;
+    acc[1] += (double)b[i] * (double)b[i];
+  }
+  double tot[2];
+  if (grid_reduce<2>(acc, w, tot) && threadIdx.x == 0) {
+    sc->rr = tot[0];
+    sc->bb = tot[1];
+    sc->rho = tot[0];
+    sc->alpha = 1.;
+    sc->omega = 1.;
+    sc->beta = tot[0];
+    sc->status = PG_OK;
+    sc->done = 0;
+    if (!finite(tot[0]) || !finite(tot[1])) {
+      sc->status = PG_NON_FINITE;
+      sc->done = 1;
+    } else if (tot[0] <= sc->tol2 * tot[1]) {
+      sc->done = 1;
+    }
+  }
+}
+
+template <class VT, class MT>
+__global__ void __launch_bounds__(kVecBlock)
+k_spmv_v(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ ph,
+         VT *__restrict__ v, const VT *__restrict__ rh, KScalars *sc,
+         RedWork w) {
+  if (sc->done) return;
+  double acc[1] = {0.};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
+       i += gridDim.x * blockDim.x) {
+    const VT vi = row_dot<VT, MT>(d.prp, d.pci, val, ph, i);
+    v[i] = vi;
+    acc[0] += (double)rh[i] * (double)vi;
+  }
+  double tot[1];
+  if (grid_reduce<1>(acc, w, tot) && threadIdx.x == 0) {
+    sc->rv = tot[0];
+    if (!finite(tot[0])) {
+      sc->status = PG_NON_FINITE;
+      sc->done = 1;
+    } else if (tot[0] == 0.) {
+      sc->status = PG_BREAKDOWN;
+      sc->done = 1;
+    } else {
+      sc->alpha = sc->rho / tot[0];
+    }
+  }
+}
+
+template <class VT, class MT>
+__global__ void __launch_bounds__(kVecBlock)
+k_spmv_t(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ sh,
+         VT *__restrict__ t, const VT *__restrict__ s, KScalars *sc,
+         RedWork w) {
+  if (sc->done) return;
+  double acc[2] = {0., 0.};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
+       i += gridDim.x * blockDim.x) {
+    const VT ti = row_dot<VT, MT>(d.prp, d.pci, val, sh, i);
+    t[i] = ti;
+    acc[0] += (double)ti * (double)ti;
+    acc[1] += (double)ti * (double)s[i];
+  }
+  double tot[2];
+  if (grid_reduce<2>(acc, w, tot) && threadIdx.x == 0) {
+    sc->tt = tot[0];
+    sc->ts = tot[1];
+    sc->omega = tot[0] > 0. ? tot[1] / tot[0] : 0.;
+  }
+}
+
+template <class VT>
+__global__ void __launch_bounds__(kVecBlock)
+k_update(int n, VT *__restrict__ x, VT *__restrict__ r,
+         const VT *__restrict__ ph, const VT *__restrict__ sh,
+         const VT *__restrict__ s, const VT *__restrict__ t,
+         const VT *__restrict__ rh, KScalars *sc, RedWork w) {
+  if (sc->done) return;
+  const double al = sc->alpha, om = sc->omega;
+  double acc[2] = {0., 0.};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    x[i] = (VT)((double)x[i] + al * (double)ph[i] + om * (double)sh[i]);
+    const VT ri = (VT)((double)s[i] - om * (double)t[i]);
+    r[i] = ri;
+    acc[0] += (double)rh[i] * (double)ri;
+    acc[1] += (double)ri * (double)ri;
+  }
+  double tot[2];
+  if (grid_reduce<2>(acc, w, tot) && threadIdx.x == 0) {
+    const double rho_new = tot[0];
+    sc->rr = tot[1];
+    sc->iter += 1;
+    if (!finite(tot[0]) || !finite(tot[1])) {
+      sc->status = PG_NON_FINITE;
+      sc->done = 1;
+    } else if (tot[1] <= sc->tol2 * sc->bb) {
+      sc->status = PG_OK;
+      sc->done = 1;
+    } else if (sc->iter >= sc->max_iter) {
+      sc->status = PG_MAX_ITERS;
+      sc->done = 1;
+    } else if (rho_new == 0. || om == 0.) {
+      sc->status = PG_BREAKDOWN;
+      sc->done = 1;
+    } else {
+      sc->beta = (rho_new / sc->rho) * (al / om);
+      sc->rho = rho_new;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kVecBlock)
+k_true_residual(SolverDev d, const double *__restrict__ val,
+                const double *__restrict__ b, const double *__restrict__ x,
+                double *__restrict__ r, KScalars *sc, RedWork w) {
+  double acc[1] = {0.};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
+       i += gridDim.x * blockDim.x) {
+    const double ri = x ? b[i] - row_dot<double, double>(d.prp, d.pci, val, x, i)
+                        : b[i];
+    if (r) r[i] = ri;
+    acc[0] += ri * ri;
+  }
+  double tot[1];
+  if (grid_reduce<1>(acc, w, tot) && threadIdx.x == 0) sc->rr_true = tot[0];
+}
+
+inline int blocks_for(int n, int bs) { return (n + bs - 1) / bs; }
+
+}  // namespace
+
+// ---------------------------------------------------------------- launchers
+void launch_assemble_interior(int nf, int off, const int32_t *cface,
+                              const int32_t *cl, const int32_t *cr,
+                              const double *dot_l, const double *dot_r,
+                              const double *msq, const int32_t *slot_lr,
+                              const int32_t *slot_rl, const int32_t *diag_l,
+                              const int32_t *diag_r, const double *sfl_x,
+                              const double *sfl_y, const double *sfr_x,
+                              const double *sfr_y, const double *gamma_face,
+                              double gamma_scalar, const double *u_face,
+                              double *vals, double *rhs, cudaStream_t st) {
+  if (nf <= 0) return;
+  k_assemble_interior<<<blocks_for(nf, 256), 256, 0, st>>>(
+      nf, off, cface, cl, cr, dot_l, dot_r, msq, slot_lr, slot_rl, diag_l,
+      diag_r, sfl_x, sfl_y, sfr_x, sfr_y, gamma_face, gamma_scalar, u_face,
+      vals, rhs);
+  count_launches(1);
+}
+
+void launch_assemble_boundary(int nf, int off, const int32_t *cface,
+                              const int32_t *cl, const int32_t *bc,
+                              const double *dot_l, const double *msq,
+                              const int32_t *diag_l, const double *sfl_x,
+                              const double *sfl_y, const double *gamma_face,
+                              double gamma_scalar, const double *bc_value,
+                              const double *u_face, double *vals, double *rhs,
+                              cudaStream_t st) {
+  if (nf <= 0) return;
+  k_assemble_boundary<<<blocks_for(nf, 256), 256, 0, st>>>(
+      nf, off, cface, cl, bc, dot_l, msq, diag_l, sfl_x, sfl_y, gamma_face,
+      gamma_scalar, bc_value, u_face, vals, rhs);
+  count_launches(1);
+}
+
+void launch_dt_over_rho(int nf, const int32_t *fl, const int32_t *fr,
+                        const double *fcx, const double *fcy, const double *cx,
+                        const double *cy, const double *gamma_cell,
+                        double rho1, double rho2, double dt, double *out,
+                        cudaStream_t st) {
+  if (nf <= 0) return;
+  k_dt_over_rho<<<blocks_for(nf, 256), 256, 0, st>>>(
+      nf, fl, fr, fcx, fcy, cx, cy, gamma_cell, rho1, rho2, dt, out);
+  count_launches(1);
+}
+
+void launch_gradient(int n_cells, int nf, const int32_t *fl,
+                     const int32_t *fr, const double *fcx, const double *fcy,
+                     const double *cx, const double *cy,
+                     const int64_t *link_ptr, const int32_t *link_face,
+                     const int8_t *, const int8_t *, const double *fnx,
+                     const double *fny, const double *phi,
+                     const double *phi_face, double *grad_face,
+                     double *grad_cell, cudaStream_t st) {
+  k_grad_faces<<<blocks_for(nf, 256), 256, 0, st>>>(nf, fl, fr, fcx, fcy, cx,
+                                                     cy, phi, phi_face,
+                                                     grad_face);
+  count_launches(1);
+  if (grad_cell)
+    k_grad_cells<<<blocks_for(n_cells, 256), 256, 0, st>>>(
+        n_cells, link_ptr, link_face, fnx, fny, grad_face, grad_cell);
+    count_launches(1);
+}
+
+void launch_permute_values(int nnz, const int32_t *psrc, const double *src,
+                           double *dst, int n_dup, const int32_t *dup_dst,
+                           const int32_t *dup_src, cudaStream_t st) {
+  k_permute_values<<<blocks_for(nnz, 256), 256, 0, st>>>(nnz, psrc, src, dst);
+  count_launches(1);
+  if (n_dup > 0) {
+    k_add_dups<<<1, 32, 0, st>>>(n_dup, dup_dst, dup_src, src, dst);
+    count_launches(1);
+  }
+}
+
+void launch_permute_vec(int n, const int32_t *perm, const double *src,
+                        double scale, double *dst, cudaStream_t st) {
+  k_permute_vec<<<blocks_for(n, 256), 256, 0, st>>>(n, perm, src, scale, dst);
+  count_launches(1);
+}
+
+void launch_unpermute_vec(int n, const int32_t *perm, const double *src,
+                          double *dst, cudaStream_t st) {
+  k_unpermute_vec<<<blocks_for(n, 256), 256, 0, st>>>(n, perm, src, dst);
+  count_launches(1);
+}
+
+template <class MT>
+void launch_ilu0_factor(const SolverDev &d, const double *pvals, MT *lu,
+                        MT *ldinv, int *bad, cudaStream_t st) {
+  const int threads = d.global_ilu ? 1024 : 128;
+  k_ilu0_factor<MT><<<d.n_sub, threads, 0, st>>>(d, pvals, lu, ldinv, bad);
+  count_launches(1);
+}
+template void launch_ilu0_factor<double>(const SolverDev &, const double *,
+                                         double *, double *, int *,
+                                         cudaStream_t);
+template void launch_ilu0_factor<float>(const SolverDev &, const double *,
+                                        float *, float *, int *, cudaStream_t);
+
+template <class VT, class MT>
+static size_t ilu_smem_bytes(const SolverDev &d) {
+  auto al = [](size_t b) { return (b + 15) & ~(size_t)15; };
+  const size_t nr = d.max_sub_rows, ne = d.max_sub_lu;
+  return al(nr * sizeof(VT)) + al(nr * sizeof(MT)) + al((nr + 1) * 4) +
+         al(nr * 4) + al(ne * 4) + al(ne * sizeof(MT));
+}
+
+template <class VT, class MT, int MODE>
+static void apply_ilu(const SolverDev &d, const MT *lu, const MT *ldinv,
+                      const VT *r, VT *pv, const VT *v, VT *z,
+                      const KScalars *sc, cudaStream_t st) {
+  const size_t smem = ilu_smem_bytes<VT, MT>(d);
+  if (!d.global_ilu && smem <= 200 * 1024) {
+    static bool attr_set = false;
+    if (!attr_set) {
+      cudaFuncSetAttribute(k_ilu0_apply_smem<VT, MT, MODE>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           200 * 1024);
+      attr_set = true;
+    }
+    k_ilu0_apply_smem<VT, MT, MODE><<<d.n_sub, 128, smem, st>>>(d, lu, ldinv, r,
+                                                               pv, v, z, sc);
+    count_launches(1);
+  } else {
+    k_ilu0_apply_global<VT, MT, MODE><<<d.n_sub, 1024, 0, st>>>(d, lu, ldinv, r,
+                                                               pv, v, z, sc);
+    count_launches(1);
+  }
+}
+
+template <class VT, class MT>
+void launch_precond(int precond, int mode, const SolverDev &d, const MT *lu,
+                    const MT *ldinv, const MT *jdinv, const VT *r, VT *pv,
+                    const VT *v, VT *z, const KScalars *sc, cudaStream_t st) {
+  if (precond == PG_PREC_ILU0) {
+    if (mode == 0) apply_ilu<VT, MT, 0>(d, lu, ldinv, r, pv, v, z, sc, st);
+    else if (mode == 1) apply_ilu<VT, MT, 1>(d, lu, ldinv, r, pv, v, z, sc, st);
+    else apply_ilu<VT, MT, 2>(d, lu, ldinv, r, pv, v, z, sc, st);
+  } else {
+    const MT *di = precond == PG_PREC_JACOBI ? jdinv : nullptr;
+    const int g = blocks_for(d.n, 256) < 1216 ? blocks_for(d.n, 256) : 1216;
+    if (mode == 0) {
+      k_diag_apply<VT, MT, 0><<<g, 256, 0, st>>>(d.n, di, r, pv, v, z, sc);
+      count_launches(1);
+    }
+    else if (mode == 1) {
+      k_diag_apply<VT, MT, 1><<<g, 256, 0, st>>>(d.n, di, r, pv, v, z, sc);
+      count_launches(1);
+    }
+    else {
+      k_diag_apply<VT, MT, 2><<<g, 256, 0, st>>>(d.n, di, r, pv, v, z, sc);
+      count_launches(1);
+    }
+  }
+}
+
+template <class VT, class MT>
+void launch_krylov_init(const SolverDev &d, const MT *val, const VT *b,
+                        const VT *x, VT *r, VT *rh, VT *p, VT *v, KScalars *sc,
+                        RedWork w, cudaStream_t st) {
+  k_krylov_init<VT, MT><<<w.grid, kVecBlock, 0, st>>>(d, val, b, x, r, rh, p, v,
+                                                      sc, w);
+  count_launches(1);
+}
+template <class VT, class MT>
+void launch_spmv_v(const SolverDev &d, const MT *val, const VT *ph, VT *v,
+                   const VT *rh, KScalars *sc, RedWork w, cudaStream_t st) {
+  k_spmv_v<VT, MT><<<w.grid, kVecBlock, 0, st>>>(d, val, ph, v, rh, sc, w);
+  count_launches(1);
+}
+template <class VT, class MT>
+void launch_spmv_t(const SolverDev &d, const MT *val, const VT *sh, VT *t,
+                   const VT *s, KScalars *sc, RedWork w, cudaStream_t st) {
+  k_spmv_t<VT, MT><<<w.grid, kVecBlock, 0, st>>>(d, val, sh, t, s, sc, w);
+  count_launches(1);
+}
+template <class VT>
+void launch_update(int n, VT *x, VT *r, const VT *ph, const VT *sh,
+                   const VT *s, const VT *t, const VT *rh, KScalars *sc,
+                   RedWork w, cudaStream_t st) {
+  k_update<VT><<<w.grid, kVecBlock, 0, st>>>(n, x, r, ph, sh, s, t, rh, sc, w);
+  count_launches(1);
+}
+void launch_true_residual(const SolverDev &d, const double *val,
+                          const double *b, const double *x, double *r,
+                          KScalars *sc, RedWork w, cudaStream_t st) {
+  k_true_residual<<<w.grid, kVecBlock, 0, st>>>(d, val, b, x, r, sc, w);
+  count_launches(1);
+}
+void launch_jacobi_diag(const SolverDev &d, const double *pvals, double *dinv,
+                        cudaStream_t st) {
+  k_jacobi_diag<<<blocks_for(d.n, 256), 256, 0, st>>>(d.n, d.prp, d.pci, pvals,
+                                                      dinv);
+  count_launches(1);
+}
+
+#define PG_INST(VT, MT)                                                       \
+  template void launch_precond<VT, MT>(int, int, const SolverDev &,           \
+                                       const MT *, const MT *, const MT *,    \
+                                       const VT *, VT *, const VT *, VT *,    \
+                                       const KScalars *, cudaStream_t);       \
+  template void launch_krylov_init<VT, MT>(const SolverDev &, const MT *,     \
+                                           const VT *, const VT *, VT *,      \
+                                           VT *, VT *, VT *, KScalars *,      \
+                                           RedWork, cudaStream_t);            \
+  template void launch_spmv_v<VT, MT>(const SolverDev &, const MT *,          \
+                                      const VT *, VT *, const VT *,           \
+                                      KScalars *, RedWork, cudaStream_t);     \
+  template void launch_spmv_t<VT, MT>(const SolverDev &, const MT *,          \
+                                      const VT *, VT *, const VT *,           \
+                                      KScalars *, RedWork, cudaStream_t);
+PG_INST(double, double)
+PG_INST(float, float)
+template void launch_update<double>(int, double *, double *, const double *,
+                                    const double *, const double *,
+                                    const double *, const double *,
+                                    KScalars *, RedWork, cudaStream_t);
+template void launch_update<float>(int, float *, float *, const float *,
+                                   const float *, const float *, const float *,
+                                   const float *, KScalars *, RedWork,
+                                   cudaStream_t);
+
+}  // namespace pg

@@ -1,0 +1,632 @@
+// The SparseMatrixSolver replacement: sparsity analysis caching, value
+// permutation, ILU(0) factorisation and the device-resident BiCGStab loop
+// (FP64, and FP32-inner / FP64-refined).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "internal.h"
+#include "kernels.cuh"
+
+using namespace pg;
+
+namespace {
+
+__global__ void k_count_diff(int64_t n, const int32_t *__restrict__ a,
+                             const int32_t *__restrict__ b,
+                             unsigned int *__restrict__ diff) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    if (a[i] != b[i]) {
+      atomicAdd(diff, 1u);
+      return;
+    }
+}
+
+__global__ void k_to_float(int64_t n, const double *__restrict__ a,
+                           float *__restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+// outer refinement helpers (FP64 residual, FP32 correction)
+__global__ void k_residual_to_float(int n, const double *__restrict__ r,
+                                    float *__restrict__ rf, double scale) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x)
+    rf[i] = (float)(r[i] * scale);
+}
+__global__ void k_add_correction(int n, double *__restrict__ x,
+                                 const float *__restrict__ d, double scale) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x)
+    x[i] += scale * (double)d[i];
+}
+
+}  // namespace
+
+struct pg_solver {
+  pg_solver_cfg cfg{};
+  int64_t rank = 0;
+  // analysis
+  Analysis a;
+  bool analysed = false;
+  uint64_t eqn_pattern = 0;  // pattern id of a device equation, 0 = host CSR
+  DevBuf<int32_t> perm, prp, pci, psrc, dup_dst, dup_src, sub_ptr, sub_lvl,
+      lvl_ptr, lrp, ldg, lci, lsrc;
+  DevBuf<int32_t> raw_rp, raw_ci, st_rp, st_ci;
+  DevBuf<double> st_vals, st_vec;
+  DevBuf<unsigned int> diff;
+  // values and factors
+  DevBuf<double> pvals, lu, ldinv, jdinv;
+  DevBuf<float> pvals32, lu32, ldinv32, jdinv32;
+  // Krylov vectors (permuted order)
+  DevBuf<double> b, x, r, rh, p, v, ph, s, sh, t, xout;
+  DevBuf<float> f_b, f_x, f_r, f_rh, f_p, f_v, f_ph, f_s, f_sh, f_t;
+  // reductions and scalars
+  DevBuf<double> partials;
+  DevBuf<unsigned int> ticket;
+  DevBuf<KScalars> sc;
+  DevBuf<int> bad;
+  KScalars *sc_host = nullptr;
+  int *bad_host = nullptr;
+  unsigned int *diff_host = nullptr;
+  bool have_rhs = false, have_x = false, have_vals = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  int red_grid = 1;
+
+  ~pg_solver() {
+    if (sc_host) cudaFreeHost(sc_host);
+    if (bad_host) cudaFreeHost(bad_host);
+    if (diff_host) cudaFreeHost(diff_host);
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+
+  SolverDev dev() const {
+    SolverDev d;
+    d.n = (int)a.n;
+    d.nnz = (int)a.nnz;
+    d.n_sub = a.n_sub;
+    d.prp = prp.p;
+    d.pci = pci.p;
+    d.sub_ptr = sub_ptr.p;
+    d.sub_lvl = sub_lvl.p;
+    d.lvl_ptr = lvl_ptr.p;
+    d.lrp = lrp.p;
+    d.ldg = ldg.p;
+    d.lci = lci.p;
+    d.lsrc = lsrc.p;
+    d.max_sub_rows = a.max_sub_rows;
+    d.max_sub_lu = a.max_sub_lu;
+    d.global_ilu = a.global_ilu ? 1 : 0;
+    return d;
+  }
+  RedWork red() const { return RedWork{partials.p, ticket.p, red_grid}; }
+};
+
+namespace {
+
+int upload_analysis(pg_solver *s) {
+  const Analysis &a = s->a;
+  cudaError_t e = cudaSuccess;
+  auto up = [&](auto &buf, const auto &vec) {
+    if (e == cudaSuccess) e = buf.upload(vec);
+  };
+  up(s->perm, a.perm);
+  up(s->prp, a.prp);
+  up(s->pci, a.pci);
+  up(s->psrc, a.psrc);
+  up(s->dup_dst, a.dup_dst);
+  up(s->dup_src, a.dup_src);
+  up(s->sub_ptr, a.sub_ptr);
+  up(s->sub_lvl, a.sub_lvl);
+  up(s->lvl_ptr, a.lvl_ptr);
+  up(s->lrp, a.lrp);
+  up(s->ldg, a.ldg);
+  up(s->lci, a.lci);
+  up(s->lsrc, a.lsrc);
+  const size_t n = a.n, nnz = a.nnz, nlu = a.lci.size();
+  for (DevBuf<double> *bf : {&s->b, &s->x, &s->r, &s->rh, &s->p, &s->v,
+                             &s->ph, &s->s, &s->sh, &s->t, &s->xout,
+                             &s->ldinv, &s->jdinv})
+    if (e == cudaSuccess) e = bf->reserve(n);
+  if (e == cudaSuccess) e = s->pvals.reserve(nnz);
+  if (e == cudaSuccess) e = s->lu.reserve(nlu);
+  if (s->cfg.precision == PG_MIXED) {
+    for (DevBuf<float> *bf : {&s->f_b, &s->f_x, &s->f_r, &s->f_rh, &s->f_p,
+                              &s->f_v, &s->f_ph, &s->f_s, &s->f_sh, &s->f_t,
+                              &s->ldinv32, &s->jdinv32})
+      if (e == cudaSuccess) e = bf->reserve(n);
+    if (e == cudaSuccess) e = s->pvals32.reserve(nnz);
+    if (e == cudaSuccess) e = s->lu32.reserve(nlu);
+  }
+  s->red_grid = (int)std::min<int64_t>(1216, (n + kVecBlock - 1) / kVecBlock);
+  if (s->red_grid < 1) s->red_grid = 1;
+  if (e == cudaSuccess) e = s->partials.reserve((size_t)kMaxDots * s->red_grid);
+  if (e == cudaSuccess) e = s->ticket.zero(1);
+  if (e == cudaSuccess) e = s->sc.reserve(1);
+  if (e == cudaSuccess) e = s->bad.reserve(1);
+  if (e == cudaSuccess) e = s->diff.reserve(1);
+  if (e != cudaSuccess) return cuda_fail(e, "solver analysis upload", __FILE__, __LINE__);
+  s->analysed = true;
+  s->have_x = false;
+  s->have_rhs = false;
+  return PG_OK;
+}
+
+int ensure_host_state(pg_solver *s) {
+  if (!s->sc_host) PG_CUDA(cudaMallocHost((void **)&s->sc_host, sizeof(KScalars)));
+  if (!s->bad_host) PG_CUDA(cudaMallocHost((void **)&s->bad_host, sizeof(int)));
+  if (!s->diff_host) PG_CUDA(cudaMallocHost((void **)&s->diff_host, sizeof(unsigned)));
+  for (auto &e : s->ev)
+    if (!e) PG_CUDA(cudaEventCreate(&e));
+  return PG_OK;
+}
+
+inline int grid_for(int64_t n) {
+  return (int)std::min<int64_t>(1216, std::max<int64_t>(1, (n + 255) / 256));
+}
+
+// One BiCGStab run on the permuted system held in the given buffers.
+// VT/MT select FP64 or FP32 storage; reductions are FP64 throughout.
+template <class VT, class MT>
+int run_bicgstab(pg_solver *s, const MT *val, const MT *lu, const MT *ldinv,
+                 const MT *jdinv, VT *b, VT *x, VT *r, VT *rh, VT *p, VT *v,
+                 VT *ph, VT *ss, VT *sh, VT *t, double tol, int max_iters,
+                 bool check_true, int *iters, int *restarts) {
+  cudaStream_t st = stream();
+  const SolverDev d = s->dev();
+  const RedWork w = s->red();
+  KScalars init{};
+  init.tol2 = tol * tol;
+  init.max_iter = max_iters;
+  *s->sc_host = init;
+  PG_CUDA(cudaMemcpyAsync(s->sc.p, s->sc_host, sizeof(KScalars),
+                          cudaMemcpyHostToDevice, st));
+  int n_restart = 0;
+  for (;;) {
+    launch_krylov_init<VT, MT>(d, val, b, x, r, rh, p, v, s->sc.p, w, st);
+    for (;;) {
+      const int chunk = 8;
+      for (int c = 0; c < chunk; ++c) {
+        launch_precond<VT, MT>(s->cfg.precond, 1, d, lu, ldinv, jdinv, r, p, v,
+                               ph, s->sc.p, st);
+        launch_spmv_v<VT, MT>(d, val, ph, v, rh, s->sc.p, w, st);
+        launch_precond<VT, MT>(s->cfg.precond, 2, d, lu, ldinv, jdinv, r, ss, v,
+                               sh, s->sc.p, st);
+        launch_spmv_t<VT, MT>(d, val, sh, t, ss, s->sc.p, w, st);
+        launch_update<VT>(d.n, x, r, ph, sh, ss, t, rh, s->sc.p, w, st);
+      }
+      PG_CUDA(cudaGetLastError());
+      PG_CUDA(cudaMemcpyAsync(s->sc_host, s->sc.p, sizeof(KScalars),
+                              cudaMemcpyDeviceToHost, st));
+      PG_CUDA(cudaStreamSynchronize(st));
+      if (s->sc_host->done) break;
+    }
+    const KScalars k = *s->sc_host;
+    *iters = k.iter;
+    *restarts = n_restart;
+    if (k.status != PG_OK || !check_true) return k.status;
+    if (k.bb == 0.) return PG_OK;
+    // confirm on the true residual (FP64 storage only)
+    if (sizeof(VT) == sizeof(double)) {
+      launch_true_residual(d, reinterpret_cast<const double *>(val),
+                           reinterpret_cast<const double *>(b),
+                           reinterpret_cast<const double *>(x), nullptr,
+                           s->sc.p, w, st);
+      PG_CUDA(cudaMemcpyAsync(s->sc_host, s->sc.p, sizeof(KScalars),
+                              cudaMemcpyDeviceToHost, st));
+      PG_CUDA(cudaStreamSynchronize(st));
+      if (s->sc_host->rr_true <= k.tol2 * k.bb) return PG_OK;
+    } else {
+      return PG_OK;
+    }
+    if (++n_restart > 20 || k.iter >= max_iters) {
+      *restarts = n_restart;
+      return k.iter >= max_iters ? PG_MAX_ITERS : PG_BREAKDOWN;
+    }
+    // restart from the true residual: keep x and the iteration count
+    s->sc_host->done = 0;
+    s->sc_host->status = PG_OK;
+    PG_CUDA(cudaMemcpyAsync(s->sc.p, s->sc_host, sizeof(KScalars),
+                            cudaMemcpyHostToDevice, st));
+  }
+}
+
+int factor(pg_solver *s) {
+  cudaStream_t st = stream();
+  const SolverDev d = s->dev();
+  if (s->cfg.precond == PG_PREC_ILU0) {
+    PG_CUDA(cudaMemsetAsync(s->bad.p, 0, sizeof(int), st));
+    launch_ilu0_factor<double>(d, s->pvals.p, s->lu.p, s->ldinv.p, s->bad.p, st);
+    PG_CUDA(cudaGetLastError());
+  } else if (s->cfg.precond == PG_PREC_JACOBI) {
+    launch_jacobi_diag(d, s->pvals.p, s->jdinv.p, st);
+  }
+  if (s->cfg.precision == PG_MIXED) {
+    const int64_t nlu = (int64_t)s->a.lci.size();
+    k_to_float<<<grid_for(s->a.nnz), 256, 0, st>>>(s->a.nnz, s->pvals.p, s->pvals32.p);
+    count_launches(1);
+    if (s->cfg.precond == PG_PREC_ILU0) {
+      k_to_float<<<grid_for(nlu), 256, 0, st>>>(nlu, s->lu.p, s->lu32.p);
+      count_launches(1);
+      k_to_float<<<grid_for(s->a.n), 256, 0, st>>>(s->a.n, s->ldinv.p, s->ldinv32.p);
+      count_launches(1);
+    } else if (s->cfg.precond == PG_PREC_JACOBI) {
+      k_to_float<<<grid_for(s->a.n), 256, 0, st>>>(s->a.n, s->jdinv.p, s->jdinv32.p);
+      count_launches(1);
+    }
+    PG_CUDA(cudaGetLastError());
+  }
+  return PG_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+extern "C" void pg_solver_default_cfg(pg_solver_cfg *cfg) {
+  if (!cfg) return;
+  cfg->tolerance = 1e-8;
+  cfg->max_iters = 500;
+  cfg->precond = PG_PREC_ILU0;
+  cfg->subdomain_rows = 0;
+  cfg->precision = PG_FP64;
+  cfg->inner_max_iters = 500;
+  cfg->inner_tolerance = 1e-4;
+}
+
+extern "C" int pg_solver_create(const pg_solver_cfg *cfg, pg_solver **out) {
+  PG_CHECK_ARG(out, "pg_solver_create: out is NULL");
+  *out = nullptr;
+  pg_solver_cfg c;
+  pg_solver_default_cfg(&c);
+  if (cfg) c = *cfg;
+  PG_CHECK_ARG(c.tolerance > 0. && c.max_iters > 0, "pg_solver_create: bad tolerance/max_iters");
+  PG_CHECK_ARG(c.precond >= PG_PREC_NONE && c.precond <= PG_PREC_ILU0,
+               "pg_solver_create: bad preconditioner");
+  PG_CHECK_ARG(c.precision == PG_FP64 || c.precision == PG_MIXED,
+               "pg_solver_create: bad precision");
+  if (c.inner_max_iters <= 0) c.inner_max_iters = c.max_iters;
+  if (!(c.inner_tolerance > 0.)) c.inner_tolerance = 1e-4;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0 || !stream()) {
+    set_error("no CUDA device available: libphase_gb300 has no CPU path");
+    return PG_CUDA_ERROR;
+  }
+  auto *s = new (std::nothrow) pg_solver();
+  PG_CHECK_ARG(s, "pg_solver_create: out of host memory");
+  s->cfg = c;
+  int rc = ensure_host_state(s);
+  if (rc) {
+    delete s;
+    return rc;
+  }
+  *out = s;
+  return PG_OK;
+}
+
+extern "C" int pg_solver_destroy(pg_solver *s) {
+  if (s) cudaStreamSynchronize(stream());
+  delete s;
+  return PG_OK;
+}
+
+extern "C" int pg_solver_set_rank(pg_solver *s, int64_t n) {
+  PG_CHECK_ARG(s && n > 0, "pg_solver_set_rank: bad argument");
+  PG_CHECK_ARG(n < ((int64_t)1 << 31), "pg_solver_set_rank: rank too large");
+  if (s->rank != n) {
+    s->analysed = false;
+    s->have_x = false;
+  }
+  s->rank = n;
+  return PG_OK;
+}
+
+extern "C" int pg_solver_set_csr(pg_solver *s, const int32_t *row_ptr,
+                                 const int32_t *col_ind, const double *vals,
+                                 int ptr_kind) {
+  PG_CHECK_ARG(s && row_ptr && col_ind && vals, "pg_solver_set_csr: NULL arg");
+  PG_CHECK_ARG(s->rank > 0, "pg_solver_set_csr: set_rank first");
+  const int64_t n = s->rank;
+  cudaStream_t st = stream();
+  // host copies of the pattern are needed for (re)analysis
+  std::vector<int32_t> h_rp, h_ci;
+  const int32_t *hrp = row_ptr, *hci = col_ind;
+  int64_t n_src;
+  if (ptr_kind == PG_DEVICE) {
+    int32_t last = 0;
+    PG_CUDA(cudaMemcpyAsync(&last, row_ptr + n, sizeof(int32_t),
+                            cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    n_src = last;
+  } else {
+    n_src = row_ptr[n];
+  }
+  PG_CHECK_ARG(n_src >= 0, "pg_solver_set_csr: bad row_ptr");
+  // stage pattern + values on the device
+  const int32_t *drp = row_ptr, *dci = col_ind;
+  const double *dv = vals;
+  if (ptr_kind != PG_DEVICE) {
+    PG_CUDA(s->st_rp.upload(row_ptr, n + 1));
+    PG_CUDA(s->st_ci.upload(col_ind, n_src));
+    PG_CUDA(s->st_vals.upload(vals, n_src));
+    drp = s->st_rp.p;
+    dci = s->st_ci.p;
+    dv = s->st_vals.p;
+  }
+  bool same = s->analysed && s->eqn_pattern == 0 && s->a.n == n &&
+              s->a.n_src == n_src;
+  if (same) {
+    *s->diff_host = 0;
+    PG_CUDA(cudaMemsetAsync(s->diff.p, 0, sizeof(unsigned), st));
+    k_count_diff<<<grid_for(n + 1), 256, 0, st>>>(n + 1, drp, s->raw_rp.p, s->diff.p);
+    count_launches(1);
+    k_count_diff<<<grid_for(n_src), 256, 0, st>>>(n_src, dci, s->raw_ci.p, s->diff.p);
+    count_launches(1);
+    PG_CUDA(cudaMemcpyAsync(s->diff_host, s->diff.p, sizeof(unsigned),
+                            cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    same = *s->diff_host == 0;
+  }
+  if (!same) {
+    if (ptr_kind == PG_DEVICE) {
+      h_rp.resize(n + 1);
+      h_ci.resize(n_src);
+      PG_CUDA(cudaMemcpyAsync(h_rp.data(), row_ptr, (n + 1) * 4,
+                              cudaMemcpyDeviceToHost, st));
+      PG_CUDA(cudaMemcpyAsync(h_ci.data(), col_ind, n_src * 4,
+                              cudaMemcpyDeviceToHost, st));
+      PG_CUDA(cudaStreamSynchronize(st));
+      hrp = h_rp.data();
+      hci = h_ci.data();
+    }
+    int rc = analyse(n, hrp, hci, s->cfg.precond == PG_PREC_ILU0 ? s->cfg.subdomain_rows : -1, s->a);
+    if (rc) return rc;
+    rc = upload_analysis(s);
+    if (rc) return rc;
+    PG_CUDA(s->raw_rp.upload(hrp, n + 1));
+    PG_CUDA(s->raw_ci.upload(hci, n_src));
+    s->eqn_pattern = 0;
+  }
+  launch_permute_values((int)s->a.nnz, s->psrc.p, dv, s->pvals.p,
+                        (int)s->a.dup_dst.size(), s->dup_dst.p, s->dup_src.p, st);
+  PG_CUDA(cudaGetLastError());
+  s->have_vals = true;
+  return PG_OK;
+}
+
+extern "C" int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e) {
+  PG_CHECK_ARG(s && e, "pg_solver_set_eqn: NULL arg");
+  cudaStream_t st = stream();
+  if (s->rank != e->p.n) {
+    s->rank = e->p.n;
+    s->analysed = false;
+  }
+  if (!s->analysed || s->eqn_pattern != e->pattern_id) {
+    int rc = analyse(e->p.n, e->p.row_ptr.data(), e->p.col_ind.data(),
+                     s->cfg.precond == PG_PREC_ILU0 ? s->cfg.subdomain_rows : -1, s->a);
+    if (rc) return rc;
+    rc = upload_analysis(s);
+    if (rc) return rc;
+    s->eqn_pattern = e->pattern_id;
+  }
+  launch_permute_values((int)s->a.nnz, s->psrc.p, e->vals.p, s->pvals.p,
+                        (int)s->a.dup_dst.size(), s->dup_dst.p, s->dup_src.p, st);
+  // the solver receives -rhs_ (FiniteVolumeEquation.tpp:179)
+  launch_permute_vec((int)s->a.n, s->perm.p, e->rhs.p, -1.0, s->b.p, st);
+  PG_CUDA(cudaGetLastError());
+  s->have_vals = true;
+  s->have_rhs = true;
+  return PG_OK;
+}
+
+extern "C" int pg_solver_set_rhs(pg_solver *s, const double *rhs, int ptr_kind) {
+  PG_CHECK_ARG(s && rhs, "pg_solver_set_rhs: NULL arg");
+  PG_CHECK_ARG(s->analysed, "pg_solver_set_rhs: set the matrix first");
+  const double *d = rhs;
+  if (ptr_kind != PG_DEVICE) {
+    PG_CUDA(s->st_vec.upload(rhs, s->a.n));
+    d = s->st_vec.p;
+  }
+  launch_permute_vec((int)s->a.n, s->perm.p, d, 1.0, s->b.p, stream());
+  PG_CUDA(cudaGetLastError());
+  s->have_rhs = true;
+  return PG_OK;
+}
+
+extern "C" int pg_solver_set_guess(pg_solver *s, const double *x0, int ptr_kind) {
+  PG_CHECK_ARG(s, "pg_solver_set_guess: NULL solver");
+  PG_CHECK_ARG(s->analysed, "pg_solver_set_guess: set the matrix first");
+  if (!x0) {  // zero initial guess
+    PG_CUDA(cudaMemsetAsync(s->x.p, 0, s->a.n * sizeof(double), stream()));
+    s->have_x = true;
+    return PG_OK;
+  }
+  const double *d = x0;
+  if (ptr_kind != PG_DEVICE) {
+    PG_CUDA(s->st_vec.upload(x0, s->a.n));
+    d = s->st_vec.p;
+  }
+  launch_permute_vec((int)s->a.n, s->perm.p, d, 1.0, s->x.p, stream());
+  PG_CUDA(cudaGetLastError());
+  s->have_x = true;
+  return PG_OK;
+}
+
+extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
+  PG_CHECK_ARG(s, "pg_solver_solve: NULL solver");
+  PG_CHECK_ARG(s->analysed && s->have_vals && s->have_rhs,
+               "pg_solver_solve: matrix and rhs must be set first");
+  cudaStream_t st = stream();
+  const int64_t n = s->a.n;
+  if (!s->have_x) PG_CUDA(cudaMemsetAsync(s->x.p, 0, n * sizeof(double), st));
+  PG_CUDA(cudaEventRecord(s->ev[0], st));
+  int rc = factor(s);
+  if (rc) return rc;
+  PG_CUDA(cudaEventRecord(s->ev[1], st));
+  if (s->cfg.precond == PG_PREC_ILU0) {
+    PG_CUDA(cudaMemcpyAsync(s->bad_host, s->bad.p, sizeof(int),
+                            cudaMemcpyDeviceToHost, st));
+  }
+  int status = PG_OK, iters = 0, outer = 0;
+  const double tol = s->cfg.tolerance;
+  const SolverDev d = s->dev();
+  const RedWork w = s->red();
+  // ||b||^2 once per solve
+  launch_true_residual(d, s->pvals.p, s->b.p, nullptr, nullptr, s->sc.p, w, st);
+  PG_CUDA(cudaMemcpyAsync(s->sc_host, s->sc.p, sizeof(KScalars),
+                          cudaMemcpyDeviceToHost, st));
+  PG_CUDA(cudaStreamSynchronize(st));
+  const double bb = s->sc_host->rr_true;
+  if (!std::isfinite(bb)) {
+    status = PG_NON_FINITE;
+  } else if (bb == 0.) {
+    PG_CUDA(cudaMemsetAsync(s->x.p, 0, n * sizeof(double), st));
+  } else if (s->cfg.precision == PG_FP64) {
+    int restarts = 0;
+    status = run_bicgstab<double, double>(
+        s, s->pvals.p, s->lu.p, s->ldinv.p, s->jdinv.p, s->b.p, s->x.p, s->r.p,
+        s->rh.p, s->p.p, s->v.p, s->ph.p, s->s.p, s->sh.p, s->t.p, tol,
+        s->cfg.max_iters, true, &iters, &restarts);
+    outer = restarts + 1;
+  } else {
+    // Iterative refinement: r = b - A x in FP64; solve A d = r / ||r|| in
+    // FP32 (FP32 SpMV and ILU sweeps, FP64 dot products and scalars) to the
+    // inner tolerance; x += ||r|| d.  Stops on the FP64 true residual.
+    const int g = grid_for(n);
+    launch_true_residual(d, s->pvals.p, s->b.p, s->x.p, s->r.p, s->sc.p, w, st);
+    PG_CUDA(cudaMemcpyAsync(s->sc_host, s->sc.p, sizeof(KScalars),
+                            cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    double rr = s->sc_host->rr_true;
+    while (rr > tol * tol * bb) {
+      if (!std::isfinite(rr)) { status = PG_NON_FINITE; break; }
+      if (outer >= 50 || iters >= s->cfg.max_iters) { status = PG_MAX_ITERS; break; }
+      const double rn = std::sqrt(rr);
+      k_residual_to_float<<<g, 256, 0, st>>>((int)n, s->r.p, s->f_b.p, 1.0 / rn);
+      count_launches(1);
+      PG_CUDA(cudaMemsetAsync(s->f_x.p, 0, n * sizeof(float), st));
+      int it = 0, rs = 0;
+      const int budget = std::max(1, std::min(s->cfg.inner_max_iters,
+                                              s->cfg.max_iters - iters));
+      const int ist = run_bicgstab<float, float>(
+          s, s->pvals32.p, s->lu32.p, s->ldinv32.p, s->jdinv32.p, s->f_b.p,
+          s->f_x.p, s->f_r.p, s->f_rh.p, s->f_p.p, s->f_v.p, s->f_ph.p,
+          s->f_s.p, s->f_sh.p, s->f_t.p, s->cfg.inner_tolerance, budget,
+          false, &it, &rs);
+      iters += it;
+      ++outer;
+      if (ist == PG_NON_FINITE) { status = ist; break; }
+      k_add_correction<<<g, 256, 0, st>>>((int)n, s->x.p, s->f_x.p, rn);
+      count_launches(1);
+      launch_true_residual(d, s->pvals.p, s->b.p, s->x.p, s->r.p, s->sc.p, w, st);
+      PG_CUDA(cudaMemcpyAsync(s->sc_host, s->sc.p, sizeof(KScalars),
+                              cudaMemcpyDeviceToHost, st));
+      PG_CUDA(cudaStreamSynchronize(st));
+      const double rr_new = s->sc_host->rr_true;
+      if (it == 0 || !(rr_new < rr)) {  // no progress: stagnation
+        status = PG_BREAKDOWN;
+        rr = rr_new;
+        break;
+      }
+      rr = rr_new;
+    }
+  }
+  // final true residual in FP64 and the solution in the caller's order
+  launch_true_residual(d, s->pvals.p, s->b.p, s->x.p, nullptr, s->sc.p, w, st);
+  launch_unpermute_vec((int)n, s->perm.p, s->x.p, s->xout.p, st);
+  PG_CUDA(cudaGetLastError());
+  PG_CUDA(cudaEventRecord(s->ev[2], st));
+  PG_CUDA(cudaMemcpyAsync(s->sc_host, s->sc.p, sizeof(KScalars),
+                          cudaMemcpyDeviceToHost, st));
+  PG_CUDA(cudaStreamSynchronize(st));
+  float ms_fact = 0.f, ms_all = 0.f;
+  cudaEventElapsedTime(&ms_fact, s->ev[0], s->ev[1]);
+  cudaEventElapsedTime(&ms_all, s->ev[0], s->ev[2]);
+  const double rel = bb > 0. ? std::sqrt(s->sc_host->rr_true / bb) : 0.;
+  if (s->cfg.precond == PG_PREC_ILU0 && *s->bad_host > 0 && !(rel <= tol))
+    status = PG_BREAKDOWN;
+  if (status == PG_OK && !(rel <= tol)) status = PG_MAX_ITERS;
+  if (!std::isfinite(rel)) status = PG_NON_FINITE;
+  s->have_x = true;  // warm start for the next solve, as Belos reuses x_
+  if (stats) {
+    stats->iters = iters;
+    stats->outer_iters = outer;
+    stats->status = status;
+    stats->rel_residual = rel;
+    stats->ms = ms_all;
+    stats->setup_ms = ms_fact;
+  }
+  if (status != PG_OK)
+    set_error("pg_solver_solve: status " + std::to_string(status) + " after " +
+              std::to_string(iters) + " iterations, relative residual " +
+              std::to_string(rel));
+  return status;
+}
+
+extern "C" int pg_solver_get_x(const pg_solver *s, double *x, int ptr_kind) {
+  PG_CHECK_ARG(s && x, "pg_solver_get_x: NULL arg");
+  PG_CHECK_ARG(s->analysed, "pg_solver_get_x: nothing solved");
+  PG_CUDA(copy_out(x, s->xout.p, s->a.n * sizeof(double), ptr_kind));
+  PG_CUDA(cudaStreamSynchronize(stream()));
+  return PG_OK;
+}
+
+extern "C" uint64_t pg_kernel_launches(void) { return launch_count(); }
+
+extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
+  PG_CHECK_ARG(s && ms && reps > 0, "pg_solver_profile: bad argument");
+  PG_CHECK_ARG(s->analysed && s->have_vals && s->have_x,
+               "pg_solver_profile: solve a system first");
+  cudaStream_t st = stream();
+  const SolverDev d = s->dev();
+  const RedWork w = s->red();
+  const int64_t n = s->a.n;
+  DevBuf<double> xs, rs;
+  PG_CUDA(xs.reserve(n));
+  PG_CUDA(rs.reserve(n));
+  PG_CUDA(cudaMemcpyAsync(xs.p, s->x.p, n * 8, cudaMemcpyDeviceToDevice, st));
+  PG_CUDA(cudaMemcpyAsync(rs.p, s->r.p, n * 8, cudaMemcpyDeviceToDevice, st));
+  KScalars k{};
+  k.max_iter = 1 << 30;
+  k.alpha = k.omega = k.beta = k.rho = 1.0;
+  k.bb = 1.0;
+  *s->sc_host = k;
+  PG_CUDA(cudaMemcpyAsync(s->sc.p, s->sc_host, sizeof(KScalars),
+                          cudaMemcpyHostToDevice, st));
+  float t = 0.f;
+  auto timed = [&](auto &&launch, double *out) -> int {
+    launch();  // warm
+    PG_CUDA(cudaEventRecord(s->ev[0], st));
+    for (int i = 0; i < reps; ++i) launch();
+    PG_CUDA(cudaEventRecord(s->ev[1], st));
+    PG_CUDA(cudaEventSynchronize(s->ev[1]));
+    PG_CUDA(cudaGetLastError());
+    cudaEventElapsedTime(&t, s->ev[0], s->ev[1]);
+    *out = (double)t / reps;
+    return PG_OK;
+  };
+  int rc = timed([&] { launch_spmv_v<double, double>(d, s->pvals.p, s->ph.p, s->v.p, s->rh.p, s->sc.p, w, st); }, &ms[0]);
+  if (!rc) rc = timed([&] { launch_precond<double, double>(s->cfg.precond, 1, d, s->lu.p, s->ldinv.p, s->jdinv.p, s->r.p, s->p.p, s->v.p, s->ph.p, s->sc.p, st); }, &ms[1]);
+  if (!rc) rc = timed([&] { launch_update<double>(d.n, xs.p, rs.p, s->ph.p, s->sh.p, s->s.p, s->t.p, s->rh.p, s->sc.p, w, st); }, &ms[2]);
+  if (!rc && s->cfg.precond == PG_PREC_ILU0)
+    rc = timed([&] { launch_ilu0_factor<double>(d, s->pvals.p, s->lu.p, s->ldinv.p, s->bad.p, st); }, &ms[3]);
+  else if (!rc)
+    ms[3] = 0.;
+  PG_CUDA(cudaStreamSynchronize(st));
+  return rc;
+}
+
+extern "C" int pg_solver_partition(const pg_solver *s, int32_t *part,
+                                   int *n_parts) {
+  PG_CHECK_ARG(s && s->analysed, "pg_solver_partition: nothing analysed");
+  if (part) std::copy(s->a.part.begin(), s->a.part.end(), part);
+  if (n_parts) *n_parts = s->a.n_sub;
+  return PG_OK;
+}

@@ -1,0 +1,225 @@
+"""CPU tests of the oracle: known answers, the reference's own CrsEquation,
+golden vectors and an independent scipy cross-check.  No GPU needed."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+from phase_gb300 import meshes
+import refreplay
+
+
+def rect(oracle, nx, ny, w=1.0, h=1.0):
+    nodes, cptr, cind = meshes.rectilinear(nx, ny, w, h)
+    return oracle.OracleMesh(nodes, cptr, cind)
+
+
+def test_rectilinear_counts_and_numbering(oracle):
+    om = rect(oracle, 5, 3, 1.0, 1.5)
+    assert om.n_cells == 15
+    assert om.n_interior == 4 * 3 + 5 * 2
+    assert om.n_boundary == 2 * (5 + 3)
+    f = om.faces()
+    # FiniteVolumeGrid2D::createCell: cell 0 creates its 4 faces first, in
+    # node order (0,1), (1,7), (7,6), (6,0)
+    assert list(f["lnode"][:4]) == [0, 1, 7, 6]
+    assert list(f["rnode"][:4]) == [1, 7, 6, 0]
+    # normal = (dy, -dx) of rNode - lNode
+    assert f["nx"][0] == 0.0 and f["ny"][0] == -0.2
+    c = om.cells()
+    assert np.allclose(c["vol"], 0.2 * 0.5)
+    assert np.allclose(c["cx"][:5], 0.1 + 0.2 * np.arange(5))
+
+
+@pytest.mark.parametrize("gamma", [1.0, 2.5])
+def test_rectilinear_coefficients(oracle, gamma):
+    nx, ny, w, h = 6, 4, 1.2, 2.0
+    om = rect(oracle, nx, ny, w, h)
+    hx, hy = w / nx, h / ny
+    bc = np.ones(om.n_faces, np.int32)
+    rp, ci, v, rhs = om.laplacian(gamma, bc, np.zeros(om.n_faces))
+    for i in range(om.n_cells):
+        row = dict(zip(ci[rp[i]:rp[i + 1]], v[rp[i]:rp[i + 1]]))
+        for j, a in row.items():
+            if j == i:
+                continue
+            expect = gamma * hy / hx if abs(j - i) == 1 else gamma * hx / hy
+            assert a == pytest.approx(expect, rel=1e-14)
+        # all-Neumann rows sum to zero
+        assert sum(row.values()) == pytest.approx(0.0, abs=1e-12 * gamma)
+    assert np.all(rhs == 0.0)
+
+
+def test_pattern_order_scalar_vs_face_gamma(oracle):
+    om = rect(oracle, 3, 3)
+    bc = np.ones(om.n_faces, np.int32)
+    rp, ci, _, _ = om.laplacian(1.0, bc, np.zeros(om.n_faces))
+    # scalar gamma: first neighbour, then diagonal (Laplacian.h:57-58)
+    assert list(ci[rp[4]:rp[5]][:2]) != [4] and ci[rp[4] + 1] == 4
+    rpf, cif, _, _ = om.laplacian(np.ones(om.n_faces), bc, np.zeros(om.n_faces))
+    # face gamma: diagonal first (Laplacian.h:141-142)
+    assert cif[rpf[4]] == 4
+    assert sorted(cif[rpf[4]:rpf[5]]) == sorted(ci[rp[4]:rp[5]])
+
+
+def test_laplacian_of_linear_field_is_zero_inside(oracle):
+    """A phi + rhs = 0 for a linear phi with FIXED boundary values on a
+    rectilinear mesh (two-point flux is exact for linear fields there)."""
+    om2 = rect(oracle, 7, 5, 1.0, 1.0)
+    c2, f2 = om2.cells(), om2.faces()
+    phi2 = 2.0 * c2["cx"] - 3.0 * c2["cy"] + 1.0
+    bc2 = np.zeros(om2.n_faces, np.int32)
+    bv2 = 2.0 * f2["fx"] - 3.0 * f2["fy"] + 1.0
+    rp, ci, v, rhs = om2.laplacian(1.0, bc2, bv2)
+    A2 = sp.csr_matrix((v, ci, rp), shape=(om2.n_cells, om2.n_cells))
+    assert np.max(np.abs(A2 @ phi2 + rhs)) < 1e-12
+
+
+def _reference_crs(oracle, om, gamma, bc, bv, u=None):
+    r = oracle.RefCrs(om.n_cells, 5)
+    ops, rows, cols, vals = refreplay.laplacian_ops(om, gamma, bc, bv)
+    r.apply(ops, rows, cols, vals)
+    if u is not None:
+        r.eq_vector(refreplay.div_u(om, u))
+    return r.export()
+
+
+@pytest.mark.parametrize("kind", ["scalar", "face"])
+@pytest.mark.parametrize("mesh", ["rect", "tri"])
+def test_slots_match_reference_crsequation(oracle, kind, mesh):
+    if oracle.ref_lib() is None:
+        pytest.skip("reference sources absent: oracle/_ref not built")
+    if mesh == "rect":
+        om = rect(oracle, 6, 5, 1.0, 2.0)
+    else:
+        om = oracle.OracleMesh(*meshes.triangulated(5, 4, 1.0, 1.0, 0.2, 1))
+    rng = np.random.default_rng(7)
+    nf = om.n_faces
+    f = om.faces()
+    bc = np.where(f["rcell"] < 0, rng.integers(0, 2, nf), 1).astype(np.int32)
+    bv = rng.standard_normal(nf)
+    gamma = 1.7 if kind == "scalar" else rng.uniform(0.0, 2.0, nf)
+    if kind == "face":
+        gamma[::7] = 0.0  # explicit zero coefficients are kept
+    u = rng.standard_normal((nf, 2))
+    ref = _reference_crs(oracle, om, gamma, bc, bv, u)
+    mine = om.laplacian(gamma, bc, bv, u, slots=True)
+    for a, b in zip(ref, mine):
+        assert a.shape == b.shape
+        assert np.array_equal(a, b), "oracle differs from CrsEquation.cpp"
+
+
+def test_row_growth_past_five_slots_matches_reference(oracle):
+    if oracle.ref_lib() is None:
+        pytest.skip("reference sources absent")
+    # a hexagon-fan mesh: the centre cell has 6 neighbours (7 entries)
+    ang = np.linspace(0, 2 * np.pi, 7)[:-1]
+    ring = np.stack([np.cos(ang), np.sin(ang)], 1)
+    outer = 2.0 * np.stack([np.cos(ang + np.pi / 6), np.sin(ang + np.pi / 6)], 1)
+    nodes = np.vstack([ring, outer])
+    cells = [list(range(6))]
+    for k in range(6):
+        a, b = k, (k + 1) % 6
+        cells.append([a, 6 + k, b])
+    cptr = np.cumsum([0] + [len(c) for c in cells]).astype(np.int64)
+    cind = np.array(sum(cells, []), np.int64)
+    om = oracle.OracleMesh(nodes, cptr, cind)
+    bc = np.ones(om.n_faces, np.int32)
+    ref = _reference_crs(oracle, om, 1.0, bc, np.zeros(om.n_faces))
+    mine = om.laplacian(1.0, bc, np.zeros(om.n_faces), slots=True)
+    assert ref[0][1] - ref[0][0] == 7
+    for a, b in zip(ref, mine):
+        assert np.array_equal(a, b)
+
+
+def test_reference_plus_drops_zeros_and_placeholders(oracle):
+    """CrsEquation::operator+= (CrsEquation.cpp:185-229) rebuilds the CSR
+    without zero values and -1 slots: the semantics GCIB rows rely on."""
+    if oracle.ref_lib() is None:
+        pytest.skip("reference sources absent")
+    a = oracle.RefCrs(3, 5)
+    a.apply([0, 0, 0, 0], [0, 0, 1, 2], [0, 1, 1, 2], [2.0, 0.0, 3.0, 4.0])
+    b = oracle.RefCrs(3, 5)
+    b.apply([0, 0], [0, 2], [2, 0], [5.0, 6.0])
+    a.plus(b)
+    rp, ci, v, _ = a.export()
+    assert list(rp) == [0, 2, 3, 5]
+    assert list(ci) == [0, 2, 1, 2, 0]
+    assert list(v) == [2.0, 5.0, 3.0, 4.0, 6.0]
+
+
+def test_dt_over_rho_and_interpolation(oracle):
+    om = rect(oracle, 4, 4)
+    c = om.cells()
+    g = np.clip(c["cx"] * 1.3 - 0.1, 0.0, 1.0)
+    gf = om.interpolate_faces(g)
+    f = om.faces()
+    inter = f["rcell"] >= 0
+    # equal spacing: distance weight 1/2
+    expect = 0.5 * g[f["lcell"][inter]] + 0.5 * g[f["rcell"][inter]]
+    assert np.allclose(gf[inter], expect, rtol=0, atol=1e-15)
+    assert np.array_equal(gf[~inter], g[f["lcell"][~inter]])
+    co = om.dt_over_rho(g, 1000.0, 1.0, 1e-4)
+    rho = 1000.0 + np.clip(gf, 0, 1) * (1.0 - 1000.0)
+    assert np.allclose(co, 1e-4 / rho, rtol=1e-15)
+
+
+def test_gradient_of_linear_field(oracle):
+    om = rect(oracle, 6, 6)
+    c, f = om.cells(), om.faces()
+    phi = 3.0 * c["cx"] - 2.0 * c["cy"]
+    pf = 3.0 * f["fx"] - 2.0 * f["fy"]
+    gf, gc = om.gradient(phi, pf)
+    assert np.allclose(gc[:, 0], 3.0, atol=1e-12)
+    assert np.allclose(gc[:, 1], -2.0, atol=1e-12)
+
+
+def _poisson_system(oracle, nx, ny, seed=0):
+    om = rect(oracle, nx, ny, 1.0, 1.0)
+    f = om.faces()
+    bc = np.where(f["rcell"] < 0, 0, 1).astype(np.int32)  # FIXED walls
+    rng = np.random.default_rng(seed)
+    gamma = rng.uniform(0.5, 2.0, om.n_faces)
+    rp, ci, v, rhs = om.laplacian(gamma, bc, np.zeros(om.n_faces))
+    b = rng.standard_normal(om.n_cells)
+    return rp, ci, v, b
+
+
+@pytest.mark.parametrize("precond", [0, 1, 2, 3])
+def test_bicgstab_matches_scipy_direct(oracle, precond):
+    rp, ci, v, b = _poisson_system(oracle, 24, 20)
+    x, st = oracle.bicgstab(rp, ci, v, b, tol=1e-10, max_iters=2000,
+                            precond=precond, ilut_fill=5)
+    assert st["status"] == 0
+    A = sp.csr_matrix((v, ci, rp))
+    xd = spla.spsolve(A.tocsc(), b)
+    assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-8
+    assert st["rel_residual"] <= 1e-10
+
+
+def test_ilu0_matches_scipy_spilu_pattern_zero_fill(oracle):
+    """ILU(0) factors satisfy (L U)_ij = a_ij on the pattern of A."""
+    rp, ci, v, _ = _poisson_system(oracle, 9, 7)
+    lu, rc = oracle.ilu0(rp, ci, v)
+    assert rc == 0
+    n = len(rp) - 1
+    A = sp.csr_matrix((v, ci, rp), shape=(n, n)).toarray()
+    F = sp.csr_matrix((lu, ci, rp), shape=(n, n)).toarray()
+    L = np.tril(F, -1) + np.eye(n)
+    U = np.triu(F)
+    P = L @ U
+    mask = A != 0
+    assert np.allclose(P[mask], A[mask], rtol=1e-12, atol=1e-12)
+
+
+def test_schwarz_ilu0_blocks_are_independent(oracle):
+    rp, ci, v, b = _poisson_system(oracle, 16, 16)
+    n = len(rp) - 1
+    part = (np.arange(n) // 64).astype(np.int32)
+    x, st = oracle.bicgstab(rp, ci, v, b, tol=1e-10, part=part)
+    assert st["status"] == 0
+    lu, rc = oracle.ilu0(rp, ci, v, part)
+    # entries that couple two subdomains are dropped from the factor
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    cross = part[rows] != part[ci]
+    assert np.all(lu[cross] == 0.0)
