@@ -260,6 +260,7 @@ def test_edge_cases(pg):
     with pytest.raises(pg.PhaseError):
         pg.SparseMatrixSolver(tolerance=-1.0)
     s4 = pg.SparseMatrixSolver()
+    s4.setRank(3)
     with pytest.raises(pg.PhaseError):
         s4.setRhs(np.ones(3))  # no matrix yet
     with pytest.raises(pg.PhaseError):
