@@ -1,0 +1,45 @@
+// The GB300 SparseMatrixSolver plugin for Phase: registered in
+// SparseMatrixSolverFactory::create (src/Math/SparseMatrixSolverFactory.cpp
+// :26-40) as `lib gb300`, it replaces the Belos BiCGStab + Ifpack2 RILUK
+// backend (src/Math/TrilinosBelosSparseMatrixSolver.cpp) by the CUDA solver
+// of libphase_gb300 through its C ABI (include/phase_gb300.h).
+#pragma once
+#include <vector>
+
+#include "Math/SparseMatrixSolver.h"
+#include "phase_gb300.h"
+
+class Gb300SparseMatrixSolver : public SparseMatrixSolver {
+ public:
+  Gb300SparseMatrixSolver();
+  ~Gb300SparseMatrixSolver() override;
+
+  Type type() const override;
+  void setRank(int rank) override;
+  void setRank(int rowRank, int colRank) override;
+  void set(const CoefficientList &eqn) override;
+  void set(const std::vector<Index> &rowPtr, const std::vector<Index> &colInds,
+           const std::vector<Scalar> &vals) override;
+  void set(const std::vector<SparseEntry> &entries) override;
+  void setGuess(const Vector &x0) override;
+  void setRhs(const Vector &rhs) override;
+  Scalar solve() override;
+  Scalar x(Index idx) const override;
+  // keys: tolerance (1e-8), maxIters (500), preconditioner
+  // (ilu0 | jacobi | none), subdomainRows (0 = default, -1 = one subdomain),
+  // precision (fp64 | mixed)
+  void setup(const boost::property_tree::ptree &parameters) override;
+  int nIters() const override;
+  Scalar error() const override;
+  bool supportsMPI() const override { return false; }
+  void printStatus(const std::string &msg) const override;
+
+ private:
+  void check(int rc, const char *method) const;
+  void recreate();
+  pg_solver *solver_ = nullptr;
+  pg_solver_cfg cfg_;
+  pg_solve_stats stats_{};
+  int rank_ = 0;
+  std::vector<Scalar> x_;
+};
