@@ -137,6 +137,18 @@ int pg_gradient(const pg_mesh *m, const double *phi_cell,
                 const double *phi_face, double *grad_face, double *grad_cell,
                 int ptr_kind);
 
+/* Allocation-free form of pg_gradient's cell gradient, for callers that
+ * cannot allocate device memory (a fixed memory budget owned by an outer
+ * framework, or code that must not let cudaMalloc/cudaFree synchronise the
+ * device).  No counterpart in the reference.  All pointers are device
+ * pointers: phi_cell[n_cells], phi_face[n_faces] in, grad_cell[2*n_cells]
+ * out.  The face-gradient scratch is a static 16 MiB device array, so meshes
+ * are limited to 1,048,576 faces (PG_BAD_ARG beyond).  The first call on a
+ * device looks the array up (make it before any stream capture); calls
+ * share the array, and calls that overlap on the GPU race on it. */
+int pg_gradient_noalloc(const pg_mesh *m, const double *phi_cell,
+                        const double *phi_face, double *grad_cell);
+
 /* ------------------------------------------------------------------------
  * Sparse solver.  Replaces the SparseMatrixSolver plugin
  * (src/Math/SparseMatrixSolver.h:11-62) as driven by

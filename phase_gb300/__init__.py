@@ -78,6 +78,7 @@ PROTOTYPES = {
     "pg_eqn_export": (_I, [_P, _P, _P, _P, _P]),
     "pg_face_dt_over_rho": (_I, [_P, _P, _D, _D, _D, _P, _I]),
     "pg_gradient": (_I, [_P, _P, _P, _P, _P, _I]),
+    "pg_gradient_noalloc": (_I, [_P, _P, _P, _P]),
     "pg_solver_default_cfg": (None, [ctypes.POINTER(SolverCfg)]),
     "pg_solver_create": (_I, [ctypes.POINTER(SolverCfg), ctypes.POINTER(_P)]),
     "pg_solver_destroy": (_I, [_P]),

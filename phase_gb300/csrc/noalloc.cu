@@ -1,0 +1,80 @@
+// pg_gradient_noalloc: the cell gradient of pg_gradient without any device
+// allocation, for callers that cannot call cudaMalloc.
+//
+// pg_gradient needs 2*n_faces doubles of scratch for the face gradients when
+// the caller does not want them back, and it allocates that scratch per call.
+// Some callers cannot allocate at that point: a time loop that runs inside a
+// fixed device-memory budget handed out by an outer framework, or code that
+// must not trigger cudaMalloc/cudaFree because those calls synchronise the
+// device and stall the other work in flight.  This entry point keeps the
+// scratch in one file-scope __device__ array instead.
+//
+// Limits and sharing:
+//  * meshes of at most kNoAllocMaxFaces faces (larger ones are rejected with
+//    PG_BAD_ARG); the array takes 16 MiB on every GPU that loads the library,
+//    for as long as the process lives;
+//  * the array's device address is looked up once per device, on the first
+//    call made with that device current; make that first call before any
+//    stream capture begins;
+//  * every call shares the one array and overwrites its first 2*n_faces
+//    entries before reading them (nothing has to start at zero); two calls
+//    whose kernels run at the same time -- e.g. issued on other streams, or
+//    from several host threads -- race on it.
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+#include "internal.h"
+#include "kernels.cuh"
+
+namespace {
+
+constexpr int64_t kNoAllocMaxFaces = (int64_t)1 << 20;
+
+__device__ __align__(256) double g_face_grad_scratch[2 * kNoAllocMaxFaces];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+double *g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array for the current device (set up once).
+int scratch_for_current_device(double **out) {
+  int dev = 0;
+  PG_CUDA(cudaGetDevice(&dev));
+  PG_CHECK_ARG(dev >= 0 && dev < kMaxDevices,
+               "pg_gradient_noalloc: device ordinal out of range");
+  std::lock_guard<std::mutex> g(g_mu);
+  if (!g_scratch_ptr[dev]) {
+    void *p = nullptr;
+    PG_CUDA(cudaGetSymbolAddress(&p, g_face_grad_scratch));
+    g_scratch_ptr[dev] = static_cast<double *>(p);
+  }
+  *out = g_scratch_ptr[dev];
+  return PG_OK;
+}
+
+}  // namespace
+
+extern "C" int pg_gradient_noalloc(const pg_mesh *m, const double *phi_cell,
+                                   const double *phi_face, double *grad_cell) {
+  PG_CHECK_ARG(m && phi_cell && phi_face && grad_cell,
+               "pg_gradient_noalloc: NULL argument");
+  const pg::HostMesh &h = m->h;
+  if (h.n_faces > kNoAllocMaxFaces) {
+    pg::set_error("pg_gradient_noalloc: mesh has " + std::to_string(h.n_faces) +
+                  " faces; the allocation-free path holds at most " +
+                  std::to_string(kNoAllocMaxFaces));
+    return PG_BAD_ARG;
+  }
+  double *scratch = nullptr;
+  int rc = scratch_for_current_device(&scratch);
+  if (rc) return rc;
+  pg::launch_gradient((int)h.n_cells, (int)h.n_faces, m->d.fl.p, m->d.fr.p,
+                      m->d.fcx.p, m->d.fcy.p, m->d.cx.p, m->d.cy.p,
+                      m->d.link_ptr.p, m->d.link_face.p, nullptr, nullptr,
+                      m->d.fnx.p, m->d.fny.p, phi_cell, phi_face, scratch,
+                      grad_cell, pg::stream());
+  PG_CUDA(cudaGetLastError());
+  PG_CUDA(cudaStreamSynchronize(pg::stream()));
+  return PG_OK;
+}
