@@ -519,6 +519,75 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
     }
     a.max_sub_lu = std::max(a.max_sub_lu, (int)((int64_t)a.lci.size() - e0));
   }
+
+  // 7. packed per-subdomain records (layout in kernels.cuh): level bounds,
+  //    L/U column slots (subdomain-local, uint16) and value slots; records
+  //    and their sections start on 16-byte boundaries for cp.async.bulk
+  PG_CHECK_ARG(a.max_sub_rows <= 65535,
+               "ILU(0) subdomains are limited to 65535 rows (use Schwarz "
+               "subdomains for larger systems)");
+  auto al16 = [](int64_t b) { return (b + 15) & ~(int64_t)15; };
+  a.meta64.resize(a.n_sub);
+  a.meta32.resize(a.n_sub);
+  int64_t off64 = 0, off32 = 0, slots = 0;
+  for (int s = 0; s < a.n_sub; ++s) {
+    const int32_t r0 = a.sub_ptr[s], r1 = a.sub_ptr[s + 1], nr = r1 - r0;
+    int kl = 0, ku = 0;
+    for (int32_t i = r0; i < r1; ++i) {
+      kl = std::max(kl, a.ldg[i] - a.lrp[i]);
+      ku = std::max(ku, a.lrp[i + 1] - a.ldg[i] - 1);
+    }
+    const int K = kl + ku;
+    const int nlev = a.sub_lvl[s + 1] - a.sub_lvl[s];
+    const int64_t col_off = al16(2 * (int64_t)(nlev + 1));
+    const int64_t val_off = col_off + al16(2 * (int64_t)nr * K);
+    for (int pass = 0; pass < 2; ++pass) {
+      const int64_t vsz = pass == 0 ? 8 : 4;
+      const int64_t bytes = val_off + al16(vsz * (int64_t)nr * (K + 1));
+      int64_t &off = pass == 0 ? off64 : off32;
+      PG_CHECK_ARG(off + bytes < ((int64_t)1 << 31), "ILU(0) records too large");
+      SubMeta m{r0, nr, nlev, K, kl, (int32_t)off, (int32_t)col_off,
+                (int32_t)val_off, (int32_t)bytes, (int32_t)slots, 0, 0};
+      (pass == 0 ? a.meta64 : a.meta32)[s] = m;
+      off += bytes;
+    }
+    slots += (int64_t)nr * (K + 1);
+  }
+  PG_CHECK_ARG(slots < ((int64_t)1 << 31), "ILU(0) factor too large");
+  a.rec64.assign(off64, 0);
+  a.rec32.assign(off32, 0);
+  a.rec_src.assign(slots, -1);
+  a.smem64 = a.smem32 = 0;
+  for (int s = 0; s < a.n_sub; ++s) {
+    const SubMeta &m = a.meta64[s];
+    const int K = m.K, kl = m.KL;
+    for (int pass = 0; pass < 2; ++pass) {
+      const SubMeta &mm = pass == 0 ? a.meta64[s] : a.meta32[s];
+      uint8_t *base = (pass == 0 ? a.rec64 : a.rec32).data() + mm.rec_off;
+      uint16_t *lvl = reinterpret_cast<uint16_t *>(base);
+      for (int l = 0; l <= m.nlev; ++l)
+        lvl[l] = (uint16_t)(a.lvl_ptr[a.sub_lvl[s] + l] - m.r0);
+      uint16_t *cols = reinterpret_cast<uint16_t *>(base + mm.col_off);
+      for (int i = 0; i < m.nr; ++i) {
+        const int32_t g = m.r0 + i;
+        const int nl = a.ldg[g] - a.lrp[g], nu = a.lrp[g + 1] - a.ldg[g] - 1;
+        for (int k = 0; k < K; ++k) cols[i * K + k] = kPadCol;
+        for (int k = 0; k < nl; ++k) cols[i * K + k] = (uint16_t)a.lci[a.lrp[g] + k];
+        for (int k = 0; k < nu; ++k)
+          cols[i * K + kl + k] = (uint16_t)a.lci[a.ldg[g] + 1 + k];
+        if (pass == 0) {
+          int32_t *src = a.rec_src.data() + m.slot_base + (int64_t)i * (K + 1);
+          for (int k = 0; k < nl; ++k) src[k] = a.lsrc[a.lrp[g] + k];
+          for (int k = 0; k < nu; ++k) src[kl + k] = a.lsrc[a.ldg[g] + 1 + k];
+          src[K] = a.lsrc[a.ldg[g]];
+        }
+      }
+      const size_t sm = (size_t)al16(mm.rec_bytes) +
+                        (size_t)m.nr * (pass == 0 ? 8 : 4);
+      size_t &mx = pass == 0 ? a.smem64 : a.smem32;
+      mx = std::max(mx, sm);
+    }
+  }
   return PG_OK;
 }
 

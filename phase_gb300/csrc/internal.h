@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/phase_gb300.h"
+#include "kernels.cuh"
 
 namespace pg {
 
@@ -171,6 +172,11 @@ struct Analysis {
   std::vector<int32_t> lci;                // subdomain-local column
   std::vector<int32_t> part;               // subdomain of each original row
   bool global_ilu = false;                 // one subdomain holding all rows
+  // packed ILU(0) records (static parts filled; values by the factor)
+  std::vector<SubMeta> meta64, meta32;
+  std::vector<uint8_t> rec64, rec32;
+  std::vector<int32_t> rec_src;            // value slot -> permuted entry
+  size_t smem64 = 0, smem32 = 0;           // max record + vector bytes
 };
 
 int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,

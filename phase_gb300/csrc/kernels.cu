@@ -266,51 +266,80 @@ __global__ void k_unpermute_vec(int n, const int32_t *__restrict__ perm,
 
 // ------------------------------------------------------------- ILU(0)
 // Row-wise IKJ ILU(0) (Saad, Iterative Methods for Sparse Linear Systems,
-// Alg. 10.4) on the diagonal block of one subdomain.  The CTA walks the
-// level schedule; rows of one level depend only on rows of earlier levels,
-// which the barrier has completed.  Pivots are computed in FP64.
-template <class MT>
-__global__ void k_ilu0_factor(SolverDev d, const double *__restrict__ pvals,
-                              MT *__restrict__ lu, MT *__restrict__ ldinv,
+// Alg. 10.4) on the diagonal block of one subdomain, in its packed record.
+// The CTA walks the level schedule; rows of one level depend only on rows of
+// earlier levels, which the barrier has completed.  Pivots are FP64; the
+// diagonal slot ends up holding 1/u_ii.
+__global__ void k_ilu0_factor(const SubMeta *__restrict__ meta,
+                              uint8_t *__restrict__ rec,
+                              const int32_t *__restrict__ rec_src,
+                              const double *__restrict__ pvals,
                               int *__restrict__ bad) {
-  const int s = blockIdx.x;
-  const int r0 = d.sub_ptr[s], r1 = d.sub_ptr[s + 1];
-  const int e0 = d.lrp[r0], e1 = d.lrp[r1];
-  for (int j = e0 + threadIdx.x; j < e1; j += blockDim.x) {
-    const int src = d.lsrc[j];
-    lu[j] = (MT)(src >= 0 ? pvals[src] : 0.);
+  const SubMeta m = meta[blockIdx.x];
+  uint8_t *base = rec + m.rec_off;
+  const uint16_t *lvl = reinterpret_cast<const uint16_t *>(base);
+  const uint16_t *cols = reinterpret_cast<const uint16_t *>(base + m.col_off);
+  double *vals = reinterpret_cast<double *>(base + m.val_off);
+  const int K = m.K, KL = m.KL, K1 = K + 1;
+  const int n_slots = m.nr * K1;
+  for (int j = threadIdx.x; j < n_slots; j += blockDim.x) {
+    const int src = rec_src[m.slot_base + j];
+    vals[j] = src >= 0 ? pvals[src] : 0.;
   }
   __syncthreads();
-  const int l0 = d.sub_lvl[s], l1 = d.sub_lvl[s + 1];
-  for (int lv = l0; lv < l1; ++lv) {
-    const int a = d.lvl_ptr[lv], b = d.lvl_ptr[lv + 1];
+  for (int lv = 0; lv < m.nlev; ++lv) {
+    const int a = lvl[lv], b = lvl[lv + 1];
     for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
-      const int rb = d.lrp[i], re = d.lrp[i + 1], dg = d.ldg[i];
-      for (int j = rb; j < dg; ++j) {
-        const int k = r0 + d.lci[j];
-        const double ukk = (double)lu[d.ldg[k]];
-        const double lik = (double)lu[j] / ukk;
-        lu[j] = (MT)lik;
-        // a_ic -= l_ik * u_kc for c in U(k) that is also in row i
-        int q = j + 1;
-        const int ke = d.lrp[k + 1];
-        for (int jj = d.ldg[k] + 1; jj < ke; ++jj) {
-          const int c = d.lci[jj];
-          while (q < re && d.lci[q] < c) ++q;
-          if (q >= re) break;
-          if (d.lci[q] == c) lu[q] = (MT)((double)lu[q] - lik * (double)lu[jj]);
+      double *wi = vals + (size_t)i * K1;
+      const uint16_t *ci = cols + (size_t)i * K;
+      for (int k = 0; k < KL; ++k) {
+        const int c = ci[k];
+        if (c == kPadCol) break;
+        const double lik = wi[k] / vals[(size_t)c * K1 + K];
+        wi[k] = lik;
+        // a_ij -= l_ik u_kj for the columns j of U(k) present in row i
+        const uint16_t *cc = cols + (size_t)c * K + KL;
+        const double *wc = vals + (size_t)c * K1 + KL;
+        for (int q = 0; q < K - KL; ++q) {
+          const int cu = cc[q];
+          if (cu == kPadCol) break;
+          const double d = lik * wc[q];
+          if (cu == i) {
+            wi[K] -= d;
+            continue;
+          }
+          for (int k2 = 0; k2 < K; ++k2)
+            if (ci[k2] == cu) {
+              wi[k2] -= d;
+              break;
+            }
         }
-      }
-      const double piv = (double)lu[dg];
-      if (piv == 0. || !isfinite(piv)) {
-        atomicAdd(bad, 1);
-        ldinv[i] = (MT)0.;
-      } else {
-        ldinv[i] = (MT)(1. / piv);
       }
     }
     __syncthreads();
   }
+  for (int i = threadIdx.x; i < m.nr; i += blockDim.x) {
+    const double piv = vals[(size_t)i * K1 + K];
+    if (piv == 0. || !isfinite(piv)) {
+      atomicAdd(bad, 1);
+      vals[(size_t)i * K1 + K] = 0.;
+    } else {
+      vals[(size_t)i * K1 + K] = 1. / piv;
+    }
+  }
+}
+
+// FP32 copy of the factor values (the FP32 records' static parts are set up
+// once on the host).
+__global__ void k_factor_to_fp32(const SubMeta *__restrict__ m64,
+                                 const uint8_t *__restrict__ rec64,
+                                 const SubMeta *__restrict__ m32,
+                                 uint8_t *__restrict__ rec32) {
+  const SubMeta a = m64[blockIdx.x], b = m32[blockIdx.x];
+  const double *src = reinterpret_cast<const double *>(rec64 + a.rec_off + a.val_off);
+  float *dst = reinterpret_cast<float *>(rec32 + b.rec_off + b.val_off);
+  const int n = a.nr * (a.K + 1);
+  for (int j = threadIdx.x; j < n; j += blockDim.x) dst[j] = (float)src[j];
 }
 
 template <class VT>
@@ -328,100 +357,159 @@ __device__ __forceinline__ VT pre_input(int mode, int i, const VT *r, VT *pv,
   return pv[i];
 }
 
-// Forward/backward sweeps of one subdomain with its factor and vector staged
-// in shared memory.  Layout: z[nr] | dinv[nr] | rp[nr+1] | dg[nr] | ci[ne] |
-// lu[ne].
+// ---- TMA / mbarrier helpers (sm_90+ PTX) ----
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                   smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_load(void *dst, const void *src,
+                                          uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], "
+      "%2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+constexpr int kWaitLimit = 1 << 22;  // try_wait polls before giving up
+
+// Bounded wait on a single-use barrier.  On expiry the error flag is set and
+// the copy still in flight is waited for once more (bounded) so the CTA does
+// not exit under it.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, int *err) {
+  for (int it = 0; it < kWaitLimit; ++it)
+    if (mbar_try_wait(bar, 0)) return true;
+  if (err) atomicExch(err, 1);
+  for (int it = 0; it < kWaitLimit; ++it)
+    if (mbar_try_wait(bar, 0)) break;
+  return false;
+}
+
+// Forward/backward sweeps of one subdomain by one warp.  The record is moved
+// into shared memory by one cp.async.bulk (TMA) while the lanes compute the
+// fused input vector; the level loop then runs entirely out of shared
+// memory with __syncwarp between levels.
 template <class VT, class MT, int MODE>
-__global__ void k_ilu0_apply_smem(SolverDev d, const MT *__restrict__ lu,
-                                  const MT *__restrict__ ldinv,
-                                  const VT *__restrict__ r, VT *__restrict__ pv,
-                                  const VT *__restrict__ v, VT *__restrict__ z,
-                                  const KScalars *__restrict__ sc) {
+__global__ void __launch_bounds__(32)
+k_ilu0_apply_tma(const SubMeta *__restrict__ meta,
+                 const uint8_t *__restrict__ rec, const VT *__restrict__ r,
+                 VT *__restrict__ pv, const VT *__restrict__ v,
+                 VT *__restrict__ z, const KScalars *__restrict__ sc,
+                 int *__restrict__ err) {
   if (sc && sc->done) return;
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int s = blockIdx.x;
-  const int r0 = d.sub_ptr[s], r1 = d.sub_ptr[s + 1], nr = r1 - r0;
-  const int e0 = d.lrp[r0], ne = d.lrp[r1] - e0;
-  VT *zs = reinterpret_cast<VT *>(smem);
-  size_t off = ((size_t)nr * sizeof(VT) + 15) & ~(size_t)15;
-  MT *dis = reinterpret_cast<MT *>(smem + off);
-  off += ((size_t)nr * sizeof(MT) + 15) & ~(size_t)15;
-  int *rps = reinterpret_cast<int *>(smem + off);
-  off += ((size_t)(nr + 1) * sizeof(int) + 15) & ~(size_t)15;
-  int *dgs = reinterpret_cast<int *>(smem + off);
-  off += ((size_t)nr * sizeof(int) + 15) & ~(size_t)15;
-  int *cis = reinterpret_cast<int *>(smem + off);
-  off += ((size_t)ne * sizeof(int) + 15) & ~(size_t)15;
-  MT *lus = reinterpret_cast<MT *>(smem + off);
+  extern __shared__ __align__(128) uint8_t smem[];
+  __shared__ __align__(8) uint64_t bar;
+  const SubMeta m = meta[blockIdx.x];
+  const int lane = threadIdx.x;
+  uint8_t *rs = smem;
+  VT *zs = reinterpret_cast<VT *>(smem + ((m.rec_bytes + 15) & ~15));
+  if (lane == 0) {
+    mbar_init(&bar, 1);
+    mbar_expect_tx(&bar, (uint32_t)m.rec_bytes);
+    bulk_load(rs, rec + m.rec_off, (uint32_t)m.rec_bytes, &bar);
+  }
+  for (int i = lane; i < m.nr; i += 32)
+    zs[i] = pre_input<VT>(MODE, m.r0 + i, r, pv, v, sc);
+  __syncwarp();
+  if (!mbar_wait_bounded(&bar, err)) return;
+  const uint16_t *lvl = reinterpret_cast<const uint16_t *>(rs);
+  const uint16_t *cols = reinterpret_cast<const uint16_t *>(rs + m.col_off);
+  const MT *vals = reinterpret_cast<const MT *>(rs + m.val_off);
+  const int K = m.K, KL = m.KL, K1 = K + 1;
+  for (int lv = 0; lv < m.nlev; ++lv) {
+    const int a = lvl[lv], b = lvl[lv + 1];
+    for (int i = a + lane; i < b; i += 32) {
+      const uint16_t *ci = cols + i * K;
+      const MT *wi = vals + i * K1;
+      VT acc = zs[i];
+      for (int k = 0; k < KL; ++k) {
+        const int c = ci[k];
+        if (c != kPadCol) acc -= (VT)wi[k] * zs[c];
+      }
+      zs[i] = acc;
+    }
+    __syncwarp();
+  }
+  for (int lv = m.nlev - 1; lv >= 0; --lv) {
+    const int a = lvl[lv], b = lvl[lv + 1];
+    for (int i = a + lane; i < b; i += 32) {
+      const uint16_t *ci = cols + i * K;
+      const MT *wi = vals + i * K1;
+      VT acc = zs[i];
+      for (int k = KL; k < K; ++k) {
+        const int c = ci[k];
+        if (c != kPadCol) acc -= (VT)wi[k] * zs[c];
+      }
+      zs[i] = acc * (VT)wi[K];
+    }
+    __syncwarp();
+  }
+  for (int i = lane; i < m.nr; i += 32) z[m.r0 + i] = zs[i];
+}
 
-  for (int j = threadIdx.x; j < ne; j += blockDim.x) {
-    cis[j] = d.lci[e0 + j];
-    lus[j] = lu[e0 + j];
-  }
-  for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-    rps[i] = d.lrp[r0 + i] - e0;
-    dgs[i] = d.ldg[r0 + i] - e0;
-    dis[i] = ldinv[r0 + i];
-    zs[i] = pre_input<VT>(MODE, r0 + i, r, pv, v, sc);
-  }
-  if (threadIdx.x == 0) rps[nr] = ne;
+// Same sweeps with the record and the vector in global memory, one CTA per
+// subdomain, for subdomains whose record exceeds shared memory (one global
+// subdomain).
+template <class VT, class MT, int MODE>
+__global__ void k_ilu0_apply_global(const SubMeta *__restrict__ meta,
+                                    const uint8_t *__restrict__ rec,
+                                    const VT *__restrict__ r,
+                                    VT *__restrict__ pv,
+                                    const VT *__restrict__ v,
+                                    VT *__restrict__ z,
+                                    const KScalars *__restrict__ sc) {
+  if (sc && sc->done) return;
+  const SubMeta m = meta[blockIdx.x];
+  const uint8_t *base = rec + m.rec_off;
+  const uint16_t *lvl = reinterpret_cast<const uint16_t *>(base);
+  const uint16_t *cols = reinterpret_cast<const uint16_t *>(base + m.col_off);
+  const MT *vals = reinterpret_cast<const MT *>(base + m.val_off);
+  VT *zs = z + m.r0;
+  const int K = m.K, KL = m.KL, K1 = K + 1;
+  for (int i = threadIdx.x; i < m.nr; i += blockDim.x)
+    zs[i] = pre_input<VT>(MODE, m.r0 + i, r, pv, v, sc);
   __syncthreads();
-
-  const int l0 = d.sub_lvl[s], l1 = d.sub_lvl[s + 1];
-  for (int lv = l0; lv < l1; ++lv) {
-    const int a = d.lvl_ptr[lv] - r0, b = d.lvl_ptr[lv + 1] - r0;
+  for (int lv = 0; lv < m.nlev; ++lv) {
+    const int a = lvl[lv], b = lvl[lv + 1];
     for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
       VT acc = zs[i];
-      for (int j = rps[i]; j < dgs[i]; ++j) acc -= (VT)lus[j] * zs[cis[j]];
+      for (int k = 0; k < KL; ++k) {
+        const int c = cols[(size_t)i * K + k];
+        if (c != kPadCol) acc -= (VT)vals[(size_t)i * K1 + k] * zs[c];
+      }
       zs[i] = acc;
     }
     __syncthreads();
   }
-  for (int lv = l1 - 1; lv >= l0; --lv) {
-    const int a = d.lvl_ptr[lv] - r0, b = d.lvl_ptr[lv + 1] - r0;
+  for (int lv = m.nlev - 1; lv >= 0; --lv) {
+    const int a = lvl[lv], b = lvl[lv + 1];
     for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
       VT acc = zs[i];
-      for (int j = dgs[i] + 1; j < rps[i + 1]; ++j) acc -= (VT)lus[j] * zs[cis[j]];
-      zs[i] = acc * (VT)dis[i];
-    }
-    __syncthreads();
-  }
-  for (int i = threadIdx.x; i < nr; i += blockDim.x) z[r0 + i] = zs[i];
-}
-
-// Same sweeps with the vector and factor in global memory, for subdomains
-// too large for shared memory (the single-subdomain global ILU(0)).
-template <class VT, class MT, int MODE>
-__global__ void k_ilu0_apply_global(SolverDev d, const MT *__restrict__ lu,
-                                    const MT *__restrict__ ldinv,
-                                    const VT *__restrict__ r,
-                                    VT *__restrict__ pv, const VT *__restrict__ v,
-                                    VT *__restrict__ z,
-                                    const KScalars *__restrict__ sc) {
-  if (sc && sc->done) return;
-  const int s = blockIdx.x;
-  const int r0 = d.sub_ptr[s], r1 = d.sub_ptr[s + 1];
-  for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
-    z[i] = pre_input<VT>(MODE, i, r, pv, v, sc);
-  __syncthreads();
-  const int l0 = d.sub_lvl[s], l1 = d.sub_lvl[s + 1];
-  for (int lv = l0; lv < l1; ++lv) {
-    const int a = d.lvl_ptr[lv], b = d.lvl_ptr[lv + 1];
-    for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
-      VT acc = z[i];
-      for (int j = d.lrp[i]; j < d.ldg[i]; ++j)
-        acc -= (VT)lu[j] * z[r0 + d.lci[j]];
-      z[i] = acc;
-    }
-    __syncthreads();
-  }
-  for (int lv = l1 - 1; lv >= l0; --lv) {
-    const int a = d.lvl_ptr[lv], b = d.lvl_ptr[lv + 1];
-    for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
-      VT acc = z[i];
-      for (int j = d.ldg[i] + 1; j < d.lrp[i + 1]; ++j)
-        acc -= (VT)lu[j] * z[r0 + d.lci[j]];
-      z[i] = acc * (VT)ldinv[i];
+      for (int k = KL; k < K; ++k) {
+        const int c = cols[(size_t)i * K + k];
+        if (c != kPadCol) acc -= (VT)vals[(size_t)i * K1 + k] * zs[c];
+      }
+      zs[i] = acc * (VT)vals[(size_t)i * K1 + K];
     }
     __syncthreads();
   }
@@ -697,70 +785,62 @@ void launch_unpermute_vec(int n, const int32_t *perm, const double *src,
   count_launches(1);
 }
 
-template <class MT>
-void launch_ilu0_factor(const SolverDev &d, const double *pvals, MT *lu,
-                        MT *ldinv, int *bad, cudaStream_t st) {
-  const int threads = d.global_ilu ? 1024 : 128;
-  k_ilu0_factor<MT><<<d.n_sub, threads, 0, st>>>(d, pvals, lu, ldinv, bad);
+void launch_ilu0_factor(const SolverDev &d, const double *pvals, int *bad,
+                        bool to_fp32, cudaStream_t st) {
+  const int threads = d.smem64 ? 32 : 1024;
+  k_ilu0_factor<<<d.n_sub, threads, 0, st>>>(d.meta64, d.rec64, d.rec_src,
+                                             pvals, bad);
   count_launches(1);
-}
-template void launch_ilu0_factor<double>(const SolverDev &, const double *,
-                                         double *, double *, int *,
-                                         cudaStream_t);
-template void launch_ilu0_factor<float>(const SolverDev &, const double *,
-                                        float *, float *, int *, cudaStream_t);
-
-template <class VT, class MT>
-static size_t ilu_smem_bytes(const SolverDev &d) {
-  auto al = [](size_t b) { return (b + 15) & ~(size_t)15; };
-  const size_t nr = d.max_sub_rows, ne = d.max_sub_lu;
-  return al(nr * sizeof(VT)) + al(nr * sizeof(MT)) + al((nr + 1) * 4) +
-         al(nr * 4) + al(ne * 4) + al(ne * sizeof(MT));
+  if (to_fp32) {
+    k_factor_to_fp32<<<d.n_sub, 256, 0, st>>>(d.meta64, d.rec64, d.meta32,
+                                              d.rec32);
+    count_launches(1);
+  }
 }
 
 template <class VT, class MT, int MODE>
-static void apply_ilu(const SolverDev &d, const MT *lu, const MT *ldinv,
-                      const VT *r, VT *pv, const VT *v, VT *z,
-                      const KScalars *sc, cudaStream_t st) {
-  const size_t smem = ilu_smem_bytes<VT, MT>(d);
-  if (!d.global_ilu && smem <= 200 * 1024) {
-    static bool attr_set = false;
-    if (!attr_set) {
-      cudaFuncSetAttribute(k_ilu0_apply_smem<VT, MT, MODE>,
+static void apply_ilu(const SolverDev &d, const VT *r, VT *pv, const VT *v,
+                      VT *z, const KScalars *sc, cudaStream_t st) {
+  const bool fp64 = sizeof(MT) == 8;
+  const SubMeta *meta = fp64 ? d.meta64 : d.meta32;
+  const uint8_t *rec = fp64 ? d.rec64 : d.rec32;
+  const size_t smem = fp64 ? d.smem64 : d.smem32;
+  if (smem) {
+    static size_t attr = 0;
+    if (smem > 48 * 1024 && attr < smem) {
+      cudaFuncSetAttribute(k_ilu0_apply_tma<VT, MT, MODE>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           200 * 1024);
-      attr_set = true;
+                           (int)smem);
+      attr = smem;
     }
-    k_ilu0_apply_smem<VT, MT, MODE><<<d.n_sub, 128, smem, st>>>(d, lu, ldinv, r,
-                                                               pv, v, z, sc);
+    k_ilu0_apply_tma<VT, MT, MODE><<<d.n_sub, 32, smem, st>>>(meta, rec, r, pv,
+                                                              v, z, sc, d.err);
     count_launches(1);
   } else {
-    k_ilu0_apply_global<VT, MT, MODE><<<d.n_sub, 1024, 0, st>>>(d, lu, ldinv, r,
+    k_ilu0_apply_global<VT, MT, MODE><<<d.n_sub, 1024, 0, st>>>(meta, rec, r,
                                                                pv, v, z, sc);
     count_launches(1);
   }
 }
 
 template <class VT, class MT>
-void launch_precond(int precond, int mode, const SolverDev &d, const MT *lu,
-                    const MT *ldinv, const MT *jdinv, const VT *r, VT *pv,
-                    const VT *v, VT *z, const KScalars *sc, cudaStream_t st) {
+void launch_precond(int precond, int mode, const SolverDev &d,
+                    const MT *jdinv, const VT *r, VT *pv, const VT *v, VT *z,
+                    const KScalars *sc, cudaStream_t st) {
   if (precond == PG_PREC_ILU0) {
-    if (mode == 0) apply_ilu<VT, MT, 0>(d, lu, ldinv, r, pv, v, z, sc, st);
-    else if (mode == 1) apply_ilu<VT, MT, 1>(d, lu, ldinv, r, pv, v, z, sc, st);
-    else apply_ilu<VT, MT, 2>(d, lu, ldinv, r, pv, v, z, sc, st);
+    if (mode == 0) apply_ilu<VT, MT, 0>(d, r, pv, v, z, sc, st);
+    else if (mode == 1) apply_ilu<VT, MT, 1>(d, r, pv, v, z, sc, st);
+    else apply_ilu<VT, MT, 2>(d, r, pv, v, z, sc, st);
   } else {
     const MT *di = precond == PG_PREC_JACOBI ? jdinv : nullptr;
     const int g = blocks_for(d.n, 256) < 1216 ? blocks_for(d.n, 256) : 1216;
     if (mode == 0) {
       k_diag_apply<VT, MT, 0><<<g, 256, 0, st>>>(d.n, di, r, pv, v, z, sc);
       count_launches(1);
-    }
-    else if (mode == 1) {
+    } else if (mode == 1) {
       k_diag_apply<VT, MT, 1><<<g, 256, 0, st>>>(d.n, di, r, pv, v, z, sc);
       count_launches(1);
-    }
-    else {
+    } else {
       k_diag_apply<VT, MT, 2><<<g, 256, 0, st>>>(d.n, di, r, pv, v, z, sc);
       count_launches(1);
     }
@@ -809,9 +889,9 @@ void launch_jacobi_diag(const SolverDev &d, const double *pvals, double *dinv,
 
 #define PG_INST(VT, MT)                                                       \
   template void launch_precond<VT, MT>(int, int, const SolverDev &,           \
-                                       const MT *, const MT *, const MT *,    \
-                                       const VT *, VT *, const VT *, VT *,    \
-                                       const KScalars *, cudaStream_t);       \
+                                       const MT *, const VT *, VT *,          \
+                                       const VT *, VT *, const KScalars *,    \
+                                       cudaStream_t);                         \
   template void launch_krylov_init<VT, MT>(const SolverDev &, const MT *,     \
                                            const VT *, const VT *, VT *,      \
                                            VT *, VT *, VT *, KScalars *,      \

@@ -69,14 +69,28 @@ void launch_gradient(int n_cells, int nf, const int32_t *fl,
                      double *grad_cell, cudaStream_t st);
 
 // ---- solver kernels ----
+// One Schwarz subdomain's ILU(0) factor is a packed record, 16-byte aligned
+// so one cp.async.bulk moves it into shared memory:
+//   uint16 lvl[nlev+1]   level boundaries (subdomain-local rows)
+//   uint16 cols[nr][K]   K = KL + KU slots: L columns then U columns,
+//                        0xFFFF marks an unused slot
+//   MT     vals[nr][K+1] L multipliers, U values, 1/u_ii
+struct SubMeta {
+  int32_t r0, nr, nlev, K, KL, rec_off, col_off, val_off, rec_bytes,
+      slot_base, pad0, pad1;
+};
+constexpr uint16_t kPadCol = 0xFFFF;
+
 struct SolverDev {
   int n, nnz, n_sub;
   // permuted CSR
   const int32_t *prp, *pci;
-  // ILU(0)
-  const int32_t *sub_ptr, *sub_lvl, *lvl_ptr, *lrp, *ldg, *lci, *lsrc;
-  int max_sub_rows, max_sub_lu;
-  int global_ilu;
+  // ILU(0) records (FP64 and FP32 copies)
+  const SubMeta *meta64, *meta32;
+  uint8_t *rec64, *rec32;
+  const int32_t *rec_src;
+  size_t smem64, smem32;  // dynamic smem of the staged apply (0 = too big)
+  int *err;               // set when a bounded device wait runs out
 };
 
 void launch_permute_values(int nnz, const int32_t *psrc, const double *src,
@@ -87,20 +101,19 @@ void launch_permute_vec(int n, const int32_t *perm, const double *src,
 void launch_unpermute_vec(int n, const int32_t *perm, const double *src,
                           double *dst, cudaStream_t st);
 
-// ILU(0) numeric factorisation; returns 0 when launched.  bad counts zero or
-// non-finite pivots.
-template <class MT>
-void launch_ilu0_factor(const SolverDev &d, const double *pvals, MT *lu,
-                        MT *ldinv, int *bad, cudaStream_t st);
+// ILU(0) numeric factorisation into the FP64 records (and the FP32 copy
+// when to_fp32); bad counts zero or non-finite pivots.
+void launch_ilu0_factor(const SolverDev &d, const double *pvals, int *bad,
+                        bool to_fp32, cudaStream_t st);
 
 // Preconditioner application with fused vector update.
 //   mode 0: z = M^-1 in
 //   mode 1: p = r + beta (p - omega v); z = M^-1 p   (p written back)
 //   mode 2: s = r - alpha v;            z = M^-1 s   (s written back)
 template <class VT, class MT>
-void launch_precond(int precond, int mode, const SolverDev &d, const MT *lu,
-                    const MT *ldinv, const MT *jdinv, const VT *r, VT *pv,
-                    const VT *v, VT *z, const KScalars *sc, cudaStream_t st);
+void launch_precond(int precond, int mode, const SolverDev &d,
+                    const MT *jdinv, const VT *r, VT *pv, const VT *v, VT *z,
+                    const KScalars *sc, cudaStream_t st);
 
 template <class VT, class MT>
 void launch_krylov_init(const SolverDev &d, const MT *val, const VT *b,

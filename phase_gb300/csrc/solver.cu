@@ -50,6 +50,8 @@ __global__ void k_add_correction(int n, double *__restrict__ x,
 
 }  // namespace
 
+constexpr size_t kMaxApplySmem = 200 * 1024;
+
 struct pg_solver {
   pg_solver_cfg cfg{};
   int64_t rank = 0;
@@ -57,14 +59,16 @@ struct pg_solver {
   Analysis a;
   bool analysed = false;
   uint64_t eqn_pattern = 0;  // pattern id of a device equation, 0 = host CSR
-  DevBuf<int32_t> perm, prp, pci, psrc, dup_dst, dup_src, sub_ptr, sub_lvl,
-      lvl_ptr, lrp, ldg, lci, lsrc;
+  DevBuf<int32_t> perm, prp, pci, psrc, dup_dst, dup_src, rec_src;
+  DevBuf<SubMeta> meta64, meta32;
+  DevBuf<uint8_t> rec64, rec32;
+  DevBuf<int> err;
   DevBuf<int32_t> raw_rp, raw_ci, st_rp, st_ci;
   DevBuf<double> st_vals, st_vec;
   DevBuf<unsigned int> diff;
   // values and factors
-  DevBuf<double> pvals, lu, ldinv, jdinv;
-  DevBuf<float> pvals32, lu32, ldinv32, jdinv32;
+  DevBuf<double> pvals, jdinv;
+  DevBuf<float> pvals32, jdinv32;
   // Krylov vectors (permuted order)
   DevBuf<double> b, x, r, rh, p, v, ph, s, sh, t, xout;
   DevBuf<float> f_b, f_x, f_r, f_rh, f_p, f_v, f_ph, f_s, f_sh, f_t;
@@ -95,16 +99,16 @@ struct pg_solver {
     d.n_sub = a.n_sub;
     d.prp = prp.p;
     d.pci = pci.p;
-    d.sub_ptr = sub_ptr.p;
-    d.sub_lvl = sub_lvl.p;
-    d.lvl_ptr = lvl_ptr.p;
-    d.lrp = lrp.p;
-    d.ldg = ldg.p;
-    d.lci = lci.p;
-    d.lsrc = lsrc.p;
-    d.max_sub_rows = a.max_sub_rows;
-    d.max_sub_lu = a.max_sub_lu;
-    d.global_ilu = a.global_ilu ? 1 : 0;
+    d.meta64 = meta64.p;
+    d.meta32 = meta32.p;
+    d.rec64 = rec64.p;
+    d.rec32 = rec32.p;
+    d.rec_src = rec_src.p;
+    // the staged (TMA) apply needs the largest record + vector in shared
+    // memory; otherwise the global-memory sweep is used
+    d.smem64 = a.smem64 <= kMaxApplySmem ? a.smem64 : 0;
+    d.smem32 = a.smem32 <= kMaxApplySmem ? a.smem32 : 0;
+    d.err = err.p;
     return d;
   }
   RedWork red() const { return RedWork{partials.p, ticket.p, red_grid}; }
@@ -124,27 +128,24 @@ int upload_analysis(pg_solver *s) {
   up(s->psrc, a.psrc);
   up(s->dup_dst, a.dup_dst);
   up(s->dup_src, a.dup_src);
-  up(s->sub_ptr, a.sub_ptr);
-  up(s->sub_lvl, a.sub_lvl);
-  up(s->lvl_ptr, a.lvl_ptr);
-  up(s->lrp, a.lrp);
-  up(s->ldg, a.ldg);
-  up(s->lci, a.lci);
-  up(s->lsrc, a.lsrc);
-  const size_t n = a.n, nnz = a.nnz, nlu = a.lci.size();
+  up(s->rec_src, a.rec_src);
+  up(s->meta64, a.meta64);
+  up(s->meta32, a.meta32);
+  up(s->rec64, a.rec64);
+  up(s->rec32, a.rec32);
+  if (e == cudaSuccess) e = s->err.zero(1);
+  const size_t n = a.n, nnz = a.nnz;
   for (DevBuf<double> *bf : {&s->b, &s->x, &s->r, &s->rh, &s->p, &s->v,
                              &s->ph, &s->s, &s->sh, &s->t, &s->xout,
-                             &s->ldinv, &s->jdinv})
+                             &s->jdinv})
     if (e == cudaSuccess) e = bf->reserve(n);
   if (e == cudaSuccess) e = s->pvals.reserve(nnz);
-  if (e == cudaSuccess) e = s->lu.reserve(nlu);
   if (s->cfg.precision == PG_MIXED) {
     for (DevBuf<float> *bf : {&s->f_b, &s->f_x, &s->f_r, &s->f_rh, &s->f_p,
                               &s->f_v, &s->f_ph, &s->f_s, &s->f_sh, &s->f_t,
-                              &s->ldinv32, &s->jdinv32})
+                              &s->jdinv32})
       if (e == cudaSuccess) e = bf->reserve(n);
     if (e == cudaSuccess) e = s->pvals32.reserve(nnz);
-    if (e == cudaSuccess) e = s->lu32.reserve(nlu);
   }
   s->red_grid = (int)std::min<int64_t>(1216, (n + kVecBlock - 1) / kVecBlock);
   if (s->red_grid < 1) s->red_grid = 1;
@@ -176,8 +177,8 @@ inline int grid_for(int64_t n) {
 // One BiCGStab run on the permuted system held in the given buffers.
 // VT/MT select FP64 or FP32 storage; reductions are FP64 throughout.
 template <class VT, class MT>
-int run_bicgstab(pg_solver *s, const MT *val, const MT *lu, const MT *ldinv,
-                 const MT *jdinv, VT *b, VT *x, VT *r, VT *rh, VT *p, VT *v,
+int run_bicgstab(pg_solver *s, const MT *val, const MT *jdinv, VT *b, VT *x,
+                 VT *r, VT *rh, VT *p, VT *v,
                  VT *ph, VT *ss, VT *sh, VT *t, double tol, int max_iters,
                  bool check_true, int *iters, int *restarts) {
   cudaStream_t st = stream();
@@ -195,11 +196,11 @@ int run_bicgstab(pg_solver *s, const MT *val, const MT *lu, const MT *ldinv,
     for (;;) {
       const int chunk = 8;
       for (int c = 0; c < chunk; ++c) {
-        launch_precond<VT, MT>(s->cfg.precond, 1, d, lu, ldinv, jdinv, r, p, v,
-                               ph, s->sc.p, st);
+        launch_precond<VT, MT>(s->cfg.precond, 1, d, jdinv, r, p, v, ph,
+                               s->sc.p, st);
         launch_spmv_v<VT, MT>(d, val, ph, v, rh, s->sc.p, w, st);
-        launch_precond<VT, MT>(s->cfg.precond, 2, d, lu, ldinv, jdinv, r, ss, v,
-                               sh, s->sc.p, st);
+        launch_precond<VT, MT>(s->cfg.precond, 2, d, jdinv, r, ss, v, sh,
+                               s->sc.p, st);
         launch_spmv_t<VT, MT>(d, val, sh, t, ss, s->sc.p, w, st);
         launch_update<VT>(d.n, x, r, ph, sh, ss, t, rh, s->sc.p, w, st);
       }
@@ -242,23 +243,18 @@ int run_bicgstab(pg_solver *s, const MT *val, const MT *lu, const MT *ldinv,
 int factor(pg_solver *s) {
   cudaStream_t st = stream();
   const SolverDev d = s->dev();
+  const bool mixed = s->cfg.precision == PG_MIXED;
   if (s->cfg.precond == PG_PREC_ILU0) {
     PG_CUDA(cudaMemsetAsync(s->bad.p, 0, sizeof(int), st));
-    launch_ilu0_factor<double>(d, s->pvals.p, s->lu.p, s->ldinv.p, s->bad.p, st);
+    launch_ilu0_factor(d, s->pvals.p, s->bad.p, mixed, st);
     PG_CUDA(cudaGetLastError());
   } else if (s->cfg.precond == PG_PREC_JACOBI) {
     launch_jacobi_diag(d, s->pvals.p, s->jdinv.p, st);
   }
-  if (s->cfg.precision == PG_MIXED) {
-    const int64_t nlu = (int64_t)s->a.lci.size();
+  if (mixed) {
     k_to_float<<<grid_for(s->a.nnz), 256, 0, st>>>(s->a.nnz, s->pvals.p, s->pvals32.p);
     count_launches(1);
-    if (s->cfg.precond == PG_PREC_ILU0) {
-      k_to_float<<<grid_for(nlu), 256, 0, st>>>(nlu, s->lu.p, s->lu32.p);
-      count_launches(1);
-      k_to_float<<<grid_for(s->a.n), 256, 0, st>>>(s->a.n, s->ldinv.p, s->ldinv32.p);
-      count_launches(1);
-    } else if (s->cfg.precond == PG_PREC_JACOBI) {
+    if (s->cfg.precond == PG_PREC_JACOBI) {
       k_to_float<<<grid_for(s->a.n), 256, 0, st>>>(s->a.n, s->jdinv.p, s->jdinv32.p);
       count_launches(1);
     }
@@ -491,7 +487,7 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
   } else if (s->cfg.precision == PG_FP64) {
     int restarts = 0;
     status = run_bicgstab<double, double>(
-        s, s->pvals.p, s->lu.p, s->ldinv.p, s->jdinv.p, s->b.p, s->x.p, s->r.p,
+        s, s->pvals.p, s->jdinv.p, s->b.p, s->x.p, s->r.p,
         s->rh.p, s->p.p, s->v.p, s->ph.p, s->s.p, s->sh.p, s->t.p, tol,
         s->cfg.max_iters, true, &iters, &restarts);
     outer = restarts + 1;
@@ -516,7 +512,7 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
       const int budget = std::max(1, std::min(s->cfg.inner_max_iters,
                                               s->cfg.max_iters - iters));
       const int ist = run_bicgstab<float, float>(
-          s, s->pvals32.p, s->lu32.p, s->ldinv32.p, s->jdinv32.p, s->f_b.p,
+          s, s->pvals32.p, s->jdinv32.p, s->f_b.p,
           s->f_x.p, s->f_r.p, s->f_rh.p, s->f_p.p, s->f_v.p, s->f_ph.p,
           s->f_s.p, s->f_sh.p, s->f_t.p, s->cfg.inner_tolerance, budget,
           false, &it, &rs);
@@ -546,6 +542,11 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
   PG_CUDA(cudaMemcpyAsync(s->sc_host, s->sc.p, sizeof(KScalars),
                           cudaMemcpyDeviceToHost, st));
   PG_CUDA(cudaStreamSynchronize(st));
+  int timed_out = 0;
+  if (s->cfg.precond == PG_PREC_ILU0) {
+    PG_CUDA(cudaMemcpy(&timed_out, s->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (timed_out) PG_CUDA(cudaMemsetAsync(s->err.p, 0, sizeof(int), st));
+  }
   float ms_fact = 0.f, ms_all = 0.f;
   cudaEventElapsedTime(&ms_fact, s->ev[0], s->ev[1]);
   cudaEventElapsedTime(&ms_all, s->ev[0], s->ev[2]);
@@ -554,6 +555,7 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
     status = PG_BREAKDOWN;
   if (status == PG_OK && !(rel <= tol)) status = PG_MAX_ITERS;
   if (!std::isfinite(rel)) status = PG_NON_FINITE;
+  if (timed_out) status = PG_TIMEOUT;
   s->have_x = true;  // warm start for the next solve, as Belos reuses x_
   if (stats) {
     stats->iters = iters;
@@ -613,10 +615,10 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
     return PG_OK;
   };
   int rc = timed([&] { launch_spmv_v<double, double>(d, s->pvals.p, s->ph.p, s->v.p, s->rh.p, s->sc.p, w, st); }, &ms[0]);
-  if (!rc) rc = timed([&] { launch_precond<double, double>(s->cfg.precond, 1, d, s->lu.p, s->ldinv.p, s->jdinv.p, s->r.p, s->p.p, s->v.p, s->ph.p, s->sc.p, st); }, &ms[1]);
+  if (!rc) rc = timed([&] { launch_precond<double, double>(s->cfg.precond, 1, d, s->jdinv.p, s->r.p, s->p.p, s->v.p, s->ph.p, s->sc.p, st); }, &ms[1]);
   if (!rc) rc = timed([&] { launch_update<double>(d.n, xs.p, rs.p, s->ph.p, s->sh.p, s->s.p, s->t.p, s->rh.p, s->sc.p, w, st); }, &ms[2]);
   if (!rc && s->cfg.precond == PG_PREC_ILU0)
-    rc = timed([&] { launch_ilu0_factor<double>(d, s->pvals.p, s->lu.p, s->ldinv.p, s->bad.p, st); }, &ms[3]);
+    rc = timed([&] { launch_ilu0_factor(d, s->pvals.p, s->bad.p, false, st); }, &ms[3]);
   else if (!rc)
     ms[3] = 0.;
   PG_CUDA(cudaStreamSynchronize(st));
