@@ -255,27 +255,32 @@ def run_ours(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t[0])
 
-    # kernel-level roofline on the same system
+    # kernel-level roofline on the same system: per-launch CUDA-event times
+    # of the hot kernels (FP64 ones for fp64, the FP32 inner ones for mixed)
     prof = solver.profile(reps=50)
     a_nnz = int(eqn.nnz)
-    # compulsory bytes per launch
-    b_spmv = 12 * a_nnz + 4 * (n + 1) + 8 * n * 3          # A, x, rhat, v
-    b_prec = 12 * a_nnz + 8 * n + 8 * n + 8 * n * 5        # LU, rp/dg, dinv, r p v in, p z out
-    b_upd = 8 * n * 9                                       # x r ph sh s t rh in; x r out
-    iters = max(1, stats[-1]["iters"])
-    shares = {"spmv": 2 * prof["spmv"], "ilu_apply": 2 * prof["precond"],
-              "update": prof["update"]}
+    vb = 8 if prec == pg.FP64 else 4
+    sfx = "" if prec == pg.FP64 else "32"
+    # compulsory bytes per launch: A values + int32
+    # columns + row pointers; streamed ILU(0) factor values + uint16
+    # columns (off-diagonal entries of A bound the factor's) + 1/u_ii
+    b_spmv = (vb + 4) * a_nnz + 4 * (n + 1) + 3 * vb * n    # A, x, rhat in; v out
+    b_prec = (vb + 2) * (a_nnz - n) + vb * n + 5 * vb * n   # LU, dinv, r p v in, p z out
+    b_upd = 9 * vb * n                                      # x r ph sh s t rh in; x r out
+    ms_of = {"spmv": prof["spmv" + sfx], "ilu_apply": prof["precond" + sfx],
+             "update": prof["update" + sfx]}
+    shares = {"spmv": 2 * ms_of["spmv"], "ilu_apply": 2 * ms_of["ilu_apply"],
+              "update": ms_of["update"]}
     dom = max(shares, key=shares.get)
     bytes_of = {"spmv": b_spmv, "ilu_apply": b_prec, "update": b_upd}
-    ms_of = {"spmv": prof["spmv"], "ilu_apply": prof["precond"],
-             "update": prof["update"]}
     peak, peak_kind = measured_peaks()
     achieved = bytes_of[dom] / (ms_of[dom] * 1e-3) / 1e9
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get(dom)
+            traffic = json.load(f).get(f"{dom}_{args.precision}")
+    iters = max(1, stats[-1]["iters"])
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
                 "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic,
@@ -283,6 +288,8 @@ def run_ours(args):
                 "launch_ms": round(ms_of[dom], 5),
                 "per_kernel_gbs": {k: round(bytes_of[k] / (ms_of[k] * 1e-3) / 1e9, 1)
                                    for k in bytes_of},
+                "per_kernel_ms": {k: round(v, 5) for k, v in ms_of.items()},
+                "factor_ms": round(prof["factor"], 4),
                 "frac_of_8tbs": round(achieved / 8000.0, 4)}
 
     # e2e through the reference-facing call sequence with host buffers

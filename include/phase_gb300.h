@@ -215,9 +215,11 @@ int pg_solver_get_x(const pg_solver *s, double *x, int ptr_kind);
 
 /* Time the solver's kernels in isolation on its current system: each is
  * launched `reps` times back to back on the library stream between CUDA
- * events.  ms[0] SpMV with fused dot, ms[1] ILU(0)/Jacobi apply with fused
- * update, ms[2] BiCGStab x/r update, ms[3] ILU(0) factorisation; per launch.
- * Leaves the solution untouched.  (No reference counterpart: measurement.) */
+ * events, on scratch vectors.  Per launch, ms[0] FP64 SpMV with fused dot,
+ * ms[1] FP64 ILU(0)/Jacobi apply with fused update, ms[2] FP64 BiCGStab x/r
+ * update, ms[3] ILU(0) factorisation, and for PG_MIXED ms[4..6] the FP32
+ * SpMV, apply and update (0 otherwise); ms[7] is reserved (0).  Leaves the
+ * solver's state untouched.  (No reference counterpart: measurement.) */
 int pg_solver_profile(pg_solver *s, int reps, double *ms);
 
 /* Number of kernels the library has launched since it was loaded. */

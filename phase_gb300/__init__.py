@@ -354,11 +354,12 @@ class SparseMatrixSolver:
         return part, k.value
 
     def profile(self, reps: int = 20):
-        """Per-launch ms of the hot kernels on the current system:
-        spmv, precond apply, update, ilu factor."""
-        ms = np.zeros(4)
+        """Per-launch ms of the hot kernels on the current system (FP64, and
+        FP32 for the mixed precision solver)."""
+        ms = np.zeros(8)
         _check(lib().pg_solver_profile(self._h, int(reps), _ptr(ms)))
-        return dict(spmv=ms[0], precond=ms[1], update=ms[2], factor=ms[3])
+        return dict(spmv=ms[0], precond=ms[1], update=ms[2], factor=ms[3],
+                    spmv32=ms[4], precond32=ms[5], update32=ms[6])
 
     def printStatus(self, msg: str):
         print(f"{msg} iterations = {self.nIters()}, error = {self.error():f}.")

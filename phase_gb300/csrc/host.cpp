@@ -170,7 +170,6 @@ int build_pattern(const HostMesh &m, int gamma_kind, const int32_t *bc_type,
     row.clear();
     const int64_t b = m.link_ptr[c], e = m.link_ptr[c + 1];
     const int64_t base = (int64_t)p.col_ind.size();
-    std::vector<std::pair<int64_t, int32_t>> off_slot, diag_slot;  // link->k
     for (int64_t k = b; k < e; ++k) {
       const int32_t f = m.link_face[k], nbc = m.link_cell[k];
       if (nbc >= 0) {
@@ -521,15 +520,18 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   }
 
   // 7. packed per-subdomain records (layout in kernels.cuh): level bounds,
-  //    L/U column slots (subdomain-local, uint16) and value slots; records
-  //    and their sections start on 16-byte boundaries for cp.async.bulk
-  PG_CHECK_ARG(a.max_sub_rows <= 65535,
-               "ILU(0) subdomains are limited to 65535 rows (use Schwarz "
+  //    then slot-major L/U column slots (subdomain-local, uint16) and value
+  //    slots, so consecutive rows of a level sit in consecutive addresses;
+  //    records and their sections start on 16-byte boundaries for
+  //    cp.async.bulk
+  PG_CHECK_ARG(a.max_sub_rows <= 65534,
+               "ILU(0) subdomains are limited to 65534 rows (use Schwarz "
                "subdomains for larger systems)");
   auto al16 = [](int64_t b) { return (b + 15) & ~(int64_t)15; };
   a.meta64.resize(a.n_sub);
   a.meta32.resize(a.n_sub);
   int64_t off64 = 0, off32 = 0, slots = 0;
+  a.max_kl = a.max_ku = 0;
   for (int s = 0; s < a.n_sub; ++s) {
     const int32_t r0 = a.sub_ptr[s], r1 = a.sub_ptr[s + 1], nr = r1 - r0;
     int kl = 0, ku = 0;
@@ -537,9 +539,12 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       kl = std::max(kl, a.ldg[i] - a.lrp[i]);
       ku = std::max(ku, a.lrp[i + 1] - a.ldg[i] - 1);
     }
+    a.max_kl = std::max(a.max_kl, kl);
+    a.max_ku = std::max(a.max_ku, ku);
     const int K = kl + ku;
     const int nlev = a.sub_lvl[s + 1] - a.sub_lvl[s];
-    const int64_t col_off = al16(2 * (int64_t)(nlev + 1));
+    // lvl[] carries one sentinel past the last level bound
+    const int64_t col_off = al16(2 * (int64_t)(nlev + 2));
     const int64_t val_off = col_off + al16(2 * (int64_t)nr * K);
     for (int pass = 0; pass < 2; ++pass) {
       const int64_t vsz = pass == 0 ? 8 : 4;
@@ -560,32 +565,231 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   a.smem64 = a.smem32 = 0;
   for (int s = 0; s < a.n_sub; ++s) {
     const SubMeta &m = a.meta64[s];
-    const int K = m.K, kl = m.KL;
+    const int K = m.K, kl = m.KL, nr = m.nr;
     for (int pass = 0; pass < 2; ++pass) {
       const SubMeta &mm = pass == 0 ? a.meta64[s] : a.meta32[s];
       uint8_t *base = (pass == 0 ? a.rec64 : a.rec32).data() + mm.rec_off;
       uint16_t *lvl = reinterpret_cast<uint16_t *>(base);
       for (int l = 0; l <= m.nlev; ++l)
         lvl[l] = (uint16_t)(a.lvl_ptr[a.sub_lvl[s] + l] - m.r0);
+      lvl[m.nlev + 1] = (uint16_t)nr;
       uint16_t *cols = reinterpret_cast<uint16_t *>(base + mm.col_off);
-      for (int i = 0; i < m.nr; ++i) {
+      for (int i = 0; i < nr; ++i) {
         const int32_t g = m.r0 + i;
         const int nl = a.ldg[g] - a.lrp[g], nu = a.lrp[g + 1] - a.ldg[g] - 1;
-        for (int k = 0; k < K; ++k) cols[i * K + k] = kPadCol;
-        for (int k = 0; k < nl; ++k) cols[i * K + k] = (uint16_t)a.lci[a.lrp[g] + k];
+        for (int k = 0; k < K; ++k) cols[(int64_t)k * nr + i] = kPadCol;
+        for (int k = 0; k < nl; ++k)
+          cols[(int64_t)k * nr + i] = (uint16_t)a.lci[a.lrp[g] + k];
         for (int k = 0; k < nu; ++k)
-          cols[i * K + kl + k] = (uint16_t)a.lci[a.ldg[g] + 1 + k];
+          cols[(int64_t)(kl + k) * nr + i] = (uint16_t)a.lci[a.ldg[g] + 1 + k];
         if (pass == 0) {
-          int32_t *src = a.rec_src.data() + m.slot_base + (int64_t)i * (K + 1);
-          for (int k = 0; k < nl; ++k) src[k] = a.lsrc[a.lrp[g] + k];
-          for (int k = 0; k < nu; ++k) src[kl + k] = a.lsrc[a.ldg[g] + 1 + k];
-          src[K] = a.lsrc[a.ldg[g]];
+          int32_t *src = a.rec_src.data() + m.slot_base;
+          for (int k = 0; k < nl; ++k) src[(int64_t)k * nr + i] = a.lsrc[a.lrp[g] + k];
+          for (int k = 0; k < nu; ++k)
+            src[(int64_t)(kl + k) * nr + i] = a.lsrc[a.ldg[g] + 1 + k];
+          src[(int64_t)K * nr + i] = a.lsrc[a.ldg[g]];
         }
       }
       const size_t sm = (size_t)al16(mm.rec_bytes) +
-                        (size_t)m.nr * (pass == 0 ? 8 : 4);
+                        (size_t)nr * (pass == 0 ? 8 : 4);
       size_t &mx = pass == 0 ? a.smem64 : a.smem32;
       mx = std::max(mx, sm);
+    }
+  }
+
+  // 8. streaming records (kernels.cuh StreamMeta): per level, the L slots
+  //    (forward sweep) and the U slots + 1/u_ii (backward sweep) of the
+  //    level's rows, slot-major; consecutive levels are grouped into pieces
+  //    of about kStreamPiece bytes.  pack_* map every value position of a
+  //    stream to its slot in the FP64 factor records.
+  a.smeta64.resize(a.n_sub);
+  a.smeta32.resize(a.n_sub);
+  a.pack_src.clear();
+  a.pack_src32.clear();
+  a.pack_dst64.clear();
+  a.pack_dst32.clear();
+  a.ssmem64 = a.ssmem32 = 0;
+  int64_t soff[2] = {0, 0};
+  std::vector<uint8_t> *sbuf[2] = {&a.srec64, &a.srec32};
+  a.srec64.clear();
+  a.srec32.clear();
+  // one slot count for all subdomains, matching the apply kernel's
+  // compile-time variants (2/2 quadrilaterals, 3/3 triangles)
+  int KLs = a.max_kl, KUs = a.max_ku;
+  if (KLs <= 2 && KUs <= 2) KLs = KUs = 2;
+  else if (KLs <= 3 && KUs <= 3) KLs = KUs = 3;
+  for (int s = 0; s < a.n_sub; ++s) {
+    const SubMeta &f = a.meta64[s];
+    const int nr = f.nr, nlev = f.nlev, KL = KLs, KU = KUs;
+    const int fKL = f.KL, fKU = f.K - f.KL;
+    const int64_t fsrc0 = (f.rec_off + f.val_off) / 8;  // double index
+    const uint16_t *flvl = reinterpret_cast<const uint16_t *>(a.rec64.data() + f.rec_off);
+    const uint16_t *fcols =
+        reinterpret_cast<const uint16_t *>(a.rec64.data() + f.rec_off + f.col_off);
+    for (int pass = 0; pass < 2; ++pass) {
+      const int64_t vs = pass == 0 ? 8 : 4;
+      auto fblob = [&](int w) { return al16(2 * (int64_t)KL * w) + al16(vs * (int64_t)KL * w); };
+      auto bblob = [&](int w) {
+        return al16(2 * (int64_t)KU * w) + al16(vs * (int64_t)KU * w) + al16(vs * (int64_t)w);
+      };
+      // pieces: {first level, bytes}
+      std::vector<std::pair<int, int64_t>> fp, bp;
+      for (int l = 0; l < nlev; ++l) {
+        const int64_t sz = fblob(flvl[l + 1] - flvl[l]);
+        if (fp.empty() || fp.back().second + sz > kStreamPiece) fp.push_back({l, 0});
+        fp.back().second += sz;
+      }
+      for (int l = nlev - 1; l >= 0; --l) {
+        const int64_t sz = bblob(flvl[l + 1] - flvl[l]);
+        if (bp.empty() || bp.back().second + sz > kStreamPiece) bp.push_back({l, 0});
+        bp.back().second += sz;
+      }
+      for (auto &q : fp) q.second = std::max<int64_t>(q.second, 16);
+      for (auto &q : bp) q.second = std::max<int64_t>(q.second, 16);
+      const int np = (int)(fp.size() + bp.size());
+      const int64_t lvl_bytes = (2 * (int64_t)(nlev + 2) + 3) & ~(int64_t)3;
+      const int64_t hdr = al16(lvl_bytes + 4 * (2 + 3 * (int64_t)np));
+      int64_t total = hdr, max_piece = 16;
+      for (auto &q : fp) total += q.second, max_piece = std::max(max_piece, q.second);
+      for (auto &q : bp) total += q.second, max_piece = std::max(max_piece, q.second);
+      PG_CHECK_ARG(soff[pass] + total < ((int64_t)1 << 31), "ILU(0) stream too large");
+      StreamMeta sm{f.r0, nr, nlev, KL, KU, (int32_t)soff[pass], (int32_t)hdr,
+                    (int32_t)max_piece};
+      (pass == 0 ? a.smeta64 : a.smeta32)[s] = sm;
+      std::vector<uint8_t> &buf = *sbuf[pass];
+      buf.resize(soff[pass] + total, 0);
+      uint8_t *base = buf.data() + soff[pass];
+      std::memcpy(base, flvl, 2 * (size_t)(nlev + 2));
+      int32_t *ints = reinterpret_cast<int32_t *>(base + lvl_bytes);
+      ints[0] = (int32_t)fp.size();
+      ints[1] = (int32_t)bp.size();
+      int64_t off = hdr;
+      auto emit_values = [&](int64_t byte_off, int64_t slot) {
+        // byte_off is relative to this record; slot indexes the factor
+        const int64_t dst = (soff[pass] + byte_off) / vs;
+        (pass == 0 ? a.pack_src : a.pack_src32).push_back((int32_t)(fsrc0 + slot));
+        (pass == 0 ? a.pack_dst64 : a.pack_dst32).push_back((int32_t)dst);
+      };
+      int t = 0;
+      for (size_t q = 0; q < fp.size(); ++q, ++t) {
+        const int l0 = fp[q].first;
+        const int l1 = q + 1 < fp.size() ? fp[q + 1].first : nlev;
+        ints[2 + 3 * t] = l0;
+        ints[3 + 3 * t] = (int32_t)off;
+        ints[4 + 3 * t] = (int32_t)fp[q].second;
+        for (int l = l0; l < l1; ++l) {
+          const int ra = flvl[l], w = flvl[l + 1] - ra;
+          uint16_t *cc = reinterpret_cast<uint16_t *>(base + off);
+          const int64_t voff = off + al16(2 * (int64_t)KL * w);
+          for (int k = 0; k < KL; ++k)
+            for (int j = 0; j < w; ++j) {
+              const int64_t slot = (int64_t)k * nr + ra + j;
+              const uint16_t col = k < fKL ? fcols[slot] : kPadCol;
+              // an unused slot points at the zero entry z[nr]
+              cc[k * w + j] = col == kPadCol ? (uint16_t)nr : col;
+              if (col != kPadCol) emit_values(voff + vs * ((int64_t)k * w + j), slot);
+            }
+          off += fblob(w);
+        }
+      }
+      for (size_t q = 0; q < bp.size(); ++q, ++t) {
+        const int lhi = bp[q].first;
+        const int llo = q + 1 < bp.size() ? bp[q + 1].first + 1 : 0;
+        ints[2 + 3 * t] = lhi;
+        ints[3 + 3 * t] = (int32_t)off;
+        ints[4 + 3 * t] = (int32_t)bp[q].second;
+        for (int l = lhi; l >= llo; --l) {
+          const int ra = flvl[l], w = flvl[l + 1] - ra;
+          uint16_t *cc = reinterpret_cast<uint16_t *>(base + off);
+          const int64_t voff = off + al16(2 * (int64_t)KU * w);
+          const int64_t doff = voff + al16(vs * (int64_t)KU * w);
+          for (int k = 0; k < KU; ++k)
+            for (int j = 0; j < w; ++j) {
+              const int64_t slot = (int64_t)(fKL + k) * nr + ra + j;
+              const uint16_t col = k < fKU ? fcols[slot] : kPadCol;
+              cc[k * w + j] = col == kPadCol ? (uint16_t)nr : col;
+              if (col != kPadCol) emit_values(voff + vs * ((int64_t)k * w + j), slot);
+            }
+          for (int j = 0; j < w; ++j)
+            emit_values(doff + vs * j, (int64_t)(fKL + fKU) * nr + ra + j);
+          off += bblob(w);
+        }
+      }
+      soff[pass] += total;
+      const size_t need = (size_t)hdr + 2 * (size_t)max_piece + (size_t)al16(vs * (int64_t)(nr + 1));
+      size_t &mx = pass == 0 ? a.ssmem64 : a.ssmem32;
+      mx = std::max(mx, need);
+    }
+  }
+
+  // 9. step streams: when no row has more than 3 L or 3 U entries, the FP32
+  //    stream uses warp-wide steps (kernels.cuh StepMeta) instead of level
+  //    blobs (the FP64 sweep stays on the blobs, where it is faster)
+  a.use_steps = a.max_kl <= 3 && a.max_ku <= 3 && a.max_sub_rows < 32767;
+  if (a.use_steps) {
+    a.tmeta32.resize(a.n_sub);
+    a.pack_src32.clear();
+    a.pack_dst32.clear();
+    a.srec32.clear();
+    a.ssmem32 = 0;
+    int64_t toff[2] = {0, 0};
+    for (int s = 0; s < a.n_sub; ++s) {
+      const SubMeta &f = a.meta64[s];
+      const int nr = f.nr, nlev = f.nlev, fKL = f.KL, fKU = f.K - f.KL;
+      const int64_t fsrc0 = (f.rec_off + f.val_off) / 8;
+      const uint16_t *flvl = reinterpret_cast<const uint16_t *>(a.rec64.data() + f.rec_off);
+      const uint16_t *fcols =
+          reinterpret_cast<const uint16_t *>(a.rec64.data() + f.rec_off + f.col_off);
+      int n_fwd = 0, n_bwd = 0;
+      for (int l = 0; l < nlev; ++l) n_fwd += (flvl[l + 1] - flvl[l] + 31) / 32;
+      n_bwd = n_fwd;
+      for (int pass = 1; pass < 2; ++pass) {
+        const int64_t vs = 4;
+        const int64_t sb = 32 * 16 + 32 * 4 * vs;
+        const int64_t bytes = (int64_t)(n_fwd + n_bwd) * sb;
+        PG_CHECK_ARG(toff[pass] + bytes < ((int64_t)1 << 31), "ILU(0) steps too large");
+        StepMeta tm{f.r0, nr, n_fwd, n_bwd, (int32_t)toff[pass], 0, 0, 0};
+        a.tmeta32[s] = tm;
+        std::vector<uint8_t> &buf = a.srec32;
+        buf.resize(toff[pass] + bytes, 0);
+        uint8_t *base = buf.data() + toff[pass];
+        int64_t step = 0;
+        auto emit = [&](int64_t byte_off, int64_t slot) {
+          a.pack_src32.push_back((int32_t)(fsrc0 + slot));
+          a.pack_dst32.push_back((int32_t)((toff[pass] + byte_off) / vs));
+        };
+        for (int dir = 0; dir < 2; ++dir) {
+          const int k0 = dir == 0 ? 0 : fKL, kn = dir == 0 ? fKL : fKU;
+          for (int li = 0; li < nlev; ++li) {
+            const int l = dir == 0 ? li : nlev - 1 - li;
+            for (int c0 = flvl[l]; c0 < flvl[l + 1]; c0 += 32, ++step) {
+              uint8_t *sp = base + step * sb;
+              uint32_t *idx = reinterpret_cast<uint32_t *>(sp);
+              const uint32_t pad = (uint32_t)(nr * vs);
+              for (int t = 0; t < 32; ++t) {
+                const int row = c0 + t;
+                uint32_t *e = idx + 4 * t;
+                e[0] = e[1] = e[2] = e[3] = pad;
+                if (row >= flvl[l + 1]) continue;
+                e[0] = (uint32_t)(row * vs);
+                for (int k = 0; k < kn; ++k) {
+                  const int64_t slot = (int64_t)(k0 + k) * nr + row;
+                  if (fcols[slot] == kPadCol) continue;
+                  e[1 + k] = (uint32_t)(fcols[slot] * vs);
+                  emit(step * sb + 512 + vs * (4 * t + k), slot);
+                }
+                if (dir == 1)
+                  emit(step * sb + 512 + vs * (4 * t + 3),
+                       (int64_t)(fKL + fKU) * nr + row);
+              }
+            }
+          }
+        }
+        toff[pass] += bytes;
+        const size_t need = 2 * (size_t)kStepsPerPiece * sb +
+                            (size_t)al16(vs * (int64_t)(nr + 1));
+        a.ssmem32 = std::max(a.ssmem32, need);
+      }
     }
   }
   return PG_OK;

@@ -1,0 +1,531 @@
+// ILU(0) on Schwarz subdomains: numeric factorisation and the triangular
+// sweeps, on the packed per-subdomain records described in kernels.cuh.
+//
+// Apply (the hot kernel): one warp owns one subdomain.  Its factor is stored
+// as a stream of level-aligned pieces (kernels.cuh StreamMeta); lane 0 moves
+// the header and then the pieces into shared memory with cp.async.bulk (TMA)
+// into two alternating buffers completed on mbarriers, so the next piece
+// arrives while the current one is swept.  Within a piece the rows of a level
+// are slot-major (the lanes read consecutive addresses) and the warp
+// synchronises with __syncwarp between levels.  A warp needs only
+// header + 2 pieces + its z vector of shared memory (about 21 KB for a
+// 1024-row FP64 subdomain), so many subdomains run per SM and hide the
+// latency of the level chain.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/phase_gb300.h"
+#include "kernels.cuh"
+
+namespace pg {
+
+namespace {
+
+// ---- TMA / mbarrier helpers (sm_90+ PTX) ----
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                   smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_load(void *dst, const void *src,
+                                          uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], "
+      "%2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+constexpr int kWaitLimit = 1 << 22;  // try_wait polls before giving up
+
+// Bounded wait on a single-use barrier.  On expiry the error flag is set and
+// the copy still in flight is waited for once more (bounded) so the CTA does
+// not exit under it.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, int *err,
+                                                  uint32_t parity = 0) {
+  for (int it = 0; it < kWaitLimit; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  if (err) atomicExch(err, 1);
+  for (int it = 0; it < kWaitLimit; ++it)
+    if (mbar_try_wait(bar, parity)) break;
+  return false;
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ int al16(int b) { return (b + 15) & ~15; }
+
+// Row-wise IKJ ILU(0) (Saad, Iterative Methods for Sparse Linear Systems,
+// Alg. 10.4) on the diagonal block of one subdomain, in its record.  The CTA
+// walks the level schedule; rows of one level depend only on rows of earlier
+// levels, which the barrier has completed.  Pivots are FP64; the diagonal
+// slot ends up holding 1/u_ii.
+__global__ void k_ilu0_factor(const SubMeta *__restrict__ meta,
+                              uint8_t *__restrict__ rec,
+                              const int32_t *__restrict__ rec_src,
+                              const double *__restrict__ pvals,
+                              int *__restrict__ bad) {
+  const SubMeta m = meta[blockIdx.x];
+  uint8_t *base = rec + m.rec_off;
+  const uint16_t *lvl = reinterpret_cast<const uint16_t *>(base);
+  const uint16_t *cols = reinterpret_cast<const uint16_t *>(base + m.col_off);
+  double *vals = reinterpret_cast<double *>(base + m.val_off);
+  const int K = m.K, KL = m.KL, KU = K - KL, nr = m.nr;
+  const int n_slots = nr * (K + 1);
+  for (int j = threadIdx.x; j < n_slots; j += blockDim.x) {
+    const int src = rec_src[m.slot_base + j];
+    vals[j] = src >= 0 ? pvals[src] : 0.;
+  }
+  __syncthreads();
+  double *dg = vals + (size_t)K * nr;
+  for (int lv = 0; lv < m.nlev; ++lv) {
+    const int a = lvl[lv], b = lvl[lv + 1];
+    for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
+      for (int k = 0; k < KL; ++k) {
+        const int c = cols[(size_t)k * nr + i];
+        if (c == kPadCol) break;
+        const double lik = vals[(size_t)k * nr + i] / dg[c];
+        vals[(size_t)k * nr + i] = lik;
+        // a_ij -= l_ik u_kj for the columns j of U(k) present in row i
+        for (int q = 0; q < KU; ++q) {
+          const int cu = cols[(size_t)(KL + q) * nr + c];
+          if (cu == kPadCol) break;
+          const double d = lik * vals[(size_t)(KL + q) * nr + c];
+          if (cu == i) {
+            dg[i] -= d;
+            continue;
+          }
+          for (int k2 = 0; k2 < K; ++k2)
+            if (cols[(size_t)k2 * nr + i] == cu) {
+              vals[(size_t)k2 * nr + i] -= d;
+              break;
+            }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+    const double piv = dg[i];
+    if (piv == 0. || !isfinite(piv)) {
+      atomicAdd(bad, 1);
+      dg[i] = 0.;
+    } else {
+      dg[i] = 1. / piv;
+    }
+  }
+}
+
+// FP32 copy of the factor values (the FP32 records' static parts are set up
+// once on the host).
+__global__ void k_factor_to_fp32(const SubMeta *__restrict__ m64,
+                                 const uint8_t *__restrict__ rec64,
+                                 const SubMeta *__restrict__ m32,
+                                 uint8_t *__restrict__ rec32) {
+  const SubMeta a = m64[blockIdx.x], b = m32[blockIdx.x];
+  const double *src =
+      reinterpret_cast<const double *>(rec64 + a.rec_off + a.val_off);
+  float *dst = reinterpret_cast<float *>(rec32 + b.rec_off + b.val_off);
+  const int n = a.nr * (a.K + 1);
+  for (int j = threadIdx.x; j < n; j += blockDim.x) dst[j] = (float)src[j];
+}
+
+// One level of a sweep: rows a .. a+w-1, slot-major columns cc and values vv
+// (KS slots, compile-time when KT > 0), optional 1/u_ii dd.
+template <class VT, class MT, int KT>
+__device__ __forceinline__ void sweep_level(VT *zs, int a, int w, int ks,
+                                            const uint16_t *cc, const MT *vv,
+                                            const MT *dd, int lane) {
+  const int K = KT > 0 ? KT : ks;
+  for (int t = lane; t < w; t += 32) {
+    VT acc = zs[a + t];
+    if (KT > 0) {
+#pragma unroll
+      for (int k = 0; k < (KT > 0 ? KT : 1); ++k)
+        acc -= (VT)vv[k * w + t] * zs[cc[k * w + t]];
+    } else {
+      for (int k = 0; k < K; ++k) acc -= (VT)vv[k * w + t] * zs[cc[k * w + t]];
+    }
+    zs[a + t] = dd ? acc * (VT)dd[t] : acc;
+  }
+}
+
+// Forward/backward sweeps of one subdomain by one warp (see file header).
+// Shared memory: header | piece buffer 0 | piece buffer 1 | z[nr+1].  Piece
+// j+2 is loaded into the buffer piece j used while piece j+1 is being
+// swept.  KLT/KUT fix the L/U slot counts at compile time (0 = from meta).
+template <class VT, class MT, int MODE, int KLT, int KUT>
+__global__ void __launch_bounds__(32)
+k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
+                    const uint8_t *__restrict__ rec, const VT *__restrict__ r,
+                    VT *__restrict__ pv, const VT *__restrict__ v,
+                    VT *__restrict__ z, const KScalars *__restrict__ sc,
+                    int *__restrict__ err) {
+  if (sc && sc->done) return;
+  extern __shared__ __align__(128) uint8_t smem[];
+  __shared__ __align__(8) uint64_t bar[3];
+  const StreamMeta m = meta[blockIdx.x];
+  const int lane = threadIdx.x;
+  const int nr = m.nr, nlev = m.nlev;
+  const int KL = KLT > 0 ? KLT : m.KL, KU = KUT > 0 ? KUT : m.KU;
+  uint8_t *hdr = smem;
+  uint8_t *const buf0 = smem + m.hdr_bytes;  // buffer b at buf0 + b*max_piece
+  VT *zs = reinterpret_cast<VT *>(smem + m.hdr_bytes + 2 * m.max_piece);
+  const uint8_t *g = rec + m.rec_off;
+  if (lane == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init(&bar[2], 1);
+    mbar_expect_tx(&bar[2], (uint32_t)m.hdr_bytes);
+    bulk_load(hdr, g, (uint32_t)m.hdr_bytes, &bar[2]);
+  }
+  for (int i = lane; i < nr; i += 32)
+    zs[i] = pre_input<VT>(MODE, m.r0 + i, r, pv, v, sc);
+  if (lane == 0) zs[nr] = (VT)0;
+  __syncwarp();
+  if (!mbar_wait_bounded(&bar[2], err)) return;
+  const uint16_t *lvl = reinterpret_cast<const uint16_t *>(hdr);
+  const int32_t *ints =
+      reinterpret_cast<const int32_t *>(hdr + ((2 * (nlev + 2) + 3) & ~3));
+  const int nF = ints[0], nB = ints[1], P = nF + nB;
+  const int32_t *tab = ints + 2;
+  if (lane == 0)
+    for (int j = 0; j < 2 && j < P; ++j) {
+      mbar_expect_tx(&bar[j], (uint32_t)tab[3 * j + 2]);
+      bulk_load(buf0 + j * m.max_piece, g + tab[3 * j + 1],
+                (uint32_t)tab[3 * j + 2], &bar[j]);
+    }
+  constexpr int vs = (int)sizeof(MT);
+  uint32_t phases = 0u;  // bit b: parity to wait for on buffer b
+  for (int j = 0; j < P; ++j) {
+    const int sb = j & 1;
+    if (!mbar_wait_bounded(&bar[sb], err, (phases >> sb) & 1u)) {
+      // a load in flight in the other buffer: wait for it (bounded), leave
+      if (j + 1 < P)
+        mbar_wait_bounded(&bar[sb ^ 1], nullptr, (phases >> (sb ^ 1)) & 1u);
+      return;
+    }
+    phases ^= 1u << sb;
+    const uint8_t *pc = buf0 + sb * m.max_piece;
+    if (j < nF) {
+      const int l1 = j + 1 < nF ? tab[3 * (j + 1)] : nlev;
+      int a = lvl[tab[3 * j]];
+      for (int l = tab[3 * j]; l < l1; ++l) {
+        const int b = lvl[l + 1], w = b - a;
+        const int ca = al16(2 * KL * w);
+        sweep_level<VT, MT, KLT>(zs, a, w, KL,
+                                 reinterpret_cast<const uint16_t *>(pc),
+                                 reinterpret_cast<const MT *>(pc + ca),
+                                 (const MT *)nullptr, lane);
+        pc += ca + al16(vs * KL * w);
+        a = b;
+        __syncwarp();
+      }
+    } else {
+      const int lhi = tab[3 * j];
+      const int llo = j + 1 < P ? tab[3 * (j + 1)] + 1 : 0;
+      int b = lvl[lhi + 1];
+      for (int l = lhi; l >= llo; --l) {
+        const int a = lvl[l], w = b - a;
+        const int ca = al16(2 * KU * w), va = al16(vs * KU * w);
+        sweep_level<VT, MT, KUT>(zs, a, w, KU,
+                                 reinterpret_cast<const uint16_t *>(pc),
+                                 reinterpret_cast<const MT *>(pc + ca),
+                                 reinterpret_cast<const MT *>(pc + ca + va),
+                                 lane);
+        pc += ca + va + al16(vs * w);
+        b = a;
+        __syncwarp();
+      }
+    }
+    if (lane == 0 && j + 2 < P) {
+      // the generic-proxy reads of this buffer are ordered before the
+      // async-proxy refill
+      fence_proxy_async();
+      mbar_expect_tx(&bar[sb], (uint32_t)tab[3 * (j + 2) + 2]);
+      bulk_load(buf0 + sb * m.max_piece, g + tab[3 * (j + 2) + 1],
+                (uint32_t)tab[3 * (j + 2) + 2], &bar[sb]);
+    }
+  }
+  for (int i = lane; i < nr; i += 32) z[m.r0 + i] = zs[i];
+}
+
+// Step-form sweeps (kernels.cuh StepMeta) for rows with at most 3 L/U
+// entries: per step each lane loads one 8-byte index word and one 4-wide
+// value vector, so a level costs a handful of instructions and the critical
+// path is the z loads, three FMAs and the store.  Pieces of kStepsPerPiece
+// steps are double-buffered through shared memory by TMA as above.
+template <class MT> struct Vec4;
+template <> struct Vec4<float> { using T = float4; };
+template <> struct Vec4<double> { using T = double4; };
+
+template <class VT, class MT, int MODE>
+__global__ void __launch_bounds__(32)
+k_ilu0_apply_steps(const StepMeta *__restrict__ meta,
+                   const uint8_t *__restrict__ rec, const VT *__restrict__ r,
+                   VT *__restrict__ pv, const VT *__restrict__ v,
+                   VT *__restrict__ z, const KScalars *__restrict__ sc,
+                   int *__restrict__ err) {
+  if (sc && sc->done) return;
+  constexpr int SB = step_bytes<MT>();
+  constexpr int PB = kStepsPerPiece * SB;
+  extern __shared__ __align__(128) uint8_t smem[];
+  __shared__ __align__(8) uint64_t bar[2];
+  const StepMeta m = meta[blockIdx.x];
+  const int lane = threadIdx.x;
+  const int nr = m.nr, nf = m.n_fwd, S = m.n_fwd + m.n_bwd;
+  const int P = (S + kStepsPerPiece - 1) / kStepsPerPiece;
+  uint8_t *const buf0 = smem;  // buffer b at buf0 + b*PB
+  VT *zs = reinterpret_cast<VT *>(smem + 2 * PB);
+  const uint8_t *g = rec + m.rec_off;
+  auto piece_bytes = [&](int j) {
+    const int n = S - j * kStepsPerPiece;
+    return (uint32_t)((n < kStepsPerPiece ? n : kStepsPerPiece) * SB);
+  };
+  if (lane == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    for (int j = 0; j < 2 && j < P; ++j) {
+      mbar_expect_tx(&bar[j], piece_bytes(j));
+      bulk_load(buf0 + j * PB, g + (size_t)j * PB, piece_bytes(j), &bar[j]);
+    }
+  }
+  for (int i = lane; i < nr; i += 32)
+    zs[i] = pre_input<VT>(MODE, m.r0 + i, r, pv, v, sc);
+  if (lane == 0) zs[nr] = (VT)0;
+  __syncwarp();
+  using V4 = typename Vec4<MT>::T;
+  const uint8_t *zb = reinterpret_cast<const uint8_t *>(zs);
+  uint8_t *zw = reinterpret_cast<uint8_t *>(zs);
+  // one step: z[row] = (z[row] - w0 z[c0] - w1 z[c1] - w2 z[c2]) (* 1/u_ii)
+  auto step = [&](const uint4 &e, const V4 &w, bool bwd) {
+    VT acc = *reinterpret_cast<const VT *>(zb + e.x);
+    acc -= (VT)w.x * *reinterpret_cast<const VT *>(zb + e.y);
+    acc -= (VT)w.y * *reinterpret_cast<const VT *>(zb + e.z);
+    acc -= (VT)w.z * *reinterpret_cast<const VT *>(zb + e.w);
+    if (bwd) acc *= (VT)w.w;
+    *reinterpret_cast<VT *>(zw + e.x) = acc;
+    __syncwarp();
+  };
+  uint32_t phases = 0u;
+  int q = 0;  // global step index
+  for (int j = 0; j < P; ++j) {
+    const int sb = j & 1;
+    if (!mbar_wait_bounded(&bar[sb], err, (phases >> sb) & 1u)) {
+      if (j + 1 < P)
+        mbar_wait_bounded(&bar[sb ^ 1], nullptr, (phases >> (sb ^ 1)) & 1u);
+      return;
+    }
+    phases ^= 1u << sb;
+    const uint8_t *pc = buf0 + sb * PB;
+    const int ns = (S - q) < kStepsPerPiece ? (S - q) : kStepsPerPiece;
+    // index/value words of a whole piece are independent of z: load them
+    // up front, two steps per unrolled iteration
+    auto E = [&](int k) { return reinterpret_cast<const uint4 *>(pc + k * SB)[lane]; };
+    auto W = [&](int k) { return reinterpret_cast<const V4 *>(pc + k * SB + 512)[lane]; };
+    int k = 0;
+    for (; k + 1 < ns; k += 2, q += 2) {
+      const uint4 e0 = E(k), e1 = E(k + 1);
+      const V4 w0 = W(k), w1 = W(k + 1);
+      step(e0, w0, q >= nf);
+      step(e1, w1, q + 1 >= nf);
+    }
+    if (k < ns) {
+      step(E(k), W(k), q >= nf);
+      ++q;
+    }
+    if (lane == 0 && j + 2 < P) {
+      fence_proxy_async();
+      mbar_expect_tx(&bar[sb], piece_bytes(j + 2));
+      bulk_load(buf0 + sb * PB, g + (size_t)(j + 2) * PB, piece_bytes(j + 2),
+                &bar[sb]);
+    }
+  }
+  for (int i = lane; i < nr; i += 32) z[m.r0 + i] = zs[i];
+}
+
+// Sweeps with the factor records and the vector in global memory, one CTA
+// per subdomain, for subdomains too large for the shared-memory forms (one
+// global subdomain on a big system) -- slow, but it needs no staging.
+template <class VT, class MT, int MODE>
+__global__ void k_ilu0_apply_global(const SubMeta *__restrict__ meta,
+                                    const uint8_t *__restrict__ rec,
+                                    const VT *__restrict__ r,
+                                    VT *__restrict__ pv,
+                                    const VT *__restrict__ v,
+                                    VT *__restrict__ z,
+                                    const KScalars *__restrict__ sc) {
+  if (sc && sc->done) return;
+  const SubMeta m = meta[blockIdx.x];
+  const uint8_t *base = rec + m.rec_off;
+  const uint16_t *lvl = reinterpret_cast<const uint16_t *>(base);
+  const uint16_t *cols = reinterpret_cast<const uint16_t *>(base + m.col_off);
+  const MT *vals = reinterpret_cast<const MT *>(base + m.val_off);
+  VT *zs = z + m.r0;
+  const int K = m.K, KL = m.KL, nr = m.nr;
+  for (int i = threadIdx.x; i < nr; i += blockDim.x)
+    zs[i] = pre_input<VT>(MODE, m.r0 + i, r, pv, v, sc);
+  __syncthreads();
+  for (int lv = 0; lv < m.nlev; ++lv) {
+    const int a = lvl[lv], b = lvl[lv + 1];
+    for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
+      VT acc = zs[i];
+      for (int k = 0; k < KL; ++k) {
+        const int c = cols[(size_t)k * nr + i];
+        if (c != kPadCol) acc -= (VT)vals[(size_t)k * nr + i] * zs[c];
+      }
+      zs[i] = acc;
+    }
+    __syncthreads();
+  }
+  for (int lv = m.nlev - 1; lv >= 0; --lv) {
+    const int a = lvl[lv], b = lvl[lv + 1];
+    for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
+      VT acc = zs[i];
+      for (int k = KL; k < K; ++k) {
+        const int c = cols[(size_t)k * nr + i];
+        if (c != kPadCol) acc -= (VT)vals[(size_t)k * nr + i] * zs[c];
+      }
+      zs[i] = acc * (VT)vals[(size_t)K * nr + i];
+    }
+    __syncthreads();
+  }
+}
+
+// Packs the FP64 factor into a streaming record (FP64 or FP32 values).
+template <class MT>
+__global__ void k_pack_stream(int n, const int32_t *__restrict__ src,
+                              const int32_t *__restrict__ dst,
+                              const double *__restrict__ factor,
+                              MT *__restrict__ out) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += gridDim.x * blockDim.x)
+    out[dst[e]] = (MT)factor[src[e]];
+}
+
+template <class VT, class MT, int MODE, int KLT, int KUT>
+void launch_stream(const SolverDev &d, size_t smem, const VT *r, VT *pv,
+                   const VT *v, VT *z, const KScalars *sc, cudaStream_t st) {
+  const bool fp64 = sizeof(MT) == 8;
+  static size_t attr = 0;
+  if (smem > 48 * 1024 && attr < smem) {
+    cudaFuncSetAttribute(k_ilu0_apply_stream<VT, MT, MODE, KLT, KUT>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    attr = smem;
+  }
+  k_ilu0_apply_stream<VT, MT, MODE, KLT, KUT><<<d.n_sub, 32, smem, st>>>(
+      fp64 ? d.smeta64 : d.smeta32, fp64 ? d.srec64 : d.srec32, r, pv, v, z, sc,
+      d.err);
+}
+
+template <class VT, class MT, int MODE>
+void apply_mode(const SolverDev &d, const VT *r, VT *pv, const VT *v, VT *z,
+                const KScalars *sc, cudaStream_t st) {
+  const bool fp64 = sizeof(MT) == 8;
+  const size_t smem = fp64 ? d.smem64 : d.smem32;
+  // compile-time slot counts for the common stencils: quadrilaterals (2/2,
+  // any subdomain whose rows have at most 2 L and 2 U entries) and
+  // triangles (3/3); padding slots make smaller rows fit
+  if (smem && d.use_steps && !fp64) {
+    static size_t attr = 0;
+    if (smem > 48 * 1024 && attr < smem) {
+      cudaFuncSetAttribute(k_ilu0_apply_steps<VT, MT, MODE>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem);
+      attr = smem;
+    }
+    k_ilu0_apply_steps<VT, MT, MODE><<<d.n_sub, 32, smem, st>>>(
+        d.tmeta32, d.srec32, r, pv, v, z, sc, d.err);
+  } else if (smem && d.max_kl <= 2 && d.max_ku <= 2)
+    launch_stream<VT, MT, MODE, 2, 2>(d, smem, r, pv, v, z, sc, st);
+  else if (smem && d.max_kl <= 3 && d.max_ku <= 3)
+    launch_stream<VT, MT, MODE, 3, 3>(d, smem, r, pv, v, z, sc, st);
+  else if (smem)
+    launch_stream<VT, MT, MODE, 0, 0>(d, smem, r, pv, v, z, sc, st);
+  else
+    k_ilu0_apply_global<VT, MT, MODE><<<d.n_sub, 1024, 0, st>>>(
+        fp64 ? d.meta64 : d.meta32, fp64 ? d.rec64 : d.rec32, r, pv, v, z, sc);
+  count_launches(1);
+}
+
+}  // namespace
+
+void launch_ilu0_factor(const SolverDev &d, const double *pvals, int *bad,
+                        bool to_fp32, cudaStream_t st) {
+  k_ilu0_factor<<<d.n_sub, 32, 0, st>>>(d.meta64, d.rec64, d.rec_src, pvals,
+                                        bad);
+  count_launches(1);
+  if (to_fp32 && !d.smem32) {  // FP32 copy for the global-memory sweep
+    k_factor_to_fp32<<<d.n_sub, 256, 0, st>>>(d.meta64, d.rec64, d.meta32,
+                                              d.rec32);
+    count_launches(1);
+  }
+  auto grid = [](int n) { return (n + 255) / 256 < 2432 ? (n + 255) / 256 : 2432; };
+  if (d.n_pack > 0 && d.smem64) {
+    k_pack_stream<double><<<grid(d.n_pack), 256, 0, st>>>(
+        d.n_pack, d.pack_src, d.pack_dst64,
+        reinterpret_cast<const double *>(d.rec64),
+        reinterpret_cast<double *>(d.srec64));
+    count_launches(1);
+  }
+  if (to_fp32 && d.n_pack32 > 0 && d.smem32) {
+    k_pack_stream<float><<<grid(d.n_pack32), 256, 0, st>>>(
+        d.n_pack32, d.pack_src32, d.pack_dst32,
+        reinterpret_cast<const double *>(d.rec64),
+        reinterpret_cast<float *>(d.srec32));
+    count_launches(1);
+  }
+}
+
+template <class VT, class MT>
+void launch_ilu0_apply(int mode, const SolverDev &d, const VT *r, VT *pv,
+                       const VT *v, VT *z, const KScalars *sc,
+                       cudaStream_t st) {
+  if (mode == 0) apply_mode<VT, MT, 0>(d, r, pv, v, z, sc, st);
+  else if (mode == 1) apply_mode<VT, MT, 1>(d, r, pv, v, z, sc, st);
+  else apply_mode<VT, MT, 2>(d, r, pv, v, z, sc, st);
+}
+
+template <class VT, class MT>
+void launch_precond(int precond, int mode, const SolverDev &d,
+                    const MT *jdinv, const VT *r, VT *pv, const VT *v, VT *z,
+                    const KScalars *sc, cudaStream_t st) {
+  if (precond == PG_PREC_ILU0)
+    launch_ilu0_apply<VT, MT>(mode, d, r, pv, v, z, sc, st);
+  else
+    launch_diag_apply<VT, MT>(mode, d, precond == PG_PREC_JACOBI ? jdinv : nullptr,
+                              r, pv, v, z, sc, st);
+}
+
+template void launch_precond<double, double>(int, int, const SolverDev &,
+                                             const double *, const double *,
+                                             double *, const double *,
+                                             double *, const KScalars *,
+                                             cudaStream_t);
+template void launch_precond<float, float>(int, int, const SolverDev &,
+                                           const float *, const float *,
+                                           float *, const float *, float *,
+                                           const KScalars *, cudaStream_t);
+
+}  // namespace pg

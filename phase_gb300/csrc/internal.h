@@ -177,7 +177,21 @@ struct Analysis {
   std::vector<uint8_t> rec64, rec32;
   std::vector<int32_t> rec_src;            // value slot -> permuted entry
   size_t smem64 = 0, smem32 = 0;           // max record + vector bytes
+  int max_kl = 0, max_ku = 0;              // widest L / U part of a row
+  // streaming records for the apply kernel (kernels.cuh StreamMeta)
+  std::vector<StreamMeta> smeta64, smeta32;
+  std::vector<uint8_t> srec64, srec32;
+  std::vector<int32_t> pack_src, pack_dst64;    // FP64 stream <- factor
+  std::vector<int32_t> pack_src32, pack_dst32;  // FP32 stream <- factor
+  size_t ssmem64 = 0, ssmem32 = 0;
+  // step stream (kernels.cuh StepMeta) replacing the FP32 level-blob stream
+  // when every row has at most 3 L and 3 U entries (in srec32/pack_*32)
+  bool use_steps = false;
+  std::vector<StepMeta> tmeta32;
 };
+
+// target bytes of one streamed piece of a subdomain's factor
+constexpr int64_t kStreamPiece = 6144;
 
 int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
             int subdomain_rows, Analysis &a);

@@ -264,257 +264,6 @@ __global__ void k_unpermute_vec(int n, const int32_t *__restrict__ perm,
   if (i < n) dst[perm[i]] = src[i];
 }
 
-// ------------------------------------------------------------- ILU(0)
-// Row-wise IKJ ILU(0) (Saad, Iterative Methods for Sparse Linear Systems,
-// Alg. 10.4) on the diagonal block of one subdomain, in its packed record.
-// The CTA walks the level schedule; rows of one level depend only on rows of
-// earlier levels, which the barrier has completed.  Pivots are FP64; the
-// diagonal slot ends up holding 1/u_ii.
-__global__ void k_ilu0_factor(const SubMeta *__restrict__ meta,
-                              uint8_t *__restrict__ rec,
-                              const int32_t *__restrict__ rec_src,
-                              const double *__restrict__ pvals,
-                              int *__restrict__ bad) {
-  const SubMeta m = meta[blockIdx.x];
-  uint8_t *base = rec + m.rec_off;
-  const uint16_t *lvl = reinterpret_cast<const uint16_t *>(base);
-  const uint16_t *cols = reinterpret_cast<const uint16_t *>(base + m.col_off);
-  double *vals = reinterpret_cast<double *>(base + m.val_off);
-  const int K = m.K, KL = m.KL, K1 = K + 1;
-  const int n_slots = m.nr * K1;
-  for (int j = threadIdx.x; j < n_slots; j += blockDim.x) {
-    const int src = rec_src[m.slot_base + j];
-    vals[j] = src >= 0 ? pvals[src] : 0.;
-  }
-  __syncthreads();
-  for (int lv = 0; lv < m.nlev; ++lv) {
-    const int a = lvl[lv], b = lvl[lv + 1];
-    for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
-      double *wi = vals + (size_t)i * K1;
-      const uint16_t *ci = cols + (size_t)i * K;
-      for (int k = 0; k < KL; ++k) {
-        const int c = ci[k];
-        if (c == kPadCol) break;
-        const double lik = wi[k] / vals[(size_t)c * K1 + K];
-        wi[k] = lik;
-        // a_ij -= l_ik u_kj for the columns j of U(k) present in row i
-        const uint16_t *cc = cols + (size_t)c * K + KL;
-        const double *wc = vals + (size_t)c * K1 + KL;
-        for (int q = 0; q < K - KL; ++q) {
-          const int cu = cc[q];
-          if (cu == kPadCol) break;
-          const double d = lik * wc[q];
-          if (cu == i) {
-            wi[K] -= d;
-            continue;
-          }
-          for (int k2 = 0; k2 < K; ++k2)
-            if (ci[k2] == cu) {
-              wi[k2] -= d;
-              break;
-            }
-        }
-      }
-    }
-    __syncthreads();
-  }
-  for (int i = threadIdx.x; i < m.nr; i += blockDim.x) {
-    const double piv = vals[(size_t)i * K1 + K];
-    if (piv == 0. || !isfinite(piv)) {
-      atomicAdd(bad, 1);
-      vals[(size_t)i * K1 + K] = 0.;
-    } else {
-      vals[(size_t)i * K1 + K] = 1. / piv;
-    }
-  }
-}
-
-// FP32 copy of the factor values (the FP32 records' static parts are set up
-// once on the host).
-__global__ void k_factor_to_fp32(const SubMeta *__restrict__ m64,
-                                 const uint8_t *__restrict__ rec64,
-                                 const SubMeta *__restrict__ m32,
-                                 uint8_t *__restrict__ rec32) {
-  const SubMeta a = m64[blockIdx.x], b = m32[blockIdx.x];
-  const double *src = reinterpret_cast<const double *>(rec64 + a.rec_off + a.val_off);
-  float *dst = reinterpret_cast<float *>(rec32 + b.rec_off + b.val_off);
-  const int n = a.nr * (a.K + 1);
-  for (int j = threadIdx.x; j < n; j += blockDim.x) dst[j] = (float)src[j];
-}
-
-template <class VT>
-__device__ __forceinline__ VT pre_input(int mode, int i, const VT *r, VT *pv,
-                                        const VT *v, const KScalars *sc) {
-  if (mode == 1) {
-    const VT val = (VT)((double)r[i] + sc->beta * ((double)pv[i] - sc->omega * (double)v[i]));
-    pv[i] = val;
-    return val;
-  } else if (mode == 2) {
-    const VT val = (VT)((double)r[i] - sc->alpha * (double)v[i]);
-    pv[i] = val;
-    return val;
-  }
-  return pv[i];
-}
-
-// ---- TMA / mbarrier helpers (sm_90+ PTX) ----
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(count)
-               : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
-                   smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_load(void *dst, const void *src,
-                                          uint32_t bytes, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
-      "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], "
-      "%2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-constexpr int kWaitLimit = 1 << 22;  // try_wait polls before giving up
-
-// Bounded wait on a single-use barrier.  On expiry the error flag is set and
-// the copy still in flight is waited for once more (bounded) so the CTA does
-// not exit under it.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, int *err) {
-  for (int it = 0; it < kWaitLimit; ++it)
-    if (mbar_try_wait(bar, 0)) return true;
-  if (err) atomicExch(err, 1);
-  for (int it = 0; it < kWaitLimit; ++it)
-    if (mbar_try_wait(bar, 0)) break;
-  return false;
-}
-
-// Forward/backward sweeps of one subdomain by one warp.  The record is moved
-// into shared memory by one cp.async.bulk (TMA) while the lanes compute the
-// fused input vector; the level loop then runs entirely out of shared
-// memory with __syncwarp between levels.
-template <class VT, class MT, int MODE>
-__global__ void __launch_bounds__(32)
-k_ilu0_apply_tma(const SubMeta *__restrict__ meta,
-                 const uint8_t *__restrict__ rec, const VT *__restrict__ r,
-                 VT *__restrict__ pv, const VT *__restrict__ v,
-                 VT *__restrict__ z, const KScalars *__restrict__ sc,
-                 int *__restrict__ err) {
-  if (sc && sc->done) return;
-  extern __shared__ __align__(128) uint8_t smem[];
-  __shared__ __align__(8) uint64_t bar;
-  const SubMeta m = meta[blockIdx.x];
-  const int lane = threadIdx.x;
-  uint8_t *rs = smem;
-  VT *zs = reinterpret_cast<VT *>(smem + ((m.rec_bytes + 15) & ~15));
-  if (lane == 0) {
-    mbar_init(&bar, 1);
-    mbar_expect_tx(&bar, (uint32_t)m.rec_bytes);
-    bulk_load(rs, rec + m.rec_off, (uint32_t)m.rec_bytes, &bar);
-  }
-  for (int i = lane; i < m.nr; i += 32)
-    zs[i] = pre_input<VT>(MODE, m.r0 + i, r, pv, v, sc);
-  __syncwarp();
-  if (!mbar_wait_bounded(&bar, err)) return;
-  const uint16_t *lvl = reinterpret_cast<const uint16_t *>(rs);
-  const uint16_t *cols = reinterpret_cast<const uint16_t *>(rs + m.col_off);
-  const MT *vals = reinterpret_cast<const MT *>(rs + m.val_off);
-  const int K = m.K, KL = m.KL, K1 = K + 1;
-  for (int lv = 0; lv < m.nlev; ++lv) {
-    const int a = lvl[lv], b = lvl[lv + 1];
-    for (int i = a + lane; i < b; i += 32) {
-      const uint16_t *ci = cols + i * K;
-      const MT *wi = vals + i * K1;
-      VT acc = zs[i];
-      for (int k = 0; k < KL; ++k) {
-        const int c = ci[k];
-        if (c != kPadCol) acc -= (VT)wi[k] * zs[c];
-      }
-      zs[i] = acc;
-    }
-    __syncwarp();
-  }
-  for (int lv = m.nlev - 1; lv >= 0; --lv) {
-    const int a = lvl[lv], b = lvl[lv + 1];
-    for (int i = a + lane; i < b; i += 32) {
-      const uint16_t *ci = cols + i * K;
-      const MT *wi = vals + i * K1;
-      VT acc = zs[i];
-      for (int k = KL; k < K; ++k) {
-        const int c = ci[k];
-        if (c != kPadCol) acc -= (VT)wi[k] * zs[c];
-      }
-      zs[i] = acc * (VT)wi[K];
-    }
-    __syncwarp();
-  }
-  for (int i = lane; i < m.nr; i += 32) z[m.r0 + i] = zs[i];
-}
-
-// Same sweeps with the record and the vector in global memory, one CTA per
-// subdomain, for subdomains whose record exceeds shared memory (one global
-// subdomain).
-template <class VT, class MT, int MODE>
-__global__ void k_ilu0_apply_global(const SubMeta *__restrict__ meta,
-                                    const uint8_t *__restrict__ rec,
-                                    const VT *__restrict__ r,
-                                    VT *__restrict__ pv,
-                                    const VT *__restrict__ v,
-                                    VT *__restrict__ z,
-                                    const KScalars *__restrict__ sc) {
-  if (sc && sc->done) return;
-  const SubMeta m = meta[blockIdx.x];
-  const uint8_t *base = rec + m.rec_off;
-  const uint16_t *lvl = reinterpret_cast<const uint16_t *>(base);
-  const uint16_t *cols = reinterpret_cast<const uint16_t *>(base + m.col_off);
-  const MT *vals = reinterpret_cast<const MT *>(base + m.val_off);
-  VT *zs = z + m.r0;
-  const int K = m.K, KL = m.KL, K1 = K + 1;
-  for (int i = threadIdx.x; i < m.nr; i += blockDim.x)
-    zs[i] = pre_input<VT>(MODE, m.r0 + i, r, pv, v, sc);
-  __syncthreads();
-  for (int lv = 0; lv < m.nlev; ++lv) {
-    const int a = lvl[lv], b = lvl[lv + 1];
-    for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
-      VT acc = zs[i];
-      for (int k = 0; k < KL; ++k) {
-        const int c = cols[(size_t)i * K + k];
-        if (c != kPadCol) acc -= (VT)vals[(size_t)i * K1 + k] * zs[c];
-      }
-      zs[i] = acc;
-    }
-    __syncthreads();
-  }
-  for (int lv = m.nlev - 1; lv >= 0; --lv) {
-    const int a = lvl[lv], b = lvl[lv + 1];
-    for (int i = a + threadIdx.x; i < b; i += blockDim.x) {
-      VT acc = zs[i];
-      for (int k = KL; k < K; ++k) {
-        const int c = cols[(size_t)i * K + k];
-        if (c != kPadCol) acc -= (VT)vals[(size_t)i * K1 + k] * zs[c];
-      }
-      zs[i] = acc * (VT)vals[(size_t)i * K1 + K];
-    }
-    __syncthreads();
-  }
-}
-
 // Jacobi / identity preconditioner with the same fused updates.
 template <class VT, class MT, int MODE>
 __global__ void k_diag_apply(int n, const MT *__restrict__ dinv,
@@ -646,11 +395,12 @@ k_update(int n, VT *__restrict__ x, VT *__restrict__ r,
          const VT *__restrict__ rh, KScalars *sc, RedWork w) {
   if (sc->done) return;
   const double al = sc->alpha, om = sc->omega;
+  const VT alv = (VT)al, omv = (VT)om;  // vector math in storage precision
   double acc[2] = {0., 0.};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += gridDim.x * blockDim.x) {
-    x[i] = (VT)((double)x[i] + al * (double)ph[i] + om * (double)sh[i]);
-    const VT ri = (VT)((double)s[i] - om * (double)t[i]);
+    x[i] = x[i] + alv * ph[i] + omv * sh[i];
+    const VT ri = s[i] - omv * t[i];
     r[i] = ri;
     acc[0] += (double)rh[i] * (double)ri;
     acc[1] += (double)ri * (double)ri;
@@ -785,68 +535,6 @@ void launch_unpermute_vec(int n, const int32_t *perm, const double *src,
   count_launches(1);
 }
 
-void launch_ilu0_factor(const SolverDev &d, const double *pvals, int *bad,
-                        bool to_fp32, cudaStream_t st) {
-  const int threads = d.smem64 ? 32 : 1024;
-  k_ilu0_factor<<<d.n_sub, threads, 0, st>>>(d.meta64, d.rec64, d.rec_src,
-                                             pvals, bad);
-  count_launches(1);
-  if (to_fp32) {
-    k_factor_to_fp32<<<d.n_sub, 256, 0, st>>>(d.meta64, d.rec64, d.meta32,
-                                              d.rec32);
-    count_launches(1);
-  }
-}
-
-template <class VT, class MT, int MODE>
-static void apply_ilu(const SolverDev &d, const VT *r, VT *pv, const VT *v,
-                      VT *z, const KScalars *sc, cudaStream_t st) {
-  const bool fp64 = sizeof(MT) == 8;
-  const SubMeta *meta = fp64 ? d.meta64 : d.meta32;
-  const uint8_t *rec = fp64 ? d.rec64 : d.rec32;
-  const size_t smem = fp64 ? d.smem64 : d.smem32;
-  if (smem) {
-    static size_t attr = 0;
-    if (smem > 48 * 1024 && attr < smem) {
-      cudaFuncSetAttribute(k_ilu0_apply_tma<VT, MT, MODE>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem);
-      attr = smem;
-    }
-    k_ilu0_apply_tma<VT, MT, MODE><<<d.n_sub, 32, smem, st>>>(meta, rec, r, pv,
-                                                              v, z, sc, d.err);
-    count_launches(1);
-  } else {
-    k_ilu0_apply_global<VT, MT, MODE><<<d.n_sub, 1024, 0, st>>>(meta, rec, r,
-                                                               pv, v, z, sc);
-    count_launches(1);
-  }
-}
-
-template <class VT, class MT>
-void launch_precond(int precond, int mode, const SolverDev &d,
-                    const MT *jdinv, const VT *r, VT *pv, const VT *v, VT *z,
-                    const KScalars *sc, cudaStream_t st) {
-  if (precond == PG_PREC_ILU0) {
-    if (mode == 0) apply_ilu<VT, MT, 0>(d, r, pv, v, z, sc, st);
-    else if (mode == 1) apply_ilu<VT, MT, 1>(d, r, pv, v, z, sc, st);
-    else apply_ilu<VT, MT, 2>(d, r, pv, v, z, sc, st);
-  } else {
-    const MT *di = precond == PG_PREC_JACOBI ? jdinv : nullptr;
-    const int g = blocks_for(d.n, 256) < 1216 ? blocks_for(d.n, 256) : 1216;
-    if (mode == 0) {
-      k_diag_apply<VT, MT, 0><<<g, 256, 0, st>>>(d.n, di, r, pv, v, z, sc);
-      count_launches(1);
-    } else if (mode == 1) {
-      k_diag_apply<VT, MT, 1><<<g, 256, 0, st>>>(d.n, di, r, pv, v, z, sc);
-      count_launches(1);
-    } else {
-      k_diag_apply<VT, MT, 2><<<g, 256, 0, st>>>(d.n, di, r, pv, v, z, sc);
-      count_launches(1);
-    }
-  }
-}
-
 template <class VT, class MT>
 void launch_krylov_init(const SolverDev &d, const MT *val, const VT *b,
                         const VT *x, VT *r, VT *rh, VT *p, VT *v, KScalars *sc,
@@ -887,11 +575,24 @@ void launch_jacobi_diag(const SolverDev &d, const double *pvals, double *dinv,
   count_launches(1);
 }
 
+template <class VT, class MT>
+void launch_diag_apply(int mode, const SolverDev &d, const MT *dinv,
+                       const VT *r, VT *pv, const VT *v, VT *z,
+                       const KScalars *sc, cudaStream_t st) {
+  const int g = blocks_for(d.n, 256) < 1216 ? blocks_for(d.n, 256) : 1216;
+  if (mode == 0)
+    k_diag_apply<VT, MT, 0><<<g, 256, 0, st>>>(d.n, dinv, r, pv, v, z, sc);
+  else if (mode == 1)
+    k_diag_apply<VT, MT, 1><<<g, 256, 0, st>>>(d.n, dinv, r, pv, v, z, sc);
+  else
+    k_diag_apply<VT, MT, 2><<<g, 256, 0, st>>>(d.n, dinv, r, pv, v, z, sc);
+  count_launches(1);
+}
+
 #define PG_INST(VT, MT)                                                       \
-  template void launch_precond<VT, MT>(int, int, const SolverDev &,           \
-                                       const MT *, const VT *, VT *,          \
-                                       const VT *, VT *, const KScalars *,    \
-                                       cudaStream_t);                         \
+  template void launch_diag_apply<VT, MT>(int, const SolverDev &, const MT *, \
+                                          const VT *, VT *, const VT *, VT *, \
+                                          const KScalars *, cudaStream_t);    \
   template void launch_krylov_init<VT, MT>(const SolverDev &, const MT *,     \
                                            const VT *, const VT *, VT *,      \
                                            VT *, VT *, VT *, KScalars *,      \

@@ -71,15 +71,47 @@ void launch_gradient(int n_cells, int nf, const int32_t *fl,
 // ---- solver kernels ----
 // One Schwarz subdomain's ILU(0) factor is a packed record, 16-byte aligned
 // so one cp.async.bulk moves it into shared memory:
-//   uint16 lvl[nlev+1]   level boundaries (subdomain-local rows)
-//   uint16 cols[nr][K]   K = KL + KU slots: L columns then U columns,
-//                        0xFFFF marks an unused slot
-//   MT     vals[nr][K+1] L multipliers, U values, 1/u_ii
+//   uint16 lvl[nlev+2]   level boundaries (subdomain-local rows) + sentinel
+//   uint16 cols[K][nr]   slot-major; K = KL + KU slots: L columns then U
+//                        columns, 0xFFFF marks an unused slot
+//   MT     vals[K+1][nr] slot-major L multipliers, U values, then 1/u_ii
 struct SubMeta {
   int32_t r0, nr, nlev, K, KL, rec_off, col_off, val_off, rec_bytes,
       slot_base, pad0, pad1;
 };
 constexpr uint16_t kPadCol = 0xFFFF;
+
+// Streaming form of a subdomain's factor for the apply kernel: the levels'
+// L data (ascending) and U data + 1/u_ii (descending) are cut into
+// level-aligned pieces that TMA double-buffers through shared memory.
+//   header: uint16 lvl[nlev+2] (4-byte padded), int32 nF, nB,
+//           int32 table[nF+nB][3] = {level, byte offset, bytes}
+//           (forward pieces start at `level`; backward pieces start at
+//           `level` and run downwards)
+//   level blob (forward):  uint16 cols[KL][w] | MT vals[KL][w]
+//   level blob (backward): uint16 cols[KU][w] | MT vals[KU][w] | MT dinv[w]
+//   every array padded to 16 bytes; w = rows of the level; an unused slot
+//   has column nr (the kernel keeps z[nr] = 0) and value 0
+struct StreamMeta {
+  int32_t r0, nr, nlev, KL, KU, rec_off, hdr_bytes, max_piece;
+};
+
+// Step form of the streams, used when every row has at most 3 L and 3 U
+// entries (quadrilateral and triangle meshes).  A step is one warp-wide
+// slice of a level (up to 32 rows):
+//   uint32 idx[32][4]  byte offsets into the subdomain's z vector of
+//                      {row, c0, c1, c2}  (unused: row/col = nr, z[nr] = 0)
+//   MT     val[32][4]  {w0, w1, w2, 1/u_ii}
+// Forward steps (L parts, levels ascending) come first, then backward steps
+// (U parts and 1/u_ii, levels descending); pieces are kStepsPerPiece steps.
+// Used for the FP32 sweep.
+struct StepMeta {
+  int32_t r0, nr, n_fwd, n_bwd, rec_off, pad0, pad1, pad2;
+};
+constexpr int kStepsPerPiece = 8;
+template <class MT> __host__ __device__ constexpr int step_bytes() {
+  return 32 * 16 + 32 * 4 * (int)sizeof(MT);
+}
 
 struct SolverDev {
   int n, nnz, n_sub;
@@ -90,6 +122,15 @@ struct SolverDev {
   uint8_t *rec64, *rec32;
   const int32_t *rec_src;
   size_t smem64, smem32;  // dynamic smem of the staged apply (0 = too big)
+  int max_kl, max_ku;     // widest L / U part of any row
+  // streaming records and the factor -> stream value maps
+  const StreamMeta *smeta64, *smeta32;
+  uint8_t *srec64, *srec32;
+  const int32_t *pack_src, *pack_dst64, *pack_src32, *pack_dst32;
+  int n_pack, n_pack32;
+  // FP32 step stream (when use_steps)
+  int use_steps;
+  const StepMeta *tmeta32;
   int *err;               // set when a bounded device wait runs out
 };
 
@@ -101,8 +142,9 @@ void launch_permute_vec(int n, const int32_t *perm, const double *src,
 void launch_unpermute_vec(int n, const int32_t *perm, const double *src,
                           double *dst, cudaStream_t st);
 
-// ILU(0) numeric factorisation into the FP64 records (and the FP32 copy
-// when to_fp32); bad counts zero or non-finite pivots.
+// ILU(0) numeric factorisation into the FP64 factor records, then packed
+// into the streaming records (FP64, and FP32 when to_fp32); bad counts zero
+// or non-finite pivots.
 void launch_ilu0_factor(const SolverDev &d, const double *pvals, int *bad,
                         bool to_fp32, cudaStream_t st);
 
@@ -136,5 +178,37 @@ void launch_true_residual(const SolverDev &d, const double *val,
 
 void launch_jacobi_diag(const SolverDev &d, const double *pvals, double *dinv,
                         cudaStream_t st);
+
+// ILU(0) application (ilu.cu) for one fused-update mode, and the
+// Jacobi/identity version (kernels.cu).
+template <class VT, class MT>
+void launch_ilu0_apply(int mode, const SolverDev &d, const VT *r, VT *pv,
+                       const VT *v, VT *z, const KScalars *sc,
+                       cudaStream_t st);
+template <class VT, class MT>
+void launch_diag_apply(int mode, const SolverDev &d, const MT *dinv,
+                       const VT *r, VT *pv, const VT *v, VT *z,
+                       const KScalars *sc, cudaStream_t st);
+
+// Input of a preconditioner application with the fused BiCGStab update:
+//   mode 0: z = M^-1 pv
+//   mode 1: p = r + beta (p - omega v), written back to pv
+//   mode 2: s = r - alpha v,            written to pv
+template <class VT>
+__device__ __forceinline__ VT pre_input(int mode, int i, const VT *r, VT *pv,
+                                        const VT *v, const KScalars *sc) {
+  // vector arithmetic in the storage precision; the scalars come from the
+  // FP64 recurrences
+  if (mode == 1) {
+    const VT val = r[i] + (VT)sc->beta * (pv[i] - (VT)sc->omega * v[i]);
+    pv[i] = val;
+    return val;
+  } else if (mode == 2) {
+    const VT val = r[i] - (VT)sc->alpha * v[i];
+    pv[i] = val;
+    return val;
+  }
+  return pv[i];
+}
 
 }  // namespace pg

@@ -34,6 +34,17 @@ __global__ void k_to_float(int64_t n, const double *__restrict__ a,
     b[i] = (float)a[i];
 }
 
+// deterministic non-zero contents for kernel timing
+__global__ void k_fill_profile(int64_t n, double *__restrict__ a,
+                               float *__restrict__ b, int salt) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = 1.0 + 0.25 * sinf(0.001f * (float)(i % 100003) + salt);
+    if (a) a[i] = v;
+    if (b) b[i] = (float)v;
+  }
+}
+
 // outer refinement helpers (FP64 residual, FP32 correction)
 __global__ void k_residual_to_float(int n, const double *__restrict__ r,
                                     float *__restrict__ rf, double scale) {
@@ -62,6 +73,10 @@ struct pg_solver {
   DevBuf<int32_t> perm, prp, pci, psrc, dup_dst, dup_src, rec_src;
   DevBuf<SubMeta> meta64, meta32;
   DevBuf<uint8_t> rec64, rec32;
+  DevBuf<StreamMeta> smeta64, smeta32;
+  DevBuf<StepMeta> tmeta32;
+  DevBuf<uint8_t> srec64, srec32;
+  DevBuf<int32_t> pack_src, pack_dst64, pack_src32, pack_dst32;
   DevBuf<int> err;
   DevBuf<int32_t> raw_rp, raw_ci, st_rp, st_ci;
   DevBuf<double> st_vals, st_vec;
@@ -83,8 +98,21 @@ struct pg_solver {
   bool have_rhs = false, have_x = false, have_vals = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   int red_grid = 1;
+  // CUDA graphs of one chunk of BiCGStab iterations (FP64, FP32); kernel
+  // arguments are fixed device pointers, so a graph stays valid until the
+  // buffers are reallocated by a new analysis
+  cudaGraphExec_t chunk_graph[2] = {nullptr, nullptr};
+
+  void drop_graphs() {
+    for (auto &g : chunk_graph)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+  }
 
   ~pg_solver() {
+    drop_graphs();
     if (sc_host) cudaFreeHost(sc_host);
     if (bad_host) cudaFreeHost(bad_host);
     if (diff_host) cudaFreeHost(diff_host);
@@ -104,10 +132,24 @@ struct pg_solver {
     d.rec64 = rec64.p;
     d.rec32 = rec32.p;
     d.rec_src = rec_src.p;
-    // the staged (TMA) apply needs the largest record + vector in shared
-    // memory; otherwise the global-memory sweep is used
-    d.smem64 = a.smem64 <= kMaxApplySmem ? a.smem64 : 0;
-    d.smem32 = a.smem32 <= kMaxApplySmem ? a.smem32 : 0;
+    // the streamed (TMA) apply needs header + 2 pieces + the subdomain's
+    // vector in shared memory; otherwise the global-memory sweep is used
+    d.smem64 = a.ssmem64 <= kMaxApplySmem ? a.ssmem64 : 0;
+    d.smem32 = a.ssmem32 <= kMaxApplySmem ? a.ssmem32 : 0;
+    d.smeta64 = smeta64.p;
+    d.smeta32 = smeta32.p;
+    d.srec64 = srec64.p;
+    d.srec32 = srec32.p;
+    d.pack_src = pack_src.p;
+    d.pack_dst64 = pack_dst64.p;
+    d.pack_src32 = pack_src32.p;
+    d.pack_dst32 = pack_dst32.p;
+    d.n_pack = (int)a.pack_src.size();
+    d.n_pack32 = (int)a.pack_src32.size();
+    d.use_steps = a.use_steps ? 1 : 0;
+    d.tmeta32 = tmeta32.p;
+    d.max_kl = a.max_kl;
+    d.max_ku = a.max_ku;
     d.err = err.p;
     return d;
   }
@@ -133,6 +175,15 @@ int upload_analysis(pg_solver *s) {
   up(s->meta32, a.meta32);
   up(s->rec64, a.rec64);
   up(s->rec32, a.rec32);
+  up(s->smeta64, a.smeta64);
+  up(s->tmeta32, a.tmeta32);
+  up(s->smeta32, a.smeta32);
+  up(s->srec64, a.srec64);
+  up(s->srec32, a.srec32);
+  up(s->pack_src, a.pack_src);
+  up(s->pack_dst64, a.pack_dst64);
+  up(s->pack_src32, a.pack_src32);
+  up(s->pack_dst32, a.pack_dst32);
   if (e == cudaSuccess) e = s->err.zero(1);
   const size_t n = a.n, nnz = a.nnz;
   for (DevBuf<double> *bf : {&s->b, &s->x, &s->r, &s->rh, &s->p, &s->v,
@@ -147,6 +198,7 @@ int upload_analysis(pg_solver *s) {
       if (e == cudaSuccess) e = bf->reserve(n);
     if (e == cudaSuccess) e = s->pvals32.reserve(nnz);
   }
+  s->drop_graphs();
   s->red_grid = (int)std::min<int64_t>(1216, (n + kVecBlock - 1) / kVecBlock);
   if (s->red_grid < 1) s->red_grid = 1;
   if (e == cudaSuccess) e = s->partials.reserve((size_t)kMaxDots * s->red_grid);
@@ -191,19 +243,44 @@ int run_bicgstab(pg_solver *s, const MT *val, const MT *jdinv, VT *b, VT *x,
   PG_CUDA(cudaMemcpyAsync(s->sc.p, s->sc_host, sizeof(KScalars),
                           cudaMemcpyHostToDevice, st));
   int n_restart = 0;
+  // one chunk = kChunk BiCGStab iterations, 5 kernels each; after the first
+  // (direct) chunk the chunk is captured once into a CUDA graph and replayed
+  constexpr int kChunk = 8;
+  auto chunk = [&]() {
+    for (int c = 0; c < kChunk; ++c) {
+      launch_precond<VT, MT>(s->cfg.precond, 1, d, jdinv, r, p, v, ph,
+                             s->sc.p, st);
+      launch_spmv_v<VT, MT>(d, val, ph, v, rh, s->sc.p, w, st);
+      launch_precond<VT, MT>(s->cfg.precond, 2, d, jdinv, r, ss, v, sh,
+                             s->sc.p, st);
+      launch_spmv_t<VT, MT>(d, val, sh, t, ss, s->sc.p, w, st);
+      launch_update<VT>(d.n, x, r, ph, sh, ss, t, rh, s->sc.p, w, st);
+    }
+  };
+  cudaGraphExec_t &gexec = s->chunk_graph[sizeof(VT) == 8 ? 0 : 1];
+  int chunks_run = 0;
   for (;;) {
     launch_krylov_init<VT, MT>(d, val, b, x, r, rh, p, v, s->sc.p, w, st);
     for (;;) {
-      const int chunk = 8;
-      for (int c = 0; c < chunk; ++c) {
-        launch_precond<VT, MT>(s->cfg.precond, 1, d, jdinv, r, p, v, ph,
-                               s->sc.p, st);
-        launch_spmv_v<VT, MT>(d, val, ph, v, rh, s->sc.p, w, st);
-        launch_precond<VT, MT>(s->cfg.precond, 2, d, jdinv, r, ss, v, sh,
-                               s->sc.p, st);
-        launch_spmv_t<VT, MT>(d, val, sh, t, ss, s->sc.p, w, st);
-        launch_update<VT>(d.n, x, r, ph, sh, ss, t, rh, s->sc.p, w, st);
+      if (gexec) {
+        PG_CUDA(cudaGraphLaunch(gexec, st));
+        count_launches(5 * kChunk);
+      } else if (chunks_run > 0) {
+        cudaGraph_t graph = nullptr;
+        PG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+        const uint64_t before = launch_count();
+        chunk();
+        const uint64_t captured = launch_count() - before;
+        PG_CUDA(cudaStreamEndCapture(st, &graph));
+        cudaError_t ge = cudaGraphInstantiate(&gexec, graph, 0);
+        cudaGraphDestroy(graph);
+        PG_CUDA(ge);
+        PG_CUDA(cudaGraphLaunch(gexec, st));
+        (void)captured;  // counted when captured, executed once here
+      } else {
+        chunk();
       }
+      ++chunks_run;
       PG_CUDA(cudaGetLastError());
       PG_CUDA(cudaMemcpyAsync(s->sc_host, s->sc.p, sizeof(KScalars),
                               cudaMemcpyDeviceToHost, st));
@@ -590,11 +667,20 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
   const SolverDev d = s->dev();
   const RedWork w = s->red();
   const int64_t n = s->a.n;
-  DevBuf<double> xs, rs;
-  PG_CUDA(xs.reserve(n));
-  PG_CUDA(rs.reserve(n));
-  PG_CUDA(cudaMemcpyAsync(xs.p, s->x.p, n * 8, cudaMemcpyDeviceToDevice, st));
-  PG_CUDA(cudaMemcpyAsync(rs.p, s->r.p, n * 8, cudaMemcpyDeviceToDevice, st));
+  const int g = grid_for(n);
+  const bool mixed = s->cfg.precision == PG_MIXED;
+  // scratch vectors with benign non-zero contents, so no kernel takes its
+  // breakdown/convergence exit; the solver's own state is left untouched
+  DevBuf<double> d8[8];
+  DevBuf<float> f4[8];
+  for (int k = 0; k < 8; ++k) {
+    PG_CUDA(d8[k].reserve(n));
+    k_fill_profile<<<g, 256, 0, st>>>(n, d8[k].p, nullptr, k);
+    if (mixed) {
+      PG_CUDA(f4[k].reserve(n));
+      k_fill_profile<<<g, 256, 0, st>>>(n, nullptr, f4[k].p, k);
+    }
+  }
   KScalars k{};
   k.max_iter = 1 << 30;
   k.alpha = k.omega = k.beta = k.rho = 1.0;
@@ -614,13 +700,18 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
     *out = (double)t / reps;
     return PG_OK;
   };
-  int rc = timed([&] { launch_spmv_v<double, double>(d, s->pvals.p, s->ph.p, s->v.p, s->rh.p, s->sc.p, w, st); }, &ms[0]);
-  if (!rc) rc = timed([&] { launch_precond<double, double>(s->cfg.precond, 1, d, s->jdinv.p, s->r.p, s->p.p, s->v.p, s->ph.p, s->sc.p, st); }, &ms[1]);
-  if (!rc) rc = timed([&] { launch_update<double>(d.n, xs.p, rs.p, s->ph.p, s->sh.p, s->s.p, s->t.p, s->rh.p, s->sc.p, w, st); }, &ms[2]);
+  for (int i = 0; i < 8; ++i) ms[i] = 0.;
+  // vectors: 0 ph/sh, 1 v/t, 2 rh, 3 r, 4 p/s, 5 x, 6 z
+  int rc = timed([&] { launch_spmv_v<double, double>(d, s->pvals.p, d8[0].p, d8[1].p, d8[2].p, s->sc.p, w, st); }, &ms[0]);
+  if (!rc) rc = timed([&] { launch_precond<double, double>(s->cfg.precond, 1, d, s->jdinv.p, d8[3].p, d8[4].p, d8[1].p, d8[6].p, s->sc.p, st); }, &ms[1]);
+  if (!rc) rc = timed([&] { launch_update<double>(d.n, d8[5].p, d8[3].p, d8[0].p, d8[6].p, d8[4].p, d8[1].p, d8[2].p, s->sc.p, w, st); }, &ms[2]);
   if (!rc && s->cfg.precond == PG_PREC_ILU0)
-    rc = timed([&] { launch_ilu0_factor(d, s->pvals.p, s->bad.p, false, st); }, &ms[3]);
-  else if (!rc)
-    ms[3] = 0.;
+    rc = timed([&] { launch_ilu0_factor(d, s->pvals.p, s->bad.p, mixed, st); }, &ms[3]);
+  if (!rc && mixed) {
+    rc = timed([&] { launch_spmv_v<float, float>(d, s->pvals32.p, f4[0].p, f4[1].p, f4[2].p, s->sc.p, w, st); }, &ms[4]);
+    if (!rc) rc = timed([&] { launch_precond<float, float>(s->cfg.precond, 1, d, s->jdinv32.p, f4[3].p, f4[4].p, f4[1].p, f4[6].p, s->sc.p, st); }, &ms[5]);
+    if (!rc) rc = timed([&] { launch_update<float>(d.n, f4[5].p, f4[3].p, f4[0].p, f4[6].p, f4[4].p, f4[1].p, f4[2].p, s->sc.p, w, st); }, &ms[6]);
+  }
   PG_CUDA(cudaStreamSynchronize(st));
   return rc;
 }
