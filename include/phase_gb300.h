@@ -119,6 +119,32 @@ int pg_assemble_laplacian(pg_eqn *e, const double *gamma_face,
 int pg_eqn_export(const pg_eqn *e, int32_t *row_ptr, int32_t *col_ind,
                   double *vals, double *rhs);
 
+/* Momentum operator of the vector equation, assembled on the device:
+ *   fv::ddt(u, dt) + fv::div(u_face, u, theta) - fv::laplacian(nu, u, theta)
+ * (TimeDerivative.h:38-48, Divergence.h:8-53, Laplacian.h:7-47) -- the
+ * predictor whose diagonal a_P gives the SIMPLE coefficient d = V/a_P.  Both
+ * velocity components share one N x N coefficient matrix (the reference
+ * stacks them as rows 0..N-1 and N..2N-1 with equal coefficients,
+ * VectorFiniteVolumeEquation.cpp:5-30); rows hold the diagonal first, then
+ * the neighbours in link order.  Explicit zero coefficients are kept (the
+ * reference's CrsEquation::operator+= drops them; the values agree).
+ * bc_type[n_faces] (host) as for pg_eqn_create; the equation's rhs holds
+ * 2*N values (x then y).  u_old_cell[2*N] (x,y per cell), u_face[2*n_faces]
+ * (the face velocities of the fluxes; on FIXED faces the boundary values). */
+int pg_eqn_create_momentum(const pg_mesh *m, const int32_t *bc_type,
+                           pg_eqn **out);
+int pg_assemble_momentum(pg_eqn *e, double dt, double nu, double theta,
+                         const double *u_old_cell, const double *u_face,
+                         int ptr_kind);
+
+/* FiniteVolumeField::interpolateFaces(DISTANCE) followed by setBoundaryFaces
+ * for a normal-gradient field (FiniteVolumeField.tpp:130-183, Face.cpp:60-64):
+ * face value g*phi_l + (1-g)*phi_r with the distance weight g, boundary faces
+ * take the owner cell's value.  cell_vals[n_cells] in, face_vals[n_faces]
+ * out. */
+int pg_interpolate_faces(const pg_mesh *m, const double *cell_vals,
+                         double *face_vals, int ptr_kind);
+
 /* Face coefficient timeStep / rho_f with rho_f = rho1 + clamp(gamma_f,0,1)
  * (rho2 - rho1) and gamma_f the distance-weighted face interpolation of the
  * cell volume fraction (FractionalStepMultiphase.cpp:175-185,

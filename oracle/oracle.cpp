@@ -863,3 +863,125 @@ extern "C" void or_spmv(int64_t n, const int32_t *row_ptr,
   Csr A{n, row_ptr, col_ind, vals};
   spmv(A, x, y);
 }
+
+// ---------------------------------------------------------------------------
+// Momentum operator (config: lid-driven cavity SIMPLE predictor)
+
+namespace {
+// CrsEquation::operator+= / -= (CrsEquation.cpp:185-229, 231-275): rebuild
+// each row from the entries of the left side that are non-zero and not
+// placeholders, then add the right side's non-zero entries (summing into an
+// existing column or appending).
+static void crs_plus(or_eqn &a, const or_eqn &b, double sign) {
+  for (size_t r = 0; r < a.rows.size(); ++r) {
+    std::vector<std::pair<int32_t, double>> out;
+    for (auto &e : a.rows[r])
+      if (e.second != 0. && e.first >= 0) out.push_back(e);
+    for (auto &e : b.rows[r]) {
+      if (e.second == 0. || e.first < 0) continue;
+      bool found = false;
+      for (auto &o : out)
+        if (o.first == e.first) {
+          o.second += sign * e.second;
+          found = true;
+          break;
+        }
+      if (!found) out.push_back({e.first, sign * e.second});
+    }
+    a.rows[r] = std::move(out);
+    a.rhs[r] += sign * b.rhs[r];
+  }
+}
+}  // namespace
+
+extern "C" or_eqn *or_momentum(const or_mesh *m, double dt, double nu,
+                               double theta, const double *u0,
+                               const double *uf, const int32_t *bc_type) {
+  const int64_t n = (int64_t)m->centroid.size();
+  auto fresh = [&]() {
+    auto *e = new or_eqn();
+    e->rows.assign(2 * n, std::vector<std::pair<int32_t, double>>(5, {-1, 0.}));
+    e->rhs.assign(2 * n, 0.);
+    return e;
+  };
+  // add to both components (FiniteVolumeEquation<Vector2D>::add, :17-30)
+  auto add2 = [&](or_eqn &e, int32_t c, int32_t col, double v) {
+    add_coeff(e, c, col, v);
+    add_coeff(e, (int32_t)(n + c), (int32_t)(n + col), v);
+  };
+  // fv::ddt(field, dt) (TimeDerivative.h:38-48)
+  or_eqn *ddt = fresh();
+  for (int32_t c = 0; c < (int32_t)n; ++c) {
+    const double v = m->volume[c];
+    add2(*ddt, c, c, v / dt);
+    ddt->rhs[c] += -v * u0[2 * c] / dt;
+    ddt->rhs[n + c] += -v * u0[2 * c + 1] / dt;
+  }
+  // fv::div(u, phi, theta) (Divergence.h:8-53), old-time terms use u0 = u
+  or_eqn *div = fresh();
+  for (int32_t c = 0; c < (int32_t)n; ++c) {
+    const V2 pc = m->centroid[c];
+    for (auto &l : m->nb[c]) {
+      const int32_t f = l.first, nbc = l.second;
+      const V2 sf = outward_norm(*m, f, pc);
+      const double flux = uf[2 * f] * sf.x + uf[2 * f + 1] * sf.y;
+      add2(*div, c, c, theta * std::max(flux, 0.));
+      add2(*div, c, nbc, theta * std::min(flux, 0.));
+      const double f0 = flux;  // old flux: same face velocity
+      div->rhs[c] += (1. - theta) * std::max(f0, 0.) * u0[2 * c];
+      div->rhs[n + c] += (1. - theta) * std::max(f0, 0.) * u0[2 * c + 1];
+      div->rhs[c] += (1. - theta) * std::min(f0, 0.) * u0[2 * nbc];
+      div->rhs[n + c] += (1. - theta) * std::min(f0, 0.) * u0[2 * nbc + 1];
+    }
+    for (int32_t f : m->bd[c]) {
+      const V2 sf = outward_norm(*m, f, pc);
+      const double flux = uf[2 * f] * sf.x + uf[2 * f + 1] * sf.y;
+      switch (bc_type[f]) {
+      case OR_FIXED:
+        div->rhs[c] += theta * flux * uf[2 * f];
+        div->rhs[n + c] += theta * flux * uf[2 * f + 1];
+        div->rhs[c] += (1. - theta) * flux * uf[2 * f];
+        div->rhs[n + c] += (1. - theta) * flux * uf[2 * f + 1];
+        break;
+      case OR_NORMAL_GRADIENT:
+        add2(*div, c, c, theta * flux);
+        div->rhs[c] += (1. - theta) * flux * u0[2 * c];
+        div->rhs[n + c] += (1. - theta) * flux * u0[2 * c + 1];
+        break;
+      default:
+        break;
+      }
+    }
+  }
+  // fv::laplacian(gamma, phi, theta) (Laplacian.h:7-47), scalar gamma
+  or_eqn *lap = fresh();
+  for (int32_t c = 0; c < (int32_t)n; ++c) {
+    const V2 pc = m->centroid[c];
+    for (auto &l : m->nb[c]) {
+      const int32_t f = l.first, nbc = l.second;
+      const V2 rc = sub(m->centroid[nbc], pc);
+      const double coeff = nu * dot(rc, outward_norm(*m, f, pc)) / mag_sqr(rc);
+      add2(*lap, c, nbc, theta * coeff);
+      add2(*lap, c, c, theta * -coeff);
+      lap->rhs[c] += (1. - theta) * coeff * (u0[2 * nbc] - u0[2 * c]);
+      lap->rhs[n + c] += (1. - theta) * coeff * (u0[2 * nbc + 1] - u0[2 * c + 1]);
+    }
+    for (int32_t f : m->bd[c]) {
+      const V2 rf = sub(m->fc[f], pc);
+      const double coeff = nu * dot(rf, outward_norm(*m, f, pc)) / mag_sqr(rf);
+      if (bc_type[f] == OR_FIXED) {
+        add2(*lap, c, c, theta * -coeff);
+        lap->rhs[c] += theta * coeff * uf[2 * f];
+        lap->rhs[n + c] += theta * coeff * uf[2 * f + 1];
+        lap->rhs[c] += (1. - theta) * coeff * (uf[2 * f] - u0[2 * c]);
+        lap->rhs[n + c] += (1. - theta) * coeff * (uf[2 * f + 1] - u0[2 * c + 1]);
+      }
+    }
+  }
+  // ddt + div == laplacian  ->  (ddt += div) -= laplacian
+  crs_plus(*ddt, *div, 1.);
+  crs_plus(*ddt, *lap, -1.);
+  delete div;
+  delete lap;
+  return ddt;
+}

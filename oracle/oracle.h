@@ -142,6 +142,18 @@ void or_ilu0_apply(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
                    const double *lu_vals, const int32_t *part,
                    const double *r, double *z);
 
+/* Momentum operator of the vector equation
+ *   fv::ddt(u, dt) + fv::div(uf, u, theta) - fv::laplacian(nu, u, theta)
+ * (TimeDerivative.h:38-48, Divergence.h:8-53, Laplacian.h:7-47) combined
+ * with CrsEquation::operator+= / -= (CrsEquation.cpp:185-275, which drop
+ * zero and placeholder entries).  Rows 0..N-1 are the x component, N..2N-1
+ * the y component (VectorFiniteVolumeEquation.cpp:5-30); both share the
+ * coefficients.  u_old_cell[2N] (x,y per cell), u_face[2F] face velocity
+ * for the fluxes and for FIXED boundary values, bc_type per face.  Returns
+ * the equation (2N rows) for or_eqn_sizes / or_eqn_export_csr. */
+or_eqn *or_momentum(const or_mesh *m, double dt, double nu, double theta,
+                    const double *u_old_cell, const double *u_face,
+                    const int32_t *bc_type);
 /* y = A x */
 void or_spmv(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
              const double *vals, const double *x, double *y);

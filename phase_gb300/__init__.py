@@ -72,6 +72,9 @@ PROTOTYPES = {
     "pg_mesh_faces": (_I, [_P, _P, _P, _P, _P, _P, _P]),
     "pg_mesh_cells": (_I, [_P, _P, _P, _P]),
     "pg_eqn_create": (_I, [_P, _I, _P, ctypes.POINTER(_P)]),
+    "pg_eqn_create_momentum": (_I, [_P, _P, ctypes.POINTER(_P)]),
+    "pg_assemble_momentum": (_I, [_P, _D, _D, _D, _P, _P, _I]),
+    "pg_interpolate_faces": (_I, [_P, _P, _P, _I]),
     "pg_eqn_destroy": (_I, [_P]),
     "pg_eqn_sizes": (_I, [_P, _P, _P]),
     "pg_assemble_laplacian": (_I, [_P, _P, _D, _P, _P, _I]),
@@ -192,6 +195,12 @@ class Mesh:
                                    _ptr(out["vol"])))
         return out
 
+    def interpolate_faces(self, cell_vals):
+        c = _f64(cell_vals, self.n_cells)
+        out = np.empty(self.n_faces)
+        _check(lib().pg_interpolate_faces(self._h, _ptr(c), _ptr(out), PG_HOST))
+        return out
+
     def dt_over_rho(self, gamma_cell, rho1, rho2, dt):
         g = _f64(gamma_cell, self.n_cells)
         out = np.empty(self.n_faces)
@@ -253,6 +262,43 @@ class Equation:
         ci = np.empty(self.nnz, np.int32)
         v = np.empty(self.nnz)
         rhs = np.empty(self.n)
+        _check(lib().pg_eqn_export(self._h, _ptr(rp), _ptr(ci), _ptr(v),
+                                   _ptr(rhs)))
+        return rp, ci, v, rhs
+
+
+class MomentumEquation:
+    """Device momentum operator ddt + div - laplacian(nu) of the vector
+    equation: one N x N matrix shared by both components, rhs[2N]."""
+
+    def __init__(self, mesh: Mesh, bc_type):
+        self.mesh = mesh
+        bc = _i32(bc_type, mesh.n_faces)
+        h = _P()
+        _check(lib().pg_eqn_create_momentum(mesh._h, _ptr(bc), ctypes.byref(h)))
+        self._h = h
+        s = np.zeros(2, np.int64)
+        _check(lib().pg_eqn_sizes(h, _ptr(s[0:1]), _ptr(s[1:2])))
+        self.n, self.nnz = int(s[0]), int(s[1])
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.pg_eqn_destroy(h)
+            self._h = None
+
+    def assemble(self, dt, nu, theta, u_old_cell, u_face):
+        u0 = _f64(u_old_cell, 2 * self.mesh.n_cells)
+        uf = _f64(u_face, 2 * self.mesh.n_faces)
+        _check(lib().pg_assemble_momentum(self._h, dt, nu, theta, _ptr(u0),
+                                          _ptr(uf), PG_HOST))
+        return self
+
+    def export(self):
+        rp = np.empty(self.n + 1, np.int32)
+        ci = np.empty(self.nnz, np.int32)
+        v = np.empty(self.nnz)
+        rhs = np.empty(2 * self.n)
         _check(lib().pg_eqn_export(self._h, _ptr(rp), _ptr(ci), _ptr(v),
                                    _ptr(rhs)))
         return rp, ci, v, rhs

@@ -220,8 +220,21 @@ static uint64_t next_pattern_id() {
   return ++id;
 }
 
+static int eqn_create(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
+                      bool momentum, pg_eqn **out);
+
 extern "C" int pg_eqn_create(const pg_mesh *m, int gamma_kind,
                              const int32_t *bc_type, pg_eqn **out) {
+  return eqn_create(m, gamma_kind, bc_type, false, out);
+}
+
+extern "C" int pg_eqn_create_momentum(const pg_mesh *m, const int32_t *bc_type,
+                                      pg_eqn **out) {
+  return eqn_create(m, PG_GAMMA_FACE, bc_type, true, out);
+}
+
+static int eqn_create(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
+                      bool momentum, pg_eqn **out) {
   PG_CHECK_ARG(out, "pg_eqn_create: out is NULL");
   *out = nullptr;
   PG_CHECK_ARG(m, "pg_eqn_create: NULL mesh");
@@ -238,7 +251,8 @@ extern "C" int pg_eqn_create(const pg_mesh *m, int gamma_kind,
   e->mesh = m;
   e->gamma_kind = gamma_kind;
   e->bc_type.assign(bc_type, bc_type + h.n_faces);
-  int rc = build_pattern(h, gamma_kind, bc_type, e->p);
+  e->momentum = momentum;
+  int rc = build_pattern(h, gamma_kind, bc_type, e->p, momentum);
   if (rc) {
     delete e;
     return rc;
@@ -283,8 +297,9 @@ extern "C" int pg_eqn_create(const pg_mesh *m, int gamma_kind,
   up(e->csfl_y, sly);
   up(e->csfr_x, srx);
   up(e->csfr_y, sry);
+  up(e->diag, p.diag);
   if (ce == cudaSuccess) ce = e->vals.zero(p.nnz);
-  if (ce == cudaSuccess) ce = e->rhs.zero(p.n);
+  if (ce == cudaSuccess) ce = e->rhs.zero(momentum ? 2 * p.n : p.n);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream());
   if (ce != cudaSuccess) {
     delete e;
@@ -311,6 +326,7 @@ extern "C" int pg_assemble_laplacian(pg_eqn *e, const double *gamma_face,
                                      const double *bc_value,
                                      const double *u_face_xy, int ptr_kind) {
   PG_CHECK_ARG(e, "pg_assemble_laplacian: NULL equation");
+  PG_CHECK_ARG(!e->momentum, "pg_assemble_laplacian: momentum equation");
   PG_CHECK_ARG((gamma_face != nullptr) == (e->gamma_kind == PG_GAMMA_FACE),
                "pg_assemble_laplacian: gamma_face must be given exactly for "
                "a PG_GAMMA_FACE equation");
@@ -357,12 +373,74 @@ extern "C" int pg_eqn_export(const pg_eqn *e, int32_t *row_ptr,
   if (row_ptr) std::copy(e->p.row_ptr.begin(), e->p.row_ptr.end(), row_ptr);
   if (col_ind) std::copy(e->p.col_ind.begin(), e->p.col_ind.end(), col_ind);
   if (vals) PG_CUDA(copy_out(vals, e->vals.p, e->p.nnz * sizeof(double), PG_HOST));
-  if (rhs) PG_CUDA(copy_out(rhs, e->rhs.p, e->p.n * sizeof(double), PG_HOST));
+  if (rhs)
+    PG_CUDA(copy_out(rhs, e->rhs.p,
+                     (e->momentum ? 2 : 1) * e->p.n * sizeof(double), PG_HOST));
   PG_CUDA(cudaStreamSynchronize(stream()));
   return PG_OK;
 }
 
+extern "C" int pg_assemble_momentum(pg_eqn *e, double dt, double nu,
+                                    double theta, const double *u_old_cell,
+                                    const double *u_face, int ptr_kind) {
+  PG_CHECK_ARG(e && e->momentum, "pg_assemble_momentum: not a momentum equation");
+  PG_CHECK_ARG(u_old_cell && u_face, "pg_assemble_momentum: NULL velocity");
+  PG_CHECK_ARG(dt > 0., "pg_assemble_momentum: dt must be positive");
+  const HostMesh &h = e->mesh->h;
+  const double *u0 = nullptr, *uf = nullptr;
+  int rc = stage(u_old_cell, 2 * h.n_cells, ptr_kind, e->stage_a, &u0);
+  if (!rc) rc = stage(u_face, 2 * h.n_faces, ptr_kind, e->stage_c, &uf);
+  if (rc) return rc;
+  cudaStream_t st = stream();
+  const int n = (int)e->p.n;
+  PG_CUDA(cudaMemsetAsync(e->vals.p, 0, e->p.nnz * sizeof(double), st));
+  launch_momentum_init(n, e->diag.p, e->mesh->d.vol.p, dt, u0, e->vals.p,
+                       e->rhs.p, st);
+  const auto &cp = e->p.color_ptr;
+  const int nic = e->p.n_interior_colors;
+  for (int c = 0; c + 1 < (int)cp.size(); ++c) {
+    const int off = cp[c], cnt = cp[c + 1] - cp[c];
+    if (c < nic)
+      launch_momentum_interior(cnt, off, e->cface.p, e->cl.p, e->cr.p,
+                               e->cdot_l.p, e->cdot_r.p, e->cmsq.p,
+                               e->slot_lr.p, e->slot_rl.p, e->diag_l.p,
+                               e->diag_r.p, e->csfl_x.p, e->csfl_y.p,
+                               e->csfr_x.p, e->csfr_y.p, nu, theta, u0, uf, n,
+                               e->vals.p, e->rhs.p, st);
+    else
+      launch_momentum_boundary(cnt, off, e->cface.p, e->cl.p, e->cbc.p,
+                               e->cdot_l.p, e->cmsq.p, e->diag_l.p,
+                               e->csfl_x.p, e->csfl_y.p, nu, theta, u0, uf, n,
+                               e->vals.p, e->rhs.p, st);
+  }
+  PG_CUDA(cudaGetLastError());
+  ++e->version;
+  return PG_OK;
+}
+
 // ------------------------------------------------------------ field ops
+extern "C" int pg_interpolate_faces(const pg_mesh *m, const double *cell_vals,
+                                    double *face_vals, int ptr_kind) {
+  PG_CHECK_ARG(m && cell_vals && face_vals, "pg_interpolate_faces: NULL arg");
+  const HostMesh &h = m->h;
+  DevBuf<double> gin, gout;
+  const double *c = nullptr;
+  int rc = stage(cell_vals, h.n_cells, ptr_kind, gin, &c);
+  if (rc) return rc;
+  double *o = face_vals;
+  if (ptr_kind != PG_DEVICE) {
+    PG_CUDA(gout.reserve(h.n_faces));
+    o = gout.p;
+  }
+  launch_interp_faces((int)h.n_faces, m->d.fl.p, m->d.fr.p, m->d.fcx.p,
+                      m->d.fcy.p, m->d.cx.p, m->d.cy.p, c, o, stream());
+  PG_CUDA(cudaGetLastError());
+  if (ptr_kind != PG_DEVICE)
+    PG_CUDA(copy_out(face_vals, o, h.n_faces * sizeof(double), PG_HOST));
+  PG_CUDA(cudaStreamSynchronize(stream()));
+  return PG_OK;
+}
+
 extern "C" int pg_face_dt_over_rho(const pg_mesh *m, const double *gamma_cell,
                                    double rho1, double rho2, double dt,
                                    double *coeff_face, int ptr_kind) {

@@ -148,7 +148,7 @@ int build_host_mesh(const double *nodes_xy, int64_t n_nodes,
 // diagonal first (:139-142); FIXED boundary links add the diagonal
 // (:66-69, :150-153).  Placeholders that stay empty are dropped.
 int build_pattern(const HostMesh &m, int gamma_kind, const int32_t *bc_type,
-                  EqnPattern &p) {
+                  EqnPattern &p, bool diag_first) {
   const int64_t n = m.n_cells;
   p.n = n;
   p.row_ptr.assign(n + 1, 0);
@@ -168,6 +168,7 @@ int build_pattern(const HostMesh &m, int gamma_kind, const int32_t *bc_type,
   };
   for (int64_t c = 0; c < n; ++c) {
     row.clear();
+    if (diag_first) add((int32_t)c);  // fv::ddt's diagonal comes first
     const int64_t b = m.link_ptr[c], e = m.link_ptr[c + 1];
     const int64_t base = (int64_t)p.col_ind.size();
     for (int64_t k = b; k < e; ++k) {

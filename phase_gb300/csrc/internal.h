@@ -129,7 +129,7 @@ struct EqnPattern {
 };
 
 int build_pattern(const HostMesh &m, int gamma_kind, const int32_t *bc_type,
-                  EqnPattern &p);
+                  EqnPattern &p, bool diag_first = false);
 
 }  // namespace pg
 
@@ -147,6 +147,8 @@ struct pg_eqn {
   pg::DevBuf<double> stage_a, stage_b, stage_c;  // host-input staging
   uint64_t version = 0;  // bumps on every assembly
   uint64_t pattern_id = 0;
+  bool momentum = false;   // vector momentum operator: rhs holds 2n values
+  pg::DevBuf<int32_t> diag;  // diagonal position per row
 };
 
 namespace pg {

@@ -155,6 +155,112 @@ __global__ void k_assemble_boundary(
   rhs[l] = acc;
 }
 
+// ---------------------------------------------------- momentum operator
+// ddt + div - laplacian of the vector equation (TimeDerivative.h:38-48,
+// Divergence.h:8-53, Laplacian.h:7-47), coefficients shared by the x and y
+// components, rhs[2n] (x then y).  fv::ddt first: diagonal V/dt, source
+// -V u0/dt; the face colours then add the upwind fluxes and subtract the
+// diffusion terms.
+__global__ void k_momentum_init(int n, const int32_t *__restrict__ diag,
+                                const double *__restrict__ vol, double dt,
+                                const double *__restrict__ u0,
+                                double *__restrict__ vals,
+                                double *__restrict__ rhs) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const double v = vol[c];
+  vals[diag[c]] = v / dt;
+  rhs[c] = -v * u0[2 * c] / dt;
+  rhs[n + c] = -v * u0[2 * c + 1] / dt;
+}
+
+__global__ void k_momentum_interior(
+    int nf, int off, const int32_t *__restrict__ cface,
+    const int32_t *__restrict__ cl, const int32_t *__restrict__ cr,
+    const double *__restrict__ dot_l, const double *__restrict__ dot_r,
+    const double *__restrict__ msq, const int32_t *__restrict__ slot_lr,
+    const int32_t *__restrict__ slot_rl, const int32_t *__restrict__ diag_l,
+    const int32_t *__restrict__ diag_r, const double *__restrict__ sfl_x,
+    const double *__restrict__ sfl_y, const double *__restrict__ sfr_x,
+    const double *__restrict__ sfr_y, double nu, double theta,
+    const double *__restrict__ u0, const double *__restrict__ uf, int n,
+    double *__restrict__ vals, double *__restrict__ rhs) {
+  const int k = off + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= off + nf) return;
+  const int f = cface[k], l = cl[k], r = cr[k];
+  const double ux = uf[2 * f], uy = uf[2 * f + 1];
+  const double m2 = msq[k];
+  // per side: flux F = u_f . Sf_out, diffusion coefficient c
+  const double Fl = ux * sfl_x[k] + uy * sfl_y[k];
+  const double Fr = ux * sfr_x[k] + uy * sfr_y[k];
+  const double cll = nu * dot_l[k] / m2, crr = nu * dot_r[k] / m2;
+  const double om = 1. - theta;
+  vals[diag_l[k]] += theta * fmax(Fl, 0.) + theta * cll;
+  vals[slot_lr[k]] += theta * fmin(Fl, 0.) - theta * cll;
+  vals[diag_r[k]] += theta * fmax(Fr, 0.) + theta * crr;
+  vals[slot_rl[k]] += theta * fmin(Fr, 0.) - theta * crr;
+  if (om != 0.) {
+    for (int d = 0; d < 2; ++d) {
+      const double ul = u0[2 * l + d], ur = u0[2 * r + d];
+      rhs[d * n + l] += om * (fmax(Fl, 0.) * ul + fmin(Fl, 0.) * ur) - om * cll * (ur - ul);
+      rhs[d * n + r] += om * (fmax(Fr, 0.) * ur + fmin(Fr, 0.) * ul) - om * crr * (ul - ur);
+    }
+  }
+}
+
+__global__ void k_momentum_boundary(
+    int nf, int off, const int32_t *__restrict__ cface,
+    const int32_t *__restrict__ cl, const int32_t *__restrict__ bc,
+    const double *__restrict__ dot_l, const double *__restrict__ msq,
+    const int32_t *__restrict__ diag_l, const double *__restrict__ sfl_x,
+    const double *__restrict__ sfl_y, double nu, double theta,
+    const double *__restrict__ u0, const double *__restrict__ uf, int n,
+    double *__restrict__ vals, double *__restrict__ rhs) {
+  const int k = off + blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= off + nf) return;
+  const int f = cface[k], l = cl[k];
+  const double ux = uf[2 * f], uy = uf[2 * f + 1];
+  const double F = ux * sfl_x[k] + uy * sfl_y[k];
+  const double om = 1. - theta;
+  if (bc[k] == PG_BC_FIXED) {
+    const double c = nu * dot_l[k] / msq[k];
+    vals[diag_l[k]] += theta * c;
+    for (int d = 0; d < 2; ++d) {
+      const double ub = uf[2 * f + d];
+      rhs[d * n + l] += theta * F * ub + om * F * ub;            // div
+      rhs[d * n + l] -= theta * c * ub + om * c * (ub - u0[2 * l + d]);  // -lap
+    }
+  } else if (bc[k] == PG_BC_NORMAL_GRADIENT) {
+    vals[diag_l[k]] += theta * F;
+    for (int d = 0; d < 2; ++d) rhs[d * n + l] += om * F * u0[2 * l + d];
+  }
+}
+
+// FiniteVolumeField::interpolateFaces(DISTANCE) + setBoundaryFaces for a
+// normal-gradient field (FiniteVolumeField.tpp:130-183, Face.cpp:60-64)
+__global__ void k_interp_faces(int nf, const int32_t *__restrict__ fl,
+                               const int32_t *__restrict__ fr,
+                               const double *__restrict__ fcx,
+                               const double *__restrict__ fcy,
+                               const double *__restrict__ cx,
+                               const double *__restrict__ cy,
+                               const double *__restrict__ cv,
+                               double *__restrict__ fv) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int l = fl[f], r = fr[f];
+  if (r < 0) {
+    fv[f] = cv[l];
+    return;
+  }
+  const double ax = __dadd_rn(fcx[f], -cx[r]), ay = __dadd_rn(fcy[f], -cy[r]);
+  const double bx = __dadd_rn(fcx[f], -cx[l]), by = __dadd_rn(fcy[f], -cy[l]);
+  const double l1 = __dsqrt_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)));
+  const double l2 = __dsqrt_rn(__dadd_rn(__dmul_rn(bx, bx), __dmul_rn(by, by)));
+  const double w = __ddiv_rn(l1, __dadd_rn(l1, l2));
+  fv[f] = __dadd_rn(__dmul_rn(w, cv[l]), __dmul_rn(__dadd_rn(1., -w), cv[r]));
+}
+
 // dt / rho_f (FractionalStepMultiphase.cpp:175-185 with the distance-weighted
 // face interpolation FiniteVolumeField.tpp:130-162, Face.cpp:60-64)
 __global__ void k_dt_over_rho(int nf, const int32_t *__restrict__ fl,
@@ -480,6 +586,52 @@ void launch_assemble_boundary(int nf, int off, const int32_t *cface,
   k_assemble_boundary<<<blocks_for(nf, 256), 256, 0, st>>>(
       nf, off, cface, cl, bc, dot_l, msq, diag_l, sfl_x, sfl_y, gamma_face,
       gamma_scalar, bc_value, u_face, vals, rhs);
+  count_launches(1);
+}
+
+void launch_momentum_init(int n, const int32_t *diag, const double *vol,
+                          double dt, const double *u0, double *vals,
+                          double *rhs, cudaStream_t st) {
+  k_momentum_init<<<blocks_for(n, 256), 256, 0, st>>>(n, diag, vol, dt, u0,
+                                                      vals, rhs);
+  count_launches(1);
+}
+void launch_momentum_interior(int nf, int off, const int32_t *cface,
+                              const int32_t *cl, const int32_t *cr,
+                              const double *dot_l, const double *dot_r,
+                              const double *msq, const int32_t *slot_lr,
+                              const int32_t *slot_rl, const int32_t *diag_l,
+                              const int32_t *diag_r, const double *sfl_x,
+                              const double *sfl_y, const double *sfr_x,
+                              const double *sfr_y, double nu, double theta,
+                              const double *u0, const double *u_face, int n,
+                              double *vals, double *rhs, cudaStream_t st) {
+  if (nf <= 0) return;
+  k_momentum_interior<<<blocks_for(nf, 256), 256, 0, st>>>(
+      nf, off, cface, cl, cr, dot_l, dot_r, msq, slot_lr, slot_rl, diag_l,
+      diag_r, sfl_x, sfl_y, sfr_x, sfr_y, nu, theta, u0, u_face, n, vals, rhs);
+  count_launches(1);
+}
+void launch_momentum_boundary(int nf, int off, const int32_t *cface,
+                              const int32_t *cl, const int32_t *bc,
+                              const double *dot_l, const double *msq,
+                              const int32_t *diag_l, const double *sfl_x,
+                              const double *sfl_y, double nu, double theta,
+                              const double *u0, const double *u_face, int n,
+                              double *vals, double *rhs, cudaStream_t st) {
+  if (nf <= 0) return;
+  k_momentum_boundary<<<blocks_for(nf, 256), 256, 0, st>>>(
+      nf, off, cface, cl, bc, dot_l, msq, diag_l, sfl_x, sfl_y, nu, theta, u0,
+      u_face, n, vals, rhs);
+  count_launches(1);
+}
+void launch_interp_faces(int nf, const int32_t *fl, const int32_t *fr,
+                         const double *fcx, const double *fcy,
+                         const double *cx, const double *cy,
+                         const double *cell_vals, double *face_vals,
+                         cudaStream_t st) {
+  k_interp_faces<<<blocks_for(nf, 256), 256, 0, st>>>(nf, fl, fr, fcx, fcy, cx,
+                                                      cy, cell_vals, face_vals);
   count_launches(1);
 }
 

@@ -54,6 +54,31 @@ void launch_assemble_boundary(int nf, int off, const int32_t *cface,
                               double gamma_scalar, const double *bc_value,
                               const double *u_face, double *vals, double *rhs,
                               cudaStream_t st);
+void launch_momentum_init(int n, const int32_t *diag, const double *vol,
+                          double dt, const double *u0, double *vals,
+                          double *rhs, cudaStream_t st);
+void launch_momentum_interior(int nf, int off, const int32_t *cface,
+                              const int32_t *cl, const int32_t *cr,
+                              const double *dot_l, const double *dot_r,
+                              const double *msq, const int32_t *slot_lr,
+                              const int32_t *slot_rl, const int32_t *diag_l,
+                              const int32_t *diag_r, const double *sfl_x,
+                              const double *sfl_y, const double *sfr_x,
+                              const double *sfr_y, double nu, double theta,
+                              const double *u0, const double *u_face, int n,
+                              double *vals, double *rhs, cudaStream_t st);
+void launch_momentum_boundary(int nf, int off, const int32_t *cface,
+                              const int32_t *cl, const int32_t *bc,
+                              const double *dot_l, const double *msq,
+                              const int32_t *diag_l, const double *sfl_x,
+                              const double *sfl_y, double nu, double theta,
+                              const double *u0, const double *u_face, int n,
+                              double *vals, double *rhs, cudaStream_t st);
+void launch_interp_faces(int nf, const int32_t *fl, const int32_t *fr,
+                         const double *fcx, const double *fcy,
+                         const double *cx, const double *cy,
+                         const double *cell_vals, double *face_vals,
+                         cudaStream_t st);
 void launch_dt_over_rho(int nf, const int32_t *fl, const int32_t *fr,
                         const double *fcx, const double *fcy, const double *cx,
                         const double *cy, const double *gamma_cell,

@@ -476,6 +476,9 @@ extern "C" int pg_solver_set_csr(pg_solver *s, const int32_t *row_ptr,
 
 extern "C" int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e) {
   PG_CHECK_ARG(s && e, "pg_solver_set_eqn: NULL arg");
+  PG_CHECK_ARG(!e->momentum,
+               "pg_solver_set_eqn: a momentum equation has two right-hand "
+               "sides; use pg_solver_set_csr/set_rhs per component");
   cudaStream_t st = stream();
   if (s->rank != e->p.n) {
     s->rank = e->p.n;

@@ -81,6 +81,8 @@ def lib():
         L.or_ilu0.argtypes = [I64, P, P, P, P, P]
         L.or_ilu0_apply.argtypes = [I64, P, P, P, P, P, P]
         L.or_spmv.argtypes = [I64, P, P, P, P, P]
+        L.or_momentum.restype = P
+        L.or_momentum.argtypes = [P, D, D, D, P, P, P]
         _lib = L
     return _lib
 
@@ -161,6 +163,24 @@ class OracleMesh:
         rhs = np.empty(n)
         (lib().or_eqn_export_slots if slots else lib().or_eqn_export_csr)(
             e, ptr(rp), ptr(ci), ptr(v), ptr(rhs))
+        lib().or_eqn_destroy(e)
+        return rp, ci, v, rhs
+
+    def momentum(self, dt, nu, theta, u_old_cell, u_face, bc_type):
+        """ddt + div - laplacian(nu) of the vector equation: compact CSR of
+        2N rows (x then y) and rhs[2N]."""
+        u0 = np.ascontiguousarray(u_old_cell, np.float64)
+        uf = np.ascontiguousarray(u_face, np.float64)
+        bc = np.ascontiguousarray(bc_type, np.int32)
+        e = lib().or_momentum(self.h, dt, nu, theta, ptr(u0), ptr(uf), ptr(bc))
+        s = np.zeros(3, np.int64)
+        lib().or_eqn_sizes(e, ptr(s[0:1]), ptr(s[1:2]), ptr(s[2:3]))
+        n, ns, nnz = map(int, s)
+        rp = np.empty(n + 1, np.int32)
+        ci = np.empty(nnz, np.int32)
+        v = np.empty(nnz)
+        rhs = np.empty(n)
+        lib().or_eqn_export_csr(e, ptr(rp), ptr(ci), ptr(v), ptr(rhs))
         lib().or_eqn_destroy(e)
         return rp, ci, v, rhs
 

@@ -223,3 +223,26 @@ def test_schwarz_ilu0_blocks_are_independent(oracle):
     rows = np.repeat(np.arange(n), np.diff(rp))
     cross = part[rows] != part[ci]
     assert np.all(lu[cross] == 0.0)
+
+
+def test_momentum_operator_known_answers(oracle):
+    """ddt + div - laplacian(nu): with no flux the x and y blocks equal
+    V/dt I - L(nu) with L the scalar Laplacian (FIXED walls), and the lid
+    value enters the x rhs only."""
+    from phase_gb300 import simple
+    w = simple.cavity_inputs(6, 5)
+    om = oracle.OracleMesh(w["nodes"], w["cptr"], w["cind"])
+    w = simple.cavity_inputs(6, 5, faces=om.faces())
+    n = om.n_cells
+    rp, ci, v, rhs = om.momentum(0.005, 0.01, 1.0, np.zeros((n, 2)),
+                                 w["u_face"], w["bc_u"])
+    A = sp.csr_matrix((v, ci, rp), shape=(2 * n, 2 * n)).toarray()
+    rpl, cil, vl, rhsl = om.laplacian(0.01, w["bc_u"], w["u_face"][:, 0])
+    L = sp.csr_matrix((vl, cil, rpl), shape=(n, n)).toarray()
+    vol = om.cells()["vol"]
+    expect = np.diag(vol / 0.005) - L
+    assert np.allclose(A[:n, :n], expect, rtol=1e-14, atol=1e-14)
+    assert np.allclose(A[n:, n:], expect, rtol=1e-14, atol=1e-14)
+    assert np.all(A[:n, n:] == 0) and np.all(A[n:, :n] == 0)
+    assert np.allclose(rhs[:n], -rhsl, rtol=1e-14, atol=1e-14)
+    assert np.all(rhs[n:] == 0.0) and np.any(rhs[:n] != 0.0)
