@@ -113,6 +113,10 @@ int pg_assemble_laplacian(pg_eqn *e, const double *gamma_face,
                           double gamma_scalar, const double *bc_value,
                           const double *u_face_xy, int ptr_kind);
 
+/* Device addresses of the equation's values (nnz) and rhs_ (n, or 2n for a
+ * momentum equation); valid until the equation is destroyed. */
+int pg_eqn_device_values(const pg_eqn *e, double **vals, double **rhs);
+
 /* Copy the assembled CSR + rhs_ (the equation's own right-hand side; the
  * solver receives -rhs_, FiniteVolumeEquation.tpp:179) to host buffers.
  * row_ptr[n+1], col_ind[nnz], vals[nnz], rhs[n]; any may be NULL. */
@@ -162,6 +166,41 @@ int pg_face_dt_over_rho(const pg_mesh *m, const double *gamma_cell,
 int pg_gradient(const pg_mesh *m, const double *phi_cell,
                 const double *phi_face, double *grad_face, double *grad_cell,
                 int ptr_kind);
+
+/* ------------------------------------------------------------------------
+ * Learned initial guess (no counterpart in the reference, which always
+ * restarts BiCGStab from the previous solution): a 3-layer message-passing
+ * network of width 32 on the matrix graph, BF16 weights and FP32
+ * accumulation, trained on the GPU by its own forward, backward and Adam
+ * kernels on (A, b, x_prev, x*) from solves of earlier steps.  The guess is
+ * x_prev plus the network's correction; callers compare its residual with
+ * the zero guess's and keep the better one.
+ * ---------------------------------------------------------------------- */
+typedef struct pg_mpnn pg_mpnn;
+int pg_mpnn_create(uint64_t seed, pg_mpnn **out);
+int pg_mpnn_destroy(pg_mpnn *net);
+int pg_mpnn_num_params(const pg_mpnn *net);
+/* graph = sparsity pattern of the systems (compact CSR, host arrays) */
+int pg_mpnn_set_graph(pg_mpnn *net, const int32_t *row_ptr,
+                      const int32_t *col_ind, int64_t n);
+/* guess[n] from vals[nnz], b[n], x_prev[n]; *rel_residual (optional)
+ * receives ||b - A guess|| / ||b|| (below 1: better than the zero guess). */
+int pg_mpnn_predict(pg_mpnn *net, const double *vals, const double *b,
+                    const double *x_prev, double *guess, double *rel_residual,
+                    int ptr_kind);
+/* one Adam step on one system; *loss (optional) = the normalised residual +
+ * error loss of this step's forward pass */
+int pg_mpnn_train_step(pg_mpnn *net, const double *vals, const double *b,
+                       const double *x_prev, const double *x_star, float lr,
+                       int ptr_kind, double *loss);
+/* forward + backward only: the loss gradient with respect to the
+ * parameters (pg_mpnn_num_params floats, host) and the loss */
+int pg_mpnn_gradient(pg_mpnn *net, const double *vals, const double *b,
+                     const double *x_prev, const double *x_star, int ptr_kind,
+                     float *grad, double *loss);
+/* FP32 master parameters (pg_mpnn_num_params floats), host memory */
+int pg_mpnn_get_params(const pg_mpnn *net, float *params);
+int pg_mpnn_set_params(pg_mpnn *net, const float *params);
 
 /* Allocation-free form of pg_gradient's cell gradient, for callers that
  * cannot allocate device memory (a fixed memory budget owned by an outer

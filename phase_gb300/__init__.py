@@ -79,6 +79,7 @@ PROTOTYPES = {
     "pg_eqn_sizes": (_I, [_P, _P, _P]),
     "pg_assemble_laplacian": (_I, [_P, _P, _D, _P, _P, _I]),
     "pg_eqn_export": (_I, [_P, _P, _P, _P, _P]),
+    "pg_eqn_device_values": (_I, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     "pg_face_dt_over_rho": (_I, [_P, _P, _D, _D, _D, _P, _I]),
     "pg_gradient": (_I, [_P, _P, _P, _P, _P, _I]),
     "pg_gradient_noalloc": (_I, [_P, _P, _P, _P]),
@@ -94,6 +95,15 @@ PROTOTYPES = {
     "pg_solver_get_x": (_I, [_P, _P, _I]),
     "pg_solver_partition": (_I, [_P, _P, ctypes.POINTER(_I)]),
     "pg_solver_profile": (_I, [_P, _I, _P]),
+    "pg_mpnn_create": (_I, [ctypes.c_uint64, ctypes.POINTER(_P)]),
+    "pg_mpnn_destroy": (_I, [_P]),
+    "pg_mpnn_num_params": (_I, [_P]),
+    "pg_mpnn_set_graph": (_I, [_P, _P, _P, _I64]),
+    "pg_mpnn_predict": (_I, [_P, _P, _P, _P, _P, _P, _I]),
+    "pg_mpnn_train_step": (_I, [_P, _P, _P, _P, _P, ctypes.c_float, _I, _P]),
+    "pg_mpnn_gradient": (_I, [_P, _P, _P, _P, _P, _I, _P, _P]),
+    "pg_mpnn_get_params": (_I, [_P, _P]),
+    "pg_mpnn_set_params": (_I, [_P, _P]),
     "pg_kernel_launches": (ctypes.c_uint64, []),
 }
 
@@ -208,6 +218,12 @@ class Mesh:
                                          _ptr(out), PG_HOST))
         return out
 
+    def dt_over_rho_device(self, gamma_cell_ptr: int, out_ptr: int, rho1,
+                           rho2, dt):
+        """dt_over_rho on device arrays (addresses as ints)."""
+        _check(lib().pg_face_dt_over_rho(self._h, _P(gamma_cell_ptr), rho1,
+                                         rho2, dt, _P(out_ptr), PG_DEVICE))
+
     def gradient(self, phi_cell, phi_face):
         pc = _f64(phi_cell, self.n_cells)
         pf = _f64(phi_face, self.n_faces)
@@ -256,6 +272,13 @@ class Equation:
             self._h, _P(gamma_face or None), gamma_scalar,
             _P(bc_value or None), _P(u_face or None), PG_DEVICE))
         return self
+
+    def device_values(self):
+        """(vals, rhs) device addresses of the assembled equation."""
+        v, r = _P(), _P()
+        _check(lib().pg_eqn_device_values(self._h, ctypes.byref(v),
+                                          ctypes.byref(r)))
+        return v.value, r.value
 
     def export(self):
         rp = np.empty(self.n + 1, np.int32)

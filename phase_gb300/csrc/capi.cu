@@ -367,6 +367,14 @@ extern "C" int pg_assemble_laplacian(pg_eqn *e, const double *gamma_face,
   return PG_OK;
 }
 
+extern "C" int pg_eqn_device_values(const pg_eqn *e, double **vals,
+                                    double **rhs) {
+  PG_CHECK_ARG(e, "pg_eqn_device_values: NULL equation");
+  if (vals) *vals = e->vals.p;
+  if (rhs) *rhs = e->rhs.p;
+  return PG_OK;
+}
+
 extern "C" int pg_eqn_export(const pg_eqn *e, int32_t *row_ptr,
                              int32_t *col_ind, double *vals, double *rhs) {
   PG_CHECK_ARG(e, "pg_eqn_export: NULL equation");

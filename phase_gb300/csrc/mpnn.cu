@@ -1,0 +1,726 @@
+// Learned initial guess for the pressure solve: a small message-passing
+// network on the matrix graph (Gilmer et al., "Neural message passing for
+// quantum chemistry", ICML 2017) with hand-written forward, backward and
+// Adam (Kingma & Ba, ICLR 2015) kernels.  No reference counterpart: Phase
+// always starts BiCGStab from its previous solution.
+//
+// Per cell i, from the system A x = b of this step and the previous
+// solution x_prev:
+//   features f_i = [x_prev_i / s_x, b_i / s_b, r_i / s_b, log(|a_ii| / m_a)]
+//                  with r = b - A x_prev, s_* root-mean-square scales
+//   h0 = relu(W0 f + b0)                                   (4 -> 32)
+//   for l = 1..3:  q_j   = P_l h_j + c_l
+//                  m_i   = sum_{j in N(i)} e_ij relu(q_j),  e_ij = -a_ij/a_ii
+//                  h_l   = relu(U_l [h_{l-1}; m] + d_l) + h_{l-1}
+//   guess_i = x_prev_i + s_d (w_o . h3_i + b_o),  s_d = rms(r_i / a_ii)
+// Loss: |A g - b|^2 / |A x_prev - b|^2 + |g - x*|^2 / |x_prev - x*|^2.
+// Weights are rounded to BF16 for every use (an FP32 master copy is kept for
+// Adam); all accumulation is FP32.  Activations are stored feature-major
+// (feature k of cell i at k*N + i) so every kernel reads coalesced.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <random>
+#include <vector>
+
+#include "internal.h"
+#include "kernels.cuh"
+
+namespace {
+
+constexpr int H = 32;      // hidden width
+constexpr int F = 4;       // input features
+constexpr int L = 3;       // message-passing layers
+constexpr int kBlock = 256;
+
+inline int grid_of(int64_t n) {
+  int64_t g = (n + kBlock - 1) / kBlock;
+  return (int)(g < 4864 ? (g > 0 ? g : 1) : 4864);
+}
+
+// ---- parameter layout (FP32 master, offsets in floats) ----
+struct Layout {
+  int w0, b0, P[L], c[L], U[L], d[L], wo, bo, total;
+  Layout() {
+    int o = 0;
+    w0 = o; o += F * H;
+    b0 = o; o += H;
+    for (int l = 0; l < L; ++l) {
+      P[l] = o; o += H * H;
+      c[l] = o; o += H;
+      U[l] = o; o += 2 * H * H;
+      d[l] = o; o += H;
+    }
+    wo = o; o += H;
+    bo = o; o += 1;
+    total = o;
+  }
+};
+
+// ---------------------------------------------------------------- kernels
+__global__ void k_round_bf16(int n, const float *__restrict__ src,
+                             float *__restrict__ dst) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x)
+    dst[i] = __bfloat162float(__float2bfloat16(src[i]));
+}
+
+// r = b - A x, diag a_ii, edge weights e_ij = -a_ij / a_ii, per-cell sums
+// for the scales (double atomics: a handful of reductions per call)
+__global__ void k_prep(int n, const int32_t *__restrict__ rp,
+                       const int32_t *__restrict__ ci,
+                       const double *__restrict__ a,
+                       const double *__restrict__ b,
+                       const double *__restrict__ xp, float *__restrict__ r,
+                       float *__restrict__ diag, float *__restrict__ e,
+                       double *__restrict__ sums) {
+  double s[4] = {0., 0., 0., 0.};  // x^2, b^2, (r/a)^2, log|a|
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    double ax = 0., dii = 0.;
+    for (int k = rp[i]; k < rp[i + 1]; ++k) {
+      ax += a[k] * xp[ci[k]];
+      if (ci[k] == i) dii = a[k];
+    }
+    const double ri = b[i] - ax;
+    r[i] = (float)ri;
+    diag[i] = (float)dii;
+    for (int k = rp[i]; k < rp[i + 1]; ++k)
+      e[k] = (ci[k] == i || dii == 0.) ? 0.f : (float)(-a[k] / dii);
+    s[0] += xp[i] * xp[i];
+    s[1] += b[i] * b[i];
+    const double q = dii != 0. ? ri / dii : 0.;
+    s[2] += q * q;
+    s[3] += log(fabs(dii) + 1e-300);
+  }
+  for (int k = 0; k < 4; ++k) {
+    double v = s[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&sums[k], v);
+  }
+}
+
+__global__ void k_features(int n, const double *__restrict__ b,
+                           const double *__restrict__ xp,
+                           const float *__restrict__ r,
+                           const float *__restrict__ diag,
+                           const double *__restrict__ sums,
+                           float *__restrict__ f) {
+  const double sx = sqrt(sums[0] / n) + 1e-300, sb = sqrt(sums[1] / n) + 1e-300;
+  const double la = sums[3] / n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    f[0 * n + i] = (float)(xp[i] / sx);
+    f[1 * n + i] = (float)(b[i] / sb);
+    f[2 * n + i] = (float)(r[i] / sb);
+    f[3 * n + i] = (float)(log(fabs((double)diag[i]) + 1e-300) - la);
+  }
+}
+
+// Y[h][i] (+)= act( sum_k X[k][i] W[k][h] + bias[h] ) for K inputs taken
+// from up to two feature-major arrays (X1 rows 0..K1-1, X2 the rest).
+// W is K x H row-major (or H x K when transposed, for input gradients).
+template <int K, int HO, bool RELU, bool ACC, bool TRANS>
+__global__ void __launch_bounds__(kBlock)
+k_dense(int n, const float *__restrict__ X1, int K1,
+        const float *__restrict__ X2, const float *__restrict__ W,
+        const float *__restrict__ bias, float *__restrict__ Y,
+        float *__restrict__ Z) {
+  __shared__ float w[K * HO];
+  __shared__ float bs[HO];
+  for (int t = threadIdx.x; t < K * HO; t += blockDim.x) {
+    const int k = t / HO, h = t % HO;
+    w[t] = TRANS ? W[h * K + k] : W[k * HO + h];
+  }
+  for (int t = threadIdx.x; t < HO; t += blockDim.x) bs[t] = bias ? bias[t] : 0.f;
+  __syncthreads();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    float acc[HO];
+#pragma unroll
+    for (int h = 0; h < HO; ++h) acc[h] = bs[h];
+    for (int k = 0; k < K; ++k) {
+      const float x = k < K1 ? X1[(size_t)k * n + i] : X2[(size_t)(k - K1) * n + i];
+#pragma unroll
+      for (int h = 0; h < HO; ++h) acc[h] = fmaf(x, w[k * HO + h], acc[h]);
+    }
+#pragma unroll
+    for (int h = 0; h < HO; ++h) {
+      if (Z) Z[(size_t)h * n + i] = acc[h];  // pre-activation
+      const float v = RELU ? fmaxf(acc[h], 0.f) : acc[h];
+      if (ACC) Y[(size_t)h * n + i] += v;
+      else Y[(size_t)h * n + i] = v;
+    }
+  }
+}
+
+// m[h][i] = sum_j e_ij relu(q[h][j])  (forward message)
+__global__ void k_message(int n, const int32_t *__restrict__ rp,
+                          const int32_t *__restrict__ ci,
+                          const float *__restrict__ e,
+                          const float *__restrict__ q, float *__restrict__ m) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    float acc[H];
+#pragma unroll
+    for (int h = 0; h < H; ++h) acc[h] = 0.f;
+    for (int k = rp[i]; k < rp[i + 1]; ++k) {
+      const float w = e[k];
+      if (w == 0.f) continue;
+      const int j = ci[k];
+#pragma unroll
+      for (int h = 0; h < H; ++h) acc[h] = fmaf(w, fmaxf(q[(size_t)h * n + j], 0.f), acc[h]);
+    }
+#pragma unroll
+    for (int h = 0; h < H; ++h) m[(size_t)h * n + i] = acc[h];
+  }
+}
+
+// dq[h][j] = relu'(q[h][j]) sum_{i in N(j)} e_ij dm[h][i]  (uses the
+// transposed entry index: entry k = (j, i) -> tr[k] = index of (i, j))
+__global__ void k_message_bwd(int n, const int32_t *__restrict__ rp,
+                              const int32_t *__restrict__ ci,
+                              const int32_t *__restrict__ tr,
+                              const float *__restrict__ e,
+                              const float *__restrict__ q,
+                              const float *__restrict__ dm,
+                              float *__restrict__ dq) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n;
+       j += gridDim.x * blockDim.x) {
+    float acc[H];
+#pragma unroll
+    for (int h = 0; h < H; ++h) acc[h] = 0.f;
+    for (int k = rp[j]; k < rp[j + 1]; ++k) {
+      const int i = ci[k];
+      if (i == j || tr[k] < 0) continue;
+      const float w = e[tr[k]];
+#pragma unroll
+      for (int h = 0; h < H; ++h) acc[h] = fmaf(w, dm[(size_t)h * n + i], acc[h]);
+    }
+#pragma unroll
+    for (int h = 0; h < H; ++h)
+      dq[(size_t)h * n + j] = q[(size_t)h * n + j] > 0.f ? acc[h] : 0.f;
+  }
+}
+
+// dz = dy * (z > 0)
+__global__ void k_relu_bwd(int64_t n, const float *__restrict__ z,
+                           const float *__restrict__ dy,
+                           float *__restrict__ dz) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dz[i] = z[i] > 0.f ? dy[i] : 0.f;
+}
+
+// G[k][h] += sum_i X[k][i] D[h][i]; gb[h] += sum_i D[h][i]   (weight grads)
+template <int K>
+__global__ void __launch_bounds__(kBlock)
+k_wgrad(int n, const float *__restrict__ X1, int K1,
+        const float *__restrict__ X2, const float *__restrict__ D,
+        float *__restrict__ G, float *__restrict__ gb) {
+  constexpr int CH = 32;  // cells staged per round
+  __shared__ float xs[K][CH];
+  __shared__ float ds[H][CH + 1];
+  float acc[(K * H + kBlock - 1) / kBlock];
+  float accb = 0.f;
+  constexpr int PER = (K * H + kBlock - 1) / kBlock;
+#pragma unroll
+  for (int p = 0; p < PER; ++p) acc[p] = 0.f;
+  for (int base = blockIdx.x * CH; base < n; base += gridDim.x * CH) {
+    for (int t = threadIdx.x; t < K * CH; t += blockDim.x) {
+      const int k = t / CH, c = t % CH, i = base + c;
+      xs[k][c] = i < n ? (k < K1 ? X1[(size_t)k * n + i] : X2[(size_t)(k - K1) * n + i]) : 0.f;
+    }
+    for (int t = threadIdx.x; t < H * CH; t += blockDim.x) {
+      const int h = t / CH, c = t % CH, i = base + c;
+      ds[h][c] = i < n ? D[(size_t)h * n + i] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int p = 0; p < PER; ++p) {
+      const int t = threadIdx.x + p * kBlock;
+      if (t < K * H) {
+        const int k = t / H, h = t % H;
+        float s = 0.f;
+#pragma unroll 8
+        for (int c = 0; c < CH; ++c) s = fmaf(xs[k][c], ds[h][c], s);
+        acc[p] += s;
+      }
+    }
+    if (threadIdx.x < H) {
+      float s = 0.f;
+      for (int c = 0; c < CH; ++c) s += ds[threadIdx.x][c];
+      accb += s;
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int p = 0; p < PER; ++p) {
+    const int t = threadIdx.x + p * kBlock;
+    if (t < K * H) atomicAdd(&G[t], acc[p]);
+  }
+  if (gb && threadIdx.x < H) atomicAdd(&gb[threadIdx.x], accb);
+}
+
+// output head: out_i = wo . h_i + bo; guess = x_prev + s_d out
+__global__ void k_head(int n, const float *__restrict__ h3,
+                       const float *__restrict__ w, const double *__restrict__ xp,
+                       const double *__restrict__ sums, float *__restrict__ out,
+                       double *__restrict__ g) {
+  const double sd = sqrt(sums[2] / n);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    float o = w[H];
+#pragma unroll
+    for (int h = 0; h < H; ++h) o = fmaf(w[h], h3[(size_t)h * n + i], o);
+    out[i] = o;
+    g[i] = xp[i] + sd * (double)o;
+  }
+}
+
+// residual res = A g - b, error err = g - x*, and the loss sums
+__global__ void k_loss(int n, const int32_t *__restrict__ rp,
+                       const int32_t *__restrict__ ci,
+                       const double *__restrict__ a,
+                       const double *__restrict__ b,
+                       const double *__restrict__ g,
+                       const double *__restrict__ xs,
+                       const double *__restrict__ xp, double *__restrict__ res,
+                       double *__restrict__ err, double *__restrict__ sums) {
+  double s[4] = {0., 0., 0., 0.};  // |res|^2, |A xp - b|^2, |err|^2, |xp-x*|^2
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    double ag = 0., ap = 0.;
+    for (int k = rp[i]; k < rp[i + 1]; ++k) {
+      ag += a[k] * g[ci[k]];
+      ap += a[k] * xp[ci[k]];
+    }
+    const double rr = ag - b[i], r0 = ap - b[i];
+    res[i] = rr;
+    s[0] += rr * rr;
+    s[1] += r0 * r0;
+    if (xs) {
+      const double ee = g[i] - xs[i], e0 = xp[i] - xs[i];
+      err[i] = ee;
+      s[2] += ee * ee;
+      s[3] += e0 * e0;
+    }
+  }
+  for (int k = 0; k < 4; ++k) {
+    double v = s[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&sums[4 + k], v);
+  }
+}
+
+// d out_i = s_d (2 (A^T res)_i / R0 + 2 err_i / E0)
+__global__ void k_dout(int n, const int32_t *__restrict__ rp,
+                       const int32_t *__restrict__ ci,
+                       const int32_t *__restrict__ tr,
+                       const double *__restrict__ a,
+                       const double *__restrict__ res,
+                       const double *__restrict__ err,
+                       const double *__restrict__ sums,
+                       float *__restrict__ dout) {
+  const double sd = sqrt(sums[2] / n);
+  const double R0 = sums[5] > 0. ? sums[5] : 1., E0 = sums[7] > 0. ? sums[7] : 1.;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    double atr = 0.;
+    for (int k = rp[i]; k < rp[i + 1]; ++k)
+      atr += a[tr[k] >= 0 ? tr[k] : k] * res[ci[k]];
+    double d = 2. * atr / R0;
+    if (err) d += 2. * err[i] / E0;
+    dout[i] = (float)(sd * d);
+  }
+}
+
+// head backward: dh3[h][i] = dout_i w[h]; g_w[h] += sum dout h3; g_b += sum dout
+__global__ void k_head_bwd(int n, const float *__restrict__ h3,
+                           const float *__restrict__ w,
+                           const float *__restrict__ dout,
+                           float *__restrict__ dh, float *__restrict__ gw) {
+  float acc[H + 1];
+#pragma unroll
+  for (int h = 0; h <= H; ++h) acc[h] = 0.f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    const float d = dout[i];
+#pragma unroll
+    for (int h = 0; h < H; ++h) {
+      dh[(size_t)h * n + i] = d * w[h];
+      acc[h] = fmaf(d, h3[(size_t)h * n + i], acc[h]);
+    }
+    acc[H] += d;
+  }
+#pragma unroll
+  for (int h = 0; h <= H; ++h) {
+    float v = acc[h];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&gw[h], v);
+  }
+}
+
+__global__ void k_axpy(int64_t n, const float *__restrict__ x,
+                       float *__restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] += x[i];
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master weights
+__global__ void k_adam(int n, float *__restrict__ p, const float *__restrict__ g,
+                       float *__restrict__ m, float *__restrict__ v, float lr,
+                       float b1, float b2, float eps, float c1, float c2) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+}  // namespace
+
+struct pg_mpnn {
+  Layout lay;
+  int64_t n = 0, nnz = 0;
+  std::vector<float> host_params;
+  pg::DevBuf<float> p, pb, g, m, v;  // master, bf16-rounded, grad, Adam
+  pg::DevBuf<int32_t> rp, ci, tr;
+  pg::DevBuf<float> feat, r, diag, e, out, dout;
+  pg::DevBuf<float> h[L + 1], z[L + 1], q[L], msg[L];
+  pg::DevBuf<float> dh, dh2, dz, dq, dmsg;
+  pg::DevBuf<double> sums, xg, res, err, st_a, st_b, st_x, st_s;
+  int step = 0;
+};
+
+namespace {
+
+int ensure(pg_mpnn *net, bool training) {
+  const int64_t n = net->n, nh = (int64_t)H * n;
+  cudaError_t e = cudaSuccess;
+  auto rs = [&](auto &buf, size_t cnt) {
+    if (e == cudaSuccess) e = buf.reserve(cnt);
+  };
+  rs(net->feat, (size_t)F * n);
+  rs(net->r, n);
+  rs(net->diag, n);
+  rs(net->e, net->nnz);
+  rs(net->out, n);
+  rs(net->sums, 16);
+  rs(net->xg, n);
+  for (int l = 0; l <= L; ++l) {
+    rs(net->h[l], nh);
+    rs(net->z[l], nh);
+  }
+  for (int l = 0; l < L; ++l) {
+    rs(net->q[l], nh);
+    rs(net->msg[l], nh);
+  }
+  if (training) {
+    rs(net->dout, n);
+    rs(net->dh, nh);
+    rs(net->dh2, 2 * nh);
+    rs(net->dz, nh);
+    rs(net->dq, nh);
+    rs(net->dmsg, nh);
+    rs(net->res, n);
+    rs(net->err, n);
+  }
+  if (e != cudaSuccess) return pg::cuda_fail(e, "mpnn buffers", __FILE__, __LINE__);
+  return PG_OK;
+}
+
+// forward pass; leaves activations for the backward pass
+int forward(pg_mpnn *net, const double *a, const double *b, const double *xp) {
+  cudaStream_t st = pg::stream();
+  const int n = (int)net->n;
+  const int g = grid_of(n);
+  const Layout &Y = net->lay;
+  const float *W = net->pb.p;
+  PG_CUDA(cudaMemsetAsync(net->sums.p, 0, 16 * sizeof(double), st));
+  k_prep<<<g, kBlock, 0, st>>>(n, net->rp.p, net->ci.p, a, b, xp, net->r.p,
+                               net->diag.p, net->e.p, net->sums.p);
+  k_features<<<g, kBlock, 0, st>>>(n, b, xp, net->r.p, net->diag.p, net->sums.p,
+                                   net->feat.p);
+  k_dense<F, H, true, false, false><<<g, kBlock, 0, st>>>(
+      n, net->feat.p, F, nullptr, W + Y.w0, W + Y.b0, net->h[0].p, net->z[0].p);
+  for (int l = 0; l < L; ++l) {
+    k_dense<H, H, false, false, false><<<g, kBlock, 0, st>>>(
+        n, net->h[l].p, H, nullptr, W + Y.P[l], W + Y.c[l], net->q[l].p, nullptr);
+    k_message<<<g, kBlock, 0, st>>>(n, net->rp.p, net->ci.p, net->e.p,
+                                    net->q[l].p, net->msg[l].p);
+    // h_{l+1} = h_l + relu(U [h_l; m] + d)
+    PG_CUDA(cudaMemcpyAsync(net->h[l + 1].p, net->h[l].p,
+                            (size_t)H * n * sizeof(float),
+                            cudaMemcpyDeviceToDevice, st));
+    k_dense<2 * H, H, true, true, false><<<g, kBlock, 0, st>>>(
+        n, net->h[l].p, H, net->msg[l].p, W + Y.U[l], W + Y.d[l],
+        net->h[l + 1].p, net->z[l + 1].p);
+  }
+  k_head<<<g, kBlock, 0, st>>>(n, net->h[L].p, W + Y.wo, xp, net->sums.p,
+                               net->out.p, net->xg.p);
+  pg::count_launches(4 + 3 * L);
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
+int stage_in(const double *src, size_t n, int ptr_kind, pg::DevBuf<double> &buf,
+             const double **out) {
+  if (ptr_kind == PG_DEVICE) {
+    *out = src;
+    return PG_OK;
+  }
+  PG_CUDA(buf.upload(src, n));
+  *out = buf.p;
+  return PG_OK;
+}
+
+}  // namespace
+
+using namespace pg;
+
+extern "C" int pg_mpnn_create(uint64_t seed, pg_mpnn **out) {
+  PG_CHECK_ARG(out, "pg_mpnn_create: out is NULL");
+  *out = nullptr;
+  auto *net = new (std::nothrow) pg_mpnn();
+  PG_CHECK_ARG(net, "pg_mpnn_create: out of memory");
+  const Layout &Y = net->lay;
+  net->host_params.assign(Y.total, 0.f);
+  std::mt19937_64 rng(seed);
+  auto init = [&](int off, int fan_in, int count) {
+    std::normal_distribution<float> d(0.f, std::sqrt(2.f / fan_in));
+    for (int i = 0; i < count; ++i) net->host_params[off + i] = d(rng);
+  };
+  init(Y.w0, F, F * H);
+  for (int l = 0; l < L; ++l) {
+    init(Y.P[l], H, H * H);
+    init(Y.U[l], 2 * H, 2 * H * H);
+    // small residual branches at start: the network begins near the
+    // previous solution
+    for (int i = 0; i < 2 * H * H; ++i) net->host_params[Y.U[l] + i] *= 0.1f;
+  }
+  // the output head starts at zero: guess = x_prev until trained
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = net->p.upload(net->host_params);
+  if (e == cudaSuccess) e = net->pb.reserve(Y.total);
+  if (e == cudaSuccess) e = net->g.zero(Y.total);
+  if (e == cudaSuccess) e = net->m.zero(Y.total);
+  if (e == cudaSuccess) e = net->v.zero(Y.total);
+  if (e != cudaSuccess) {
+    delete net;
+    return cuda_fail(e, "pg_mpnn_create", __FILE__, __LINE__);
+  }
+  k_round_bf16<<<grid_of(Y.total), kBlock, 0, stream()>>>(Y.total, net->p.p,
+                                                         net->pb.p);
+  count_launches(1);
+  PG_CUDA(cudaStreamSynchronize(stream()));
+  *out = net;
+  return PG_OK;
+}
+
+extern "C" int pg_mpnn_destroy(pg_mpnn *net) {
+  if (net) cudaStreamSynchronize(stream());
+  delete net;
+  return PG_OK;
+}
+
+extern "C" int pg_mpnn_num_params(const pg_mpnn *net) {
+  return net ? net->lay.total : 0;
+}
+
+extern "C" int pg_mpnn_set_graph(pg_mpnn *net, const int32_t *row_ptr,
+                                 const int32_t *col_ind, int64_t n) {
+  PG_CHECK_ARG(net && row_ptr && col_ind && n > 0, "pg_mpnn_set_graph: bad arg");
+  const int64_t nnz = row_ptr[n];
+  // transposed entry of every (i, j): the index of (j, i), or -1
+  std::vector<int32_t> tr(nnz, -1);
+  for (int64_t i = 0; i < n; ++i)
+    for (int32_t k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+      const int32_t j = col_ind[k];
+      PG_CHECK_ARG(j >= 0 && j < n, "pg_mpnn_set_graph: column out of range");
+      for (int32_t kk = row_ptr[j]; kk < row_ptr[j + 1]; ++kk)
+        if (col_ind[kk] == i) {
+          tr[k] = kk;
+          break;
+        }
+    }
+  net->n = n;
+  net->nnz = nnz;
+  PG_CUDA(net->rp.upload(row_ptr, n + 1));
+  PG_CUDA(net->ci.upload(col_ind, nnz));
+  PG_CUDA(net->tr.upload(tr));
+  int rc = ensure(net, false);
+  if (rc) return rc;
+  PG_CUDA(cudaStreamSynchronize(stream()));
+  return PG_OK;
+}
+
+extern "C" int pg_mpnn_predict(pg_mpnn *net, const double *vals,
+                               const double *b, const double *x_prev,
+                               double *guess, double *rel_residual,
+                               int ptr_kind) {
+  PG_CHECK_ARG(net && net->n > 0, "pg_mpnn_predict: set the graph first");
+  PG_CHECK_ARG(vals && b && x_prev && guess, "pg_mpnn_predict: NULL arg");
+  const double *a = nullptr, *bb = nullptr, *xp = nullptr;
+  int rc = stage_in(vals, net->nnz, ptr_kind, net->st_a, &a);
+  if (!rc) rc = stage_in(b, net->n, ptr_kind, net->st_b, &bb);
+  if (!rc) rc = stage_in(x_prev, net->n, ptr_kind, net->st_x, &xp);
+  if (!rc) rc = forward(net, a, bb, xp);
+  if (rc) return rc;
+  cudaStream_t st = stream();
+  if (rel_residual) {  // ||b - A g|| / ||b||
+    const int n = (int)net->n;
+    if (!net->res.p) PG_CUDA(net->res.reserve(n));
+    k_loss<<<grid_of(n), kBlock, 0, st>>>(n, net->rp.p, net->ci.p, a, bb,
+                                         net->xg.p, nullptr, xp, net->res.p,
+                                         nullptr, net->sums.p);
+    count_launches(1);
+    double s[16];
+    PG_CUDA(cudaMemcpyAsync(s, net->sums.p, sizeof(s), cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    *rel_residual = s[1] > 0. ? std::sqrt(s[4] / s[1]) : 0.;
+  }
+  PG_CUDA(copy_out(guess, net->xg.p, net->n * sizeof(double), ptr_kind));
+  PG_CUDA(cudaStreamSynchronize(st));
+  return PG_OK;
+}
+
+// forward + backward: the parameter gradients land in net->g
+static int backward_pass(pg_mpnn *net, const double *vals, const double *b,
+                         const double *x_prev, const double *x_star,
+                         int ptr_kind, double *loss) {
+  PG_CHECK_ARG(net && net->n > 0, "pg_mpnn: set the graph first");
+  PG_CHECK_ARG(vals && b && x_prev && x_star, "pg_mpnn: NULL arg");
+  int rc = ensure(net, true);
+  if (rc) return rc;
+  const double *a = nullptr, *bb = nullptr, *xp = nullptr, *xs = nullptr;
+  rc = stage_in(vals, net->nnz, ptr_kind, net->st_a, &a);
+  if (!rc) rc = stage_in(b, net->n, ptr_kind, net->st_b, &bb);
+  if (!rc) rc = stage_in(x_prev, net->n, ptr_kind, net->st_x, &xp);
+  if (!rc) rc = stage_in(x_star, net->n, ptr_kind, net->st_s, &xs);
+  if (!rc) rc = forward(net, a, bb, xp);
+  if (rc) return rc;
+  cudaStream_t st = stream();
+  const int n = (int)net->n;
+  const int g = grid_of(n);
+  const Layout &Y = net->lay;
+  const float *W = net->pb.p;
+  float *G = net->g.p;
+  const size_t nh = (size_t)H * n;
+  const int gh = grid_of((int64_t)nh);
+  int launches = 0;
+  PG_CUDA(cudaMemsetAsync(G, 0, Y.total * sizeof(float), st));
+  k_loss<<<g, kBlock, 0, st>>>(n, net->rp.p, net->ci.p, a, bb, net->xg.p, xs,
+                               xp, net->res.p, net->err.p, net->sums.p);
+  k_dout<<<g, kBlock, 0, st>>>(n, net->rp.p, net->ci.p, net->tr.p, a,
+                               net->res.p, net->err.p, net->sums.p,
+                               net->dout.p);
+  // head: dh = dL/dh_L
+  k_head_bwd<<<g, kBlock, 0, st>>>(n, net->h[L].p, W + Y.wo, net->dout.p,
+                                   net->dh.p, G + Y.wo);
+  launches += 3;
+  for (int l = L - 1; l >= 0; --l) {
+    // h_{l+1} = h_l + relu(z_{l+1}),  z_{l+1} = U_l [h_l; m_l] + d_l
+    k_relu_bwd<<<gh, kBlock, 0, st>>>((int64_t)nh, net->z[l + 1].p, net->dh.p,
+                                      net->dz.p);
+    k_wgrad<2 * H><<<g, kBlock, 0, st>>>(n, net->h[l].p, H, net->msg[l].p,
+                                        net->dz.p, G + Y.U[l], G + Y.d[l]);
+    // [dh_l part; dm] = dz U_l^T   (2H outputs)
+    k_dense<H, 2 * H, false, false, true><<<g, kBlock, 0, st>>>(
+        n, net->dz.p, H, nullptr, W + Y.U[l], nullptr, net->dh2.p, nullptr);
+    // m_l = E relu(q_l):  dq = relu'(q_l) (E^T dm)
+    k_message_bwd<<<g, kBlock, 0, st>>>(n, net->rp.p, net->ci.p, net->tr.p,
+                                        net->e.p, net->q[l].p, net->dh2.p + nh,
+                                        net->dq.p);
+    k_wgrad<H><<<g, kBlock, 0, st>>>(n, net->h[l].p, H, nullptr, net->dq.p,
+                                    G + Y.P[l], G + Y.c[l]);
+    // dh_l = dh_{l+1} (residual) + dh2[0:H] + dq P_l^T
+    k_axpy<<<gh, kBlock, 0, st>>>((int64_t)nh, net->dh2.p, net->dh.p);
+    k_dense<H, H, false, true, true><<<g, kBlock, 0, st>>>(
+        n, net->dq.p, H, nullptr, W + Y.P[l], nullptr, net->dh.p, nullptr);
+    launches += 7;
+  }
+  // encoder: h_0 = relu(W0 f + b0)
+  k_relu_bwd<<<gh, kBlock, 0, st>>>((int64_t)nh, net->z[0].p, net->dh.p,
+                                    net->dz.p);
+  k_wgrad<F><<<g, kBlock, 0, st>>>(n, net->feat.p, F, nullptr, net->dz.p,
+                                  G + Y.w0, G + Y.b0);
+  count_launches(launches + 2);
+  PG_CUDA(cudaGetLastError());
+  double sm[16];
+  PG_CUDA(cudaMemcpyAsync(sm, net->sums.p, sizeof(sm), cudaMemcpyDeviceToHost, st));
+  PG_CUDA(cudaStreamSynchronize(st));
+  // loss of the forward pass that produced these gradients
+  const double lv = (sm[5] > 0. ? sm[4] / sm[5] : 0.) + (sm[7] > 0. ? sm[6] / sm[7] : 0.);
+  if (loss) *loss = lv;
+  if (!std::isfinite(lv)) {
+    set_error("pg_mpnn: non-finite loss");
+    return PG_NON_FINITE;
+  }
+  return PG_OK;
+}
+
+extern "C" int pg_mpnn_gradient(pg_mpnn *net, const double *vals,
+                                const double *b, const double *x_prev,
+                                const double *x_star, int ptr_kind,
+                                float *grad, double *loss) {
+  int rc = backward_pass(net, vals, b, x_prev, x_star, ptr_kind, loss);
+  if (rc) return rc;
+  PG_CHECK_ARG(grad, "pg_mpnn_gradient: NULL grad");
+  PG_CUDA(cudaMemcpyAsync(grad, net->g.p, net->lay.total * sizeof(float),
+                          cudaMemcpyDeviceToHost, stream()));
+  PG_CUDA(cudaStreamSynchronize(stream()));
+  return PG_OK;
+}
+
+extern "C" int pg_mpnn_train_step(pg_mpnn *net, const double *vals,
+                                  const double *b, const double *x_prev,
+                                  const double *x_star, float lr, int ptr_kind,
+                                  double *loss) {
+  int rc = backward_pass(net, vals, b, x_prev, x_star, ptr_kind, loss);
+  if (rc) return rc;
+  cudaStream_t st = stream();
+  const Layout &Y = net->lay;
+  // Adam on the FP32 master weights, then the BF16-rounded copy
+  ++net->step;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - std::pow(b1, (float)net->step);
+  const float c2 = 1.f - std::pow(b2, (float)net->step);
+  k_adam<<<grid_of(Y.total), kBlock, 0, st>>>(Y.total, net->p.p, net->g.p, net->m.p,
+                                             net->v.p, lr, b1, b2, 1e-8f, c1,
+                                             c2);
+  k_round_bf16<<<grid_of(Y.total), kBlock, 0, st>>>(Y.total, net->p.p,
+                                                   net->pb.p);
+  count_launches(2);
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
+extern "C" int pg_mpnn_get_params(const pg_mpnn *net, float *params) {
+  PG_CHECK_ARG(net && params, "pg_mpnn_get_params: NULL arg");
+  PG_CUDA(cudaMemcpyAsync(params, net->p.p, net->lay.total * sizeof(float),
+                          cudaMemcpyDeviceToHost, stream()));
+  PG_CUDA(cudaStreamSynchronize(stream()));
+  return PG_OK;
+}
+
+extern "C" int pg_mpnn_set_params(pg_mpnn *net, const float *params) {
+  PG_CHECK_ARG(net && params, "pg_mpnn_set_params: NULL arg");
+  const int n = net->lay.total;
+  PG_CUDA(net->p.upload(params, n));
+  k_round_bf16<<<grid_of(n), kBlock, 0, stream()>>>(n, net->p.p, net->pb.p);
+  count_launches(1);
+  PG_CUDA(cudaMemsetAsync(net->m.p, 0, n * sizeof(float), stream()));
+  PG_CUDA(cudaMemsetAsync(net->v.p, 0, n * sizeof(float), stream()));
+  net->step = 0;
+  PG_CUDA(cudaStreamSynchronize(stream()));
+  return PG_OK;
+}
