@@ -53,7 +53,10 @@ extern "C" {
 
 /* arithmetic of the Krylov iteration */
 #define PG_FP64 0
-#define PG_MIXED 1 /* FP32 inner BiCGStab + ILU inside FP64 refinement */
+#define PG_MIXED 1 /* FP64 vectors, SpMV and dot products; ILU(0) factors
+                      stored and swept in FP32 (a preconditioner may be
+                      inexact: convergence is still judged on the FP64 true
+                      residual).  With Jacobi/none identical to PG_FP64. */
 
 typedef struct pg_mesh pg_mesh;
 typedef struct pg_eqn pg_eqn;
@@ -229,13 +232,14 @@ typedef struct {
   int subdomain_rows; /* target rows per Schwarz subdomain; 0 = default;
                          -1 = one subdomain (global ILU(0)) */
   int precision;      /* PG_FP64 | PG_MIXED */
-  int inner_max_iters;     /* PG_MIXED: inner iterations per refinement step */
-  double inner_tolerance;  /* PG_MIXED: inner relative residual target */
+  int reserved_i;     /* ignored; keeps the layout fixed */
+  double reserved_d;  /* ignored */
 } pg_solver_cfg;
 
 typedef struct {
-  int iters;           /* BiCGStab iterations (inner iterations if mixed) */
-  int outer_iters;     /* refinement steps (mixed) or restarts + 1 */
+  int iters;           /* BiCGStab iterations */
+  int outer_iters;     /* reliable updates: true-residual replacements and
+                          restarts */
   int status;          /* PG_OK, PG_MAX_ITERS, PG_BREAKDOWN, PG_NON_FINITE */
   double rel_residual; /* true ||b - A x||_2 / ||b||_2 computed in FP64 */
   double ms;           /* device time of the solve (CUDA events) */
@@ -282,8 +286,8 @@ int pg_solver_get_x(const pg_solver *s, double *x, int ptr_kind);
  * launched `reps` times back to back on the library stream between CUDA
  * events, on scratch vectors.  Per launch, ms[0] FP64 SpMV with fused dot,
  * ms[1] FP64 ILU(0)/Jacobi apply with fused update, ms[2] FP64 BiCGStab x/r
- * update, ms[3] ILU(0) factorisation, and for PG_MIXED ms[4..6] the FP32
- * SpMV, apply and update (0 otherwise); ms[7] is reserved (0).  Leaves the
+ * update, ms[3] ILU(0) factorisation, and for PG_MIXED with ILU(0) ms[4]
+ * the FP32-factor apply (0 otherwise); ms[5..7] are reserved (0).  Leaves the
  * solver's state untouched.  (No reference counterpart: measurement.) */
 int pg_solver_profile(pg_solver *s, int reps, double *ms);
 
@@ -293,6 +297,15 @@ uint64_t pg_kernel_launches(void);
 /* Subdomain id of every row of the last analysed pattern (host, part[n]);
  * returns the number of subdomains in *n_parts. */
 int pg_solver_partition(const pg_solver *s, int32_t *part, int *n_parts);
+
+/* z = M^-1 r for the solver's preconditioner on its current matrix (the
+ * ILU(0) factors are recomputed from the current values; FP32 factors and
+ * sweeps under PG_MIXED), r and z in the caller's row order.  The Ifpack2
+ * preconditioner's apply() (TrilinosBelosSparseMatrixSolver.cpp:63-85, used
+ * by Belos inside the iteration); exposed for parity checks of the sweeps.
+ * Overwrites the solver's Krylov work vectors but not its solution. */
+int pg_solver_apply_precond(pg_solver *s, const double *r, double *z,
+                            int ptr_kind);
 
 #ifdef __cplusplus
 }

@@ -43,8 +43,8 @@ class PhaseError(RuntimeError):
 class SolverCfg(ctypes.Structure):
     _fields_ = [("tolerance", ctypes.c_double), ("max_iters", ctypes.c_int),
                 ("precond", ctypes.c_int), ("subdomain_rows", ctypes.c_int),
-                ("precision", ctypes.c_int), ("inner_max_iters", ctypes.c_int),
-                ("inner_tolerance", ctypes.c_double)]
+                ("precision", ctypes.c_int), ("reserved_i", ctypes.c_int),
+                ("reserved_d", ctypes.c_double)]
 
 
 class SolveStats(ctypes.Structure):
@@ -95,6 +95,7 @@ PROTOTYPES = {
     "pg_solver_get_x": (_I, [_P, _P, _I]),
     "pg_solver_partition": (_I, [_P, _P, ctypes.POINTER(_I)]),
     "pg_solver_profile": (_I, [_P, _I, _P]),
+    "pg_solver_apply_precond": (_I, [_P, _P, _P, _I]),
     "pg_mpnn_create": (_I, [ctypes.c_uint64, ctypes.POINTER(_P)]),
     "pg_mpnn_destroy": (_I, [_P]),
     "pg_mpnn_num_params": (_I, [_P]),
@@ -422,13 +423,23 @@ class SparseMatrixSolver:
         _check(lib().pg_solver_partition(self._h, _ptr(part), ctypes.byref(k)))
         return part, k.value
 
+    def apply_precond(self, r):
+        """z = M^-1 r with the solver's preconditioner (FP32 ILU(0) factors
+        under MIXED), in the caller's row order."""
+        r = np.ascontiguousarray(r, np.float64)
+        assert r.shape == (self.n,)
+        z = np.empty(self.n)
+        _check(lib().pg_solver_apply_precond(self._h, _ptr(r), _ptr(z), PG_HOST))
+        return z
+
     def profile(self, reps: int = 20):
-        """Per-launch ms of the hot kernels on the current system (FP64, and
-        FP32 for the mixed precision solver)."""
+        """Per-launch ms of the hot kernels on the current system: FP64 SpMV,
+        preconditioner apply, x/r update, ILU(0) factorisation, and the
+        FP32-factor ILU(0) apply of the mixed precision solver."""
         ms = np.zeros(8)
         _check(lib().pg_solver_profile(self._h, int(reps), _ptr(ms)))
         return dict(spmv=ms[0], precond=ms[1], update=ms[2], factor=ms[3],
-                    spmv32=ms[4], precond32=ms[5], update32=ms[6])
+                    precond32=ms[4])
 
     def printStatus(self, msg: str):
         print(f"{msg} iterations = {self.nIters()}, error = {self.error():f}.")

@@ -190,7 +190,7 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
   const int KL = KLT > 0 ? KLT : m.KL, KU = KUT > 0 ? KUT : m.KU;
   uint8_t *hdr = smem;
   uint8_t *const buf0 = smem + m.hdr_bytes;  // buffer b at buf0 + b*max_piece
-  VT *zs = reinterpret_cast<VT *>(smem + m.hdr_bytes + 2 * m.max_piece);
+  MT *zs = reinterpret_cast<MT *>(smem + m.hdr_bytes + 2 * m.max_piece);
   const uint8_t *g = rec + m.rec_off;
   if (lane == 0) {
     mbar_init(&bar[0], 1);
@@ -200,8 +200,8 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
     bulk_load(hdr, g, (uint32_t)m.hdr_bytes, &bar[2]);
   }
   for (int i = lane; i < nr; i += 32)
-    zs[i] = pre_input<VT>(MODE, m.r0 + i, r, pv, v, sc);
-  if (lane == 0) zs[nr] = (VT)0;
+    zs[i] = (MT)pre_input<VT>(MODE, m.r0 + i, r, pv, v, sc);
+  if (lane == 0) zs[nr] = (MT)0;
   __syncwarp();
   if (!mbar_wait_bounded(&bar[2], err)) return;
   const uint16_t *lvl = reinterpret_cast<const uint16_t *>(hdr);
@@ -233,7 +233,7 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
       for (int l = tab[3 * j]; l < l1; ++l) {
         const int b = lvl[l + 1], w = b - a;
         const int ca = al16(2 * KL * w);
-        sweep_level<VT, MT, KLT>(zs, a, w, KL,
+        sweep_level<MT, MT, KLT>(zs, a, w, KL,
                                  reinterpret_cast<const uint16_t *>(pc),
                                  reinterpret_cast<const MT *>(pc + ca),
                                  (const MT *)nullptr, lane);
@@ -248,7 +248,7 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
       for (int l = lhi; l >= llo; --l) {
         const int a = lvl[l], w = b - a;
         const int ca = al16(2 * KU * w), va = al16(vs * KU * w);
-        sweep_level<VT, MT, KUT>(zs, a, w, KU,
+        sweep_level<MT, MT, KUT>(zs, a, w, KU,
                                  reinterpret_cast<const uint16_t *>(pc),
                                  reinterpret_cast<const MT *>(pc + ca),
                                  reinterpret_cast<const MT *>(pc + ca + va),
@@ -267,7 +267,7 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
                 (uint32_t)tab[3 * (j + 2) + 2], &bar[sb]);
     }
   }
-  for (int i = lane; i < nr; i += 32) z[m.r0 + i] = zs[i];
+  for (int i = lane; i < nr; i += 32) z[m.r0 + i] = (VT)zs[i];
 }
 
 // Step-form sweeps (kernels.cuh StepMeta) for rows with at most 3 L/U
@@ -296,7 +296,7 @@ k_ilu0_apply_steps(const StepMeta *__restrict__ meta,
   const int nr = m.nr, nf = m.n_fwd, S = m.n_fwd + m.n_bwd;
   const int P = (S + kStepsPerPiece - 1) / kStepsPerPiece;
   uint8_t *const buf0 = smem;  // buffer b at buf0 + b*PB
-  VT *zs = reinterpret_cast<VT *>(smem + 2 * PB);
+  MT *zs = reinterpret_cast<MT *>(smem + 2 * PB);
   const uint8_t *g = rec + m.rec_off;
   auto piece_bytes = [&](int j) {
     const int n = S - j * kStepsPerPiece;
@@ -311,20 +311,20 @@ k_ilu0_apply_steps(const StepMeta *__restrict__ meta,
     }
   }
   for (int i = lane; i < nr; i += 32)
-    zs[i] = pre_input<VT>(MODE, m.r0 + i, r, pv, v, sc);
-  if (lane == 0) zs[nr] = (VT)0;
+    zs[i] = (MT)pre_input<VT>(MODE, m.r0 + i, r, pv, v, sc);
+  if (lane == 0) zs[nr] = (MT)0;
   __syncwarp();
   using V4 = typename Vec4<MT>::T;
   const uint8_t *zb = reinterpret_cast<const uint8_t *>(zs);
   uint8_t *zw = reinterpret_cast<uint8_t *>(zs);
   // one step: z[row] = (z[row] - w0 z[c0] - w1 z[c1] - w2 z[c2]) (* 1/u_ii)
   auto step = [&](const uint4 &e, const V4 &w, bool bwd) {
-    VT acc = *reinterpret_cast<const VT *>(zb + e.x);
-    acc -= (VT)w.x * *reinterpret_cast<const VT *>(zb + e.y);
-    acc -= (VT)w.y * *reinterpret_cast<const VT *>(zb + e.z);
-    acc -= (VT)w.z * *reinterpret_cast<const VT *>(zb + e.w);
-    if (bwd) acc *= (VT)w.w;
-    *reinterpret_cast<VT *>(zw + e.x) = acc;
+    MT acc = *reinterpret_cast<const MT *>(zb + e.x);
+    acc -= w.x * *reinterpret_cast<const MT *>(zb + e.y);
+    acc -= w.y * *reinterpret_cast<const MT *>(zb + e.z);
+    acc -= w.z * *reinterpret_cast<const MT *>(zb + e.w);
+    if (bwd) acc *= w.w;
+    *reinterpret_cast<MT *>(zw + e.x) = acc;
     __syncwarp();
   };
   uint32_t phases = 0u;
@@ -361,7 +361,7 @@ k_ilu0_apply_steps(const StepMeta *__restrict__ meta,
                 &bar[sb]);
     }
   }
-  for (int i = lane; i < nr; i += 32) z[m.r0 + i] = zs[i];
+  for (int i = lane; i < nr; i += 32) z[m.r0 + i] = (VT)zs[i];
 }
 
 // Sweeps with the factor records and the vector in global memory, one CTA
@@ -527,5 +527,11 @@ template void launch_precond<float, float>(int, int, const SolverDev &,
                                            const float *, const float *,
                                            float *, const float *, float *,
                                            const KScalars *, cudaStream_t);
+
+void launch_ilu0_apply_fp32(int mode, const SolverDev &d, const double *r,
+                            double *pv, const double *v, double *z,
+                            const KScalars *sc, cudaStream_t st) {
+  launch_ilu0_apply<double, float>(mode, d, r, pv, v, z, sc, st);
+}
 
 }  // namespace pg

@@ -519,18 +519,82 @@ k_update(int n, VT *__restrict__ x, VT *__restrict__ r,
     if (!finite(tot[0]) || !finite(tot[1])) {
       sc->status = PG_NON_FINITE;
       sc->done = 1;
-    } else if (tot[1] <= sc->tol2 * sc->bb) {
-      sc->status = PG_OK;
+    } else {
+      // rho_prev/rho advance on every exit, so a residual replacement after
+      // a stop can continue the recurrence
+      if (om != 0. && sc->rho != 0.) sc->beta = (rho_new / sc->rho) * (al / om);
+      sc->rho_prev = sc->rho;
+      sc->rho = rho_new;
+      if (tot[1] <= sc->tol2 * sc->bb) {
+        sc->status = PG_OK;
+        sc->done = 1;
+      } else if (sc->iter >= sc->max_iter) {
+        sc->status = PG_MAX_ITERS;
+        sc->done = 1;
+      } else if (rho_new == 0. || om == 0.) {
+        sc->status = PG_BREAKDOWN;
+        sc->done = 1;
+      }
+    }
+  }
+}
+
+// Fresh start from the true residual in r: rhat = r, p = v = 0,
+// rho = <r, r>, alpha = omega = 1.
+__global__ void __launch_bounds__(kVecBlock)
+k_init_from_r(int n, const double *__restrict__ r, double *__restrict__ rh,
+              double *__restrict__ p, double *__restrict__ v, KScalars *sc,
+              RedWork w) {
+  double acc[1] = {0.};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    const double ri = r[i];
+    rh[i] = ri;
+    p[i] = 0.;
+    v[i] = 0.;
+    acc[0] += ri * ri;
+  }
+  double tot[1];
+  if (grid_reduce<1>(acc, w, tot) && threadIdx.x == 0) {
+    sc->rr = tot[0];
+    sc->rho = tot[0];
+    sc->rho_prev = 1.;
+    sc->alpha = 1.;
+    sc->omega = 1.;
+    sc->beta = tot[0];
+    sc->status = PG_OK;
+    sc->done = 0;
+    if (!finite(tot[0]) || tot[0] == 0.) {
+      sc->status = tot[0] == 0. ? PG_OK : PG_NON_FINITE;
       sc->done = 1;
-    } else if (sc->iter >= sc->max_iter) {
-      sc->status = PG_MAX_ITERS;
-      sc->done = 1;
-    } else if (rho_new == 0. || om == 0.) {
+    }
+  }
+}
+
+// Residual replacement: r already holds b - A x; the search directions are
+// kept and rho_{i+1}, beta_i are recomputed from the replaced r.
+__global__ void __launch_bounds__(kVecBlock)
+k_replace_r(int n, const double *__restrict__ r, const double *__restrict__ rh,
+            KScalars *sc, RedWork w) {
+  double acc[2] = {0., 0.};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    const double ri = r[i];
+    acc[0] += rh[i] * ri;
+    acc[1] += ri * ri;
+  }
+  double tot[2];
+  if (grid_reduce<2>(acc, w, tot) && threadIdx.x == 0) {
+    sc->rr = tot[1];
+    sc->done = 0;
+    sc->status = PG_OK;
+    if (!finite(tot[0]) || !finite(tot[1]) || tot[0] == 0. ||
+        sc->omega == 0. || sc->rho_prev == 0.) {
       sc->status = PG_BREAKDOWN;
       sc->done = 1;
     } else {
-      sc->beta = (rho_new / sc->rho) * (al / om);
-      sc->rho = rho_new;
+      sc->beta = (tot[0] / sc->rho_prev) * (sc->alpha / sc->omega);
+      sc->rho = tot[0];
     }
   }
 }
@@ -714,6 +778,17 @@ void launch_update(int n, VT *x, VT *r, const VT *ph, const VT *sh,
   k_update<VT><<<w.grid, kVecBlock, 0, st>>>(n, x, r, ph, sh, s, t, rh, sc, w);
   count_launches(1);
 }
+void launch_init_from_r(int n, double *r, double *rh, double *p, double *v,
+                        KScalars *sc, RedWork w, cudaStream_t st) {
+  k_init_from_r<<<w.grid, kVecBlock, 0, st>>>(n, r, rh, p, v, sc, w);
+  count_launches(1);
+}
+void launch_replace_r(int n, const double *r, const double *rh, KScalars *sc,
+                      RedWork w, cudaStream_t st) {
+  k_replace_r<<<w.grid, kVecBlock, 0, st>>>(n, r, rh, sc, w);
+  count_launches(1);
+}
+
 void launch_true_residual(const SolverDev &d, const double *val,
                           const double *b, const double *x, double *r,
                           KScalars *sc, RedWork w, cudaStream_t st) {

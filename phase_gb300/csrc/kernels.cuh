@@ -15,7 +15,7 @@ uint64_t launch_count();
 // every reducing kernel updates them, so the iteration never waits on the
 // host; kernels read them at entry and return at once when `done` is set.
 struct KScalars {
-  double rho, alpha, omega, beta;
+  double rho, rho_prev, alpha, omega, beta;
   double rv, tt, ts, rr, bb;
   double rr_true;
   double tol2;
@@ -196,6 +196,18 @@ template <class VT>
 void launch_update(int n, VT *x, VT *r, const VT *ph, const VT *sh,
                    const VT *s, const VT *t, const VT *rh, KScalars *sc,
                    RedWork w, cudaStream_t st);
+// Reliable updates (van der Vorst & Ye): restart the iteration from the
+// true residual held in r (fresh shadow residual), or keep the search
+// directions and only recompute rho/beta from the replaced r.
+void launch_init_from_r(int n, double *r, double *rh, double *p, double *v,
+                        KScalars *sc, RedWork w, cudaStream_t st);
+void launch_replace_r(int n, const double *r, const double *rh, KScalars *sc,
+                      RedWork w, cudaStream_t st);
+// ILU(0) application with FP32 factors and FP32 sweeps on FP64 vectors
+void launch_ilu0_apply_fp32(int mode, const SolverDev &d, const double *r,
+                            double *pv, const double *v, double *z,
+                            const KScalars *sc, cudaStream_t st);
+
 // rr_true = ||b - A x||^2 (FP64 matrix and vectors); x == NULL gives ||b||^2
 void launch_true_residual(const SolverDev &d, const double *val,
                           const double *b, const double *x, double *r,

@@ -1,10 +1,13 @@
 // The SparseMatrixSolver replacement: sparsity analysis caching, value
 // permutation, ILU(0) factorisation and the device-resident BiCGStab loop
-// (FP64, and FP32-inner / FP64-refined).
+// with reliable residual updates.  FP64 vectors and SpMV throughout; in
+// PG_MIXED the ILU(0) factors are stored and swept in FP32.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -27,13 +30,6 @@ __global__ void k_count_diff(int64_t n, const int32_t *__restrict__ a,
     }
 }
 
-__global__ void k_to_float(int64_t n, const double *__restrict__ a,
-                           float *__restrict__ b) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    b[i] = (float)a[i];
-}
-
 // deterministic non-zero contents for kernel timing
 __global__ void k_fill_profile(int64_t n, double *__restrict__ a,
                                float *__restrict__ b, int salt) {
@@ -43,20 +39,6 @@ __global__ void k_fill_profile(int64_t n, double *__restrict__ a,
     if (a) a[i] = v;
     if (b) b[i] = (float)v;
   }
-}
-
-// outer refinement helpers (FP64 residual, FP32 correction)
-__global__ void k_residual_to_float(int n, const double *__restrict__ r,
-                                    float *__restrict__ rf, double scale) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += gridDim.x * blockDim.x)
-    rf[i] = (float)(r[i] * scale);
-}
-__global__ void k_add_correction(int n, double *__restrict__ x,
-                                 const float *__restrict__ d, double scale) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += gridDim.x * blockDim.x)
-    x[i] += scale * (double)d[i];
 }
 
 }  // namespace
@@ -83,10 +65,8 @@ struct pg_solver {
   DevBuf<unsigned int> diff;
   // values and factors
   DevBuf<double> pvals, jdinv;
-  DevBuf<float> pvals32, jdinv32;
   // Krylov vectors (permuted order)
   DevBuf<double> b, x, r, rh, p, v, ph, s, sh, t, xout;
-  DevBuf<float> f_b, f_x, f_r, f_rh, f_p, f_v, f_ph, f_s, f_sh, f_t;
   // reductions and scalars
   DevBuf<double> partials;
   DevBuf<unsigned int> ticket;
@@ -98,7 +78,8 @@ struct pg_solver {
   bool have_rhs = false, have_x = false, have_vals = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   int red_grid = 1;
-  // CUDA graphs of one chunk of BiCGStab iterations (FP64, FP32); kernel
+  // CUDA graphs of one chunk of BiCGStab iterations (FP64 and FP32 ILU
+  // sweeps); kernel
   // arguments are fixed device pointers, so a graph stays valid until the
   // buffers are reallocated by a new analysis
   cudaGraphExec_t chunk_graph[2] = {nullptr, nullptr};
@@ -191,13 +172,6 @@ int upload_analysis(pg_solver *s) {
                              &s->jdinv})
     if (e == cudaSuccess) e = bf->reserve(n);
   if (e == cudaSuccess) e = s->pvals.reserve(nnz);
-  if (s->cfg.precision == PG_MIXED) {
-    for (DevBuf<float> *bf : {&s->f_b, &s->f_x, &s->f_r, &s->f_rh, &s->f_p,
-                              &s->f_v, &s->f_ph, &s->f_s, &s->f_sh, &s->f_t,
-                              &s->jdinv32})
-      if (e == cudaSuccess) e = bf->reserve(n);
-    if (e == cudaSuccess) e = s->pvals32.reserve(nnz);
-  }
   s->drop_graphs();
   s->red_grid = (int)std::min<int64_t>(1216, (n + kVecBlock - 1) / kVecBlock);
   if (s->red_grid < 1) s->red_grid = 1;
@@ -222,98 +196,145 @@ int ensure_host_state(pg_solver *s) {
   return PG_OK;
 }
 
+// PG_SOLVER_TRACE=1 prints the Krylov scalars at every chunk boundary
+bool trace_enabled() {
+  static const int on = [] {
+    const char *e = std::getenv("PG_SOLVER_TRACE");
+    return e && e[0] == '1' ? 1 : 0;
+  }();
+  return on != 0;
+}
+
 inline int grid_for(int64_t n) {
   return (int)std::min<int64_t>(1216, std::max<int64_t>(1, (n + 255) / 256));
 }
 
-// One BiCGStab run on the permuted system held in the given buffers.
-// VT/MT select FP64 or FP32 storage; reductions are FP64 throughout.
-template <class VT, class MT>
-int run_bicgstab(pg_solver *s, const MT *val, const MT *jdinv, VT *b, VT *x,
-                 VT *r, VT *rh, VT *p, VT *v,
-                 VT *ph, VT *ss, VT *sh, VT *t, double tol, int max_iters,
-                 bool check_true, int *iters, int *restarts) {
+// Right-preconditioned BiCGStab on the permuted system (b, x), as Belos
+// BICGSTAB with an Ifpack2 RILUK right preconditioner
+// (TrilinosBelosSparseMatrixSolver.cpp:18-29,44-86), with reliable residual
+// updates (van der Vorst & Ye 2000): at a chunk boundary where the recursive
+// residual has dropped by kDelta2 since the last update, or has met the
+// tolerance, the FP64 true residual b - A x replaces it; the search
+// directions are kept unless the recurrence broke down, in which case the
+// iteration restarts from x with a fresh shadow residual.  Convergence is
+// only ever declared on the true residual.
+int run_bicgstab(pg_solver *s, double tol, int max_iters, int *iters,
+                 int *updates) {
   cudaStream_t st = stream();
   const SolverDev d = s->dev();
   const RedWork w = s->red();
+  const bool fp32_ilu =
+      s->cfg.precision == PG_MIXED && s->cfg.precond == PG_PREC_ILU0;
+  double *const val = s->pvals.p, *const jd = s->jdinv.p;
+  double *const x = s->x.p, *const r = s->r.p, *const rh = s->rh.p;
+  double *const p = s->p.p, *const v = s->v.p, *const ph = s->ph.p;
+  double *const ss = s->s.p, *const sh = s->sh.p, *const t = s->t.p;
+  auto precond = [&](int mode, double *pv, double *z) {
+    if (fp32_ilu)
+      launch_ilu0_apply_fp32(mode, d, r, pv, v, z, s->sc.p, st);
+    else
+      launch_precond<double, double>(s->cfg.precond, mode, d, jd, r, pv, v, z,
+                                     s->sc.p, st);
+  };
+  // one chunk = kChunk iterations, 5 kernels each; captured once into a CUDA
+  // graph after the first direct chunk and replayed
+  constexpr int kChunk = 8;
+  constexpr double kDelta2 = 1e-4;   // replace when rr < kDelta2 * rr_ref
+  constexpr int kMaxRestarts = 50;
+  auto chunk = [&]() {
+    for (int c = 0; c < kChunk; ++c) {
+      precond(1, p, ph);
+      launch_spmv_v<double, double>(d, val, ph, v, rh, s->sc.p, w, st);
+      precond(2, ss, sh);
+      launch_spmv_t<double, double>(d, val, sh, t, ss, s->sc.p, w, st);
+      launch_update<double>(d.n, x, r, ph, sh, ss, t, rh, s->sc.p, w, st);
+    }
+  };
+  auto read_scalars = [&]() -> int {
+    PG_CUDA(cudaMemcpyAsync(s->sc_host, s->sc.p, sizeof(KScalars),
+                            cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    return PG_OK;
+  };
   KScalars init{};
   init.tol2 = tol * tol;
   init.max_iter = max_iters;
   *s->sc_host = init;
   PG_CUDA(cudaMemcpyAsync(s->sc.p, s->sc_host, sizeof(KScalars),
                           cudaMemcpyHostToDevice, st));
-  int n_restart = 0;
-  // one chunk = kChunk BiCGStab iterations, 5 kernels each; after the first
-  // (direct) chunk the chunk is captured once into a CUDA graph and replayed
-  constexpr int kChunk = 8;
-  auto chunk = [&]() {
-    for (int c = 0; c < kChunk; ++c) {
-      launch_precond<VT, MT>(s->cfg.precond, 1, d, jdinv, r, p, v, ph,
-                             s->sc.p, st);
-      launch_spmv_v<VT, MT>(d, val, ph, v, rh, s->sc.p, w, st);
-      launch_precond<VT, MT>(s->cfg.precond, 2, d, jdinv, r, ss, v, sh,
-                             s->sc.p, st);
-      launch_spmv_t<VT, MT>(d, val, sh, t, ss, s->sc.p, w, st);
-      launch_update<VT>(d.n, x, r, ph, sh, ss, t, rh, s->sc.p, w, st);
-    }
-  };
-  cudaGraphExec_t &gexec = s->chunk_graph[sizeof(VT) == 8 ? 0 : 1];
-  int chunks_run = 0;
+  // ||b||^2 and r = b - A x, then a fresh start
+  launch_true_residual(d, val, s->b.p, nullptr, nullptr, s->sc.p, w, st);
+  int rc = read_scalars();
+  if (rc) return rc;
+  const double bb = s->sc_host->rr_true;
+  *iters = 0;
+  *updates = 0;
+  if (!std::isfinite(bb)) return PG_NON_FINITE;
+  if (bb == 0.) {
+    PG_CUDA(cudaMemsetAsync(x, 0, d.n * sizeof(double), st));
+    return PG_OK;
+  }
+  init.bb = bb;
+  init.rr_true = bb;
+  *s->sc_host = init;
+  PG_CUDA(cudaMemcpyAsync(s->sc.p, s->sc_host, sizeof(KScalars),
+                          cudaMemcpyHostToDevice, st));
+  launch_true_residual(d, val, s->b.p, x, r, s->sc.p, w, st);
+  launch_init_from_r(d.n, r, rh, p, v, s->sc.p, w, st);
+  if ((rc = read_scalars())) return rc;
+  if (s->sc_host->status == PG_NON_FINITE) return PG_NON_FINITE;
+  if (s->sc_host->rr_true <= init.tol2 * bb) return PG_OK;
+  double rr_ref = s->sc_host->rr_true;
+  int restarts = 0;
+  cudaGraphExec_t &gexec = s->chunk_graph[fp32_ilu ? 1 : 0];
+  bool direct_done = false;
   for (;;) {
-    launch_krylov_init<VT, MT>(d, val, b, x, r, rh, p, v, s->sc.p, w, st);
-    for (;;) {
-      if (gexec) {
-        PG_CUDA(cudaGraphLaunch(gexec, st));
-        count_launches(5 * kChunk);
-      } else if (chunks_run > 0) {
-        cudaGraph_t graph = nullptr;
-        PG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
-        const uint64_t before = launch_count();
-        chunk();
-        const uint64_t captured = launch_count() - before;
-        PG_CUDA(cudaStreamEndCapture(st, &graph));
-        cudaError_t ge = cudaGraphInstantiate(&gexec, graph, 0);
-        cudaGraphDestroy(graph);
-        PG_CUDA(ge);
-        PG_CUDA(cudaGraphLaunch(gexec, st));
-        (void)captured;  // counted when captured, executed once here
-      } else {
-        chunk();
-      }
-      ++chunks_run;
-      PG_CUDA(cudaGetLastError());
-      PG_CUDA(cudaMemcpyAsync(s->sc_host, s->sc.p, sizeof(KScalars),
-                              cudaMemcpyDeviceToHost, st));
-      PG_CUDA(cudaStreamSynchronize(st));
-      if (s->sc_host->done) break;
+    if (gexec) {
+      PG_CUDA(cudaGraphLaunch(gexec, st));
+      count_launches(5 * kChunk);
+    } else if (direct_done) {
+      cudaGraph_t graph = nullptr;
+      PG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+      chunk();  // launches are counted here, executed once below
+      PG_CUDA(cudaStreamEndCapture(st, &graph));
+      cudaError_t ge = cudaGraphInstantiate(&gexec, graph, 0);
+      cudaGraphDestroy(graph);
+      PG_CUDA(ge);
+      PG_CUDA(cudaGraphLaunch(gexec, st));
+    } else {
+      chunk();
+      direct_done = true;
     }
+    PG_CUDA(cudaGetLastError());
+    if ((rc = read_scalars())) return rc;
     const KScalars k = *s->sc_host;
     *iters = k.iter;
-    *restarts = n_restart;
-    if (k.status != PG_OK || !check_true) return k.status;
-    if (k.bb == 0.) return PG_OK;
-    // confirm on the true residual (FP64 storage only)
-    if (sizeof(VT) == sizeof(double)) {
-      launch_true_residual(d, reinterpret_cast<const double *>(val),
-                           reinterpret_cast<const double *>(b),
-                           reinterpret_cast<const double *>(x), nullptr,
-                           s->sc.p, w, st);
-      PG_CUDA(cudaMemcpyAsync(s->sc_host, s->sc.p, sizeof(KScalars),
-                              cudaMemcpyDeviceToHost, st));
-      PG_CUDA(cudaStreamSynchronize(st));
-      if (s->sc_host->rr_true <= k.tol2 * k.bb) return PG_OK;
+    if (trace_enabled())
+      std::fprintf(stderr,
+                   "pg_solver: it %d rr/bb %.3e rho %.3e alpha %.3e omega "
+                   "%.3e status %d done %d\n",
+                   k.iter, k.rr / bb, k.rho, k.alpha, k.omega, k.status,
+                   k.done);
+    if (k.status == PG_NON_FINITE) return PG_NON_FINITE;
+    if (!k.done && !(k.rr < kDelta2 * rr_ref)) continue;
+    // reliable update: r = b - A x in FP64
+    launch_true_residual(d, val, s->b.p, x, r, s->sc.p, w, st);
+    if ((rc = read_scalars())) return rc;
+    const double rr_true = s->sc_host->rr_true;
+    ++*updates;
+    if (trace_enabled())
+      std::fprintf(stderr, "pg_solver: it %d true rr/bb %.3e (%s)\n", k.iter,
+                   rr_true / bb, k.status == PG_BREAKDOWN ? "restart" : "replace");
+    if (!std::isfinite(rr_true)) return PG_NON_FINITE;
+    if (rr_true <= init.tol2 * bb) return PG_OK;
+    if (k.iter >= max_iters) return PG_MAX_ITERS;
+    if (k.status == PG_BREAKDOWN) {
+      if (++restarts > kMaxRestarts) return PG_BREAKDOWN;
+      launch_init_from_r(d.n, r, rh, p, v, s->sc.p, w, st);
     } else {
-      return PG_OK;
+      launch_replace_r(d.n, r, rh, s->sc.p, w, st);
     }
-    if (++n_restart > 20 || k.iter >= max_iters) {
-      *restarts = n_restart;
-      return k.iter >= max_iters ? PG_MAX_ITERS : PG_BREAKDOWN;
-    }
-    // restart from the true residual: keep x and the iteration count
-    s->sc_host->done = 0;
-    s->sc_host->status = PG_OK;
-    PG_CUDA(cudaMemcpyAsync(s->sc.p, s->sc_host, sizeof(KScalars),
-                            cudaMemcpyHostToDevice, st));
+    rr_ref = rr_true;
   }
 }
 
@@ -328,15 +349,6 @@ int factor(pg_solver *s) {
   } else if (s->cfg.precond == PG_PREC_JACOBI) {
     launch_jacobi_diag(d, s->pvals.p, s->jdinv.p, st);
   }
-  if (mixed) {
-    k_to_float<<<grid_for(s->a.nnz), 256, 0, st>>>(s->a.nnz, s->pvals.p, s->pvals32.p);
-    count_launches(1);
-    if (s->cfg.precond == PG_PREC_JACOBI) {
-      k_to_float<<<grid_for(s->a.n), 256, 0, st>>>(s->a.n, s->jdinv.p, s->jdinv32.p);
-      count_launches(1);
-    }
-    PG_CUDA(cudaGetLastError());
-  }
   return PG_OK;
 }
 
@@ -350,8 +362,8 @@ extern "C" void pg_solver_default_cfg(pg_solver_cfg *cfg) {
   cfg->precond = PG_PREC_ILU0;
   cfg->subdomain_rows = 0;
   cfg->precision = PG_FP64;
-  cfg->inner_max_iters = 500;
-  cfg->inner_tolerance = 1e-4;
+  cfg->reserved_i = 0;
+  cfg->reserved_d = 0.;
 }
 
 extern "C" int pg_solver_create(const pg_solver_cfg *cfg, pg_solver **out) {
@@ -365,8 +377,6 @@ extern "C" int pg_solver_create(const pg_solver_cfg *cfg, pg_solver **out) {
                "pg_solver_create: bad preconditioner");
   PG_CHECK_ARG(c.precision == PG_FP64 || c.precision == PG_MIXED,
                "pg_solver_create: bad precision");
-  if (c.inner_max_iters <= 0) c.inner_max_iters = c.max_iters;
-  if (!(c.inner_tolerance > 0.)) c.inner_tolerance = 1e-4;
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0 || !stream()) {
     set_error("no CUDA device available: libphase_gb300 has no CPU path");
@@ -550,70 +560,13 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
     PG_CUDA(cudaMemcpyAsync(s->bad_host, s->bad.p, sizeof(int),
                             cudaMemcpyDeviceToHost, st));
   }
-  int status = PG_OK, iters = 0, outer = 0;
+  int iters = 0, outer = 0;
   const double tol = s->cfg.tolerance;
   const SolverDev d = s->dev();
   const RedWork w = s->red();
-  // ||b||^2 once per solve
-  launch_true_residual(d, s->pvals.p, s->b.p, nullptr, nullptr, s->sc.p, w, st);
-  PG_CUDA(cudaMemcpyAsync(s->sc_host, s->sc.p, sizeof(KScalars),
-                          cudaMemcpyDeviceToHost, st));
-  PG_CUDA(cudaStreamSynchronize(st));
-  const double bb = s->sc_host->rr_true;
-  if (!std::isfinite(bb)) {
-    status = PG_NON_FINITE;
-  } else if (bb == 0.) {
-    PG_CUDA(cudaMemsetAsync(s->x.p, 0, n * sizeof(double), st));
-  } else if (s->cfg.precision == PG_FP64) {
-    int restarts = 0;
-    status = run_bicgstab<double, double>(
-        s, s->pvals.p, s->jdinv.p, s->b.p, s->x.p, s->r.p,
-        s->rh.p, s->p.p, s->v.p, s->ph.p, s->s.p, s->sh.p, s->t.p, tol,
-        s->cfg.max_iters, true, &iters, &restarts);
-    outer = restarts + 1;
-  } else {
-    // Iterative refinement: r = b - A x in FP64; solve A d = r / ||r|| in
-    // FP32 (FP32 SpMV and ILU sweeps, FP64 dot products and scalars) to the
-    // inner tolerance; x += ||r|| d.  Stops on the FP64 true residual.
-    const int g = grid_for(n);
-    launch_true_residual(d, s->pvals.p, s->b.p, s->x.p, s->r.p, s->sc.p, w, st);
-    PG_CUDA(cudaMemcpyAsync(s->sc_host, s->sc.p, sizeof(KScalars),
-                            cudaMemcpyDeviceToHost, st));
-    PG_CUDA(cudaStreamSynchronize(st));
-    double rr = s->sc_host->rr_true;
-    while (rr > tol * tol * bb) {
-      if (!std::isfinite(rr)) { status = PG_NON_FINITE; break; }
-      if (outer >= 50 || iters >= s->cfg.max_iters) { status = PG_MAX_ITERS; break; }
-      const double rn = std::sqrt(rr);
-      k_residual_to_float<<<g, 256, 0, st>>>((int)n, s->r.p, s->f_b.p, 1.0 / rn);
-      count_launches(1);
-      PG_CUDA(cudaMemsetAsync(s->f_x.p, 0, n * sizeof(float), st));
-      int it = 0, rs = 0;
-      const int budget = std::max(1, std::min(s->cfg.inner_max_iters,
-                                              s->cfg.max_iters - iters));
-      const int ist = run_bicgstab<float, float>(
-          s, s->pvals32.p, s->jdinv32.p, s->f_b.p,
-          s->f_x.p, s->f_r.p, s->f_rh.p, s->f_p.p, s->f_v.p, s->f_ph.p,
-          s->f_s.p, s->f_sh.p, s->f_t.p, s->cfg.inner_tolerance, budget,
-          false, &it, &rs);
-      iters += it;
-      ++outer;
-      if (ist == PG_NON_FINITE) { status = ist; break; }
-      k_add_correction<<<g, 256, 0, st>>>((int)n, s->x.p, s->f_x.p, rn);
-      count_launches(1);
-      launch_true_residual(d, s->pvals.p, s->b.p, s->x.p, s->r.p, s->sc.p, w, st);
-      PG_CUDA(cudaMemcpyAsync(s->sc_host, s->sc.p, sizeof(KScalars),
-                              cudaMemcpyDeviceToHost, st));
-      PG_CUDA(cudaStreamSynchronize(st));
-      const double rr_new = s->sc_host->rr_true;
-      if (it == 0 || !(rr_new < rr)) {  // no progress: stagnation
-        status = PG_BREAKDOWN;
-        rr = rr_new;
-        break;
-      }
-      rr = rr_new;
-    }
-  }
+  int status = run_bicgstab(s, tol, s->cfg.max_iters, &iters, &outer);
+  if (status == PG_CUDA_ERROR) return status;
+  const double bb = s->sc_host->bb;
   // final true residual in FP64 and the solution in the caller's order
   launch_true_residual(d, s->pvals.p, s->b.p, s->x.p, nullptr, s->sc.p, w, st);
   launch_unpermute_vec((int)n, s->perm.p, s->x.p, s->xout.p, st);
@@ -630,7 +583,8 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
   float ms_fact = 0.f, ms_all = 0.f;
   cudaEventElapsedTime(&ms_fact, s->ev[0], s->ev[1]);
   cudaEventElapsedTime(&ms_all, s->ev[0], s->ev[2]);
-  const double rel = bb > 0. ? std::sqrt(s->sc_host->rr_true / bb) : 0.;
+  const double rel = bb > 0. ? std::sqrt(s->sc_host->rr_true / bb)
+                   : status == PG_NON_FINITE ? NAN : 0.;
   if (s->cfg.precond == PG_PREC_ILU0 && *s->bad_host > 0 && !(rel <= tol))
     status = PG_BREAKDOWN;
   if (status == PG_OK && !(rel <= tol)) status = PG_MAX_ITERS;
@@ -671,22 +625,18 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
   const RedWork w = s->red();
   const int64_t n = s->a.n;
   const int g = grid_for(n);
-  const bool mixed = s->cfg.precision == PG_MIXED;
+  const bool fp32_ilu =
+      s->cfg.precision == PG_MIXED && s->cfg.precond == PG_PREC_ILU0;
   // scratch vectors with benign non-zero contents, so no kernel takes its
   // breakdown/convergence exit; the solver's own state is left untouched
   DevBuf<double> d8[8];
-  DevBuf<float> f4[8];
   for (int k = 0; k < 8; ++k) {
     PG_CUDA(d8[k].reserve(n));
     k_fill_profile<<<g, 256, 0, st>>>(n, d8[k].p, nullptr, k);
-    if (mixed) {
-      PG_CUDA(f4[k].reserve(n));
-      k_fill_profile<<<g, 256, 0, st>>>(n, nullptr, f4[k].p, k);
-    }
   }
   KScalars k{};
   k.max_iter = 1 << 30;
-  k.alpha = k.omega = k.beta = k.rho = 1.0;
+  k.alpha = k.omega = k.beta = k.rho = k.rho_prev = 1.0;
   k.bb = 1.0;
   *s->sc_host = k;
   PG_CUDA(cudaMemcpyAsync(s->sc.p, s->sc_host, sizeof(KScalars),
@@ -709,14 +659,47 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
   if (!rc) rc = timed([&] { launch_precond<double, double>(s->cfg.precond, 1, d, s->jdinv.p, d8[3].p, d8[4].p, d8[1].p, d8[6].p, s->sc.p, st); }, &ms[1]);
   if (!rc) rc = timed([&] { launch_update<double>(d.n, d8[5].p, d8[3].p, d8[0].p, d8[6].p, d8[4].p, d8[1].p, d8[2].p, s->sc.p, w, st); }, &ms[2]);
   if (!rc && s->cfg.precond == PG_PREC_ILU0)
-    rc = timed([&] { launch_ilu0_factor(d, s->pvals.p, s->bad.p, mixed, st); }, &ms[3]);
-  if (!rc && mixed) {
-    rc = timed([&] { launch_spmv_v<float, float>(d, s->pvals32.p, f4[0].p, f4[1].p, f4[2].p, s->sc.p, w, st); }, &ms[4]);
-    if (!rc) rc = timed([&] { launch_precond<float, float>(s->cfg.precond, 1, d, s->jdinv32.p, f4[3].p, f4[4].p, f4[1].p, f4[6].p, s->sc.p, st); }, &ms[5]);
-    if (!rc) rc = timed([&] { launch_update<float>(d.n, f4[5].p, f4[3].p, f4[0].p, f4[6].p, f4[4].p, f4[1].p, f4[2].p, s->sc.p, w, st); }, &ms[6]);
-  }
+    rc = timed([&] { launch_ilu0_factor(d, s->pvals.p, s->bad.p, fp32_ilu, st); }, &ms[3]);
+  if (!rc && fp32_ilu)
+    rc = timed([&] { launch_ilu0_apply_fp32(1, d, d8[3].p, d8[4].p, d8[1].p, d8[6].p, s->sc.p, st); }, &ms[4]);
   PG_CUDA(cudaStreamSynchronize(st));
   return rc;
+}
+
+extern "C" int pg_solver_apply_precond(pg_solver *s, const double *r,
+                                       double *z, int ptr_kind) {
+  PG_CHECK_ARG(s && r && z, "pg_solver_apply_precond: NULL arg");
+  PG_CHECK_ARG(s->analysed && s->have_vals,
+               "pg_solver_apply_precond: set the matrix first");
+  cudaStream_t st = stream();
+  const SolverDev d = s->dev();
+  const int64_t n = s->a.n;
+  int rc = factor(s);
+  if (rc) return rc;
+  const double *dr = r;
+  if (ptr_kind != PG_DEVICE) {
+    PG_CUDA(s->st_vec.upload(r, n));
+    dr = s->st_vec.p;
+  }
+  // z = M^-1 r in the permuted order (mode 0 reads p, writes ph)
+  launch_permute_vec((int)n, s->perm.p, dr, 1.0, s->p.p, st);
+  if (s->cfg.precision == PG_MIXED && s->cfg.precond == PG_PREC_ILU0)
+    launch_ilu0_apply_fp32(0, d, nullptr, s->p.p, nullptr, s->ph.p, nullptr, st);
+  else
+    launch_precond<double, double>(s->cfg.precond, 0, d, s->jdinv.p, nullptr,
+                                   s->p.p, nullptr, s->ph.p, nullptr, st);
+  launch_unpermute_vec((int)n, s->perm.p, s->ph.p, s->t.p, st);
+  PG_CUDA(cudaGetLastError());
+  PG_CUDA(copy_out(z, s->t.p, n * sizeof(double), ptr_kind));
+  PG_CUDA(cudaStreamSynchronize(st));
+  int timed_out = 0;
+  PG_CUDA(cudaMemcpy(&timed_out, s->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (timed_out) {
+    PG_CUDA(cudaMemset(s->err.p, 0, sizeof(int)));
+    set_error("pg_solver_apply_precond: a bounded device wait ran out");
+    return PG_TIMEOUT;
+  }
+  return PG_OK;
 }
 
 extern "C" int pg_solver_partition(const pg_solver *s, int32_t *part,

@@ -225,6 +225,9 @@ def train(nx=1024, steps=2000, epochs=3, lr=2e-3, out=DEFAULT_WEIGHTS,
     for t in range(1, steps + 1):
         solver.set_eqn(seq.assemble(t))
         solver.solve()
+        if solver.stats.status != pg.PG_OK:
+            raise RuntimeError(f"dump: step {t} did not converge "
+                               f"({solver.stats.as_dict()})")
         solver.x_device(xs[t].data_ptr())
         iters.append(solver.nIters())
     log(f"dumped {steps} solves in {time.time() - t0:.1f} s "

@@ -245,6 +245,17 @@ def ilu0(rp, ci, v, part=None):
     return out, rc
 
 
+def ilu0_apply(rp, ci, lu, r, part=None):
+    """z = (LU)^-1 r for the factors of ilu0() (per subdomain with part)."""
+    z = np.empty(len(rp) - 1)
+    pa = None if part is None else np.ascontiguousarray(part, np.int32)
+    lib().or_ilu0_apply(len(rp) - 1, ptr(np.ascontiguousarray(rp, np.int32)),
+                        ptr(np.ascontiguousarray(ci, np.int32)),
+                        ptr(np.ascontiguousarray(lu, np.float64)), ptr(pa),
+                        ptr(np.ascontiguousarray(r, np.float64)), ptr(z))
+    return z
+
+
 def spmv(rp, ci, v, x):
     y = np.empty(len(rp) - 1)
     lib().or_spmv(len(rp) - 1, ptr(np.ascontiguousarray(rp, np.int32)),

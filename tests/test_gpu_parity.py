@@ -149,6 +149,51 @@ def test_solver_matches_oracle(case, pg, oracle, sub_rows):
     assert np.linalg.norm(b - A @ x) / np.linalg.norm(b) <= 1.01e-12
 
 
+def _bubble_system(pg, nx, ny):
+    w = workloads.rising_bubble(nx, ny, seed=3)
+    m = pg.Mesh(w["nodes"], w["cptr"], w["cind"])
+    w = workloads.rising_bubble(nx, ny, seed=3, faces=m.faces(),
+                                cells=m.cells())
+    coeff = m.dt_over_rho(w["gamma"], w["rho1"], w["rho2"], w["dt"])
+    eqn = pg.fv.laplacian(coeff, m, w["bc_type"], w["bc_value"], w["u"])
+    return eqn.export()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("mesh", ["bubble", "tri"])
+def test_ilu_apply_matches_oracle(pg, oracle, precision, mesh):
+    """The Schwarz ILU(0) sweeps alone, z = M^-1 r, against the oracle's
+    factor and triangular solves on the device's own partition.  FP64
+    factors: 1e-12 relative (the factor's FP64 operation order differs);
+    FP32 factors and sweeps: 2e-5 relative (single-precision rounding
+    through the level chains of these well-conditioned blocks)."""
+    if mesh == "bubble":
+        rp, ci, v, rhs = _bubble_system(pg, 128, 96)
+        sub = 1024
+    else:
+        nodes, cptr, cind = meshes.triangulated(70, 60, 1.0, 1.0,
+                                                jitter=0.25, seed=9)
+        om = oracle.OracleMesh(nodes, cptr, cind)
+        rp, ci, v, rhs = _system(om)
+        sub = 512
+    n = len(rp) - 1
+    s = pg.SparseMatrixSolver(subdomain_rows=sub, precision=pg.MIXED
+                              if precision == "mixed" else pg.FP64)
+    s.setRank(n)
+    s.set(rp, ci, v)
+    part, nparts = s.partition()
+    assert nparts > 4
+    lu, rc = oracle.ilu0(rp, ci, v, part)
+    assert rc == 0
+    rng = np.random.default_rng(5)
+    tol = 1e-12 if precision == "fp64" else 2e-5
+    for r in (rng.standard_normal(n), -rhs):
+        z = s.apply_precond(r)
+        zo = oracle.ilu0_apply(rp, ci, lu, r, part)
+        assert np.all(np.isfinite(z))
+        assert np.linalg.norm(z - zo) / np.linalg.norm(zo) < tol
+
+
 def test_solver_accepts_crsequation_slots(case, pg, oracle):
     """set() receives CrsEquation's arrays with -1 placeholders
     (FiniteVolumeEquation.tpp:178)."""
@@ -318,10 +363,15 @@ def test_pattern_change_is_detected(pg):
         assert np.linalg.norm(b - A @ s.x()) / np.linalg.norm(b) <= 1.01e-10
 
 
-def test_rising_bubble_full_size_properties(pg, oracle):
+@pytest.mark.parametrize("precision,sub_rows",
+                         [("fp64", 0), ("mixed", 0), ("fp64", 2048),
+                          ("mixed", 512)])
+def test_rising_bubble_full_size_properties(pg, oracle, precision, sub_rows):
     """1024x1024 rising-bubble system: pattern bit-exact with the oracle,
     1000x coefficient contrast, and the device solve's true residual meets
-    1e-8 (size-independent properties; the full oracle solve is too slow)."""
+    1e-8 in FP64 and with FP32 ILU factors, for several Schwarz subdomain
+    sizes (size-independent properties; the full oracle solve is too
+    slow)."""
     nx = ny = 1024
     w = workloads.rising_bubble(nx, ny, seed=3)
     m = pg.Mesh(w["nodes"], w["cptr"], w["cind"])
@@ -336,7 +386,9 @@ def test_rising_bubble_full_size_properties(pg, oracle):
     om = oracle.OracleMesh(w["nodes"], w["cptr"], w["cind"])
     rpo, cio, vo, rhso = om.laplacian(coeff, w["bc_type"], w["bc_value"], w["u"])
     _check_rows(rp, ci, v, rhs, rpo, cio, vo, rhso)
-    s = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=5000)
+    s = pg.SparseMatrixSolver(
+        tolerance=1e-8, max_iters=8000, subdomain_rows=sub_rows,
+        precision=pg.MIXED if precision == "mixed" else pg.FP64)
     s.set_eqn(eqn)
     err = s.solve()
     assert s.stats.status == pg.PG_OK and err <= 1e-8
