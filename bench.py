@@ -256,20 +256,19 @@ def run_ours(args):
         ms = float(t[0])
 
     # kernel-level roofline on the same system: per-launch CUDA-event times
-    # of the hot kernels (SpMV and update are FP64 in both modes; the ILU(0)
-    # apply reads FP32 factors in the mixed mode)
+    # of the hot kernels (FP64 ones, or the float-float ones of the mixed
+    # solver; both move 8-byte values and vector entries)
     prof = solver.profile(reps=50)
     a_nnz = int(eqn.nnz)
-    fb = 8 if prec == pg.FP64 else 4
     # compulsory bytes per launch: A values + int32
-    # columns + row pointers; streamed ILU(0) factor values + uint16
-    # columns (off-diagonal entries of A bound the factor's) + 1/u_ii
+    # columns + row pointers; ILU(0) factor values + 2-byte columns
+    # (off-diagonal entries of A bound the factor's) + 1/u_ii
     b_spmv = 12 * a_nnz + 4 * (n + 1) + 3 * 8 * n          # A, x, rhat in; v out
-    b_prec = (fb + 2) * (a_nnz - n) + fb * n + 5 * 8 * n   # LU, dinv, r p v in, p z out
+    b_prec = 10 * (a_nnz - n) + 8 * n + 5 * 8 * n          # LU, dinv, r p v in, p z out
     b_upd = 9 * 8 * n                                      # x r ph sh s t rh in; x r out
-    ms_of = {"spmv": prof["spmv"],
-             "ilu_apply": prof["precond32" if prec == pg.MIXED else "precond"],
-             "update": prof["update"]}
+    sfx = "_dd" if prec == pg.MIXED else ""
+    ms_of = {"spmv": prof["spmv" + sfx], "ilu_apply": prof["precond" + sfx],
+             "update": prof["update" + sfx]}
     shares = {"spmv": 2 * ms_of["spmv"], "ilu_apply": 2 * ms_of["ilu_apply"],
               "update": ms_of["update"]}
     dom = max(shares, key=shares.get)
@@ -358,7 +357,7 @@ def run_ours(args):
             "n_gpus": world, "steps": args.steps, "warmup": max(3, args.warmup),
             "ms_per_step": round(ms, 3), "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype":
-                "f64" if prec == pg.FP64 else "f64 (f32 ILU factors)",
+                "f64" if prec == pg.FP64 else "f32x2 (float-float) + f64 residual",
             "converged": converged,
             "data": "synthetic (seeded rising-bubble fields, no dataset)",
             "config": {"workload": WORKLOAD, "n_cells": n, "nnz": a_nnz,

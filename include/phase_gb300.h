@@ -102,6 +102,28 @@ int pg_mesh_cells(const pg_mesh *m, double *cx, double *cy, double *vol);
  * ---------------------------------------------------------------------- */
 int pg_eqn_create(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
                   pg_eqn **out);
+/* Ghost-cell immersed-boundary pressure equation of FractionalStepGCIB
+ * (src/2D/Unstructured/Solvers/FractionalStepGCIB.cpp:44-46):
+ *   (fv::laplacian(gamma, p) + ib.bcs(p)) == src::div(u)
+ * for circles[3k..3k+2] = (cx, cy, r), k < n_circles.  Cells whose centroid
+ * is strictly inside a circle are IB cells when a face or node neighbour
+ * is outside it, else solid (GhostCellImmersedBoundary::updateCells,
+ * GhostCellImmersedBoundary.cpp:12-30); the Laplacian and the source run
+ * over the fluid cells; IB rows carry the bilinear image-point stencils of
+ * GhostCellImmersedBoundary::bcs (:32-74) for ib_bc PG_BC_FIXED or
+ * PG_BC_NORMAL_GRADIENT with value ib_ref, solid rows the identity.  The
+ * IB rows are built once on the host (they depend on geometry only) and
+ * the device assembly (pg_assemble_laplacian) fills the fluid rows.  The
+ * sum is CrsEquation::operator+ (CrsEquation.cpp:185-229), which drops
+ * exact zeros; here a fluid entry that assembles to exactly 0 keeps its
+ * slot.  Fails with PG_BAD_ARG when an image point's nearest node does not
+ * have four cells or a stencil matrix is singular. */
+int pg_eqn_create_gcib(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
+                       int n_circles, const double *circles, int ib_bc,
+                       double ib_ref, pg_eqn **out);
+/* Cell classes of a ghost-cell IB equation: 0 fluid, 1 IB, 2 solid (all 0
+ * for other equations).  cls[n_rows]. */
+int pg_eqn_cell_class(const pg_eqn *e, int32_t *cls);
 int pg_eqn_destroy(pg_eqn *e);
 int pg_eqn_sizes(const pg_eqn *e, int64_t *n_rows, int64_t *nnz);
 
@@ -290,6 +312,33 @@ int pg_solver_get_x(const pg_solver *s, double *x, int ptr_kind);
  * the FP32-factor apply (0 otherwise); ms[5..7] are reserved (0).  Leaves the
  * solver's state untouched.  (No reference counterpart: measurement.) */
 int pg_solver_profile(pg_solver *s, int reps, double *ms);
+
+/* ---------------------------------------------------------------------
+ * Batched solves: many independent pressure systems of uneven sizes
+ * (e.g. one per immersed-boundary case) solved together.  The reference
+ * solves them one FiniteVolumeEquation::solve() at a time
+ * (FiniteVolumeEquation.tpp:64-86); here they share one analysis, one
+ * ILU(0) factorisation launch and one CUDA graph launch for the whole
+ * BiCGStab iteration, with per-system scalars, convergence and statistics.
+ * FP64, Schwarz ILU(0) (the cfg's subdomain size applies per system), zero
+ * initial guess.  The tile shape of the row kernels is autotuned per batch
+ * pattern.
+ * --------------------------------------------------------------------- */
+typedef struct pg_batch pg_batch;
+int pg_batch_create(const pg_solver_cfg *cfg, pg_batch **out);
+int pg_batch_destroy(pg_batch *b);
+/* Device equations, one per system (values and -rhs_ are copied at this
+ * call; a new list of patterns triggers a new analysis and autotuning). */
+int pg_batch_set_eqns(pg_batch *b, int n_systems, const pg_eqn *const *eqns);
+/* stats[n_systems] (may be NULL); ms_total: device time of the batch solve
+ * (factorisation included).  Returns PG_OK when every system converged on
+ * its FP64 true residual, else the first failing status. */
+int pg_batch_solve(pg_batch *b, pg_solve_stats *stats, double *ms_total);
+/* solution of one system, in its own row order */
+int pg_batch_get_x(const pg_batch *b, int system, double *x, int ptr_kind);
+/* the autotuned tile shape: threads per CTA, rows per thread, tile count */
+int pg_batch_tuning(const pg_batch *b, int *block, int *rows_per_thread,
+                    int *n_tiles);
 
 /* Number of kernels the library has launched since it was loaded. */
 uint64_t pg_kernel_launches(void);

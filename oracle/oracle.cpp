@@ -47,6 +47,8 @@ struct or_mesh {
   // (face), each in face-id order (FiniteVolumeGrid2D::init :405-419)
   std::vector<std::vector<std::pair<int32_t, int32_t>>> nb;
   std::vector<std::vector<int32_t>> bd;
+  // Node::cells(): the cells of each node in creation order; cell nodes
+  std::vector<std::vector<int32_t>> node_cells, cell_nodes;
   int64_t n_interior = 0, n_boundary = 0;
 };
 
@@ -66,6 +68,8 @@ extern "C" or_mesh *or_mesh_create(const double *nodes_xy, int64_t n_nodes,
 
   m->centroid.resize(n_cells);
   m->volume.resize(n_cells);
+  m->node_cells.resize(n_nodes);
+  m->cell_nodes.resize(n_cells);
   std::map<std::pair<int64_t, int64_t>, int32_t> dir;  // faceDirectory_
 
   for (int64_t c = 0; c < n_cells; ++c) {
@@ -85,6 +89,10 @@ extern "C" or_mesh *or_mesh_create(const double *nodes_xy, int64_t n_nodes,
     m->centroid[c] = {sx / (3. * a2), sy / (3. * a2)};
 
     // FiniteVolumeGrid2D::createCell (FiniteVolumeGrid2D.cpp:84-114)
+    for (int64_t i = 0; i < k; ++i) {
+      m->node_cells[cind[b + i]].push_back((int32_t)c);
+      m->cell_nodes[c].push_back((int32_t)cind[b + i]);
+    }
     for (int64_t i = 0; i < k; ++i) {
       int64_t n1 = cind[b + i], n2 = cind[b + (i + 1) % k];
       auto key = n1 < n2 ? std::make_pair(n1, n2) : std::make_pair(n2, n1);
@@ -235,16 +243,18 @@ static void add_coeff(or_eqn &e, int32_t row, int32_t col, double val) {
   r.push_back({col, val});
 }
 
-extern "C" or_eqn *or_laplacian(const or_mesh *m, const double *gamma_face,
-                                double gamma_scalar, const int32_t *bc_type,
-                                const double *bc_value,
-                                const double *u_face_xy) {
+// fv::laplacian over the cells with mask[c] != 0 (all when mask is NULL)
+static or_eqn *laplacian_rows(const or_mesh *m, const double *gamma_face,
+                              double gamma_scalar, const int32_t *bc_type,
+                              const double *bc_value, const double *u_face_xy,
+                              const uint8_t *mask) {
   const int64_t n = (int64_t)m->centroid.size();
   auto *e = new or_eqn();
   e->rows.assign(n, std::vector<std::pair<int32_t, double>>(5, {-1, 0.}));
   e->rhs.assign(n, 0.);
 
   for (int32_t c = 0; c < (int32_t)n; ++c) {
+    if (mask && !mask[c]) continue;
     const V2 pc = m->centroid[c];
     for (auto &l : m->nb[c]) {
       const int32_t f = l.first, nbc = l.second;
@@ -282,6 +292,7 @@ extern "C" or_eqn *or_laplacian(const or_mesh *m, const double *gamma_face,
     // src::div(u) (Source.cpp:5-21), then operator==(Vector) -> rhs_ -= divU
     // (CrsEquation.cpp:432-435,459-461)
     for (int32_t c = 0; c < (int32_t)n; ++c) {
+      if (mask && !mask[c]) continue;
       const V2 pc = m->centroid[c];
       double d = 0.;
       for (auto &l : m->nb[c]) {
@@ -297,6 +308,14 @@ extern "C" or_eqn *or_laplacian(const or_mesh *m, const double *gamma_face,
     }
   }
   return e;
+}
+
+extern "C" or_eqn *or_laplacian(const or_mesh *m, const double *gamma_face,
+                                double gamma_scalar, const int32_t *bc_type,
+                                const double *bc_value,
+                                const double *u_face_xy) {
+  return laplacian_rows(m, gamma_face, gamma_scalar, bc_type, bc_value,
+                        u_face_xy, nullptr);
 }
 
 extern "C" void or_eqn_destroy(or_eqn *e) { delete e; }
@@ -984,4 +1003,177 @@ extern "C" or_eqn *or_momentum(const or_mesh *m, double dt, double nu,
   delete div;
   delete lap;
   return ddt;
+}
+
+// ---------------------------------------------------------------- GCIB
+namespace {
+
+// LU factorisation with partial pivoting followed by inversion, the
+// algorithm of LAPACK dgetrf + dgetri that StaticMatrix::invert calls
+// (src/Math/StaticMatrix.h:82-91); returns false for a singular matrix.
+static bool invert4(const double (&a_in)[4][4], double (&inv)[4][4]) {
+  double a[4][4];
+  int piv[4];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) a[i][j] = a_in[i][j];
+  for (int k = 0; k < 4; ++k) {
+    int p = k;
+    for (int i = k + 1; i < 4; ++i)
+      if (std::fabs(a[i][k]) > std::fabs(a[p][k])) p = i;
+    piv[k] = p;
+    if (a[p][k] == 0.) return false;
+    if (p != k)
+      for (int j = 0; j < 4; ++j) std::swap(a[k][j], a[p][j]);
+    for (int i = k + 1; i < 4; ++i) {
+      a[i][k] /= a[k][k];
+      for (int j = k + 1; j < 4; ++j) a[i][j] -= a[i][k] * a[k][j];
+    }
+  }
+  // solve A X = P^T I column by column: forward (unit L), backward (U)
+  double e[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
+  for (int k = 0; k < 4; ++k)
+    if (piv[k] != k)
+      for (int j = 0; j < 4; ++j) std::swap(e[k][j], e[piv[k]][j]);
+  for (int c = 0; c < 4; ++c) {
+    double y[4];
+    for (int i = 0; i < 4; ++i) {
+      double s = e[i][c];
+      for (int j = 0; j < i; ++j) s -= a[i][j] * y[j];
+      y[i] = s;
+    }
+    for (int i = 3; i >= 0; --i) {
+      double s = y[i];
+      for (int j = i + 1; j < 4; ++j) s -= a[i][j] * inv[j][c];
+      inv[i][c] = s / a[i][i];
+    }
+  }
+  return true;
+}
+
+static inline V2 unit(V2 v) {
+  const double m = std::sqrt(v.x * v.x + v.y * v.y);
+  return {v.x / m, v.y / m};
+}
+
+}  // namespace
+
+// Ghost-cell immersed-boundary pressure equation of FractionalStepGCIB
+// (src/2D/Unstructured/Solvers/FractionalStepGCIB.cpp:44-46):
+//   (fv::laplacian(gamma, p) + ib.bcs(p)) == src::div(u)
+// with the cell classes of GhostCellImmersedBoundary::updateCells
+// (GhostCellImmersedBoundary.cpp:12-30): a cell whose centroid is strictly
+// inside a circle (Circle::isInside) is an IB cell when one of its
+// cellLinks (face and node neighbours) is outside that circle
+// (ImmersedBoundaryObject.tpp internalPerimeterCells, includeDiagonals),
+// otherwise solid; the rest are fluid, and the Laplacian and the source
+// run over the fluid cells only.  bcs(p) (GhostCellImmersedBoundary.cpp:
+// 32-74) adds, per IB cell, the stencil of GhostCellImmersedBoundary
+// BcStencil (GhostCellImmersedBoundaryBcStencil.cpp:3-69): bp = nearest
+// point of the circle, ip = 2 bp - x_c, nw = unit(centre - bp), the four
+// cells of the node nearest to ip (FiniteVolumeGrid2D::findNearestNode,
+// Node::cells in creation order) and Ainv = inverse of the rows
+// [x y, x, y, 1] of their centroids; NORMAL_GRADIENT
+// (…NormalGradientBcStencil.cpp:17-40): [bp.y nx + bp.x ny, nx, ny, 0] Ainv
+// if the IB cell is one of the four, else -[ip.x ip.y, ip.x, ip.y, 1] Ainv/l
+// and 1/l on the cell itself (l = |ip - x_c|); FIXED (…FixedBcStencil.cpp:
+// 17-22): [ip.x ip.y, ip.x, ip.y, 1] Ainv / 2 and 1/2 on the cell; source
+// -ref.  Solid cells: identity row, source -ref (FIXED) or rhs 0.  The sum
+// is CrsEquation::operator+ (crs_plus above).  circles[3k..3k+2] = cx, cy, r.
+// Returns NULL when a stencil matrix is singular or a node has other than
+// four cells.
+extern "C" or_eqn *or_gcib_laplacian(const or_mesh *m, const double *gamma_face,
+                                     double gamma_scalar,
+                                     const int32_t *bc_type,
+                                     const double *bc_value,
+                                     const double *u_face_xy, int n_circles,
+                                     const double *circles, int ib_bc,
+                                     double ib_ref, int32_t *cell_class) {
+  const int32_t n = (int32_t)m->centroid.size();
+  std::vector<int32_t> cls(n, 0);  // 0 fluid, 1 IB, 2 solid
+  std::vector<std::vector<int32_t>> ibc(n_circles);
+  for (int k = 0; k < n_circles; ++k) {
+    const V2 cc{circles[3 * k], circles[3 * k + 1]};
+    const double r = circles[3 * k + 2];
+    auto inside = [&](int32_t c) { return mag_sqr(sub(m->centroid[c], cc)) < r * r; };
+    for (int32_t c = 0; c < n; ++c) {
+      if (cls[c] != 0 || !inside(c)) continue;
+      bool perimeter = false;
+      for (int32_t nd : m->cell_nodes[c])
+        for (int32_t o : m->node_cells[nd])
+          if (o != c && !inside(o)) perimeter = true;
+      cls[c] = perimeter ? 1 : 2;
+      if (perimeter) ibc[k].push_back(c);
+    }
+  }
+  std::vector<uint8_t> fluid(n);
+  for (int32_t c = 0; c < n; ++c) fluid[c] = cls[c] == 0;
+  or_eqn *lap = laplacian_rows(m, gamma_face, gamma_scalar, bc_type, bc_value,
+                               u_face_xy, fluid.data());
+  or_eqn bcs;
+  bcs.rows.assign(n, std::vector<std::pair<int32_t, double>>(5, {-1, 0.}));
+  bcs.rhs.assign(n, 0.);
+  for (int k = 0; k < n_circles; ++k) {
+    const V2 cc{circles[3 * k], circles[3 * k + 1]};
+    const double r = circles[3 * k + 2];
+    for (int32_t c : ibc[k]) {
+      const V2 xc = m->centroid[c];
+      const V2 u = unit(sub(xc, cc));
+      const V2 bp{u.x * r + cc.x, u.y * r + cc.y};
+      const V2 ip{2. * bp.x - xc.x, 2. * bp.y - xc.y};
+      const V2 nw = unit(sub(cc, bp));
+      // nearest node (first of equals in id order)
+      int32_t best = -1;
+      double bd = 0.;
+      for (int32_t v = 0; v < (int32_t)m->nodes.size(); ++v) {
+        const double d = mag_sqr(sub(m->nodes[v], ip));
+        if (best < 0 || d < bd) { best = v; bd = d; }
+      }
+      const auto &st = m->node_cells[best];
+      if (st.size() != 4) { delete lap; return nullptr; }
+      double A[4][4], Ai[4][4];
+      for (int i = 0; i < 4; ++i) {
+        const V2 x = m->centroid[st[i]];
+        A[i][0] = x.x * x.y; A[i][1] = x.x; A[i][2] = x.y; A[i][3] = 1.;
+      }
+      if (!invert4(A, Ai)) { delete lap; return nullptr; }
+      auto rowvec = [&](const double (&w)[4], double (&out)[4]) {
+        for (int j = 0; j < 4; ++j) {
+          double s = 0.;
+          for (int i = 0; i < 4; ++i) s += w[i] * Ai[i][j];
+          out[j] = s;
+        }
+      };
+      double co[4];
+      if (ib_bc == OR_FIXED) {
+        const double w[4] = {ip.x * ip.y, ip.x, ip.y, 1.};
+        rowvec(w, co);
+        for (int j = 0; j < 4; ++j) add_coeff(bcs, c, st[j], co[j] / 2.);
+        add_coeff(bcs, c, c, 0.5);
+      } else {
+        bool in_st = false;
+        for (int32_t o : st) in_st |= o == c;
+        if (in_st) {
+          const double w[4] = {bp.y * nw.x + bp.x * nw.y, nw.x, nw.y, 0.};
+          rowvec(w, co);
+          for (int j = 0; j < 4; ++j) add_coeff(bcs, c, st[j], co[j]);
+        } else {
+          const double l = std::sqrt(mag_sqr(sub(ip, xc)));
+          const double w[4] = {ip.x * ip.y, ip.x, ip.y, 1.};
+          rowvec(w, co);
+          for (int j = 0; j < 4; ++j) add_coeff(bcs, c, st[j], -co[j] / l);
+          add_coeff(bcs, c, c, 1. / l);
+        }
+      }
+      bcs.rhs[c] += -ib_ref;
+    }
+  }
+  for (int32_t c = 0; c < n; ++c) {
+    if (cls[c] != 2) continue;
+    add_coeff(bcs, c, c, 1.);
+    if (ib_bc == OR_FIXED) bcs.rhs[c] += -ib_ref;
+    else bcs.rhs[c] = 0.;
+  }
+  crs_plus(*lap, bcs, 1.);
+  if (cell_class) std::copy(cls.begin(), cls.end(), cell_class);
+  return lap;
 }

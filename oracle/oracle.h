@@ -154,6 +154,18 @@ void or_ilu0_apply(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
 or_eqn *or_momentum(const or_mesh *m, double dt, double nu, double theta,
                     const double *u_old_cell, const double *u_face,
                     const int32_t *bc_type);
+/* Ghost-cell immersed-boundary pressure equation
+ *   (fv::laplacian(gamma, p) + ib.bcs(p)) == src::div(u)
+ * (FractionalStepGCIB.cpp:44-46, GhostCellImmersedBoundary.cpp:12-74,
+ * GhostCellImmersedBoundary*BcStencil.cpp) for circles[3k..3k+2] =
+ * (cx, cy, r); ib_bc OR_FIXED or OR_NORMAL_GRADIENT with reference value
+ * ib_ref.  cell_class[n] (optional) receives 0 fluid, 1 IB, 2 solid.
+ * Returns NULL when a stencil is degenerate. */
+or_eqn *or_gcib_laplacian(const or_mesh *m, const double *gamma_face,
+                          double gamma_scalar, const int32_t *bc_type,
+                          const double *bc_value, const double *u_face_xy,
+                          int n_circles, const double *circles, int ib_bc,
+                          double ib_ref, int32_t *cell_class);
 /* y = A x */
 void or_spmv(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
              const double *vals, const double *x, double *y);

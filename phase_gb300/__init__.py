@@ -72,6 +72,8 @@ PROTOTYPES = {
     "pg_mesh_faces": (_I, [_P, _P, _P, _P, _P, _P, _P]),
     "pg_mesh_cells": (_I, [_P, _P, _P, _P]),
     "pg_eqn_create": (_I, [_P, _I, _P, ctypes.POINTER(_P)]),
+    "pg_eqn_create_gcib": (_I, [_P, _I, _P, _I, _P, _I, _D, ctypes.POINTER(_P)]),
+    "pg_eqn_cell_class": (_I, [_P, _P]),
     "pg_eqn_create_momentum": (_I, [_P, _P, ctypes.POINTER(_P)]),
     "pg_assemble_momentum": (_I, [_P, _D, _D, _D, _P, _P, _I]),
     "pg_interpolate_faces": (_I, [_P, _P, _P, _I]),
@@ -96,6 +98,13 @@ PROTOTYPES = {
     "pg_solver_partition": (_I, [_P, _P, ctypes.POINTER(_I)]),
     "pg_solver_profile": (_I, [_P, _I, _P]),
     "pg_solver_apply_precond": (_I, [_P, _P, _P, _I]),
+    "pg_batch_create": (_I, [_P, ctypes.POINTER(_P)]),
+    "pg_batch_destroy": (_I, [_P]),
+    "pg_batch_set_eqns": (_I, [_P, _I, _P]),
+    "pg_batch_solve": (_I, [_P, _P, ctypes.POINTER(_D)]),
+    "pg_batch_get_x": (_I, [_P, _I, _P, _I]),
+    "pg_batch_tuning": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I),
+                             ctypes.POINTER(_I)]),
     "pg_mpnn_create": (_I, [ctypes.c_uint64, ctypes.POINTER(_P)]),
     "pg_mpnn_destroy": (_I, [_P]),
     "pg_mpnn_num_params": (_I, [_P]),
@@ -238,12 +247,21 @@ class Mesh:
 class Equation:
     """Device FiniteVolumeEquation<Scalar> for one fv::laplacian overload."""
 
-    def __init__(self, mesh: Mesh, gamma_kind: int, bc_type):
+    def __init__(self, mesh: Mesh, gamma_kind: int, bc_type, ib_circles=None,
+                 ib_bc=NORMAL_GRADIENT, ib_ref=0.0):
+        """ib_circles [(cx, cy, r), ...] makes the ghost-cell immersed-boundary
+        pressure equation (fv::laplacian + ib.bcs) of FractionalStepGCIB."""
         self.mesh = mesh
         bc = _i32(bc_type, mesh.n_faces)
         h = _P()
-        _check(lib().pg_eqn_create(mesh._h, gamma_kind, _ptr(bc),
-                                   ctypes.byref(h)))
+        if ib_circles is None:
+            _check(lib().pg_eqn_create(mesh._h, gamma_kind, _ptr(bc),
+                                       ctypes.byref(h)))
+        else:
+            c = np.ascontiguousarray(np.asarray(ib_circles, np.float64).reshape(-1, 3))
+            _check(lib().pg_eqn_create_gcib(mesh._h, gamma_kind, _ptr(bc),
+                                            len(c), _ptr(c), int(ib_bc),
+                                            float(ib_ref), ctypes.byref(h)))
         self._h = h
         self.gamma_kind = gamma_kind
         s = np.zeros(2, np.int64)
@@ -273,6 +291,12 @@ class Equation:
             self._h, _P(gamma_face or None), gamma_scalar,
             _P(bc_value or None), _P(u_face or None), PG_DEVICE))
         return self
+
+    def cell_class(self):
+        """0 fluid, 1 IB, 2 solid per cell (all 0 without an IB)."""
+        out = np.empty(self.n, np.int32)
+        _check(lib().pg_eqn_cell_class(self._h, _ptr(out)))
+        return out
 
     def device_values(self):
         """(vals, rhs) device addresses of the assembled equation."""
@@ -424,7 +448,7 @@ class SparseMatrixSolver:
         return part, k.value
 
     def apply_precond(self, r):
-        """z = M^-1 r with the solver's preconditioner (FP32 ILU(0) factors
+        """z = M^-1 r with the solver's preconditioner (float-float sweeps
         under MIXED), in the caller's row order."""
         r = np.ascontiguousarray(r, np.float64)
         assert r.shape == (self.n,)
@@ -434,15 +458,60 @@ class SparseMatrixSolver:
 
     def profile(self, reps: int = 20):
         """Per-launch ms of the hot kernels on the current system: FP64 SpMV,
-        preconditioner apply, x/r update, ILU(0) factorisation, and the
-        FP32-factor ILU(0) apply of the mixed precision solver."""
+        preconditioner apply, x/r update, ILU(0) factorisation, and for the
+        mixed precision solver the float-float ILU(0) apply, SpMV and
+        update."""
         ms = np.zeros(8)
         _check(lib().pg_solver_profile(self._h, int(reps), _ptr(ms)))
         return dict(spmv=ms[0], precond=ms[1], update=ms[2], factor=ms[3],
-                    precond32=ms[4])
+                    precond_dd=ms[4], spmv_dd=ms[5], update_dd=ms[6])
 
     def printStatus(self, msg: str):
         print(f"{msg} iterations = {self.nIters()}, error = {self.error():f}.")
+
+
+class BatchSolver:
+    """Independent pressure systems solved together (pg_batch_*)."""
+
+    def __init__(self, **cfg):
+        c = default_cfg(**cfg)
+        h = _P()
+        _check(lib().pg_batch_create(ctypes.byref(c), ctypes.byref(h)))
+        self._h = h
+        self.eqns = []
+        self.stats = []
+        self.ms = 0.0
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.pg_batch_destroy(h)
+            self._h = None
+
+    def set_eqns(self, eqns):
+        self.eqns = list(eqns)
+        arr = (_P * len(self.eqns))(*[e._h for e in self.eqns])
+        _check(lib().pg_batch_set_eqns(self._h, len(self.eqns), arr))
+
+    def solve(self):
+        st = (SolveStats * len(self.eqns))()
+        ms = _D()
+        _check(lib().pg_batch_solve(self._h, st, ctypes.byref(ms)),
+               allow=(PG_OK, PG_MAX_ITERS, PG_BREAKDOWN, PG_NON_FINITE))
+        self.stats = list(st)
+        self.ms = ms.value
+        return self.stats
+
+    def x(self, i):
+        out = np.empty(self.eqns[i].n)
+        _check(lib().pg_batch_get_x(self._h, int(i), _ptr(out), PG_HOST))
+        return out
+
+    def tuning(self):
+        a, b, c = _I(), _I(), _I()
+        _check(lib().pg_batch_tuning(self._h, ctypes.byref(a), ctypes.byref(b),
+                                     ctypes.byref(c)))
+        return dict(block=a.value, rows_per_thread=b.value, n_tiles=c.value)
 
 
 @dataclass

@@ -221,7 +221,7 @@ static uint64_t next_pattern_id() {
 }
 
 static int eqn_create(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
-                      bool momentum, pg_eqn **out);
+                      bool momentum, pg_eqn **out, const GcibRows *ib = nullptr);
 
 extern "C" int pg_eqn_create(const pg_mesh *m, int gamma_kind,
                              const int32_t *bc_type, pg_eqn **out) {
@@ -234,7 +234,7 @@ extern "C" int pg_eqn_create_momentum(const pg_mesh *m, const int32_t *bc_type,
 }
 
 static int eqn_create(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
-                      bool momentum, pg_eqn **out) {
+                      bool momentum, pg_eqn **out, const GcibRows *ib) {
   PG_CHECK_ARG(out, "pg_eqn_create: out is NULL");
   *out = nullptr;
   PG_CHECK_ARG(m, "pg_eqn_create: NULL mesh");
@@ -252,7 +252,7 @@ static int eqn_create(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
   e->gamma_kind = gamma_kind;
   e->bc_type.assign(bc_type, bc_type + h.n_faces);
   e->momentum = momentum;
-  int rc = build_pattern(h, gamma_kind, bc_type, e->p, momentum);
+  int rc = build_pattern(h, gamma_kind, bc_type, e->p, momentum, ib);
   if (rc) {
     delete e;
     return rc;
@@ -265,8 +265,10 @@ static int eqn_create(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
       sry(nf);
   for (int64_t k = 0; k < nf; ++k) {
     const int32_t f = p.cface[k];
-    cl[k] = h.fl[f];
-    cr[k] = h.fr[f];
+    // a side whose cell is not fluid (ghost-cell IB) gets no Laplacian or
+    // source contribution: the kernels skip sides with cell -1
+    cl[k] = ib && ib->cls[h.fl[f]] != 0 ? -1 : h.fl[f];
+    cr[k] = ib && h.fr[f] >= 0 && ib->cls[h.fr[f]] != 0 ? -1 : h.fr[f];
     cbc[k] = h.fr[f] < 0 ? bc_type[f] : -1;
     dl[k] = m->dot_l[f];
     dr[k] = m->dot_r[f];
@@ -298,6 +300,21 @@ static int eqn_create(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
   up(e->csfr_x, srx);
   up(e->csfr_y, sry);
   up(e->diag, p.diag);
+  if (ib) {
+    // constant IB and solid rows: the assembly starts from these values
+    std::vector<double> bv(p.nnz, 0.);
+    for (int64_t c = 0; c < p.n; ++c)
+      for (const auto &en : ib->rows[c])
+        for (int32_t q = p.row_ptr[c]; q < p.row_ptr[c + 1]; ++q)
+          if (p.col_ind[q] == en.first) {
+            bv[q] = en.second;
+            break;
+          }
+    up(e->base_vals, bv);
+    up(e->base_rhs, ib->rhs);
+    e->cell_class = ib->cls;
+    e->has_base = true;
+  }
   if (ce == cudaSuccess) ce = e->vals.zero(p.nnz);
   if (ce == cudaSuccess) ce = e->rhs.zero(momentum ? 2 * p.n : p.n);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream());
@@ -306,6 +323,26 @@ static int eqn_create(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
     return cuda_fail(ce, "equation upload", __FILE__, __LINE__);
   }
   *out = e;
+  return PG_OK;
+}
+
+extern "C" int pg_eqn_create_gcib(const pg_mesh *m, int gamma_kind,
+                                  const int32_t *bc_type, int n_circles,
+                                  const double *circles, int ib_bc,
+                                  double ib_ref, pg_eqn **out) {
+  PG_CHECK_ARG(out, "pg_eqn_create_gcib: out is NULL");
+  *out = nullptr;
+  PG_CHECK_ARG(m, "pg_eqn_create_gcib: NULL mesh");
+  GcibRows g;
+  int rc = build_gcib(m->h, n_circles, circles, ib_bc, ib_ref, g);
+  if (rc) return rc;
+  return eqn_create(m, gamma_kind, bc_type, false, out, &g);
+}
+
+extern "C" int pg_eqn_cell_class(const pg_eqn *e, int32_t *cls) {
+  PG_CHECK_ARG(e && cls, "pg_eqn_cell_class: NULL arg");
+  for (int64_t c = 0; c < e->p.n; ++c)
+    cls[c] = e->cell_class.empty() ? 0 : e->cell_class[c];
   return PG_OK;
 }
 
@@ -343,8 +380,15 @@ extern "C" int pg_assemble_laplacian(pg_eqn *e, const double *gamma_face,
   if (!rc) rc = stage(u_face_xy, 2 * nf, ptr_kind, e->stage_c, &u);
   if (rc) return rc;
   cudaStream_t st = stream();
-  PG_CUDA(cudaMemsetAsync(e->vals.p, 0, e->p.nnz * sizeof(double), st));
-  PG_CUDA(cudaMemsetAsync(e->rhs.p, 0, e->p.n * sizeof(double), st));
+  if (e->has_base) {
+    PG_CUDA(cudaMemcpyAsync(e->vals.p, e->base_vals.p, e->p.nnz * sizeof(double),
+                            cudaMemcpyDeviceToDevice, st));
+    PG_CUDA(cudaMemcpyAsync(e->rhs.p, e->base_rhs.p, e->p.n * sizeof(double),
+                            cudaMemcpyDeviceToDevice, st));
+  } else {
+    PG_CUDA(cudaMemsetAsync(e->vals.p, 0, e->p.nnz * sizeof(double), st));
+    PG_CUDA(cudaMemsetAsync(e->rhs.p, 0, e->p.n * sizeof(double), st));
+  }
   const auto &cp = e->p.color_ptr;
   const int nic = e->p.n_interior_colors;
   for (int c = 0; c + 1 < (int)cp.size(); ++c) {

@@ -35,6 +35,14 @@ int build_host_mesh(const double *nodes_xy, int64_t n_nodes,
                  "pg_mesh_create: node index out of range");
 
   m.n_cells = n_cells;
+  m.node_x.resize(n_nodes);
+  m.node_y.resize(n_nodes);
+  for (int64_t i = 0; i < n_nodes; ++i) {
+    m.node_x[i] = nodes_xy[2 * i];
+    m.node_y[i] = nodes_xy[2 * i + 1];
+  }
+  m.cptr.assign(cptr, cptr + n_cells + 1);
+  m.cind.assign(cind, cind + cptr[n_cells]);
   m.cx.resize(n_cells);
   m.cy.resize(n_cells);
   m.vol.resize(n_cells);
@@ -148,7 +156,7 @@ int build_host_mesh(const double *nodes_xy, int64_t n_nodes,
 // diagonal first (:139-142); FIXED boundary links add the diagonal
 // (:66-69, :150-153).  Placeholders that stay empty are dropped.
 int build_pattern(const HostMesh &m, int gamma_kind, const int32_t *bc_type,
-                  EqnPattern &p, bool diag_first) {
+                  EqnPattern &p, bool diag_first, const GcibRows *extra) {
   const int64_t n = m.n_cells;
   p.n = n;
   p.row_ptr.assign(n + 1, 0);
@@ -169,8 +177,11 @@ int build_pattern(const HostMesh &m, int gamma_kind, const int32_t *bc_type,
   for (int64_t c = 0; c < n; ++c) {
     row.clear();
     if (diag_first) add((int32_t)c);  // fv::ddt's diagonal comes first
-    const int64_t b = m.link_ptr[c], e = m.link_ptr[c + 1];
+    const bool fluid = !extra || extra->cls[c] == 0;
+    const int64_t b = fluid ? m.link_ptr[c] : 0, e = fluid ? m.link_ptr[c + 1] : 0;
     const int64_t base = (int64_t)p.col_ind.size();
+    if (extra)  // CrsEquation::operator+ appends the IB row's entries
+      for (const auto &en : extra->rows[c]) add(en.first);
     for (int64_t k = b; k < e; ++k) {
       const int32_t f = m.link_face[k], nbc = m.link_cell[k];
       if (nbc >= 0) {
@@ -306,7 +317,8 @@ struct Bisector {
 }  // namespace
 
 int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
-            int subdomain_rows, Analysis &a) {
+            int subdomain_rows, Analysis &a,
+            const std::vector<int64_t> *sys_rows) {
   PG_CHECK_ARG(n > 0 && row_ptr && col_ind, "analyse: empty matrix");
   PG_CHECK_ARG(row_ptr[0] == 0, "row_ptr[0] must be 0");
   for (int64_t i = 0; i < n; ++i)
@@ -385,12 +397,22 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   std::vector<int32_t> order(n);
   std::iota(order.begin(), order.end(), 0);
   std::vector<std::pair<int64_t, int64_t>> parts;  // ranges of `order`
-  if (target < 0 || n <= target) {
+  if (!sys_rows && (target < 0 || n <= target)) {
     parts.push_back({0, n});
     a.global_ilu = (target < 0) || n <= target;
   } else {
+    if (target < 0) target = INT32_MAX;
     Bisector bs(n, ap, aj);
     std::vector<std::pair<int64_t, int64_t>> stack{{0, n}};
+    if (sys_rows) {  // one root range per system, popped in system order
+      PG_CHECK_ARG(sys_rows->size() >= 2 && sys_rows->front() == 0 &&
+                       sys_rows->back() == n,
+                   "analyse: bad system row offsets");
+      stack.clear();
+      for (size_t k = sys_rows->size() - 1; k-- > 0;)
+        if ((*sys_rows)[k + 1] > (*sys_rows)[k])
+          stack.push_back({(*sys_rows)[k], (*sys_rows)[k + 1]});
+    }
     while (!stack.empty()) {
       auto [lo, hi] = stack.back();
       stack.pop_back();
@@ -530,8 +552,7 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
                "subdomains for larger systems)");
   auto al16 = [](int64_t b) { return (b + 15) & ~(int64_t)15; };
   a.meta64.resize(a.n_sub);
-  a.meta32.resize(a.n_sub);
-  int64_t off64 = 0, off32 = 0, slots = 0;
+  int64_t off64 = 0, slots = 0;
   a.max_kl = a.max_ku = 0;
   for (int s = 0; s < a.n_sub; ++s) {
     const int32_t r0 = a.sub_ptr[s], r1 = a.sub_ptr[s + 1], nr = r1 - r0;
@@ -547,29 +568,23 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
     // lvl[] carries one sentinel past the last level bound
     const int64_t col_off = al16(2 * (int64_t)(nlev + 2));
     const int64_t val_off = col_off + al16(2 * (int64_t)nr * K);
-    for (int pass = 0; pass < 2; ++pass) {
-      const int64_t vsz = pass == 0 ? 8 : 4;
-      const int64_t bytes = val_off + al16(vsz * (int64_t)nr * (K + 1));
-      int64_t &off = pass == 0 ? off64 : off32;
-      PG_CHECK_ARG(off + bytes < ((int64_t)1 << 31), "ILU(0) records too large");
-      SubMeta m{r0, nr, nlev, K, kl, (int32_t)off, (int32_t)col_off,
-                (int32_t)val_off, (int32_t)bytes, (int32_t)slots, 0, 0};
-      (pass == 0 ? a.meta64 : a.meta32)[s] = m;
-      off += bytes;
-    }
+    const int64_t bytes = val_off + al16(8 * (int64_t)nr * (K + 1));
+    PG_CHECK_ARG(off64 + bytes < ((int64_t)1 << 31), "ILU(0) records too large");
+    a.meta64[s] = SubMeta{r0, nr, nlev, K, kl, (int32_t)off64, (int32_t)col_off,
+                          (int32_t)val_off, (int32_t)bytes, (int32_t)slots, 0, 0};
+    off64 += bytes;
     slots += (int64_t)nr * (K + 1);
   }
   PG_CHECK_ARG(slots < ((int64_t)1 << 31), "ILU(0) factor too large");
   a.rec64.assign(off64, 0);
-  a.rec32.assign(off32, 0);
   a.rec_src.assign(slots, -1);
-  a.smem64 = a.smem32 = 0;
+  a.smem64 = 0;
   for (int s = 0; s < a.n_sub; ++s) {
     const SubMeta &m = a.meta64[s];
     const int K = m.K, kl = m.KL, nr = m.nr;
-    for (int pass = 0; pass < 2; ++pass) {
-      const SubMeta &mm = pass == 0 ? a.meta64[s] : a.meta32[s];
-      uint8_t *base = (pass == 0 ? a.rec64 : a.rec32).data() + mm.rec_off;
+    {
+      const SubMeta &mm = m;
+      uint8_t *base = a.rec64.data() + mm.rec_off;
       uint16_t *lvl = reinterpret_cast<uint16_t *>(base);
       for (int l = 0; l <= m.nlev; ++l)
         lvl[l] = (uint16_t)(a.lvl_ptr[a.sub_lvl[s] + l] - m.r0);
@@ -583,18 +598,13 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
           cols[(int64_t)k * nr + i] = (uint16_t)a.lci[a.lrp[g] + k];
         for (int k = 0; k < nu; ++k)
           cols[(int64_t)(kl + k) * nr + i] = (uint16_t)a.lci[a.ldg[g] + 1 + k];
-        if (pass == 0) {
-          int32_t *src = a.rec_src.data() + m.slot_base;
-          for (int k = 0; k < nl; ++k) src[(int64_t)k * nr + i] = a.lsrc[a.lrp[g] + k];
-          for (int k = 0; k < nu; ++k)
-            src[(int64_t)(kl + k) * nr + i] = a.lsrc[a.ldg[g] + 1 + k];
-          src[(int64_t)K * nr + i] = a.lsrc[a.ldg[g]];
-        }
+        int32_t *src = a.rec_src.data() + m.slot_base;
+        for (int k = 0; k < nl; ++k) src[(int64_t)k * nr + i] = a.lsrc[a.lrp[g] + k];
+        for (int k = 0; k < nu; ++k)
+          src[(int64_t)(kl + k) * nr + i] = a.lsrc[a.ldg[g] + 1 + k];
+        src[(int64_t)K * nr + i] = a.lsrc[a.ldg[g]];
       }
-      const size_t sm = (size_t)al16(mm.rec_bytes) +
-                        (size_t)nr * (pass == 0 ? 8 : 4);
-      size_t &mx = pass == 0 ? a.smem64 : a.smem32;
-      mx = std::max(mx, sm);
+      a.smem64 = std::max(a.smem64, (size_t)al16(mm.rec_bytes) + (size_t)nr * 8);
     }
   }
 
@@ -604,16 +614,11 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   //    of about kStreamPiece bytes.  pack_* map every value position of a
   //    stream to its slot in the FP64 factor records.
   a.smeta64.resize(a.n_sub);
-  a.smeta32.resize(a.n_sub);
   a.pack_src.clear();
-  a.pack_src32.clear();
   a.pack_dst64.clear();
-  a.pack_dst32.clear();
-  a.ssmem64 = a.ssmem32 = 0;
-  int64_t soff[2] = {0, 0};
-  std::vector<uint8_t> *sbuf[2] = {&a.srec64, &a.srec32};
+  a.ssmem64 = 0;
+  int64_t soff = 0;
   a.srec64.clear();
-  a.srec32.clear();
   // one slot count for all subdomains, matching the apply kernel's
   // compile-time variants (2/2 quadrilaterals, 3/3 triangles)
   int KLs = a.max_kl, KUs = a.max_ku;
@@ -627,8 +632,8 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
     const uint16_t *flvl = reinterpret_cast<const uint16_t *>(a.rec64.data() + f.rec_off);
     const uint16_t *fcols =
         reinterpret_cast<const uint16_t *>(a.rec64.data() + f.rec_off + f.col_off);
-    for (int pass = 0; pass < 2; ++pass) {
-      const int64_t vs = pass == 0 ? 8 : 4;
+    {
+      const int64_t vs = 8;
       auto fblob = [&](int w) { return al16(2 * (int64_t)KL * w) + al16(vs * (int64_t)KL * w); };
       auto bblob = [&](int w) {
         return al16(2 * (int64_t)KU * w) + al16(vs * (int64_t)KU * w) + al16(vs * (int64_t)w);
@@ -653,13 +658,12 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       int64_t total = hdr, max_piece = 16;
       for (auto &q : fp) total += q.second, max_piece = std::max(max_piece, q.second);
       for (auto &q : bp) total += q.second, max_piece = std::max(max_piece, q.second);
-      PG_CHECK_ARG(soff[pass] + total < ((int64_t)1 << 31), "ILU(0) stream too large");
-      StreamMeta sm{f.r0, nr, nlev, KL, KU, (int32_t)soff[pass], (int32_t)hdr,
-                    (int32_t)max_piece};
-      (pass == 0 ? a.smeta64 : a.smeta32)[s] = sm;
-      std::vector<uint8_t> &buf = *sbuf[pass];
-      buf.resize(soff[pass] + total, 0);
-      uint8_t *base = buf.data() + soff[pass];
+      PG_CHECK_ARG(soff + total < ((int64_t)1 << 31), "ILU(0) stream too large");
+      a.smeta64[s] = StreamMeta{f.r0, nr, nlev, KL, KU, (int32_t)soff,
+                                (int32_t)hdr, (int32_t)max_piece};
+      std::vector<uint8_t> &buf = a.srec64;
+      buf.resize(soff + total, 0);
+      uint8_t *base = buf.data() + soff;
       std::memcpy(base, flvl, 2 * (size_t)(nlev + 2));
       int32_t *ints = reinterpret_cast<int32_t *>(base + lvl_bytes);
       ints[0] = (int32_t)fp.size();
@@ -667,9 +671,8 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       int64_t off = hdr;
       auto emit_values = [&](int64_t byte_off, int64_t slot) {
         // byte_off is relative to this record; slot indexes the factor
-        const int64_t dst = (soff[pass] + byte_off) / vs;
-        (pass == 0 ? a.pack_src : a.pack_src32).push_back((int32_t)(fsrc0 + slot));
-        (pass == 0 ? a.pack_dst64 : a.pack_dst32).push_back((int32_t)dst);
+        a.pack_src.push_back((int32_t)(fsrc0 + slot));
+        a.pack_dst64.push_back((int32_t)((soff + byte_off) / vs));
       };
       int t = 0;
       for (size_t q = 0; q < fp.size(); ++q, ++t) {
@@ -716,24 +719,27 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
           off += bblob(w);
         }
       }
-      soff[pass] += total;
+      soff += total;
       const size_t need = (size_t)hdr + 2 * (size_t)max_piece + (size_t)al16(vs * (int64_t)(nr + 1));
-      size_t &mx = pass == 0 ? a.ssmem64 : a.ssmem32;
-      mx = std::max(mx, need);
+      a.ssmem64 = std::max(a.ssmem64, need);
     }
   }
 
-  // 9. step streams: when no row has more than 3 L or 3 U entries, the FP32
-  //    stream uses warp-wide steps (kernels.cuh StepMeta) instead of level
-  //    blobs (the FP64 sweep stays on the blobs, where it is faster)
+  // 9. step stream for the float-float sweep of the mixed-precision solver
+  //    (kernels.cuh StepMeta), when no row has more than 3 L or 3 U
+  //    entries: warp-wide slices of a level with byte offsets into the
+  //    subdomain's 8-byte z entries and {w0, w1, w2, 1/u_ii} as float pairs
   a.use_steps = a.max_kl <= 3 && a.max_ku <= 3 && a.max_sub_rows < 32767;
+  a.tmeta_dd.clear();
+  a.pack_src_dd.clear();
+  a.pack_dst_dd.clear();
+  a.srec_dd.clear();
+  a.ssmem_dd = 0;
   if (a.use_steps) {
-    a.tmeta32.resize(a.n_sub);
-    a.pack_src32.clear();
-    a.pack_dst32.clear();
-    a.srec32.clear();
-    a.ssmem32 = 0;
-    int64_t toff[2] = {0, 0};
+    constexpr int64_t es = 8;  // bytes of a z entry and of a float pair
+    constexpr int64_t sb = kStepIdxBytes + 32 * 4 * es;
+    a.tmeta_dd.resize(a.n_sub);
+    int64_t toff = 0;
     for (int s = 0; s < a.n_sub; ++s) {
       const SubMeta &f = a.meta64[s];
       const int nr = f.nr, nlev = f.nlev, fKL = f.KL, fKU = f.K - f.KL;
@@ -741,59 +747,268 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       const uint16_t *flvl = reinterpret_cast<const uint16_t *>(a.rec64.data() + f.rec_off);
       const uint16_t *fcols =
           reinterpret_cast<const uint16_t *>(a.rec64.data() + f.rec_off + f.col_off);
-      int n_fwd = 0, n_bwd = 0;
+      int n_fwd = 0;
       for (int l = 0; l < nlev; ++l) n_fwd += (flvl[l + 1] - flvl[l] + 31) / 32;
-      n_bwd = n_fwd;
-      for (int pass = 1; pass < 2; ++pass) {
-        const int64_t vs = 4;
-        const int64_t sb = 32 * 16 + 32 * 4 * vs;
-        const int64_t bytes = (int64_t)(n_fwd + n_bwd) * sb;
-        PG_CHECK_ARG(toff[pass] + bytes < ((int64_t)1 << 31), "ILU(0) steps too large");
-        StepMeta tm{f.r0, nr, n_fwd, n_bwd, (int32_t)toff[pass], 0, 0, 0};
-        a.tmeta32[s] = tm;
-        std::vector<uint8_t> &buf = a.srec32;
-        buf.resize(toff[pass] + bytes, 0);
-        uint8_t *base = buf.data() + toff[pass];
-        int64_t step = 0;
-        auto emit = [&](int64_t byte_off, int64_t slot) {
-          a.pack_src32.push_back((int32_t)(fsrc0 + slot));
-          a.pack_dst32.push_back((int32_t)((toff[pass] + byte_off) / vs));
-        };
-        for (int dir = 0; dir < 2; ++dir) {
-          const int k0 = dir == 0 ? 0 : fKL, kn = dir == 0 ? fKL : fKU;
-          for (int li = 0; li < nlev; ++li) {
-            const int l = dir == 0 ? li : nlev - 1 - li;
-            for (int c0 = flvl[l]; c0 < flvl[l + 1]; c0 += 32, ++step) {
-              uint8_t *sp = base + step * sb;
-              uint32_t *idx = reinterpret_cast<uint32_t *>(sp);
-              const uint32_t pad = (uint32_t)(nr * vs);
-              for (int t = 0; t < 32; ++t) {
-                const int row = c0 + t;
-                uint32_t *e = idx + 4 * t;
-                e[0] = e[1] = e[2] = e[3] = pad;
-                if (row >= flvl[l + 1]) continue;
-                e[0] = (uint32_t)(row * vs);
-                for (int k = 0; k < kn; ++k) {
-                  const int64_t slot = (int64_t)(k0 + k) * nr + row;
-                  if (fcols[slot] == kPadCol) continue;
-                  e[1 + k] = (uint32_t)(fcols[slot] * vs);
-                  emit(step * sb + 512 + vs * (4 * t + k), slot);
-                }
-                if (dir == 1)
-                  emit(step * sb + 512 + vs * (4 * t + 3),
-                       (int64_t)(fKL + fKU) * nr + row);
+      const int n_bwd = n_fwd;
+      const int64_t bytes = (int64_t)(n_fwd + n_bwd) * sb;
+      PG_CHECK_ARG(toff + bytes < ((int64_t)1 << 31), "ILU(0) steps too large");
+      a.tmeta_dd[s] = StepMeta{f.r0, nr, n_fwd, n_bwd, (int32_t)toff, 0, 0, 0};
+      a.srec_dd.resize(toff + bytes, 0);
+      uint8_t *base = a.srec_dd.data() + toff;
+      int64_t step = 0;
+      auto emit = [&](int64_t byte_off, int64_t slot) {
+        a.pack_src_dd.push_back((int32_t)(fsrc0 + slot));
+        a.pack_dst_dd.push_back((int32_t)((toff + byte_off) / es));
+      };
+      for (int dir = 0; dir < 2; ++dir) {
+        const int k0 = dir == 0 ? 0 : fKL, kn = dir == 0 ? fKL : fKU;
+        for (int li = 0; li < nlev; ++li) {
+          const int l = dir == 0 ? li : nlev - 1 - li;
+          for (int c0 = flvl[l]; c0 < flvl[l + 1]; c0 += 32, ++step) {
+            uint32_t *idx = reinterpret_cast<uint32_t *>(base + step * sb);
+            const uint32_t pad = (uint32_t)(nr * es);  // z[nr] == 0
+            for (int t = 0; t < 32; ++t) {
+              const int row = c0 + t;
+              uint32_t *e = idx + 4 * t;
+              e[0] = e[1] = e[2] = e[3] = pad;
+              if (row >= flvl[l + 1]) continue;
+              e[0] = (uint32_t)(row * es);
+              for (int k = 0; k < kn; ++k) {
+                const int64_t slot = (int64_t)(k0 + k) * nr + row;
+                if (fcols[slot] == kPadCol) continue;
+                e[1 + k] = (uint32_t)(fcols[slot] * es);
+                emit(step * sb + kStepIdxBytes + es * (4 * t + k), slot);
               }
+              if (dir == 1)
+                emit(step * sb + kStepIdxBytes + es * (4 * t + 3),
+                     (int64_t)(fKL + fKU) * nr + row);
             }
           }
         }
-        toff[pass] += bytes;
-        const size_t need = 2 * (size_t)kStepsPerPiece * sb +
-                            (size_t)al16(vs * (int64_t)(nr + 1));
-        a.ssmem32 = std::max(a.ssmem32, need);
       }
+      toff += bytes;
+      const size_t need = 2 * (size_t)kStepsPerPiece * sb +
+                          (size_t)al16(es * (int64_t)(nr + 1));
+      a.ssmem_dd = std::max(a.ssmem_dd, need);
     }
   }
   return PG_OK;
 }
 
+
+// ---------------------------------------------------------------- GCIB
+namespace {
+
+// inverse of a 4x4 matrix by Gauss-Jordan elimination with partial
+// pivoting on the augmented matrix [A | I]; false if singular
+bool inverse4(const double (&a)[4][4], double (&out)[4][4]) {
+  double w[4][8];
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 8; ++j) w[i][j] = j < 4 ? a[i][j] : (j - 4 == i ? 1. : 0.);
+  for (int k = 0; k < 4; ++k) {
+    int p = k;
+    for (int i = k + 1; i < 4; ++i)
+      if (std::fabs(w[i][k]) > std::fabs(w[p][k])) p = i;
+    if (w[p][k] == 0.) return false;
+    if (p != k)
+      for (int j = 0; j < 8; ++j) std::swap(w[p][j], w[k][j]);
+    const double piv = w[k][k];
+    for (int j = 0; j < 8; ++j) w[k][j] /= piv;
+    for (int i = 0; i < 4; ++i) {
+      if (i == k) continue;
+      const double f = w[i][k];
+      for (int j = 0; j < 8; ++j) w[i][j] -= f * w[k][j];
+    }
+  }
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) out[i][j] = w[i][4 + j];
+  return true;
+}
+
+// uniform bucket grid over the mesh nodes for nearest-node queries
+struct NodeGrid {
+  double x0 = 0., y0 = 0., h = 1.;
+  int nx = 1, ny = 1;
+  std::vector<int32_t> start, items;
+  const HostMesh *m = nullptr;
+  void build(const HostMesh &mesh) {
+    m = &mesh;
+    const int64_t nn = (int64_t)mesh.node_x.size();
+    double x1 = mesh.node_x[0], y1 = mesh.node_y[0];
+    x0 = x1;
+    y0 = y1;
+    for (int64_t i = 0; i < nn; ++i) {
+      x0 = std::min(x0, mesh.node_x[i]);
+      y0 = std::min(y0, mesh.node_y[i]);
+      x1 = std::max(x1, mesh.node_x[i]);
+      y1 = std::max(y1, mesh.node_y[i]);
+    }
+    const double w = std::max(x1 - x0, 1e-300), hh = std::max(y1 - y0, 1e-300);
+    h = std::sqrt(w * hh / (double)std::max<int64_t>(nn, 1)) * 2.;
+    nx = std::max(1, (int)std::min(1e6, std::ceil(w / h)));
+    ny = std::max(1, (int)std::min(1e6, std::ceil(hh / h)));
+    std::vector<int32_t> cnt((size_t)nx * ny + 1, 0);
+    auto bucket = [&](int64_t i) { return cell_of(mesh.node_x[i], mesh.node_y[i]); };
+    for (int64_t i = 0; i < nn; ++i) ++cnt[bucket(i) + 1];
+    for (size_t b = 1; b < cnt.size(); ++b) cnt[b] += cnt[b - 1];
+    start = cnt;
+    items.resize(nn);
+    for (int64_t i = 0; i < nn; ++i) items[cnt[bucket(i)]++] = (int32_t)i;
+  }
+  int64_t cell_of(double x, double y) const {
+    int ix = (int)std::floor((x - x0) / h), iy = (int)std::floor((y - y0) / h);
+    ix = std::min(std::max(ix, 0), nx - 1);
+    iy = std::min(std::max(iy, 0), ny - 1);
+    return (int64_t)iy * nx + ix;
+  }
+  // nearest node (smallest squared distance, then smallest id)
+  int32_t nearest(double x, double y) const {
+    const int64_t c = cell_of(x, y);
+    const int cx = (int)(c % nx), cy = (int)(c / nx);
+    int32_t best = -1;
+    double bd = 0.;
+    for (int ring = 0;; ++ring) {
+      for (int iy = cy - ring; iy <= cy + ring; ++iy) {
+        if (iy < 0 || iy >= ny) continue;
+        for (int ix = cx - ring; ix <= cx + ring; ++ix) {
+          if (ix < 0 || ix >= nx) continue;
+          if (std::max(std::abs(ix - cx), std::abs(iy - cy)) != ring) continue;
+          const int64_t b = (int64_t)iy * nx + ix;
+          for (int32_t k = start[b]; k < start[b + 1]; ++k) {
+            const int32_t v = items[k];
+            const double dx = m->node_x[v] - x, dy = m->node_y[v] - y;
+            const double d = dx * dx + dy * dy;
+            if (best < 0 || d < bd || (d == bd && v < best)) {
+              best = v;
+              bd = d;
+            }
+          }
+        }
+      }
+      // every node outside the searched square is farther than ring * h
+      // from the query point's bucket edge
+      if (best >= 0 && (double)ring * h >= std::sqrt(bd)) return best;
+      if (ring > nx + ny) return best;
+    }
+  }
+};
+
+}  // namespace
+
+int build_gcib(const HostMesh &m, int n_circles, const double *circles,
+               int ib_bc, double ib_ref, GcibRows &g) {
+  PG_CHECK_ARG(n_circles >= 0 && (n_circles == 0 || circles),
+               "pg_eqn_create_gcib: bad circles");
+  PG_CHECK_ARG(ib_bc == PG_BC_FIXED || ib_bc == PG_BC_NORMAL_GRADIENT,
+               "pg_eqn_create_gcib: IB boundary type must be FIXED or "
+               "NORMAL_GRADIENT");
+  const int64_t n = m.n_cells, nn = (int64_t)m.node_x.size();
+  // node -> cells in creation order
+  std::vector<int64_t> nptr(nn + 1, 0);
+  for (int64_t k = 0; k < (int64_t)m.cind.size(); ++k) ++nptr[m.cind[k] + 1];
+  for (int64_t i = 0; i < nn; ++i) nptr[i + 1] += nptr[i];
+  std::vector<int32_t> ncell(m.cind.size());
+  {
+    std::vector<int64_t> fill(nptr.begin(), nptr.end() - 1);
+    for (int64_t c = 0; c < n; ++c)
+      for (int64_t k = m.cptr[c]; k < m.cptr[c + 1]; ++k)
+        ncell[fill[m.cind[k]]++] = (int32_t)c;
+  }
+  g.cls.assign(n, 0);
+  g.rows.assign(n, {});
+  g.rhs.assign(n, 0.);
+  NodeGrid grid;
+  grid.build(m);
+  auto add = [&](int64_t row, int32_t col, double v) {
+    for (auto &e : g.rows[row])
+      if (e.first == col) {
+        e.second += v;
+        return;
+      }
+    g.rows[row].push_back({col, v});
+  };
+  for (int k = 0; k < n_circles; ++k) {
+    const double ccx = circles[3 * k], ccy = circles[3 * k + 1], r = circles[3 * k + 2];
+    PG_CHECK_ARG(r > 0., "pg_eqn_create_gcib: circle radius must be positive");
+    auto inside = [&](int64_t c) {
+      const double dx = m.cx[c] - ccx, dy = m.cy[c] - ccy;
+      return dx * dx + dy * dy < r * r;
+    };
+    std::vector<int32_t> ib;
+    for (int64_t c = 0; c < n; ++c) {
+      if (g.cls[c] != 0 || !inside(c)) continue;
+      bool perimeter = false;
+      for (int64_t q = m.cptr[c]; q < m.cptr[c + 1] && !perimeter; ++q) {
+        const int64_t v = m.cind[q];
+        for (int64_t t = nptr[v]; t < nptr[v + 1]; ++t)
+          if (ncell[t] != c && !inside(ncell[t])) {
+            perimeter = true;
+            break;
+          }
+      }
+      g.cls[c] = perimeter ? 1 : 2;
+      if (perimeter) ib.push_back((int32_t)c);
+    }
+    for (int32_t c : ib) {
+      const double xc = m.cx[c], yc = m.cy[c];
+      const double dx = xc - ccx, dy = yc - ccy, dm = std::sqrt(dx * dx + dy * dy);
+      const double bpx = dx / dm * r + ccx, bpy = dy / dm * r + ccy;
+      const double ipx = 2. * bpx - xc, ipy = 2. * bpy - yc;
+      const double tx = ccx - bpx, ty = ccy - bpy, tm = std::sqrt(tx * tx + ty * ty);
+      const double nwx = tx / tm, nwy = ty / tm;
+      const int32_t node = grid.nearest(ipx, ipy);
+      PG_CHECK_ARG(node >= 0 && nptr[node + 1] - nptr[node] == 4,
+                   "pg_eqn_create_gcib: the node nearest to an image point "
+                   "does not have four cells");
+      const int32_t *st = ncell.data() + nptr[node];
+      double A[4][4], Ai[4][4];
+      for (int i = 0; i < 4; ++i) {
+        const double x = m.cx[st[i]], y = m.cy[st[i]];
+        A[i][0] = x * y;
+        A[i][1] = x;
+        A[i][2] = y;
+        A[i][3] = 1.;
+      }
+      PG_CHECK_ARG(inverse4(A, Ai), "pg_eqn_create_gcib: singular IB stencil");
+      auto times_ainv = [&](const double (&w)[4], double (&o)[4]) {
+        for (int j = 0; j < 4; ++j)
+          o[j] = w[0] * Ai[0][j] + w[1] * Ai[1][j] + w[2] * Ai[2][j] + w[3] * Ai[3][j];
+      };
+      double co[4];
+      if (ib_bc == PG_BC_FIXED) {
+        const double w[4] = {ipx * ipy, ipx, ipy, 1.};
+        times_ainv(w, co);
+        for (int j = 0; j < 4; ++j) add(c, st[j], co[j] / 2.);
+        add(c, c, 0.5);
+      } else {
+        const bool self = st[0] == c || st[1] == c || st[2] == c || st[3] == c;
+        if (self) {
+          const double w[4] = {bpy * nwx + bpx * nwy, nwx, nwy, 0.};
+          times_ainv(w, co);
+          for (int j = 0; j < 4; ++j) add(c, st[j], co[j]);
+        } else {
+          const double lx = ipx - xc, ly = ipy - yc, l = std::sqrt(lx * lx + ly * ly);
+          const double w[4] = {ipx * ipy, ipx, ipy, 1.};
+          times_ainv(w, co);
+          for (int j = 0; j < 4; ++j) add(c, st[j], -co[j] / l);
+          add(c, c, 1. / l);
+        }
+      }
+      g.rhs[c] += -ib_ref;
+    }
+  }
+  for (int64_t c = 0; c < n; ++c) {
+    if (g.cls[c] != 2) continue;
+    add(c, (int32_t)c, 1.);
+    g.rhs[c] = ib_bc == PG_BC_FIXED ? -ib_ref : 0.;
+  }
+  // CrsEquation::operator+ keeps only non-zero entries
+  for (auto &row : g.rows) {
+    std::vector<std::pair<int32_t, double>> kept;
+    for (auto &e : row)
+      if (e.second != 0.) kept.push_back(e);
+    row.swap(kept);
+  }
+  return PG_OK;
+}
 }  // namespace pg

@@ -16,6 +16,7 @@
 #include <cstdint>
 
 #include "../../include/phase_gb300.h"
+#include "dd.cuh"
 #include "kernels.cuh"
 
 namespace pg {
@@ -136,20 +137,6 @@ __global__ void k_ilu0_factor(const SubMeta *__restrict__ meta,
   }
 }
 
-// FP32 copy of the factor values (the FP32 records' static parts are set up
-// once on the host).
-__global__ void k_factor_to_fp32(const SubMeta *__restrict__ m64,
-                                 const uint8_t *__restrict__ rec64,
-                                 const SubMeta *__restrict__ m32,
-                                 uint8_t *__restrict__ rec32) {
-  const SubMeta a = m64[blockIdx.x], b = m32[blockIdx.x];
-  const double *src =
-      reinterpret_cast<const double *>(rec64 + a.rec_off + a.val_off);
-  float *dst = reinterpret_cast<float *>(rec32 + b.rec_off + b.val_off);
-  const int n = a.nr * (a.K + 1);
-  for (int j = threadIdx.x; j < n; j += blockDim.x) dst[j] = (float)src[j];
-}
-
 // One level of a sweep: rows a .. a+w-1, slot-major columns cc and values vv
 // (KS slots, compile-time when KT > 0), optional 1/u_ii dd.
 template <class VT, class MT, int KT>
@@ -179,8 +166,12 @@ __global__ void __launch_bounds__(32)
 k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
                     const uint8_t *__restrict__ rec, const VT *__restrict__ r,
                     VT *__restrict__ pv, const VT *__restrict__ v,
-                    VT *__restrict__ z, const KScalars *__restrict__ sc,
+                    VT *__restrict__ z, const KScalars *__restrict__ sc_base,
+                    const int32_t *__restrict__ sub_sys,
                     int *__restrict__ err) {
+  // batched solves: the scalars of this subdomain's system
+  const KScalars *sc =
+      sc_base && sub_sys ? sc_base + sub_sys[blockIdx.x] : sc_base;
   if (sc && sc->done) return;
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ __align__(8) uint64_t bar[3];
@@ -270,24 +261,22 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
   for (int i = lane; i < nr; i += 32) z[m.r0 + i] = (VT)zs[i];
 }
 
-// Step-form sweeps (kernels.cuh StepMeta) for rows with at most 3 L/U
-// entries: per step each lane loads one 8-byte index word and one 4-wide
-// value vector, so a level costs a handful of instructions and the critical
-// path is the z loads, three FMAs and the store.  Pieces of kStepsPerPiece
-// steps are double-buffered through shared memory by TMA as above.
-template <class MT> struct Vec4;
-template <> struct Vec4<float> { using T = float4; };
-template <> struct Vec4<double> { using T = double4; };
-
-template <class VT, class MT, int MODE>
+// Float-float step-form sweeps (kernels.cuh StepMeta) of the mixed
+// solver: per step each lane loads one 16-byte index word and its four
+// float-pair values, then z[row] = (z[row] - w0 z[c0] - w1 z[c1] - w2 z[c2])
+// (* 1/u_ii) with a compensated (Dot2) accumulation whose only serial
+// dependence is one FP32 add per term.  Pieces of kStepsPerPiece steps are
+// double-buffered through shared memory by TMA as in the FP64 stream
+// kernel; z (8-byte entries) stays in shared memory.
+template <int MODE>
 __global__ void __launch_bounds__(32)
-k_ilu0_apply_steps(const StepMeta *__restrict__ meta,
-                   const uint8_t *__restrict__ rec, const VT *__restrict__ r,
-                   VT *__restrict__ pv, const VT *__restrict__ v,
-                   VT *__restrict__ z, const KScalars *__restrict__ sc,
-                   int *__restrict__ err) {
+k_ilu0_apply_dd(const StepMeta *__restrict__ meta,
+                const uint8_t *__restrict__ rec, const float2 *__restrict__ r,
+                float2 *__restrict__ pv, const float2 *__restrict__ v,
+                float2 *__restrict__ z, const KScalars *__restrict__ sc,
+                int *__restrict__ err) {
   if (sc && sc->done) return;
-  constexpr int SB = step_bytes<MT>();
+  constexpr int SB = kStepBytesDd;
   constexpr int PB = kStepsPerPiece * SB;
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ __align__(8) uint64_t bar[2];
@@ -296,7 +285,7 @@ k_ilu0_apply_steps(const StepMeta *__restrict__ meta,
   const int nr = m.nr, nf = m.n_fwd, S = m.n_fwd + m.n_bwd;
   const int P = (S + kStepsPerPiece - 1) / kStepsPerPiece;
   uint8_t *const buf0 = smem;  // buffer b at buf0 + b*PB
-  MT *zs = reinterpret_cast<MT *>(smem + 2 * PB);
+  float2 *zs = reinterpret_cast<float2 *>(smem + 2 * PB);
   const uint8_t *g = rec + m.rec_off;
   auto piece_bytes = [&](int j) {
     const int n = S - j * kStepsPerPiece;
@@ -311,20 +300,22 @@ k_ilu0_apply_steps(const StepMeta *__restrict__ meta,
     }
   }
   for (int i = lane; i < nr; i += 32)
-    zs[i] = (MT)pre_input<VT>(MODE, m.r0 + i, r, pv, v, sc);
-  if (lane == 0) zs[nr] = (MT)0;
+    zs[i] = dd_pre_input(MODE, m.r0 + i, r, pv, v, sc);
+  if (lane == 0) zs[nr] = make_float2(0.f, 0.f);
   __syncwarp();
-  using V4 = typename Vec4<MT>::T;
   const uint8_t *zb = reinterpret_cast<const uint8_t *>(zs);
   uint8_t *zw = reinterpret_cast<uint8_t *>(zs);
-  // one step: z[row] = (z[row] - w0 z[c0] - w1 z[c1] - w2 z[c2]) (* 1/u_ii)
-  auto step = [&](const uint4 &e, const V4 &w, bool bwd) {
-    MT acc = *reinterpret_cast<const MT *>(zb + e.x);
-    acc -= w.x * *reinterpret_cast<const MT *>(zb + e.y);
-    acc -= w.y * *reinterpret_cast<const MT *>(zb + e.z);
-    acc -= w.z * *reinterpret_cast<const MT *>(zb + e.w);
-    if (bwd) acc *= w.w;
-    *reinterpret_cast<MT *>(zw + e.x) = acc;
+  auto zat = [&](uint32_t off) { return *reinterpret_cast<const float2 *>(zb + off); };
+  // one step; the values arrive as two float4 = {w0, w1}, {w2, 1/u_ii}
+  auto step = [&](const uint4 &e, const float4 &wa, const float4 &wb,
+                  bool bwd) {
+    DdAcc acc = dd_acc(zat(e.x));
+    dd_acc_fma(acc, make_float2(-wa.x, -wa.y), zat(e.y));
+    dd_acc_fma(acc, make_float2(-wa.z, -wa.w), zat(e.z));
+    dd_acc_fma(acc, make_float2(-wb.x, -wb.y), zat(e.w));
+    float2 out = dd_value(acc);
+    if (bwd) out = dd_mul(out, make_float2(wb.z, wb.w));
+    *reinterpret_cast<float2 *>(zw + e.x) = out;
     __syncwarp();
   };
   uint32_t phases = 0u;
@@ -339,19 +330,21 @@ k_ilu0_apply_steps(const StepMeta *__restrict__ meta,
     phases ^= 1u << sb;
     const uint8_t *pc = buf0 + sb * PB;
     const int ns = (S - q) < kStepsPerPiece ? (S - q) : kStepsPerPiece;
-    // index/value words of a whole piece are independent of z: load them
-    // up front, two steps per unrolled iteration
-    auto E = [&](int k) { return reinterpret_cast<const uint4 *>(pc + k * SB)[lane]; };
-    auto W = [&](int k) { return reinterpret_cast<const V4 *>(pc + k * SB + 512)[lane]; };
+    auto E = [&](int k) {
+      return reinterpret_cast<const uint4 *>(pc + k * SB)[lane];
+    };
+    auto W = [&](int k, int h) {
+      return reinterpret_cast<const float4 *>(pc + k * SB + kStepIdxBytes)[2 * lane + h];
+    };
     int k = 0;
     for (; k + 1 < ns; k += 2, q += 2) {
       const uint4 e0 = E(k), e1 = E(k + 1);
-      const V4 w0 = W(k), w1 = W(k + 1);
-      step(e0, w0, q >= nf);
-      step(e1, w1, q + 1 >= nf);
+      const float4 a0 = W(k, 0), b0 = W(k, 1), a1 = W(k + 1, 0), b1 = W(k + 1, 1);
+      step(e0, a0, b0, q >= nf);
+      step(e1, a1, b1, q + 1 >= nf);
     }
     if (k < ns) {
-      step(E(k), W(k), q >= nf);
+      step(E(k), W(k, 0), W(k, 1), q >= nf);
       ++q;
     }
     if (lane == 0 && j + 2 < P) {
@@ -361,7 +354,7 @@ k_ilu0_apply_steps(const StepMeta *__restrict__ meta,
                 &bar[sb]);
     }
   }
-  for (int i = lane; i < nr; i += 32) z[m.r0 + i] = (VT)zs[i];
+  for (int i = lane; i < nr; i += 32) z[m.r0 + i] = zs[i];
 }
 
 // Sweeps with the factor records and the vector in global memory, one CTA
@@ -374,7 +367,10 @@ __global__ void k_ilu0_apply_global(const SubMeta *__restrict__ meta,
                                     VT *__restrict__ pv,
                                     const VT *__restrict__ v,
                                     VT *__restrict__ z,
-                                    const KScalars *__restrict__ sc) {
+                                    const KScalars *__restrict__ sc_base,
+                                    const int32_t *__restrict__ sub_sys) {
+  const KScalars *sc =
+      sc_base && sub_sys ? sc_base + sub_sys[blockIdx.x] : sc_base;
   if (sc && sc->done) return;
   const SubMeta m = meta[blockIdx.x];
   const uint8_t *base = rec + m.rec_off;
@@ -423,10 +419,19 @@ __global__ void k_pack_stream(int n, const int32_t *__restrict__ src,
     out[dst[e]] = (MT)factor[src[e]];
 }
 
+// Packs the FP64 factor into the float-float step stream.
+__global__ void k_pack_dd(int n, const int32_t *__restrict__ src,
+                          const int32_t *__restrict__ dst,
+                          const double *__restrict__ factor,
+                          float2 *__restrict__ out) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += gridDim.x * blockDim.x)
+    out[dst[e]] = dd_from(factor[src[e]]);
+}
+
 template <class VT, class MT, int MODE, int KLT, int KUT>
 void launch_stream(const SolverDev &d, size_t smem, const VT *r, VT *pv,
                    const VT *v, VT *z, const KScalars *sc, cudaStream_t st) {
-  const bool fp64 = sizeof(MT) == 8;
   static size_t attr = 0;
   if (smem > 48 * 1024 && attr < smem) {
     cudaFuncSetAttribute(k_ilu0_apply_stream<VT, MT, MODE, KLT, KUT>,
@@ -435,29 +440,17 @@ void launch_stream(const SolverDev &d, size_t smem, const VT *r, VT *pv,
     attr = smem;
   }
   k_ilu0_apply_stream<VT, MT, MODE, KLT, KUT><<<d.n_sub, 32, smem, st>>>(
-      fp64 ? d.smeta64 : d.smeta32, fp64 ? d.srec64 : d.srec32, r, pv, v, z, sc,
-      d.err);
+      d.smeta64, d.srec64, r, pv, v, z, sc, d.sub_sys, d.err);
 }
 
 template <class VT, class MT, int MODE>
 void apply_mode(const SolverDev &d, const VT *r, VT *pv, const VT *v, VT *z,
                 const KScalars *sc, cudaStream_t st) {
-  const bool fp64 = sizeof(MT) == 8;
-  const size_t smem = fp64 ? d.smem64 : d.smem32;
+  const size_t smem = d.smem64;
   // compile-time slot counts for the common stencils: quadrilaterals (2/2,
   // any subdomain whose rows have at most 2 L and 2 U entries) and
   // triangles (3/3); padding slots make smaller rows fit
-  if (smem && d.use_steps && !fp64) {
-    static size_t attr = 0;
-    if (smem > 48 * 1024 && attr < smem) {
-      cudaFuncSetAttribute(k_ilu0_apply_steps<VT, MT, MODE>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem);
-      attr = smem;
-    }
-    k_ilu0_apply_steps<VT, MT, MODE><<<d.n_sub, 32, smem, st>>>(
-        d.tmeta32, d.srec32, r, pv, v, z, sc, d.err);
-  } else if (smem && d.max_kl <= 2 && d.max_ku <= 2)
+  if (smem && d.max_kl <= 2 && d.max_ku <= 2)
     launch_stream<VT, MT, MODE, 2, 2>(d, smem, r, pv, v, z, sc, st);
   else if (smem && d.max_kl <= 3 && d.max_ku <= 3)
     launch_stream<VT, MT, MODE, 3, 3>(d, smem, r, pv, v, z, sc, st);
@@ -465,22 +458,33 @@ void apply_mode(const SolverDev &d, const VT *r, VT *pv, const VT *v, VT *z,
     launch_stream<VT, MT, MODE, 0, 0>(d, smem, r, pv, v, z, sc, st);
   else
     k_ilu0_apply_global<VT, MT, MODE><<<d.n_sub, 1024, 0, st>>>(
-        fp64 ? d.meta64 : d.meta32, fp64 ? d.rec64 : d.rec32, r, pv, v, z, sc);
+        d.meta64, d.rec64, r, pv, v, z, sc, d.sub_sys);
+  count_launches(1);
+}
+
+template <int MODE>
+void apply_mode_dd(const SolverDev &d, const float2 *r, float2 *pv,
+                   const float2 *v, float2 *z, const KScalars *sc,
+                   cudaStream_t st) {
+  static size_t attr = 0;
+  if (d.smem_dd > 48 * 1024 && attr < d.smem_dd) {
+    cudaFuncSetAttribute(k_ilu0_apply_dd<MODE>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)d.smem_dd);
+    attr = d.smem_dd;
+  }
+  k_ilu0_apply_dd<MODE><<<d.n_sub, 32, d.smem_dd, st>>>(
+      d.tmeta_dd, d.srec_dd, r, pv, v, z, sc, d.err);
   count_launches(1);
 }
 
 }  // namespace
 
 void launch_ilu0_factor(const SolverDev &d, const double *pvals, int *bad,
-                        bool to_fp32, cudaStream_t st) {
+                        bool to_dd, cudaStream_t st) {
   k_ilu0_factor<<<d.n_sub, 32, 0, st>>>(d.meta64, d.rec64, d.rec_src, pvals,
                                         bad);
   count_launches(1);
-  if (to_fp32 && !d.smem32) {  // FP32 copy for the global-memory sweep
-    k_factor_to_fp32<<<d.n_sub, 256, 0, st>>>(d.meta64, d.rec64, d.meta32,
-                                              d.rec32);
-    count_launches(1);
-  }
   auto grid = [](int n) { return (n + 255) / 256 < 2432 ? (n + 255) / 256 : 2432; };
   if (d.n_pack > 0 && d.smem64) {
     k_pack_stream<double><<<grid(d.n_pack), 256, 0, st>>>(
@@ -489,13 +493,21 @@ void launch_ilu0_factor(const SolverDev &d, const double *pvals, int *bad,
         reinterpret_cast<double *>(d.srec64));
     count_launches(1);
   }
-  if (to_fp32 && d.n_pack32 > 0 && d.smem32) {
-    k_pack_stream<float><<<grid(d.n_pack32), 256, 0, st>>>(
-        d.n_pack32, d.pack_src32, d.pack_dst32,
+  if (to_dd && d.n_pack_dd > 0) {
+    k_pack_dd<<<grid(d.n_pack_dd), 256, 0, st>>>(
+        d.n_pack_dd, d.pack_src_dd, d.pack_dst_dd,
         reinterpret_cast<const double *>(d.rec64),
-        reinterpret_cast<float *>(d.srec32));
+        reinterpret_cast<float2 *>(d.srec_dd));
     count_launches(1);
   }
+}
+
+void launch_ilu0_apply_dd(int mode, const SolverDev &d, const float2 *r,
+                          float2 *pv, const float2 *v, float2 *z,
+                          const KScalars *sc, cudaStream_t st) {
+  if (mode == 0) apply_mode_dd<0>(d, r, pv, v, z, sc, st);
+  else if (mode == 1) apply_mode_dd<1>(d, r, pv, v, z, sc, st);
+  else apply_mode_dd<2>(d, r, pv, v, z, sc, st);
 }
 
 template <class VT, class MT>
@@ -523,15 +535,4 @@ template void launch_precond<double, double>(int, int, const SolverDev &,
                                              double *, const double *,
                                              double *, const KScalars *,
                                              cudaStream_t);
-template void launch_precond<float, float>(int, int, const SolverDev &,
-                                           const float *, const float *,
-                                           float *, const float *, float *,
-                                           const KScalars *, cudaStream_t);
-
-void launch_ilu0_apply_fp32(int mode, const SolverDev &d, const double *r,
-                            double *pv, const double *v, double *z,
-                            const KScalars *sc, cudaStream_t st) {
-  launch_ilu0_apply<double, float>(mode, d, r, pv, v, z, sc, st);
-}
-
 }  // namespace pg

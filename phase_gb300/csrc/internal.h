@@ -85,6 +85,9 @@ struct HostMesh {
   std::vector<int64_t> link_ptr;
   std::vector<int32_t> link_face, link_cell;    // link_cell = -1 boundary
   std::vector<int32_t> n_interior_links;        // per cell
+  // nodes and the cell -> node lists (ghost-cell IB stencils)
+  std::vector<double> node_x, node_y;
+  std::vector<int64_t> cptr, cind;
 };
 
 int build_host_mesh(const double *nodes_xy, int64_t n_nodes,
@@ -128,8 +131,22 @@ struct EqnPattern {
   int n_interior_colors = 0;
 };
 
+// Ghost-cell immersed-boundary rows of the pressure equation: cell classes
+// and, for every IB and solid cell, its row entries (CrsEquation order,
+// zeros dropped) and rhs value.
+struct GcibRows {
+  std::vector<int32_t> cls;  // 0 fluid, 1 IB, 2 solid
+  std::vector<std::vector<std::pair<int32_t, double>>> rows;  // per cell
+  std::vector<double> rhs;                                    // per cell
+};
+int build_gcib(const HostMesh &m, int n_circles, const double *circles,
+               int ib_bc, double ib_ref, GcibRows &g);
+
+// row_mask (optional): rows with mask 0 get no Laplacian entries; extra
+// (optional): entries appended to each row (the GCIB rows)
 int build_pattern(const HostMesh &m, int gamma_kind, const int32_t *bc_type,
-                  EqnPattern &p, bool diag_first = false);
+                  EqnPattern &p, bool diag_first = false,
+                  const GcibRows *extra = nullptr);
 
 }  // namespace pg
 
@@ -149,6 +166,10 @@ struct pg_eqn {
   uint64_t pattern_id = 0;
   bool momentum = false;   // vector momentum operator: rhs holds 2n values
   pg::DevBuf<int32_t> diag;  // diagonal position per row
+  // ghost-cell IB equation: constant IB/solid rows the assembly starts from
+  bool has_base = false;
+  pg::DevBuf<double> base_vals, base_rhs;
+  std::vector<int32_t> cell_class;
 };
 
 namespace pg {
@@ -175,27 +196,32 @@ struct Analysis {
   std::vector<int32_t> part;               // subdomain of each original row
   bool global_ilu = false;                 // one subdomain holding all rows
   // packed ILU(0) records (static parts filled; values by the factor)
-  std::vector<SubMeta> meta64, meta32;
-  std::vector<uint8_t> rec64, rec32;
+  std::vector<SubMeta> meta64;
+  std::vector<uint8_t> rec64;
   std::vector<int32_t> rec_src;            // value slot -> permuted entry
-  size_t smem64 = 0, smem32 = 0;           // max record + vector bytes
+  size_t smem64 = 0;                       // max record + vector bytes
   int max_kl = 0, max_ku = 0;              // widest L / U part of a row
   // streaming records for the apply kernel (kernels.cuh StreamMeta)
-  std::vector<StreamMeta> smeta64, smeta32;
-  std::vector<uint8_t> srec64, srec32;
+  std::vector<StreamMeta> smeta64;
+  std::vector<uint8_t> srec64;
   std::vector<int32_t> pack_src, pack_dst64;    // FP64 stream <- factor
-  std::vector<int32_t> pack_src32, pack_dst32;  // FP32 stream <- factor
-  size_t ssmem64 = 0, ssmem32 = 0;
-  // step stream (kernels.cuh StepMeta) replacing the FP32 level-blob stream
-  // when every row has at most 3 L and 3 U entries (in srec32/pack_*32)
+  size_t ssmem64 = 0;
+  // float-float step stream (kernels.cuh StepMeta) of the mixed solver,
+  // when every row has at most 3 L and 3 U entries
   bool use_steps = false;
-  std::vector<StepMeta> tmeta32;
+  std::vector<StepMeta> tmeta_dd;
+  std::vector<uint8_t> srec_dd;
+  std::vector<int32_t> pack_src_dd, pack_dst_dd;  // step values <- factor
+  size_t ssmem_dd = 0;
 };
 
 // target bytes of one streamed piece of a subdomain's factor
 constexpr int64_t kStreamPiece = 6144;
 
+// sys_rows (optional): row offsets of independent systems stacked block-
+// diagonally (batched solves); every subdomain then lies in one system
 int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
-            int subdomain_rows, Analysis &a);
+            int subdomain_rows, Analysis &a,
+            const std::vector<int64_t> *sys_rows = nullptr);
 
 }  // namespace pg

@@ -111,17 +111,22 @@ __global__ void k_assemble_interior(
   const double m2 = msq[k];
   const double c_l = __ddiv_rn(__dmul_rn(g, dot_l[k]), m2);
   const double c_r = __ddiv_rn(__dmul_rn(g, dot_r[k]), m2);
-  vals[slot_lr[k]] = __dadd_rn(vals[slot_lr[k]], c_l);
-  vals[slot_rl[k]] = __dadd_rn(vals[slot_rl[k]], c_r);
-  vals[diag_l[k]] = __dadd_rn(vals[diag_l[k]], -c_l);
-  vals[diag_r[k]] = __dadd_rn(vals[diag_r[k]], -c_r);
+  // a side with cell -1 is not a fluid row (ghost-cell IB equations)
+  if (l >= 0) {
+    vals[slot_lr[k]] = __dadd_rn(vals[slot_lr[k]], c_l);
+    vals[diag_l[k]] = __dadd_rn(vals[diag_l[k]], -c_l);
+  }
+  if (r >= 0) {
+    vals[slot_rl[k]] = __dadd_rn(vals[slot_rl[k]], c_r);
+    vals[diag_r[k]] = __dadd_rn(vals[diag_r[k]], -c_r);
+  }
   if (u_face) {
     // src::div(u): rhs_ -= dot(u_f, Sf_out) for both cells (Source.cpp:11-15)
     const double ux = u_face[2 * f], uy = u_face[2 * f + 1];
     const double dl = __dadd_rn(__dmul_rn(ux, sfl_x[k]), __dmul_rn(uy, sfl_y[k]));
     const double dr = __dadd_rn(__dmul_rn(ux, sfr_x[k]), __dmul_rn(uy, sfr_y[k]));
-    rhs[l] = __dadd_rn(rhs[l], -dl);
-    rhs[r] = __dadd_rn(rhs[r], -dr);
+    if (l >= 0) rhs[l] = __dadd_rn(rhs[l], -dl);
+    if (r >= 0) rhs[r] = __dadd_rn(rhs[r], -dr);
   }
 }
 
@@ -141,6 +146,7 @@ __global__ void k_assemble_boundary(
   if (k >= off + nf) return;
   const int f = cface[k];
   const int l = cl[k];
+  if (l < 0) return;  // owner is not a fluid row (ghost-cell IB equations)
   double acc = rhs[l];
   if (bc[k] == PG_BC_FIXED) {
     const double g = gamma_face ? gamma_face[f] : gamma_scalar;
@@ -831,14 +837,9 @@ void launch_diag_apply(int mode, const SolverDev &d, const MT *dinv,
                                       const VT *, VT *, const VT *,           \
                                       KScalars *, RedWork, cudaStream_t);
 PG_INST(double, double)
-PG_INST(float, float)
 template void launch_update<double>(int, double *, double *, const double *,
                                     const double *, const double *,
                                     const double *, const double *,
                                     KScalars *, RedWork, cudaStream_t);
-template void launch_update<float>(int, float *, float *, const float *,
-                                   const float *, const float *, const float *,
-                                   const float *, KScalars *, RedWork,
-                                   cudaStream_t);
 
 }  // namespace pg

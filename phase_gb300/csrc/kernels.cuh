@@ -19,6 +19,13 @@ struct KScalars {
   double rv, tt, ts, rr, bb;
   double rr_true;
   double tol2;
+  // float-float copies of alpha, omega, beta for the mixed-precision
+  // kernels, written next to the FP64 values by the same thread
+  float2 alpha_dd, omega_dd, beta_dd;
+  // batched solves: device-side reliable updates (batch.cu)
+  double rr_ref;  // true ||r||^2 at the last replacement
+  int action;     // 0 none, 1 confirm convergence, 2 restart, 3 replace
+  int restarts;
   int iter, max_iter;
   int done;    // 0 running, 1 stopped
   int status;  // PG_OK (converged candidate), PG_MAX_ITERS, PG_BREAKDOWN,
@@ -121,42 +128,47 @@ struct StreamMeta {
   int32_t r0, nr, nlev, KL, KU, rec_off, hdr_bytes, max_piece;
 };
 
-// Step form of the streams, used when every row has at most 3 L and 3 U
-// entries (quadrilateral and triangle meshes).  A step is one warp-wide
-// slice of a level (up to 32 rows):
-//   uint32 idx[32][4]  byte offsets into the subdomain's z vector of
-//                      {row, c0, c1, c2}  (unused: row/col = nr, z[nr] = 0)
-//   MT     val[32][4]  {w0, w1, w2, 1/u_ii}
+// Step form of the factor for the float-float sweep of the mixed solver,
+// used when every row has at most 3 L and 3 U entries (quadrilateral and
+// triangle meshes).  A step is one warp-wide slice of a level (up to 32
+// rows):
+//   uint32 idx[32][4]  byte offsets into the subdomain's z vector (8-byte
+//                      entries) of {row, c0, c1, c2}; unused: nr (z[nr] = 0)
+//   float2 val[32][4]  {w0, w1, w2, 1/u_ii} as float pairs
 // Forward steps (L parts, levels ascending) come first, then backward steps
 // (U parts and 1/u_ii, levels descending); pieces are kStepsPerPiece steps.
-// Used for the FP32 sweep.
 struct StepMeta {
   int32_t r0, nr, n_fwd, n_bwd, rec_off, pad0, pad1, pad2;
 };
 constexpr int kStepsPerPiece = 8;
-template <class MT> __host__ __device__ constexpr int step_bytes() {
-  return 32 * 16 + 32 * 4 * (int)sizeof(MT);
-}
+constexpr int kStepIdxBytes = 32 * 16;
+constexpr int kStepBytesDd = kStepIdxBytes + 32 * 4 * 8;
 
 struct SolverDev {
   int n, nnz, n_sub;
   // permuted CSR
   const int32_t *prp, *pci;
-  // ILU(0) records (FP64 and FP32 copies)
-  const SubMeta *meta64, *meta32;
-  uint8_t *rec64, *rec32;
+  // ILU(0) records (FP64)
+  const SubMeta *meta64;
+  uint8_t *rec64;
   const int32_t *rec_src;
-  size_t smem64, smem32;  // dynamic smem of the staged apply (0 = too big)
-  int max_kl, max_ku;     // widest L / U part of any row
-  // streaming records and the factor -> stream value maps
-  const StreamMeta *smeta64, *smeta32;
-  uint8_t *srec64, *srec32;
-  const int32_t *pack_src, *pack_dst64, *pack_src32, *pack_dst32;
-  int n_pack, n_pack32;
-  // FP32 step stream (when use_steps)
+  size_t smem64, smem_dd;  // dynamic smem of the staged applies (0 = too big)
+  int max_kl, max_ku;      // widest L / U part of any row
+  // FP64 streaming records and the factor -> stream value map
+  const StreamMeta *smeta64;
+  uint8_t *srec64;
+  const int32_t *pack_src, *pack_dst64;
+  int n_pack;
+  // float-float step stream of the mixed solver (when use_steps)
   int use_steps;
-  const StepMeta *tmeta32;
+  const StepMeta *tmeta_dd;
+  uint8_t *srec_dd;
+  const int32_t *pack_src_dd, *pack_dst_dd;
+  int n_pack_dd;
   int *err;               // set when a bounded device wait runs out
+  // batched solves: system of every subdomain (NULL for one system); the
+  // apply kernels then read the scalars sc[sub_sys[subdomain]]
+  const int32_t *sub_sys;
 };
 
 void launch_permute_values(int nnz, const int32_t *psrc, const double *src,
@@ -168,10 +180,10 @@ void launch_unpermute_vec(int n, const int32_t *perm, const double *src,
                           double *dst, cudaStream_t st);
 
 // ILU(0) numeric factorisation into the FP64 factor records, then packed
-// into the streaming records (FP64, and FP32 when to_fp32); bad counts zero
-// or non-finite pivots.
+// into the FP64 streaming records and, when to_dd, the float-float step
+// stream; bad counts zero or non-finite pivots.
 void launch_ilu0_factor(const SolverDev &d, const double *pvals, int *bad,
-                        bool to_fp32, cudaStream_t st);
+                        bool to_dd, cudaStream_t st);
 
 // Preconditioner application with fused vector update.
 //   mode 0: z = M^-1 in
@@ -203,10 +215,87 @@ void launch_init_from_r(int n, double *r, double *rh, double *p, double *v,
                         KScalars *sc, RedWork w, cudaStream_t st);
 void launch_replace_r(int n, const double *r, const double *rh, KScalars *sc,
                       RedWork w, cudaStream_t st);
-// ILU(0) application with FP32 factors and FP32 sweeps on FP64 vectors
-void launch_ilu0_apply_fp32(int mode, const SolverDev &d, const double *r,
-                            double *pv, const double *v, double *z,
-                            const KScalars *sc, cudaStream_t st);
+
+// ---- mixed-precision (float-float) solver kernels, dd.cu / ilu.cu ----
+// Vectors are float2 {hi, lo} in the permuted order; the matrix values are
+// a float-float copy of the permuted FP64 values.  Dot products leave the
+// kernels as FP64 scalars in KScalars, like the FP64 kernels'.
+void launch_dd_split(int64_t n, const double *src, double scale, float2 *dst,
+                     cudaStream_t st);
+void launch_dd_join(int n, const float2 *src, double scale, double *dst,
+                    cudaStream_t st);
+// x64 += xw / scale; xw = 0
+void launch_dd_fold(int n, double *x64, float2 *xw, double inv_scale,
+                    cudaStream_t st);
+// r = dd(r64 * scale); restart (rhat = r, p = v = 0, rho = <r,r>) when
+// restart, else residual replacement (rho, beta from the new r)
+void launch_dd_set_r(int n, const double *r64, double scale, float2 *r,
+                     float2 *rh, float2 *p, float2 *v, bool restart,
+                     KScalars *sc, RedWork w, cudaStream_t st);
+void launch_dd_spmv_v(const SolverDev &d, const float2 *val, const float2 *ph,
+                      float2 *v, const float2 *rh, KScalars *sc, RedWork w,
+                      cudaStream_t st);
+void launch_dd_spmv_t(const SolverDev &d, const float2 *val, const float2 *sh,
+                      float2 *t, const float2 *s, KScalars *sc, RedWork w,
+                      cudaStream_t st);
+void launch_dd_update(int n, float2 *x, float2 *r, const float2 *ph,
+                      const float2 *sh, const float2 *s, const float2 *t,
+                      const float2 *rh, KScalars *sc, RedWork w,
+                      cudaStream_t st);
+// Jacobi / identity preconditioner on float pairs (dinv NULL: identity)
+void launch_dd_diag_apply(int mode, int n, const float2 *dinv, const float2 *r,
+                          float2 *pv, const float2 *v, float2 *z,
+                          const KScalars *sc, cudaStream_t st);
+// ILU(0) sweeps in float-float arithmetic over the step stream (ilu.cu)
+void launch_ilu0_apply_dd(int mode, const SolverDev &d, const float2 *r,
+                          float2 *pv, const float2 *v, float2 *z,
+                          const KScalars *sc, cudaStream_t st);
+
+// ---- batched solves (batch.cu) ----
+// Tiles of rows: tile t covers permuted rows [tile_r0[t], tile_r1[t]) of
+// system tile_sys[t]; the tiles of system s are [tile_ptr[s], tile_ptr[s+1]).
+struct BatchTiles {
+  const int32_t *tile_sys, *tile_r0, *tile_r1, *tile_ptr;
+  int n_tiles;
+};
+// per-tile partial sums [kMaxDots][n_tiles] and one ticket per system
+struct BatchRed {
+  double *partials;
+  unsigned int *tickets;
+  int n_tiles;
+};
+void launch_b_init(const BatchTiles &T, const BatchRed &R, int block,
+                   const int32_t *rp, const int32_t *ci, const double *val,
+                   const double *b, const double *x, double *r, double *rh,
+                   double *p, double *v, KScalars *sc, const int *init,
+                   cudaStream_t st);
+void launch_b_spmv_v(const BatchTiles &T, const BatchRed &R, int block,
+                     const int32_t *rp, const int32_t *ci, const double *val,
+                     const double *ph, double *v, const double *rh,
+                     KScalars *sc, cudaStream_t st);
+void launch_b_spmv_t(const BatchTiles &T, const BatchRed &R, int block,
+                     const int32_t *rp, const int32_t *ci, const double *val,
+                     const double *sh, double *t, const double *s,
+                     KScalars *sc, cudaStream_t st);
+void launch_b_update(const BatchTiles &T, const BatchRed &R, int block,
+                     double *x, double *r, const double *ph, const double *sh,
+                     const double *s, const double *t, const double *rh,
+                     KScalars *sc, cudaStream_t st);
+void launch_b_true_residual(const BatchTiles &T, const BatchRed &R, int block,
+                            const int32_t *rp, const int32_t *ci,
+                            const double *val, const double *b,
+                            const double *x, double *r, const double *rh,
+                            KScalars *sc, const int *sel, cudaStream_t st);
+// end-of-chunk fix-up of the systems with a pending action: r = b - A x in
+// FP64, then confirm convergence, replace the recursive residual, or
+// restart with a fresh shadow residual
+void launch_b_fix(const BatchTiles &T, const BatchRed &R, int block,
+                  const int32_t *rp, const int32_t *ci, const double *val,
+                  const double *b, const double *x, double *r, double *rh,
+                  double *p, double *v, KScalars *sc, cudaStream_t st);
+void launch_b_check(int n_sys, const KScalars *sc, int *chunks,
+                    int max_chunks, cudaGraphConditionalHandle h,
+                    cudaStream_t st);
 
 // rr_true = ||b - A x||^2 (FP64 matrix and vectors); x == NULL gives ||b||^2
 void launch_true_residual(const SolverDev &d, const double *val,

@@ -1,7 +1,8 @@
 // The SparseMatrixSolver replacement: sparsity analysis caching, value
 // permutation, ILU(0) factorisation and the device-resident BiCGStab loop
-// with reliable residual updates.  FP64 vectors and SpMV throughout; in
-// PG_MIXED the ILU(0) factors are stored and swept in FP32.
+// with reliable residual updates: in FP64 (PG_FP64), or with the whole
+// iteration in float-float arithmetic on the FP32 pipes and the FP64 true
+// residual at every reliable update (PG_MIXED).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -53,12 +54,12 @@ struct pg_solver {
   bool analysed = false;
   uint64_t eqn_pattern = 0;  // pattern id of a device equation, 0 = host CSR
   DevBuf<int32_t> perm, prp, pci, psrc, dup_dst, dup_src, rec_src;
-  DevBuf<SubMeta> meta64, meta32;
-  DevBuf<uint8_t> rec64, rec32;
-  DevBuf<StreamMeta> smeta64, smeta32;
-  DevBuf<StepMeta> tmeta32;
-  DevBuf<uint8_t> srec64, srec32;
-  DevBuf<int32_t> pack_src, pack_dst64, pack_src32, pack_dst32;
+  DevBuf<SubMeta> meta64;
+  DevBuf<uint8_t> rec64;
+  DevBuf<StreamMeta> smeta64;
+  DevBuf<StepMeta> tmeta_dd;
+  DevBuf<uint8_t> srec64, srec_dd;
+  DevBuf<int32_t> pack_src, pack_dst64, pack_src_dd, pack_dst_dd;
   DevBuf<int> err;
   DevBuf<int32_t> raw_rp, raw_ci, st_rp, st_ci;
   DevBuf<double> st_vals, st_vec;
@@ -67,6 +68,9 @@ struct pg_solver {
   DevBuf<double> pvals, jdinv;
   // Krylov vectors (permuted order)
   DevBuf<double> b, x, r, rh, p, v, ph, s, sh, t, xout;
+  // float-float matrix, Jacobi diagonal and Krylov vectors of PG_MIXED
+  DevBuf<float2> pvals_dd, jdinv_dd;
+  DevBuf<float2> xd, rd, rhd, pd, vd, phd, sd, shd, td;
   // reductions and scalars
   DevBuf<double> partials;
   DevBuf<unsigned int> ticket;
@@ -78,8 +82,8 @@ struct pg_solver {
   bool have_rhs = false, have_x = false, have_vals = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   int red_grid = 1;
-  // CUDA graphs of one chunk of BiCGStab iterations (FP64 and FP32 ILU
-  // sweeps); kernel
+  // CUDA graphs of one chunk of BiCGStab iterations (FP64, float-float);
+  // kernel
   // arguments are fixed device pointers, so a graph stays valid until the
   // buffers are reallocated by a new analysis
   cudaGraphExec_t chunk_graph[2] = {nullptr, nullptr};
@@ -109,29 +113,27 @@ struct pg_solver {
     d.prp = prp.p;
     d.pci = pci.p;
     d.meta64 = meta64.p;
-    d.meta32 = meta32.p;
     d.rec64 = rec64.p;
-    d.rec32 = rec32.p;
     d.rec_src = rec_src.p;
     // the streamed (TMA) apply needs header + 2 pieces + the subdomain's
     // vector in shared memory; otherwise the global-memory sweep is used
     d.smem64 = a.ssmem64 <= kMaxApplySmem ? a.ssmem64 : 0;
-    d.smem32 = a.ssmem32 <= kMaxApplySmem ? a.ssmem32 : 0;
     d.smeta64 = smeta64.p;
-    d.smeta32 = smeta32.p;
     d.srec64 = srec64.p;
-    d.srec32 = srec32.p;
     d.pack_src = pack_src.p;
     d.pack_dst64 = pack_dst64.p;
-    d.pack_src32 = pack_src32.p;
-    d.pack_dst32 = pack_dst32.p;
     d.n_pack = (int)a.pack_src.size();
-    d.n_pack32 = (int)a.pack_src32.size();
     d.use_steps = a.use_steps ? 1 : 0;
-    d.tmeta32 = tmeta32.p;
+    d.smem_dd = a.use_steps && a.ssmem_dd <= kMaxApplySmem ? a.ssmem_dd : 0;
+    d.tmeta_dd = tmeta_dd.p;
+    d.srec_dd = srec_dd.p;
+    d.pack_src_dd = pack_src_dd.p;
+    d.pack_dst_dd = pack_dst_dd.p;
+    d.n_pack_dd = (int)a.pack_src_dd.size();
     d.max_kl = a.max_kl;
     d.max_ku = a.max_ku;
     d.err = err.p;
+    d.sub_sys = nullptr;
     return d;
   }
   RedWork red() const { return RedWork{partials.p, ticket.p, red_grid}; }
@@ -153,18 +155,15 @@ int upload_analysis(pg_solver *s) {
   up(s->dup_src, a.dup_src);
   up(s->rec_src, a.rec_src);
   up(s->meta64, a.meta64);
-  up(s->meta32, a.meta32);
   up(s->rec64, a.rec64);
-  up(s->rec32, a.rec32);
   up(s->smeta64, a.smeta64);
-  up(s->tmeta32, a.tmeta32);
-  up(s->smeta32, a.smeta32);
   up(s->srec64, a.srec64);
-  up(s->srec32, a.srec32);
   up(s->pack_src, a.pack_src);
   up(s->pack_dst64, a.pack_dst64);
-  up(s->pack_src32, a.pack_src32);
-  up(s->pack_dst32, a.pack_dst32);
+  up(s->tmeta_dd, a.tmeta_dd);
+  up(s->srec_dd, a.srec_dd);
+  up(s->pack_src_dd, a.pack_src_dd);
+  up(s->pack_dst_dd, a.pack_dst_dd);
   if (e == cudaSuccess) e = s->err.zero(1);
   const size_t n = a.n, nnz = a.nnz;
   for (DevBuf<double> *bf : {&s->b, &s->x, &s->r, &s->rh, &s->p, &s->v,
@@ -172,6 +171,12 @@ int upload_analysis(pg_solver *s) {
                              &s->jdinv})
     if (e == cudaSuccess) e = bf->reserve(n);
   if (e == cudaSuccess) e = s->pvals.reserve(nnz);
+  if (s->cfg.precision == PG_MIXED) {
+    for (DevBuf<float2> *bf : {&s->xd, &s->rd, &s->rhd, &s->pd, &s->vd,
+                               &s->phd, &s->sd, &s->shd, &s->td, &s->jdinv_dd})
+      if (e == cudaSuccess) e = bf->reserve(n);
+    if (e == cudaSuccess) e = s->pvals_dd.reserve(nnz);
+  }
   s->drop_graphs();
   s->red_grid = (int)std::min<int64_t>(1216, (n + kVecBlock - 1) / kVecBlock);
   if (s->red_grid < 1) s->red_grid = 1;
@@ -196,6 +201,12 @@ int ensure_host_state(pg_solver *s) {
   return PG_OK;
 }
 
+// one chunk = kChunk BiCGStab iterations, 5 kernels each; captured once into
+// a CUDA graph after the first direct chunk and replayed
+constexpr int kChunk = 8;
+constexpr double kDelta2 = 1e-4;  // reliable update when rr < kDelta2 * rr_ref
+constexpr int kMaxRestarts = 50;
+
 // PG_SOLVER_TRACE=1 prints the Krylov scalars at every chunk boundary
 bool trace_enabled() {
   static const int on = [] {
@@ -203,6 +214,30 @@ bool trace_enabled() {
     return e && e[0] == '1' ? 1 : 0;
   }();
   return on != 0;
+}
+
+// Replays the captured chunk graph (capturing it on the second call).
+template <class F>
+int run_chunk(cudaGraphExec_t &gexec, bool &direct_done, F &&chunk) {
+  cudaStream_t st = stream();
+  if (gexec) {
+    PG_CUDA(cudaGraphLaunch(gexec, st));
+    count_launches(5 * kChunk);
+  } else if (direct_done) {
+    cudaGraph_t graph = nullptr;
+    PG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    chunk();  // launches are counted here, executed once below
+    PG_CUDA(cudaStreamEndCapture(st, &graph));
+    cudaError_t ge = cudaGraphInstantiate(&gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    PG_CUDA(ge);
+    PG_CUDA(cudaGraphLaunch(gexec, st));
+  } else {
+    chunk();
+    direct_done = true;
+  }
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
 }
 
 inline int grid_for(int64_t n) {
@@ -219,28 +254,18 @@ inline int grid_for(int64_t n) {
 // iteration restarts from x with a fresh shadow residual.  Convergence is
 // only ever declared on the true residual.
 int run_bicgstab(pg_solver *s, double tol, int max_iters, int *iters,
-                 int *updates) {
+                 int *updates, double *bb_out) {
   cudaStream_t st = stream();
   const SolverDev d = s->dev();
   const RedWork w = s->red();
-  const bool fp32_ilu =
-      s->cfg.precision == PG_MIXED && s->cfg.precond == PG_PREC_ILU0;
   double *const val = s->pvals.p, *const jd = s->jdinv.p;
   double *const x = s->x.p, *const r = s->r.p, *const rh = s->rh.p;
   double *const p = s->p.p, *const v = s->v.p, *const ph = s->ph.p;
   double *const ss = s->s.p, *const sh = s->sh.p, *const t = s->t.p;
   auto precond = [&](int mode, double *pv, double *z) {
-    if (fp32_ilu)
-      launch_ilu0_apply_fp32(mode, d, r, pv, v, z, s->sc.p, st);
-    else
-      launch_precond<double, double>(s->cfg.precond, mode, d, jd, r, pv, v, z,
-                                     s->sc.p, st);
+    launch_precond<double, double>(s->cfg.precond, mode, d, jd, r, pv, v, z,
+                                   s->sc.p, st);
   };
-  // one chunk = kChunk iterations, 5 kernels each; captured once into a CUDA
-  // graph after the first direct chunk and replayed
-  constexpr int kChunk = 8;
-  constexpr double kDelta2 = 1e-4;   // replace when rr < kDelta2 * rr_ref
-  constexpr int kMaxRestarts = 50;
   auto chunk = [&]() {
     for (int c = 0; c < kChunk; ++c) {
       precond(1, p, ph);
@@ -267,6 +292,7 @@ int run_bicgstab(pg_solver *s, double tol, int max_iters, int *iters,
   int rc = read_scalars();
   if (rc) return rc;
   const double bb = s->sc_host->rr_true;
+  *bb_out = bb;  // unscaled ||b||^2 for the caller's final check
   *iters = 0;
   *updates = 0;
   if (!std::isfinite(bb)) return PG_NON_FINITE;
@@ -286,26 +312,10 @@ int run_bicgstab(pg_solver *s, double tol, int max_iters, int *iters,
   if (s->sc_host->rr_true <= init.tol2 * bb) return PG_OK;
   double rr_ref = s->sc_host->rr_true;
   int restarts = 0;
-  cudaGraphExec_t &gexec = s->chunk_graph[fp32_ilu ? 1 : 0];
+  cudaGraphExec_t &gexec = s->chunk_graph[0];
   bool direct_done = false;
   for (;;) {
-    if (gexec) {
-      PG_CUDA(cudaGraphLaunch(gexec, st));
-      count_launches(5 * kChunk);
-    } else if (direct_done) {
-      cudaGraph_t graph = nullptr;
-      PG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
-      chunk();  // launches are counted here, executed once below
-      PG_CUDA(cudaStreamEndCapture(st, &graph));
-      cudaError_t ge = cudaGraphInstantiate(&gexec, graph, 0);
-      cudaGraphDestroy(graph);
-      PG_CUDA(ge);
-      PG_CUDA(cudaGraphLaunch(gexec, st));
-    } else {
-      chunk();
-      direct_done = true;
-    }
-    PG_CUDA(cudaGetLastError());
+    if ((rc = run_chunk(gexec, direct_done, chunk))) return rc;
     if ((rc = read_scalars())) return rc;
     const KScalars k = *s->sc_host;
     *iters = k.iter;
@@ -338,17 +348,130 @@ int run_bicgstab(pg_solver *s, double tol, int max_iters, int *iters,
   }
 }
 
+// The same iteration with every per-element operation in float-float
+// arithmetic (dd.cuh, dd.cu, the step-form ILU sweep in ilu.cu).  The
+// system is scaled by a power of two (exact) so that ||b|| is about 1; the
+// float-float correction x_w is folded into the FP64 solution at every
+// reliable update, where the FP64 true residual b - A x replaces the
+// recursive one.  Attainable accuracy is then set by the FP64 residual, and
+// each cycle's float-float work only has to reduce it by kDelta.
+int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
+                    int *updates, double *bb_out) {
+  cudaStream_t st = stream();
+  const SolverDev d = s->dev();
+  const RedWork w = s->red();
+  const int n = d.n;
+  const bool ilu = s->cfg.precond == PG_PREC_ILU0;
+  const float2 *jd = s->cfg.precond == PG_PREC_JACOBI ? s->jdinv_dd.p : nullptr;
+  float2 *const val = s->pvals_dd.p;
+  float2 *const x = s->xd.p, *const r = s->rd.p, *const rh = s->rhd.p;
+  float2 *const p = s->pd.p, *const v = s->vd.p, *const ph = s->phd.p;
+  float2 *const ss = s->sd.p, *const sh = s->shd.p, *const t = s->td.p;
+  auto precond = [&](int mode, float2 *pv, float2 *z) {
+    if (ilu)
+      launch_ilu0_apply_dd(mode, d, r, pv, v, z, s->sc.p, st);
+    else
+      launch_dd_diag_apply(mode, n, jd, r, pv, v, z, s->sc.p, st);
+  };
+  auto chunk = [&]() {
+    for (int c = 0; c < kChunk; ++c) {
+      precond(1, p, ph);
+      launch_dd_spmv_v(d, val, ph, v, rh, s->sc.p, w, st);
+      precond(2, ss, sh);
+      launch_dd_spmv_t(d, val, sh, t, ss, s->sc.p, w, st);
+      launch_dd_update(n, x, r, ph, sh, ss, t, rh, s->sc.p, w, st);
+    }
+  };
+  auto read_scalars = [&]() -> int {
+    PG_CUDA(cudaMemcpyAsync(s->sc_host, s->sc.p, sizeof(KScalars),
+                            cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    return PG_OK;
+  };
+  KScalars init{};
+  init.tol2 = tol * tol;
+  init.max_iter = max_iters;
+  *s->sc_host = init;
+  PG_CUDA(cudaMemcpyAsync(s->sc.p, s->sc_host, sizeof(KScalars),
+                          cudaMemcpyHostToDevice, st));
+  launch_true_residual(d, s->pvals.p, s->b.p, nullptr, nullptr, s->sc.p, w, st);
+  int rc = read_scalars();
+  if (rc) return rc;
+  const double bb = s->sc_host->rr_true;
+  *bb_out = bb;  // unscaled ||b||^2 for the caller's final check
+  *iters = 0;
+  *updates = 0;
+  if (!std::isfinite(bb)) return PG_NON_FINITE;
+  if (bb == 0.) {
+    PG_CUDA(cudaMemsetAsync(s->x.p, 0, n * sizeof(double), st));
+    return PG_OK;
+  }
+  // power-of-two scale: ||b|| * scale in [0.5, 1)
+  const double scale = std::ldexp(1.0, -std::ilogb(std::sqrt(bb)) - 1);
+  init.bb = bb * scale * scale;
+  init.rr_true = bb;
+  *s->sc_host = init;
+  PG_CUDA(cudaMemcpyAsync(s->sc.p, s->sc_host, sizeof(KScalars),
+                          cudaMemcpyHostToDevice, st));
+  PG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(float2), st));
+  launch_true_residual(d, s->pvals.p, s->b.p, s->x.p, s->r.p, s->sc.p, w, st);
+  launch_dd_set_r(n, s->r.p, scale, r, rh, p, v, true, s->sc.p, w, st);
+  if ((rc = read_scalars())) return rc;
+  if (s->sc_host->status == PG_NON_FINITE) return PG_NON_FINITE;
+  if (s->sc_host->rr_true <= init.tol2 * bb) return PG_OK;
+  double rr_ref = s->sc_host->rr_true;
+  int restarts = 0;
+  bool direct_done = false;
+  for (;;) {
+    if ((rc = run_chunk(s->chunk_graph[1], direct_done, chunk))) return rc;
+    if ((rc = read_scalars())) return rc;
+    const KScalars k = *s->sc_host;
+    *iters = k.iter;
+    if (trace_enabled())
+      std::fprintf(stderr,
+                   "pg_solver(dd): it %d rr/bb %.3e rho %.3e alpha %.3e omega "
+                   "%.3e status %d done %d\n",
+                   k.iter, k.rr / init.bb, k.rho, k.alpha, k.omega, k.status,
+                   k.done);
+    if (k.status == PG_NON_FINITE) return PG_NON_FINITE;
+    if (!k.done && !(k.rr < kDelta2 * rr_ref * scale * scale)) continue;
+    // reliable update: x += x_w, r = b - A x in FP64
+    launch_dd_fold(n, s->x.p, x, 1.0 / scale, st);
+    launch_true_residual(d, s->pvals.p, s->b.p, s->x.p, s->r.p, s->sc.p, w, st);
+    if ((rc = read_scalars())) return rc;
+    const double rr_true = s->sc_host->rr_true;
+    ++*updates;
+    if (trace_enabled())
+      std::fprintf(stderr, "pg_solver(dd): it %d true rr/bb %.3e\n", k.iter,
+                   rr_true / bb);
+    if (!std::isfinite(rr_true)) return PG_NON_FINITE;
+    if (rr_true <= init.tol2 * bb) return PG_OK;
+    if (k.iter >= max_iters) return PG_MAX_ITERS;
+    const bool restart = k.status == PG_BREAKDOWN;
+    if (restart && ++restarts > kMaxRestarts) return PG_BREAKDOWN;
+    launch_dd_set_r(n, s->r.p, scale, r, rh, p, v, restart, s->sc.p, w, st);
+    rr_ref = rr_true;
+  }
+}
+
+bool use_dd(const pg_solver *s) {
+  return s->cfg.precision == PG_MIXED &&
+         (s->cfg.precond != PG_PREC_ILU0 || s->dev().smem_dd > 0);
+}
+
 int factor(pg_solver *s) {
   cudaStream_t st = stream();
   const SolverDev d = s->dev();
-  const bool mixed = s->cfg.precision == PG_MIXED;
+  const bool dd = use_dd(s);
   if (s->cfg.precond == PG_PREC_ILU0) {
     PG_CUDA(cudaMemsetAsync(s->bad.p, 0, sizeof(int), st));
-    launch_ilu0_factor(d, s->pvals.p, s->bad.p, mixed, st);
-    PG_CUDA(cudaGetLastError());
+    launch_ilu0_factor(d, s->pvals.p, s->bad.p, dd, st);
   } else if (s->cfg.precond == PG_PREC_JACOBI) {
     launch_jacobi_diag(d, s->pvals.p, s->jdinv.p, st);
+    if (dd) launch_dd_split(d.n, s->jdinv.p, 1.0, s->jdinv_dd.p, st);
   }
+  if (dd) launch_dd_split(d.nnz, s->pvals.p, 1.0, s->pvals_dd.p, st);
+  PG_CUDA(cudaGetLastError());
   return PG_OK;
 }
 
@@ -564,9 +687,10 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
   const double tol = s->cfg.tolerance;
   const SolverDev d = s->dev();
   const RedWork w = s->red();
-  int status = run_bicgstab(s, tol, s->cfg.max_iters, &iters, &outer);
+  double bb = 0.;
+  int status = use_dd(s) ? run_bicgstab_dd(s, tol, s->cfg.max_iters, &iters, &outer, &bb)
+                         : run_bicgstab(s, tol, s->cfg.max_iters, &iters, &outer, &bb);
   if (status == PG_CUDA_ERROR) return status;
-  const double bb = s->sc_host->bb;
   // final true residual in FP64 and the solution in the caller's order
   launch_true_residual(d, s->pvals.p, s->b.p, s->x.p, nullptr, s->sc.p, w, st);
   launch_unpermute_vec((int)n, s->perm.p, s->x.p, s->xout.p, st);
@@ -625,18 +749,23 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
   const RedWork w = s->red();
   const int64_t n = s->a.n;
   const int g = grid_for(n);
-  const bool fp32_ilu =
-      s->cfg.precision == PG_MIXED && s->cfg.precond == PG_PREC_ILU0;
+  const bool dd = use_dd(s);
   // scratch vectors with benign non-zero contents, so no kernel takes its
   // breakdown/convergence exit; the solver's own state is left untouched
   DevBuf<double> d8[8];
+  DevBuf<float2> f8[8];
   for (int k = 0; k < 8; ++k) {
     PG_CUDA(d8[k].reserve(n));
     k_fill_profile<<<g, 256, 0, st>>>(n, d8[k].p, nullptr, k);
+    if (dd) {
+      PG_CUDA(f8[k].reserve(n));
+      launch_dd_split(n, d8[k].p, 1.0, f8[k].p, st);
+    }
   }
   KScalars k{};
   k.max_iter = 1 << 30;
   k.alpha = k.omega = k.beta = k.rho = k.rho_prev = 1.0;
+  k.alpha_dd = k.omega_dd = k.beta_dd = make_float2(1.f, 0.f);
   k.bb = 1.0;
   *s->sc_host = k;
   PG_CUDA(cudaMemcpyAsync(s->sc.p, s->sc_host, sizeof(KScalars),
@@ -659,9 +788,14 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
   if (!rc) rc = timed([&] { launch_precond<double, double>(s->cfg.precond, 1, d, s->jdinv.p, d8[3].p, d8[4].p, d8[1].p, d8[6].p, s->sc.p, st); }, &ms[1]);
   if (!rc) rc = timed([&] { launch_update<double>(d.n, d8[5].p, d8[3].p, d8[0].p, d8[6].p, d8[4].p, d8[1].p, d8[2].p, s->sc.p, w, st); }, &ms[2]);
   if (!rc && s->cfg.precond == PG_PREC_ILU0)
-    rc = timed([&] { launch_ilu0_factor(d, s->pvals.p, s->bad.p, fp32_ilu, st); }, &ms[3]);
-  if (!rc && fp32_ilu)
-    rc = timed([&] { launch_ilu0_apply_fp32(1, d, d8[3].p, d8[4].p, d8[1].p, d8[6].p, s->sc.p, st); }, &ms[4]);
+    rc = timed([&] { launch_ilu0_factor(d, s->pvals.p, s->bad.p, dd, st); }, &ms[3]);
+  if (!rc && dd) {
+    launch_dd_split(d.nnz, s->pvals.p, 1.0, s->pvals_dd.p, st);
+    if (s->cfg.precond == PG_PREC_ILU0)
+      rc = timed([&] { launch_ilu0_apply_dd(1, d, f8[3].p, f8[4].p, f8[1].p, f8[6].p, s->sc.p, st); }, &ms[4]);
+    if (!rc) rc = timed([&] { launch_dd_spmv_v(d, s->pvals_dd.p, f8[0].p, f8[1].p, f8[2].p, s->sc.p, w, st); }, &ms[5]);
+    if (!rc) rc = timed([&] { launch_dd_update(d.n, f8[5].p, f8[3].p, f8[0].p, f8[6].p, f8[4].p, f8[1].p, f8[2].p, s->sc.p, w, st); }, &ms[6]);
+  }
   PG_CUDA(cudaStreamSynchronize(st));
   return rc;
 }
@@ -683,11 +817,18 @@ extern "C" int pg_solver_apply_precond(pg_solver *s, const double *r,
   }
   // z = M^-1 r in the permuted order (mode 0 reads p, writes ph)
   launch_permute_vec((int)n, s->perm.p, dr, 1.0, s->p.p, st);
-  if (s->cfg.precision == PG_MIXED && s->cfg.precond == PG_PREC_ILU0)
-    launch_ilu0_apply_fp32(0, d, nullptr, s->p.p, nullptr, s->ph.p, nullptr, st);
-  else
+  if (use_dd(s)) {
+    launch_dd_split(n, s->p.p, 1.0, s->pd.p, st);
+    if (s->cfg.precond == PG_PREC_ILU0)
+      launch_ilu0_apply_dd(0, d, nullptr, s->pd.p, nullptr, s->phd.p, nullptr, st);
+    else
+      launch_dd_diag_apply(0, (int)n, s->cfg.precond == PG_PREC_JACOBI ? s->jdinv_dd.p : nullptr,
+                           nullptr, s->pd.p, nullptr, s->phd.p, nullptr, st);
+    launch_dd_join((int)n, s->phd.p, 1.0, s->ph.p, st);
+  } else {
     launch_precond<double, double>(s->cfg.precond, 0, d, s->jdinv.p, nullptr,
                                    s->p.p, nullptr, s->ph.p, nullptr, st);
+  }
   launch_unpermute_vec((int)n, s->perm.p, s->ph.p, s->t.p, st);
   PG_CUDA(cudaGetLastError());
   PG_CUDA(copy_out(z, s->t.p, n * sizeof(double), ptr_kind));
@@ -707,5 +848,435 @@ extern "C" int pg_solver_partition(const pg_solver *s, int32_t *part,
   PG_CHECK_ARG(s && s->analysed, "pg_solver_partition: nothing analysed");
   if (part) std::copy(s->a.part.begin(), s->a.part.end(), part);
   if (n_parts) *n_parts = s->a.n_sub;
+  return PG_OK;
+}
+
+// ------------------------------------------------------------ batched solves
+// Many independent systems (different sizes and patterns) stacked block-
+// diagonally: one analysis (every Schwarz subdomain inside one system), one
+// ILU(0) factorisation launch, and BiCGStab kernels whose CTAs each own a
+// tile of one system's rows with per-system scalars (batch.cu).  The
+// iteration runs as one CUDA graph launch: a WHILE conditional node
+// repeats a chunk of kChunk iterations until the device-side check finds
+// every system stopped (bounded by the chunk budget).  Tile shape (threads
+// per CTA and rows per thread) is chosen per batch by timing the candidate
+// shapes on the batch's own SpMV.
+struct pg_batch {
+  pg_solver *s = nullptr;  // analysis, factor and vector storage
+  int n_sys = 0;
+  std::vector<int64_t> sys_rows;      // original row offsets
+  std::vector<uint64_t> eqn_ids;      // pattern ids of set_eqns systems
+  std::vector<int32_t> h_tile_ptr;
+  DevBuf<int32_t> sub_sys, tile_sys, tile_r0, tile_r1, tile_ptr;
+  DevBuf<double> partials, st_vals, st_rhs;
+  DevBuf<unsigned int> tickets;
+  DevBuf<KScalars> sc;
+  DevBuf<int> flags, chunks;  // flags: [n_sys] init / replacement selector
+  KScalars *sc_host = nullptr;
+  int *flags_host = nullptr;
+  int block = 256, rpt = 1, n_tiles = 0;
+  bool persistent = false;
+  cudaGraphExec_t exec = nullptr;
+  int max_chunks = 0;
+
+  ~pg_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (sc_host) cudaFreeHost(sc_host);
+    if (flags_host) cudaFreeHost(flags_host);
+    if (s) pg_solver_destroy(s);
+  }
+  BatchTiles tiles() const {
+    return BatchTiles{tile_sys.p, tile_r0.p, tile_r1.p, tile_ptr.p, n_tiles};
+  }
+  BatchRed red() const { return BatchRed{partials.p, tickets.p, n_tiles}; }
+  SolverDev dev() const {
+    SolverDev d = s->dev();
+    d.sub_sys = sub_sys.p;
+    return d;
+  }
+};
+
+namespace {
+
+// permuted row range of every system
+std::vector<int32_t> sys_prow(const pg_batch *b) {
+  const Analysis &a = b->s->a;
+  std::vector<int32_t> pr(b->n_sys + 1, (int32_t)a.n);
+  // subdomains are grouped by system in system order
+  std::vector<int32_t> first(b->n_sys, -1);
+  for (int k = 0; k < a.n_sub; ++k) {
+    const int32_t row = a.perm[a.sub_ptr[k]];
+    const int sys = (int)(std::upper_bound(b->sys_rows.begin(),
+                                           b->sys_rows.end(), (int64_t)row) -
+                          b->sys_rows.begin()) - 1;
+    if (first[sys] < 0) first[sys] = a.sub_ptr[k];
+  }
+  for (int i = b->n_sys - 1; i >= 0; --i)
+    pr[i] = first[i] >= 0 ? first[i] : pr[i + 1];
+  return pr;
+}
+
+int build_tiles(pg_batch *b, int block, int rpt) {
+  const std::vector<int32_t> pr = sys_prow(b);
+  std::vector<int32_t> ts, t0, t1, tp(b->n_sys + 1, 0);
+  const int64_t tr = (int64_t)block * rpt;
+  for (int i = 0; i < b->n_sys; ++i) {
+    for (int64_t r = pr[i]; r < pr[i + 1]; r += tr) {
+      ts.push_back(i);
+      t0.push_back((int32_t)r);
+      t1.push_back((int32_t)std::min<int64_t>(r + tr, pr[i + 1]));
+    }
+    tp[i + 1] = (int32_t)ts.size();
+  }
+  cudaError_t e = b->tile_sys.upload(ts);
+  if (e == cudaSuccess) e = b->tile_r0.upload(t0);
+  if (e == cudaSuccess) e = b->tile_r1.upload(t1);
+  if (e == cudaSuccess) e = b->tile_ptr.upload(tp);
+  b->n_tiles = (int)ts.size();
+  if (e == cudaSuccess) e = b->partials.reserve((size_t)kMaxDots * std::max(1, b->n_tiles));
+  if (e != cudaSuccess) return cuda_fail(e, "batch tiles", __FILE__, __LINE__);
+  b->h_tile_ptr = tp;
+  b->block = block;
+  b->rpt = rpt;
+  return PG_OK;
+}
+
+// Tile-shape autotuner: every candidate times the batched SpMV (the
+// dominant row kernel) on this batch's matrix; the fastest shape is kept.
+int autotune(pg_batch *b) {
+  static const int cand[][2] = {{128, 1}, {128, 2}, {128, 4}, {256, 1},
+                                {256, 2}, {256, 4}, {512, 1}, {512, 2}};
+  cudaStream_t st = stream();
+  pg_solver *s = b->s;
+  const int64_t n = s->a.n;
+  // benign scalars: running, finite
+  for (int i = 0; i < b->n_sys; ++i) {
+    KScalars k{};
+    k.rho = k.alpha = k.omega = k.beta = k.rho_prev = 1.;
+    k.max_iter = 1 << 30;
+    b->sc_host[i] = k;
+  }
+  PG_CUDA(cudaMemcpyAsync(b->sc.p, b->sc_host, b->n_sys * sizeof(KScalars),
+                          cudaMemcpyHostToDevice, st));
+  // generic non-zero vectors, so no system takes a breakdown exit
+  k_fill_profile<<<grid_for(n), 256, 0, st>>>(n, s->ph.p, nullptr, 1);
+  k_fill_profile<<<grid_for(n), 256, 0, st>>>(n, s->rh.p, nullptr, 2);
+  count_launches(2);
+  float best = 1e30f;
+  int bb = 256, br = 1;
+  for (const auto &c : cand) {
+    int rc = build_tiles(b, c[0], c[1]);
+    if (rc) return rc;
+    auto run = [&] {
+      launch_b_spmv_v(b->tiles(), b->red(), b->block, s->prp.p, s->pci.p,
+                      s->pvals.p, s->ph.p, s->v.p, s->rh.p, b->sc.p, st);
+    };
+    run();
+    PG_CUDA(cudaEventRecord(s->ev[0], st));
+    for (int k = 0; k < 5; ++k) run();
+    PG_CUDA(cudaEventRecord(s->ev[1], st));
+    PG_CUDA(cudaEventSynchronize(s->ev[1]));
+    PG_CUDA(cudaGetLastError());
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]);
+    if (ms < best) {
+      best = ms;
+      bb = c[0];
+      br = c[1];
+    }
+  }
+  return build_tiles(b, bb, br);
+}
+
+// Analysis of the stacked pattern (when it changed) and the per-batch
+// device state.
+int batch_analyse(pg_batch *b, const std::vector<int32_t> &rp,
+                  const std::vector<int32_t> &ci) {
+  pg_solver *s = b->s;
+  const int64_t n = (int64_t)rp.size() - 1;
+  int rc = analyse(n, rp.data(), ci.data(), s->cfg.subdomain_rows, s->a,
+                   &b->sys_rows);
+  if (rc) return rc;
+  s->rank = n;
+  rc = upload_analysis(s);
+  if (rc) return rc;
+  s->eqn_pattern = 0;
+  // system of every subdomain
+  std::vector<int32_t> ss(s->a.n_sub);
+  for (int k = 0; k < s->a.n_sub; ++k) {
+    const int32_t row = s->a.perm[s->a.sub_ptr[k]];
+    ss[k] = (int32_t)(std::upper_bound(b->sys_rows.begin(), b->sys_rows.end(),
+                                       (int64_t)row) - b->sys_rows.begin()) - 1;
+  }
+  PG_CUDA(b->sub_sys.upload(ss));
+  PG_CUDA(b->sc.reserve(b->n_sys));
+  PG_CUDA(b->tickets.zero(b->n_sys));
+  PG_CUDA(b->flags.reserve(b->n_sys));
+  PG_CUDA(b->chunks.zero(1));
+  if (b->sc_host) cudaFreeHost(b->sc_host);
+  if (b->flags_host) cudaFreeHost(b->flags_host);
+  b->sc_host = nullptr;
+  b->flags_host = nullptr;
+  PG_CUDA(cudaMallocHost((void **)&b->sc_host, b->n_sys * sizeof(KScalars)));
+  PG_CUDA(cudaMallocHost((void **)&b->flags_host, b->n_sys * sizeof(int)));
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  return PG_OK;
+}
+
+// The whole iteration as one graph: WHILE(cond) { kChunk iterations; check }
+int build_batch_graph(pg_batch *b) {
+  cudaStream_t st = stream();
+  pg_solver *s = b->s;
+  const SolverDev d = b->dev();
+  const BatchTiles T = b->tiles();
+  const BatchRed R = b->red();
+  cudaGraph_t g = nullptr;
+  PG_CUDA(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle h;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+  cudaGraphNodeParams prm = {};
+  prm.type = cudaGraphNodeTypeConditional;
+  prm.conditional.handle = h;
+  prm.conditional.type = cudaGraphCondTypeWhile;
+  prm.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &prm);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return cuda_fail(e, "batch graph conditional node", __FILE__, __LINE__);
+  }
+  cudaGraph_t body = prm.conditional.phGraph_out[0];
+  const uint64_t before = launch_count();
+  e = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeRelaxed);
+  if (e == cudaSuccess) {
+    for (int c = 0; c < kChunk; ++c) {
+      launch_precond<double, double>(PG_PREC_ILU0, 1, d, nullptr, s->r.p,
+                                     s->p.p, s->v.p, s->ph.p, b->sc.p, st);
+      launch_b_spmv_v(T, R, b->block, s->prp.p, s->pci.p, s->pvals.p, s->ph.p,
+                      s->v.p, s->rh.p, b->sc.p, st);
+      launch_precond<double, double>(PG_PREC_ILU0, 2, d, nullptr, s->r.p,
+                                     s->s.p, s->v.p, s->sh.p, b->sc.p, st);
+      launch_b_spmv_t(T, R, b->block, s->prp.p, s->pci.p, s->pvals.p, s->sh.p,
+                      s->t.p, s->s.p, b->sc.p, st);
+      launch_b_update(T, R, b->block, s->x.p, s->r.p, s->ph.p, s->sh.p,
+                      s->s.p, s->t.p, s->rh.p, b->sc.p, st);
+    }
+    launch_b_fix(T, R, b->block, s->prp.p, s->pci.p, s->pvals.p, s->b.p,
+                 s->x.p, s->r.p, s->rh.p, s->p.p, s->v.p, b->sc.p, st);
+    launch_b_check(b->n_sys, b->sc.p, b->chunks.p, b->max_chunks, h, st);
+    cudaGraph_t captured = nullptr;
+    e = cudaStreamEndCapture(st, &captured);
+  }
+  // capture issues nothing: the replays are counted per chunk at solve time
+  count_launches(-(int)(launch_count() - before));
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    b->exec = nullptr;
+    return cuda_fail(e, "batch graph", __FILE__, __LINE__);
+  }
+  b->persistent = true;
+  return PG_OK;
+}
+
+}  // namespace
+
+extern "C" int pg_batch_create(const pg_solver_cfg *cfg, pg_batch **out) {
+  PG_CHECK_ARG(out, "pg_batch_create: out is NULL");
+  *out = nullptr;
+  pg_solver_cfg c;
+  pg_solver_default_cfg(&c);
+  if (cfg) c = *cfg;
+  PG_CHECK_ARG(c.precond == PG_PREC_ILU0,
+               "pg_batch_create: batched solves use the Schwarz ILU(0) "
+               "preconditioner");
+  PG_CHECK_ARG(c.precision == PG_FP64,
+               "pg_batch_create: batched solves run in FP64");
+  auto *b = new (std::nothrow) pg_batch();
+  PG_CHECK_ARG(b, "pg_batch_create: out of host memory");
+  int rc = pg_solver_create(&c, &b->s);
+  if (rc) {
+    delete b;
+    return rc;
+  }
+  *out = b;
+  return PG_OK;
+}
+
+extern "C" int pg_batch_destroy(pg_batch *b) {
+  if (b) cudaStreamSynchronize(stream());
+  delete b;
+  return PG_OK;
+}
+
+extern "C" int pg_batch_set_eqns(pg_batch *b, int n_systems,
+                                 const pg_eqn *const *eqns) {
+  PG_CHECK_ARG(b && eqns && n_systems > 0, "pg_batch_set_eqns: bad argument");
+  std::vector<uint64_t> ids(n_systems);
+  std::vector<int64_t> rows(n_systems + 1, 0), ents(n_systems + 1, 0);
+  for (int i = 0; i < n_systems; ++i) {
+    PG_CHECK_ARG(eqns[i] && !eqns[i]->momentum,
+                 "pg_batch_set_eqns: NULL or momentum equation");
+    ids[i] = eqns[i]->pattern_id;
+    rows[i + 1] = rows[i] + eqns[i]->p.n;
+    ents[i + 1] = ents[i] + eqns[i]->p.nnz;
+  }
+  PG_CHECK_ARG(rows[n_systems] < ((int64_t)1 << 31) &&
+                   ents[n_systems] < ((int64_t)1 << 31),
+               "pg_batch_set_eqns: batch too large");
+  pg_solver *s = b->s;
+  cudaStream_t st = stream();
+  if (!s->analysed || ids != b->eqn_ids) {
+    b->n_sys = n_systems;
+    b->sys_rows = rows;
+    std::vector<int32_t> rp(rows[n_systems] + 1, 0), ci(ents[n_systems]);
+    for (int i = 0; i < n_systems; ++i) {
+      const EqnPattern &p = eqns[i]->p;
+      for (int64_t r = 0; r < p.n; ++r)
+        rp[rows[i] + r + 1] = (int32_t)(ents[i] + p.row_ptr[r + 1]);
+      for (int64_t k = 0; k < p.nnz; ++k)
+        ci[ents[i] + k] = (int32_t)(p.col_ind[k] + rows[i]);
+    }
+    int rc = batch_analyse(b, rp, ci);
+    if (rc) return rc;
+    b->eqn_ids = ids;
+    PG_CUDA(b->st_vals.reserve(ents[n_systems]));
+    PG_CUDA(b->st_rhs.reserve(rows[n_systems]));
+    // values for the autotuner's timing
+    for (int i = 0; i < n_systems; ++i)
+      PG_CUDA(cudaMemcpyAsync(b->st_vals.p + ents[i], eqns[i]->vals.p,
+                              eqns[i]->p.nnz * sizeof(double),
+                              cudaMemcpyDeviceToDevice, st));
+    launch_permute_values((int)s->a.nnz, s->psrc.p, b->st_vals.p, s->pvals.p,
+                          (int)s->a.dup_dst.size(), s->dup_dst.p,
+                          s->dup_src.p, st);
+    rc = autotune(b);
+    if (rc) return rc;
+  }
+  for (int i = 0; i < n_systems; ++i) {
+    PG_CUDA(cudaMemcpyAsync(b->st_vals.p + ents[i], eqns[i]->vals.p,
+                            eqns[i]->p.nnz * sizeof(double),
+                            cudaMemcpyDeviceToDevice, st));
+    PG_CUDA(cudaMemcpyAsync(b->st_rhs.p + rows[i], eqns[i]->rhs.p,
+                            eqns[i]->p.n * sizeof(double),
+                            cudaMemcpyDeviceToDevice, st));
+  }
+  launch_permute_values((int)s->a.nnz, s->psrc.p, b->st_vals.p, s->pvals.p,
+                        (int)s->a.dup_dst.size(), s->dup_dst.p, s->dup_src.p,
+                        st);
+  // the solver receives -rhs_ (FiniteVolumeEquation.tpp:73)
+  launch_permute_vec((int)s->a.n, s->perm.p, b->st_rhs.p, -1.0, s->b.p, st);
+  PG_CUDA(cudaGetLastError());
+  s->have_vals = true;
+  s->have_rhs = true;
+  return PG_OK;
+}
+
+extern "C" int pg_batch_solve(pg_batch *b, pg_solve_stats *stats,
+                              double *ms_total) {
+  PG_CHECK_ARG(b && b->s && b->s->analysed && b->s->have_vals && b->s->have_rhs,
+               "pg_batch_solve: set the systems first");
+  pg_solver *s = b->s;
+  cudaStream_t st = stream();
+  const int64_t n = s->a.n;
+  const int S = b->n_sys;
+  const SolverDev d = b->dev();
+  const BatchTiles T = b->tiles();
+  const BatchRed R = b->red();
+  b->max_chunks = (s->cfg.max_iters + kChunk - 1) / kChunk + 1;
+  if (!b->exec) {
+    int rc = build_batch_graph(b);
+    if (rc) return rc;
+  }
+  PG_CUDA(cudaEventRecord(s->ev[0], st));
+  PG_CUDA(cudaMemsetAsync(s->bad.p, 0, sizeof(int), st));
+  launch_ilu0_factor(d, s->pvals.p, s->bad.p, false, st);
+  for (int i = 0; i < S; ++i) {
+    KScalars k{};
+    k.tol2 = s->cfg.tolerance * s->cfg.tolerance;
+    k.max_iter = s->cfg.max_iters;
+    b->sc_host[i] = k;
+    b->flags_host[i] = 1;
+  }
+  PG_CUDA(cudaMemcpyAsync(b->sc.p, b->sc_host, S * sizeof(KScalars),
+                          cudaMemcpyHostToDevice, st));
+  PG_CUDA(cudaMemcpyAsync(b->flags.p, b->flags_host, S * sizeof(int),
+                          cudaMemcpyHostToDevice, st));
+  PG_CUDA(cudaMemsetAsync(s->x.p, 0, n * sizeof(double), st));
+  launch_b_init(T, R, b->block, s->prp.p, s->pci.p, s->pvals.p, s->b.p,
+                nullptr, s->r.p, s->rh.p, s->p.p, s->v.p, b->sc.p, b->flags.p,
+                st);
+  for (;;) {
+    PG_CUDA(cudaMemsetAsync(b->chunks.p, 0, sizeof(int), st));
+    PG_CUDA(cudaGraphLaunch(b->exec, st));
+    // the graph's launches are counted when it was captured; count the
+    // replays by the chunks the device ran
+    int ch = 0;
+    PG_CUDA(cudaMemcpyAsync(&ch, b->chunks.p, sizeof(int),
+                            cudaMemcpyDeviceToHost, st));
+    // confirm every converged system on its true residual
+    launch_b_true_residual(T, R, b->block, s->prp.p, s->pci.p, s->pvals.p,
+                           s->b.p, s->x.p, nullptr, nullptr, b->sc.p, nullptr,
+                           st);
+    PG_CUDA(cudaMemcpyAsync(b->sc_host, b->sc.p, S * sizeof(KScalars),
+                            cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    count_launches((5 * kChunk + 2) * ch);
+    break;
+  }
+  launch_unpermute_vec((int)n, s->perm.p, s->x.p, s->xout.p, st);
+  PG_CUDA(cudaEventRecord(s->ev[2], st));
+  PG_CUDA(cudaEventSynchronize(s->ev[2]));
+  PG_CUDA(cudaGetLastError());
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, s->ev[0], s->ev[2]);
+  if (ms_total) *ms_total = ms;
+  int timed_out = 0;
+  PG_CUDA(cudaMemcpy(&timed_out, s->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (timed_out) PG_CUDA(cudaMemset(s->err.p, 0, sizeof(int)));
+  int worst = PG_OK;
+  for (int i = 0; i < S; ++i) {
+    const KScalars &k = b->sc_host[i];
+    const double rel = k.bb > 0. ? std::sqrt(k.rr_true / k.bb) : 0.;
+    int status = k.status;
+    if (status == PG_OK && !(rel <= s->cfg.tolerance)) status = PG_MAX_ITERS;
+    if (!std::isfinite(rel)) status = PG_NON_FINITE;
+    if (timed_out) status = PG_TIMEOUT;
+    if (stats) {
+      stats[i].iters = k.iter;
+      stats[i].outer_iters = k.restarts + 1;
+      stats[i].status = status;
+      stats[i].rel_residual = rel;
+      stats[i].ms = ms;
+      stats[i].setup_ms = 0.;
+    }
+    if (status != PG_OK && worst == PG_OK) worst = status;
+  }
+  if (worst != PG_OK)
+    set_error("pg_batch_solve: a system stopped with status " +
+              std::to_string(worst));
+  return worst;
+}
+
+extern "C" int pg_batch_get_x(const pg_batch *b, int system, double *x,
+                              int ptr_kind) {
+  PG_CHECK_ARG(b && x && system >= 0 && system < b->n_sys,
+               "pg_batch_get_x: bad argument");
+  const int64_t r0 = b->sys_rows[system], r1 = b->sys_rows[system + 1];
+  PG_CUDA(copy_out(x, b->s->xout.p + r0, (r1 - r0) * sizeof(double), ptr_kind));
+  PG_CUDA(cudaStreamSynchronize(stream()));
+  return PG_OK;
+}
+
+extern "C" int pg_batch_tuning(const pg_batch *b, int *block,
+                               int *rows_per_thread, int *n_tiles) {
+  PG_CHECK_ARG(b, "pg_batch_tuning: NULL batch");
+  if (block) *block = b->block;
+  if (rows_per_thread) *rows_per_thread = b->rpt;
+  if (n_tiles) *n_tiles = b->n_tiles;
   return PG_OK;
 }

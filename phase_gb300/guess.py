@@ -216,8 +216,7 @@ def train(nx=1024, steps=2000, epochs=3, lr=2e-3, out=DEFAULT_WEIGHTS,
     n_train = int(0.8 * steps)
     n_val = int(0.1 * steps)
     # 1. dump triples with the plain solver (warm-started, as in a time loop)
-    solver = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
-                                   precision=pg.MIXED)
+    solver = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000)
     xs = torch.zeros((steps + 1, n), dtype=torch.float64, device=dev)
     torch.cuda.synchronize()
     t0 = time.time()
@@ -267,14 +266,14 @@ def train(nx=1024, steps=2000, epochs=3, lr=2e-3, out=DEFAULT_WEIGHTS,
     return report
 
 
-def evaluate(seq, net, xs, test, log=print):
+def evaluate(seq, net, xs, test, log=print, precisions=("fp64",)):
     """Iterations and device ms of the held-out steps for the three guesses
-    with the FP64 and the mixed solver."""
+    (zero, previous step's solution, learned) with the given solvers."""
     import torch
     pg = _pg()
     n = seq.n
     res = {}
-    for prec in ("fp64", "mixed"):
+    for prec in precisions:
         s = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
                                   precision=pg.FP64 if prec == "fp64" else pg.MIXED)
         rows = {"zero": [], "previous": [], "learned": []}

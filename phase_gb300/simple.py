@@ -40,18 +40,15 @@ def cavity_inputs(nx=80, ny=80, lid=1.0, faces=None):
     return out
 
 
-def simple_pcorr(pg, nx=80, ny=80, rho=1.0, mu=0.01, dt=0.005, lid=1.0,
-                 tol=1e-12):
-    """Run the predictor on the device and return the pCorr equation and
-    the intermediate fields."""
-    w = cavity_inputs(nx, ny, lid)
-    mesh = pg.Mesh(w["nodes"], w["cptr"], w["cind"])
+def predictor_pcorr(pg, mesh, bc_u, u_face, u0, bc_p, p_value, rho, mu, dt,
+                    tol=1e-12):
+    """Momentum predictor from u0 (cells) with boundary velocities u_face,
+    then the pCorr equation laplacian(rho d_f, pCorr) == div(rho u*_f) with
+    pressure boundary types bc_p and values p_value (per face)."""
     faces, cells = mesh.faces(), mesh.cells()
-    w = cavity_inputs(nx, ny, lid, faces)
-    n, nf = mesh.n_cells, mesh.n_faces
-    u0 = np.zeros((n, 2))
-    mom = pg.MomentumEquation(mesh, w["bc_u"]).assemble(
-        dt, mu / rho, 1.0, u0, w["u_face"])
+    n = mesh.n_cells
+    mom = pg.MomentumEquation(mesh, bc_u).assemble(dt, mu / rho, 1.0, u0,
+                                                   u_face)
     rp, ci, v, rhs = mom.export()
     s = pg.SparseMatrixSolver(tolerance=tol, max_iters=5000)
     s.setRank(n)
@@ -69,7 +66,52 @@ def simple_pcorr(pg, nx=80, ny=80, rho=1.0, mu=0.01, dt=0.005, lid=1.0,
     uf = np.stack([mesh.interpolate_faces(u[:, 0]),
                    mesh.interpolate_faces(u[:, 1])], 1)
     bnd = faces["rcell"] < 0
-    uf[bnd] = w["u_face"][bnd]
-    eqn = pg.fv.laplacian(gamma_f, mesh, w["bc_p"], None, rho * uf)
+    uf[bnd] = u_face[bnd]
+    eqn = pg.fv.laplacian(gamma_f, mesh, bc_p, p_value, rho * uf)
     return dict(mesh=mesh, eqn=eqn, u=u, d=dcoef, gamma_f=gamma_f, u_face=uf,
-                momentum=(rp, ci, v, rhs), inputs=w)
+                momentum=(rp, ci, v, rhs))
+
+
+def simple_pcorr(pg, nx=80, ny=80, rho=1.0, mu=0.01, dt=0.005, lid=1.0,
+                 tol=1e-12):
+    """Run the predictor on the device and return the pCorr equation and
+    the intermediate fields."""
+    w = cavity_inputs(nx, ny, lid)
+    mesh = pg.Mesh(w["nodes"], w["cptr"], w["cind"])
+    w = cavity_inputs(nx, ny, lid, mesh.faces())
+    u0 = np.zeros((mesh.n_cells, 2))
+    out = predictor_pcorr(pg, mesh, w["bc_u"], w["u_face"], u0, w["bc_p"],
+                          None, rho, mu, dt, tol)
+    out["inputs"] = w
+    return out
+
+
+def cylinder_pcorr(pg, mesh_args=None, u_in=1.0, re=100.0, rho=1.0, dt=0.01,
+                   tol=1e-10):
+    """The pressure-correction system of one PISO-style predictor step of
+    the flow around a cylinder (D = 1, Re = u_in D / nu) on the graded
+    triangle mesh of meshes.cylinder_channel, boundary types as
+    Examples/UnstructuredFlowAroundCylinder/case/boundaries.info: u fixed
+    (u_in, 0) at the inlet and 0 on the cylinder, normal gradient at the
+    outlet and on the top/bottom; p fixed 0 at the outlet and top/bottom,
+    normal gradient at the inlet and on the cylinder.  Starts from the
+    uniform inflow u = (u_in, 0)."""
+    from . import meshes
+    nodes, cptr, cind = meshes.cylinder_channel(**(mesh_args or {}))
+    mesh = pg.Mesh(nodes, cptr, cind)
+    f = mesh.faces()
+    patch = meshes.cylinder_patch_of_faces(f["fx"], f["fy"], f["rcell"])
+    nf, n = mesh.n_faces, mesh.n_cells
+    bc_u = np.ones(nf, np.int32)                       # NORMAL_GRADIENT
+    bc_u[(patch == 0) | (patch == 3)] = 0              # FIXED
+    u_face = np.zeros((nf, 2))
+    u_face[patch == 0, 0] = u_in
+    u_face[patch < 0, 0] = u_in
+    bc_p = np.ones(nf, np.int32)
+    bc_p[(patch == 1) | (patch == 2)] = 0
+    u0 = np.zeros((n, 2))
+    u0[:, 0] = u_in
+    out = predictor_pcorr(pg, mesh, bc_u, u_face, u0, bc_p, np.zeros(nf),
+                          rho, u_in * 1.0 / re * rho, dt, tol)
+    out.update(patch=patch, nodes=nodes, cptr=cptr, cind=cind)
+    return out

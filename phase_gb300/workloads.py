@@ -80,3 +80,57 @@ def rising_bubble(nx=1024, ny=1024, seed=3, faces=None, cells=None):
         out.update(bc_type=bc_type, bc_value=bc_value, patch=patch)
         out["u"] = divergent_velocity(faces, patch, seed)
     return out
+
+
+# ---------------------------------------------------------------------------
+# Ghost-cell immersed-boundary channels (batched solves): the pressure
+# equation of FractionalStepGCIB, (fv::laplacian(dt/rho, p) + ib.bcs(p)) ==
+# src::div(u), on a quad channel [0, 3H] x [0, H] with one cylinder.
+GC_HEIGHT = 2.0
+GC_LENGTH = 3.0 * GC_HEIGHT
+
+
+def gcib_specs(n_systems=256, seed=5, min_cells=2_000, max_cells=200_000):
+    """Seeded case list: cell counts log-uniform in [min_cells, max_cells]
+    (ny rows, nx = 3 ny columns), cylinder radius uniform in [0.1, 0.5],
+    centre uniform in the channel interior with a margin that keeps every
+    image-point stencil inside the mesh."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_systems):
+        n = float(np.exp(rng.uniform(np.log(min_cells), np.log(max_cells))))
+        ny = max(8, int(round(np.sqrt(n / 3.0))))
+        nx = 3 * ny
+        h = GC_HEIGHT / ny
+        r = float(rng.uniform(0.1, 0.5))
+        m = r + 4.0 * h + 0.05
+        cx = float(rng.uniform(1.0, GC_LENGTH - 2.0))
+        cy = float(rng.uniform(m, GC_HEIGHT - m))
+        out.append(dict(nx=nx, ny=ny, circle=(cx, cy, r),
+                        seed=int(rng.integers(1 << 30))))
+    return out
+
+
+def gcib_case(spec, faces=None):
+    """Mesh arrays and, given the mesh's faces, the inputs of one case:
+    p FIXED 0 at the outlet (x+), NORMAL_GRADIENT elsewhere; scalar
+    coefficient dt/rho = 1e-3; u* a seeded divergent field (inflow 1 at x-,
+    no slip on the walls)."""
+    nx, ny = spec["nx"], spec["ny"]
+    nodes, cptr, cind = meshes.rectilinear(nx, ny, GC_LENGTH, GC_HEIGHT)
+    out = dict(nodes=nodes, cptr=cptr, cind=cind, circle=spec["circle"],
+               gamma=1e-3)
+    if faces is not None:
+        patch = meshes.rect_patch_of_faces(faces["fx"], faces["fy"],
+                                           faces["rcell"], GC_LENGTH, GC_HEIGHT)
+        bc = np.ones(patch.shape, np.int32)
+        bc[patch == 1] = 0
+        rng = np.random.default_rng(spec["seed"])
+        x, y = faces["fx"], faces["fy"]
+        u = np.zeros((x.size, 2))
+        u[:, 0] = 4.0 * y * (GC_HEIGHT - y) / GC_HEIGHT ** 2
+        u += 0.05 * rng.standard_normal(u.shape)
+        u[(patch == 2) | (patch == 3)] = 0.0
+        out.update(bc_type=bc, bc_value=np.zeros(patch.shape), u=u,
+                   patch=patch)
+    return out

@@ -83,6 +83,9 @@ def lib():
         L.or_spmv.argtypes = [I64, P, P, P, P, P]
         L.or_momentum.restype = P
         L.or_momentum.argtypes = [P, D, D, D, P, P, P]
+        L.or_gcib_laplacian.restype = P
+        L.or_gcib_laplacian.argtypes = [P, P, D, P, P, P, ctypes.c_int, P,
+                                        ctypes.c_int, D, P]
         _lib = L
     return _lib
 
@@ -165,6 +168,34 @@ class OracleMesh:
             e, ptr(rp), ptr(ci), ptr(v), ptr(rhs))
         lib().or_eqn_destroy(e)
         return rp, ci, v, rhs
+
+    def gcib_laplacian(self, gamma, bc_type, bc_value, u_face, circles,
+                       ib_bc=1, ib_ref=0.0):
+        """(fv::laplacian(gamma, p) + ib.bcs(p)) == src::div(u) with
+        ghost-cell IB circles [(cx, cy, r), ...]: (row_ptr, col, vals, rhs,
+        cell class 0 fluid / 1 IB / 2 solid)."""
+        face = not np.isscalar(gamma)
+        g = np.ascontiguousarray(gamma, np.float64) if face else None
+        bc = np.ascontiguousarray(bc_type, np.int32)
+        bv = np.ascontiguousarray(bc_value, np.float64)
+        u = None if u_face is None else np.ascontiguousarray(u_face, np.float64)
+        c = np.ascontiguousarray(np.asarray(circles, np.float64).reshape(-1, 3))
+        cls = np.empty(self.n_cells, np.int32)
+        e = lib().or_gcib_laplacian(self.h, ptr(g), 0.0 if face else float(gamma),
+                                    ptr(bc), ptr(bv), ptr(u), len(c), ptr(c),
+                                    int(ib_bc), float(ib_ref), ptr(cls))
+        if not e:
+            raise RuntimeError("or_gcib_laplacian: degenerate IB stencil")
+        s = np.zeros(3, np.int64)
+        lib().or_eqn_sizes(e, ptr(s[0:1]), ptr(s[1:2]), ptr(s[2:3]))
+        n, ns, nnz = map(int, s)
+        rp = np.empty(n + 1, np.int32)
+        ci = np.empty(nnz, np.int32)
+        v = np.empty(nnz)
+        rhs = np.empty(n)
+        lib().or_eqn_export_csr(e, ptr(rp), ptr(ci), ptr(v), ptr(rhs))
+        lib().or_eqn_destroy(e)
+        return rp, ci, v, rhs, cls
 
     def momentum(self, dt, nu, theta, u_old_cell, u_face, bc_type):
         """ddt + div - laplacian(nu) of the vector equation: compact CSR of

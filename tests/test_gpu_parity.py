@@ -163,10 +163,9 @@ def _bubble_system(pg, nx, ny):
 @pytest.mark.parametrize("mesh", ["bubble", "tri"])
 def test_ilu_apply_matches_oracle(pg, oracle, precision, mesh):
     """The Schwarz ILU(0) sweeps alone, z = M^-1 r, against the oracle's
-    factor and triangular solves on the device's own partition.  FP64
-    factors: 1e-12 relative (the factor's FP64 operation order differs);
-    FP32 factors and sweeps: 2e-5 relative (single-precision rounding
-    through the level chains of these well-conditioned blocks)."""
+    factor and triangular solves on the device's own partition.  FP64:
+    1e-12 relative (the factor's FP64 operation order differs); float-float
+    factors and sweeps (about 48-bit arithmetic): 1e-10 relative."""
     if mesh == "bubble":
         rp, ci, v, rhs = _bubble_system(pg, 128, 96)
         sub = 1024
@@ -186,7 +185,7 @@ def test_ilu_apply_matches_oracle(pg, oracle, precision, mesh):
     lu, rc = oracle.ilu0(rp, ci, v, part)
     assert rc == 0
     rng = np.random.default_rng(5)
-    tol = 1e-12 if precision == "fp64" else 2e-5
+    tol = 1e-12 if precision == "fp64" else 1e-10
     for r in (rng.standard_normal(n), -rhs):
         z = s.apply_precond(r)
         zo = oracle.ilu0_apply(rp, ci, lu, r, part)
