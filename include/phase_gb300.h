@@ -254,7 +254,9 @@ typedef struct {
   int subdomain_rows; /* target rows per Schwarz subdomain; 0 = default;
                          -1 = one subdomain (global ILU(0)) */
   int precision;      /* PG_FP64 | PG_MIXED */
-  int reserved_i;     /* ignored; keeps the layout fixed */
+  int mixed_sweep;    /* PG_MIXED ILU(0) sweep form: 0 = timed choice at the
+                         first factorisation, 1 = warp-wide steps, 2 = level
+                         blobs */
   double reserved_d;  /* ignored */
 } pg_solver_cfg;
 

@@ -43,7 +43,7 @@ class PhaseError(RuntimeError):
 class SolverCfg(ctypes.Structure):
     _fields_ = [("tolerance", ctypes.c_double), ("max_iters", ctypes.c_int),
                 ("precond", ctypes.c_int), ("subdomain_rows", ctypes.c_int),
-                ("precision", ctypes.c_int), ("reserved_i", ctypes.c_int),
+                ("precision", ctypes.c_int), ("mixed_sweep", ctypes.c_int),
                 ("reserved_d", ctypes.c_double)]
 
 
@@ -418,6 +418,13 @@ class SparseMatrixSolver:
         """set() with device pointers (e.g. torch.Tensor.data_ptr())."""
         _check(lib().pg_solver_set_csr(self._h, _P(row_ptr), _P(col_ind),
                                        _P(vals), PG_DEVICE))
+
+    def setGuess_device(self, ptr: int):
+        """Initial guess from device memory at ptr (0 = zero guess)."""
+        if not ptr:
+            _check(lib().pg_solver_set_guess(self._h, None, PG_HOST))
+        else:
+            _check(lib().pg_solver_set_guess(self._h, _P(ptr), PG_DEVICE))
 
     def x_device(self, out_ptr: int):
         """Copy the solution into device memory at out_ptr."""

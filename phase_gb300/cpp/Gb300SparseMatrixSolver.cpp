@@ -117,6 +117,7 @@ void Gb300SparseMatrixSolver::setup(const boost::property_tree::ptree &p) {
   cfg_.subdomain_rows = p.get<int>("subdomainRows", 0);
   cfg_.precision =
       p.get<std::string>("precision", "fp64") == "mixed" ? PG_MIXED : PG_FP64;
+  cfg_.mixed_sweep = p.get<int>("mixedSweep", 0);
   recreate();
 }
 

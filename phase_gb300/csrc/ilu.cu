@@ -157,18 +157,77 @@ __device__ __forceinline__ void sweep_level(VT *zs, int a, int w, int ks,
   }
 }
 
+// One level of a sweep in float-float arithmetic (dd.cuh): the products
+// are accumulated with the compensated Dot2 scheme, so the level's serial
+// dependence is one FP32 add per entry.
+template <int KT>
+__device__ __forceinline__ void sweep_level_dd(float2 *zs, int a, int w,
+                                               int ks, const uint16_t *cc,
+                                               const float2 *vv,
+                                               const float2 *dd, int lane) {
+  const int K = KT > 0 ? KT : ks;
+  for (int t = lane; t < w; t += 32) {
+    DdAcc acc = dd_acc(zs[a + t]);
+    if (KT > 0) {
+#pragma unroll
+      for (int k = 0; k < (KT > 0 ? KT : 1); ++k)
+        dd_acc_fma(acc, dd_neg(vv[k * w + t]), zs[cc[k * w + t]]);
+    } else {
+      for (int k = 0; k < K; ++k)
+        dd_acc_fma(acc, dd_neg(vv[k * w + t]), zs[cc[k * w + t]]);
+    }
+    const float2 out = dd_value(acc);
+    zs[a + t] = dd ? dd_mul(out, dd[t]) : out;
+  }
+}
+
+// Arithmetic of the streamed sweep: FP64, or float-float on the same
+// record layout (a float pair takes the 8 bytes of a double).
+struct ArithF64 {
+  using V = double;
+  __device__ static V pre(int mode, int i, const V *r, V *pv, const V *v,
+                          const KScalars *sc) {
+    return pre_input<double>(mode, i, r, pv, v, sc);
+  }
+  __device__ static V zero() { return 0.; }
+  template <int KT>
+  __device__ static void level(V *zs, int a, int w, int ks,
+                               const uint16_t *cc, const V *vv, const V *dd,
+                               int lane) {
+    sweep_level<double, double, KT>(zs, a, w, ks, cc, vv, dd, lane);
+  }
+};
+struct ArithDD {
+  using V = float2;
+  __device__ static V pre(int mode, int i, const V *r, V *pv, const V *v,
+                          const KScalars *sc) {
+    return dd_pre_input(mode, i, r, pv, v, sc);
+  }
+  __device__ static V zero() { return make_float2(0.f, 0.f); }
+  template <int KT>
+  __device__ static void level(V *zs, int a, int w, int ks,
+                               const uint16_t *cc, const V *vv, const V *dd,
+                               int lane) {
+    sweep_level_dd<KT>(zs, a, w, ks, cc, vv, dd, lane);
+  }
+};
+
 // Forward/backward sweeps of one subdomain by one warp (see file header).
 // Shared memory: header | piece buffer 0 | piece buffer 1 | z[nr+1].  Piece
 // j+2 is loaded into the buffer piece j used while piece j+1 is being
 // swept.  KLT/KUT fix the L/U slot counts at compile time (0 = from meta).
-template <class VT, class MT, int MODE, int KLT, int KUT>
+template <class AR, int MODE, int KLT, int KUT>
 __global__ void __launch_bounds__(32)
 k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
-                    const uint8_t *__restrict__ rec, const VT *__restrict__ r,
-                    VT *__restrict__ pv, const VT *__restrict__ v,
-                    VT *__restrict__ z, const KScalars *__restrict__ sc_base,
+                    const uint8_t *__restrict__ rec,
+                    const typename AR::V *__restrict__ r,
+                    typename AR::V *__restrict__ pv,
+                    const typename AR::V *__restrict__ v,
+                    typename AR::V *__restrict__ z,
+                    const KScalars *__restrict__ sc_base,
                     const int32_t *__restrict__ sub_sys,
                     int *__restrict__ err) {
+  using MT = typename AR::V;
   // batched solves: the scalars of this subdomain's system
   const KScalars *sc =
       sc_base && sub_sys ? sc_base + sub_sys[blockIdx.x] : sc_base;
@@ -191,8 +250,8 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
     bulk_load(hdr, g, (uint32_t)m.hdr_bytes, &bar[2]);
   }
   for (int i = lane; i < nr; i += 32)
-    zs[i] = (MT)pre_input<VT>(MODE, m.r0 + i, r, pv, v, sc);
-  if (lane == 0) zs[nr] = (MT)0;
+    zs[i] = AR::pre(MODE, m.r0 + i, r, pv, v, sc);
+  if (lane == 0) zs[nr] = AR::zero();
   __syncwarp();
   if (!mbar_wait_bounded(&bar[2], err)) return;
   const uint16_t *lvl = reinterpret_cast<const uint16_t *>(hdr);
@@ -224,7 +283,7 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
       for (int l = tab[3 * j]; l < l1; ++l) {
         const int b = lvl[l + 1], w = b - a;
         const int ca = al16(2 * KL * w);
-        sweep_level<MT, MT, KLT>(zs, a, w, KL,
+        AR::template level<KLT>(zs, a, w, KL,
                                  reinterpret_cast<const uint16_t *>(pc),
                                  reinterpret_cast<const MT *>(pc + ca),
                                  (const MT *)nullptr, lane);
@@ -239,7 +298,7 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
       for (int l = lhi; l >= llo; --l) {
         const int a = lvl[l], w = b - a;
         const int ca = al16(2 * KU * w), va = al16(vs * KU * w);
-        sweep_level<MT, MT, KUT>(zs, a, w, KU,
+        AR::template level<KUT>(zs, a, w, KU,
                                  reinterpret_cast<const uint16_t *>(pc),
                                  reinterpret_cast<const MT *>(pc + ca),
                                  reinterpret_cast<const MT *>(pc + ca + va),
@@ -258,7 +317,7 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
                 (uint32_t)tab[3 * (j + 2) + 2], &bar[sb]);
     }
   }
-  for (int i = lane; i < nr; i += 32) z[m.r0 + i] = (VT)zs[i];
+  for (int i = lane; i < nr; i += 32) z[m.r0 + i] = zs[i];
 }
 
 // Float-float step-form sweeps (kernels.cuh StepMeta) of the mixed
@@ -408,7 +467,7 @@ __global__ void k_ilu0_apply_global(const SubMeta *__restrict__ meta,
   }
 }
 
-// Packs the FP64 factor into a streaming record (FP64 or FP32 values).
+// Packs the FP64 factor into the FP64 streaming record.
 template <class MT>
 __global__ void k_pack_stream(int n, const int32_t *__restrict__ src,
                               const int32_t *__restrict__ dst,
@@ -429,18 +488,20 @@ __global__ void k_pack_dd(int n, const int32_t *__restrict__ src,
     out[dst[e]] = dd_from(factor[src[e]]);
 }
 
-template <class VT, class MT, int MODE, int KLT, int KUT>
-void launch_stream(const SolverDev &d, size_t smem, const VT *r, VT *pv,
-                   const VT *v, VT *z, const KScalars *sc, cudaStream_t st) {
+template <class AR, int MODE, int KLT, int KUT>
+void launch_stream(const SolverDev &d, size_t smem, const uint8_t *rec,
+                   const typename AR::V *r, typename AR::V *pv,
+                   const typename AR::V *v, typename AR::V *z,
+                   const KScalars *sc, cudaStream_t st) {
   static size_t attr = 0;
   if (smem > 48 * 1024 && attr < smem) {
-    cudaFuncSetAttribute(k_ilu0_apply_stream<VT, MT, MODE, KLT, KUT>,
+    cudaFuncSetAttribute(k_ilu0_apply_stream<AR, MODE, KLT, KUT>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
     attr = smem;
   }
-  k_ilu0_apply_stream<VT, MT, MODE, KLT, KUT><<<d.n_sub, 32, smem, st>>>(
-      d.smeta64, d.srec64, r, pv, v, z, sc, d.sub_sys, d.err);
+  k_ilu0_apply_stream<AR, MODE, KLT, KUT><<<d.n_sub, 32, smem, st>>>(
+      d.smeta64, rec, r, pv, v, z, sc, d.sub_sys, d.err);
 }
 
 template <class VT, class MT, int MODE>
@@ -451,11 +512,11 @@ void apply_mode(const SolverDev &d, const VT *r, VT *pv, const VT *v, VT *z,
   // any subdomain whose rows have at most 2 L and 2 U entries) and
   // triangles (3/3); padding slots make smaller rows fit
   if (smem && d.max_kl <= 2 && d.max_ku <= 2)
-    launch_stream<VT, MT, MODE, 2, 2>(d, smem, r, pv, v, z, sc, st);
+    launch_stream<ArithF64, MODE, 2, 2>(d, smem, d.srec64, r, pv, v, z, sc, st);
   else if (smem && d.max_kl <= 3 && d.max_ku <= 3)
-    launch_stream<VT, MT, MODE, 3, 3>(d, smem, r, pv, v, z, sc, st);
+    launch_stream<ArithF64, MODE, 3, 3>(d, smem, d.srec64, r, pv, v, z, sc, st);
   else if (smem)
-    launch_stream<VT, MT, MODE, 0, 0>(d, smem, r, pv, v, z, sc, st);
+    launch_stream<ArithF64, MODE, 0, 0>(d, smem, d.srec64, r, pv, v, z, sc, st);
   else
     k_ilu0_apply_global<VT, MT, MODE><<<d.n_sub, 1024, 0, st>>>(
         d.meta64, d.rec64, r, pv, v, z, sc, d.sub_sys);
@@ -466,6 +527,17 @@ template <int MODE>
 void apply_mode_dd(const SolverDev &d, const float2 *r, float2 *pv,
                    const float2 *v, float2 *z, const KScalars *sc,
                    cudaStream_t st) {
+  if (d.dd_stream) {  // level blobs, float pairs in the FP64 record layout
+    const size_t smem = d.smem64;
+    if (d.max_kl <= 2 && d.max_ku <= 2)
+      launch_stream<ArithDD, MODE, 2, 2>(d, smem, d.srec_dds, r, pv, v, z, sc, st);
+    else if (d.max_kl <= 3 && d.max_ku <= 3)
+      launch_stream<ArithDD, MODE, 3, 3>(d, smem, d.srec_dds, r, pv, v, z, sc, st);
+    else
+      launch_stream<ArithDD, MODE, 0, 0>(d, smem, d.srec_dds, r, pv, v, z, sc, st);
+    count_launches(1);
+    return;
+  }
   static size_t attr = 0;
   if (d.smem_dd > 48 * 1024 && attr < d.smem_dd) {
     cudaFuncSetAttribute(k_ilu0_apply_dd<MODE>,
@@ -491,6 +563,13 @@ void launch_ilu0_factor(const SolverDev &d, const double *pvals, int *bad,
         d.n_pack, d.pack_src, d.pack_dst64,
         reinterpret_cast<const double *>(d.rec64),
         reinterpret_cast<double *>(d.srec64));
+    count_launches(1);
+  }
+  if (to_dd && d.srec_dds && d.n_pack > 0 && d.smem64) {
+    k_pack_dd<<<grid(d.n_pack), 256, 0, st>>>(
+        d.n_pack, d.pack_src, d.pack_dst64,
+        reinterpret_cast<const double *>(d.rec64),
+        reinterpret_cast<float2 *>(d.srec_dds));
     count_launches(1);
   }
   if (to_dd && d.n_pack_dd > 0) {

@@ -165,11 +165,36 @@ struct SolverDev {
   uint8_t *srec_dd;
   const int32_t *pack_src_dd, *pack_dst_dd;
   int n_pack_dd;
+  // float-float copy of the FP64 streaming records (same layout, float
+  // pairs in place of doubles) and whether the mixed solver sweeps it
+  // instead of the step stream
+  uint8_t *srec_dds;
+  int dd_stream;
   int *err;               // set when a bounded device wait runs out
   // batched solves: system of every subdomain (NULL for one system); the
   // apply kernels then read the scalars sc[sub_sys[subdomain]]
   const int32_t *sub_sys;
+  // SELL-32 layout of the permuted matrix for the Krylov SpMV (values are
+  // passed separately: FP64 or float pairs)
+  const int32_t *sell_ptr, *sell_w, *sell_col;
 };
+
+// Row i of A x on the SELL-32 layout: the lanes of a warp read 32
+// consecutive values and columns per entry (one coalesced 256-byte or
+// 128-byte line each); the entries are summed in CSR order and padding adds
+// exact zeros, so the result equals the CSR row sum.
+template <class VT, class MT>
+__device__ __forceinline__ VT row_dot_sell(const SolverDev &d,
+                                           const MT *__restrict__ val,
+                                           const VT *__restrict__ x, int i) {
+  const int q = i >> 5;
+  const int w = d.sell_w[q];
+  const int base = d.sell_ptr[q] + (i & 31);
+  VT s = 0;
+  for (int k = 0; k < w; ++k)
+    s += (VT)val[base + 32 * k] * x[d.sell_col[base + 32 * k]];
+  return s;
+}
 
 void launch_permute_values(int nnz, const int32_t *psrc, const double *src,
                            double *dst, int n_dup, const int32_t *dup_dst,

@@ -31,6 +31,15 @@ __global__ void k_count_diff(int64_t n, const int32_t *__restrict__ a,
     }
 }
 
+// SELL values from the permuted CSR values (padding 0)
+__global__ void k_sell_gather(int64_t n, const int32_t *__restrict__ src,
+                              const double *__restrict__ vals,
+                              double *__restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = src[i] >= 0 ? vals[src[i]] : 0.;
+}
+
 // deterministic non-zero contents for kernel timing
 __global__ void k_fill_profile(int64_t n, double *__restrict__ a,
                                float *__restrict__ b, int salt) {
@@ -58,7 +67,8 @@ struct pg_solver {
   DevBuf<uint8_t> rec64;
   DevBuf<StreamMeta> smeta64;
   DevBuf<StepMeta> tmeta_dd;
-  DevBuf<uint8_t> srec64, srec_dd;
+  DevBuf<uint8_t> srec64, srec_dd, srec_dds;
+  int dd_stream = -1;  // mixed ILU sweep: -1 not chosen, 0 steps, 1 stream
   DevBuf<int32_t> pack_src, pack_dst64, pack_src_dd, pack_dst_dd;
   DevBuf<int> err;
   DevBuf<int32_t> raw_rp, raw_ci, st_rp, st_ci;
@@ -68,8 +78,13 @@ struct pg_solver {
   DevBuf<double> pvals, jdinv;
   // Krylov vectors (permuted order)
   DevBuf<double> b, x, r, rh, p, v, ph, s, sh, t, xout;
-  // float-float matrix, Jacobi diagonal and Krylov vectors of PG_MIXED
-  DevBuf<float2> pvals_dd, jdinv_dd;
+  // SELL-32 layout of the permuted matrix and its values (FP64 and float
+  // pairs) for the Krylov SpMV
+  DevBuf<int32_t> sell_ptr, sell_w, sell_col, sell_src;
+  DevBuf<double> sell_vals;
+  DevBuf<float2> sell_vals_dd;
+  // float-float Jacobi diagonal and Krylov vectors of PG_MIXED
+  DevBuf<float2> jdinv_dd;
   DevBuf<float2> xd, rd, rhd, pd, vd, phd, sd, shd, td;
   // reductions and scalars
   DevBuf<double> partials;
@@ -130,16 +145,34 @@ struct pg_solver {
     d.pack_src_dd = pack_src_dd.p;
     d.pack_dst_dd = pack_dst_dd.p;
     d.n_pack_dd = (int)a.pack_src_dd.size();
+    d.srec_dds = srec_dds.p;
+    d.dd_stream = dd_stream == 1 ? 1 : 0;
     d.max_kl = a.max_kl;
     d.max_ku = a.max_ku;
     d.err = err.p;
     d.sub_sys = nullptr;
+    d.sell_ptr = sell_ptr.p;
+    d.sell_w = sell_w.p;
+    d.sell_col = sell_col.p;
     return d;
   }
   RedWork red() const { return RedWork{partials.p, ticket.p, red_grid}; }
 };
 
 namespace {
+
+// CTAs of the reducing vector kernels (grid-stride loops): every thread
+// ends with a warp/block reduction whose FP64 shuffles and adds are not
+// free on GB300's FP64 pipe, so fewer threads with more rows each win until
+// memory parallelism runs short.  PG_RED_GRID overrides the cap.
+int red_grid_cap() {
+  static const int cap = [] {
+    const char *e = std::getenv("PG_RED_GRID");
+    const int v = e ? std::atoi(e) : 0;
+    return v > 0 ? v : 1216;
+  }();
+  return cap;
+}
 
 int upload_analysis(pg_solver *s) {
   const Analysis &a = s->a;
@@ -162,8 +195,17 @@ int upload_analysis(pg_solver *s) {
   up(s->pack_dst64, a.pack_dst64);
   up(s->tmeta_dd, a.tmeta_dd);
   up(s->srec_dd, a.srec_dd);
+  s->dd_stream = -1;
+  if (s->cfg.precision == PG_MIXED) up(s->srec_dds, a.srec64);  // static parts
   up(s->pack_src_dd, a.pack_src_dd);
   up(s->pack_dst_dd, a.pack_dst_dd);
+  up(s->sell_ptr, a.sell_ptr);
+  up(s->sell_w, a.sell_w);
+  up(s->sell_col, a.sell_col);
+  up(s->sell_src, a.sell_src);
+  if (e == cudaSuccess) e = s->sell_vals.reserve(a.sell_col.size());
+  if (e == cudaSuccess && s->cfg.precision == PG_MIXED)
+    e = s->sell_vals_dd.reserve(a.sell_col.size());
   if (e == cudaSuccess) e = s->err.zero(1);
   const size_t n = a.n, nnz = a.nnz;
   for (DevBuf<double> *bf : {&s->b, &s->x, &s->r, &s->rh, &s->p, &s->v,
@@ -175,10 +217,9 @@ int upload_analysis(pg_solver *s) {
     for (DevBuf<float2> *bf : {&s->xd, &s->rd, &s->rhd, &s->pd, &s->vd,
                                &s->phd, &s->sd, &s->shd, &s->td, &s->jdinv_dd})
       if (e == cudaSuccess) e = bf->reserve(n);
-    if (e == cudaSuccess) e = s->pvals_dd.reserve(nnz);
   }
   s->drop_graphs();
-  s->red_grid = (int)std::min<int64_t>(1216, (n + kVecBlock - 1) / kVecBlock);
+  s->red_grid = (int)std::min<int64_t>(red_grid_cap(), (n + kVecBlock - 1) / kVecBlock);
   if (s->red_grid < 1) s->red_grid = 1;
   if (e == cudaSuccess) e = s->partials.reserve((size_t)kMaxDots * s->red_grid);
   if (e == cudaSuccess) e = s->ticket.zero(1);
@@ -269,9 +310,9 @@ int run_bicgstab(pg_solver *s, double tol, int max_iters, int *iters,
   auto chunk = [&]() {
     for (int c = 0; c < kChunk; ++c) {
       precond(1, p, ph);
-      launch_spmv_v<double, double>(d, val, ph, v, rh, s->sc.p, w, st);
+      launch_spmv_v<double, double>(d, s->sell_vals.p, ph, v, rh, s->sc.p, w, st);
       precond(2, ss, sh);
-      launch_spmv_t<double, double>(d, val, sh, t, ss, s->sc.p, w, st);
+      launch_spmv_t<double, double>(d, s->sell_vals.p, sh, t, ss, s->sc.p, w, st);
       launch_update<double>(d.n, x, r, ph, sh, ss, t, rh, s->sc.p, w, st);
     }
   };
@@ -363,7 +404,6 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
   const int n = d.n;
   const bool ilu = s->cfg.precond == PG_PREC_ILU0;
   const float2 *jd = s->cfg.precond == PG_PREC_JACOBI ? s->jdinv_dd.p : nullptr;
-  float2 *const val = s->pvals_dd.p;
   float2 *const x = s->xd.p, *const r = s->rd.p, *const rh = s->rhd.p;
   float2 *const p = s->pd.p, *const v = s->vd.p, *const ph = s->phd.p;
   float2 *const ss = s->sd.p, *const sh = s->shd.p, *const t = s->td.p;
@@ -376,9 +416,9 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
   auto chunk = [&]() {
     for (int c = 0; c < kChunk; ++c) {
       precond(1, p, ph);
-      launch_dd_spmv_v(d, val, ph, v, rh, s->sc.p, w, st);
+      launch_dd_spmv_v(d, s->sell_vals_dd.p, ph, v, rh, s->sc.p, w, st);
       precond(2, ss, sh);
-      launch_dd_spmv_t(d, val, sh, t, ss, s->sc.p, w, st);
+      launch_dd_spmv_t(d, s->sell_vals_dd.p, sh, t, ss, s->sc.p, w, st);
       launch_dd_update(n, x, r, ph, sh, ss, t, rh, s->sc.p, w, st);
     }
   };
@@ -455,8 +495,63 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
 }
 
 bool use_dd(const pg_solver *s) {
+  const SolverDev d = s->dev();
   return s->cfg.precision == PG_MIXED &&
-         (s->cfg.precond != PG_PREC_ILU0 || s->dev().smem_dd > 0);
+         (s->cfg.precond != PG_PREC_ILU0 || d.smem_dd > 0 ||
+          (d.smem64 > 0 && d.srec_dds));
+}
+
+// The mixed solver's ILU(0) sweep has two record forms: warp-wide steps
+// (few instructions per level, but every step padded to 32 rows) and the
+// level blobs of the FP64 stream (compact).  Which is faster depends on the
+// level widths of the mesh, so the first factorisation after an analysis
+// times three applications of each and keeps the faster.
+int choose_dd_sweep(pg_solver *s) {
+  const SolverDev d0 = s->dev();
+  const bool has_steps = d0.smem_dd > 0, has_blobs = d0.smem64 > 0 && d0.srec_dds;
+  if (has_steps && s->cfg.mixed_sweep == 1) {
+    s->dd_stream = 0;
+    return PG_OK;
+  }
+  if (has_blobs && s->cfg.mixed_sweep == 2) {
+    s->dd_stream = 1;
+    return PG_OK;
+  }
+  if (!has_steps || !has_blobs) {
+    s->dd_stream = has_blobs ? 1 : 0;
+    return PG_OK;
+  }
+  cudaStream_t st = stream();
+  const int64_t n = s->a.n;
+  PG_CUDA(cudaMemsetAsync(s->pd.p, 0, n * sizeof(float2), st));
+  float best = 1e30f;
+  int pick = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;  // the solve's own events stay put
+  PG_CUDA(cudaEventCreate(&e0));
+  cudaError_t ce = cudaEventCreate(&e1);
+  for (int form = 0; form < 2 && ce == cudaSuccess; ++form) {
+    s->dd_stream = form;
+    const SolverDev d = s->dev();
+    launch_ilu0_apply_dd(0, d, nullptr, s->pd.p, nullptr, s->phd.p, nullptr, st);
+    ce = cudaEventRecord(e0, st);
+    for (int k = 0; k < 3; ++k)
+      launch_ilu0_apply_dd(0, d, nullptr, s->pd.p, nullptr, s->phd.p, nullptr, st);
+    if (ce == cudaSuccess) ce = cudaEventRecord(e1, st);
+    if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+    if (ce == cudaSuccess) ce = cudaGetLastError();
+    float ms = 0.f;
+    if (ce == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      pick = form;
+    }
+  }
+  cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  PG_CUDA(ce);
+  s->dd_stream = pick;
+  s->drop_graphs();  // the chunk graph holds the apply kernel
+  return PG_OK;
 }
 
 int factor(pg_solver *s) {
@@ -470,8 +565,14 @@ int factor(pg_solver *s) {
     launch_jacobi_diag(d, s->pvals.p, s->jdinv.p, st);
     if (dd) launch_dd_split(d.n, s->jdinv.p, 1.0, s->jdinv_dd.p, st);
   }
-  if (dd) launch_dd_split(d.nnz, s->pvals.p, 1.0, s->pvals_dd.p, st);
+  const int64_t n_sell = (int64_t)s->a.sell_col.size();
+  k_sell_gather<<<grid_for(n_sell), 256, 0, st>>>(n_sell, s->sell_src.p,
+                                                  s->pvals.p, s->sell_vals.p);
+  count_launches(1);
+  if (dd) launch_dd_split(n_sell, s->sell_vals.p, 1.0, s->sell_vals_dd.p, st);
   PG_CUDA(cudaGetLastError());
+  if (dd && s->cfg.precond == PG_PREC_ILU0 && s->dd_stream < 0)
+    return choose_dd_sweep(s);
   return PG_OK;
 }
 
@@ -485,7 +586,7 @@ extern "C" void pg_solver_default_cfg(pg_solver_cfg *cfg) {
   cfg->precond = PG_PREC_ILU0;
   cfg->subdomain_rows = 0;
   cfg->precision = PG_FP64;
-  cfg->reserved_i = 0;
+  cfg->mixed_sweep = 0;
   cfg->reserved_d = 0.;
 }
 
@@ -500,6 +601,8 @@ extern "C" int pg_solver_create(const pg_solver_cfg *cfg, pg_solver **out) {
                "pg_solver_create: bad preconditioner");
   PG_CHECK_ARG(c.precision == PG_FP64 || c.precision == PG_MIXED,
                "pg_solver_create: bad precision");
+  PG_CHECK_ARG(c.mixed_sweep >= 0 && c.mixed_sweep <= 2,
+               "pg_solver_create: bad mixed_sweep");
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0 || !stream()) {
     set_error("no CUDA device available: libphase_gb300 has no CPU path");
@@ -784,16 +887,15 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
   };
   for (int i = 0; i < 8; ++i) ms[i] = 0.;
   // vectors: 0 ph/sh, 1 v/t, 2 rh, 3 r, 4 p/s, 5 x, 6 z
-  int rc = timed([&] { launch_spmv_v<double, double>(d, s->pvals.p, d8[0].p, d8[1].p, d8[2].p, s->sc.p, w, st); }, &ms[0]);
+  int rc = timed([&] { launch_spmv_v<double, double>(d, s->sell_vals.p, d8[0].p, d8[1].p, d8[2].p, s->sc.p, w, st); }, &ms[0]);
   if (!rc) rc = timed([&] { launch_precond<double, double>(s->cfg.precond, 1, d, s->jdinv.p, d8[3].p, d8[4].p, d8[1].p, d8[6].p, s->sc.p, st); }, &ms[1]);
   if (!rc) rc = timed([&] { launch_update<double>(d.n, d8[5].p, d8[3].p, d8[0].p, d8[6].p, d8[4].p, d8[1].p, d8[2].p, s->sc.p, w, st); }, &ms[2]);
   if (!rc && s->cfg.precond == PG_PREC_ILU0)
     rc = timed([&] { launch_ilu0_factor(d, s->pvals.p, s->bad.p, dd, st); }, &ms[3]);
   if (!rc && dd) {
-    launch_dd_split(d.nnz, s->pvals.p, 1.0, s->pvals_dd.p, st);
     if (s->cfg.precond == PG_PREC_ILU0)
       rc = timed([&] { launch_ilu0_apply_dd(1, d, f8[3].p, f8[4].p, f8[1].p, f8[6].p, s->sc.p, st); }, &ms[4]);
-    if (!rc) rc = timed([&] { launch_dd_spmv_v(d, s->pvals_dd.p, f8[0].p, f8[1].p, f8[2].p, s->sc.p, w, st); }, &ms[5]);
+    if (!rc) rc = timed([&] { launch_dd_spmv_v(d, s->sell_vals_dd.p, f8[0].p, f8[1].p, f8[2].p, s->sc.p, w, st); }, &ms[5]);
     if (!rc) rc = timed([&] { launch_dd_update(d.n, f8[5].p, f8[3].p, f8[0].p, f8[6].p, f8[4].p, f8[1].p, f8[2].p, s->sc.p, w, st); }, &ms[6]);
   }
   PG_CUDA(cudaStreamSynchronize(st));

@@ -145,8 +145,11 @@ class BubbleSequence:
         self.row_ptr, self.col_ind = rp, ci
         self.seed = seed
 
-    def centre(self, t):
-        return (0.5, 0.5 + 0.5 * t * workloads.RB_HEIGHT / self.nx)
+    def centre(self, t, span=2000):
+        """Bubble centre at step t: rises from y = 0.5 to 1.5 over ``span``
+        steps (0.26 cells per step at 1024 x 1024), staying inside the
+        column for the whole sequence."""
+        return (0.5, 0.5 + min(t, span) / span)
 
     def _fields(self, t):
         """gamma (cells) and u* (faces) of step t, generated on the device:
@@ -206,7 +209,7 @@ class BubbleSequence:
         return v, b
 
 
-def train(nx=1024, steps=2000, epochs=3, lr=2e-3, out=DEFAULT_WEIGHTS,
+def train(nx=1024, steps=2000, epochs=8, lr=2e-3, out=DEFAULT_WEIGHTS,
           eval_steps=20, log=print):
     import torch
     pg = _pg()
@@ -231,20 +234,27 @@ def train(nx=1024, steps=2000, epochs=3, lr=2e-3, out=DEFAULT_WEIGHTS,
         iters.append(solver.nIters())
     log(f"dumped {steps} solves in {time.time() - t0:.1f} s "
         f"(mean {np.mean(iters):.0f} iterations)")
-    # 2. train on steps 1..n_train (x_prev = x_{t-1})
+    # 2. train on steps 1..n_train (x_prev = x_{t-1}); cosine learning-rate
+    #    decay to lr/20; the parameters of the epoch with the best validation
+    #    residual are kept
     net = Mpnn(seed=1)
     net.set_graph(seq.row_ptr, seq.col_ind)
     rng = np.random.default_rng(0)
     hist = []
+    best = (float("inf"), None, -1)
     t0 = time.time()
+    n_steps = epochs * (n_train - 1)
+    k = 0
     for ep in range(epochs):
         order = rng.permutation(np.arange(2, n_train + 1))
         losses = []
         for t in order:
             v, b = seq.device_system(int(t))
-            losses.append(net.train_step_device(v, b.data_ptr(),
-                                                xs[t - 1].data_ptr(),
-                                                xs[t].data_ptr(), lr))
+            lr_k = lr * (0.05 + 0.95 * 0.5 * (1.0 + np.cos(np.pi * k / n_steps)))
+            k += 1
+            loss = net.train_step_device(v, b.data_ptr(), xs[t - 1].data_ptr(),
+                                         xs[t].data_ptr(), lr_k)
+            losses.append(loss)
         val = []
         for t in range(n_train + 1, n_train + n_val + 1):
             v, b = seq.device_system(t)
@@ -255,13 +265,18 @@ def train(nx=1024, steps=2000, epochs=3, lr=2e-3, out=DEFAULT_WEIGHTS,
                          val_rel_residual=float(np.mean(val))))
         log(f"epoch {ep}: train loss {np.mean(losses):.4f}, validation "
             f"||b - A g||/||b|| {np.mean(val):.4f} ({time.time() - t0:.1f} s)")
+        if np.mean(val) < best[0]:
+            best = (float(np.mean(val)), net.get_params(), ep)
+    net.set_params(best[1])
+    log(f"kept epoch {best[2]} (validation {best[0]:.4f})")
     params = net.get_params()
     os.makedirs(os.path.dirname(out), exist_ok=True)
     np.save(out, params)
     # 3. held-out comparison: zero guess, previous solution, learned guess
     test = list(range(n_train + n_val + 1, steps + 1))[:eval_steps]
-    report = evaluate(seq, net, xs, test, log)
-    report.update(train_history=hist, n_params=int(net.n_params), nx=nx,
+    report = evaluate(seq, net, xs, test, log, precisions=("fp64", "mixed"))
+    report.update(train_history=hist, best_epoch=best[2],
+                  n_params=int(net.n_params), nx=nx,
                   steps=steps, split=[n_train, n_val, steps - n_train - n_val])
     return report
 
@@ -305,7 +320,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--nx", type=int, default=1024)
     ap.add_argument("--steps", type=int, default=2000)
-    ap.add_argument("--epochs", type=int, default=3)
+    ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--eval-steps", type=int, default=20)
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)

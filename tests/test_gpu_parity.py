@@ -159,7 +159,7 @@ def _bubble_system(pg, nx, ny):
     return eqn.export()
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed-steps", "mixed-blobs"])
 @pytest.mark.parametrize("mesh", ["bubble", "tri"])
 def test_ilu_apply_matches_oracle(pg, oracle, precision, mesh):
     """The Schwarz ILU(0) sweeps alone, z = M^-1 r, against the oracle's
@@ -176,8 +176,10 @@ def test_ilu_apply_matches_oracle(pg, oracle, precision, mesh):
         rp, ci, v, rhs = _system(om)
         sub = 512
     n = len(rp) - 1
-    s = pg.SparseMatrixSolver(subdomain_rows=sub, precision=pg.MIXED
-                              if precision == "mixed" else pg.FP64)
+    s = pg.SparseMatrixSolver(
+        subdomain_rows=sub,
+        precision=pg.FP64 if precision == "fp64" else pg.MIXED,
+        mixed_sweep={"fp64": 0, "mixed-steps": 1, "mixed-blobs": 2}[precision])
     s.setRank(n)
     s.set(rp, ci, v)
     part, nparts = s.partition()
