@@ -226,6 +226,11 @@ int pg_mpnn_gradient(pg_mpnn *net, const double *vals, const double *b,
 /* FP32 master parameters (pg_mpnn_num_params floats), host memory */
 int pg_mpnn_get_params(const pg_mpnn *net, float *params);
 int pg_mpnn_set_params(pg_mpnn *net, const float *params);
+/* Weights file: 8-byte tag "PGMPNN01", int32 parameter count, the FP32
+ * master parameters (little-endian).  load checks the tag and the count
+ * against this network's layout and resets the Adam state. */
+int pg_mpnn_save(const pg_mpnn *net, const char *path);
+int pg_mpnn_load(pg_mpnn *net, const char *path);
 
 /* Allocation-free form of pg_gradient's cell gradient, for callers that
  * cannot allocate device memory (a fixed memory budget owned by an outer

@@ -114,6 +114,8 @@ PROTOTYPES = {
     "pg_mpnn_gradient": (_I, [_P, _P, _P, _P, _P, _I, _P, _P]),
     "pg_mpnn_get_params": (_I, [_P, _P]),
     "pg_mpnn_set_params": (_I, [_P, _P]),
+    "pg_mpnn_save": (_I, [_P, ctypes.c_char_p]),
+    "pg_mpnn_load": (_I, [_P, ctypes.c_char_p]),
     "pg_kernel_launches": (ctypes.c_uint64, []),
 }
 

@@ -20,6 +20,9 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <cstdio>
+#include <cstring>
+
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -766,4 +769,35 @@ extern "C" int pg_mpnn_set_params(pg_mpnn *net, const float *params) {
   net->step = 0;
   PG_CUDA(cudaStreamSynchronize(stream()));
   return PG_OK;
+}
+
+extern "C" int pg_mpnn_save(const pg_mpnn *net, const char *path) {
+  PG_CHECK_ARG(net && path, "pg_mpnn_save: NULL arg");
+  std::vector<float> p(net->lay.total);
+  int rc = pg_mpnn_get_params(net, p.data());
+  if (rc) return rc;
+  FILE *f = std::fopen(path, "wb");
+  PG_CHECK_ARG(f, "pg_mpnn_save: cannot open the file for writing");
+  const int32_t n = (int32_t)p.size();
+  bool ok = std::fwrite("PGMPNN01", 1, 8, f) == 8 &&
+            std::fwrite(&n, sizeof(n), 1, f) == 1 &&
+            std::fwrite(p.data(), sizeof(float), p.size(), f) == p.size();
+  ok = (std::fclose(f) == 0) && ok;
+  PG_CHECK_ARG(ok, "pg_mpnn_save: write failed");
+  return PG_OK;
+}
+
+extern "C" int pg_mpnn_load(pg_mpnn *net, const char *path) {
+  PG_CHECK_ARG(net && path, "pg_mpnn_load: NULL arg");
+  FILE *f = std::fopen(path, "rb");
+  PG_CHECK_ARG(f, "pg_mpnn_load: cannot open the file");
+  char tag[8] = {0};
+  int32_t n = 0;
+  bool ok = std::fread(tag, 1, 8, f) == 8 && std::memcmp(tag, "PGMPNN01", 8) == 0 &&
+            std::fread(&n, sizeof(n), 1, f) == 1 && n == net->lay.total;
+  std::vector<float> p(ok ? n : 0);
+  if (ok) ok = std::fread(p.data(), sizeof(float), p.size(), f) == p.size();
+  std::fclose(f);
+  PG_CHECK_ARG(ok, "pg_mpnn_load: not a weights file of this network layout");
+  return pg_mpnn_set_params(net, p.data());
 }

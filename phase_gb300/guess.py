@@ -115,6 +115,14 @@ class Mpnn:
         pg._check(pg.lib().pg_mpnn_get_params(self._h, pg._ptr(p)))
         return p
 
+    def save(self, path):
+        pg = _pg()
+        pg._check(pg.lib().pg_mpnn_save(self._h, str(path).encode()))
+
+    def load(self, path):
+        pg = _pg()
+        pg._check(pg.lib().pg_mpnn_load(self._h, str(path).encode()))
+
     def set_params(self, p):
         pg = _pg()
         p = np.ascontiguousarray(p, np.float32)

@@ -89,3 +89,16 @@ def test_training_beats_previous_solution(pg):
         xprev = xs[t - 1].cpu().numpy()
         previous.append(np.linalg.norm(bb - A @ xprev) / np.linalg.norm(bb))
     assert np.mean(learned) < np.mean(previous)
+
+
+def test_weights_file_round_trip(pg, tmp_path):
+    from phase_gb300 import guess
+    a, b = guess.Mpnn(seed=3), guess.Mpnn(seed=4)
+    f = tmp_path / "w.bin"
+    a.save(f)
+    b.load(f)
+    assert np.array_equal(a.get_params(), b.get_params())
+    bad = tmp_path / "bad.bin"
+    bad.write_bytes(b"not a weights file")
+    with pytest.raises(pg.PhaseError):
+        b.load(bad)
