@@ -294,12 +294,13 @@ void launch_b_init(const BatchTiles &T, const BatchRed &R, int block,
                    const double *b, const double *x, double *r, double *rh,
                    double *p, double *v, KScalars *sc, const int *init,
                    cudaStream_t st);
+// the SpMV kernels read the SELL-32 layout (row_dot_sell)
 void launch_b_spmv_v(const BatchTiles &T, const BatchRed &R, int block,
-                     const int32_t *rp, const int32_t *ci, const double *val,
+                     const SolverDev &d, const double *sell_val,
                      const double *ph, double *v, const double *rh,
                      KScalars *sc, cudaStream_t st);
 void launch_b_spmv_t(const BatchTiles &T, const BatchRed &R, int block,
-                     const int32_t *rp, const int32_t *ci, const double *val,
+                     const SolverDev &d, const double *sell_val,
                      const double *sh, double *t, const double *s,
                      KScalars *sc, cudaStream_t st);
 void launch_b_update(const BatchTiles &T, const BatchRed &R, int block,

@@ -494,6 +494,15 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
   }
 }
 
+// SELL values of the current permuted values; returns the slot count
+int64_t sell_gather(pg_solver *s) {
+  const int64_t n_sell = (int64_t)s->a.sell_col.size();
+  k_sell_gather<<<grid_for(n_sell), 256, 0, stream()>>>(
+      n_sell, s->sell_src.p, s->pvals.p, s->sell_vals.p);
+  count_launches(1);
+  return n_sell;
+}
+
 bool use_dd(const pg_solver *s) {
   const SolverDev d = s->dev();
   return s->cfg.precision == PG_MIXED &&
@@ -565,10 +574,7 @@ int factor(pg_solver *s) {
     launch_jacobi_diag(d, s->pvals.p, s->jdinv.p, st);
     if (dd) launch_dd_split(d.n, s->jdinv.p, 1.0, s->jdinv_dd.p, st);
   }
-  const int64_t n_sell = (int64_t)s->a.sell_col.size();
-  k_sell_gather<<<grid_for(n_sell), 256, 0, st>>>(n_sell, s->sell_src.p,
-                                                  s->pvals.p, s->sell_vals.p);
-  count_launches(1);
+  const int64_t n_sell = sell_gather(s);
   if (dd) launch_dd_split(n_sell, s->sell_vals.p, 1.0, s->sell_vals_dd.p, st);
   PG_CUDA(cudaGetLastError());
   if (dd && s->cfg.precond == PG_PREC_ILU0 && s->dd_stream < 0)
@@ -1070,8 +1076,8 @@ int autotune(pg_batch *b) {
     int rc = build_tiles(b, c[0], c[1]);
     if (rc) return rc;
     auto run = [&] {
-      launch_b_spmv_v(b->tiles(), b->red(), b->block, s->prp.p, s->pci.p,
-                      s->pvals.p, s->ph.p, s->v.p, s->rh.p, b->sc.p, st);
+      launch_b_spmv_v(b->tiles(), b->red(), b->block, b->dev(),
+                      s->sell_vals.p, s->ph.p, s->v.p, s->rh.p, b->sc.p, st);
     };
     run();
     PG_CUDA(cudaEventRecord(s->ev[0], st));
@@ -1158,12 +1164,12 @@ int build_batch_graph(pg_batch *b) {
     for (int c = 0; c < kChunk; ++c) {
       launch_precond<double, double>(PG_PREC_ILU0, 1, d, nullptr, s->r.p,
                                      s->p.p, s->v.p, s->ph.p, b->sc.p, st);
-      launch_b_spmv_v(T, R, b->block, s->prp.p, s->pci.p, s->pvals.p, s->ph.p,
-                      s->v.p, s->rh.p, b->sc.p, st);
+      launch_b_spmv_v(T, R, b->block, d, s->sell_vals.p, s->ph.p, s->v.p,
+                      s->rh.p, b->sc.p, st);
       launch_precond<double, double>(PG_PREC_ILU0, 2, d, nullptr, s->r.p,
                                      s->s.p, s->v.p, s->sh.p, b->sc.p, st);
-      launch_b_spmv_t(T, R, b->block, s->prp.p, s->pci.p, s->pvals.p, s->sh.p,
-                      s->t.p, s->s.p, b->sc.p, st);
+      launch_b_spmv_t(T, R, b->block, d, s->sell_vals.p, s->sh.p, s->t.p,
+                      s->s.p, b->sc.p, st);
       launch_b_update(T, R, b->block, s->x.p, s->r.p, s->ph.p, s->sh.p,
                       s->s.p, s->t.p, s->rh.p, b->sc.p, st);
     }
@@ -1256,6 +1262,7 @@ extern "C" int pg_batch_set_eqns(pg_batch *b, int n_systems,
     launch_permute_values((int)s->a.nnz, s->psrc.p, b->st_vals.p, s->pvals.p,
                           (int)s->a.dup_dst.size(), s->dup_dst.p,
                           s->dup_src.p, st);
+    sell_gather(s);
     rc = autotune(b);
     if (rc) return rc;
   }
@@ -1297,6 +1304,7 @@ extern "C" int pg_batch_solve(pg_batch *b, pg_solve_stats *stats,
   PG_CUDA(cudaEventRecord(s->ev[0], st));
   PG_CUDA(cudaMemsetAsync(s->bad.p, 0, sizeof(int), st));
   launch_ilu0_factor(d, s->pvals.p, s->bad.p, false, st);
+  sell_gather(s);
   for (int i = 0; i < S; ++i) {
     KScalars k{};
     k.tol2 = s->cfg.tolerance * s->cfg.tolerance;
