@@ -150,7 +150,7 @@ __global__ void k_b_spmv_v(BatchTiles T, BatchRed R, SolverDev d,
   if (sc[sys].done) return;
   double acc[1] = {0.};
   for (int i = T.tile_r0[tile] + threadIdx.x; i < T.tile_r1[tile]; i += blockDim.x) {
-    const double vi = row_dot_sell<double, double>(d, val, ph, i);
+    const double vi = row_dot_b(d.prp, d.pci, val, ph, i);
     v[i] = vi;
     acc[0] += rh[i] * vi;
   }
@@ -178,7 +178,7 @@ __global__ void k_b_spmv_t(BatchTiles T, BatchRed R, SolverDev d,
   if (sc[sys].done) return;
   double acc[2] = {0., 0.};
   for (int i = T.tile_r0[tile] + threadIdx.x; i < T.tile_r1[tile]; i += blockDim.x) {
-    const double ti = row_dot_sell<double, double>(d, val, sh, i);
+    const double ti = row_dot_b(d.prp, d.pci, val, sh, i);
     t[i] = ti;
     acc[0] += ti * ti;
     acc[1] += ti * s_[i];
@@ -373,17 +373,17 @@ void launch_b_init(const BatchTiles &T, const BatchRed &R, int block,
   count_launches(1);
 }
 void launch_b_spmv_v(const BatchTiles &T, const BatchRed &R, int block,
-                     const SolverDev &d, const double *sell_val,
+                     const SolverDev &d, const double *val,
                      const double *ph, double *v, const double *rh,
                      KScalars *sc, cudaStream_t st) {
-  k_b_spmv_v<<<T.n_tiles, block, 0, st>>>(T, R, d, sell_val, ph, v, rh, sc);
+  k_b_spmv_v<<<T.n_tiles, block, 0, st>>>(T, R, d, val, ph, v, rh, sc);
   count_launches(1);
 }
 void launch_b_spmv_t(const BatchTiles &T, const BatchRed &R, int block,
-                     const SolverDev &d, const double *sell_val,
+                     const SolverDev &d, const double *val,
                      const double *sh, double *t, const double *s,
                      KScalars *sc, cudaStream_t st) {
-  k_b_spmv_t<<<T.n_tiles, block, 0, st>>>(T, R, d, sell_val, sh, t, s, sc);
+  k_b_spmv_t<<<T.n_tiles, block, 0, st>>>(T, R, d, val, sh, t, s, sc);
   count_launches(1);
 }
 void launch_b_update(const BatchTiles &T, const BatchRed &R, int block,

@@ -86,17 +86,14 @@ __device__ bool grid_reduce_dd(DdAcc (&v)[ND], const RedWork &w,
 
 __device__ __forceinline__ bool finite_d(double v) { return isfinite(v); }
 
-// row i of A x on the SELL-32 layout (row_dot_sell in kernels.cuh)
-__device__ __forceinline__ float2 row_dot_dd_sell(const SolverDev &d,
-                                                  const float2 *__restrict__ val,
-                                                  const float2 *__restrict__ x,
-                                                  int i) {
+__device__ __forceinline__ float2 row_dot_dd(const int32_t *__restrict__ rp,
+                                             const int32_t *__restrict__ ci,
+                                             const float2 *__restrict__ val,
+                                             const float2 *__restrict__ x,
+                                             int i) {
   DdAcc a{0.f, 0.f};
-  const int q = i >> 5;
-  const int w = d.sell_w[q];
-  const int base = d.sell_ptr[q] + (i & 31);
-  for (int k = 0; k < w; ++k)
-    dd_acc_fma(a, val[base + 32 * k], x[d.sell_col[base + 32 * k]]);
+  const int b = rp[i], e = rp[i + 1];
+  for (int j = b; j < e; ++j) dd_acc_fma(a, val[j], x[ci[j]]);
   return dd_value(a);
 }
 
@@ -182,7 +179,7 @@ k_dd_spmv_v(SolverDev d, const float2 *__restrict__ val,
   DdAcc acc[1] = {{0.f, 0.f}};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
        i += gridDim.x * blockDim.x) {
-    const float2 vi = row_dot_dd_sell(d, val, ph, i);
+    const float2 vi = row_dot_dd(d.prp, d.pci, val, ph, i);
     v[i] = vi;
     dd_acc_fma(acc[0], rh[i], vi);
   }
@@ -210,7 +207,7 @@ k_dd_spmv_t(SolverDev d, const float2 *__restrict__ val,
   DdAcc acc[2] = {{0.f, 0.f}, {0.f, 0.f}};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
        i += gridDim.x * blockDim.x) {
-    const float2 ti = row_dot_dd_sell(d, val, sh, i);
+    const float2 ti = row_dot_dd(d.prp, d.pci, val, sh, i);
     t[i] = ti;
     dd_acc_fma(acc[0], ti, ti);
     dd_acc_fma(acc[1], ti, s[i]);

@@ -542,37 +542,6 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
     a.max_sub_lu = std::max(a.max_sub_lu, (int)((int64_t)a.lci.size() - e0));
   }
 
-  // 6b. SELL-32 layout of the permuted matrix (SpMV)
-  {
-    const int64_t n_sl = (n + 31) / 32;
-    a.sell_ptr.assign(n_sl + 1, 0);
-    a.sell_w.assign(n_sl, 0);
-    for (int64_t q = 0; q < n_sl; ++q) {
-      int w = 0;
-      for (int64_t i = 32 * q; i < std::min<int64_t>(n, 32 * q + 32); ++i)
-        w = std::max(w, a.prp[i + 1] - a.prp[i]);
-      a.sell_w[q] = w;
-      a.sell_ptr[q + 1] = a.sell_ptr[q] + 32 * w;
-    }
-    PG_CHECK_ARG((int64_t)a.sell_ptr[n_sl] < ((int64_t)1 << 31),
-                 "SELL layout too large");
-    a.sell_col.assign(a.sell_ptr[n_sl], 0);
-    a.sell_src.assign(a.sell_ptr[n_sl], -1);
-    for (int64_t q = 0; q < n_sl; ++q)
-      for (int l = 0; l < 32; ++l) {
-        const int64_t i = 32 * q + l;
-        for (int k = 0; k < a.sell_w[q]; ++k) {
-          const int64_t slot = a.sell_ptr[q] + 32 * k + l;
-          if (i < n && a.prp[i] + k < a.prp[i + 1]) {
-            a.sell_col[slot] = a.pci[a.prp[i] + k];
-            a.sell_src[slot] = a.prp[i] + k;
-          } else {
-            a.sell_col[slot] = (int32_t)std::min<int64_t>(i, n - 1);
-          }
-        }
-      }
-  }
-
   // 7. packed per-subdomain records (layout in kernels.cuh): level bounds,
   //    then slot-major L/U column slots (subdomain-local, uint16) and value
   //    slots, so consecutive rows of a level sit in consecutive addresses;

@@ -186,11 +186,6 @@ struct Analysis {
   int max_sub_rows = 0, max_sub_lu = 0, max_levels = 0;
   std::vector<int32_t> perm, iperm;        // new->old, old->new
   std::vector<int32_t> prp, pci, psrc;     // permuted CSR; psrc -> caller idx
-  // SELL-32 copy of the permuted matrix for the SpMV: slices of 32 rows,
-  // column-major within a slice (entry k of row 32 q + l at
-  // sell_ptr[q] + 32 k + l), padded to the slice's longest row with the
-  // row's own column and value 0; sell_src -> permuted CSR entry (-1 pad)
-  std::vector<int32_t> sell_ptr, sell_w, sell_col, sell_src;
   std::vector<int32_t> dup_dst, dup_src;   // extra summed duplicates
   std::vector<int32_t> sub_ptr;            // [n_sub+1] permuted row starts
   std::vector<int32_t> sub_lvl;            // [n_sub+1] index into lvl_ptr

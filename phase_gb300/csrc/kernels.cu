@@ -458,7 +458,7 @@ k_spmv_v(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ ph,
   double acc[1] = {0.};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
        i += gridDim.x * blockDim.x) {
-    const VT vi = row_dot_sell<VT, MT>(d, val, ph, i);
+    const VT vi = row_dot<VT, MT>(d.prp, d.pci, val, ph, i);
     v[i] = vi;
     acc[0] += (double)rh[i] * (double)vi;
   }
@@ -486,7 +486,7 @@ k_spmv_t(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ sh,
   double acc[2] = {0., 0.};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
        i += gridDim.x * blockDim.x) {
-    const VT ti = row_dot_sell<VT, MT>(d, val, sh, i);
+    const VT ti = row_dot<VT, MT>(d.prp, d.pci, val, sh, i);
     t[i] = ti;
     acc[0] += (double)ti * (double)ti;
     acc[1] += (double)ti * (double)s[i];

@@ -174,27 +174,9 @@ struct SolverDev {
   // batched solves: system of every subdomain (NULL for one system); the
   // apply kernels then read the scalars sc[sub_sys[subdomain]]
   const int32_t *sub_sys;
-  // SELL-32 layout of the permuted matrix for the Krylov SpMV (values are
-  // passed separately: FP64 or float pairs)
-  const int32_t *sell_ptr, *sell_w, *sell_col;
 };
 
-// Row i of A x on the SELL-32 layout: the lanes of a warp read 32
-// consecutive values and columns per entry (one coalesced 256-byte or
-// 128-byte line each); the entries are summed in CSR order and padding adds
-// exact zeros, so the result equals the CSR row sum.
-template <class VT, class MT>
-__device__ __forceinline__ VT row_dot_sell(const SolverDev &d,
-                                           const MT *__restrict__ val,
-                                           const VT *__restrict__ x, int i) {
-  const int q = i >> 5;
-  const int w = d.sell_w[q];
-  const int base = d.sell_ptr[q] + (i & 31);
-  VT s = 0;
-  for (int k = 0; k < w; ++k)
-    s += (VT)val[base + 32 * k] * x[d.sell_col[base + 32 * k]];
-  return s;
-}
+
 
 void launch_permute_values(int nnz, const int32_t *psrc, const double *src,
                            double *dst, int n_dup, const int32_t *dup_dst,
@@ -294,13 +276,12 @@ void launch_b_init(const BatchTiles &T, const BatchRed &R, int block,
                    const double *b, const double *x, double *r, double *rh,
                    double *p, double *v, KScalars *sc, const int *init,
                    cudaStream_t st);
-// the SpMV kernels read the SELL-32 layout (row_dot_sell)
 void launch_b_spmv_v(const BatchTiles &T, const BatchRed &R, int block,
-                     const SolverDev &d, const double *sell_val,
+                     const SolverDev &d, const double *val,
                      const double *ph, double *v, const double *rh,
                      KScalars *sc, cudaStream_t st);
 void launch_b_spmv_t(const BatchTiles &T, const BatchRed &R, int block,
-                     const SolverDev &d, const double *sell_val,
+                     const SolverDev &d, const double *val,
                      const double *sh, double *t, const double *s,
                      KScalars *sc, cudaStream_t st);
 void launch_b_update(const BatchTiles &T, const BatchRed &R, int block,

@@ -31,15 +31,6 @@ __global__ void k_count_diff(int64_t n, const int32_t *__restrict__ a,
     }
 }
 
-// SELL values from the permuted CSR values (padding 0)
-__global__ void k_sell_gather(int64_t n, const int32_t *__restrict__ src,
-                              const double *__restrict__ vals,
-                              double *__restrict__ out) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = src[i] >= 0 ? vals[src[i]] : 0.;
-}
-
 // deterministic non-zero contents for kernel timing
 __global__ void k_fill_profile(int64_t n, double *__restrict__ a,
                                float *__restrict__ b, int salt) {
@@ -78,13 +69,8 @@ struct pg_solver {
   DevBuf<double> pvals, jdinv;
   // Krylov vectors (permuted order)
   DevBuf<double> b, x, r, rh, p, v, ph, s, sh, t, xout;
-  // SELL-32 layout of the permuted matrix and its values (FP64 and float
-  // pairs) for the Krylov SpMV
-  DevBuf<int32_t> sell_ptr, sell_w, sell_col, sell_src;
-  DevBuf<double> sell_vals;
-  DevBuf<float2> sell_vals_dd;
-  // float-float Jacobi diagonal and Krylov vectors of PG_MIXED
-  DevBuf<float2> jdinv_dd;
+  // float-float matrix, Jacobi diagonal and Krylov vectors of PG_MIXED
+  DevBuf<float2> pvals_dd, jdinv_dd;
   DevBuf<float2> xd, rd, rhd, pd, vd, phd, sd, shd, td;
   // reductions and scalars
   DevBuf<double> partials;
@@ -151,9 +137,6 @@ struct pg_solver {
     d.max_ku = a.max_ku;
     d.err = err.p;
     d.sub_sys = nullptr;
-    d.sell_ptr = sell_ptr.p;
-    d.sell_w = sell_w.p;
-    d.sell_col = sell_col.p;
     return d;
   }
   RedWork red() const { return RedWork{partials.p, ticket.p, red_grid}; }
@@ -199,13 +182,7 @@ int upload_analysis(pg_solver *s) {
   if (s->cfg.precision == PG_MIXED) up(s->srec_dds, a.srec64);  // static parts
   up(s->pack_src_dd, a.pack_src_dd);
   up(s->pack_dst_dd, a.pack_dst_dd);
-  up(s->sell_ptr, a.sell_ptr);
-  up(s->sell_w, a.sell_w);
-  up(s->sell_col, a.sell_col);
-  up(s->sell_src, a.sell_src);
-  if (e == cudaSuccess) e = s->sell_vals.reserve(a.sell_col.size());
-  if (e == cudaSuccess && s->cfg.precision == PG_MIXED)
-    e = s->sell_vals_dd.reserve(a.sell_col.size());
+
   if (e == cudaSuccess) e = s->err.zero(1);
   const size_t n = a.n, nnz = a.nnz;
   for (DevBuf<double> *bf : {&s->b, &s->x, &s->r, &s->rh, &s->p, &s->v,
@@ -217,6 +194,7 @@ int upload_analysis(pg_solver *s) {
     for (DevBuf<float2> *bf : {&s->xd, &s->rd, &s->rhd, &s->pd, &s->vd,
                                &s->phd, &s->sd, &s->shd, &s->td, &s->jdinv_dd})
       if (e == cudaSuccess) e = bf->reserve(n);
+    if (e == cudaSuccess) e = s->pvals_dd.reserve(nnz);
   }
   s->drop_graphs();
   s->red_grid = (int)std::min<int64_t>(red_grid_cap(), (n + kVecBlock - 1) / kVecBlock);
@@ -310,9 +288,9 @@ int run_bicgstab(pg_solver *s, double tol, int max_iters, int *iters,
   auto chunk = [&]() {
     for (int c = 0; c < kChunk; ++c) {
       precond(1, p, ph);
-      launch_spmv_v<double, double>(d, s->sell_vals.p, ph, v, rh, s->sc.p, w, st);
+      launch_spmv_v<double, double>(d, val, ph, v, rh, s->sc.p, w, st);
       precond(2, ss, sh);
-      launch_spmv_t<double, double>(d, s->sell_vals.p, sh, t, ss, s->sc.p, w, st);
+      launch_spmv_t<double, double>(d, val, sh, t, ss, s->sc.p, w, st);
       launch_update<double>(d.n, x, r, ph, sh, ss, t, rh, s->sc.p, w, st);
     }
   };
@@ -404,6 +382,7 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
   const int n = d.n;
   const bool ilu = s->cfg.precond == PG_PREC_ILU0;
   const float2 *jd = s->cfg.precond == PG_PREC_JACOBI ? s->jdinv_dd.p : nullptr;
+  float2 *const val = s->pvals_dd.p;
   float2 *const x = s->xd.p, *const r = s->rd.p, *const rh = s->rhd.p;
   float2 *const p = s->pd.p, *const v = s->vd.p, *const ph = s->phd.p;
   float2 *const ss = s->sd.p, *const sh = s->shd.p, *const t = s->td.p;
@@ -416,9 +395,9 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
   auto chunk = [&]() {
     for (int c = 0; c < kChunk; ++c) {
       precond(1, p, ph);
-      launch_dd_spmv_v(d, s->sell_vals_dd.p, ph, v, rh, s->sc.p, w, st);
+      launch_dd_spmv_v(d, val, ph, v, rh, s->sc.p, w, st);
       precond(2, ss, sh);
-      launch_dd_spmv_t(d, s->sell_vals_dd.p, sh, t, ss, s->sc.p, w, st);
+      launch_dd_spmv_t(d, val, sh, t, ss, s->sc.p, w, st);
       launch_dd_update(n, x, r, ph, sh, ss, t, rh, s->sc.p, w, st);
     }
   };
@@ -494,15 +473,6 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
   }
 }
 
-// SELL values of the current permuted values; returns the slot count
-int64_t sell_gather(pg_solver *s) {
-  const int64_t n_sell = (int64_t)s->a.sell_col.size();
-  k_sell_gather<<<grid_for(n_sell), 256, 0, stream()>>>(
-      n_sell, s->sell_src.p, s->pvals.p, s->sell_vals.p);
-  count_launches(1);
-  return n_sell;
-}
-
 bool use_dd(const pg_solver *s) {
   const SolverDev d = s->dev();
   return s->cfg.precision == PG_MIXED &&
@@ -574,8 +544,7 @@ int factor(pg_solver *s) {
     launch_jacobi_diag(d, s->pvals.p, s->jdinv.p, st);
     if (dd) launch_dd_split(d.n, s->jdinv.p, 1.0, s->jdinv_dd.p, st);
   }
-  const int64_t n_sell = sell_gather(s);
-  if (dd) launch_dd_split(n_sell, s->sell_vals.p, 1.0, s->sell_vals_dd.p, st);
+  if (dd) launch_dd_split(d.nnz, s->pvals.p, 1.0, s->pvals_dd.p, st);
   PG_CUDA(cudaGetLastError());
   if (dd && s->cfg.precond == PG_PREC_ILU0 && s->dd_stream < 0)
     return choose_dd_sweep(s);
@@ -893,7 +862,7 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
   };
   for (int i = 0; i < 8; ++i) ms[i] = 0.;
   // vectors: 0 ph/sh, 1 v/t, 2 rh, 3 r, 4 p/s, 5 x, 6 z
-  int rc = timed([&] { launch_spmv_v<double, double>(d, s->sell_vals.p, d8[0].p, d8[1].p, d8[2].p, s->sc.p, w, st); }, &ms[0]);
+  int rc = timed([&] { launch_spmv_v<double, double>(d, s->pvals.p, d8[0].p, d8[1].p, d8[2].p, s->sc.p, w, st); }, &ms[0]);
   if (!rc) rc = timed([&] { launch_precond<double, double>(s->cfg.precond, 1, d, s->jdinv.p, d8[3].p, d8[4].p, d8[1].p, d8[6].p, s->sc.p, st); }, &ms[1]);
   if (!rc) rc = timed([&] { launch_update<double>(d.n, d8[5].p, d8[3].p, d8[0].p, d8[6].p, d8[4].p, d8[1].p, d8[2].p, s->sc.p, w, st); }, &ms[2]);
   if (!rc && s->cfg.precond == PG_PREC_ILU0)
@@ -901,7 +870,7 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
   if (!rc && dd) {
     if (s->cfg.precond == PG_PREC_ILU0)
       rc = timed([&] { launch_ilu0_apply_dd(1, d, f8[3].p, f8[4].p, f8[1].p, f8[6].p, s->sc.p, st); }, &ms[4]);
-    if (!rc) rc = timed([&] { launch_dd_spmv_v(d, s->sell_vals_dd.p, f8[0].p, f8[1].p, f8[2].p, s->sc.p, w, st); }, &ms[5]);
+    if (!rc) rc = timed([&] { launch_dd_spmv_v(d, s->pvals_dd.p, f8[0].p, f8[1].p, f8[2].p, s->sc.p, w, st); }, &ms[5]);
     if (!rc) rc = timed([&] { launch_dd_update(d.n, f8[5].p, f8[3].p, f8[0].p, f8[6].p, f8[4].p, f8[1].p, f8[2].p, s->sc.p, w, st); }, &ms[6]);
   }
   PG_CUDA(cudaStreamSynchronize(st));
@@ -1077,7 +1046,7 @@ int autotune(pg_batch *b) {
     if (rc) return rc;
     auto run = [&] {
       launch_b_spmv_v(b->tiles(), b->red(), b->block, b->dev(),
-                      s->sell_vals.p, s->ph.p, s->v.p, s->rh.p, b->sc.p, st);
+                      s->pvals.p, s->ph.p, s->v.p, s->rh.p, b->sc.p, st);
     };
     run();
     PG_CUDA(cudaEventRecord(s->ev[0], st));
@@ -1164,11 +1133,11 @@ int build_batch_graph(pg_batch *b) {
     for (int c = 0; c < kChunk; ++c) {
       launch_precond<double, double>(PG_PREC_ILU0, 1, d, nullptr, s->r.p,
                                      s->p.p, s->v.p, s->ph.p, b->sc.p, st);
-      launch_b_spmv_v(T, R, b->block, d, s->sell_vals.p, s->ph.p, s->v.p,
+      launch_b_spmv_v(T, R, b->block, d, s->pvals.p, s->ph.p, s->v.p,
                       s->rh.p, b->sc.p, st);
       launch_precond<double, double>(PG_PREC_ILU0, 2, d, nullptr, s->r.p,
                                      s->s.p, s->v.p, s->sh.p, b->sc.p, st);
-      launch_b_spmv_t(T, R, b->block, d, s->sell_vals.p, s->sh.p, s->t.p,
+      launch_b_spmv_t(T, R, b->block, d, s->pvals.p, s->sh.p, s->t.p,
                       s->s.p, b->sc.p, st);
       launch_b_update(T, R, b->block, s->x.p, s->r.p, s->ph.p, s->sh.p,
                       s->s.p, s->t.p, s->rh.p, b->sc.p, st);
@@ -1262,7 +1231,6 @@ extern "C" int pg_batch_set_eqns(pg_batch *b, int n_systems,
     launch_permute_values((int)s->a.nnz, s->psrc.p, b->st_vals.p, s->pvals.p,
                           (int)s->a.dup_dst.size(), s->dup_dst.p,
                           s->dup_src.p, st);
-    sell_gather(s);
     rc = autotune(b);
     if (rc) return rc;
   }
@@ -1304,7 +1272,6 @@ extern "C" int pg_batch_solve(pg_batch *b, pg_solve_stats *stats,
   PG_CUDA(cudaEventRecord(s->ev[0], st));
   PG_CUDA(cudaMemsetAsync(s->bad.p, 0, sizeof(int), st));
   launch_ilu0_factor(d, s->pvals.p, s->bad.p, false, st);
-  sell_gather(s);
   for (int i = 0; i < S; ++i) {
     KScalars k{};
     k.tol2 = s->cfg.tolerance * s->cfg.tolerance;

@@ -134,9 +134,15 @@ class BubbleSequence:
     """Device-resident rising-bubble sequence: step t's system is assembled
     on the GPU from the bubble position and a reseeded u*."""
 
-    def __init__(self, nx=1024, seed=3):
+    def __init__(self, nx=1024, seed=3, host_fields=False):
+        """host_fields: generate each step's gamma and u* on the host with
+        workloads.rising_bubble_step (reproducible off the GPU, so a CPU run
+        can build the same systems) instead of with torch on the device;
+        prefetch() moves them to the device ahead of time."""
         import torch
         pg = _pg()
+        self.host_fields = host_fields
+        self._cache = {}
         self.torch = torch
         self.nx = nx
         w = workloads.rising_bubble(nx, nx, seed=seed)
@@ -188,10 +194,26 @@ class BubbleSequence:
         u[self._wall] = 0.0
         return gamma.contiguous(), u.contiguous()
 
+    def prefetch(self, steps):
+        """Generate (host mode) and upload the fields of the given steps."""
+        torch = self.torch
+        for t in steps:
+            if t in self._cache:
+                continue
+            g, u = workloads.rising_bubble_step(self.faces, self.cells,
+                                                self.patch, self.nx, t,
+                                                seed=self.seed)
+            self._cache[t] = (torch.from_numpy(g).to(self.dev),
+                              torch.from_numpy(np.ascontiguousarray(u)).to(self.dev))
+
     def assemble(self, t):
         """Assemble step t on the device; returns the equation."""
         torch = self.torch
-        gamma, u = self._fields(t)
+        if self.host_fields:
+            self.prefetch([t])
+            gamma, u = self._cache[t]
+        else:
+            gamma, u = self._fields(t)
         torch.cuda.synchronize()
         self._coeff = torch.empty(self.mesh.n_faces, dtype=torch.float64,
                                   device=self.dev)

@@ -134,3 +134,25 @@ def gcib_case(spec, faces=None):
         out.update(bc_type=bc, bc_value=np.zeros(patch.shape), u=u,
                    patch=patch)
     return out
+
+
+def rising_bubble_step(faces, cells, patch, nx, t, seed=3, span=2000):
+    """Host (numpy) fields of step t of the rising-bubble sequence: gamma per
+    cell (the bubble centre rises from y = 0.5 to 1.5 over ``span`` steps)
+    and the face velocity u* (a smooth swirl plus noise from a generator
+    seeded by (seed, t), zero on the walls).  The bench's timed steps and
+    the CPU reference arm build their systems from these, so both solve the
+    same matrices."""
+    cx0, cy0 = 0.5, 0.5 + min(t, span) / span
+    hx, hy = RB_WIDTH / nx, RB_HEIGHT / nx
+    eps = 1.5 * max(hx, hy)
+    phi = RB_RADIUS - np.hypot(cells["cx"] - cx0, cells["cy"] - cy0)
+    gamma = smoothed_heaviside(phi, eps)
+    rng = np.random.default_rng([seed, t])
+    x, y = faces["fx"], faces["fy"]
+    u = np.empty((x.size, 2))
+    u[:, 0] = 0.1 * np.sin(np.pi * x) * np.cos(0.5 * np.pi * y)
+    u[:, 1] = 0.1 * np.cos(np.pi * x) * np.sin(0.5 * np.pi * y) + 0.02
+    u += 0.01 * rng.standard_normal(u.shape)
+    u[(patch == 0) | (patch == 1) | (patch == 2)] = 0.0
+    return gamma, u
