@@ -523,7 +523,7 @@ def run_batch(args):
                    u_face=w["u"])
         systems.append((m, e))
     eqns = [e for _, e in systems]
-    b = pg.BatchSolver(tolerance=1e-8, max_iters=5000)
+    b = pg.BatchSolver(tolerance=1e-8, max_iters=20000)
     b.set_eqns(eqns)
     setup_s = time.perf_counter() - t_setup
     for _ in range(max(1, args.warmup)):
@@ -547,7 +547,7 @@ def run_batch(args):
     ok = all(st.status == pg.PG_OK and st.rel_residual <= 1e-8 for st in stats)
     # one solver call per system (the reference's one solve() per equation),
     # on one GPU only: the comparison is for the whole batch
-    s = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=5000)
+    s = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000)
     single_ms, single_ok = [], True
     for e in (eqns if world == 1 else []):
         s.set_eqn(e)
