@@ -97,26 +97,6 @@ __device__ __forceinline__ float2 row_dot_dd(const int32_t *__restrict__ rp,
   return dd_value(a);
 }
 
-// rows i and j together (independent loads in flight, as row_dot2 in
-// kernels.cu)
-__device__ __forceinline__ void row_dot_dd2(const int32_t *__restrict__ rp,
-                                            const int32_t *__restrict__ ci,
-                                            const float2 *__restrict__ val,
-                                            const float2 *__restrict__ x,
-                                            int i, int j, float2 &si,
-                                            float2 &sj) {
-  const int bi = rp[i], ei = rp[i + 1], bj = rp[j], ej = rp[j + 1];
-  const int m = (ei - bi) > (ej - bj) ? (ei - bi) : (ej - bj);
-  DdAcc a{0.f, 0.f}, c{0.f, 0.f};
-#pragma unroll 5
-  for (int k = 0; k < m; ++k) {
-    if (bi + k < ei) dd_acc_fma(a, val[bi + k], x[ci[bi + k]]);
-    if (bj + k < ej) dd_acc_fma(c, val[bj + k], x[ci[bj + k]]);
-  }
-  si = dd_value(a);
-  sj = dd_value(c);
-}
-
 __global__ void k_dd_split(int64_t n, const double *__restrict__ src,
                            double scale, float2 *__restrict__ dst) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -197,17 +177,8 @@ k_dd_spmv_v(SolverDev d, const float2 *__restrict__ val,
             const float2 *__restrict__ rh, KScalars *sc, RedWork w) {
   if (sc->done) return;
   DdAcc acc[1] = {{0.f, 0.f}};
-  const int stride = gridDim.x * blockDim.x;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i + stride < d.n; i += 2 * stride) {
-    float2 vi, vj;
-    row_dot_dd2(d.prp, d.pci, val, ph, i, i + stride, vi, vj);
-    v[i] = vi;
-    v[i + stride] = vj;
-    dd_acc_fma(acc[0], rh[i], vi);
-    dd_acc_fma(acc[0], rh[i + stride], vj);
-  }
-  if (i < d.n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
+       i += gridDim.x * blockDim.x) {
     const float2 vi = row_dot_dd(d.prp, d.pci, val, ph, i);
     v[i] = vi;
     dd_acc_fma(acc[0], rh[i], vi);
@@ -234,19 +205,8 @@ k_dd_spmv_t(SolverDev d, const float2 *__restrict__ val,
             const float2 *__restrict__ s, KScalars *sc, RedWork w) {
   if (sc->done) return;
   DdAcc acc[2] = {{0.f, 0.f}, {0.f, 0.f}};
-  const int stride = gridDim.x * blockDim.x;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i + stride < d.n; i += 2 * stride) {
-    float2 ti, tj;
-    row_dot_dd2(d.prp, d.pci, val, sh, i, i + stride, ti, tj);
-    t[i] = ti;
-    t[i + stride] = tj;
-    dd_acc_fma(acc[0], ti, ti);
-    dd_acc_fma(acc[1], ti, s[i]);
-    dd_acc_fma(acc[0], tj, tj);
-    dd_acc_fma(acc[1], tj, s[i + stride]);
-  }
-  if (i < d.n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
+       i += gridDim.x * blockDim.x) {
     const float2 ti = row_dot_dd(d.prp, d.pci, val, sh, i);
     t[i] = ti;
     dd_acc_fma(acc[0], ti, ti);

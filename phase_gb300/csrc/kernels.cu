@@ -414,26 +414,6 @@ __device__ __forceinline__ VT row_dot(const int32_t *__restrict__ rp,
   return s;
 }
 
-// Rows i and j of A x together: the two rows' loads are independent, so a
-// thread keeps twice the memory requests in flight (the SpMV waits on
-// memory latency, not bandwidth, at this occupancy).
-template <class VT, class MT>
-__device__ __forceinline__ void row_dot2(const int32_t *__restrict__ rp,
-                                         const int32_t *__restrict__ ci,
-                                         const MT *__restrict__ val,
-                                         const VT *__restrict__ x, int i,
-                                         int j, VT &si, VT &sj) {
-  const int bi = rp[i], ei = rp[i + 1], bj = rp[j], ej = rp[j + 1];
-  const int m = (ei - bi) > (ej - bj) ? (ei - bi) : (ej - bj);
-  si = 0;
-  sj = 0;
-#pragma unroll 5
-  for (int k = 0; k < m; ++k) {
-    if (bi + k < ei) si += (VT)val[bi + k] * x[ci[bi + k]];
-    if (bj + k < ej) sj += (VT)val[bj + k] * x[ci[bj + k]];
-  }
-}
-
 template <class VT, class MT>
 __global__ void __launch_bounds__(kVecBlock)
 k_krylov_init(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ b,
@@ -476,17 +456,8 @@ k_spmv_v(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ ph,
          RedWork w) {
   if (sc->done) return;
   double acc[1] = {0.};
-  const int stride = gridDim.x * blockDim.x;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i + stride < d.n; i += 2 * stride) {
-    VT vi, vj;
-    row_dot2<VT, MT>(d.prp, d.pci, val, ph, i, i + stride, vi, vj);
-    v[i] = vi;
-    v[i + stride] = vj;
-    acc[0] += (double)rh[i] * (double)vi;
-    acc[0] += (double)rh[i + stride] * (double)vj;
-  }
-  if (i < d.n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
+       i += gridDim.x * blockDim.x) {
     const VT vi = row_dot<VT, MT>(d.prp, d.pci, val, ph, i);
     v[i] = vi;
     acc[0] += (double)rh[i] * (double)vi;
@@ -513,19 +484,8 @@ k_spmv_t(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ sh,
          RedWork w) {
   if (sc->done) return;
   double acc[2] = {0., 0.};
-  const int stride = gridDim.x * blockDim.x;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i + stride < d.n; i += 2 * stride) {
-    VT ti, tj;
-    row_dot2<VT, MT>(d.prp, d.pci, val, sh, i, i + stride, ti, tj);
-    t[i] = ti;
-    t[i + stride] = tj;
-    acc[0] += (double)ti * (double)ti;
-    acc[1] += (double)ti * (double)s[i];
-    acc[0] += (double)tj * (double)tj;
-    acc[1] += (double)tj * (double)s[i + stride];
-  }
-  if (i < d.n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
+       i += gridDim.x * blockDim.x) {
     const VT ti = row_dot<VT, MT>(d.prp, d.pci, val, sh, i);
     t[i] = ti;
     acc[0] += (double)ti * (double)ti;
