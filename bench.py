@@ -65,6 +65,9 @@ def parse():
     ap.add_argument("--nx", type=int, default=1024)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--subdomain-rows", type=int, default=0)
+    ap.add_argument("--mixed-sweep", type=int, default=0, choices=[0, 1, 2],
+                    help="mixed ILU(0) sweep form: 0 timed choice, 1 steps, "
+                         "2 level blobs")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -618,7 +621,8 @@ def run_single(args):
     prec = pg.MIXED if args.precision == "mixed" else pg.FP64
     solver = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
                                    precision=prec,
-                                   subdomain_rows=args.subdomain_rows)
+                                   subdomain_rows=args.subdomain_rows,
+                                   mixed_sweep=args.mixed_sweep)
     stream = torch.cuda.ExternalStream(pg.stream_handle(), device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
