@@ -837,7 +837,7 @@ def run_reference(args):
         vals, its, rels = [], [], []
         for t in list(range(t0 - W, t0 + K)):
             rp, ci, v, rhs = system(t)
-            x, st = ob.bicgstab(rp, ci, v, -rhs, tol=1e-8, max_iters=8000,
+            x, st = ob.bicgstab(rp, ci, v, -rhs, tol=1e-8, max_iters=6000,
                                 part=part, x0=x, threads=threads)
             if t >= t0:
                 vals.append(st["ms"] + st["setup_ms"])
@@ -845,7 +845,7 @@ def run_reference(args):
                 rels.append(st["rel_residual"])
         value = float(np.mean(vals))
         workload = workload_name(nx) + f", time steps {t0}..{t0 + K - 1}"
-        sample = (f"{K} consecutive time steps, each solved to 1e-8 (max 8000 "
+        sample = (f"{K} consecutive time steps, each solved to 1e-8 (max 6000 "
                   f"iterations) from the previous step's solution; iterations "
                   f"{its}, rel. residuals {[f'{r:.1e}' for r in rels]}")
     else:
