@@ -416,41 +416,6 @@ __device__ __forceinline__ VT row_dot(const int32_t *__restrict__ rp,
 
 template <class VT, class MT>
 __global__ void __launch_bounds__(kVecBlock)
-k_krylov_init(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ b,
-              const VT *__restrict__ x, VT *__restrict__ r, VT *__restrict__ rh,
-              VT *__restrict__ p, VT *__restrict__ v, KScalars *sc, RedWork w) {
-  double acc[2] = {0., 0.};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
-       i += gridDim.x * blockDim.x) {
-    const VT ri = b[i] - row_dot<VT, MT>(d.prp, d.pci, val, x, i);
-    r[i] = ri;
-    rh[i] = ri;
-    p[i] = 0;
-    v[i] = 0;
-    acc[0] += (double)ri * (double)ri;
-    acc[1] += (double)b[i] * (double)b[i];
-  }
-  double tot[2];
-  if (grid_reduce<2>(acc, w, tot) && threadIdx.x == 0) {
-    sc->rr = tot[0];
-    sc->bb = tot[1];
-    sc->rho = tot[0];
-    sc->alpha = 1.;
-    sc->omega = 1.;
-    sc->beta = tot[0];
-    sc->status = PG_OK;
-    sc->done = 0;
-    if (!finite(tot[0]) || !finite(tot[1])) {
-      sc->status = PG_NON_FINITE;
-      sc->done = 1;
-    } else if (tot[0] <= sc->tol2 * tot[1]) {
-      sc->done = 1;
-    }
-  }
-}
-
-template <class VT, class MT>
-__global__ void __launch_bounds__(kVecBlock)
 k_spmv_v(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ ph,
          VT *__restrict__ v, const VT *__restrict__ rh, KScalars *sc,
          RedWork w) {
@@ -758,14 +723,6 @@ void launch_unpermute_vec(int n, const int32_t *perm, const double *src,
 }
 
 template <class VT, class MT>
-void launch_krylov_init(const SolverDev &d, const MT *val, const VT *b,
-                        const VT *x, VT *r, VT *rh, VT *p, VT *v, KScalars *sc,
-                        RedWork w, cudaStream_t st) {
-  k_krylov_init<VT, MT><<<w.grid, kVecBlock, 0, st>>>(d, val, b, x, r, rh, p, v,
-                                                      sc, w);
-  count_launches(1);
-}
-template <class VT, class MT>
 void launch_spmv_v(const SolverDev &d, const MT *val, const VT *ph, VT *v,
                    const VT *rh, KScalars *sc, RedWork w, cudaStream_t st) {
   k_spmv_v<VT, MT><<<w.grid, kVecBlock, 0, st>>>(d, val, ph, v, rh, sc, w);
@@ -826,10 +783,6 @@ void launch_diag_apply(int mode, const SolverDev &d, const MT *dinv,
   template void launch_diag_apply<VT, MT>(int, const SolverDev &, const MT *, \
                                           const VT *, VT *, const VT *, VT *, \
                                           const KScalars *, cudaStream_t);    \
-  template void launch_krylov_init<VT, MT>(const SolverDev &, const MT *,     \
-                                           const VT *, const VT *, VT *,      \
-                                           VT *, VT *, VT *, KScalars *,      \
-                                           RedWork, cudaStream_t);            \
   template void launch_spmv_v<VT, MT>(const SolverDev &, const MT *,          \
                                       const VT *, VT *, const VT *,           \
                                       KScalars *, RedWork, cudaStream_t);     \

@@ -202,10 +202,6 @@ void launch_precond(int precond, int mode, const SolverDev &d,
                     const KScalars *sc, cudaStream_t st);
 
 template <class VT, class MT>
-void launch_krylov_init(const SolverDev &d, const MT *val, const VT *b,
-                        const VT *x, VT *r, VT *rh, VT *p, VT *v, KScalars *sc,
-                        RedWork w, cudaStream_t st);
-template <class VT, class MT>
 void launch_spmv_v(const SolverDev &d, const MT *val, const VT *ph, VT *v,
                    const VT *rh, KScalars *sc, RedWork w, cudaStream_t st);
 template <class VT, class MT>
