@@ -102,6 +102,18 @@ int pg_mesh_cells(const pg_mesh *m, double *cx, double *cy, double *vol);
  * ---------------------------------------------------------------------- */
 int pg_eqn_create(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
                   pg_eqn **out);
+/* Projection step after the pressure solve: u -= dt / rho * grad p on every
+ * cell and every face (FractionalStep::correctVelocity,
+ * src/2D/Unstructured/Solvers/FractionalStep.cpp:109-117, and its
+ * multiphase form FractionalStepMultiphase.cpp:165-173).  rho_cell[n] and
+ * rho_face[nf] are both given (multiphase) or both NULL (rho = 1).
+ * grad_cell/u_cell hold x,y per cell (2n), grad_face/u_face per face (2nf),
+ * e.g. from pg_gradient; u_cell and u_face are updated in place. */
+int pg_correct_velocity(const pg_mesh *m, double dt, const double *rho_cell,
+                        const double *rho_face, const double *grad_cell,
+                        const double *grad_face, double *u_cell,
+                        double *u_face, int ptr_kind);
+
 /* Ghost-cell immersed-boundary pressure equation of FractionalStepGCIB
  * (src/2D/Unstructured/Solvers/FractionalStepGCIB.cpp:44-46):
  *   (fv::laplacian(gamma, p) + ib.bcs(p)) == src::div(u)

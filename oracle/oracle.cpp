@@ -1177,3 +1177,26 @@ extern "C" or_eqn *or_gcib_laplacian(const or_mesh *m, const double *gamma_face,
   if (cell_class) std::copy(cls.begin(), cls.end(), cell_class);
   return lap;
 }
+
+// FractionalStep::correctVelocity (src/2D/Unstructured/Solvers/
+// FractionalStep.cpp:109-117) and FractionalStepMultiphase::correctVelocity
+// (FractionalStepMultiphase.cpp:165-173): u -= timeStep / rho * gradP on
+// every cell and every face; rho NULL = 1.
+extern "C" void or_correct_velocity(const or_mesh *m, double dt,
+                                    const double *rho_cell,
+                                    const double *rho_face,
+                                    const double *grad_cell,
+                                    const double *grad_face, double *u_cell,
+                                    double *u_face) {
+  const int64_t n = (int64_t)m->centroid.size(), nf = (int64_t)m->fl.size();
+  for (int64_t c = 0; c < n; ++c) {
+    const double k = rho_cell ? dt / rho_cell[c] : dt;
+    u_cell[2 * c] -= k * grad_cell[2 * c];
+    u_cell[2 * c + 1] -= k * grad_cell[2 * c + 1];
+  }
+  for (int64_t f = 0; f < nf; ++f) {
+    const double k = rho_face ? dt / rho_face[f] : dt;
+    u_face[2 * f] -= k * grad_face[2 * f];
+    u_face[2 * f + 1] -= k * grad_face[2 * f + 1];
+  }
+}

@@ -166,6 +166,13 @@ or_eqn *or_gcib_laplacian(const or_mesh *m, const double *gamma_face,
                           const double *bc_value, const double *u_face_xy,
                           int n_circles, const double *circles, int ib_bc,
                           double ib_ref, int32_t *cell_class);
+/* FractionalStep::correctVelocity: u -= dt / rho * grad p on cells and
+ * faces (FractionalStep.cpp:109-117, FractionalStepMultiphase.cpp:165-173);
+ * rho arrays NULL = 1.  x,y interleaved. */
+void or_correct_velocity(const or_mesh *m, double dt, const double *rho_cell,
+                         const double *rho_face, const double *grad_cell,
+                         const double *grad_face, double *u_cell,
+                         double *u_face);
 /* y = A x */
 void or_spmv(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
              const double *vals, const double *x, double *y);

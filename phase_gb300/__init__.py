@@ -72,6 +72,7 @@ PROTOTYPES = {
     "pg_mesh_faces": (_I, [_P, _P, _P, _P, _P, _P, _P]),
     "pg_mesh_cells": (_I, [_P, _P, _P, _P]),
     "pg_eqn_create": (_I, [_P, _I, _P, ctypes.POINTER(_P)]),
+    "pg_correct_velocity": (_I, [_P, _D, _P, _P, _P, _P, _P, _P, _I]),
     "pg_eqn_create_gcib": (_I, [_P, _I, _P, _I, _P, _I, _D, ctypes.POINTER(_P)]),
     "pg_eqn_cell_class": (_I, [_P, _P]),
     "pg_eqn_create_momentum": (_I, [_P, _P, ctypes.POINTER(_P)]),
@@ -244,6 +245,21 @@ class Mesh:
         _check(lib().pg_gradient(self._h, _ptr(pc), _ptr(pf), _ptr(gf),
                                  _ptr(gc), PG_HOST))
         return gf.reshape(-1, 2), gc.reshape(-1, 2)
+
+    def correct_velocity(self, dt, grad_cell, grad_face, u_cell, u_face,
+                         rho_cell=None, rho_face=None):
+        """FractionalStep::correctVelocity: returns (u_cell, u_face) after
+        u -= dt / rho * grad p (rho = 1 when not given)."""
+        uc = np.array(u_cell, np.float64).reshape(-1)
+        uf = np.array(u_face, np.float64).reshape(-1)
+        rc = None if rho_cell is None else _f64(rho_cell, self.n_cells)
+        rf = None if rho_face is None else _f64(rho_face, self.n_faces)
+        _check(lib().pg_correct_velocity(
+            self._h, float(dt), _ptr(rc), _ptr(rf),
+            _ptr(_f64(np.asarray(grad_cell).reshape(-1), 2 * self.n_cells)),
+            _ptr(_f64(np.asarray(grad_face).reshape(-1), 2 * self.n_faces)),
+            _ptr(uc), _ptr(uf), PG_HOST))
+        return uc.reshape(-1, 2), uf.reshape(-1, 2)
 
 
 class Equation:

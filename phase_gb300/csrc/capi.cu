@@ -550,3 +550,40 @@ extern "C" int pg_gradient(const pg_mesh *m, const double *phi_cell,
   PG_CUDA(cudaStreamSynchronize(stream()));
   return PG_OK;
 }
+
+extern "C" int pg_correct_velocity(const pg_mesh *m, double dt,
+                                   const double *rho_cell,
+                                   const double *rho_face,
+                                   const double *grad_cell,
+                                   const double *grad_face, double *u_cell,
+                                   double *u_face, int ptr_kind) {
+  PG_CHECK_ARG(m && grad_cell && grad_face && u_cell && u_face,
+               "pg_correct_velocity: NULL arg");
+  PG_CHECK_ARG((rho_cell == nullptr) == (rho_face == nullptr),
+               "pg_correct_velocity: give both densities or neither");
+  const HostMesh &h = m->h;
+  const int64_t n = h.n_cells, nf = h.n_faces;
+  DevBuf<double> a, b, c, d, e, f;
+  const double *rc = nullptr, *rf = nullptr, *gc = nullptr, *gf = nullptr;
+  int rcode = stage(rho_cell, n, ptr_kind, a, &rc);
+  if (!rcode) rcode = stage(rho_face, nf, ptr_kind, b, &rf);
+  if (!rcode) rcode = stage(grad_cell, 2 * n, ptr_kind, c, &gc);
+  if (!rcode) rcode = stage(grad_face, 2 * nf, ptr_kind, d, &gf);
+  if (rcode) return rcode;
+  double *uc = u_cell, *uf = u_face;
+  if (ptr_kind != PG_DEVICE) {
+    PG_CUDA(e.upload(u_cell, 2 * n));
+    PG_CUDA(f.upload(u_face, 2 * nf));
+    uc = e.p;
+    uf = f.p;
+  }
+  launch_correct_velocity((int)n, dt, rc, gc, uc, stream());
+  launch_correct_velocity((int)nf, dt, rf, gf, uf, stream());
+  PG_CUDA(cudaGetLastError());
+  if (ptr_kind != PG_DEVICE) {
+    PG_CUDA(copy_out(u_cell, uc, 2 * n * sizeof(double), PG_HOST));
+    PG_CUDA(copy_out(u_face, uf, 2 * nf * sizeof(double), PG_HOST));
+  }
+  PG_CUDA(cudaStreamSynchronize(stream()));
+  return PG_OK;
+}

@@ -588,6 +588,22 @@ k_true_residual(SolverDev d, const double *__restrict__ val,
 
 inline int blocks_for(int n, int bs) { return (n + bs - 1) / bs; }
 
+// u -= (dt / rho) * grad p per cell and per face (FractionalStep.cpp:109-117,
+// FractionalStepMultiphase.cpp:165-173); rho NULL means 1 (single phase:
+// u -= dt * grad p).  The coefficient is formed first, as the reference
+// evaluates timeStep / rho_(cell) * gradP_(cell).
+__global__ void k_correct_velocity(int n, double dt,
+                                   const double *__restrict__ rho,
+                                   const double *__restrict__ grad,
+                                   double *__restrict__ u) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    const double c = rho ? __ddiv_rn(dt, rho[i]) : dt;
+    u[2 * i] = __dadd_rn(u[2 * i], -__dmul_rn(c, grad[2 * i]));
+    u[2 * i + 1] = __dadd_rn(u[2 * i + 1], -__dmul_rn(c, grad[2 * i + 1]));
+  }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- launchers
@@ -621,6 +637,14 @@ void launch_assemble_boundary(int nf, int off, const int32_t *cface,
   k_assemble_boundary<<<blocks_for(nf, 256), 256, 0, st>>>(
       nf, off, cface, cl, bc, dot_l, msq, diag_l, sfl_x, sfl_y, gamma_face,
       gamma_scalar, bc_value, u_face, vals, rhs);
+  count_launches(1);
+}
+
+void launch_correct_velocity(int n, double dt, const double *rho,
+                             const double *grad, double *u, cudaStream_t st) {
+  if (n <= 0) return;
+  const int g = blocks_for(n, 256) < 2432 ? blocks_for(n, 256) : 2432;
+  k_correct_velocity<<<g, 256, 0, st>>>(n, dt, rho, grad, u);
   count_launches(1);
 }
 

@@ -81,6 +81,8 @@ void launch_momentum_boundary(int nf, int off, const int32_t *cface,
                               const double *sfl_y, double nu, double theta,
                               const double *u0, const double *u_face, int n,
                               double *vals, double *rhs, cudaStream_t st);
+void launch_correct_velocity(int n, double dt, const double *rho,
+                             const double *grad, double *u, cudaStream_t st);
 void launch_interp_faces(int nf, const int32_t *fl, const int32_t *fr,
                          const double *fcx, const double *fcy,
                          const double *cx, const double *cy,

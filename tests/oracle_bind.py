@@ -83,6 +83,7 @@ def lib():
         L.or_spmv.argtypes = [I64, P, P, P, P, P]
         L.or_momentum.restype = P
         L.or_momentum.argtypes = [P, D, D, D, P, P, P]
+        L.or_correct_velocity.argtypes = [P, D, P, P, P, P, P, P]
         L.or_gcib_laplacian.restype = P
         L.or_gcib_laplacian.argtypes = [P, P, D, P, P, P, ctypes.c_int, P,
                                         ctypes.c_int, D, P]
@@ -196,6 +197,18 @@ class OracleMesh:
         lib().or_eqn_export_csr(e, ptr(rp), ptr(ci), ptr(v), ptr(rhs))
         lib().or_eqn_destroy(e)
         return rp, ci, v, rhs, cls
+
+    def correct_velocity(self, dt, grad_cell, grad_face, u_cell, u_face,
+                         rho_cell=None, rho_face=None):
+        uc = np.array(u_cell, np.float64).reshape(-1)
+        uf = np.array(u_face, np.float64).reshape(-1)
+        rc = None if rho_cell is None else np.ascontiguousarray(rho_cell, np.float64)
+        rf = None if rho_face is None else np.ascontiguousarray(rho_face, np.float64)
+        gc = np.ascontiguousarray(np.asarray(grad_cell, np.float64).reshape(-1))
+        gf = np.ascontiguousarray(np.asarray(grad_face, np.float64).reshape(-1))
+        lib().or_correct_velocity(self.h, float(dt), ptr(rc), ptr(rf), ptr(gc),
+                                  ptr(gf), ptr(uc), ptr(uf))
+        return uc.reshape(-1, 2), uf.reshape(-1, 2)
 
     def momentum(self, dt, nu, theta, u_old_cell, u_face, bc_type):
         """ddt + div - laplacian(nu) of the vector equation: compact CSR of

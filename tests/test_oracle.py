@@ -246,3 +246,30 @@ def test_momentum_operator_known_answers(oracle):
     assert np.all(A[:n, n:] == 0) and np.all(A[n:, :n] == 0)
     assert np.allclose(rhs[:n], -rhsl, rtol=1e-14, atol=1e-14)
     assert np.all(rhs[n:] == 0.0) and np.any(rhs[:n] != 0.0)
+
+
+def test_projection_property_of_correct_velocity(oracle):
+    """After fv::laplacian(dt/rho, p) == src::div(u*) is solved (scipy direct)
+    and u* is corrected with the face gradient (FractionalStep::
+    correctVelocity), src::div of the corrected face velocity vanishes."""
+    from phase_gb300 import workloads
+    w = workloads.rising_bubble(32, 32, seed=3)
+    om = oracle.OracleMesh(w["nodes"], w["cptr"], w["cind"])
+    f = om.faces()
+    w = workloads.rising_bubble(32, 32, seed=3, faces=f, cells=om.cells())
+    coeff = om.dt_over_rho(w["gamma"], w["rho1"], w["rho2"], w["dt"])
+    rp, ci, v, rhs = om.laplacian(coeff, w["bc_type"], w["bc_value"], w["u"])
+    A = sp.csr_matrix((v, ci, rp), shape=(om.n_cells,) * 2)
+    p = spla.spsolve(A.tocsc(), -rhs)
+    bnd = f["rcell"] < 0
+    p_face = np.zeros(om.n_faces)
+    p_face[bnd] = np.where(w["bc_type"][bnd] == 0, w["bc_value"][bnd],
+                           p[f["lcell"][bnd]])
+    gf, gc = om.gradient(p, p_face)
+    _, uf = om.correct_velocity(w["dt"], gc, gf, np.zeros((om.n_cells, 2)),
+                                w["u"], None, w["dt"] / coeff)
+
+    def div(u):
+        return -om.laplacian(0.0, w["bc_type"], w["bc_value"], u)[3]
+
+    assert np.abs(div(uf)).max() <= 1e-9 * np.abs(div(w["u"])).max()
