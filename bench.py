@@ -280,9 +280,11 @@ def run_sequence(args):
     have_w = os.path.exists(guess.DEFAULT_WEIGHTS)
     if have_w:
         net.set_params(np.load(guess.DEFAULT_WEIGHTS))
-    sp = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000)
+    sp = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
+                               subdomain_rows=args.subdomain_rows)
     sm = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
-                               precision=pg.MIXED)
+                               precision=pg.MIXED,
+                               subdomain_rows=args.subdomain_rows)
     xp_p = torch.zeros(n, dtype=torch.float64, device=dev)
     xp_m = torch.zeros(n, dtype=torch.float64, device=dev)
     g = torch.empty(n, dtype=torch.float64, device=dev)

@@ -112,21 +112,25 @@ __device__ __forceinline__ double dd_acc_to_double(const DdAcc &a) {
 // BiCGStab update (modes as pre_input in kernels.cuh):
 //   mode 1: p = r + beta (p - omega v), written back to pv
 //   mode 2: s = r - alpha v,            written to pv
+__device__ __forceinline__ float2 dd_pre_combine(int mode, float2 ri,
+                                                 float2 pi, float2 vi,
+                                                 const KScalars *sc) {
+  if (mode == 1)
+    return dd_add(ri, dd_mul(sc->beta_dd, dd_sub(pi, dd_mul(sc->omega_dd, vi))));
+  if (mode == 2) return dd_sub(ri, dd_mul(sc->alpha_dd, vi));
+  return pi;
+}
+
 __device__ __forceinline__ float2 dd_pre_input(int mode, int i,
                                                const float2 *r, float2 *pv,
                                                const float2 *v,
                                                const KScalars *sc) {
-  if (mode == 1) {
-    const float2 t = dd_sub(pv[i], dd_mul(sc->omega_dd, v[i]));
-    const float2 val = dd_add(r[i], dd_mul(sc->beta_dd, t));
-    pv[i] = val;
-    return val;
-  } else if (mode == 2) {
-    const float2 val = dd_sub(r[i], dd_mul(sc->alpha_dd, v[i]));
-    pv[i] = val;
-    return val;
-  }
-  return pv[i];
+  const float2 zero = make_float2(0.f, 0.f);
+  const float2 val = dd_pre_combine(mode, mode ? r[i] : zero,
+                                    mode != 2 ? pv[i] : zero,
+                                    mode ? v[i] : zero, sc);
+  if (mode) pv[i] = val;
+  return val;
 }
 
 }  // namespace pg

@@ -268,6 +268,7 @@ namespace {
 // vertices is reordered by breadth-first distance from a pseudo-peripheral
 // vertex (two sweeps) and cut so both halves hold whole multiples of the
 // target subdomain size; cuts recurse until a range fits one subdomain.
+// (With row coordinates, analyse() cuts by coordinate instead.)
 // Emission order is left-to-right, so consecutive subdomains are neighbours.
 struct Bisector {
   int64_t n;
@@ -318,7 +319,8 @@ struct Bisector {
 
 int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
             int subdomain_rows, Analysis &a,
-            const std::vector<int64_t> *sys_rows) {
+            const std::vector<int64_t> *sys_rows, const double *cx,
+            const double *cy) {
   PG_CHECK_ARG(n > 0 && row_ptr && col_ind, "analyse: empty matrix");
   PG_CHECK_ARG(row_ptr[0] == 0, "row_ptr[0] must be 0");
   for (int64_t i = 0; i < n; ++i)
@@ -404,6 +406,7 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
     if (target < 0) target = INT32_MAX;
     Bisector bs(n, ap, aj);
     std::vector<std::pair<int64_t, int64_t>> stack{{0, n}};
+    const bool rcb = cx && cy;
     if (sys_rows) {  // one root range per system, popped in system order
       PG_CHECK_ARG(sys_rows->size() >= 2 && sys_rows->front() == 0 &&
                        sys_rows->back() == n,
@@ -421,14 +424,30 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
         parts.push_back({lo, hi});
         continue;
       }
-      ++bs.range_stamp;
-      for (int64_t k = lo; k < hi; ++k) bs.in_range[order[k]] = bs.range_stamp;
-      int32_t start = *std::min_element(order.begin() + lo, order.begin() + hi);
-      int32_t far = bs.bfs(start, order.data() + lo, cnt);
-      bs.bfs(far, order.data() + lo, cnt);
-      std::copy(bs.queue.begin(), bs.queue.end(), order.begin() + lo);
       const int64_t k_parts = (cnt + target - 1) / target;
       const int64_t left = cnt * (k_parts / 2) / k_parts;
+      if (rcb) {
+        // coordinate bisection across the longer extent of the range's
+        // cell centres (ties broken by row index)
+        double x0 = cx[order[lo]], x1 = x0, y0 = cy[order[lo]], y1 = y0;
+        for (int64_t k = lo; k < hi; ++k) {
+          const int32_t r = order[k];
+          x0 = std::min(x0, cx[r]), x1 = std::max(x1, cx[r]);
+          y0 = std::min(y0, cy[r]), y1 = std::max(y1, cy[r]);
+        }
+        const double *c = x1 - x0 >= y1 - y0 ? cx : cy;
+        std::nth_element(order.begin() + lo, order.begin() + lo + left,
+                         order.begin() + hi, [c](int32_t p, int32_t q) {
+                           return c[p] < c[q] || (c[p] == c[q] && p < q);
+                         });
+      } else {
+        ++bs.range_stamp;
+        for (int64_t k = lo; k < hi; ++k) bs.in_range[order[k]] = bs.range_stamp;
+        int32_t start = *std::min_element(order.begin() + lo, order.begin() + hi);
+        int32_t far = bs.bfs(start, order.data() + lo, cnt);
+        bs.bfs(far, order.data() + lo, cnt);
+        std::copy(bs.queue.begin(), bs.queue.end(), order.begin() + lo);
+      }
       stack.push_back({lo + left, hi});
       stack.push_back({lo, lo + left});
     }
@@ -660,7 +679,7 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       for (auto &q : bp) total += q.second, max_piece = std::max(max_piece, q.second);
       PG_CHECK_ARG(soff + total < ((int64_t)1 << 31), "ILU(0) stream too large");
       a.smeta64[s] = StreamMeta{f.r0, nr, nlev, KL, KU, (int32_t)soff,
-                                (int32_t)hdr, (int32_t)max_piece};
+                                (int32_t)hdr, (int32_t)max_piece, 0, 0, 0, 0};
       std::vector<uint8_t> &buf = a.srec64;
       buf.resize(soff + total, 0);
       uint8_t *base = buf.data() + soff;
@@ -718,6 +737,13 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
             emit_values(doff + vs * j, (int64_t)(fKL + fKU) * nr + ra + j);
           off += bblob(w);
         }
+      }
+      StreamMeta &sm = a.smeta64[s];
+      sm.p0_off = ints[3];
+      sm.p0_bytes = ints[4];
+      if (np > 1) {
+        sm.p1_off = ints[6];
+        sm.p1_bytes = ints[7];
       }
       soff += total;
       const size_t need = (size_t)hdr + 2 * (size_t)max_piece + (size_t)al16(vs * (int64_t)(nr + 1));

@@ -181,6 +181,40 @@ __device__ __forceinline__ void sweep_level_dd(float2 *zs, int a, int w,
   }
 }
 
+// One lane's row of a level (lane < w), held in registers: the KT column
+// slots, their weights and, for the backward sweep, 1/u_ii.  Record layout
+// of a level of width w: columns (uint16, slot-major, 16-byte padded), the
+// weights (slot-major, padded), then 1/u_ii for a backward level.
+template <class V, int KT>
+struct LevelRegs {
+  uint16_t c[KT];
+  V v[KT];
+  V d;
+  template <bool DIAG>
+  __device__ __forceinline__ void load(const uint8_t *p, int w, int lane) {
+    if (lane >= w || w > 32) return;
+    const uint16_t *cp = reinterpret_cast<const uint16_t *>(p);
+    const V *vp = reinterpret_cast<const V *>(p + al16(2 * KT * w));
+#pragma unroll
+    for (int k = 0; k < KT; ++k) {
+      c[k] = cp[k * w + lane];
+      v[k] = vp[k * w + lane];
+    }
+    if (DIAG)
+      d = reinterpret_cast<const V *>(p + al16(2 * KT * w) +
+                                      al16((int)sizeof(V) * KT * w))[lane];
+  }
+  // the row's new z: (z_self - sum_k v_k z[c_k]) (* 1/u_ii), with the
+  // arithmetic of sweep_level / sweep_level_dd
+  template <class AR, bool DIAG>
+  __device__ __forceinline__ V sweep(const V *zs, V self) const {
+    V x[KT];
+#pragma unroll
+    for (int k = 0; k < KT; ++k) x[k] = zs[c[k]];
+    return AR::template row<KT, DIAG>(self, v, x, d);
+  }
+};
+
 // Arithmetic of the streamed sweep: FP64, or float-float on the same
 // record layout (a float pair takes the 8 bytes of a double).
 struct ArithF64 {
@@ -189,7 +223,17 @@ struct ArithF64 {
                           const KScalars *sc) {
     return pre_input<double>(mode, i, r, pv, v, sc);
   }
+  __device__ static V combine(int mode, V ri, V pi, V vi, const KScalars *sc) {
+    return pre_combine<double>(mode, ri, pi, vi, sc);
+  }
   __device__ static V zero() { return 0.; }
+  template <int KT, bool DIAG>
+  __device__ static V row(V self, const V (&v)[KT], const V (&x)[KT], V d) {
+    V acc = self;
+#pragma unroll
+    for (int k = 0; k < KT; ++k) acc -= v[k] * x[k];
+    return DIAG ? acc * d : acc;
+  }
   template <int KT>
   __device__ static void level(V *zs, int a, int w, int ks,
                                const uint16_t *cc, const V *vv, const V *dd,
@@ -203,7 +247,18 @@ struct ArithDD {
                           const KScalars *sc) {
     return dd_pre_input(mode, i, r, pv, v, sc);
   }
+  __device__ static V combine(int mode, V ri, V pi, V vi, const KScalars *sc) {
+    return dd_pre_combine(mode, ri, pi, vi, sc);
+  }
   __device__ static V zero() { return make_float2(0.f, 0.f); }
+  template <int KT, bool DIAG>
+  __device__ static V row(V self, const V (&v)[KT], const V (&x)[KT], V d) {
+    DdAcc acc = dd_acc(self);
+#pragma unroll
+    for (int k = 0; k < KT; ++k) dd_acc_fma(acc, dd_neg(v[k]), x[k]);
+    const float2 out = dd_value(acc);
+    return DIAG ? dd_mul(out, d) : out;
+  }
   template <int KT>
   __device__ static void level(V *zs, int a, int w, int ks,
                                const uint16_t *cc, const V *vv, const V *dd,
@@ -242,29 +297,61 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
   uint8_t *const buf0 = smem + m.hdr_bytes;  // buffer b at buf0 + b*max_piece
   MT *zs = reinterpret_cast<MT *>(smem + m.hdr_bytes + 2 * m.max_piece);
   const uint8_t *g = rec + m.rec_off;
+  // the header and the first two pieces are in flight while the input is
+  // staged
   if (lane == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     mbar_init(&bar[2], 1);
     mbar_expect_tx(&bar[2], (uint32_t)m.hdr_bytes);
     bulk_load(hdr, g, (uint32_t)m.hdr_bytes, &bar[2]);
+    mbar_expect_tx(&bar[0], (uint32_t)m.p0_bytes);
+    bulk_load(buf0, g + m.p0_off, (uint32_t)m.p0_bytes, &bar[0]);
+    if (m.p1_bytes > 0) {
+      mbar_expect_tx(&bar[1], (uint32_t)m.p1_bytes);
+      bulk_load(buf0 + m.max_piece, g + m.p1_off, (uint32_t)m.p1_bytes,
+                &bar[1]);
+    }
   }
-  for (int i = lane; i < nr; i += 32)
-    zs[i] = AR::pre(MODE, m.r0 + i, r, pv, v, sc);
+  {
+    // input staging, four rows per lane in flight
+    constexpr int U = 4;
+    const MT zero = AR::zero();
+    for (int i0 = lane; i0 < nr; i0 += 32 * U) {
+      MT ri[U], pi[U], vi[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + 32 * u;
+        ri[u] = pi[u] = vi[u] = zero;
+        if (i < nr) {
+          if (MODE != 0) ri[u] = r[m.r0 + i], vi[u] = v[m.r0 + i];
+          if (MODE != 2) pi[u] = pv[m.r0 + i];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + 32 * u;
+        if (i < nr) {
+          const MT val = AR::combine(MODE, ri[u], pi[u], vi[u], sc);
+          if (MODE != 0) pv[m.r0 + i] = val;
+          zs[i] = val;
+        }
+      }
+    }
+  }
   if (lane == 0) zs[nr] = AR::zero();
   __syncwarp();
-  if (!mbar_wait_bounded(&bar[2], err)) return;
+  if (!mbar_wait_bounded(&bar[2], err)) {
+    // the first pieces are in flight: wait for them (bounded), leave
+    mbar_wait_bounded(&bar[0], nullptr, 0u);
+    if (m.p1_bytes > 0) mbar_wait_bounded(&bar[1], nullptr, 0u);
+    return;
+  }
   const uint16_t *lvl = reinterpret_cast<const uint16_t *>(hdr);
   const int32_t *ints =
       reinterpret_cast<const int32_t *>(hdr + ((2 * (nlev + 2) + 3) & ~3));
   const int nF = ints[0], nB = ints[1], P = nF + nB;
   const int32_t *tab = ints + 2;
-  if (lane == 0)
-    for (int j = 0; j < 2 && j < P; ++j) {
-      mbar_expect_tx(&bar[j], (uint32_t)tab[3 * j + 2]);
-      bulk_load(buf0 + j * m.max_piece, g + tab[3 * j + 1],
-                (uint32_t)tab[3 * j + 2], &bar[j]);
-    }
   constexpr int vs = (int)sizeof(MT);
   uint32_t phases = 0u;  // bit b: parity to wait for on buffer b
   for (int j = 0; j < P; ++j) {
@@ -277,7 +364,65 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
     }
     phases ^= 1u << sb;
     const uint8_t *pc = buf0 + sb * m.max_piece;
-    if (j < nF) {
+    if constexpr (KLT > 0 && KUT > 0) {
+      // Software-pipelined walk: a level's columns, weights (and 1/u_ii)
+      // are read from the piece into registers while the level before it
+      // is swept, so each level waits only for its z operands.  Levels
+      // wider than a warp take the generic loop.
+      if (j < nF) {
+        const int l0 = tab[3 * j];
+        const int l1 = j + 1 < nF ? tab[3 * (j + 1)] : nlev;
+        int a = lvl[l0], w = lvl[l0 + 1] - a;
+        LevelRegs<MT, KLT> cur, nxt;
+        cur.template load<false>(pc, w, lane);
+        for (int l = l0; l < l1; ++l) {
+          const int ca = al16(2 * KLT * w);
+          const uint8_t *pn = pc + ca + al16(vs * KLT * w);
+          const int wn = l + 1 < l1 ? lvl[l + 2] - lvl[l + 1] : 0;
+          nxt.template load<false>(pn, wn, lane);
+          if (w <= 32) {
+            if (lane < w) zs[a + lane] = cur.template sweep<AR, false>(zs, zs[a + lane]);
+          } else {
+            AR::template level<KLT>(zs, a, w, KLT,
+                                     reinterpret_cast<const uint16_t *>(pc),
+                                     reinterpret_cast<const MT *>(pc + ca),
+                                     (const MT *)nullptr, lane);
+          }
+          a += w;
+          w = wn;
+          pc = pn;
+          cur = nxt;
+          __syncwarp();
+        }
+      } else {
+        const int lhi = tab[3 * j];
+        const int llo = j + 1 < P ? tab[3 * (j + 1)] + 1 : 0;
+        int b = lvl[lhi + 1], w = b - lvl[lhi];
+        LevelRegs<MT, KUT> cur, nxt;
+        cur.template load<true>(pc, w, lane);
+        for (int l = lhi; l >= llo; --l) {
+          const int a = b - w;
+          const int ca = al16(2 * KUT * w), va = al16(vs * KUT * w);
+          const uint8_t *pn = pc + ca + va + al16(vs * w);
+          const int wn = l - 1 >= llo ? a - lvl[l - 1] : 0;
+          nxt.template load<true>(pn, wn, lane);
+          if (w <= 32) {
+            if (lane < w) zs[a + lane] = cur.template sweep<AR, true>(zs, zs[a + lane]);
+          } else {
+            AR::template level<KUT>(zs, a, w, KUT,
+                                     reinterpret_cast<const uint16_t *>(pc),
+                                     reinterpret_cast<const MT *>(pc + ca),
+                                     reinterpret_cast<const MT *>(pc + ca + va),
+                                     lane);
+          }
+          b = a;
+          w = wn;
+          pc = pn;
+          cur = nxt;
+          __syncwarp();
+        }
+      }
+    } else if (j < nF) {
       const int l1 = j + 1 < nF ? tab[3 * (j + 1)] : nlev;
       int a = lvl[tab[3 * j]];
       for (int l = tab[3 * j]; l < l1; ++l) {

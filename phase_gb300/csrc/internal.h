@@ -219,9 +219,15 @@ struct Analysis {
 constexpr int64_t kStreamPiece = 6144;
 
 // sys_rows (optional): row offsets of independent systems stacked block-
-// diagonally (batched solves); every subdomain then lies in one system
+// diagonally (batched solves); every subdomain then lies in one system.
+// cx/cy (optional): a point per row (the cell centres of a finite-volume
+// equation); ranges are then cut by coordinate bisection across their
+// longer extent instead of by graph distance, which gives compact
+// subdomains with short level schedules (a 32 x 32 block of a structured
+// grid has 63 levels).
 int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
             int subdomain_rows, Analysis &a,
-            const std::vector<int64_t> *sys_rows = nullptr);
+            const std::vector<int64_t> *sys_rows = nullptr,
+            const double *cx = nullptr, const double *cy = nullptr);
 
 }  // namespace pg

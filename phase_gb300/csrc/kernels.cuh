@@ -128,6 +128,8 @@ constexpr uint16_t kPadCol = 0xFFFF;
 //   has column nr (the kernel keeps z[nr] = 0) and value 0
 struct StreamMeta {
   int32_t r0, nr, nlev, KL, KU, rec_off, hdr_bytes, max_piece;
+  // the first two pieces (offsets in the record), loaded at kernel start
+  int32_t p0_off, p0_bytes, p1_off, p1_bytes;
 };
 
 // Step form of the factor for the float-float sweep of the mixed solver,
@@ -325,21 +327,27 @@ void launch_diag_apply(int mode, const SolverDev &d, const MT *dinv,
 //   mode 0: z = M^-1 pv
 //   mode 1: p = r + beta (p - omega v), written back to pv
 //   mode 2: s = r - alpha v,            written to pv
+// pre_combine: the same arithmetic on operands already loaded (ri = r[i],
+// pi = pv[i], vi = v[i]; unused ones are ignored).
+template <class VT>
+__device__ __forceinline__ VT pre_combine(int mode, VT ri, VT pi, VT vi,
+                                          const KScalars *sc) {
+  // vector arithmetic in the storage precision; the scalars come from the
+  // FP64 recurrences
+  if (mode == 1) return ri + (VT)sc->beta * (pi - (VT)sc->omega * vi);
+  if (mode == 2) return ri - (VT)sc->alpha * vi;
+  return pi;
+}
+
 template <class VT>
 __device__ __forceinline__ VT pre_input(int mode, int i, const VT *r, VT *pv,
                                         const VT *v, const KScalars *sc) {
-  // vector arithmetic in the storage precision; the scalars come from the
-  // FP64 recurrences
-  if (mode == 1) {
-    const VT val = r[i] + (VT)sc->beta * (pv[i] - (VT)sc->omega * v[i]);
-    pv[i] = val;
-    return val;
-  } else if (mode == 2) {
-    const VT val = r[i] - (VT)sc->alpha * v[i];
-    pv[i] = val;
-    return val;
-  }
-  return pv[i];
+  const VT zero = VT(0);
+  const VT val = pre_combine<VT>(mode, mode ? r[i] : zero,
+                                 mode != 2 ? pv[i] : zero,
+                                 mode ? v[i] : zero, sc);
+  if (mode) pv[i] = val;
+  return val;
 }
 
 }  // namespace pg

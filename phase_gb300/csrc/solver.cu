@@ -696,8 +696,13 @@ extern "C" int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e) {
     s->analysed = false;
   }
   if (!s->analysed || s->eqn_pattern != e->pattern_id) {
+    // rows are cells: cut the Schwarz subdomains by the cell centres
+    const pg::HostMesh &hm = e->mesh->h;
+    const bool xy = e->p.n == hm.n_cells;
     int rc = analyse(e->p.n, e->p.row_ptr.data(), e->p.col_ind.data(),
-                     s->cfg.precond == PG_PREC_ILU0 ? s->cfg.subdomain_rows : -1, s->a);
+                     s->cfg.precond == PG_PREC_ILU0 ? s->cfg.subdomain_rows : -1, s->a,
+                     nullptr, xy ? hm.cx.data() : nullptr,
+                     xy ? hm.cy.data() : nullptr);
     if (rc) return rc;
     rc = upload_analysis(s);
     if (rc) return rc;
@@ -1068,11 +1073,12 @@ int autotune(pg_batch *b) {
 // Analysis of the stacked pattern (when it changed) and the per-batch
 // device state.
 int batch_analyse(pg_batch *b, const std::vector<int32_t> &rp,
-                  const std::vector<int32_t> &ci) {
+                  const std::vector<int32_t> &ci, const double *cx,
+                  const double *cy) {
   pg_solver *s = b->s;
   const int64_t n = (int64_t)rp.size() - 1;
   int rc = analyse(n, rp.data(), ci.data(), s->cfg.subdomain_rows, s->a,
-                   &b->sys_rows);
+                   &b->sys_rows, cx, cy);
   if (rc) return rc;
   s->rank = n;
   rc = upload_analysis(s);
@@ -1218,7 +1224,20 @@ extern "C" int pg_batch_set_eqns(pg_batch *b, int n_systems,
       for (int64_t k = 0; k < p.nnz; ++k)
         ci[ents[i] + k] = (int32_t)(p.col_ind[k] + rows[i]);
     }
-    int rc = batch_analyse(b, rp, ci);
+    // cell centres of every system (each system's subdomains are cut
+    // inside its own row range)
+    std::vector<double> cx(rows[n_systems]), cy(rows[n_systems]);
+    bool xy = true;
+    for (int i = 0; i < n_systems && xy; ++i) {
+      const pg::HostMesh &hm = eqns[i]->mesh->h;
+      xy = eqns[i]->p.n == hm.n_cells;
+      if (xy) {
+        std::copy(hm.cx.begin(), hm.cx.end(), cx.begin() + rows[i]);
+        std::copy(hm.cy.begin(), hm.cy.end(), cy.begin() + rows[i]);
+      }
+    }
+    int rc = batch_analyse(b, rp, ci, xy ? cx.data() : nullptr,
+                           xy ? cy.data() : nullptr);
     if (rc) return rc;
     b->eqn_ids = ids;
     PG_CUDA(b->st_vals.reserve(ents[n_systems]));

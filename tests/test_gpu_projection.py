@@ -37,9 +37,9 @@ def test_projection_makes_faces_divergence_free(pg, oracle):
     w = workloads.rising_bubble(nx, nx, seed=3, faces=faces, cells=cells)
     coeff = m.dt_over_rho(w["gamma"], w["rho1"], w["rho2"], w["dt"])
     eqn = pg.fv.laplacian(coeff, m, w["bc_type"], w["bc_value"], w["u"])
-    s = pg.SparseMatrixSolver(tolerance=1e-12, max_iters=20000)
+    s = pg.SparseMatrixSolver(tolerance=1e-10, max_iters=20000)
     s.set_eqn(eqn)
-    assert s.solve() <= 1e-12
+    assert s.solve() <= 1e-10 and s.stats.status == pg.PG_OK
     p = s.x()
     # setBoundaryFaces: fixed faces take their value, the others the cell's
     bnd = faces["rcell"] < 0
@@ -60,4 +60,6 @@ def test_projection_makes_faces_divergence_free(pg, oracle):
         return -om.laplacian(0.0, w["bc_type"], w["bc_value"], u)[3]
 
     d0, d1 = div(w["u"]), div(uf)
-    assert np.abs(d1).max() <= 1e-8 * np.abs(d0).max()
+    # ||div u*  - A p||_2 <= 1e-10 ||div u*||_2 bounds the largest cell
+    # residual by 1e-10 sqrt(n) max|div u*|
+    assert np.abs(d1).max() <= 1e-10 * nx * np.abs(d0).max()
