@@ -69,6 +69,9 @@ def parse():
                     help="mixed ILU(0) sweep form: 0 timed choice, 1 steps, "
                          "2 level blobs")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--coarse", type=int, choices=(0, 1), default=0,
+                    help="two-level Schwarz: add the subdomain-constant "
+                         "coarse correction")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--mode", default="sequence",
@@ -281,10 +284,12 @@ def run_sequence(args):
     if have_w:
         net.set_params(np.load(guess.DEFAULT_WEIGHTS))
     sp = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
-                               subdomain_rows=args.subdomain_rows)
+                               subdomain_rows=args.subdomain_rows,
+                               coarse=args.coarse)
     sm = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
                                precision=pg.MIXED,
-                               subdomain_rows=args.subdomain_rows)
+                               subdomain_rows=args.subdomain_rows,
+                               coarse=args.coarse)
     xp_p = torch.zeros(n, dtype=torch.float64, device=dev)
     xp_m = torch.zeros(n, dtype=torch.float64, device=dev)
     g = torch.empty(n, dtype=torch.float64, device=dev)
@@ -416,13 +421,15 @@ def run_sequence(args):
                                                          f"{steps[0]}..{steps[-1]}",
                        "n_cells": n, "nnz": nnz, "tolerance": 1e-8,
                        "preconditioner": "Schwarz ILU(0), "
-                       f"{sm.partition()[1]} subdomains",
+                       f"{sm.partition()[1]} subdomains"
+                       + (" + coarse correction" if args.coarse else ""),
                        "learned_weights": os.path.relpath(guess.DEFAULT_WEIGHTS, ROOT)
                        if have_w else None,
                        "l2": "256 MB flush write before every step; working "
                              "set > 129 MB L2"},
             "learned_mixed": {"ms": [round(x, 3) for x in ms_m],
                               "iters": [s_["iters"] for s_ in st_m],
+                              "fp64_iters": [s_["fp64_iters"] for s_ in st_m],
                               "guess_rel_residual": [round(s_["guess_rel"], 4)
                                                      for s_ in st_m],
                               "learned_guess_used": [s_["learned"] for s_ in st_m],
@@ -624,7 +631,8 @@ def run_single(args):
     solver = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
                                    precision=prec,
                                    subdomain_rows=args.subdomain_rows,
-                                   mixed_sweep=args.mixed_sweep)
+                                   mixed_sweep=args.mixed_sweep,
+                                   coarse=args.coarse)
     stream = torch.cuda.ExternalStream(pg.stream_handle(), device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
@@ -775,7 +783,8 @@ def run_single(args):
             "config": {"workload": workload_name(nx), "n_cells": n, "nnz": a_nnz,
                        "precision": args.precision,
                        "preconditioner": "Schwarz ILU(0), "
-                       f"{solver.partition()[1]} subdomains",
+                       f"{solver.partition()[1]} subdomains"
+                       + (" + coarse correction" if args.coarse else ""),
                        "tolerance": 1e-8, "guess": "zero",
                        "l2": "256 MB flush write before every step; working "
                              "set > 129 MB L2"},

@@ -53,10 +53,14 @@ extern "C" {
 
 /* arithmetic of the Krylov iteration */
 #define PG_FP64 0
-#define PG_MIXED 1 /* FP64 vectors, SpMV and dot products; ILU(0) factors
-                      stored and swept in FP32 (a preconditioner may be
-                      inexact: convergence is still judged on the FP64 true
-                      residual).  With Jacobi/none identical to PG_FP64. */
+#define PG_MIXED 1 /* float-float (pairs of FP32, about 48 bits) Krylov
+                      vectors, SpMV, ILU(0) sweeps and updates on the FP32
+                      pipes, scalars in FP64; the recursive residual is
+                      replaced by the FP64 true residual b - A x whenever it
+                      has fallen 1e4-fold and at convergence, which is judged
+                      on the FP64 true residual.  A solve whose true residual
+                      stalls is finished by the FP64 solver from its iterate
+                      (pg_solve_stats.fp64_iters). */
 
 typedef struct pg_mesh pg_mesh;
 typedef struct pg_eqn pg_eqn;
@@ -274,6 +278,10 @@ typedef struct {
   int mixed_sweep;    /* PG_MIXED ILU(0) sweep form: 0 = timed choice at the
                          first factorisation, 1 = warp-wide steps, 2 = level
                          blobs */
+  int coarse;         /* PG_PREC_ILU0: 0 = one-level Schwarz (as Ifpack2);
+                         1 = add the two-level coarse correction on the
+                         space of subdomain-constant vectors (at most 2048
+                         subdomains).  Not used by pg_batch_*. */
   double reserved_d;  /* ignored */
 } pg_solver_cfg;
 
@@ -282,6 +290,9 @@ typedef struct {
   int outer_iters;     /* reliable updates: true-residual replacements and
                           restarts */
   int status;          /* PG_OK, PG_MAX_ITERS, PG_BREAKDOWN, PG_NON_FINITE */
+  int fp64_iters;      /* PG_MIXED: iterations of the FP64 solver that took
+                          over from a stalled float-float solve (included in
+                          iters); 0 otherwise */
   double rel_residual; /* true ||b - A x||_2 / ||b||_2 computed in FP64 */
   double ms;           /* device time of the solve (CUDA events) */
   double setup_ms;     /* device time of the value permutation + ILU factor */
@@ -365,6 +376,14 @@ uint64_t pg_kernel_launches(void);
 /* Subdomain id of every row of the last analysed pattern (host, part[n]);
  * returns the number of subdomains in *n_parts. */
 int pg_solver_partition(const pg_solver *s, int32_t *part, int *n_parts);
+
+/* The two-level preconditioner's coarse inverse (cfg.coarse = 1) after the
+ * last factorisation: the K x K row-major FP32 approximation of
+ * (Z^T A Z)^-1 that the solver applies, K = *n_parts of pg_solver_partition
+ * and Z the subdomain indicator vectors (host, out[K*K]).  Returns
+ * PG_INVALID_ARG when no coarse space is active.  (Inspection; no reference
+ * counterpart.) */
+int pg_solver_coarse_inverse(pg_solver *s, float *out, int *k);
 
 /* z = M^-1 r for the solver's preconditioner on its current matrix (the
  * ILU(0) factors are recomputed from the current values; FP32 factors and

@@ -44,12 +44,14 @@ class SolverCfg(ctypes.Structure):
     _fields_ = [("tolerance", ctypes.c_double), ("max_iters", ctypes.c_int),
                 ("precond", ctypes.c_int), ("subdomain_rows", ctypes.c_int),
                 ("precision", ctypes.c_int), ("mixed_sweep", ctypes.c_int),
+                ("coarse", ctypes.c_int),
                 ("reserved_d", ctypes.c_double)]
 
 
 class SolveStats(ctypes.Structure):
     _fields_ = [("iters", ctypes.c_int), ("outer_iters", ctypes.c_int),
-                ("status", ctypes.c_int), ("rel_residual", ctypes.c_double),
+                ("status", ctypes.c_int), ("fp64_iters", ctypes.c_int),
+                ("rel_residual", ctypes.c_double),
                 ("ms", ctypes.c_double), ("setup_ms", ctypes.c_double)]
 
     def as_dict(self):
@@ -97,6 +99,7 @@ PROTOTYPES = {
     "pg_solver_solve": (_I, [_P, ctypes.POINTER(SolveStats)]),
     "pg_solver_get_x": (_I, [_P, _P, _I]),
     "pg_solver_partition": (_I, [_P, _P, ctypes.POINTER(_I)]),
+    "pg_solver_coarse_inverse": (_I, [_P, _P, ctypes.POINTER(_I)]),
     "pg_solver_profile": (_I, [_P, _I, _P]),
     "pg_solver_apply_precond": (_I, [_P, _P, _P, _I]),
     "pg_batch_create": (_I, [_P, ctypes.POINTER(_P)]),
@@ -471,6 +474,14 @@ class SparseMatrixSolver:
         k = ctypes.c_int()
         _check(lib().pg_solver_partition(self._h, _ptr(part), ctypes.byref(k)))
         return part, k.value
+
+    def coarse_inverse(self):
+        """The FP32 coarse inverse (K x K) of the two-level preconditioner."""
+        k = ctypes.c_int()
+        _check(lib().pg_solver_coarse_inverse(self._h, None, ctypes.byref(k)))
+        out = np.empty((k.value, k.value), np.float32)
+        _check(lib().pg_solver_coarse_inverse(self._h, _ptr(out), ctypes.byref(k)))
+        return out
 
     def apply_precond(self, r):
         """z = M^-1 r with the solver's preconditioner (float-float sweeps

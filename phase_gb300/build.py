@@ -18,7 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libphase_gb300.so")
-SOURCES = ["host.cpp", "capi.cu", "solver.cu", "kernels.cu", "ilu.cu", "dd.cu", "batch.cu",
+SOURCES = ["host.cpp", "capi.cu", "solver.cu", "kernels.cu", "ilu.cu", "dd.cu", "batch.cu", "coarse.cu",
            "mpnn.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -118,6 +118,7 @@ void Gb300SparseMatrixSolver::setup(const boost::property_tree::ptree &p) {
   cfg_.precision =
       p.get<std::string>("precision", "fp64") == "mixed" ? PG_MIXED : PG_FP64;
   cfg_.mixed_sweep = p.get<int>("mixedSweep", 0);
+  cfg_.coarse = p.get<int>("coarseSpace", 0);
   recreate();
 }
 

@@ -525,6 +525,33 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   }
   for (auto &d : a.dup_dst) d = cmap[d];
 
+  // 5b. coarse-space structure (subdomain couplings of the permuted CSR)
+  {
+    std::vector<int32_t> sub_of(n);
+    for (int s = 0; s < a.n_sub; ++s)
+      for (int32_t i = a.sub_ptr[s]; i < a.sub_ptr[s + 1]; ++i) sub_of[i] = s;
+    a.cptr.assign(a.n_sub + 1, 0);
+    a.cnb.clear();
+    a.cslot.assign(a.nnz, 0);
+    a.max_cnb = 0;
+    std::vector<int32_t> nb;
+    for (int s = 0; s < a.n_sub; ++s) {
+      nb.clear();
+      const int32_t e0 = a.prp[a.sub_ptr[s]], e1 = a.prp[a.sub_ptr[s + 1]];
+      for (int32_t k = e0; k < e1; ++k) nb.push_back(sub_of[a.pci[k]]);
+      std::sort(nb.begin(), nb.end());
+      nb.erase(std::unique(nb.begin(), nb.end()), nb.end());
+      a.max_cnb = std::max(a.max_cnb, (int)nb.size());
+      if ((int)nb.size() <= kMaxCoarseNb)
+        for (int32_t k = e0; k < e1; ++k)
+          a.cslot[k] = (uint8_t)(std::lower_bound(nb.begin(), nb.end(),
+                                                  sub_of[a.pci[k]]) -
+                                 nb.begin());
+      a.cnb.insert(a.cnb.end(), nb.begin(), nb.end());
+      a.cptr[s + 1] = (int32_t)a.cnb.size();
+    }
+  }
+
   // 6. ILU(0) storage: the entries of each row inside its subdomain,
   //    L (columns before the row), diagonal, U (columns after)
   a.lrp.assign(n + 1, 0);

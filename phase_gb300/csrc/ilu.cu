@@ -227,6 +227,15 @@ struct ArithF64 {
     return pre_combine<double>(mode, ri, pi, vi, sc);
   }
   __device__ static V zero() { return 0.; }
+  // subdomain sums for the coarse correction
+  using Sum = double;
+  __device__ static Sum sum_init() { return 0.; }
+  __device__ static void sum_add(Sum &a, V x) { a += x; }
+  __device__ static double sum_warp(Sum a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    return a;
+  }
   template <int KT, bool DIAG>
   __device__ static V row(V self, const V (&v)[KT], const V (&x)[KT], V d) {
     V acc = self;
@@ -251,6 +260,19 @@ struct ArithDD {
     return dd_pre_combine(mode, ri, pi, vi, sc);
   }
   __device__ static V zero() { return make_float2(0.f, 0.f); }
+  using Sum = DdAcc;
+  __device__ static Sum sum_init() { return dd_acc(make_float2(0.f, 0.f)); }
+  __device__ static void sum_add(Sum &a, V x) { dd_acc_add(a, x); }
+  __device__ static double sum_warp(Sum a) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      DdAcc b;
+      b.s = __shfl_xor_sync(0xffffffffu, a.s, o);
+      b.c = __shfl_xor_sync(0xffffffffu, a.c, o);
+      dd_acc_merge(a, b);
+    }
+    return dd_acc_to_double(a);
+  }
   template <int KT, bool DIAG>
   __device__ static V row(V self, const V (&v)[KT], const V (&x)[KT], V d) {
     DdAcc acc = dd_acc(self);
@@ -281,7 +303,7 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
                     typename AR::V *__restrict__ z,
                     const KScalars *__restrict__ sc_base,
                     const int32_t *__restrict__ sub_sys,
-                    int *__restrict__ err) {
+                    int *__restrict__ err, double *__restrict__ csum) {
   using MT = typename AR::V;
   // batched solves: the scalars of this subdomain's system
   const KScalars *sc =
@@ -314,9 +336,11 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
     }
   }
   {
-    // input staging, four rows per lane in flight
+    // input staging, four rows per lane in flight; with a coarse space the
+    // subdomain's input sum (lane order, then a fixed butterfly)
     constexpr int U = 4;
     const MT zero = AR::zero();
+    typename AR::Sum part = AR::sum_init();
     for (int i0 = lane; i0 < nr; i0 += 32 * U) {
       MT ri[U], pi[U], vi[U];
 #pragma unroll
@@ -335,8 +359,13 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
           const MT val = AR::combine(MODE, ri[u], pi[u], vi[u], sc);
           if (MODE != 0) pv[m.r0 + i] = val;
           zs[i] = val;
+          if (csum) AR::sum_add(part, val);
         }
       }
+    }
+    if (csum) {
+      const double t = AR::sum_warp(part);
+      if (lane == 0) csum[blockIdx.x] = t;
     }
   }
   if (lane == 0) zs[nr] = AR::zero();
@@ -646,7 +675,7 @@ void launch_stream(const SolverDev &d, size_t smem, const uint8_t *rec,
     attr = smem;
   }
   k_ilu0_apply_stream<AR, MODE, KLT, KUT><<<d.n_sub, 32, smem, st>>>(
-      d.smeta64, rec, r, pv, v, z, sc, d.sub_sys, d.err);
+      d.smeta64, rec, r, pv, v, z, sc, d.sub_sys, d.err, d.csum);
 }
 
 template <class VT, class MT, int MODE>

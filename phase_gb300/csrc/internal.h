@@ -213,7 +213,18 @@ struct Analysis {
   std::vector<uint8_t> srec_dd;
   std::vector<int32_t> pack_src_dd, pack_dst_dd;  // step values <- factor
   size_t ssmem_dd = 0;
+  // coarse space of the two-level Schwarz preconditioner (one indicator
+  // vector per subdomain): the coarse matrix row of subdomain s has the
+  // columns cnb[cptr[s] .. cptr[s+1]) (the subdomains its rows couple to,
+  // ascending), and cslot[k] is the position of permuted entry k's column
+  // subdomain in its row's list
+  std::vector<int32_t> cptr, cnb;
+  std::vector<uint8_t> cslot;
+  int max_cnb = 0;
 };
+
+// most subdomains one coarse matrix row may couple to
+constexpr int kMaxCoarseNb = 32;
 
 // target bytes of one streamed piece of a subdomain's factor
 constexpr int64_t kStreamPiece = 6144;

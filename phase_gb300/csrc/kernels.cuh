@@ -178,9 +178,38 @@ struct SolverDev {
   // batched solves: system of every subdomain (NULL for one system); the
   // apply kernels then read the scalars sc[sub_sys[subdomain]]
   const int32_t *sub_sys;
+  // two-level Schwarz: the streamed sweeps write the sum of each
+  // subdomain's input here (NULL: no coarse correction)
+  double *csum;
 };
 
 
+
+// Coarse space of the two-level Schwarz preconditioner (coarse.cu): the
+// subdomain row ranges, the coupling structure of A_c = Z^T A Z, the dense
+// K x K FP32 matrix (inverted in place by launch_coarse_setup), Gauss-Jordan
+// pivot buffers and the FP64 subdomain sums of an application's input.
+struct CoarseDev {
+  int K = 0, max_cnb = 0;
+  const int32_t *sub_ptr = nullptr, *cptr = nullptr, *cnb = nullptr;
+  const uint8_t *cslot = nullptr;
+  float *ac = nullptr, *rowb = nullptr, *colb = nullptr, *dg0 = nullptr;
+  double *csum = nullptr;
+};
+
+// A_c from the permuted values, then A_c^-1 in place (the K elimination
+// steps are captured into *gj_graph on first use when gj_graph is given)
+void launch_coarse_setup(const CoarseDev &c, const double *pvals,
+                         const int32_t *prp, cudaGraphExec_t *gj_graph,
+                         cudaStream_t st);
+// z += Z A_c^-1 Z^T in  (in and z in the permuted order); have_sums: the
+// sweep already wrote Z^T in to c.csum (the streamed ILU(0) kernels do)
+// (sc: the solve's scalars; the kernels do nothing once it has converged)
+void launch_coarse_apply(const CoarseDev &c, const double *in, double *z,
+                         bool have_sums, const KScalars *sc, cudaStream_t st);
+void launch_coarse_apply_dd(const CoarseDev &c, const float2 *in, float2 *z,
+                            bool have_sums, const KScalars *sc,
+                            cudaStream_t st);
 
 void launch_permute_values(int nnz, const int32_t *psrc, const double *src,
                            double *dst, int n_dup, const int32_t *dup_dst,

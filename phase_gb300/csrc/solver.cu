@@ -88,6 +88,16 @@ struct pg_solver {
   // arguments are fixed device pointers, so a graph stays valid until the
   // buffers are reallocated by a new analysis
   cudaGraphExec_t chunk_graph[2] = {nullptr, nullptr};
+  int chunk_launches[2] = {0, 0};  // kernels in one replay of each graph
+  // two-level Schwarz coarse space (cfg.coarse): structure, the dense
+  // coarse matrix / its inverse, elimination buffers, subdomain sums and the
+  // graph of the K elimination steps
+  bool coarse_on = false;
+  DevBuf<int32_t> c_sub_ptr, c_cptr, c_cnb;
+  DevBuf<uint8_t> c_slot;
+  DevBuf<float> c_ac, c_rowb, c_colb, c_dg0;
+  DevBuf<double> c_sum;
+  cudaGraphExec_t gj_graph = nullptr;
 
   void drop_graphs() {
     for (auto &g : chunk_graph)
@@ -95,6 +105,27 @@ struct pg_solver {
         cudaGraphExecDestroy(g);
         g = nullptr;
       }
+    if (gj_graph) {
+      cudaGraphExecDestroy(gj_graph);
+      gj_graph = nullptr;
+    }
+  }
+
+  CoarseDev coarse() const {
+    CoarseDev c;
+    if (!coarse_on) return c;
+    c.K = a.n_sub;
+    c.max_cnb = a.max_cnb;
+    c.sub_ptr = c_sub_ptr.p;
+    c.cptr = c_cptr.p;
+    c.cnb = c_cnb.p;
+    c.cslot = c_slot.p;
+    c.ac = c_ac.p;
+    c.rowb = c_rowb.p;
+    c.colb = c_colb.p;
+    c.dg0 = c_dg0.p;
+    c.csum = c_sum.p;
+    return c;
   }
 
   ~pg_solver() {
@@ -137,6 +168,7 @@ struct pg_solver {
     d.max_ku = a.max_ku;
     d.err = err.p;
     d.sub_sys = nullptr;
+    d.csum = coarse_on ? c_sum.p : nullptr;
     return d;
   }
   RedWork red() const { return RedWork{partials.p, ticket.p, red_grid}; }
@@ -156,6 +188,8 @@ int red_grid_cap() {
   }();
   return cap;
 }
+
+constexpr int kMaxCoarseK = 2048;  // the coarse matrix is K x K, dense
 
 int upload_analysis(pg_solver *s) {
   const Analysis &a = s->a;
@@ -197,6 +231,26 @@ int upload_analysis(pg_solver *s) {
     if (e == cudaSuccess) e = s->pvals_dd.reserve(nnz);
   }
   s->drop_graphs();
+  s->coarse_on = false;
+  if (s->cfg.coarse && s->cfg.precond == PG_PREC_ILU0 && a.n_sub > 1) {
+    PG_CHECK_ARG(a.n_sub <= kMaxCoarseK,
+                 "coarse correction: more than 2048 subdomains (raise "
+                 "subdomain_rows)");
+    PG_CHECK_ARG(a.max_cnb <= kMaxCoarseNb,
+                 "coarse correction: a subdomain couples to more than 32 "
+                 "others");
+    const size_t K = a.n_sub;
+    up(s->c_sub_ptr, a.sub_ptr);
+    up(s->c_cptr, a.cptr);
+    up(s->c_cnb, a.cnb);
+    up(s->c_slot, a.cslot);
+    if (e == cudaSuccess) e = s->c_ac.reserve(K * K);
+    for (DevBuf<float> *bf : {&s->c_rowb, &s->c_colb})
+      if (e == cudaSuccess) e = bf->reserve(2 * K);
+    if (e == cudaSuccess) e = s->c_dg0.reserve(K);
+    if (e == cudaSuccess) e = s->c_sum.reserve(K);
+    s->coarse_on = true;
+  }
   s->red_grid = (int)std::min<int64_t>(red_grid_cap(), (n + kVecBlock - 1) / kVecBlock);
   if (s->red_grid < 1) s->red_grid = 1;
   if (e == cudaSuccess) e = s->partials.reserve((size_t)kMaxDots * s->red_grid);
@@ -225,6 +279,11 @@ int ensure_host_state(pg_solver *s) {
 constexpr int kChunk = 8;
 constexpr double kDelta2 = 1e-4;  // reliable update when rr < kDelta2 * rr_ref
 constexpr int kMaxRestarts = 50;
+// float-float solver: hand over to FP64 when the true residual norm has not
+// fallen 10x in kDdStallIters iterations or after kDdMaxRestarts breakdowns
+constexpr int kDdStallIters = 1200;
+constexpr int kDdMaxRestarts = 4;
+constexpr int kDdStalled = -1000;  // internal status of run_bicgstab_dd
 
 // PG_SOLVER_TRACE=1 prints the Krylov scalars at every chunk boundary
 bool trace_enabled() {
@@ -237,15 +296,18 @@ bool trace_enabled() {
 
 // Replays the captured chunk graph (capturing it on the second call).
 template <class F>
-int run_chunk(cudaGraphExec_t &gexec, bool &direct_done, F &&chunk) {
+int run_chunk(cudaGraphExec_t &gexec, int &n_launch, bool &direct_done,
+              F &&chunk) {
   cudaStream_t st = stream();
   if (gexec) {
     PG_CUDA(cudaGraphLaunch(gexec, st));
-    count_launches(5 * kChunk);
+    count_launches(n_launch);
   } else if (direct_done) {
     cudaGraph_t graph = nullptr;
     PG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    const uint64_t before = launch_count();
     chunk();  // launches are counted here, executed once below
+    n_launch = (int)(launch_count() - before);
     PG_CUDA(cudaStreamEndCapture(st, &graph));
     cudaError_t ge = cudaGraphInstantiate(&gexec, graph, 0);
     cudaGraphDestroy(graph);
@@ -281,9 +343,14 @@ int run_bicgstab(pg_solver *s, double tol, int max_iters, int *iters,
   double *const x = s->x.p, *const r = s->r.p, *const rh = s->rh.p;
   double *const p = s->p.p, *const v = s->v.p, *const ph = s->ph.p;
   double *const ss = s->s.p, *const sh = s->sh.p, *const t = s->t.p;
+  const CoarseDev cdev = s->coarse();
+  const bool ilu_stream = s->cfg.precond == PG_PREC_ILU0 && d.smem64 > 0;
   auto precond = [&](int mode, double *pv, double *z) {
     launch_precond<double, double>(s->cfg.precond, mode, d, jd, r, pv, v, z,
                                    s->sc.p, st);
+    // the input (p or s) is in pv after the fused update; the streamed
+    // ILU(0) sweep has summed it per subdomain already
+    if (cdev.K) launch_coarse_apply(cdev, pv, z, ilu_stream, s->sc.p, st);
   };
   auto chunk = [&]() {
     for (int c = 0; c < kChunk; ++c) {
@@ -334,7 +401,7 @@ int run_bicgstab(pg_solver *s, double tol, int max_iters, int *iters,
   cudaGraphExec_t &gexec = s->chunk_graph[0];
   bool direct_done = false;
   for (;;) {
-    if ((rc = run_chunk(gexec, direct_done, chunk))) return rc;
+    if ((rc = run_chunk(gexec, s->chunk_launches[0], direct_done, chunk))) return rc;
     if ((rc = read_scalars())) return rc;
     const KScalars k = *s->sc_host;
     *iters = k.iter;
@@ -386,11 +453,13 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
   float2 *const x = s->xd.p, *const r = s->rd.p, *const rh = s->rhd.p;
   float2 *const p = s->pd.p, *const v = s->vd.p, *const ph = s->phd.p;
   float2 *const ss = s->sd.p, *const sh = s->shd.p, *const t = s->td.p;
+  const CoarseDev cdev = s->coarse();
   auto precond = [&](int mode, float2 *pv, float2 *z) {
     if (ilu)
       launch_ilu0_apply_dd(mode, d, r, pv, v, z, s->sc.p, st);
     else
       launch_dd_diag_apply(mode, n, jd, r, pv, v, z, s->sc.p, st);
+    if (cdev.K) launch_coarse_apply_dd(cdev, pv, z, ilu && d.dd_stream, s->sc.p, st);
   };
   auto chunk = [&]() {
     for (int c = 0; c < kChunk; ++c) {
@@ -439,10 +508,14 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
   if (s->sc_host->status == PG_NON_FINITE) return PG_NON_FINITE;
   if (s->sc_host->rr_true <= init.tol2 * bb) return PG_OK;
   double rr_ref = s->sc_host->rr_true;
+  // progress watch: the true residual norm must fall 10x within
+  // kDdStallIters iterations (checked at least that often)
+  double prog_rr = rr_ref;
+  int prog_it = 0, last_update = 0;
   int restarts = 0;
   bool direct_done = false;
   for (;;) {
-    if ((rc = run_chunk(s->chunk_graph[1], direct_done, chunk))) return rc;
+    if ((rc = run_chunk(s->chunk_graph[1], s->chunk_launches[1], direct_done, chunk))) return rc;
     if ((rc = read_scalars())) return rc;
     const KScalars k = *s->sc_host;
     *iters = k.iter;
@@ -453,7 +526,10 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
                    k.iter, k.rr / init.bb, k.rho, k.alpha, k.omega, k.status,
                    k.done);
     if (k.status == PG_NON_FINITE) return PG_NON_FINITE;
-    if (!k.done && !(k.rr < kDelta2 * rr_ref * scale * scale)) continue;
+    if (!k.done && !(k.rr < kDelta2 * rr_ref * scale * scale) &&
+        k.iter - last_update < kDdStallIters)
+      continue;
+    last_update = k.iter;
     // reliable update: x += x_w, r = b - A x in FP64
     launch_dd_fold(n, s->x.p, x, 1.0 / scale, st);
     launch_true_residual(d, s->pvals.p, s->b.p, s->x.p, s->r.p, s->sc.p, w, st);
@@ -467,7 +543,15 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
     if (rr_true <= init.tol2 * bb) return PG_OK;
     if (k.iter >= max_iters) return PG_MAX_ITERS;
     const bool restart = k.status == PG_BREAKDOWN;
-    if (restart && ++restarts > kMaxRestarts) return PG_BREAKDOWN;
+    if (rr_true < 1e-2 * prog_rr) {
+      prog_rr = rr_true;
+      prog_it = k.iter;
+    }
+    // stalled or breaking down in float-float: the FP64 solver carries on
+    // from the FP64 iterate
+    if (k.iter - prog_it >= kDdStallIters ||
+        (restart && ++restarts > kDdMaxRestarts))
+      return kDdStalled;
     launch_dd_set_r(n, s->r.p, scale, r, rh, p, v, restart, s->sc.p, w, st);
     rr_ref = rr_true;
   }
@@ -540,6 +624,8 @@ int factor(pg_solver *s) {
   if (s->cfg.precond == PG_PREC_ILU0) {
     PG_CUDA(cudaMemsetAsync(s->bad.p, 0, sizeof(int), st));
     launch_ilu0_factor(d, s->pvals.p, s->bad.p, dd, st);
+    if (s->coarse_on)
+      launch_coarse_setup(s->coarse(), s->pvals.p, s->prp.p, &s->gj_graph, st);
   } else if (s->cfg.precond == PG_PREC_JACOBI) {
     launch_jacobi_diag(d, s->pvals.p, s->jdinv.p, st);
     if (dd) launch_dd_split(d.n, s->jdinv.p, 1.0, s->jdinv_dd.p, st);
@@ -562,6 +648,7 @@ extern "C" void pg_solver_default_cfg(pg_solver_cfg *cfg) {
   cfg->subdomain_rows = 0;
   cfg->precision = PG_FP64;
   cfg->mixed_sweep = 0;
+  cfg->coarse = 0;
   cfg->reserved_d = 0.;
 }
 
@@ -578,6 +665,7 @@ extern "C" int pg_solver_create(const pg_solver_cfg *cfg, pg_solver **out) {
                "pg_solver_create: bad precision");
   PG_CHECK_ARG(c.mixed_sweep >= 0 && c.mixed_sweep <= 2,
                "pg_solver_create: bad mixed_sweep");
+  PG_CHECK_ARG(c.coarse == 0 || c.coarse == 1, "pg_solver_create: bad coarse");
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0 || !stream()) {
     set_error("no CUDA device available: libphase_gb300 has no CPU path");
@@ -771,8 +859,21 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
   const SolverDev d = s->dev();
   const RedWork w = s->red();
   double bb = 0.;
+  int fp64_iters = 0;  // FP64 iterations after a float-float hand-over
   int status = use_dd(s) ? run_bicgstab_dd(s, tol, s->cfg.max_iters, &iters, &outer, &bb)
                          : run_bicgstab(s, tol, s->cfg.max_iters, &iters, &outer, &bb);
+  if (status == kDdStalled) {
+    // FP64 BiCGStab from the float-float solver's (folded FP64) iterate
+    int it2 = 0, up2 = 0;
+    if (trace_enabled())
+      std::fprintf(stderr, "pg_solver(dd): stalled at it %d, FP64 continues\n",
+                   iters);
+    status = run_bicgstab(s, tol, std::max(s->cfg.max_iters - iters, 1), &it2,
+                          &up2, &bb);
+    iters += it2;
+    outer += up2;
+    fp64_iters = it2;
+  }
   if (status == PG_CUDA_ERROR) return status;
   // final true residual in FP64 and the solution in the caller's order
   launch_true_residual(d, s->pvals.p, s->b.p, s->x.p, nullptr, s->sc.p, w, st);
@@ -802,6 +903,7 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
     stats->iters = iters;
     stats->outer_iters = outer;
     stats->status = status;
+    stats->fp64_iters = fp64_iters;
     stats->rel_residual = rel;
     stats->ms = ms_all;
     stats->setup_ms = ms_fact;
@@ -888,10 +990,10 @@ extern "C" int pg_solver_apply_precond(pg_solver *s, const double *r,
   PG_CHECK_ARG(s->analysed && s->have_vals,
                "pg_solver_apply_precond: set the matrix first");
   cudaStream_t st = stream();
-  const SolverDev d = s->dev();
   const int64_t n = s->a.n;
   int rc = factor(s);
   if (rc) return rc;
+  const SolverDev d = s->dev();  // after factor(): the sweep form is chosen
   const double *dr = r;
   if (ptr_kind != PG_DEVICE) {
     PG_CUDA(s->st_vec.upload(r, n));
@@ -906,10 +1008,18 @@ extern "C" int pg_solver_apply_precond(pg_solver *s, const double *r,
     else
       launch_dd_diag_apply(0, (int)n, s->cfg.precond == PG_PREC_JACOBI ? s->jdinv_dd.p : nullptr,
                            nullptr, s->pd.p, nullptr, s->phd.p, nullptr, st);
+    if (s->coarse_on)
+      launch_coarse_apply_dd(s->coarse(), s->pd.p, s->phd.p,
+                             s->cfg.precond == PG_PREC_ILU0 && d.dd_stream,
+                             nullptr, st);
     launch_dd_join((int)n, s->phd.p, 1.0, s->ph.p, st);
   } else {
     launch_precond<double, double>(s->cfg.precond, 0, d, s->jdinv.p, nullptr,
                                    s->p.p, nullptr, s->ph.p, nullptr, st);
+    if (s->coarse_on)
+      launch_coarse_apply(s->coarse(), s->p.p, s->ph.p,
+                          s->cfg.precond == PG_PREC_ILU0 && d.smem64 > 0,
+                          nullptr, st);
   }
   launch_unpermute_vec((int)n, s->perm.p, s->ph.p, s->t.p, st);
   PG_CUDA(cudaGetLastError());
@@ -930,6 +1040,20 @@ extern "C" int pg_solver_partition(const pg_solver *s, int32_t *part,
   PG_CHECK_ARG(s && s->analysed, "pg_solver_partition: nothing analysed");
   if (part) std::copy(s->a.part.begin(), s->a.part.end(), part);
   if (n_parts) *n_parts = s->a.n_sub;
+  return PG_OK;
+}
+
+extern "C" int pg_solver_coarse_inverse(pg_solver *s, float *out, int *k) {
+  PG_CHECK_ARG(s && s->analysed && s->coarse_on,
+               "pg_solver_coarse_inverse: no coarse space");
+  const size_t K = s->a.n_sub;
+  if (k) *k = (int)K;
+  if (out) {
+    cudaStream_t st = stream();
+    PG_CUDA(cudaMemcpyAsync(out, s->c_ac.p, K * K * sizeof(float),
+                            cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+  }
   return PG_OK;
 }
 
@@ -1179,6 +1303,7 @@ extern "C" int pg_batch_create(const pg_solver_cfg *cfg, pg_batch **out) {
                "preconditioner");
   PG_CHECK_ARG(c.precision == PG_FP64,
                "pg_batch_create: batched solves run in FP64");
+  c.coarse = 0;  // the batched drivers apply the one-level preconditioner
   auto *b = new (std::nothrow) pg_batch();
   PG_CHECK_ARG(b, "pg_batch_create: out of host memory");
   int rc = pg_solver_create(&c, &b->s);
@@ -1346,6 +1471,7 @@ extern "C" int pg_batch_solve(pg_batch *b, pg_solve_stats *stats,
       stats[i].iters = k.iter;
       stats[i].outer_iters = k.restarts + 1;
       stats[i].status = status;
+      stats[i].fp64_iters = 0;
       stats[i].rel_residual = rel;
       stats[i].ms = ms;
       stats[i].setup_ms = 0.;
