@@ -8,9 +8,13 @@ elsewhere, rhs = src::div(u*) of a seeded divergent velocity; the bubble
 rises one step at a time).  Two solvers run the same steps, each warm from
 its own previous solution as a time loop runs them:
 
-  plain FP64      FP64 BiCGStab + Schwarz ILU(0), guess = previous step's x
-  learned+mixed   float-float BiCGStab + ILU(0) (FP64-class accuracy on the
-                  FP32 pipes, FP64 true residual at every reliable update),
+  plain FP64      FP64 BiCGStab + two-level Schwarz ILU(0) (subdomain ILU(0)
+                  blocks plus a coarse correction on the subdomain-constant
+                  vectors; --coarse 0 for the one-level preconditioner),
+                  guess = previous step's x
+  learned+mixed   float-float BiCGStab + the same preconditioner (about
+                  48-bit arithmetic on the FP32 pipes, FP64 true residual at
+                  every reliable update, FP64 hand-over if it stalls),
                   guess = the message-passing network's prediction from
                   (A, b, previous x), replaced by the zero guess when the
                   prediction's residual is not below ||b||
@@ -69,7 +73,7 @@ def parse():
                     help="mixed ILU(0) sweep form: 0 timed choice, 1 steps, "
                          "2 level blobs")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
-    ap.add_argument("--coarse", type=int, choices=(0, 1), default=0,
+    ap.add_argument("--coarse", type=int, choices=(0, 1), default=1,
                     help="two-level Schwarz: add the subdomain-constant "
                          "coarse correction")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -241,8 +245,14 @@ def kernel_roofline(pg, solver, n, nnz, dd):
              "update": prof["update" + sfx]}
     shares = {"spmv": 2 * ms_of["spmv"], "ilu_apply": 2 * ms_of["ilu_apply"],
               "update": ms_of["update"]}
-    dom = max(shares, key=shares.get)
     bytes_of = {"spmv": b_spmv, "ilu_apply": b_prec, "update": b_upd}
+    if prof["coarse"] > 0:
+        # coarse correction: FP32 K x K inverse, K float-pair sums, z in/out
+        K = solver.partition()[1]
+        ms_of["coarse"] = prof["coarse"]
+        shares["coarse"] = 2 * prof["coarse"]
+        bytes_of["coarse"] = 4 * K * K + 8 * K + 2 * 8 * n
+    dom = max(shares, key=shares.get)
     peak, peak_kind = measured_peaks()
     achieved = bytes_of[dom] / (ms_of[dom] * 1e-3) / 1e9
     return {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
@@ -370,7 +380,9 @@ def run_sequence(args):
         ms, plain_ms = float(tt[0]), float(tt[1])
     # zero-guess FP64 solve of the first timed step (the reference arm's
     # configuration)
-    sz = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000)
+    sz = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
+                               subdomain_rows=args.subdomain_rows,
+                               coarse=args.coarse)
     eqn = seq.assemble(t0)
     sz.set_eqn(eqn)
     sz.setGuess(None)
@@ -389,7 +401,8 @@ def run_sequence(args):
 
     e2e = None
     if not args.no_e2e:
-        e2e = e2e_learned(pg, guess, seq, net, have_w, steps[:3], torch, dev)
+        e2e = e2e_learned(pg, guess, seq, net, have_w, steps[:3], torch, dev,
+                          args.coarse)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -455,14 +468,17 @@ def run_sequence(args):
         torch.distributed.destroy_process_group()
 
 
-def e2e_learned(pg, guess, seq, net, have_w, steps, torch, dev):
+def e2e_learned(pg, guess, seq, net, have_w, steps, torch, dev, coarse):
     """The learned+mixed solve through the C ABI with host buffers: the
     caller holds the step's CrsEquation (5-slot layout), its rhs and the
     previous solution on the host; they are uploaded, the network predicts
     from host inputs, the solver runs from its guess, and x comes back."""
     import numpy as np
     s2 = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
-                               precision=pg.MIXED)
+                               precision=pg.MIXED, coarse=coarse)
+    # the caller's geometry hint: cell centroids cut the Schwarz subdomains
+    s2.setRank(seq.n)
+    s2.set_row_coords(np.stack([seq.cells["cx"], seq.cells["cy"]], axis=1))
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
     x_prev = pin(np.zeros(seq.n))
     times, sts, h2d, d2h = [], [], 0, 0
@@ -691,8 +707,14 @@ def run_single(args):
              "update": prof["update" + sfx]}
     shares = {"spmv": 2 * ms_of["spmv"], "ilu_apply": 2 * ms_of["ilu_apply"],
               "update": ms_of["update"]}
-    dom = max(shares, key=shares.get)
     bytes_of = {"spmv": b_spmv, "ilu_apply": b_prec, "update": b_upd}
+    if prof["coarse"] > 0:
+        # coarse correction: FP32 K x K inverse, K float-pair sums, z in/out
+        K = solver.partition()[1]
+        ms_of["coarse"] = prof["coarse"]
+        shares["coarse"] = 2 * prof["coarse"]
+        bytes_of["coarse"] = 4 * K * K + 8 * K + 2 * 8 * n
+    dom = max(shares, key=shares.get)
     peak, peak_kind = measured_peaks()
     achieved = bytes_of[dom] / (ms_of[dom] * 1e-3) / 1e9
     traffic = None
@@ -722,7 +744,11 @@ def run_single(args):
         xh = torch.empty(n, dtype=torch.float64).pin_memory().numpy()
         s2 = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
                                    precision=prec,
-                                   subdomain_rows=args.subdomain_rows)
+                                   subdomain_rows=args.subdomain_rows,
+                                   coarse=args.coarse)
+        s2.setRank(n)
+        cells = mesh.cells()
+        s2.set_row_coords(np.stack([cells["cx"], cells["cy"]], axis=1))
 
         def e2e_step():
             s2.setRank(n)

@@ -316,6 +316,15 @@ int pg_solver_set_csr(pg_solver *s, const int32_t *row_ptr,
                       const int32_t *col_ind, const double *vals,
                       int ptr_kind);
 
+/* Optional geometry hint for pg_solver_set_csr: a point per row (for a
+ * finite-volume system the cell centroids, FiniteVolumeGrid2D's
+ * cells()[i].centroid()), host xy[2n] interleaved.  Later analyses cut the
+ * Schwarz subdomains by coordinate bisection, as pg_solver_set_eqn does
+ * with its mesh, instead of by graph distance.  NULL clears the hint.
+ * Call after pg_solver_set_rank.  (No reference counterpart: the
+ * SparseMatrixSolver interface carries no geometry.) */
+int pg_solver_set_row_coords(pg_solver *s, const double *xy);
+
 /* Take the matrix and -rhs_ of a device equation without a host round trip
  * (the device form of FiniteVolumeEquation::solve's set + setRhs). */
 int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e);
@@ -338,8 +347,10 @@ int pg_solver_get_x(const pg_solver *s, double *x, int ptr_kind);
  * launched `reps` times back to back on the library stream between CUDA
  * events, on scratch vectors.  Per launch, ms[0] FP64 SpMV with fused dot,
  * ms[1] FP64 ILU(0)/Jacobi apply with fused update, ms[2] FP64 BiCGStab x/r
- * update, ms[3] ILU(0) factorisation, and for PG_MIXED with ILU(0) ms[4]
- * the FP32-factor apply (0 otherwise); ms[5..7] are reserved (0).  Leaves the
+ * update, ms[3] ILU(0) factorisation (with the coarse matrix and its
+ * inverse when cfg.coarse), for PG_MIXED ms[4] the float-float ILU(0)
+ * apply, ms[5] SpMV and ms[6] update (0 otherwise), and ms[7] the coarse
+ * correction of one application (0 without a coarse space).  Leaves the
  * solver's state untouched.  (No reference counterpart: measurement.) */
 int pg_solver_profile(pg_solver *s, int reps, double *ms);
 

@@ -100,6 +100,7 @@ PROTOTYPES = {
     "pg_solver_get_x": (_I, [_P, _P, _I]),
     "pg_solver_partition": (_I, [_P, _P, ctypes.POINTER(_I)]),
     "pg_solver_coarse_inverse": (_I, [_P, _P, ctypes.POINTER(_I)]),
+    "pg_solver_set_row_coords": (_I, [_P, _P]),
     "pg_solver_profile": (_I, [_P, _I, _P]),
     "pg_solver_apply_precond": (_I, [_P, _P, _P, _I]),
     "pg_batch_create": (_I, [_P, ctypes.POINTER(_P)]),
@@ -412,6 +413,15 @@ class SparseMatrixSolver:
         _check(lib().pg_solver_set_rank(self._h, int(n)))
         self.n = int(n)
 
+    def set_row_coords(self, xy):
+        """A point per row (cell centroids, [n, 2]) so set() cuts the
+        Schwarz subdomains by coordinates; None clears it."""
+        if xy is None:
+            _check(lib().pg_solver_set_row_coords(self._h, None))
+            return
+        a = _f64(np.asarray(xy, np.float64).reshape(-1), 2 * self.n)
+        _check(lib().pg_solver_set_row_coords(self._h, _ptr(a)))
+
     def set(self, row_ptr, col_ind, vals):
         rp = _i32(row_ptr, self.n + 1)
         ci = _i32(col_ind, int(rp[-1]))
@@ -494,13 +504,14 @@ class SparseMatrixSolver:
 
     def profile(self, reps: int = 20):
         """Per-launch ms of the hot kernels on the current system: FP64 SpMV,
-        preconditioner apply, x/r update, ILU(0) factorisation, and for the
-        mixed precision solver the float-float ILU(0) apply, SpMV and
-        update."""
+        preconditioner apply, x/r update, ILU(0) factorisation (with the
+        coarse inverse), for the mixed precision solver the float-float
+        ILU(0) apply, SpMV and update, and the coarse correction."""
         ms = np.zeros(8)
         _check(lib().pg_solver_profile(self._h, int(reps), _ptr(ms)))
         return dict(spmv=ms[0], precond=ms[1], update=ms[2], factor=ms[3],
-                    precond_dd=ms[4], spmv_dd=ms[5], update_dd=ms[6])
+                    precond_dd=ms[4], spmv_dd=ms[5], update_dd=ms[6],
+                    coarse=ms[7])
 
     def printStatus(self, msg: str):
         print(f"{msg} iterations = {self.nIters()}, error = {self.error():f}.")

@@ -17,10 +17,10 @@
 // unknown).  The elimination runs in FP32: it is K^3 multiply-adds, which
 // the FP32 pipes do about 64x faster than the FP64 pipe, and an approximate
 // coarse inverse leaves the preconditioner a fixed linear operator as long
-// as it is applied in FP64, which it is.  An application is then the K
+// as it is applied accurately, which it is (to about 1e-14).  An application is then the K
 // subdomain sums of the input (fused into the streamed ILU(0) sweeps), one
-// K x K matrix-vector product accumulated in FP64 and a constant added to
-// every row of a subdomain.  All reductions run in a fixed order, so
+// K x K matrix-vector product with a compensated float-float accumulation
+// and a constant added to every row of a subdomain.  All reductions run in a fixed order, so
 // results are reproducible.
 #include <type_traits>
 
@@ -31,6 +31,9 @@ namespace pg {
 namespace {
 
 constexpr int kCoarseBlock = 128;
+constexpr int kCorrectBlock = 256;
+constexpr int kGjB = 32;     // pivots per block of the Gauss-Jordan inversion
+constexpr int kGjRows = 16;  // rows per CTA of the block update
 
 // deterministic block sum (fixed tree); every thread gets the total
 __device__ double block_sum(double v, double *red) {
@@ -70,52 +73,133 @@ k_coarse_assemble(int K, const int32_t *__restrict__ sub_ptr,
   }
 }
 
-// pivot row / column 0 and the diagonal before elimination
-__global__ void k_gj_init(int K, const float *__restrict__ ac,
-                          float *__restrict__ rowb, float *__restrict__ colb,
+// the diagonal before elimination (reference for vanishing pivots)
+__global__ void k_gj_diag(int K, const float *__restrict__ ac,
                           float *__restrict__ dg0) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= K) return;
-  rowb[i] = ac[i];
-  colb[i] = ac[(size_t)i * K];
-  dg0[i] = ac[(size_t)i * K + i];
+  if (i < K) dg0[i] = ac[(size_t)i * K + i];
 }
 
-// Gauss-Jordan step k on the K x K matrix in place, row i = blockIdx.y
-// (the pivot row and column of this step are read from rowb/colb[k & 1];
-// the ones of step k+1 are written to the other half as they are computed)
+// Blocked Gauss-Jordan inversion in place.  For the pivot block
+// k0 .. k0+b-1 with P = A[blk, blk], R = A[blk, :] and C = A[:, blk], b
+// single-pivot eliminations amount to
+//     A[blk, blk] <- P^-1          A[blk, j] <- (P^-1 R)[:, j]
+//     A[i, blk]   <- -(C P^-1)[i]  A[i, j]   <- A[i, j] - C[i, :] (P^-1 R)[:, j]
+// (the sweep operator of a block is the product of its pivots' sweeps).
+
+// P^-1 by single-pivot Gauss-Jordan in shared memory (one CTA of
+// kGjB x kGjB threads); a pivot below 1e-5 of its original diagonal is
+// dropped (its row and column of the inverse are zero)
+__global__ void __launch_bounds__(kGjB * kGjB)
+k_gjb_pivot_block(int K, int k0, int b, const float *__restrict__ ac,
+                  const float *__restrict__ dg0, float *__restrict__ pinv) {
+  __shared__ float P[kGjB][kGjB + 1];
+  __shared__ float rowk[kGjB], colk[kGjB];
+  const int q = threadIdx.x % kGjB, p = threadIdx.x / kGjB;
+  P[p][q] = p < b && q < b ? ac[(size_t)(k0 + p) * K + k0 + q] : 0.f;
+  __syncthreads();
+  for (int k = 0; k < b; ++k) {
+    if (p == 0) rowk[q] = P[k][q];
+    if (q == 0) colk[p] = P[p][k];
+    __syncthreads();
+    const float piv = rowk[k];
+    const float ip = fabsf(piv) > 1e-5f * fabsf(dg0[k0 + k]) ? 1.f / piv : 0.f;
+    float v;
+    if (p == k && q == k)
+      v = ip;
+    else if (p == k)
+      v = rowk[q] * ip;
+    else if (q == k)
+      v = -colk[p] * ip;
+    else
+      v = P[p][q] - colk[p] * (rowk[q] * ip);
+    __syncthreads();
+    P[p][q] = v;
+    __syncthreads();
+  }
+  pinv[p * kGjB + q] = P[p][q];
+}
+
+// W = P^-1 R (b x K) and V = C P^-1 (K x b); C is kept (K x b) for the
+// update, which overwrites the block columns
 __global__ void __launch_bounds__(256)
-k_gj_step(int K, int k, float *__restrict__ ac, float *__restrict__ rowb,
-          float *__restrict__ colb, const float *__restrict__ dg0) {
-  const int i = blockIdx.y;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= K) return;
-  const int b = k & 1;
-  const float piv = rowb[b * K + k];
-  const float ip = fabsf(piv) > 1e-5f * fabsf(dg0[k]) ? 1.f / piv : 0.f;
-  const float a_ik = colb[b * K + i], a_kj = rowb[b * K + j];
-  const size_t idx = (size_t)i * K + j;
-  float v;
-  if (i == k && j == k)
-    v = ip;
-  else if (i == k)
-    v = a_kj * ip;
-  else if (j == k)
-    v = -a_ik * ip;
-  else
-    v = ac[idx] - a_ik * (a_kj * ip);
-  ac[idx] = v;
-  if (k + 1 < K) {
-    const int nb = b ^ 1;
-    if (i == k + 1) rowb[nb * K + j] = v;
-    if (j == k + 1) colb[nb * K + i] = v;
+k_gjb_panel(int K, int k0, int b, const float *__restrict__ ac,
+            const float *__restrict__ pinv, float *__restrict__ W,
+            float *__restrict__ V, float *__restrict__ C) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < K) {  // column j = t of W
+    float r[kGjB];
+#pragma unroll
+    for (int q = 0; q < kGjB; ++q)
+      r[q] = q < b ? ac[(size_t)(k0 + q) * K + t] : 0.f;
+    for (int p = 0; p < b; ++p) {
+      float acc = 0.f;
+#pragma unroll
+      for (int q = 0; q < kGjB; ++q) acc += pinv[p * kGjB + q] * r[q];
+      W[(size_t)p * K + t] = acc;
+    }
+  } else if (t < 2 * K) {  // row i of V and C
+    const int i = t - K;
+    float c[kGjB];
+#pragma unroll
+    for (int q = 0; q < kGjB; ++q) {
+      c[q] = q < b ? ac[(size_t)i * K + k0 + q] : 0.f;
+      C[(size_t)i * kGjB + q] = c[q];
+    }
+    for (int p = 0; p < b; ++p) {
+      float acc = 0.f;
+#pragma unroll
+      for (int q = 0; q < kGjB; ++q) acc += c[q] * pinv[q * kGjB + p];
+      V[(size_t)i * kGjB + p] = acc;
+    }
   }
 }
 
-// Z^T in: one sum per subdomain
+// the update of every entry; a CTA owns kGjRows rows x 256 columns and each
+// thread keeps its column of W in registers
+__global__ void __launch_bounds__(256)
+k_gjb_update(int K, int k0, int b, float *__restrict__ ac,
+             const float *__restrict__ pinv, const float *__restrict__ W,
+             const float *__restrict__ V, const float *__restrict__ C) {
+  __shared__ float cs[kGjRows][kGjB];
+  const int j = blockIdx.x * 256 + threadIdx.x;
+  const int i0 = blockIdx.y * kGjRows;
+  for (int e = threadIdx.x; e < kGjRows * kGjB; e += 256) {
+    const int ii = i0 + e / kGjB;
+    cs[e / kGjB][e % kGjB] = ii < K ? C[(size_t)ii * kGjB + e % kGjB] : 0.f;
+  }
+  __syncthreads();
+  if (j >= K) return;
+  float w[kGjB];
+#pragma unroll
+  for (int q = 0; q < kGjB; ++q) w[q] = q < b ? W[(size_t)q * K + j] : 0.f;
+  const bool jin = j >= k0 && j < k0 + b;
+  for (int r = 0; r < kGjRows; ++r) {
+    const int i = i0 + r;
+    if (i >= K) break;
+    const bool iin = i >= k0 && i < k0 + b;
+    const size_t idx = (size_t)i * K + j;
+    float v;
+    if (iin && jin)
+      v = pinv[(i - k0) * kGjB + (j - k0)];
+    else if (iin)
+      v = w[i - k0];
+    else if (jin)
+      v = -V[(size_t)i * kGjB + (j - k0)];
+    else {
+      float acc = 0.f;
+#pragma unroll
+      for (int q = 0; q < kGjB; ++q) acc += cs[r][q] * w[q];
+      v = ac[idx] - acc;
+    }
+    ac[idx] = v;
+  }
+}
+
+// Z^T in: one sum per subdomain, stored as a float pair (hi + lo)
 __global__ void __launch_bounds__(kCoarseBlock)
 k_coarse_sum(const int32_t *__restrict__ sub_ptr, const double *__restrict__ in,
-             double *__restrict__ csum, const KScalars *__restrict__ sc) {
+             float2 *__restrict__ csum, const KScalars *__restrict__ sc) {
   if (sc && sc->done) return;
   __shared__ double red[kCoarseBlock];
   const int s = blockIdx.x;
@@ -123,12 +207,12 @@ k_coarse_sum(const int32_t *__restrict__ sub_ptr, const double *__restrict__ in,
   for (int32_t i = sub_ptr[s] + threadIdx.x; i < sub_ptr[s + 1]; i += kCoarseBlock)
     acc += in[i];
   const double t = block_sum(acc, red);
-  if (threadIdx.x == 0) csum[s] = t;
+  if (threadIdx.x == 0) csum[s] = dd_from(t);
 }
 
 __global__ void __launch_bounds__(kCoarseBlock)
 k_coarse_sum_dd(const int32_t *__restrict__ sub_ptr,
-                const float2 *__restrict__ in, double *__restrict__ csum,
+                const float2 *__restrict__ in, float2 *__restrict__ csum,
                 const KScalars *__restrict__ sc) {
   if (sc && sc->done) return;
   __shared__ double red[kCoarseBlock];
@@ -137,30 +221,60 @@ k_coarse_sum_dd(const int32_t *__restrict__ sub_ptr,
   for (int32_t i = sub_ptr[s] + threadIdx.x; i < sub_ptr[s + 1]; i += kCoarseBlock)
     dd_acc_add(acc, in[i]);
   const double t = block_sum(dd_acc_to_double(acc), red);
-  if (threadIdx.x == 0) csum[s] = t;
+  if (threadIdx.x == 0) csum[s] = dd_from(t);
 }
 
-// y_s = (A_c^-1)_s . csum, then z += y_s on the rows of subdomain s
+// y_s = (A_c^-1)_s . csum with a compensated float-float accumulation on
+// the FP32 pipes (the FP32 inverse entries times the float-pair sums:
+// TwoProduct of the high parts plus the low-part product; about 1e-14
+// relative, so the correction stays a linear operator to that level), then
+// z += y_s on the rows of subdomain s
 template <class VT>
-__global__ void __launch_bounds__(kCoarseBlock)
+__global__ void __launch_bounds__(kCorrectBlock)
 k_coarse_correct(int K, const int32_t *__restrict__ sub_ptr,
                  const float *__restrict__ ainv,
-                 const double *__restrict__ csum, VT *__restrict__ z,
+                 const float2 *__restrict__ csum, VT *__restrict__ z,
                  const KScalars *__restrict__ sc) {
   if (sc && sc->done) return;
-  __shared__ double red[kCoarseBlock];
+  __shared__ float red_s[kCorrectBlock / 32], red_c[kCorrectBlock / 32];
+  __shared__ double y_sh;
   const int s = blockIdx.x;
   const float *row = ainv + (size_t)s * K;
-  double acc = 0.;
-  for (int j = threadIdx.x; j < K; j += kCoarseBlock)
-    acc += (double)row[j] * csum[j];
-  const double y = block_sum(acc, red);
+  DdAcc acc = dd_acc(make_float2(0.f, 0.f));
+  for (int j = threadIdx.x; j < K; j += kCorrectBlock)
+    dd_acc_fma(acc, make_float2(row[j], 0.f), csum[j]);
+  // fixed-order reduction: butterfly within the warp, then warp order
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    DdAcc b;
+    b.s = __shfl_xor_sync(0xffffffffu, acc.s, o);
+    b.c = __shfl_xor_sync(0xffffffffu, acc.c, o);
+    dd_acc_merge(acc, b);
+  }
+  const int wid = threadIdx.x / 32;
+  if ((threadIdx.x & 31) == 0) {
+    red_s[wid] = acc.s;
+    red_c[wid] = acc.c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    DdAcc t = dd_acc(make_float2(red_s[0], red_c[0]));
+    for (int w = 1; w < kCorrectBlock / 32; ++w) {
+      DdAcc b;
+      b.s = red_s[w];
+      b.c = red_c[w];
+      dd_acc_merge(t, b);
+    }
+    y_sh = dd_acc_to_double(t);
+  }
+  __syncthreads();
+  const double y = y_sh;
   if constexpr (std::is_same<VT, double>::value) {
-    for (int32_t i = sub_ptr[s] + threadIdx.x; i < sub_ptr[s + 1]; i += kCoarseBlock)
+    for (int32_t i = sub_ptr[s] + threadIdx.x; i < sub_ptr[s + 1]; i += kCorrectBlock)
       z[i] += y;
   } else {
     const float2 yd = dd_from(y);
-    for (int32_t i = sub_ptr[s] + threadIdx.x; i < sub_ptr[s + 1]; i += kCoarseBlock)
+    for (int32_t i = sub_ptr[s] + threadIdx.x; i < sub_ptr[s + 1]; i += kCorrectBlock)
       z[i] = dd_add(z[i], yd);
   }
 }
@@ -175,14 +289,20 @@ void launch_coarse_setup(const CoarseDev &c, const double *pvals,
   const size_t smem = (size_t)kCoarseBlock * c.max_cnb * sizeof(double);
   k_coarse_assemble<<<K, kCoarseBlock, smem, st>>>(K, c.sub_ptr, prp, pvals,
                                                    c.cptr, c.cnb, c.cslot, c.ac);
-  k_gj_init<<<(K + 255) / 256, 256, 0, st>>>(K, c.ac, c.rowb, c.colb, c.dg0);
+  k_gj_diag<<<(K + 255) / 256, 256, 0, st>>>(K, c.ac, c.dg0);
   count_launches(2);
-  // the K elimination steps: captured once into a graph, replayed (run
+  // the K / kGjB block steps: captured once into a graph, replayed (run
   // directly when the capture is not possible)
-  const dim3 grid((K + 255) / 256, K);
+  const int nblk = (K + kGjB - 1) / kGjB;
+  const dim3 ugrid((K + 255) / 256, (K + kGjRows - 1) / kGjRows);
   auto steps = [&]() {
-    for (int k = 0; k < K; ++k)
-      k_gj_step<<<grid, 256, 0, st>>>(K, k, c.ac, c.rowb, c.colb, c.dg0);
+    for (int k0 = 0; k0 < K; k0 += kGjB) {
+      const int b = K - k0 < kGjB ? K - k0 : kGjB;
+      k_gjb_pivot_block<<<1, kGjB * kGjB, 0, st>>>(K, k0, b, c.ac, c.dg0, c.pinv);
+      k_gjb_panel<<<(2 * K + 255) / 256, 256, 0, st>>>(K, k0, b, c.ac, c.pinv,
+                                                       c.W, c.V, c.C);
+      k_gjb_update<<<ugrid, 256, 0, st>>>(K, k0, b, c.ac, c.pinv, c.W, c.V, c.C);
+    }
   };
   if (gj_graph && !*gj_graph) {
     cudaGraph_t g = nullptr;
@@ -199,7 +319,7 @@ void launch_coarse_setup(const CoarseDev &c, const double *pvals,
     cudaGraphLaunch(*gj_graph, st);
   else
     steps();
-  count_launches(K);
+  count_launches(3 * nblk);
 }
 
 void launch_coarse_apply(const CoarseDev &c, const double *in, double *z,
@@ -208,7 +328,7 @@ void launch_coarse_apply(const CoarseDev &c, const double *in, double *z,
     k_coarse_sum<<<c.K, kCoarseBlock, 0, st>>>(c.sub_ptr, in, c.csum, sc);
     count_launches(1);
   }
-  k_coarse_correct<double><<<c.K, kCoarseBlock, 0, st>>>(c.K, c.sub_ptr, c.ac,
+  k_coarse_correct<double><<<c.K, kCorrectBlock, 0, st>>>(c.K, c.sub_ptr, c.ac,
                                                          c.csum, z, sc);
   count_launches(1);
 }
@@ -220,7 +340,7 @@ void launch_coarse_apply_dd(const CoarseDev &c, const float2 *in, float2 *z,
     k_coarse_sum_dd<<<c.K, kCoarseBlock, 0, st>>>(c.sub_ptr, in, c.csum, sc);
     count_launches(1);
   }
-  k_coarse_correct<float2><<<c.K, kCoarseBlock, 0, st>>>(c.K, c.sub_ptr, c.ac,
+  k_coarse_correct<float2><<<c.K, kCorrectBlock, 0, st>>>(c.K, c.sub_ptr, c.ac,
                                                          c.csum, z, sc);
   count_launches(1);
 }

@@ -231,10 +231,10 @@ struct ArithF64 {
   using Sum = double;
   __device__ static Sum sum_init() { return 0.; }
   __device__ static void sum_add(Sum &a, V x) { a += x; }
-  __device__ static double sum_warp(Sum a) {
+  __device__ static float2 sum_warp(Sum a) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-    return a;
+    return dd_from(a);
   }
   template <int KT, bool DIAG>
   __device__ static V row(V self, const V (&v)[KT], const V (&x)[KT], V d) {
@@ -263,7 +263,7 @@ struct ArithDD {
   using Sum = DdAcc;
   __device__ static Sum sum_init() { return dd_acc(make_float2(0.f, 0.f)); }
   __device__ static void sum_add(Sum &a, V x) { dd_acc_add(a, x); }
-  __device__ static double sum_warp(Sum a) {
+  __device__ static float2 sum_warp(Sum a) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       DdAcc b;
@@ -271,7 +271,7 @@ struct ArithDD {
       b.c = __shfl_xor_sync(0xffffffffu, a.c, o);
       dd_acc_merge(a, b);
     }
-    return dd_acc_to_double(a);
+    return dd_value(a);
   }
   template <int KT, bool DIAG>
   __device__ static V row(V self, const V (&v)[KT], const V (&x)[KT], V d) {
@@ -303,7 +303,7 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
                     typename AR::V *__restrict__ z,
                     const KScalars *__restrict__ sc_base,
                     const int32_t *__restrict__ sub_sys,
-                    int *__restrict__ err, double *__restrict__ csum) {
+                    int *__restrict__ err, float2 *__restrict__ csum) {
   using MT = typename AR::V;
   // batched solves: the scalars of this subdomain's system
   const KScalars *sc =
@@ -364,7 +364,7 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
       }
     }
     if (csum) {
-      const double t = AR::sum_warp(part);
+      const float2 t = AR::sum_warp(part);
       if (lane == 0) csum[blockIdx.x] = t;
     }
   }

@@ -179,22 +179,25 @@ struct SolverDev {
   // apply kernels then read the scalars sc[sub_sys[subdomain]]
   const int32_t *sub_sys;
   // two-level Schwarz: the streamed sweeps write the sum of each
-  // subdomain's input here (NULL: no coarse correction)
-  double *csum;
+  // subdomain's input here, as a float pair (NULL: no coarse correction)
+  float2 *csum;
 };
 
 
 
 // Coarse space of the two-level Schwarz preconditioner (coarse.cu): the
 // subdomain row ranges, the coupling structure of A_c = Z^T A Z, the dense
-// K x K FP32 matrix (inverted in place by launch_coarse_setup), Gauss-Jordan
-// pivot buffers and the FP64 subdomain sums of an application's input.
+// K x K FP32 matrix (inverted in place by launch_coarse_setup), the
+// original diagonal, the blocked Gauss-Jordan work arrays (pivot-block
+// inverse 32 x 32, W 32 x K, V and C K x 32) and the subdomain sums of an
+// application's input (float pairs).
 struct CoarseDev {
   int K = 0, max_cnb = 0;
   const int32_t *sub_ptr = nullptr, *cptr = nullptr, *cnb = nullptr;
   const uint8_t *cslot = nullptr;
-  float *ac = nullptr, *rowb = nullptr, *colb = nullptr, *dg0 = nullptr;
-  double *csum = nullptr;
+  float *ac = nullptr, *dg0 = nullptr;
+  float *pinv = nullptr, *W = nullptr, *V = nullptr, *C = nullptr;
+  float2 *csum = nullptr;
 };
 
 // A_c from the permuted values, then A_c^-1 in place (the K elimination

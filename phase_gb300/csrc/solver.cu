@@ -63,6 +63,7 @@ struct pg_solver {
   DevBuf<int32_t> pack_src, pack_dst64, pack_src_dd, pack_dst_dd;
   DevBuf<int> err;
   DevBuf<int32_t> raw_rp, raw_ci, st_rp, st_ci;
+  std::vector<double> row_x, row_y;  // pg_solver_set_row_coords hint
   DevBuf<double> st_vals, st_vec;
   DevBuf<unsigned int> diff;
   // values and factors
@@ -95,8 +96,8 @@ struct pg_solver {
   bool coarse_on = false;
   DevBuf<int32_t> c_sub_ptr, c_cptr, c_cnb;
   DevBuf<uint8_t> c_slot;
-  DevBuf<float> c_ac, c_rowb, c_colb, c_dg0;
-  DevBuf<double> c_sum;
+  DevBuf<float> c_ac, c_dg0, c_pinv, c_W, c_V, c_C;
+  DevBuf<float2> c_sum;
   cudaGraphExec_t gj_graph = nullptr;
 
   void drop_graphs() {
@@ -121,9 +122,11 @@ struct pg_solver {
     c.cnb = c_cnb.p;
     c.cslot = c_slot.p;
     c.ac = c_ac.p;
-    c.rowb = c_rowb.p;
-    c.colb = c_colb.p;
     c.dg0 = c_dg0.p;
+    c.pinv = c_pinv.p;
+    c.W = c_W.p;
+    c.V = c_V.p;
+    c.C = c_C.p;
     c.csum = c_sum.p;
     return c;
   }
@@ -245,9 +248,10 @@ int upload_analysis(pg_solver *s) {
     up(s->c_cnb, a.cnb);
     up(s->c_slot, a.cslot);
     if (e == cudaSuccess) e = s->c_ac.reserve(K * K);
-    for (DevBuf<float> *bf : {&s->c_rowb, &s->c_colb})
-      if (e == cudaSuccess) e = bf->reserve(2 * K);
     if (e == cudaSuccess) e = s->c_dg0.reserve(K);
+    if (e == cudaSuccess) e = s->c_pinv.reserve(32 * 32);
+    for (DevBuf<float> *bf : {&s->c_W, &s->c_V, &s->c_C})
+      if (e == cudaSuccess) e = bf->reserve(32 * K);
     if (e == cudaSuccess) e = s->c_sum.reserve(K);
     s->coarse_on = true;
   }
@@ -700,6 +704,23 @@ extern "C" int pg_solver_set_rank(pg_solver *s, int64_t n) {
   return PG_OK;
 }
 
+extern "C" int pg_solver_set_row_coords(pg_solver *s, const double *xy) {
+  PG_CHECK_ARG(s, "pg_solver_set_row_coords: NULL solver");
+  s->row_x.clear();
+  s->row_y.clear();
+  if (xy) {
+    PG_CHECK_ARG(s->rank > 0, "pg_solver_set_row_coords: set_rank first");
+    s->row_x.resize(s->rank);
+    s->row_y.resize(s->rank);
+    for (int64_t i = 0; i < s->rank; ++i) {
+      s->row_x[i] = xy[2 * i];
+      s->row_y[i] = xy[2 * i + 1];
+    }
+  }
+  s->analysed = false;  // the next set_csr re-cuts the subdomains
+  return PG_OK;
+}
+
 extern "C" int pg_solver_set_csr(pg_solver *s, const int32_t *row_ptr,
                                  const int32_t *col_ind, const double *vals,
                                  int ptr_kind) {
@@ -758,7 +779,10 @@ extern "C" int pg_solver_set_csr(pg_solver *s, const int32_t *row_ptr,
       hrp = h_rp.data();
       hci = h_ci.data();
     }
-    int rc = analyse(n, hrp, hci, s->cfg.precond == PG_PREC_ILU0 ? s->cfg.subdomain_rows : -1, s->a);
+    const bool xy = (int64_t)s->row_x.size() == n;
+    int rc = analyse(n, hrp, hci, s->cfg.precond == PG_PREC_ILU0 ? s->cfg.subdomain_rows : -1, s->a,
+                     nullptr, xy ? s->row_x.data() : nullptr,
+                     xy ? s->row_y.data() : nullptr);
     if (rc) return rc;
     rc = upload_analysis(s);
     if (rc) return rc;
@@ -973,7 +997,13 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
   if (!rc) rc = timed([&] { launch_precond<double, double>(s->cfg.precond, 1, d, s->jdinv.p, d8[3].p, d8[4].p, d8[1].p, d8[6].p, s->sc.p, st); }, &ms[1]);
   if (!rc) rc = timed([&] { launch_update<double>(d.n, d8[5].p, d8[3].p, d8[0].p, d8[6].p, d8[4].p, d8[1].p, d8[2].p, s->sc.p, w, st); }, &ms[2]);
   if (!rc && s->cfg.precond == PG_PREC_ILU0)
-    rc = timed([&] { launch_ilu0_factor(d, s->pvals.p, s->bad.p, dd, st); }, &ms[3]);
+    rc = timed([&] {
+      launch_ilu0_factor(d, s->pvals.p, s->bad.p, dd, st);
+      if (s->coarse_on)
+        launch_coarse_setup(s->coarse(), s->pvals.p, s->prp.p, &s->gj_graph, st);
+    }, &ms[3]);
+  if (!rc && s->coarse_on)
+    rc = timed([&] { launch_coarse_apply(s->coarse(), d8[4].p, d8[6].p, true, s->sc.p, st); }, &ms[7]);
   if (!rc && dd) {
     if (s->cfg.precond == PG_PREC_ILU0)
       rc = timed([&] { launch_ilu0_apply_dd(1, d, f8[3].p, f8[4].p, f8[1].p, f8[6].p, s->sc.p, st); }, &ms[4]);
