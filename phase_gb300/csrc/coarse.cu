@@ -87,70 +87,78 @@ __global__ void k_gj_diag(int K, const float *__restrict__ ac,
 //     A[i, blk]   <- -(C P^-1)[i]  A[i, j]   <- A[i, j] - C[i, :] (P^-1 R)[:, j]
 // (the sweep operator of a block is the product of its pivots' sweeps).
 
-// P^-1 by single-pivot Gauss-Jordan in shared memory (one CTA of
-// kGjB x kGjB threads); a pivot below 1e-5 of its original diagonal is
-// dropped (its row and column of the inverse are zero)
-__global__ void __launch_bounds__(kGjB * kGjB)
+// P^-1 by single-pivot Gauss-Jordan in the registers of one warp: lane q
+// holds column q of the pivot block; a pivot below 1e-5 of its original
+// diagonal is dropped (its row and column of the inverse are zero)
+__global__ void __launch_bounds__(32)
 k_gjb_pivot_block(int K, int k0, int b, const float *__restrict__ ac,
                   const float *__restrict__ dg0, float *__restrict__ pinv) {
-  __shared__ float P[kGjB][kGjB + 1];
-  __shared__ float rowk[kGjB], colk[kGjB];
-  const int q = threadIdx.x % kGjB, p = threadIdx.x / kGjB;
-  P[p][q] = p < b && q < b ? ac[(size_t)(k0 + p) * K + k0 + q] : 0.f;
-  __syncthreads();
-  for (int k = 0; k < b; ++k) {
-    if (p == 0) rowk[q] = P[k][q];
-    if (q == 0) colk[p] = P[p][k];
-    __syncthreads();
-    const float piv = rowk[k];
-    const float ip = fabsf(piv) > 1e-5f * fabsf(dg0[k0 + k]) ? 1.f / piv : 0.f;
-    float v;
-    if (p == k && q == k)
-      v = ip;
-    else if (p == k)
-      v = rowk[q] * ip;
-    else if (q == k)
-      v = -colk[p] * ip;
-    else
-      v = P[p][q] - colk[p] * (rowk[q] * ip);
-    __syncthreads();
-    P[p][q] = v;
-    __syncthreads();
+  const int q = threadIdx.x;
+  float c[kGjB];
+#pragma unroll
+  for (int p = 0; p < kGjB; ++p)
+    c[p] = p < b && q < b ? ac[(size_t)(k0 + p) * K + k0 + q] : 0.f;
+#pragma unroll
+  for (int k = 0; k < kGjB; ++k) {
+    if (k < b) {
+      const float piv = __shfl_sync(0xffffffffu, c[k], k);
+      const float ip = fabsf(piv) > 1e-5f * fabsf(dg0[k0 + k]) ? 1.f / piv : 0.f;
+      const float rk = c[k];  // P[k][q]
+#pragma unroll
+      for (int p = 0; p < kGjB; ++p) {
+        const float cpk = __shfl_sync(0xffffffffu, c[p], k);  // P[p][k]
+        if (p == k)
+          c[p] = q == k ? ip : rk * ip;
+        else
+          c[p] = q == k ? -cpk * ip : c[p] - cpk * (rk * ip);
+      }
+    }
   }
-  pinv[p * kGjB + q] = P[p][q];
+#pragma unroll
+  for (int p = 0; p < kGjB; ++p) pinv[p * kGjB + q] = c[p];
 }
 
 // W = P^-1 R (b x K) and V = C P^-1 (K x b); C is kept (K x b) for the
-// update, which overwrites the block columns
+// update, which overwrites the block columns.  Blocks [0, nw): 32 columns
+// of W each (thread (x, y): column x, rows y, y+8, ...); blocks after:
+// rows of V and C (four threads per row, eight columns each).
 __global__ void __launch_bounds__(256)
-k_gjb_panel(int K, int k0, int b, const float *__restrict__ ac,
+k_gjb_panel(int K, int k0, int b, int nw, const float *__restrict__ ac,
             const float *__restrict__ pinv, float *__restrict__ W,
             float *__restrict__ V, float *__restrict__ C) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < K) {  // column j = t of W
+  __shared__ float pi[kGjB][kGjB + 1];
+  for (int e = threadIdx.x; e < kGjB * kGjB; e += 256)
+    pi[e / kGjB][e % kGjB] = pinv[e];
+  __syncthreads();
+  if ((int)blockIdx.x < nw) {
+    const int j = blockIdx.x * 32 + (threadIdx.x & 31);
+    if (j >= K) return;
     float r[kGjB];
 #pragma unroll
     for (int q = 0; q < kGjB; ++q)
-      r[q] = q < b ? ac[(size_t)(k0 + q) * K + t] : 0.f;
-    for (int p = 0; p < b; ++p) {
+      r[q] = q < b ? ac[(size_t)(k0 + q) * K + j] : 0.f;
+    for (int p = threadIdx.x >> 5; p < b; p += 8) {
       float acc = 0.f;
 #pragma unroll
-      for (int q = 0; q < kGjB; ++q) acc += pinv[p * kGjB + q] * r[q];
-      W[(size_t)p * K + t] = acc;
+      for (int q = 0; q < kGjB; ++q) acc += pi[p][q] * r[q];
+      W[(size_t)p * K + j] = acc;
     }
-  } else if (t < 2 * K) {  // row i of V and C
-    const int i = t - K;
+  } else {
+    const int t = (blockIdx.x - nw) * 256 + threadIdx.x;
+    const int i = t >> 2, p0 = (t & 3) * 8;
+    if (i >= K) return;
     float c[kGjB];
 #pragma unroll
-    for (int q = 0; q < kGjB; ++q) {
+    for (int q = 0; q < kGjB; ++q)
       c[q] = q < b ? ac[(size_t)i * K + k0 + q] : 0.f;
-      C[(size_t)i * kGjB + q] = c[q];
-    }
-    for (int p = 0; p < b; ++p) {
+#pragma unroll
+    for (int pp = 0; pp < 8; ++pp) {
+      const int p = p0 + pp;
       float acc = 0.f;
 #pragma unroll
-      for (int q = 0; q < kGjB; ++q) acc += c[q] * pinv[q * kGjB + p];
+      for (int q = 0; q < kGjB; ++q) acc += c[q] * pi[q][p];
       V[(size_t)i * kGjB + p] = acc;
+      C[(size_t)i * kGjB + p] = c[p];
     }
   }
 }
@@ -228,7 +236,7 @@ k_coarse_sum_dd(const int32_t *__restrict__ sub_ptr,
 // the FP32 pipes (the FP32 inverse entries times the float-pair sums:
 // TwoProduct of the high parts plus the low-part product; about 1e-14
 // relative, so the correction stays a linear operator to that level), then
-// z += y_s on the rows of subdomain s
+// z += y_s on the rows of subdomain s (one CTA per subdomain)
 template <class VT>
 __global__ void __launch_bounds__(kCorrectBlock)
 k_coarse_correct(int K, const int32_t *__restrict__ sub_ptr,
@@ -294,13 +302,14 @@ void launch_coarse_setup(const CoarseDev &c, const double *pvals,
   // the K / kGjB block steps: captured once into a graph, replayed (run
   // directly when the capture is not possible)
   const int nblk = (K + kGjB - 1) / kGjB;
+  const int nw = (K + 31) / 32;
   const dim3 ugrid((K + 255) / 256, (K + kGjRows - 1) / kGjRows);
   auto steps = [&]() {
     for (int k0 = 0; k0 < K; k0 += kGjB) {
       const int b = K - k0 < kGjB ? K - k0 : kGjB;
-      k_gjb_pivot_block<<<1, kGjB * kGjB, 0, st>>>(K, k0, b, c.ac, c.dg0, c.pinv);
-      k_gjb_panel<<<(2 * K + 255) / 256, 256, 0, st>>>(K, k0, b, c.ac, c.pinv,
-                                                       c.W, c.V, c.C);
+      k_gjb_pivot_block<<<1, 32, 0, st>>>(K, k0, b, c.ac, c.dg0, c.pinv);
+      k_gjb_panel<<<nw + (4 * K + 255) / 256, 256, 0, st>>>(K, k0, b, nw, c.ac,
+                                                            c.pinv, c.W, c.V, c.C);
       k_gjb_update<<<ugrid, 256, 0, st>>>(K, k0, b, c.ac, c.pinv, c.W, c.V, c.C);
     }
   };
@@ -329,7 +338,7 @@ void launch_coarse_apply(const CoarseDev &c, const double *in, double *z,
     count_launches(1);
   }
   k_coarse_correct<double><<<c.K, kCorrectBlock, 0, st>>>(c.K, c.sub_ptr, c.ac,
-                                                         c.csum, z, sc);
+                                                          c.csum, z, sc);
   count_launches(1);
 }
 
@@ -341,7 +350,7 @@ void launch_coarse_apply_dd(const CoarseDev &c, const float2 *in, float2 *z,
     count_launches(1);
   }
   k_coarse_correct<float2><<<c.K, kCorrectBlock, 0, st>>>(c.K, c.sub_ptr, c.ac,
-                                                         c.csum, z, sc);
+                                                          c.csum, z, sc);
   count_launches(1);
 }
 
