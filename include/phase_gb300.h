@@ -272,8 +272,10 @@ typedef struct {
   double tolerance;   /* ||b - A x||_2 / ||b||_2 target (Belos default 1e-8) */
   int max_iters;      /* Belos default 500 */
   int precond;        /* PG_PREC_* */
-  int subdomain_rows; /* target rows per Schwarz subdomain; 0 = default;
-                         -1 = one subdomain (global ILU(0)) */
+  int subdomain_rows; /* target rows per Schwarz subdomain; 0 = default
+                         (1024; with the coarse correction 512, or
+                         n / 2048 when larger); -1 = one subdomain
+                         (global ILU(0)) */
   int precision;      /* PG_FP64 | PG_MIXED */
   int mixed_sweep;    /* PG_MIXED ILU(0) sweep form: 0 = timed choice at the
                          first factorisation, 1 = warp-wide steps, 2 = level

@@ -659,7 +659,13 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   //    level's rows, slot-major; consecutive levels are grouped into pieces
   //    of about kStreamPiece bytes.  pack_* map every value position of a
   //    stream to its slot in the FP64 factor records.
-  a.smeta64.resize(a.n_sub);
+  //    A record is a sweep group: one subdomain, or two consecutive ones
+  //    whose levels fit side by side in one warp (every level of the pair
+  //    at most 32 rows wide together); the group's level l holds level l of
+  //    each member, so one warp sweeps both independent blocks at once.
+  //    Pairs are formed only for single systems with compile-time slot
+  //    counts (at most 3 L and 3 U entries per row).
+  a.smeta64.clear();
   a.pack_src.clear();
   a.pack_dst64.clear();
   a.ssmem64 = 0;
@@ -670,14 +676,47 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   int KLs = a.max_kl, KUs = a.max_ku;
   if (KLs <= 2 && KUs <= 2) KLs = KUs = 2;
   else if (KLs <= 3 && KUs <= 3) KLs = KUs = 3;
-  for (int s = 0; s < a.n_sub; ++s) {
+  const bool may_pair = !sys_rows && KLs <= 3 && KUs <= 3;
+  auto lvl_of = [&](int s) {
     const SubMeta &f = a.meta64[s];
-    const int nr = f.nr, nlev = f.nlev, KL = KLs, KU = KUs;
-    const int fKL = f.KL, fKU = f.K - f.KL;
-    const int64_t fsrc0 = (f.rec_off + f.val_off) / 8;  // double index
-    const uint16_t *flvl = reinterpret_cast<const uint16_t *>(a.rec64.data() + f.rec_off);
-    const uint16_t *fcols =
-        reinterpret_cast<const uint16_t *>(a.rec64.data() + f.rec_off + f.col_off);
+    return reinterpret_cast<const uint16_t *>(a.rec64.data() + f.rec_off);
+  };
+  auto width = [&](int s, int l) {
+    const uint16_t *lv = lvl_of(s);
+    return l < a.meta64[s].nlev ? lv[l + 1] - lv[l] : 0;
+  };
+  auto pairs_fit = [&](int s) {
+    if (!may_pair || s + 1 >= a.n_sub) return false;
+    if (a.meta64[s].nr + a.meta64[s + 1].nr + 1 > 65535) return false;
+    const int nl = std::max(a.meta64[s].nlev, a.meta64[s + 1].nlev);
+    for (int l = 0; l < nl; ++l)
+      if (width(s, l) + width(s + 1, l) > 32) return false;
+    return true;
+  };
+  for (int s = 0; s < a.n_sub;) {
+    const int G = pairs_fit(s) ? 2 : 1;
+    const SubMeta *mf[2] = {&a.meta64[s], G == 2 ? &a.meta64[s + 1] : nullptr};
+    const int nr = mf[0]->nr + (G == 2 ? mf[1]->nr : 0);
+    const int nlev = std::max(mf[0]->nlev, G == 2 ? mf[1]->nlev : 0);
+    const int base[2] = {0, mf[0]->nr};
+    const int KL = KLs, KU = KUs;
+    // group level l: member m's rows [a_m, a_m + w_m) (group-local)
+    auto lev = [&](int l, int m, int &am, int &wm) {
+      wm = 0;
+      am = base[m];
+      if (m >= G) return;
+      const uint16_t *lv = lvl_of(s + m);
+      if (l < mf[m]->nlev) {
+        am = base[m] + lv[l];
+        wm = lv[l + 1] - lv[l];
+      }
+    };
+    auto gw = [&](int l) {
+      int a0, w0, a1, w1;
+      lev(l, 0, a0, w0);
+      lev(l, 1, a1, w1);
+      return w0 + w1;
+    };
     {
       const int64_t vs = 8;
       auto fblob = [&](int w) { return al16(2 * (int64_t)KL * w) + al16(vs * (int64_t)KL * w); };
@@ -687,38 +726,98 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       // pieces: {first level, bytes}
       std::vector<std::pair<int, int64_t>> fp, bp;
       for (int l = 0; l < nlev; ++l) {
-        const int64_t sz = fblob(flvl[l + 1] - flvl[l]);
+        const int64_t sz = fblob(gw(l));
         if (fp.empty() || fp.back().second + sz > kStreamPiece) fp.push_back({l, 0});
         fp.back().second += sz;
       }
       for (int l = nlev - 1; l >= 0; --l) {
-        const int64_t sz = bblob(flvl[l + 1] - flvl[l]);
+        const int64_t sz = bblob(gw(l));
         if (bp.empty() || bp.back().second + sz > kStreamPiece) bp.push_back({l, 0});
         bp.back().second += sz;
       }
       for (auto &q : fp) q.second = std::max<int64_t>(q.second, 16);
       for (auto &q : bp) q.second = std::max<int64_t>(q.second, 16);
       const int np = (int)(fp.size() + bp.size());
-      const int64_t lvl_bytes = (2 * (int64_t)(nlev + 2) + 3) & ~(int64_t)3;
+      const int64_t lvl_bytes = 8 * (int64_t)nlev;  // 4 uint16 per level
       const int64_t hdr = al16(lvl_bytes + 4 * (2 + 3 * (int64_t)np));
       int64_t total = hdr, max_piece = 16;
       for (auto &q : fp) total += q.second, max_piece = std::max(max_piece, q.second);
       for (auto &q : bp) total += q.second, max_piece = std::max(max_piece, q.second);
       PG_CHECK_ARG(soff + total < ((int64_t)1 << 31), "ILU(0) stream too large");
-      a.smeta64[s] = StreamMeta{f.r0, nr, nlev, KL, KU, (int32_t)soff,
-                                (int32_t)hdr, (int32_t)max_piece, 0, 0, 0, 0};
+      StreamMeta sm{};
+      sm.r0 = mf[0]->r0;
+      sm.nr = nr;
+      sm.nlev = nlev;
+      sm.KL = KL;
+      sm.KU = KU;
+      sm.rec_off = (int32_t)soff;
+      sm.hdr_bytes = (int32_t)hdr;
+      sm.max_piece = (int32_t)max_piece;
+      sm.sub0 = s;
+      sm.nsub = G;
+      sm.nr0 = mf[0]->nr;
       std::vector<uint8_t> &buf = a.srec64;
       buf.resize(soff + total, 0);
-      uint8_t *base = buf.data() + soff;
-      std::memcpy(base, flvl, 2 * (size_t)(nlev + 2));
-      int32_t *ints = reinterpret_cast<int32_t *>(base + lvl_bytes);
+      uint8_t *recb = buf.data() + soff;
+      uint16_t *hl = reinterpret_cast<uint16_t *>(recb);
+      for (int l = 0; l < nlev; ++l) {
+        int a0, w0, a1, w1;
+        lev(l, 0, a0, w0);
+        lev(l, 1, a1, w1);
+        hl[4 * l] = (uint16_t)a0;
+        hl[4 * l + 1] = (uint16_t)w0;
+        hl[4 * l + 2] = (uint16_t)a1;
+        hl[4 * l + 3] = (uint16_t)w1;
+      }
+      int32_t *ints = reinterpret_cast<int32_t *>(recb + lvl_bytes);
       ints[0] = (int32_t)fp.size();
       ints[1] = (int32_t)bp.size();
       int64_t off = hdr;
-      auto emit_values = [&](int64_t byte_off, int64_t slot) {
-        // byte_off is relative to this record; slot indexes the factor
+      auto emit_values = [&](int m, int64_t byte_off, int64_t slot) {
+        // byte_off is relative to this record; slot indexes member m's
+        // factor record
+        const int64_t fsrc0 = (mf[m]->rec_off + mf[m]->val_off) / 8;
         a.pack_src.push_back((int32_t)(fsrc0 + slot));
         a.pack_dst64.push_back((int32_t)((soff + byte_off) / vs));
+      };
+      // lane t of a group level: member m and its member-local row
+      auto lane_row = [&](int l, int t, int &m, int &row) {
+        int a0, w0, a1, w1;
+        lev(l, 0, a0, w0);
+        lev(l, 1, a1, w1);
+        m = t < w0 ? 0 : 1;
+        row = (m == 0 ? a0 + t : a1 + (t - w0)) - base[m];
+      };
+      auto emit_level = [&](int l, bool fwd) {
+        const int w = gw(l);
+        const int KS = fwd ? KL : KU;
+        uint16_t *cc = reinterpret_cast<uint16_t *>(recb + off);
+        const int64_t voff = off + al16(2 * (int64_t)KS * w);
+        const int64_t doff = voff + al16(vs * (int64_t)KS * w);
+        for (int k = 0; k < KS; ++k)
+          for (int t = 0; t < w; ++t) {
+            int m, row;
+            lane_row(l, t, m, row);
+            const SubMeta &f = *mf[m];
+            const int fKL = f.KL, fKU = f.K - f.KL;
+            const uint16_t *fcols = reinterpret_cast<const uint16_t *>(
+                a.rec64.data() + f.rec_off + f.col_off);
+            const int kk = fwd ? k : fKL + k;
+            const bool used = fwd ? k < fKL : k < fKU;
+            const int64_t slot = (int64_t)kk * f.nr + row;
+            const uint16_t col = used ? fcols[slot] : kPadCol;
+            // an unused slot points at the zero entry z[nr]
+            cc[k * w + t] = col == kPadCol ? (uint16_t)nr : (uint16_t)(col + base[m]);
+            if (col != kPadCol) emit_values(m, voff + vs * ((int64_t)k * w + t), slot);
+          }
+        if (!fwd)
+          for (int t = 0; t < w; ++t) {
+            int m, row;
+            lane_row(l, t, m, row);
+            const SubMeta &f = *mf[m];
+            emit_values(m, doff + vs * t, (int64_t)f.K * f.nr + row);
+          }
+        off += fwd ? fblob(w) : bblob(w);
       };
       int t = 0;
       for (size_t q = 0; q < fp.size(); ++q, ++t) {
@@ -727,20 +826,7 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
         ints[2 + 3 * t] = l0;
         ints[3 + 3 * t] = (int32_t)off;
         ints[4 + 3 * t] = (int32_t)fp[q].second;
-        for (int l = l0; l < l1; ++l) {
-          const int ra = flvl[l], w = flvl[l + 1] - ra;
-          uint16_t *cc = reinterpret_cast<uint16_t *>(base + off);
-          const int64_t voff = off + al16(2 * (int64_t)KL * w);
-          for (int k = 0; k < KL; ++k)
-            for (int j = 0; j < w; ++j) {
-              const int64_t slot = (int64_t)k * nr + ra + j;
-              const uint16_t col = k < fKL ? fcols[slot] : kPadCol;
-              // an unused slot points at the zero entry z[nr]
-              cc[k * w + j] = col == kPadCol ? (uint16_t)nr : col;
-              if (col != kPadCol) emit_values(voff + vs * ((int64_t)k * w + j), slot);
-            }
-          off += fblob(w);
-        }
+        for (int l = l0; l < l1; ++l) emit_level(l, true);
       }
       for (size_t q = 0; q < bp.size(); ++q, ++t) {
         const int lhi = bp[q].first;
@@ -748,35 +834,22 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
         ints[2 + 3 * t] = lhi;
         ints[3 + 3 * t] = (int32_t)off;
         ints[4 + 3 * t] = (int32_t)bp[q].second;
-        for (int l = lhi; l >= llo; --l) {
-          const int ra = flvl[l], w = flvl[l + 1] - ra;
-          uint16_t *cc = reinterpret_cast<uint16_t *>(base + off);
-          const int64_t voff = off + al16(2 * (int64_t)KU * w);
-          const int64_t doff = voff + al16(vs * (int64_t)KU * w);
-          for (int k = 0; k < KU; ++k)
-            for (int j = 0; j < w; ++j) {
-              const int64_t slot = (int64_t)(fKL + k) * nr + ra + j;
-              const uint16_t col = k < fKU ? fcols[slot] : kPadCol;
-              cc[k * w + j] = col == kPadCol ? (uint16_t)nr : col;
-              if (col != kPadCol) emit_values(voff + vs * ((int64_t)k * w + j), slot);
-            }
-          for (int j = 0; j < w; ++j)
-            emit_values(doff + vs * j, (int64_t)(fKL + fKU) * nr + ra + j);
-          off += bblob(w);
-        }
+        for (int l = lhi; l >= llo; --l) emit_level(l, false);
       }
-      StreamMeta &sm = a.smeta64[s];
       sm.p0_off = ints[3];
       sm.p0_bytes = ints[4];
       if (np > 1) {
         sm.p1_off = ints[6];
         sm.p1_bytes = ints[7];
       }
+      a.smeta64.push_back(sm);
       soff += total;
       const size_t need = (size_t)hdr + 2 * (size_t)max_piece + (size_t)al16(vs * (int64_t)(nr + 1));
       a.ssmem64 = std::max(a.ssmem64, need);
     }
+    s += G;
   }
+  a.n_grp = (int)a.smeta64.size();
 
   // 9. step stream for the float-float sweep of the mixed-precision solver
   //    (kernels.cuh StepMeta), when no row has more than 3 L or 3 U

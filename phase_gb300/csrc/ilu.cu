@@ -181,6 +181,25 @@ __device__ __forceinline__ void sweep_level_dd(float2 *zs, int a, int w,
   }
 }
 
+// A level of a sweep group: rows [a0, a0+w0) of its first subdomain and
+// [a1, a1+w1) of its second (group-local); lane t sweeps row(t)
+struct GroupLevel {
+  int a0 = 0, w0 = 0, a1 = 0, w1 = 0;
+  __device__ __forceinline__ int w() const { return w0 + w1; }
+  __device__ __forceinline__ int row(int t) const {
+    return t < w0 ? a0 + t : a1 + (t - w0);
+  }
+};
+__device__ __forceinline__ GroupLevel group_level(const uint2 *L, int l) {
+  const uint2 x = L[l];
+  GroupLevel g;
+  g.a0 = (int)(x.x & 0xFFFFu);
+  g.w0 = (int)(x.x >> 16);
+  g.a1 = (int)(x.y & 0xFFFFu);
+  g.w1 = (int)(x.y >> 16);
+  return g;
+}
+
 // One lane's row of a level (lane < w), held in registers: the KT column
 // slots, their weights and, for the backward sweep, 1/u_ii.  Record layout
 // of a level of width w: columns (uint16, slot-major, 16-byte padded), the
@@ -337,10 +356,11 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
   }
   {
     // input staging, four rows per lane in flight; with a coarse space the
-    // subdomain's input sum (lane order, then a fixed butterfly)
+    // input sum of each subdomain of the group (lane order, then a fixed
+    // butterfly)
     constexpr int U = 4;
     const MT zero = AR::zero();
-    typename AR::Sum part = AR::sum_init();
+    typename AR::Sum part0 = AR::sum_init(), part1 = AR::sum_init();
     for (int i0 = lane; i0 < nr; i0 += 32 * U) {
       MT ri[U], pi[U], vi[U];
 #pragma unroll
@@ -359,13 +379,17 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
           const MT val = AR::combine(MODE, ri[u], pi[u], vi[u], sc);
           if (MODE != 0) pv[m.r0 + i] = val;
           zs[i] = val;
-          if (csum) AR::sum_add(part, val);
+          if (csum) AR::sum_add(i < m.nr0 ? part0 : part1, val);
         }
       }
     }
     if (csum) {
-      const float2 t = AR::sum_warp(part);
-      if (lane == 0) csum[blockIdx.x] = t;
+      const float2 t0 = AR::sum_warp(part0);
+      if (lane == 0) csum[m.sub0] = t0;
+      if (m.nsub > 1) {
+        const float2 t1 = AR::sum_warp(part1);
+        if (lane == 0) csum[m.sub0 + 1] = t1;
+      }
     }
   }
   if (lane == 0) zs[nr] = AR::zero();
@@ -376,9 +400,8 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
     if (m.p1_bytes > 0) mbar_wait_bounded(&bar[1], nullptr, 0u);
     return;
   }
-  const uint16_t *lvl = reinterpret_cast<const uint16_t *>(hdr);
-  const int32_t *ints =
-      reinterpret_cast<const int32_t *>(hdr + ((2 * (nlev + 2) + 3) & ~3));
+  const uint2 *L = reinterpret_cast<const uint2 *>(hdr);  // lev[nlev][4]
+  const int32_t *ints = reinterpret_cast<const int32_t *>(hdr + 8 * nlev);
   const int nF = ints[0], nB = ints[1], P = nF + nB;
   const int32_t *tab = ints + 2;
   constexpr int vs = (int)sizeof(MT);
@@ -397,27 +420,33 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
       // Software-pipelined walk: a level's columns, weights (and 1/u_ii)
       // are read from the piece into registers while the level before it
       // is swept, so each level waits only for its z operands.  Levels
-      // wider than a warp take the generic loop.
+      // wider than a warp (single-subdomain groups only) take the generic
+      // loop.
       if (j < nF) {
         const int l0 = tab[3 * j];
         const int l1 = j + 1 < nF ? tab[3 * (j + 1)] : nlev;
-        int a = lvl[l0], w = lvl[l0 + 1] - a;
+        GroupLevel cl = group_level(L, l0);
+        int w = cl.w();
         LevelRegs<MT, KLT> cur, nxt;
         cur.template load<false>(pc, w, lane);
         for (int l = l0; l < l1; ++l) {
           const int ca = al16(2 * KLT * w);
           const uint8_t *pn = pc + ca + al16(vs * KLT * w);
-          const int wn = l + 1 < l1 ? lvl[l + 2] - lvl[l + 1] : 0;
+          const GroupLevel nl = l + 1 < l1 ? group_level(L, l + 1) : GroupLevel{};
+          const int wn = nl.w();
           nxt.template load<false>(pn, wn, lane);
           if (w <= 32) {
-            if (lane < w) zs[a + lane] = cur.template sweep<AR, false>(zs, zs[a + lane]);
+            if (lane < w) {
+              const int row = cl.row(lane);
+              zs[row] = cur.template sweep<AR, false>(zs, zs[row]);
+            }
           } else {
-            AR::template level<KLT>(zs, a, w, KLT,
+            AR::template level<KLT>(zs, cl.a0, cl.w0, KLT,
                                      reinterpret_cast<const uint16_t *>(pc),
                                      reinterpret_cast<const MT *>(pc + ca),
                                      (const MT *)nullptr, lane);
           }
-          a += w;
+          cl = nl;
           w = wn;
           pc = pn;
           cur = nxt;
@@ -426,25 +455,29 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
       } else {
         const int lhi = tab[3 * j];
         const int llo = j + 1 < P ? tab[3 * (j + 1)] + 1 : 0;
-        int b = lvl[lhi + 1], w = b - lvl[lhi];
+        GroupLevel cl = group_level(L, lhi);
+        int w = cl.w();
         LevelRegs<MT, KUT> cur, nxt;
         cur.template load<true>(pc, w, lane);
         for (int l = lhi; l >= llo; --l) {
-          const int a = b - w;
           const int ca = al16(2 * KUT * w), va = al16(vs * KUT * w);
           const uint8_t *pn = pc + ca + va + al16(vs * w);
-          const int wn = l - 1 >= llo ? a - lvl[l - 1] : 0;
+          const GroupLevel nl = l - 1 >= llo ? group_level(L, l - 1) : GroupLevel{};
+          const int wn = nl.w();
           nxt.template load<true>(pn, wn, lane);
           if (w <= 32) {
-            if (lane < w) zs[a + lane] = cur.template sweep<AR, true>(zs, zs[a + lane]);
+            if (lane < w) {
+              const int row = cl.row(lane);
+              zs[row] = cur.template sweep<AR, true>(zs, zs[row]);
+            }
           } else {
-            AR::template level<KUT>(zs, a, w, KUT,
+            AR::template level<KUT>(zs, cl.a0, cl.w0, KUT,
                                      reinterpret_cast<const uint16_t *>(pc),
                                      reinterpret_cast<const MT *>(pc + ca),
                                      reinterpret_cast<const MT *>(pc + ca + va),
                                      lane);
           }
-          b = a;
+          cl = nl;
           w = wn;
           pc = pn;
           cur = nxt;
@@ -452,25 +485,25 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
         }
       }
     } else if (j < nF) {
+      // generic slot counts: single-subdomain groups (w1 = 0)
       const int l1 = j + 1 < nF ? tab[3 * (j + 1)] : nlev;
-      int a = lvl[tab[3 * j]];
       for (int l = tab[3 * j]; l < l1; ++l) {
-        const int b = lvl[l + 1], w = b - a;
+        const GroupLevel cl = group_level(L, l);
+        const int a = cl.a0, w = cl.w0;
         const int ca = al16(2 * KL * w);
         AR::template level<KLT>(zs, a, w, KL,
                                  reinterpret_cast<const uint16_t *>(pc),
                                  reinterpret_cast<const MT *>(pc + ca),
                                  (const MT *)nullptr, lane);
         pc += ca + al16(vs * KL * w);
-        a = b;
         __syncwarp();
       }
     } else {
       const int lhi = tab[3 * j];
       const int llo = j + 1 < P ? tab[3 * (j + 1)] + 1 : 0;
-      int b = lvl[lhi + 1];
       for (int l = lhi; l >= llo; --l) {
-        const int a = lvl[l], w = b - a;
+        const GroupLevel cl = group_level(L, l);
+        const int a = cl.a0, w = cl.w0;
         const int ca = al16(2 * KU * w), va = al16(vs * KU * w);
         AR::template level<KUT>(zs, a, w, KU,
                                  reinterpret_cast<const uint16_t *>(pc),
@@ -478,7 +511,6 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
                                  reinterpret_cast<const MT *>(pc + ca + va),
                                  lane);
         pc += ca + va + al16(vs * w);
-        b = a;
         __syncwarp();
       }
     }
@@ -674,7 +706,7 @@ void launch_stream(const SolverDev &d, size_t smem, const uint8_t *rec,
                          (int)smem);
     attr = smem;
   }
-  k_ilu0_apply_stream<AR, MODE, KLT, KUT><<<d.n_sub, 32, smem, st>>>(
+  k_ilu0_apply_stream<AR, MODE, KLT, KUT><<<d.n_grp, 32, smem, st>>>(
       d.smeta64, rec, r, pv, v, z, sc, d.sub_sys, d.err, d.csum);
 }
 

@@ -201,8 +201,10 @@ struct Analysis {
   std::vector<int32_t> rec_src;            // value slot -> permuted entry
   size_t smem64 = 0;                       // max record + vector bytes
   int max_kl = 0, max_ku = 0;              // widest L / U part of a row
-  // streaming records for the apply kernel (kernels.cuh StreamMeta)
+  // streaming records for the apply kernel (kernels.cuh StreamMeta), one
+  // per sweep group
   std::vector<StreamMeta> smeta64;
+  int n_grp = 0;
   std::vector<uint8_t> srec64;
   std::vector<int32_t> pack_src, pack_dst64;    // FP64 stream <- factor
   size_t ssmem64 = 0;

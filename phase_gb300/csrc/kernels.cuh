@@ -115,21 +115,28 @@ struct SubMeta {
 };
 constexpr uint16_t kPadCol = 0xFFFF;
 
-// Streaming form of a subdomain's factor for the apply kernel: the levels'
-// L data (ascending) and U data + 1/u_ii (descending) are cut into
+// Streaming form of a sweep group's factor for the apply kernel (a group is
+// one subdomain, or two whose levels fit side by side in a warp): the
+// levels' L data (ascending) and U data + 1/u_ii (descending) are cut into
 // level-aligned pieces that TMA double-buffers through shared memory.
-//   header: uint16 lvl[nlev+2] (4-byte padded), int32 nF, nB,
-//           int32 table[nF+nB][3] = {level, byte offset, bytes}
-//           (forward pieces start at `level`; backward pieces start at
-//           `level` and run downwards)
+//   header: uint16 lev[nlev][4] = {a0, w0, a1, w1}: level l is group-local
+//           rows [a0, a0+w0) of the first subdomain and [a1, a1+w1) of the
+//           second (w1 = 0 for a single subdomain); lane t < w0 sweeps row
+//           a0+t, lane w0 <= t < w0+w1 row a1+t-w0;
+//           int32 nF, nB, int32 table[nF+nB][3] = {level, byte offset,
+//           bytes} (forward pieces start at `level`; backward pieces start
+//           at `level` and run downwards)
 //   level blob (forward):  uint16 cols[KL][w] | MT vals[KL][w]
 //   level blob (backward): uint16 cols[KU][w] | MT vals[KU][w] | MT dinv[w]
-//   every array padded to 16 bytes; w = rows of the level; an unused slot
-//   has column nr (the kernel keeps z[nr] = 0) and value 0
+//   every array padded to 16 bytes; w = w0 + w1; columns are group-local;
+//   an unused slot has column nr (the kernel keeps z[nr] = 0) and value 0
 struct StreamMeta {
   int32_t r0, nr, nlev, KL, KU, rec_off, hdr_bytes, max_piece;
   // the first two pieces (offsets in the record), loaded at kernel start
   int32_t p0_off, p0_bytes, p1_off, p1_bytes;
+  // the group's subdomains: sub0 .. sub0+nsub-1 (nsub 1 or 2), the first
+  // holding group-local rows [0, nr0)
+  int32_t sub0, nsub, nr0, pad0;
 };
 
 // Step form of the factor for the float-float sweep of the mixed solver,
@@ -160,6 +167,7 @@ struct SolverDev {
   int max_kl, max_ku;      // widest L / U part of any row
   // FP64 streaming records and the factor -> stream value map
   const StreamMeta *smeta64;
+  int n_grp;  // stream records (sweep groups of one or two subdomains)
   uint8_t *srec64;
   const int32_t *pack_src, *pack_dst64;
   int n_pack;

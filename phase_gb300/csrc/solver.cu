@@ -154,6 +154,7 @@ struct pg_solver {
     // vector in shared memory; otherwise the global-memory sweep is used
     d.smem64 = a.ssmem64 <= kMaxApplySmem ? a.ssmem64 : 0;
     d.smeta64 = smeta64.p;
+    d.n_grp = a.n_grp;
     d.srec64 = srec64.p;
     d.pack_src = pack_src.p;
     d.pack_dst64 = pack_dst64.p;
@@ -193,6 +194,18 @@ int red_grid_cap() {
 }
 
 constexpr int kMaxCoarseK = 2048;  // the coarse matrix is K x K, dense
+
+// Schwarz subdomain size for the analysis: the configured one, else 1024
+// rows for the one-level preconditioner and 512 with a coarse space (the
+// coarse correction carries the global coupling, so smaller, faster ILU(0)
+// blocks pay), enlarged so the coarse matrix stays within kMaxCoarseK;
+// -1 (one subdomain) for the other preconditioners
+int subdomain_rows_for(const pg_solver_cfg &c, int64_t n) {
+  if (c.precond != PG_PREC_ILU0) return -1;
+  if (c.subdomain_rows) return c.subdomain_rows;
+  if (!c.coarse) return 1024;
+  return (int)std::max<int64_t>(512, (n + kMaxCoarseK - 1) / kMaxCoarseK);
+}
 
 int upload_analysis(pg_solver *s) {
   const Analysis &a = s->a;
@@ -780,7 +793,7 @@ extern "C" int pg_solver_set_csr(pg_solver *s, const int32_t *row_ptr,
       hci = h_ci.data();
     }
     const bool xy = (int64_t)s->row_x.size() == n;
-    int rc = analyse(n, hrp, hci, s->cfg.precond == PG_PREC_ILU0 ? s->cfg.subdomain_rows : -1, s->a,
+    int rc = analyse(n, hrp, hci, subdomain_rows_for(s->cfg, n), s->a,
                      nullptr, xy ? s->row_x.data() : nullptr,
                      xy ? s->row_y.data() : nullptr);
     if (rc) return rc;
@@ -812,7 +825,7 @@ extern "C" int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e) {
     const pg::HostMesh &hm = e->mesh->h;
     const bool xy = e->p.n == hm.n_cells;
     int rc = analyse(e->p.n, e->p.row_ptr.data(), e->p.col_ind.data(),
-                     s->cfg.precond == PG_PREC_ILU0 ? s->cfg.subdomain_rows : -1, s->a,
+                     subdomain_rows_for(s->cfg, e->p.n), s->a,
                      nullptr, xy ? hm.cx.data() : nullptr,
                      xy ? hm.cy.data() : nullptr);
     if (rc) return rc;

@@ -160,13 +160,23 @@ def _bubble_system(pg, nx, ny):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed-steps", "mixed-blobs"])
-@pytest.mark.parametrize("mesh", ["bubble", "tri"])
+@pytest.mark.parametrize("mesh", ["bubble", "tri", "bubble-xy"])
 def test_ilu_apply_matches_oracle(pg, oracle, precision, mesh):
     """The Schwarz ILU(0) sweeps alone, z = M^-1 r, against the oracle's
     factor and triangular solves on the device's own partition.  FP64:
     1e-12 relative (the factor's FP64 operation order differs); float-float
-    factors and sweeps (about 48-bit arithmetic): 1e-10 relative."""
-    if mesh == "bubble":
+    factors and sweeps (about 48-bit arithmetic): 1e-10 relative.
+    bubble-xy: subdomains cut by cell-centre bisection into 8 x 16 blocks,
+    swept two per warp."""
+    xy = None
+    if mesh == "bubble-xy":
+        w = workloads.rising_bubble(128, 96, seed=3)
+        m = pg.Mesh(w["nodes"], w["cptr"], w["cind"])
+        c = m.cells()
+        xy = np.stack([c["cx"], c["cy"]], axis=1)
+        rp, ci, v, rhs = _bubble_system(pg, 128, 96)
+        sub = 128
+    elif mesh == "bubble":
         rp, ci, v, rhs = _bubble_system(pg, 128, 96)
         sub = 1024
     else:
@@ -181,6 +191,8 @@ def test_ilu_apply_matches_oracle(pg, oracle, precision, mesh):
         precision=pg.FP64 if precision == "fp64" else pg.MIXED,
         mixed_sweep={"fp64": 0, "mixed-steps": 1, "mixed-blobs": 2}[precision])
     s.setRank(n)
+    if xy is not None:
+        s.set_row_coords(xy)
     s.set(rp, ci, v)
     part, nparts = s.partition()
     assert nparts > 4
