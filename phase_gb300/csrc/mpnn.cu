@@ -71,15 +71,58 @@ __global__ void k_round_bf16(int n, const float *__restrict__ src,
     dst[i] = __bfloat162float(__float2bfloat16(src[i]));
 }
 
-// r = b - A x, diag a_ii, edge weights e_ij = -a_ij / a_ii, per-cell sums
-// for the scales (double atomics: a handful of reductions per call)
-__global__ void k_prep(int n, const int32_t *__restrict__ rp,
-                       const int32_t *__restrict__ ci,
-                       const double *__restrict__ a,
-                       const double *__restrict__ b,
-                       const double *__restrict__ xp, float *__restrict__ r,
-                       float *__restrict__ diag, float *__restrict__ e,
-                       double *__restrict__ sums) {
+// per-block sums of four doubles (fixed order: warp butterfly, then warps in
+// order) written to part[blockIdx.x * 4 + k]; k_finish_sums adds the blocks'
+// partials in block order, so the scales are reproducible
+__device__ void block_sums4(const double (&s)[4], double *__restrict__ part) {
+  __shared__ double ws[4][kBlock / 32];
+  for (int k = 0; k < 4; ++k) {
+    double v = s[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) ws[k][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double t = 0.;
+    for (int w = 0; w < kBlock / 32; ++w) t += ws[threadIdx.x][w];
+    part[blockIdx.x * 4 + threadIdx.x] = t;
+  }
+}
+
+__global__ void k_finish_sums(int nblk, const double *__restrict__ part,
+                              double *__restrict__ sums) {
+  __shared__ double red[4][kBlock];
+  for (int k = 0; k < 4; ++k) {
+    double t = 0.;
+    for (int b = threadIdx.x; b < nblk; b += kBlock) t += part[b * 4 + k];
+    red[k][threadIdx.x] = t;
+  }
+  __syncthreads();
+  for (int h = kBlock / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h)
+      for (int k = 0; k < 4; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) sums[threadIdx.x] = red[threadIdx.x][0];
+}
+
+// log|d| for any finite double without FP64 log: frexp splits off the
+// binary exponent, FP32 log of the mantissa in [0.5, 1); log(1e-300) for 0
+__device__ __forceinline__ float log_abs(double d) {
+  if (d == 0.) return -690.7755f;
+  int ex;
+  const double m = frexp(fabs(d), &ex);
+  return logf((float)m) + (float)ex * 0.69314718f;
+}
+
+// r = b - A x, diag a_ii, edge weights e_ij = -a_ij / a_ii, and per-block
+// sums of x^2, b^2, (r/a_ii)^2, log|a_ii| for the feature scales
+__global__ void __launch_bounds__(kBlock)
+k_prep(int n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+       const double *__restrict__ a, const double *__restrict__ b,
+       const double *__restrict__ xp, float *__restrict__ r,
+       float *__restrict__ diag, float *__restrict__ e,
+       double *__restrict__ part) {
   double s[4] = {0., 0., 0., 0.};  // x^2, b^2, (r/a)^2, log|a|
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += gridDim.x * blockDim.x) {
@@ -91,35 +134,94 @@ __global__ void k_prep(int n, const int32_t *__restrict__ rp,
     const double ri = b[i] - ax;
     r[i] = (float)ri;
     diag[i] = (float)dii;
+    const double inv = dii != 0. ? 1. / dii : 0.;
     for (int k = rp[i]; k < rp[i + 1]; ++k)
-      e[k] = (ci[k] == i || dii == 0.) ? 0.f : (float)(-a[k] / dii);
+      e[k] = ci[k] == i ? 0.f : (float)(-a[k] * inv);
     s[0] += xp[i] * xp[i];
     s[1] += b[i] * b[i];
-    const double q = dii != 0. ? ri / dii : 0.;
+    const double q = ri * inv;
     s[2] += q * q;
-    s[3] += log(fabs(dii) + 1e-300);
+    s[3] += (double)log_abs(dii);
   }
-  for (int k = 0; k < 4; ++k) {
-    double v = s[k];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&sums[k], v);
+  block_sums4(s, part);
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_features(int n, const double *__restrict__ b, const double *__restrict__ xp,
+           const float *__restrict__ r, const float *__restrict__ diag,
+           const double *__restrict__ sums, float *__restrict__ f) {
+  __shared__ double sc[3];
+  if (threadIdx.x == 0) {
+    sc[0] = 1. / (sqrt(sums[0] / n) + 1e-300);
+    sc[1] = 1. / (sqrt(sums[1] / n) + 1e-300);
+    sc[2] = sums[3] / n;
+  }
+  __syncthreads();
+  const double isx = sc[0], isb = sc[1];
+  const float la = (float)sc[2];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    f[0 * n + i] = (float)(xp[i] * isx);
+    f[1 * n + i] = (float)(b[i] * isb);
+    f[2 * n + i] = (float)(r[i] * isb);
+    f[3 * n + i] = log_abs((double)diag[i]) - la;
   }
 }
 
-__global__ void k_features(int n, const double *__restrict__ b,
-                           const double *__restrict__ xp,
-                           const float *__restrict__ r,
-                           const float *__restrict__ diag,
-                           const double *__restrict__ sums,
-                           float *__restrict__ f) {
-  const double sx = sqrt(sums[0] / n) + 1e-300, sb = sqrt(sums[1] / n) + 1e-300;
-  const double la = sums[3] / n;
+// Forward dense layer: Y[h][i] = act(sum_k X[k][i] W[k][h] + bias[h])
+// (+ X[h][i] when RESID: the residual connection h_l + relu(...)), K inputs
+// from X1 (rows 0..KA-1) and X2 (the rest), W K x HO row-major.  Each thread
+// loads its inputs eight at a time (all eight loads in flight), the weights
+// come from shared memory as float4 over h; the products are accumulated in
+// the same order as k_dense, so results are identical.  Z (optional): the
+// pre-activations, for the backward pass.
+template <int K, int KA, int HO, bool RELU, bool RESID>
+__global__ void __launch_bounds__(kBlock, 2)
+k_dense_fwd(int n, const float *__restrict__ X1, const float *__restrict__ X2,
+            const float *__restrict__ W, const float *__restrict__ bias,
+            float *__restrict__ Y, float *__restrict__ Z) {
+  static_assert(HO % 4 == 0, "HO must be a multiple of 4");
+  __shared__ float4 w4[K * HO / 4];
+  __shared__ float bs[HO];
+  float *w = reinterpret_cast<float *>(w4);
+  for (int t = threadIdx.x; t < K * HO; t += blockDim.x) w[t] = W[t];
+  for (int t = threadIdx.x; t < HO; t += blockDim.x) bs[t] = bias ? bias[t] : 0.f;
+  __syncthreads();
+  constexpr int KC = K < 8 ? K : 8;  // inputs loaded together
+  static_assert(K % KC == 0, "K must be a multiple of the load chunk");
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += gridDim.x * blockDim.x) {
-    f[0 * n + i] = (float)(xp[i] / sx);
-    f[1 * n + i] = (float)(b[i] / sb);
-    f[2 * n + i] = (float)(r[i] / sb);
-    f[3 * n + i] = (float)(log(fabs((double)diag[i]) + 1e-300) - la);
+    float acc[HO];
+#pragma unroll
+    for (int h = 0; h < HO; ++h) acc[h] = bs[h];
+#pragma unroll 1
+    for (int k0 = 0; k0 < K; k0 += KC) {
+      float x[KC];
+#pragma unroll
+      for (int u = 0; u < KC; ++u) {
+        const int k = k0 + u;
+        x[u] = k < KA ? X1[(size_t)k * n + i] : X2[(size_t)(k - KA) * n + i];
+      }
+#pragma unroll
+      for (int u = 0; u < KC; ++u) {
+        const int k = k0 + u;
+#pragma unroll
+        for (int q = 0; q < HO / 4; ++q) {
+          const float4 wv = w4[k * (HO / 4) + q];
+          acc[4 * q + 0] = fmaf(x[u], wv.x, acc[4 * q + 0]);
+          acc[4 * q + 1] = fmaf(x[u], wv.y, acc[4 * q + 1]);
+          acc[4 * q + 2] = fmaf(x[u], wv.z, acc[4 * q + 2]);
+          acc[4 * q + 3] = fmaf(x[u], wv.w, acc[4 * q + 3]);
+        }
+      }
+    }
+#pragma unroll
+    for (int h = 0; h < HO; ++h) {
+      if (Z) Z[(size_t)h * n + i] = acc[h];
+      float v = RELU ? fmaxf(acc[h], 0.f) : acc[h];
+      if (RESID) v = X1[(size_t)h * n + i] + v;
+      Y[(size_t)h * n + i] = v;
+    }
   }
 }
 
@@ -284,15 +386,16 @@ __global__ void k_head(int n, const float *__restrict__ h3,
   }
 }
 
-// residual res = A g - b, error err = g - x*, and the loss sums
-__global__ void k_loss(int n, const int32_t *__restrict__ rp,
+// residual res = A g - b, error err = g - x*, and per-block loss sums
+// (k_finish_sums adds them into sums[4..7])
+__global__ void __launch_bounds__(kBlock) k_loss(int n, const int32_t *__restrict__ rp,
                        const int32_t *__restrict__ ci,
                        const double *__restrict__ a,
                        const double *__restrict__ b,
                        const double *__restrict__ g,
                        const double *__restrict__ xs,
                        const double *__restrict__ xp, double *__restrict__ res,
-                       double *__restrict__ err, double *__restrict__ sums) {
+                       double *__restrict__ err, double *__restrict__ part) {
   double s[4] = {0., 0., 0., 0.};  // |res|^2, |A xp - b|^2, |err|^2, |xp-x*|^2
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += gridDim.x * blockDim.x) {
@@ -312,11 +415,7 @@ __global__ void k_loss(int n, const int32_t *__restrict__ rp,
       s[3] += e0 * e0;
     }
   }
-  for (int k = 0; k < 4; ++k) {
-    double v = s[k];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&sums[4 + k], v);
-  }
+  block_sums4(s, part);
 }
 
 // d out_i = s_d (2 (A^T res)_i / R0 + 2 err_i / E0)
@@ -401,6 +500,7 @@ struct pg_mpnn {
   pg::DevBuf<float> h[L + 1], z[L + 1], q[L], msg[L];
   pg::DevBuf<float> dh, dh2, dz, dq, dmsg;
   pg::DevBuf<double> sums, xg, res, err, st_a, st_b, st_x, st_s;
+  pg::DevBuf<double> part;  // per-block partial sums (k_prep, k_loss)
   int step = 0;
   // inference captured as a CUDA graph for one (vals, b, x_prev) address
   // triple; the weights are read from pb at every replay
@@ -430,6 +530,7 @@ int ensure(pg_mpnn *net, bool training) {
   rs(net->e, net->nnz);
   rs(net->out, n);
   rs(net->sums, 16);
+  rs(net->part, 4 * (size_t)grid_of(n));
   rs(net->xg, n);
   for (int l = 0; l <= L; ++l) {
     rs(net->h[l], nh);
@@ -453,8 +554,10 @@ int ensure(pg_mpnn *net, bool training) {
   return PG_OK;
 }
 
-// forward pass; leaves activations for the backward pass
-int forward(pg_mpnn *net, const double *a, const double *b, const double *xp) {
+// forward pass; with `training` it keeps the pre-activations z for the
+// backward pass
+int forward(pg_mpnn *net, const double *a, const double *b, const double *xp,
+            bool training) {
   cudaStream_t st = pg::stream();
   const int n = (int)net->n;
   const int g = grid_of(n);
@@ -462,27 +565,26 @@ int forward(pg_mpnn *net, const double *a, const double *b, const double *xp) {
   const float *W = net->pb.p;
   PG_CUDA(cudaMemsetAsync(net->sums.p, 0, 16 * sizeof(double), st));
   k_prep<<<g, kBlock, 0, st>>>(n, net->rp.p, net->ci.p, a, b, xp, net->r.p,
-                               net->diag.p, net->e.p, net->sums.p);
+                               net->diag.p, net->e.p, net->part.p);
+  k_finish_sums<<<1, kBlock, 0, st>>>(g, net->part.p, net->sums.p);
   k_features<<<g, kBlock, 0, st>>>(n, b, xp, net->r.p, net->diag.p, net->sums.p,
                                    net->feat.p);
-  k_dense<F, H, true, false, false><<<g, kBlock, 0, st>>>(
-      n, net->feat.p, F, nullptr, W + Y.w0, W + Y.b0, net->h[0].p, net->z[0].p);
+  k_dense_fwd<F, F, H, true, false><<<g, kBlock, 0, st>>>(
+      n, net->feat.p, nullptr, W + Y.w0, W + Y.b0, net->h[0].p,
+      training ? net->z[0].p : nullptr);
   for (int l = 0; l < L; ++l) {
-    k_dense<H, H, false, false, false><<<g, kBlock, 0, st>>>(
-        n, net->h[l].p, H, nullptr, W + Y.P[l], W + Y.c[l], net->q[l].p, nullptr);
+    k_dense_fwd<H, H, H, false, false><<<g, kBlock, 0, st>>>(
+        n, net->h[l].p, nullptr, W + Y.P[l], W + Y.c[l], net->q[l].p, nullptr);
     k_message<<<g, kBlock, 0, st>>>(n, net->rp.p, net->ci.p, net->e.p,
                                     net->q[l].p, net->msg[l].p);
     // h_{l+1} = h_l + relu(U [h_l; m] + d)
-    PG_CUDA(cudaMemcpyAsync(net->h[l + 1].p, net->h[l].p,
-                            (size_t)H * n * sizeof(float),
-                            cudaMemcpyDeviceToDevice, st));
-    k_dense<2 * H, H, true, true, false><<<g, kBlock, 0, st>>>(
-        n, net->h[l].p, H, net->msg[l].p, W + Y.U[l], W + Y.d[l],
-        net->h[l + 1].p, net->z[l + 1].p);
+    k_dense_fwd<2 * H, H, H, true, true><<<g, kBlock, 0, st>>>(
+        n, net->h[l].p, net->msg[l].p, W + Y.U[l], W + Y.d[l],
+        net->h[l + 1].p, training ? net->z[l + 1].p : nullptr);
   }
   k_head<<<g, kBlock, 0, st>>>(n, net->h[L].p, W + Y.wo, xp, net->sums.p,
                                net->out.p, net->xg.p);
-  pg::count_launches(4 + 3 * L);
+  pg::count_launches(5 + 3 * L);
   PG_CUDA(cudaGetLastError());
   return PG_OK;
 }
@@ -597,12 +699,13 @@ extern "C" int pg_mpnn_predict(pg_mpnn *net, const double *vals,
   // forward + ||b - A g||^2: captured once per input address triple into a
   // CUDA graph and replayed
   auto record = [&]() -> int {
-    int r = forward(net, a, bb, xp);
+    int r = forward(net, a, bb, xp, false);
     if (r) return r;
     k_loss<<<grid_of(n), kBlock, 0, st>>>(n, net->rp.p, net->ci.p, a, bb,
                                          net->xg.p, nullptr, xp, net->res.p,
-                                         nullptr, net->sums.p);
-    count_launches(1);
+                                         nullptr, net->part.p);
+    k_finish_sums<<<1, kBlock, 0, st>>>(grid_of(n), net->part.p, net->sums.p + 4);
+    count_launches(2);
     return PG_OK;
   };
   if (!net->infer || net->inf_a != a || net->inf_b != bb || net->inf_x != xp) {
@@ -652,7 +755,7 @@ static int backward_pass(pg_mpnn *net, const double *vals, const double *b,
   if (!rc) rc = stage_in(b, net->n, ptr_kind, net->st_b, &bb);
   if (!rc) rc = stage_in(x_prev, net->n, ptr_kind, net->st_x, &xp);
   if (!rc) rc = stage_in(x_star, net->n, ptr_kind, net->st_s, &xs);
-  if (!rc) rc = forward(net, a, bb, xp);
+  if (!rc) rc = forward(net, a, bb, xp, true);
   if (rc) return rc;
   cudaStream_t st = stream();
   const int n = (int)net->n;
@@ -665,7 +768,9 @@ static int backward_pass(pg_mpnn *net, const double *vals, const double *b,
   int launches = 0;
   PG_CUDA(cudaMemsetAsync(G, 0, Y.total * sizeof(float), st));
   k_loss<<<g, kBlock, 0, st>>>(n, net->rp.p, net->ci.p, a, bb, net->xg.p, xs,
-                               xp, net->res.p, net->err.p, net->sums.p);
+                               xp, net->res.p, net->err.p, net->part.p);
+  k_finish_sums<<<1, kBlock, 0, st>>>(g, net->part.p, net->sums.p + 4);
+  ++launches;
   k_dout<<<g, kBlock, 0, st>>>(n, net->rp.p, net->ci.p, net->tr.p, a,
                                net->res.p, net->err.p, net->sums.p,
                                net->dout.p);
