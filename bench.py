@@ -19,7 +19,9 @@ its own previous solution as a time loop runs them:
                   (A, b, previous x), replaced by the zero guess when the
                   prediction's residual is not below ||b||
 
-Both stop at ||b - A x||_2 / ||b||_2 <= 1e-8 on the FP64 true residual.
+A third arm, float-float warm from its own previous x without the network
+(`mixed_prev_x_ms`), shows what the learned guess competes with.  All stop
+at ||b - A x||_2 / ||b||_2 <= 1e-8 on the FP64 true residual.
 One step = device assembly of fv::laplacian(dt/rho, p) == src::div(u*) +
 hand-over + (inference) + ILU(0) factorisation + BiCGStab, inputs resident
 in HBM; `value` is the learned+mixed ms per solve, `plain_fp64_ms` the
@@ -312,6 +314,20 @@ def run_sequence(args):
         sp.x_device(xp_p.data_ptr())
         return dict(sp.stats.as_dict())
 
+    xp_q = torch.zeros(n, dtype=torch.float64, device=dev)
+    sq = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
+                               precision=pg.MIXED,
+                               subdomain_rows=args.subdomain_rows,
+                               coarse=args.coarse)
+
+    def mixed_prev_step(t):
+        """Float-float solve warm from its own previous x (no network)."""
+        sq.set_eqn(seq.assemble(t))
+        sq.setGuess_device(xp_q.data_ptr())
+        sq.solve()
+        sq.x_device(xp_q.data_ptr())
+        return dict(sq.stats.as_dict())
+
     def learned_step(t):
         eqn = seq.assemble(t)
         v, r = eqn.device_values()
@@ -361,6 +377,11 @@ def run_sequence(args):
     clocks = ClockSampler(local)
     clocks.start()
     ms_p, st_p = timed(plain_step, steps)
+    # float-float arm warm from the previous x (what the network competes
+    # with)
+    for t in warm:
+        mixed_prev_step(t)
+    ms_q, st_q = timed(mixed_prev_step, steps)
     # learned+mixed arm (headline), with the launch count
     for t in warm:
         learned_step(t)
@@ -419,7 +440,7 @@ def run_sequence(args):
                "ms_per_iter": round(info["ms_per_iter"], 3)}
 
     converged = all(st["status"] == 0 and st["rel_residual"] <= 1e-8
-                    for st in st_m + st_p)
+                    for st in st_m + st_p + st_q)
     if rank == 0:
         mean = lambda xs: round(float(np.mean(xs)), 1)
         out = {
@@ -452,6 +473,11 @@ def run_sequence(args):
                            "iters": [s_["iters"] for s_ in st_p],
                            "rel_residual": [s_["rel_residual"] for s_ in st_p]},
             "speedup_vs_plain_fp64": round(plain_ms / ms, 3),
+            "mixed_prev_x_ms": round(sum(ms_q) / len(ms_q), 3),
+            "mixed_prev_x": {"ms": [round(x, 3) for x in ms_q],
+                             "iters": [s_["iters"] for s_ in st_q],
+                             "fp64_iters": [s_["fp64_iters"] for s_ in st_q],
+                             "rel_residual": [s_["rel_residual"] for s_ in st_q]},
             "plain_fp64_zero_guess": {"ms": round(zero["ms"], 3),
                                       "iters": zero["iters"],
                                       "rel_residual": zero["rel_residual"]},
