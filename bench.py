@@ -332,16 +332,20 @@ def run_sequence(args):
 
     def learned_step(t):
         eqn = seq.assemble(t)
+        # hand the system over first: the solver factors its preconditioner
+        # on a side stream while the network runs
+        sm.set_eqn(eqn)
         v, r = eqn.device_values()
         pg.synchronize()
         # b = -rhs_ in a fixed buffer, so the captured inference graph
         # (keyed on its input addresses) is replayed every step
         torch.neg(torch.as_tensor(guess._DeviceView(r, n), device=dev), out=b_buf)
-        torch.cuda.synchronize()
+        # torch's stream only: a device-wide sync would wait for the
+        # factorisation running beside the network
+        torch.cuda.current_stream().synchronize()
         rel = net.predict_device(v, b_buf.data_ptr(), xp_m.data_ptr(),
                                  g.data_ptr()) if have_w else float("inf")
         use = rel < 1.0
-        sm.set_eqn(eqn)
         sm.setGuess_device(g.data_ptr() if use else 0)
         sm.solve()
         sm.x_device(xp_m.data_ptr())

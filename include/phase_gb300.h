@@ -297,7 +297,10 @@ typedef struct {
                           iters); 0 otherwise */
   double rel_residual; /* true ||b - A x||_2 / ||b||_2 computed in FP64 */
   double ms;           /* device time of the solve (CUDA events) */
-  double setup_ms;     /* device time of the value permutation + ILU factor */
+  double setup_ms;     /* device time the solve spent on (or waiting for)
+                          the preconditioner factorisation; set_csr /
+                          set_eqn start it on a side stream, so work issued
+                          between the hand-over and the solve overlaps it */
 } pg_solve_stats;
 
 /* Defaults: tolerance 1e-8, max_iters 500, ILU(0) Schwarz, FP64. */

@@ -131,7 +131,20 @@ struct pg_solver {
     return c;
   }
 
+  // the factorisation of the last hand-over runs on `side` (started by
+  // set_eqn/set_csr) while the caller prepares the guess; solve waits on
+  // ev_fact
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_vals = nullptr, ev_fact = nullptr;
+  bool fact_pending = false;
+
   ~pg_solver() {
+    if (side) {
+      cudaStreamSynchronize(side);
+      cudaStreamDestroy(side);
+    }
+    if (ev_vals) cudaEventDestroy(ev_vals);
+    if (ev_fact) cudaEventDestroy(ev_fact);
     drop_graphs();
     if (sc_host) cudaFreeHost(sc_host);
     if (bad_host) cudaFreeHost(bad_host);
@@ -208,6 +221,10 @@ int subdomain_rows_for(const pg_solver_cfg &c, int64_t n) {
 }
 
 int upload_analysis(pg_solver *s) {
+  if (s->fact_pending) {  // buffers are about to be reallocated
+    PG_CUDA(cudaStreamSynchronize(s->side));
+    s->fact_pending = false;
+  }
   const Analysis &a = s->a;
   cudaError_t e = cudaSuccess;
   auto up = [&](auto &buf, const auto &vec) {
@@ -288,6 +305,18 @@ int ensure_host_state(pg_solver *s) {
   if (!s->diff_host) PG_CUDA(cudaMallocHost((void **)&s->diff_host, sizeof(unsigned)));
   for (auto &e : s->ev)
     if (!e) PG_CUDA(cudaEventCreate(&e));
+  if (!s->side) PG_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+  if (!s->ev_vals) PG_CUDA(cudaEventCreateWithFlags(&s->ev_vals, cudaEventDisableTiming));
+  if (!s->ev_fact) PG_CUDA(cudaEventCreateWithFlags(&s->ev_fact, cudaEventDisableTiming));
+  return PG_OK;
+}
+
+// The library stream waits for a factorisation still running on the side
+// stream (before anything on it reads or rewrites the values or factors).
+int join_factor(pg_solver *s) {
+  if (!s->fact_pending) return PG_OK;
+  PG_CUDA(cudaStreamWaitEvent(stream(), s->ev_fact, 0));
+  s->fact_pending = false;
   return PG_OK;
 }
 
@@ -634,8 +663,7 @@ int choose_dd_sweep(pg_solver *s) {
   return PG_OK;
 }
 
-int factor(pg_solver *s) {
-  cudaStream_t st = stream();
+int factor(pg_solver *s, cudaStream_t st) {
   const SolverDev d = s->dev();
   const bool dd = use_dd(s);
   if (s->cfg.precond == PG_PREC_ILU0) {
@@ -650,7 +678,23 @@ int factor(pg_solver *s) {
   if (dd) launch_dd_split(d.nnz, s->pvals.p, 1.0, s->pvals_dd.p, st);
   PG_CUDA(cudaGetLastError());
   if (dd && s->cfg.precond == PG_PREC_ILU0 && s->dd_stream < 0)
-    return choose_dd_sweep(s);
+    return choose_dd_sweep(s);  // library stream only (see start_factor)
+  return PG_OK;
+}
+
+// After a value hand-over: factor on the side stream, so the work the
+// caller issues next on the library stream (an initial-guess inference, a
+// right-hand side) overlaps it.  The first factorisation of a mixed solver
+// times its sweep forms and stays on the library stream.
+int start_factor(pg_solver *s) {
+  if (use_dd(s) && s->cfg.precond == PG_PREC_ILU0 && s->dd_stream < 0)
+    return PG_OK;
+  PG_CUDA(cudaEventRecord(s->ev_vals, stream()));
+  PG_CUDA(cudaStreamWaitEvent(s->side, s->ev_vals, 0));
+  int rc = factor(s, s->side);
+  if (rc) return rc;
+  PG_CUDA(cudaEventRecord(s->ev_fact, s->side));
+  s->fact_pending = true;
   return PG_OK;
 }
 
@@ -803,11 +847,13 @@ extern "C" int pg_solver_set_csr(pg_solver *s, const int32_t *row_ptr,
     PG_CUDA(s->raw_ci.upload(hci, n_src));
     s->eqn_pattern = 0;
   }
+  int rj = join_factor(s);  // a pending factorisation still reads pvals
+  if (rj) return rj;
   launch_permute_values((int)s->a.nnz, s->psrc.p, dv, s->pvals.p,
                         (int)s->a.dup_dst.size(), s->dup_dst.p, s->dup_src.p, st);
   PG_CUDA(cudaGetLastError());
   s->have_vals = true;
-  return PG_OK;
+  return start_factor(s);
 }
 
 extern "C" int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e) {
@@ -833,6 +879,8 @@ extern "C" int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e) {
     if (rc) return rc;
     s->eqn_pattern = e->pattern_id;
   }
+  int rj = join_factor(s);  // a pending factorisation still reads pvals
+  if (rj) return rj;
   launch_permute_values((int)s->a.nnz, s->psrc.p, e->vals.p, s->pvals.p,
                         (int)s->a.dup_dst.size(), s->dup_dst.p, s->dup_src.p, st);
   // the solver receives -rhs_ (FiniteVolumeEquation.tpp:179)
@@ -840,7 +888,7 @@ extern "C" int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e) {
   PG_CUDA(cudaGetLastError());
   s->have_vals = true;
   s->have_rhs = true;
-  return PG_OK;
+  return start_factor(s);
 }
 
 extern "C" int pg_solver_set_rhs(pg_solver *s, const double *rhs, int ptr_kind) {
@@ -884,7 +932,8 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
   const int64_t n = s->a.n;
   if (!s->have_x) PG_CUDA(cudaMemsetAsync(s->x.p, 0, n * sizeof(double), st));
   PG_CUDA(cudaEventRecord(s->ev[0], st));
-  int rc = factor(s);
+  // the factorisation started at the hand-over, or now
+  int rc = s->fact_pending ? join_factor(s) : factor(s, st);
   if (rc) return rc;
   PG_CUDA(cudaEventRecord(s->ev[1], st));
   if (s->cfg.precond == PG_PREC_ILU0) {
@@ -966,6 +1015,8 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
   PG_CHECK_ARG(s && ms && reps > 0, "pg_solver_profile: bad argument");
   PG_CHECK_ARG(s->analysed && s->have_vals && s->have_x,
                "pg_solver_profile: solve a system first");
+  int rj = join_factor(s);
+  if (rj) return rj;
   cudaStream_t st = stream();
   const SolverDev d = s->dev();
   const RedWork w = s->red();
@@ -1034,7 +1085,7 @@ extern "C" int pg_solver_apply_precond(pg_solver *s, const double *r,
                "pg_solver_apply_precond: set the matrix first");
   cudaStream_t st = stream();
   const int64_t n = s->a.n;
-  int rc = factor(s);
+  int rc = s->fact_pending ? join_factor(s) : factor(s, st);
   if (rc) return rc;
   const SolverDev d = s->dev();  // after factor(): the sweep form is chosen
   const double *dr = r;
@@ -1089,6 +1140,8 @@ extern "C" int pg_solver_partition(const pg_solver *s, int32_t *part,
 extern "C" int pg_solver_coarse_inverse(pg_solver *s, float *out, int *k) {
   PG_CHECK_ARG(s && s->analysed && s->coarse_on,
                "pg_solver_coarse_inverse: no coarse space");
+  int rj = join_factor(s);
+  if (rj) return rj;
   const size_t K = s->a.n_sub;
   if (k) *k = (int)K;
   if (out) {
