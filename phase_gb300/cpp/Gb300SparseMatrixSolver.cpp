@@ -36,6 +36,14 @@ SparseMatrixSolver::Type Gb300SparseMatrixSolver::type() const {
 void Gb300SparseMatrixSolver::setRank(int rank) {
   rank_ = rank;
   check(pg_solver_set_rank(solver_, rank), "setRank");
+  if (rank > 0 && xy_.size() == 2 * (size_t)rank)
+    check(pg_solver_set_row_coords(solver_, xy_.data()), "setRank");
+}
+
+void Gb300SparseMatrixSolver::setRowCoordinates(const std::vector<Scalar> &xy) {
+  xy_ = xy;
+  if (rank_ > 0 && xy_.size() == 2 * (size_t)rank_)
+    check(pg_solver_set_row_coords(solver_, xy_.data()), "setRowCoordinates");
 }
 
 void Gb300SparseMatrixSolver::setRank(int rowRank, int colRank) {

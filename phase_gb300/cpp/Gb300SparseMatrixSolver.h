@@ -27,8 +27,14 @@ class Gb300SparseMatrixSolver : public SparseMatrixSolver {
   Scalar x(Index idx) const override;
   // keys: tolerance (1e-8), maxIters (500), preconditioner
   // (ilu0 | jacobi | none), subdomainRows (0 = default, -1 = one subdomain),
-  // precision (fp64 | mixed)
+  // precision (fp64 | mixed), mixedSweep (0 | 1 | 2), coarseSpace (0 | 1:
+  // two-level Schwarz with a coarse correction)
   void setup(const boost::property_tree::ptree &parameters) override;
+  // Optional geometry hint (no SparseMatrixSolver counterpart): a point per
+  // row, xy[2 * rank] interleaved (the cell centroids), so the Schwarz
+  // subdomains are cut by coordinate bisection.  Kept across setRank calls
+  // of the same rank.
+  void setRowCoordinates(const std::vector<Scalar> &xy);
   int nIters() const override;
   Scalar error() const override;
   bool supportsMPI() const override { return false; }
@@ -42,4 +48,5 @@ class Gb300SparseMatrixSolver : public SparseMatrixSolver {
   pg_solve_stats stats_{};
   int rank_ = 0;
   std::vector<Scalar> x_;
+  std::vector<Scalar> xy_;  // setRowCoordinates
 };

@@ -763,17 +763,19 @@ extern "C" int pg_solver_set_rank(pg_solver *s, int64_t n) {
 
 extern "C" int pg_solver_set_row_coords(pg_solver *s, const double *xy) {
   PG_CHECK_ARG(s, "pg_solver_set_row_coords: NULL solver");
-  s->row_x.clear();
-  s->row_y.clear();
+  std::vector<double> nx, ny;
   if (xy) {
     PG_CHECK_ARG(s->rank > 0, "pg_solver_set_row_coords: set_rank first");
-    s->row_x.resize(s->rank);
-    s->row_y.resize(s->rank);
+    nx.resize(s->rank);
+    ny.resize(s->rank);
     for (int64_t i = 0; i < s->rank; ++i) {
-      s->row_x[i] = xy[2 * i];
-      s->row_y[i] = xy[2 * i + 1];
+      nx[i] = xy[2 * i];
+      ny[i] = xy[2 * i + 1];
     }
   }
+  if (nx == s->row_x && ny == s->row_y) return PG_OK;  // unchanged
+  s->row_x.swap(nx);
+  s->row_y.swap(ny);
   s->analysed = false;  // the next set_csr re-cuts the subdomains
   return PG_OK;
 }
