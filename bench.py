@@ -593,7 +593,7 @@ def run_batch(args):
                    u_face=w["u"])
         systems.append((m, e))
     eqns = [e for _, e in systems]
-    b = pg.BatchSolver(tolerance=1e-8, max_iters=20000)
+    b = pg.BatchSolver(tolerance=1e-8, max_iters=20000, coarse=args.coarse)
     b.set_eqns(eqns)
     setup_s = time.perf_counter() - t_setup
     for _ in range(max(1, args.warmup)):
@@ -661,6 +661,9 @@ def run_batch(args):
                                "systems, quad meshes 2k-200k cells "
                                "(log-uniform), one cylinder r in [0.1, 0.5] each",
                    "total_cells": int(sum(n_cells)), "tolerance": 1e-8,
+                   "preconditioner": "Schwarz ILU(0)"
+                   + (" + block-diagonal coarse correction" if args.coarse
+                      else ""),
                    "tuning": b.tuning()},
         "converged": bool(ok and single_ok),
         "batch_ms": [round(x, 3) for x in batch_ms],

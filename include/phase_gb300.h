@@ -283,7 +283,8 @@ typedef struct {
   int coarse;         /* PG_PREC_ILU0: 0 = one-level Schwarz (as Ifpack2);
                          1 = add the two-level coarse correction on the
                          space of subdomain-constant vectors (at most 2048
-                         subdomains).  Not used by pg_batch_*. */
+                         subdomains; pg_batch_*: a block per system, at most
+                         4096 subdomains each) */
   double reserved_d;  /* ignored */
 } pg_solver_cfg;
 

@@ -287,7 +287,152 @@ k_coarse_correct(int K, const int32_t *__restrict__ sub_ptr,
   }
 }
 
+// ------------------------------------------------------ batched systems
+// Block-diagonal coarse space of stacked independent systems: system t owns
+// subdomains [k0[t], k0[t+1]) and a dense K_t x K_t block of A_c at float
+// offset off[t]; nothing couples systems.
+
+__global__ void __launch_bounds__(kCoarseBlock)
+k_coarse_assemble_b(CoarseBatchDev c, const int32_t *__restrict__ prp,
+                    const double *__restrict__ val) {
+  extern __shared__ double part[];  // [kCoarseBlock][S]
+  const int s = blockIdx.x;
+  const int t = c.sub_sys[s];
+  const int k0 = c.k0[t], Kt = c.k0[t + 1] - k0;
+  const int S = c.cptr[s + 1] - c.cptr[s];
+  for (int j = 0; j < S; ++j) part[threadIdx.x * S + j] = 0.;
+  const int32_t e0 = prp[c.sub_ptr[s]], e1 = prp[c.sub_ptr[s + 1]];
+  for (int32_t k = e0 + threadIdx.x; k < e1; k += kCoarseBlock)
+    part[threadIdx.x * S + c.cslot[k]] += val[k];
+  __syncthreads();
+  float *blk = c.ac + c.off[t] + (size_t)(s - k0) * Kt;
+  for (int j = threadIdx.x; j < S; j += kCoarseBlock) {
+    double sum = 0.;
+    for (int q = 0; q < kCoarseBlock; ++q) sum += part[q * S + j];
+    blk[c.cnb[c.cptr[s] + j] - k0] = (float)sum;
+  }
+}
+
+// Gauss-Jordan inversion of one system's block in place by one CTA of
+// 32 x 32 threads (single pivots, the same arithmetic as the blocked form;
+// a pivot below 1e-5 of its original diagonal is dropped)
+__global__ void __launch_bounds__(1024)
+k_gj_block(CoarseBatchDev c) {
+  extern __shared__ float sm[];  // dg0 | rowk | colk, max_k each
+  const int t = blockIdx.x;
+  const int Kt = c.k0[t + 1] - c.k0[t];
+  float *a = c.ac + c.off[t];
+  float *dg0 = sm, *rowk = sm + c.max_k, *colk = sm + 2 * c.max_k;
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  for (int i = tid; i < Kt; i += 1024) dg0[i] = a[(size_t)i * Kt + i];
+  for (int k = 0; k < Kt; ++k) {
+    __syncthreads();  // the previous step's writes are done
+    for (int j = tid; j < Kt; j += 1024) {
+      rowk[j] = a[(size_t)k * Kt + j];
+      colk[j] = a[(size_t)j * Kt + k];
+    }
+    __syncthreads();
+    const float piv = rowk[k];
+    const float ip = fabsf(piv) > 1e-5f * fabsf(dg0[k]) ? 1.f / piv : 0.f;
+    for (int i = ty; i < Kt; i += 32) {
+      const float a_ik = colk[i];
+      for (int j = tx; j < Kt; j += 32) {
+        const size_t idx = (size_t)i * Kt + j;
+        const float a_kj = rowk[j];
+        float v;
+        if (i == k && j == k)
+          v = ip;
+        else if (i == k)
+          v = a_kj * ip;
+        else if (j == k)
+          v = -a_ik * ip;
+        else
+          v = a[idx] - a_ik * (a_kj * ip);
+        a[idx] = v;
+      }
+    }
+  }
+}
+
+// per-subdomain input sums of the systems still running
+__global__ void __launch_bounds__(kCoarseBlock)
+k_coarse_sum_b(CoarseBatchDev c, const double *__restrict__ in,
+               const KScalars *__restrict__ sc) {
+  const int s = blockIdx.x;
+  if (sc[c.sub_sys[s]].done) return;
+  __shared__ double red[kCoarseBlock];
+  double acc = 0.;
+  for (int32_t i = c.sub_ptr[s] + threadIdx.x; i < c.sub_ptr[s + 1]; i += kCoarseBlock)
+    acc += in[i];
+  const double t = block_sum(acc, red);
+  if (threadIdx.x == 0) c.csum[s] = dd_from(t);
+}
+
+// y_s = (A_t^-1)_s . csum over the system's subdomains, z += y_s
+__global__ void __launch_bounds__(kCorrectBlock)
+k_coarse_correct_b(CoarseBatchDev c, double *__restrict__ z,
+                   const KScalars *__restrict__ sc) {
+  const int s = blockIdx.x;
+  const int t = c.sub_sys[s];
+  if (sc[t].done) return;
+  __shared__ float red_s[kCorrectBlock / 32], red_c[kCorrectBlock / 32];
+  __shared__ double y_sh;
+  const int k0 = c.k0[t], Kt = c.k0[t + 1] - k0;
+  const float *row = c.ac + c.off[t] + (size_t)(s - k0) * Kt;
+  DdAcc acc = dd_acc(make_float2(0.f, 0.f));
+  for (int j = threadIdx.x; j < Kt; j += kCorrectBlock)
+    dd_acc_fma(acc, make_float2(row[j], 0.f), c.csum[k0 + j]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    DdAcc b;
+    b.s = __shfl_xor_sync(0xffffffffu, acc.s, o);
+    b.c = __shfl_xor_sync(0xffffffffu, acc.c, o);
+    dd_acc_merge(acc, b);
+  }
+  const int wid = threadIdx.x / 32;
+  if ((threadIdx.x & 31) == 0) {
+    red_s[wid] = acc.s;
+    red_c[wid] = acc.c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    DdAcc u = dd_acc(make_float2(red_s[0], red_c[0]));
+    for (int w = 1; w < kCorrectBlock / 32; ++w) {
+      DdAcc b;
+      b.s = red_s[w];
+      b.c = red_c[w];
+      dd_acc_merge(u, b);
+    }
+    y_sh = dd_acc_to_double(u);
+  }
+  __syncthreads();
+  const double y = y_sh;
+  for (int32_t i = c.sub_ptr[s] + threadIdx.x; i < c.sub_ptr[s + 1]; i += kCorrectBlock)
+    z[i] += y;
+}
+
 }  // namespace
+
+void launch_coarse_setup_b(const CoarseBatchDev &c, int K, int64_t n_blk,
+                           const double *pvals, const int32_t *prp,
+                           cudaStream_t st) {
+  cudaMemsetAsync(c.ac, 0, (size_t)n_blk * sizeof(float), st);
+  const size_t smem = (size_t)kCoarseBlock * c.max_cnb * sizeof(double);
+  k_coarse_assemble_b<<<K, kCoarseBlock, smem, st>>>(c, prp, pvals);
+  k_gj_block<<<c.n_sys, 1024, 3 * (size_t)c.max_k * sizeof(float), st>>>(c);
+  count_launches(2);
+}
+
+void launch_coarse_apply_b(const CoarseBatchDev &c, int K, const double *in,
+                           double *z, bool have_sums, const KScalars *sc,
+                           cudaStream_t st) {
+  if (!have_sums) {
+    k_coarse_sum_b<<<K, kCoarseBlock, 0, st>>>(c, in, sc);
+    count_launches(1);
+  }
+  k_coarse_correct_b<<<K, kCorrectBlock, 0, st>>>(c, z, sc);
+  count_launches(1);
+}
 
 void launch_coarse_setup(const CoarseDev &c, const double *pvals,
                          const int32_t *prp, cudaGraphExec_t *gj_graph,

@@ -208,6 +208,29 @@ struct CoarseDev {
   float2 *csum = nullptr;
 };
 
+// Block-diagonal coarse space of a batch of independent systems: system t
+// owns subdomains [k0[t], k0[t+1]) and a dense K_t x K_t FP32 block of A_c
+// (then its inverse) at float offset off[t] of ac.
+struct CoarseBatchDev {
+  int n_sys = 0, max_cnb = 0, max_k = 0;
+  const int32_t *k0 = nullptr;
+  const int64_t *off = nullptr;
+  const int32_t *sub_ptr = nullptr, *cptr = nullptr, *cnb = nullptr;
+  const uint8_t *cslot = nullptr;
+  const int32_t *sub_sys = nullptr;
+  float *ac = nullptr;
+  float2 *csum = nullptr;
+};
+// A_c blocks from the permuted values, each inverted in place (one CTA per
+// system; n_blk = total floats of the blocks)
+void launch_coarse_setup_b(const CoarseBatchDev &c, int K, int64_t n_blk,
+                           const double *pvals, const int32_t *prp,
+                           cudaStream_t st);
+// z += Z A_c^-1 Z^T in for the systems still running
+void launch_coarse_apply_b(const CoarseBatchDev &c, int K, const double *in,
+                           double *z, bool have_sums, const KScalars *sc,
+                           cudaStream_t st);
+
 // A_c from the permuted values, then A_c^-1 in place (the K elimination
 // steps are captured into *gj_graph on first use when gj_graph is given)
 void launch_coarse_setup(const CoarseDev &c, const double *pvals,

@@ -94,6 +94,7 @@ struct pg_solver {
   // coarse matrix / its inverse, elimination buffers, subdomain sums and the
   // graph of the K elimination steps
   bool coarse_on = false;
+  bool batch_mode = false;  // inner solver of a pg_batch (its own coarse space)
   DevBuf<int32_t> c_sub_ptr, c_cptr, c_cnb;
   DevBuf<uint8_t> c_slot;
   DevBuf<float> c_ac, c_dg0, c_pinv, c_W, c_V, c_C;
@@ -265,7 +266,8 @@ int upload_analysis(pg_solver *s) {
   }
   s->drop_graphs();
   s->coarse_on = false;
-  if (s->cfg.coarse && s->cfg.precond == PG_PREC_ILU0 && a.n_sub > 1) {
+  if (s->cfg.coarse && !s->batch_mode && s->cfg.precond == PG_PREC_ILU0 &&
+      a.n_sub > 1) {
     PG_CHECK_ARG(a.n_sub <= kMaxCoarseK,
                  "coarse correction: more than 2048 subdomains (raise "
                  "subdomain_rows)");
@@ -1182,6 +1184,16 @@ struct pg_batch {
   bool persistent = false;
   cudaGraphExec_t exec = nullptr;
   int max_chunks = 0;
+  // block-diagonal coarse space (cfg.coarse): first subdomain and block
+  // offset per system, coupling structure, the blocks, subdomain sums
+  bool coarse = false;
+  int max_k = 0;
+  int64_t n_blk = 0;
+  DevBuf<int32_t> c_k0, c_sub_ptr, c_cptr, c_cnb;
+  DevBuf<int64_t> c_off;
+  DevBuf<uint8_t> c_slot;
+  DevBuf<float> c_ac;
+  DevBuf<float2> c_sum;
 
   ~pg_batch() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -1196,7 +1208,24 @@ struct pg_batch {
   SolverDev dev() const {
     SolverDev d = s->dev();
     d.sub_sys = sub_sys.p;
+    d.csum = coarse ? c_sum.p : nullptr;
     return d;
+  }
+  CoarseBatchDev coarse_dev() const {
+    CoarseBatchDev c;
+    c.n_sys = n_sys;
+    c.max_cnb = s->a.max_cnb;
+    c.max_k = max_k;
+    c.k0 = c_k0.p;
+    c.off = c_off.p;
+    c.sub_ptr = c_sub_ptr.p;
+    c.cptr = c_cptr.p;
+    c.cnb = c_cnb.p;
+    c.cslot = c_slot.p;
+    c.sub_sys = sub_sys.p;
+    c.ac = c_ac.p;
+    c.csum = c_sum.p;
+    return c;
   }
 };
 
@@ -1299,8 +1328,11 @@ int batch_analyse(pg_batch *b, const std::vector<int32_t> &rp,
                   const double *cy) {
   pg_solver *s = b->s;
   const int64_t n = (int64_t)rp.size() - 1;
-  int rc = analyse(n, rp.data(), ci.data(), s->cfg.subdomain_rows, s->a,
-                   &b->sys_rows, cx, cy);
+  const int sub_rows = s->cfg.subdomain_rows ? s->cfg.subdomain_rows
+                       : s->cfg.coarse           ? 512
+                                                 : 1024;
+  int rc = analyse(n, rp.data(), ci.data(), sub_rows, s->a, &b->sys_rows, cx,
+                   cy);
   if (rc) return rc;
   s->rank = n;
   rc = upload_analysis(s);
@@ -1314,6 +1346,38 @@ int batch_analyse(pg_batch *b, const std::vector<int32_t> &rp,
                                        (int64_t)row) - b->sys_rows.begin()) - 1;
   }
   PG_CUDA(b->sub_sys.upload(ss));
+  b->coarse = false;
+  if (s->cfg.coarse) {
+    // subdomains are grouped by system in system order
+    const Analysis &a = s->a;
+    std::vector<int32_t> k0(b->n_sys + 1, a.n_sub);
+    for (int k = a.n_sub - 1; k >= 0; --k) k0[ss[k]] = k;
+    for (int t = b->n_sys - 1; t >= 0; --t)
+      if (k0[t] == a.n_sub || k0[t] > k0[t + 1]) k0[t] = k0[t + 1];
+    std::vector<int64_t> off(b->n_sys + 1, 0);
+    b->max_k = 0;
+    for (int t = 0; t < b->n_sys; ++t) {
+      const int64_t kt = k0[t + 1] - k0[t];
+      b->max_k = std::max<int>(b->max_k, (int)kt);
+      off[t + 1] = off[t] + kt * kt;
+    }
+    PG_CHECK_ARG(b->max_k <= 4096,
+                 "batched coarse correction: a system has more than 4096 "
+                 "subdomains (raise subdomain_rows)");
+    PG_CHECK_ARG(a.max_cnb <= kMaxCoarseNb,
+                 "batched coarse correction: a subdomain couples to more "
+                 "than 32 others");
+    b->n_blk = off[b->n_sys];
+    PG_CUDA(b->c_k0.upload(k0));
+    PG_CUDA(b->c_off.upload(off));
+    PG_CUDA(b->c_sub_ptr.upload(a.sub_ptr));
+    PG_CUDA(b->c_cptr.upload(a.cptr));
+    PG_CUDA(b->c_cnb.upload(a.cnb));
+    PG_CUDA(b->c_slot.upload(a.cslot));
+    PG_CUDA(b->c_ac.reserve((size_t)b->n_blk));
+    PG_CUDA(b->c_sum.reserve((size_t)a.n_sub));
+    b->coarse = true;
+  }
   PG_CUDA(b->sc.reserve(b->n_sys));
   PG_CUDA(b->tickets.zero(b->n_sys));
   PG_CUDA(b->flags.reserve(b->n_sys));
@@ -1336,6 +1400,7 @@ int build_batch_graph(pg_batch *b) {
   cudaStream_t st = stream();
   pg_solver *s = b->s;
   const SolverDev d = b->dev();
+  const CoarseBatchDev cb = b->coarse_dev();
   const BatchTiles T = b->tiles();
   const BatchRed R = b->red();
   cudaGraph_t g = nullptr;
@@ -1361,10 +1426,16 @@ int build_batch_graph(pg_batch *b) {
     for (int c = 0; c < kChunk; ++c) {
       launch_precond<double, double>(PG_PREC_ILU0, 1, d, nullptr, s->r.p,
                                      s->p.p, s->v.p, s->ph.p, b->sc.p, st);
+      if (b->coarse)
+        launch_coarse_apply_b(cb, d.n_sub, s->p.p, s->ph.p, d.smem64 > 0,
+                              b->sc.p, st);
       launch_b_spmv_v(T, R, b->block, d, s->pvals.p, s->ph.p, s->v.p,
                       s->rh.p, b->sc.p, st);
       launch_precond<double, double>(PG_PREC_ILU0, 2, d, nullptr, s->r.p,
                                      s->s.p, s->v.p, s->sh.p, b->sc.p, st);
+      if (b->coarse)
+        launch_coarse_apply_b(cb, d.n_sub, s->s.p, s->sh.p, d.smem64 > 0,
+                              b->sc.p, st);
       launch_b_spmv_t(T, R, b->block, d, s->pvals.p, s->sh.p, s->t.p,
                       s->s.p, b->sc.p, st);
       launch_b_update(T, R, b->block, s->x.p, s->r.p, s->ph.p, s->sh.p,
@@ -1401,7 +1472,6 @@ extern "C" int pg_batch_create(const pg_solver_cfg *cfg, pg_batch **out) {
                "preconditioner");
   PG_CHECK_ARG(c.precision == PG_FP64,
                "pg_batch_create: batched solves run in FP64");
-  c.coarse = 0;  // the batched drivers apply the one-level preconditioner
   auto *b = new (std::nothrow) pg_batch();
   PG_CHECK_ARG(b, "pg_batch_create: out of host memory");
   int rc = pg_solver_create(&c, &b->s);
@@ -1409,6 +1479,7 @@ extern "C" int pg_batch_create(const pg_solver_cfg *cfg, pg_batch **out) {
     delete b;
     return rc;
   }
+  b->s->batch_mode = true;
   *out = b;
   return PG_OK;
 }
@@ -1514,6 +1585,9 @@ extern "C" int pg_batch_solve(pg_batch *b, pg_solve_stats *stats,
   PG_CUDA(cudaEventRecord(s->ev[0], st));
   PG_CUDA(cudaMemsetAsync(s->bad.p, 0, sizeof(int), st));
   launch_ilu0_factor(d, s->pvals.p, s->bad.p, false, st);
+  if (b->coarse)
+    launch_coarse_setup_b(b->coarse_dev(), d.n_sub, b->n_blk, s->pvals.p,
+                          s->prp.p, st);
   for (int i = 0; i < S; ++i) {
     KScalars k{};
     k.tol2 = s->cfg.tolerance * s->cfg.tolerance;
@@ -1544,7 +1618,7 @@ extern "C" int pg_batch_solve(pg_batch *b, pg_solve_stats *stats,
     PG_CUDA(cudaMemcpyAsync(b->sc_host, b->sc.p, S * sizeof(KScalars),
                             cudaMemcpyDeviceToHost, st));
     PG_CUDA(cudaStreamSynchronize(st));
-    count_launches((5 * kChunk + 2) * ch);
+    count_launches(((b->coarse ? (d.smem64 > 0 ? 7 : 9) : 5) * kChunk + 2) * ch);
     break;
   }
   launch_unpermute_vec((int)n, s->perm.p, s->x.p, s->xout.p, st);

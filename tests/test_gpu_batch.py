@@ -28,17 +28,22 @@ def _systems(pg, n, seed, max_cells=20_000):
     return out
 
 
-def test_batch_matches_individual_solves(pg):
+@pytest.mark.parametrize("coarse", [0, 1])
+def test_batch_matches_individual_solves(pg, coarse):
+    """coarse = 1: a block-diagonal coarse space per system in the batch
+    (single-pivot Gauss-Jordan per block) and the dense one of a lone
+    solver (blocked Gauss-Jordan) round differently, so the solutions are
+    compared at 1e-6 rather than 1e-8."""
     systems = _systems(pg, 12, seed=7)
     eqns = [e for _, e in systems]
-    b = pg.BatchSolver(tolerance=1e-10, max_iters=5000)
+    b = pg.BatchSolver(tolerance=1e-10, max_iters=5000, coarse=coarse)
     b.set_eqns(eqns)
     stats = b.solve()
     t = b.tuning()
     assert (t["block"], t["rows_per_thread"]) in {
         (128, 1), (128, 2), (128, 4), (256, 1), (256, 2), (256, 4), (512, 1),
         (512, 2)}
-    s = pg.SparseMatrixSolver(tolerance=1e-10, max_iters=5000)
+    s = pg.SparseMatrixSolver(tolerance=1e-10, max_iters=5000, coarse=coarse)
     for i, e in enumerate(eqns):
         st = stats[i]
         assert st.status == pg.PG_OK and st.rel_residual <= 1e-10, (i, st.as_dict())
@@ -50,7 +55,7 @@ def test_batch_matches_individual_solves(pg):
         s.setGuess(None)
         assert s.solve() <= 1e-10
         xs = s.x()
-        assert np.linalg.norm(x - xs) / np.linalg.norm(xs) < 1e-8
+        assert np.linalg.norm(x - xs) / np.linalg.norm(xs) < (1e-6 if coarse else 1e-8)
 
 
 def test_batch_resolve_is_deterministic(pg):
