@@ -106,6 +106,15 @@ int pg_mesh_cells(const pg_mesh *m, double *cx, double *cy, double *vol);
  * ---------------------------------------------------------------------- */
 int pg_eqn_create(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
                   pg_eqn **out);
+/* FiniteVolumeField::setBoundaryFaces (FiniteVolumeField.tpp:165-183):
+ * on boundary faces of type PG_BC_NORMAL_GRADIENT or PG_BC_SYMMETRY,
+ * phi_face[f] = phi_cell[lCell(f)]; fixed boundary faces and interior faces
+ * keep their values.  bc_type[n_faces] (the field's boundary type per
+ * face), phi_cell[n_cells], phi_face[n_faces] in ptr_kind memory. */
+int pg_set_boundary_faces(const pg_mesh *m, const int32_t *bc_type,
+                          const double *phi_cell, double *phi_face,
+                          int ptr_kind);
+
 /* Projection step after the pressure solve: u -= dt / rho * grad p on every
  * cell and every face (FractionalStep::correctVelocity,
  * src/2D/Unstructured/Solvers/FractionalStep.cpp:109-117, and its

@@ -1178,6 +1178,18 @@ extern "C" or_eqn *or_gcib_laplacian(const or_mesh *m, const double *gamma_face,
   return lap;
 }
 
+// FiniteVolumeField::setBoundaryFaces (src/2D/Unstructured/FiniteVolume/
+// Field/FiniteVolumeField.tpp:165-183): every face of a NORMAL_GRADIENT or
+// SYMMETRY patch takes the value of its lCell; FIXED patches and interior
+// faces are left as they are.
+extern "C" void or_set_boundary_faces(const or_mesh *m, const int32_t *bc_type,
+                                      const double *phi_cell,
+                                      double *phi_face) {
+  for (size_t f = 0; f < m->fl.size(); ++f)
+    if (m->fr[f] < 0 && bc_type[f] != OR_FIXED)
+      phi_face[f] = phi_cell[m->fl[f]];
+}
+
 // FractionalStep::correctVelocity (src/2D/Unstructured/Solvers/
 // FractionalStep.cpp:109-117) and FractionalStepMultiphase::correctVelocity
 // (FractionalStepMultiphase.cpp:165-173): u -= timeStep / rho * gradP on

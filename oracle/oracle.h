@@ -166,6 +166,10 @@ or_eqn *or_gcib_laplacian(const or_mesh *m, const double *gamma_face,
                           const double *bc_value, const double *u_face_xy,
                           int n_circles, const double *circles, int ib_bc,
                           double ib_ref, int32_t *cell_class);
+/* FiniteVolumeField::setBoundaryFaces: faces of NORMAL_GRADIENT/SYMMETRY
+ * boundaries take their cell's value (FiniteVolumeField.tpp:165-183). */
+void or_set_boundary_faces(const or_mesh *m, const int32_t *bc_type,
+                           const double *phi_cell, double *phi_face);
 /* FractionalStep::correctVelocity: u -= dt / rho * grad p on cells and
  * faces (FractionalStep.cpp:109-117, FractionalStepMultiphase.cpp:165-173);
  * rho arrays NULL = 1.  x,y interleaved. */

@@ -75,6 +75,7 @@ PROTOTYPES = {
     "pg_mesh_cells": (_I, [_P, _P, _P, _P]),
     "pg_eqn_create": (_I, [_P, _I, _P, ctypes.POINTER(_P)]),
     "pg_correct_velocity": (_I, [_P, _D, _P, _P, _P, _P, _P, _P, _I]),
+    "pg_set_boundary_faces": (_I, [_P, _P, _P, _P, _I]),
     "pg_eqn_create_gcib": (_I, [_P, _I, _P, _I, _P, _I, _D, ctypes.POINTER(_P)]),
     "pg_eqn_cell_class": (_I, [_P, _P]),
     "pg_eqn_create_momentum": (_I, [_P, _P, ctypes.POINTER(_P)]),
@@ -249,6 +250,16 @@ class Mesh:
         _check(lib().pg_gradient(self._h, _ptr(pc), _ptr(pf), _ptr(gf),
                                  _ptr(gc), PG_HOST))
         return gf.reshape(-1, 2), gc.reshape(-1, 2)
+
+    def set_boundary_faces(self, bc_type, phi_cell, phi_face):
+        """FiniteVolumeField::setBoundaryFaces: returns phi_face with the
+        normal-gradient/symmetry boundary faces set to their cell values."""
+        bc = _i32(bc_type, self.n_faces)
+        pc = _f64(phi_cell, self.n_cells)
+        pf = np.array(phi_face, np.float64).reshape(-1)
+        _check(lib().pg_set_boundary_faces(self._h, _ptr(bc), _ptr(pc),
+                                           _ptr(pf), PG_HOST))
+        return pf
 
     def correct_velocity(self, dt, grad_cell, grad_face, u_cell, u_face,
                          rho_cell=None, rho_face=None):

@@ -551,6 +551,34 @@ extern "C" int pg_gradient(const pg_mesh *m, const double *phi_cell,
   return PG_OK;
 }
 
+extern "C" int pg_set_boundary_faces(const pg_mesh *m, const int32_t *bc_type,
+                                     const double *phi_cell, double *phi_face,
+                                     int ptr_kind) {
+  PG_CHECK_ARG(m && bc_type && phi_cell && phi_face,
+               "pg_set_boundary_faces: NULL arg");
+  const HostMesh &h = m->h;
+  const int64_t n = h.n_cells, nf = h.n_faces;
+  DevBuf<int32_t> bcd;
+  DevBuf<double> pc, pf;
+  const int32_t *bc = bc_type;
+  const double *c = phi_cell;
+  double *f = phi_face;
+  if (ptr_kind != PG_DEVICE) {
+    PG_CUDA(bcd.upload(bc_type, nf));
+    PG_CUDA(pc.upload(phi_cell, n));
+    PG_CUDA(pf.upload(phi_face, nf));
+    bc = bcd.p;
+    c = pc.p;
+    f = pf.p;
+  }
+  launch_set_boundary_faces((int)nf, m->d.fl.p, m->d.fr.p, bc, c, f, stream());
+  PG_CUDA(cudaGetLastError());
+  if (ptr_kind != PG_DEVICE)
+    PG_CUDA(copy_out(phi_face, f, nf * sizeof(double), PG_HOST));
+  PG_CUDA(cudaStreamSynchronize(stream()));
+  return PG_OK;
+}
+
 extern "C" int pg_correct_velocity(const pg_mesh *m, double dt,
                                    const double *rho_cell,
                                    const double *rho_face,

@@ -604,6 +604,19 @@ __global__ void k_correct_velocity(int n, double dt,
   }
 }
 
+// FiniteVolumeField::setBoundaryFaces (FiniteVolumeField.tpp:165-183):
+// normal-gradient and symmetry boundary faces take their cell's value,
+// fixed ones keep theirs, interior faces are untouched
+__global__ void k_set_boundary_faces(int nf, const int32_t *__restrict__ fl,
+                                     const int32_t *__restrict__ fr,
+                                     const int32_t *__restrict__ bc,
+                                     const double *__restrict__ phi_cell,
+                                     double *__restrict__ phi_face) {
+  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < nf;
+       f += gridDim.x * blockDim.x)
+    if (fr[f] < 0 && bc[f] != PG_BC_FIXED) phi_face[f] = phi_cell[fl[f]];
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------- launchers
@@ -645,6 +658,15 @@ void launch_correct_velocity(int n, double dt, const double *rho,
   if (n <= 0) return;
   const int g = blocks_for(n, 256) < 2432 ? blocks_for(n, 256) : 2432;
   k_correct_velocity<<<g, 256, 0, st>>>(n, dt, rho, grad, u);
+  count_launches(1);
+}
+
+void launch_set_boundary_faces(int nf, const int32_t *fl, const int32_t *fr,
+                               const int32_t *bc, const double *phi_cell,
+                               double *phi_face, cudaStream_t st) {
+  if (nf <= 0) return;
+  const int g = blocks_for(nf, 256) < 2432 ? blocks_for(nf, 256) : 2432;
+  k_set_boundary_faces<<<g, 256, 0, st>>>(nf, fl, fr, bc, phi_cell, phi_face);
   count_launches(1);
 }
 

@@ -83,6 +83,9 @@ void launch_momentum_boundary(int nf, int off, const int32_t *cface,
                               double *vals, double *rhs, cudaStream_t st);
 void launch_correct_velocity(int n, double dt, const double *rho,
                              const double *grad, double *u, cudaStream_t st);
+void launch_set_boundary_faces(int nf, const int32_t *fl, const int32_t *fr,
+                               const int32_t *bc, const double *phi_cell,
+                               double *phi_face, cudaStream_t st);
 void launch_interp_faces(int nf, const int32_t *fl, const int32_t *fr,
                          const double *fcx, const double *fcy,
                          const double *cx, const double *cy,

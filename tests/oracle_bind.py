@@ -84,6 +84,7 @@ def lib():
         L.or_momentum.restype = P
         L.or_momentum.argtypes = [P, D, D, D, P, P, P]
         L.or_correct_velocity.argtypes = [P, D, P, P, P, P, P, P]
+        L.or_set_boundary_faces.argtypes = [P, P, P, P]
         L.or_gcib_laplacian.restype = P
         L.or_gcib_laplacian.argtypes = [P, P, D, P, P, P, ctypes.c_int, P,
                                         ctypes.c_int, D, P]
@@ -197,6 +198,13 @@ class OracleMesh:
         lib().or_eqn_export_csr(e, ptr(rp), ptr(ci), ptr(v), ptr(rhs))
         lib().or_eqn_destroy(e)
         return rp, ci, v, rhs, cls
+
+    def set_boundary_faces(self, bc_type, phi_cell, phi_face):
+        out = np.array(phi_face, np.float64)
+        lib().or_set_boundary_faces(self.h, ptr(np.ascontiguousarray(bc_type, np.int32)),
+                                    ptr(np.ascontiguousarray(phi_cell, np.float64)),
+                                    ptr(out))
+        return out
 
     def correct_velocity(self, dt, grad_cell, grad_face, u_cell, u_face,
                          rho_cell=None, rho_face=None):

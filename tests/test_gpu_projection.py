@@ -29,6 +29,23 @@ def test_correct_velocity_matches_oracle(pg, oracle, with_rho, mesh):
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
 
 
+@pytest.mark.parametrize("mesh", ["rect", "tri"])
+def test_set_boundary_faces_matches_oracle(pg, oracle, mesh):
+    nodes, cptr, cind = (meshes.rectilinear(11, 6, 1.1, 0.6) if mesh == "rect"
+                         else meshes.triangulated(8, 9, 1.0, 1.0, jitter=0.2, seed=3))
+    m = pg.Mesh(nodes, cptr, cind)
+    om = oracle.OracleMesh(nodes, cptr, cind)
+    rng = np.random.default_rng(4)
+    f = om.faces()
+    bc = np.where(f["rcell"] < 0, rng.integers(0, 3, om.n_faces), 1).astype(np.int32)
+    pc, pf = rng.standard_normal(om.n_cells), rng.standard_normal(om.n_faces)
+    a = m.set_boundary_faces(bc, pc, pf)
+    b = om.set_boundary_faces(bc, pc, pf)
+    assert np.array_equal(a, b)
+    inner = f["rcell"] >= 0
+    assert np.array_equal(a[inner], pf[inner])
+
+
 def test_projection_makes_faces_divergence_free(pg, oracle):
     nx = 64
     w = workloads.rising_bubble(nx, nx, seed=3)
@@ -41,11 +58,10 @@ def test_projection_makes_faces_divergence_free(pg, oracle):
     s.set_eqn(eqn)
     assert s.solve() <= 1e-10 and s.stats.status == pg.PG_OK
     p = s.x()
-    # setBoundaryFaces: fixed faces take their value, the others the cell's
-    bnd = faces["rcell"] < 0
-    p_face = np.zeros(m.n_faces)
-    p_face[bnd] = np.where(w["bc_type"][bnd] == 0, w["bc_value"][bnd],
-                           p[faces["lcell"][bnd]])
+    # setBoundaryFaces on the device: fixed faces keep their value (here the
+    # boundary value), the others take the cell's
+    p_face = m.set_boundary_faces(w["bc_type"], p,
+                                  np.where(faces["rcell"] < 0, w["bc_value"], 0.0))
     grad_face, grad_cell = m.gradient(p, p_face)
     rho_face = w["dt"] / coeff
     rho_cell = w["rho1"] + np.clip(w["gamma"], 0, 1) * (w["rho2"] - w["rho1"])

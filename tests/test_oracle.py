@@ -265,6 +265,8 @@ def test_projection_property_of_correct_velocity(oracle):
     p_face = np.zeros(om.n_faces)
     p_face[bnd] = np.where(w["bc_type"][bnd] == 0, w["bc_value"][bnd],
                            p[f["lcell"][bnd]])
+    assert np.array_equal(p_face, om.set_boundary_faces(
+        w["bc_type"], p, np.where(bnd, w["bc_value"], 0.0)))
     gf, gc = om.gradient(p, p_face)
     _, uf = om.correct_velocity(w["dt"], gc, gf, np.zeros((om.n_cells, 2)),
                                 w["u"], None, w["dt"] / coeff)
