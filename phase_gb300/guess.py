@@ -239,6 +239,33 @@ class BubbleSequence:
         return v, b
 
 
+def dump_sequence(path, nx=1024, steps=range(1, 11), coarse=1, seed=3):
+    """Solve the rising-bubble sequence with the plain FP64 solver (warm from
+    the previous step, as a time loop runs it) and write the (A_t, b_t, x_t)
+    triples to ``path`` in the triples.py format."""
+    from . import triples
+    pg = _pg()
+    seq = BubbleSequence(nx, seed=seed)
+    keep = seq.col_ind >= 0  # CrsEquation placeholder slots are dropped
+    rows = np.repeat(np.arange(seq.n), np.diff(seq.row_ptr))[keep]
+    rp = np.zeros(seq.n + 1, np.int32)
+    np.add.at(rp, rows + 1, 1)
+    rp = np.cumsum(rp).astype(np.int32)
+    w = triples.TripleWriter(path, rp, seq.col_ind[keep], nx=nx, seed=seed,
+                             workload="rising bubble", tolerance=1e-8)
+    solver = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
+                                   coarse=coarse)
+    for t in steps:
+        eqn = seq.assemble(int(t))
+        solver.set_eqn(eqn)
+        solver.solve()
+        if solver.stats.status != pg.PG_OK:
+            raise RuntimeError(f"dump: step {t} did not converge")
+        _, _, v, rhs = eqn.export()
+        w.write(int(t), v[keep], -rhs, solver.x())
+    return w
+
+
 def train(nx=1024, steps=2000, epochs=8, lr=2e-3, out=DEFAULT_WEIGHTS,
           eval_steps=20, log=print):
     import torch

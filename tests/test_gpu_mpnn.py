@@ -102,3 +102,16 @@ def test_weights_file_round_trip(pg, tmp_path):
     bad.write_bytes(b"not a weights file")
     with pytest.raises(pg.PhaseError):
         b.load(bad)
+
+
+def test_triple_dump_of_a_sequence(pg, tmp_path):
+    """The sequence dump (triples.py format) holds systems whose stored
+    solutions meet the solver tolerance."""
+    import scipy.sparse as sp
+    from phase_gb300 import guess, triples
+    guess.dump_sequence(str(tmp_path / "d"), nx=64, steps=[5, 6, 7])
+    r = triples.TripleReader(str(tmp_path / "d"))
+    assert r.steps == [5, 6, 7] and r.n == 64 * 64
+    for t, vals, b, x in r:
+        A = sp.csr_matrix((vals, r.col_ind, r.row_ptr), shape=(r.n, r.n))
+        assert np.linalg.norm(b - A @ x) / np.linalg.norm(b) <= 1.01e-8
