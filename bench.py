@@ -300,10 +300,12 @@ def run_sequence(args):
     sp = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
                                subdomain_rows=args.subdomain_rows,
                                coarse=args.coarse)
+    # the learned arm overlaps the coarse inverse with the network's
+    # inference, so its solves wait for the inverse instead of warming up
     sm = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
                                precision=pg.MIXED,
                                subdomain_rows=args.subdomain_rows,
-                               coarse=args.coarse)
+                               coarse=args.coarse, coarse_warm=0)
     xp_p = torch.zeros(n, dtype=torch.float64, device=dev)
     xp_m = torch.zeros(n, dtype=torch.float64, device=dev)
     g = torch.empty(n, dtype=torch.float64, device=dev)
@@ -517,7 +519,8 @@ def e2e_learned(pg, guess, seq, net, have_w, steps, torch, dev, coarse):
     from host inputs, the solver runs from its guess, and x comes back."""
     import numpy as np
     s2 = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
-                               precision=pg.MIXED, coarse=coarse)
+                               precision=pg.MIXED, coarse=coarse,
+                               coarse_warm=0)
     # the caller's geometry hint: cell centroids cut the Schwarz subdomains
     s2.setRank(seq.n)
     s2.set_row_coords(np.stack([seq.cells["cx"], seq.cells["cy"]], axis=1))

@@ -294,6 +294,12 @@ typedef struct {
                          space of subdomain-constant vectors (at most 2048
                          subdomains; pg_batch_*: a block per system, at most
                          4096 subdomains each) */
+  int coarse_warm;    /* one-level iterations a solve runs while the coarse
+                         inverse is built beside them, before it restarts
+                         with the two-level preconditioner: -1 = default (16
+                         with at least 1024 subdomains, else 0), 0 = wait
+                         for the inverse (when the caller already had work
+                         to overlap it with after the hand-over) */
   double reserved_d;  /* ignored */
 } pg_solver_cfg;
 

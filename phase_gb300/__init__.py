@@ -44,7 +44,7 @@ class SolverCfg(ctypes.Structure):
     _fields_ = [("tolerance", ctypes.c_double), ("max_iters", ctypes.c_int),
                 ("precond", ctypes.c_int), ("subdomain_rows", ctypes.c_int),
                 ("precision", ctypes.c_int), ("mixed_sweep", ctypes.c_int),
-                ("coarse", ctypes.c_int),
+                ("coarse", ctypes.c_int), ("coarse_warm", ctypes.c_int),
                 ("reserved_d", ctypes.c_double)]
 
 

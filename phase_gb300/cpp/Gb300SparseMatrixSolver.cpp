@@ -127,6 +127,7 @@ void Gb300SparseMatrixSolver::setup(const boost::property_tree::ptree &p) {
       p.get<std::string>("precision", "fp64") == "mixed" ? PG_MIXED : PG_FP64;
   cfg_.mixed_sweep = p.get<int>("mixedSweep", 0);
   cfg_.coarse = p.get<int>("coarseSpace", 0);
+  cfg_.coarse_warm = p.get<int>("coarseWarmIters", -1);
   recreate();
 }
 

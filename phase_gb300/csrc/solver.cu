@@ -88,13 +88,21 @@ struct pg_solver {
   // kernel
   // arguments are fixed device pointers, so a graph stays valid until the
   // buffers are reallocated by a new analysis
-  cudaGraphExec_t chunk_graph[2] = {nullptr, nullptr};
-  int chunk_launches[2] = {0, 0};  // kernels in one replay of each graph
+  // [0] FP64, [1] float-float; [2], [3] the same without the coarse
+  // correction (the warm-up iterations while the coarse inverse is built)
+  cudaGraphExec_t chunk_graph[4] = {nullptr, nullptr, nullptr, nullptr};
+  int chunk_launches[4] = {0, 0, 0, 0};  // kernels in one replay of each graph
   // two-level Schwarz coarse space (cfg.coarse): structure, the dense
   // coarse matrix / its inverse, elimination buffers, subdomain sums and the
   // graph of the K elimination steps
   bool coarse_on = false;
+  bool coarse_use = true;   // the drivers apply the coarse correction
   bool batch_mode = false;  // inner solver of a pg_batch (its own coarse space)
+  // the coarse matrix and its inverse are built on side2 beside the first
+  // (one-level) iterations; ev_coarse marks them done
+  cudaStream_t side2 = nullptr;
+  cudaEvent_t ev_cvals = nullptr, ev_coarse = nullptr;
+  bool coarse_pending = false;
   DevBuf<int32_t> c_sub_ptr, c_cptr, c_cnb;
   DevBuf<uint8_t> c_slot;
   DevBuf<float> c_ac, c_dg0, c_pinv, c_W, c_V, c_C;
@@ -115,7 +123,7 @@ struct pg_solver {
 
   CoarseDev coarse() const {
     CoarseDev c;
-    if (!coarse_on) return c;
+    if (!coarse_on || !coarse_use) return c;
     c.K = a.n_sub;
     c.max_cnb = a.max_cnb;
     c.sub_ptr = c_sub_ptr.p;
@@ -144,8 +152,14 @@ struct pg_solver {
       cudaStreamSynchronize(side);
       cudaStreamDestroy(side);
     }
+    if (side2) {
+      cudaStreamSynchronize(side2);
+      cudaStreamDestroy(side2);
+    }
     if (ev_vals) cudaEventDestroy(ev_vals);
     if (ev_fact) cudaEventDestroy(ev_fact);
+    if (ev_cvals) cudaEventDestroy(ev_cvals);
+    if (ev_coarse) cudaEventDestroy(ev_coarse);
     drop_graphs();
     if (sc_host) cudaFreeHost(sc_host);
     if (bad_host) cudaFreeHost(bad_host);
@@ -208,6 +222,11 @@ int red_grid_cap() {
 }
 
 constexpr int kMaxCoarseK = 2048;  // the coarse matrix is K x K, dense
+// by default, coarse spaces of at least kCoarseStagedK subdomains are
+// inverted beside kCoarseWarmIters one-level iterations (the inversion
+// takes ~2 ms at 2048; cfg.coarse_warm overrides)
+constexpr int kCoarseStagedK = 1024;
+constexpr int kCoarseWarmIters = 16;
 
 // Schwarz subdomain size for the analysis: the configured one, else 1024
 // rows for the one-level preconditioner and 512 with a coarse space (the
@@ -222,9 +241,11 @@ int subdomain_rows_for(const pg_solver_cfg &c, int64_t n) {
 }
 
 int upload_analysis(pg_solver *s) {
-  if (s->fact_pending) {  // buffers are about to be reallocated
+  if (s->fact_pending || s->coarse_pending) {  // buffers are about to move
     PG_CUDA(cudaStreamSynchronize(s->side));
+    PG_CUDA(cudaStreamSynchronize(s->side2));
     s->fact_pending = false;
+    s->coarse_pending = false;
   }
   const Analysis &a = s->a;
   cudaError_t e = cudaSuccess;
@@ -310,6 +331,17 @@ int ensure_host_state(pg_solver *s) {
   if (!s->side) PG_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
   if (!s->ev_vals) PG_CUDA(cudaEventCreateWithFlags(&s->ev_vals, cudaEventDisableTiming));
   if (!s->ev_fact) PG_CUDA(cudaEventCreateWithFlags(&s->ev_fact, cudaEventDisableTiming));
+  if (!s->side2) PG_CUDA(cudaStreamCreateWithFlags(&s->side2, cudaStreamNonBlocking));
+  if (!s->ev_cvals) PG_CUDA(cudaEventCreateWithFlags(&s->ev_cvals, cudaEventDisableTiming));
+  if (!s->ev_coarse) PG_CUDA(cudaEventCreateWithFlags(&s->ev_coarse, cudaEventDisableTiming));
+  return PG_OK;
+}
+
+// The library stream waits for the coarse matrix and inverse built on side2.
+int join_coarse(pg_solver *s) {
+  if (!s->coarse_pending) return PG_OK;
+  PG_CUDA(cudaStreamWaitEvent(stream(), s->ev_coarse, 0));
+  s->coarse_pending = false;
   return PG_OK;
 }
 
@@ -446,10 +478,11 @@ int run_bicgstab(pg_solver *s, double tol, int max_iters, int *iters,
   if (s->sc_host->rr_true <= init.tol2 * bb) return PG_OK;
   double rr_ref = s->sc_host->rr_true;
   int restarts = 0;
-  cudaGraphExec_t &gexec = s->chunk_graph[0];
+  const int slot = cdev.K ? 0 : 2;
+  cudaGraphExec_t &gexec = s->chunk_graph[slot];
   bool direct_done = false;
   for (;;) {
-    if ((rc = run_chunk(gexec, s->chunk_launches[0], direct_done, chunk))) return rc;
+    if ((rc = run_chunk(gexec, s->chunk_launches[slot], direct_done, chunk))) return rc;
     if ((rc = read_scalars())) return rc;
     const KScalars k = *s->sc_host;
     *iters = k.iter;
@@ -563,7 +596,9 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
   int restarts = 0;
   bool direct_done = false;
   for (;;) {
-    if ((rc = run_chunk(s->chunk_graph[1], s->chunk_launches[1], direct_done, chunk))) return rc;
+    if ((rc = run_chunk(s->chunk_graph[cdev.K ? 1 : 3],
+                        s->chunk_launches[cdev.K ? 1 : 3], direct_done, chunk)))
+      return rc;
     if ((rc = read_scalars())) return rc;
     const KScalars k = *s->sc_host;
     *iters = k.iter;
@@ -671,8 +706,18 @@ int factor(pg_solver *s, cudaStream_t st) {
   if (s->cfg.precond == PG_PREC_ILU0) {
     PG_CUDA(cudaMemsetAsync(s->bad.p, 0, sizeof(int), st));
     launch_ilu0_factor(d, s->pvals.p, s->bad.p, dd, st);
-    if (s->coarse_on)
-      launch_coarse_setup(s->coarse(), s->pvals.p, s->prp.p, &s->gj_graph, st);
+    if (s->coarse_on) {
+      // beside the ILU(0) factorisation and the first iterations
+      PG_CUDA(cudaEventRecord(s->ev_cvals, st));
+      PG_CUDA(cudaStreamWaitEvent(s->side2, s->ev_cvals, 0));
+      const bool use = s->coarse_use;
+      s->coarse_use = true;
+      launch_coarse_setup(s->coarse(), s->pvals.p, s->prp.p, &s->gj_graph,
+                          s->side2);
+      s->coarse_use = use;
+      PG_CUDA(cudaEventRecord(s->ev_coarse, s->side2));
+      s->coarse_pending = true;
+    }
   } else if (s->cfg.precond == PG_PREC_JACOBI) {
     launch_jacobi_diag(d, s->pvals.p, s->jdinv.p, st);
     if (dd) launch_dd_split(d.n, s->jdinv.p, 1.0, s->jdinv_dd.p, st);
@@ -712,6 +757,7 @@ extern "C" void pg_solver_default_cfg(pg_solver_cfg *cfg) {
   cfg->precision = PG_FP64;
   cfg->mixed_sweep = 0;
   cfg->coarse = 0;
+  cfg->coarse_warm = -1;
   cfg->reserved_d = 0.;
 }
 
@@ -729,6 +775,7 @@ extern "C" int pg_solver_create(const pg_solver_cfg *cfg, pg_solver **out) {
   PG_CHECK_ARG(c.mixed_sweep >= 0 && c.mixed_sweep <= 2,
                "pg_solver_create: bad mixed_sweep");
   PG_CHECK_ARG(c.coarse == 0 || c.coarse == 1, "pg_solver_create: bad coarse");
+  PG_CHECK_ARG(c.coarse_warm >= -1, "pg_solver_create: bad coarse_warm");
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0 || !stream()) {
     set_error("no CUDA device available: libphase_gb300 has no CPU path");
@@ -852,6 +899,7 @@ extern "C" int pg_solver_set_csr(pg_solver *s, const int32_t *row_ptr,
     s->eqn_pattern = 0;
   }
   int rj = join_factor(s);  // a pending factorisation still reads pvals
+  if (!rj) rj = join_coarse(s);
   if (rj) return rj;
   launch_permute_values((int)s->a.nnz, s->psrc.p, dv, s->pvals.p,
                         (int)s->a.dup_dst.size(), s->dup_dst.p, s->dup_src.p, st);
@@ -884,6 +932,7 @@ extern "C" int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e) {
     s->eqn_pattern = e->pattern_id;
   }
   int rj = join_factor(s);  // a pending factorisation still reads pvals
+  if (!rj) rj = join_coarse(s);
   if (rj) return rj;
   launch_permute_values((int)s->a.nnz, s->psrc.p, e->vals.p, s->pvals.p,
                         (int)s->a.dup_dst.size(), s->dup_dst.p, s->dup_src.p, st);
@@ -950,8 +999,35 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
   const RedWork w = s->red();
   double bb = 0.;
   int fp64_iters = 0;  // FP64 iterations after a float-float hand-over
-  int status = use_dd(s) ? run_bicgstab_dd(s, tol, s->cfg.max_iters, &iters, &outer, &bb)
-                         : run_bicgstab(s, tol, s->cfg.max_iters, &iters, &outer, &bb);
+  const bool dd = use_dd(s);
+  auto run = [&](int max_iters, int *it, int *up) {
+    return dd ? run_bicgstab_dd(s, tol, max_iters, it, up, &bb)
+              : run_bicgstab(s, tol, max_iters, it, up, &bb);
+  };
+  int status;
+  const int warm = s->cfg.coarse_warm >= 0 ? s->cfg.coarse_warm
+                   : s->a.n_sub >= kCoarseStagedK ? kCoarseWarmIters
+                                                  : 0;
+  if (s->coarse_pending && warm > 0 && s->cfg.max_iters > warm) {
+    // while the coarse inverse is built on side2: `warm` one-level
+    // iterations, then a restart from their x with the two-level
+    // preconditioner (a fixed count, so results do not depend on timing)
+    s->coarse_use = false;
+    status = run(warm, &iters, &outer);
+    s->coarse_use = true;
+    if (status == PG_MAX_ITERS || status == kDdStalled || status == PG_BREAKDOWN) {
+      int rj = join_coarse(s);
+      if (rj) return rj;
+      int it2 = 0, up2 = 0;
+      status = run(s->cfg.max_iters - iters, &it2, &up2);
+      iters += it2;
+      outer += up2;
+    }
+  } else {
+    int rj = join_coarse(s);
+    if (rj) return rj;
+    status = run(s->cfg.max_iters, &iters, &outer);
+  }
   if (status == kDdStalled) {
     // FP64 BiCGStab from the float-float solver's (folded FP64) iterate
     int it2 = 0, up2 = 0;
@@ -1020,6 +1096,7 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
   PG_CHECK_ARG(s->analysed && s->have_vals && s->have_x,
                "pg_solver_profile: solve a system first");
   int rj = join_factor(s);
+  if (!rj) rj = join_coarse(s);
   if (rj) return rj;
   cudaStream_t st = stream();
   const SolverDev d = s->dev();
@@ -1090,6 +1167,7 @@ extern "C" int pg_solver_apply_precond(pg_solver *s, const double *r,
   cudaStream_t st = stream();
   const int64_t n = s->a.n;
   int rc = s->fact_pending ? join_factor(s) : factor(s, st);
+  if (!rc) rc = join_coarse(s);
   if (rc) return rc;
   const SolverDev d = s->dev();  // after factor(): the sweep form is chosen
   const double *dr = r;
@@ -1145,6 +1223,7 @@ extern "C" int pg_solver_coarse_inverse(pg_solver *s, float *out, int *k) {
   PG_CHECK_ARG(s && s->analysed && s->coarse_on,
                "pg_solver_coarse_inverse: no coarse space");
   int rj = join_factor(s);
+  if (!rj) rj = join_coarse(s);
   if (rj) return rj;
   const size_t K = s->a.n_sub;
   if (k) *k = (int)K;
