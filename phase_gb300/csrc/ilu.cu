@@ -1,16 +1,19 @@
 // ILU(0) on Schwarz subdomains: numeric factorisation and the triangular
 // sweeps, on the packed per-subdomain records described in kernels.cuh.
 //
-// Apply (the hot kernel): one warp owns one subdomain.  Its factor is stored
-// as a stream of level-aligned pieces (kernels.cuh StreamMeta); lane 0 moves
-// the header and then the pieces into shared memory with cp.async.bulk (TMA)
-// into two alternating buffers completed on mbarriers, so the next piece
-// arrives while the current one is swept.  Within a piece the rows of a level
-// are slot-major (the lanes read consecutive addresses) and the warp
-// synchronises with __syncwarp between levels.  A warp needs only
-// header + 2 pieces + its z vector of shared memory (about 21 KB for a
-// 1024-row FP64 subdomain), so many subdomains run per SM and hide the
-// latency of the level chain.
+// Apply (the hot kernel): one warp owns one sweep group (one subdomain, or
+// two independent ones whose levels share the warp's lanes).  Its factor is
+// stored as a stream of level-aligned pieces (kernels.cuh StreamMeta); lane
+// 0 moves the header and the first two pieces into shared memory with
+// cp.async.bulk (TMA) while the warp stages the input vector, then refills
+// the two alternating buffers (completed on mbarriers with bounded waits) so
+// the next piece arrives while the current one is swept.  Within a piece the
+// rows of a level are slot-major (the lanes read consecutive addresses); each
+// lane reads its next level's columns and weights into registers while the
+// current level is swept, and the warp synchronises with __syncwarp between
+// levels.  A warp needs only header + 2 pieces + its z vector of shared
+// memory (about 21 KB for 1024 FP64 rows), so several groups run per SM.
+// With a coarse space the kernel also sums each subdomain's input.
 #include <cuda_runtime.h>
 
 #include <cstdint>

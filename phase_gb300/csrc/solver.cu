@@ -354,7 +354,8 @@ int join_factor(pg_solver *s) {
   return PG_OK;
 }
 
-// one chunk = kChunk BiCGStab iterations, 5 kernels each; captured once into
+// one chunk = kChunk BiCGStab iterations (5 kernels each, 7 with the coarse
+// correction); captured once into
 // a CUDA graph after the first direct chunk and replayed
 constexpr int kChunk = 8;
 constexpr double kDelta2 = 1e-4;  // reliable update when rr < kDelta2 * rr_ref
