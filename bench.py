@@ -9,8 +9,8 @@ rises one step at a time).  Two solvers run the same steps, each warm from
 its own previous solution as a time loop runs them:
 
   plain FP64      FP64 BiCGStab + two-level Schwarz ILU(0) (subdomain ILU(0)
-                  blocks plus a coarse correction on the subdomain-constant
-                  vectors; --coarse 0 for the one-level preconditioner),
+                  blocks plus a deflated coarse correction on the
+                  subdomain-constant vectors; --coarse 1 additive, 0 none),
                   guess = previous step's x
   learned+mixed   float-float BiCGStab + the same preconditioner (about
                   48-bit arithmetic on the FP32 pipes, FP64 true residual at
@@ -75,9 +75,10 @@ def parse():
                     help="mixed ILU(0) sweep form: 0 timed choice, 1 steps, "
                          "2 level blobs")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
-    ap.add_argument("--coarse", type=int, choices=(0, 1), default=1,
-                    help="two-level Schwarz: add the subdomain-constant "
-                         "coarse correction")
+    ap.add_argument("--coarse", type=int, choices=(0, 1, 2), default=2,
+                    help="two-level Schwarz coarse correction on the "
+                         "subdomain-constant vectors: 0 none, 1 additive, "
+                         "2 deflated (A-DEF1)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--mode", default="sequence",
@@ -474,7 +475,8 @@ def run_sequence(args):
                        "n_cells": n, "nnz": nnz, "tolerance": 1e-8,
                        "preconditioner": "Schwarz ILU(0), "
                        f"{sm.partition()[1]} subdomains"
-                       + (" + coarse correction" if args.coarse else ""),
+                       + {0: "", 1: " + additive coarse correction",
+                          2: " + deflated coarse correction (A-DEF1)"}[args.coarse],
                        "learned_weights": os.path.relpath(guess.DEFAULT_WEIGHTS, ROOT)
                        if have_w else None,
                        "l2": "256 MB flush write before every step; working "
@@ -632,7 +634,8 @@ def run_batch(args):
     # first factorisation in a warm-up pass, then timed)
     two_ms, two_ok, two_iters = [], True, []
     if world == 1:
-        s2s = [pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000, coarse=1)
+        s2s = [pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
+                                     coarse=args.coarse or 1)
                for _ in eqns]
         for s2, e in zip(s2s, eqns):
             s2.set_eqn(e)
@@ -892,7 +895,8 @@ def run_single(args):
                        "precision": args.precision,
                        "preconditioner": "Schwarz ILU(0), "
                        f"{solver.partition()[1]} subdomains"
-                       + (" + coarse correction" if args.coarse else ""),
+                       + {0: "", 1: " + additive coarse correction",
+                          2: " + deflated coarse correction (A-DEF1)"}[args.coarse],
                        "tolerance": 1e-8, "guess": "zero",
                        "l2": "256 MB flush write before every step; working "
                              "set > 129 MB L2"},

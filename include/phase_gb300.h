@@ -290,10 +290,14 @@ typedef struct {
                          first factorisation, 1 = warp-wide steps, 2 = level
                          blobs */
   int coarse;         /* PG_PREC_ILU0: 0 = one-level Schwarz (as Ifpack2);
-                         1 = add the two-level coarse correction on the
-                         space of subdomain-constant vectors (at most 2048
+                         two-level, with a coarse space of subdomain-constant
+                         vectors Z and y = (Z^T A Z)^-1 Z^T r (at most 2048
                          subdomains; pg_batch_*: a block per system, at most
-                         4096 subdomains each) */
+                         4096 subdomains each):
+                         1 = additive, M^-1 r = B r + Z y;
+                         2 = deflated (A-DEF1), M^-1 r = B (r - A Z y) + Z y
+                         (fewer iterations; pg_batch_* applies the additive
+                         form) */
   int coarse_warm;    /* one-level iterations a solve runs while the coarse
                          inverse is built beside them, before it restarts
                          with the two-level preconditioner: -1 = default (16

@@ -287,6 +287,172 @@ k_coarse_correct(int K, const int32_t *__restrict__ sub_ptr,
   }
 }
 
+// ------------------------------------------------ deflated application
+// A-DEF1 (Tang, Nabben, Vuik & Erlangga, J. Sci. Comput. 39, 2009):
+//     M^-1 r = B (r - A Z y) + Z y,   y = A_c^-1 Z^T r,
+// B the Schwarz ILU(0) sweeps.  A Z is kept per row as the sums of the
+// row's entries over each subdomain its columns fall in.
+
+// (A Z) values from the permuted matrix, row by row in entry order
+__global__ void k_az_values(int n, const int32_t *__restrict__ prp,
+                            const int32_t *__restrict__ azp,
+                            const uint8_t *__restrict__ azslot,
+                            const double *__restrict__ val,
+                            double *__restrict__ azv) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    for (int32_t q = azp[i]; q < azp[i + 1]; ++q) azv[q] = 0.;
+    for (int32_t k = prp[i]; k < prp[i + 1]; ++k) azv[azp[i] + azslot[k]] += val[k];
+  }
+}
+
+// the preconditioner's input with the fused BiCGStab update (written back
+// to pv) and its subdomain sums (one CTA per subdomain)
+__global__ void __launch_bounds__(kCoarseBlock)
+k_def_pre(int mode, const int32_t *__restrict__ sub_ptr,
+          const double *__restrict__ r, double *__restrict__ pv,
+          const double *__restrict__ v, const KScalars *__restrict__ sc,
+          float2 *__restrict__ csum) {
+  if (sc && sc->done) return;
+  __shared__ double red[kCoarseBlock];
+  const int s = blockIdx.x;
+  double acc = 0.;
+  for (int32_t i = sub_ptr[s] + threadIdx.x; i < sub_ptr[s + 1]; i += kCoarseBlock) {
+    const double val = pre_combine<double>(mode, mode ? r[i] : 0.,
+                                           mode != 2 ? pv[i] : 0.,
+                                           mode ? v[i] : 0., sc);
+    if (mode) pv[i] = val;
+    acc += val;
+  }
+  const double t = block_sum(acc, red);
+  if (threadIdx.x == 0) csum[s] = dd_from(t);
+}
+
+// y_s = (A_c^-1)_s . csum (compensated float-float dot, as k_coarse_correct)
+__global__ void __launch_bounds__(kCorrectBlock)
+k_coarse_y(int K, const float *__restrict__ ainv,
+           const float2 *__restrict__ csum, double *__restrict__ y,
+           const KScalars *__restrict__ sc) {
+  if (sc && sc->done) return;
+  __shared__ float red_s[kCorrectBlock / 32], red_c[kCorrectBlock / 32];
+  const int s = blockIdx.x;
+  const float *row = ainv + (size_t)s * K;
+  DdAcc acc = dd_acc(make_float2(0.f, 0.f));
+  for (int j = threadIdx.x; j < K; j += kCorrectBlock)
+    dd_acc_fma(acc, make_float2(row[j], 0.f), csum[j]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    DdAcc b;
+    b.s = __shfl_xor_sync(0xffffffffu, acc.s, o);
+    b.c = __shfl_xor_sync(0xffffffffu, acc.c, o);
+    dd_acc_merge(acc, b);
+  }
+  const int wid = threadIdx.x / 32;
+  if ((threadIdx.x & 31) == 0) {
+    red_s[wid] = acc.s;
+    red_c[wid] = acc.c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    DdAcc u = dd_acc(make_float2(red_s[0], red_c[0]));
+    for (int w = 1; w < kCorrectBlock / 32; ++w) {
+      DdAcc b;
+      b.s = red_s[w];
+      b.c = red_c[w];
+      dd_acc_merge(u, b);
+    }
+    y[s] = dd_acc_to_double(u);
+  }
+}
+
+// t = pv - (A Z) y
+__global__ void k_def_in(int n, const int32_t *__restrict__ azp,
+                         const int32_t *__restrict__ azj,
+                         const double *__restrict__ azv,
+                         const double *__restrict__ y,
+                         const double *__restrict__ pv, double *__restrict__ t,
+                         const KScalars *__restrict__ sc) {
+  if (sc && sc->done) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    double acc = pv[i];
+    for (int32_t q = azp[i]; q < azp[i + 1]; ++q) acc -= azv[q] * y[azj[q]];
+    t[i] = acc;
+  }
+}
+
+// z += y_s on the rows of subdomain s
+__global__ void __launch_bounds__(kCorrectBlock)
+k_coarse_add(const int32_t *__restrict__ sub_ptr, const double *__restrict__ y,
+             double *__restrict__ z, const KScalars *__restrict__ sc) {
+  if (sc && sc->done) return;
+  const int s = blockIdx.x;
+  const double ys = y[s];
+  for (int32_t i = sub_ptr[s] + threadIdx.x; i < sub_ptr[s + 1]; i += kCorrectBlock)
+    z[i] += ys;
+}
+
+// float-float forms of the deflated application (the mixed solver)
+__global__ void __launch_bounds__(kCoarseBlock)
+k_def_pre_dd(int mode, const int32_t *__restrict__ sub_ptr,
+             const float2 *__restrict__ r, float2 *__restrict__ pv,
+             const float2 *__restrict__ v, const KScalars *__restrict__ sc,
+             float2 *__restrict__ csum) {
+  if (sc && sc->done) return;
+  __shared__ double red[kCoarseBlock];
+  const int s = blockIdx.x;
+  const float2 zero = make_float2(0.f, 0.f);
+  DdAcc acc = dd_acc(zero);
+  for (int32_t i = sub_ptr[s] + threadIdx.x; i < sub_ptr[s + 1]; i += kCoarseBlock) {
+    const float2 val = dd_pre_combine(mode, mode ? r[i] : zero,
+                                      mode != 2 ? pv[i] : zero,
+                                      mode ? v[i] : zero, sc);
+    if (mode) pv[i] = val;
+    dd_acc_add(acc, val);
+  }
+  const double t = block_sum(dd_acc_to_double(acc), red);
+  if (threadIdx.x == 0) csum[s] = dd_from(t);
+}
+
+// y as float pairs (one conversion per subdomain)
+__global__ void k_y_split(int K, const double *__restrict__ y,
+                          float2 *__restrict__ y_dd,
+                          const KScalars *__restrict__ sc) {
+  if (sc && sc->done) return;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < K;
+       s += gridDim.x * blockDim.x)
+    y_dd[s] = dd_from(y[s]);
+}
+
+// t = pv - (A Z) y in float-float
+__global__ void k_def_in_dd(int n, const int32_t *__restrict__ azp,
+                            const int32_t *__restrict__ azj,
+                            const float2 *__restrict__ azv,
+                            const float2 *__restrict__ y,
+                            const float2 *__restrict__ pv,
+                            float2 *__restrict__ t,
+                            const KScalars *__restrict__ sc) {
+  if (sc && sc->done) return;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x) {
+    DdAcc acc = dd_acc(pv[i]);
+    for (int32_t q = azp[i]; q < azp[i + 1]; ++q)
+      dd_acc_fma(acc, dd_neg(azv[q]), y[azj[q]]);
+    t[i] = dd_value(acc);
+  }
+}
+
+__global__ void __launch_bounds__(kCorrectBlock)
+k_coarse_add_dd(const int32_t *__restrict__ sub_ptr,
+                const float2 *__restrict__ y, float2 *__restrict__ z,
+                const KScalars *__restrict__ sc) {
+  if (sc && sc->done) return;
+  const int s = blockIdx.x;
+  const float2 ys = y[s];
+  for (int32_t i = sub_ptr[s] + threadIdx.x; i < sub_ptr[s + 1]; i += kCorrectBlock)
+    z[i] = dd_add(z[i], ys);
+}
+
 // ------------------------------------------------------ batched systems
 // Block-diagonal coarse space of stacked independent systems: system t owns
 // subdomains [k0[t], k0[t+1]) and a dense K_t x K_t block of A_c at float
@@ -412,6 +578,55 @@ k_coarse_correct_b(CoarseBatchDev c, double *__restrict__ z,
 }
 
 }  // namespace
+
+void launch_az_values(const CoarseDev &c, int n, const int32_t *prp,
+                      const double *pvals, cudaStream_t st) {
+  const int g = (n + 255) / 256 < 2432 ? (n + 255) / 256 : 2432;
+  k_az_values<<<g, 256, 0, st>>>(n, prp, c.azp, c.azslot, pvals, c.azv);
+  count_launches(1);
+}
+
+void launch_def_pre(const CoarseDev &c, int mode, const double *r, double *pv,
+                    const double *v, const KScalars *sc, cudaStream_t st) {
+  k_def_pre<<<c.K, kCoarseBlock, 0, st>>>(mode, c.sub_ptr, r, pv, v, sc, c.csum);
+  k_coarse_y<<<c.K, kCorrectBlock, 0, st>>>(c.K, c.ac, c.csum, c.y, sc);
+  count_launches(2);
+}
+
+void launch_def_in(const CoarseDev &c, int n, const double *pv, double *t,
+                   const KScalars *sc, cudaStream_t st) {
+  const int g = (n + 255) / 256 < 2432 ? (n + 255) / 256 : 2432;
+  k_def_in<<<g, 256, 0, st>>>(n, c.azp, c.azj, c.azv, c.y, pv, t, sc);
+  count_launches(1);
+}
+
+void launch_coarse_add(const CoarseDev &c, double *z, const KScalars *sc,
+                       cudaStream_t st) {
+  k_coarse_add<<<c.K, kCorrectBlock, 0, st>>>(c.sub_ptr, c.y, z, sc);
+  count_launches(1);
+}
+
+void launch_def_pre_dd(const CoarseDev &c, int mode, const float2 *r,
+                       float2 *pv, const float2 *v, const KScalars *sc,
+                       cudaStream_t st) {
+  k_def_pre_dd<<<c.K, kCoarseBlock, 0, st>>>(mode, c.sub_ptr, r, pv, v, sc, c.csum);
+  k_coarse_y<<<c.K, kCorrectBlock, 0, st>>>(c.K, c.ac, c.csum, c.y, sc);
+  k_y_split<<<(c.K + 255) / 256, 256, 0, st>>>(c.K, c.y, c.y_dd, sc);
+  count_launches(3);
+}
+
+void launch_def_in_dd(const CoarseDev &c, int n, const float2 *pv, float2 *t,
+                      const KScalars *sc, cudaStream_t st) {
+  const int g = (n + 255) / 256 < 2432 ? (n + 255) / 256 : 2432;
+  k_def_in_dd<<<g, 256, 0, st>>>(n, c.azp, c.azj, c.azv_dd, c.y_dd, pv, t, sc);
+  count_launches(1);
+}
+
+void launch_coarse_add_dd(const CoarseDev &c, float2 *z, const KScalars *sc,
+                          cudaStream_t st) {
+  k_coarse_add_dd<<<c.K, kCorrectBlock, 0, st>>>(c.sub_ptr, c.y_dd, z, sc);
+  count_launches(1);
+}
 
 void launch_coarse_setup_b(const CoarseBatchDev &c, int K, int64_t n_blk,
                            const double *pvals, const int32_t *prp,

@@ -550,6 +550,23 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       a.cnb.insert(a.cnb.end(), nb.begin(), nb.end());
       a.cptr[s + 1] = (int32_t)a.cnb.size();
     }
+    // A Z per row (deflated coarse correction): the subdomains of the row's
+    // columns, ascending, and each entry's position among them
+    a.azp.assign(n + 1, 0);
+    a.azj.clear();
+    a.azslot.assign(a.nnz, 0);
+    std::vector<int32_t> rs;
+    for (int64_t i = 0; i < n; ++i) {
+      rs.clear();
+      for (int32_t k = a.prp[i]; k < a.prp[i + 1]; ++k) rs.push_back(sub_of[a.pci[k]]);
+      std::sort(rs.begin(), rs.end());
+      rs.erase(std::unique(rs.begin(), rs.end()), rs.end());
+      for (int32_t k = a.prp[i]; k < a.prp[i + 1]; ++k)
+        a.azslot[k] = (uint8_t)(std::lower_bound(rs.begin(), rs.end(),
+                                                 sub_of[a.pci[k]]) - rs.begin());
+      a.azj.insert(a.azj.end(), rs.begin(), rs.end());
+      a.azp[i + 1] = (int32_t)a.azj.size();
+    }
   }
 
   // 6. ILU(0) storage: the entries of each row inside its subdomain,

@@ -223,6 +223,11 @@ struct Analysis {
   std::vector<int32_t> cptr, cnb;
   std::vector<uint8_t> cslot;
   int max_cnb = 0;
+  // A Z (Z the subdomain indicators) per permuted row: the subdomains
+  // azj[azp[i] .. azp[i+1]) its columns fall in, and each entry's position
+  // among them (azslot[k])
+  std::vector<int32_t> azp, azj;
+  std::vector<uint8_t> azslot;
 };
 
 // most subdomains one coarse matrix row may couple to

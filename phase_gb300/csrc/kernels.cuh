@@ -209,7 +209,33 @@ struct CoarseDev {
   float *ac = nullptr, *dg0 = nullptr;
   float *pinv = nullptr, *W = nullptr, *V = nullptr, *C = nullptr;
   float2 *csum = nullptr;
+  // deflated application (cfg.coarse = 2): A Z per row, y, the deflated
+  // input
+  const int32_t *azp = nullptr, *azj = nullptr;
+  const uint8_t *azslot = nullptr;
+  double *azv = nullptr, *y = nullptr, *tmp = nullptr;
+  // float-float copies for the mixed solver
+  float2 *azv_dd = nullptr, *y_dd = nullptr, *tmp_dd = nullptr;
 };
+void launch_az_values(const CoarseDev &c, int n, const int32_t *prp,
+                      const double *pvals, cudaStream_t st);
+// pv = the preconditioner's input (fused update), csum = Z^T pv, y = A_c^-1 csum
+void launch_def_pre(const CoarseDev &c, int mode, const double *r, double *pv,
+                    const double *v, const KScalars *sc, cudaStream_t st);
+// t = pv - (A Z) y
+void launch_def_in(const CoarseDev &c, int n, const double *pv, double *t,
+                   const KScalars *sc, cudaStream_t st);
+// z += Z y
+void launch_coarse_add(const CoarseDev &c, double *z, const KScalars *sc,
+                       cudaStream_t st);
+// the same in float-float (azv_dd, y_dd, tmp_dd)
+void launch_def_pre_dd(const CoarseDev &c, int mode, const float2 *r,
+                       float2 *pv, const float2 *v, const KScalars *sc,
+                       cudaStream_t st);
+void launch_def_in_dd(const CoarseDev &c, int n, const float2 *pv, float2 *t,
+                      const KScalars *sc, cudaStream_t st);
+void launch_coarse_add_dd(const CoarseDev &c, float2 *z, const KScalars *sc,
+                          cudaStream_t st);
 
 // Block-diagonal coarse space of a batch of independent systems: system t
 // owns subdomains [k0[t], k0[t+1]) and a dense K_t x K_t FP32 block of A_c

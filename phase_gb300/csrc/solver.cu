@@ -107,6 +107,10 @@ struct pg_solver {
   DevBuf<uint8_t> c_slot;
   DevBuf<float> c_ac, c_dg0, c_pinv, c_W, c_V, c_C;
   DevBuf<float2> c_sum;
+  DevBuf<int32_t> c_azp, c_azj;
+  DevBuf<uint8_t> c_azslot;
+  DevBuf<double> c_azv, c_y, c_tmp;
+  DevBuf<float2> c_azv_dd, c_y_dd, c_tmp_dd;
   cudaGraphExec_t gj_graph = nullptr;
 
   void drop_graphs() {
@@ -137,6 +141,15 @@ struct pg_solver {
     c.V = c_V.p;
     c.C = c_C.p;
     c.csum = c_sum.p;
+    c.azp = c_azp.p;
+    c.azj = c_azj.p;
+    c.azslot = c_azslot.p;
+    c.azv = c_azv.p;
+    c.y = c_y.p;
+    c.tmp = c_tmp.p;
+    c.azv_dd = c_azv_dd.p;
+    c.y_dd = c_y_dd.p;
+    c.tmp_dd = c_tmp_dd.p;
     return c;
   }
 
@@ -306,6 +319,19 @@ int upload_analysis(pg_solver *s) {
     for (DevBuf<float> *bf : {&s->c_W, &s->c_V, &s->c_C})
       if (e == cudaSuccess) e = bf->reserve(32 * K);
     if (e == cudaSuccess) e = s->c_sum.reserve(K);
+    if (s->cfg.coarse == 2) {
+      up(s->c_azp, a.azp);
+      up(s->c_azj, a.azj);
+      up(s->c_azslot, a.azslot);
+      if (e == cudaSuccess) e = s->c_azv.reserve(a.azj.size());
+      if (e == cudaSuccess) e = s->c_y.reserve(K);
+      if (e == cudaSuccess) e = s->c_tmp.reserve(a.n);
+      if (s->cfg.precision == PG_MIXED) {
+        if (e == cudaSuccess) e = s->c_azv_dd.reserve(a.azj.size());
+        if (e == cudaSuccess) e = s->c_y_dd.reserve(K);
+        if (e == cudaSuccess) e = s->c_tmp_dd.reserve(a.n);
+      }
+    }
     s->coarse_on = true;
   }
   s->red_grid = (int)std::min<int64_t>(red_grid_cap(), (n + kVecBlock - 1) / kVecBlock);
@@ -426,7 +452,18 @@ int run_bicgstab(pg_solver *s, double tol, int max_iters, int *iters,
   double *const ss = s->s.p, *const sh = s->sh.p, *const t = s->t.p;
   const CoarseDev cdev = s->coarse();
   const bool ilu_stream = s->cfg.precond == PG_PREC_ILU0 && d.smem64 > 0;
+  SolverDev d0 = d;  // the deflated form's sweep needs no subdomain sums
+  d0.csum = nullptr;
   auto precond = [&](int mode, double *pv, double *z) {
+    if (cdev.K && s->cfg.coarse == 2) {
+      // A-DEF1: y = A_c^-1 Z^T p, z = B (p - A Z y) + Z y
+      launch_def_pre(cdev, mode, r, pv, v, s->sc.p, st);
+      launch_def_in(cdev, d.n, pv, cdev.tmp, s->sc.p, st);
+      launch_precond<double, double>(s->cfg.precond, 0, d0, jd, r, cdev.tmp,
+                                     v, z, s->sc.p, st);
+      launch_coarse_add(cdev, z, s->sc.p, st);
+      return;
+    }
     launch_precond<double, double>(s->cfg.precond, mode, d, jd, r, pv, v, z,
                                    s->sc.p, st);
     // the input (p or s) is in pv after the fused update; the streamed
@@ -536,7 +573,20 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
   float2 *const p = s->pd.p, *const v = s->vd.p, *const ph = s->phd.p;
   float2 *const ss = s->sd.p, *const sh = s->shd.p, *const t = s->td.p;
   const CoarseDev cdev = s->coarse();
+  SolverDev d0 = d;  // the deflated form's sweep needs no subdomain sums
+  d0.csum = nullptr;
   auto precond = [&](int mode, float2 *pv, float2 *z) {
+    if (cdev.K && s->cfg.coarse == 2) {
+      // A-DEF1 in float-float
+      launch_def_pre_dd(cdev, mode, r, pv, v, s->sc.p, st);
+      launch_def_in_dd(cdev, n, pv, cdev.tmp_dd, s->sc.p, st);
+      if (ilu)
+        launch_ilu0_apply_dd(0, d0, r, cdev.tmp_dd, v, z, s->sc.p, st);
+      else
+        launch_dd_diag_apply(0, n, jd, r, cdev.tmp_dd, v, z, s->sc.p, st);
+      launch_coarse_add_dd(cdev, z, s->sc.p, st);
+      return;
+    }
     if (ilu)
       launch_ilu0_apply_dd(mode, d, r, pv, v, z, s->sc.p, st);
     else
@@ -715,6 +765,12 @@ int factor(pg_solver *s, cudaStream_t st) {
       s->coarse_use = true;
       launch_coarse_setup(s->coarse(), s->pvals.p, s->prp.p, &s->gj_graph,
                           s->side2);
+      if (s->cfg.coarse == 2) {
+        launch_az_values(s->coarse(), (int)s->a.n, s->prp.p, s->pvals.p, s->side2);
+        if (dd)
+          launch_dd_split((int64_t)s->a.azj.size(), s->c_azv.p, 1.0,
+                          s->c_azv_dd.p, s->side2);
+      }
       s->coarse_use = use;
       PG_CUDA(cudaEventRecord(s->ev_coarse, s->side2));
       s->coarse_pending = true;
@@ -775,7 +831,7 @@ extern "C" int pg_solver_create(const pg_solver_cfg *cfg, pg_solver **out) {
                "pg_solver_create: bad precision");
   PG_CHECK_ARG(c.mixed_sweep >= 0 && c.mixed_sweep <= 2,
                "pg_solver_create: bad mixed_sweep");
-  PG_CHECK_ARG(c.coarse == 0 || c.coarse == 1, "pg_solver_create: bad coarse");
+  PG_CHECK_ARG(c.coarse >= 0 && c.coarse <= 2, "pg_solver_create: bad coarse");
   PG_CHECK_ARG(c.coarse_warm >= -1, "pg_solver_create: bad coarse_warm");
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0 || !stream()) {
@@ -1180,23 +1236,46 @@ extern "C" int pg_solver_apply_precond(pg_solver *s, const double *r,
   launch_permute_vec((int)n, s->perm.p, dr, 1.0, s->p.p, st);
   if (use_dd(s)) {
     launch_dd_split(n, s->p.p, 1.0, s->pd.p, st);
+    const bool def = s->coarse_on && s->cfg.coarse == 2;
+    const CoarseDev c = s->coarse();
+    SolverDev d0 = d;
+    d0.csum = def ? nullptr : d.csum;
+    float2 *in = s->pd.p;
+    if (def) {  // A-DEF1: the sweep runs on p - A Z y
+      launch_def_pre_dd(c, 0, nullptr, s->pd.p, nullptr, nullptr, st);
+      launch_def_in_dd(c, (int)n, s->pd.p, c.tmp_dd, nullptr, st);
+      in = c.tmp_dd;
+    }
     if (s->cfg.precond == PG_PREC_ILU0)
-      launch_ilu0_apply_dd(0, d, nullptr, s->pd.p, nullptr, s->phd.p, nullptr, st);
+      launch_ilu0_apply_dd(0, d0, nullptr, in, nullptr, s->phd.p, nullptr, st);
     else
       launch_dd_diag_apply(0, (int)n, s->cfg.precond == PG_PREC_JACOBI ? s->jdinv_dd.p : nullptr,
-                           nullptr, s->pd.p, nullptr, s->phd.p, nullptr, st);
-    if (s->coarse_on)
-      launch_coarse_apply_dd(s->coarse(), s->pd.p, s->phd.p,
+                           nullptr, in, nullptr, s->phd.p, nullptr, st);
+    if (def)
+      launch_coarse_add_dd(c, s->phd.p, nullptr, st);
+    else if (s->coarse_on)
+      launch_coarse_apply_dd(c, s->pd.p, s->phd.p,
                              s->cfg.precond == PG_PREC_ILU0 && d.dd_stream,
                              nullptr, st);
     launch_dd_join((int)n, s->phd.p, 1.0, s->ph.p, st);
   } else {
-    launch_precond<double, double>(s->cfg.precond, 0, d, s->jdinv.p, nullptr,
-                                   s->p.p, nullptr, s->ph.p, nullptr, st);
-    if (s->coarse_on)
-      launch_coarse_apply(s->coarse(), s->p.p, s->ph.p,
-                          s->cfg.precond == PG_PREC_ILU0 && d.smem64 > 0,
-                          nullptr, st);
+    if (s->coarse_on && s->cfg.coarse == 2) {
+      const CoarseDev c = s->coarse();
+      SolverDev d0 = d;
+      d0.csum = nullptr;
+      launch_def_pre(c, 0, nullptr, s->p.p, nullptr, nullptr, st);
+      launch_def_in(c, d.n, s->p.p, c.tmp, nullptr, st);
+      launch_precond<double, double>(s->cfg.precond, 0, d0, s->jdinv.p, nullptr,
+                                     c.tmp, nullptr, s->ph.p, nullptr, st);
+      launch_coarse_add(c, s->ph.p, nullptr, st);
+    } else {
+      launch_precond<double, double>(s->cfg.precond, 0, d, s->jdinv.p, nullptr,
+                                     s->p.p, nullptr, s->ph.p, nullptr, st);
+      if (s->coarse_on)
+        launch_coarse_apply(s->coarse(), s->p.p, s->ph.p,
+                            s->cfg.precond == PG_PREC_ILU0 && d.smem64 > 0,
+                            nullptr, st);
+    }
   }
   launch_unpermute_vec((int)n, s->perm.p, s->ph.p, s->t.p, st);
   PG_CUDA(cudaGetLastError());

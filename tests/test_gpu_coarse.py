@@ -33,9 +33,12 @@ def _coarse(rp, ci, v, part, nparts):
     return Z, (Z.T @ A @ Z).toarray()
 
 
+@pytest.mark.parametrize("variant", [1, 2])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("mesh", ["bubble", "tri"])
-def test_two_level_apply_matches_oracle(pg, oracle, precision, mesh):
+def test_two_level_apply_matches_oracle(pg, oracle, precision, mesh, variant):
+    """variant 1: additive, z = B r + Z X Z^T r; variant 2: deflated
+    (A-DEF1), z = B (r - A Z y) + Z y with y = X Z^T r."""
     if mesh == "bubble":
         m, w, eqn = _bubble(pg, 128, 96)
         sub = 256
@@ -54,7 +57,7 @@ def test_two_level_apply_matches_oracle(pg, oracle, precision, mesh):
     rp, ci, v, rhs = eqn.export()
     keep = ci >= 0
     n = len(rp) - 1
-    s = pg.SparseMatrixSolver(subdomain_rows=sub, coarse=1,
+    s = pg.SparseMatrixSolver(subdomain_rows=sub, coarse=variant,
                               precision=pg.FP64 if precision == "fp64" else pg.MIXED)
     s.set_eqn(eqn)
     part, nparts = s.partition()
@@ -79,8 +82,13 @@ def test_two_level_apply_matches_oracle(pg, oracle, precision, mesh):
     # ... and applied exactly (FP64): the operator is the oracle's ILU(0)
     # sweeps plus Z X Z^T
     tol = 1e-12 if precision == "fp64" else 1e-10
+    AZ = sp.csr_matrix((av, aci, arp), shape=(n, n)) @ Z
     for r, z in ((r1, z1), (r2, z2)):
-        zo = oracle.ilu0_apply(arp, aci, lu, r, part) + Z @ (X @ (Z.T @ r))
+        y = X @ (Z.T @ r)
+        if variant == 1:
+            zo = oracle.ilu0_apply(arp, aci, lu, r, part) + Z @ y
+        else:
+            zo = oracle.ilu0_apply(arp, aci, lu, r - AZ @ y, part) + Z @ y
         assert np.all(np.isfinite(z))
         assert np.linalg.norm(z - zo) / np.linalg.norm(zo) < tol
     # a fixed linear operator
@@ -88,8 +96,9 @@ def test_two_level_apply_matches_oracle(pg, oracle, precision, mesh):
     assert np.linalg.norm(z12 - (0.75 * z1 - 2.0 * z2)) / np.linalg.norm(z12) < tol
 
 
+@pytest.mark.parametrize("variant", [1, 2])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_two_level_solve_converges_faster(pg, precision):
+def test_two_level_solve_converges_faster(pg, precision, variant):
     m, w, eqn = _bubble(pg, 256, 256)
     rp, ci, v, rhs = eqn.export()
     keep = ci >= 0
@@ -98,7 +107,7 @@ def test_two_level_solve_converges_faster(pg, precision):
     A = sp.csr_matrix((v[keep], (rows, ci[keep])), shape=(n, n))
     b = -rhs
     its = {}
-    for coarse in (0, 1):
+    for coarse in (0, variant):
         s = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000, coarse=coarse,
                                   precision=pg.FP64 if precision == "fp64" else pg.MIXED)
         s.set_eqn(eqn)
@@ -108,7 +117,7 @@ def test_two_level_solve_converges_faster(pg, precision):
         assert np.linalg.norm(b - A @ x) / np.linalg.norm(b) <= 1.01e-8
         its[coarse] = s.nIters()
     print("iterations one-level / two-level:", its)
-    assert its[1] < its[0]
+    assert its[variant] < its[0]
 
 
 def test_two_level_singular_cavity(pg):
