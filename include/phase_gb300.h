@@ -296,8 +296,7 @@ typedef struct {
                          4096 subdomains each):
                          1 = additive, M^-1 r = B r + Z y;
                          2 = deflated (A-DEF1), M^-1 r = B (r - A Z y) + Z y
-                         (fewer iterations; pg_batch_* applies the additive
-                         form) */
+                         (fewer iterations) */
   int coarse_warm;    /* one-level iterations a solve runs while the coarse
                          inverse is built beside them, before it restarts
                          with the two-level preconditioner: -1 = default (16

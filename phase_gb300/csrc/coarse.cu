@@ -577,7 +577,102 @@ k_coarse_correct_b(CoarseBatchDev c, double *__restrict__ z,
     z[i] += y;
 }
 
+// deflated application for batches: one CTA per subdomain, the scalars of
+// its system (done systems skip)
+__global__ void __launch_bounds__(kCoarseBlock)
+k_def_pre_b(int mode, CoarseBatchDev c, const double *__restrict__ r,
+            double *__restrict__ pv, const double *__restrict__ v,
+            const KScalars *__restrict__ sc_base) {
+  const int s = blockIdx.x;
+  const KScalars *sc = sc_base + c.sub_sys[s];
+  if (sc->done) return;
+  __shared__ double red[kCoarseBlock];
+  double acc = 0.;
+  for (int32_t i = c.sub_ptr[s] + threadIdx.x; i < c.sub_ptr[s + 1]; i += kCoarseBlock) {
+    const double val = pre_combine<double>(mode, mode ? r[i] : 0.,
+                                           mode != 2 ? pv[i] : 0.,
+                                           mode ? v[i] : 0., sc);
+    if (mode) pv[i] = val;
+    acc += val;
+  }
+  const double t = block_sum(acc, red);
+  if (threadIdx.x == 0) c.csum[s] = dd_from(t);
+}
+
+__global__ void __launch_bounds__(kCorrectBlock)
+k_coarse_y_b(CoarseBatchDev c, const KScalars *__restrict__ sc) {
+  const int s = blockIdx.x;
+  const int t = c.sub_sys[s];
+  if (sc[t].done) return;
+  __shared__ float red_s[kCorrectBlock / 32], red_c[kCorrectBlock / 32];
+  const int k0 = c.k0[t], Kt = c.k0[t + 1] - k0;
+  const float *row = c.ac + c.off[t] + (size_t)(s - k0) * Kt;
+  DdAcc acc = dd_acc(make_float2(0.f, 0.f));
+  for (int j = threadIdx.x; j < Kt; j += kCorrectBlock)
+    dd_acc_fma(acc, make_float2(row[j], 0.f), c.csum[k0 + j]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    DdAcc b;
+    b.s = __shfl_xor_sync(0xffffffffu, acc.s, o);
+    b.c = __shfl_xor_sync(0xffffffffu, acc.c, o);
+    dd_acc_merge(acc, b);
+  }
+  const int wid = threadIdx.x / 32;
+  if ((threadIdx.x & 31) == 0) {
+    red_s[wid] = acc.s;
+    red_c[wid] = acc.c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    DdAcc u = dd_acc(make_float2(red_s[0], red_c[0]));
+    for (int w = 1; w < kCorrectBlock / 32; ++w) {
+      DdAcc b;
+      b.s = red_s[w];
+      b.c = red_c[w];
+      dd_acc_merge(u, b);
+    }
+    c.y[s] = dd_acc_to_double(u);
+  }
+}
+
+__global__ void __launch_bounds__(kCorrectBlock)
+k_def_in_b(CoarseBatchDev c, const double *__restrict__ pv,
+           double *__restrict__ tmp, const KScalars *__restrict__ sc) {
+  const int s = blockIdx.x;
+  if (sc[c.sub_sys[s]].done) return;
+  for (int32_t i = c.sub_ptr[s] + threadIdx.x; i < c.sub_ptr[s + 1]; i += kCorrectBlock) {
+    double acc = pv[i];
+    for (int32_t q = c.azp[i]; q < c.azp[i + 1]; ++q) acc -= c.azv[q] * c.y[c.azj[q]];
+    tmp[i] = acc;
+  }
+}
+
+__global__ void __launch_bounds__(kCorrectBlock)
+k_coarse_add_b(CoarseBatchDev c, double *__restrict__ z,
+               const KScalars *__restrict__ sc) {
+  const int s = blockIdx.x;
+  if (sc[c.sub_sys[s]].done) return;
+  const double ys = c.y[s];
+  for (int32_t i = c.sub_ptr[s] + threadIdx.x; i < c.sub_ptr[s + 1]; i += kCorrectBlock)
+    z[i] += ys;
+}
+
 }  // namespace
+
+void launch_def_pre_b(const CoarseBatchDev &c, int K, int mode, const double *r,
+                      double *pv, const double *v, double *tmp,
+                      const KScalars *sc, cudaStream_t st) {
+  k_def_pre_b<<<K, kCoarseBlock, 0, st>>>(mode, c, r, pv, v, sc);
+  k_coarse_y_b<<<K, kCorrectBlock, 0, st>>>(c, sc);
+  k_def_in_b<<<K, kCorrectBlock, 0, st>>>(c, pv, tmp, sc);
+  count_launches(3);
+}
+
+void launch_coarse_add_b(const CoarseBatchDev &c, int K, double *z,
+                         const KScalars *sc, cudaStream_t st) {
+  k_coarse_add_b<<<K, kCorrectBlock, 0, st>>>(c, z, sc);
+  count_launches(1);
+}
 
 void launch_az_values(const CoarseDev &c, int n, const int32_t *prp,
                       const double *pvals, cudaStream_t st) {

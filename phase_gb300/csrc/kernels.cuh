@@ -249,12 +249,23 @@ struct CoarseBatchDev {
   const int32_t *sub_sys = nullptr;
   float *ac = nullptr;
   float2 *csum = nullptr;
+  // deflated form (cfg.coarse = 2): A Z per row and y per subdomain
+  const int32_t *azp = nullptr, *azj = nullptr;
+  const double *azv = nullptr;
+  double *y = nullptr;
 };
 // A_c blocks from the permuted values, each inverted in place (one CTA per
 // system; n_blk = total floats of the blocks)
 void launch_coarse_setup_b(const CoarseBatchDev &c, int K, int64_t n_blk,
                            const double *pvals, const int32_t *prp,
                            cudaStream_t st);
+// deflated form for batches: pv = the input (fused update), y = A_t^-1
+// Z^T pv per system, tmp = pv - A Z y; then (after the sweep) z += Z y
+void launch_def_pre_b(const CoarseBatchDev &c, int K, int mode, const double *r,
+                      double *pv, const double *v, double *tmp,
+                      const KScalars *sc, cudaStream_t st);
+void launch_coarse_add_b(const CoarseBatchDev &c, int K, double *z,
+                         const KScalars *sc, cudaStream_t st);
 // z += Z A_c^-1 Z^T in for the systems still running
 void launch_coarse_apply_b(const CoarseBatchDev &c, int K, const double *in,
                            double *z, bool have_sums, const KScalars *sc,

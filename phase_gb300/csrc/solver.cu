@@ -1353,6 +1353,10 @@ struct pg_batch {
   DevBuf<uint8_t> c_slot;
   DevBuf<float> c_ac;
   DevBuf<float2> c_sum;
+  DevBuf<int32_t> c_azp, c_azj;
+  DevBuf<uint8_t> c_azslot;
+  DevBuf<double> c_azv, c_y, c_tmp;
+  bool deflated() const { return coarse && s->cfg.coarse == 2; }
 
   ~pg_batch() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -1384,6 +1388,10 @@ struct pg_batch {
     c.sub_sys = sub_sys.p;
     c.ac = c_ac.p;
     c.csum = c_sum.p;
+    c.azp = c_azp.p;
+    c.azj = c_azj.p;
+    c.azv = c_azv.p;
+    c.y = c_y.p;
     return c;
   }
 };
@@ -1535,6 +1543,14 @@ int batch_analyse(pg_batch *b, const std::vector<int32_t> &rp,
     PG_CUDA(b->c_slot.upload(a.cslot));
     PG_CUDA(b->c_ac.reserve((size_t)b->n_blk));
     PG_CUDA(b->c_sum.reserve((size_t)a.n_sub));
+    if (s->cfg.coarse == 2) {
+      PG_CUDA(b->c_azp.upload(a.azp));
+      PG_CUDA(b->c_azj.upload(a.azj));
+      PG_CUDA(b->c_azslot.upload(a.azslot));
+      PG_CUDA(b->c_azv.reserve(a.azj.size()));
+      PG_CUDA(b->c_y.reserve((size_t)a.n_sub));
+      PG_CUDA(b->c_tmp.reserve((size_t)a.n));
+    }
     b->coarse = true;
   }
   PG_CUDA(b->sc.reserve(b->n_sys));
@@ -1559,6 +1575,8 @@ int build_batch_graph(pg_batch *b) {
   cudaStream_t st = stream();
   pg_solver *s = b->s;
   const SolverDev d = b->dev();
+  SolverDev d0 = d;  // the deflated form's sweep needs no subdomain sums
+  d0.csum = nullptr;
   const CoarseBatchDev cb = b->coarse_dev();
   const BatchTiles T = b->tiles();
   const BatchRed R = b->red();
@@ -1583,18 +1601,34 @@ int build_batch_graph(pg_batch *b) {
                                     cudaStreamCaptureModeRelaxed);
   if (e == cudaSuccess) {
     for (int c = 0; c < kChunk; ++c) {
-      launch_precond<double, double>(PG_PREC_ILU0, 1, d, nullptr, s->r.p,
-                                     s->p.p, s->v.p, s->ph.p, b->sc.p, st);
-      if (b->coarse)
-        launch_coarse_apply_b(cb, d.n_sub, s->p.p, s->ph.p, d.smem64 > 0,
-                              b->sc.p, st);
+      if (b->deflated()) {
+        launch_def_pre_b(cb, d.n_sub, 1, s->r.p, s->p.p, s->v.p, b->c_tmp.p,
+                         b->sc.p, st);
+        launch_precond<double, double>(PG_PREC_ILU0, 0, d0, nullptr, s->r.p,
+                                       b->c_tmp.p, s->v.p, s->ph.p, b->sc.p, st);
+        launch_coarse_add_b(cb, d.n_sub, s->ph.p, b->sc.p, st);
+      } else {
+        launch_precond<double, double>(PG_PREC_ILU0, 1, d, nullptr, s->r.p,
+                                       s->p.p, s->v.p, s->ph.p, b->sc.p, st);
+        if (b->coarse)
+          launch_coarse_apply_b(cb, d.n_sub, s->p.p, s->ph.p, d.smem64 > 0,
+                                b->sc.p, st);
+      }
       launch_b_spmv_v(T, R, b->block, d, s->pvals.p, s->ph.p, s->v.p,
                       s->rh.p, b->sc.p, st);
-      launch_precond<double, double>(PG_PREC_ILU0, 2, d, nullptr, s->r.p,
-                                     s->s.p, s->v.p, s->sh.p, b->sc.p, st);
-      if (b->coarse)
-        launch_coarse_apply_b(cb, d.n_sub, s->s.p, s->sh.p, d.smem64 > 0,
-                              b->sc.p, st);
+      if (b->deflated()) {
+        launch_def_pre_b(cb, d.n_sub, 2, s->r.p, s->s.p, s->v.p, b->c_tmp.p,
+                         b->sc.p, st);
+        launch_precond<double, double>(PG_PREC_ILU0, 0, d0, nullptr, s->r.p,
+                                       b->c_tmp.p, s->v.p, s->sh.p, b->sc.p, st);
+        launch_coarse_add_b(cb, d.n_sub, s->sh.p, b->sc.p, st);
+      } else {
+        launch_precond<double, double>(PG_PREC_ILU0, 2, d, nullptr, s->r.p,
+                                       s->s.p, s->v.p, s->sh.p, b->sc.p, st);
+        if (b->coarse)
+          launch_coarse_apply_b(cb, d.n_sub, s->s.p, s->sh.p, d.smem64 > 0,
+                                b->sc.p, st);
+      }
       launch_b_spmv_t(T, R, b->block, d, s->pvals.p, s->sh.p, s->t.p,
                       s->s.p, b->sc.p, st);
       launch_b_update(T, R, b->block, s->x.p, s->r.p, s->ph.p, s->sh.p,
@@ -1747,6 +1781,13 @@ extern "C" int pg_batch_solve(pg_batch *b, pg_solve_stats *stats,
   if (b->coarse)
     launch_coarse_setup_b(b->coarse_dev(), d.n_sub, b->n_blk, s->pvals.p,
                           s->prp.p, st);
+  if (b->deflated()) {
+    CoarseDev c;
+    c.azp = b->c_azp.p;
+    c.azslot = b->c_azslot.p;
+    c.azv = b->c_azv.p;
+    launch_az_values(c, (int)n, s->prp.p, s->pvals.p, st);
+  }
   for (int i = 0; i < S; ++i) {
     KScalars k{};
     k.tol2 = s->cfg.tolerance * s->cfg.tolerance;
@@ -1777,7 +1818,8 @@ extern "C" int pg_batch_solve(pg_batch *b, pg_solve_stats *stats,
     PG_CUDA(cudaMemcpyAsync(b->sc_host, b->sc.p, S * sizeof(KScalars),
                             cudaMemcpyDeviceToHost, st));
     PG_CUDA(cudaStreamSynchronize(st));
-    count_launches(((b->coarse ? (d.smem64 > 0 ? 7 : 9) : 5) * kChunk + 2) * ch);
+    count_launches(((b->deflated() ? 13 : b->coarse ? (d.smem64 > 0 ? 7 : 9) : 5) *
+                    kChunk + 2) * ch);
     break;
   }
   launch_unpermute_vec((int)n, s->perm.p, s->x.p, s->xout.p, st);

@@ -28,7 +28,7 @@ def _systems(pg, n, seed, max_cells=20_000):
     return out
 
 
-@pytest.mark.parametrize("coarse", [0, 1])
+@pytest.mark.parametrize("coarse", [0, 1, 2])
 def test_batch_matches_individual_solves(pg, coarse):
     """coarse = 1: a block-diagonal coarse space per system in the batch
     (single-pivot Gauss-Jordan per block) and the dense one of a lone
