@@ -249,6 +249,10 @@ struct ArithF64 {
     return pre_combine<double>(mode, ri, pi, vi, sc);
   }
   __device__ static V zero() { return 0.; }
+  // output z + y_s of the deflated form (mode 3)
+  __device__ static V add_y(V z, const void *y, int sub) {
+    return z + static_cast<const double *>(y)[sub];
+  }
   // subdomain sums for the coarse correction
   using Sum = double;
   __device__ static Sum sum_init() { return 0.; }
@@ -282,6 +286,9 @@ struct ArithDD {
     return dd_pre_combine(mode, ri, pi, vi, sc);
   }
   __device__ static V zero() { return make_float2(0.f, 0.f); }
+  __device__ static V add_y(V z, const void *y, int sub) {
+    return dd_add(z, static_cast<const float2 *>(y)[sub]);
+  }
   using Sum = DdAcc;
   __device__ static Sum sum_init() { return dd_acc(make_float2(0.f, 0.f)); }
   __device__ static void sum_add(Sum &a, V x) { dd_acc_add(a, x); }
@@ -325,7 +332,8 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
                     typename AR::V *__restrict__ z,
                     const KScalars *__restrict__ sc_base,
                     const int32_t *__restrict__ sub_sys,
-                    int *__restrict__ err, float2 *__restrict__ csum) {
+                    int *__restrict__ err, float2 *__restrict__ csum,
+                    const void *__restrict__ def_y) {
   using MT = typename AR::V;
   // batched solves: the scalars of this subdomain's system
   const KScalars *sc =
@@ -371,7 +379,7 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
         const int i = i0 + 32 * u;
         ri[u] = pi[u] = vi[u] = zero;
         if (i < nr) {
-          if (MODE != 0) ri[u] = r[m.r0 + i], vi[u] = v[m.r0 + i];
+          if (MODE == 1 || MODE == 2) ri[u] = r[m.r0 + i], vi[u] = v[m.r0 + i];
           if (MODE != 2) pi[u] = pv[m.r0 + i];
         }
       }
@@ -379,8 +387,12 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
       for (int u = 0; u < U; ++u) {
         const int i = i0 + 32 * u;
         if (i < nr) {
-          const MT val = AR::combine(MODE, ri[u], pi[u], vi[u], sc);
-          if (MODE != 0) pv[m.r0 + i] = val;
+          MT val;
+          if constexpr (MODE == 3)
+            val = pi[u];
+          else
+            val = AR::combine(MODE, ri[u], pi[u], vi[u], sc);
+          if (MODE == 1 || MODE == 2) pv[m.r0 + i] = val;
           zs[i] = val;
           if (csum) AR::sum_add(i < m.nr0 ? part0 : part1, val);
         }
@@ -526,7 +538,12 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
                 (uint32_t)tab[3 * (j + 2) + 2], &bar[sb]);
     }
   }
-  for (int i = lane; i < nr; i += 32) z[m.r0 + i] = zs[i];
+  if constexpr (MODE == 3) {
+    for (int i = lane; i < nr; i += 32)
+      z[m.r0 + i] = AR::add_y(zs[i], def_y, i < m.nr0 ? m.sub0 : m.sub0 + 1);
+  } else {
+    for (int i = lane; i < nr; i += 32) z[m.r0 + i] = zs[i];
+  }
 }
 
 // Float-float step-form sweeps (kernels.cuh StepMeta) of the mixed
@@ -710,7 +727,7 @@ void launch_stream(const SolverDev &d, size_t smem, const uint8_t *rec,
     attr = smem;
   }
   k_ilu0_apply_stream<AR, MODE, KLT, KUT><<<d.n_grp, 32, smem, st>>>(
-      d.smeta64, rec, r, pv, v, z, sc, d.sub_sys, d.err, d.csum);
+      d.smeta64, rec, r, pv, v, z, sc, d.sub_sys, d.err, d.csum, d.def_y);
 }
 
 template <class VT, class MT, int MODE>
@@ -788,6 +805,36 @@ void launch_ilu0_factor(const SolverDev &d, const double *pvals, int *bad,
         reinterpret_cast<float2 *>(d.srec_dd));
     count_launches(1);
   }
+}
+
+bool launch_ilu0_apply_def(const SolverDev &d, const double *in, double *z,
+                           const KScalars *sc, cudaStream_t st) {
+  const size_t smem = d.smem64;
+  if (!smem || !d.def_y) return false;
+  double *pv = const_cast<double *>(in);  // mode 3 reads it only
+  if (d.max_kl <= 2 && d.max_ku <= 2)
+    launch_stream<ArithF64, 3, 2, 2>(d, smem, d.srec64, nullptr, pv, nullptr, z, sc, st);
+  else if (d.max_kl <= 3 && d.max_ku <= 3)
+    launch_stream<ArithF64, 3, 3, 3>(d, smem, d.srec64, nullptr, pv, nullptr, z, sc, st);
+  else
+    launch_stream<ArithF64, 3, 0, 0>(d, smem, d.srec64, nullptr, pv, nullptr, z, sc, st);
+  count_launches(1);
+  return true;
+}
+
+bool launch_ilu0_apply_def_dd(const SolverDev &d, const float2 *in, float2 *z,
+                              const KScalars *sc, cudaStream_t st) {
+  if (!d.dd_stream || !d.def_y) return false;
+  const size_t smem = d.smem64;
+  float2 *pv = const_cast<float2 *>(in);  // mode 3 reads it only
+  if (d.max_kl <= 2 && d.max_ku <= 2)
+    launch_stream<ArithDD, 3, 2, 2>(d, smem, d.srec_dds, nullptr, pv, nullptr, z, sc, st);
+  else if (d.max_kl <= 3 && d.max_ku <= 3)
+    launch_stream<ArithDD, 3, 3, 3>(d, smem, d.srec_dds, nullptr, pv, nullptr, z, sc, st);
+  else
+    launch_stream<ArithDD, 3, 0, 0>(d, smem, d.srec_dds, nullptr, pv, nullptr, z, sc, st);
+  count_launches(1);
+  return true;
 }
 
 void launch_ilu0_apply_dd(int mode, const SolverDev &d, const float2 *r,

@@ -192,6 +192,11 @@ struct SolverDev {
   // two-level Schwarz: the streamed sweeps write the sum of each
   // subdomain's input here, as a float pair (NULL: no coarse correction)
   float2 *csum;
+  // deflated coarse correction (mode 3 of the streamed sweep): the input
+  // is already p - (A Z) y and the sweep writes z + y_s, y_s the coarse
+  // value of the row's subdomain in the sweep's arithmetic (double or
+  // float pairs)
+  const void *def_y;
 };
 
 
@@ -303,6 +308,16 @@ void launch_ilu0_factor(const SolverDev &d, const double *pvals, int *bad,
 //   mode 0: z = M^-1 in
 //   mode 1: p = r + beta (p - omega v); z = M^-1 p   (p written back)
 //   mode 2: s = r - alpha v;            z = M^-1 s   (s written back)
+//   mode 3: z = M^-1 (in - (A Z) y) + Z y  (the deflated coarse correction
+//           around the ILU(0) sweeps; streamed sweep forms only)
+// mode 3 of the streamed ILU(0) sweep (d.def_y set): z = B in + Z y for a
+// deflated input in = p - A Z y; false when the streamed form is not
+// available
+bool launch_ilu0_apply_def(const SolverDev &d, const double *in, double *z,
+                           const KScalars *sc, cudaStream_t st);
+bool launch_ilu0_apply_def_dd(const SolverDev &d, const float2 *in, float2 *z,
+                              const KScalars *sc, cudaStream_t st);
+
 template <class VT, class MT>
 void launch_precond(int precond, int mode, const SolverDev &d,
                     const MT *jdinv, const VT *r, VT *pv, const VT *v, VT *z,

@@ -214,6 +214,7 @@ struct pg_solver {
     d.err = err.p;
     d.sub_sys = nullptr;
     d.csum = coarse_on ? c_sum.p : nullptr;
+    d.def_y = nullptr;
     return d;
   }
   RedWork red() const { return RedWork{partials.p, ticket.p, red_grid}; }
@@ -454,11 +455,17 @@ int run_bicgstab(pg_solver *s, double tol, int max_iters, int *iters,
   const bool ilu_stream = s->cfg.precond == PG_PREC_ILU0 && d.smem64 > 0;
   SolverDev d0 = d;  // the deflated form's sweep needs no subdomain sums
   d0.csum = nullptr;
+  SolverDev d3 = d0;  // ... and adds y on output (mode 3)
+  d3.def_y = cdev.y;
   auto precond = [&](int mode, double *pv, double *z) {
     if (cdev.K && s->cfg.coarse == 2) {
-      // A-DEF1: y = A_c^-1 Z^T p, z = B (p - A Z y) + Z y
+      // A-DEF1: y = A_c^-1 Z^T p, z = B (p - A Z y) + Z y; the streamed
+      // sweep adds y as it writes z
       launch_def_pre(cdev, mode, r, pv, v, s->sc.p, st);
       launch_def_in(cdev, d.n, pv, cdev.tmp, s->sc.p, st);
+      if (s->cfg.precond == PG_PREC_ILU0 &&
+          launch_ilu0_apply_def(d3, cdev.tmp, z, s->sc.p, st))
+        return;
       launch_precond<double, double>(s->cfg.precond, 0, d0, jd, r, cdev.tmp,
                                      v, z, s->sc.p, st);
       launch_coarse_add(cdev, z, s->sc.p, st);
@@ -575,11 +582,15 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
   const CoarseDev cdev = s->coarse();
   SolverDev d0 = d;  // the deflated form's sweep needs no subdomain sums
   d0.csum = nullptr;
+  SolverDev d3 = d0;
+  d3.def_y = cdev.y_dd;
   auto precond = [&](int mode, float2 *pv, float2 *z) {
     if (cdev.K && s->cfg.coarse == 2) {
       // A-DEF1 in float-float
       launch_def_pre_dd(cdev, mode, r, pv, v, s->sc.p, st);
       launch_def_in_dd(cdev, n, pv, cdev.tmp_dd, s->sc.p, st);
+      if (ilu && launch_ilu0_apply_def_dd(d3, cdev.tmp_dd, z, s->sc.p, st))
+        return;
       if (ilu)
         launch_ilu0_apply_dd(0, d0, r, cdev.tmp_dd, v, z, s->sc.p, st);
       else
@@ -1241,19 +1252,26 @@ extern "C" int pg_solver_apply_precond(pg_solver *s, const double *r,
     SolverDev d0 = d;
     d0.csum = def ? nullptr : d.csum;
     float2 *in = s->pd.p;
+    bool fused = false;
     if (def) {  // A-DEF1: the sweep runs on p - A Z y
       launch_def_pre_dd(c, 0, nullptr, s->pd.p, nullptr, nullptr, st);
       launch_def_in_dd(c, (int)n, s->pd.p, c.tmp_dd, nullptr, st);
       in = c.tmp_dd;
+      SolverDev d3 = d0;
+      d3.def_y = c.y_dd;
+      fused = s->cfg.precond == PG_PREC_ILU0 &&
+              launch_ilu0_apply_def_dd(d3, in, s->phd.p, nullptr, st);
     }
-    if (s->cfg.precond == PG_PREC_ILU0)
+    if (fused)
+      ;
+    else if (s->cfg.precond == PG_PREC_ILU0)
       launch_ilu0_apply_dd(0, d0, nullptr, in, nullptr, s->phd.p, nullptr, st);
     else
       launch_dd_diag_apply(0, (int)n, s->cfg.precond == PG_PREC_JACOBI ? s->jdinv_dd.p : nullptr,
                            nullptr, in, nullptr, s->phd.p, nullptr, st);
-    if (def)
+    if (def && !fused)
       launch_coarse_add_dd(c, s->phd.p, nullptr, st);
-    else if (s->coarse_on)
+    else if (!def && s->coarse_on)
       launch_coarse_apply_dd(c, s->pd.p, s->phd.p,
                              s->cfg.precond == PG_PREC_ILU0 && d.dd_stream,
                              nullptr, st);
@@ -1265,9 +1283,15 @@ extern "C" int pg_solver_apply_precond(pg_solver *s, const double *r,
       d0.csum = nullptr;
       launch_def_pre(c, 0, nullptr, s->p.p, nullptr, nullptr, st);
       launch_def_in(c, d.n, s->p.p, c.tmp, nullptr, st);
-      launch_precond<double, double>(s->cfg.precond, 0, d0, s->jdinv.p, nullptr,
-                                     c.tmp, nullptr, s->ph.p, nullptr, st);
-      launch_coarse_add(c, s->ph.p, nullptr, st);
+      SolverDev d3 = d0;
+      d3.def_y = c.y;
+      if (!(s->cfg.precond == PG_PREC_ILU0 &&
+            launch_ilu0_apply_def(d3, c.tmp, s->ph.p, nullptr, st))) {
+        launch_precond<double, double>(s->cfg.precond, 0, d0, s->jdinv.p,
+                                       nullptr, c.tmp, nullptr, s->ph.p,
+                                       nullptr, st);
+        launch_coarse_add(c, s->ph.p, nullptr, st);
+      }
     } else {
       launch_precond<double, double>(s->cfg.precond, 0, d, s->jdinv.p, nullptr,
                                      s->p.p, nullptr, s->ph.p, nullptr, st);
