@@ -234,7 +234,18 @@ def slots_layout(rp, ci, v):
     return srp, sci, sv
 
 
-def kernel_roofline(pg, solver, n, nnz, dd):
+def az_nnz(eqn, part):
+    """Nonzeros of A Z, Z the subdomain indicator vectors: per row, the
+    number of distinct subdomains among its columns."""
+    import numpy as np
+    rp, ci, _, _ = eqn.export()
+    rows = np.repeat(np.arange(len(rp) - 1, dtype=np.int64), np.diff(rp))
+    keep = ci >= 0
+    K = int(part.max()) + 1
+    return int(np.unique(rows[keep] * K + part[ci[keep]]).size)
+
+
+def kernel_roofline(pg, solver, n, nnz, dd, eqn=None, coarse=0):
     """Per-launch CUDA-event times of the hot kernels of one solver on its
     current system (pg_solver_profile) and the roofline of the dominant
     one.  Compulsory bytes per launch: A values +
@@ -252,11 +263,18 @@ def kernel_roofline(pg, solver, n, nnz, dd):
               "update": ms_of["update"]}
     bytes_of = {"spmv": b_spmv, "ilu_apply": b_prec, "update": b_upd}
     if prof["coarse"] > 0:
-        # coarse correction: FP32 K x K inverse, K float-pair sums, z in/out
-        K = solver.partition()[1]
+        part, K = solver.partition()
         ms_of["coarse"] = prof["coarse"]
         shares["coarse"] = 2 * prof["coarse"]
-        bytes_of["coarse"] = 4 * K * K + 8 * K + 2 * 8 * n
+        if coarse == 2:
+            # deflation: r p v in, p out (with the subdomain sums); FP32
+            # K x K inverse, sums in, y out; p, A Z (row pointers, int32
+            # columns, 8-byte values) and y in, p - A Z y out
+            bytes_of["coarse"] = (4 * 8 * n + 4 * K * K + 24 * K + 2 * 8 * n
+                                  + 4 * (n + 1) + 12 * az_nnz(eqn, part))
+        else:
+            # additive: FP32 K x K inverse, K float-pair sums, z in/out
+            bytes_of["coarse"] = 4 * K * K + 8 * K + 2 * 8 * n
     dom = max(shares, key=shares.get)
     peak, peak_kind = measured_peaks()
     achieved = bytes_of[dom] / (ms_of[dom] * 1e-3) / 1e9
@@ -418,8 +436,8 @@ def run_sequence(args):
     sz.setGuess(None)
     sz.solve()
     zero = dict(sz.stats.as_dict())
-    roof_m = kernel_roofline(pg, sm, n, nnz, dd=True)
-    roof_p = kernel_roofline(pg, sp, n, nnz, dd=False)
+    roof_m = kernel_roofline(pg, sm, n, nnz, dd=True, eqn=eqn, coarse=args.coarse)
+    roof_p = kernel_roofline(pg, sp, n, nnz, dd=False, eqn=eqn, coarse=args.coarse)
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
@@ -773,45 +791,16 @@ def run_single(args):
     # kernel-level roofline on the same system: per-launch CUDA-event times
     # of the hot kernels (FP64 ones, or the float-float ones of the mixed
     # solver; both move 8-byte values and vector entries)
-    prof = solver.profile(reps=50)
     a_nnz = int(eqn.nnz)
-    # compulsory bytes per launch: A values + int32
-    # columns + row pointers; ILU(0) factor values + 2-byte columns
-    # (off-diagonal entries of A bound the factor's) + 1/u_ii
-    b_spmv = 12 * a_nnz + 4 * (n + 1) + 3 * 8 * n          # A, x, rhat in; v out
-    b_prec = 10 * (a_nnz - n) + 8 * n + 5 * 8 * n          # LU, dinv, r p v in, p z out
-    b_upd = 9 * 8 * n                                      # x r ph sh s t rh in; x r out
-    sfx = "_dd" if prec == pg.MIXED else ""
-    ms_of = {"spmv": prof["spmv" + sfx], "ilu_apply": prof["precond" + sfx],
-             "update": prof["update" + sfx]}
-    shares = {"spmv": 2 * ms_of["spmv"], "ilu_apply": 2 * ms_of["ilu_apply"],
-              "update": ms_of["update"]}
-    bytes_of = {"spmv": b_spmv, "ilu_apply": b_prec, "update": b_upd}
-    if prof["coarse"] > 0:
-        # coarse correction: FP32 K x K inverse, K float-pair sums, z in/out
-        K = solver.partition()[1]
-        ms_of["coarse"] = prof["coarse"]
-        shares["coarse"] = 2 * prof["coarse"]
-        bytes_of["coarse"] = 4 * K * K + 8 * K + 2 * 8 * n
-    dom = max(shares, key=shares.get)
-    peak, peak_kind = measured_peaks()
-    achieved = bytes_of[dom] / (ms_of[dom] * 1e-3) / 1e9
-    traffic = None
+    roofline = kernel_roofline(pg, solver, n, a_nnz, dd=prec == pg.MIXED,
+                               eqn=eqn, coarse=args.coarse)
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    roofline["traffic"] = None
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get(f"{dom}_{args.precision}")
+            roofline["traffic"] = json.load(f).get(
+                f"{roofline['kernel']}_{args.precision}")
     iters = max(1, stats[-1]["iters"])
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
-                "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": traffic,
-                "algorithmic_bytes": bytes_of[dom],
-                "launch_ms": round(ms_of[dom], 5),
-                "per_kernel_gbs": {k: round(bytes_of[k] / (ms_of[k] * 1e-3) / 1e9, 1)
-                                   for k in bytes_of},
-                "per_kernel_ms": {k: round(v, 5) for k, v in ms_of.items()},
-                "factor_ms": round(prof["factor"], 4),
-                "frac_of_8tbs": round(achieved / 8000.0, 4)}
 
     # e2e through the reference-facing call sequence with host buffers
     e2e = None

@@ -374,8 +374,12 @@ int pg_solver_get_x(const pg_solver *s, double *x, int ptr_kind);
  * update, ms[3] ILU(0) factorisation (with the coarse matrix and its
  * inverse when cfg.coarse), for PG_MIXED ms[4] the float-float ILU(0)
  * apply, ms[5] SpMV and ms[6] update (0 otherwise), and ms[7] the coarse
- * correction of one application (0 without a coarse space).  Leaves the
- * solver's state untouched.  (No reference counterpart: measurement.) */
+ * stage of one application (0 without a coarse space): for cfg.coarse = 1
+ * the subdomain sums and the correction z += Z y, for cfg.coarse = 2 the
+ * deflation's kernels beside the sweep (the combined input with its
+ * subdomain sums, y = A_c^-1 Z^T p and p - A Z y; float-float ones under
+ * PG_MIXED).  Leaves the solver's state untouched.  (No reference
+ * counterpart: measurement.) */
 int pg_solver_profile(pg_solver *s, int reps, double *ms);
 
 /* ---------------------------------------------------------------------

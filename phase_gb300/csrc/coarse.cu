@@ -328,11 +328,12 @@ k_def_pre(int mode, const int32_t *__restrict__ sub_ptr,
   if (threadIdx.x == 0) csum[s] = dd_from(t);
 }
 
-// y_s = (A_c^-1)_s . csum (compensated float-float dot, as k_coarse_correct)
+// y_s = (A_c^-1)_s . csum (compensated float-float dot, as k_coarse_correct);
+// y_dd (optional) receives y as float pairs for the float-float solver
 __global__ void __launch_bounds__(kCorrectBlock)
 k_coarse_y(int K, const float *__restrict__ ainv,
            const float2 *__restrict__ csum, double *__restrict__ y,
-           const KScalars *__restrict__ sc) {
+           float2 *__restrict__ y_dd, const KScalars *__restrict__ sc) {
   if (sc && sc->done) return;
   __shared__ float red_s[kCorrectBlock / 32], red_c[kCorrectBlock / 32];
   const int s = blockIdx.x;
@@ -361,7 +362,9 @@ k_coarse_y(int K, const float *__restrict__ ainv,
       b.c = red_c[w];
       dd_acc_merge(u, b);
     }
-    y[s] = dd_acc_to_double(u);
+    const double v = dd_acc_to_double(u);
+    y[s] = v;
+    if (y_dd) y_dd[s] = dd_from(v);
   }
 }
 
@@ -412,16 +415,6 @@ k_def_pre_dd(int mode, const int32_t *__restrict__ sub_ptr,
   }
   const double t = block_sum(dd_acc_to_double(acc), red);
   if (threadIdx.x == 0) csum[s] = dd_from(t);
-}
-
-// y as float pairs (one conversion per subdomain)
-__global__ void k_y_split(int K, const double *__restrict__ y,
-                          float2 *__restrict__ y_dd,
-                          const KScalars *__restrict__ sc) {
-  if (sc && sc->done) return;
-  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < K;
-       s += gridDim.x * blockDim.x)
-    y_dd[s] = dd_from(y[s]);
 }
 
 // t = pv - (A Z) y in float-float
@@ -684,7 +677,7 @@ void launch_az_values(const CoarseDev &c, int n, const int32_t *prp,
 void launch_def_pre(const CoarseDev &c, int mode, const double *r, double *pv,
                     const double *v, const KScalars *sc, cudaStream_t st) {
   k_def_pre<<<c.K, kCoarseBlock, 0, st>>>(mode, c.sub_ptr, r, pv, v, sc, c.csum);
-  k_coarse_y<<<c.K, kCorrectBlock, 0, st>>>(c.K, c.ac, c.csum, c.y, sc);
+  k_coarse_y<<<c.K, kCorrectBlock, 0, st>>>(c.K, c.ac, c.csum, c.y, nullptr, sc);
   count_launches(2);
 }
 
@@ -705,9 +698,8 @@ void launch_def_pre_dd(const CoarseDev &c, int mode, const float2 *r,
                        float2 *pv, const float2 *v, const KScalars *sc,
                        cudaStream_t st) {
   k_def_pre_dd<<<c.K, kCoarseBlock, 0, st>>>(mode, c.sub_ptr, r, pv, v, sc, c.csum);
-  k_coarse_y<<<c.K, kCorrectBlock, 0, st>>>(c.K, c.ac, c.csum, c.y, sc);
-  k_y_split<<<(c.K + 255) / 256, 256, 0, st>>>(c.K, c.y, c.y_dd, sc);
-  count_launches(3);
+  k_coarse_y<<<c.K, kCorrectBlock, 0, st>>>(c.K, c.ac, c.csum, c.y, c.y_dd, sc);
+  count_launches(2);
 }
 
 void launch_def_in_dd(const CoarseDev &c, int n, const float2 *pv, float2 *t,

@@ -1215,8 +1215,21 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
       if (s->coarse_on)
         launch_coarse_setup(s->coarse(), s->pvals.p, s->prp.p, &s->gj_graph, st);
     }, &ms[3]);
-  if (!rc && s->coarse_on)
-    rc = timed([&] { launch_coarse_apply(s->coarse(), d8[4].p, d8[6].p, true, s->sc.p, st); }, &ms[7]);
+  if (!rc && s->coarse_on) {
+    const CoarseDev c = s->coarse();
+    if (s->cfg.coarse == 2 && dd)
+      rc = timed([&] {
+        launch_def_pre_dd(c, 1, f8[3].p, f8[4].p, f8[1].p, s->sc.p, st);
+        launch_def_in_dd(c, (int)n, f8[4].p, c.tmp_dd, s->sc.p, st);
+      }, &ms[7]);
+    else if (s->cfg.coarse == 2)
+      rc = timed([&] {
+        launch_def_pre(c, 1, d8[3].p, d8[4].p, d8[1].p, s->sc.p, st);
+        launch_def_in(c, d.n, d8[4].p, c.tmp, s->sc.p, st);
+      }, &ms[7]);
+    else
+      rc = timed([&] { launch_coarse_apply(c, d8[4].p, d8[6].p, true, s->sc.p, st); }, &ms[7]);
+  }
   if (!rc && dd) {
     if (s->cfg.precond == PG_PREC_ILU0)
       rc = timed([&] { launch_ilu0_apply_dd(1, d, f8[3].p, f8[4].p, f8[1].p, f8[6].p, s->sc.p, st); }, &ms[4]);
