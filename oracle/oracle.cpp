@@ -422,10 +422,23 @@ static void spmv(const Csr &A, const double *x, double *y) {
   }
 }
 
+// Dot product with a fixed summation order for a given thread count: each
+// thread sums a contiguous chunk and the partials are added in thread order
+// (an OpenMP reduction combines partials in an unspecified order, and the
+// one-level BiCGStab is sensitive enough to those last bits to change its
+// iteration count from run to run).
 static double vdot(int64_t n, const double *a, const double *b) {
+  std::vector<double> part(omp_get_max_threads(), 0.);
+#pragma omp parallel
+  {
+    const int t = omp_get_thread_num(), nt = omp_get_num_threads();
+    const int64_t lo = n * t / nt, hi = n * (t + 1) / nt;
+    double s = 0.;
+    for (int64_t i = lo; i < hi; ++i) s += a[i] * b[i];
+    part[t] = s;
+  }
   double s = 0.;
-#pragma omp parallel for schedule(static) reduction(+ : s)
-  for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+  for (double q : part) s += q;
   return s;
 }
 
