@@ -31,9 +31,12 @@ x uploaded, the solution read back).
 
 --mode single: one system solved from a zero guess (the kernel roofline
 and sweep configuration).  --impl reference times the CPU implementation
-of the zero-guess solve (the oracle's OpenMP BiCGStab with one ILU(0)
-subdomain per thread -- Ifpack2 Schwarz/RILUK as run on that many MPI
-ranks) on a bounded sample.
+(the oracle's OpenMP BiCGStab with one ILU(0) subdomain per thread --
+Ifpack2 Schwarz/RILUK as run on that many MPI ranks) on the same workload:
+in sequence mode the same held-out steps, each warm from its previous CPU
+solution; in single mode the zero-guess solve on a bounded sample.
+`iters_saved_by_guess` compares the learned arm's iteration counts with the
+float-float arm warm from the previous x, step by step.
 """
 from __future__ import annotations
 
@@ -516,6 +519,13 @@ def run_sequence(args):
                              "iters": [s_["iters"] for s_ in st_q],
                              "fp64_iters": [s_["fp64_iters"] for s_ in st_q],
                              "rel_residual": [s_["rel_residual"] for s_ in st_q]},
+            # the guess's effect alone: the same float-float solver from the
+            # network's guess vs from the previous step's x
+            "iters_saved_by_guess": {
+                "per_step": [q["iters"] - m_["iters"] for q, m_ in zip(st_q, st_m)],
+                "mean": round(sum(q["iters"] - m_["iters"]
+                                  for q, m_ in zip(st_q, st_m)) / len(st_m), 2),
+                "against": "float-float solve warm from the previous x"},
             "plain_fp64_zero_guess": {"ms": round(zero["ms"], 3),
                                       "iters": zero["iters"],
                                       "rel_residual": zero["rel_residual"]},
