@@ -27,8 +27,9 @@ class Gb300SparseMatrixSolver : public SparseMatrixSolver {
   Scalar x(Index idx) const override;
   // keys: tolerance (1e-8), maxIters (500), preconditioner
   // (ilu0 | jacobi | none), subdomainRows (0 = default, -1 = one subdomain),
-  // precision (fp64 | mixed), mixedSweep (0 | 1 | 2), coarseSpace (0 | 1:
-  // two-level Schwarz with a coarse correction)
+  // precision (fp64 | mixed), mixedSweep (0 | 1 | 2), coarseSpace (2
+  // default: deflated two-level Schwarz; 1 additive; 0 one-level, as
+  // Ifpack2), coarseWarmIters (-1 default)
   void setup(const boost::property_tree::ptree &parameters) override;
   // Optional geometry hint (no SparseMatrixSolver counterpart): a point per
   // row, xy[2 * rank] interleaved (the cell centroids), so the Schwarz
