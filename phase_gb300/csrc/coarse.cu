@@ -313,6 +313,7 @@ k_def_pre(int mode, const int32_t *__restrict__ sub_ptr,
           const double *__restrict__ r, double *__restrict__ pv,
           const double *__restrict__ v, const KScalars *__restrict__ sc,
           float2 *__restrict__ csum) {
+  pdl_wait();
   if (sc && sc->done) return;
   __shared__ double red[kCoarseBlock];
   const int s = blockIdx.x;
@@ -334,6 +335,7 @@ __global__ void __launch_bounds__(kCorrectBlock)
 k_coarse_y(int K, const float *__restrict__ ainv,
            const float2 *__restrict__ csum, double *__restrict__ y,
            float2 *__restrict__ y_dd, const KScalars *__restrict__ sc) {
+  pdl_wait();
   if (sc && sc->done) return;
   __shared__ float red_s[kCorrectBlock / 32], red_c[kCorrectBlock / 32];
   const int s = blockIdx.x;
@@ -375,6 +377,7 @@ __global__ void k_def_in(int n, const int32_t *__restrict__ azp,
                          const double *__restrict__ y,
                          const double *__restrict__ pv, double *__restrict__ t,
                          const KScalars *__restrict__ sc) {
+  pdl_wait();
   if (sc && sc->done) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += gridDim.x * blockDim.x) {
@@ -401,6 +404,7 @@ k_def_pre_dd(int mode, const int32_t *__restrict__ sub_ptr,
              const float2 *__restrict__ r, float2 *__restrict__ pv,
              const float2 *__restrict__ v, const KScalars *__restrict__ sc,
              float2 *__restrict__ csum) {
+  pdl_wait();
   if (sc && sc->done) return;
   __shared__ double red[kCoarseBlock];
   const int s = blockIdx.x;
@@ -425,6 +429,7 @@ __global__ void k_def_in_dd(int n, const int32_t *__restrict__ azp,
                             const float2 *__restrict__ pv,
                             float2 *__restrict__ t,
                             const KScalars *__restrict__ sc) {
+  pdl_wait();
   if (sc && sc->done) return;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += gridDim.x * blockDim.x) {
@@ -676,15 +681,15 @@ void launch_az_values(const CoarseDev &c, int n, const int32_t *prp,
 
 void launch_def_pre(const CoarseDev &c, int mode, const double *r, double *pv,
                     const double *v, const KScalars *sc, cudaStream_t st) {
-  k_def_pre<<<c.K, kCoarseBlock, 0, st>>>(mode, c.sub_ptr, r, pv, v, sc, c.csum);
-  k_coarse_y<<<c.K, kCorrectBlock, 0, st>>>(c.K, c.ac, c.csum, c.y, nullptr, sc);
+  launch_pdl(k_def_pre, c.K, kCoarseBlock, 0, st, mode, c.sub_ptr, r, pv, v, sc, c.csum);
+  launch_pdl(k_coarse_y, c.K, kCorrectBlock, 0, st, c.K, (const float *)c.ac, (const float2 *)c.csum, c.y, (float2 *)nullptr, sc);
   count_launches(2);
 }
 
 void launch_def_in(const CoarseDev &c, int n, const double *pv, double *t,
                    const KScalars *sc, cudaStream_t st) {
   const int g = (n + 255) / 256 < 2432 ? (n + 255) / 256 : 2432;
-  k_def_in<<<g, 256, 0, st>>>(n, c.azp, c.azj, c.azv, c.y, pv, t, sc);
+  launch_pdl(k_def_in, g, 256, 0, st, n, c.azp, c.azj, c.azv, c.y, pv, t, sc);
   count_launches(1);
 }
 
@@ -697,15 +702,15 @@ void launch_coarse_add(const CoarseDev &c, double *z, const KScalars *sc,
 void launch_def_pre_dd(const CoarseDev &c, int mode, const float2 *r,
                        float2 *pv, const float2 *v, const KScalars *sc,
                        cudaStream_t st) {
-  k_def_pre_dd<<<c.K, kCoarseBlock, 0, st>>>(mode, c.sub_ptr, r, pv, v, sc, c.csum);
-  k_coarse_y<<<c.K, kCorrectBlock, 0, st>>>(c.K, c.ac, c.csum, c.y, c.y_dd, sc);
+  launch_pdl(k_def_pre_dd, c.K, kCoarseBlock, 0, st, mode, c.sub_ptr, r, pv, v, sc, c.csum);
+  launch_pdl(k_coarse_y, c.K, kCorrectBlock, 0, st, c.K, (const float *)c.ac, (const float2 *)c.csum, c.y, c.y_dd, sc);
   count_launches(2);
 }
 
 void launch_def_in_dd(const CoarseDev &c, int n, const float2 *pv, float2 *t,
                       const KScalars *sc, cudaStream_t st) {
   const int g = (n + 255) / 256 < 2432 ? (n + 255) / 256 : 2432;
-  k_def_in_dd<<<g, 256, 0, st>>>(n, c.azp, c.azj, c.azv_dd, c.y_dd, pv, t, sc);
+  launch_pdl(k_def_in_dd, g, 256, 0, st, n, c.azp, c.azj, c.azv_dd, c.y_dd, pv, t, sc);
   count_launches(1);
 }
 

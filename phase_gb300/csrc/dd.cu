@@ -175,6 +175,7 @@ __global__ void __launch_bounds__(kVecBlock)
 k_dd_spmv_v(SolverDev d, const float2 *__restrict__ val,
             const float2 *__restrict__ ph, float2 *__restrict__ v,
             const float2 *__restrict__ rh, KScalars *sc, RedWork w) {
+  pdl_wait();
   if (sc->done) return;
   DdAcc acc[1] = {{0.f, 0.f}};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
@@ -203,6 +204,7 @@ __global__ void __launch_bounds__(kVecBlock)
 k_dd_spmv_t(SolverDev d, const float2 *__restrict__ val,
             const float2 *__restrict__ sh, float2 *__restrict__ t,
             const float2 *__restrict__ s, KScalars *sc, RedWork w) {
+  pdl_wait();
   if (sc->done) return;
   DdAcc acc[2] = {{0.f, 0.f}, {0.f, 0.f}};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
@@ -226,6 +228,7 @@ k_dd_update(int n, float2 *__restrict__ x, float2 *__restrict__ r,
             const float2 *__restrict__ ph, const float2 *__restrict__ sh,
             const float2 *__restrict__ s, const float2 *__restrict__ t,
             const float2 *__restrict__ rh, KScalars *sc, RedWork w) {
+  pdl_wait();
   if (sc->done) return;
   const float2 al = sc->alpha_dd, om = sc->omega_dd;
   DdAcc acc[2] = {{0.f, 0.f}, {0.f, 0.f}};
@@ -315,14 +318,14 @@ void launch_dd_set_r(int n, const double *r64, double scale, float2 *r,
 void launch_dd_spmv_v(const SolverDev &d, const float2 *val, const float2 *ph,
                       float2 *v, const float2 *rh, KScalars *sc, RedWork w,
                       cudaStream_t st) {
-  k_dd_spmv_v<<<w.grid, kVecBlock, 0, st>>>(d, val, ph, v, rh, sc, w);
+  launch_pdl(k_dd_spmv_v, w.grid, kVecBlock, 0, st, d, val, ph, v, rh, sc, w);
   count_launches(1);
 }
 
 void launch_dd_spmv_t(const SolverDev &d, const float2 *val, const float2 *sh,
                       float2 *t, const float2 *s, KScalars *sc, RedWork w,
                       cudaStream_t st) {
-  k_dd_spmv_t<<<w.grid, kVecBlock, 0, st>>>(d, val, sh, t, s, sc, w);
+  launch_pdl(k_dd_spmv_t, w.grid, kVecBlock, 0, st, d, val, sh, t, s, sc, w);
   count_launches(1);
 }
 
@@ -330,7 +333,7 @@ void launch_dd_update(int n, float2 *x, float2 *r, const float2 *ph,
                       const float2 *sh, const float2 *s, const float2 *t,
                       const float2 *rh, KScalars *sc, RedWork w,
                       cudaStream_t st) {
-  k_dd_update<<<w.grid, kVecBlock, 0, st>>>(n, x, r, ph, sh, s, t, rh, sc, w);
+  launch_pdl(k_dd_update, w.grid, kVecBlock, 0, st, n, x, r, ph, sh, s, t, rh, sc, w);
   count_launches(1);
 }
 

@@ -338,6 +338,7 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
   // batched solves: the scalars of this subdomain's system
   const KScalars *sc =
       sc_base && sub_sys ? sc_base + sub_sys[blockIdx.x] : sc_base;
+  pdl_wait();
   if (sc && sc->done) return;
   extern __shared__ __align__(128) uint8_t smem[];
   __shared__ __align__(8) uint64_t bar[3];
@@ -726,8 +727,9 @@ void launch_stream(const SolverDev &d, size_t smem, const uint8_t *rec,
                          (int)smem);
     attr = smem;
   }
-  k_ilu0_apply_stream<AR, MODE, KLT, KUT><<<d.n_grp, 32, smem, st>>>(
-      d.smeta64, rec, r, pv, v, z, sc, d.sub_sys, d.err, d.csum, d.def_y);
+  launch_pdl(k_ilu0_apply_stream<AR, MODE, KLT, KUT>, d.n_grp, 32, smem, st,
+             d.smeta64, rec, r, pv, v, z, sc, d.sub_sys, d.err, d.csum,
+             d.def_y);
 }
 
 template <class VT, class MT, int MODE>

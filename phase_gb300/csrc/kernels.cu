@@ -16,6 +16,7 @@
 
 #include <atomic>
 #include <cstdint>
+#include <cstdlib>
 
 #include "../../include/phase_gb300.h"
 #include "kernels.cuh"
@@ -25,6 +26,13 @@ namespace pg {
 static std::atomic<uint64_t> g_launches{0};
 void count_launches(int k) { g_launches.fetch_add((uint64_t)k, std::memory_order_relaxed); }
 uint64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char *e = std::getenv("PG_PDL");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
 
 namespace {
 
@@ -419,6 +427,7 @@ __global__ void __launch_bounds__(kVecBlock)
 k_spmv_v(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ ph,
          VT *__restrict__ v, const VT *__restrict__ rh, KScalars *sc,
          RedWork w) {
+  pdl_wait();
   if (sc->done) return;
   double acc[1] = {0.};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
@@ -447,6 +456,7 @@ __global__ void __launch_bounds__(kVecBlock)
 k_spmv_t(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ sh,
          VT *__restrict__ t, const VT *__restrict__ s, KScalars *sc,
          RedWork w) {
+  pdl_wait();
   if (sc->done) return;
   double acc[2] = {0., 0.};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
@@ -470,6 +480,7 @@ k_update(int n, VT *__restrict__ x, VT *__restrict__ r,
          const VT *__restrict__ ph, const VT *__restrict__ sh,
          const VT *__restrict__ s, const VT *__restrict__ t,
          const VT *__restrict__ rh, KScalars *sc, RedWork w) {
+  pdl_wait();
   if (sc->done) return;
   const double al = sc->alpha, om = sc->omega;
   const VT alv = (VT)al, omv = (VT)om;  // vector math in storage precision
@@ -771,20 +782,20 @@ void launch_unpermute_vec(int n, const int32_t *perm, const double *src,
 template <class VT, class MT>
 void launch_spmv_v(const SolverDev &d, const MT *val, const VT *ph, VT *v,
                    const VT *rh, KScalars *sc, RedWork w, cudaStream_t st) {
-  k_spmv_v<VT, MT><<<w.grid, kVecBlock, 0, st>>>(d, val, ph, v, rh, sc, w);
+  launch_pdl(k_spmv_v<VT, MT>, w.grid, kVecBlock, 0, st, d, val, ph, v, rh, sc, w);
   count_launches(1);
 }
 template <class VT, class MT>
 void launch_spmv_t(const SolverDev &d, const MT *val, const VT *sh, VT *t,
                    const VT *s, KScalars *sc, RedWork w, cudaStream_t st) {
-  k_spmv_t<VT, MT><<<w.grid, kVecBlock, 0, st>>>(d, val, sh, t, s, sc, w);
+  launch_pdl(k_spmv_t<VT, MT>, w.grid, kVecBlock, 0, st, d, val, sh, t, s, sc, w);
   count_launches(1);
 }
 template <class VT>
 void launch_update(int n, VT *x, VT *r, const VT *ph, const VT *sh,
                    const VT *s, const VT *t, const VT *rh, KScalars *sc,
                    RedWork w, cudaStream_t st) {
-  k_update<VT><<<w.grid, kVecBlock, 0, st>>>(n, x, r, ph, sh, s, t, rh, sc, w);
+  launch_pdl(k_update<VT>, w.grid, kVecBlock, 0, st, n, x, r, ph, sh, s, t, rh, sc, w);
   count_launches(1);
 }
 void launch_init_from_r(int n, double *r, double *rh, double *p, double *v,

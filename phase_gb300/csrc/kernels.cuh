@@ -11,6 +11,36 @@ namespace pg {
 void count_launches(int k);
 uint64_t launch_count();
 
+// Programmatic dependent launch.  A kernel started by launch_pdl may be
+// scheduled while the previous kernel of its stream is finishing (captured
+// CUDA graphs keep this as a programmatic edge): it calls pdl_wait() before
+// touching anything that kernel writes (the wait returns once that grid
+// has completed and its writes are visible; at once without PDL), and
+// pdl_trigger() so the next kernel may be scheduled in turn.  PG_PDL=0 in
+// the environment launches them in plain stream order.
+__device__ __forceinline__ void pdl_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+bool pdl_enabled();
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block,
+                       size_t smem, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 // Scalars of one BiCGStab run, resident in device memory.  The last block of
 // every reducing kernel updates them, so the iteration never waits on the
 // host; kernels read them at entry and return at once when `done` is set.
