@@ -82,6 +82,11 @@ def parse():
                     help="two-level Schwarz coarse correction on the "
                          "subdomain-constant vectors: 0 none, 1 additive, "
                          "2 deflated (A-DEF1)")
+    ap.add_argument("--learned-coarse-warm", type=int, default=0,
+                    help="one-level iterations the learned arm runs while "
+                         "the coarse inverse is built (0: it waits, its "
+                         "inference overlapping the inversion; -1: the "
+                         "solver's default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--mode", default="sequence",
@@ -323,11 +328,13 @@ def run_sequence(args):
                                subdomain_rows=args.subdomain_rows,
                                coarse=args.coarse)
     # the learned arm overlaps the coarse inverse with the network's
-    # inference, so its solves wait for the inverse instead of warming up
+    # inference; by default its solves then wait for the inverse instead of
+    # warming up (--learned-coarse-warm)
     sm = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
                                precision=pg.MIXED,
                                subdomain_rows=args.subdomain_rows,
-                               coarse=args.coarse, coarse_warm=0)
+                               coarse=args.coarse,
+                               coarse_warm=args.learned_coarse_warm)
     xp_p = torch.zeros(n, dtype=torch.float64, device=dev)
     xp_m = torch.zeros(n, dtype=torch.float64, device=dev)
     g = torch.empty(n, dtype=torch.float64, device=dev)
@@ -453,7 +460,7 @@ def run_sequence(args):
     e2e = None
     if not args.no_e2e:
         e2e = e2e_learned(pg, guess, seq, net, have_w, steps[:3], torch, dev,
-                          args.coarse)
+                          args.coarse, args.learned_coarse_warm)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -498,6 +505,7 @@ def run_sequence(args):
                        f"{sm.partition()[1]} subdomains"
                        + {0: "", 1: " + additive coarse correction",
                           2: " + deflated coarse correction (A-DEF1)"}[args.coarse],
+                       "learned_coarse_warm": args.learned_coarse_warm,
                        "learned_weights": os.path.relpath(guess.DEFAULT_WEIGHTS, ROOT)
                        if have_w else None,
                        "l2": "256 MB flush write before every step; working "
@@ -542,7 +550,8 @@ def run_sequence(args):
         torch.distributed.destroy_process_group()
 
 
-def e2e_learned(pg, guess, seq, net, have_w, steps, torch, dev, coarse):
+def e2e_learned(pg, guess, seq, net, have_w, steps, torch, dev, coarse,
+                coarse_warm=0):
     """The learned+mixed solve through the C ABI with host buffers: the
     caller holds the step's CrsEquation (5-slot layout), its rhs and the
     previous solution on the host; they are uploaded, the network predicts
@@ -550,7 +559,7 @@ def e2e_learned(pg, guess, seq, net, have_w, steps, torch, dev, coarse):
     import numpy as np
     s2 = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
                                precision=pg.MIXED, coarse=coarse,
-                               coarse_warm=0)
+                               coarse_warm=coarse_warm)
     # the caller's geometry hint: cell centroids cut the Schwarz subdomains
     s2.setRank(seq.n)
     s2.set_row_coords(np.stack([seq.cells["cx"], seq.cells["cy"]], axis=1))
