@@ -36,7 +36,10 @@ Ifpack2 Schwarz/RILUK as run on that many MPI ranks) on the same workload:
 in sequence mode the same held-out steps, each warm from its previous CPU
 solution; in single mode the zero-guess solve on a bounded sample.
 `iters_saved_by_guess` compares the learned arm's iteration counts with the
-float-float arm warm from the previous x, step by step.
+float-float arm warm from the previous x, step by step.  With --coarse-reuse 1
+every arm's solve applies the previous step's coarse inverse while the new
+one is built beside it (measured slower on this sequence: more iterations
+on several steps, and the inversion competes with the solve).
 """
 from __future__ import annotations
 
@@ -82,6 +85,10 @@ def parse():
                     help="two-level Schwarz coarse correction on the "
                          "subdomain-constant vectors: 0 none, 1 additive, "
                          "2 deflated (A-DEF1)")
+    ap.add_argument("--coarse-reuse", type=int, choices=(0, 1), default=0,
+                    help="sequence mode: each solve applies the previous "
+                         "step's coarse inverse while the new one is built "
+                         "beside it (the solver's coarse_warm = -2)")
     ap.add_argument("--learned-coarse-warm", type=int, default=0,
                     help="one-level iterations the learned arm runs while "
                          "the coarse inverse is built (0: it waits, its "
@@ -324,17 +331,21 @@ def run_sequence(args):
     have_w = os.path.exists(guess.DEFAULT_WEIGHTS)
     if have_w:
         net.set_params(np.load(guess.DEFAULT_WEIGHTS))
+    # with --coarse-reuse every arm applies the previous step's coarse
+    # inverse while the new one is built; without it the learned arm
+    # overlaps the inversion with the network's inference and then waits
+    # for it (--learned-coarse-warm), the others warm up beside it
+    reuse = -2 if args.coarse_reuse else None
     sp = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
                                subdomain_rows=args.subdomain_rows,
-                               coarse=args.coarse)
-    # the learned arm overlaps the coarse inverse with the network's
-    # inference; by default its solves then wait for the inverse instead of
-    # warming up (--learned-coarse-warm)
+                               coarse=args.coarse,
+                               coarse_warm=reuse if reuse else -1)
     sm = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
                                precision=pg.MIXED,
                                subdomain_rows=args.subdomain_rows,
                                coarse=args.coarse,
-                               coarse_warm=args.learned_coarse_warm)
+                               coarse_warm=reuse if reuse
+                               else args.learned_coarse_warm)
     xp_p = torch.zeros(n, dtype=torch.float64, device=dev)
     xp_m = torch.zeros(n, dtype=torch.float64, device=dev)
     g = torch.empty(n, dtype=torch.float64, device=dev)
@@ -351,7 +362,8 @@ def run_sequence(args):
     sq = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
                                precision=pg.MIXED,
                                subdomain_rows=args.subdomain_rows,
-                               coarse=args.coarse)
+                               coarse=args.coarse,
+                               coarse_warm=reuse if reuse else -1)
 
     def mixed_prev_step(t):
         """Float-float solve warm from its own previous x (no network)."""
@@ -460,7 +472,8 @@ def run_sequence(args):
     e2e = None
     if not args.no_e2e:
         e2e = e2e_learned(pg, guess, seq, net, have_w, steps[:3], torch, dev,
-                          args.coarse, args.learned_coarse_warm)
+                          args.coarse, reuse if reuse
+                          else args.learned_coarse_warm)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -505,6 +518,7 @@ def run_sequence(args):
                        f"{sm.partition()[1]} subdomains"
                        + {0: "", 1: " + additive coarse correction",
                           2: " + deflated coarse correction (A-DEF1)"}[args.coarse],
+                       "coarse_reuse": bool(args.coarse_reuse),
                        "learned_coarse_warm": args.learned_coarse_warm,
                        "learned_weights": os.path.relpath(guess.DEFAULT_WEIGHTS, ROOT)
                        if have_w else None,

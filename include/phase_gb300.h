@@ -302,7 +302,12 @@ typedef struct {
                          with the two-level preconditioner: -1 = default (16
                          with at least 1024 subdomains, else 0), 0 = wait
                          for the inverse (when the caller already had work
-                         to overlap it with after the hand-over) */
+                         to overlap it with after the hand-over), -2 = apply
+                         the previous factorisation's inverse (same
+                         pattern) for the whole solve while the new one is
+                         built beside it, for the next solve (time loops,
+                         where the coarse matrix changes little from step
+                         to step; the first solve behaves as -1) */
   double reserved_d;  /* ignored */
 } pg_solver_cfg;
 

@@ -89,9 +89,10 @@ struct pg_solver {
   // arguments are fixed device pointers, so a graph stays valid until the
   // buffers are reallocated by a new analysis
   // [0] FP64, [1] float-float; [2], [3] the same without the coarse
-  // correction (the warm-up iterations while the coarse inverse is built)
-  cudaGraphExec_t chunk_graph[4] = {nullptr, nullptr, nullptr, nullptr};
-  int chunk_launches[4] = {0, 0, 0, 0};  // kernels in one replay of each graph
+  // correction (the warm-up iterations while the coarse inverse is built);
+  // [4], [5] as [0], [1] with the second coarse-inverse buffer
+  cudaGraphExec_t chunk_graph[6] = {};
+  int chunk_launches[6] = {};  // kernels in one replay of each graph
   // two-level Schwarz coarse space (cfg.coarse): structure, the dense
   // coarse matrix / its inverse, elimination buffers, subdomain sums and the
   // graph of the K elimination steps
@@ -112,6 +113,17 @@ struct pg_solver {
   DevBuf<double> c_azv, c_y, c_tmp;
   DevBuf<float2> c_azv_dd, c_y_dd, c_tmp_dd;
   cudaGraphExec_t gj_graph = nullptr;
+  // cfg.coarse_warm = -2: a solve applies the previous factorisation's
+  // inverse while the new one is built on side2 into the other buffer
+  // (c_ac / c_ac2, one Gauss-Jordan graph each); a join makes the new one
+  // current
+  DevBuf<float> c_ac2;
+  cudaGraphExec_t gj_graph2 = nullptr;
+  int ac_ready = 0;      // the buffer the drivers apply
+  int ac_next = -1;      // the buffer being inverted on side2 (-1: none)
+  bool ac_valid = false; // ac_ready holds an inverse for this analysis
+  float *ac_buf(int b) const { return b ? c_ac2.p : c_ac.p; }
+  cudaGraphExec_t *gj_graph_of(int b) { return b ? &gj_graph2 : &gj_graph; }
 
   void drop_graphs() {
     for (auto &g : chunk_graph)
@@ -119,10 +131,11 @@ struct pg_solver {
         cudaGraphExecDestroy(g);
         g = nullptr;
       }
-    if (gj_graph) {
-      cudaGraphExecDestroy(gj_graph);
-      gj_graph = nullptr;
-    }
+    for (cudaGraphExec_t *g : {&gj_graph, &gj_graph2})
+      if (*g) {
+        cudaGraphExecDestroy(*g);
+        *g = nullptr;
+      }
   }
 
   CoarseDev coarse() const {
@@ -134,7 +147,7 @@ struct pg_solver {
     c.cptr = c_cptr.p;
     c.cnb = c_cnb.p;
     c.cslot = c_slot.p;
-    c.ac = c_ac.p;
+    c.ac = ac_buf(ac_ready);
     c.dg0 = c_dg0.p;
     c.pinv = c_pinv.p;
     c.W = c_W.p;
@@ -315,6 +328,10 @@ int upload_analysis(pg_solver *s) {
     up(s->c_cnb, a.cnb);
     up(s->c_slot, a.cslot);
     if (e == cudaSuccess) e = s->c_ac.reserve(K * K);
+    if (e == cudaSuccess && s->cfg.coarse_warm == -2) e = s->c_ac2.reserve(K * K);
+    s->ac_ready = 0;
+    s->ac_next = -1;
+    s->ac_valid = false;
     if (e == cudaSuccess) e = s->c_dg0.reserve(K);
     if (e == cudaSuccess) e = s->c_pinv.reserve(32 * 32);
     for (DevBuf<float> *bf : {&s->c_W, &s->c_V, &s->c_C})
@@ -369,6 +386,9 @@ int join_coarse(pg_solver *s) {
   if (!s->coarse_pending) return PG_OK;
   PG_CUDA(cudaStreamWaitEvent(stream(), s->ev_coarse, 0));
   s->coarse_pending = false;
+  if (s->ac_next >= 0) s->ac_ready = s->ac_next;  // the new inverse is current
+  s->ac_next = -1;
+  s->ac_valid = true;
   return PG_OK;
 }
 
@@ -523,7 +543,7 @@ int run_bicgstab(pg_solver *s, double tol, int max_iters, int *iters,
   if (s->sc_host->rr_true <= init.tol2 * bb) return PG_OK;
   double rr_ref = s->sc_host->rr_true;
   int restarts = 0;
-  const int slot = cdev.K ? 0 : 2;
+  const int slot = cdev.K ? (s->ac_ready ? 4 : 0) : 2;
   cudaGraphExec_t &gexec = s->chunk_graph[slot];
   bool direct_done = false;
   for (;;) {
@@ -658,8 +678,9 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
   int restarts = 0;
   bool direct_done = false;
   for (;;) {
-    if ((rc = run_chunk(s->chunk_graph[cdev.K ? 1 : 3],
-                        s->chunk_launches[cdev.K ? 1 : 3], direct_done, chunk)))
+    const int slot = cdev.K ? (s->ac_ready ? 5 : 1) : 3;
+    if ((rc = run_chunk(s->chunk_graph[slot], s->chunk_launches[slot],
+                        direct_done, chunk)))
       return rc;
     if ((rc = read_scalars())) return rc;
     const KScalars k = *s->sc_host;
@@ -769,22 +790,41 @@ int factor(pg_solver *s, cudaStream_t st) {
     PG_CUDA(cudaMemsetAsync(s->bad.p, 0, sizeof(int), st));
     launch_ilu0_factor(d, s->pvals.p, s->bad.p, dd, st);
     if (s->coarse_on) {
-      // beside the ILU(0) factorisation and the first iterations
-      PG_CUDA(cudaEventRecord(s->ev_cvals, st));
-      PG_CUDA(cudaStreamWaitEvent(s->side2, s->ev_cvals, 0));
+      // beside the ILU(0) factorisation and the first iterations; with
+      // cfg.coarse_warm = -2 into the buffer the next solve will apply,
+      // the current one staying in use, and the A Z values (read by the
+      // solve) on the factorisation stream
+      const bool reuse = s->cfg.coarse_warm == -2;
+      if (reuse) {
+        int rj = join_coarse(s);  // the previous inverse becomes current
+        if (rj) return rj;
+      }
+      const int target = reuse && s->ac_valid ? 1 - s->ac_ready : s->ac_ready;
       const bool use = s->coarse_use;
       s->coarse_use = true;
-      launch_coarse_setup(s->coarse(), s->pvals.p, s->prp.p, &s->gj_graph,
-                          s->side2);
-      if (s->cfg.coarse == 2) {
-        launch_az_values(s->coarse(), (int)s->a.n, s->prp.p, s->pvals.p, s->side2);
+      CoarseDev ct = s->coarse();
+      ct.ac = s->ac_buf(target);
+      cudaStream_t azs = reuse ? st : s->side2;
+      if (reuse && s->cfg.coarse == 2) {
+        launch_az_values(ct, (int)s->a.n, s->prp.p, s->pvals.p, azs);
         if (dd)
           launch_dd_split((int64_t)s->a.azj.size(), s->c_azv.p, 1.0,
-                          s->c_azv_dd.p, s->side2);
+                          s->c_azv_dd.p, azs);
+      }
+      PG_CUDA(cudaEventRecord(s->ev_cvals, st));
+      PG_CUDA(cudaStreamWaitEvent(s->side2, s->ev_cvals, 0));
+      launch_coarse_setup(ct, s->pvals.p, s->prp.p, s->gj_graph_of(target),
+                          s->side2);
+      if (!reuse && s->cfg.coarse == 2) {
+        launch_az_values(ct, (int)s->a.n, s->prp.p, s->pvals.p, azs);
+        if (dd)
+          launch_dd_split((int64_t)s->a.azj.size(), s->c_azv.p, 1.0,
+                          s->c_azv_dd.p, azs);
       }
       s->coarse_use = use;
       PG_CUDA(cudaEventRecord(s->ev_coarse, s->side2));
       s->coarse_pending = true;
+      s->ac_next = target;
     }
   } else if (s->cfg.precond == PG_PREC_JACOBI) {
     launch_jacobi_diag(d, s->pvals.p, s->jdinv.p, st);
@@ -843,7 +883,7 @@ extern "C" int pg_solver_create(const pg_solver_cfg *cfg, pg_solver **out) {
   PG_CHECK_ARG(c.mixed_sweep >= 0 && c.mixed_sweep <= 2,
                "pg_solver_create: bad mixed_sweep");
   PG_CHECK_ARG(c.coarse >= 0 && c.coarse <= 2, "pg_solver_create: bad coarse");
-  PG_CHECK_ARG(c.coarse_warm >= -1, "pg_solver_create: bad coarse_warm");
+  PG_CHECK_ARG(c.coarse_warm >= -2, "pg_solver_create: bad coarse_warm");
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0 || !stream()) {
     set_error("no CUDA device available: libphase_gb300 has no CPU path");
@@ -1076,7 +1116,11 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
   const int warm = s->cfg.coarse_warm >= 0 ? s->cfg.coarse_warm
                    : s->a.n_sub >= kCoarseStagedK ? kCoarseWarmIters
                                                   : 0;
-  if (s->coarse_pending && warm > 0 && s->cfg.max_iters > warm) {
+  if (s->coarse_pending && s->cfg.coarse_warm == -2 && s->ac_valid) {
+    // the previous factorisation's coarse inverse preconditions the whole
+    // solve (a fixed operator) while the new one is built on side2
+    status = run(s->cfg.max_iters, &iters, &outer);
+  } else if (s->coarse_pending && warm > 0 && s->cfg.max_iters > warm) {
     // while the coarse inverse is built on side2: `warm` one-level
     // iterations, then a restart from their x with the two-level
     // preconditioner (a fixed count, so results do not depend on timing)
@@ -1213,7 +1257,8 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
     rc = timed([&] {
       launch_ilu0_factor(d, s->pvals.p, s->bad.p, dd, st);
       if (s->coarse_on)
-        launch_coarse_setup(s->coarse(), s->pvals.p, s->prp.p, &s->gj_graph, st);
+        launch_coarse_setup(s->coarse(), s->pvals.p, s->prp.p,
+                            s->gj_graph_of(s->ac_ready), st);
     }, &ms[3]);
   if (!rc && s->coarse_on) {
     const CoarseDev c = s->coarse();
@@ -1346,7 +1391,7 @@ extern "C" int pg_solver_coarse_inverse(pg_solver *s, float *out, int *k) {
   if (k) *k = (int)K;
   if (out) {
     cudaStream_t st = stream();
-    PG_CUDA(cudaMemcpyAsync(out, s->c_ac.p, K * K * sizeof(float),
+    PG_CUDA(cudaMemcpyAsync(out, s->ac_buf(s->ac_ready), K * K * sizeof(float),
                             cudaMemcpyDeviceToHost, st));
     PG_CUDA(cudaStreamSynchronize(st));
   }
