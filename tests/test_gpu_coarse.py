@@ -168,3 +168,40 @@ def test_two_level_gcib_and_cylinder(pg):
                 its[(coarse, prec)] = s.nIters()
         print("iterations (coarse, precision):", its)
         assert its[(1, pg.FP64)] < its[(0, pg.FP64)]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_coarse_inverse_reuse_sequence(pg, precision):
+    """cfg.coarse_warm = -2: each solve of a time sequence applies the
+    previous factorisation's coarse inverse while the new one is built
+    beside it (double-buffered).  Every solve still meets the tolerance on
+    the FP64 true residual, and a join makes the newest inverse current:
+    after the last step the solver's inverse is bit-identical to that of a
+    fresh solver on the last system."""
+    pytest.importorskip("torch")
+    from phase_gb300 import guess
+    seq = guess.BubbleSequence(nx=256, seed=3)
+    prec = pg.FP64 if precision == "fp64" else pg.MIXED
+    s = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000, coarse=2,
+                              coarse_warm=-2, precision=prec)
+    x = None
+    for t in (100, 101, 102, 103):
+        eqn = seq.assemble(t)
+        rp, ci, v, rhs = eqn.export()
+        keep = ci >= 0
+        n = len(rp) - 1
+        rows = np.repeat(np.arange(n), np.diff(rp))[keep]
+        A = sp.csr_matrix((v[keep], (rows, ci[keep])), shape=(n, n))
+        s.set_eqn(eqn)
+        s.setGuess(x)
+        s.solve()
+        assert s.stats.status == pg.PG_OK
+        x = s.x()
+        b = -rhs
+        assert np.linalg.norm(b - A @ x) / np.linalg.norm(b) <= 1.01e-8
+    X = s.coarse_inverse()
+    f = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000, coarse=2,
+                              precision=prec)
+    f.set_eqn(eqn)
+    f.solve()
+    np.testing.assert_array_equal(X, f.coarse_inverse())
