@@ -421,8 +421,9 @@ uint64_t pg_kernel_launches(void);
  * returns the number of subdomains in *n_parts. */
 int pg_solver_partition(const pg_solver *s, int32_t *part, int *n_parts);
 
-/* The two-level preconditioner's coarse inverse (cfg.coarse = 1) after the
- * last factorisation: the K x K row-major FP32 approximation of
+/* The two-level preconditioner's coarse inverse (cfg.coarse = 1 or 2) of
+ * the last factorisation (an inversion still running is joined first): the
+ * K x K row-major FP32 approximation of
  * (Z^T A Z)^-1 that the solver applies, K = *n_parts of pg_solver_partition
  * and Z the subdomain indicator vectors (host, out[K*K]).  Returns
  * PG_INVALID_ARG when no coarse space is active.  (Inspection; no reference

@@ -131,8 +131,8 @@ def solver_options(tree: Node, equation: str = "pEqn") -> dict:
     ``LinearAlgebra.<equation>``: tolerance, maxIters, preconditioner
     (ilu0 | jacobi | none, or the Ifpack2 names of the Trilinos backend:
     RILUK/ILUT/Schwarz -> ILU(0) blocks, diagonal/relaxation -> Jacobi),
-    subdomainRows, coarseSpace, precision (fp64 | mixed), mixedSweep.
-    Absent keys keep the solver's defaults."""
+    subdomainRows, coarseSpace, coarseWarmIters, precision (fp64 | mixed),
+    mixedSweep.  Absent keys keep the solver's defaults."""
     sec = tree.child("LinearAlgebra")
     sec = sec.child(equation) if sec is not None else None
     if sec is None:
@@ -152,6 +152,8 @@ def solver_options(tree: Node, equation: str = "pEqn") -> dict:
         out["subdomain_rows"] = int(sec.get("subdomainRows"))
     if sec.get("coarseSpace") is not None:
         out["coarse"] = int(sec.get("coarseSpace"))
+    if sec.get("coarseWarmIters") is not None:
+        out["coarse_warm"] = int(sec.get("coarseWarmIters"))
     if sec.get("precision") is not None:
         p = sec.get("precision").strip().lower()
         if p not in ("fp64", "mixed"):

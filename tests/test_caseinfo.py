@@ -40,6 +40,7 @@ LinearAlgebra
     maxIters 500
     preconditioner ilu0
     coarseSpace 1
+    coarseWarmIters 0
     precision mixed
   }
   gammaEqn { lib trilinos }
@@ -96,7 +97,8 @@ def test_parse_info_rejects_malformed(bad):
 def test_solver_options():
     t = caseinfo.parse_info(CASE)
     assert caseinfo.solver_options(t, "pEqn") == dict(
-        tolerance=1e-8, max_iters=500, precond=2, coarse=1, precision=1)
+        tolerance=1e-8, max_iters=500, precond=2, coarse=1, coarse_warm=0,
+        precision=1)
     # the reference's Trilinos keys map onto the same options
     assert caseinfo.solver_options(t, "uEqn") == dict(
         tolerance=1e-10, max_iters=100, precond=1)
