@@ -197,6 +197,20 @@ def test_bicgstab_matches_scipy_direct(oracle, precond):
     assert st["rel_residual"] <= 1e-10
 
 
+def test_threaded_bicgstab_is_reproducible(oracle):
+    """The oracle's dot products sum fixed per-thread chunks in thread order,
+    so a threaded solve repeats bit for bit (the CPU baseline's iteration
+    counts depend on it)."""
+    rp, ci, v, b = _poisson_system(oracle, 60, 50)
+    n = len(rp) - 1
+    part = (np.arange(n) * 4 // n).astype(np.int32)
+    runs = [oracle.bicgstab(rp, ci, v, b, tol=1e-13, max_iters=60, part=part,
+                            threads=4) for _ in range(3)]
+    for x, st in runs[1:]:
+        assert st["iters"] == runs[0][1]["iters"]
+        assert np.array_equal(x, runs[0][0])
+
+
 def test_ilu0_matches_scipy_spilu_pattern_zero_fill(oracle):
     """ILU(0) factors satisfy (L U)_ij = a_ij on the pattern of A."""
     rp, ci, v, _ = _poisson_system(oracle, 9, 7)
