@@ -263,8 +263,8 @@ def az_nnz(eqn, part):
 def kernel_roofline(pg, solver, n, nnz, dd, eqn=None, coarse=0):
     """Per-launch CUDA-event times of the hot kernels of one solver on its
     current system (pg_solver_profile) and the roofline of the dominant
-    one.  Compulsory bytes per launch: A values +
-    int32 columns + row pointers; ILU(0) factor values + 2-byte columns
+    one.  Compulsory bytes per launch: A values + int32 columns + row
+    pointers; ILU(0) factor values + 2-byte columns
     (off-diagonal entries of A bound the factor's) + 1/u_ii; 8-byte vector
     entries in both precisions."""
     prof = solver.profile(reps=50)
