@@ -6,6 +6,7 @@ import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
 from phase_gb300 import meshes
+import golden_cases
 import refreplay
 
 
@@ -129,6 +130,30 @@ def test_row_growth_past_five_slots_matches_reference(oracle):
     mine = om.laplacian(1.0, bc, np.zeros(om.n_faces), slots=True)
     assert ref[0][1] - ref[0][0] == 7
     for a, b in zip(ref, mine):
+        assert np.array_equal(a, b)
+
+
+def test_golden_fixtures_present():
+    """tests/golden holds the reference CrsEquation's output for the five
+    seeded cases of tests/golden/make_golden.py."""
+    assert len(golden_cases.CASES) >= 5
+
+
+@pytest.mark.parametrize("name", golden_cases.CASES)
+def test_oracle_matches_reference_golden(oracle, name):
+    """The oracle reproduces the fixtures the reference's own CrsEquation
+    wrote (slot arrays, placeholders and the rows grown past five slots
+    included) bit for bit, and its compact form is those arrays without
+    the placeholders."""
+    z, gamma, u = golden_cases.load(name)
+    om = oracle.OracleMesh(z["nodes"], z["cptr"], z["cind"])
+    ref = (z["row_ptr"], z["col_ind"], z["vals"], z["rhs"])
+    mine = om.laplacian(gamma, z["bc_type"], z["bc_value"], u, slots=True)
+    for a, b in zip(ref, mine):
+        assert a.shape == b.shape
+        assert np.array_equal(a, b), "oracle differs from the reference fixture"
+    compact = om.laplacian(gamma, z["bc_type"], z["bc_value"], u)
+    for a, b in zip(golden_cases.compact(z), compact):
         assert np.array_equal(a, b)
 
 
