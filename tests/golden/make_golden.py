@@ -51,7 +51,7 @@ def cases():
     return out
 
 
-def make(name, mesh, kind, with_u, seed=7):
+def make(name, mesh, kind, with_u, seed=7, out_dir=HERE):
     nodes, cptr, cind = mesh
     om = ob.OracleMesh(nodes, cptr, cind)
     rng = np.random.default_rng(seed)
@@ -72,7 +72,7 @@ def make(name, mesh, kind, with_u, seed=7):
     if u is not None:
         r.eq_vector(refreplay.div_u(om, u))
     rp, ci, v, rhs = r.export()
-    np.savez(os.path.join(HERE, name + ".npz"),
+    np.savez(os.path.join(out_dir, name + ".npz"),
              nodes=nodes, cptr=cptr, cind=cind,
              gamma=np.asarray(gamma, np.float64),
              gamma_is_scalar=np.array(kind == "scalar"),

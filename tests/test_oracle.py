@@ -1,5 +1,7 @@
 """CPU tests of the oracle: known answers, the reference's own CrsEquation,
 golden vectors and an independent scipy cross-check.  No GPU needed."""
+import os
+
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -137,6 +139,29 @@ def test_golden_fixtures_present():
     """tests/golden holds the reference CrsEquation's output for the five
     seeded cases of tests/golden/make_golden.py."""
     assert len(golden_cases.CASES) >= 5
+
+
+def test_golden_fixtures_regenerate_identically(oracle, tmp_path):
+    """The committed fixtures are what tests/golden/make_golden.py writes
+    from the reference's CrsEquation (where its sources can be built)."""
+    if oracle.ref_lib() is None:
+        pytest.skip("reference sources absent: oracle/_ref not built")
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_golden", os.path.join(golden_cases.GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    names = []
+    for name, mesh, kind, with_u in mg.cases():
+        mg.make(name, mesh, kind, with_u, out_dir=str(tmp_path))
+        names.append(name)
+    assert sorted(names) == golden_cases.CASES
+    for name in names:
+        a = np.load(os.path.join(golden_cases.GOLDEN, name + ".npz"))
+        b = np.load(os.path.join(str(tmp_path), name + ".npz"))
+        assert sorted(a.files) == sorted(b.files)
+        for k in a.files:
+            assert np.array_equal(a[k], b[k]), (name, k)
 
 
 @pytest.mark.parametrize("name", golden_cases.CASES)
