@@ -338,11 +338,11 @@ void launch_ilu0_factor(const SolverDev &d, const double *pvals, int *bad,
 //   mode 0: z = M^-1 in
 //   mode 1: p = r + beta (p - omega v); z = M^-1 p   (p written back)
 //   mode 2: s = r - alpha v;            z = M^-1 s   (s written back)
-//   mode 3: z = M^-1 (in - (A Z) y) + Z y  (the deflated coarse correction
-//           around the ILU(0) sweeps; streamed sweep forms only)
-// mode 3 of the streamed ILU(0) sweep (d.def_y set): z = B in + Z y for a
-// deflated input in = p - A Z y; false when the streamed form is not
-// available
+//   mode 3: z = B in + Z y, in = p - (A Z) y already formed by k_def_in
+//           (the output half of the deflated coarse correction; streamed
+//           sweep forms only)
+// Mode 3 of the streamed ILU(0) sweep (d.def_y set); false when the
+// streamed form is not available
 bool launch_ilu0_apply_def(const SolverDev &d, const double *in, double *z,
                            const KScalars *sc, cudaStream_t st);
 bool launch_ilu0_apply_def_dd(const SolverDev &d, const float2 *in, float2 *z,
