@@ -291,7 +291,11 @@ k_coarse_correct(int K, const int32_t *__restrict__ sub_ptr,
 // A-DEF1 (Tang, Nabben, Vuik & Erlangga, J. Sci. Comput. 39, 2009):
 //     M^-1 r = B (r - A Z y) + Z y,   y = A_c^-1 Z^T r,
 // B the Schwarz ILU(0) sweeps.  A Z is kept per row as the sums of the
-// row's entries over each subdomain its columns fall in.
+// row's entries over each subdomain its columns fall in.  One application:
+// k_def_pre (the Krylov update of the input and its subdomain sums),
+// k_coarse_y (y), k_def_in (r - A Z y), then the sweep; the streamed sweep
+// adds Z y as it writes z (its mode 3), k_coarse_add does it after the
+// other sweep forms.
 
 // (A Z) values from the permuted matrix, row by row in entry order
 __global__ void k_az_values(int n, const int32_t *__restrict__ prp,
