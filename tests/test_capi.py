@@ -59,3 +59,18 @@ def test_no_silent_cpu_path_without_gpu(built):
     assert ei.value.status == built.PG_CUDA_ERROR
     with pytest.raises(built.PhaseError):
         built.SparseMatrixSolver()
+
+
+def test_header_is_c99_and_links_from_c(built, tmp_path):
+    """A C caller: the header compiles as strict C99 and the program links
+    against the library and reads the default configuration (no GPU call)."""
+    exe = str(tmp_path / "c_abi_check")
+    lib_dir = os.path.dirname(built.LIB_PATH)
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror",
+                    "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "c_abi_check.c"),
+                    "-L", lib_dir, "-lphase_gb300", "-Wl,-rpath," + lib_dir,
+                    "-o", exe], check=True, capture_output=True, text=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "max_iters 500" in r.stdout
