@@ -822,22 +822,33 @@ extern "C" int or_bicgstab(int64_t n, const int32_t *row_ptr,
   return st.status;
 }
 
-extern "C" int or_bicgstab_history(int64_t n, const int32_t *row_ptr,
-                                   const int32_t *col_ind, const double *vals,
-                                   const double *b, const or_solver_cfg *cfg,
-                                   double *hist, double *ms_out,
-                                   double *setup_ms_out) {
+extern "C" int or_bicgstab_history_x0(int64_t n, const int32_t *row_ptr,
+                                      const int32_t *col_ind,
+                                      const double *vals, const double *b,
+                                      const double *x0,
+                                      const or_solver_cfg *cfg, double *hist,
+                                      double *ms_out, double *setup_ms_out) {
   ThreadScope ts(cfg->n_threads);
   Csr A{n, row_ptr, col_ind, vals};
   std::vector<double> x(n, 0.);
+  if (x0) std::copy(x0, x0 + n, x.begin());
   or_solver_cfg c = *cfg;
-  c.use_guess = 0;
+  c.use_guess = x0 ? 1 : 0;
   std::vector<double> h(c.max_iters + 3, 0.);
   int it = bicgstab(A, b, x.data(), c, nullptr, h.data(), 0);
   for (int i = 0; i <= it; ++i) hist[i] = h[i];
   *ms_out = h[c.max_iters + 1];
   *setup_ms_out = h[c.max_iters + 2];
   return it;
+}
+
+extern "C" int or_bicgstab_history(int64_t n, const int32_t *row_ptr,
+                                   const int32_t *col_ind, const double *vals,
+                                   const double *b, const or_solver_cfg *cfg,
+                                   double *hist, double *ms_out,
+                                   double *setup_ms_out) {
+  return or_bicgstab_history_x0(n, row_ptr, col_ind, vals, b, nullptr, cfg,
+                                hist, ms_out, setup_ms_out);
 }
 
 extern "C" int or_ilu0(int64_t n, const int32_t *row_ptr,

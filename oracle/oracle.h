@@ -130,6 +130,13 @@ int or_bicgstab_history(int64_t n, const int32_t *row_ptr,
                         const int32_t *col_ind, const double *vals,
                         const double *b, const or_solver_cfg *cfg,
                         double *hist, double *ms_out, double *setup_ms_out);
+/* The same from the initial guess x0[n] (NULL: zero), as a time loop's
+ * solve warm from the previous step's solution. */
+int or_bicgstab_history_x0(int64_t n, const int32_t *row_ptr,
+                           const int32_t *col_ind, const double *vals,
+                           const double *b, const double *x0,
+                           const or_solver_cfg *cfg, double *hist,
+                           double *ms_out, double *setup_ms_out);
 
 /* ILU(0) factor in place on a compact CSR (per subdomain when part given);
  * out_vals receives the L (unit, strictly lower) and U values in the CSR

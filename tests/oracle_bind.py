@@ -77,6 +77,9 @@ def lib():
         L.or_bicgstab_history.restype = ctypes.c_int
         L.or_bicgstab_history.argtypes = [I64, P, P, P, P,
                                           ctypes.POINTER(OrCfg), P, P, P]
+        L.or_bicgstab_history_x0.restype = ctypes.c_int
+        L.or_bicgstab_history_x0.argtypes = [I64, P, P, P, P, P,
+                                             ctypes.POINTER(OrCfg), P, P, P]
         L.or_ilu0.restype = ctypes.c_int
         L.or_ilu0.argtypes = [I64, P, P, P, P, P]
         L.or_ilu0_apply.argtypes = [I64, P, P, P, P, P, P]
@@ -267,8 +270,9 @@ def bicgstab(rp, ci, v, b, tol=1e-8, max_iters=500, precond=OR_PREC_ILU0,
 
 
 def bicgstab_history(rp, ci, v, b, max_iters, precond=OR_PREC_ILU0, part=None,
-                     threads=0):
-    """Run max_iters iterations; return (residual history, ms, setup_ms)."""
+                     threads=0, x0=None):
+    """Run max_iters iterations from x0 (None: zero); return (residual
+    history, ms, setup_ms)."""
     rp = np.ascontiguousarray(rp, np.int32)
     ci = np.ascontiguousarray(ci, np.int32)
     v = np.ascontiguousarray(v, np.float64)
@@ -281,9 +285,10 @@ def bicgstab_history(rp, ci, v, b, max_iters, precond=OR_PREC_ILU0, part=None,
     hist = np.zeros(max_iters + 1)
     ms = np.zeros(1)
     sms = np.zeros(1)
-    it = lib().or_bicgstab_history(b.size, ptr(rp), ptr(ci), ptr(v), ptr(b),
-                                   ctypes.byref(cfg), ptr(hist), ptr(ms),
-                                   ptr(sms))
+    x = None if x0 is None else np.ascontiguousarray(x0, np.float64)
+    it = lib().or_bicgstab_history_x0(b.size, ptr(rp), ptr(ci), ptr(v),
+                                      ptr(b), ptr(x), ctypes.byref(cfg),
+                                      ptr(hist), ptr(ms), ptr(sms))
     return hist[:it + 1], float(ms[0]), float(sms[0])
 
 

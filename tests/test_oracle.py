@@ -261,6 +261,25 @@ def test_threaded_bicgstab_is_reproducible(oracle):
         assert np.array_equal(x, runs[0][0])
 
 
+def test_history_from_a_guess(oracle):
+    """The residual-history solve from an initial guess: from the exact
+    solution it starts at (nearly) zero residual; from a perturbed one it
+    starts at the perturbation's residual and follows the full solve's
+    iteration from the same guess."""
+    rp, ci, v, b = _poisson_system(oracle, 30, 24)
+    n = len(rp) - 1
+    A = sp.csr_matrix((v, ci, rp), shape=(n, n))
+    xs = spla.spsolve(A.tocsc(), b)
+    h, _, _ = oracle.bicgstab_history(rp, ci, v, b, 5, x0=xs)
+    assert h[0] < 1e-12
+    x0 = xs + 1e-3 * np.random.default_rng(3).standard_normal(n)
+    h0, _, _ = oracle.bicgstab_history(rp, ci, v, b, 5)
+    h1, _, _ = oracle.bicgstab_history(rp, ci, v, b, 5, x0=x0)
+    r0 = np.linalg.norm(b - A @ x0) / np.linalg.norm(b)
+    assert abs(h1[0] - r0) <= 1e-12 * max(r0, 1.0)
+    assert h1[0] < 1e-2 < h0[0]
+
+
 def test_ilu0_matches_scipy_spilu_pattern_zero_fill(oracle):
     """ILU(0) factors satisfy (L U)_ij = a_ij on the pattern of A."""
     rp, ci, v, _ = _poisson_system(oracle, 9, 7)
