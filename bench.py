@@ -234,7 +234,7 @@ def build_system(nx, want_device=True):
 def slots_layout(rp, ci, v):
     """Expand a compact CSR into CrsEquation's layout: 5 slots per row (more
     when a row is longer), unused slots with column -1
-    (CrsEquation.cpp:159-164)."""
+    (CrsEquation.cpp:9-14)."""
     import numpy as np
     n = len(rp) - 1
     cnt = np.diff(rp)

@@ -51,6 +51,12 @@ extern "C" {
                           Ifpack2 "schwarz" + "RILUK" level-of-fill 0
                           (TrilinosBelosSparseMatrixSolver.cpp:63-85) */
 
+/* Krylov methods (the Belos solver names of TrilinosBelosSparseMatrixSolver
+ * .cpp:59-60, key "solver") */
+#define PG_KRYLOV_BICGSTAB 0 /* "BICGSTAB" (the default) */
+#define PG_KRYLOV_TFQMR 1    /* "TFQMR" */
+#define PG_KRYLOV_GMRES 2    /* "GMRES" (restarted, right preconditioned) */
+
 /* arithmetic of the Krylov iteration */
 #define PG_FP64 0
 #define PG_MIXED 1 /* float-float (pairs of FP32, about 48 bits) Krylov
@@ -100,7 +106,7 @@ int pg_mesh_cells(const pg_mesh *m, double *cx, double *cy, double *vol);
  * Pressure equation on the device.  A pg_eqn is a FiniteVolumeEquation<Scalar>
  * (src/2D/Unstructured/FiniteVolume/Equation/FiniteVolumeEquation.h:14-98)
  * whose CSR lives in HBM.  Its sparsity pattern is that of CrsEquation after
- * fv::laplacian (CrsEquation.cpp:159-164,263-281): placeholder slots dropped,
+ * fv::laplacian (CrsEquation.cpp:9-14,113-131): placeholder slots dropped,
  * entries in order of first addCoeff.  bc_type[n_faces] (host) fixes the
  * boundary type of each boundary face for the life of the equation.
  * ---------------------------------------------------------------------- */
@@ -156,7 +162,7 @@ int pg_eqn_sizes(const pg_eqn *e, int64_t *n_rows, int64_t *nnz);
  * face-coloured kernels.  Replaces Laplacian.h:49-83 (gamma_face == NULL,
  * scalar gamma) or :132-167 (gamma_face[n_faces]), Source.cpp:5-21
  * (u_face_xy[2*n_faces], NULL = no divergence source) and
- * CrsEquation::operator==(Vector) (CrsEquation.cpp:459-461).
+ * CrsEquation::operator==(Vector) (CrsEquation.cpp:309-311).
  * bc_value[n_faces] holds phi on FIXED boundary faces (may be NULL when no
  * face is FIXED).  ptr_kind says where the arrays live. */
 int pg_assemble_laplacian(pg_eqn *e, const double *gamma_face,
@@ -168,7 +174,7 @@ int pg_assemble_laplacian(pg_eqn *e, const double *gamma_face,
 int pg_eqn_device_values(const pg_eqn *e, double **vals, double **rhs);
 
 /* Copy the assembled CSR + rhs_ (the equation's own right-hand side; the
- * solver receives -rhs_, FiniteVolumeEquation.tpp:179) to host buffers.
+ * solver receives -rhs_, FiniteVolumeEquation.tpp:73) to host buffers.
  * row_ptr[n+1], col_ind[nnz], vals[nnz], rhs[n]; any may be NULL. */
 int pg_eqn_export(const pg_eqn *e, int32_t *row_ptr, int32_t *col_ind,
                   double *vals, double *rhs);
@@ -202,7 +208,7 @@ int pg_interpolate_faces(const pg_mesh *m, const double *cell_vals,
 /* Face coefficient timeStep / rho_f with rho_f = rho1 + clamp(gamma_f,0,1)
  * (rho2 - rho1) and gamma_f the distance-weighted face interpolation of the
  * cell volume fraction (FractionalStepMultiphase.cpp:175-185,
- * FiniteVolumeField.tpp:130-162, ScalarFiniteVolumeField.cpp:75-86).
+ * FiniteVolumeField.tpp:130-162, ScalarFiniteVolumeField.cpp:68-81).
  * Boundary faces take the owner cell's value (normal-gradient gamma).
  * gamma_cell[n_cells] in, coeff_face[n_faces] out. */
 int pg_face_dt_over_rho(const pg_mesh *m, const double *gamma_cell,
@@ -263,16 +269,18 @@ int pg_mpnn_load(pg_mpnn *net, const char *path);
  * device).  No counterpart in the reference.  All pointers are device
  * pointers: phi_cell[n_cells], phi_face[n_faces] in, grad_cell[2*n_cells]
  * out.  The face-gradient scratch is a static 16 MiB device array, so meshes
- * are limited to 1,048,576 faces (PG_BAD_ARG beyond).  The first call on a
- * device looks the array up (make it before any stream capture); calls
- * share the array, and calls that overlap on the GPU race on it. */
+ * are limited to 1,048,576 faces (PG_BAD_ARG beyond).  One device: the
+ * current device must be the mesh's, and the three pointers device memory
+ * on it (PG_BAD_ARG otherwise).  The first call looks the array up (make it
+ * before any stream capture); calls share the array, and calls that overlap
+ * on the GPU race on it. */
 int pg_gradient_noalloc(const pg_mesh *m, const double *phi_cell,
                         const double *phi_face, double *grad_cell);
 
 /* ------------------------------------------------------------------------
  * Sparse solver.  Replaces the SparseMatrixSolver plugin
  * (src/Math/SparseMatrixSolver.h:11-62) as driven by
- * FiniteVolumeEquation<T>::solve (FiniteVolumeEquation.tpp:171-192), with
+ * FiniteVolumeEquation<T>::solve (FiniteVolumeEquation.tpp:64-86), with
  * the semantics of the Belos BiCGStab + Ifpack2 right preconditioner backend
  * (TrilinosBelosSparseMatrixSolver.cpp:18-99, TrilinosSparseMatrixSolver.cpp
  * :23-112).
@@ -308,6 +316,13 @@ typedef struct {
                          built beside it, for the next solve (time loops,
                          where the coarse matrix changes little from step
                          to step; the first solve behaves as -1) */
+  int krylov;         /* PG_KRYLOV_*: the Krylov method (BiCGStab default) */
+  int ilu_fill;       /* level of fill k of the ILU blocks, Ifpack2 RILUK
+                         "fact: iluk level-of-fill" (key iluFill,
+                         TrilinosBelosSparseMatrixSolver.cpp:70): 0 = ILU(0) */
+  int krylov_dim;     /* PG_KRYLOV_GMRES: Krylov vectors per restart cycle
+                         (Belos "Num Blocks"); 0 = 300, Belos' default */
+  int reserved_i;     /* ignored */
   double reserved_d;  /* ignored */
 } pg_solver_cfg;
 

@@ -219,8 +219,8 @@ extern "C" void or_dt_over_rho_faces(const or_mesh *m, const double *gf,
 }
 
 // ---------------------------------------------------------------------------
-// CrsEquation semantics (CrsEquation.cpp:159-164 ctor with nnz=5 placeholder
-// slots per row, :263-281 addCoeff).  Each row keeps its slots in a vector;
+// CrsEquation semantics (CrsEquation.cpp:9-14 ctor with nnz=5 placeholder
+// slots per row, :113-131 addCoeff).  Each row keeps its slots in a vector;
 // an addCoeff that finds no free slot appends at the end of the row, which
 // is where the reference inserts (colInd_.insert at rowPtr_[row+1]).
 struct or_eqn {
@@ -290,7 +290,7 @@ static or_eqn *laplacian_rows(const or_mesh *m, const double *gamma_face,
 
   if (u_face_xy) {
     // src::div(u) (Source.cpp:5-21), then operator==(Vector) -> rhs_ -= divU
-    // (CrsEquation.cpp:432-435,459-461)
+    // (CrsEquation.cpp:282-285,309-311)
     for (int32_t c = 0; c < (int32_t)n; ++c) {
       if (mask && !mask[c]) continue;
       const V2 pc = m->centroid[c];

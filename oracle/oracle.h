@@ -59,14 +59,15 @@ void or_mesh_links(const or_mesh *m, int64_t *link_ptr, int32_t *link_face,
 void or_interpolate_faces(const or_mesh *m, const double *cell_vals,
                           double *face_vals);
 /* dt / rho_f with rho_f = rho1 + clamp(gamma_f,0,1)*(rho2-rho1)
- * (FractionalStepMultiphase.cpp:175-185, ScalarFiniteVolumeField.cpp:75-86) */
+ * (FractionalStepMultiphase.cpp:175-185, ScalarFiniteVolumeField.cpp:68-81) */
 void or_dt_over_rho_faces(const or_mesh *m, const double *gamma_face,
                           double rho1, double rho2, double dt, double *out);
 
 /* ---- assembly ---- */
 /* fv::laplacian(gamma, phi) (Laplacian.h:49-83 scalar gamma, :132-167 face
  * field gamma) == src::div(u) (Source.cpp:5-25) with CrsEquation semantics
- * (CrsEquation.cpp:159-164,263-281,432-435,459-461).
+ * (CrsEquation.cpp:9-14 ctor, :113-131 addCoeff, :282-285,309-311
+ * operator==(Vector)).
  * gamma_face NULL -> scalar gamma overload.  u_face_xy NULL -> no div term.
  * bc_type/bc_value indexed by face id (only boundary faces are read). */
 or_eqn *or_laplacian(const or_mesh *m, const double *gamma_face,

@@ -27,6 +27,7 @@ FIXED, NORMAL_GRADIENT, SYMMETRY = 0, 1, 2
 GAMMA_SCALAR, GAMMA_FACE = 0, 1
 PREC_NONE, PREC_JACOBI, PREC_ILU0 = 0, 1, 2
 FP64, MIXED = 0, 1
+KRYLOV_BICGSTAB, KRYLOV_TFQMR, KRYLOV_GMRES = 0, 1, 2
 
 STATUS_NAMES = {0: "converged", 1: "max_iters", 2: "breakdown",
                 3: "non_finite", 4: "bad_arg", 5: "timeout", 6: "cuda_error"}
@@ -45,6 +46,8 @@ class SolverCfg(ctypes.Structure):
                 ("precond", ctypes.c_int), ("subdomain_rows", ctypes.c_int),
                 ("precision", ctypes.c_int), ("mixed_sweep", ctypes.c_int),
                 ("coarse", ctypes.c_int), ("coarse_warm", ctypes.c_int),
+                ("krylov", ctypes.c_int), ("ilu_fill", ctypes.c_int),
+                ("krylov_dim", ctypes.c_int), ("reserved_i", ctypes.c_int),
                 ("reserved_d", ctypes.c_double)]
 
 

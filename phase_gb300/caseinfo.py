@@ -122,17 +122,23 @@ def read_info(path: str) -> Node:
 
 
 # --------------------------------------------------------------- solver
-_PRECOND = {"ilu0": 2, "riluk": 2, "iluk": 2, "ilut": 2, "schwarz": 2,
-            "jacobi": 1, "diagonal": 1, "relaxation": 1, "none": 0}
+_KRYLOV = {"BICGSTAB": 0, "TFQMR": 1, "GMRES": 2}
 
 
 def solver_options(tree: Node, equation: str = "pEqn") -> dict:
     """Keyword arguments for SparseMatrixSolver from
-    ``LinearAlgebra.<equation>``: tolerance, maxIters, preconditioner
-    (ilu0 | jacobi | none, or the Ifpack2 names of the Trilinos backend:
-    RILUK/ILUT/Schwarz -> ILU(0) blocks, diagonal/relaxation -> Jacobi),
-    subdomainRows, coarseSpace, coarseWarmIters, precision (fp64 | mixed),
-    mixedSweep.  Absent keys keep the solver's defaults."""
+    ``LinearAlgebra.<equation>``, read as the Belos backend reads them
+    (src/Math/TrilinosBelosSparseMatrixSolver.cpp:44-86): tolerance,
+    maxIters, solver (BICGSTAB | TFQMR | GMRES), innerPreconditioner
+    (RILUK, or RELAXATION / DIAGONAL: point Jacobi), iluFill (the RILUK
+    level of fill), schwarzIters (1), schwarzCombineMode (ADD),
+    schwarzOverlap (0).  ``preconditioner`` is ignored as the reference
+    ignores it without an ifpackParamFile (always Schwarz), except this
+    library's own values none and jacobi.  Own keys: numBlocks (GMRES
+    restart length), subdomainRows, coarseSpace, coarseWarmIters, precision
+    (fp64 | mixed), mixedSweep.  Absent keys keep the solver's defaults; a
+    value the library does not build raises ValueError (no silent
+    substitution)."""
     sec = tree.child("LinearAlgebra")
     sec = sec.child(equation) if sec is not None else None
     if sec is None:
@@ -142,12 +148,39 @@ def solver_options(tree: Node, equation: str = "pEqn") -> dict:
         out["tolerance"] = float(sec.get("tolerance"))
     if sec.get("maxIters") is not None:
         out["max_iters"] = int(sec.get("maxIters"))
-    pre = sec.get("preconditioner")
-    if pre is not None:
-        key = pre.strip().lower()
-        if key not in _PRECOND:
-            raise ValueError(f"unknown preconditioner {pre!r}")
-        out["precond"] = _PRECOND[key]
+    for key in ("belosParamFile", "ifpackParamFile"):
+        if (sec.get(key) or "").strip():
+            raise ValueError(f"{key}: Teuchos XML parameter lists are not "
+                             "read; give the keys directly")
+    solver = (sec.get("solver") or "BICGSTAB").strip().upper()
+    if solver not in _KRYLOV:
+        raise ValueError(f"solver {solver!r} is not built "
+                         f"({', '.join(_KRYLOV)} are)")
+    out["krylov"] = _KRYLOV[solver]
+    if sec.get("numBlocks") is not None:
+        out["krylov_dim"] = int(sec.get("numBlocks"))
+    pre = (sec.get("preconditioner") or "schwarz").strip().lower()
+    inner = (sec.get("innerPreconditioner") or "RILUK").strip().upper()
+    if pre == "none":
+        out["precond"] = 0
+    elif pre == "jacobi" or inner in ("RELAXATION", "DIAGONAL"):
+        out["precond"] = 1  # Schwarz over point-Jacobi blocks = point Jacobi
+    elif inner == "RILUK":
+        out["precond"] = 2
+    else:
+        raise ValueError(f"innerPreconditioner {inner!r} is not built "
+                         "(RILUK with iluFill, RELAXATION, DIAGONAL are)")
+    if sec.get("iluFill") is not None:
+        fill = float(sec.get("iluFill"))
+        if fill < 0 or fill != int(fill):
+            raise ValueError("iluFill must be a non-negative whole level")
+        out["ilu_fill"] = int(fill)
+    if int(sec.get("schwarzIters") or 1) != 1:
+        raise ValueError("schwarzIters other than 1 is not built")
+    if (sec.get("schwarzCombineMode") or "ADD").strip().upper() != "ADD":
+        raise ValueError("schwarzCombineMode other than ADD is not built")
+    if int(sec.get("schwarzOverlap") or 0) != 0:
+        raise ValueError("schwarzOverlap other than 0 is not built")
     if sec.get("subdomainRows") is not None:
         out["subdomain_rows"] = int(sec.get("subdomainRows"))
     if sec.get("coarseSpace") is not None:

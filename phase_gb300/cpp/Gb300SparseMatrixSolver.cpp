@@ -1,6 +1,7 @@
 #include "Gb300SparseMatrixSolver.h"
 
 #include <algorithm>
+#include <cctype>
 #include <cstdio>
 #include <string>
 
@@ -17,13 +18,14 @@ void Gb300SparseMatrixSolver::check(int rc, const char *method) const {
 Gb300SparseMatrixSolver::Gb300SparseMatrixSolver() {
   pg_solver_default_cfg(&cfg_);
   cfg_.coarse = 2;  // as setup() without a coarseSpace key
-  recreate();
 }
 
 Gb300SparseMatrixSolver::~Gb300SparseMatrixSolver() {
   if (solver_) pg_solver_destroy(solver_);
 }
 
+// The library solver is created at the first setRank after construction or
+// setup, so a configuration is checked before any device work.
 void Gb300SparseMatrixSolver::recreate() {
   if (solver_) pg_solver_destroy(solver_);
   solver_ = nullptr;
@@ -35,6 +37,7 @@ SparseMatrixSolver::Type Gb300SparseMatrixSolver::type() const {
 }
 
 void Gb300SparseMatrixSolver::setRank(int rank) {
+  if (!solver_) recreate();
   rank_ = rank;
   check(pg_solver_set_rank(solver_, rank), "setRank");
   if (rank > 0 && xy_.size() == 2 * (size_t)rank)
@@ -43,7 +46,7 @@ void Gb300SparseMatrixSolver::setRank(int rank) {
 
 void Gb300SparseMatrixSolver::setRowCoordinates(const std::vector<Scalar> &xy) {
   xy_ = xy;
-  if (rank_ > 0 && xy_.size() == 2 * (size_t)rank_)
+  if (solver_ && rank_ > 0 && xy_.size() == 2 * (size_t)rank_)
     check(pg_solver_set_row_coords(solver_, xy_.data()), "setRowCoordinates");
 }
 
@@ -116,23 +119,83 @@ Scalar Gb300SparseMatrixSolver::solve() {
 
 Scalar Gb300SparseMatrixSolver::x(Index idx) const { return x_[idx]; }
 
+namespace {
+
+std::string upper(std::string s) {
+  for (auto &c : s) c = (char)std::toupper((unsigned char)c);
+  return s;
+}
+
+[[noreturn]] void unsupported(const std::string &what) {
+  throw Exception("Gb300SparseMatrixSolver", "setup", what);
+}
+
+}  // namespace
+
+// The keys of TrilinosBelosSparseMatrixSolver::setup
+// (src/Math/TrilinosBelosSparseMatrixSolver.cpp:44-86) with their defaults,
+// plus this backend's own.  A value the backend does not build throws
+// instead of being replaced by another method.
 void Gb300SparseMatrixSolver::setup(const boost::property_tree::ptree &p) {
+  pg_solver_default_cfg(&cfg_);
   cfg_.tolerance = p.get<Scalar>("tolerance", 1e-8);
   cfg_.max_iters = p.get<int>("maxIters", 500);
-  const std::string pre = p.get<std::string>("preconditioner", "ilu0");
-  cfg_.precond = pre == "none" ? PG_PREC_NONE
-                 : pre == "jacobi" || pre == "diagonal" ? PG_PREC_JACOBI
-                                                        : PG_PREC_ILU0;
+  if (!p.get<std::string>("belosParamFile", "").empty() ||
+      !p.get<std::string>("ifpackParamFile", "").empty())
+    unsupported("belosParamFile/ifpackParamFile (Teuchos XML parameter "
+                "lists) are not read by lib gb300; give the keys directly.");
+  const std::string solver = upper(p.get<std::string>("solver", "BICGSTAB"));
+  if (solver == "BICGSTAB")
+    cfg_.krylov = PG_KRYLOV_BICGSTAB;
+  else if (solver == "TFQMR")
+    cfg_.krylov = PG_KRYLOV_TFQMR;
+  else if (solver == "GMRES")
+    cfg_.krylov = PG_KRYLOV_GMRES;
+  else
+    unsupported("solver \"" + solver + "\" is not built (BICGSTAB, TFQMR, "
+                "GMRES are).");
+  cfg_.krylov_dim = p.get<int>("numBlocks", 0);
+  // Without ifpackParamFile the reference always builds Ifpack2 "schwarz"
+  // whatever "preconditioner" says (:63-67); "none" and "jacobi" are this
+  // backend's own values.
+  const std::string pre = upper(p.get<std::string>("preconditioner", "schwarz"));
+  const std::string inner =
+      upper(p.get<std::string>("innerPreconditioner", "RILUK"));
+  if (pre == "NONE") {
+    cfg_.precond = PG_PREC_NONE;
+  } else if (pre == "JACOBI" || inner == "RELAXATION" || inner == "DIAGONAL") {
+    // Schwarz over point-Jacobi blocks is point Jacobi (one sweep, no damping)
+    cfg_.precond = PG_PREC_JACOBI;
+  } else if (inner == "RILUK") {
+    cfg_.precond = PG_PREC_ILU0;
+  } else {
+    unsupported("innerPreconditioner \"" + inner + "\" is not built "
+                "(RILUK with iluFill k, RELAXATION and DIAGONAL are).");
+  }
+  const double fill = p.get<Scalar>("iluFill", 0.);
+  if (!(fill >= 0.) || fill != (double)(int)fill)
+    unsupported("iluFill must be a non-negative whole level of fill.");
+  cfg_.ilu_fill = (int)fill;
+  if (p.get<int>("schwarzIters", 1) != 1)
+    unsupported("schwarzIters other than 1 is not built.");
+  if (upper(p.get<std::string>("schwarzCombineMode", "ADD")) != "ADD")
+    unsupported("schwarzCombineMode other than ADD is not built.");
+  if (p.get<int>("schwarzOverlap", 0) != 0)
+    unsupported("schwarzOverlap other than 0 is not built.");
   cfg_.subdomain_rows = p.get<int>("subdomainRows", 0);
-  cfg_.precision =
-      p.get<std::string>("precision", "fp64") == "mixed" ? PG_MIXED : PG_FP64;
+  const std::string prec = upper(p.get<std::string>("precision", "fp64"));
+  if (prec != "FP64" && prec != "MIXED")
+    unsupported("precision must be fp64 or mixed.");
+  cfg_.precision = prec == "MIXED" ? PG_MIXED : PG_FP64;
   cfg_.mixed_sweep = p.get<int>("mixedSweep", 0);
   // two-level by default: the plugin is selected for speed, and the
   // deflated coarse correction cuts pressure solves 20-30x in iterations;
   // coarseSpace 0 gives the one-level Schwarz of Ifpack2
   cfg_.coarse = p.get<int>("coarseSpace", 2);
   cfg_.coarse_warm = p.get<int>("coarseWarmIters", -1);
-  recreate();
+  if (solver_) pg_solver_destroy(solver_);
+  solver_ = nullptr;  // created with this configuration at the next setRank
+  rank_ = 0;
 }
 
 int Gb300SparseMatrixSolver::nIters() const { return stats_.iters; }

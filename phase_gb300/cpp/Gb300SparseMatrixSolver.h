@@ -25,11 +25,17 @@ class Gb300SparseMatrixSolver : public SparseMatrixSolver {
   void setRhs(const Vector &rhs) override;
   Scalar solve() override;
   Scalar x(Index idx) const override;
-  // keys: tolerance (1e-8), maxIters (500), preconditioner
-  // (ilu0 | jacobi | none), subdomainRows (0 = default, -1 = one subdomain),
-  // precision (fp64 | mixed), mixedSweep (0 | 1 | 2), coarseSpace (2
-  // default: deflated two-level Schwarz; 1 additive; 0 one-level, as
-  // Ifpack2), coarseWarmIters (-1 default)
+  // keys of the Belos backend: tolerance (1e-8), maxIters (500), solver
+  // (BICGSTAB | TFQMR | GMRES), innerPreconditioner (RILUK | RELAXATION |
+  // DIAGONAL), iluFill (level of fill, 0), schwarzIters (1),
+  // schwarzCombineMode (ADD), schwarzOverlap (0); preconditioner is
+  // ignored as the reference does (always Schwarz) except this backend's
+  // own values none and jacobi.  Own keys: numBlocks (GMRES restart length,
+  // 300), subdomainRows (0 = default, -1 = one subdomain), precision (fp64
+  // | mixed), mixedSweep (0 | 1 | 2), coarseSpace (2 default: deflated
+  // two-level Schwarz; 1 additive; 0 one-level, as Ifpack2),
+  // coarseWarmIters (-1 default).  Other values of the reference's keys,
+  // and belosParamFile / ifpackParamFile, throw Exception.
   void setup(const boost::property_tree::ptree &parameters) override;
   // Optional geometry hint (no SparseMatrixSolver counterpart): a point per
   // row, xy[2 * rank] interleaved (the cell centroids), so the Schwarz

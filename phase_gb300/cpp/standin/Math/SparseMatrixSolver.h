@@ -1,7 +1,7 @@
 // Stand-in for Phase's src/Math/SparseMatrixSolver.h (:11-62): the same
 // virtual interface, plus a GB300 enumerator that a Phase build adds next to
-// EIGEN/TRILINOS_* (see INTEGRATION.md).  Inside Phase the real header is
-// used.
+// EIGEN/TRILINOS_* when it registers this backend.  Inside Phase the real
+// header is used.
 #pragma once
 #include <string>
 #include <tuple>

@@ -149,8 +149,8 @@ int build_host_mesh(const double *nodes_xy, int64_t n_nodes,
 
 // ---------------------------------------------------------------- pattern
 // The pattern CrsEquation holds after fv::laplacian: each row starts with 5
-// placeholder slots (CrsEquation.cpp:159-164) that addCoeff fills in order of
-// first appearance of a column, appending past the fifth (:263-281).  The
+// placeholder slots (CrsEquation.cpp:9-14) that addCoeff fills in order of
+// first appearance of a column, appending past the fifth (:113-131).  The
 // scalar-gamma overload adds (cell, nb) before (cell, cell) for every
 // interior link (Laplacian.h:55-58); the face-gamma overload adds the
 // diagonal first (:139-142); FIXED boundary links add the diagonal

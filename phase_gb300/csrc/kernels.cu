@@ -750,10 +750,11 @@ void launch_gradient(int n_cells, int nf, const int32_t *fl,
                                                      cy, phi, phi_face,
                                                      grad_face);
   count_launches(1);
-  if (grad_cell)
+  if (grad_cell) {
     k_grad_cells<<<blocks_for(n_cells, 256), 256, 0, st>>>(
         n_cells, link_ptr, link_face, fnx, fny, grad_face, grad_cell);
     count_launches(1);
+  }
 }
 
 void launch_permute_values(int nnz, const int32_t *psrc, const double *src,

@@ -866,6 +866,10 @@ extern "C" void pg_solver_default_cfg(pg_solver_cfg *cfg) {
   cfg->mixed_sweep = 0;
   cfg->coarse = 0;
   cfg->coarse_warm = -1;
+  cfg->krylov = PG_KRYLOV_BICGSTAB;
+  cfg->ilu_fill = 0;
+  cfg->krylov_dim = 0;
+  cfg->reserved_i = 0;
   cfg->reserved_d = 0.;
 }
 
@@ -884,6 +888,11 @@ extern "C" int pg_solver_create(const pg_solver_cfg *cfg, pg_solver **out) {
                "pg_solver_create: bad mixed_sweep");
   PG_CHECK_ARG(c.coarse >= 0 && c.coarse <= 2, "pg_solver_create: bad coarse");
   PG_CHECK_ARG(c.coarse_warm >= -2, "pg_solver_create: bad coarse_warm");
+  PG_CHECK_ARG(c.krylov == PG_KRYLOV_BICGSTAB,
+               "pg_solver_create: only BiCGStab is built");
+  PG_CHECK_ARG(c.ilu_fill == 0,
+               "pg_solver_create: only ILU(0) blocks are built (ilu_fill 0)");
+  PG_CHECK_ARG(c.krylov_dim >= 0, "pg_solver_create: bad krylov_dim");
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0 || !stream()) {
     set_error("no CUDA device available: libphase_gb300 has no CPU path");
@@ -1044,7 +1053,7 @@ extern "C" int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e) {
   if (rj) return rj;
   launch_permute_values((int)s->a.nnz, s->psrc.p, e->vals.p, s->pvals.p,
                         (int)s->a.dup_dst.size(), s->dup_dst.p, s->dup_src.p, st);
-  // the solver receives -rhs_ (FiniteVolumeEquation.tpp:179)
+  // the solver receives -rhs_ (FiniteVolumeEquation.tpp:73)
   launch_permute_vec((int)s->a.n, s->perm.p, e->rhs.p, -1.0, s->b.p, st);
   PG_CUDA(cudaGetLastError());
   s->have_vals = true;

@@ -97,13 +97,42 @@ def test_parse_info_rejects_malformed(bad):
 def test_solver_options():
     t = caseinfo.parse_info(CASE)
     assert caseinfo.solver_options(t, "pEqn") == dict(
-        tolerance=1e-8, max_iters=500, precond=2, coarse=1, coarse_warm=0,
-        precision=1)
-    # the reference's Trilinos keys map onto the same options
+        tolerance=1e-8, max_iters=500, krylov=0, precond=2, coarse=1,
+        coarse_warm=0, precision=1)
+    # "preconditioner diagonal" is ignored as the Belos backend ignores it
+    # without an ifpackParamFile (TrilinosBelosSparseMatrixSolver.cpp:63-67):
+    # Schwarz over RILUK blocks
     assert caseinfo.solver_options(t, "uEqn") == dict(
-        tolerance=1e-10, max_iters=100, precond=1)
+        tolerance=1e-10, max_iters=100, krylov=0, precond=2)
     with pytest.raises(KeyError):
         caseinfo.solver_options(t, "nope")
+
+
+def _opts(body):
+    return caseinfo.solver_options(
+        caseinfo.parse_info("LinearAlgebra\n{\n pEqn\n {\n" + body +
+                            "\n }\n}\n"), "pEqn")
+
+
+def test_solver_options_follow_the_belos_keys():
+    assert _opts("solver TFQMR")["krylov"] == 1
+    assert _opts("solver gmres\nnumBlocks 40") == dict(krylov=2, krylov_dim=40,
+                                                       precond=2)
+    assert _opts("innerPreconditioner RELAXATION")["precond"] == 1
+    assert _opts("iluFill 1")["ilu_fill"] == 1
+    assert _opts("preconditioner none")["precond"] == 0
+
+
+@pytest.mark.parametrize("body", [
+    "solver CG", "innerPreconditioner ILUT", "innerPreconditioner CHEBYSHEV",
+    "iluFill 0.5", "schwarzOverlap 1", "schwarzCombineMode ZERO",
+    "schwarzIters 2", "belosParamFile belos.xml", "ifpackParamFile p.xml",
+    "precision fp16"])
+def test_unbuilt_solver_options_raise(body):
+    """A value the library does not build raises instead of being replaced
+    by another method."""
+    with pytest.raises(ValueError):
+        _opts(body)
 
 
 def test_boundaries_give_the_rising_bubble_bcs(oracle):

@@ -232,7 +232,7 @@ def test_ilu_apply_matches_oracle(pg, oracle, precision, mesh):
 
 def test_solver_accepts_crsequation_slots(case, pg, oracle):
     """set() receives CrsEquation's arrays with -1 placeholders
-    (FiniteVolumeEquation.tpp:178)."""
+    (FiniteVolumeEquation.tpp:72)."""
     om = case["om"]
     rng = np.random.default_rng(5)
     f = om.faces()
