@@ -145,10 +145,12 @@ int pg_correct_velocity(const pg_mesh *m, double dt, const double *rho_cell,
  * PG_BC_NORMAL_GRADIENT with value ib_ref, solid rows the identity.  The
  * IB rows are built once on the host (they depend on geometry only) and
  * the device assembly (pg_assemble_laplacian) fills the fluid rows.  The
- * sum is CrsEquation::operator+ (CrsEquation.cpp:185-229), which drops
- * exact zeros; here a fluid entry that assembles to exactly 0 keeps its
- * slot.  Fails with PG_BAD_ARG when an image point's nearest node does not
- * have four cells or a stencil matrix is singular. */
+ * sum is CrsEquation::operator+ (CrsEquation.cpp:185-229), which leaves out
+ * entries that are exactly zero: the device matrix keeps their slots (with
+ * value 0, the same operator), and pg_eqn_export drops them, so the
+ * exported CSR is CrsEquation's.  Fails with PG_BAD_ARG when an image
+ * point's nearest node does not have four cells or a stencil matrix is
+ * singular. */
 int pg_eqn_create_gcib(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
                        int n_circles, const double *circles, int ib_bc,
                        double ib_ref, pg_eqn **out);
@@ -175,7 +177,10 @@ int pg_eqn_device_values(const pg_eqn *e, double **vals, double **rhs);
 
 /* Copy the assembled CSR + rhs_ (the equation's own right-hand side; the
  * solver receives -rhs_, FiniteVolumeEquation.tpp:73) to host buffers.
- * row_ptr[n+1], col_ind[nnz], vals[nnz], rhs[n]; any may be NULL. */
+ * row_ptr[n+1], col_ind[nnz], vals[nnz], rhs[n] with nnz from
+ * pg_eqn_sizes; any may be NULL.  A ghost-cell IB equation exports the
+ * entries of its last assembly that are not exactly zero (CrsEquation's
+ * operator+), row_ptr[n] of them. */
 int pg_eqn_export(const pg_eqn *e, int32_t *row_ptr, int32_t *col_ind,
                   double *vals, double *rhs);
 

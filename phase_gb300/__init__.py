@@ -348,7 +348,8 @@ class Equation:
         rhs = np.empty(self.n)
         _check(lib().pg_eqn_export(self._h, _ptr(rp), _ptr(ci), _ptr(v),
                                    _ptr(rhs)))
-        return rp, ci, v, rhs
+        # a ghost-cell IB equation leaves out exact zeros (row_ptr[n] entries)
+        return rp, ci[:rp[-1]].copy(), v[:rp[-1]].copy(), rhs
 
 
 class MomentumEquation:

@@ -422,6 +422,30 @@ extern "C" int pg_eqn_device_values(const pg_eqn *e, double **vals,
 extern "C" int pg_eqn_export(const pg_eqn *e, int32_t *row_ptr,
                              int32_t *col_ind, double *vals, double *rhs) {
   PG_CHECK_ARG(e, "pg_eqn_export: NULL equation");
+  if (e->has_base && (row_ptr || col_ind || vals)) {
+    // A ghost-cell IB equation is CrsEquation::operator+ of the Laplacian and
+    // the IB rows (CrsEquation.cpp:185-229), which leaves out every entry of
+    // either operand that is exactly zero.  The device matrix keeps those
+    // slots (the same operator); the exported CSR drops them.
+    const int64_t n = e->p.n, nnz = e->p.nnz;
+    std::vector<double> hv(nnz);
+    PG_CUDA(copy_out(hv.data(), e->vals.p, nnz * sizeof(double), PG_HOST));
+    PG_CUDA(cudaStreamSynchronize(stream()));
+    int64_t k = 0;
+    if (row_ptr) row_ptr[0] = 0;
+    for (int64_t r = 0; r < n; ++r) {
+      for (int32_t j = e->p.row_ptr[r]; j < e->p.row_ptr[r + 1]; ++j) {
+        if (hv[j] == 0.) continue;
+        if (col_ind) col_ind[k] = e->p.col_ind[j];
+        if (vals) vals[k] = hv[j];
+        ++k;
+      }
+      if (row_ptr) row_ptr[r + 1] = (int32_t)k;
+    }
+    row_ptr = nullptr;
+    col_ind = nullptr;
+    vals = nullptr;
+  }
   if (row_ptr) std::copy(e->p.row_ptr.begin(), e->p.row_ptr.end(), row_ptr);
   if (col_ind) std::copy(e->p.col_ind.begin(), e->p.col_ind.end(), col_ind);
   if (vals) PG_CUDA(copy_out(vals, e->vals.p, e->p.nnz * sizeof(double), PG_HOST));

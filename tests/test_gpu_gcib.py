@@ -68,3 +68,43 @@ def test_gcib_solve_matches_oracle(pg, oracle, precision):
     assert st["status"] == 0
     x = s.x()
     assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-8
+
+
+def test_gcib_exact_zeros_are_dropped_as_crsequation_does(pg, oracle):
+    """CrsEquation::operator+ (CrsEquation.cpp:185-229) leaves out entries
+    that are exactly zero.  With gamma = 0 on a fifth of the interior faces
+    the Laplacian's coefficients there are exactly 0: the exported CSR drops
+    them as the oracle's CrsEquation merge does (pattern identical), while
+    a plain pressure equation (operator==(Vector), no merge) keeps them."""
+    L, H, nx, ny = 6.0, 3.0, 60, 30
+    nodes, cptr, cind = meshes.rectilinear(nx, ny, L, H)
+    m = pg.Mesh(nodes, cptr, cind)
+    om = oracle.OracleMesh(nodes, cptr, cind)
+    f = om.faces()
+    patch = meshes.rect_patch_of_faces(f["fx"], f["fy"], f["rcell"], L, H)
+    bc = np.ones(om.n_faces, np.int32)
+    bc[patch == 1] = 0
+    rng = np.random.default_rng(8)
+    gamma = rng.uniform(0.5, 2.0, om.n_faces)
+    zero = (f["rcell"] >= 0) & (rng.random(om.n_faces) < 0.2)
+    gamma[zero] = 0.0
+    u = rng.standard_normal((om.n_faces, 2))
+    bv = np.zeros(om.n_faces)
+    circle = (2.0, 1.5, 0.5)
+    eqn = pg.Equation(m, pg.GAMMA_FACE, bc, ib_circles=[circle], ib_bc=1)
+    eqn.assemble(gamma_face=gamma, bc_value=bv, u_face=u)
+    rpo, cio, vo, rhso, clso = om.gcib_laplacian(gamma, bc, bv, u, [circle],
+                                                 ib_bc=1)
+    rp, ci, v, rhs = eqn.export()
+    assert len(ci) < eqn.nnz  # entries were dropped
+    assert not np.any(vo == 0.0)
+    assert np.array_equal(rp, rpo) and np.array_equal(ci, cio)
+    rows = np.repeat(np.arange(len(rp) - 1), np.diff(rp))
+    scale = np.add.reduceat(np.abs(vo), rpo[:-1])[rows]
+    assert np.all(np.abs(v - vo) <= 1e-11 * scale)
+    # the plain equation keeps the zero-valued slots, as CrsEquation does
+    plain = pg.fv.laplacian(gamma, m, bc, bv, u)
+    rpp, cip, vp, _ = plain.export()
+    rpq, ciq, vq, _ = om.laplacian(gamma, bc, bv, u)
+    assert np.array_equal(rpp, rpq) and np.array_equal(cip, ciq)
+    assert np.count_nonzero(vp == 0.0) == np.count_nonzero(vq == 0.0) > 0
