@@ -250,6 +250,16 @@ def slots_layout(rp, ci, v):
     return srp, sci, sv
 
 
+def in_subdomain_nnz(eqn, part):
+    """Entries whose row and column lie in the same Schwarz subdomain (the
+    entries of the ILU(0) factor)."""
+    import numpy as np
+    rp, ci, _, _ = eqn.export()
+    rows = np.repeat(np.arange(len(rp) - 1, dtype=np.int64), np.diff(rp))
+    keep = ci >= 0
+    return int(np.count_nonzero(part[rows[keep]] == part[ci[keep]]))
+
+
 def az_nnz(eqn, part):
     """Nonzeros of A Z, Z the subdomain indicator vectors: per row, the
     number of distinct subdomains among its columns."""
@@ -268,9 +278,15 @@ def kernel_roofline(pg, solver, n, nnz, dd, eqn=None, coarse=0):
     pointers; ILU(0) factor values + 2-byte columns
     (off-diagonal entries of A bound the factor's) + 1/u_ii; 8-byte vector
     entries in both precisions."""
+    import numpy as np
     prof = solver.profile(reps=50)
+    part, K = solver.partition()
+    off_in = in_subdomain_nnz(eqn, part) - n  # off-diagonal factor entries
+    form = solver.sweep_form()
     b_spmv = 12 * nnz + 4 * (n + 1) + 3 * 8 * n          # A, x, rhat in; v out
-    b_prec = 10 * (nnz - n) + 8 * n + 5 * 8 * n          # LU, dinv, r p v in, p z out
+    # factor weights (8 B; the stream form adds a 2-byte column each, the
+    # line form's columns are implicit), 1/u_ii, r p v in, p z out
+    b_prec = (8 if form == 1 else 10) * off_in + 8 * n + 5 * 8 * n
     b_upd = 9 * 8 * n                                    # x r ph sh s t rh in; x r out
     sfx = "_dd" if dd else ""
     ms_of = {"spmv": prof["spmv" + sfx], "ilu_apply": prof["precond" + sfx],
@@ -279,7 +295,6 @@ def kernel_roofline(pg, solver, n, nnz, dd, eqn=None, coarse=0):
               "update": ms_of["update"]}
     bytes_of = {"spmv": b_spmv, "ilu_apply": b_prec, "update": b_upd}
     if prof["coarse"] > 0:
-        part, K = solver.partition()
         ms_of["coarse"] = prof["coarse"]
         shares["coarse"] = 2 * prof["coarse"]
         if coarse == 2:
@@ -295,6 +310,7 @@ def kernel_roofline(pg, solver, n, nnz, dd, eqn=None, coarse=0):
     peak, peak_kind = measured_peaks()
     achieved = bytes_of[dom] / (ms_of[dom] * 1e-3) / 1e9
     return {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
+            "sweep_form": {1: "line", 0: "stream"}.get(form, "none"),
             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
             "frac": round(achieved / peak, 4),
             "algorithmic_bytes": bytes_of[dom],
@@ -830,12 +846,7 @@ def run_single(args):
     a_nnz = int(eqn.nnz)
     roofline = kernel_roofline(pg, solver, n, a_nnz, dd=prec == pg.MIXED,
                                eqn=eqn, coarse=args.coarse)
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    roofline["traffic"] = None
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            roofline["traffic"] = json.load(f).get(
-                f"{roofline['kernel']}_{args.precision}")
+    roofline["traffic"] = None  # needs a profiler: see the ncu summaries
     iters = max(1, stats[-1]["iters"])
 
     # e2e through the reference-facing call sequence with host buffers

@@ -437,6 +437,14 @@ int pg_batch_tuning(const pg_batch *b, int *block, int *rows_per_thread,
 /* Number of kernels the library has launched since it was loaded. */
 uint64_t pg_kernel_launches(void);
 
+/* The form of the ILU(0) sweep the solver runs on its current analysis: 1
+ * the line form (every Schwarz subdomain a rectangular block of a structured
+ * grid: one grid line per lane, levels carried by warp shuffles, no column
+ * indices read), 0 the stream form (level blobs with 2-byte columns), -1 no
+ * ILU(0) sweep (another preconditioner, or nothing analysed).
+ * (Inspection; no reference counterpart.) */
+int pg_solver_sweep_form(const pg_solver *s);
+
 /* Subdomain id of every row of the last analysed pattern (host, part[n]);
  * returns the number of subdomains in *n_parts. */
 int pg_solver_partition(const pg_solver *s, int32_t *part, int *n_parts);

@@ -92,6 +92,7 @@ PROTOTYPES = {
     "pg_face_dt_over_rho": (_I, [_P, _P, _D, _D, _D, _P, _I]),
     "pg_gradient": (_I, [_P, _P, _P, _P, _P, _I]),
     "pg_gradient_noalloc": (_I, [_P, _P, _P, _P]),
+    "pg_solver_sweep_form": (_I, [_P]),
     "pg_solver_default_cfg": (None, [ctypes.POINTER(SolverCfg)]),
     "pg_solver_create": (_I, [ctypes.POINTER(SolverCfg), ctypes.POINTER(_P)]),
     "pg_solver_destroy": (_I, [_P]),
@@ -507,6 +508,10 @@ class SparseMatrixSolver:
         out = np.empty((k.value, k.value), np.float32)
         _check(lib().pg_solver_coarse_inverse(self._h, _ptr(out), ctypes.byref(k)))
         return out
+
+    def sweep_form(self) -> int:
+        """1 line form, 0 stream form, -1 no ILU(0) sweep."""
+        return int(lib().pg_solver_sweep_form(self._h))
 
     def apply_precond(self, r):
         """z = M^-1 r with the solver's preconditioner (float-float sweeps

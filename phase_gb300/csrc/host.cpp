@@ -4,6 +4,7 @@
 // All of it runs once per mesh / per pattern, never per solve.
 // Built with -ffp-contract=off so geometry rounds as the reference's does.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -317,6 +318,108 @@ struct Bisector {
 
 }  // namespace
 
+// Grid coordinates of a subdomain that is a rectangular block of a
+// structured grid with a 5-point pattern: every in-subdomain neighbour of a
+// row is one level before or after it and is the row's neighbour along one
+// grid axis, and the block is full (W x H rows).  Coordinates are built level
+// by level: the level-0 row is the corner (0, 0); of the two level-1 rows the
+// one with the smaller index is (1, 0); a row with two earlier neighbours
+// (i-1, j) and (i, j-1) is (i, j); a row with one earlier neighbour extends
+// the edge that neighbour lies on.  Lines run along the shorter side
+// (gline = the line, gpos = the position along it).  Returns the number of
+// lines, or 0 when the subdomain is not such a block.
+static int grid_block(const std::vector<int32_t> &rows, int s,
+               const std::vector<int32_t> &level,
+               const std::vector<int64_t> &ap, const std::vector<int32_t> &aj,
+               const std::vector<int32_t> &part, std::vector<int32_t> &gline,
+               std::vector<int32_t> &gpos) {
+  const int64_t nr = (int64_t)rows.size();
+  if (nr < 2 || nr > 65535) return 0;
+  int32_t nlev = 0;
+  for (int32_t r : rows) nlev = std::max(nlev, level[r] + 1);
+  if (nlev < 2) return 0;
+  std::vector<std::vector<int32_t>> by_level(nlev);
+  for (int32_t r : rows) by_level[level[r]].push_back(r);  // index order
+  if (by_level[0].size() != 1 || by_level[1].empty() || by_level[1].size() > 2)
+    return 0;
+  std::vector<int32_t> ci(nr), cj(nr);
+  auto slot = [&](int32_t r) {  // position of r in rows
+    return std::lower_bound(rows.begin(), rows.end(), r) - rows.begin();
+  };
+  ci[slot(by_level[0][0])] = 0;
+  cj[slot(by_level[0][0])] = 0;
+  int32_t W = 1, H = 1;
+  for (int32_t l = 1; l < nlev; ++l) {
+    for (size_t q = 0; q < by_level[l].size(); ++q) {
+      const int32_t r = by_level[l][q];
+      int32_t lnb[2], nlnb = 0;
+      for (int64_t k = ap[r]; k < ap[r + 1]; ++k) {
+        const int32_t c = aj[k];
+        if (part[c] != s) continue;
+        if (level[c] == l - 1) {
+          if (nlnb == 2) return 0;
+          lnb[nlnb++] = c;
+        } else if (level[c] != l + 1) {
+          return 0;
+        }
+      }
+      int32_t i, j;
+      if (nlnb == 2) {
+        const int64_t p = slot(lnb[0]), qq = slot(lnb[1]);
+        i = std::max(ci[p], ci[qq]);
+        j = std::max(cj[p], cj[qq]);
+        const bool ok = (ci[p] == i - 1 && cj[p] == j && ci[qq] == i && cj[qq] == j - 1) ||
+                        (ci[qq] == i - 1 && cj[qq] == j && ci[p] == i && cj[p] == j - 1);
+        if (!ok) return 0;
+      } else if (nlnb == 1) {
+        const int64_t p = slot(lnb[0]);
+        if (l == 1) {
+          i = q == 0 ? 1 : 0;
+          j = q == 0 ? 0 : 1;
+        } else if (cj[p] == 0 && ci[p] > 0) {
+          i = ci[p] + 1;
+          j = 0;
+        } else if (ci[p] == 0 && cj[p] > 0) {
+          i = 0;
+          j = cj[p] + 1;
+        } else {
+          return 0;
+        }
+      } else {
+        return 0;
+      }
+      const int64_t sr = slot(r);
+      ci[sr] = i;
+      cj[sr] = j;
+      W = std::max(W, i + 1);
+      H = std::max(H, j + 1);
+    }
+  }
+  if ((int64_t)W * H != nr) return 0;
+  std::vector<int32_t> grid((size_t)W * H, -1);
+  for (int64_t k = 0; k < nr; ++k) {
+    int32_t &g = grid[(size_t)cj[k] * W + ci[k]];
+    if (g >= 0) return 0;
+    g = (int32_t)k;
+  }
+  // every in-subdomain neighbour is a grid neighbour
+  for (int64_t k = 0; k < nr; ++k) {
+    const int32_t r = rows[k];
+    for (int64_t e = ap[r]; e < ap[r + 1]; ++e) {
+      const int32_t c = aj[e];
+      if (part[c] != s) continue;
+      const int64_t p = slot(c);
+      if (std::abs(ci[p] - ci[k]) + std::abs(cj[p] - cj[k]) != 1) return 0;
+    }
+  }
+  const bool swap = W > H;
+  for (int64_t k = 0; k < nr; ++k) {
+    gline[rows[k]] = swap ? cj[k] : ci[k];
+    gpos[rows[k]] = swap ? ci[k] : cj[k];
+  }
+  return swap ? H : W;
+}
+
 int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
             int subdomain_rows, Analysis &a,
             const std::vector<int64_t> *sys_rows, const double *cx,
@@ -460,8 +563,23 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
 
   // 4. levels inside each subdomain (rows visited in increasing original
   //    index; a row's level is one more than its deepest earlier neighbour
-  //    in the same subdomain) and the level-ordered permutation
+  //    in the same subdomain) and the level-ordered permutation.  A
+  //    subdomain that is a rectangular block of a structured grid gets grid
+  //    coordinates (line, position on the line) and each of its levels is
+  //    ordered by line, for the line form of the sweep (kernels.cuh
+  //    LineMeta); rows of one level are independent, so the order inside a
+  //    level leaves the ILU(0) unchanged.
   std::vector<int32_t> level(n, 0);
+  std::vector<int32_t> gline, gpos;  // grid coordinates of line-form rows
+  std::vector<int32_t> sub_lines(a.n_sub, 0);  // lines per block, 0 = none
+  const bool want_line = !sys_rows && [] {
+    const char *e = std::getenv("PG_LINE");
+    return !(e && e[0] == '0');
+  }();
+  if (want_line) {
+    gline.assign(n, -1);
+    gpos.assign(n, -1);
+  }
   a.perm.resize(n);
   a.sub_ptr.assign(a.n_sub + 1, 0);
   a.sub_lvl.assign(a.n_sub + 1, 0);
@@ -481,9 +599,17 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       level[i] = lv;
       nl = std::max(nl, lv + 1);
     }
-    std::stable_sort(rows.begin(), rows.end(), [&](int32_t x, int32_t y) {
-      return level[x] < level[y];
-    });
+    if (want_line)
+      sub_lines[s] = grid_block(rows, s, level, ap, aj, a.part, gline, gpos);
+    if (sub_lines[s] > 0)
+      std::stable_sort(rows.begin(), rows.end(), [&](int32_t x, int32_t y) {
+        return level[x] < level[y] ||
+               (level[x] == level[y] && gline[x] < gline[y]);
+      });
+    else
+      std::stable_sort(rows.begin(), rows.end(), [&](int32_t x, int32_t y) {
+        return level[x] < level[y];
+      });
     a.sub_ptr[s] = (int32_t)out;
     for (size_t k = 0; k < rows.size(); ++k) {
       if (k == 0 || level[rows[k]] != level[rows[k - 1]])
@@ -867,6 +993,175 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
     s += G;
   }
   a.n_grp = (int)a.smeta64.size();
+
+  // 8b. line form (kernels.cuh LineMeta) when every subdomain is a grid
+  //     block: consecutive blocks of at most 16 lines are paired into one
+  //     warp, other blocks of at most 32 lines take a warp each.  pack_l*
+  //     map every weight of a line record to its slot in the FP64 factor
+  //     records.
+  a.lmeta.clear();
+  a.lrec.clear();
+  a.lpack_src.clear();
+  a.lpack_dst.clear();
+  a.lsmem = 0;
+  bool all_lines = want_line && a.n_sub > 0;
+  for (int s = 0; s < a.n_sub && all_lines; ++s)
+    all_lines = sub_lines[s] > 0 && sub_lines[s] <= 32 &&
+                a.meta64[s].nlev <= 255;
+  if (all_lines) {
+    constexpr int64_t kLinePiece = 8192;
+    const int64_t vs = 8;
+    int64_t loff = 0;
+    for (int s = 0; s < a.n_sub;) {
+      const bool pair = s + 1 < a.n_sub && sub_lines[s] <= 16 &&
+                        sub_lines[s + 1] <= 16 &&
+                        a.meta64[s].nr + a.meta64[s + 1].nr < 65535;
+      const int G = pair ? 2 : 1;
+      const SubMeta *mf[2] = {&a.meta64[s], pair ? &a.meta64[s + 1] : nullptr};
+      const int nr = mf[0]->nr + (pair ? mf[1]->nr : 0);
+      const int nlev = std::max(mf[0]->nlev, pair ? mf[1]->nlev : 0);
+      const int base[2] = {0, mf[0]->nr};
+      // member m's rows of level l: group-local start, count, first line
+      auto lev = [&](int l, int m, int &am, int &wm, int &lom) {
+        am = base[m];
+        wm = 0;
+        lom = 0;
+        if (m >= G || l >= mf[m]->nlev) return;
+        const int32_t *lp = a.lvl_ptr.data() + a.sub_lvl[s + m];
+        am = base[m] + (lp[l] - mf[m]->r0);
+        wm = lp[l + 1] - lp[l];
+        lom = gline[a.perm[lp[l]]];
+      };
+      auto wsum = [&](int l) {
+        int am, w0, w1, lo;
+        lev(l, 0, am, w0, lo);
+        lev(l, 1, am, w1, lo);
+        return w0 + w1;
+      };
+      auto fblob = [&](int w) { return al16(2 * vs * w); };
+      auto bblob = [&](int w) { return al16(3 * vs * w); };
+      std::vector<std::pair<int, int64_t>> fp, bp;
+      for (int l = 0; l < nlev; ++l) {
+        const int64_t sz = fblob(wsum(l));
+        if (fp.empty() || fp.back().second + sz > kLinePiece) fp.push_back({l, 0});
+        fp.back().second += sz;
+      }
+      for (int l = nlev - 1; l >= 0; --l) {
+        const int64_t sz = bblob(wsum(l));
+        if (bp.empty() || bp.back().second + sz > kLinePiece) bp.push_back({l, 0});
+        bp.back().second += sz;
+      }
+      for (auto &q : fp) q.second = std::max<int64_t>(q.second, 16);
+      for (auto &q : bp) q.second = std::max<int64_t>(q.second, 16);
+      const int np = (int)(fp.size() + bp.size());
+      const int64_t hdr = al16(8 * (int64_t)nlev + 4 * (2 + 3 * (int64_t)np));
+      int64_t total = hdr, max_piece = 16;
+      for (auto &q : fp) total += q.second, max_piece = std::max(max_piece, q.second);
+      for (auto &q : bp) total += q.second, max_piece = std::max(max_piece, q.second);
+      PG_CHECK_ARG(loff + total < ((int64_t)1 << 31), "ILU(0) line records too large");
+      a.lrec.resize(loff + total, 0);
+      uint8_t *recb = a.lrec.data() + loff;
+      for (int l = 0; l < nlev; ++l) {
+        int a0, w0, lo0, a1, w1, lo1;
+        lev(l, 0, a0, w0, lo0);
+        lev(l, 1, a1, w1, lo1);
+        uint16_t *h16 = reinterpret_cast<uint16_t *>(recb + 8 * l);
+        h16[0] = (uint16_t)a0;
+        h16[1] = (uint16_t)a1;
+        uint8_t *h8 = recb + 8 * l + 4;
+        h8[0] = (uint8_t)w0;
+        h8[1] = (uint8_t)lo0;
+        h8[2] = (uint8_t)w1;
+        h8[3] = (uint8_t)lo1;
+      }
+      int32_t *ints = reinterpret_cast<int32_t *>(recb + 8 * nlev);
+      ints[0] = (int32_t)fp.size();
+      ints[1] = (int32_t)bp.size();
+      // the weight of the grid neighbour (line + dl, pos + dp) of member m's
+      // factor row `row`: its slot in the factor record, or -1
+      auto nb_slot = [&](int m, int row, bool lower, int dl, int dp) -> int64_t {
+        const SubMeta &f = *mf[m];
+        const int fKL = f.KL, fKU = f.K - f.KL;
+        const uint16_t *fcols = reinterpret_cast<const uint16_t *>(
+            a.rec64.data() + f.rec_off + f.col_off);
+        const int32_t g = a.perm[f.r0 + row];
+        const int k0 = lower ? 0 : fKL, kn = lower ? fKL : fKU;
+        for (int k = 0; k < kn; ++k) {
+          const int64_t sl = (int64_t)(k0 + k) * f.nr + row;
+          if (fcols[sl] == kPadCol) continue;
+          const int32_t c = a.perm[f.r0 + fcols[sl]];
+          if (gline[c] == gline[g] + dl && gpos[c] == gpos[g] + dp) return sl;
+        }
+        return -1;
+      };
+      auto emit = [&](int m, int64_t byte_off, int64_t sl) {
+        if (sl < 0) return;  // weight stays 0
+        const int64_t fsrc0 = (mf[m]->rec_off + mf[m]->val_off) / 8;
+        a.lpack_src.push_back((int32_t)(fsrc0 + sl));
+        a.lpack_dst.push_back((int32_t)((loff + byte_off) / vs));
+      };
+      int64_t off = hdr;
+      auto emit_level = [&](int l, bool fwd) {
+        int am[2], wm[2], lom[2];
+        lev(l, 0, am[0], wm[0], lom[0]);
+        lev(l, 1, am[1], wm[1], lom[1]);
+        int t = 0;
+        for (int m = 0; m < 2; ++m)
+          for (int k = 0; k < wm[m]; ++k, ++t) {
+            const int row = am[m] - base[m] + k;  // member-local row
+            if (fwd) {
+              emit(m, off + vs * (2 * t), nb_slot(m, row, true, -1, 0));
+              emit(m, off + vs * (2 * t + 1), nb_slot(m, row, true, 0, -1));
+            } else {
+              emit(m, off + vs * (3 * t), nb_slot(m, row, false, 1, 0));
+              emit(m, off + vs * (3 * t + 1), nb_slot(m, row, false, 0, 1));
+              emit(m, off + vs * (3 * t + 2),
+                   (int64_t)mf[m]->K * mf[m]->nr + row);
+            }
+          }
+        off += fwd ? fblob(t) : bblob(t);
+      };
+      int tq = 0;
+      for (size_t q = 0; q < fp.size(); ++q, ++tq) {
+        const int l0 = fp[q].first;
+        const int l1 = q + 1 < fp.size() ? fp[q + 1].first : nlev;
+        ints[2 + 3 * tq] = l0;
+        ints[3 + 3 * tq] = (int32_t)off;
+        ints[4 + 3 * tq] = (int32_t)fp[q].second;
+        for (int l = l0; l < l1; ++l) emit_level(l, true);
+      }
+      for (size_t q = 0; q < bp.size(); ++q, ++tq) {
+        const int lhi = bp[q].first;
+        const int llo = q + 1 < bp.size() ? bp[q + 1].first + 1 : 0;
+        ints[2 + 3 * tq] = lhi;
+        ints[3 + 3 * tq] = (int32_t)off;
+        ints[4 + 3 * tq] = (int32_t)bp[q].second;
+        for (int l = lhi; l >= llo; --l) emit_level(l, false);
+      }
+      LineMeta lm{};
+      lm.r0 = mf[0]->r0;
+      lm.nr = nr;
+      lm.nlev = nlev;
+      lm.rec_off = (int32_t)loff;
+      lm.hdr_bytes = (int32_t)hdr;
+      lm.max_piece = (int32_t)max_piece;
+      lm.p0_off = ints[3];
+      lm.p0_bytes = ints[4];
+      if (np > 1) {
+        lm.p1_off = ints[6];
+        lm.p1_bytes = ints[7];
+      }
+      lm.sub0 = s;
+      lm.nsub = G;
+      lm.nr0 = mf[0]->nr;
+      lm.lanes = pair ? 16 : 32;
+      a.lmeta.push_back(lm);
+      loff += total;
+      a.lsmem = std::max(a.lsmem, (size_t)hdr + 2 * (size_t)max_piece +
+                                      (size_t)al16(vs * (int64_t)(nr + 1)));
+      s += G;
+    }
+  }
 
   // 9. step stream for the float-float sweep of the mixed-precision solver
   //    (kernels.cuh StepMeta), when no row has more than 3 L or 3 U

@@ -253,6 +253,10 @@ struct ArithF64 {
   __device__ static V add_y(V z, const void *y, int sub) {
     return z + static_cast<const double *>(y)[sub];
   }
+  __device__ static V load_y(const void *y, int sub) {
+    return static_cast<const double *>(y)[sub];
+  }
+  __device__ static V add(V a, V b) { return a + b; }
   // subdomain sums for the coarse correction
   using Sum = double;
   __device__ static Sum sum_init() { return 0.; }
@@ -289,6 +293,10 @@ struct ArithDD {
   __device__ static V add_y(V z, const void *y, int sub) {
     return dd_add(z, static_cast<const float2 *>(y)[sub]);
   }
+  __device__ static V load_y(const void *y, int sub) {
+    return static_cast<const float2 *>(y)[sub];
+  }
+  __device__ static V add(V a, V b) { return dd_add(a, b); }
   using Sum = DdAcc;
   __device__ static Sum sum_init() { return dd_acc(make_float2(0.f, 0.f)); }
   __device__ static void sum_add(Sum &a, V x) { dd_acc_add(a, x); }
@@ -540,8 +548,317 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
     }
   }
   if constexpr (MODE == 3) {
+    const MT y0 = AR::load_y(def_y, m.sub0);
+    const MT y1 = m.nsub > 1 ? AR::load_y(def_y, m.sub0 + 1) : y0;
     for (int i = lane; i < nr; i += 32)
-      z[m.r0 + i] = AR::add_y(zs[i], def_y, i < m.nr0 ? m.sub0 : m.sub0 + 1);
+      z[m.r0 + i] = AR::add(zs[i], i < m.nr0 ? y0 : y1);
+  } else {
+    for (int i = lane; i < nr; i += 32) z[m.r0 + i] = zs[i];
+  }
+}
+
+// Line-form sweeps (kernels.cuh LineMeta) of a group of structured blocks.
+// Lane i of a member walks grid line i, one row per level: on level l it
+// owns row (i, l - i).  Forward, z(i, j) = x(i, j) - f0 z(i-1, j) - f1
+// z(i, j-1): z(i-1, j) is lane i-1's result of level l-1 (a shuffle) and
+// z(i, j-1) the lane's own (`carry`); backward, z(i, j) = (z(i, j) - b1
+// z(i, j+1) - b0 z(i+1, j)) / u_ii with z(i+1, j) from lane i+1.  The chain
+// of a level is a shuffle and two multiply-adds; the weights and the
+// row's input are read from shared memory one level ahead.  The products
+// are subtracted in the order of the row's factor slots (increasing
+// column), as the stream form does, so both give the same results.  Pieces
+// of the record are double-buffered through shared memory by TMA as in
+// k_ilu0_apply_stream; input staging, subdomain sums and the output (with
+// y_s in mode 3) are the same too.
+template <class AR>
+__device__ __forceinline__ typename AR::V shfl_up_v(typename AR::V x, int w);
+template <>
+__device__ __forceinline__ double shfl_up_v<ArithF64>(double x, int w) {
+  return __shfl_up_sync(0xffffffffu, x, 1, w);
+}
+template <>
+__device__ __forceinline__ float2 shfl_up_v<ArithDD>(float2 x, int w) {
+  return make_float2(__shfl_up_sync(0xffffffffu, x.x, 1, w),
+                     __shfl_up_sync(0xffffffffu, x.y, 1, w));
+}
+template <class AR>
+__device__ __forceinline__ typename AR::V shfl_down_v(typename AR::V x, int w);
+template <>
+__device__ __forceinline__ double shfl_down_v<ArithF64>(double x, int w) {
+  return __shfl_down_sync(0xffffffffu, x, 1, w);
+}
+template <>
+__device__ __forceinline__ float2 shfl_down_v<ArithDD>(float2 x, int w) {
+  return make_float2(__shfl_down_sync(0xffffffffu, x.x, 1, w),
+                     __shfl_down_sync(0xffffffffu, x.y, 1, w));
+}
+
+// a level's members: start row, rows, first line
+struct LineLevel {
+  int a, w, lo, t0;  // this lane's member: rows a .. a+w-1 on lines lo ..;
+                     // its entries start at t0 in the level blob
+  int wsum;          // entries of the level (both members)
+};
+__device__ __forceinline__ LineLevel line_level(const uint2 *L, int l,
+                                                int mem) {
+  const uint2 x = L[l];
+  const int w0 = (int)(x.y & 0xFFu), w1 = (int)((x.y >> 16) & 0xFFu);
+  LineLevel g;
+  g.a = mem ? (int)(x.x >> 16) : (int)(x.x & 0xFFFFu);
+  g.w = mem ? w1 : w0;
+  g.lo = mem ? (int)(x.y >> 24) : (int)((x.y >> 8) & 0xFFu);
+  g.t0 = mem ? w0 : 0;
+  g.wsum = w0 + w1;
+  return g;
+}
+
+template <class AR, int MODE>
+__global__ void __launch_bounds__(32)
+k_ilu0_apply_line(const LineMeta *__restrict__ meta,
+                  const uint8_t *__restrict__ rec,
+                  const typename AR::V *__restrict__ r,
+                  typename AR::V *__restrict__ pv,
+                  const typename AR::V *__restrict__ v,
+                  typename AR::V *__restrict__ z,
+                  const KScalars *__restrict__ sc, int *__restrict__ err,
+                  float2 *__restrict__ csum, const void *__restrict__ def_y) {
+  using MT = typename AR::V;
+  pdl_wait();
+  if (sc && sc->done) return;
+  extern __shared__ __align__(128) uint8_t smem[];
+  __shared__ __align__(8) uint64_t bar[4];
+  const LineMeta m = meta[blockIdx.x];
+  const int lane = threadIdx.x;
+  const int nr = m.nr, nlev = m.nlev;
+  uint8_t *hdr = smem;
+  uint8_t *const buf0 = smem + m.hdr_bytes;
+  MT *zs = reinterpret_cast<MT *>(smem + m.hdr_bytes + 2 * m.max_piece);
+  const uint8_t *g = rec + m.rec_off;
+  // modes 0 and 3 read one input vector: one bulk copy straight into z,
+  // in flight with the factor pieces (16-byte aligned ranges only)
+  const bool tma_in =
+      (MODE == 0 || MODE == 3) && (nr & 1) == 0 &&
+      (reinterpret_cast<uintptr_t>(pv + m.r0) & 15u) == 0;
+  if (lane == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init(&bar[2], 1);
+    mbar_init(&bar[3], 1);
+    mbar_expect_tx(&bar[2], (uint32_t)m.hdr_bytes);
+    bulk_load(hdr, g, (uint32_t)m.hdr_bytes, &bar[2]);
+    if (tma_in) {
+      mbar_expect_tx(&bar[3], (uint32_t)(nr * sizeof(MT)));
+      bulk_load(zs, pv + m.r0, (uint32_t)(nr * sizeof(MT)), &bar[3]);
+    }
+    mbar_expect_tx(&bar[0], (uint32_t)m.p0_bytes);
+    bulk_load(buf0, g + m.p0_off, (uint32_t)m.p0_bytes, &bar[0]);
+    if (m.p1_bytes > 0) {
+      mbar_expect_tx(&bar[1], (uint32_t)m.p1_bytes);
+      bulk_load(buf0 + m.max_piece, g + m.p1_off, (uint32_t)m.p1_bytes,
+                &bar[1]);
+    }
+  }
+  if (tma_in) {
+    __syncwarp();  // lane 0 has initialised the barriers
+    if (!mbar_wait_bounded(&bar[3], err)) {
+      mbar_wait_bounded(&bar[2], nullptr, 0u);
+      mbar_wait_bounded(&bar[0], nullptr, 0u);
+      if (m.p1_bytes > 0) mbar_wait_bounded(&bar[1], nullptr, 0u);
+      return;
+    }
+    if (csum) {  // the same lane-strided order as the register staging
+      typename AR::Sum part0 = AR::sum_init(), part1 = AR::sum_init();
+      for (int i = lane; i < nr; i += 32)
+        AR::sum_add(i < m.nr0 ? part0 : part1, zs[i]);
+      const float2 t0 = AR::sum_warp(part0);
+      if (lane == 0) csum[m.sub0] = t0;
+      if (m.nsub > 1) {
+        const float2 t1 = AR::sum_warp(part1);
+        if (lane == 0) csum[m.sub0 + 1] = t1;
+      }
+    }
+  } else {
+    constexpr int U = 4;
+    const MT zero = AR::zero();
+    typename AR::Sum part0 = AR::sum_init(), part1 = AR::sum_init();
+    for (int i0 = lane; i0 < nr; i0 += 32 * U) {
+      MT ri[U], pi[U], vi[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + 32 * u;
+        ri[u] = pi[u] = vi[u] = zero;
+        if (i < nr) {
+          if (MODE == 1 || MODE == 2) ri[u] = r[m.r0 + i], vi[u] = v[m.r0 + i];
+          if (MODE != 2) pi[u] = pv[m.r0 + i];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + 32 * u;
+        if (i < nr) {
+          MT val;
+          if constexpr (MODE == 3)
+            val = pi[u];
+          else
+            val = AR::combine(MODE, ri[u], pi[u], vi[u], sc);
+          if (MODE == 1 || MODE == 2) pv[m.r0 + i] = val;
+          zs[i] = val;
+          if (csum) AR::sum_add(i < m.nr0 ? part0 : part1, val);
+        }
+      }
+    }
+    if (csum) {
+      const float2 t0 = AR::sum_warp(part0);
+      if (lane == 0) csum[m.sub0] = t0;
+      if (m.nsub > 1) {
+        const float2 t1 = AR::sum_warp(part1);
+        if (lane == 0) csum[m.sub0 + 1] = t1;
+      }
+    }
+  }
+  __syncwarp();
+  if (!mbar_wait_bounded(&bar[2], err)) {
+    mbar_wait_bounded(&bar[0], nullptr, 0u);
+    if (m.p1_bytes > 0) mbar_wait_bounded(&bar[1], nullptr, 0u);
+    return;
+  }
+  const uint2 *L = reinterpret_cast<const uint2 *>(hdr);
+  const int32_t *ints = reinterpret_cast<const int32_t *>(hdr + 8 * nlev);
+  const int nF = ints[0], nB = ints[1], P = nF + nB;
+  const int32_t *tab = ints + 2;
+  constexpr int vs = (int)sizeof(MT);
+  const int width = m.lanes;  // shuffle segment: 16 (pair) or 32
+  const int mem = width == 16 ? lane >> 4 : 0;
+  const int li = width == 16 ? lane & 15 : lane;
+  MT carry = AR::zero();
+  uint32_t phases = 0u;
+  for (int j = 0; j < P; ++j) {
+    const int sb = j & 1;
+    if (!mbar_wait_bounded(&bar[sb], err, (phases >> sb) & 1u)) {
+      if (j + 1 < P)
+        mbar_wait_bounded(&bar[sb ^ 1], nullptr, (phases >> (sb ^ 1)) & 1u);
+      return;
+    }
+    phases ^= 1u << sb;
+    const uint8_t *pc = buf0 + sb * m.max_piece;
+    if (j == nF) carry = AR::zero();  // the backward sweep starts
+    if (j < nF) {
+      const int l0 = tab[3 * j];
+      const int l1 = j + 1 < nF ? tab[3 * (j + 1)] : nlev;
+      // operands of level l0, then each level reads the next one's
+      LineLevel cl = line_level(L, l0, mem);
+      int k = li - cl.lo;
+      bool ok = (unsigned)k < (unsigned)cl.w;
+      MT f0 = AR::zero(), f1 = AR::zero(), x = AR::zero();
+      if (ok) {
+        const MT *fp = reinterpret_cast<const MT *>(pc) + 2 * (cl.t0 + k);
+        f0 = fp[0];
+        f1 = fp[1];
+        x = zs[cl.a + k];
+      }
+      for (int l = l0; l < l1; ++l) {
+        const uint8_t *pn = pc + al16(2 * vs * cl.wsum);
+        LineLevel nl{};
+        int kn = 0;
+        bool okn = false;
+        MT g0 = AR::zero(), g1 = AR::zero(), xn = AR::zero();
+        if (l + 1 < l1) {
+          nl = line_level(L, l + 1, mem);
+          kn = li - nl.lo;
+          okn = (unsigned)kn < (unsigned)nl.w;
+          if (okn) {
+            const MT *fp = reinterpret_cast<const MT *>(pn) + 2 * (nl.t0 + kn);
+            g0 = fp[0];
+            g1 = fp[1];
+            xn = zs[nl.a + kn];
+          }
+        }
+        MT left = shfl_up_v<AR>(carry, width);
+        if (li == 0) left = AR::zero();
+        MT out = AR::zero();
+        if (ok) {
+          const MT wv[2] = {f0, f1}, zv[2] = {left, carry};
+          out = AR::template row<2, false>(x, wv, zv, AR::zero());
+          zs[cl.a + k] = out;
+        }
+        carry = out;
+        cl = nl;
+        k = kn;
+        ok = okn;
+        f0 = g0;
+        f1 = g1;
+        x = xn;
+        pc = pn;
+      }
+    } else {
+      const int lhi = tab[3 * j];
+      const int llo = j + 1 < P ? tab[3 * (j + 1)] + 1 : 0;
+      LineLevel cl = line_level(L, lhi, mem);
+      int k = li - cl.lo;
+      bool ok = (unsigned)k < (unsigned)cl.w;
+      MT b0 = AR::zero(), b1 = AR::zero(), dg = AR::zero(), x = AR::zero();
+      if (ok) {
+        const MT *bp = reinterpret_cast<const MT *>(pc) + 3 * (cl.t0 + k);
+        b0 = bp[0];
+        b1 = bp[1];
+        dg = bp[2];
+        x = zs[cl.a + k];
+      }
+      for (int l = lhi; l >= llo; --l) {
+        const uint8_t *pn = pc + al16(3 * vs * cl.wsum);
+        LineLevel nl{};
+        int kn = 0;
+        bool okn = false;
+        MT c0 = AR::zero(), c1 = AR::zero(), cd = AR::zero(), xn = AR::zero();
+        if (l - 1 >= llo) {
+          nl = line_level(L, l - 1, mem);
+          kn = li - nl.lo;
+          okn = (unsigned)kn < (unsigned)nl.w;
+          if (okn) {
+            const MT *bp = reinterpret_cast<const MT *>(pn) + 3 * (nl.t0 + kn);
+            c0 = bp[0];
+            c1 = bp[1];
+            cd = bp[2];
+            xn = zs[nl.a + kn];
+          }
+        }
+        MT right = shfl_down_v<AR>(carry, width);
+        if (li == width - 1) right = AR::zero();
+        MT out = AR::zero();
+        if (ok) {
+          // U slots in increasing column: (i, j+1) (this lane's line) is
+          // on an earlier line than (i+1, j)
+          const MT wv[2] = {b1, b0}, zv[2] = {carry, right};
+          out = AR::template row<2, true>(x, wv, zv, dg);
+          zs[cl.a + k] = out;
+        }
+        carry = out;
+        cl = nl;
+        k = kn;
+        ok = okn;
+        b0 = c0;
+        b1 = c1;
+        dg = cd;
+        x = xn;
+        pc = pn;
+      }
+    }
+    // every lane has consumed its reads of this buffer before it is refilled
+    __syncwarp();
+    if (lane == 0 && j + 2 < P) {
+      fence_proxy_async();
+      mbar_expect_tx(&bar[sb], (uint32_t)tab[3 * (j + 2) + 2]);
+      bulk_load(buf0 + sb * m.max_piece, g + tab[3 * (j + 2) + 1],
+                (uint32_t)tab[3 * (j + 2) + 2], &bar[sb]);
+    }
+  }
+  __syncwarp();
+  if constexpr (MODE == 3) {
+    // y of the group's (at most two) subdomains, read once
+    const MT y0 = AR::load_y(def_y, m.sub0);
+    const MT y1 = m.nsub > 1 ? AR::load_y(def_y, m.sub0 + 1) : y0;
+    for (int i = lane; i < nr; i += 32)
+      z[m.r0 + i] = AR::add(zs[i], i < m.nr0 ? y0 : y1);
   } else {
     for (int i = lane; i < nr; i += 32) z[m.r0 + i] = zs[i];
   }
@@ -732,9 +1049,30 @@ void launch_stream(const SolverDev &d, size_t smem, const uint8_t *rec,
              d.def_y);
 }
 
+template <class AR, int MODE>
+void launch_line(const SolverDev &d, const uint8_t *rec,
+                 const typename AR::V *r, typename AR::V *pv,
+                 const typename AR::V *v, typename AR::V *z,
+                 const KScalars *sc, cudaStream_t st) {
+  static size_t attr = 0;
+  if (d.lsmem > 48 * 1024 && attr < d.lsmem) {
+    cudaFuncSetAttribute(k_ilu0_apply_line<AR, MODE>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)d.lsmem);
+    attr = d.lsmem;
+  }
+  launch_pdl(k_ilu0_apply_line<AR, MODE>, d.n_lgrp, 32, d.lsmem, st, d.lmeta,
+             rec, r, pv, v, z, sc, d.err, d.csum, d.def_y);
+  count_launches(1);
+}
+
 template <class VT, class MT, int MODE>
 void apply_mode(const SolverDev &d, const VT *r, VT *pv, const VT *v, VT *z,
                 const KScalars *sc, cudaStream_t st) {
+  if (d.n_lgrp > 0 && !d.sub_sys) {
+    launch_line<ArithF64, MODE>(d, d.lrec64, r, pv, v, z, sc, st);
+    return;
+  }
   const size_t smem = d.smem64;
   // compile-time slot counts for the common stencils: quadrilaterals (2/2,
   // any subdomain whose rows have at most 2 L and 2 U entries) and
@@ -755,6 +1093,10 @@ template <int MODE>
 void apply_mode_dd(const SolverDev &d, const float2 *r, float2 *pv,
                    const float2 *v, float2 *z, const KScalars *sc,
                    cudaStream_t st) {
+  if (d.dd_stream && d.n_lgrp > 0 && d.lrec_dds && !d.sub_sys) {
+    launch_line<ArithDD, MODE>(d, d.lrec_dds, r, pv, v, z, sc, st);
+    return;
+  }
   if (d.dd_stream) {  // level blobs, float pairs in the FP64 record layout
     const size_t smem = d.smem64;
     if (d.max_kl <= 2 && d.max_ku <= 2)
@@ -786,6 +1128,20 @@ void launch_ilu0_factor(const SolverDev &d, const double *pvals, int *bad,
                                         bad);
   count_launches(1);
   auto grid = [](int n) { return (n + 255) / 256 < 2432 ? (n + 255) / 256 : 2432; };
+  if (d.n_lpack > 0) {  // line-form records
+    k_pack_stream<double><<<grid(d.n_lpack), 256, 0, st>>>(
+        d.n_lpack, d.lpack_src, d.lpack_dst,
+        reinterpret_cast<const double *>(d.rec64),
+        reinterpret_cast<double *>(d.lrec64));
+    count_launches(1);
+    if (to_dd && d.lrec_dds) {
+      k_pack_dd<<<grid(d.n_lpack), 256, 0, st>>>(
+          d.n_lpack, d.lpack_src, d.lpack_dst,
+          reinterpret_cast<const double *>(d.rec64),
+          reinterpret_cast<float2 *>(d.lrec_dds));
+      count_launches(1);
+    }
+  }
   if (d.n_pack > 0 && d.smem64) {
     k_pack_stream<double><<<grid(d.n_pack), 256, 0, st>>>(
         d.n_pack, d.pack_src, d.pack_dst64,
@@ -812,8 +1168,12 @@ void launch_ilu0_factor(const SolverDev &d, const double *pvals, int *bad,
 bool launch_ilu0_apply_def(const SolverDev &d, const double *in, double *z,
                            const KScalars *sc, cudaStream_t st) {
   const size_t smem = d.smem64;
-  if (!smem || !d.def_y) return false;
   double *pv = const_cast<double *>(in);  // mode 3 reads it only
+  if (d.def_y && d.n_lgrp > 0 && !d.sub_sys) {
+    launch_line<ArithF64, 3>(d, d.lrec64, nullptr, pv, nullptr, z, sc, st);
+    return true;
+  }
+  if (!smem || !d.def_y) return false;
   if (d.max_kl <= 2 && d.max_ku <= 2)
     launch_stream<ArithF64, 3, 2, 2>(d, smem, d.srec64, nullptr, pv, nullptr, z, sc, st);
   else if (d.max_kl <= 3 && d.max_ku <= 3)
@@ -829,6 +1189,10 @@ bool launch_ilu0_apply_def_dd(const SolverDev &d, const float2 *in, float2 *z,
   if (!d.dd_stream || !d.def_y) return false;
   const size_t smem = d.smem64;
   float2 *pv = const_cast<float2 *>(in);  // mode 3 reads it only
+  if (d.n_lgrp > 0 && d.lrec_dds && !d.sub_sys) {
+    launch_line<ArithDD, 3>(d, d.lrec_dds, nullptr, pv, nullptr, z, sc, st);
+    return true;
+  }
   if (d.max_kl <= 2 && d.max_ku <= 2)
     launch_stream<ArithDD, 3, 2, 2>(d, smem, d.srec_dds, nullptr, pv, nullptr, z, sc, st);
   else if (d.max_kl <= 3 && d.max_ku <= 3)

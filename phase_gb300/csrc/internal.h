@@ -208,6 +208,12 @@ struct Analysis {
   std::vector<uint8_t> srec64;
   std::vector<int32_t> pack_src, pack_dst64;    // FP64 stream <- factor
   size_t ssmem64 = 0;
+  // line form of the sweep records (kernels.cuh LineMeta) when every
+  // subdomain is a structured block (empty otherwise)
+  std::vector<LineMeta> lmeta;
+  std::vector<uint8_t> lrec;
+  std::vector<int32_t> lpack_src, lpack_dst;  // line record <- factor
+  size_t lsmem = 0;
   // float-float step stream (kernels.cuh StepMeta) of the mixed solver,
   // when every row has at most 3 L and 3 U entries
   bool use_steps = false;

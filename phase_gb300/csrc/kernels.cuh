@@ -172,6 +172,33 @@ struct StreamMeta {
   int32_t sub0, nsub, nr0, pad0;
 };
 
+// Line form of a sweep group's factor, for subdomains that are rectangular
+// blocks of a structured grid (5-point rows: the L part of row (i, j) holds
+// at most (i-1, j) and (i, j-1), the U part (i+1, j) and (i, j+1), so row
+// (i, j) is on level i + j).  Lane i of a member owns grid line i and walks
+// it one row per level: the value of (i-1, j) comes from lane i-1 by a warp
+// shuffle and that of (i, j-1) is the lane's own previous row, so no level
+// waits for shared memory.  A pair group puts two blocks of at most 16
+// lines side by side (member m uses lanes 16 m .. 16 m + 15); a single
+// block may have up to 32 lines.  Each level's rows are stored in
+// increasing line order.
+//   header: per level 8 bytes {uint16 a0, a1; uint8 w0, lo0, w1, lo1}:
+//           member m's rows of level l are group-local rows a_m .. a_m+w_m-1
+//           on lines lo_m .. lo_m+w_m-1; then int32 nF, nB and the piece
+//           table int32[nF+nB][3] = {level, byte offset, bytes} as in the
+//           stream form
+//   level blob (forward):  MT f[w][2]  {weight of (i-1, j), of (i, j-1)}
+//   level blob (backward): MT b[w][3]  {weight of (i+1, j), of (i, j+1),
+//                                       1/u_ii}
+//   entry t of a level: member 0's lines first (t = i - lo0), then member
+//   1's (t = w0 + i - lo1); blobs padded to 16 bytes; w = w0 + w1; a
+//   missing neighbour has weight 0.
+struct LineMeta {
+  int32_t r0, nr, nlev, rec_off, hdr_bytes, max_piece;
+  int32_t p0_off, p0_bytes, p1_off, p1_bytes;
+  int32_t sub0, nsub, nr0, lanes;  // lanes per member: 16 (pair) or 32
+};
+
 // Step form of the factor for the float-float sweep of the mixed solver,
 // used when every row has at most 3 L and 3 U entries (quadrilateral and
 // triangle meshes).  A step is one warp-wide slice of a level (up to 32
@@ -227,6 +254,14 @@ struct SolverDev {
   // value of the row's subdomain in the sweep's arithmetic (double or
   // float pairs)
   const void *def_y;
+  // line form (every group a structured block; n_lgrp > 0): FP64 records,
+  // their float-pair copy for the mixed solver, shared memory per CTA
+  int n_lgrp;
+  const LineMeta *lmeta;
+  uint8_t *lrec64, *lrec_dds;
+  size_t lsmem;
+  const int32_t *lpack_src, *lpack_dst;
+  int n_lpack;
 };
 
 

@@ -61,6 +61,11 @@ struct pg_solver {
   DevBuf<uint8_t> srec64, srec_dd, srec_dds;
   int dd_stream = -1;  // mixed ILU sweep: -1 not chosen, 0 steps, 1 stream
   DevBuf<int32_t> pack_src, pack_dst64, pack_src_dd, pack_dst_dd;
+  // line form of the sweep records (structured blocks)
+  DevBuf<LineMeta> lmeta;
+  DevBuf<uint8_t> lrec64, lrec_dds;
+  DevBuf<int32_t> lpack_src, lpack_dst;
+  bool line_sweep = true;  // PG_LINE_SWEEP=0 at the analysis: stream kernel
   DevBuf<int> err;
   DevBuf<int32_t> raw_rp, raw_ci, st_rp, st_ci;
   std::vector<double> row_x, row_y;  // pg_solver_set_row_coords hint
@@ -228,6 +233,16 @@ struct pg_solver {
     d.sub_sys = nullptr;
     d.csum = coarse_on ? c_sum.p : nullptr;
     d.def_y = nullptr;
+    const bool line =
+        line_sweep && !a.lmeta.empty() && a.lsmem <= kMaxApplySmem;
+    d.n_lgrp = line ? (int)a.lmeta.size() : 0;
+    d.lmeta = lmeta.p;
+    d.lrec64 = lrec64.p;
+    d.lrec_dds = cfg.precision == PG_MIXED ? lrec_dds.p : nullptr;
+    d.lsmem = a.lsmem;
+    d.lpack_src = lpack_src.p;
+    d.lpack_dst = lpack_dst.p;
+    d.n_lpack = line ? (int)a.lpack_src.size() : 0;
     return d;
   }
   RedWork red() const { return RedWork{partials.p, ticket.p, red_grid}; }
@@ -298,6 +313,15 @@ int upload_analysis(pg_solver *s) {
   if (s->cfg.precision == PG_MIXED) up(s->srec_dds, a.srec64);  // static parts
   up(s->pack_src_dd, a.pack_src_dd);
   up(s->pack_dst_dd, a.pack_dst_dd);
+  {
+    const char *e = std::getenv("PG_LINE_SWEEP");
+    s->line_sweep = !(e && e[0] == '0');
+  }
+  up(s->lmeta, a.lmeta);
+  up(s->lrec64, a.lrec);
+  if (s->cfg.precision == PG_MIXED) up(s->lrec_dds, a.lrec);  // static parts
+  up(s->lpack_src, a.lpack_src);
+  up(s->lpack_dst, a.lpack_dst);
 
   if (e == cudaSuccess) e = s->err.zero(1);
   const size_t n = a.n, nnz = a.nnz;
@@ -1380,6 +1404,11 @@ extern "C" int pg_solver_apply_precond(pg_solver *s, const double *r,
     return PG_TIMEOUT;
   }
   return PG_OK;
+}
+
+extern "C" int pg_solver_sweep_form(const pg_solver *s) {
+  if (!s || !s->analysed || s->cfg.precond != PG_PREC_ILU0) return -1;
+  return s->dev().n_lgrp > 0 ? 1 : 0;
 }
 
 extern "C" int pg_solver_partition(const pg_solver *s, int32_t *part,
