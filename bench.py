@@ -77,9 +77,10 @@ def parse():
     ap.add_argument("--nx", type=int, default=1024)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--subdomain-rows", type=int, default=0)
-    ap.add_argument("--mixed-sweep", type=int, default=0, choices=[0, 1, 2],
+    ap.add_argument("--mixed-sweep", type=int, default=3, choices=[0, 1, 2, 3],
                     help="mixed ILU(0) sweep form: 0 timed choice, 1 steps, "
-                         "2 level blobs")
+                         "2 level blobs, 3 FP32-stored factor weights (line "
+                         "form of structured blocks)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--coarse", type=int, choices=(0, 1, 2), default=2,
                     help="two-level Schwarz coarse correction on the "
@@ -284,9 +285,11 @@ def kernel_roofline(pg, solver, n, nnz, dd, eqn=None, coarse=0):
     off_in = in_subdomain_nnz(eqn, part) - n  # off-diagonal factor entries
     form = solver.sweep_form()
     b_spmv = 12 * nnz + 4 * (n + 1) + 3 * 8 * n          # A, x, rhat in; v out
-    # factor weights (8 B; the stream form adds a 2-byte column each, the
-    # line form's columns are implicit), 1/u_ii, r p v in, p z out
-    b_prec = (8 if form == 1 else 10) * off_in + 8 * n + 5 * 8 * n
+    # factor weights (8 B, or 4 B for the mixed solver's FP32-stored factor;
+    # the stream form adds a 2-byte column each, the line form's columns are
+    # implicit), 1/u_ii, r p v in, p z out
+    wb = 4 if (dd and form == 1 and solver.cfg.mixed_sweep == 3) else 8
+    b_prec = (wb if form == 1 else wb + 2) * off_in + wb * n + 5 * 8 * n
     b_upd = 9 * 8 * n                                    # x r ph sh s t rh in; x r out
     sfx = "_dd" if dd else ""
     ms_of = {"spmv": prof["spmv" + sfx], "ilu_apply": prof["precond" + sfx],
@@ -311,6 +314,7 @@ def kernel_roofline(pg, solver, n, nnz, dd, eqn=None, coarse=0):
     achieved = bytes_of[dom] / (ms_of[dom] * 1e-3) / 1e9
     return {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
             "sweep_form": {1: "line", 0: "stream"}.get(form, "none"),
+            "factor_weight_bytes": wb,
             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
             "frac": round(achieved / peak, 4),
             "algorithmic_bytes": bytes_of[dom],
@@ -359,6 +363,7 @@ def run_sequence(args):
                                coarse_warm=reuse if reuse else -1)
     sm = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
                                precision=pg.MIXED,
+                               mixed_sweep=args.mixed_sweep,
                                subdomain_rows=args.subdomain_rows,
                                coarse=args.coarse,
                                coarse_warm=reuse if reuse
@@ -378,6 +383,7 @@ def run_sequence(args):
     xp_q = torch.zeros(n, dtype=torch.float64, device=dev)
     sq = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
                                precision=pg.MIXED,
+                               mixed_sweep=args.mixed_sweep,
                                subdomain_rows=args.subdomain_rows,
                                coarse=args.coarse,
                                coarse_warm=reuse if reuse else -1)
@@ -489,7 +495,7 @@ def run_sequence(args):
     if not args.no_e2e:
         e2e = e2e_learned(pg, guess, seq, net, have_w, steps, torch, dev,
                           args.coarse, reuse if reuse
-                          else args.learned_coarse_warm)
+                          else args.learned_coarse_warm, args.mixed_sweep)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -530,7 +536,8 @@ def run_sequence(args):
             "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": round(ms, 3), "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32x2 (float-float) + f64 residual",
+            "dtype": "f32x2 (float-float) + f64 residual"
+                     + (", f32 ILU factor" if args.mixed_sweep == 3 else ""),
             "data": "synthetic (seeded rising-bubble sequence, no dataset)",
             "converged": converged,
             "config": {"workload": workload_name(args.nx) + ", time steps "
@@ -540,6 +547,9 @@ def run_sequence(args):
                        f"{sm.partition()[1]} subdomains"
                        + {0: "", 1: " + additive coarse correction",
                           2: " + deflated coarse correction (A-DEF1)"}[args.coarse],
+                       "mixed_sweep": {0: "timed choice", 1: "steps",
+                                       2: "level blobs",
+                                       3: "FP32-stored factor, line form"}[args.mixed_sweep],
                        "coarse_reuse": bool(args.coarse_reuse),
                        "learned_coarse_warm": args.learned_coarse_warm,
                        "learned_weights": os.path.relpath(guess.DEFAULT_WEIGHTS, ROOT)
@@ -584,7 +594,7 @@ def run_sequence(args):
 
 
 def e2e_learned(pg, guess, seq, net, have_w, steps, torch, dev, coarse,
-                coarse_warm=0):
+                coarse_warm=0, mixed_sweep=0):
     """The learned+mixed solve through the C ABI with host buffers: the
     caller holds the step's CrsEquation (5-slot layout), its rhs and the
     previous solution on the host; they are uploaded, the network predicts
@@ -592,7 +602,7 @@ def e2e_learned(pg, guess, seq, net, have_w, steps, torch, dev, coarse,
     import numpy as np
     s2 = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
                                precision=pg.MIXED, coarse=coarse,
-                               coarse_warm=coarse_warm)
+                               coarse_warm=coarse_warm, mixed_sweep=mixed_sweep)
     # the caller's geometry hint: cell centroids cut the Schwarz subdomains
     s2.setRank(seq.n)
     s2.set_row_coords(np.stack([seq.cells["cx"], seq.cells["cy"]], axis=1))

@@ -301,7 +301,10 @@ typedef struct {
   int precision;      /* PG_FP64 | PG_MIXED */
   int mixed_sweep;    /* PG_MIXED ILU(0) sweep form: 0 = timed choice at the
                          first factorisation, 1 = warp-wide steps, 2 = level
-                         blobs */
+                         blobs, 3 = FP32-stored factor weights swept in
+                         float-float arithmetic (the line form of
+                         structured blocks; elsewhere as 0): half the factor
+                         bytes, the factors rounded to FP32 */
   int coarse;         /* PG_PREC_ILU0: 0 = one-level Schwarz (as Ifpack2);
                          two-level, with a coarse space of subdomain-constant
                          vectors Z and y = (Z^T A Z)^-1 Z^T r (at most 2048

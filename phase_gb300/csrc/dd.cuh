@@ -76,6 +76,22 @@ __device__ __forceinline__ void dd_acc_fma(DdAcc &a, float2 x, float2 y) {
   a.c = __fadd_rn(a.c, __fadd_rn(t.y, pe));
 }
 
+// a += w * y for an FP32 w (a factor weight stored in FP32)
+__device__ __forceinline__ void dd_acc_fma_f(DdAcc &a, float w, float2 y) {
+  const float p = __fmul_rn(w, y.x);
+  const float pe = __fmaf_rn(w, y.y, __fmaf_rn(w, y.x, -p));
+  const float2 t = two_sum(a.s, p);
+  a.s = t.x;
+  a.c = __fadd_rn(a.c, __fadd_rn(t.y, pe));
+}
+
+// x * d for an FP32 d
+__device__ __forceinline__ float2 dd_mul_f(float2 x, float d) {
+  const float p = __fmul_rn(x.x, d);
+  const float e = __fmaf_rn(x.y, d, __fmaf_rn(x.x, d, -p));
+  return fast_two_sum(p, e);
+}
+
 // a += x
 __device__ __forceinline__ void dd_acc_add(DdAcc &a, float2 x) {
   const float2 t = two_sum(a.s, x.x);

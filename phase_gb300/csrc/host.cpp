@@ -9,6 +9,7 @@
 #include <cstring>
 #include <numeric>
 #include <string>
+#include <tuple>
 
 #include "internal.h"
 
@@ -508,7 +509,9 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   } else {
     if (target < 0) target = INT32_MAX;
     Bisector bs(n, ap, aj);
-    std::vector<std::pair<int64_t, int64_t>> stack{{0, n}};
+    // ranges to cut; the flag marks a range whose cut was moved to a grid
+    // line, which may then hold up to a quarter more than the target
+    std::vector<std::tuple<int64_t, int64_t, bool>> stack{{0, n, false}};
     const bool rcb = cx && cy;
     if (sys_rows) {  // one root range per system, popped in system order
       PG_CHECK_ARG(sys_rows->size() >= 2 && sys_rows->front() == 0 &&
@@ -517,18 +520,18 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       stack.clear();
       for (size_t k = sys_rows->size() - 1; k-- > 0;)
         if ((*sys_rows)[k + 1] > (*sys_rows)[k])
-          stack.push_back({(*sys_rows)[k], (*sys_rows)[k + 1]});
+          stack.push_back({(*sys_rows)[k], (*sys_rows)[k + 1], false});
     }
     while (!stack.empty()) {
-      auto [lo, hi] = stack.back();
+      auto [lo, hi, snapped] = stack.back();
       stack.pop_back();
       const int64_t cnt = hi - lo;
-      if (cnt <= target) {
+      if (cnt <= target || (snapped && cnt <= target + target / 4)) {
         parts.push_back({lo, hi});
         continue;
       }
       const int64_t k_parts = (cnt + target - 1) / target;
-      const int64_t left = cnt * (k_parts / 2) / k_parts;
+      int64_t left = cnt * (k_parts / 2) / k_parts;
       if (rcb) {
         // coordinate bisection across the longer extent of the range's
         // cell centres (ties broken by row index)
@@ -539,10 +542,40 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
           y0 = std::min(y0, cy[r]), y1 = std::max(y1, cy[r]);
         }
         const double *c = x1 - x0 >= y1 - y0 ? cx : cy;
+        auto by_c = [c](int32_t p, int32_t q) {
+          return c[p] < c[q] || (c[p] == c[q] && p < q);
+        };
         std::nth_element(order.begin() + lo, order.begin() + lo + left,
-                         order.begin() + hi, [c](int32_t p, int32_t q) {
-                           return c[p] < c[q] || (c[p] == c[q] && p < q);
-                         });
+                         order.begin() + hi, by_c);
+        // On a structured grid the cells of one grid line share their
+        // coordinate up to rounding: move the cut to the nearer boundary of
+        // the cut cell's line, so blocks stay whole rectangles (the line
+        // form of the sweep needs them).  Unstructured centres are distinct
+        // beyond the tolerance, and their cut does not move.
+        const double tol = 1e-9 * std::max(x1 - x0, y1 - y0);
+        const double cv = c[order[lo + left]];
+        int64_t below = 0, upto = 0;
+        for (int64_t k = lo; k < hi; ++k) {
+          const double ck = c[order[k]];
+          below += ck < cv - tol;
+          upto += ck <= cv + tol;
+        }
+        int64_t cut = left;
+        if (below != left) {
+          const bool lo_ok = below > 0, hi_ok = upto < cnt;
+          if (lo_ok && (!hi_ok || left - below <= upto - left)) cut = below;
+          else if (hi_ok) cut = upto;
+        }
+        if (cut != left) {
+          if (cut == below)
+            std::partition(order.begin() + lo, order.begin() + hi,
+                           [&](int32_t r) { return c[r] < cv - tol; });
+          else
+            std::partition(order.begin() + lo, order.begin() + hi,
+                           [&](int32_t r) { return c[r] <= cv + tol; });
+        }
+        snapped = snapped || cut != left;
+        left = cut;
       } else {
         ++bs.range_stamp;
         for (int64_t k = lo; k < hi; ++k) bs.in_range[order[k]] = bs.range_stamp;
@@ -551,8 +584,8 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
         bs.bfs(far, order.data() + lo, cnt);
         std::copy(bs.queue.begin(), bs.queue.end(), order.begin() + lo);
       }
-      stack.push_back({lo + left, hi});
-      stack.push_back({lo, lo + left});
+      stack.push_back({lo + left, hi, snapped});
+      stack.push_back({lo, lo + left, snapped});
     }
   }
   a.n_sub = (int)parts.size();
@@ -1004,13 +1037,23 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   a.lpack_src.clear();
   a.lpack_dst.clear();
   a.lsmem = 0;
+  a.lmeta32.clear();
+  a.lrec32.clear();
+  a.lpack32_src.clear();
+  a.lpack32_dst.clear();
+  a.lsmem32 = 0;
   bool all_lines = want_line && a.n_sub > 0;
   for (int s = 0; s < a.n_sub && all_lines; ++s)
     all_lines = sub_lines[s] > 0 && sub_lines[s] <= 32 &&
                 a.meta64[s].nlev <= 255;
-  if (all_lines) {
-    constexpr int64_t kLinePiece = 8192;
-    const int64_t vs = 8;
+  // vs: bytes of a stored weight (8: FP64 or a float pair, 4: FP32);
+  // piece: target bytes of a piece (the FP32 records keep the whole forward
+  // and the whole backward data in one piece each, both loaded at kernel
+  // start)
+  auto build_lines = [&](int64_t vs, int64_t piece, std::vector<LineMeta> &lmeta,
+                         std::vector<uint8_t> &lrec,
+                         std::vector<int32_t> &lpack_src,
+                         std::vector<int32_t> &lpack_dst, size_t &lsmem) -> int {
     int64_t loff = 0;
     for (int s = 0; s < a.n_sub;) {
       const bool pair = s + 1 < a.n_sub && sub_lines[s] <= 16 &&
@@ -1043,12 +1086,12 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       std::vector<std::pair<int, int64_t>> fp, bp;
       for (int l = 0; l < nlev; ++l) {
         const int64_t sz = fblob(wsum(l));
-        if (fp.empty() || fp.back().second + sz > kLinePiece) fp.push_back({l, 0});
+        if (fp.empty() || fp.back().second + sz > piece) fp.push_back({l, 0});
         fp.back().second += sz;
       }
       for (int l = nlev - 1; l >= 0; --l) {
         const int64_t sz = bblob(wsum(l));
-        if (bp.empty() || bp.back().second + sz > kLinePiece) bp.push_back({l, 0});
+        if (bp.empty() || bp.back().second + sz > piece) bp.push_back({l, 0});
         bp.back().second += sz;
       }
       for (auto &q : fp) q.second = std::max<int64_t>(q.second, 16);
@@ -1059,8 +1102,8 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       for (auto &q : fp) total += q.second, max_piece = std::max(max_piece, q.second);
       for (auto &q : bp) total += q.second, max_piece = std::max(max_piece, q.second);
       PG_CHECK_ARG(loff + total < ((int64_t)1 << 31), "ILU(0) line records too large");
-      a.lrec.resize(loff + total, 0);
-      uint8_t *recb = a.lrec.data() + loff;
+      lrec.resize(loff + total, 0);
+      uint8_t *recb = lrec.data() + loff;
       for (int l = 0; l < nlev; ++l) {
         int a0, w0, lo0, a1, w1, lo1;
         lev(l, 0, a0, w0, lo0);
@@ -1097,8 +1140,8 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       auto emit = [&](int m, int64_t byte_off, int64_t sl) {
         if (sl < 0) return;  // weight stays 0
         const int64_t fsrc0 = (mf[m]->rec_off + mf[m]->val_off) / 8;
-        a.lpack_src.push_back((int32_t)(fsrc0 + sl));
-        a.lpack_dst.push_back((int32_t)((loff + byte_off) / vs));
+        lpack_src.push_back((int32_t)(fsrc0 + sl));
+        lpack_dst.push_back((int32_t)((loff + byte_off) / vs));
       };
       int64_t off = hdr;
       auto emit_level = [&](int l, bool fwd) {
@@ -1155,12 +1198,24 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       lm.nsub = G;
       lm.nr0 = mf[0]->nr;
       lm.lanes = pair ? 16 : 32;
-      a.lmeta.push_back(lm);
+      // buffer 1 follows buffer 0; with two pieces each takes its own size
+      lm.buf1 = np == 2 ? (int32_t)al16(ints[4]) : (int32_t)max_piece;
+      lm.zs_off = (int32_t)(hdr + lm.buf1 + (np == 2 ? al16(ints[7]) : max_piece));
+      lmeta.push_back(lm);
       loff += total;
-      a.lsmem = std::max(a.lsmem, (size_t)hdr + 2 * (size_t)max_piece +
-                                      (size_t)al16(vs * (int64_t)(nr + 1)));
+      lsmem = std::max(lsmem, (size_t)lm.zs_off +
+                                  (size_t)al16(8 * (int64_t)(nr + 1)));
       s += G;
     }
+    return PG_OK;
+  };
+  if (all_lines) {
+    int rc = build_lines(8, 8192, a.lmeta, a.lrec, a.lpack_src, a.lpack_dst,
+                         a.lsmem);
+    if (!rc)
+      rc = build_lines(4, (int64_t)1 << 30, a.lmeta32, a.lrec32, a.lpack32_src,
+                       a.lpack32_dst, a.lsmem32);
+    if (rc) return rc;
   }
 
   // 9. step stream for the float-float sweep of the mixed-precision solver

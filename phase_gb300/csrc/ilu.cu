@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "../../include/phase_gb300.h"
 #include "dd.cuh"
@@ -612,7 +613,26 @@ __device__ __forceinline__ LineLevel line_level(const uint2 *L, int l,
   return g;
 }
 
-template <class AR, int MODE>
+// One row of a line sweep: self - w0 x0 - w1 x1 (* d), with the weights in
+// their storage type WT (the vector arithmetic's own type, or FP32 weights
+// in float-float arithmetic).
+template <class AR, class WT, bool DIAG>
+__device__ __forceinline__ typename AR::V line_row(typename AR::V self, WT w0,
+                                                   WT w1, typename AR::V x0,
+                                                   typename AR::V x1, WT d) {
+  if constexpr (std::is_same<WT, float>::value) {
+    DdAcc acc = dd_acc(self);
+    dd_acc_fma_f(acc, -w0, x0);
+    dd_acc_fma_f(acc, -w1, x1);
+    const float2 out = dd_value(acc);
+    return DIAG ? dd_mul_f(out, d) : out;
+  } else {
+    const typename AR::V wv[2] = {w0, w1}, zv[2] = {x0, x1};
+    return AR::template row<2, DIAG>(self, wv, zv, d);
+  }
+}
+
+template <class AR, int MODE, class WT>
 __global__ void __launch_bounds__(32)
 k_ilu0_apply_line(const LineMeta *__restrict__ meta,
                   const uint8_t *__restrict__ rec,
@@ -632,7 +652,7 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
   const int nr = m.nr, nlev = m.nlev;
   uint8_t *hdr = smem;
   uint8_t *const buf0 = smem + m.hdr_bytes;
-  MT *zs = reinterpret_cast<MT *>(smem + m.hdr_bytes + 2 * m.max_piece);
+  MT *zs = reinterpret_cast<MT *>(smem + m.zs_off);
   const uint8_t *g = rec + m.rec_off;
   // modes 0 and 3 read one input vector: one bulk copy straight into z,
   // in flight with the factor pieces (16-byte aligned ranges only)
@@ -654,8 +674,7 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
     bulk_load(buf0, g + m.p0_off, (uint32_t)m.p0_bytes, &bar[0]);
     if (m.p1_bytes > 0) {
       mbar_expect_tx(&bar[1], (uint32_t)m.p1_bytes);
-      bulk_load(buf0 + m.max_piece, g + m.p1_off, (uint32_t)m.p1_bytes,
-                &bar[1]);
+      bulk_load(buf0 + m.buf1, g + m.p1_off, (uint32_t)m.p1_bytes, &bar[1]);
     }
   }
   if (tma_in) {
@@ -726,7 +745,7 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
   const int32_t *ints = reinterpret_cast<const int32_t *>(hdr + 8 * nlev);
   const int nF = ints[0], nB = ints[1], P = nF + nB;
   const int32_t *tab = ints + 2;
-  constexpr int vs = (int)sizeof(MT);
+  constexpr int vs = (int)sizeof(WT);
   const int width = m.lanes;  // shuffle segment: 16 (pair) or 32
   const int mem = width == 16 ? lane >> 4 : 0;
   const int li = width == 16 ? lane & 15 : lane;
@@ -740,7 +759,7 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
       return;
     }
     phases ^= 1u << sb;
-    const uint8_t *pc = buf0 + sb * m.max_piece;
+    const uint8_t *pc = buf0 + (sb ? m.buf1 : 0);
     if (j == nF) carry = AR::zero();  // the backward sweep starts
     if (j < nF) {
       const int l0 = tab[3 * j];
@@ -749,9 +768,10 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
       LineLevel cl = line_level(L, l0, mem);
       int k = li - cl.lo;
       bool ok = (unsigned)k < (unsigned)cl.w;
-      MT f0 = AR::zero(), f1 = AR::zero(), x = AR::zero();
+      WT f0 = WT(), f1 = WT();
+      MT x = AR::zero();
       if (ok) {
-        const MT *fp = reinterpret_cast<const MT *>(pc) + 2 * (cl.t0 + k);
+        const WT *fp = reinterpret_cast<const WT *>(pc) + 2 * (cl.t0 + k);
         f0 = fp[0];
         f1 = fp[1];
         x = zs[cl.a + k];
@@ -761,13 +781,14 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
         LineLevel nl{};
         int kn = 0;
         bool okn = false;
-        MT g0 = AR::zero(), g1 = AR::zero(), xn = AR::zero();
+        WT g0 = WT(), g1 = WT();
+        MT xn = AR::zero();
         if (l + 1 < l1) {
           nl = line_level(L, l + 1, mem);
           kn = li - nl.lo;
           okn = (unsigned)kn < (unsigned)nl.w;
           if (okn) {
-            const MT *fp = reinterpret_cast<const MT *>(pn) + 2 * (nl.t0 + kn);
+            const WT *fp = reinterpret_cast<const WT *>(pn) + 2 * (nl.t0 + kn);
             g0 = fp[0];
             g1 = fp[1];
             xn = zs[nl.a + kn];
@@ -777,8 +798,7 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
         if (li == 0) left = AR::zero();
         MT out = AR::zero();
         if (ok) {
-          const MT wv[2] = {f0, f1}, zv[2] = {left, carry};
-          out = AR::template row<2, false>(x, wv, zv, AR::zero());
+          out = line_row<AR, WT, false>(x, f0, f1, left, carry, WT());
           zs[cl.a + k] = out;
         }
         carry = out;
@@ -796,9 +816,10 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
       LineLevel cl = line_level(L, lhi, mem);
       int k = li - cl.lo;
       bool ok = (unsigned)k < (unsigned)cl.w;
-      MT b0 = AR::zero(), b1 = AR::zero(), dg = AR::zero(), x = AR::zero();
+      WT b0 = WT(), b1 = WT(), dg = WT();
+      MT x = AR::zero();
       if (ok) {
-        const MT *bp = reinterpret_cast<const MT *>(pc) + 3 * (cl.t0 + k);
+        const WT *bp = reinterpret_cast<const WT *>(pc) + 3 * (cl.t0 + k);
         b0 = bp[0];
         b1 = bp[1];
         dg = bp[2];
@@ -809,13 +830,14 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
         LineLevel nl{};
         int kn = 0;
         bool okn = false;
-        MT c0 = AR::zero(), c1 = AR::zero(), cd = AR::zero(), xn = AR::zero();
+        WT c0 = WT(), c1 = WT(), cd = WT();
+        MT xn = AR::zero();
         if (l - 1 >= llo) {
           nl = line_level(L, l - 1, mem);
           kn = li - nl.lo;
           okn = (unsigned)kn < (unsigned)nl.w;
           if (okn) {
-            const MT *bp = reinterpret_cast<const MT *>(pn) + 3 * (nl.t0 + kn);
+            const WT *bp = reinterpret_cast<const WT *>(pn) + 3 * (nl.t0 + kn);
             c0 = bp[0];
             c1 = bp[1];
             cd = bp[2];
@@ -828,8 +850,7 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
         if (ok) {
           // U slots in increasing column: (i, j+1) (this lane's line) is
           // on an earlier line than (i+1, j)
-          const MT wv[2] = {b1, b0}, zv[2] = {carry, right};
-          out = AR::template row<2, true>(x, wv, zv, dg);
+          out = line_row<AR, WT, true>(x, b1, b0, carry, right, dg);
           zs[cl.a + k] = out;
         }
         carry = out;
@@ -848,7 +869,7 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
     if (lane == 0 && j + 2 < P) {
       fence_proxy_async();
       mbar_expect_tx(&bar[sb], (uint32_t)tab[3 * (j + 2) + 2]);
-      bulk_load(buf0 + sb * m.max_piece, g + tab[3 * (j + 2) + 1],
+      bulk_load(buf0 + (sb ? m.buf1 : 0), g + tab[3 * (j + 2) + 1],
                 (uint32_t)tab[3 * (j + 2) + 2], &bar[sb]);
     }
   }
@@ -1049,21 +1070,40 @@ void launch_stream(const SolverDev &d, size_t smem, const uint8_t *rec,
              d.def_y);
 }
 
+template <class AR, int MODE, class WT>
+void launch_line_w(int n_grp, const LineMeta *meta, size_t smem,
+                   const SolverDev &d, const uint8_t *rec,
+                   const typename AR::V *r, typename AR::V *pv,
+                   const typename AR::V *v, typename AR::V *z,
+                   const KScalars *sc, cudaStream_t st) {
+  static size_t attr = 0;
+  if (smem > 48 * 1024 && attr < smem) {
+    cudaFuncSetAttribute(k_ilu0_apply_line<AR, MODE, WT>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    attr = smem;
+  }
+  launch_pdl(k_ilu0_apply_line<AR, MODE, WT>, n_grp, 32, smem, st, meta, rec,
+             r, pv, v, z, sc, d.err, d.csum, d.def_y);
+  count_launches(1);
+}
+
+// the line form: FP64 records for FP64, float-pair copies for float-float,
+// or the FP32-weight records when the mixed solver uses them (n_lgrp32)
 template <class AR, int MODE>
 void launch_line(const SolverDev &d, const uint8_t *rec,
                  const typename AR::V *r, typename AR::V *pv,
                  const typename AR::V *v, typename AR::V *z,
                  const KScalars *sc, cudaStream_t st) {
-  static size_t attr = 0;
-  if (d.lsmem > 48 * 1024 && attr < d.lsmem) {
-    cudaFuncSetAttribute(k_ilu0_apply_line<AR, MODE>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)d.lsmem);
-    attr = d.lsmem;
+  if constexpr (std::is_same<AR, ArithDD>::value) {
+    if (d.n_lgrp32 > 0) {
+      launch_line_w<AR, MODE, float>(d.n_lgrp32, d.lmeta32, d.lsmem32, d, d.lrec32,
+                                     r, pv, v, z, sc, st);
+      return;
+    }
   }
-  launch_pdl(k_ilu0_apply_line<AR, MODE>, d.n_lgrp, 32, d.lsmem, st, d.lmeta,
-             rec, r, pv, v, z, sc, d.err, d.csum, d.def_y);
-  count_launches(1);
+  launch_line_w<AR, MODE, typename AR::V>(d.n_lgrp, d.lmeta, d.lsmem, d, rec,
+                                          r, pv, v, z, sc, st);
 }
 
 template <class VT, class MT, int MODE>
@@ -1093,7 +1133,8 @@ template <int MODE>
 void apply_mode_dd(const SolverDev &d, const float2 *r, float2 *pv,
                    const float2 *v, float2 *z, const KScalars *sc,
                    cudaStream_t st) {
-  if (d.dd_stream && d.n_lgrp > 0 && d.lrec_dds && !d.sub_sys) {
+  if (d.dd_stream && (d.n_lgrp32 > 0 || (d.n_lgrp > 0 && d.lrec_dds)) &&
+      !d.sub_sys) {
     launch_line<ArithDD, MODE>(d, d.lrec_dds, r, pv, v, z, sc, st);
     return;
   }
@@ -1128,6 +1169,13 @@ void launch_ilu0_factor(const SolverDev &d, const double *pvals, int *bad,
                                         bad);
   count_launches(1);
   auto grid = [](int n) { return (n + 255) / 256 < 2432 ? (n + 255) / 256 : 2432; };
+  if (to_dd && d.n_lpack32 > 0) {  // FP32-weight line records
+    k_pack_stream<float><<<grid(d.n_lpack32), 256, 0, st>>>(
+        d.n_lpack32, d.lpack32_src, d.lpack32_dst,
+        reinterpret_cast<const double *>(d.rec64),
+        reinterpret_cast<float *>(d.lrec32));
+    count_launches(1);
+  }
   if (d.n_lpack > 0) {  // line-form records
     k_pack_stream<double><<<grid(d.n_lpack), 256, 0, st>>>(
         d.n_lpack, d.lpack_src, d.lpack_dst,
@@ -1189,7 +1237,7 @@ bool launch_ilu0_apply_def_dd(const SolverDev &d, const float2 *in, float2 *z,
   if (!d.dd_stream || !d.def_y) return false;
   const size_t smem = d.smem64;
   float2 *pv = const_cast<float2 *>(in);  // mode 3 reads it only
-  if (d.n_lgrp > 0 && d.lrec_dds && !d.sub_sys) {
+  if ((d.n_lgrp32 > 0 || (d.n_lgrp > 0 && d.lrec_dds)) && !d.sub_sys) {
     launch_line<ArithDD, 3>(d, d.lrec_dds, nullptr, pv, nullptr, z, sc, st);
     return true;
   }

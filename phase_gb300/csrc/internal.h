@@ -214,6 +214,12 @@ struct Analysis {
   std::vector<uint8_t> lrec;
   std::vector<int32_t> lpack_src, lpack_dst;  // line record <- factor
   size_t lsmem = 0;
+  // the same with FP32 weights (mixed solver, mixed_sweep 3): one forward
+  // and one backward piece per group
+  std::vector<LineMeta> lmeta32;
+  std::vector<uint8_t> lrec32;
+  std::vector<int32_t> lpack32_src, lpack32_dst;  // in 4-byte units
+  size_t lsmem32 = 0;
   // float-float step stream (kernels.cuh StepMeta) of the mixed solver,
   // when every row has at most 3 L and 3 U entries
   bool use_steps = false;

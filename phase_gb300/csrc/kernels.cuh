@@ -197,6 +197,8 @@ struct LineMeta {
   int32_t r0, nr, nlev, rec_off, hdr_bytes, max_piece;
   int32_t p0_off, p0_bytes, p1_off, p1_bytes;
   int32_t sub0, nsub, nr0, lanes;  // lanes per member: 16 (pair) or 32
+  int32_t buf1;    // byte offset of piece buffer 1 from buffer 0
+  int32_t zs_off;  // byte offset of the group's z vector in shared memory
 };
 
 // Step form of the factor for the float-float sweep of the mixed solver,
@@ -262,6 +264,14 @@ struct SolverDev {
   size_t lsmem;
   const int32_t *lpack_src, *lpack_dst;
   int n_lpack;
+  // FP32-weight line records of the mixed solver (mixed_sweep 3; n_lgrp32
+  // > 0 when they are in use)
+  int n_lgrp32;
+  const LineMeta *lmeta32;
+  uint8_t *lrec32;
+  size_t lsmem32;
+  const int32_t *lpack32_src, *lpack32_dst;
+  int n_lpack32;
 };
 
 

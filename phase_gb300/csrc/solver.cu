@@ -65,6 +65,9 @@ struct pg_solver {
   DevBuf<LineMeta> lmeta;
   DevBuf<uint8_t> lrec64, lrec_dds;
   DevBuf<int32_t> lpack_src, lpack_dst;
+  DevBuf<LineMeta> lmeta32;  // FP32 weights (mixed_sweep 3)
+  DevBuf<uint8_t> lrec32;
+  DevBuf<int32_t> lpack32_src, lpack32_dst;
   bool line_sweep = true;  // PG_LINE_SWEEP=0 at the analysis: stream kernel
   DevBuf<int> err;
   DevBuf<int32_t> raw_rp, raw_ci, st_rp, st_ci;
@@ -243,6 +246,16 @@ struct pg_solver {
     d.lpack_src = lpack_src.p;
     d.lpack_dst = lpack_dst.p;
     d.n_lpack = line ? (int)a.lpack_src.size() : 0;
+    const bool line32 = line && cfg.precision == PG_MIXED &&
+                        cfg.mixed_sweep == 3 && !a.lmeta32.empty() &&
+                        a.lsmem32 <= kMaxApplySmem;
+    d.n_lgrp32 = line32 ? (int)a.lmeta32.size() : 0;
+    d.lmeta32 = lmeta32.p;
+    d.lrec32 = lrec32.p;
+    d.lsmem32 = a.lsmem32;
+    d.lpack32_src = lpack32_src.p;
+    d.lpack32_dst = lpack32_dst.p;
+    d.n_lpack32 = line32 ? (int)a.lpack32_src.size() : 0;
     return d;
   }
   RedWork red() const { return RedWork{partials.p, ticket.p, red_grid}; }
@@ -322,6 +335,12 @@ int upload_analysis(pg_solver *s) {
   if (s->cfg.precision == PG_MIXED) up(s->lrec_dds, a.lrec);  // static parts
   up(s->lpack_src, a.lpack_src);
   up(s->lpack_dst, a.lpack_dst);
+  if (s->cfg.precision == PG_MIXED && s->cfg.mixed_sweep == 3) {
+    up(s->lmeta32, a.lmeta32);
+    up(s->lrec32, a.lrec32);
+    up(s->lpack32_src, a.lpack32_src);
+    up(s->lpack32_dst, a.lpack32_dst);
+  }
 
   if (e == cudaSuccess) e = s->err.zero(1);
   const size_t n = a.n, nnz = a.nnz;
@@ -762,6 +781,10 @@ bool use_dd(const pg_solver *s) {
 int choose_dd_sweep(pg_solver *s) {
   const SolverDev d0 = s->dev();
   const bool has_steps = d0.smem_dd > 0, has_blobs = d0.smem64 > 0 && d0.srec_dds;
+  if (d0.n_lgrp32 > 0) {  // mixed_sweep 3: FP32-weight line form
+    s->dd_stream = 1;
+    return PG_OK;
+  }
   if (has_steps && s->cfg.mixed_sweep == 1) {
     s->dd_stream = 0;
     return PG_OK;
@@ -908,7 +931,7 @@ extern "C" int pg_solver_create(const pg_solver_cfg *cfg, pg_solver **out) {
                "pg_solver_create: bad preconditioner");
   PG_CHECK_ARG(c.precision == PG_FP64 || c.precision == PG_MIXED,
                "pg_solver_create: bad precision");
-  PG_CHECK_ARG(c.mixed_sweep >= 0 && c.mixed_sweep <= 2,
+  PG_CHECK_ARG(c.mixed_sweep >= 0 && c.mixed_sweep <= 3,
                "pg_solver_create: bad mixed_sweep");
   PG_CHECK_ARG(c.coarse >= 0 && c.coarse <= 2, "pg_solver_create: bad coarse");
   PG_CHECK_ARG(c.coarse_warm >= -2, "pg_solver_create: bad coarse_warm");

@@ -100,10 +100,16 @@ def test_line_ordering_solves_as_before(pg, oracle):
         assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-9
 
 
-def test_irregular_blocks_keep_the_stream_form(pg):
-    """Blocks that are not full rectangles (a 100 x 37 grid cut into 300-row
-    subdomains) take the stream form; the solve is unaffected."""
-    nodes, cptr, cind = meshes.rectilinear(100, 37, 1.0, 1.3)
+@pytest.mark.parametrize("mesh", ["rect", "tri"])
+def test_sweep_form_by_mesh(pg, mesh):
+    """A 100 x 37 grid cut into ~300-row subdomains (cuts moved to grid
+    lines, so every block is a full rectangle) takes the line form; a
+    triangle mesh takes the stream form.  Both solve to the tolerance."""
+    if mesh == "rect":
+        nodes, cptr, cind = meshes.rectilinear(100, 37, 1.0, 1.3)
+    else:
+        nodes, cptr, cind = meshes.triangulated(40, 30, 1.0, 1.0, jitter=0.2,
+                                                seed=4)
     m = pg.Mesh(nodes, cptr, cind)
     f = m.faces()
     bc = np.where(f["rcell"] < 0, 0, 1).astype(np.int32)
@@ -114,7 +120,79 @@ def test_irregular_blocks_keep_the_stream_form(pg):
     rp, ci, v, _ = eqn.export()
     b = rng.standard_normal(eqn.n)
     s.setRhs(b)
-    assert s.sweep_form() == 0
+    assert s.sweep_form() == (1 if mesh == "rect" else 0)
     assert s.solve() <= 1e-10
     A = sp.csr_matrix((v, ci, rp))
     assert np.linalg.norm(b - A @ s.x()) / np.linalg.norm(b) <= 1.01e-10
+
+
+def _ilu_apply_f32_weights(rp, ci, lu, part, r):
+    """z = (LU)^-1 r per subdomain in FP64 arithmetic with the factor stored
+    as the device's FP32 records hold it: L multipliers and 1/u_ii rounded
+    to FP32, the diagonal applied as a product."""
+    n = len(rp) - 1
+    f32 = lambda a: np.asarray(a, np.float32).astype(np.float64)
+    z = np.array(r, np.float64)
+    rows = [np.asarray(ci[rp[i]:rp[i + 1]]) for i in range(n)]
+    vals = [f32(lu[rp[i]:rp[i + 1]]) for i in range(n)]
+    dinv = np.empty(n)
+    for i in range(n):
+        d = lu[rp[i]:rp[i + 1]][rows[i] == i][0]
+        dinv[i] = np.float32(1.0 / d)
+    for i in range(n):
+        c, w = rows[i], vals[i]
+        sel = (c < i) & (part[c] == part[i])
+        z[i] -= np.dot(w[sel], z[c[sel]]) if sel.any() else 0.0
+    for i in range(n - 1, -1, -1):
+        c, w = rows[i], vals[i]
+        sel = (c > i) & (part[c] == part[i])
+        acc = z[i] - (np.dot(w[sel], z[c[sel]]) if sel.any() else 0.0)
+        z[i] = acc * dinv[i]
+    return z
+
+
+@pytest.mark.parametrize("sub", [128, 1024])
+def test_fp32_weight_sweep_matches_rounded_factors(pg, oracle, sub):
+    """mixed_sweep 3: the ILU(0) factor stored in FP32 and swept in
+    float-float arithmetic equals the FP64 sweep of the same FP32-rounded
+    factor (1e-10 relative; the sweep arithmetic is about 48-bit).  128-row
+    blocks of the 128 x 96 grid are paired in a warp, 1024-row blocks take
+    a warp each."""
+    w = workloads.rising_bubble(128, 96, seed=3)
+    m = pg.Mesh(w["nodes"], w["cptr"], w["cind"])
+    w = workloads.rising_bubble(128, 96, seed=3, faces=m.faces(), cells=m.cells())
+    coeff = m.dt_over_rho(w["gamma"], w["rho1"], w["rho2"], w["dt"])
+    eqn = pg.fv.laplacian(coeff, m, w["bc_type"], w["bc_value"], w["u"])
+    rp, ci, v, rhs = eqn.export()
+    s = pg.SparseMatrixSolver(subdomain_rows=sub, precision=pg.MIXED,
+                              mixed_sweep=3)
+    s.set_eqn(eqn)
+    assert s.sweep_form() == 1
+    part, nparts = s.partition()
+    assert nparts > 4
+    lu, rc = oracle.ilu0(rp, ci, v, part)
+    assert rc == 0
+    rng = np.random.default_rng(5)
+    for r in (rng.standard_normal(eqn.n), -rhs):
+        z = s.apply_precond(r)
+        zo = _ilu_apply_f32_weights(rp, ci, lu, part, r)
+        assert np.linalg.norm(z - zo) / np.linalg.norm(zo) < 1e-10
+
+
+def test_fp32_weight_sweep_solves_the_bubble(pg):
+    """The float-float solver with FP32-stored factors (a fixed linear
+    preconditioner) reaches the FP64 true residual 1e-8 on the 256 x 256
+    bubble with the deflated coarse correction, in about as many
+    iterations as with float-pair factors."""
+    eqn = _bubble_eqn(pg, 256)
+    its = {}
+    for ms in (2, 3):
+        s = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=5000, coarse=2,
+                                  precision=pg.MIXED, mixed_sweep=ms)
+        s.set_eqn(eqn)
+        assert s.solve() <= 1e-8 and s.stats.status == pg.PG_OK
+        its[ms] = s.nIters()
+        rp, ci, v, rhs = eqn.export()
+        A = sp.csr_matrix((v, ci, rp))
+        assert np.linalg.norm(-rhs - A @ s.x()) / np.linalg.norm(rhs) <= 1.01e-8
+    assert its[3] <= 1.25 * its[2] + 4, its
