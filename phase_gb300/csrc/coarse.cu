@@ -33,7 +33,6 @@ namespace {
 constexpr int kCoarseBlock = 128;
 constexpr int kCorrectBlock = 256;
 constexpr int kGjB = 32;     // pivots per block of the Gauss-Jordan inversion
-constexpr int kGjRows = 16;  // rows per CTA of the block update
 
 // deterministic block sum (fixed tree); every thread gets the total
 __device__ double block_sum(double v, double *red) {
@@ -89,33 +88,51 @@ __global__ void k_gj_diag(int K, const float *__restrict__ ac,
 
 // P^-1 by single-pivot Gauss-Jordan in the registers of one warp: lane q
 // holds column q of the pivot block; a pivot below 1e-5 of its original
-// diagonal is dropped (its row and column of the inverse are zero)
-__global__ void __launch_bounds__(32)
-k_gjb_pivot_block(int K, int k0, int b, const float *__restrict__ ac,
-                  const float *__restrict__ dg0, float *__restrict__ pinv) {
+// diagonal is dropped (its row and column of the inverse are zero).  The
+// rows are kept rotated so the pivot row of step k is always c[0] (after
+// step k the array shifts by one row), which lets the step loop stay rolled
+// (a short loop body instead of 32 unrolled copies) with every register
+// index fixed at compile time.  The result goes to pi (shared memory) and,
+// to pinv (either may be NULL).
+__device__ __forceinline__ void gjb_pivot_block(int K, int k0, int b,
+                                                const float *ac,
+                                                const float *__restrict__ dg0,
+                                                float (*pi)[kGjB + 1],
+                                                float *__restrict__ pinv) {
   const int q = threadIdx.x;
   float c[kGjB];
+  // read from L2: the block may have been written by this CTA's other
+  // warps just before
 #pragma unroll
   for (int p = 0; p < kGjB; ++p)
-    c[p] = p < b && q < b ? ac[(size_t)(k0 + p) * K + k0 + q] : 0.f;
+    c[p] = p < b && q < b ? __ldcg(ac + (size_t)(k0 + p) * K + k0 + q) : 0.f;
+  // the original diagonal of the block: lane q holds pivot q's, read once
+  const float d0 = q < b ? fabsf(dg0[k0 + q]) : 0.f;
+#pragma unroll 1
+  for (int k = 0; k < b; ++k) {
+    // c[p] holds row (k + p) mod 32
+    const float piv = __shfl_sync(0xffffffffu, c[0], k);
+    const float dk = __shfl_sync(0xffffffffu, d0, k);
+    const float ip = fabsf(piv) > 1e-5f * dk ? 1.f / piv : 0.f;
+    const float rk = c[0];  // P[k][q]
+    c[0] = q == k ? ip : rk * ip;
 #pragma unroll
-  for (int k = 0; k < kGjB; ++k) {
-    if (k < b) {
-      const float piv = __shfl_sync(0xffffffffu, c[k], k);
-      const float ip = fabsf(piv) > 1e-5f * fabsf(dg0[k0 + k]) ? 1.f / piv : 0.f;
-      const float rk = c[k];  // P[k][q]
-#pragma unroll
-      for (int p = 0; p < kGjB; ++p) {
-        const float cpk = __shfl_sync(0xffffffffu, c[p], k);  // P[p][k]
-        if (p == k)
-          c[p] = q == k ? ip : rk * ip;
-        else
-          c[p] = q == k ? -cpk * ip : c[p] - cpk * (rk * ip);
-      }
+    for (int p = 1; p < kGjB; ++p) {
+      const float cpk = __shfl_sync(0xffffffffu, c[p], k);  // P[k+p][k]
+      c[p] = q == k ? -cpk * ip : c[p] - cpk * (rk * ip);
     }
-  }
+    const float t0 = c[0];
 #pragma unroll
-  for (int p = 0; p < kGjB; ++p) pinv[p * kGjB + q] = c[p];
+    for (int p = 0; p + 1 < kGjB; ++p) c[p] = c[p + 1];
+    c[kGjB - 1] = t0;
+  }
+  // after b steps c[p] holds row (b + p) mod 32
+#pragma unroll
+  for (int p = 0; p < kGjB; ++p) {
+    const int row = (b + p) & (kGjB - 1);
+    if (pi) pi[row][q] = c[p];
+    if (pinv) pinv[row * kGjB + q] = c[p];
+  }
 }
 
 // W = P^-1 R (b x K) and V = C P^-1 (K x b); C is kept (K x b) for the
@@ -124,19 +141,36 @@ k_gjb_pivot_block(int K, int k0, int b, const float *__restrict__ ac,
 // rows of V and C (four threads per row, eight columns each).
 __global__ void __launch_bounds__(256)
 k_gjb_panel(int K, int k0, int b, int nw, const float *__restrict__ ac,
-            const float *__restrict__ pinv, float *__restrict__ W,
-            float *__restrict__ V, float *__restrict__ C) {
+            const float *__restrict__ dg0, float *__restrict__ pinv,
+            int invert, float *__restrict__ W, float *__restrict__ V,
+            float *__restrict__ C) {
+  pdl_wait();
+  // the pivot block's inverse: the previous step's update computed it
+  // (pinv), except on the first step, where every CTA inverts the block
+  // itself (one warp) and the first one stores it; the CTA's own operands
+  // are read first, in flight meanwhile
   __shared__ float pi[kGjB][kGjB + 1];
-  for (int e = threadIdx.x; e < kGjB * kGjB; e += 256)
-    pi[e / kGjB][e % kGjB] = pinv[e];
-  __syncthreads();
-  if ((int)blockIdx.x < nw) {
-    const int j = blockIdx.x * 32 + (threadIdx.x & 31);
-    if (j >= K) return;
-    float r[kGjB];
+  const bool wpart = (int)blockIdx.x < nw;
+  const int t = wpart ? 0 : ((int)blockIdx.x - nw) * 256 + (int)threadIdx.x;
+  const int j = wpart ? (int)blockIdx.x * 32 + (int)(threadIdx.x & 31) : 0;
+  const int i = t >> 2, p0 = (t & 3) * 8;
+  const bool live = wpart ? j < K : i < K;
+  float r[kGjB];  // W part: column j of R; V part: row i of C
 #pragma unroll
-    for (int q = 0; q < kGjB; ++q)
-      r[q] = q < b ? ac[(size_t)(k0 + q) * K + j] : 0.f;
+  for (int q = 0; q < kGjB; ++q)
+    r[q] = live && q < b ? (wpart ? ac[(size_t)(k0 + q) * K + j]
+                                  : ac[(size_t)i * K + k0 + q])
+                         : 0.f;
+  if (invert) {
+    if (threadIdx.x < 32)
+      gjb_pivot_block(K, k0, b, ac, dg0, pi, blockIdx.x == 0 ? pinv : nullptr);
+  } else {
+    for (int e = threadIdx.x; e < kGjB * kGjB; e += 256)
+      pi[e / kGjB][e % kGjB] = pinv[e];
+  }
+  __syncthreads();
+  if (!live) return;
+  if (wpart) {
     for (int p = threadIdx.x >> 5; p < b; p += 8) {
       float acc = 0.f;
 #pragma unroll
@@ -144,63 +178,144 @@ k_gjb_panel(int K, int k0, int b, int nw, const float *__restrict__ ac,
       W[(size_t)p * K + j] = acc;
     }
   } else {
-    const int t = (blockIdx.x - nw) * 256 + threadIdx.x;
-    const int i = t >> 2, p0 = (t & 3) * 8;
-    if (i >= K) return;
-    float c[kGjB];
-#pragma unroll
-    for (int q = 0; q < kGjB; ++q)
-      c[q] = q < b ? ac[(size_t)i * K + k0 + q] : 0.f;
 #pragma unroll
     for (int pp = 0; pp < 8; ++pp) {
       const int p = p0 + pp;
       float acc = 0.f;
 #pragma unroll
-      for (int q = 0; q < kGjB; ++q) acc += c[q] * pi[q][p];
+      for (int q = 0; q < kGjB; ++q) acc += r[q] * pi[q][p];
       V[(size_t)i * kGjB + p] = acc;
-      C[(size_t)i * kGjB + p] = c[p];
+      C[(size_t)i * kGjB + p] = p < b ? ac[(size_t)i * K + k0 + p] : 0.f;
     }
   }
 }
 
-// the update of every entry; a CTA owns kGjRows rows x 256 columns and each
-// thread keeps its column of W in registers
-__global__ void __launch_bounds__(256)
-k_gjb_update(int K, int k0, int b, float *__restrict__ ac,
-             const float *__restrict__ pinv, const float *__restrict__ W,
-             const float *__restrict__ V, const float *__restrict__ C) {
-  __shared__ float cs[kGjRows][kGjB];
-  const int j = blockIdx.x * 256 + threadIdx.x;
-  const int i0 = blockIdx.y * kGjRows;
-  for (int e = threadIdx.x; e < kGjRows * kGjB; e += 256) {
-    const int ii = i0 + e / kGjB;
-    cs[e / kGjB][e % kGjB] = ii < K ? C[(size_t)ii * kGjB + e % kGjB] : 0.f;
+// The update of every entry, register-tiled: a CTA owns a kUpdRows x
+// kUpdCols tile; the pivot block's rows of C (transposed, 32 x kUpdRows) and
+// columns of W (32 x kUpdCols) are staged in shared memory, and each thread
+// keeps 4 rows x 4 consecutive columns of sums in registers, reading its 4
+// W values and its 4 C values with one 16-byte load each per pivot (a warp
+// shares its rows, so its C loads are broadcasts).  The tile's entries of A
+// are read at the start, all in flight together (16-byte accesses when
+// every row of A is 16-byte aligned, VEC), and each sum runs over the 32
+// pivots in order, as C[i, :] . W[:, j] with zeros past b.
+constexpr int kUpdRows = 32, kUpdCols = 128;
+template <bool VEC>
+__global__ void __launch_bounds__(256, 4)
+k_gjb_update(int K, int k0, int b, float *ac, const float *__restrict__ pinv,
+             const float *__restrict__ dg0, float *__restrict__ pinv_next,
+             const float *__restrict__ W, const float *__restrict__ V,
+             const float *__restrict__ C) {
+  pdl_wait();
+  __shared__ __align__(16) float ws[kGjB][kUpdCols];
+  __shared__ __align__(16) float ct[kGjB][kUpdRows];
+  // The tile holding the next pivot block (rows and columns k0+32 ..
+  // k0+63) is given to the first CTA, which afterwards inverts that block
+  // for the next step's panel while the other tiles are being updated.
+  const int k1 = k0 + kGjB;
+  const int tiles_x = gridDim.x, n_tiles = gridDim.x * gridDim.y;
+  const int own = k1 < K ? (k1 / kUpdRows) * tiles_x + k1 / kUpdCols : 0;
+  const int tile = ((int)(blockIdx.y * gridDim.x + blockIdx.x) + own) % n_tiles;
+  const int j0 = (tile % tiles_x) * kUpdCols, i0 = (tile / tiles_x) * kUpdRows;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int jt = j0 + 4 * tx;  // this thread's first column
+  float a_old[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int i = i0 + ty * 4 + r;
+    if (VEC && i < K && jt + 3 < K) {
+      const float4 x = *reinterpret_cast<const float4 *>(ac + (size_t)i * K + jt);
+      a_old[r][0] = x.x, a_old[r][1] = x.y, a_old[r][2] = x.z, a_old[r][3] = x.w;
+    } else {
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        a_old[r][c] = i < K && jt + c < K ? ac[(size_t)i * K + jt + c] : 0.f;
+    }
+  }
+  // W and C tiles: every load is issued before the first store to shared
+  // memory, so the tile arrives in one round trip
+  {
+    constexpr int NW = kGjB * kUpdCols / 4 / 256;  // 16-byte pieces per thread
+    float4 wl[NW];
+#pragma unroll
+    for (int u = 0; u < NW; ++u) {
+      const int e = threadIdx.x + 256 * u;
+      const int q = e / (kUpdCols / 4), jj = j0 + 4 * (e % (kUpdCols / 4));
+      const float *src = W + (size_t)q * K + jj;
+      if (VEC && q < b && jj + 3 < K) {
+        wl[u] = *reinterpret_cast<const float4 *>(src);
+      } else {
+        wl[u].x = q < b && jj < K ? src[0] : 0.f;
+        wl[u].y = q < b && jj + 1 < K ? src[1] : 0.f;
+        wl[u].z = q < b && jj + 2 < K ? src[2] : 0.f;
+        wl[u].w = q < b && jj + 3 < K ? src[3] : 0.f;
+      }
+    }
+    // C rows are 32 contiguous floats (16-byte aligned): thread e takes row
+    // e / 8, pivots 4 (e % 8) .. +3
+    const int ii = i0 + threadIdx.x / 8, q4 = 4 * (threadIdx.x % 8);
+    float4 cl = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (ii < K) cl = *reinterpret_cast<const float4 *>(C + (size_t)ii * kGjB + q4);
+#pragma unroll
+    for (int u = 0; u < NW; ++u) {
+      const int e = threadIdx.x + 256 * u;
+      *reinterpret_cast<float4 *>(&ws[e / (kUpdCols / 4)][4 * (e % (kUpdCols / 4))]) = wl[u];
+    }
+    ct[q4][threadIdx.x / 8] = cl.x;
+    ct[q4 + 1][threadIdx.x / 8] = cl.y;
+    ct[q4 + 2][threadIdx.x / 8] = cl.z;
+    ct[q4 + 3][threadIdx.x / 8] = cl.w;
   }
   __syncthreads();
-  if (j >= K) return;
-  float w[kGjB];
+  float acc[4][4];
 #pragma unroll
-  for (int q = 0; q < kGjB; ++q) w[q] = q < b ? W[(size_t)q * K + j] : 0.f;
-  const bool jin = j >= k0 && j < k0 + b;
-  for (int r = 0; r < kGjRows; ++r) {
-    const int i = i0 + r;
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[r][c] = 0.f;
+#pragma unroll 8
+  for (int q = 0; q < kGjB; ++q) {
+    const float4 w = *reinterpret_cast<const float4 *>(&ws[q][4 * tx]);
+    const float4 cv = *reinterpret_cast<const float4 *>(&ct[q][4 * ty]);
+    const float wv[4] = {w.x, w.y, w.z, w.w}, cr[4] = {cv.x, cv.y, cv.z, cv.w};
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[r][c] += cr[r] * wv[c];
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int i = i0 + ty * 4 + r;
     if (i >= K) break;
     const bool iin = i >= k0 && i < k0 + b;
-    const size_t idx = (size_t)i * K + j;
-    float v;
-    if (iin && jin)
-      v = pinv[(i - k0) * kGjB + (j - k0)];
-    else if (iin)
-      v = w[i - k0];
-    else if (jin)
-      v = -V[(size_t)i * kGjB + (j - k0)];
-    else {
-      float acc = 0.f;
+    float v[4];
 #pragma unroll
-      for (int q = 0; q < kGjB; ++q) acc += cs[r][q] * w[q];
-      v = ac[idx] - acc;
+    for (int c = 0; c < 4; ++c) {
+      const int j = jt + c;
+      const bool jin = j >= k0 && j < k0 + b;
+      if (iin && jin)
+        v[c] = pinv[(i - k0) * kGjB + (j - k0)];
+      else if (iin)
+        v[c] = ws[i - k0][4 * tx + c];
+      else if (jin)
+        v[c] = -V[(size_t)i * kGjB + (j - k0)];
+      else
+        v[c] = a_old[r][c] - acc[r][c];
     }
-    ac[idx] = v;
+    if (VEC && jt + 3 < K) {
+      *reinterpret_cast<float4 *>(ac + (size_t)i * K + jt) =
+          make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 4; ++c)
+        if (jt + c < K) ac[(size_t)i * K + jt + c] = v[c];
+    }
+  }
+  if (k1 < K && blockIdx.x == 0 && blockIdx.y == 0) {
+    __threadfence();  // this CTA's entries of A are in L2 ...
+    __syncthreads();  // ... for every warp
+    if (threadIdx.x < 32)
+      gjb_pivot_block(K, k1, K - k1 < kGjB ? K - k1 : kGjB, ac, dg0, nullptr,
+                      pinv_next);
   }
 }
 
@@ -759,14 +874,24 @@ void launch_coarse_setup(const CoarseDev &c, const double *pvals,
   // directly when the capture is not possible)
   const int nblk = (K + kGjB - 1) / kGjB;
   const int nw = (K + 31) / 32;
-  const dim3 ugrid((K + 255) / 256, (K + kGjRows - 1) / kGjRows);
+  const dim3 ugrid((K + kUpdCols - 1) / kUpdCols, (K + kUpdRows - 1) / kUpdRows);
+  // programmatic dependent launch: each kernel waits at entry for its
+  // predecessor, so its launch overlaps the predecessor's tail
   auto steps = [&]() {
     for (int k0 = 0; k0 < K; k0 += kGjB) {
       const int b = K - k0 < kGjB ? K - k0 : kGjB;
-      k_gjb_pivot_block<<<1, 32, 0, st>>>(K, k0, b, c.ac, c.dg0, c.pinv);
-      k_gjb_panel<<<nw + (4 * K + 255) / 256, 256, 0, st>>>(K, k0, b, nw, c.ac,
-                                                            c.pinv, c.W, c.V, c.C);
-      k_gjb_update<<<ugrid, 256, 0, st>>>(K, k0, b, c.ac, c.pinv, c.W, c.V, c.C);
+      // the pivot inverse of step s is in pinv[s % 2] (the update of step
+      // s - 1 writes it while step s - 1's own is still being read)
+      float *pv = c.pinv + ((k0 / kGjB) & 1) * kGjB * kGjB;
+      float *pv_next = c.pinv + (((k0 / kGjB) + 1) & 1) * kGjB * kGjB;
+      launch_pdl(k_gjb_panel, nw + (4 * K + 255) / 256, 256, 0, st, K, k0, b,
+                 nw, (const float *)c.ac, (const float *)c.dg0, pv,
+                 k0 == 0 ? 1 : 0, c.W, c.V, c.C);
+      // 16-byte rows need K % 4 == 0 (the buffer itself is 256-byte aligned)
+      launch_pdl(K % 4 == 0 ? k_gjb_update<true> : k_gjb_update<false>, ugrid,
+                 256, 0, st, K, k0, b, c.ac, (const float *)pv,
+                 (const float *)c.dg0, pv_next, (const float *)c.W,
+                 (const float *)c.V, (const float *)c.C);
     }
   };
   if (gj_graph && !*gj_graph) {
@@ -784,7 +909,7 @@ void launch_coarse_setup(const CoarseDev &c, const double *pvals,
     cudaGraphLaunch(*gj_graph, st);
   else
     steps();
-  count_launches(3 * nblk);
+  count_launches(2 * nblk);
 }
 
 void launch_coarse_apply(const CoarseDev &c, const double *in, double *z,

@@ -280,8 +280,8 @@ struct SolverDev {
 // subdomain row ranges, the coupling structure of A_c = Z^T A Z, the dense
 // K x K FP32 matrix (inverted in place by launch_coarse_setup), the
 // original diagonal, the blocked Gauss-Jordan work arrays (pivot-block
-// inverse 32 x 32, W 32 x K, V and C K x 32) and the subdomain sums of an
-// application's input (float pairs).
+// inverses 2 x 32 x 32, one per step parity; W 32 x K, V and C K x 32) and
+// the subdomain sums of an application's input (float pairs).
 struct CoarseDev {
   int K = 0, max_cnb = 0;
   const int32_t *sub_ptr = nullptr, *cptr = nullptr, *cnb = nullptr;

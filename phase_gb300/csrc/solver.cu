@@ -376,7 +376,7 @@ int upload_analysis(pg_solver *s) {
     s->ac_next = -1;
     s->ac_valid = false;
     if (e == cudaSuccess) e = s->c_dg0.reserve(K);
-    if (e == cudaSuccess) e = s->c_pinv.reserve(32 * 32);
+    if (e == cudaSuccess) e = s->c_pinv.reserve(2 * 32 * 32);  // two steps
     for (DevBuf<float> *bf : {&s->c_W, &s->c_V, &s->c_C})
       if (e == cudaSuccess) e = bf->reserve(32 * K);
     if (e == cudaSuccess) e = s->c_sum.reserve(K);
