@@ -171,6 +171,11 @@ int pg_assemble_laplacian(pg_eqn *e, const double *gamma_face,
                           double gamma_scalar, const double *bc_value,
                           const double *u_face_xy, int ptr_kind);
 
+/* The diagonal coefficient a_P of every row (0 for a row without one),
+ * diag[n] in ptr_kind memory: for a momentum equation the a_P of the SIMPLE
+ * coefficient d = V / a_P. */
+int pg_eqn_diagonal(const pg_eqn *e, double *diag, int ptr_kind);
+
 /* Device addresses of the equation's values (nnz) and rhs_ (n, or 2n for a
  * momentum equation); valid until the equation is destroyed. */
 int pg_eqn_device_values(const pg_eqn *e, double **vals, double **rhs);
@@ -380,6 +385,15 @@ int pg_solver_set_row_coords(pg_solver *s, const double *xy);
 /* Take the matrix and -rhs_ of a device equation without a host round trip
  * (the device form of FiniteVolumeEquation::solve's set + setRhs). */
 int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e);
+
+/* The same for one component of a momentum equation (component 0: the x
+ * rows, 1: the y rows; VectorFiniteVolumeEquation::solve solves the rank-2N
+ * system whose two diagonal blocks are this one matrix,
+ * src/2D/Unstructured/FiniteVolume/Equation/VectorFiniteVolumeEquation.cpp
+ * :5-30,129-146); component 0 for any other equation.  Handing over the
+ * other component of the same equation at the same assembly replaces only
+ * the right-hand side and keeps the factorisation. */
+int pg_solver_set_eqn_component(pg_solver *s, const pg_eqn *e, int component);
 
 /* SparseMatrixSolver::setRhs (receives the already negated rhs) and
  * setGuess (SparseMatrixSolver.h:38-40).  rhs[n], x0[n]; x0 == NULL sets a

@@ -93,6 +93,8 @@ PROTOTYPES = {
     "pg_gradient": (_I, [_P, _P, _P, _P, _P, _I]),
     "pg_gradient_noalloc": (_I, [_P, _P, _P, _P]),
     "pg_solver_sweep_form": (_I, [_P]),
+    "pg_solver_set_eqn_component": (_I, [_P, _P, _I]),
+    "pg_eqn_diagonal": (_I, [_P, _P, _I]),
     "pg_solver_default_cfg": (None, [ctypes.POINTER(SolverCfg)]),
     "pg_solver_create": (_I, [ctypes.POINTER(SolverCfg), ctypes.POINTER(_P)]),
     "pg_solver_destroy": (_I, [_P]),
@@ -233,6 +235,11 @@ class Mesh:
         _check(lib().pg_interpolate_faces(self._h, _ptr(c), _ptr(out), PG_HOST))
         return out
 
+    def interpolate_faces_device(self, cell_ptr: int, face_ptr: int):
+        """interpolate_faces() from and to device memory."""
+        _check(lib().pg_interpolate_faces(self._h, _P(cell_ptr), _P(face_ptr),
+                                          PG_DEVICE))
+
     def dt_over_rho(self, gamma_cell, rho1, rho2, dt):
         g = _f64(gamma_cell, self.n_cells)
         out = np.empty(self.n_faces)
@@ -353,6 +360,19 @@ class Equation:
         return rp, ci[:rp[-1]].copy(), v[:rp[-1]].copy(), rhs
 
 
+def _eqn_diagonal(eqn, out_ptr=None):
+    """a_P per row: a host array, or written to device memory at out_ptr."""
+    if out_ptr is not None:
+        _check(lib().pg_eqn_diagonal(eqn._h, _P(out_ptr), PG_DEVICE))
+        return None
+    d = np.empty(eqn.n)
+    _check(lib().pg_eqn_diagonal(eqn._h, _ptr(d), PG_HOST))
+    return d
+
+
+Equation.diagonal = _eqn_diagonal
+
+
 class MomentumEquation:
     """Device momentum operator ddt + div - laplacian(nu) of the vector
     equation: one N x N matrix shared by both components, rhs[2N]."""
@@ -380,6 +400,14 @@ class MomentumEquation:
                                           _ptr(uf), PG_HOST))
         return self
 
+    def assemble_device(self, dt, nu, theta, u_old_ptr: int, u_face_ptr: int):
+        """assemble() with device pointers (x, y interleaved per cell and
+        per face)."""
+        _check(lib().pg_assemble_momentum(self._h, dt, nu, theta,
+                                          _P(u_old_ptr), _P(u_face_ptr),
+                                          PG_DEVICE))
+        return self
+
     def export(self):
         rp = np.empty(self.n + 1, np.int32)
         ci = np.empty(self.nnz, np.int32)
@@ -388,6 +416,8 @@ class MomentumEquation:
         _check(lib().pg_eqn_export(self._h, _ptr(rp), _ptr(ci), _ptr(v),
                                    _ptr(rhs)))
         return rp, ci, v, rhs
+
+    diagonal = _eqn_diagonal
 
 
 def default_cfg(**kw) -> SolverCfg:
@@ -445,8 +475,14 @@ class SparseMatrixSolver:
         _check(lib().pg_solver_set_csr(self._h, _ptr(rp), _ptr(ci), _ptr(v),
                                        PG_HOST))
 
-    def set_eqn(self, eqn: Equation):
-        _check(lib().pg_solver_set_eqn(self._h, eqn._h))
+    def set_eqn(self, eqn, component: int | None = None):
+        """Hand over a device equation; a MomentumEquation needs the
+        component (0: x, 1: y) whose right-hand side is solved."""
+        if component is None:
+            _check(lib().pg_solver_set_eqn(self._h, eqn._h))
+        else:
+            _check(lib().pg_solver_set_eqn_component(self._h, eqn._h,
+                                                     int(component)))
         self.n = eqn.n
 
     def setRhs(self, rhs):

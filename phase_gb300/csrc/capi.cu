@@ -456,6 +456,39 @@ extern "C" int pg_eqn_export(const pg_eqn *e, int32_t *row_ptr,
   return PG_OK;
 }
 
+// the diagonal a_ii of every row (the slot of e->diag; 0 where a row has
+// none), device kernel
+__global__ void k_eqn_diagonal(int n, const int32_t *__restrict__ diag,
+                               const double *__restrict__ vals,
+                               double *__restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += gridDim.x * blockDim.x)
+    out[i] = diag[i] >= 0 ? vals[diag[i]] : 0.;
+}
+
+extern "C" int pg_eqn_diagonal(const pg_eqn *e, double *diag, int ptr_kind) {
+  PG_CHECK_ARG(e && diag, "pg_eqn_diagonal: NULL arg");
+  PG_CHECK_ARG(e->diag.p, "pg_eqn_diagonal: equation has no diagonal map");
+  const int n = (int)e->p.n;
+  cudaStream_t st = stream();
+  double *dst = diag;
+  pg::DevBuf<double> tmp;
+  if (ptr_kind != PG_DEVICE) {
+    PG_CUDA(tmp.reserve(n));
+    dst = tmp.p;
+  }
+  if (n > 0) {
+    k_eqn_diagonal<<<(n + 255) / 256 < 2432 ? (n + 255) / 256 : 2432, 256, 0,
+                     st>>>(n, e->diag.p, e->vals.p, dst);
+    count_launches(1);
+    PG_CUDA(cudaGetLastError());
+  }
+  if (ptr_kind != PG_DEVICE)
+    PG_CUDA(copy_out(diag, dst, n * sizeof(double), PG_HOST));
+  PG_CUDA(cudaStreamSynchronize(st));
+  return PG_OK;
+}
+
 extern "C" int pg_assemble_momentum(pg_eqn *e, double dt, double nu,
                                     double theta, const double *u_old_cell,
                                     const double *u_face, int ptr_kind) {

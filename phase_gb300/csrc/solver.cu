@@ -69,6 +69,12 @@ struct pg_solver {
   DevBuf<uint8_t> lrec32;
   DevBuf<int32_t> lpack32_src, lpack32_dst;
   bool line_sweep = true;  // PG_LINE_SWEEP=0 at the analysis: stream kernel
+  // the device equation of the last hand-over and its assembly count
+  const pg_eqn *eqn_src = nullptr;
+  uint64_t eqn_version = 0;
+  // the factorisation (and coarse inverse) matches the current values: a
+  // solve after a right-hand-side-only hand-over does not redo it
+  bool factored = false;
   DevBuf<int> err;
   DevBuf<int32_t> raw_rp, raw_ci, st_rp, st_ci;
   std::vector<double> row_x, row_y;  // pg_solver_set_row_coords hint
@@ -406,6 +412,7 @@ int upload_analysis(pg_solver *s) {
   s->analysed = true;
   s->have_x = false;
   s->have_rhs = false;
+  s->factored = false;
   return PG_OK;
 }
 
@@ -1069,15 +1076,28 @@ extern "C" int pg_solver_set_csr(pg_solver *s, const int32_t *row_ptr,
                         (int)s->a.dup_dst.size(), s->dup_dst.p, s->dup_src.p, st);
   PG_CUDA(cudaGetLastError());
   s->have_vals = true;
+  s->factored = false;
+  s->eqn_src = nullptr;  // the values no longer come from a device equation
   return start_factor(s);
 }
 
-extern "C" int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e) {
-  PG_CHECK_ARG(s && e, "pg_solver_set_eqn: NULL arg");
-  PG_CHECK_ARG(!e->momentum,
-               "pg_solver_set_eqn: a momentum equation has two right-hand "
-               "sides; use pg_solver_set_csr/set_rhs per component");
+// The matrix of a device equation and its right-hand side `component`
+// (0, or 1 for the y rows of a momentum equation, whose two components
+// share one matrix).  A call with the same equation at the same assembly
+// as the previous one only replaces the right-hand side: the values, the
+// factorisation and the coarse inverse are kept.
+static int set_eqn(pg_solver *s, const pg_eqn *e, int component) {
   cudaStream_t st = stream();
+  const double *rhs = e->rhs.p + (size_t)component * e->p.n;
+  if (s->eqn_src == e && s->eqn_version == e->version && s->analysed &&
+      s->eqn_pattern == e->pattern_id && s->rank == e->p.n) {
+    int rj = join_factor(s);  // the solve's own rhs buffer is reused
+    if (rj) return rj;
+    launch_permute_vec((int)s->a.n, s->perm.p, rhs, -1.0, s->b.p, st);
+    PG_CUDA(cudaGetLastError());
+    s->have_rhs = true;
+    return PG_OK;
+  }
   if (s->rank != e->p.n) {
     s->rank = e->p.n;
     s->analysed = false;
@@ -1101,11 +1121,31 @@ extern "C" int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e) {
   launch_permute_values((int)s->a.nnz, s->psrc.p, e->vals.p, s->pvals.p,
                         (int)s->a.dup_dst.size(), s->dup_dst.p, s->dup_src.p, st);
   // the solver receives -rhs_ (FiniteVolumeEquation.tpp:73)
-  launch_permute_vec((int)s->a.n, s->perm.p, e->rhs.p, -1.0, s->b.p, st);
+  launch_permute_vec((int)s->a.n, s->perm.p, rhs, -1.0, s->b.p, st);
   PG_CUDA(cudaGetLastError());
   s->have_vals = true;
   s->have_rhs = true;
+  s->factored = false;
+  s->eqn_src = e;
+  s->eqn_version = e->version;
   return start_factor(s);
+}
+
+extern "C" int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e) {
+  PG_CHECK_ARG(s && e, "pg_solver_set_eqn: NULL arg");
+  PG_CHECK_ARG(!e->momentum,
+               "pg_solver_set_eqn: a momentum equation has two right-hand "
+               "sides; use pg_solver_set_eqn_component");
+  return set_eqn(s, e, 0);
+}
+
+extern "C" int pg_solver_set_eqn_component(pg_solver *s, const pg_eqn *e,
+                                           int component) {
+  PG_CHECK_ARG(s && e, "pg_solver_set_eqn_component: NULL arg");
+  PG_CHECK_ARG(component == 0 || (component == 1 && e->momentum),
+               "pg_solver_set_eqn_component: component must be 0, or 1 for "
+               "a momentum equation");
+  return set_eqn(s, e, component);
 }
 
 extern "C" int pg_solver_set_rhs(pg_solver *s, const double *rhs, int ptr_kind) {
@@ -1149,9 +1189,11 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
   const int64_t n = s->a.n;
   if (!s->have_x) PG_CUDA(cudaMemsetAsync(s->x.p, 0, n * sizeof(double), st));
   PG_CUDA(cudaEventRecord(s->ev[0], st));
-  // the factorisation started at the hand-over, or now
-  int rc = s->fact_pending ? join_factor(s) : factor(s, st);
+  // the factorisation started at the hand-over, or now (unless the values
+  // are those of the last factorisation)
+  int rc = s->fact_pending ? join_factor(s) : s->factored ? PG_OK : factor(s, st);
   if (rc) return rc;
+  s->factored = true;
   PG_CUDA(cudaEventRecord(s->ev[1], st));
   if (s->cfg.precond == PG_PREC_ILU0) {
     PG_CUDA(cudaMemcpyAsync(s->bad_host, s->bad.p, sizeof(int),
@@ -1351,6 +1393,7 @@ extern "C" int pg_solver_apply_precond(pg_solver *s, const double *r,
   int rc = s->fact_pending ? join_factor(s) : factor(s, st);
   if (!rc) rc = join_coarse(s);
   if (rc) return rc;
+  s->factored = true;
   const SolverDev d = s->dev();  // after factor(): the sweep form is chosen
   const double *dr = r;
   if (ptr_kind != PG_DEVICE) {
@@ -1899,6 +1942,8 @@ extern "C" int pg_batch_set_eqns(pg_batch *b, int n_systems,
   PG_CUDA(cudaGetLastError());
   s->have_vals = true;
   s->have_rhs = true;
+  s->factored = false;
+  s->eqn_src = nullptr;
   return PG_OK;
 }
 

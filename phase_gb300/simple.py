@@ -5,7 +5,8 @@ Phase has no SIMPLE solver (its solvers are fractional-step), so this
 driver is project code written over the library's own operators:
 
 1. momentum predictor  ddt(u) + div(u_f, u) - laplacian(mu/rho, u) = 0
-   (pg_assemble_momentum), solved per component with the GPU BiCGStab;
+   (pg_assemble_momentum), solved per component on the device from the
+   device matrix (pg_solver_set_eqn_component);
 2. d_P = V_P / a_P from the momentum diagonal, interpolated to the faces
    with the distance weights (pg_interpolate_faces);
 3. u*_f = interpolated predictor velocity on interior faces, the boundary
@@ -44,32 +45,62 @@ def predictor_pcorr(pg, mesh, bc_u, u_face, u0, bc_p, p_value, rho, mu, dt,
                     tol=1e-12):
     """Momentum predictor from u0 (cells) with boundary velocities u_face,
     then the pCorr equation laplacian(rho d_f, pCorr) == div(rho u*_f) with
-    pressure boundary types bc_p and values p_value (per face)."""
+    pressure boundary types bc_p and values p_value (per face).
+
+    Device-resident: the momentum operator is assembled on the device, each
+    velocity component is solved from it by the device solver
+    (pg_solver_set_eqn_component, one factorisation for both), d = V / a_P
+    comes from the device diagonal, the face values are interpolated and
+    the pCorr equation assembled on the device; only the returned fields
+    are copied to the host (for inspection)."""
+    import torch
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    f64 = torch.float64
+    n, nf = mesh.n_cells, mesh.n_faces
+    on_dev = lambda a: torch.from_numpy(
+        np.ascontiguousarray(a, np.float64)).to(dev)
     faces, cells = mesh.faces(), mesh.cells()
-    n = mesh.n_cells
-    mom = pg.MomentumEquation(mesh, bc_u).assemble(dt, mu / rho, 1.0, u0,
-                                                   u_face)
-    rp, ci, v, rhs = mom.export()
+    u0_d = on_dev(np.asarray(u0).reshape(-1))
+    ufb_d = on_dev(np.asarray(u_face).reshape(-1))
+    torch.cuda.synchronize()
+    mom = pg.MomentumEquation(mesh, bc_u).assemble_device(
+        dt, mu / rho, 1.0, u0_d.data_ptr(), ufb_d.data_ptr())
     s = pg.SparseMatrixSolver(tolerance=tol, max_iters=5000)
-    s.setRank(n)
-    s.set(rp, ci, v)
-    u = np.empty((n, 2))
+    u_d = torch.empty((2, n), dtype=f64, device=dev)
     for d in range(2):
-        s.setRhs(-rhs[d * n:(d + 1) * n])
+        s.set_eqn(mom, component=d)
         s.setGuess(None)
         s.solve()
-        u[:, d] = s.x()
-    rows = np.repeat(np.arange(n), np.diff(rp))
-    a_p = v[(ci == rows)]
-    dcoef = cells["vol"] / a_p
-    gamma_f = rho * mesh.interpolate_faces(dcoef)
-    uf = np.stack([mesh.interpolate_faces(u[:, 0]),
-                   mesh.interpolate_faces(u[:, 1])], 1)
-    bnd = faces["rcell"] < 0
-    uf[bnd] = u_face[bnd]
-    eqn = pg.fv.laplacian(gamma_f, mesh, bc_p, p_value, rho * uf)
-    return dict(mesh=mesh, eqn=eqn, u=u, d=dcoef, gamma_f=gamma_f, u_face=uf,
-                momentum=(rp, ci, v, rhs))
+        s.x_device(u_d[d].data_ptr())
+    # the library and torch run on their own streams: each hands over after
+    # a synchronisation
+    a_p = torch.empty(n, dtype=f64, device=dev)
+    mom.diagonal(a_p.data_ptr())
+    pg.synchronize()
+    dcoef = on_dev(cells["vol"]) / a_p
+    gamma_f = torch.empty(nf, dtype=f64, device=dev)
+    uf = torch.empty((2, nf), dtype=f64, device=dev)
+    torch.cuda.synchronize()
+    mesh.interpolate_faces_device(dcoef.data_ptr(), gamma_f.data_ptr())
+    for d in range(2):
+        mesh.interpolate_faces_device(u_d[d].data_ptr(), uf[d].data_ptr())
+    pg.synchronize()
+    gamma_f *= rho
+    uf = uf.t().contiguous()
+    bnd = on_dev((faces["rcell"] < 0).astype(np.float64)).bool()
+    uf[bnd] = ufb_d.view(nf, 2)[bnd]
+    rho_uf = (rho * uf).contiguous()
+    pv = None if p_value is None else on_dev(p_value)
+    torch.cuda.synchronize()
+    eqn = pg.Equation(mesh, pg.GAMMA_FACE, bc_p).assemble_device(
+        gamma_face=gamma_f.data_ptr(),
+        bc_value=0 if pv is None else pv.data_ptr(), u_face=rho_uf.data_ptr())
+    pg.synchronize()
+    return dict(mesh=mesh, eqn=eqn, u=u_d.t().cpu().numpy(),
+                d=dcoef.cpu().numpy(), gamma_f=gamma_f.cpu().numpy(),
+                u_face=uf.cpu().numpy(), momentum=mom,
+                momentum_iters=s.nIters())
 
 
 def simple_pcorr(pg, nx=80, ny=80, rho=1.0, mu=0.01, dt=0.005, lid=1.0,
