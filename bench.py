@@ -97,6 +97,9 @@ def parse():
                          "solver's default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="sequence mode: leave out the cylinder and batched "
+                         "summaries")
     ap.add_argument("--mode", default="sequence",
                     choices=["sequence", "single", "batch"])
     ap.add_argument("--systems", type=int, default=256,
@@ -523,6 +526,18 @@ def run_sequence(args):
                "iterations": info["iterations"],
                "ms_per_iter": round(info["ms_per_iter"], 3)}
 
+    # the same step on the host cores with the device's own algorithm (the
+    # oracle's deflated two-level Schwarz ILU(0) on the device's partition),
+    # which splits the GPU/CPU ratio into algorithm and hardware
+    cpu2 = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.coarse:
+        cpu2 = cpu_two_level(sp, seq.assemble(t0), x_prev_host, args.coarse)
+
+    extras = {}
+    if rank == 0 and world == 1 and not args.no_extras:
+        extras["cylinder"] = cylinder_summary(pg, torch, args)
+        extras["batch"] = batch_summary(pg, torch, args)
+
     converged = all(st["status"] == 0 and st["rel_residual"] <= 1e-8
                     for st in st_m + st_p + st_q)
     if rank == 0:
@@ -582,15 +597,109 @@ def run_sequence(args):
                                       "rel_residual": zero["rel_residual"]},
             "solves_per_s": round(1000.0 / ms * world, 3),
             "roofline": roof_m, "roofline_plain_fp64": roof_p,
-            "cpu_baseline": cpu, "e2e": e2e,
+            "cpu_baseline": cpu, "cpu_two_level": cpu2, "e2e": e2e,
             "gpu_launches": int(launches), "clocks": clk,
             "wall_s": round(wall, 3),
         }
+        out.update(extras)
         if not converged:
             out["invalid"] = "a timed solve stopped above the 1e-8 residual"
         print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def cpu_two_level(solver, eqn, x0, coarse):
+    """The oracle's BiCGStab with the device solver's preconditioner: Schwarz
+    ILU(0) on the device's partition plus the subdomain-constant coarse
+    space (explicit coarse inverse, as on the device), FP64, all host
+    threads, from x0 (the previous step's solution)."""
+    import oracle_bind as ob
+    rp, ci, v, rhs = eqn.export()
+    part, K = solver.partition()
+    threads = len(os.sched_getaffinity(0))
+    x, st = ob.bicgstab(rp, ci, v, -rhs, tol=1e-8, max_iters=20000, part=part,
+                        x0=x0, threads=threads, coarse=coarse)
+    return {"value": round(st["ms"] + st["setup_ms"], 1), "unit": "ms",
+            "cores": threads, "kind": "port", "iterations": st["iters"],
+            "setup_ms": round(st["setup_ms"], 1),
+            "rel_residual": st["rel_residual"], "converged": st["status"] == 0,
+            "sample": f"oracle BiCGStab + Schwarz-ILU(0) on the device's {K} "
+                      f"subdomains + {'deflated' if coarse == 2 else 'additive'}"
+                      " coarse correction (the device's algorithm), FP64, the "
+                      "first timed step from the previous step's solution"}
+
+
+def cylinder_summary(pg, torch, args):
+    """The ~500k-triangle cylinder-channel pCorr system (one PISO-style
+    predictor step): FP64 and mixed two-level solves to 1e-8 from a zero
+    guess, device time per solve (mean of three), and the FP64 kernels'
+    roofline."""
+    import numpy as np
+    from phase_gb300 import simple
+    c = simple.cylinder_pcorr(pg)
+    eqn = c["eqn"]
+    out = {"workload": "cylinder channel, graded Delaunay triangles",
+           "n_cells": int(eqn.n), "nnz": int(eqn.nnz), "tolerance": 1e-8}
+    for name, prec in (("fp64", pg.FP64), ("mixed", pg.MIXED)):
+        s = pg.SparseMatrixSolver(tolerance=1e-8, max_iters=20000,
+                                  coarse=args.coarse, precision=prec,
+                                  mixed_sweep=args.mixed_sweep)
+        ms, its, ok = [], [], True
+        for _ in range(4):  # every hand-over factors anew (pg_solver_set_eqn)
+            s.set_eqn(eqn)
+            s.setGuess(None)
+            s.solve()
+            ms.append(s.stats.ms)
+            its.append(s.stats.iters)
+            ok &= s.stats.status == pg.PG_OK and s.stats.rel_residual <= 1e-8
+        out[name] = {"ms": round(float(np.mean(ms[1:])), 3),
+                     "iters": its[1:], "converged": bool(ok),
+                     "sweep_form": {1: "line", 0: "stream"}.get(s.sweep_form())}
+        if name == "fp64":
+            r = kernel_roofline(pg, s, eqn.n, int(eqn.nnz), dd=False, eqn=eqn,
+                                coarse=args.coarse)
+            out["fp64"]["per_kernel_frac"] = r["per_kernel_frac"]
+            out["fp64"]["per_kernel_ms"] = r["per_kernel_ms"]
+    return out
+
+
+def batch_summary(pg, torch, args, n_systems=256):
+    """The 256 ghost-cell IB channel systems (quad meshes of 2k-200k cells,
+    log-uniform) solved as one batch: solves/s (mean of three batch
+    solves after one warm-up)."""
+    import numpy as np
+    from phase_gb300 import workloads
+    t0 = time.perf_counter()
+    eqns = []
+    for sp_ in workloads.gcib_specs(n_systems, seed=5):
+        w = workloads.gcib_case(sp_)
+        m = pg.Mesh(w["nodes"], w["cptr"], w["cind"])
+        w = workloads.gcib_case(sp_, m.faces())
+        e = pg.Equation(m, pg.GAMMA_SCALAR, w["bc_type"],
+                        ib_circles=[w["circle"]])
+        e.assemble(gamma_scalar=w["gamma"], bc_value=w["bc_value"],
+                   u_face=w["u"])
+        eqns.append((m, e))
+    b = pg.BatchSolver(tolerance=1e-8, max_iters=20000, coarse=args.coarse)
+    b.set_eqns([e for _, e in eqns])
+    setup_s = time.perf_counter() - t0
+    b.solve()
+    ms, ok, iters = [], True, []
+    for _ in range(3):
+        st = b.solve()
+        ms.append(b.ms)
+        ok &= all(s_.status == pg.PG_OK and s_.rel_residual <= 1e-8 for s_ in st)
+        iters = [s_.iters for s_ in st]
+    bm = float(np.mean(ms))
+    return {"workload": f"{n_systems} ghost-cell IB channel pressure systems, "
+                        "quad meshes 2k-200k cells (log-uniform)",
+            "total_cells": int(sum(e.n for _, e in eqns)),
+            "ms_per_batch": round(bm, 3),
+            "solves_per_s": round(1000.0 * n_systems / bm, 2),
+            "iters": {"min": int(min(iters)), "median": float(np.median(iters)),
+                      "max": int(max(iters))},
+            "converged": bool(ok), "host_setup_s": round(setup_s, 2)}
 
 
 def e2e_learned(pg, guess, seq, net, have_w, steps, torch, dev, coarse,

@@ -390,9 +390,10 @@ int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e);
  * rows, 1: the y rows; VectorFiniteVolumeEquation::solve solves the rank-2N
  * system whose two diagonal blocks are this one matrix,
  * src/2D/Unstructured/FiniteVolume/Equation/VectorFiniteVolumeEquation.cpp
- * :5-30,129-146); component 0 for any other equation.  Handing over the
- * other component of the same equation at the same assembly replaces only
- * the right-hand side and keeps the factorisation. */
+ * :5-30,129-146); component 0 for any other equation.  Handing over a
+ * component of the same equation at the same assembly as the previous
+ * call replaces only the right-hand side and keeps the factorisation
+ * (pg_solver_set_eqn always factors anew). */
 int pg_solver_set_eqn_component(pg_solver *s, const pg_eqn *e, int component);
 
 /* SparseMatrixSolver::setRhs (receives the already negated rhs) and

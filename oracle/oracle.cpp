@@ -664,14 +664,120 @@ struct Ilut {
   }
 };
 
+// Two-level coarse correction on the subdomain-constant vectors (the
+// device solver's preconditioner, restated for an algorithm-matched CPU
+// baseline; Nicolaides 1987, Tang, Nabben, Vuik & Erlangga 2009): A_c =
+// Z^T A Z summed in FP64, factored by dense LU with partial pivoting
+// (rows parallel over threads); a pivot below 1e-14 of the largest entry
+// drops its coarse unknown (a singular, all-Neumann A_c).
+struct Coarse {
+  int K = 0;
+  std::vector<double> lu;     // K x K, row-major, L unit-lower and U
+  std::vector<int> piv;       // row permutation
+  std::vector<char> dead;     // dropped unknowns
+  const int32_t *part = nullptr;
+
+  void build(const Csr &A, const int32_t *p, int k) {
+    K = k;
+    part = p;
+    lu.assign((size_t)K * K, 0.);
+    for (int64_t i = 0; i < A.n; ++i)
+      for (int32_t j = A.rp[i]; j < A.rp[i + 1]; ++j)
+        lu[(size_t)part[i] * K + part[A.ci[j]]] += A.v[j];
+    double amax = 0.;
+    for (double v : lu) amax = std::max(amax, std::fabs(v));
+    piv.resize(K);
+    dead.assign(K, 0);
+    for (int c = 0; c < K; ++c) {
+      int pr = c;
+      for (int r = c + 1; r < K; ++r)
+        if (std::fabs(lu[(size_t)r * K + c]) > std::fabs(lu[(size_t)pr * K + c])) pr = r;
+      piv[c] = pr;
+      if (pr != c)
+        for (int j = 0; j < K; ++j) std::swap(lu[(size_t)c * K + j], lu[(size_t)pr * K + j]);
+      const double d = lu[(size_t)c * K + c];
+      if (std::fabs(d) <= 1e-14 * amax) {
+        dead[c] = 1;
+        continue;
+      }
+#pragma omp parallel for schedule(static)
+      for (int r = c + 1; r < K; ++r) {
+        double *row = &lu[(size_t)r * K];
+        const double l = row[c] / d;
+        row[c] = l;
+        if (l != 0.)
+          for (int j = c + 1; j < K; ++j) row[j] -= l * lu[(size_t)c * K + j];
+      }
+    }
+    invert();
+  }
+  // y = A_c^-1 s with the LU factors (s overwritten)
+  void lu_solve(std::vector<double> &s, std::vector<double> &y) const {
+    for (int c = 0; c < K; ++c) std::swap(s[c], s[piv[c]]);
+    for (int r = 0; r < K; ++r) {
+      double acc = s[r];
+      for (int j = 0; j < r; ++j) acc -= lu[(size_t)r * K + j] * s[j];
+      s[r] = acc;
+    }
+    y.assign(K, 0.);
+    for (int r = K - 1; r >= 0; --r) {
+      if (dead[r]) continue;
+      double acc = s[r];
+      for (int j = r + 1; j < K; ++j) acc -= lu[(size_t)r * K + j] * y[j];
+      y[r] = acc / lu[(size_t)r * K + r];
+    }
+  }
+  // the explicit inverse (as the device applies it): column c solved from
+  // the unit vector e_c, columns in parallel
+  std::vector<double> inv;
+  void invert() {
+    inv.assign((size_t)K * K, 0.);
+#pragma omp parallel
+    {
+      std::vector<double> e, y;
+#pragma omp for schedule(dynamic, 8)
+      for (int c = 0; c < K; ++c) {
+        e.assign(K, 0.);
+        e[c] = 1.;
+        lu_solve(e, y);
+        for (int r = 0; r < K; ++r) inv[(size_t)r * K + c] = y[r];
+      }
+    }
+  }
+  // y = A_c^-1 s (rows in parallel)
+  void solve(std::vector<double> &s, std::vector<double> &y) const {
+    y.assign(K, 0.);
+#pragma omp parallel for schedule(static)
+    for (int r = 0; r < K; ++r) {
+      double acc = 0.;
+      const double *row = &inv[(size_t)r * K];
+      for (int c = 0; c < K; ++c) acc += row[c] * s[c];
+      y[r] = acc;
+    }
+  }
+  // Z^T r: subdomain sums in row order
+  void sums(int64_t n, const double *r, std::vector<double> &s) const {
+    s.assign(K, 0.);
+    for (int64_t i = 0; i < n; ++i) s[part[i]] += r[i];
+  }
+};
+
 struct Precond {
   int kind = OR_PREC_NONE;
   Ilu0 ilu0;
   Ilut ilut;
   std::vector<double> dinv;
   int status = 0;
+  int coarse = 0;
+  Coarse cs;
+  const Csr *A = nullptr;
+  mutable std::vector<double> s_, y_, t_;
 
-  void build(const Csr &A, const or_solver_cfg &cfg) {
+  void build(const Csr &Am, const or_solver_cfg &cfg) {
+    A = &Am;
+    const Csr &A = Am;
+    coarse = cfg.part && cfg.n_parts > 1 ? cfg.coarse : 0;
+    if (coarse) cs.build(A, cfg.part, cfg.n_parts);
     kind = cfg.precond;
     if (kind == OR_PREC_ILU0) {
       ilu0.build(A, cfg.part, cfg.n_parts);
@@ -687,6 +793,31 @@ struct Precond {
     }
   }
   void apply(int64_t n, const double *r, double *z) const {
+    if (coarse == 2) {  // A-DEF1: y = A_c^-1 Z^T r, z = B (r - A Z y) + Z y
+      cs.sums(n, r, s_);
+      cs.solve(s_, y_);
+      t_.resize(n);
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < n; ++i) {
+        double acc = r[i];
+        for (int32_t j = A->rp[i]; j < A->rp[i + 1]; ++j)
+          acc -= A->v[j] * y_[cs.part[A->ci[j]]];
+        t_[i] = acc;
+      }
+      apply_one(n, t_.data(), z);
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < n; ++i) z[i] += y_[cs.part[i]];
+      return;
+    }
+    apply_one(n, r, z);
+    if (coarse == 1) {  // additive: z += Z A_c^-1 Z^T r
+      cs.sums(n, r, s_);
+      cs.solve(s_, y_);
+#pragma omp parallel for schedule(static)
+      for (int64_t i = 0; i < n; ++i) z[i] += y_[cs.part[i]];
+    }
+  }
+  void apply_one(int64_t n, const double *r, double *z) const {
     switch (kind) {
     case OR_PREC_ILU0: ilu0.apply(r, z); break;
     case OR_PREC_ILUT: ilut.apply(r, z); break;

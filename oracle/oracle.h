@@ -106,6 +106,11 @@ typedef struct {
                           overlap 0); NULL = one global subdomain */
   int n_parts;
   int use_guess;       /* 1: x holds the initial guess; 0: zero guess */
+  int coarse;          /* with part: 0 one-level Schwarz; two-level with the
+                          subdomain-constant coarse space Z (A_c = Z^T A Z,
+                          dense LU with partial pivoting): 1 additive
+                          M^-1 r = B r + Z A_c^-1 Z^T r, 2 deflated (A-DEF1)
+                          M^-1 r = B (r - A Z y) + Z y, y = A_c^-1 Z^T r */
 } or_solver_cfg;
 
 typedef struct {

@@ -1083,13 +1083,13 @@ extern "C" int pg_solver_set_csr(pg_solver *s, const int32_t *row_ptr,
 
 // The matrix of a device equation and its right-hand side `component`
 // (0, or 1 for the y rows of a momentum equation, whose two components
-// share one matrix).  A call with the same equation at the same assembly
-// as the previous one only replaces the right-hand side: the values, the
-// factorisation and the coarse inverse are kept.
-static int set_eqn(pg_solver *s, const pg_eqn *e, int component) {
+// share one matrix).  With reuse, a call with the same equation at the
+// same assembly as the previous one only replaces the right-hand side: the
+// values, the factorisation and the coarse inverse are kept.
+static int set_eqn(pg_solver *s, const pg_eqn *e, int component, bool reuse) {
   cudaStream_t st = stream();
   const double *rhs = e->rhs.p + (size_t)component * e->p.n;
-  if (s->eqn_src == e && s->eqn_version == e->version && s->analysed &&
+  if (reuse && s->eqn_src == e && s->eqn_version == e->version && s->analysed &&
       s->eqn_pattern == e->pattern_id && s->rank == e->p.n) {
     int rj = join_factor(s);  // the solve's own rhs buffer is reused
     if (rj) return rj;
@@ -1136,7 +1136,7 @@ extern "C" int pg_solver_set_eqn(pg_solver *s, const pg_eqn *e) {
   PG_CHECK_ARG(!e->momentum,
                "pg_solver_set_eqn: a momentum equation has two right-hand "
                "sides; use pg_solver_set_eqn_component");
-  return set_eqn(s, e, 0);
+  return set_eqn(s, e, 0, false);
 }
 
 extern "C" int pg_solver_set_eqn_component(pg_solver *s, const pg_eqn *e,
@@ -1145,7 +1145,7 @@ extern "C" int pg_solver_set_eqn_component(pg_solver *s, const pg_eqn *e,
   PG_CHECK_ARG(component == 0 || (component == 1 && e->momentum),
                "pg_solver_set_eqn_component: component must be 0, or 1 for "
                "a momentum equation");
-  return set_eqn(s, e, component);
+  return set_eqn(s, e, component, true);
 }
 
 extern "C" int pg_solver_set_rhs(pg_solver *s, const double *rhs, int ptr_kind) {
