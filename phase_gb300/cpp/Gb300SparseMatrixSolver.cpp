@@ -101,6 +101,13 @@ void Gb300SparseMatrixSolver::set(const std::vector<SparseEntry> &entries) {
   set(rp, ci, v);
 }
 
+void Gb300SparseMatrixSolver::setDeviceEquation(const pg_eqn *eqn) {
+  int64_t n = 0;
+  check(pg_eqn_sizes(eqn, &n, nullptr), "setDeviceEquation");
+  if (!solver_ || rank_ != (int)n) setRank((int)n);
+  check(pg_solver_set_eqn(solver_, eqn), "setDeviceEquation");
+}
+
 void Gb300SparseMatrixSolver::setGuess(const Vector &x0) {
   check(pg_solver_set_guess(solver_, x0.data().data(), PG_HOST), "setGuess");
 }

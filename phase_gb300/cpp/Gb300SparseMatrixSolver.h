@@ -42,6 +42,10 @@ class Gb300SparseMatrixSolver : public SparseMatrixSolver {
   // subdomains are cut by coordinate bisection.  Kept across setRank calls
   // of the same rank.
   void setRowCoordinates(const std::vector<Scalar> &xy);
+  // The matrix and -rhs_ of an equation assembled on the device (the
+  // device form of FiniteVolumeEquation::solve's setRank + set + setRhs,
+  // FiniteVolumeEquation.tpp:71-73): no host copy of the CSR is made.
+  void setDeviceEquation(const pg_eqn *eqn);
   int nIters() const override;
   Scalar error() const override;
   bool supportsMPI() const override { return false; }
