@@ -924,6 +924,204 @@ static int bicgstab(const Csr &A, const double *b, double *x,
   return it;
 }
 
+// TFQMR (Freund 1993; Saad, Iterative Methods for Sparse Linear Systems,
+// 2nd ed., Alg. 7.8) on A M^-1, x advanced by M^-1 d; one iteration is two
+// half-steps.  Converged when sqrt(m+1) tau reaches the tolerance and the
+// true residual confirms it; a failed confirmation or a breakdown restarts
+// from the current x.
+static int tfqmr(const Csr &A, const double *b, double *x,
+                 const or_solver_cfg &cfg, or_solver_stats *st) {
+  const int64_t n = A.n;
+  auto t_setup = Clock::now();
+  Precond M;
+  M.build(A, cfg);
+  const double setup_ms = ms_since(t_setup);
+  auto t0 = Clock::now();
+  if (!cfg.use_guess) std::fill(x, x + n, 0.);
+  std::vector<double> w(n), u(n), uh(n), Bu(n), u1(n), uh1(n), Bu1(n), v(n),
+      dh(n), rs(n), tmp(n);
+  const double bn = std::sqrt(vdot(n, b, b));
+  auto true_res = [&](std::vector<double> &r) {
+    spmv(A, x, r.data());
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) r[i] = b[i] - r[i];
+    return std::sqrt(vdot(n, r.data(), r.data()));
+  };
+  auto axpy = [&](double *out, double a, const double *p, double c,
+                  const double *q) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) out[i] = a * p[i] + c * q[i];
+  };
+  int status = 1, it = 0, restarts = 0;
+  double rn = 0.;
+  if (bn == 0.) {
+    std::fill(x, x + n, 0.);
+    status = 0;
+  } else if (M.status) {
+    status = M.status;
+  } else {
+    for (;;) {
+      rn = true_res(w);
+      if (!std::isfinite(rn)) { status = 3; break; }
+      if (rn / bn <= cfg.tol) { status = 0; break; }
+      if (it >= cfg.max_iters) { status = 1; break; }
+      u = w;
+      rs = w;
+      std::fill(dh.begin(), dh.end(), 0.);
+      M.apply(n, u.data(), uh.data());
+      spmv(A, uh.data(), Bu.data());
+      v = Bu;
+      double tau = rn, theta = 0., eta = 0., rho = rn * rn, alpha = 0.;
+      int m = 0;
+      bool restart = false, done = false;
+      auto half = [&](const double *uhm, const double *Bum) {
+        axpy(w.data(), 1., w.data(), -alpha, Bum);
+        axpy(dh.data(), 1., uhm, theta * theta / alpha * eta, dh.data());
+        theta = std::sqrt(vdot(n, w.data(), w.data())) / tau;
+        const double c = 1. / std::sqrt(1. + theta * theta);
+        tau = tau * theta * c;
+        eta = c * c * alpha;
+        axpy(x, 1., x, eta, dh.data());
+        ++m;
+        done = tau * std::sqrt((double)m + 1.) <= cfg.tol * bn;
+      };
+      while (it < cfg.max_iters) {
+        const double sigma = vdot(n, v.data(), rs.data());
+        if (sigma == 0. || rho == 0. || !std::isfinite(sigma)) {
+          restart = true;
+          break;
+        }
+        alpha = rho / sigma;
+        axpy(u1.data(), 1., u.data(), -alpha, v.data());
+        half(uh.data(), Bu.data());
+        M.apply(n, u1.data(), uh1.data());
+        spmv(A, uh1.data(), Bu1.data());
+        if (!done) half(uh1.data(), Bu1.data());
+        ++it;
+        if (done) break;
+        const double rho_new = vdot(n, w.data(), rs.data());
+        const double beta = rho_new / rho;
+        rho = rho_new;
+        axpy(u.data(), 1., w.data(), beta, u1.data());
+        M.apply(n, u.data(), uh.data());
+        spmv(A, uh.data(), tmp.data());
+        axpy(v.data(), 1., Bu1.data(), beta, v.data());
+        axpy(v.data(), 1., tmp.data(), beta, v.data());
+        Bu = tmp;
+      }
+      if (restart && ++restarts > 50) { status = 2; break; }
+    }
+  }
+  if (st) {
+    rn = true_res(w);
+    st->iters = it;
+    st->status = status;
+    st->rel_residual = bn > 0 ? rn / bn : 0.;
+    st->ms = ms_since(t0);
+    st->setup_ms = setup_ms;
+  }
+  return it;
+}
+
+// Restarted GMRES (Saad & Schultz 1986) on A M^-1 with modified
+// Gram-Schmidt and Givens rotations; x += M^-1 (V y) at the end of each
+// cycle; converged when the implicit residual |g_{j+1}| reaches the
+// tolerance and the true residual confirms it.
+static int gmres(const Csr &A, const double *b, double *x,
+                 const or_solver_cfg &cfg, or_solver_stats *st) {
+  const int64_t n = A.n;
+  const int dim = cfg.krylov_dim > 0 ? cfg.krylov_dim : 300;
+  auto t_setup = Clock::now();
+  Precond M;
+  M.build(A, cfg);
+  const double setup_ms = ms_since(t_setup);
+  auto t0 = Clock::now();
+  if (!cfg.use_guess) std::fill(x, x + n, 0.);
+  std::vector<double> r(n), z(n), w(n), V((size_t)(dim + 1) * n);
+  std::vector<double> H((size_t)(dim + 1) * dim), cs(dim), sn(dim), g(dim + 1),
+      y(dim);
+  const double bn = std::sqrt(vdot(n, b, b));
+  auto true_res = [&]() {
+    spmv(A, x, r.data());
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) r[i] = b[i] - r[i];
+    return std::sqrt(vdot(n, r.data(), r.data()));
+  };
+  int status = 1, it = 0;
+  double rn = 0.;
+  if (bn == 0.) {
+    std::fill(x, x + n, 0.);
+    status = 0;
+  } else if (M.status) {
+    status = M.status;
+  } else {
+    for (;;) {
+      rn = true_res();
+      if (!std::isfinite(rn)) { status = 3; break; }
+      if (rn / bn <= cfg.tol) { status = 0; break; }
+      if (it >= cfg.max_iters) { status = 1; break; }
+      for (int64_t i = 0; i < n; ++i) V[i] = r[i] / rn;
+      std::fill(g.begin(), g.end(), 0.);
+      g[0] = rn;
+      int j = 0;
+      for (; j < dim && it < cfg.max_iters; ++j) {
+        const double *vj = &V[(size_t)j * n];
+        M.apply(n, vj, z.data());
+        spmv(A, z.data(), w.data());
+        for (int i = 0; i <= j; ++i) {
+          const double *vi = &V[(size_t)i * n];
+          const double hij = vdot(n, w.data(), vi);
+          H[(size_t)i * dim + j] = hij;
+#pragma omp parallel for schedule(static)
+          for (int64_t k = 0; k < n; ++k) w[k] -= hij * vi[k];
+        }
+        const double hn = std::sqrt(vdot(n, w.data(), w.data()));
+        ++it;
+        if (hn > 0.)
+          for (int64_t k = 0; k < n; ++k) V[(size_t)(j + 1) * n + k] = w[k] / hn;
+        double hj1 = hn;
+        for (int i = 0; i < j; ++i) {
+          double &a0 = H[(size_t)i * dim + j], &a1 = H[(size_t)(i + 1) * dim + j];
+          const double t = cs[i] * a0 + sn[i] * a1;
+          a1 = -sn[i] * a0 + cs[i] * a1;
+          a0 = t;
+        }
+        double &hjj = H[(size_t)j * dim + j];
+        const double den = std::hypot(hjj, hj1);
+        cs[j] = den > 0. ? hjj / den : 1.;
+        sn[j] = den > 0. ? hj1 / den : 0.;
+        hjj = den;
+        g[j + 1] = -sn[j] * g[j];
+        g[j] = cs[j] * g[j];
+        if (std::fabs(g[j + 1]) <= cfg.tol * bn || den == 0.) {
+          ++j;
+          break;
+        }
+      }
+      for (int i = j - 1; i >= 0; --i) {
+        double acc = g[i];
+        for (int k = i + 1; k < j; ++k) acc -= H[(size_t)i * dim + k] * y[k];
+        const double hii = H[(size_t)i * dim + i];
+        y[i] = hii != 0. ? acc / hii : 0.;
+      }
+      std::fill(w.begin(), w.end(), 0.);
+      for (int i = 0; i < j; ++i)
+        for (int64_t k = 0; k < n; ++k) w[k] += y[i] * V[(size_t)i * n + k];
+      M.apply(n, w.data(), z.data());
+      for (int64_t k = 0; k < n; ++k) x[k] += z[k];
+    }
+  }
+  if (st) {
+    rn = true_res();
+    st->iters = it;
+    st->status = status;
+    st->rel_residual = bn > 0 ? rn / bn : 0.;
+    st->ms = ms_since(t0);
+    st->setup_ms = setup_ms;
+  }
+  return it;
+}
+
 struct ThreadScope {
   int saved = 0;
   explicit ThreadScope(int k) {
@@ -948,7 +1146,12 @@ extern "C" int or_bicgstab(int64_t n, const int32_t *row_ptr,
   ThreadScope ts(cfg->n_threads);
   Csr A{n, row_ptr, col_ind, vals};
   or_solver_stats st{};
-  bicgstab(A, b, x, *cfg, &st, nullptr, 1);
+  if (cfg->krylov == 1)
+    tfqmr(A, b, x, *cfg, &st);
+  else if (cfg->krylov == 2)
+    gmres(A, b, x, *cfg, &st);
+  else
+    bicgstab(A, b, x, *cfg, &st, nullptr, 1);
   if (stats) *stats = st;
   return st.status;
 }

@@ -111,6 +111,9 @@ typedef struct {
                           dense LU with partial pivoting): 1 additive
                           M^-1 r = B r + Z A_c^-1 Z^T r, 2 deflated (A-DEF1)
                           M^-1 r = B (r - A Z y) + Z y, y = A_c^-1 Z^T r */
+  int krylov;          /* 0 BiCGStab, 1 TFQMR, 2 GMRES (Belos "solver",
+                          TrilinosBelosSparseMatrixSolver.cpp:59-60) */
+  int krylov_dim;      /* GMRES restart length (0 = 300, Belos' default) */
 } or_solver_cfg;
 
 typedef struct {

@@ -497,6 +497,21 @@ void launch_b_check(int n_sys, const KScalars *sc, int *chunks,
                     int max_chunks, cudaGraphConditionalHandle h,
                     cudaStream_t st);
 
+// ---- TFQMR / GMRES drivers (krylov.cu) ----
+// y = A x on the permuted CSR (FP64)
+void launch_spmv_plain(const SolverDev &d, const double *val, const double *x,
+                       double *y, cudaStream_t st);
+// out = a x + b y (out may be x or y; b == 0 ignores y)
+void launch_lincomb(int n, double a, const double *x, double b,
+                    const double *y, double *out, cudaStream_t st);
+// out[k] = <V_k, w> for the kn vectors V_k = V + k ld (partial: kn x 64
+// scratch), reduced in a fixed order
+void launch_mdot(int n, int kn, const double *V, size_t ld, const double *w,
+                 double *partial, double *out, cudaStream_t st);
+// w -= sum_k h[k] V_k
+void launch_vsub(int n, int kn, const double *V, size_t ld, const double *h,
+                 double *w, cudaStream_t st);
+
 // rr_true = ||b - A x||^2 (FP64 matrix and vectors); x == NULL gives ||b||^2
 void launch_true_residual(const SolverDev &d, const double *val,
                           const double *b, const double *x, double *r,

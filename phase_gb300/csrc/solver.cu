@@ -75,6 +75,9 @@ struct pg_solver {
   // the factorisation (and coarse inverse) matches the current values: a
   // solve after a right-hand-side-only hand-over does not redo it
   bool factored = false;
+  // TFQMR / GMRES work vectors (allocated on first use): three more
+  // vectors, the GMRES basis ((restart + 1) x n), dot-product scratch
+  DevBuf<double> k1, k2, k3, kV, kpart, kdot;
   DevBuf<int> err;
   DevBuf<int32_t> raw_rp, raw_ci, st_rp, st_ci;
   std::vector<double> row_x, row_y;  // pg_solver_set_row_coords hint
@@ -773,6 +776,269 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
   }
 }
 
+// z = M^-1 in for the FP64 preconditioner (permuted order): the Schwarz
+// ILU(0) sweeps or Jacobi, with the coarse correction of the solver's
+// configuration.  in is only read.
+int apply_m64(pg_solver *s, const double *in, double *z) {
+  cudaStream_t st = stream();
+  const SolverDev d = s->dev();
+  double *pin = const_cast<double *>(in);  // mode 0 reads it only
+  if (s->coarse_on && s->coarse_use && s->cfg.coarse == 2) {
+    const CoarseDev c = s->coarse();
+    SolverDev d0 = d;
+    d0.csum = nullptr;
+    launch_def_pre(c, 0, nullptr, pin, nullptr, nullptr, st);
+    launch_def_in(c, d.n, pin, c.tmp, nullptr, st);
+    SolverDev d3 = d0;
+    d3.def_y = c.y;
+    if (!(s->cfg.precond == PG_PREC_ILU0 &&
+          launch_ilu0_apply_def(d3, c.tmp, z, nullptr, st))) {
+      launch_precond<double, double>(s->cfg.precond, 0, d0, s->jdinv.p,
+                                     nullptr, c.tmp, nullptr, z, nullptr, st);
+      launch_coarse_add(c, z, nullptr, st);
+    }
+  } else {
+    SolverDev d1 = d;
+    if (!(s->coarse_on && s->coarse_use)) d1.csum = nullptr;
+    launch_precond<double, double>(s->cfg.precond, 0, d1, s->jdinv.p, nullptr,
+                                   pin, nullptr, z, nullptr, st);
+    if (s->coarse_on && s->coarse_use)
+      launch_coarse_apply(s->coarse(), pin, z,
+                          s->cfg.precond == PG_PREC_ILU0 &&
+                              (d.smem64 > 0 || d.n_lgrp > 0),
+                          nullptr, st);
+  }
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
+// <a, b> in FP64 with a fixed reduction order, read back to the host
+int dot64(pg_solver *s, const double *a, const double *b, double *out) {
+  cudaStream_t st = stream();
+  launch_mdot((int)s->a.n, 1, a, s->a.n, b, s->kpart.p, s->kdot.p, st);
+  PG_CUDA(cudaMemcpyAsync(out, s->kdot.p, sizeof(double),
+                          cudaMemcpyDeviceToHost, st));
+  PG_CUDA(cudaStreamSynchronize(st));
+  return PG_OK;
+}
+
+int krylov_buffers(pg_solver *s, int basis) {
+  const size_t n = s->a.n;
+  for (DevBuf<double> *bf : {&s->k1, &s->k2, &s->k3})
+    PG_CUDA(bf->reserve(n));
+  const int kmax = basis > 0 ? basis : 1;
+  PG_CUDA(s->kpart.reserve((size_t)kmax * 64));
+  PG_CUDA(s->kdot.reserve(kmax));
+  if (basis > 0) PG_CUDA(s->kV.reserve((size_t)basis * n));
+  return PG_OK;
+}
+
+// r = b - A x; returns ||r||^2 (and ||b||^2 in *bb when asked)
+int true_res64(pg_solver *s, double *r, double *rr) {
+  cudaStream_t st = stream();
+  const SolverDev d = s->dev();
+  launch_spmv_plain(d, s->pvals.p, s->x.p, r, st);
+  launch_lincomb(d.n, 1.0, s->b.p, -1.0, r, r, st);
+  return dot64(s, r, r, rr);
+}
+
+// TFQMR (Freund, SIAM J. Sci. Comput. 14, 1993; Saad, Iterative Methods
+// for Sparse Linear Systems, 2nd ed., Alg. 7.8) right-preconditioned as
+// Belos "TFQMR" with the Ifpack2 preconditioner: the iteration runs on
+// A M^-1 and x advances by M^-1 d, carried as dh.  One iteration here is
+// two of the algorithm's half-steps (two products with A M^-1, as one
+// BiCGStab iteration).  Stops when the bound sqrt(m+1) tau reaches the
+// tolerance and the true residual b - A x confirms it.
+int run_tfqmr(pg_solver *s, double tol, int max_iters, int *iters,
+              double *bb_out) {
+  cudaStream_t st = stream();
+  const SolverDev d = s->dev();
+  const int n = d.n;
+  int rc = krylov_buffers(s, 0);
+  if (rc) return rc;
+  double *const x = s->x.p, *const w = s->r.p, *const u = s->rh.p;
+  double *const uh = s->p.p, *const Bu = s->v.p, *const u1 = s->ph.p;
+  double *const uh1 = s->s.p, *const Bu1 = s->sh.p, *const v = s->t.p;
+  double *const dh = s->k1.p, *const rstar = s->k2.p, *const tmp = s->k3.p;
+  double bb = 0., rr = 0.;
+  if ((rc = dot64(s, s->b.p, s->b.p, &bb))) return rc;
+  *bb_out = bb;
+  *iters = 0;
+  if (!std::isfinite(bb)) return PG_NON_FINITE;
+  if (bb == 0.) {
+    PG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), st));
+    return PG_OK;
+  }
+  const double bnorm = std::sqrt(bb);
+  int restarts = 0;
+  for (;;) {  // (re)start from the current x
+    if ((rc = true_res64(s, w, &rr))) return rc;
+    if (!std::isfinite(rr)) return PG_NON_FINITE;
+    if (std::sqrt(rr) <= tol * bnorm) return PG_OK;
+    if (*iters >= max_iters) return PG_MAX_ITERS;
+    PG_CUDA(cudaMemcpyAsync(u, w, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    PG_CUDA(cudaMemcpyAsync(rstar, w, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    PG_CUDA(cudaMemsetAsync(dh, 0, n * sizeof(double), st));
+    if ((rc = apply_m64(s, u, uh))) return rc;
+    launch_spmv_plain(d, s->pvals.p, uh, Bu, st);
+    PG_CUDA(cudaMemcpyAsync(v, Bu, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    double tau = std::sqrt(rr), theta = 0., eta = 0., rho = rr, alpha = 0.;
+    int m = 0;
+    bool restart = false;
+    // one half-step: w -= alpha Bu_m; dh = uh_m + (theta^2 / alpha) eta dh;
+    // x += eta dh; returns 1 when the bound says converged
+    auto half = [&](const double *uh_m, const double *Bu_m, int *done) -> int {
+      launch_lincomb(n, 1.0, w, -alpha, Bu_m, w, st);
+      launch_lincomb(n, 1.0, uh_m, theta * theta / alpha * eta, dh, dh, st);
+      double ww = 0.;
+      int r2 = dot64(s, w, w, &ww);
+      if (r2) return r2;
+      theta = std::sqrt(ww) / tau;
+      const double c = 1.0 / std::sqrt(1.0 + theta * theta);
+      tau = tau * theta * c;
+      eta = c * c * alpha;
+      launch_lincomb(n, 1.0, x, eta, dh, x, st);
+      ++m;
+      *done = tau * std::sqrt((double)m + 1.0) <= tol * bnorm;
+      return PG_OK;
+    };
+    while (*iters < max_iters) {
+      double sigma = 0.;
+      if ((rc = dot64(s, v, rstar, &sigma))) return rc;
+      if (sigma == 0. || rho == 0. || !std::isfinite(sigma)) {
+        restart = true;
+        break;
+      }
+      alpha = rho / sigma;
+      launch_lincomb(n, 1.0, u, -alpha, v, u1, st);          // u_{m+1}
+      int done = 0;
+      if ((rc = half(uh, Bu, &done))) return rc;             // even m
+      if ((rc = apply_m64(s, u1, uh1))) return rc;
+      launch_spmv_plain(d, s->pvals.p, uh1, Bu1, st);
+      if (!done && (rc = half(uh1, Bu1, &done))) return rc;  // odd m
+      ++*iters;
+      if (done) break;
+      double rho_new = 0.;
+      if ((rc = dot64(s, w, rstar, &rho_new))) return rc;
+      const double beta = rho_new / rho;
+      rho = rho_new;
+      launch_lincomb(n, 1.0, w, beta, u1, u, st);            // u = w + beta u1
+      if ((rc = apply_m64(s, u, uh))) return rc;
+      launch_spmv_plain(d, s->pvals.p, uh, tmp, st);         // A M^-1 u
+      // v = A M^-1 u + beta (Bu1 + beta v)
+      launch_lincomb(n, 1.0, Bu1, beta, v, v, st);
+      launch_lincomb(n, 1.0, tmp, beta, v, v, st);
+      PG_CUDA(cudaMemcpyAsync(Bu, tmp, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      if (!std::isfinite(tau)) return PG_NON_FINITE;
+    }
+    if (restart && ++restarts > kMaxRestarts) return PG_BREAKDOWN;
+    // converged by the bound, breakdown or out of iterations: the true
+    // residual decides at the top of the loop
+    if (!restart && *iters >= max_iters) {
+      if ((rc = true_res64(s, w, &rr))) return rc;
+      return std::sqrt(rr) <= tol * bnorm ? PG_OK : PG_MAX_ITERS;
+    }
+  }
+}
+
+// Restarted GMRES (Saad & Schultz, SIAM J. Sci. Stat. Comput. 7, 1986)
+// right-preconditioned as Belos "GMRES": restart length `dim` (Belos' "Num
+// Blocks"), classical Gram-Schmidt applied twice for the orthogonalisation
+// (the dot products of a step in one kernel), Givens rotations on the
+// host, x += M^-1 (V y) at the end of every cycle; convergence is the
+// implicit residual |g_{j+1}| confirmed by the true residual.
+int run_gmres(pg_solver *s, double tol, int max_iters, int dim, int *iters,
+              int *cycles, double *bb_out) {
+  cudaStream_t st = stream();
+  const SolverDev d = s->dev();
+  const int n = d.n;
+  int rc = krylov_buffers(s, dim + 1);
+  if (rc) return rc;
+  double *const x = s->x.p, *const r = s->r.p, *const z = s->ph.p;
+  double *const w = s->t.p, *const hd = s->kdot.p;
+  double *const V = s->kV.p;
+  double bb = 0., rr = 0.;
+  if ((rc = dot64(s, s->b.p, s->b.p, &bb))) return rc;
+  *bb_out = bb;
+  *iters = 0;
+  *cycles = 0;
+  if (!std::isfinite(bb)) return PG_NON_FINITE;
+  if (bb == 0.) {
+    PG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), st));
+    return PG_OK;
+  }
+  const double bnorm = std::sqrt(bb);
+  std::vector<double> H((size_t)(dim + 1) * dim, 0.), cs(dim), sn(dim),
+      g(dim + 1), h(dim + 1), h2(dim + 1), y(dim);
+  for (;;) {
+    if ((rc = true_res64(s, r, &rr))) return rc;
+    if (!std::isfinite(rr)) return PG_NON_FINITE;
+    const double beta = std::sqrt(rr);
+    if (beta <= tol * bnorm) return PG_OK;
+    if (*iters >= max_iters) return PG_MAX_ITERS;
+    ++*cycles;
+    launch_lincomb(n, 1.0 / beta, r, 0.0, nullptr, V, st);
+    std::fill(g.begin(), g.end(), 0.);
+    g[0] = beta;
+    int j = 0;
+    for (; j < dim && *iters < max_iters; ++j) {
+      double *vj = V + (size_t)j * n;
+      if ((rc = apply_m64(s, vj, z))) return rc;
+      launch_spmv_plain(d, s->pvals.p, z, w, st);
+      // two passes of classical Gram-Schmidt against v_0 .. v_j
+      for (int pass = 0; pass < 2; ++pass) {
+        launch_mdot(n, j + 1, V, n, w, s->kpart.p, hd, st);
+        PG_CUDA(cudaMemcpyAsync(pass ? h2.data() : h.data(), hd,
+                                (j + 1) * sizeof(double),
+                                cudaMemcpyDeviceToHost, st));
+        launch_vsub(n, j + 1, V, n, hd, w, st);
+      }
+      double ww = 0.;
+      if ((rc = dot64(s, w, w, &ww))) return rc;  // also waits for h, h2
+      for (int i = 0; i <= j; ++i) h[i] += h2[i];
+      h[j + 1] = std::sqrt(ww);
+      ++*iters;
+      if (!std::isfinite(h[j + 1])) return PG_NON_FINITE;
+      if (h[j + 1] > 0.)
+        launch_lincomb(n, 1.0 / h[j + 1], w, 0.0, nullptr, V + (size_t)(j + 1) * n, st);
+      // apply the previous rotations to the new column, then its own
+      for (int i = 0; i < j; ++i) {
+        const double t = cs[i] * h[i] + sn[i] * h[i + 1];
+        h[i + 1] = -sn[i] * h[i] + cs[i] * h[i + 1];
+        h[i] = t;
+      }
+      const double den = std::hypot(h[j], h[j + 1]);
+      cs[j] = den > 0. ? h[j] / den : 1.;
+      sn[j] = den > 0. ? h[j + 1] / den : 0.;
+      h[j] = den;
+      h[j + 1] = 0.;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = cs[j] * g[j];
+      for (int i = 0; i <= j; ++i) H[(size_t)i * dim + j] = h[i];
+      if (std::fabs(g[j + 1]) <= tol * bnorm || den == 0.) {
+        ++j;
+        break;
+      }
+    }
+    // y = H^-1 g (upper triangular, j columns); x += M^-1 (V y)
+    for (int i = j - 1; i >= 0; --i) {
+      double acc = g[i];
+      for (int k = i + 1; k < j; ++k) acc -= H[(size_t)i * dim + k] * y[k];
+      const double hii = H[(size_t)i * dim + i];
+      y[i] = hii != 0. ? acc / hii : 0.;
+    }
+    PG_CUDA(cudaMemsetAsync(w, 0, n * sizeof(double), st));
+    // w = V y, as w -= V (-y)
+    for (int i = 0; i < j; ++i) y[i] = -y[i];
+    PG_CUDA(cudaMemcpyAsync(hd, y.data(), j * sizeof(double),
+                            cudaMemcpyHostToDevice, st));
+    launch_vsub(n, j, V, n, hd, w, st);
+    if ((rc = apply_m64(s, w, z))) return rc;
+    launch_lincomb(n, 1.0, x, 1.0, z, x, st);
+    PG_CUDA(cudaStreamSynchronize(st));
+  }
+}
+
 bool use_dd(const pg_solver *s) {
   const SolverDev d = s->dev();
   return s->cfg.precision == PG_MIXED &&
@@ -942,8 +1208,10 @@ extern "C" int pg_solver_create(const pg_solver_cfg *cfg, pg_solver **out) {
                "pg_solver_create: bad mixed_sweep");
   PG_CHECK_ARG(c.coarse >= 0 && c.coarse <= 2, "pg_solver_create: bad coarse");
   PG_CHECK_ARG(c.coarse_warm >= -2, "pg_solver_create: bad coarse_warm");
-  PG_CHECK_ARG(c.krylov == PG_KRYLOV_BICGSTAB,
-               "pg_solver_create: only BiCGStab is built");
+  PG_CHECK_ARG(c.krylov >= PG_KRYLOV_BICGSTAB && c.krylov <= PG_KRYLOV_GMRES,
+               "pg_solver_create: bad krylov");
+  PG_CHECK_ARG(c.krylov == PG_KRYLOV_BICGSTAB || c.precision == PG_FP64,
+               "pg_solver_create: TFQMR and GMRES run in FP64");
   PG_CHECK_ARG(c.ilu_fill == 0,
                "pg_solver_create: only ILU(0) blocks are built (ilu_fill 0)");
   PG_CHECK_ARG(c.krylov_dim >= 0, "pg_solver_create: bad krylov_dim");
@@ -1207,6 +1475,14 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
   int fp64_iters = 0;  // FP64 iterations after a float-float hand-over
   const bool dd = use_dd(s);
   auto run = [&](int max_iters, int *it, int *up) {
+    if (s->cfg.krylov == PG_KRYLOV_TFQMR) {
+      *up = 0;
+      return run_tfqmr(s, tol, max_iters, it, &bb);
+    }
+    if (s->cfg.krylov == PG_KRYLOV_GMRES)
+      return run_gmres(s, tol, max_iters,
+                       s->cfg.krylov_dim > 0 ? s->cfg.krylov_dim : 300, it, up,
+                       &bb);
     return dd ? run_bicgstab_dd(s, tol, max_iters, it, up, &bb)
               : run_bicgstab(s, tol, max_iters, it, up, &bb);
   };

@@ -28,7 +28,8 @@ class OrCfg(ctypes.Structure):
                 ("precond", ctypes.c_int), ("ilut_drop", D),
                 ("ilut_fill", ctypes.c_int), ("n_threads", ctypes.c_int),
                 ("part", P), ("n_parts", ctypes.c_int),
-                ("use_guess", ctypes.c_int), ("coarse", ctypes.c_int)]
+                ("use_guess", ctypes.c_int), ("coarse", ctypes.c_int),
+                ("krylov", ctypes.c_int), ("krylov_dim", ctypes.c_int)]
 
 
 class OrStats(ctypes.Structure):
@@ -250,7 +251,7 @@ class OracleMesh:
 
 def bicgstab(rp, ci, v, b, tol=1e-8, max_iters=500, precond=OR_PREC_ILU0,
              part=None, x0=None, threads=0, ilut_drop=1e-4, ilut_fill=10,
-             coarse=0):
+             coarse=0, krylov=0, krylov_dim=0):
     """Oracle BiCGStab solve; returns (x, stats dict)."""
     rp = np.ascontiguousarray(rp, np.int32)
     ci = np.ascontiguousarray(ci, np.int32)
@@ -263,7 +264,8 @@ def bicgstab(rp, ci, v, b, tol=1e-8, max_iters=500, precond=OR_PREC_ILU0,
                 ilut_drop=ilut_drop, ilut_fill=ilut_fill, n_threads=threads,
                 part=None if pa is None else pa.ctypes.data,
                 n_parts=0 if pa is None else int(pa.max()) + 1,
-                use_guess=0 if x0 is None else 1, coarse=coarse)
+                use_guess=0 if x0 is None else 1, coarse=coarse,
+                krylov=krylov, krylov_dim=krylov_dim)
     st = OrStats()
     lib().or_bicgstab(n, ptr(rp), ptr(ci), ptr(v), ptr(b), ptr(x),
                       ctypes.byref(cfg), ctypes.byref(st))

@@ -385,3 +385,28 @@ def test_two_level_oracle_converges_in_fewer_iterations(oracle, coarse):
         assert np.linalg.norm(-rhs - A @ x) / np.linalg.norm(rhs) <= 1.01e-8
         its[c] = st["iters"]
     assert its[coarse] < 0.5 * its[0], its
+
+
+@pytest.mark.parametrize("krylov", [1, 2])
+def test_oracle_tfqmr_and_gmres_solve(oracle, krylov):
+    """The oracle's TFQMR and GMRES (Belos' other solvers in Phase's cases)
+    with the Schwarz ILU(0) right preconditioner reach the tolerance on the
+    true residual, and agree with scipy's direct solve."""
+    nodes, cptr, cind = meshes.triangulated(30, 24, 1.0, 1.0, jitter=0.2,
+                                            seed=3)
+    om = oracle.OracleMesh(nodes, cptr, cind)
+    f = om.faces()
+    bc = np.where(f["rcell"] < 0, 0, 1).astype(np.int32)
+    rng = np.random.default_rng(4)
+    rp, ci, v, rhs = om.laplacian(rng.uniform(1, 3, om.n_faces), bc,
+                                  np.zeros(om.n_faces),
+                                  rng.standard_normal((om.n_faces, 2)))
+    n = len(rp) - 1
+    part = (np.arange(n) * 4 // n).astype(np.int32)
+    x, st = oracle.bicgstab(rp, ci, v, -rhs, tol=1e-10, max_iters=2000,
+                            part=part, krylov=krylov, krylov_dim=30)
+    A = sp.csr_matrix((v, ci, rp))
+    assert st["status"] == 0, st
+    assert np.linalg.norm(-rhs - A @ x) / np.linalg.norm(rhs) <= 1.01e-10
+    xd = spla.spsolve(A.tocsc(), -rhs)
+    assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-8
