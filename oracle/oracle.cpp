@@ -545,6 +545,121 @@ struct Ilu0 {
   }
 };
 
+// ILU(k) by levels of fill (Saad, Iterative Methods for Sparse Linear
+// Systems, 2nd ed., sec. 10.3.3; Ifpack2 RILUK with "fact: iluk
+// level-of-fill" k) on the diagonal blocks of a row partition: rows of a
+// subdomain in increasing index, A's entries at level 0, a fill entry
+// (i, j) at level lev(i,m) + lev(m,j) + 1 for m < i in row i and j > m in
+// row m, kept when at most k; then the IKJ elimination on that pattern.
+struct IluK {
+  int64_t n = 0;
+  std::vector<int64_t> rp, diag;
+  std::vector<int32_t> ci;
+  std::vector<double> v;
+  std::vector<std::vector<int32_t>> groups;
+  int status = 0;
+
+  void build(const Csr &A, const int32_t *part, int n_parts, int p) {
+    n = A.n;
+    if (part) {
+      groups.assign(n_parts, {});
+      for (int64_t i = 0; i < n; ++i) groups[part[i]].push_back((int32_t)i);
+    } else {
+      groups.assign(1, {});
+      for (int64_t i = 0; i < n; ++i) groups[0].push_back((int32_t)i);
+    }
+    // symbolic, per subdomain in row order; rows[i] = (column, level)
+    std::vector<std::vector<std::pair<int32_t, int32_t>>> rows(n);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t gi = 0; gi < (int64_t)groups.size(); ++gi) {
+      std::map<int32_t, int32_t> lev;
+      for (int32_t i : groups[gi]) {
+        lev.clear();
+        lev[i] = 0;
+        for (int32_t j = A.rp[i]; j < A.rp[i + 1]; ++j)
+          if (!part || part[A.ci[j]] == part[i]) lev[A.ci[j]] = 0;
+        // keys inserted below are larger than the current one, so the
+        // walk visits every lower entry, fill included, in increasing order
+        for (auto it = lev.begin(); it != lev.end() && it->first < i; ++it) {
+          const int32_t lim = it->second;
+          for (const auto &e : rows[it->first]) {
+            if (e.first <= it->first) continue;
+            const int32_t lnew = lim + e.second + 1;
+            if (lnew > p) continue;
+            auto f = lev.find(e.first);
+            if (f == lev.end()) lev.emplace(e.first, lnew);
+            else if (lnew < f->second) f->second = lnew;
+          }
+        }
+        rows[i].assign(lev.begin(), lev.end());
+      }
+    }
+    rp.assign(n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) rp[i + 1] = rp[i] + (int64_t)rows[i].size();
+    ci.resize(rp[n]);
+    v.assign(rp[n], 0.);
+    diag.assign(n, -1);
+    for (int64_t i = 0; i < n; ++i) {
+      for (size_t q = 0; q < rows[i].size(); ++q) {
+        ci[rp[i] + q] = rows[i][q].first;
+        if (rows[i][q].first == i) diag[i] = rp[i] + (int64_t)q;
+      }
+      for (int32_t j = A.rp[i]; j < A.rp[i + 1]; ++j) {
+        if (part && part[A.ci[j]] != part[i]) continue;
+        const auto b = ci.begin() + rp[i], e = ci.begin() + rp[i + 1];
+        v[std::lower_bound(b, e, A.ci[j]) - ci.begin()] += A.v[j];
+      }
+    }
+    // numeric IKJ on the pattern
+    int bad = 0;
+#pragma omp parallel reduction(+ : bad)
+    {
+      std::vector<int64_t> pos(n, -1);
+#pragma omp for schedule(dynamic, 1)
+      for (int64_t gi = 0; gi < (int64_t)groups.size(); ++gi) {
+        for (int32_t i : groups[gi]) {
+          for (int64_t j = rp[i]; j < rp[i + 1]; ++j) pos[ci[j]] = j;
+          for (int64_t j = rp[i]; j < rp[i + 1] && ci[j] < i; ++j) {
+            const int32_t m = ci[j];
+            const double umm = v[diag[m]];
+            if (umm == 0.) {
+              ++bad;
+              continue;
+            }
+            const double l = v[j] / umm;
+            v[j] = l;
+            for (int64_t q = diag[m] + 1; q < rp[m + 1]; ++q) {
+              const int64_t pq = pos[ci[q]];
+              if (pq >= 0) v[pq] -= l * v[q];
+            }
+          }
+          for (int64_t j = rp[i]; j < rp[i + 1]; ++j) pos[ci[j]] = -1;
+          if (v[diag[i]] == 0. || !std::isfinite(v[diag[i]])) ++bad;
+        }
+      }
+    }
+    status = bad ? 2 : 0;
+  }
+
+  void apply(const double *r, double *z) const {
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t g = 0; g < (int64_t)groups.size(); ++g) {
+      const auto &gr = groups[g];
+      for (int32_t i : gr) {
+        double s = r[i];
+        for (int64_t j = rp[i]; j < diag[i]; ++j) s -= v[j] * z[ci[j]];
+        z[i] = s;
+      }
+      for (auto it = gr.rbegin(); it != gr.rend(); ++it) {
+        const int32_t i = *it;
+        double s = z[i];
+        for (int64_t j = diag[i] + 1; j < rp[i + 1]; ++j) s -= v[j] * z[ci[j]];
+        z[i] = s / v[diag[i]];
+      }
+    }
+  }
+};
+
 // ILUT(p, tau): dual-threshold incomplete LU (Saad, "ILUT: a dual threshold
 // incomplete LU factorization", Numer. Linear Algebra Appl. 1 (1994);
 // Iterative Methods for Sparse Linear Systems, Alg. 10.6).  Row i is
@@ -765,6 +880,8 @@ struct Coarse {
 struct Precond {
   int kind = OR_PREC_NONE;
   Ilu0 ilu0;
+  IluK iluk;
+  int fill = 0;
   Ilut ilut;
   std::vector<double> dinv;
   int status = 0;
@@ -779,7 +896,11 @@ struct Precond {
     coarse = cfg.part && cfg.n_parts > 1 ? cfg.coarse : 0;
     if (coarse) cs.build(A, cfg.part, cfg.n_parts);
     kind = cfg.precond;
-    if (kind == OR_PREC_ILU0) {
+    fill = kind == OR_PREC_ILU0 ? cfg.ilu_fill : 0;
+    if (kind == OR_PREC_ILU0 && fill > 0) {
+      iluk.build(A, cfg.part, cfg.n_parts, fill);
+      status = iluk.status;
+    } else if (kind == OR_PREC_ILU0) {
       ilu0.build(A, cfg.part, cfg.n_parts);
       status = ilu0.status;
     } else if (kind == OR_PREC_ILUT) {
@@ -819,7 +940,10 @@ struct Precond {
   }
   void apply_one(int64_t n, const double *r, double *z) const {
     switch (kind) {
-    case OR_PREC_ILU0: ilu0.apply(r, z); break;
+    case OR_PREC_ILU0:
+      if (fill > 0) iluk.apply(r, z);
+      else ilu0.apply(r, z);
+      break;
     case OR_PREC_ILUT: ilut.apply(r, z); break;
     case OR_PREC_JACOBI:
 #pragma omp parallel for schedule(static)
@@ -1183,6 +1307,21 @@ extern "C" int or_bicgstab_history(int64_t n, const int32_t *row_ptr,
                                    double *setup_ms_out) {
   return or_bicgstab_history_x0(n, row_ptr, col_ind, vals, b, nullptr, cfg,
                                 hist, ms_out, setup_ms_out);
+}
+
+extern "C" int or_iluk_apply(int64_t n, const int32_t *row_ptr,
+                             const int32_t *col_ind, const double *vals,
+                             const int32_t *part, int fill, const double *r,
+                             double *z) {
+  Csr A{n, row_ptr, col_ind, vals};
+  int np = 0;
+  if (part)
+    for (int64_t i = 0; i < n; ++i) np = std::max(np, part[i] + 1);
+  IluK f;
+  f.build(A, part, np, fill);
+  if (f.status) return f.status;
+  f.apply(r, z);
+  return 0;
 }
 
 extern "C" int or_ilu0(int64_t n, const int32_t *row_ptr,

@@ -114,6 +114,8 @@ typedef struct {
   int krylov;          /* 0 BiCGStab, 1 TFQMR, 2 GMRES (Belos "solver",
                           TrilinosBelosSparseMatrixSolver.cpp:59-60) */
   int krylov_dim;      /* GMRES restart length (0 = 300, Belos' default) */
+  int ilu_fill;        /* OR_PREC_ILU0 blocks: level of fill k (ILU(k),
+                          Ifpack2 RILUK "fact: iluk level-of-fill") */
 } or_solver_cfg;
 
 typedef struct {
@@ -146,6 +148,13 @@ int or_bicgstab_history_x0(int64_t n, const int32_t *row_ptr,
                            const double *b, const double *x0,
                            const or_solver_cfg *cfg, double *hist,
                            double *ms_out, double *setup_ms_out);
+
+/* z = (LU)^-1 r with the ILU(k) factor (level of fill k) of each subdomain
+ * (part, or one subdomain when NULL) of a compact CSR; returns 0, or 2 on a
+ * zero pivot. */
+int or_iluk_apply(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
+                  const double *vals, const int32_t *part, int fill,
+                  const double *r, double *z);
 
 /* ILU(0) factor in place on a compact CSR (per subdomain when part given);
  * out_vals receives the L (unit, strictly lower) and U values in the CSR

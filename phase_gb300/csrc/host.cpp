@@ -7,6 +7,7 @@
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <numeric>
 #include <string>
 #include <tuple>
@@ -319,6 +320,52 @@ struct Bisector {
 
 }  // namespace
 
+// ILU(k) pattern of one subdomain by levels of fill (Saad, Iterative
+// Methods for Sparse Linear Systems, 2nd ed., sec. 10.3.3; Ifpack2 RILUK's
+// "fact: iluk level-of-fill"): rows in increasing index, the entries of A
+// inside the subdomain at level 0, and a fill entry (i, j) at level
+// lev(i,k) + lev(k,j) + 1 for every k < i in row i's pattern and j > k in
+// row k's; entries above level p are dropped.  out[r] receives row r's
+// columns (original ids, ascending, diagonal included) for every r in rows.
+static void iluk_pattern(const std::vector<int32_t> &rows, int s,
+                         const std::vector<int64_t> &cp,
+                         const std::vector<int32_t> &cc,
+                         const std::vector<int32_t> &part, int p,
+                         std::vector<std::vector<int32_t>> &out) {
+  const size_t nr = rows.size();
+  auto local = [&](int32_t r) {
+    return (int32_t)(std::lower_bound(rows.begin(), rows.end(), r) - rows.begin());
+  };
+  // per local row: its U part (local col > row) with levels, for later rows
+  std::vector<std::vector<std::pair<int32_t, int32_t>>> upart(nr);
+  std::map<int32_t, int32_t> lev;  // local col -> level
+  for (size_t i = 0; i < nr; ++i) {
+    lev.clear();
+    const int32_t r = rows[i];
+    lev[(int32_t)i] = 0;
+    for (int64_t k = cp[r]; k < cp[r + 1]; ++k)
+      if (part[cc[k]] == s) lev[local(cc[k])] = 0;
+    for (auto it = lev.begin(); it != lev.end() && it->first < (int32_t)i; ++it) {
+      const int32_t k = it->first, lik = it->second;
+      if (lik > p) continue;
+      for (const auto &e : upart[k]) {
+        const int32_t lnew = lik + e.second + 1;
+        if (lnew > p) continue;
+        auto f = lev.find(e.first);
+        if (f == lev.end()) lev.emplace(e.first, lnew);
+        else if (lnew < f->second) f->second = lnew;
+      }
+    }
+    std::vector<int32_t> &cols = out[r];
+    cols.clear();
+    for (const auto &e : lev) {
+      if (e.second > p) continue;
+      cols.push_back(rows[e.first]);
+      if (e.first > (int32_t)i) upart[i].push_back(e);
+    }
+  }
+}
+
 // Grid coordinates of a subdomain that is a rectangular block of a
 // structured grid with a 5-point pattern: every in-subdomain neighbour of a
 // row is one level before or after it and is the row's neighbour along one
@@ -424,7 +471,7 @@ static int grid_block(const std::vector<int32_t> &rows, int s,
 int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
             int subdomain_rows, Analysis &a,
             const std::vector<int64_t> *sys_rows, const double *cx,
-            const double *cy) {
+            const double *cy, int fill) {
   PG_CHECK_ARG(n > 0 && row_ptr && col_ind, "analyse: empty matrix");
   PG_CHECK_ARG(row_ptr[0] == 0, "row_ptr[0] must be 0");
   for (int64_t i = 0; i < n; ++i)
@@ -605,6 +652,9 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   std::vector<int32_t> level(n, 0);
   std::vector<int32_t> gline, gpos;  // grid coordinates of line-form rows
   std::vector<int32_t> sub_lines(a.n_sub, 0);  // lines per block, 0 = none
+  // ILU(k): each row's filled pattern (original column ids)
+  std::vector<std::vector<int32_t>> fill_cols(fill > 0 ? n : 0),
+      fill_dep(fill > 0 ? n : 0);
   const bool want_line = !sys_rows && [] {
     const char *e = std::getenv("PG_LINE");
     return !(e && e[0] == '0');
@@ -623,16 +673,32 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
                               order.begin() + parts[s].second);
     std::sort(rows.begin(), rows.end());
     int32_t nl = 0;
+    if (fill > 0) {
+      iluk_pattern(rows, s, cp, cc, a.part, fill, fill_cols);
+      // the filled pattern in both directions (it need not be symmetric):
+      // a row comes after every earlier row it is coupled to, so the level
+      // order keeps the original order of every coupled pair
+      for (int32_t r : rows) fill_dep[r].clear();
+      for (int32_t r : rows)
+        for (int32_t c : fill_cols[r])
+          if (c > r) fill_dep[c].push_back(r);
+    }
     for (int32_t i : rows) {
       int32_t lv = 0;
-      for (int64_t k = ap[i]; k < ap[i + 1]; ++k) {
-        const int32_t j = aj[k];
-        if (j < i && a.part[j] == s) lv = std::max(lv, level[j] + 1);
+      if (fill > 0) {  // the filled pattern decides the schedule
+        for (int32_t j : fill_cols[i])
+          if (j < i) lv = std::max(lv, level[j] + 1);
+        for (int32_t j : fill_dep[i]) lv = std::max(lv, level[j] + 1);
+      } else {
+        for (int64_t k = ap[i]; k < ap[i + 1]; ++k) {
+          const int32_t j = aj[k];
+          if (j < i && a.part[j] == s) lv = std::max(lv, level[j] + 1);
+        }
       }
       level[i] = lv;
       nl = std::max(nl, lv + 1);
     }
-    if (want_line)
+    if (want_line && fill == 0)
       sub_lines[s] = grid_block(rows, s, level, ap, aj, a.part, gline, gpos);
     if (sub_lines[s] > 0)
       std::stable_sort(rows.begin(), rows.end(), [&](int32_t x, int32_t y) {
@@ -734,10 +800,29 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   a.ldg.assign(n, -1);
   a.lci.clear();
   a.lsrc.clear();
+  std::vector<std::pair<int32_t, int32_t>> frow;  // (permuted col, entry)
   for (int s = 0; s < a.n_sub; ++s) {
     const int32_t r0 = a.sub_ptr[s], r1 = a.sub_ptr[s + 1];
     const int64_t e0 = (int64_t)a.lci.size();
-    for (int32_t i = r0; i < r1; ++i) {
+    for (int32_t i = r0; i < r1 && fill > 0; ++i) {
+      // ILU(k): the filled pattern, each entry with its permuted-CSR source
+      // (-1 for fill, which starts at zero)
+      frow.clear();
+      for (int32_t c : fill_cols[a.perm[i]]) frow.push_back({a.iperm[c], -1});
+      std::sort(frow.begin(), frow.end());
+      for (int32_t k = a.prp[i]; k < a.prp[i + 1]; ++k) {
+        auto it = std::lower_bound(frow.begin(), frow.end(),
+                                   std::make_pair(a.pci[k], INT32_MIN));
+        if (it != frow.end() && it->first == a.pci[k]) it->second = k;
+      }
+      for (const auto &e : frow) {
+        if (e.first == i) a.ldg[i] = (int32_t)a.lci.size();
+        a.lci.push_back(e.first - r0);
+        a.lsrc.push_back(e.second);
+      }
+      a.lrp[i + 1] = (int32_t)a.lci.size();
+    }
+    for (int32_t i = r0; i < r1 && fill == 0; ++i) {
       bool have_diag = false;
       for (int32_t k = a.prp[i]; k < a.prp[i + 1]; ++k) {
         const int32_t c = a.pci[k];

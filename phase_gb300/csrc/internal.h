@@ -255,9 +255,11 @@ constexpr int64_t kStreamPiece = 6144;
 // longer extent instead of by graph distance, which gives compact
 // subdomains with short level schedules (a 32 x 32 block of a structured
 // grid has 63 levels).
+// fill: level of fill k of the ILU(k) blocks (0: ILU(0)).
 int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
             int subdomain_rows, Analysis &a,
             const std::vector<int64_t> *sys_rows = nullptr,
-            const double *cx = nullptr, const double *cy = nullptr);
+            const double *cx = nullptr, const double *cy = nullptr,
+            int fill = 0);
 
 }  // namespace pg

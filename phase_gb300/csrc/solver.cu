@@ -304,6 +304,11 @@ int subdomain_rows_for(const pg_solver_cfg &c, int64_t n) {
   return (int)std::max<int64_t>(512, (n + kMaxCoarseK - 1) / kMaxCoarseK);
 }
 
+// level of fill of the ILU blocks (ILU preconditioner only)
+int ilu_fill_of(const pg_solver_cfg &c) {
+  return c.precond == PG_PREC_ILU0 ? c.ilu_fill : 0;
+}
+
 int upload_analysis(pg_solver *s) {
   if (s->fact_pending || s->coarse_pending) {  // buffers are about to move
     PG_CUDA(cudaStreamSynchronize(s->side));
@@ -1212,8 +1217,8 @@ extern "C" int pg_solver_create(const pg_solver_cfg *cfg, pg_solver **out) {
                "pg_solver_create: bad krylov");
   PG_CHECK_ARG(c.krylov == PG_KRYLOV_BICGSTAB || c.precision == PG_FP64,
                "pg_solver_create: TFQMR and GMRES run in FP64");
-  PG_CHECK_ARG(c.ilu_fill == 0,
-               "pg_solver_create: only ILU(0) blocks are built (ilu_fill 0)");
+  PG_CHECK_ARG(c.ilu_fill >= 0 && c.ilu_fill <= 8,
+               "pg_solver_create: ilu_fill must be 0 .. 8");
   PG_CHECK_ARG(c.krylov_dim >= 0, "pg_solver_create: bad krylov_dim");
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0 || !stream()) {
@@ -1329,7 +1334,7 @@ extern "C" int pg_solver_set_csr(pg_solver *s, const int32_t *row_ptr,
     const bool xy = (int64_t)s->row_x.size() == n;
     int rc = analyse(n, hrp, hci, subdomain_rows_for(s->cfg, n), s->a,
                      nullptr, xy ? s->row_x.data() : nullptr,
-                     xy ? s->row_y.data() : nullptr);
+                     xy ? s->row_y.data() : nullptr, ilu_fill_of(s->cfg));
     if (rc) return rc;
     rc = upload_analysis(s);
     if (rc) return rc;
@@ -1377,7 +1382,7 @@ static int set_eqn(pg_solver *s, const pg_eqn *e, int component, bool reuse) {
     int rc = analyse(e->p.n, e->p.row_ptr.data(), e->p.col_ind.data(),
                      subdomain_rows_for(s->cfg, e->p.n), s->a,
                      nullptr, xy ? hm.cx.data() : nullptr,
-                     xy ? hm.cy.data() : nullptr);
+                     xy ? hm.cy.data() : nullptr, ilu_fill_of(s->cfg));
     if (rc) return rc;
     rc = upload_analysis(s);
     if (rc) return rc;
@@ -1961,7 +1966,7 @@ int batch_analyse(pg_batch *b, const std::vector<int32_t> &rp,
                        : s->cfg.coarse           ? 512
                                                  : 1024;
   int rc = analyse(n, rp.data(), ci.data(), sub_rows, s->a, &b->sys_rows, cx,
-                   cy);
+                   cy, ilu_fill_of(s->cfg));
   if (rc) return rc;
   s->rank = n;
   rc = upload_analysis(s);

@@ -29,7 +29,8 @@ class OrCfg(ctypes.Structure):
                 ("ilut_fill", ctypes.c_int), ("n_threads", ctypes.c_int),
                 ("part", P), ("n_parts", ctypes.c_int),
                 ("use_guess", ctypes.c_int), ("coarse", ctypes.c_int),
-                ("krylov", ctypes.c_int), ("krylov_dim", ctypes.c_int)]
+                ("krylov", ctypes.c_int), ("krylov_dim", ctypes.c_int),
+                ("ilu_fill", ctypes.c_int)]
 
 
 class OrStats(ctypes.Structure):
@@ -85,6 +86,7 @@ def lib():
         L.or_ilu0.argtypes = [I64, P, P, P, P, P]
         L.or_ilu0_apply.argtypes = [I64, P, P, P, P, P, P]
         L.or_spmv.argtypes = [I64, P, P, P, P, P]
+        L.or_iluk_apply.argtypes = [I64, P, P, P, P, ctypes.c_int, P, P]
         L.or_momentum.restype = P
         L.or_momentum.argtypes = [P, D, D, D, P, P, P]
         L.or_correct_velocity.argtypes = [P, D, P, P, P, P, P, P]
@@ -251,7 +253,7 @@ class OracleMesh:
 
 def bicgstab(rp, ci, v, b, tol=1e-8, max_iters=500, precond=OR_PREC_ILU0,
              part=None, x0=None, threads=0, ilut_drop=1e-4, ilut_fill=10,
-             coarse=0, krylov=0, krylov_dim=0):
+             coarse=0, krylov=0, krylov_dim=0, ilu_fill=0):
     """Oracle BiCGStab solve; returns (x, stats dict)."""
     rp = np.ascontiguousarray(rp, np.int32)
     ci = np.ascontiguousarray(ci, np.int32)
@@ -265,7 +267,7 @@ def bicgstab(rp, ci, v, b, tol=1e-8, max_iters=500, precond=OR_PREC_ILU0,
                 part=None if pa is None else pa.ctypes.data,
                 n_parts=0 if pa is None else int(pa.max()) + 1,
                 use_guess=0 if x0 is None else 1, coarse=coarse,
-                krylov=krylov, krylov_dim=krylov_dim)
+                krylov=krylov, krylov_dim=krylov_dim, ilu_fill=ilu_fill)
     st = OrStats()
     lib().or_bicgstab(n, ptr(rp), ptr(ci), ptr(v), ptr(b), ptr(x),
                       ctypes.byref(cfg), ctypes.byref(st))
@@ -314,6 +316,19 @@ def ilu0_apply(rp, ci, lu, r, part=None):
                         ptr(np.ascontiguousarray(lu, np.float64)), ptr(pa),
                         ptr(np.ascontiguousarray(r, np.float64)), ptr(z))
     return z
+
+
+def iluk_apply(rp, ci, v, r, fill, part=None):
+    """z = (LU)^-1 r with the level-of-fill ILU(k) factor of each subdomain
+    (natural row order); returns (z, status)."""
+    z = np.zeros(len(rp) - 1)
+    pa = None if part is None else np.ascontiguousarray(part, np.int32)
+    rc = lib().or_iluk_apply(len(rp) - 1, ptr(np.ascontiguousarray(rp, np.int32)),
+                             ptr(np.ascontiguousarray(ci, np.int32)),
+                             ptr(np.ascontiguousarray(v, np.float64)), ptr(pa),
+                             int(fill), ptr(np.ascontiguousarray(r, np.float64)),
+                             ptr(z))
+    return z, rc
 
 
 def spmv(rp, ci, v, x):
