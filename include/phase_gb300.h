@@ -143,8 +143,10 @@ int pg_correct_velocity(const pg_mesh *m, double dt, const double *rho_cell,
  * over the fluid cells; IB rows carry the bilinear image-point stencils of
  * GhostCellImmersedBoundary::bcs (:32-74) for ib_bc PG_BC_FIXED or
  * PG_BC_NORMAL_GRADIENT with value ib_ref, solid rows the identity.  The
- * IB rows are built once on the host (they depend on geometry only) and
- * the device assembly (pg_assemble_laplacian) fills the fluid rows.  The
+ * classes and the IB stencils (boundary point, image point, the cells of
+ * the node nearest to it, the 4x4 inverse) are built on the device; the
+ * host builds the pattern from them, and the device assembly
+ * (pg_assemble_laplacian) fills the fluid rows.  The
  * sum is CrsEquation::operator+ (CrsEquation.cpp:185-229), which leaves out
  * entries that are exactly zero: the device matrix keeps their slots (with
  * value 0, the same operator), and pg_eqn_export drops them, so the
@@ -154,6 +156,22 @@ int pg_correct_velocity(const pg_mesh *m, double dt, const double *rho_cell,
 int pg_eqn_create_gcib(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
                        int n_circles, const double *circles, int ib_bc,
                        double ib_ref, pg_eqn **out);
+/* Moves the bodies of a ghost-cell IB equation: circles[3k..3k+2] are the
+ * new (cx, cy, r), ib_ref the new boundary value, as
+ * GhostCellImmersedBoundary::updateCells after the bodies' Motion::update
+ * (FractionalStepDFIB.cpp:29-31 does both every step; OscillatingMotion.cpp:
+ * 12-24 is one motion).  Classes and stencils are rebuilt on the device.
+ * When every cell keeps its class and every IB row its non-zero columns,
+ * the new IB rows are written into the equation's constant rows on the
+ * device and *pattern_changed = 0: the pattern, and a solver's analysis of
+ * it, stay valid.  Otherwise the equation is rebuilt with the new pattern
+ * (a new pattern: a solver given it re-analyses) and *pattern_changed = 1.
+ * Either way the next pg_assemble_laplacian assembles the moved equation.
+ * Fails with PG_BAD_ARG for an equation without an IB, or as
+ * pg_eqn_create_gcib (the equation is then unchanged, except after a
+ * failure of the rebuild itself, after which it must be destroyed). */
+int pg_eqn_update_gcib(pg_eqn *e, int n_circles, const double *circles,
+                       double ib_ref, int *pattern_changed);
 /* Cell classes of a ghost-cell IB equation: 0 fluid, 1 IB, 2 solid (all 0
  * for other equations).  cls[n_rows]. */
 int pg_eqn_cell_class(const pg_eqn *e, int32_t *cls);

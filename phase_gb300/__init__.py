@@ -81,6 +81,7 @@ PROTOTYPES = {
     "pg_set_boundary_faces": (_I, [_P, _P, _P, _P, _I]),
     "pg_eqn_create_gcib": (_I, [_P, _I, _P, _I, _P, _I, _D, ctypes.POINTER(_P)]),
     "pg_eqn_cell_class": (_I, [_P, _P]),
+    "pg_eqn_update_gcib": (_I, [_P, _I, _P, _D, _P]),
     "pg_eqn_create_momentum": (_I, [_P, _P, ctypes.POINTER(_P)]),
     "pg_assemble_momentum": (_I, [_P, _D, _D, _D, _P, _P, _I]),
     "pg_interpolate_faces": (_I, [_P, _P, _P, _I]),
@@ -335,6 +336,21 @@ class Equation:
             self._h, _P(gamma_face or None), gamma_scalar,
             _P(bc_value or None), _P(u_face or None), PG_DEVICE))
         return self
+
+    def move_ib(self, circles, ib_ref=0.0) -> bool:
+        """GhostCellImmersedBoundary::updateCells after the bodies moved to
+        ``circles`` [(cx, cy, r), ...]: classes and stencils rebuilt on the
+        device.  Returns True when the pattern changed (the equation was
+        rebuilt; a solver given it re-analyses), False when the new IB rows
+        were written in place.  assemble() afterwards."""
+        c = np.ascontiguousarray(np.asarray(circles, np.float64).reshape(-1, 3))
+        flag = np.zeros(1, np.int32)
+        _check(lib().pg_eqn_update_gcib(self._h, len(c), _ptr(c), float(ib_ref),
+                                        _ptr(flag)))
+        s = np.zeros(2, np.int64)
+        _check(lib().pg_eqn_sizes(self._h, _ptr(s[0:1]), _ptr(s[1:2])))
+        self.n, self.nnz = int(s[0]), int(s[1])
+        return bool(flag[0])
 
     def cell_class(self):
         """0 fluid, 1 IB, 2 solid per cell (all 0 without an IB)."""

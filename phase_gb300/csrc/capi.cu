@@ -233,30 +233,18 @@ extern "C" int pg_eqn_create_momentum(const pg_mesh *m, const int32_t *bc_type,
   return eqn_create(m, PG_GAMMA_FACE, bc_type, true, out);
 }
 
-static int eqn_create(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
-                      bool momentum, pg_eqn **out, const GcibRows *ib) {
-  PG_CHECK_ARG(out, "pg_eqn_create: out is NULL");
-  *out = nullptr;
-  PG_CHECK_ARG(m, "pg_eqn_create: NULL mesh");
-  PG_CHECK_ARG(bc_type, "pg_eqn_create: bc_type is NULL");
-  PG_CHECK_ARG(gamma_kind == PG_GAMMA_SCALAR || gamma_kind == PG_GAMMA_FACE,
-               "pg_eqn_create: bad gamma_kind");
+// Fills e (new, or a ghost-cell IB equation whose pattern changed) with
+// the pattern, the face schedule and the constant rows; bc_type must not
+// alias e->bc_type.
+static int eqn_fill(pg_eqn *e, const pg_mesh *m, int gamma_kind,
+                    const int32_t *bc_type, bool momentum, const GcibRows *ib) {
   const HostMesh &h = m->h;
-  for (int64_t f = 0; f < h.n_faces; ++f)
-    if (h.fr[f] < 0)
-      PG_CHECK_ARG(bc_type[f] >= PG_BC_FIXED && bc_type[f] <= PG_BC_SYMMETRY,
-                   "fv::laplacian: unrecognized or unspecified boundary type");
-  auto *e = new (std::nothrow) pg_eqn();
-  PG_CHECK_ARG(e, "pg_eqn_create: out of host memory");
   e->mesh = m;
   e->gamma_kind = gamma_kind;
   e->bc_type.assign(bc_type, bc_type + h.n_faces);
   e->momentum = momentum;
   int rc = build_pattern(h, gamma_kind, bc_type, e->p, momentum, ib);
-  if (rc) {
-    delete e;
-    return rc;
-  }
+  if (rc) return rc;
   e->pattern_id = next_pattern_id();
   const EqnPattern &p = e->p;
   const int64_t nf = h.n_faces;
@@ -318,9 +306,29 @@ static int eqn_create(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
   if (ce == cudaSuccess) ce = e->vals.zero(p.nnz);
   if (ce == cudaSuccess) ce = e->rhs.zero(momentum ? 2 * p.n : p.n);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream());
-  if (ce != cudaSuccess) {
+  if (ce != cudaSuccess) return cuda_fail(ce, "equation upload", __FILE__, __LINE__);
+  return PG_OK;
+}
+
+static int eqn_create(const pg_mesh *m, int gamma_kind, const int32_t *bc_type,
+                      bool momentum, pg_eqn **out, const GcibRows *ib) {
+  PG_CHECK_ARG(out, "pg_eqn_create: out is NULL");
+  *out = nullptr;
+  PG_CHECK_ARG(m, "pg_eqn_create: NULL mesh");
+  PG_CHECK_ARG(bc_type, "pg_eqn_create: bc_type is NULL");
+  PG_CHECK_ARG(gamma_kind == PG_GAMMA_SCALAR || gamma_kind == PG_GAMMA_FACE,
+               "pg_eqn_create: bad gamma_kind");
+  const HostMesh &h = m->h;
+  for (int64_t f = 0; f < h.n_faces; ++f)
+    if (h.fr[f] < 0)
+      PG_CHECK_ARG(bc_type[f] >= PG_BC_FIXED && bc_type[f] <= PG_BC_SYMMETRY,
+                   "fv::laplacian: unrecognized or unspecified boundary type");
+  auto *e = new (std::nothrow) pg_eqn();
+  PG_CHECK_ARG(e, "pg_eqn_create: out of host memory");
+  const int rc = eqn_fill(e, m, gamma_kind, bc_type, momentum, ib);
+  if (rc) {
     delete e;
-    return cuda_fail(ce, "equation upload", __FILE__, __LINE__);
+    return rc;
   }
   *out = e;
   return PG_OK;
@@ -333,10 +341,40 @@ extern "C" int pg_eqn_create_gcib(const pg_mesh *m, int gamma_kind,
   PG_CHECK_ARG(out, "pg_eqn_create_gcib: out is NULL");
   *out = nullptr;
   PG_CHECK_ARG(m, "pg_eqn_create_gcib: NULL mesh");
+  auto S = std::make_unique<GcibState>();
+  S->ib_bc = ib_bc;
+  S->ib_ref = ib_ref;
   GcibRows g;
-  int rc = build_gcib(m->h, n_circles, circles, ib_bc, ib_ref, g);
+  int rc = gcib_build(m, *S, n_circles, circles, g);
   if (rc) return rc;
-  return eqn_create(m, gamma_kind, bc_type, false, out, &g);
+  rc = eqn_create(m, gamma_kind, bc_type, false, out, &g);
+  if (rc) return rc;
+  (*out)->ib = std::move(S);
+  return PG_OK;
+}
+
+extern "C" int pg_eqn_update_gcib(pg_eqn *e, int n_circles,
+                                  const double *circles, double ib_ref,
+                                  int *pattern_changed) {
+  PG_CHECK_ARG(e && e->ib, "pg_eqn_update_gcib: not a ghost-cell IB equation");
+  GcibState &S = *e->ib;
+  const double old_ref = S.ib_ref;
+  S.ib_ref = ib_ref;
+  GcibRows g;
+  bool changed = false;
+  int rc = gcib_build(e->mesh, S, n_circles, circles, g, true, e->row_ptr.p,
+                      e->col_ind.p, e->base_vals.p, e->base_rhs.p, &changed);
+  if (rc) {
+    S.ib_ref = old_ref;
+    return rc;
+  }
+  if (changed) {
+    const std::vector<int32_t> bc = e->bc_type;
+    rc = eqn_fill(e, e->mesh, e->gamma_kind, bc.data(), false, &g);
+    if (rc) return rc;
+  }
+  if (pattern_changed) *pattern_changed = changed ? 1 : 0;
+  return PG_OK;
 }
 
 extern "C" int pg_eqn_cell_class(const pg_eqn *e, int32_t *cls) {

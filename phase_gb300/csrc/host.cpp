@@ -1373,220 +1373,4 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   return PG_OK;
 }
 
-
-// ---------------------------------------------------------------- GCIB
-namespace {
-
-// inverse of a 4x4 matrix by Gauss-Jordan elimination with partial
-// pivoting on the augmented matrix [A | I]; false if singular
-bool inverse4(const double (&a)[4][4], double (&out)[4][4]) {
-  double w[4][8];
-  for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 8; ++j) w[i][j] = j < 4 ? a[i][j] : (j - 4 == i ? 1. : 0.);
-  for (int k = 0; k < 4; ++k) {
-    int p = k;
-    for (int i = k + 1; i < 4; ++i)
-      if (std::fabs(w[i][k]) > std::fabs(w[p][k])) p = i;
-    if (w[p][k] == 0.) return false;
-    if (p != k)
-      for (int j = 0; j < 8; ++j) std::swap(w[p][j], w[k][j]);
-    const double piv = w[k][k];
-    for (int j = 0; j < 8; ++j) w[k][j] /= piv;
-    for (int i = 0; i < 4; ++i) {
-      if (i == k) continue;
-      const double f = w[i][k];
-      for (int j = 0; j < 8; ++j) w[i][j] -= f * w[k][j];
-    }
-  }
-  for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 4; ++j) out[i][j] = w[i][4 + j];
-  return true;
-}
-
-// uniform bucket grid over the mesh nodes for nearest-node queries
-struct NodeGrid {
-  double x0 = 0., y0 = 0., h = 1.;
-  int nx = 1, ny = 1;
-  std::vector<int32_t> start, items;
-  const HostMesh *m = nullptr;
-  void build(const HostMesh &mesh) {
-    m = &mesh;
-    const int64_t nn = (int64_t)mesh.node_x.size();
-    double x1 = mesh.node_x[0], y1 = mesh.node_y[0];
-    x0 = x1;
-    y0 = y1;
-    for (int64_t i = 0; i < nn; ++i) {
-      x0 = std::min(x0, mesh.node_x[i]);
-      y0 = std::min(y0, mesh.node_y[i]);
-      x1 = std::max(x1, mesh.node_x[i]);
-      y1 = std::max(y1, mesh.node_y[i]);
-    }
-    const double w = std::max(x1 - x0, 1e-300), hh = std::max(y1 - y0, 1e-300);
-    h = std::sqrt(w * hh / (double)std::max<int64_t>(nn, 1)) * 2.;
-    nx = std::max(1, (int)std::min(1e6, std::ceil(w / h)));
-    ny = std::max(1, (int)std::min(1e6, std::ceil(hh / h)));
-    std::vector<int32_t> cnt((size_t)nx * ny + 1, 0);
-    auto bucket = [&](int64_t i) { return cell_of(mesh.node_x[i], mesh.node_y[i]); };
-    for (int64_t i = 0; i < nn; ++i) ++cnt[bucket(i) + 1];
-    for (size_t b = 1; b < cnt.size(); ++b) cnt[b] += cnt[b - 1];
-    start = cnt;
-    items.resize(nn);
-    for (int64_t i = 0; i < nn; ++i) items[cnt[bucket(i)]++] = (int32_t)i;
-  }
-  int64_t cell_of(double x, double y) const {
-    int ix = (int)std::floor((x - x0) / h), iy = (int)std::floor((y - y0) / h);
-    ix = std::min(std::max(ix, 0), nx - 1);
-    iy = std::min(std::max(iy, 0), ny - 1);
-    return (int64_t)iy * nx + ix;
-  }
-  // nearest node (smallest squared distance, then smallest id)
-  int32_t nearest(double x, double y) const {
-    const int64_t c = cell_of(x, y);
-    const int cx = (int)(c % nx), cy = (int)(c / nx);
-    int32_t best = -1;
-    double bd = 0.;
-    for (int ring = 0;; ++ring) {
-      for (int iy = cy - ring; iy <= cy + ring; ++iy) {
-        if (iy < 0 || iy >= ny) continue;
-        for (int ix = cx - ring; ix <= cx + ring; ++ix) {
-          if (ix < 0 || ix >= nx) continue;
-          if (std::max(std::abs(ix - cx), std::abs(iy - cy)) != ring) continue;
-          const int64_t b = (int64_t)iy * nx + ix;
-          for (int32_t k = start[b]; k < start[b + 1]; ++k) {
-            const int32_t v = items[k];
-            const double dx = m->node_x[v] - x, dy = m->node_y[v] - y;
-            const double d = dx * dx + dy * dy;
-            if (best < 0 || d < bd || (d == bd && v < best)) {
-              best = v;
-              bd = d;
-            }
-          }
-        }
-      }
-      // every node outside the searched square is farther than ring * h
-      // from the query point's bucket edge
-      if (best >= 0 && (double)ring * h >= std::sqrt(bd)) return best;
-      if (ring > nx + ny) return best;
-    }
-  }
-};
-
-}  // namespace
-
-int build_gcib(const HostMesh &m, int n_circles, const double *circles,
-               int ib_bc, double ib_ref, GcibRows &g) {
-  PG_CHECK_ARG(n_circles >= 0 && (n_circles == 0 || circles),
-               "pg_eqn_create_gcib: bad circles");
-  PG_CHECK_ARG(ib_bc == PG_BC_FIXED || ib_bc == PG_BC_NORMAL_GRADIENT,
-               "pg_eqn_create_gcib: IB boundary type must be FIXED or "
-               "NORMAL_GRADIENT");
-  const int64_t n = m.n_cells, nn = (int64_t)m.node_x.size();
-  // node -> cells in creation order
-  std::vector<int64_t> nptr(nn + 1, 0);
-  for (int64_t k = 0; k < (int64_t)m.cind.size(); ++k) ++nptr[m.cind[k] + 1];
-  for (int64_t i = 0; i < nn; ++i) nptr[i + 1] += nptr[i];
-  std::vector<int32_t> ncell(m.cind.size());
-  {
-    std::vector<int64_t> fill(nptr.begin(), nptr.end() - 1);
-    for (int64_t c = 0; c < n; ++c)
-      for (int64_t k = m.cptr[c]; k < m.cptr[c + 1]; ++k)
-        ncell[fill[m.cind[k]]++] = (int32_t)c;
-  }
-  g.cls.assign(n, 0);
-  g.rows.assign(n, {});
-  g.rhs.assign(n, 0.);
-  NodeGrid grid;
-  grid.build(m);
-  auto add = [&](int64_t row, int32_t col, double v) {
-    for (auto &e : g.rows[row])
-      if (e.first == col) {
-        e.second += v;
-        return;
-      }
-    g.rows[row].push_back({col, v});
-  };
-  for (int k = 0; k < n_circles; ++k) {
-    const double ccx = circles[3 * k], ccy = circles[3 * k + 1], r = circles[3 * k + 2];
-    PG_CHECK_ARG(r > 0., "pg_eqn_create_gcib: circle radius must be positive");
-    auto inside = [&](int64_t c) {
-      const double dx = m.cx[c] - ccx, dy = m.cy[c] - ccy;
-      return dx * dx + dy * dy < r * r;
-    };
-    std::vector<int32_t> ib;
-    for (int64_t c = 0; c < n; ++c) {
-      if (g.cls[c] != 0 || !inside(c)) continue;
-      bool perimeter = false;
-      for (int64_t q = m.cptr[c]; q < m.cptr[c + 1] && !perimeter; ++q) {
-        const int64_t v = m.cind[q];
-        for (int64_t t = nptr[v]; t < nptr[v + 1]; ++t)
-          if (ncell[t] != c && !inside(ncell[t])) {
-            perimeter = true;
-            break;
-          }
-      }
-      g.cls[c] = perimeter ? 1 : 2;
-      if (perimeter) ib.push_back((int32_t)c);
-    }
-    for (int32_t c : ib) {
-      const double xc = m.cx[c], yc = m.cy[c];
-      const double dx = xc - ccx, dy = yc - ccy, dm = std::sqrt(dx * dx + dy * dy);
-      const double bpx = dx / dm * r + ccx, bpy = dy / dm * r + ccy;
-      const double ipx = 2. * bpx - xc, ipy = 2. * bpy - yc;
-      const double tx = ccx - bpx, ty = ccy - bpy, tm = std::sqrt(tx * tx + ty * ty);
-      const double nwx = tx / tm, nwy = ty / tm;
-      const int32_t node = grid.nearest(ipx, ipy);
-      PG_CHECK_ARG(node >= 0 && nptr[node + 1] - nptr[node] == 4,
-                   "pg_eqn_create_gcib: the node nearest to an image point "
-                   "does not have four cells");
-      const int32_t *st = ncell.data() + nptr[node];
-      double A[4][4], Ai[4][4];
-      for (int i = 0; i < 4; ++i) {
-        const double x = m.cx[st[i]], y = m.cy[st[i]];
-        A[i][0] = x * y;
-        A[i][1] = x;
-        A[i][2] = y;
-        A[i][3] = 1.;
-      }
-      PG_CHECK_ARG(inverse4(A, Ai), "pg_eqn_create_gcib: singular IB stencil");
-      auto times_ainv = [&](const double (&w)[4], double (&o)[4]) {
-        for (int j = 0; j < 4; ++j)
-          o[j] = w[0] * Ai[0][j] + w[1] * Ai[1][j] + w[2] * Ai[2][j] + w[3] * Ai[3][j];
-      };
-      double co[4];
-      if (ib_bc == PG_BC_FIXED) {
-        const double w[4] = {ipx * ipy, ipx, ipy, 1.};
-        times_ainv(w, co);
-        for (int j = 0; j < 4; ++j) add(c, st[j], co[j] / 2.);
-        add(c, c, 0.5);
-      } else {
-        const bool self = st[0] == c || st[1] == c || st[2] == c || st[3] == c;
-        if (self) {
-          const double w[4] = {bpy * nwx + bpx * nwy, nwx, nwy, 0.};
-          times_ainv(w, co);
-          for (int j = 0; j < 4; ++j) add(c, st[j], co[j]);
-        } else {
-          const double lx = ipx - xc, ly = ipy - yc, l = std::sqrt(lx * lx + ly * ly);
-          const double w[4] = {ipx * ipy, ipx, ipy, 1.};
-          times_ainv(w, co);
-          for (int j = 0; j < 4; ++j) add(c, st[j], -co[j] / l);
-          add(c, c, 1. / l);
-        }
-      }
-      g.rhs[c] += -ib_ref;
-    }
-  }
-  for (int64_t c = 0; c < n; ++c) {
-    if (g.cls[c] != 2) continue;
-    add(c, (int32_t)c, 1.);
-    g.rhs[c] = ib_bc == PG_BC_FIXED ? -ib_ref : 0.;
-  }
-  // CrsEquation::operator+ keeps only non-zero entries
-  for (auto &row : g.rows) {
-    std::vector<std::pair<int32_t, double>> kept;
-    for (auto &e : row)
-      if (e.second != 0.) kept.push_back(e);
-    row.swap(kept);
-  }
-  return PG_OK;
-}
 }  // namespace pg

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -104,11 +106,52 @@ struct DevMesh {
   DevBuf<int32_t> link_face;
 };
 
+// Mesh-static device data of the ghost-cell IB stencil builder (gcib.cu),
+// made on the first IB build: the cell -> node and node -> cell lists (node
+// cells in creation order, as Node::cells) and a uniform bucket grid over
+// the nodes (bucket (bx, by) holds the nodes with floor((x - x0) / h) = bx,
+// floor((y - y0) / h) = by) for nearest-node queries.
+struct GcibMesh {
+  DevBuf<int32_t> cptr, cind, nptr, ncell, bstart, bitems;
+  DevBuf<double> node_x, node_y;
+  double x0 = 0., y0 = 0., h = 1.;
+  int nx = 1, ny = 1;
+};
+
+// One IB cell's image-point stencil as the device builds it: the four
+// cells of the node nearest to the image point (st, creation order) with
+// their coefficients, and the coefficient on the cell itself (has_self 0:
+// none).  The row is the sum of these entries in this order.
+struct GcibStencil {
+  int32_t cell, circle, has_self, pad;
+  int32_t st[4];
+  double co[4];
+  double self;
+};
+
+// Per-equation state of a ghost-cell IB equation: its boundary type and
+// reference value, the current cell classes on the device, and the
+// builder's scratch (counters: [0] IB cells, [1] error code, [2] first
+// failing cell, [3] pattern-changed flag).
+struct GcibState {
+  int ib_bc = 0;
+  double ib_ref = 0.;
+  int n_circles = 0;
+  DevBuf<int32_t> cls, new_cls, counters;
+  DevBuf<int2> ib;
+  DevBuf<GcibStencil> st;
+  DevBuf<double> circles;
+  int64_t n_ib = 0;
+};
+
 }  // namespace pg
 
 struct pg_mesh {
   pg::HostMesh h;
   pg::DevMesh d;
+  // ghost-cell IB builder data, made on first use (gcib.cu)
+  mutable std::unique_ptr<pg::GcibMesh> gcib;
+  mutable std::mutex gcib_mu;
   // link geometry per face side: dot(r, Sf_out) for the lCell and rCell
   // links, |r|^2, and the sign that turns the face normal into each side's
   // outward normal
@@ -139,8 +182,17 @@ struct GcibRows {
   std::vector<std::vector<std::pair<int32_t, double>>> rows;  // per cell
   std::vector<double> rhs;                                    // per cell
 };
-int build_gcib(const HostMesh &m, int n_circles, const double *circles,
-               int ib_bc, double ib_ref, GcibRows &g);
+// The device IB builder (gcib.cu): classify the cells of m for the circles
+// (cx, cy, r per circle, host), build the stencils of the IB cells into
+// st, and return the rows of the equation in g.  With check_pattern, the
+// classes are compared with st.cls, and when they match the new IB rows
+// are written into base_vals (the equation's pattern row_ptr/col_ind);
+// *changed says whether the pattern must be rebuilt (g is filled then).
+int gcib_build(const pg_mesh *m, GcibState &st, int n_circles, const double *circles,
+               GcibRows &g, bool check_pattern = false,
+               const int32_t *row_ptr = nullptr, const int32_t *col_ind = nullptr,
+               double *base_vals = nullptr, double *base_rhs = nullptr,
+               bool *changed = nullptr);
 
 // row_mask (optional): rows with mask 0 get no Laplacian entries; extra
 // (optional): entries appended to each row (the GCIB rows)
@@ -170,6 +222,7 @@ struct pg_eqn {
   bool has_base = false;
   pg::DevBuf<double> base_vals, base_rhs;
   std::vector<int32_t> cell_class;
+  std::unique_ptr<pg::GcibState> ib;  // ghost-cell IB equations only
 };
 
 namespace pg {
