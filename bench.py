@@ -405,13 +405,14 @@ def run_sequence(args):
         # on a side stream while the network runs
         sm.set_eqn(eqn)
         v, r = eqn.device_values()
-        pg.synchronize()
         # b = -rhs_ in a fixed buffer, so the captured inference graph
-        # (keyed on its input addresses) is replayed every step
-        torch.neg(torch.as_tensor(guess._DeviceView(r, n), device=dev), out=b_buf)
-        # torch's stream only: a device-wide sync would wait for the
-        # factorisation running beside the network
-        torch.cuda.current_stream().synchronize()
+        # (keyed on its input addresses) is replayed every step; computed on
+        # the library stream, which orders it after the assembly and before
+        # the network without a host wait (the factorisation runs beside
+        # them on the solver's own streams)
+        with torch.cuda.stream(stream):
+            torch.neg(torch.as_tensor(guess._DeviceView(r, n), device=dev),
+                      out=b_buf)
         rel = net.predict_device(v, b_buf.data_ptr(), xp_m.data_ptr(),
                                  g.data_ptr()) if have_w else float("inf")
         use = rel < 1.0

@@ -161,6 +161,12 @@ extern "C" int pg_mesh_create(const double *nodes_xy, int64_t n_nodes,
   up(d.fny, h.fny);
   up(d.link_ptr, h.link_ptr);
   up(d.link_face, h.link_face);
+  if (e == cudaSuccess) e = d.fw.reserve(nf);
+  if (e == cudaSuccess) {
+    launch_face_weights((int)nf, d.fl.p, d.fr.p, d.fcx.p, d.fcy.p, d.cx.p,
+                        d.cy.p, d.fw.p, stream());
+    e = cudaGetLastError();
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream());
   if (e != cudaSuccess) {
     delete m;
@@ -246,6 +252,9 @@ static int eqn_fill(pg_eqn *e, const pg_mesh *m, int gamma_kind,
   int rc = build_pattern(h, gamma_kind, bc_type, e->p, momentum, ib);
   if (rc) return rc;
   e->pattern_id = next_pattern_id();
+  e->any_fixed = false;
+  for (int64_t f = 0; f < h.n_faces && !e->any_fixed; ++f)
+    e->any_fixed = h.fr[f] < 0 && bc_type[f] == PG_BC_FIXED;
   const EqnPattern &p = e->p;
   const int64_t nf = h.n_faces;
   std::vector<int32_t> cl(nf), cr(nf), cbc(nf);
@@ -407,10 +416,7 @@ extern "C" int pg_assemble_laplacian(pg_eqn *e, const double *gamma_face,
                "a PG_GAMMA_FACE equation");
   const HostMesh &h = e->mesh->h;
   const int64_t nf = h.n_faces;
-  bool any_fixed = false;
-  for (int64_t f = 0; f < nf && !any_fixed; ++f)
-    any_fixed = h.fr[f] < 0 && e->bc_type[f] == PG_BC_FIXED;
-  PG_CHECK_ARG(!any_fixed || bc_value,
+  PG_CHECK_ARG(!e->any_fixed || bc_value,
                "pg_assemble_laplacian: bc_value needed for FIXED faces");
   const double *g = nullptr, *bv = nullptr, *u = nullptr;
   int rc = stage(gamma_face, nf, ptr_kind, e->stage_a, &g);
@@ -579,12 +585,13 @@ extern "C" int pg_interpolate_faces(const pg_mesh *m, const double *cell_vals,
     PG_CUDA(gout.reserve(h.n_faces));
     o = gout.p;
   }
-  launch_interp_faces((int)h.n_faces, m->d.fl.p, m->d.fr.p, m->d.fcx.p,
-                      m->d.fcy.p, m->d.cx.p, m->d.cy.p, c, o, stream());
+  launch_interp_faces((int)h.n_faces, m->d.fl.p, m->d.fr.p, m->d.fw.p, c, o,
+                      stream());
   PG_CUDA(cudaGetLastError());
-  if (ptr_kind != PG_DEVICE)
+  if (ptr_kind != PG_DEVICE) {
     PG_CUDA(copy_out(face_vals, o, h.n_faces * sizeof(double), PG_HOST));
-  PG_CUDA(cudaStreamSynchronize(stream()));
+    PG_CUDA(cudaStreamSynchronize(stream()));
+  }
   return PG_OK;
 }
 
@@ -602,13 +609,13 @@ extern "C" int pg_face_dt_over_rho(const pg_mesh *m, const double *gamma_cell,
     PG_CUDA(gout.reserve(h.n_faces));
     o = gout.p;
   }
-  launch_dt_over_rho((int)h.n_faces, m->d.fl.p, m->d.fr.p, m->d.fcx.p,
-                     m->d.fcy.p, m->d.cx.p, m->d.cy.p, g, rho1, rho2, dt, o,
-                     stream());
+  launch_dt_over_rho((int)h.n_faces, m->d.fl.p, m->d.fr.p, m->d.fw.p, g,
+                     rho1, rho2, dt, o, stream());
   PG_CUDA(cudaGetLastError());
-  if (ptr_kind != PG_DEVICE)
+  if (ptr_kind != PG_DEVICE) {
     PG_CUDA(copy_out(coeff_face, o, h.n_faces * sizeof(double), PG_HOST));
-  PG_CUDA(cudaStreamSynchronize(stream()));
+    PG_CUDA(cudaStreamSynchronize(stream()));
+  }
   return PG_OK;
 }
 

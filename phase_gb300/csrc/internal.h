@@ -102,6 +102,7 @@ struct DevMesh {
   DevBuf<double> cx, cy, vol;
   DevBuf<int32_t> fl, fr;
   DevBuf<double> fcx, fcy, fnx, fny;
+  DevBuf<double> fw;  // Face::distanceWeight per face (1 on boundaries)
   DevBuf<int64_t> link_ptr;
   DevBuf<int32_t> link_face;
 };
@@ -217,6 +218,7 @@ struct pg_eqn {
   uint64_t version = 0;  // bumps on every assembly
   uint64_t pattern_id = 0;
   bool momentum = false;   // vector momentum operator: rhs holds 2n values
+  bool any_fixed = false;  // a boundary face has a FIXED condition
   pg::DevBuf<int32_t> diag;  // diagonal position per row
   // ghost-cell IB equation: constant IB/solid rows the assembly starts from
   bool has_base = false;

@@ -252,53 +252,58 @@ __global__ void k_momentum_boundary(
 
 // FiniteVolumeField::interpolateFaces(DISTANCE) + setBoundaryFaces for a
 // normal-gradient field (FiniteVolumeField.tpp:130-183, Face.cpp:60-64)
-__global__ void k_interp_faces(int nf, const int32_t *__restrict__ fl,
+// Face::distanceWeight (Face.cpp:54-58) of every interior face: with l1 =
+// |x_f - x_r| and l2 = |x_f - x_l|, g = l1 / (l1 + l2) weights the lCell
+// (FiniteVolumeField.tpp:130-162 interpolates g phi_l + (1 - g) phi_r).
+// Geometry only: computed once per mesh; boundary faces get 1.
+__global__ void k_face_weights(int nf, const int32_t *__restrict__ fl,
                                const int32_t *__restrict__ fr,
                                const double *__restrict__ fcx,
                                const double *__restrict__ fcy,
                                const double *__restrict__ cx,
                                const double *__restrict__ cy,
-                               const double *__restrict__ cv,
-                               double *__restrict__ fv) {
+                               double *__restrict__ fw) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   const int l = fl[f], r = fr[f];
   if (r < 0) {
-    fv[f] = cv[l];
+    fw[f] = 1.;
     return;
   }
   const double ax = __dadd_rn(fcx[f], -cx[r]), ay = __dadd_rn(fcy[f], -cy[r]);
   const double bx = __dadd_rn(fcx[f], -cx[l]), by = __dadd_rn(fcy[f], -cy[l]);
   const double l1 = __dsqrt_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)));
   const double l2 = __dsqrt_rn(__dadd_rn(__dmul_rn(bx, bx), __dmul_rn(by, by)));
-  const double w = __ddiv_rn(l1, __dadd_rn(l1, l2));
-  fv[f] = __dadd_rn(__dmul_rn(w, cv[l]), __dmul_rn(__dadd_rn(1., -w), cv[r]));
+  fw[f] = __ddiv_rn(l1, __dadd_rn(l1, l2));
+}
+
+// g phi_l + (1 - g) phi_r on interior faces, phi_l on boundary faces
+__device__ __forceinline__ double face_interp(int l, int r, double w,
+                                              const double *__restrict__ cv) {
+  if (r < 0) return cv[l];
+  return __dadd_rn(__dmul_rn(w, cv[l]), __dmul_rn(__dadd_rn(1., -w), cv[r]));
+}
+
+__global__ void k_interp_faces(int nf, const int32_t *__restrict__ fl,
+                               const int32_t *__restrict__ fr,
+                               const double *__restrict__ fw,
+                               const double *__restrict__ cv,
+                               double *__restrict__ fv) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  fv[f] = face_interp(fl[f], fr[f], fw[f], cv);
 }
 
 // dt / rho_f (FractionalStepMultiphase.cpp:175-185 with the distance-weighted
 // face interpolation FiniteVolumeField.tpp:130-162, Face.cpp:60-64)
 __global__ void k_dt_over_rho(int nf, const int32_t *__restrict__ fl,
                               const int32_t *__restrict__ fr,
-                              const double *__restrict__ fcx,
-                              const double *__restrict__ fcy,
-                              const double *__restrict__ cx,
-                              const double *__restrict__ cy,
+                              const double *__restrict__ fw,
                               const double *__restrict__ gc, double rho1,
                               double rho2, double dt, double *__restrict__ out) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nf) return;
-  const int l = fl[f], r = fr[f];
-  double gf;
-  if (r < 0) {
-    gf = gc[l];
-  } else {
-    const double ax = __dadd_rn(fcx[f], -cx[r]), ay = __dadd_rn(fcy[f], -cy[r]);
-    const double bx = __dadd_rn(fcx[f], -cx[l]), by = __dadd_rn(fcy[f], -cy[l]);
-    const double l1 = __dsqrt_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)));
-    const double l2 = __dsqrt_rn(__dadd_rn(__dmul_rn(bx, bx), __dmul_rn(by, by)));
-    const double w = __ddiv_rn(l1, __dadd_rn(l1, l2));
-    gf = __dadd_rn(__dmul_rn(w, gc[l]), __dmul_rn(__dadd_rn(1., -w), gc[r]));
-  }
+  const double gf = face_interp(fl[f], fr[f], fw[f], gc);
   const double c = fmin(fmax(gf, 0.), 1.);
   const double rho = __dadd_rn(rho1, __dmul_rn(c, __dadd_rn(rho2, -rho1)));
   out[f] = __ddiv_rn(dt, rho);
@@ -717,24 +722,33 @@ void launch_momentum_boundary(int nf, int off, const int32_t *cface,
       u_face, n, vals, rhs);
   count_launches(1);
 }
-void launch_interp_faces(int nf, const int32_t *fl, const int32_t *fr,
+void launch_face_weights(int nf, const int32_t *fl, const int32_t *fr,
                          const double *fcx, const double *fcy,
-                         const double *cx, const double *cy,
-                         const double *cell_vals, double *face_vals,
+                         const double *cx, const double *cy, double *fw,
                          cudaStream_t st) {
-  k_interp_faces<<<blocks_for(nf, 256), 256, 0, st>>>(nf, fl, fr, fcx, fcy, cx,
-                                                      cy, cell_vals, face_vals);
+  if (nf <= 0) return;
+  k_face_weights<<<blocks_for(nf, 256), 256, 0, st>>>(nf, fl, fr, fcx, fcy, cx,
+                                                      cy, fw);
+  count_launches(1);
+}
+
+void launch_interp_faces(int nf, const int32_t *fl, const int32_t *fr,
+                         const double *fw, const double *cell_vals,
+                         double *face_vals, cudaStream_t st) {
+  if (nf <= 0) return;
+  k_interp_faces<<<blocks_for(nf, 256), 256, 0, st>>>(nf, fl, fr, fw,
+                                                      cell_vals, face_vals);
   count_launches(1);
 }
 
 void launch_dt_over_rho(int nf, const int32_t *fl, const int32_t *fr,
-                        const double *fcx, const double *fcy, const double *cx,
-                        const double *cy, const double *gamma_cell,
+                        const double *fw, const double *gamma_cell,
                         double rho1, double rho2, double dt, double *out,
                         cudaStream_t st) {
   if (nf <= 0) return;
-  k_dt_over_rho<<<blocks_for(nf, 256), 256, 0, st>>>(
-      nf, fl, fr, fcx, fcy, cx, cy, gamma_cell, rho1, rho2, dt, out);
+  k_dt_over_rho<<<blocks_for(nf, 256), 256, 0, st>>>(nf, fl, fr, fw,
+                                                     gamma_cell, rho1, rho2,
+                                                     dt, out);
   count_launches(1);
 }
 

@@ -116,14 +116,17 @@ void launch_correct_velocity(int n, double dt, const double *rho,
 void launch_set_boundary_faces(int nf, const int32_t *fl, const int32_t *fr,
                                const int32_t *bc, const double *phi_cell,
                                double *phi_face, cudaStream_t st);
-void launch_interp_faces(int nf, const int32_t *fl, const int32_t *fr,
+// fw: Face::distanceWeight of every face (1 on boundary faces), made once
+// per mesh by launch_face_weights
+void launch_face_weights(int nf, const int32_t *fl, const int32_t *fr,
                          const double *fcx, const double *fcy,
-                         const double *cx, const double *cy,
-                         const double *cell_vals, double *face_vals,
+                         const double *cx, const double *cy, double *fw,
                          cudaStream_t st);
+void launch_interp_faces(int nf, const int32_t *fl, const int32_t *fr,
+                         const double *fw, const double *cell_vals,
+                         double *face_vals, cudaStream_t st);
 void launch_dt_over_rho(int nf, const int32_t *fl, const int32_t *fr,
-                        const double *fcx, const double *fcy, const double *cx,
-                        const double *cy, const double *gamma_cell,
+                        const double *fw, const double *gamma_cell,
                         double rho1, double rho2, double dt, double *out,
                         cudaStream_t st);
 void launch_gradient(int n_cells, int nf, const int32_t *fl,

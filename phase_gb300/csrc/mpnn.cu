@@ -134,13 +134,15 @@ k_prep(int n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
     const double ri = b[i] - ax;
     r[i] = (float)ri;
     diag[i] = (float)dii;
-    const double inv = dii != 0. ? 1. / dii : 0.;
+    // edge weights and r / a_ii are FP32 quantities: one FP32 reciprocal
+    // instead of FP64 division and products (FP64 is a slow pipe here)
+    const float inv = dii != 0. ? 1.f / (float)dii : 0.f;
     for (int k = rp[i]; k < rp[i + 1]; ++k)
-      e[k] = ci[k] == i ? 0.f : (float)(-a[k] * inv);
+      e[k] = ci[k] == i ? 0.f : -(float)a[k] * inv;
     s[0] += xp[i] * xp[i];
     s[1] += b[i] * b[i];
-    const double q = ri * inv;
-    s[2] += q * q;
+    const float q = (float)ri * inv;
+    s[2] += (double)(q * q);
     s[3] += (double)log_abs(dii);
   }
   block_sums4(s, part);
@@ -386,6 +388,289 @@ __global__ void k_head(int n, const float *__restrict__ h3,
   }
 }
 
+// ---- inference: one kernel per layer, dense products on tensor cores ----
+// A CTA takes a tile of kTile = 64 cells.  Its 128 threads gather the
+// message m = sum_j e_ij relu(q_j) (FP32 FMAs in row order, as k_message)
+// and stage [h | m] in shared memory as a 64 x 64 row-major tile; each warp
+// then multiplies its 16 rows by U (64 x 32) and, for the next layer, the
+// new h by P (32 x 32) with mma.sync m16n8k8 TF32.  The weights are BF16
+// values, exact in TF32; each activation is split into a TF32 high part
+// and a TF32 low part (two MMAs), so the products carry FP32 accuracy and
+// only the summation order differs from the training forward.  h' and the
+// next relu(q) are written back feature-major with coalesced stores.
+constexpr int kTile = 64;          // cells per CTA tile
+constexpr int kTileThreads = 128;  // 4 warps, 16 cells each
+constexpr int kAS = 2 * H + 4;     // smem row stride of the [h | m] tile
+constexpr int kWS = H + 8;         // smem row stride of a weight matrix
+
+__device__ __forceinline__ uint32_t tf32_of(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4],
+                                         uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 "
+      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// acc[nt] (+)= rows r0..r0+15 of the tile (columns c0..c0+K-1) times W
+// (K x H in smem, stride kWS), for the warp's four 8-column n-tiles.
+// Fragments of m16n8k8: a = A[g][t], A[g+8][t], A[g][t+4], A[g+8][t+4];
+// b = B[t][g], B[t+4][g]; c = C[g][2t], C[g][2t+1], C[g+8][2t], C[g+8][2t+1]
+// with g = lane / 4, t = lane % 4.
+template <int K>
+__device__ __forceinline__ void warp_gemm(float (&acc)[H / 8][4],
+                                          const float *__restrict__ tile,
+                                          int r0, int c0,
+                                          const float *__restrict__ W) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int k0 = 0; k0 < K; k0 += 8) {
+    const float av[4] = {tile[(r0 + g) * kAS + c0 + k0 + t],
+                         tile[(r0 + g + 8) * kAS + c0 + k0 + t],
+                         tile[(r0 + g) * kAS + c0 + k0 + t + 4],
+                         tile[(r0 + g + 8) * kAS + c0 + k0 + t + 4]};
+    uint32_t hi[4], lo[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      hi[q] = tf32_of(av[q]);
+      lo[q] = tf32_of(av[q] - __uint_as_float(hi[q]));
+    }
+#pragma unroll
+    for (int nt = 0; nt < H / 8; ++nt) {
+      const uint32_t b0 = __float_as_uint(W[(k0 + t) * kWS + nt * 8 + g]);
+      const uint32_t b1 = __float_as_uint(W[(k0 + t + 4) * kWS + nt * 8 + g]);
+      mma_tf32(acc[nt], lo, b0, b1);
+      mma_tf32(acc[nt], hi, b0, b1);
+    }
+  }
+}
+
+__device__ __forceinline__ void load_weights(float *__restrict__ dst,
+                                             const float *__restrict__ W, int K) {
+  for (int x = threadIdx.x; x < K * H; x += blockDim.x)
+    dst[(x / H) * kWS + (x % H)] = W[x];
+}
+
+// features, h0 = relu(W0 f + b0) (FP32 FMAs) and relu(q_0) = relu(P_0 h0 +
+// c_0) (tensor cores)
+__global__ void __launch_bounds__(kTileThreads)
+k_infer_in(int n, const double *__restrict__ b, const double *__restrict__ xp,
+           const float *__restrict__ r, const float *__restrict__ diag,
+           const double *__restrict__ sums, const float *__restrict__ W0,
+           const float *__restrict__ b0, const float *__restrict__ P,
+           const float *__restrict__ c, float *__restrict__ h0,
+           float *__restrict__ q0) {
+  __shared__ float tile[kTile * kAS];
+  __shared__ float ps[H * kWS];
+  __shared__ float w0s[F * H], bs0[H], cs[H];
+  __shared__ double sc[3];
+  load_weights(ps, P, H);
+  for (int x = threadIdx.x; x < F * H; x += blockDim.x) w0s[x] = W0[x];
+  for (int x = threadIdx.x; x < H; x += blockDim.x) {
+    bs0[x] = b0[x];
+    cs[x] = c[x];
+  }
+  if (threadIdx.x == 0) {
+    sc[0] = 1. / (sqrt(sums[0] / n) + 1e-300);
+    sc[1] = 1. / (sqrt(sums[1] / n) + 1e-300);
+    sc[2] = sums[3] / n;
+  }
+  __syncthreads();
+  const double isx = sc[0], isb = sc[1];
+  const float la = (float)sc[2];
+  const int cell = threadIdx.x & (kTile - 1), half = threadIdx.x / kTile;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane >> 2, t = lane & 3;
+  const int n_tiles = (n + kTile - 1) / kTile;
+  for (int tl = blockIdx.x; tl < n_tiles; tl += gridDim.x) {
+    const int i = tl * kTile + cell;
+    float hv[H / 2];
+    if (i < n) {
+      const float f[F] = {(float)(xp[i] * isx), (float)(b[i] * isb),
+                          (float)(r[i] * isb), log_abs((double)diag[i]) - la};
+#pragma unroll
+      for (int k = 0; k < H / 2; ++k) {
+        const int hh = half * (H / 2) + k;
+        float a = bs0[hh];
+#pragma unroll
+        for (int u = 0; u < F; ++u) a = fmaf(f[u], w0s[u * H + hh], a);
+        hv[k] = fmaxf(a, 0.f);
+        h0[(size_t)hh * n + i] = hv[k];
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < H / 2; ++k) hv[k] = 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < H / 2; ++k) tile[cell * kAS + half * (H / 2) + k] = hv[k];
+    __syncthreads();
+    float acc[H / 8][4];
+#pragma unroll
+    for (int nt = 0; nt < H / 8; ++nt) {
+      acc[nt][0] = acc[nt][2] = cs[nt * 8 + 2 * t];
+      acc[nt][1] = acc[nt][3] = cs[nt * 8 + 2 * t + 1];
+    }
+    const int r0 = warp * 16;
+    warp_gemm<H>(acc, tile, r0, 0, ps);
+#pragma unroll
+    for (int nt = 0; nt < H / 8; ++nt) {
+      const int col = H + nt * 8 + 2 * t;
+      tile[(r0 + g) * kAS + col] = fmaxf(acc[nt][0], 0.f);
+      tile[(r0 + g) * kAS + col + 1] = fmaxf(acc[nt][1], 0.f);
+      tile[(r0 + g + 8) * kAS + col] = fmaxf(acc[nt][2], 0.f);
+      tile[(r0 + g + 8) * kAS + col + 1] = fmaxf(acc[nt][3], 0.f);
+    }
+    __syncthreads();
+    if (i < n)
+#pragma unroll
+      for (int k = 0; k < H / 2; ++k) {
+        const int hh = half * (H / 2) + k;
+        q0[(size_t)hh * n + i] = tile[cell * kAS + H + hh];
+      }
+    __syncthreads();
+  }
+}
+
+// one message-passing layer: m = sum_j e_ij relu(q_j),
+// h' = h + relu(U [h; m] + d), then relu(q') = relu(P' h' + c') for the
+// next layer, or (LAST) the head out = wo . h' + bo, g = x_prev + s_d out
+template <bool LAST>
+__global__ void __launch_bounds__(kTileThreads)
+k_infer_layer(int n, const int32_t *__restrict__ rp,
+              const int32_t *__restrict__ ci, const float *__restrict__ e,
+              const float *__restrict__ qr, const float *__restrict__ hin,
+              const float *__restrict__ U, const float *__restrict__ d,
+              const float *__restrict__ P, const float *__restrict__ c,
+              const float *__restrict__ wo, const double *__restrict__ xp,
+              const double *__restrict__ sums, float *__restrict__ hout,
+              float *__restrict__ qout, float *__restrict__ out,
+              double *__restrict__ g) {
+  __shared__ float tile[kTile * kAS];
+  __shared__ float us[2 * H * kWS];
+  __shared__ float ps[LAST ? 1 : H * kWS];
+  __shared__ float ds[H], cs[H], wos[H + 1];
+  load_weights(us, U, 2 * H);
+  if (!LAST) load_weights(ps, P, H);
+  for (int x = threadIdx.x; x < H; x += blockDim.x) {
+    ds[x] = d[x];
+    if (!LAST) cs[x] = c[x];
+  }
+  if (LAST)
+    for (int x = threadIdx.x; x <= H; x += blockDim.x) wos[x] = wo[x];
+  __syncthreads();
+  const double sd = LAST ? sqrt(sums[2] / n) : 0.;
+  const int cell = threadIdx.x & (kTile - 1), half = threadIdx.x / kTile;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gq = lane >> 2, t = lane & 3;
+  const int r0 = warp * 16;
+  const int n_tiles = (n + kTile - 1) / kTile;
+  for (int tl = blockIdx.x; tl < n_tiles; tl += gridDim.x) {
+    const int i = tl * kTile + cell;
+    // [h | m] of the tile, each thread half of one cell's features
+    float m[H / 2], hv[H / 2];
+#pragma unroll
+    for (int k = 0; k < H / 2; ++k) m[k] = hv[k] = 0.f;
+    if (i < n) {
+#pragma unroll
+      for (int k = 0; k < H / 2; ++k)
+        hv[k] = hin[(size_t)(half * (H / 2) + k) * n + i];
+      // edges four at a time: every gather of the four is issued before the
+      // FMAs, which run in row order skipping zero weights (as k_message)
+      const int k1 = rp[i + 1];
+      for (int kb = rp[i]; kb < k1; kb += 4) {
+        float w[4];
+        int j[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const bool in = kb + u < k1;
+          w[u] = in ? e[kb + u] : 0.f;
+          j[u] = in ? ci[kb + u] : i;
+        }
+        float qv[4][H / 2];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int k2 = 0; k2 < H / 2; ++k2)
+            qv[u][k2] = qr[(size_t)(half * (H / 2) + k2) * n + j[u]];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (w[u] == 0.f) continue;
+#pragma unroll
+          for (int k2 = 0; k2 < H / 2; ++k2) m[k2] = fmaf(w[u], qv[u][k2], m[k2]);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < H / 2; ++k) {
+      tile[cell * kAS + half * (H / 2) + k] = hv[k];
+      tile[cell * kAS + H + half * (H / 2) + k] = m[k];
+    }
+    __syncthreads();
+    float acc[H / 8][4];
+#pragma unroll
+    for (int nt = 0; nt < H / 8; ++nt) {
+      acc[nt][0] = acc[nt][2] = ds[nt * 8 + 2 * t];
+      acc[nt][1] = acc[nt][3] = ds[nt * 8 + 2 * t + 1];
+    }
+    warp_gemm<2 * H>(acc, tile, r0, 0, us);
+    __syncwarp();
+    // h' = h + relu(acc) over the warp's own rows (columns 0..H-1)
+#pragma unroll
+    for (int nt = 0; nt < H / 8; ++nt) {
+      const int col = nt * 8 + 2 * t;
+      float *p0 = tile + (r0 + gq) * kAS + col, *p1 = tile + (r0 + gq + 8) * kAS + col;
+      p0[0] = p0[0] + fmaxf(acc[nt][0], 0.f);
+      p0[1] = p0[1] + fmaxf(acc[nt][1], 0.f);
+      p1[0] = p1[0] + fmaxf(acc[nt][2], 0.f);
+      p1[1] = p1[1] + fmaxf(acc[nt][3], 0.f);
+    }
+    __syncwarp();
+    if (!LAST) {
+#pragma unroll
+      for (int nt = 0; nt < H / 8; ++nt) {
+        acc[nt][0] = acc[nt][2] = cs[nt * 8 + 2 * t];
+        acc[nt][1] = acc[nt][3] = cs[nt * 8 + 2 * t + 1];
+      }
+      warp_gemm<H>(acc, tile, r0, 0, ps);
+      __syncwarp();
+#pragma unroll
+      for (int nt = 0; nt < H / 8; ++nt) {
+        const int col = H + nt * 8 + 2 * t;
+        tile[(r0 + gq) * kAS + col] = fmaxf(acc[nt][0], 0.f);
+        tile[(r0 + gq) * kAS + col + 1] = fmaxf(acc[nt][1], 0.f);
+        tile[(r0 + gq + 8) * kAS + col] = fmaxf(acc[nt][2], 0.f);
+        tile[(r0 + gq + 8) * kAS + col + 1] = fmaxf(acc[nt][3], 0.f);
+      }
+    }
+    __syncthreads();
+    if (i < n) {
+      if (LAST) {
+        if (half == 0) {
+          float o = wos[H];
+#pragma unroll
+          for (int k = 0; k < H; ++k) o = fmaf(wos[k], tile[cell * kAS + k], o);
+          out[i] = o;
+          g[i] = xp[i] + sd * (double)o;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < H / 2; ++k) {
+          const int hh = half * (H / 2) + k;
+          hout[(size_t)hh * n + i] = tile[cell * kAS + hh];
+          qout[(size_t)hh * n + i] = tile[cell * kAS + H + hh];
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // residual res = A g - b, error err = g - x*, and per-block loss sums
 // (k_finish_sums adds them into sums[4..7])
 __global__ void __launch_bounds__(kBlock) k_loss(int n, const int32_t *__restrict__ rp,
@@ -402,12 +687,15 @@ __global__ void __launch_bounds__(kBlock) k_loss(int n, const int32_t *__restric
     double ag = 0., ap = 0.;
     for (int k = rp[i]; k < rp[i + 1]; ++k) {
       ag += a[k] * g[ci[k]];
-      ap += a[k] * xp[ci[k]];
+      if (res) ap += a[k] * xp[ci[k]];
     }
-    const double rr = ag - b[i], r0 = ap - b[i];
-    res[i] = rr;
+    const double rr = ag - b[i];
     s[0] += rr * rr;
-    s[1] += r0 * r0;
+    if (res) {  // training: the residual vector and |A x_prev - b|^2 too
+      const double r0 = ap - b[i];
+      res[i] = rr;
+      s[1] += r0 * r0;
+    }
     if (xs) {
       const double ee = g[i] - xs[i], e0 = xp[i] - xs[i];
       err[i] = ee;
@@ -589,6 +877,54 @@ int forward(pg_mpnn *net, const double *a, const double *b, const double *xp,
   return PG_OK;
 }
 
+// inference forward (fused layers; the guess lands in net->xg): 2 + L + 1
+// launches after k_prep / k_finish_sums
+int infer_forward(pg_mpnn *net, const double *a, const double *b,
+                  const double *xp) {
+  cudaStream_t st = pg::stream();
+  const int n = (int)net->n;
+  const int g = grid_of(n);
+  const Layout &Y = net->lay;
+  const float *W = net->pb.p;
+  PG_CUDA(cudaMemsetAsync(net->sums.p, 0, 16 * sizeof(double), st));
+  k_prep<<<g, kBlock, 0, st>>>(n, net->rp.p, net->ci.p, a, b, xp, net->r.p,
+                               net->diag.p, net->e.p, net->part.p);
+  k_finish_sums<<<1, kBlock, 0, st>>>(g, net->part.p, net->sums.p);
+  // h and relu(q) alternate between two buffers each; tiles of kTile cells,
+  // a grid of as many CTAs as are resident at once
+  static int resident = 0;
+  if (!resident) {
+    int dev = 0, sms = 0, per_sm = 0;
+    PG_CUDA(cudaGetDevice(&dev));
+    PG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, k_infer_layer<false>, kTileThreads, 0));
+    resident = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  const int tiles = (n + kTile - 1) / kTile;
+  const int gt = tiles < resident ? tiles : resident;
+  k_infer_in<<<gt, kTileThreads, 0, st>>>(n, b, xp, net->r.p, net->diag.p,
+                                   net->sums.p, W + Y.w0, W + Y.b0, W + Y.P[0],
+                                   W + Y.c[0], net->h[0].p, net->q[0].p);
+  for (int l = 0; l < L; ++l) {
+    float *hi = net->h[l & 1].p, *ho = net->h[(l + 1) & 1].p;
+    float *qi = net->q[l & 1].p, *qo = net->q[(l + 1) & 1].p;
+    if (l + 1 < L)
+      k_infer_layer<false><<<gt, kTileThreads, 0, st>>>(
+          n, net->rp.p, net->ci.p, net->e.p, qi, hi, W + Y.U[l], W + Y.d[l],
+          W + Y.P[l + 1], W + Y.c[l + 1], nullptr, xp, net->sums.p, ho, qo,
+          nullptr, nullptr);
+    else
+      k_infer_layer<true><<<gt, kTileThreads, 0, st>>>(
+          n, net->rp.p, net->ci.p, net->e.p, qi, hi, W + Y.U[l], W + Y.d[l],
+          nullptr, nullptr, W + Y.wo, xp, net->sums.p, nullptr, nullptr,
+          net->out.p, net->xg.p);
+  }
+  pg::count_launches(3 + L);
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
 int stage_in(const double *src, size_t n, int ptr_kind, pg::DevBuf<double> &buf,
              const double **out) {
   if (ptr_kind == PG_DEVICE) {
@@ -699,10 +1035,11 @@ extern "C" int pg_mpnn_predict(pg_mpnn *net, const double *vals,
   // forward + ||b - A g||^2: captured once per input address triple into a
   // CUDA graph and replayed
   auto record = [&]() -> int {
-    int r = forward(net, a, bb, xp, false);
+    int r = infer_forward(net, a, bb, xp);
     if (r) return r;
+    // ||b - A g||^2 only (no residual vector, no |A x_prev - b|^2)
     k_loss<<<grid_of(n), kBlock, 0, st>>>(n, net->rp.p, net->ci.p, a, bb,
-                                         net->xg.p, nullptr, xp, net->res.p,
+                                         net->xg.p, nullptr, xp, nullptr,
                                          nullptr, net->part.p);
     k_finish_sums<<<1, kBlock, 0, st>>>(grid_of(n), net->part.p, net->sums.p + 4);
     count_launches(2);

@@ -430,10 +430,18 @@ int ensure_host_state(pg_solver *s) {
   if (!s->diff_host) PG_CUDA(cudaMallocHost((void **)&s->diff_host, sizeof(unsigned)));
   for (auto &e : s->ev)
     if (!e) PG_CUDA(cudaEventCreate(&e));
-  if (!s->side) PG_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+  // the factorisation streams run at the highest priority: their kernels
+  // form short dependent chains (the coarse inverse is ~130 launches) that
+  // must not queue behind the blocks of whatever the library stream runs
+  // meanwhile (a network's inference, one-level iterations)
+  int prio_lo = 0, prio_hi = 0;
+  PG_CUDA(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+  if (!s->side)
+    PG_CUDA(cudaStreamCreateWithPriority(&s->side, cudaStreamNonBlocking, prio_hi));
   if (!s->ev_vals) PG_CUDA(cudaEventCreateWithFlags(&s->ev_vals, cudaEventDisableTiming));
   if (!s->ev_fact) PG_CUDA(cudaEventCreateWithFlags(&s->ev_fact, cudaEventDisableTiming));
-  if (!s->side2) PG_CUDA(cudaStreamCreateWithFlags(&s->side2, cudaStreamNonBlocking));
+  if (!s->side2)
+    PG_CUDA(cudaStreamCreateWithPriority(&s->side2, cudaStreamNonBlocking, prio_hi));
   if (!s->ev_cvals) PG_CUDA(cudaEventCreateWithFlags(&s->ev_cvals, cudaEventDisableTiming));
   if (!s->ev_coarse) PG_CUDA(cudaEventCreateWithFlags(&s->ev_coarse, cudaEventDisableTiming));
   return PG_OK;

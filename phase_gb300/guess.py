@@ -214,9 +214,20 @@ class BubbleSequence:
             gamma, u = self._cache[t]
         else:
             gamma, u = self._fields(t)
-        torch.cuda.synchronize()
-        self._coeff = torch.empty(self.mesh.n_faces, dtype=torch.float64,
-                                  device=self.dev)
+        # the library stream reads what torch's stream wrote: order the two
+        # on the device (no host wait), and keep torch from reusing the
+        # fields' memory before the library's reads are done
+        if not hasattr(self, "_lib_stream"):
+            self._lib_stream = torch.cuda.ExternalStream(_pg().stream_handle(),
+                                                         device=self.dev)
+            self._coeff = torch.empty(self.mesh.n_faces, dtype=torch.float64,
+                                      device=self.dev)
+        ready = torch.cuda.Event()
+        ready.record(torch.cuda.current_stream(self.dev))
+        self._lib_stream.wait_event(ready)
+        gamma.record_stream(self._lib_stream)
+        u.record_stream(self._lib_stream)
+        self._gamma = gamma
         self._u = u.view(-1)
         self.mesh.dt_over_rho_device(gamma.data_ptr(), self._coeff.data_ptr(),
                                      workloads.RB_RHO1, workloads.RB_RHO2,

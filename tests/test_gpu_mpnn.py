@@ -57,6 +57,37 @@ def test_mpnn_loss_and_gradients_match_cpu_restatement(pg, oracle):
         assert abs(g_gpu[k] - fd) <= 3e-2 * abs(fd) + 1e-6, (k, g_gpu[k], fd)
 
 
+def test_fused_inference_matches_training_forward_and_restatement(pg, oracle):
+    """pg_mpnn_predict runs the forward pass as one kernel per layer with
+    the dense products on tensor cores (TF32 with split activations, FP32
+    accuracy).  Its guess matches the training forward (FP32 FMAs) up to the
+    summation order: the FP64 loss of the predicted guess equals the loss
+    the training path reports to 1e-5 relative; and it agrees with the FP64
+    restatement's guess (FP32 activations: the correction g - x_prev within
+    1e-3 relative), as does the reported residual."""
+    from phase_gb300.guess import Mpnn
+    # 23 x 17 = 391 cells: six full 64-cell tiles and a ragged one
+    rp, ci, v, b, xp, xs = _system(oracle, 23, 17, seed=3)
+    net = Mpnn(seed=2)
+    rng = np.random.default_rng(7)
+    params = (0.25 * rng.standard_normal(net.n_params)).astype(np.float32)
+    net.set_params(params)
+    net.set_graph(rp, ci)
+    g, rel = net.predict(v, b, xp)
+    _, loss_train = net.gradient(v, b, xp, xs)
+    A = sp.csr_matrix((v, ci, rp))
+    r0 = A @ xp - b
+    res = A @ g - b
+    loss_pred = (res @ res) / (r0 @ r0) + ((g - xs) @ (g - xs)) / ((xp - xs) @ (xp - xs))
+    assert abs(loss_pred - loss_train) <= 1e-5 * loss_train
+    w = mpnn_oracle.round_bf16(params).astype(np.float64)
+    _, g_cpu = mpnn_oracle.loss(w, rp, ci, v, b, xp, xs)
+    assert np.linalg.norm((g - xp) - (g_cpu - xp)) <= 1e-3 * np.linalg.norm(g_cpu - xp)
+    rel_cpu = np.linalg.norm(A @ g_cpu - b) / np.linalg.norm(b)
+    assert abs(rel - rel_cpu) <= 1e-3 * rel_cpu
+    assert abs(rel - np.linalg.norm(res) / np.linalg.norm(b)) <= 1e-12 * rel
+
+
 def test_training_beats_previous_solution(pg):
     torch = pytest.importorskip("torch")
     from phase_gb300.guess import BubbleSequence, Mpnn
