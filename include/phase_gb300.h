@@ -470,6 +470,70 @@ int pg_batch_get_x(const pg_batch *b, int system, double *x, int ptr_kind);
 int pg_batch_tuning(const pg_batch *b, int *block, int *rows_per_thread,
                     int *n_tiles);
 
+/* ---------------------------------------------------------------------
+ * Direct sparse solve.  Replaces the SparseMatrixSolver backend that most
+ * of Phase's cases select for the pressure equation (`lib eigen`):
+ * EigenSparseMatrixSolver (src/Math/EigenSparseMatrixSolver.cpp:5-64),
+ * whose set() builds the matrix from the entries with col >= 0 (repeated
+ * entries summed, :17-48) and whose solve() factorises and solves on every
+ * call (SparseLU::compute + solve, :60-64), reporting nIters() = 1 and
+ * error() = 0 (EigenSparseMatrixSolver.h:43-45).  Here: a multifrontal LU
+ * over a nested-dissection ordering (cut by the row coordinates when given,
+ * by graph bisection otherwise), FP64, partial pivoting inside the fully
+ * summed rows of each front (32-row blocks of the larger fronts); the
+ * ordering and front structure are computed once per pattern, the numeric
+ * factorisation on every solve after new values (as the reference's
+ * compute), and a solve with only a new right-hand side reuses the
+ * factors.  A pivot at most 1e-13 of its column's largest entry in A is
+ * replaced by that entry and counted (replaced_pivots): a consistent
+ * singular system (all-Neumann pressure) gets one of its solutions.
+ * --------------------------------------------------------------------- */
+typedef struct pg_lu pg_lu;
+typedef struct {
+  int n_fronts;           /* nodes of the nested-dissection tree */
+  int n_heights;          /* levels of fronts factorised one after another */
+  int max_front;          /* order of the largest front */
+  int replaced_pivots;    /* vanishing pivots replaced (see above) */
+  int64_t factor_entries; /* entries of L and U */
+  double flops;           /* factorisation flops (multiply-add = 2) */
+  double analyse_ms;      /* host time of the last ordering + symbolic */
+  double factor_ms;       /* device time of the last factorisation */
+  double solve_ms;        /* device time of the last triangular solves */
+  double rel_residual;    /* ||b - A x||_2 / ||b||_2 computed in FP64 */
+} pg_lu_stats;
+int pg_lu_create(pg_lu **out);
+int pg_lu_destroy(pg_lu *lu);
+/* setRank (EigenSparseMatrixSolver.cpp:5-9) */
+int pg_lu_set_rank(pg_lu *lu, int64_t n);
+/* optional point per row (xy[2 n], e.g. cell centres) for the ordering;
+ * NULL clears it */
+int pg_lu_set_row_coords(pg_lu *lu, const double *xy);
+/* set(rowPtr, colInds, vals) (EigenSparseMatrixSolver.cpp:31-40): entries
+ * with a negative column are skipped, repeated columns summed */
+int pg_lu_set_csr(pg_lu *lu, const int32_t *row_ptr, const int32_t *col_ind,
+                  const double *vals, int ptr_kind);
+/* the matrix and -rhs_ of a device equation (FiniteVolumeEquation::solve's
+ * setRank + set + setRhs, FiniteVolumeEquation.tpp:71-73), cells' centres
+ * as the ordering's coordinates */
+int pg_lu_set_eqn(pg_lu *lu, const pg_eqn *e);
+/* setRhs (EigenSparseMatrixSolver.cpp:55-58) */
+int pg_lu_set_rhs(pg_lu *lu, const double *rhs, int ptr_kind);
+/* solve (EigenSparseMatrixSolver.cpp:60-64); stats may be NULL */
+int pg_lu_solve(pg_lu *lu, pg_lu_stats *stats);
+/* x (EigenSparseMatrixSolver.h:39) for all rows */
+int pg_lu_get_x(const pg_lu *lu, double *x, int ptr_kind);
+/* The ordering and front structure alone (host work, no GPU needed), for
+ * inspection: sizes[4] = {fronts, index-list length, heights, largest
+ * front}; when the arrays are non-NULL also perm[n] (elimination order:
+ * new -> old row), fronts[4 * n_fronts] = (first new index, fully summed
+ * count k, order m, parent or -1) in elimination order, and fidx[] (each
+ * front's index list: its k own rows, then its update rows ascending).
+ * xy: optional point per row.  (Inspection; no reference counterpart.) */
+int pg_lu_analyse_pattern(int64_t n, const int32_t *row_ptr,
+                          const int32_t *col_ind, const double *xy,
+                          int64_t *sizes, int32_t *perm, int32_t *fronts,
+                          int32_t *fidx);
+
 /* Number of kernels the library has launched since it was loaded. */
 uint64_t pg_kernel_launches(void);
 

@@ -1709,3 +1709,156 @@ extern "C" void or_correct_velocity(const or_mesh *m, double dt,
     u_face[2 * f + 1] -= k * grad_face[2 * f + 1];
   }
 }
+
+// ------------------------------------------------------------ direct solve
+// EigenSparseMatrixSolver (src/Math/EigenSparseMatrixSolver.cpp:17-64): the
+// matrix of the entries with col >= 0 (repeated entries summed, as
+// setFromTriplets), factorised with partial pivoting and solved.  Restated
+// as a band LU: a reverse Cuthill-McKee ordering (Cuthill & McKee 1969,
+// reversed as George 1971) of the symmetrised pattern, then Gaussian
+// elimination with row partial pivoting inside the band (the storage
+// scheme of LAPACK's dgbtrf: pivoting widens the upper band from ku to
+// kl + ku).  Any stable LU gives the same x up to rounding, which is what
+// the parity tests compare.  A pivot at most 1e-13 of its column's largest
+// entry in A is replaced by that entry (a consistent singular system then
+// gets one of its solutions).
+namespace {
+
+std::vector<int32_t> rcm_order(int64_t n, const std::vector<int64_t> &ap,
+                               const std::vector<int32_t> &aj) {
+  std::vector<int32_t> order;
+  order.reserve(n);
+  std::vector<char> done(n, 0);
+  std::vector<int64_t> deg(n);
+  for (int64_t i = 0; i < n; ++i) deg[i] = ap[i + 1] - ap[i];
+  auto bfs = [&](int32_t s, std::vector<int32_t> &out) {
+    std::vector<char> seen(n, 0);
+    out.clear();
+    out.push_back(s);
+    seen[s] = 1;
+    for (size_t h = 0; h < out.size(); ++h) {
+      const int32_t u = out[h];
+      std::vector<int32_t> nb;
+      for (int64_t e = ap[u]; e < ap[u + 1]; ++e)
+        if (!seen[aj[e]] && !done[aj[e]]) nb.push_back(aj[e]);
+      std::sort(nb.begin(), nb.end(), [&](int32_t a, int32_t b) {
+        return deg[a] < deg[b] || (deg[a] == deg[b] && a < b);
+      });
+      for (int32_t w : nb) {
+        seen[w] = 1;
+        out.push_back(w);
+      }
+    }
+  };
+  std::vector<int32_t> comp;
+  for (int64_t s0 = 0; s0 < n; ++s0) {
+    if (done[s0]) continue;
+    // pseudo-peripheral start: the last vertex of a BFS from the
+    // component's first vertex
+    bfs((int32_t)s0, comp);
+    bfs(comp.back(), comp);
+    for (int32_t u : comp) done[u] = 1;
+    order.insert(order.end(), comp.begin(), comp.end());
+  }
+  std::reverse(order.begin(), order.end());
+  return order;
+}
+
+}  // namespace
+
+extern "C" int or_sparse_lu_solve(int64_t n, const int32_t *row_ptr,
+                                  const int32_t *col_ind, const double *vals,
+                                  const double *b, double *x, int64_t *band,
+                                  int *replaced) {
+  // compact matrix, duplicates summed
+  std::vector<std::map<int32_t, double>> rows(n);
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t k = row_ptr[i]; k < row_ptr[i + 1]; ++k)
+      if (col_ind[k] >= 0) rows[i][col_ind[k]] += vals[k];
+  std::vector<double> cmax(n, 0.);
+  std::vector<int64_t> ap(n + 1, 0);
+  std::vector<int32_t> aj;
+  {
+    std::vector<std::vector<int32_t>> adj(n);
+    for (int64_t i = 0; i < n; ++i)
+      for (auto &e : rows[i]) {
+        cmax[e.first] = std::max(cmax[e.first], std::fabs(e.second));
+        if (e.first != i) {
+          adj[i].push_back(e.first);
+          adj[e.first].push_back((int32_t)i);
+        }
+      }
+    for (int64_t i = 0; i < n; ++i) {
+      std::sort(adj[i].begin(), adj[i].end());
+      adj[i].erase(std::unique(adj[i].begin(), adj[i].end()), adj[i].end());
+      ap[i + 1] = ap[i] + (int64_t)adj[i].size();
+      aj.insert(aj.end(), adj[i].begin(), adj[i].end());
+    }
+  }
+  const std::vector<int32_t> order = rcm_order(n, ap, aj);  // new -> old
+  std::vector<int32_t> inv(n);
+  for (int64_t i = 0; i < n; ++i) inv[order[i]] = (int32_t)i;
+  int64_t kl = 0, ku = 0;
+  for (int64_t i = 0; i < n; ++i)
+    for (auto &e : rows[i]) {
+      const int64_t r = inv[i], c = inv[e.first];
+      kl = std::max(kl, r - c);
+      ku = std::max(ku, c - r);
+    }
+  const int64_t w = 2 * kl + ku + 1;  // row window: columns i-kl .. i+kl+ku
+  std::vector<double> W((size_t)(n * w), 0.);
+  auto at = [&](int64_t i, int64_t j) -> double & {
+    return W[(size_t)(i * w + (j - i + kl))];
+  };
+  for (int64_t i = 0; i < n; ++i)
+    for (auto &e : rows[i]) at(inv[i], inv[e.first]) = e.second;
+  std::vector<int64_t> piv(n);
+  int nrep = 0;
+  for (int64_t c = 0; c < n; ++c) {
+    const int64_t rlast = std::min(n - 1, c + kl);
+    const int64_t jlast = std::min(n - 1, c + kl + ku);
+    int64_t p = c;
+    double best = std::fabs(at(c, c));
+    for (int64_t r = c + 1; r <= rlast; ++r)
+      if (std::fabs(at(r, c)) > best) {
+        best = std::fabs(at(r, c));
+        p = r;
+      }
+    piv[c] = p;
+    if (p != c)
+      for (int64_t j = c; j <= jlast; ++j) std::swap(at(c, j), at(p, j));
+    const double cs = cmax[order[c]];
+    if (std::fabs(at(c, c)) <= 1e-13 * cs || at(c, c) == 0.) {
+      at(c, c) = cs > 0. ? cs : 1.;
+      ++nrep;
+    }
+    const double d = at(c, c);
+    for (int64_t r = c + 1; r <= rlast; ++r) {
+      const double l = at(r, c) / d;
+      at(r, c) = l;
+      if (l != 0.)
+        for (int64_t j = c + 1; j <= jlast; ++j) at(r, j) -= l * at(c, j);
+    }
+  }
+  std::vector<double> y(n);
+  for (int64_t i = 0; i < n; ++i) y[i] = b[order[i]];
+  for (int64_t c = 0; c < n; ++c) {
+    if (piv[c] != c) std::swap(y[c], y[piv[c]]);
+    const double yc = y[c];
+    const int64_t rlast = std::min(n - 1, c + kl);
+    for (int64_t r = c + 1; r <= rlast; ++r) y[r] -= at(r, c) * yc;
+  }
+  for (int64_t c = n - 1; c >= 0; --c) {
+    const int64_t jlast = std::min(n - 1, c + kl + ku);
+    double s = y[c];
+    for (int64_t j = c + 1; j <= jlast; ++j) s -= at(c, j) * y[j];
+    y[c] = s / at(c, c);
+  }
+  for (int64_t i = 0; i < n; ++i) x[order[i]] = y[i];
+  if (band) {
+    band[0] = kl;
+    band[1] = ku;
+  }
+  if (replaced) *replaced = nrep;
+  return 0;
+}

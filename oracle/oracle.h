@@ -206,6 +206,14 @@ void or_correct_velocity(const or_mesh *m, double dt, const double *rho_cell,
 void or_spmv(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
              const double *vals, const double *x, double *y);
 
+/* Direct solve of the matrix of the entries with col >= 0 (repeated
+ * entries summed): band LU with partial pivoting in a reverse Cuthill-McKee
+ * order (EigenSparseMatrixSolver.cpp:17-64 semantics).  band[2] receives the
+ * (lower, upper) bandwidths, *replaced the vanishing pivots replaced. */
+int or_sparse_lu_solve(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
+                       const double *vals, const double *b, double *x,
+                       int64_t *band, int *replaced);
+
 #ifdef __cplusplus
 }
 #endif

@@ -51,6 +51,18 @@ class SolverCfg(ctypes.Structure):
                 ("reserved_d", ctypes.c_double)]
 
 
+class LuStats(ctypes.Structure):
+    _fields_ = [("n_fronts", ctypes.c_int), ("n_heights", ctypes.c_int),
+                ("max_front", ctypes.c_int), ("replaced_pivots", ctypes.c_int),
+                ("factor_entries", ctypes.c_int64), ("flops", ctypes.c_double),
+                ("analyse_ms", ctypes.c_double), ("factor_ms", ctypes.c_double),
+                ("solve_ms", ctypes.c_double),
+                ("rel_residual", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class SolveStats(ctypes.Structure):
     _fields_ = [("iters", ctypes.c_int), ("outer_iters", ctypes.c_int),
                 ("status", ctypes.c_int), ("fp64_iters", ctypes.c_int),
@@ -129,6 +141,16 @@ PROTOTYPES = {
     "pg_mpnn_set_params": (_I, [_P, _P]),
     "pg_mpnn_save": (_I, [_P, ctypes.c_char_p]),
     "pg_mpnn_load": (_I, [_P, ctypes.c_char_p]),
+    "pg_lu_create": (_I, [ctypes.POINTER(_P)]),
+    "pg_lu_destroy": (_I, [_P]),
+    "pg_lu_set_rank": (_I, [_P, _I64]),
+    "pg_lu_set_row_coords": (_I, [_P, _P]),
+    "pg_lu_set_csr": (_I, [_P, _P, _P, _P, _I]),
+    "pg_lu_set_eqn": (_I, [_P, _P]),
+    "pg_lu_set_rhs": (_I, [_P, _P, _I]),
+    "pg_lu_solve": (_I, [_P, ctypes.POINTER(LuStats)]),
+    "pg_lu_get_x": (_I, [_P, _P, _I]),
+    "pg_lu_analyse_pattern": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P]),
     "pg_kernel_launches": (ctypes.c_uint64, []),
 }
 
@@ -587,6 +609,101 @@ class SparseMatrixSolver:
 
     def printStatus(self, msg: str):
         print(f"{msg} iterations = {self.nIters()}, error = {self.error():f}.")
+
+
+class SparseLU:
+    """The direct backend (pg_lu_*), mirroring EigenSparseMatrixSolver
+    (src/Math/EigenSparseMatrixSolver.cpp:5-64): setRank, set(rowPtr,
+    colInds, vals) (negative columns skipped, repeated ones summed), setRhs,
+    solve (factorise + solve; a new right-hand side alone reuses the
+    factors), x, nIters() = 1 and error() = 0 as the reference reports.
+    ``set_eqn`` hands over a device equation; ``stats`` holds the
+    factorisation's figures and the FP64 true residual."""
+
+    def __init__(self):
+        h = _P()
+        _check(lib().pg_lu_create(ctypes.byref(h)))
+        self._h = h
+        self.n = 0
+        self.stats = LuStats()
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.pg_lu_destroy(h)
+            self._h = None
+
+    def setRank(self, n: int):
+        _check(lib().pg_lu_set_rank(self._h, int(n)))
+        self.n = int(n)
+
+    def set_row_coords(self, xy):
+        if xy is None:
+            _check(lib().pg_lu_set_row_coords(self._h, None))
+            return
+        a = _f64(np.asarray(xy, np.float64).reshape(-1), 2 * self.n)
+        _check(lib().pg_lu_set_row_coords(self._h, _ptr(a)))
+
+    def set(self, row_ptr, col_ind, vals):
+        rp = _i32(row_ptr, self.n + 1)
+        ci = _i32(col_ind, int(rp[-1]))
+        v = _f64(vals, int(rp[-1]))
+        _check(lib().pg_lu_set_csr(self._h, _ptr(rp), _ptr(ci), _ptr(v),
+                                   PG_HOST))
+
+    def set_eqn(self, eqn):
+        _check(lib().pg_lu_set_eqn(self._h, eqn._h))
+        self.n = eqn.n
+
+    def setRhs(self, rhs):
+        r = _f64(rhs, self.n)
+        _check(lib().pg_lu_set_rhs(self._h, _ptr(r), PG_HOST))
+
+    def setGuess(self, x0):
+        """Ignored, as EigenSparseMatrixSolver's solve ignores it."""
+
+    def solve(self) -> float:
+        st = LuStats()
+        _check(lib().pg_lu_solve(self._h, ctypes.byref(st)))
+        self.stats = st
+        return 0.0
+
+    def x(self):
+        out = np.empty(self.n)
+        _check(lib().pg_lu_get_x(self._h, _ptr(out), PG_HOST))
+        return out
+
+    def nIters(self) -> int:
+        return 1
+
+    def error(self) -> float:
+        return 0.0
+
+
+def lu_analyse_pattern(row_ptr, col_ind, xy=None):
+    """The direct solver's nested-dissection ordering and fronts (host
+    analysis only): (perm new->old, fronts [n_fronts, 4] = (s0, k, m,
+    parent), list of index arrays per front, heights)."""
+    rp = _i32(row_ptr)
+    n = rp.size - 1
+    ci = _i32(col_ind, int(rp[-1]))
+    xa = None if xy is None else _f64(np.asarray(xy).reshape(-1), 2 * n)
+    sizes = np.zeros(4, np.int64)
+    _check(lib().pg_lu_analyse_pattern(n, _ptr(rp), _ptr(ci),
+                                       None if xa is None else _ptr(xa),
+                                       _ptr(sizes), None, None, None))
+    perm = np.empty(n, np.int32)
+    fr = np.empty((int(sizes[0]), 4), np.int32)
+    fidx = np.empty(int(sizes[1]), np.int32)
+    _check(lib().pg_lu_analyse_pattern(n, _ptr(rp), _ptr(ci),
+                                       None if xa is None else _ptr(xa),
+                                       _ptr(sizes), _ptr(perm), _ptr(fr),
+                                       _ptr(fidx)))
+    lists, o = [], 0
+    for s0, k, m, parent in fr:
+        lists.append(fidx[o:o + m])
+        o += m
+    return perm, fr, lists, int(sizes[2])
 
 
 class BatchSolver:

@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libphase_gb300.so")
 SOURCES = ["host.cpp", "capi.cu", "solver.cu", "kernels.cu", "ilu.cu", "dd.cu", "batch.cu", "coarse.cu",
-           "mpnn.cu", "noalloc.cu", "krylov.cu", "gcib.cu"]
+           "mpnn.cu", "noalloc.cu", "krylov.cu", "gcib.cu", "lu_host.cpp", "lu.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -94,6 +94,7 @@ def lib():
         L.or_gcib_laplacian.restype = P
         L.or_gcib_laplacian.argtypes = [P, P, D, P, P, P, ctypes.c_int, P,
                                         ctypes.c_int, D, P]
+        L.or_sparse_lu_solve.argtypes = [I64, P, P, P, P, P, P, P]
         _lib = L
     return _lib
 
@@ -249,6 +250,22 @@ class OracleMesh:
         gc = np.empty(2 * self.n_cells)
         lib().or_gradient(self.h, ptr(pc), ptr(pf), ptr(gf), ptr(gc))
         return gf.reshape(-1, 2), gc.reshape(-1, 2)
+
+
+def sparse_lu_solve(rp, ci, v, b):
+    """Oracle direct solve (RCM band LU with partial pivoting); returns
+    (x, dict(band=(kl, ku), replaced=count))."""
+    rp = np.ascontiguousarray(rp, np.int32)
+    ci = np.ascontiguousarray(ci, np.int32)
+    v = np.ascontiguousarray(v, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.zeros(b.size)
+    band = np.zeros(2, np.int64)
+    rep = ctypes.c_int()
+    lib().or_sparse_lu_solve(b.size, rp.ctypes.data, ci.ctypes.data,
+                             v.ctypes.data, b.ctypes.data, x.ctypes.data,
+                             band.ctypes.data, ctypes.byref(rep))
+    return x, dict(band=(int(band[0]), int(band[1])), replaced=rep.value)
 
 
 def bicgstab(rp, ci, v, b, tol=1e-8, max_iters=500, precond=OR_PREC_ILU0,

@@ -1,0 +1,191 @@
+"""The direct backend (pg_lu_*): Phase's EigenSparseMatrixSolver
+(src/Math/EigenSparseMatrixSolver.cpp:5-64) on the device, against the
+oracle's band LU with partial pivoting.
+
+Two direct solvers of the same system agree to about cond(A) times the unit
+roundoff; the bars below are relative errors of 1e-10 on the well
+conditioned systems and 1e-8 on the 1000:1 rising bubble, with every FP64
+true residual at most 1e-11 (1e-10 for the bubble).  Singular all-Neumann
+systems are compared with the constant null-space component removed.
+Factorisations repeat bit for bit.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from phase_gb300 import meshes, simple, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(x, ref, singular=False):
+    if singular:
+        x, ref = x - x.mean(), ref - ref.mean()
+    return float(np.linalg.norm(x - ref) / np.linalg.norm(ref))
+
+
+def _fixed_wall_system(pg, nodes, cptr, cind, seed):
+    m = pg.Mesh(nodes, cptr, cind)
+    f = m.faces()
+    bc = np.where(f["rcell"] < 0, 0, 1).astype(np.int32)
+    rng = np.random.default_rng(seed)
+    eqn = pg.Equation(m, pg.GAMMA_FACE, bc)
+    eqn.assemble(gamma_face=rng.uniform(0.5, 2.0, m.n_faces),
+                 bc_value=rng.standard_normal(m.n_faces),
+                 u_face=rng.standard_normal((m.n_faces, 2)))
+    return m, eqn
+
+
+@pytest.mark.parametrize("coords", [True, False])
+def test_lu_host_csr_matches_oracle(pg, oracle, coords):
+    """set(rowPtr, colInds, vals) + setRhs + solve on a triangle mesh, the
+    ordering cut by cell centres or by graph bisection."""
+    nodes, cptr, cind = meshes.triangulated(40, 30, 2.0, 1.5, jitter=0.2,
+                                            seed=11)
+    m, eqn = _fixed_wall_system(pg, nodes, cptr, cind, 2)
+    rp, ci, v, rhs = eqn.export()
+    b = -rhs
+    lu = pg.SparseLU()
+    lu.setRank(m.n_cells)
+    if coords:
+        c = m.cells()
+        lu.set_row_coords(np.stack([c["cx"], c["cy"]], axis=1))
+    lu.set(rp, ci, v)
+    lu.setRhs(b)
+    lu.solve()
+    x = lu.x()
+    xo, _ = oracle.sparse_lu_solve(rp, ci, v, b)
+    st = lu.stats
+    assert st.rel_residual < 1e-12, st.as_dict()
+    assert _rel(x, xo) < 1e-10
+    assert lu.nIters() == 1 and lu.error() == 0.0
+    assert st.n_fronts > 1 and st.replaced_pivots == 0
+
+
+def test_lu_pivoting_placeholders_and_repeats(pg, oracle):
+    """Small diagonals that need row interchanges; placeholder columns and
+    repeated entries in the caller's CSR; no coordinates (graph
+    bisection; a random pattern has large separators, so the panel path of
+    the large fronts runs)."""
+    rng = np.random.default_rng(7)
+    n = 600
+    A = sp.random(n, n, density=0.012, random_state=8, format="lil")
+    for i in range(n):
+        A[i, (i + 1) % n] = 1.0 + rng.random()
+        A[i, i] = 0.05 * (1.0 + rng.random()) * (1 if i % 2 else -1)
+    A = A.tocsr()
+    A.sort_indices()
+    rows_c, rows_v = [], []
+    for i in range(n):
+        c = list(A.indices[A.indptr[i]:A.indptr[i + 1]])
+        w = list(A.data[A.indptr[i]:A.indptr[i + 1]])
+        c += [-1, c[0]]
+        w += [77.0, 0.5 * w[0]]
+        w[0] *= 0.5
+        rows_c.append(c)
+        rows_v.append(w)
+    rp = np.concatenate([[0], np.cumsum([len(c) for c in rows_c])])
+    ci = np.concatenate(rows_c).astype(np.int32)
+    v = np.concatenate(rows_v)
+    b = rng.standard_normal(n)
+    lu = pg.SparseLU()
+    lu.setRank(n)
+    lu.set(rp, ci, v)
+    lu.setRhs(b)
+    lu.solve()
+    x = lu.x()
+    xd = np.linalg.solve(A.toarray(), b)
+    assert lu.stats.max_front > 112  # the large-front (panel) path ran
+    assert _rel(x, xd) < 1e-9, lu.stats.as_dict()
+    xo, _ = oracle.sparse_lu_solve(rp, ci, v, b)
+    assert _rel(x, xo) < 1e-9
+
+
+def test_lu_cavity_pcorr_singular(pg, oracle):
+    """The lid-driven cavity's all-Neumann pCorr system (singular,
+    consistent): a solution, equal to the oracle's up to a constant."""
+    out = simple.simple_pcorr(pg, 80, 80)
+    eqn = out["eqn"]
+    rp, ci, v, rhs = eqn.export()
+    b = -rhs
+    lu = pg.SparseLU()
+    lu.set_eqn(eqn)
+    lu.solve()
+    x = lu.x()
+    A = sp.csr_matrix((v, ci, rp))
+    assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-10
+    assert lu.stats.replaced_pivots >= 1
+    xo, info = oracle.sparse_lu_solve(rp, ci, v, b)
+    assert _rel(x, xo, singular=True) < 1e-8
+
+
+def test_lu_gcib_channel_nonsymmetric(pg, oracle):
+    L, H, nx, ny = 6.0, 3.0, 96, 48
+    nodes, cptr, cind = meshes.rectilinear(nx, ny, L, H)
+    m = pg.Mesh(nodes, cptr, cind)
+    f = m.faces()
+    patch = meshes.rect_patch_of_faces(f["fx"], f["fy"], f["rcell"], L, H)
+    bc = np.ones(m.n_faces, np.int32)
+    bc[patch == 1] = 0
+    rng = np.random.default_rng(5)
+    for ib_bc in (0, 1):
+        eqn = pg.Equation(m, pg.GAMMA_FACE, bc, ib_circles=[(2.4, 1.4, 0.6)],
+                          ib_bc=ib_bc)
+        eqn.assemble(gamma_face=rng.uniform(0.5, 2.0, m.n_faces),
+                     bc_value=np.zeros(m.n_faces),
+                     u_face=rng.standard_normal((m.n_faces, 2)))
+        rp, ci, v, rhs = eqn.export()
+        b = -rhs
+        lu = pg.SparseLU()
+        lu.set_eqn(eqn)
+        lu.solve()
+        x = lu.x()
+        xo, _ = oracle.sparse_lu_solve(rp, ci, v, b)
+        assert lu.stats.rel_residual < 1e-11, lu.stats.as_dict()
+        assert _rel(x, xo) < 1e-10
+
+
+def _bubble_eqn(pg, nx, ny, seed=3):
+    w = workloads.rising_bubble(nx, ny, seed=seed)
+    m = pg.Mesh(w["nodes"], w["cptr"], w["cind"])
+    w = workloads.rising_bubble(nx, ny, seed=seed, faces=m.faces(),
+                                cells=m.cells())
+    coeff = m.dt_over_rho(w["gamma"], w["rho1"], w["rho2"], w["dt"])
+    return m, pg.fv.laplacian(coeff, m, w["bc_type"], w["bc_value"], w["u"])
+
+
+def test_lu_rising_bubble_matches_oracle_and_repeats(pg, oracle):
+    """1000:1 coefficient contrast, 128 x 128; a second factorisation of
+    the same values is bit-identical, and a new right-hand side alone
+    reuses the factors."""
+    m, eqn = _bubble_eqn(pg, 128, 128)
+    rp, ci, v, rhs = eqn.export()
+    b = -rhs
+    lu = pg.SparseLU()
+    lu.set_eqn(eqn)
+    lu.solve()
+    x1 = lu.x()
+    xo, _ = oracle.sparse_lu_solve(rp, ci, v, b)
+    assert lu.stats.rel_residual < 1e-10, lu.stats.as_dict()
+    assert _rel(x1, xo) < 1e-8
+    lu.set_eqn(eqn)  # same values: factorised again
+    lu.solve()
+    assert np.array_equal(lu.x(), x1)
+    b2 = np.random.default_rng(1).standard_normal(b.size)
+    lu.setRhs(b2)
+    lu.solve()
+    xo2, _ = oracle.sparse_lu_solve(rp, ci, v, b2)
+    assert _rel(lu.x(), xo2) < 1e-8
+
+
+def test_lu_rising_bubble_1m_residual(pg):
+    """The full 1024 x 1024 system (no oracle at this size): the FP64 true
+    residual of the direct solve."""
+    m, eqn = _bubble_eqn(pg, 1024, 1024)
+    lu = pg.SparseLU()
+    lu.set_eqn(eqn)
+    lu.solve()
+    st = lu.stats.as_dict()
+    print("lu 1M bubble", st)
+    assert st["rel_residual"] < 1e-10, st
+    assert st["replaced_pivots"] == 0

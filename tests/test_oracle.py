@@ -496,3 +496,64 @@ def test_iluk_solve_takes_fewer_iterations(oracle):
         assert np.linalg.norm(-rhs - A @ x) / np.linalg.norm(rhs) <= 1.01e-10
         its[k] = st["iters"]
     assert its[2] < its[0], its
+
+
+# ------------------------------------------------------------ direct solve
+def test_sparse_lu_oracle_matches_dense_solve(oracle):
+    """The oracle's band LU (EigenSparseMatrixSolver semantics) against
+    numpy's dense LAPACK solve on a pressure system."""
+    rp, ci, v, b = _poisson_system(oracle, 30, 22, seed=4)
+    x, info = oracle.sparse_lu_solve(rp, ci, v, b)
+    A = sp.csr_matrix((v, ci, rp)).toarray()
+    xd = np.linalg.solve(A, b)
+    assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-12
+    assert info["replaced"] == 0 and 0 < info["band"][0] <= 60
+
+
+def test_sparse_lu_oracle_pivots_placeholders_and_repeats(oracle):
+    """Zero diagonals need row interchanges; -1 columns are skipped and
+    repeated columns summed, as setFromTriplets does
+    (EigenSparseMatrixSolver.cpp:31-40)."""
+    rng = np.random.default_rng(7)
+    n = 300
+    A = sp.random(n, n, density=0.02, random_state=8, format="lil")
+    for i in range(n):
+        A[i, (i + 1) % n] = 1.0 + rng.random()  # keeps A nonsingular
+        A[i, i] = 0.0 if i % 3 == 0 else 0.1 * rng.standard_normal()
+    A = A.tocsr()
+    A.sort_indices()
+    rp, ci, v = A.indptr, A.indices, A.data
+    # rebuild with a placeholder and a split (repeated) entry in every row
+    rows_c, rows_v = [], []
+    for i in range(n):
+        c = list(ci[rp[i]:rp[i + 1]])
+        w = list(v[rp[i]:rp[i + 1]])
+        c += [-1, c[0]]
+        w += [123.0, 0.25 * w[0]]
+        w[0] *= 0.75
+        rows_c.append(c)
+        rows_v.append(w)
+    rp2 = np.concatenate([[0], np.cumsum([len(c) for c in rows_c])])
+    ci2 = np.concatenate(rows_c).astype(np.int32)
+    v2 = np.concatenate(rows_v)
+    b = rng.standard_normal(n)
+    x, info = oracle.sparse_lu_solve(rp2, ci2, v2, b)
+    xd = np.linalg.solve(A.toarray(), b)
+    assert np.linalg.norm(x - xd) / np.linalg.norm(xd) < 1e-10
+
+
+def test_sparse_lu_oracle_singular_neumann_gets_a_solution(oracle):
+    """All-Neumann pressure system (singular, consistent rhs): the vanishing
+    last pivot is replaced and the result solves the system."""
+    om = rect(oracle, 20, 16, 1.0, 1.0)
+    f = om.faces()
+    bc = np.ones(om.n_faces, np.int32)  # normal gradient everywhere
+    rng = np.random.default_rng(3)
+    rp, ci, v, _ = om.laplacian(rng.uniform(0.5, 2.0, om.n_faces), bc,
+                                np.zeros(om.n_faces))
+    A = sp.csr_matrix((v, ci, rp))
+    b = rng.standard_normal(om.n_cells)
+    b -= b.mean()  # consistent: orthogonal to the constant null vector
+    x, info = oracle.sparse_lu_solve(rp, ci, v, b)
+    assert info["replaced"] >= 1
+    assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-9
