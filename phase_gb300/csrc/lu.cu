@@ -15,14 +15,17 @@
 //    with partial pivoting over its fully summed rows, and writes it back;
 //  * large fronts: a warp per row assembles the row in global memory (the
 //    same sums in the same order), a CTA adds the owned matrix entries, then
-//    32-column panels: the panel's diagonal block is factorised by one warp
-//    (partial pivoting inside the block), L21 = F21 U11^-1 and U12 =
-//    L11^-1 P F12 by TRSM tiles, and the trailing block F22 -= L21 U12 by
-//    64 x 64 update tiles.
+//    32-column panels as LAPACK's blocked dgetrf does them: the tall panel
+//    is factorised by one CTA with partial pivoting over the front's fully
+//    summed rows, its interchanges are applied to the columns right of it
+//    and U12 = L11^-1 A12 by TRSM tiles, and the trailing block F22 -= L21
+//    U12 by 64 x 64 update tiles.
 //
-// Row interchanges follow LINPACK's convention (dgefa/dgesl): pivot step c
-// exchanges two rows in columns c.. only and records the partner row, and
-// the forward solve replays exchange and elimination step by step.  A pivot
+// Row interchanges: inside a panel whole panel rows are exchanged (LAPACK's
+// convention), across panels the columns left of the panel are not
+// touched (LINPACK's, dgefa/dgesl), so the forward solve applies each
+// panel's interchanges to the right-hand side just before that panel's
+// eliminations; a small front is one panel per column.  A pivot
 // whose magnitude is at most 1e-13 of the largest entry of its column in A
 // is replaced by that entry's magnitude and counted: a consistent singular
 // system (pure Neumann pressure) then gets one of its solutions instead of
@@ -204,20 +207,35 @@ k_lu_scatter(const int32_t *__restrict__ list, LuArgs a,
     F[a.e_pos[e]] += entry_sum(a, vals, e);
 }
 
-// panel q's diagonal block, one warp per front
-__global__ void __launch_bounds__(32)
-k_lu_diag(const int32_t *__restrict__ list, int q, LuArgs a) {
-  __shared__ double D[kLuPanel][kLuPanel + 1];
-  const int lane = threadIdx.x;
+// panel q of the large fronts, one CTA per front: the tall panel (rows
+// c0 .. m-1, columns c0 .. c0+b-1) is factorised with partial pivoting over
+// the fully summed rows c .. k-1 of each column c; an interchange swaps the
+// whole panel rows (LAPACK's convention inside a panel), which the TRSM
+// kernel then applies to the columns right of the panel.  Warps own rows,
+// lanes the panel's columns.
+constexpr int kPanelThreads = 1024;
+__global__ void __launch_bounds__(kPanelThreads)
+k_lu_panel(const int32_t *__restrict__ list, int q, LuArgs a) {
+  __shared__ double wbest[kPanelThreads / 32];
+  __shared__ int wrow[kPanelThreads / 32];
+  __shared__ int piv_row;
+  __shared__ double piv_val;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const LuFront f = a.fronts[list[blockIdx.x]];
-  const int m = f.m, c0 = q * kLuPanel, b = min(kLuPanel, f.k - c0);
+  const int m = f.m, k = f.k, c0 = q * kLuPanel, b = min(kLuPanel, k - c0);
   double *F = a.pool + f.off;
-  for (int r = 0; r < b; ++r)
-    D[r][lane] = lane < b ? F[(size_t)(c0 + r) * m + c0 + lane] : 0.;
-  __syncwarp();
   for (int s = 0; s < b; ++s) {
-    double best = lane >= s && lane < b ? fabs(D[lane][s]) : -1.;
-    int br = lane;
+    const int c = c0 + s;
+    // pivot search: thread per row, then warps, then the block
+    double best = -1.;
+    int br = c;
+    for (int r = c + tid; r < k; r += kPanelThreads) {
+      const double v = fabs(F[(size_t)r * m + c]);
+      if (v > best) {
+        best = v;
+        br = r;
+      }
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const double ob = __shfl_down_sync(0xffffffffu, best, o);
@@ -227,89 +245,93 @@ k_lu_diag(const int32_t *__restrict__ list, int q, LuArgs a) {
         br = orr;
       }
     }
-    const int r = __shfl_sync(0xffffffffu, br, 0);
-    if (r != s && lane >= s) {
-      const double t = D[s][lane];
-      D[s][lane] = D[r][lane];
-      D[r][lane] = t;
-    }
-    __syncwarp();
-    double p = D[s][s];
     if (lane == 0) {
-      a.ipiv[f.s0 + c0 + s] = c0 + r;
-      p = checked_pivot(a, p, f.s0 + c0 + s);
-      D[s][s] = p;
+      wbest[warp] = best;
+      wrow[warp] = br;
     }
-    p = __shfl_sync(0xffffffffu, p, 0);
-    __syncwarp();
-    if (lane > s && lane < b) D[lane][s] /= p;
-    __syncwarp();
-    if (lane > s && lane < b)
-      for (int i = s + 1; i < b; ++i) D[i][lane] -= D[i][s] * D[s][lane];
-    __syncwarp();
+    __syncthreads();
+    if (warp == 0) {
+      best = wbest[lane];
+      br = wrow[lane];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_down_sync(0xffffffffu, best, o);
+        const int orr = __shfl_down_sync(0xffffffffu, br, o);
+        if (ob > best || (ob == best && orr < br)) {
+          best = ob;
+          br = orr;
+        }
+      }
+      const int r = __shfl_sync(0xffffffffu, br, 0);
+      if (r != c && lane < b) {
+        const double t = F[(size_t)c * m + c0 + lane];
+        F[(size_t)c * m + c0 + lane] = F[(size_t)r * m + c0 + lane];
+        F[(size_t)r * m + c0 + lane] = t;
+      }
+      __syncwarp();
+      if (lane == 0) {
+        a.ipiv[f.s0 + c] = r;
+        const double p = checked_pivot(a, F[(size_t)c * m + c], f.s0 + c);
+        F[(size_t)c * m + c] = p;
+        piv_row = r;
+        piv_val = p;
+      }
+    }
+    __syncthreads();
+    const double p = piv_val;
+    const double prow = lane < b ? F[(size_t)c * m + c0 + lane] : 0.;
+    for (int i = c + 1 + warp; i < m; i += kPanelThreads / 32) {
+      double *row = F + (size_t)i * m + c0;
+      double v = lane < b ? row[lane] : 0.;
+      const double l = __shfl_sync(0xffffffffu, v, s) / p;
+      if (lane == s) v = l;
+      else if (lane > s) v -= l * prow;
+      if (lane >= s && lane < b) row[lane] = v;
+    }
+    __syncthreads();
   }
-  for (int r = 0; r < b; ++r)
-    if (lane < b) F[(size_t)(c0 + r) * m + c0 + lane] = D[r][lane];
+  (void)piv_row;
 }
 
-// TRSM tiles of panel q: kind 0, L21 = F21 U11^-1 (a thread per row); kind
-// 1, U12 = L11^-1 P F12 (a thread per column, exchanges and eliminations
-// interleaved as in the forward solve)
-__global__ void __launch_bounds__(kLuTrsmRows)
+// U12 tiles of panel q: the panel's interchanges replayed on the columns
+// right of it (rows c0 .. k-1, in global memory), then U12 = L11^-1 A12
+// (a thread per column)
+__global__ void __launch_bounds__(kLuTrsmCols)
 k_lu_trsm(const int32_t *__restrict__ tasks, int q, LuArgs a) {
   __shared__ double D[kLuPanel][kLuPanel + 1];
-  __shared__ double T[kLuPanel][kLuTrsmCols + 1];
   __shared__ int pr[kLuPanel];
   const int tid = threadIdx.x;
-  const int t = tasks[3 * blockIdx.x], kind = tasks[3 * blockIdx.x + 1],
-            t0 = tasks[3 * blockIdx.x + 2];
+  const int t = tasks[3 * blockIdx.x], t0 = tasks[3 * blockIdx.x + 2];
   const LuFront f = a.fronts[t];
   const int m = f.m, c0 = q * kLuPanel, b = min(kLuPanel, f.k - c0);
   double *F = a.pool + f.off;
-  for (int e = tid; e < kLuPanel * kLuPanel; e += kLuTrsmRows) {
+  for (int e = tid; e < kLuPanel * kLuPanel; e += kLuTrsmCols) {
     const int r = e / kLuPanel, c = e % kLuPanel;
     D[r][c] = r < b && c < b ? F[(size_t)(c0 + r) * m + c0 + c] : 0.;
   }
-  if (tid < kLuPanel) pr[tid] = tid < b ? a.ipiv[f.s0 + c0 + tid] - c0 : tid;
+  if (tid < kLuPanel) pr[tid] = tid < b ? a.ipiv[f.s0 + c0 + tid] : 0;
   __syncthreads();
-  const int base = c0 + b;
-  if (kind == 0) {
-    const int i = base + t0 + tid;
-    if (i >= m) return;
-    double *row = F + (size_t)i * m + c0;
-    double l[kLuPanel];
-#pragma unroll
-    for (int s = 0; s < kLuPanel; ++s) l[s] = s < b ? row[s] : 0.;
-#pragma unroll
-    for (int s = 0; s < kLuPanel; ++s) {
-      if (s < b) {
-        l[s] /= D[s][s];
-#pragma unroll
-        for (int j = s + 1; j < kLuPanel; ++j)
-          if (j < b) l[j] -= l[s] * D[s][j];
-      }
+  const int j = c0 + b + t0 + tid;
+  if (j >= m) return;
+  for (int s = 0; s < b; ++s) {
+    const int r = pr[s];
+    if (r != c0 + s) {
+      const double x = F[(size_t)(c0 + s) * m + j];
+      F[(size_t)(c0 + s) * m + j] = F[(size_t)r * m + j];
+      F[(size_t)r * m + j] = x;
     }
-#pragma unroll
-    for (int s = 0; s < kLuPanel; ++s)
-      if (s < b) row[s] = l[s];
-  } else {
-    const int j = base + t0 + tid;
-    const bool live = j < m;
-    for (int r = 0; r < b; ++r)
-      T[r][tid] = live ? F[(size_t)(c0 + r) * m + j] : 0.;
-    if (!live) return;
-    for (int s = 0; s < b; ++s) {
-      const int r = pr[s];
-      if (r != s) {
-        const double x = T[s][tid];
-        T[s][tid] = T[r][tid];
-        T[r][tid] = x;
-      }
-      const double ts = T[s][tid];
-      for (int i = s + 1; i < b; ++i) T[i][tid] -= D[i][s] * ts;
-    }
-    for (int r = 0; r < b; ++r) F[(size_t)(c0 + r) * m + j] = T[r][tid];
   }
+  double T[kLuPanel];
+#pragma unroll
+  for (int r = 0; r < kLuPanel; ++r) T[r] = r < b ? F[(size_t)(c0 + r) * m + j] : 0.;
+#pragma unroll
+  for (int s = 0; s < kLuPanel; ++s) {
+#pragma unroll
+    for (int i = s + 1; i < kLuPanel; ++i) T[i] -= D[i][s] * T[s];
+  }
+#pragma unroll
+  for (int r = 0; r < kLuPanel; ++r)
+    if (r < b) F[(size_t)(c0 + r) * m + j] = T[r];
 }
 
 // trailing update of panel q: F22 -= L21 U12 on a 64 x 64 tile; each thread
@@ -416,8 +438,9 @@ k_lu_fwd(const int32_t *__restrict__ list, LuArgs a,
       }
       __syncthreads();
       if (warp == 0) {
-        for (int s = 0; s < b; ++s) {
-          if (lane == 0) {
+        // the panel's interchanges (rows c0 .. k-1), then L11
+        if (lane == 0)
+          for (int s = 0; s < b; ++s) {
             const int r = a.ipiv[f.s0 + c0 + s];
             if (r != c0 + s) {
               const double x = w[c0 + s];
@@ -425,7 +448,8 @@ k_lu_fwd(const int32_t *__restrict__ list, LuArgs a,
               w[r] = x;
             }
           }
-          __syncwarp();
+        __syncwarp();
+        for (int s = 0; s < b; ++s) {
           const double ws = w[c0 + s];
           if (lane > s && lane < b) w[c0 + lane] -= D[lane][s] * ws;
           __syncwarp();
@@ -713,11 +737,11 @@ int factor(pg_lu *L, const double *vals) {
     count_launches(2);
     for (const LuSymbolic::PanelStep &p : s.steps) {
       if (p.height != h) continue;
-      k_lu_diag<<<p.diag_end - p.diag_ptr, 32, 0, st>>>(L->pt_diag.p + p.diag_ptr,
-                                                       p.panel, a);
+      k_lu_panel<<<p.diag_end - p.diag_ptr, kPanelThreads, 0, st>>>(
+          L->pt_diag.p + p.diag_ptr, p.panel, a);
       count_launches(1);
       if (p.trsm_end > p.trsm_ptr) {
-        k_lu_trsm<<<p.trsm_end - p.trsm_ptr, kLuTrsmRows, 0, st>>>(
+        k_lu_trsm<<<p.trsm_end - p.trsm_ptr, kLuTrsmCols, 0, st>>>(
             L->pt_trsm.p + 3 * (size_t)p.trsm_ptr, p.panel, a);
         count_launches(1);
       }

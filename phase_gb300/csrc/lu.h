@@ -12,7 +12,6 @@ namespace pg {
 // in global memory and factorised in 32-column panels by batched kernels.
 constexpr int kLuSmallM = 112;
 constexpr int kLuPanel = 32;
-constexpr int kLuTrsmRows = 128;  // rows of L21 per TRSM tile (thread per row)
 constexpr int kLuTrsmCols = 128;  // columns of U12 per TRSM tile
 constexpr int kLuUpd = 64;        // edge of a trailing-update tile
 
@@ -62,8 +61,8 @@ struct LuSymbolic {
   // k > 32 q (diag), their TRSM tiles and their update tiles
   struct PanelStep {
     int height, panel;
-    int diag_ptr, diag_end;    // into pt_diag (front ids)
-    int trsm_ptr, trsm_end;    // into pt_trsm (front, kind, tile)
+    int diag_ptr, diag_end;    // into pt_diag (front ids): panel CTAs
+    int trsm_ptr, trsm_end;    // into pt_trsm (front, 1, first column)
     int upd_ptr, upd_end;      // into pt_upd (front, tile_i, tile_j)
   };
   std::vector<PanelStep> steps;

@@ -400,11 +400,6 @@ int lu_analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
         const int b = std::min(kLuPanel, f.k - c0);
         const int rest = f.m - c0 - b;  // trailing rows and columns
         s.pt_diag.push_back(t);
-        for (int r0 = 0; r0 < rest; r0 += kLuTrsmRows) {  // L21 tiles
-          s.pt_trsm.push_back(t);
-          s.pt_trsm.push_back(0);
-          s.pt_trsm.push_back(r0);
-        }
         for (int j0 = 0; j0 < rest; j0 += kLuTrsmCols) {  // U12 tiles
           s.pt_trsm.push_back(t);
           s.pt_trsm.push_back(1);

@@ -9,13 +9,13 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CPP = os.path.join(ROOT, "phase_gb300", "cpp")
 
 
-def compile_shim(out, main="shim_test.cpp"):
+def compile_shim(out, main="shim_test.cpp", plugin="Gb300SparseMatrixSolver.cpp"):
     import __graft_entry__
     __graft_entry__.build()
     cmd = ["g++", "-std=c++17", "-O1", "-I", os.path.join(CPP, "standin"),
            "-I", CPP, "-I", os.path.join(ROOT, "include"),
            os.path.join(ROOT, "tests", "cpp", main),
-           os.path.join(CPP, "Gb300SparseMatrixSolver.cpp"),
+           os.path.join(CPP, plugin),
            "-L", os.path.join(ROOT, "phase_gb300"), "-lphase_gb300",
            "-Wl,-rpath," + os.path.join(ROOT, "phase_gb300"), "-o", out]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
@@ -106,3 +106,19 @@ def test_fv_shim_solves_the_bubble_pressure_step_on_gpu(tmp_path, oracle):
     # two solves stopped at 1e-10 on a 1000:1 system differ by up to
     # ~200x their residual
     assert np.linalg.norm(p - xo) / np.linalg.norm(xo) < 1e-6
+
+
+def test_lu_shim_compiles(tmp_path):
+    """The direct backend (drop-in for EigenSparseMatrixSolver) compiles
+    against the stand-in Phase headers."""
+    compile_shim(str(tmp_path / "lu_shim_test"), "lu_shim_test.cpp",
+                 "Gb300SparseLUSolver.cpp")
+
+
+@pytest.mark.gpu
+def test_lu_shim_solves_on_gpu(tmp_path):
+    exe = str(tmp_path / "lu_shim_test")
+    compile_shim(exe, "lu_shim_test.cpp", "Gb300SparseLUSolver.cpp")
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "direct solve" in r.stdout
