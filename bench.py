@@ -101,7 +101,7 @@ def parse():
                     help="sequence mode: leave out the cylinder and batched "
                          "summaries")
     ap.add_argument("--mode", default="sequence",
-                    choices=["sequence", "single", "batch"])
+                    choices=["sequence", "single", "batch", "direct"])
     ap.add_argument("--systems", type=int, default=256,
                     help="batch mode: number of immersed-boundary systems")
     ap.add_argument("--t0", type=int, default=1801,
@@ -538,6 +538,7 @@ def run_sequence(args):
     if rank == 0 and world == 1 and not args.no_extras:
         extras["cylinder"] = cylinder_summary(pg, torch, args)
         extras["batch"] = batch_summary(pg, torch, args)
+        extras["direct"] = direct_summary(pg, args)
 
     converged = all(st["status"] == 0 and st["rel_residual"] <= 1e-8
                     for st in st_m + st_p + st_q)
@@ -701,6 +702,71 @@ def batch_summary(pg, torch, args, n_systems=256):
             "iters": {"min": int(min(iters)), "median": float(np.median(iters)),
                       "max": int(max(iters))},
             "converged": bool(ok), "host_setup_s": round(setup_s, 2)}
+
+
+def direct_summary(pg, args, nx_list=(80, 1024), cpu_nx=128):
+    """The direct backend (the drop-in for EigenSparseMatrixSolver, which
+    factorises and solves on every call): per workload the device time of
+    the factorisation and of the solve (mean of three after a warm-up), the
+    host analysis once per pattern, the factorisation's flops, and the FP64
+    true residual; the CPU leg is the oracle's band LU (single thread) on
+    the bubble system of the cpu_nx mesh, beside the device on the same
+    system."""
+    import numpy as np
+    from phase_gb300 import simple
+    out = {}
+
+    def run(name, eqn):
+        lu = pg.SparseLU()
+        fac, sol, res = [], [], []
+        for _ in range(4):
+            lu.set_eqn(eqn)  # new values: factorised again
+            lu.solve()
+            st = lu.stats
+            fac.append(st.factor_ms)
+            sol.append(st.solve_ms)
+            res.append(st.rel_residual)
+        st = lu.stats
+        f_ms = float(np.mean(fac[1:]))
+        out[name] = {"n": int(eqn.n), "analyse_ms": round(st.analyse_ms, 1),
+                     "factor_ms": round(f_ms, 3),
+                     "solve_ms": round(float(np.mean(sol[1:])), 3),
+                     "factor_gflops": round(st.flops / f_ms * 1e-6, 1),
+                     "fronts": st.n_fronts, "heights": st.n_heights,
+                     "max_front": st.max_front,
+                     "factor_entries": int(st.factor_entries),
+                     "replaced_pivots": st.replaced_pivots,
+                     "rel_residual": float(max(res))}
+        return lu
+
+    for nx in nx_list:
+        if nx == 80:
+            eqn = simple.simple_pcorr(pg, 80, 80)["eqn"]
+            run("cavity_80x80_pcorr", eqn)
+        else:
+            mesh, w, coeff = build_system(nx)
+            eqn = pg.fv.laplacian(coeff, mesh, w["bc_type"], w["bc_value"],
+                                  w["u"])
+            run(f"rising_bubble_{nx}x{nx}", eqn)
+    if not args.no_cpu_baseline:
+        import oracle_bind
+        mesh, w, coeff = build_system(cpu_nx)
+        eqn = pg.fv.laplacian(coeff, mesh, w["bc_type"], w["bc_value"], w["u"])
+        lu = run(f"rising_bubble_{cpu_nx}x{cpu_nx}", eqn)
+        rp, ci, v, rhs = eqn.export()
+        t0 = time.perf_counter()
+        xo, info = oracle_bind.sparse_lu_solve(rp, ci, v, -rhs)
+        cpu_ms = (time.perf_counter() - t0) * 1e3
+        x = lu.x()
+        out["cpu_baseline"] = {
+            "kind": "port", "cores": 1, "ms": round(cpu_ms, 1),
+            "sample": f"oracle band LU (RCM order, partial pivoting) of the "
+                      f"{cpu_nx}x{cpu_nx} rising-bubble system, factorise + "
+                      f"solve; bandwidths {info['band']}",
+            "device_ms": round(out[f"rising_bubble_{cpu_nx}x{cpu_nx}"]["factor_ms"]
+                               + out[f"rising_bubble_{cpu_nx}x{cpu_nx}"]["solve_ms"], 3),
+            "x_rel_diff": float(np.linalg.norm(x - xo) / np.linalg.norm(xo))}
+    return out
 
 
 def e2e_learned(pg, guess, seq, net, have_w, steps, torch, dev, coarse,
@@ -1156,13 +1222,22 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_direct(args):
+    """--mode direct: the direct backend alone (the summary of the default
+    line), for profiling."""
+    import __graft_entry__
+    __graft_entry__.build()
+    import phase_gb300 as pg
+    print(json.dumps({"direct": direct_summary(pg, args, nx_list=(args.nx,))}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     else:
         {"sequence": run_sequence, "single": run_single,
-         "batch": run_batch}[args.mode](args)
+         "batch": run_batch, "direct": run_direct}[args.mode](args)
 
 
 if __name__ == "__main__":
