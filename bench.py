@@ -328,6 +328,7 @@ def kernel_roofline(pg, solver, n, nnz, dd, eqn=None, coarse=0):
                                          / peak, 4) for k in bytes_of},
             "per_kernel_ms": {k: round(v, 5) for k, v in ms_of.items()},
             "factor_ms": round(prof["factor"], 4),
+            "coarse_inverse_ms": round(prof["coarse_inverse"], 4),
             "frac_of_8tbs": round(achieved / 8000.0, 4)}
 
 

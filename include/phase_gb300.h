@@ -439,8 +439,9 @@ int pg_solver_get_x(const pg_solver *s, double *x, int ptr_kind);
  * the subdomain sums and the correction z += Z y, for cfg.coarse = 2 the
  * deflation's kernels beside the sweep (the combined input with its
  * subdomain sums, y = A_c^-1 Z^T p and p - A Z y; float-float ones under
- * PG_MIXED).  Leaves the solver's state untouched.  (No reference
- * counterpart: measurement.) */
+ * PG_MIXED), ms[8] the coarse matrix's assembly and inversion alone (0
+ * without a coarse space).  Leaves the solver's state untouched.  (No
+ * reference counterpart: measurement.) */
 int pg_solver_profile(pg_solver *s, int reps, double *ms);
 
 /* ---------------------------------------------------------------------

@@ -600,12 +600,13 @@ class SparseMatrixSolver:
         """Per-launch ms of the hot kernels on the current system: FP64 SpMV,
         preconditioner apply, x/r update, ILU(0) factorisation (with the
         coarse inverse), for the mixed precision solver the float-float
-        ILU(0) apply, SpMV and update, and the coarse correction."""
-        ms = np.zeros(8)
+        ILU(0) apply, SpMV and update, the coarse correction, and the coarse
+        matrix's assembly and inversion alone."""
+        ms = np.zeros(9)
         _check(lib().pg_solver_profile(self._h, int(reps), _ptr(ms)))
         return dict(spmv=ms[0], precond=ms[1], update=ms[2], factor=ms[3],
                     precond_dd=ms[4], spmv_dd=ms[5], update_dd=ms[6],
-                    coarse=ms[7])
+                    coarse=ms[7], coarse_inverse=ms[8])
 
     def printStatus(self, msg: str):
         print(f"{msg} iterations = {self.nIters()}, error = {self.error():f}.")

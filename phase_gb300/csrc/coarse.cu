@@ -26,6 +26,7 @@
 
 #include "dd.cuh"
 #include "kernels.cuh"
+#include "lu.h"
 
 namespace pg {
 namespace {
@@ -69,6 +70,30 @@ k_coarse_assemble(int K, const int32_t *__restrict__ sub_ptr,
     double sum = 0.;
     for (int t = 0; t < kCoarseBlock; ++t) sum += part[t * S + j];
     ac[(size_t)s * K + cnb[cptr[s] + j]] = (float)sum;
+  }
+}
+
+// the same sums as k_coarse_assemble, kept in FP64 as the values of the
+// coarse matrix's CSR (row s: columns cnb[cptr[s] .. cptr[s+1]))
+__global__ void __launch_bounds__(kCoarseBlock)
+k_coarse_assemble_csr(const int32_t *__restrict__ sub_ptr,
+                      const int32_t *__restrict__ prp,
+                      const double *__restrict__ val,
+                      const int32_t *__restrict__ cptr,
+                      const uint8_t *__restrict__ cslot,
+                      double *__restrict__ cvals) {
+  extern __shared__ double part[];  // [kCoarseBlock][S]
+  const int s = blockIdx.x;
+  const int S = cptr[s + 1] - cptr[s];
+  for (int j = 0; j < S; ++j) part[threadIdx.x * S + j] = 0.;
+  const int32_t e0 = prp[sub_ptr[s]], e1 = prp[sub_ptr[s + 1]];
+  for (int32_t k = e0 + threadIdx.x; k < e1; k += kCoarseBlock)
+    part[threadIdx.x * S + cslot[k]] += val[k];
+  __syncthreads();
+  for (int j = threadIdx.x; j < S; j += kCoarseBlock) {
+    double sum = 0.;
+    for (int t = 0; t < kCoarseBlock; ++t) sum += part[t * S + j];
+    cvals[cptr[s] + j] = sum;
   }
 }
 
@@ -910,6 +935,16 @@ void launch_coarse_setup(const CoarseDev &c, const double *pvals,
   else
     steps();
   count_launches(2 * nblk);
+}
+
+int launch_coarse_setup_lu(const CoarseDev &c, pg_lu *lu, double *cvals,
+                           const double *pvals, const int32_t *prp,
+                           cudaStream_t st) {
+  const size_t smem = (size_t)kCoarseBlock * c.max_cnb * sizeof(double);
+  k_coarse_assemble_csr<<<c.K, kCoarseBlock, smem, st>>>(c.sub_ptr, prp, pvals,
+                                                         c.cptr, c.cslot, cvals);
+  count_launches(1);
+  return lu_inverse_run(lu, cvals, c.ac, st);
 }
 
 void launch_coarse_apply(const CoarseDev &c, const double *in, double *z,

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 
+struct pg_lu;
+
 namespace pg {
 
 // Host-side count of kernel launches issued by the library.
@@ -356,6 +358,11 @@ void launch_coarse_apply_b(const CoarseBatchDev &c, int K, const double *in,
 
 // A_c from the permuted values, then A_c^-1 in place (the K elimination
 // steps are captured into *gj_graph on first use when gj_graph is given)
+// The coarse matrix assembled as a CSR in FP64 (cvals, the pattern of
+// cptr / cnb) and inverted through the sparse LU into c.ac (FP32, dense)
+int launch_coarse_setup_lu(const CoarseDev &c, pg_lu *lu,
+                           double *cvals, const double *pvals,
+                           const int32_t *prp, cudaStream_t st);
 void launch_coarse_setup(const CoarseDev &c, const double *pvals,
                          const int32_t *prp, cudaGraphExec_t *gj_graph,
                          cudaStream_t st);

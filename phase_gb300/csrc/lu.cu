@@ -591,6 +591,100 @@ k_lu_residual(int n, const int32_t *__restrict__ rp, const int32_t *__restrict__
   }
 }
 
+// ------------------------------------------------- dense inverse (FP32)
+// A^-1 column tile by column tile: the identity (new numbering) as 32
+// right-hand sides per CTA, forward eliminated front by front (LINPACK
+// order, FP64 factors read and rounded to FP32), then back substituted
+// from the root down; a front's tile whose columns lie outside its subtree
+// is zero and is only written as zeros.  Small fronts only (m <= kLuSmallM).
+constexpr int kInvCols = 32, kInvRows = 8;
+
+__global__ void __launch_bounds__(kInvCols * kInvRows)
+k_lu_inv_fwd(const int32_t *__restrict__ list, LuArgs a, int n,
+             float *__restrict__ Y, float *__restrict__ CP) {
+  __shared__ float W[kLuSmallM][kInvCols + 1];
+  const int cc = threadIdx.x & (kInvCols - 1), ty = threadIdx.x / kInvCols;
+  const LuFront f = a.fronts[list[blockIdx.x]];
+  const int m = f.m, k = f.k, j0 = blockIdx.y * kInvCols;
+  const int j = j0 + cc;
+  const bool live = j0 + kInvCols > f.first && j0 < f.s0 + k;
+  for (int i = ty; i < m; i += kInvRows)
+    W[i][cc] = live && i < k && f.s0 + i == j ? 1.f : 0.f;
+  __syncthreads();
+  if (live) {
+    for (int c = 0; c < f.n_child; ++c) {
+      const LuFront ch = a.fronts[a.children[f.child_ptr + c]];
+      const int u = ch.m - ch.k;
+      const int32_t *rel = a.rel + ch.rel_off;
+      for (int e = ty; e < u; e += kInvRows)
+        if (j < n) W[rel[e]][cc] += CP[(size_t)(ch.coff + e) * n + j];
+      __syncthreads();
+    }
+    const double *F = a.pool + f.off;
+    for (int c = 0; c < k; ++c) {
+      if (ty == 0) {
+        const int r = a.ipiv[f.s0 + c];
+        if (r != c) {
+          const float x = W[c][cc];
+          W[c][cc] = W[r][cc];
+          W[r][cc] = x;
+        }
+      }
+      __syncthreads();
+      const float wc = W[c][cc];
+      for (int i = c + 1 + ty; i < m; i += kInvRows)
+        W[i][cc] -= (float)F[i * m + c] * wc;
+      __syncthreads();
+    }
+  }
+  if (j >= n) return;
+  for (int i = ty; i < m; i += kInvRows) {
+    if (i < k) Y[(size_t)(f.s0 + i) * n + j] = W[i][cc];
+    else CP[(size_t)(f.coff + i - k) * n + j] = W[i][cc];
+  }
+}
+
+__global__ void __launch_bounds__(kInvCols * kInvRows)
+k_lu_inv_bwd(const int32_t *__restrict__ list, LuArgs a, int n,
+             float *__restrict__ Y) {
+  __shared__ float W[kLuSmallM][kInvCols + 1];
+  const int cc = threadIdx.x & (kInvCols - 1), ty = threadIdx.x / kInvCols;
+  const LuFront f = a.fronts[list[blockIdx.x]];
+  const int m = f.m, k = f.k, j = blockIdx.y * kInvCols + cc;
+  const bool ok = j < n;
+  for (int i = ty; i < m; i += kInvRows)
+    W[i][cc] = !ok ? 0.f
+               : i < k ? Y[(size_t)(f.s0 + i) * n + j]
+                       : Y[(size_t)a.fidx[f.idx + i] * n + j];
+  __syncthreads();
+  const double *F = a.pool + f.off;
+  // r = y_S - U12 x_U
+  for (int i = ty; i < k; i += kInvRows) {
+    float acc = 0.f;
+    for (int u = k; u < m; ++u) acc += (float)F[i * m + u] * W[u][cc];
+    W[i][cc] -= acc;
+  }
+  __syncthreads();
+  for (int c = k - 1; c >= 0; --c) {
+    if (ty == 0) W[c][cc] /= (float)F[c * m + c];
+    __syncthreads();
+    const float xc = W[c][cc];
+    for (int i = ty; i < c; i += kInvRows) W[i][cc] -= (float)F[i * m + c] * xc;
+    __syncthreads();
+  }
+  if (!ok) return;
+  for (int i = ty; i < k; i += kInvRows) Y[(size_t)(f.s0 + i) * n + j] = W[i][cc];
+}
+
+// out[I][J] = X[iperm[I]][iperm[J]] (caller's numbering)
+__global__ void k_lu_inv_out(int n, const int32_t *__restrict__ iperm,
+                             const float *__restrict__ X, float *__restrict__ out) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)n * n) return;
+  const int I = (int)(e / n), J = (int)(e % n);
+  out[e] = X[(size_t)iperm[I] * n + iperm[J]];
+}
+
 int grid_of(int64_t n, int b) { return (int)((n + b - 1) / b); }
 
 // opt in to large dynamic shared memory once per process
@@ -631,6 +725,10 @@ struct pg_lu {
   DevBuf<int32_t> ipiv, rp_st, ci_st;
   DevBuf<unsigned long long> cmax;
   DevBuf<int> n_rep;
+  // dense inverse (lu_inverse_run): the n x n result in new numbering, the
+  // contribution rows of every front x n, old -> new numbering
+  DevBuf<float> inv_y, inv_cp;
+  DevBuf<int32_t> iperm;
   // the CSR the last factorisation read (device), for the residual
   const int32_t *m_rp = nullptr, *m_ci = nullptr;
   const double *m_vals = nullptr;
@@ -705,8 +803,7 @@ int analyse_and_upload(pg_lu *L, const int32_t *rp, const int32_t *ci,
 }
 
 // the numeric factorisation of the values vals (caller's index space)
-int factor(pg_lu *L, const double *vals) {
-  cudaStream_t st = stream();
+int factor(pg_lu *L, const double *vals, cudaStream_t st) {
   const LuSymbolic &s = L->s;
   LuArgs a = args_of(L);
   PG_CUDA(cudaEventRecord(L->ev[0], st));
@@ -975,7 +1072,7 @@ extern "C" int pg_lu_solve(pg_lu *L, pg_lu_stats *stats) {
   PG_CHECK_ARG(L->analysed && L->have_vals && L->have_rhs,
                "pg_lu_solve: matrix and rhs must be set first");
   if (!L->factored) {
-    int rc = factor(L, L->m_vals);
+    int rc = factor(L, L->m_vals, stream());
     if (rc) return rc;
   }
   int rc = solve_now(L);
@@ -1041,3 +1138,57 @@ extern "C" int pg_lu_analyse_pattern(int64_t n, const int32_t *row_ptr,
   if (fidx) std::copy(s.fidx.begin(), s.fidx.end(), fidx);
   return PG_OK;
 }
+
+namespace pg {
+
+int lu_inverse_setup(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
+                     pg_lu **out) {
+  *out = nullptr;
+  pg_lu *L = nullptr;
+  int rc = pg_lu_create(&L);
+  if (rc) return rc;
+  L->rank = n;
+  rc = analyse_and_upload(L, row_ptr, col_ind, nullptr, nullptr);
+  if (rc || L->s.max_m > kLuSmallM) {
+    pg_lu_destroy(L);
+    return rc;
+  }
+  const size_t nn = (size_t)n * n;
+  cudaError_t e = L->inv_y.reserve(nn);
+  if (e == cudaSuccess) e = L->inv_cp.reserve((size_t)std::max<int64_t>(L->s.cpool, 1) * n);
+  if (e == cudaSuccess) e = L->iperm.upload(L->s.iperm);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream());
+  if (e != cudaSuccess) {
+    pg_lu_destroy(L);
+    return cuda_fail(e, "lu_inverse_setup", __FILE__, __LINE__);
+  }
+  *out = L;
+  return PG_OK;
+}
+
+int lu_inverse_run(pg_lu *L, const double *vals, float *out, cudaStream_t st) {
+  const LuSymbolic &s = L->s;
+  int rc = factor(L, vals, st);
+  if (rc) return rc;
+  LuArgs a = args_of(L);
+  const int n = (int)s.n;
+  const int tiles = (n + kInvCols - 1) / kInvCols;
+  for (int h = 0; h < s.n_heights; ++h) {
+    const int nf = s.h_all_ptr[h + 1] - s.h_all_ptr[h];
+    k_lu_inv_fwd<<<dim3(nf, tiles), kInvCols * kInvRows, 0, st>>>(
+        L->h_all.p + s.h_all_ptr[h], a, n, L->inv_y.p, L->inv_cp.p);
+  }
+  for (int h = s.n_heights - 1; h >= 0; --h) {
+    const int nf = s.h_all_ptr[h + 1] - s.h_all_ptr[h];
+    k_lu_inv_bwd<<<dim3(nf, tiles), kInvCols * kInvRows, 0, st>>>(
+        L->h_all.p + s.h_all_ptr[h], a, n, L->inv_y.p);
+  }
+  const int64_t nn = (int64_t)n * n;
+  k_lu_inv_out<<<(int)((nn + 255) / 256), 256, 0, st>>>(n, L->iperm.p,
+                                                         L->inv_y.p, out);
+  count_launches(2 * s.n_heights + 1);
+  PG_CUDA(cudaGetLastError());
+  return PG_OK;
+}
+
+}  // namespace pg

@@ -2,6 +2,8 @@
 // shared by the host analysis (lu_host.cpp) and the device factorisation and
 // solves (lu.cu).
 #pragma once
+#include <cuda_runtime.h>
+
 #include <cstdint>
 #include <vector>
 
@@ -32,6 +34,8 @@ struct LuFront {
   int32_t inv_off;   // parent-position -> this front's U index map
                      // (parent m entries, -1 where absent); large parents
   int32_t ent_ptr, ent_end;  // range of its original entries
+  int32_t first;             // smallest new index in its subtree
+  int32_t pad_;
 };
 
 struct LuSymbolic {
@@ -85,4 +89,20 @@ struct LuSymbolic {
 int lu_analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
                const double *x, const double *y, int leaf, LuSymbolic &s);
 
+}  // namespace pg
+
+// The LU as an inverse builder for small dense inverses of sparse matrices
+// (the two-level preconditioner's coarse matrix): analysis and buffers once
+// per pattern, then per set of values a factorisation and the dense inverse
+// issued on the caller's stream with no host synchronisation.
+struct pg_lu;
+namespace pg {
+// *out = nullptr (and PG_OK) when a front is larger than kLuSmallM: the
+// caller keeps its own method for such patterns
+int lu_inverse_setup(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
+                     pg_lu **out);
+// A^-1 (row-major n x n, FP32, the caller's numbering) of the values vals
+// (indexed like col_ind); FP64 factorisation, FP32 multi-right-hand-side
+// triangular solves
+int lu_inverse_run(pg_lu *lu, const double *vals, float *out, cudaStream_t st);
 }  // namespace pg

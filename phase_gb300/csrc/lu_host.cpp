@@ -338,6 +338,14 @@ int lu_analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
     }
   }
 
+  // subtree ranges (postorder: a subtree's indices are contiguous)
+  for (int t = 0; t < nf; ++t) {
+    LuFront &f = s.fronts[t];
+    f.first = f.s0;
+    for (int c = 0; c < f.n_child; ++c)
+      f.first = std::min(f.first, s.fronts[s.children[f.child_ptr + c]].first);
+  }
+
   // heights, storage, task lists
   std::vector<int32_t> height(nf, 0);
   for (int t = 0; t < nf; ++t) {

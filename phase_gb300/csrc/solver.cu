@@ -15,6 +15,7 @@
 
 #include "internal.h"
 #include "kernels.cuh"
+#include "lu.h"
 
 using namespace pg;
 
@@ -130,6 +131,12 @@ struct pg_solver {
   DevBuf<double> c_azv, c_y, c_tmp;
   DevBuf<float2> c_azv_dd, c_y_dd, c_tmp_dd;
   cudaGraphExec_t gj_graph = nullptr;
+  // the coarse inverse through the sparse LU of A_c (nested dissection,
+  // FP64 factorisation, FP32 dense inverse): built at the analysis when
+  // every front of A_c's pattern is small; otherwise (or with
+  // PG_COARSE_GJ=1) the blocked Gauss-Jordan inversion runs
+  pg_lu *c_lu = nullptr;
+  DevBuf<double> c_vals;
   // cfg.coarse_warm = -2: a solve applies the previous factorisation's
   // inverse while the new one is built on side2 into the other buffer
   // (c_ac / c_ac2, one Gauss-Jordan graph each); a join makes the new one
@@ -204,6 +211,7 @@ struct pg_solver {
     if (ev_cvals) cudaEventDestroy(ev_cvals);
     if (ev_coarse) cudaEventDestroy(ev_coarse);
     drop_graphs();
+    if (c_lu) pg_lu_destroy(c_lu);
     if (sc_host) cudaFreeHost(sc_host);
     if (bad_host) cudaFreeHost(bad_host);
     if (diff_host) cudaFreeHost(diff_host);
@@ -394,6 +402,16 @@ int upload_analysis(pg_solver *s) {
     for (DevBuf<float> *bf : {&s->c_W, &s->c_V, &s->c_C})
       if (e == cudaSuccess) e = bf->reserve(32 * K);
     if (e == cudaSuccess) e = s->c_sum.reserve(K);
+    if (s->c_lu) {
+      pg_lu_destroy(s->c_lu);
+      s->c_lu = nullptr;
+    }
+    const char *gj = std::getenv("PG_COARSE_GJ");
+    if (e == cudaSuccess && !(gj && gj[0] == '1')) {
+      int rc = lu_inverse_setup((int64_t)K, a.cptr.data(), a.cnb.data(), &s->c_lu);
+      if (rc) return rc;
+      if (s->c_lu) e = s->c_vals.reserve(a.cnb.size());
+    }
     if (s->cfg.coarse == 2) {
       up(s->c_azp, a.azp);
       up(s->c_azj, a.azj);
@@ -1146,8 +1164,14 @@ int factor(pg_solver *s, cudaStream_t st) {
       }
       PG_CUDA(cudaEventRecord(s->ev_cvals, st));
       PG_CUDA(cudaStreamWaitEvent(s->side2, s->ev_cvals, 0));
-      launch_coarse_setup(ct, s->pvals.p, s->prp.p, s->gj_graph_of(target),
-                          s->side2);
+      if (s->c_lu) {
+        int rc = launch_coarse_setup_lu(ct, s->c_lu, s->c_vals.p, s->pvals.p,
+                                        s->prp.p, s->side2);
+        if (rc) return rc;
+      } else {
+        launch_coarse_setup(ct, s->pvals.p, s->prp.p, s->gj_graph_of(target),
+                            s->side2);
+      }
       if (!reuse && s->cfg.coarse == 2) {
         launch_az_values(ct, (int)s->a.n, s->prp.p, s->pvals.p, azs);
         if (dd)
@@ -1635,18 +1659,26 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
     *out = (double)t / reps;
     return PG_OK;
   };
-  for (int i = 0; i < 8; ++i) ms[i] = 0.;
+  for (int i = 0; i < 9; ++i) ms[i] = 0.;
   // vectors: 0 ph/sh, 1 v/t, 2 rh, 3 r, 4 p/s, 5 x, 6 z
   int rc = timed([&] { launch_spmv_v<double, double>(d, s->pvals.p, d8[0].p, d8[1].p, d8[2].p, s->sc.p, w, st); }, &ms[0]);
   if (!rc) rc = timed([&] { launch_precond<double, double>(s->cfg.precond, 1, d, s->jdinv.p, d8[3].p, d8[4].p, d8[1].p, d8[6].p, s->sc.p, st); }, &ms[1]);
   if (!rc) rc = timed([&] { launch_update<double>(d.n, d8[5].p, d8[3].p, d8[0].p, d8[6].p, d8[4].p, d8[1].p, d8[2].p, s->sc.p, w, st); }, &ms[2]);
+  // the coarse matrix and its inverse (into the buffer the solves apply)
+  auto coarse_setup = [&] {
+    if (s->c_lu)
+      launch_coarse_setup_lu(s->coarse(), s->c_lu, s->c_vals.p, s->pvals.p,
+                             s->prp.p, st);
+    else
+      launch_coarse_setup(s->coarse(), s->pvals.p, s->prp.p,
+                          s->gj_graph_of(s->ac_ready), st);
+  };
   if (!rc && s->cfg.precond == PG_PREC_ILU0)
     rc = timed([&] {
       launch_ilu0_factor(d, s->pvals.p, s->bad.p, dd, st);
-      if (s->coarse_on)
-        launch_coarse_setup(s->coarse(), s->pvals.p, s->prp.p,
-                            s->gj_graph_of(s->ac_ready), st);
+      if (s->coarse_on) coarse_setup();
     }, &ms[3]);
+  if (!rc && s->coarse_on) rc = timed(coarse_setup, &ms[8]);
   if (!rc && s->coarse_on) {
     const CoarseDev c = s->coarse();
     if (s->cfg.coarse == 2 && dd)
