@@ -599,15 +599,31 @@ k_lu_residual(int n, const int32_t *__restrict__ rp, const int32_t *__restrict__
 // is zero and is only written as zeros.  Small fronts only (m <= kLuSmallM).
 constexpr int kInvCols = 32, kInvRows = 8;
 
+// FP32 copy of the factor pool (read by the inverse's triangular solves)
+__global__ void k_lu_pool_f32(int64_t n, const double *__restrict__ src,
+                              float *__restrict__ dst) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (float)src[i];
+}
+
+// the front's m x m factor staged in shared memory (FP32), then W
+__device__ __forceinline__ void stage_front(const float *__restrict__ F32,
+                                            int m, float *Fs) {
+  for (int e = threadIdx.x; e < m * m; e += kInvCols * kInvRows) Fs[e] = F32[e];
+}
+
 __global__ void __launch_bounds__(kInvCols * kInvRows)
-k_lu_inv_fwd(const int32_t *__restrict__ list, LuArgs a, int n,
-             float *__restrict__ Y, float *__restrict__ CP) {
-  __shared__ float W[kLuSmallM][kInvCols + 1];
+k_lu_inv_fwd(const int32_t *__restrict__ list, LuArgs a,
+             const float *__restrict__ pool32, int n, float *__restrict__ Y,
+             float *__restrict__ CP) {
+  extern __shared__ float smf[];
   const int cc = threadIdx.x & (kInvCols - 1), ty = threadIdx.x / kInvCols;
   const LuFront f = a.fronts[list[blockIdx.x]];
   const int m = f.m, k = f.k, j0 = blockIdx.y * kInvCols;
   const int j = j0 + cc;
+  float *Fs = smf, (*W)[kInvCols + 1] = (float(*)[kInvCols + 1])(smf + m * m);
   const bool live = j0 + kInvCols > f.first && j0 < f.s0 + k;
+  if (live) stage_front(pool32 + f.off, m, Fs);
   for (int i = ty; i < m; i += kInvRows)
     W[i][cc] = live && i < k && f.s0 + i == j ? 1.f : 0.f;
   __syncthreads();
@@ -620,7 +636,6 @@ k_lu_inv_fwd(const int32_t *__restrict__ list, LuArgs a, int n,
         if (j < n) W[rel[e]][cc] += CP[(size_t)(ch.coff + e) * n + j];
       __syncthreads();
     }
-    const double *F = a.pool + f.off;
     for (int c = 0; c < k; ++c) {
       if (ty == 0) {
         const int r = a.ipiv[f.s0 + c];
@@ -632,8 +647,7 @@ k_lu_inv_fwd(const int32_t *__restrict__ list, LuArgs a, int n,
       }
       __syncthreads();
       const float wc = W[c][cc];
-      for (int i = c + 1 + ty; i < m; i += kInvRows)
-        W[i][cc] -= (float)F[i * m + c] * wc;
+      for (int i = c + 1 + ty; i < m; i += kInvRows) W[i][cc] -= Fs[i * m + c] * wc;
       __syncthreads();
     }
   }
@@ -645,31 +659,32 @@ k_lu_inv_fwd(const int32_t *__restrict__ list, LuArgs a, int n,
 }
 
 __global__ void __launch_bounds__(kInvCols * kInvRows)
-k_lu_inv_bwd(const int32_t *__restrict__ list, LuArgs a, int n,
-             float *__restrict__ Y) {
-  __shared__ float W[kLuSmallM][kInvCols + 1];
+k_lu_inv_bwd(const int32_t *__restrict__ list, LuArgs a,
+             const float *__restrict__ pool32, int n, float *__restrict__ Y) {
+  extern __shared__ float smf[];
   const int cc = threadIdx.x & (kInvCols - 1), ty = threadIdx.x / kInvCols;
   const LuFront f = a.fronts[list[blockIdx.x]];
   const int m = f.m, k = f.k, j = blockIdx.y * kInvCols + cc;
   const bool ok = j < n;
+  float *Fs = smf, (*W)[kInvCols + 1] = (float(*)[kInvCols + 1])(smf + m * m);
+  stage_front(pool32 + f.off, m, Fs);
   for (int i = ty; i < m; i += kInvRows)
     W[i][cc] = !ok ? 0.f
                : i < k ? Y[(size_t)(f.s0 + i) * n + j]
                        : Y[(size_t)a.fidx[f.idx + i] * n + j];
   __syncthreads();
-  const double *F = a.pool + f.off;
   // r = y_S - U12 x_U
   for (int i = ty; i < k; i += kInvRows) {
     float acc = 0.f;
-    for (int u = k; u < m; ++u) acc += (float)F[i * m + u] * W[u][cc];
+    for (int u = k; u < m; ++u) acc += Fs[i * m + u] * W[u][cc];
     W[i][cc] -= acc;
   }
   __syncthreads();
   for (int c = k - 1; c >= 0; --c) {
-    if (ty == 0) W[c][cc] /= (float)F[c * m + c];
+    if (ty == 0) W[c][cc] /= Fs[c * m + c];
     __syncthreads();
     const float xc = W[c][cc];
-    for (int i = ty; i < c; i += kInvRows) W[i][cc] -= (float)F[i * m + c] * xc;
+    for (int i = ty; i < c; i += kInvRows) W[i][cc] -= Fs[i * m + c] * xc;
     __syncthreads();
   }
   if (!ok) return;
@@ -726,8 +741,9 @@ struct pg_lu {
   DevBuf<unsigned long long> cmax;
   DevBuf<int> n_rep;
   // dense inverse (lu_inverse_run): the n x n result in new numbering, the
-  // contribution rows of every front x n, old -> new numbering
-  DevBuf<float> inv_y, inv_cp;
+  // contribution rows of every front x n, the factor pool in FP32, old ->
+  // new numbering
+  DevBuf<float> inv_y, inv_cp, pool32;
   DevBuf<int32_t> iperm;
   // the CSR the last factorisation read (device), for the residual
   const int32_t *m_rp = nullptr, *m_ci = nullptr;
@@ -1157,6 +1173,19 @@ int lu_inverse_setup(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   cudaError_t e = L->inv_y.reserve(nn);
   if (e == cudaSuccess) e = L->inv_cp.reserve((size_t)std::max<int64_t>(L->s.cpool, 1) * n);
   if (e == cudaSuccess) e = L->iperm.upload(L->s.iperm);
+  if (e == cudaSuccess) e = L->pool32.reserve(L->s.pool);
+  {
+    const size_t smem = ((size_t)kLuSmallM * kLuSmallM +
+                         (size_t)kLuSmallM * (kInvCols + 1)) * sizeof(float);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_lu_inv_fwd,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_lu_inv_bwd,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream());
   if (e != cudaSuccess) {
     pg_lu_destroy(L);
@@ -1173,20 +1202,26 @@ int lu_inverse_run(pg_lu *L, const double *vals, float *out, cudaStream_t st) {
   LuArgs a = args_of(L);
   const int n = (int)s.n;
   const int tiles = (n + kInvCols - 1) / kInvCols;
+  k_lu_pool_f32<<<(int)((s.pool + 255) / 256), 256, 0, st>>>(s.pool, L->pool.p,
+                                                            L->pool32.p);
   for (int h = 0; h < s.n_heights; ++h) {
     const int nf = s.h_all_ptr[h + 1] - s.h_all_ptr[h];
-    k_lu_inv_fwd<<<dim3(nf, tiles), kInvCols * kInvRows, 0, st>>>(
-        L->h_all.p + s.h_all_ptr[h], a, n, L->inv_y.p, L->inv_cp.p);
+    const int mm = s.h_maxm[h];
+    const size_t smem = ((size_t)mm * mm + (size_t)mm * (kInvCols + 1)) * sizeof(float);
+    k_lu_inv_fwd<<<dim3(nf, tiles), kInvCols * kInvRows, smem, st>>>(
+        L->h_all.p + s.h_all_ptr[h], a, L->pool32.p, n, L->inv_y.p, L->inv_cp.p);
   }
   for (int h = s.n_heights - 1; h >= 0; --h) {
     const int nf = s.h_all_ptr[h + 1] - s.h_all_ptr[h];
-    k_lu_inv_bwd<<<dim3(nf, tiles), kInvCols * kInvRows, 0, st>>>(
-        L->h_all.p + s.h_all_ptr[h], a, n, L->inv_y.p);
+    const int mm = s.h_maxm[h];
+    const size_t smem = ((size_t)mm * mm + (size_t)mm * (kInvCols + 1)) * sizeof(float);
+    k_lu_inv_bwd<<<dim3(nf, tiles), kInvCols * kInvRows, smem, st>>>(
+        L->h_all.p + s.h_all_ptr[h], a, L->pool32.p, n, L->inv_y.p);
   }
   const int64_t nn = (int64_t)n * n;
   k_lu_inv_out<<<(int)((nn + 255) / 256), 256, 0, st>>>(n, L->iperm.p,
                                                          L->inv_y.p, out);
-  count_launches(2 * s.n_heights + 1);
+  count_launches(2 * s.n_heights + 2);
   PG_CUDA(cudaGetLastError());
   return PG_OK;
 }
