@@ -529,9 +529,10 @@ int pg_lu_get_x(const pg_lu *lu, double *x, int ptr_kind);
  * new -> old row), fronts[4 * n_fronts] = (first new index, fully summed
  * count k, order m, parent or -1) in elimination order, and fidx[] (each
  * front's index list: its k own rows, then its update rows ascending).
- * xy: optional point per row.  (Inspection; no reference counterpart.) */
+ * xy: optional point per row; leaf: largest vertex set that is not cut
+ * (0: the solver's default, 64).  (Inspection; no reference counterpart.) */
 int pg_lu_analyse_pattern(int64_t n, const int32_t *row_ptr,
-                          const int32_t *col_ind, const double *xy,
+                          const int32_t *col_ind, const double *xy, int leaf,
                           int64_t *sizes, int32_t *perm, int32_t *fronts,
                           int32_t *fidx);
 

@@ -150,7 +150,7 @@ PROTOTYPES = {
     "pg_lu_set_rhs": (_I, [_P, _P, _I]),
     "pg_lu_solve": (_I, [_P, ctypes.POINTER(LuStats)]),
     "pg_lu_get_x": (_I, [_P, _P, _I]),
-    "pg_lu_analyse_pattern": (_I, [_I64, _P, _P, _P, _P, _P, _P, _P]),
+    "pg_lu_analyse_pattern": (_I, [_I64, _P, _P, _P, _I, _P, _P, _P, _P]),
     "pg_kernel_launches": (ctypes.c_uint64, []),
 }
 
@@ -681,7 +681,7 @@ class SparseLU:
         return 0.0
 
 
-def lu_analyse_pattern(row_ptr, col_ind, xy=None):
+def lu_analyse_pattern(row_ptr, col_ind, xy=None, leaf=0):
     """The direct solver's nested-dissection ordering and fronts (host
     analysis only): (perm new->old, fronts [n_fronts, 4] = (s0, k, m,
     parent), list of index arrays per front, heights)."""
@@ -692,14 +692,15 @@ def lu_analyse_pattern(row_ptr, col_ind, xy=None):
     sizes = np.zeros(4, np.int64)
     _check(lib().pg_lu_analyse_pattern(n, _ptr(rp), _ptr(ci),
                                        None if xa is None else _ptr(xa),
-                                       _ptr(sizes), None, None, None))
+                                       int(leaf), _ptr(sizes), None, None,
+                                       None))
     perm = np.empty(n, np.int32)
     fr = np.empty((int(sizes[0]), 4), np.int32)
     fidx = np.empty(int(sizes[1]), np.int32)
     _check(lib().pg_lu_analyse_pattern(n, _ptr(rp), _ptr(ci),
                                        None if xa is None else _ptr(xa),
-                                       _ptr(sizes), _ptr(perm), _ptr(fr),
-                                       _ptr(fidx)))
+                                       int(leaf), _ptr(sizes), _ptr(perm),
+                                       _ptr(fr), _ptr(fidx)))
     lists, o = [], 0
     for s0, k, m, parent in fr:
         lists.append(fidx[o:o + m])

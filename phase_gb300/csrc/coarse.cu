@@ -27,6 +27,7 @@
 #include "dd.cuh"
 #include "kernels.cuh"
 #include "lu.h"
+#include "../../include/phase_gb300.h"
 
 namespace pg {
 namespace {
@@ -939,12 +940,37 @@ void launch_coarse_setup(const CoarseDev &c, const double *pvals,
 
 int launch_coarse_setup_lu(const CoarseDev &c, pg_lu *lu, double *cvals,
                            const double *pvals, const int32_t *prp,
-                           cudaStream_t st) {
-  const size_t smem = (size_t)kCoarseBlock * c.max_cnb * sizeof(double);
-  k_coarse_assemble_csr<<<c.K, kCoarseBlock, smem, st>>>(c.sub_ptr, prp, pvals,
-                                                         c.cptr, c.cslot, cvals);
-  count_launches(1);
-  return lu_inverse_run(lu, cvals, c.ac, st);
+                           cudaGraphExec_t *graph, cudaStream_t st) {
+  // about 30 short dependent launches: captured once into a graph (per
+  // inverse buffer), replayed; run directly when the capture fails
+  int rc = PG_OK;
+  auto run = [&]() {
+    const size_t smem = (size_t)kCoarseBlock * c.max_cnb * sizeof(double);
+    k_coarse_assemble_csr<<<c.K, kCoarseBlock, smem, st>>>(
+        c.sub_ptr, prp, pvals, c.cptr, c.cslot, cvals);
+    count_launches(1);
+    return lu_inverse_run(lu, cvals, c.ac, st);
+  };
+  if (graph && !*graph) {
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
+      rc = run();
+      if (cudaStreamEndCapture(st, &g) == cudaSuccess && g && rc == PG_OK &&
+          cudaGraphInstantiate(graph, g, 0) != cudaSuccess)
+        *graph = nullptr;
+      if (g) cudaGraphDestroy(g);
+    }
+    cudaGetLastError();  // a failed capture falls back to direct launches
+  }
+  if (graph && *graph) {
+    // the capture counted the kernels of one run: a replay counts them
+    // again only when it is not the capture's own first execution
+    if (cudaGraphLaunch(*graph, st) != cudaSuccess) return run();
+    if (lu_inverse_captured(lu)) count_launches(1 + lu_inverse_launches(lu));
+    lu_inverse_set_captured(lu);
+    return PG_OK;
+  }
+  return run();
 }
 
 void launch_coarse_apply(const CoarseDev &c, const double *in, double *z,

@@ -362,7 +362,8 @@ void launch_coarse_apply_b(const CoarseBatchDev &c, int K, const double *in,
 // cptr / cnb) and inverted through the sparse LU into c.ac (FP32, dense)
 int launch_coarse_setup_lu(const CoarseDev &c, pg_lu *lu,
                            double *cvals, const double *pvals,
-                           const int32_t *prp, cudaStream_t st);
+                           const int32_t *prp, cudaGraphExec_t *graph,
+                           cudaStream_t st);
 void launch_coarse_setup(const CoarseDev &c, const double *pvals,
                          const int32_t *prp, cudaGraphExec_t *gj_graph,
                          cudaStream_t st);

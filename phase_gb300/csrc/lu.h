@@ -105,4 +105,9 @@ int lu_inverse_setup(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
 // (indexed like col_ind); FP64 factorisation, FP32 multi-right-hand-side
 // triangular solves
 int lu_inverse_run(pg_lu *lu, const double *vals, float *out, cudaStream_t st);
+// kernels one lu_inverse_run launches; whether a captured graph of it has
+// run once (launch accounting of graph replays)
+int lu_inverse_launches(const pg_lu *lu);
+bool lu_inverse_captured(const pg_lu *lu);
+void lu_inverse_set_captured(pg_lu *lu);
 }  // namespace pg

@@ -1166,7 +1166,8 @@ int factor(pg_solver *s, cudaStream_t st) {
       PG_CUDA(cudaStreamWaitEvent(s->side2, s->ev_cvals, 0));
       if (s->c_lu) {
         int rc = launch_coarse_setup_lu(ct, s->c_lu, s->c_vals.p, s->pvals.p,
-                                        s->prp.p, s->side2);
+                                        s->prp.p, s->gj_graph_of(target),
+                                        s->side2);
         if (rc) return rc;
       } else {
         launch_coarse_setup(ct, s->pvals.p, s->prp.p, s->gj_graph_of(target),
@@ -1668,7 +1669,7 @@ extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
   auto coarse_setup = [&] {
     if (s->c_lu)
       launch_coarse_setup_lu(s->coarse(), s->c_lu, s->c_vals.p, s->pvals.p,
-                             s->prp.p, st);
+                             s->prp.p, s->gj_graph_of(s->ac_ready), st);
     else
       launch_coarse_setup(s->coarse(), s->pvals.p, s->prp.p,
                           s->gj_graph_of(s->ac_ready), st);
