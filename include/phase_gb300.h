@@ -338,8 +338,11 @@ typedef struct {
                          (fewer iterations) */
   int coarse_warm;    /* one-level iterations a solve runs while the coarse
                          inverse is built beside them, before it restarts
-                         with the two-level preconditioner: -1 = default (16
-                         with at least 1024 subdomains, else 0), 0 = wait
+                         with the two-level preconditioner: -1 = default (0
+                         when the coarse inverse is built through the
+                         sparse LU of the coarse matrix -- every front of
+                         its nested dissection small, the usual case -- else
+                         16 with at least 1024 subdomains), 0 = wait
                          for the inverse (when the caller already had work
                          to overlap it with after the hand-over), -2 = apply
                          the previous factorisation's inverse (same

@@ -81,15 +81,20 @@ __device__ __forceinline__ double entry_sum(const LuArgs &a, const double *vals,
   return v;
 }
 
-// pivot value with the vanishing-pivot replacement
-__device__ __forceinline__ double checked_pivot(const LuArgs &a, double p,
-                                                int col) {
-  const double cs = col_scale(a, col);
+// pivot value with the vanishing-pivot replacement (cs: the column's
+// largest magnitude in A)
+__device__ __forceinline__ double checked_pivot_scaled(const LuArgs &a,
+                                                       double p, double cs) {
   if (fabs(p) <= kPivotRel * cs || p == 0.) {
     atomicAdd(a.n_replaced, 1);
     return cs > 0. ? cs : 1.;
   }
   return p;
+}
+
+__device__ __forceinline__ double checked_pivot(const LuArgs &a, double p,
+                                                int col) {
+  return checked_pivot_scaled(a, p, col_scale(a, col));
 }
 
 // ---------------------------------------------------------- small fronts
@@ -99,10 +104,12 @@ k_lu_small(const int32_t *__restrict__ list, LuArgs a,
   extern __shared__ double F[];
   __shared__ int piv_row;
   __shared__ double piv_val;
+  __shared__ double cscale[kLuSmallM];
   const int tid = threadIdx.x;
   const LuFront f = a.fronts[list[blockIdx.x]];
   const int m = f.m, k = f.k;
   for (int e = tid; e < m * m; e += kSmallThreads) F[e] = 0.;
+  for (int c = tid; c < k; c += kSmallThreads) cscale[c] = col_scale(a, f.s0 + c);
   __syncthreads();
   for (int c = 0; c < f.n_child; ++c) {
     const LuFront ch = a.fronts[a.children[f.child_ptr + c]];
@@ -153,7 +160,7 @@ k_lu_small(const int32_t *__restrict__ list, LuArgs a,
       }
     __syncthreads();
     if (tid == 0) {
-      const double p = checked_pivot(a, F[c * m + c], f.s0 + c);
+      const double p = checked_pivot_scaled(a, F[c * m + c], cscale[c]);
       F[c * m + c] = p;
       piv_val = p;
     }
@@ -597,7 +604,7 @@ k_lu_residual(int n, const int32_t *__restrict__ rp, const int32_t *__restrict__
 // order, FP64 factors read and rounded to FP32), then back substituted
 // from the root down; a front's tile whose columns lie outside its subtree
 // is zero and is only written as zeros.  Small fronts only (m <= kLuSmallM).
-constexpr int kInvCols = 32, kInvRows = 8;
+constexpr int kInvCols = 128;  // right-hand-side columns per CTA
 
 // FP32 copy of the factor pool (read by the inverse's triangular solves)
 __global__ void k_lu_pool_f32(int64_t n, const double *__restrict__ src,
@@ -606,89 +613,84 @@ __global__ void k_lu_pool_f32(int64_t n, const double *__restrict__ src,
   if (i < n) dst[i] = (float)src[i];
 }
 
-// the front's m x m factor staged in shared memory (FP32), then W
-__device__ __forceinline__ void stage_front(const float *__restrict__ F32,
-                                            int m, float *Fs) {
-  for (int e = threadIdx.x; e < m * m; e += kInvCols * kInvRows) Fs[e] = F32[e];
-}
-
-__global__ void __launch_bounds__(kInvCols * kInvRows)
+// Each thread owns one column of the right-hand sides (W[i][thread], a
+// column per shared-memory bank) and runs the whole elimination of its
+// column; the front's factor is staged once in shared memory and only
+// broadcast-read, so no barrier is needed inside the loops.
+__global__ void __launch_bounds__(kInvCols)
 k_lu_inv_fwd(const int32_t *__restrict__ list, LuArgs a,
              const float *__restrict__ pool32, int n, float *__restrict__ Y,
              float *__restrict__ CP) {
   extern __shared__ float smf[];
-  const int cc = threadIdx.x & (kInvCols - 1), ty = threadIdx.x / kInvCols;
+  const int cc = threadIdx.x;
   const LuFront f = a.fronts[list[blockIdx.x]];
   const int m = f.m, k = f.k, j0 = blockIdx.y * kInvCols;
   const int j = j0 + cc;
-  float *Fs = smf, (*W)[kInvCols + 1] = (float(*)[kInvCols + 1])(smf + m * m);
+  float *Fs = smf, *W = smf + m * m;  // W[i * kInvCols + cc]
   const bool live = j0 + kInvCols > f.first && j0 < f.s0 + k;
-  if (live) stage_front(pool32 + f.off, m, Fs);
-  for (int i = ty; i < m; i += kInvRows)
-    W[i][cc] = live && i < k && f.s0 + i == j ? 1.f : 0.f;
-  __syncthreads();
   if (live) {
+    const float *F32 = pool32 + f.off;
+    for (int e = cc; e < m * m; e += kInvCols) Fs[e] = F32[e];
+  }
+  for (int i = 0; i < m; ++i)
+    W[i * kInvCols + cc] = live && i < k && f.s0 + i == j ? 1.f : 0.f;
+  __syncthreads();
+  if (live && j < n) {
     for (int c = 0; c < f.n_child; ++c) {
       const LuFront ch = a.fronts[a.children[f.child_ptr + c]];
       const int u = ch.m - ch.k;
       const int32_t *rel = a.rel + ch.rel_off;
-      for (int e = ty; e < u; e += kInvRows)
-        if (j < n) W[rel[e]][cc] += CP[(size_t)(ch.coff + e) * n + j];
-      __syncthreads();
+      for (int e = 0; e < u; ++e)
+        W[rel[e] * kInvCols + cc] += CP[(size_t)(ch.coff + e) * n + j];
     }
     for (int c = 0; c < k; ++c) {
-      if (ty == 0) {
-        const int r = a.ipiv[f.s0 + c];
-        if (r != c) {
-          const float x = W[c][cc];
-          W[c][cc] = W[r][cc];
-          W[r][cc] = x;
-        }
+      const int r = a.ipiv[f.s0 + c];
+      float wc = W[c * kInvCols + cc];
+      if (r != c) {
+        const float x = W[r * kInvCols + cc];
+        W[r * kInvCols + cc] = wc;
+        W[c * kInvCols + cc] = x;
+        wc = x;
       }
-      __syncthreads();
-      const float wc = W[c][cc];
-      for (int i = c + 1 + ty; i < m; i += kInvRows) W[i][cc] -= Fs[i * m + c] * wc;
-      __syncthreads();
+      for (int i = c + 1; i < m; ++i) W[i * kInvCols + cc] -= Fs[i * m + c] * wc;
     }
   }
   if (j >= n) return;
-  for (int i = ty; i < m; i += kInvRows) {
-    if (i < k) Y[(size_t)(f.s0 + i) * n + j] = W[i][cc];
-    else CP[(size_t)(f.coff + i - k) * n + j] = W[i][cc];
+  for (int i = 0; i < m; ++i) {
+    if (i < k) Y[(size_t)(f.s0 + i) * n + j] = W[i * kInvCols + cc];
+    else CP[(size_t)(f.coff + i - k) * n + j] = W[i * kInvCols + cc];
   }
 }
 
-__global__ void __launch_bounds__(kInvCols * kInvRows)
+__global__ void __launch_bounds__(kInvCols)
 k_lu_inv_bwd(const int32_t *__restrict__ list, LuArgs a,
              const float *__restrict__ pool32, int n, float *__restrict__ Y) {
   extern __shared__ float smf[];
-  const int cc = threadIdx.x & (kInvCols - 1), ty = threadIdx.x / kInvCols;
+  const int cc = threadIdx.x;
   const LuFront f = a.fronts[list[blockIdx.x]];
   const int m = f.m, k = f.k, j = blockIdx.y * kInvCols + cc;
-  const bool ok = j < n;
-  float *Fs = smf, (*W)[kInvCols + 1] = (float(*)[kInvCols + 1])(smf + m * m);
-  stage_front(pool32 + f.off, m, Fs);
-  for (int i = ty; i < m; i += kInvRows)
-    W[i][cc] = !ok ? 0.f
-               : i < k ? Y[(size_t)(f.s0 + i) * n + j]
-                       : Y[(size_t)a.fidx[f.idx + i] * n + j];
+  float *Fs = smf, *W = smf + m * m;
+  {
+    const float *F32 = pool32 + f.off;
+    for (int e = cc; e < m * m; e += kInvCols) Fs[e] = F32[e];
+  }
   __syncthreads();
-  // r = y_S - U12 x_U
-  for (int i = ty; i < k; i += kInvRows) {
+  if (j >= n) return;
+  for (int i = 0; i < m; ++i)
+    W[i * kInvCols + cc] = i < k ? Y[(size_t)(f.s0 + i) * n + j]
+                                 : Y[(size_t)a.fidx[f.idx + i] * n + j];
+  // r = y_S - U12 x_U, then U11 back substitution
+  for (int i = 0; i < k; ++i) {
     float acc = 0.f;
-    for (int u = k; u < m; ++u) acc += Fs[i * m + u] * W[u][cc];
-    W[i][cc] -= acc;
+    for (int u = k; u < m; ++u) acc += Fs[i * m + u] * W[u * kInvCols + cc];
+    W[i * kInvCols + cc] -= acc;
   }
-  __syncthreads();
   for (int c = k - 1; c >= 0; --c) {
-    if (ty == 0) W[c][cc] /= Fs[c * m + c];
-    __syncthreads();
-    const float xc = W[c][cc];
-    for (int i = ty; i < c; i += kInvRows) W[i][cc] -= Fs[i * m + c] * xc;
-    __syncthreads();
+    const float xc = W[c * kInvCols + cc] / Fs[c * m + c];
+    W[c * kInvCols + cc] = xc;
+    for (int i = 0; i < c; ++i) W[i * kInvCols + cc] -= Fs[i * m + c] * xc;
   }
-  if (!ok) return;
-  for (int i = ty; i < k; i += kInvRows) Y[(size_t)(f.s0 + i) * n + j] = W[i][cc];
+  for (int i = 0; i < k; ++i) Y[(size_t)(f.s0 + i) * n + j] = W[i * kInvCols + cc];
 }
 
 // out[I][J] = X[iperm[I]][iperm[J]] (caller's numbering)
@@ -1182,7 +1184,7 @@ int lu_inverse_setup(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   if (e == cudaSuccess) e = L->pool32.reserve(L->s.pool);
   {
     const size_t smem = ((size_t)kLuSmallM * kLuSmallM +
-                         (size_t)kLuSmallM * (kInvCols + 1)) * sizeof(float);
+                         (size_t)kLuSmallM * kInvCols) * sizeof(float);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(k_lu_inv_fwd,
                                cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1218,15 +1220,15 @@ int lu_inverse_run(pg_lu *L, const double *vals, float *out, cudaStream_t st) {
   for (int h = 0; h < s.n_heights; ++h) {
     const int nf = s.h_all_ptr[h + 1] - s.h_all_ptr[h];
     const int mm = s.h_maxm[h];
-    const size_t smem = ((size_t)mm * mm + (size_t)mm * (kInvCols + 1)) * sizeof(float);
-    k_lu_inv_fwd<<<dim3(nf, tiles), kInvCols * kInvRows, smem, st>>>(
+    const size_t smem = ((size_t)mm * mm + (size_t)mm * kInvCols) * sizeof(float);
+    k_lu_inv_fwd<<<dim3(nf, tiles), kInvCols, smem, st>>>(
         L->h_all.p + s.h_all_ptr[h], a, L->pool32.p, n, L->inv_y.p, L->inv_cp.p);
   }
   for (int h = s.n_heights - 1; h >= 0; --h) {
     const int nf = s.h_all_ptr[h + 1] - s.h_all_ptr[h];
     const int mm = s.h_maxm[h];
-    const size_t smem = ((size_t)mm * mm + (size_t)mm * (kInvCols + 1)) * sizeof(float);
-    k_lu_inv_bwd<<<dim3(nf, tiles), kInvCols * kInvRows, smem, st>>>(
+    const size_t smem = ((size_t)mm * mm + (size_t)mm * kInvCols) * sizeof(float);
+    k_lu_inv_bwd<<<dim3(nf, tiles), kInvCols, smem, st>>>(
         L->h_all.p + s.h_all_ptr[h], a, L->pool32.p, n, L->inv_y.p);
   }
   const int64_t nn = (int64_t)n * n;

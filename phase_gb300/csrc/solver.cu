@@ -294,9 +294,11 @@ int red_grid_cap() {
 }
 
 constexpr int kMaxCoarseK = 2048;  // the coarse matrix is K x K, dense
-// by default, coarse spaces of at least kCoarseStagedK subdomains are
-// inverted beside kCoarseWarmIters one-level iterations (the inversion
-// takes ~2 ms at 2048; cfg.coarse_warm overrides)
+// by default, coarse spaces of at least kCoarseStagedK subdomains that are
+// inverted by Gauss-Jordan elimination (~1.5 ms at 2048) are inverted
+// beside kCoarseWarmIters one-level iterations; an inverse built through
+// the sparse LU (well under a millisecond) is waited for (cfg.coarse_warm
+// overrides both)
 constexpr int kCoarseStagedK = 1024;
 constexpr int kCoarseWarmIters = 16;
 
@@ -1526,8 +1528,8 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
   };
   int status;
   const int warm = s->cfg.coarse_warm >= 0 ? s->cfg.coarse_warm
-                   : s->a.n_sub >= kCoarseStagedK ? kCoarseWarmIters
-                                                  : 0;
+                   : s->a.n_sub >= kCoarseStagedK && !s->c_lu ? kCoarseWarmIters
+                                                              : 0;
   if (s->coarse_pending && s->cfg.coarse_warm == -2 && s->ac_valid) {
     // the previous factorisation's coarse inverse preconditions the whole
     // solve (a fixed operator) while the new one is built on side2
