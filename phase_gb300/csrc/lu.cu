@@ -98,39 +98,46 @@ __device__ __forceinline__ double checked_pivot(const LuArgs &a, double p,
 }
 
 // ---------------------------------------------------------- small fronts
+// T = double for the direct solver; T = float for the dense inverse built
+// from it (the two-level preconditioner's coarse matrix, whose inverse is
+// applied in FP32), where fpool is the FP32 factor pool.
+template <class T>
 __global__ void __launch_bounds__(kSmallThreads)
 k_lu_small(const int32_t *__restrict__ list, LuArgs a,
-           const double *__restrict__ vals) {
-  extern __shared__ double F[];
+           const double *__restrict__ vals, T *__restrict__ fpool) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T *F = reinterpret_cast<T *>(sm_raw);
   __shared__ int piv_row;
-  __shared__ double piv_val;
+  __shared__ T piv_val;
   __shared__ double cscale[kLuSmallM];
   const int tid = threadIdx.x;
   const LuFront f = a.fronts[list[blockIdx.x]];
   const int m = f.m, k = f.k;
-  for (int e = tid; e < m * m; e += kSmallThreads) F[e] = 0.;
+  for (int e = tid; e < m * m; e += kSmallThreads) F[e] = T(0);
   for (int c = tid; c < k; c += kSmallThreads) cscale[c] = col_scale(a, f.s0 + c);
   __syncthreads();
   for (int c = 0; c < f.n_child; ++c) {
     const LuFront ch = a.fronts[a.children[f.child_ptr + c]];
     const int u = ch.m - ch.k;
-    const double *cb = a.pool + ch.off;
+    const T *cb = fpool + ch.off;
     const int32_t *rel = a.rel + ch.rel_off;
-    for (int e = tid; e < u * u; e += kSmallThreads) {
-      const int ra = e / u, rb = e - ra * u;
-      F[rel[ra] * m + rel[rb]] += cb[(size_t)(ch.k + ra) * ch.m + ch.k + rb];
+    // a warp per contribution row, lanes along it
+    for (int ra = tid >> 5; ra < u; ra += kSmallThreads / 32) {
+      const int pr = rel[ra] * m;
+      const T *src = cb + (size_t)(ch.k + ra) * ch.m + ch.k;
+      for (int rb = tid & 31; rb < u; rb += 32) F[pr + rel[rb]] += src[rb];
     }
     __syncthreads();
   }
   for (int e = f.ent_ptr + tid; e < f.ent_end; e += kSmallThreads)
-    F[a.e_pos[e]] += entry_sum(a, vals, e);
+    F[a.e_pos[e]] += (T)entry_sum(a, vals, e);
   __syncthreads();
   for (int c = 0; c < k; ++c) {
     if (tid < 32) {
       double best = -1.;
       int br = c;
       for (int r = c + tid; r < k; r += 32) {
-        const double v = fabs(F[r * m + c]);
+        const double v = fabs((double)F[r * m + c]);
         if (v > best) {
           best = v;
           br = r;
@@ -148,34 +155,33 @@ k_lu_small(const int32_t *__restrict__ list, LuArgs a,
       if (tid == 0) {
         piv_row = br;
         a.ipiv[f.s0 + c] = br;
+        // the exchange of rows c and br (columns c ..) and the pivot
+        T p = F[br * m + c];
+        if (br != c) {
+          for (int j = c; j < m; ++j) {
+            const T t = F[c * m + j];
+            F[c * m + j] = F[br * m + j];
+            F[br * m + j] = t;
+          }
+        }
+        p = (T)checked_pivot_scaled(a, (double)p, cscale[c]);
+        F[c * m + c] = p;
+        piv_val = p;
       }
     }
     __syncthreads();
-    const int r = piv_row;
-    if (r != c)
-      for (int j = c + tid; j < m; j += kSmallThreads) {
-        const double t = F[c * m + j];
-        F[c * m + j] = F[r * m + j];
-        F[r * m + j] = t;
-      }
-    __syncthreads();
-    if (tid == 0) {
-      const double p = checked_pivot_scaled(a, F[c * m + c], cscale[c]);
-      F[c * m + c] = p;
-      piv_val = p;
-    }
-    __syncthreads();
-    const double p = piv_val;
-    for (int i = c + 1 + tid; i < m; i += kSmallThreads) F[i * m + c] /= p;
-    __syncthreads();
-    const int w = m - c - 1;
-    for (int e = tid; e < w * w; e += kSmallThreads) {
-      const int i = c + 1 + e / w, j = c + 1 + e % w;
-      F[i * m + j] -= F[i * m + c] * F[c * m + j];
+    const T p = piv_val;
+    // multipliers and the rank-1 update: a warp per row, lanes along it
+    for (int i = c + 1 + (tid >> 5); i < m; i += kSmallThreads / 32) {
+      const T l = F[i * m + c] / p;
+      for (int j = c + 1 + (tid & 31); j < m; j += 32)
+        F[i * m + j] -= l * F[c * m + j];
+      __syncwarp();
+      if ((tid & 31) == 0) F[i * m + c] = l;
     }
     __syncthreads();
   }
-  double *out = a.pool + f.off;
+  T *out = fpool + f.off;
   for (int e = tid; e < m * m; e += kSmallThreads) out[e] = F[e];
 }
 
@@ -606,13 +612,6 @@ k_lu_residual(int n, const int32_t *__restrict__ rp, const int32_t *__restrict__
 // is zero and is only written as zeros.  Small fronts only (m <= kLuSmallM).
 constexpr int kInvCols = 128;  // right-hand-side columns per CTA
 
-// FP32 copy of the factor pool (read by the inverse's triangular solves)
-__global__ void k_lu_pool_f32(int64_t n, const double *__restrict__ src,
-                              float *__restrict__ dst) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) dst[i] = (float)src[i];
-}
-
 // Each thread owns one column of the right-hand sides (W[i][thread], a
 // column per shared-memory bank) and runs the whole elimination of its
 // column; the front's factor is staged once in shared memory and only
@@ -640,8 +639,16 @@ k_lu_inv_fwd(const int32_t *__restrict__ list, LuArgs a,
       const LuFront ch = a.fronts[a.children[f.child_ptr + c]];
       const int u = ch.m - ch.k;
       const int32_t *rel = a.rel + ch.rel_off;
-      for (int e = 0; e < u; ++e)
-        W[rel[e] * kInvCols + cc] += CP[(size_t)(ch.coff + e) * n + j];
+      // eight independent loads in flight per batch
+      for (int e0 = 0; e0 < u; e0 += 8) {
+        float v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          v[q] = e0 + q < u ? CP[(size_t)(ch.coff + e0 + q) * n + j] : 0.f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (e0 + q < u) W[rel[e0 + q] * kInvCols + cc] += v[q];
+      }
     }
     for (int c = 0; c < k; ++c) {
       const int r = a.ipiv[f.s0 + c];
@@ -676,9 +683,19 @@ k_lu_inv_bwd(const int32_t *__restrict__ list, LuArgs a,
   }
   __syncthreads();
   if (j >= n) return;
-  for (int i = 0; i < m; ++i)
-    W[i * kInvCols + cc] = i < k ? Y[(size_t)(f.s0 + i) * n + j]
-                                 : Y[(size_t)a.fidx[f.idx + i] * n + j];
+  for (int i0 = 0; i0 < m; i0 += 8) {  // eight loads in flight per batch
+    float v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int i = i0 + q;
+      v[q] = i >= m ? 0.f
+             : i < k ? Y[(size_t)(f.s0 + i) * n + j]
+                     : Y[(size_t)a.fidx[f.idx + i] * n + j];
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (i0 + q < m) W[(i0 + q) * kInvCols + cc] = v[q];
+  }
   // r = y_S - U12 x_U, then U11 back substitution
   for (int i = 0; i < k; ++i) {
     float acc = 0.f;
@@ -710,8 +727,11 @@ int lu_smem_setup() {
   static cudaError_t err = cudaSuccess;
   std::call_once(once, [] {
     const int big = 200 * 1024;
-    err = cudaFuncSetAttribute(k_lu_small,
+    err = cudaFuncSetAttribute(k_lu_small<double>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    if (err == cudaSuccess)
+      err = cudaFuncSetAttribute(k_lu_small<float>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     if (err == cudaSuccess)
       err = cudaFuncSetAttribute(k_lu_fwd,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, big);
@@ -822,8 +842,9 @@ int analyse_and_upload(pg_lu *L, const int32_t *rp, const int32_t *ci,
   return PG_OK;
 }
 
-// the numeric factorisation of the values vals (caller's index space)
-int factor(pg_lu *L, const double *vals, cudaStream_t st) {
+// the numeric factorisation of the values vals (caller's index space);
+// f32: small fronts only, in FP32 into pool32 (the dense-inverse path)
+int factor(pg_lu *L, const double *vals, cudaStream_t st, bool f32 = false) {
   const LuSymbolic &s = L->s;
   LuArgs a = args_of(L);
   PG_CUDA(cudaEventRecord(L->ev[0], st));
@@ -840,9 +861,14 @@ int factor(pg_lu *L, const double *vals, cudaStream_t st) {
       int mm = 0;
       for (int i = s.h_small_ptr[h]; i < s.h_small_ptr[h + 1]; ++i)
         mm = std::max(mm, s.fronts[s.h_small[i]].m);
-      const size_t smem = (size_t)mm * mm * sizeof(double);
-      k_lu_small<<<ns, kSmallThreads, smem, st>>>(L->h_small.p + s.h_small_ptr[h],
-                                                  a, vals);
+      if (f32)
+        k_lu_small<float><<<ns, kSmallThreads, (size_t)mm * mm * sizeof(float),
+                            st>>>(L->h_small.p + s.h_small_ptr[h], a, vals,
+                                  L->pool32.p);
+      else
+        k_lu_small<double><<<ns, kSmallThreads, (size_t)mm * mm * sizeof(double),
+                             st>>>(L->h_small.p + s.h_small_ptr[h], a, vals,
+                                   L->pool.p);
       count_launches(1);
     }
     const int nl = s.h_large_ptr[h + 1] - s.h_large_ptr[h];
@@ -1210,13 +1236,11 @@ void lu_inverse_set_captured(pg_lu *L) { L->inv_captured = true; }
 int lu_inverse_run(pg_lu *L, const double *vals, float *out, cudaStream_t st) {
   const LuSymbolic &s = L->s;
   const uint64_t before = launch_count();
-  int rc = factor(L, vals, st);
+  int rc = factor(L, vals, st, true);
   if (rc) return rc;
   LuArgs a = args_of(L);
   const int n = (int)s.n;
   const int tiles = (n + kInvCols - 1) / kInvCols;
-  k_lu_pool_f32<<<(int)((s.pool + 255) / 256), 256, 0, st>>>(s.pool, L->pool.p,
-                                                            L->pool32.p);
   for (int h = 0; h < s.n_heights; ++h) {
     const int nf = s.h_all_ptr[h + 1] - s.h_all_ptr[h];
     const int mm = s.h_maxm[h];
@@ -1234,7 +1258,7 @@ int lu_inverse_run(pg_lu *L, const double *vals, float *out, cudaStream_t st) {
   const int64_t nn = (int64_t)n * n;
   k_lu_inv_out<<<(int)((nn + 255) / 256), 256, 0, st>>>(n, L->iperm.p,
                                                          L->inv_y.p, out);
-  count_launches(2 * s.n_heights + 2);
+  count_launches(2 * s.n_heights + 1);
   L->inv_launches = (int)(launch_count() - before);
   PG_CUDA(cudaGetLastError());
   return PG_OK;
