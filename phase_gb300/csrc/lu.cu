@@ -224,39 +224,42 @@ k_lu_scatter(const int32_t *__restrict__ list, LuArgs a,
 // c0 .. m-1, columns c0 .. c0+b-1) is factorised with partial pivoting over
 // the fully summed rows c .. k-1 of each column c; an interchange swaps the
 // whole panel rows (LAPACK's convention inside a panel), which the TRSM
-// kernel then applies to the columns right of the panel.  Warps own rows,
-// lanes the panel's columns.
+// kernel then applies to the columns right of it.  Warps own rows, lanes
+// the panel's columns; a warp keeps kPanelBatch rows' loads in flight, and
+// the candidates for the next column's pivot are ranked as the rows are
+// updated, so each step reads the panel once.
 constexpr int kPanelThreads = 1024;
+constexpr int kPanelBatch = 4;
+
+__device__ __forceinline__ void better(double &best, int &br, double v, int r) {
+  if (v > best || (v == best && r < br)) {
+    best = v;
+    br = r;
+  }
+}
+
 __global__ void __launch_bounds__(kPanelThreads)
 k_lu_panel(const int32_t *__restrict__ list, int q, LuArgs a) {
-  __shared__ double wbest[kPanelThreads / 32];
-  __shared__ int wrow[kPanelThreads / 32];
-  __shared__ int piv_row;
+  constexpr int NW = kPanelThreads / 32;
+  __shared__ double wbest[NW];
+  __shared__ int wrow[NW];
   __shared__ double piv_val;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const LuFront f = a.fronts[list[blockIdx.x]];
   const int m = f.m, k = f.k, c0 = q * kLuPanel, b = min(kLuPanel, k - c0);
   double *F = a.pool + f.off;
+  // candidates for the first column: a thread per row
+  double best = -1.;
+  int br = c0;
+  for (int r = c0 + tid; r < k; r += kPanelThreads)
+    better(best, br, fabs(F[(size_t)r * m + c0]), r);
   for (int s = 0; s < b; ++s) {
     const int c = c0 + s;
-    // pivot search: thread per row, then warps, then the block
-    double best = -1.;
-    int br = c;
-    for (int r = c + tid; r < k; r += kPanelThreads) {
-      const double v = fabs(F[(size_t)r * m + c]);
-      if (v > best) {
-        best = v;
-        br = r;
-      }
-    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const double ob = __shfl_down_sync(0xffffffffu, best, o);
       const int orr = __shfl_down_sync(0xffffffffu, br, o);
-      if (ob > best || (ob == best && orr < br)) {
-        best = ob;
-        br = orr;
-      }
+      better(best, br, ob, orr);
     }
     if (lane == 0) {
       wbest[warp] = best;
@@ -270,10 +273,7 @@ k_lu_panel(const int32_t *__restrict__ list, int q, LuArgs a) {
       for (int o = 16; o > 0; o >>= 1) {
         const double ob = __shfl_down_sync(0xffffffffu, best, o);
         const int orr = __shfl_down_sync(0xffffffffu, br, o);
-        if (ob > best || (ob == best && orr < br)) {
-          best = ob;
-          br = orr;
-        }
+        better(best, br, ob, orr);
       }
       const int r = __shfl_sync(0xffffffffu, br, 0);
       if (r != c && lane < b) {
@@ -286,24 +286,38 @@ k_lu_panel(const int32_t *__restrict__ list, int q, LuArgs a) {
         a.ipiv[f.s0 + c] = r;
         const double p = checked_pivot(a, F[(size_t)c * m + c], f.s0 + c);
         F[(size_t)c * m + c] = p;
-        piv_row = r;
         piv_val = p;
       }
     }
     __syncthreads();
     const double p = piv_val;
     const double prow = lane < b ? F[(size_t)c * m + c0 + lane] : 0.;
-    for (int i = c + 1 + warp; i < m; i += kPanelThreads / 32) {
-      double *row = F + (size_t)i * m + c0;
-      double v = lane < b ? row[lane] : 0.;
-      const double l = __shfl_sync(0xffffffffu, v, s) / p;
-      if (lane == s) v = l;
-      else if (lane > s) v -= l * prow;
-      if (lane >= s && lane < b) row[lane] = v;
+    best = -1.;
+    br = c + 1;
+    for (int i0 = c + 1 + warp; i0 < m; i0 += NW * kPanelBatch) {
+      double v[kPanelBatch];
+#pragma unroll
+      for (int u = 0; u < kPanelBatch; ++u) {
+        const int i = i0 + u * NW;
+        v[u] = i < m && lane < b ? F[(size_t)i * m + c0 + lane] : 0.;
+      }
+#pragma unroll
+      for (int u = 0; u < kPanelBatch; ++u) {
+        const int i = i0 + u * NW;
+        const double l = __shfl_sync(0xffffffffu, v[u], s) / p;
+        if (lane == s) v[u] = l;
+        else if (lane > s) v[u] -= l * prow;
+        if (i < m && lane >= s && lane < b) F[(size_t)i * m + c0 + lane] = v[u];
+        // the next column's candidate of this row (fully summed rows only;
+        // the condition is the same for the whole warp)
+        if (s + 1 < b && i < k) {
+          const double nv = fabs(__shfl_sync(0xffffffffu, v[u], s + 1));
+          better(best, br, nv, i);
+        }
+      }
     }
     __syncthreads();
   }
-  (void)piv_row;
 }
 
 // U12 tiles of panel q: the panel's interchanges replayed on the columns
@@ -403,6 +417,29 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// out[i] -= F[i][c0 .. c0+b) . vec for the rows i = first, first + 16, ...
+// below last: a warp per row (lanes along the block, lane l holding vec's
+// entry l), four rows' loads in flight
+__device__ __forceinline__ void gemv_rows(const double *F, int m, int c0, int b,
+                                          int lane, double vl, int first,
+                                          int last, double *out) {
+  constexpr int NW = kSolveThreads / 32, R = 4;
+  for (int i0 = first; i0 < last; i0 += NW * R) {
+    double part[R];
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const int i = i0 + u * NW;
+      part[u] = i < last && lane < b ? F[(size_t)i * m + c0 + lane] * vl : 0.;
+    }
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const double sum = warp_sum(part[u]);
+      const int i = i0 + u * NW;
+      if (lane == 0 && i < last) out[i] -= sum;
+    }
+  }
+}
+
 // forward elimination of one height: b (new numbering) -> y for the fully
 // summed rows, contribution vectors for the update rows
 __global__ void __launch_bounds__(kSolveThreads)
@@ -470,12 +507,7 @@ k_lu_fwd(const int32_t *__restrict__ list, LuArgs a,
       }
       __syncthreads();
       const double wl = lane < b ? w[c0 + lane] : 0.;
-      for (int i = c0 + b + warp; i < m; i += kSolveThreads / 32) {
-        const double part =
-            lane < b ? F[(size_t)i * m + c0 + lane] * wl : 0.;
-        const double sum = warp_sum(part);
-        if (lane == 0) w[i] -= sum;
-      }
+      gemv_rows(F, m, c0, b, lane, wl, c0 + b + warp, m, w);
       __syncthreads();
     }
   }
@@ -538,11 +570,7 @@ k_lu_bwd(const int32_t *__restrict__ list, LuArgs a,
       }
       __syncthreads();
       const double xl = lane < b ? r[c0 + lane] : 0.;
-      for (int i = warp; i < c0; i += kSolveThreads / 32) {
-        const double part = lane < b ? F[(size_t)i * m + c0 + lane] * xl : 0.;
-        const double sum = warp_sum(part);
-        if (lane == 0) r[i] -= sum;
-      }
+      gemv_rows(F, m, c0, b, lane, xl, warp, c0, r);
       __syncthreads();
     }
   }
