@@ -108,7 +108,7 @@ k_lu_small(const int32_t *__restrict__ list, LuArgs a,
   extern __shared__ __align__(16) unsigned char sm_raw[];
   T *F = reinterpret_cast<T *>(sm_raw);
   __shared__ int piv_row;
-  __shared__ T piv_val;
+  __shared__ T piv_inv;
   __shared__ double cscale[kLuSmallM];
   const int tid = threadIdx.x;
   const LuFront f = a.fronts[list[blockIdx.x]];
@@ -166,14 +166,14 @@ k_lu_small(const int32_t *__restrict__ list, LuArgs a,
         }
         p = (T)checked_pivot_scaled(a, (double)p, cscale[c]);
         F[c * m + c] = p;
-        piv_val = p;
+        piv_inv = T(1) / p;  // one division per pivot
       }
     }
     __syncthreads();
-    const T p = piv_val;
+    const T rp = piv_inv;
     // multipliers and the rank-1 update: a warp per row, lanes along it
     for (int i = c + 1 + (tid >> 5); i < m; i += kSmallThreads / 32) {
-      const T l = F[i * m + c] / p;
+      const T l = F[i * m + c] * rp;
       for (int j = c + 1 + (tid & 31); j < m; j += 32)
         F[i * m + j] -= l * F[c * m + j];
       __syncwarp();
@@ -243,7 +243,7 @@ k_lu_panel(const int32_t *__restrict__ list, int q, LuArgs a) {
   constexpr int NW = kPanelThreads / 32;
   __shared__ double wbest[NW];
   __shared__ int wrow[NW];
-  __shared__ double piv_val;
+  __shared__ double piv_inv;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const LuFront f = a.fronts[list[blockIdx.x]];
   const int m = f.m, k = f.k, c0 = q * kLuPanel, b = min(kLuPanel, k - c0);
@@ -286,11 +286,11 @@ k_lu_panel(const int32_t *__restrict__ list, int q, LuArgs a) {
         a.ipiv[f.s0 + c] = r;
         const double p = checked_pivot(a, F[(size_t)c * m + c], f.s0 + c);
         F[(size_t)c * m + c] = p;
-        piv_val = p;
+        piv_inv = 1. / p;  // one division per pivot
       }
     }
     __syncthreads();
-    const double p = piv_val;
+    const double rp = piv_inv;
     const double prow = lane < b ? F[(size_t)c * m + c0 + lane] : 0.;
     best = -1.;
     br = c + 1;
@@ -304,7 +304,7 @@ k_lu_panel(const int32_t *__restrict__ list, int q, LuArgs a) {
 #pragma unroll
       for (int u = 0; u < kPanelBatch; ++u) {
         const int i = i0 + u * NW;
-        const double l = __shfl_sync(0xffffffffu, v[u], s) / p;
+        const double l = __shfl_sync(0xffffffffu, v[u], s) * rp;
         if (lane == s) v[u] = l;
         else if (lane > s) v[u] -= l * prow;
         if (i < m && lane >= s && lane < b) F[(size_t)i * m + c0 + lane] = v[u];
