@@ -237,3 +237,72 @@ def rect_face_bcs(tree: Node, fld: str, patch_of_face):
         bc_type[sel] = t
         bc_value[sel] = float(v) if v else 0.0
     return bc_type, bc_value
+
+
+# -------------------------------------------------------------- backend
+_DIRECT = ("eigen", "eigen3", "amesos", "amesos2")
+_ITERATIVE = ("belos", "gb300")
+
+
+def backend(tree: Node, equation: str = "pEqn") -> str:
+    """Which library backend ``LinearAlgebra.<equation>.lib`` selects, read
+    as FiniteVolumeEquation::configureSparseSolver does (lower-cased, no
+    default; FiniteVolumeEquation.tpp:48-62) and mapped onto this library
+    as SparseMatrixSolverFactory::create maps the names
+    (SparseMatrixSolverFactory.cpp:26-40): "direct" for eigen / eigen3
+    (SparseLU) and amesos / amesos2 (a direct Trilinos solver) -- the
+    pg_lu backend --, "iterative" for belos and gb300 -- pg_solver.  muelu
+    (algebraic multigrid) is not built and raises ValueError, as an unknown
+    name raises in the factory."""
+    sec = tree.child("LinearAlgebra")
+    sec = sec.child(equation) if sec is not None else None
+    if sec is None or sec.get("lib") is None:
+        raise KeyError(f"LinearAlgebra.{equation}.lib not in the case")
+    lib = sec.get("lib").strip().lower()
+    if lib in _DIRECT:
+        return "direct"
+    if lib in _ITERATIVE:
+        return "iterative"
+    if lib == "muelu":
+        raise ValueError("lib muelu (algebraic multigrid) is not built")
+    raise ValueError(f'bad solver type "{lib}"')
+
+
+# ----------------------------------------------------------------- grid
+def _point(text: str):
+    v = text.strip().strip("()").split(",")
+    return float(v[0]), float(v[1])
+
+
+def grid(tree: Node, case_root: str):
+    """The grid of a case whose ``Grid.type`` is cgns
+    (CgnsUnstructuredGrid(Input), CgnsUnstructuredGrid.cpp:7-11:
+    ``Grid.filename`` relative to the directory the case runs in, optional
+    ``Grid.origin``), read by phase_gb300.cgns.read_mesh."""
+    from . import cgns
+    import os
+    sec = tree.child("Grid")
+    if sec is None:
+        raise KeyError("Grid not in the case")
+    kind = (sec.get("type") or "").strip().lower()
+    if kind != "cgns":
+        raise ValueError(f"grid type {kind!r}: only cgns files are read here "
+                         "(meshes.rectilinear builds rectilinear grids)")
+    origin = _point(sec.get("origin", "(0,0)"))
+    return cgns.read_mesh(os.path.join(case_root, sec.get("filename")),
+                          origin=origin)
+
+
+def face_bcs(tree: Node, fld: str, patch_of_face, names):
+    """Per-face (bc_type, bc_value) arrays of a scalar field for patches
+    ``names`` (patch_of_face: index into names, -1 interior: type 1, 0)."""
+    import numpy as np
+    bcs = boundary_conditions(tree, fld, names)
+    bc_type = np.ones(np.shape(patch_of_face), np.int32)
+    bc_value = np.zeros(np.shape(patch_of_face))
+    for pid, name in enumerate(names):
+        t, v = bcs[name]
+        sel = np.asarray(patch_of_face) == pid
+        bc_type[sel] = t
+        bc_value[sel] = float(v) if v else 0.0
+    return bc_type, bc_value

@@ -169,3 +169,20 @@ def test_triples_round_trip(tmp_path, oracle):
     assert len(list(r)) == 2
     with pytest.raises(ValueError):
         triples.TripleWriter(str(tmp_path / "e"), rp, np.where(ci == 0, -1, ci))
+
+
+def test_backend_of_the_lib_key():
+    """LinearAlgebra.<eqn>.lib selects the backend as Phase's factory
+    names them (SparseMatrixSolverFactory.cpp:26-40)."""
+    def case(lib):
+        return caseinfo.parse_info(
+            "LinearAlgebra\n{\n  pEqn\n  {\n    lib %s\n  }\n}\n" % lib)
+    assert caseinfo.backend(case("eigen")) == "direct"
+    assert caseinfo.backend(case("Eigen3")) == "direct"
+    assert caseinfo.backend(case("amesos2")) == "direct"
+    assert caseinfo.backend(case("belos")) == "iterative"
+    assert caseinfo.backend(case("gb300")) == "iterative"
+    with pytest.raises(ValueError, match="muelu"):
+        caseinfo.backend(case("muelu"))
+    with pytest.raises(ValueError, match="bad solver type"):
+        caseinfo.backend(case("petsc"))
