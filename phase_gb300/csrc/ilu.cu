@@ -560,17 +560,19 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
 
 // Line-form sweeps (kernels.cuh LineMeta) of a group of structured blocks.
 // Lane i of a member walks grid line i, one row per level: on level l it
-// owns row (i, l - i).  Forward, z(i, j) = x(i, j) - f0 z(i-1, j) - f1
-// z(i, j-1): z(i-1, j) is lane i-1's result of level l-1 (a shuffle) and
-// z(i, j-1) the lane's own (`carry`); backward, z(i, j) = (z(i, j) - b1
-// z(i, j+1) - b0 z(i+1, j)) / u_ii with z(i+1, j) from lane i+1.  The chain
-// of a level is a shuffle and two multiply-adds; the weights and the
-// row's input are read from shared memory one level ahead.  The products
-// are subtracted in the order of the row's factor slots (increasing
-// column), as the stream form does, so both give the same results.  Pieces
-// of the record are double-buffered through shared memory by TMA as in
-// k_ilu0_apply_stream; input staging, subdomain sums and the output (with
-// y_s in mode 3) are the same too.
+// owns position s = l - i of its line.  Forward, z(i, j) = x(i, j) - f0
+// z(i-1, j) - f1 z(i, j-1): z(i-1, j) is lane i-1's result of level l-1 (a
+// shuffle) and z(i, j-1) the lane's own (`carry`); backward, z(i, j) =
+// (z(i, j) - b1 z(i, j+1) - b0 z(i+1, j)) / u_ii with z(i+1, j) from lane
+// i+1.  The group's vector is copied into line-major order in shared memory
+// and the weights are stored line by line, so a lane's next row and
+// weights are consecutive and read one level ahead; the chain of a level is
+// a shuffle and two multiply-adds.  The products are subtracted in the
+// order of the row's factor slots (increasing column), as the stream form
+// does, so both give the same results.  The record's map and both weight
+// arrays are bulk-copied into shared memory at kernel start, beside the
+// input staging; subdomain sums and the output (with y_s in mode 3) are as
+// in k_ilu0_apply_stream.
 template <class AR>
 __device__ __forceinline__ typename AR::V shfl_up_v(typename AR::V x, int w);
 template <>
@@ -592,25 +594,6 @@ template <>
 __device__ __forceinline__ float2 shfl_down_v<ArithDD>(float2 x, int w) {
   return make_float2(__shfl_down_sync(0xffffffffu, x.x, 1, w),
                      __shfl_down_sync(0xffffffffu, x.y, 1, w));
-}
-
-// a level's members: start row, rows, first line
-struct LineLevel {
-  int a, w, lo, t0;  // this lane's member: rows a .. a+w-1 on lines lo ..;
-                     // its entries start at t0 in the level blob
-  int wsum;          // entries of the level (both members)
-};
-__device__ __forceinline__ LineLevel line_level(const uint2 *L, int l,
-                                                int mem) {
-  const uint2 x = L[l];
-  const int w0 = (int)(x.y & 0xFFu), w1 = (int)((x.y >> 16) & 0xFFu);
-  LineLevel g;
-  g.a = mem ? (int)(x.x >> 16) : (int)(x.x & 0xFFFFu);
-  g.w = mem ? w1 : w0;
-  g.lo = mem ? (int)(x.y >> 24) : (int)((x.y >> 8) & 0xFFu);
-  g.t0 = mem ? w0 : 0;
-  g.wsum = w0 + w1;
-  return g;
 }
 
 // One row of a line sweep: self - w0 x0 - w1 x1 (* d), with the weights in
@@ -672,17 +655,15 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
     }
     mbar_expect_tx(&bar[0], (uint32_t)m.p0_bytes);
     bulk_load(buf0, g + m.p0_off, (uint32_t)m.p0_bytes, &bar[0]);
-    if (m.p1_bytes > 0) {
-      mbar_expect_tx(&bar[1], (uint32_t)m.p1_bytes);
-      bulk_load(buf0 + m.buf1, g + m.p1_off, (uint32_t)m.p1_bytes, &bar[1]);
-    }
+    mbar_expect_tx(&bar[1], (uint32_t)m.p1_bytes);
+    bulk_load(buf0 + m.buf1, g + m.p1_off, (uint32_t)m.p1_bytes, &bar[1]);
   }
   if (tma_in) {
     __syncwarp();  // lane 0 has initialised the barriers
     if (!mbar_wait_bounded(&bar[3], err)) {
       mbar_wait_bounded(&bar[2], nullptr, 0u);
       mbar_wait_bounded(&bar[0], nullptr, 0u);
-      if (m.p1_bytes > 0) mbar_wait_bounded(&bar[1], nullptr, 0u);
+      mbar_wait_bounded(&bar[1], nullptr, 0u);
       return;
     }
     if (csum) {  // the same lane-strided order as the register staging
@@ -738,139 +719,99 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
   __syncwarp();
   if (!mbar_wait_bounded(&bar[2], err)) {
     mbar_wait_bounded(&bar[0], nullptr, 0u);
-    if (m.p1_bytes > 0) mbar_wait_bounded(&bar[1], nullptr, 0u);
+    mbar_wait_bounded(&bar[1], nullptr, 0u);
     return;
   }
-  const uint2 *L = reinterpret_cast<const uint2 *>(hdr);
-  const int32_t *ints = reinterpret_cast<const int32_t *>(hdr + 8 * nlev);
-  const int nF = ints[0], nB = ints[1], P = nF + nB;
-  const int32_t *tab = ints + 2;
-  constexpr int vs = (int)sizeof(WT);
+  // the group's vector in line-major order
+  const uint16_t *map = reinterpret_cast<const uint16_t *>(hdr);
+  MT *zl = zs + al16(8 * (nr + 1)) / (int)sizeof(MT);
+  for (int i = lane; i < nr; i += 32) zl[map[i]] = zs[i];
   const int width = m.lanes;  // shuffle segment: 16 (pair) or 32
   const int mem = width == 16 ? lane >> 4 : 0;
   const int li = width == 16 ? lane & 15 : lane;
-  MT carry = AR::zero();
-  uint32_t phases = 0u;
-  for (int j = 0; j < P; ++j) {
-    const int sb = j & 1;
-    if (!mbar_wait_bounded(&bar[sb], err, (phases >> sb) & 1u)) {
-      if (j + 1 < P)
-        mbar_wait_bounded(&bar[sb ^ 1], nullptr, (phases >> (sb ^ 1)) & 1u);
-      return;
+  const int len = mem ? m.len1 : m.len0;
+  const bool mine = li < (mem ? m.lines1 : m.lines0);
+  const int pos0 = (mem ? m.nr0 : 0) + li * len;  // this lane's line start
+  MT *zline = zl + pos0;
+  __syncwarp();
+  // forward: on level l this lane owns position s = l - li of its line
+  if (!mbar_wait_bounded(&bar[0], err, 0u)) {
+    mbar_wait_bounded(&bar[1], nullptr, 0u);
+    return;
+  }
+  {
+    const WT *fw = reinterpret_cast<const WT *>(buf0) + 2 * pos0;
+    MT carry = AR::zero();
+    // operands of the next active position, read one level ahead
+    WT f0 = WT(), f1 = WT();
+    MT x = AR::zero();
+    if (mine && len > 0) {
+      f0 = fw[0];
+      f1 = fw[1];
+      x = zline[0];
     }
-    phases ^= 1u << sb;
-    const uint8_t *pc = buf0 + (sb ? m.buf1 : 0);
-    if (j == nF) carry = AR::zero();  // the backward sweep starts
-    if (j < nF) {
-      const int l0 = tab[3 * j];
-      const int l1 = j + 1 < nF ? tab[3 * (j + 1)] : nlev;
-      // operands of level l0, then each level reads the next one's
-      LineLevel cl = line_level(L, l0, mem);
-      int k = li - cl.lo;
-      bool ok = (unsigned)k < (unsigned)cl.w;
-      WT f0 = WT(), f1 = WT();
-      MT x = AR::zero();
-      if (ok) {
-        const WT *fp = reinterpret_cast<const WT *>(pc) + 2 * (cl.t0 + k);
-        f0 = fp[0];
-        f1 = fp[1];
-        x = zs[cl.a + k];
+    for (int l = 0; l < nlev; ++l) {
+      const int sp = l - li;
+      const bool ok = mine && (unsigned)sp < (unsigned)len;
+      WT g0 = f0, g1 = f1;
+      MT xn = x;
+      if (ok && sp + 1 < len) {
+        g0 = fw[2 * (sp + 1)];
+        g1 = fw[2 * (sp + 1) + 1];
+        xn = zline[sp + 1];
       }
-      for (int l = l0; l < l1; ++l) {
-        const uint8_t *pn = pc + al16(2 * vs * cl.wsum);
-        LineLevel nl{};
-        int kn = 0;
-        bool okn = false;
-        WT g0 = WT(), g1 = WT();
-        MT xn = AR::zero();
-        if (l + 1 < l1) {
-          nl = line_level(L, l + 1, mem);
-          kn = li - nl.lo;
-          okn = (unsigned)kn < (unsigned)nl.w;
-          if (okn) {
-            const WT *fp = reinterpret_cast<const WT *>(pn) + 2 * (nl.t0 + kn);
-            g0 = fp[0];
-            g1 = fp[1];
-            xn = zs[nl.a + kn];
-          }
-        }
-        MT left = shfl_up_v<AR>(carry, width);
-        if (li == 0) left = AR::zero();
-        MT out = AR::zero();
-        if (ok) {
-          out = line_row<AR, WT, false>(x, f0, f1, left, carry, WT());
-          zs[cl.a + k] = out;
-        }
-        carry = out;
-        cl = nl;
-        k = kn;
-        ok = okn;
+      MT left = shfl_up_v<AR>(carry, width);
+      if (li == 0) left = AR::zero();
+      MT out = AR::zero();
+      if (ok) {
+        out = line_row<AR, WT, false>(x, f0, f1, left, carry, WT());
+        zline[sp] = out;
         f0 = g0;
         f1 = g1;
         x = xn;
-        pc = pn;
       }
-    } else {
-      const int lhi = tab[3 * j];
-      const int llo = j + 1 < P ? tab[3 * (j + 1)] + 1 : 0;
-      LineLevel cl = line_level(L, lhi, mem);
-      int k = li - cl.lo;
-      bool ok = (unsigned)k < (unsigned)cl.w;
-      WT b0 = WT(), b1 = WT(), dg = WT();
-      MT x = AR::zero();
+      carry = out;
+    }
+  }
+  // backward: on level l this lane owns position s = l - li, descending
+  if (!mbar_wait_bounded(&bar[1], err, 0u)) return;
+  {
+    const WT *bw = reinterpret_cast<const WT *>(buf0 + m.buf1) + 3 * pos0;
+    MT carry = AR::zero();
+    WT b0 = WT(), b1 = WT(), dg = WT();
+    MT x = AR::zero();
+    const int last = len - 1;
+    if (mine && len > 0) {
+      b0 = bw[3 * last];
+      b1 = bw[3 * last + 1];
+      dg = bw[3 * last + 2];
+      x = zline[last];
+    }
+    for (int l = nlev - 1; l >= 0; --l) {
+      const int sp = l - li;
+      const bool ok = mine && (unsigned)sp < (unsigned)len;
+      WT c0 = b0, c1 = b1, cd = dg;
+      MT xn = x;
+      if (ok && sp > 0) {
+        c0 = bw[3 * (sp - 1)];
+        c1 = bw[3 * (sp - 1) + 1];
+        cd = bw[3 * (sp - 1) + 2];
+        xn = zline[sp - 1];
+      }
+      MT right = shfl_down_v<AR>(carry, width);
+      if (li == width - 1) right = AR::zero();
+      MT out = AR::zero();
       if (ok) {
-        const WT *bp = reinterpret_cast<const WT *>(pc) + 3 * (cl.t0 + k);
-        b0 = bp[0];
-        b1 = bp[1];
-        dg = bp[2];
-        x = zs[cl.a + k];
-      }
-      for (int l = lhi; l >= llo; --l) {
-        const uint8_t *pn = pc + al16(3 * vs * cl.wsum);
-        LineLevel nl{};
-        int kn = 0;
-        bool okn = false;
-        WT c0 = WT(), c1 = WT(), cd = WT();
-        MT xn = AR::zero();
-        if (l - 1 >= llo) {
-          nl = line_level(L, l - 1, mem);
-          kn = li - nl.lo;
-          okn = (unsigned)kn < (unsigned)nl.w;
-          if (okn) {
-            const WT *bp = reinterpret_cast<const WT *>(pn) + 3 * (nl.t0 + kn);
-            c0 = bp[0];
-            c1 = bp[1];
-            cd = bp[2];
-            xn = zs[nl.a + kn];
-          }
-        }
-        MT right = shfl_down_v<AR>(carry, width);
-        if (li == width - 1) right = AR::zero();
-        MT out = AR::zero();
-        if (ok) {
-          // U slots in increasing column: (i, j+1) (this lane's line) is
-          // on an earlier line than (i+1, j)
-          out = line_row<AR, WT, true>(x, b1, b0, carry, right, dg);
-          zs[cl.a + k] = out;
-        }
-        carry = out;
-        cl = nl;
-        k = kn;
-        ok = okn;
+        // U slots in increasing column: (i, j+1) (this lane's line) is on
+        // an earlier line than (i+1, j)
+        out = line_row<AR, WT, true>(x, b1, b0, carry, right, dg);
+        zline[sp] = out;
         b0 = c0;
         b1 = c1;
         dg = cd;
         x = xn;
-        pc = pn;
       }
-    }
-    // every lane has consumed its reads of this buffer before it is refilled
-    __syncwarp();
-    if (lane == 0 && j + 2 < P) {
-      fence_proxy_async();
-      mbar_expect_tx(&bar[sb], (uint32_t)tab[3 * (j + 2) + 2]);
-      bulk_load(buf0 + (sb ? m.buf1 : 0), g + tab[3 * (j + 2) + 1],
-                (uint32_t)tab[3 * (j + 2) + 2], &bar[sb]);
+      carry = out;
     }
   }
   __syncwarp();
@@ -879,9 +820,9 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
     const MT y0 = AR::load_y(def_y, m.sub0);
     const MT y1 = m.nsub > 1 ? AR::load_y(def_y, m.sub0 + 1) : y0;
     for (int i = lane; i < nr; i += 32)
-      z[m.r0 + i] = AR::add(zs[i], i < m.nr0 ? y0 : y1);
+      z[m.r0 + i] = AR::add(zl[map[i]], i < m.nr0 ? y0 : y1);
   } else {
-    for (int i = lane; i < nr; i += 32) z[m.r0 + i] = zs[i];
+    for (int i = lane; i < nr; i += 32) z[m.r0 + i] = zl[map[i]];
   }
 }
 
