@@ -1225,9 +1225,9 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       lm.len1 = (uint16_t)len[1];
       lmeta.push_back(lm);
       loff += total;
-      // level-order and line-major copies of the group's vector
+      // the group's vector (line-major)
       lsmem = std::max(lsmem, (size_t)lm.zs_off +
-                                  2 * (size_t)al16(8 * (int64_t)(nr + 1)));
+                                  (size_t)al16(8 * (int64_t)(nr + 1)));
       s += G;
     }
     return PG_OK;

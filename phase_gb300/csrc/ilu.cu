@@ -570,9 +570,9 @@ k_ilu0_apply_stream(const StreamMeta *__restrict__ meta,
 // a shuffle and two multiply-adds.  The products are subtracted in the
 // order of the row's factor slots (increasing column), as the stream form
 // does, so both give the same results.  The record's map and both weight
-// arrays are bulk-copied into shared memory at kernel start, beside the
-// input staging; subdomain sums and the output (with y_s in mode 3) are as
-// in k_ilu0_apply_stream.
+// arrays are bulk-copied into shared memory at kernel start; the input is
+// staged through the map with the subdomain sums taken in the stream
+// form's order, and the output (with y_s in mode 3) goes back through it.
 template <class AR>
 __device__ __forceinline__ typename AR::V shfl_up_v(typename AR::V x, int w);
 template <>
@@ -629,55 +629,36 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
   pdl_wait();
   if (sc && sc->done) return;
   extern __shared__ __align__(128) uint8_t smem[];
-  __shared__ __align__(8) uint64_t bar[4];
+  __shared__ __align__(8) uint64_t bar[3];
   const LineMeta m = meta[blockIdx.x];
   const int lane = threadIdx.x;
   const int nr = m.nr, nlev = m.nlev;
   uint8_t *hdr = smem;
   uint8_t *const buf0 = smem + m.hdr_bytes;
-  MT *zs = reinterpret_cast<MT *>(smem + m.zs_off);
+  // the group's vector, in line-major order
+  MT *zl = reinterpret_cast<MT *>(smem + m.zs_off);
   const uint8_t *g = rec + m.rec_off;
-  // modes 0 and 3 read one input vector: one bulk copy straight into z,
-  // in flight with the factor pieces (16-byte aligned ranges only)
-  const bool tma_in =
-      (MODE == 0 || MODE == 3) && (nr & 1) == 0 &&
-      (reinterpret_cast<uintptr_t>(pv + m.r0) & 15u) == 0;
   if (lane == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     mbar_init(&bar[2], 1);
-    mbar_init(&bar[3], 1);
     mbar_expect_tx(&bar[2], (uint32_t)m.hdr_bytes);
     bulk_load(hdr, g, (uint32_t)m.hdr_bytes, &bar[2]);
-    if (tma_in) {
-      mbar_expect_tx(&bar[3], (uint32_t)(nr * sizeof(MT)));
-      bulk_load(zs, pv + m.r0, (uint32_t)(nr * sizeof(MT)), &bar[3]);
-    }
     mbar_expect_tx(&bar[0], (uint32_t)m.p0_bytes);
     bulk_load(buf0, g + m.p0_off, (uint32_t)m.p0_bytes, &bar[0]);
     mbar_expect_tx(&bar[1], (uint32_t)m.p1_bytes);
     bulk_load(buf0 + m.buf1, g + m.p1_off, (uint32_t)m.p1_bytes, &bar[1]);
   }
-  if (tma_in) {
-    __syncwarp();  // lane 0 has initialised the barriers
-    if (!mbar_wait_bounded(&bar[3], err)) {
-      mbar_wait_bounded(&bar[2], nullptr, 0u);
-      mbar_wait_bounded(&bar[0], nullptr, 0u);
-      mbar_wait_bounded(&bar[1], nullptr, 0u);
-      return;
-    }
-    if (csum) {  // the same lane-strided order as the register staging
-      typename AR::Sum part0 = AR::sum_init(), part1 = AR::sum_init();
-      for (int i = lane; i < nr; i += 32)
-        AR::sum_add(i < m.nr0 ? part0 : part1, zs[i]);
-      const float2 t0 = AR::sum_warp(part0);
-      if (lane == 0) csum[m.sub0] = t0;
-      if (m.nsub > 1) {
-        const float2 t1 = AR::sum_warp(part1);
-        if (lane == 0) csum[m.sub0 + 1] = t1;
-      }
-    }
-  } else {
+  __syncwarp();  // lane 0 has initialised the barriers
+  // the level-order -> line-major map, then the input staged through it
+  // (the subdomain sums in lane-strided level order)
+  if (!mbar_wait_bounded(&bar[2], err)) {
+    mbar_wait_bounded(&bar[0], nullptr, 0u);
+    mbar_wait_bounded(&bar[1], nullptr, 0u);
+    return;
+  }
+  const uint16_t *map = reinterpret_cast<const uint16_t *>(hdr);
+  {
     constexpr int U = 4;
     const MT zero = AR::zero();
     typename AR::Sum part0 = AR::sum_init(), part1 = AR::sum_init();
@@ -697,12 +678,12 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
         const int i = i0 + 32 * u;
         if (i < nr) {
           MT val;
-          if constexpr (MODE == 3)
+          if constexpr (MODE == 0 || MODE == 3)
             val = pi[u];
           else
             val = AR::combine(MODE, ri[u], pi[u], vi[u], sc);
           if (MODE == 1 || MODE == 2) pv[m.r0 + i] = val;
-          zs[i] = val;
+          zl[map[i]] = val;
           if (csum) AR::sum_add(i < m.nr0 ? part0 : part1, val);
         }
       }
@@ -716,16 +697,6 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
       }
     }
   }
-  __syncwarp();
-  if (!mbar_wait_bounded(&bar[2], err)) {
-    mbar_wait_bounded(&bar[0], nullptr, 0u);
-    mbar_wait_bounded(&bar[1], nullptr, 0u);
-    return;
-  }
-  // the group's vector in line-major order
-  const uint16_t *map = reinterpret_cast<const uint16_t *>(hdr);
-  MT *zl = zs + al16(8 * (nr + 1)) / (int)sizeof(MT);
-  for (int i = lane; i < nr; i += 32) zl[map[i]] = zs[i];
   const int width = m.lanes;  // shuffle segment: 16 (pair) or 32
   const int mem = width == 16 ? lane >> 4 : 0;
   const int li = width == 16 ? lane & 15 : lane;

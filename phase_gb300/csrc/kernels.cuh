@@ -199,8 +199,8 @@ struct LineMeta {
   int32_t p0_off, p0_bytes, p1_off, p1_bytes;  // forward, backward weights
   int32_t sub0, nsub, nr0, lanes;  // lanes per member: 16 (pair) or 32
   int32_t buf1;    // byte offset of piece buffer 1 from buffer 0
-  int32_t zs_off;  // byte offset of the group's z vector in shared memory
-                   // (level order; its line-major copy follows)
+  int32_t zs_off;  // byte offset of the group's z vector (line-major) in
+                   // shared memory
   int16_t lines0, lines1;  // grid lines of member 0 / 1
   uint16_t len0, len1;     // line length (cells) of member 0 / 1
 };
