@@ -721,6 +721,7 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
       f1 = fw[1];
       x = zline[0];
     }
+#pragma unroll 2
     for (int l = 0; l < nlev; ++l) {
       const int sp = l - li;
       const bool ok = mine && (unsigned)sp < (unsigned)len;
@@ -758,6 +759,7 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
       dg = bw[3 * last + 2];
       x = zline[last];
     }
+#pragma unroll 2
     for (int l = nlev - 1; l >= 0; --l) {
       const int sp = l - li;
       const bool ok = mine && (unsigned)sp < (unsigned)len;
