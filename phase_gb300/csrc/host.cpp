@@ -1218,7 +1218,9 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       lm.nr0 = mf[0]->nr;
       lm.lanes = pair ? 16 : 32;
       lm.buf1 = (int32_t)fw_bytes;
-      lm.zs_off = (int32_t)(map_bytes + fw_bytes + bw_bytes);
+      // FP32 weights are held in shared memory, 8-byte ones are read from
+      // global memory (k_ilu0_apply_line)
+      lm.zs_off = (int32_t)(vs == 4 ? map_bytes + fw_bytes + bw_bytes : map_bytes);
       lm.lines0 = (int16_t)lines[0];
       lm.lines1 = (int16_t)lines[1];
       lm.len0 = (uint16_t)len[0];

@@ -638,23 +638,32 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
   // the group's vector, in line-major order
   MT *zl = reinterpret_cast<MT *>(smem + m.zs_off);
   const uint8_t *g = rec + m.rec_off;
+  // FP32 weights (the mixed solver's records) are copied into shared memory
+  // with the map; 8-byte weights (FP64, float pairs) would take more shared
+  // memory than keeps all groups resident at once, so they are read from
+  // global memory, two levels ahead
+  constexpr bool kSmemW = sizeof(WT) == 4;
   if (lane == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     mbar_init(&bar[2], 1);
     mbar_expect_tx(&bar[2], (uint32_t)m.hdr_bytes);
     bulk_load(hdr, g, (uint32_t)m.hdr_bytes, &bar[2]);
-    mbar_expect_tx(&bar[0], (uint32_t)m.p0_bytes);
-    bulk_load(buf0, g + m.p0_off, (uint32_t)m.p0_bytes, &bar[0]);
-    mbar_expect_tx(&bar[1], (uint32_t)m.p1_bytes);
-    bulk_load(buf0 + m.buf1, g + m.p1_off, (uint32_t)m.p1_bytes, &bar[1]);
+    if (kSmemW) {
+      mbar_expect_tx(&bar[0], (uint32_t)m.p0_bytes);
+      bulk_load(buf0, g + m.p0_off, (uint32_t)m.p0_bytes, &bar[0]);
+      mbar_expect_tx(&bar[1], (uint32_t)m.p1_bytes);
+      bulk_load(buf0 + m.buf1, g + m.p1_off, (uint32_t)m.p1_bytes, &bar[1]);
+    }
   }
   __syncwarp();  // lane 0 has initialised the barriers
   // the level-order -> line-major map, then the input staged through it
   // (the subdomain sums in lane-strided level order)
   if (!mbar_wait_bounded(&bar[2], err)) {
-    mbar_wait_bounded(&bar[0], nullptr, 0u);
-    mbar_wait_bounded(&bar[1], nullptr, 0u);
+    if (kSmemW) {
+      mbar_wait_bounded(&bar[0], nullptr, 0u);
+      mbar_wait_bounded(&bar[1], nullptr, 0u);
+    }
     return;
   }
   const uint16_t *map = reinterpret_cast<const uint16_t *>(hdr);
@@ -705,33 +714,38 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
   const int pos0 = (mem ? m.nr0 : 0) + li * len;  // this lane's line start
   MT *zline = zl + pos0;
   __syncwarp();
-  // forward: on level l this lane owns position s = l - li of its line
-  if (!mbar_wait_bounded(&bar[0], err, 0u)) {
+  // forward: on level l this lane owns position s = l - li of its line;
+  // weights are read two positions ahead, the row one position ahead
+  if (kSmemW && !mbar_wait_bounded(&bar[0], err, 0u)) {
     mbar_wait_bounded(&bar[1], nullptr, 0u);
     return;
   }
   {
-    const WT *fw = reinterpret_cast<const WT *>(buf0) + 2 * pos0;
+    const WT *fw = reinterpret_cast<const WT *>(kSmemW ? buf0 : g + m.p0_off) +
+                   2 * pos0;
     MT carry = AR::zero();
-    // operands of the next active position, read one level ahead
-    WT f0 = WT(), f1 = WT();
+    WT f0 = WT(), f1 = WT(), g0 = WT(), g1 = WT();
     MT x = AR::zero();
     if (mine && len > 0) {
       f0 = fw[0];
       f1 = fw[1];
       x = zline[0];
+      if (len > 1) {
+        g0 = fw[2];
+        g1 = fw[3];
+      }
     }
 #pragma unroll 2
     for (int l = 0; l < nlev; ++l) {
       const int sp = l - li;
       const bool ok = mine && (unsigned)sp < (unsigned)len;
-      WT g0 = f0, g1 = f1;
+      WT h0 = g0, h1 = g1;
       MT xn = x;
-      if (ok && sp + 1 < len) {
-        g0 = fw[2 * (sp + 1)];
-        g1 = fw[2 * (sp + 1) + 1];
-        xn = zline[sp + 1];
+      if (ok && sp + 2 < len) {
+        h0 = fw[2 * (sp + 2)];
+        h1 = fw[2 * (sp + 2) + 1];
       }
+      if (ok && sp + 1 < len) xn = zline[sp + 1];
       MT left = shfl_up_v<AR>(carry, width);
       if (li == 0) left = AR::zero();
       MT out = AR::zero();
@@ -740,17 +754,21 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
         zline[sp] = out;
         f0 = g0;
         f1 = g1;
+        g0 = h0;
+        g1 = h1;
         x = xn;
       }
       carry = out;
     }
   }
   // backward: on level l this lane owns position s = l - li, descending
-  if (!mbar_wait_bounded(&bar[1], err, 0u)) return;
+  if (kSmemW && !mbar_wait_bounded(&bar[1], err, 0u)) return;
   {
-    const WT *bw = reinterpret_cast<const WT *>(buf0 + m.buf1) + 3 * pos0;
+    const WT *bw = reinterpret_cast<const WT *>(kSmemW ? buf0 + m.buf1
+                                                       : g + m.p1_off) +
+                   3 * pos0;
     MT carry = AR::zero();
-    WT b0 = WT(), b1 = WT(), dg = WT();
+    WT b0 = WT(), b1 = WT(), dg = WT(), c0 = WT(), c1 = WT(), cd = WT();
     MT x = AR::zero();
     const int last = len - 1;
     if (mine && len > 0) {
@@ -758,19 +776,24 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
       b1 = bw[3 * last + 1];
       dg = bw[3 * last + 2];
       x = zline[last];
+      if (last > 0) {
+        c0 = bw[3 * (last - 1)];
+        c1 = bw[3 * (last - 1) + 1];
+        cd = bw[3 * (last - 1) + 2];
+      }
     }
 #pragma unroll 2
     for (int l = nlev - 1; l >= 0; --l) {
       const int sp = l - li;
       const bool ok = mine && (unsigned)sp < (unsigned)len;
-      WT c0 = b0, c1 = b1, cd = dg;
+      WT e0 = c0, e1 = c1, ed = cd;
       MT xn = x;
-      if (ok && sp > 0) {
-        c0 = bw[3 * (sp - 1)];
-        c1 = bw[3 * (sp - 1) + 1];
-        cd = bw[3 * (sp - 1) + 2];
-        xn = zline[sp - 1];
+      if (ok && sp > 1) {
+        e0 = bw[3 * (sp - 2)];
+        e1 = bw[3 * (sp - 2) + 1];
+        ed = bw[3 * (sp - 2) + 2];
       }
+      if (ok && sp > 0) xn = zline[sp - 1];
       MT right = shfl_down_v<AR>(carry, width);
       if (li == width - 1) right = AR::zero();
       MT out = AR::zero();
@@ -782,6 +805,9 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
         b0 = c0;
         b1 = c1;
         dg = cd;
+        c0 = e0;
+        c1 = e1;
+        cd = ed;
         x = xn;
       }
       carry = out;
