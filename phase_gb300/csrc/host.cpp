@@ -1135,9 +1135,171 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   bool all_lines = want_line && a.n_sub > 0;
   for (int s = 0; s < a.n_sub && all_lines; ++s)
     all_lines = sub_lines[s] > 0 && sub_lines[s] <= 32 &&
-                a.meta64[s].nr % sub_lines[s] == 0 &&
-                a.meta64[s].nr / sub_lines[s] + sub_lines[s] - 1 <= 65535;
-  // vs: bytes of a stored weight (8: FP64 or a float pair, 4: FP32)
+                a.meta64[s].nlev <= 255 &&
+                a.meta64[s].nr % sub_lines[s] == 0;
+  // level-major records for 8-byte weights (k_ilu0_apply_line_lv): a
+  // header of per-level member tables, then level blobs of weights in
+  // pieces of about `piece` bytes streamed through shared memory
+  auto build_lines_lv = [&](int64_t vs, int64_t piece, std::vector<LineMeta> &lmeta,
+                         std::vector<uint8_t> &lrec,
+                         std::vector<int32_t> &lpack_src,
+                         std::vector<int32_t> &lpack_dst, size_t &lsmem) -> int {
+    int64_t loff = 0;
+    for (int s = 0; s < a.n_sub;) {
+      const bool pair = s + 1 < a.n_sub && sub_lines[s] <= 16 &&
+                        sub_lines[s + 1] <= 16 &&
+                        a.meta64[s].nr + a.meta64[s + 1].nr < 65535;
+      const int G = pair ? 2 : 1;
+      const SubMeta *mf[2] = {&a.meta64[s], pair ? &a.meta64[s + 1] : nullptr};
+      const int nr = mf[0]->nr + (pair ? mf[1]->nr : 0);
+      const int nlev = std::max(mf[0]->nlev, pair ? mf[1]->nlev : 0);
+      const int base[2] = {0, mf[0]->nr};
+      // member m's rows of level l: group-local start, count, first line
+      auto lev = [&](int l, int m, int &am, int &wm, int &lom) {
+        am = base[m];
+        wm = 0;
+        lom = 0;
+        if (m >= G || l >= mf[m]->nlev) return;
+        const int32_t *lp = a.lvl_ptr.data() + a.sub_lvl[s + m];
+        am = base[m] + (lp[l] - mf[m]->r0);
+        wm = lp[l + 1] - lp[l];
+        lom = gline[a.perm[lp[l]]];
+      };
+      auto wsum = [&](int l) {
+        int am, w0, w1, lo;
+        lev(l, 0, am, w0, lo);
+        lev(l, 1, am, w1, lo);
+        return w0 + w1;
+      };
+      auto fblob = [&](int w) { return al16(2 * vs * w); };
+      auto bblob = [&](int w) { return al16(3 * vs * w); };
+      std::vector<std::pair<int, int64_t>> fp, bp;
+      for (int l = 0; l < nlev; ++l) {
+        const int64_t sz = fblob(wsum(l));
+        if (fp.empty() || fp.back().second + sz > piece) fp.push_back({l, 0});
+        fp.back().second += sz;
+      }
+      for (int l = nlev - 1; l >= 0; --l) {
+        const int64_t sz = bblob(wsum(l));
+        if (bp.empty() || bp.back().second + sz > piece) bp.push_back({l, 0});
+        bp.back().second += sz;
+      }
+      for (auto &q : fp) q.second = std::max<int64_t>(q.second, 16);
+      for (auto &q : bp) q.second = std::max<int64_t>(q.second, 16);
+      const int np = (int)(fp.size() + bp.size());
+      const int64_t hdr = al16(8 * (int64_t)nlev + 4 * (2 + 3 * (int64_t)np));
+      int64_t total = hdr, max_piece = 16;
+      for (auto &q : fp) total += q.second, max_piece = std::max(max_piece, q.second);
+      for (auto &q : bp) total += q.second, max_piece = std::max(max_piece, q.second);
+      PG_CHECK_ARG(loff + total < ((int64_t)1 << 31), "ILU(0) line records too large");
+      lrec.resize(loff + total, 0);
+      uint8_t *recb = lrec.data() + loff;
+      for (int l = 0; l < nlev; ++l) {
+        int a0, w0, lo0, a1, w1, lo1;
+        lev(l, 0, a0, w0, lo0);
+        lev(l, 1, a1, w1, lo1);
+        uint16_t *h16 = reinterpret_cast<uint16_t *>(recb + 8 * l);
+        h16[0] = (uint16_t)a0;
+        h16[1] = (uint16_t)a1;
+        uint8_t *h8 = recb + 8 * l + 4;
+        h8[0] = (uint8_t)w0;
+        h8[1] = (uint8_t)lo0;
+        h8[2] = (uint8_t)w1;
+        h8[3] = (uint8_t)lo1;
+      }
+      int32_t *ints = reinterpret_cast<int32_t *>(recb + 8 * nlev);
+      ints[0] = (int32_t)fp.size();
+      ints[1] = (int32_t)bp.size();
+      // the weight of the grid neighbour (line + dl, pos + dp) of member m's
+      // factor row `row`: its slot in the factor record, or -1
+      auto nb_slot = [&](int m, int row, bool lower, int dl, int dp) -> int64_t {
+        const SubMeta &f = *mf[m];
+        const int fKL = f.KL, fKU = f.K - f.KL;
+        const uint16_t *fcols = reinterpret_cast<const uint16_t *>(
+            a.rec64.data() + f.rec_off + f.col_off);
+        const int32_t g = a.perm[f.r0 + row];
+        const int k0 = lower ? 0 : fKL, kn = lower ? fKL : fKU;
+        for (int k = 0; k < kn; ++k) {
+          const int64_t sl = (int64_t)(k0 + k) * f.nr + row;
+          if (fcols[sl] == kPadCol) continue;
+          const int32_t c = a.perm[f.r0 + fcols[sl]];
+          if (gline[c] == gline[g] + dl && gpos[c] == gpos[g] + dp) return sl;
+        }
+        return -1;
+      };
+      auto emit = [&](int m, int64_t byte_off, int64_t sl) {
+        if (sl < 0) return;  // weight stays 0
+        const int64_t fsrc0 = (mf[m]->rec_off + mf[m]->val_off) / 8;
+        lpack_src.push_back((int32_t)(fsrc0 + sl));
+        lpack_dst.push_back((int32_t)((loff + byte_off) / vs));
+      };
+      int64_t off = hdr;
+      auto emit_level = [&](int l, bool fwd) {
+        int am[2], wm[2], lom[2];
+        lev(l, 0, am[0], wm[0], lom[0]);
+        lev(l, 1, am[1], wm[1], lom[1]);
+        int t = 0;
+        for (int m = 0; m < 2; ++m)
+          for (int k = 0; k < wm[m]; ++k, ++t) {
+            const int row = am[m] - base[m] + k;  // member-local row
+            if (fwd) {
+              emit(m, off + vs * (2 * t), nb_slot(m, row, true, -1, 0));
+              emit(m, off + vs * (2 * t + 1), nb_slot(m, row, true, 0, -1));
+            } else {
+              emit(m, off + vs * (3 * t), nb_slot(m, row, false, 1, 0));
+              emit(m, off + vs * (3 * t + 1), nb_slot(m, row, false, 0, 1));
+              emit(m, off + vs * (3 * t + 2),
+                   (int64_t)mf[m]->K * mf[m]->nr + row);
+            }
+          }
+        off += fwd ? fblob(t) : bblob(t);
+      };
+      int tq = 0;
+      for (size_t q = 0; q < fp.size(); ++q, ++tq) {
+        const int l0 = fp[q].first;
+        const int l1 = q + 1 < fp.size() ? fp[q + 1].first : nlev;
+        ints[2 + 3 * tq] = l0;
+        ints[3 + 3 * tq] = (int32_t)off;
+        ints[4 + 3 * tq] = (int32_t)fp[q].second;
+        for (int l = l0; l < l1; ++l) emit_level(l, true);
+      }
+      for (size_t q = 0; q < bp.size(); ++q, ++tq) {
+        const int lhi = bp[q].first;
+        const int llo = q + 1 < bp.size() ? bp[q + 1].first + 1 : 0;
+        ints[2 + 3 * tq] = lhi;
+        ints[3 + 3 * tq] = (int32_t)off;
+        ints[4 + 3 * tq] = (int32_t)bp[q].second;
+        for (int l = lhi; l >= llo; --l) emit_level(l, false);
+      }
+      LineMeta lm{};
+      lm.r0 = mf[0]->r0;
+      lm.nr = nr;
+      lm.nlev = nlev;
+      lm.rec_off = (int32_t)loff;
+      lm.hdr_bytes = (int32_t)hdr;
+      lm.max_piece = (int32_t)max_piece;
+      lm.p0_off = ints[3];
+      lm.p0_bytes = ints[4];
+      if (np > 1) {
+        lm.p1_off = ints[6];
+        lm.p1_bytes = ints[7];
+      }
+      lm.sub0 = s;
+      lm.nsub = G;
+      lm.nr0 = mf[0]->nr;
+      lm.lanes = pair ? 16 : 32;
+      // buffer 1 follows buffer 0; with two pieces each takes its own size
+      lm.buf1 = np == 2 ? (int32_t)al16(ints[4]) : (int32_t)max_piece;
+      lm.zs_off = (int32_t)(hdr + lm.buf1 + (np == 2 ? al16(ints[7]) : max_piece));
+      lmeta.push_back(lm);
+      loff += total;
+      lsmem = std::max(lsmem, (size_t)lm.zs_off +
+                                  (size_t)al16(8 * (int64_t)(nr + 1)));
+      s += G;
+    }
+    return PG_OK;
+  };
+  // line-major records for FP32 weights (k_ilu0_apply_line)
   auto build_lines = [&](int64_t vs, std::vector<LineMeta> &lmeta,
                          std::vector<uint8_t> &lrec,
                          std::vector<int32_t> &lpack_src,
@@ -1218,9 +1380,7 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
       lm.nr0 = mf[0]->nr;
       lm.lanes = pair ? 16 : 32;
       lm.buf1 = (int32_t)fw_bytes;
-      // FP32 weights are held in shared memory, 8-byte ones are read from
-      // global memory (k_ilu0_apply_line)
-      lm.zs_off = (int32_t)(vs == 4 ? map_bytes + fw_bytes + bw_bytes : map_bytes);
+      lm.zs_off = (int32_t)(map_bytes + fw_bytes + bw_bytes);
       lm.lines0 = (int16_t)lines[0];
       lm.lines1 = (int16_t)lines[1];
       lm.len0 = (uint16_t)len[0];
@@ -1235,7 +1395,8 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
     return PG_OK;
   };
   if (all_lines) {
-    int rc = build_lines(8, a.lmeta, a.lrec, a.lpack_src, a.lpack_dst, a.lsmem);
+    int rc = build_lines_lv(8, 8192, a.lmeta, a.lrec, a.lpack_src, a.lpack_dst,
+                            a.lsmem);
     if (!rc)
       rc = build_lines(4, a.lmeta32, a.lrec32, a.lpack32_src, a.lpack32_dst,
                        a.lsmem32);

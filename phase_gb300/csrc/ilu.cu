@@ -638,11 +638,10 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
   // the group's vector, in line-major order
   MT *zl = reinterpret_cast<MT *>(smem + m.zs_off);
   const uint8_t *g = rec + m.rec_off;
-  // FP32 weights (the mixed solver's records) are copied into shared memory
-  // with the map; 8-byte weights (FP64, float pairs) would take more shared
-  // memory than keeps all groups resident at once, so they are read from
-  // global memory, two levels ahead
-  constexpr bool kSmemW = sizeof(WT) == 4;
+  // used for FP32 weights only (the map and both weight arrays fit in
+  // shared memory beside the group's vector); 8-byte weights take the
+  // level-major form, k_ilu0_apply_line_lv
+  constexpr bool kSmemW = true;
   if (lane == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -822,6 +821,285 @@ k_ilu0_apply_line(const LineMeta *__restrict__ meta,
       z[m.r0 + i] = AR::add(zl[map[i]], i < m.nr0 ? y0 : y1);
   } else {
     for (int i = lane; i < nr; i += 32) z[m.r0 + i] = zl[map[i]];
+  }
+}
+
+// a level's members: start row, rows, first line
+struct LineLevel {
+  int a, w, lo, t0;  // this lane's member: rows a .. a+w-1 on lines lo ..;
+                     // its entries start at t0 in the level blob
+  int wsum;          // entries of the level (both members)
+};
+__device__ __forceinline__ LineLevel line_level(const uint2 *L, int l,
+                                                int mem) {
+  const uint2 x = L[l];
+  const int w0 = (int)(x.y & 0xFFu), w1 = (int)((x.y >> 16) & 0xFFu);
+  LineLevel g;
+  g.a = mem ? (int)(x.x >> 16) : (int)(x.x & 0xFFFFu);
+  g.w = mem ? w1 : w0;
+  g.lo = mem ? (int)(x.y >> 24) : (int)((x.y >> 8) & 0xFFu);
+  g.t0 = mem ? w0 : 0;
+  g.wsum = w0 + w1;
+  return g;
+}
+
+// Level-major form of the line sweep, for 8-byte weights (FP64 records and
+// their float-pair copies): the record is a header of per-level member
+// tables and level blobs of weights (kernels.cuh LineMeta, built by
+// analyse() for these records), streamed through two shared-memory buffers
+// by TMA, so a group needs little shared memory; lane i's entry of level l
+// is found from the level's table.  Same arithmetic, in the same order, as
+// k_ilu0_apply_line.
+template <class AR, int MODE, class WT>
+__global__ void __launch_bounds__(32)
+k_ilu0_apply_line_lv(const LineMeta *__restrict__ meta,
+                  const uint8_t *__restrict__ rec,
+                  const typename AR::V *__restrict__ r,
+                  typename AR::V *__restrict__ pv,
+                  const typename AR::V *__restrict__ v,
+                  typename AR::V *__restrict__ z,
+                  const KScalars *__restrict__ sc, int *__restrict__ err,
+                  float2 *__restrict__ csum, const void *__restrict__ def_y) {
+  using MT = typename AR::V;
+  pdl_wait();
+  if (sc && sc->done) return;
+  extern __shared__ __align__(128) uint8_t smem[];
+  __shared__ __align__(8) uint64_t bar[4];
+  const LineMeta m = meta[blockIdx.x];
+  const int lane = threadIdx.x;
+  const int nr = m.nr, nlev = m.nlev;
+  uint8_t *hdr = smem;
+  uint8_t *const buf0 = smem + m.hdr_bytes;
+  MT *zs = reinterpret_cast<MT *>(smem + m.zs_off);
+  const uint8_t *g = rec + m.rec_off;
+  // modes 0 and 3 read one input vector: one bulk copy straight into z,
+  // in flight with the factor pieces (16-byte aligned ranges only)
+  const bool tma_in =
+      (MODE == 0 || MODE == 3) && (nr & 1) == 0 &&
+      (reinterpret_cast<uintptr_t>(pv + m.r0) & 15u) == 0;
+  if (lane == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init(&bar[2], 1);
+    mbar_init(&bar[3], 1);
+    mbar_expect_tx(&bar[2], (uint32_t)m.hdr_bytes);
+    bulk_load(hdr, g, (uint32_t)m.hdr_bytes, &bar[2]);
+    if (tma_in) {
+      mbar_expect_tx(&bar[3], (uint32_t)(nr * sizeof(MT)));
+      bulk_load(zs, pv + m.r0, (uint32_t)(nr * sizeof(MT)), &bar[3]);
+    }
+    mbar_expect_tx(&bar[0], (uint32_t)m.p0_bytes);
+    bulk_load(buf0, g + m.p0_off, (uint32_t)m.p0_bytes, &bar[0]);
+    if (m.p1_bytes > 0) {
+      mbar_expect_tx(&bar[1], (uint32_t)m.p1_bytes);
+      bulk_load(buf0 + m.buf1, g + m.p1_off, (uint32_t)m.p1_bytes, &bar[1]);
+    }
+  }
+  if (tma_in) {
+    __syncwarp();  // lane 0 has initialised the barriers
+    if (!mbar_wait_bounded(&bar[3], err)) {
+      mbar_wait_bounded(&bar[2], nullptr, 0u);
+      mbar_wait_bounded(&bar[0], nullptr, 0u);
+      if (m.p1_bytes > 0) mbar_wait_bounded(&bar[1], nullptr, 0u);
+      return;
+    }
+    if (csum) {  // the same lane-strided order as the register staging
+      typename AR::Sum part0 = AR::sum_init(), part1 = AR::sum_init();
+      for (int i = lane; i < nr; i += 32)
+        AR::sum_add(i < m.nr0 ? part0 : part1, zs[i]);
+      const float2 t0 = AR::sum_warp(part0);
+      if (lane == 0) csum[m.sub0] = t0;
+      if (m.nsub > 1) {
+        const float2 t1 = AR::sum_warp(part1);
+        if (lane == 0) csum[m.sub0 + 1] = t1;
+      }
+    }
+  } else {
+    constexpr int U = 4;
+    const MT zero = AR::zero();
+    typename AR::Sum part0 = AR::sum_init(), part1 = AR::sum_init();
+    for (int i0 = lane; i0 < nr; i0 += 32 * U) {
+      MT ri[U], pi[U], vi[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + 32 * u;
+        ri[u] = pi[u] = vi[u] = zero;
+        if (i < nr) {
+          if (MODE == 1 || MODE == 2) ri[u] = r[m.r0 + i], vi[u] = v[m.r0 + i];
+          if (MODE != 2) pi[u] = pv[m.r0 + i];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + 32 * u;
+        if (i < nr) {
+          MT val;
+          if constexpr (MODE == 3)
+            val = pi[u];
+          else
+            val = AR::combine(MODE, ri[u], pi[u], vi[u], sc);
+          if (MODE == 1 || MODE == 2) pv[m.r0 + i] = val;
+          zs[i] = val;
+          if (csum) AR::sum_add(i < m.nr0 ? part0 : part1, val);
+        }
+      }
+    }
+    if (csum) {
+      const float2 t0 = AR::sum_warp(part0);
+      if (lane == 0) csum[m.sub0] = t0;
+      if (m.nsub > 1) {
+        const float2 t1 = AR::sum_warp(part1);
+        if (lane == 0) csum[m.sub0 + 1] = t1;
+      }
+    }
+  }
+  __syncwarp();
+  if (!mbar_wait_bounded(&bar[2], err)) {
+    mbar_wait_bounded(&bar[0], nullptr, 0u);
+    if (m.p1_bytes > 0) mbar_wait_bounded(&bar[1], nullptr, 0u);
+    return;
+  }
+  const uint2 *L = reinterpret_cast<const uint2 *>(hdr);
+  const int32_t *ints = reinterpret_cast<const int32_t *>(hdr + 8 * nlev);
+  const int nF = ints[0], nB = ints[1], P = nF + nB;
+  const int32_t *tab = ints + 2;
+  constexpr int vs = (int)sizeof(WT);
+  const int width = m.lanes;  // shuffle segment: 16 (pair) or 32
+  const int mem = width == 16 ? lane >> 4 : 0;
+  const int li = width == 16 ? lane & 15 : lane;
+  MT carry = AR::zero();
+  uint32_t phases = 0u;
+  for (int j = 0; j < P; ++j) {
+    const int sb = j & 1;
+    if (!mbar_wait_bounded(&bar[sb], err, (phases >> sb) & 1u)) {
+      if (j + 1 < P)
+        mbar_wait_bounded(&bar[sb ^ 1], nullptr, (phases >> (sb ^ 1)) & 1u);
+      return;
+    }
+    phases ^= 1u << sb;
+    const uint8_t *pc = buf0 + (sb ? m.buf1 : 0);
+    if (j == nF) carry = AR::zero();  // the backward sweep starts
+    if (j < nF) {
+      const int l0 = tab[3 * j];
+      const int l1 = j + 1 < nF ? tab[3 * (j + 1)] : nlev;
+      // operands of level l0, then each level reads the next one's
+      LineLevel cl = line_level(L, l0, mem);
+      int k = li - cl.lo;
+      bool ok = (unsigned)k < (unsigned)cl.w;
+      WT f0 = WT(), f1 = WT();
+      MT x = AR::zero();
+      if (ok) {
+        const WT *fp = reinterpret_cast<const WT *>(pc) + 2 * (cl.t0 + k);
+        f0 = fp[0];
+        f1 = fp[1];
+        x = zs[cl.a + k];
+      }
+      for (int l = l0; l < l1; ++l) {
+        const uint8_t *pn = pc + al16(2 * vs * cl.wsum);
+        LineLevel nl{};
+        int kn = 0;
+        bool okn = false;
+        WT g0 = WT(), g1 = WT();
+        MT xn = AR::zero();
+        if (l + 1 < l1) {
+          nl = line_level(L, l + 1, mem);
+          kn = li - nl.lo;
+          okn = (unsigned)kn < (unsigned)nl.w;
+          if (okn) {
+            const WT *fp = reinterpret_cast<const WT *>(pn) + 2 * (nl.t0 + kn);
+            g0 = fp[0];
+            g1 = fp[1];
+            xn = zs[nl.a + kn];
+          }
+        }
+        MT left = shfl_up_v<AR>(carry, width);
+        if (li == 0) left = AR::zero();
+        MT out = AR::zero();
+        if (ok) {
+          out = line_row<AR, WT, false>(x, f0, f1, left, carry, WT());
+          zs[cl.a + k] = out;
+        }
+        carry = out;
+        cl = nl;
+        k = kn;
+        ok = okn;
+        f0 = g0;
+        f1 = g1;
+        x = xn;
+        pc = pn;
+      }
+    } else {
+      const int lhi = tab[3 * j];
+      const int llo = j + 1 < P ? tab[3 * (j + 1)] + 1 : 0;
+      LineLevel cl = line_level(L, lhi, mem);
+      int k = li - cl.lo;
+      bool ok = (unsigned)k < (unsigned)cl.w;
+      WT b0 = WT(), b1 = WT(), dg = WT();
+      MT x = AR::zero();
+      if (ok) {
+        const WT *bp = reinterpret_cast<const WT *>(pc) + 3 * (cl.t0 + k);
+        b0 = bp[0];
+        b1 = bp[1];
+        dg = bp[2];
+        x = zs[cl.a + k];
+      }
+      for (int l = lhi; l >= llo; --l) {
+        const uint8_t *pn = pc + al16(3 * vs * cl.wsum);
+        LineLevel nl{};
+        int kn = 0;
+        bool okn = false;
+        WT c0 = WT(), c1 = WT(), cd = WT();
+        MT xn = AR::zero();
+        if (l - 1 >= llo) {
+          nl = line_level(L, l - 1, mem);
+          kn = li - nl.lo;
+          okn = (unsigned)kn < (unsigned)nl.w;
+          if (okn) {
+            const WT *bp = reinterpret_cast<const WT *>(pn) + 3 * (nl.t0 + kn);
+            c0 = bp[0];
+            c1 = bp[1];
+            cd = bp[2];
+            xn = zs[nl.a + kn];
+          }
+        }
+        MT right = shfl_down_v<AR>(carry, width);
+        if (li == width - 1) right = AR::zero();
+        MT out = AR::zero();
+        if (ok) {
+          // U slots in increasing column: (i, j+1) (this lane's line) is
+          // on an earlier line than (i+1, j)
+          out = line_row<AR, WT, true>(x, b1, b0, carry, right, dg);
+          zs[cl.a + k] = out;
+        }
+        carry = out;
+        cl = nl;
+        k = kn;
+        ok = okn;
+        b0 = c0;
+        b1 = c1;
+        dg = cd;
+        x = xn;
+        pc = pn;
+      }
+    }
+    // every lane has consumed its reads of this buffer before it is refilled
+    __syncwarp();
+    if (lane == 0 && j + 2 < P) {
+      fence_proxy_async();
+      mbar_expect_tx(&bar[sb], (uint32_t)tab[3 * (j + 2) + 2]);
+      bulk_load(buf0 + (sb ? m.buf1 : 0), g + tab[3 * (j + 2) + 1],
+                (uint32_t)tab[3 * (j + 2) + 2], &bar[sb]);
+    }
+  }
+  __syncwarp();
+  if constexpr (MODE == 3) {
+    // y of the group's (at most two) subdomains, read once
+    const MT y0 = AR::load_y(def_y, m.sub0);
+    const MT y1 = m.nsub > 1 ? AR::load_y(def_y, m.sub0 + 1) : y0;
+    for (int i = lane; i < nr; i += 32)
+      z[m.r0 + i] = AR::add(zs[i], i < m.nr0 ? y0 : y1);
+  } else {
+    for (int i = lane; i < nr; i += 32) z[m.r0 + i] = zs[i];
   }
 }
 
@@ -1016,15 +1294,18 @@ void launch_line_w(int n_grp, const LineMeta *meta, size_t smem,
                    const typename AR::V *r, typename AR::V *pv,
                    const typename AR::V *v, typename AR::V *z,
                    const KScalars *sc, cudaStream_t st) {
+  // FP32 weights: the line-major form; 8-byte weights: the level-major one
+  constexpr bool kLineMajor = sizeof(WT) == 4;
+  auto kern = kLineMajor ? k_ilu0_apply_line<AR, MODE, WT>
+                         : k_ilu0_apply_line_lv<AR, MODE, WT>;
   static size_t attr = 0;
   if (smem > 48 * 1024 && attr < smem) {
-    cudaFuncSetAttribute(k_ilu0_apply_line<AR, MODE, WT>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)smem);
     attr = smem;
   }
-  launch_pdl(k_ilu0_apply_line<AR, MODE, WT>, n_grp, 32, smem, st, meta, rec,
-             r, pv, v, z, sc, d.err, d.csum, d.def_y);
+  launch_pdl(kern, n_grp, 32, smem, st, meta, rec, r, pv, v, z, sc, d.err,
+             d.csum, d.def_y);
   count_launches(1);
 }
 

@@ -185,15 +185,28 @@ struct StreamMeta {
 // shuffle and that of (i, j-1) is the lane's own previous row, so no level
 // waits for shared memory.  A pair group puts two blocks of at most 16
 // lines side by side (member m uses lanes 16 m .. 16 m + 15); a single
-// block may have up to 32 lines.  Rows are addressed line-major: member m's
-// row (i, j) has position nr0 m + i len_m + j, and each lane reads its own
-// line's weights in order.
-//   map:      uint16 map[nr]: the line-major position of the group's
-//             level-order row r (padded to 16 bytes)
-//   forward:  WT f[nr][2]  {weight of (i-1, j), of (i, j-1)} by position
-//   backward: WT b[nr][3]  {weight of (i+1, j), of (i, j+1), 1/u_ii}
-//   (each padded to 16 bytes; a missing neighbour has weight 0; the two
-//   weight arrays are the pieces p0 and p1, loaded at kernel start)
+// block may have up to 32 lines.  Two record layouts (a missing neighbour
+// has weight 0 in both):
+// * line-major, for FP32 weights (k_ilu0_apply_line): member m's row (i, j)
+//   has position nr0 m + i len_m + j, and each lane reads its own line's
+//   weights in order; map, forward and backward weights are all held in
+//   shared memory
+//     map:      uint16 map[nr]: the line-major position of the group's
+//               level-order row r (padded to 16 bytes)
+//     forward:  WT f[nr][2]  {weight of (i-1, j), of (i, j-1)} by position
+//     backward: WT b[nr][3]  {weight of (i+1, j), of (i, j+1), 1/u_ii}
+//     (each padded to 16 bytes: pieces p0 and p1, loaded at kernel start)
+// * level-major, for 8-byte weights (k_ilu0_apply_line_lv), streamed in
+//   pieces through two shared-memory buffers:
+//     header: per level 8 bytes {uint16 a0, a1; uint8 w0, lo0, w1, lo1}:
+//             member m's rows of level l are group-local rows a_m ..
+//             a_m+w_m-1 on lines lo_m .. lo_m+w_m-1; then int32 nF, nB and
+//             the piece table int32[nF+nB][3] = {level, byte offset, bytes}
+//     level blob (forward):  MT f[w][2]  {weight of (i-1, j), of (i, j-1)}
+//     level blob (backward): MT b[w][3]  {weight of (i+1, j), of (i, j+1),
+//                                         1/u_ii}
+//     entry t of a level: member 0's lines first (t = i - lo0), then member
+//     1's (t = w0 + i - lo1); blobs padded to 16 bytes; w = w0 + w1.
 struct LineMeta {
   int32_t r0, nr, nlev, rec_off, hdr_bytes, max_piece;
   int32_t p0_off, p0_bytes, p1_off, p1_bytes;  // forward, backward weights
@@ -201,8 +214,8 @@ struct LineMeta {
   int32_t buf1;    // byte offset of piece buffer 1 from buffer 0
   int32_t zs_off;  // byte offset of the group's z vector (line-major) in
                    // shared memory
-  int16_t lines0, lines1;  // grid lines of member 0 / 1
-  uint16_t len0, len1;     // line length (cells) of member 0 / 1
+  int16_t lines0, lines1;  // line-major form: grid lines of member 0 / 1
+  uint16_t len0, len1;     // line-major form: line length of member 0 / 1
 };
 
 // Step form of the factor for the float-float sweep of the mixed solver,
