@@ -15,7 +15,7 @@
 //    with partial pivoting over its fully summed rows, and writes it back;
 //  * large fronts: a warp per row assembles the row in global memory (the
 //    same sums in the same order), a CTA adds the owned matrix entries, then
-//    32-column panels as LAPACK's blocked dgetrf does them: the tall panel
+//    kLuPanel-column panels as LAPACK's blocked dgetrf does them: the tall panel
 //    is factorised by one CTA with partial pivoting over the front's fully
 //    summed rows, its interchanges are applied to the columns right of it
 //    and U12 = L11^-1 A12 by TRSM tiles, and the trailing block F22 -= L21
@@ -633,8 +633,8 @@ k_lu_residual(int n, const int32_t *__restrict__ rp, const int32_t *__restrict__
 }
 
 // ------------------------------------------------- dense inverse (FP32)
-// A^-1 column tile by column tile: the identity (new numbering) as 32
-// right-hand sides per CTA, forward eliminated front by front (LINPACK
+// A^-1 column tile by column tile: the identity (new numbering) as
+// kInvCols right-hand sides per CTA, forward eliminated front by front (LINPACK
 // order, FP64 factors read and rounded to FP32), then back substituted
 // from the root down; a front's tile whose columns lie outside its subtree
 // is zero and is only written as zeros.  Small fronts only (m <= kLuSmallM).
