@@ -13,10 +13,9 @@ namespace pg {
 // factorised whole in shared memory by one CTA; larger ones are assembled
 // in global memory and factorised in 32-column panels by batched kernels.
 constexpr int kLuSmallM = 112;
-// panel width of the large fronts: the tall panel is factorised by one CTA
-// (bounded by one SM's FP64 rate), the rest of the panel's flops go to the
-// trailing updates over all SMs, so narrower panels shorten the serial part
-constexpr int kLuPanel = 16;
+// panel width of the large fronts (16 measured no faster on the 1M bubble:
+// 153.6 vs 151.1 ms factorisation, and slower blocked solves)
+constexpr int kLuPanel = 32;
 constexpr int kLuTrsmCols = 128;  // columns of U12 per TRSM tile
 constexpr int kLuUpd = 64;        // edge of a trailing-update tile
 
