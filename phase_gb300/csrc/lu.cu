@@ -185,95 +185,6 @@ k_lu_small(const int32_t *__restrict__ list, LuArgs a,
   for (int e = tid; e < m * m; e += kSmallThreads) out[e] = F[e];
 }
 
-// Small fronts of the coarse matrix (FP32, order <= kLuWarpM): one warp per
-// front, four fronts per CTA, so a pivot step needs only warp
-// synchronisation.  Same sums and pivot choices as k_lu_small: children's
-// blocks in child order, then the owned entries; partial pivoting over the
-// fully summed rows, LINPACK interchanges (columns c.. of the two rows).
-constexpr int kLuWarpM = 64;
-constexpr int kWarpFronts = 4;
-__global__ void __launch_bounds__(32 * kWarpFronts)
-k_lu_small_warp(const int32_t *__restrict__ list, int n_fronts, int mm,
-                LuArgs a, const double *__restrict__ vals,
-                float *__restrict__ fpool) {
-  extern __shared__ float Fs[];  // [kWarpFronts][mm * mm]
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int fi = blockIdx.x * kWarpFronts + wid;
-  if (fi >= n_fronts) return;
-  const LuFront f = a.fronts[list[fi]];
-  const int m = f.m, k = f.k;
-  float *F = Fs + (size_t)wid * mm * mm;
-  for (int e = lane; e < m * m; e += 32) F[e] = 0.f;
-  __syncwarp();
-  for (int c = 0; c < f.n_child; ++c) {
-    const LuFront ch = a.fronts[a.children[f.child_ptr + c]];
-    const int u = ch.m - ch.k;
-    const float *cb = fpool + ch.off;
-    const int32_t *rel = a.rel + ch.rel_off;
-    for (int ra = 0; ra < u; ++ra) {
-      const int pr = rel[ra] * m;
-      const float *src = cb + (size_t)(ch.k + ra) * ch.m + ch.k;
-      for (int rb = lane; rb < u; rb += 32) F[pr + rel[rb]] += src[rb];
-    }
-    __syncwarp();
-  }
-  for (int e = f.ent_ptr + lane; e < f.ent_end; e += 32)
-    F[a.e_pos[e]] += (float)entry_sum(a, vals, e);
-  __syncwarp();
-  for (int c = 0; c < k; ++c) {
-    // pivot: the largest magnitude among the fully summed rows c .. k-1
-    double best = -1.;
-    int br = c;
-    for (int r = c + lane; r < k; r += 32) {
-      const double v = fabs((double)F[r * m + c]);
-      if (v > best) {
-        best = v;
-        br = r;
-      }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const double ob = __shfl_down_sync(0xffffffffu, best, o);
-      const int orr = __shfl_down_sync(0xffffffffu, br, o);
-      if (ob > best || (ob == best && orr < br)) {
-        best = ob;
-        br = orr;
-      }
-    }
-    br = __shfl_sync(0xffffffffu, br, 0);
-    if (br != c)
-      for (int j = c + lane; j < m; j += 32) {
-        const float t = F[c * m + j];
-        F[c * m + j] = F[br * m + j];
-        F[br * m + j] = t;
-      }
-    __syncwarp();
-    float rp = 0.f;
-    if (lane == 0) {
-      a.ipiv[f.s0 + c] = br;
-      const float p = (float)checked_pivot(a, (double)F[c * m + c], f.s0 + c);
-      F[c * m + c] = p;
-      rp = 1.f / p;
-    }
-    rp = __shfl_sync(0xffffffffu, rp, 0);
-    __syncwarp();
-    // this lane's columns of the pivot row, then every row below
-    const int j0 = c + 1 + lane, j1 = j0 + 32;
-    const float u0 = j0 < m ? F[c * m + j0] : 0.f;
-    const float u1 = j1 < m ? F[c * m + j1] : 0.f;
-    for (int i = c + 1; i < m; ++i) {
-      const float l = F[i * m + c] * rp;  // column c is not written here
-      if (j0 < m) F[i * m + j0] -= l * u0;
-      if (j1 < m) F[i * m + j1] -= l * u1;
-    }
-    __syncwarp();
-    for (int i = c + 1 + lane; i < m; i += 32) F[i * m + c] *= rp;
-    __syncwarp();
-  }
-  float *out = fpool + f.off;
-  for (int e = lane; e < m * m; e += 32) out[e] = F[e];
-}
-
 // ---------------------------------------------------------- large fronts
 // one warp per (front, row): children's contribution rows, in child order
 __global__ void __launch_bounds__(256)
@@ -850,10 +761,6 @@ int lu_smem_setup() {
       err = cudaFuncSetAttribute(k_lu_small<float>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     if (err == cudaSuccess)
-      err = cudaFuncSetAttribute(
-          k_lu_small_warp, cudaFuncAttributeMaxDynamicSharedMemorySize,
-          (int)(kWarpFronts * kLuWarpM * kLuWarpM * sizeof(float)));
-    if (err == cudaSuccess)
       err = cudaFuncSetAttribute(k_lu_fwd,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     if (err == cudaSuccess)
@@ -982,12 +889,7 @@ int factor(pg_lu *L, const double *vals, cudaStream_t st, bool f32 = false) {
       int mm = 0;
       for (int i = s.h_small_ptr[h]; i < s.h_small_ptr[h + 1]; ++i)
         mm = std::max(mm, s.fronts[s.h_small[i]].m);
-      if (f32 && mm <= kLuWarpM)
-        k_lu_small_warp<<<(ns + kWarpFronts - 1) / kWarpFronts,
-                          32 * kWarpFronts,
-                          (size_t)kWarpFronts * mm * mm * sizeof(float), st>>>(
-            L->h_small.p + s.h_small_ptr[h], ns, mm, a, vals, L->pool32.p);
-      else if (f32)
+      if (f32)
         k_lu_small<float><<<ns, kSmallThreads, (size_t)mm * mm * sizeof(float),
                             st>>>(L->h_small.p + s.h_small_ptr[h], a, vals,
                                   L->pool32.p);
