@@ -750,6 +750,35 @@ int analyse(int64_t n, const int32_t *row_ptr, const int32_t *col_ind,
   }
   for (auto &d : a.dup_dst) d = cmap[d];
 
+  // 5a. sliced ELLPACK copy of the permuted pattern (slices of 32 rows,
+  //     each as wide as its longest row, stored column-major: entry k of
+  //     row r at sell_ptr[r / 32] + 32 k + r % 32), read by the FP64
+  //     SpMVs so a warp's loads of one entry slot are contiguous; padding
+  //     has column r and no source (value 0)
+  {
+    const int64_t ns = (n + 31) / 32;
+    a.sell_ptr.assign(ns + 1, 0);
+    for (int64_t sl = 0; sl < ns; ++sl) {
+      int32_t w = 0;
+      for (int64_t r = 32 * sl; r < std::min<int64_t>(n, 32 * sl + 32); ++r)
+        w = std::max(w, a.prp[r + 1] - a.prp[r]);
+      a.sell_ptr[sl + 1] = a.sell_ptr[sl] + 32 * w;
+    }
+    a.sell_col.assign(a.sell_ptr[ns], 0);
+    a.sell_src.assign(a.sell_ptr[ns], -1);
+    for (int64_t sl = 0; sl < ns; ++sl) {
+      const int32_t w = (a.sell_ptr[sl + 1] - a.sell_ptr[sl]) / 32;
+      for (int64_t r = 32 * sl; r < 32 * sl + 32; ++r) {
+        const int32_t len = r < n ? a.prp[r + 1] - a.prp[r] : 0;
+        for (int32_t k = 0; k < w; ++k) {
+          const int64_t e = a.sell_ptr[sl] + 32 * (int64_t)k + (r - 32 * sl);
+          a.sell_col[e] = k < len ? a.pci[a.prp[r] + k] : (int32_t)std::min<int64_t>(r, n - 1);
+          a.sell_src[e] = k < len ? a.prp[r] + k : -1;
+        }
+      }
+    }
+  }
+
   // 5b. coarse-space structure (subdomain couplings of the permuted CSR)
   {
     std::vector<int32_t> sub_of(n);

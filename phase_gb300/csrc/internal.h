@@ -241,6 +241,9 @@ struct Analysis {
   int max_sub_rows = 0, max_sub_lu = 0, max_levels = 0;
   std::vector<int32_t> perm, iperm;        // new->old, old->new
   std::vector<int32_t> prp, pci, psrc;     // permuted CSR; psrc -> caller idx
+  // sliced ELLPACK (32-row slices) of the permuted pattern: slice offsets,
+  // columns, permuted-CSR source of each entry (-1 padding)
+  std::vector<int32_t> sell_ptr, sell_col, sell_src;
   std::vector<int32_t> dup_dst, dup_src;   // extra summed duplicates
   std::vector<int32_t> sub_ptr;            // [n_sub+1] permuted row starts
   std::vector<int32_t> sub_lvl;            // [n_sub+1] index into lvl_ptr

@@ -19,6 +19,8 @@
 #include <cstdlib>
 
 #include "../../include/phase_gb300.h"
+#include <type_traits>
+
 #include "kernels.cuh"
 
 namespace pg {
@@ -427,6 +429,31 @@ __device__ __forceinline__ VT row_dot(const int32_t *__restrict__ rp,
   return s;
 }
 
+// row i of the sliced ELLPACK copy: the 32 rows of a slice are one warp's
+// (the block size is a multiple of 32), so each entry slot is one
+// contiguous 256-byte value load and 128-byte column load; the padding adds
+// 0 x x[i] after the row's entries, leaving the CSR sum unchanged
+__device__ __forceinline__ double row_dot_sell(const SolverDev &d,
+                                               const double *__restrict__ x,
+                                               int i) {
+  const int e0 = d.sell_ptr[i >> 5], w = (d.sell_ptr[(i >> 5) + 1] - e0) >> 5;
+  const double *v = d.sell_val + e0 + (i & 31);
+  const int32_t *c = d.sell_col + e0 + (i & 31);
+  double s = 0.;
+  for (int k = 0; k < w; ++k) s += v[32 * k] * x[c[32 * k]];
+  return s;
+}
+
+template <class VT, class MT>
+__device__ __forceinline__ VT row_dot_any(const SolverDev &d,
+                                          const MT *__restrict__ val,
+                                          const VT *__restrict__ x, int i) {
+  if constexpr (std::is_same<VT, double>::value && std::is_same<MT, double>::value) {
+    if (d.sell_val) return row_dot_sell(d, x, i);
+  }
+  return row_dot<VT, MT>(d.prp, d.pci, val, x, i);
+}
+
 template <class VT, class MT>
 __global__ void __launch_bounds__(kVecBlock)
 k_spmv_v(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ ph,
@@ -437,7 +464,7 @@ k_spmv_v(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ ph,
   double acc[1] = {0.};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
        i += gridDim.x * blockDim.x) {
-    const VT vi = row_dot<VT, MT>(d.prp, d.pci, val, ph, i);
+    const VT vi = row_dot_any<VT, MT>(d, val, ph, i);
     v[i] = vi;
     acc[0] += (double)rh[i] * (double)vi;
   }
@@ -466,7 +493,7 @@ k_spmv_t(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ sh,
   double acc[2] = {0., 0.};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n;
        i += gridDim.x * blockDim.x) {
-    const VT ti = row_dot<VT, MT>(d.prp, d.pci, val, sh, i);
+    const VT ti = row_dot_any<VT, MT>(d, val, sh, i);
     t[i] = ti;
     acc[0] += (double)ti * (double)ti;
     acc[1] += (double)ti * (double)s[i];
@@ -769,6 +796,21 @@ void launch_gradient(int n_cells, int nf, const int32_t *fl,
         n_cells, link_ptr, link_face, fnx, fny, grad_face, grad_cell);
     count_launches(1);
   }
+}
+
+__global__ void k_sell_values(int64_t n_ent, const int32_t *__restrict__ src,
+                              const double *__restrict__ pvals,
+                              double *__restrict__ out) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e < n_ent) out[e] = src[e] >= 0 ? pvals[src[e]] : 0.;
+}
+
+void launch_sell_values(int64_t n_ent, const int32_t *sell_src,
+                        const double *pvals, double *sell_val, cudaStream_t st) {
+  if (n_ent <= 0) return;
+  k_sell_values<<<(int)((n_ent + 255) / 256), 256, 0, st>>>(n_ent, sell_src,
+                                                            pvals, sell_val);
+  count_launches(1);
 }
 
 void launch_permute_values(int nnz, const int32_t *psrc, const double *src,

@@ -238,6 +238,10 @@ struct SolverDev {
   int n, nnz, n_sub;
   // permuted CSR
   const int32_t *prp, *pci;
+  // its sliced ELLPACK copy for the FP64 SpMVs (sell_val refreshed with the
+  // values; NULL: the CSR is used)
+  const int32_t *sell_ptr = nullptr, *sell_col = nullptr;
+  const double *sell_val = nullptr;
   // ILU(0) records (FP64)
   const SubMeta *meta64;
   uint8_t *rec64;
@@ -388,6 +392,9 @@ void launch_coarse_apply_dd(const CoarseDev &c, const float2 *in, float2 *z,
                             bool have_sums, const KScalars *sc,
                             cudaStream_t st);
 
+// sliced ELLPACK values from the permuted CSR values (0 on padding)
+void launch_sell_values(int64_t n_ent, const int32_t *sell_src,
+                        const double *pvals, double *sell_val, cudaStream_t st);
 void launch_permute_values(int nnz, const int32_t *psrc, const double *src,
                            double *dst, int n_dup, const int32_t *dup_dst,
                            const int32_t *dup_src, cudaStream_t st);

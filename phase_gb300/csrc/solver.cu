@@ -55,6 +55,10 @@ struct pg_solver {
   bool analysed = false;
   uint64_t eqn_pattern = 0;  // pattern id of a device equation, 0 = host CSR
   DevBuf<int32_t> perm, prp, pci, psrc, dup_dst, dup_src, rec_src;
+  // sliced ELLPACK copy of the matrix for the FP64 SpMVs (PG_FP64 solvers)
+  DevBuf<int32_t> sell_ptr, sell_col, sell_src;
+  DevBuf<double> sell_val;
+  bool sell_on = false;
   DevBuf<SubMeta> meta64;
   DevBuf<uint8_t> rec64;
   DevBuf<StreamMeta> smeta64;
@@ -226,6 +230,11 @@ struct pg_solver {
     d.n_sub = a.n_sub;
     d.prp = prp.p;
     d.pci = pci.p;
+    if (sell_on) {
+      d.sell_ptr = sell_ptr.p;
+      d.sell_col = sell_col.p;
+      d.sell_val = sell_val.p;
+    }
     d.meta64 = meta64.p;
     d.rec64 = rec64.p;
     d.rec_src = rec_src.p;
@@ -334,6 +343,14 @@ int upload_analysis(pg_solver *s) {
   up(s->perm, a.perm);
   up(s->prp, a.prp);
   up(s->pci, a.pci);
+  s->sell_on = s->cfg.precision == PG_FP64 && !s->batch_mode &&
+               !a.sell_ptr.empty();
+  if (s->sell_on) {
+    up(s->sell_ptr, a.sell_ptr);
+    up(s->sell_col, a.sell_col);
+    up(s->sell_src, a.sell_src);
+    if (e == cudaSuccess) e = s->sell_val.reserve(a.sell_col.size());
+  }
   up(s->psrc, a.psrc);
   up(s->dup_dst, a.dup_dst);
   up(s->dup_src, a.dup_src);
@@ -1382,6 +1399,9 @@ extern "C" int pg_solver_set_csr(pg_solver *s, const int32_t *row_ptr,
   if (rj) return rj;
   launch_permute_values((int)s->a.nnz, s->psrc.p, dv, s->pvals.p,
                         (int)s->a.dup_dst.size(), s->dup_dst.p, s->dup_src.p, st);
+  if (s->sell_on)
+    launch_sell_values((int64_t)s->a.sell_col.size(), s->sell_src.p, s->pvals.p,
+                       s->sell_val.p, st);
   PG_CUDA(cudaGetLastError());
   s->have_vals = true;
   s->factored = false;
@@ -1428,6 +1448,9 @@ static int set_eqn(pg_solver *s, const pg_eqn *e, int component, bool reuse) {
   if (rj) return rj;
   launch_permute_values((int)s->a.nnz, s->psrc.p, e->vals.p, s->pvals.p,
                         (int)s->a.dup_dst.size(), s->dup_dst.p, s->dup_src.p, st);
+  if (s->sell_on)
+    launch_sell_values((int64_t)s->a.sell_col.size(), s->sell_src.p, s->pvals.p,
+                       s->sell_val.p, st);
   // the solver receives -rhs_ (FiniteVolumeEquation.tpp:73)
   launch_permute_vec((int)s->a.n, s->perm.p, rhs, -1.0, s->b.p, st);
   PG_CUDA(cudaGetLastError());
