@@ -475,52 +475,41 @@ k_def_pre(int mode, const int32_t *__restrict__ sub_ptr,
 }
 
 // y_s = (A_c^-1)_s . csum (compensated float-float dot, as k_coarse_correct);
-// y_dd (optional) receives y as float pairs for the float-float solver.  A
-// warp per coarse row: each lane keeps four independent compensated
-// accumulators (columns j = lane + 32 (4 q + u)), so four dependent chains
-// are in flight per lane; the accumulators are merged in a fixed order,
-// then the lanes by a butterfly (results repeat bit for bit).
-constexpr int kCoarseYWarps = 8;
-__global__ void __launch_bounds__(32 * kCoarseYWarps)
+// y_dd (optional) receives y as float pairs for the float-float solver
+__global__ void __launch_bounds__(kCorrectBlock)
 k_coarse_y(int K, const float *__restrict__ ainv,
            const float2 *__restrict__ csum, double *__restrict__ y,
            float2 *__restrict__ y_dd, const KScalars *__restrict__ sc) {
   pdl_wait();
   if (sc && sc->done) return;
-  const int lane = threadIdx.x & 31;
-  const int s = blockIdx.x * kCoarseYWarps + (threadIdx.x >> 5);
-  if (s >= K) return;
+  __shared__ float red_s[kCorrectBlock / 32], red_c[kCorrectBlock / 32];
+  const int s = blockIdx.x;
   const float *row = ainv + (size_t)s * K;
-  DdAcc acc[4];
-#pragma unroll
-  for (int u = 0; u < 4; ++u) acc[u] = dd_acc(make_float2(0.f, 0.f));
-  int j = lane;
-  for (; j + 96 < K; j += 128) {
-    float a[4];
-    float2 c[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      a[u] = row[j + 32 * u];
-      c[u] = csum[j + 32 * u];
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) dd_acc_fma(acc[u], make_float2(a[u], 0.f), c[u]);
-  }
-  for (int u = 0; j < K; j += 32, ++u)
-    dd_acc_fma(acc[u & 3], make_float2(row[j], 0.f), csum[j]);
-  dd_acc_merge(acc[0], acc[1]);
-  dd_acc_merge(acc[2], acc[3]);
-  dd_acc_merge(acc[0], acc[2]);
-  DdAcc t = acc[0];
+  DdAcc acc = dd_acc(make_float2(0.f, 0.f));
+  for (int j = threadIdx.x; j < K; j += kCorrectBlock)
+    dd_acc_fma(acc, make_float2(row[j], 0.f), csum[j]);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     DdAcc b;
-    b.s = __shfl_xor_sync(0xffffffffu, t.s, o);
-    b.c = __shfl_xor_sync(0xffffffffu, t.c, o);
-    dd_acc_merge(t, b);
+    b.s = __shfl_xor_sync(0xffffffffu, acc.s, o);
+    b.c = __shfl_xor_sync(0xffffffffu, acc.c, o);
+    dd_acc_merge(acc, b);
   }
-  if (lane == 0) {
-    const double v = dd_acc_to_double(t);
+  const int wid = threadIdx.x / 32;
+  if ((threadIdx.x & 31) == 0) {
+    red_s[wid] = acc.s;
+    red_c[wid] = acc.c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    DdAcc u = dd_acc(make_float2(red_s[0], red_c[0]));
+    for (int w = 1; w < kCorrectBlock / 32; ++w) {
+      DdAcc b;
+      b.s = red_s[w];
+      b.c = red_c[w];
+      dd_acc_merge(u, b);
+    }
+    const double v = dd_acc_to_double(u);
     y[s] = v;
     if (y_dd) y_dd[s] = dd_from(v);
   }
@@ -838,7 +827,7 @@ void launch_az_values(const CoarseDev &c, int n, const int32_t *prp,
 void launch_def_pre(const CoarseDev &c, int mode, const double *r, double *pv,
                     const double *v, const KScalars *sc, cudaStream_t st) {
   launch_pdl(k_def_pre, c.K, kCoarseBlock, 0, st, mode, c.sub_ptr, r, pv, v, sc, c.csum);
-  launch_pdl(k_coarse_y, (c.K + kCoarseYWarps - 1) / kCoarseYWarps, 32 * kCoarseYWarps, 0, st, c.K, (const float *)c.ac, (const float2 *)c.csum, c.y, (float2 *)nullptr, sc);
+  launch_pdl(k_coarse_y, c.K, kCorrectBlock, 0, st, c.K, (const float *)c.ac, (const float2 *)c.csum, c.y, (float2 *)nullptr, sc);
   count_launches(2);
 }
 
@@ -859,7 +848,7 @@ void launch_def_pre_dd(const CoarseDev &c, int mode, const float2 *r,
                        float2 *pv, const float2 *v, const KScalars *sc,
                        cudaStream_t st) {
   launch_pdl(k_def_pre_dd, c.K, kCoarseBlock, 0, st, mode, c.sub_ptr, r, pv, v, sc, c.csum);
-  launch_pdl(k_coarse_y, (c.K + kCoarseYWarps - 1) / kCoarseYWarps, 32 * kCoarseYWarps, 0, st, c.K, (const float *)c.ac, (const float2 *)c.csum, c.y, c.y_dd, sc);
+  launch_pdl(k_coarse_y, c.K, kCorrectBlock, 0, st, c.K, (const float *)c.ac, (const float2 *)c.csum, c.y, c.y_dd, sc);
   count_launches(2);
 }
 
