@@ -275,13 +275,31 @@ def az_nnz(eqn, part):
     return int(np.unique(rows[keep] * K + part[ci[keep]]).size)
 
 
-def kernel_roofline(pg, solver, n, nnz, dd, eqn=None, coarse=0):
-    """Per-launch CUDA-event times of the hot kernels of one solver on its
-    current system (pg_solver_profile) and the roofline of the dominant
-    one.  Compulsory bytes per launch: A values + int32 columns + row
-    pointers; ILU(0) factor values + 2-byte columns
-    (off-diagonal entries of A bound the factor's) + 1/u_ii; 8-byte vector
-    entries in both precisions."""
+def traced_solve(solver, eqn, x0):
+    """One solve of eqn from x0 with the kernel trace on: the device time
+    of each launch-group kind inside the solve (CUDA events on the library
+    stream between the groups; the chunks are launched directly)."""
+    solver.set_eqn(eqn)
+    solver.setGuess(x0)
+    solver.trace_kernels(True)
+    try:
+        solver.solve()
+        kt = solver.kernel_times()
+    finally:
+        solver.trace_kernels(False)
+    return {"iters": solver.nIters(), "kinds": kt}
+
+
+def kernel_roofline(pg, solver, n, nnz, dd, eqn=None, coarse=0, in_solve=None):
+    """Per-launch CUDA-event times of the hot kernels of one solver and the
+    roofline of the dominant one.  With in_solve (traced_solve's result)
+    the launch times are those inside a real solve, where the iteration's
+    working set (> 129 MB) does not stay in L2; the back-to-back times of
+    each kernel alone on its current system (pg_solver_profile, inputs
+    partly L2-resident) are kept beside them.  Compulsory bytes per launch:
+    A values + int32 columns + row pointers; ILU(0) factor values + 2-byte
+    columns (off-diagonal entries of A bound the factor's) + 1/u_ii; 8-byte
+    vector entries in both precisions."""
     import numpy as np
     prof = solver.profile(reps=50)
     part, K = solver.partition()
@@ -312,10 +330,35 @@ def kernel_roofline(pg, solver, n, nnz, dd, eqn=None, coarse=0):
         else:
             # additive: FP32 K x K inverse, K float-pair sums, z in/out
             bytes_of["coarse"] = 4 * K * K + 8 * K + 2 * 8 * n
+    iso_ms = dict(ms_of)
+    timing = "back-to-back launches of each kernel alone (pg_solver_profile)"
+    in_solve_out = None
+    if in_solve is not None:
+        kt = in_solve["kinds"]
+        key = {"spmv": "spmv", "ilu_apply": "sweep", "update": "update",
+               "coarse": "coarse"}
+        if all(kt[key[k]][1] > 0 for k in ms_of):
+            ms_of = {k: kt[key[k]][0] / kt[key[k]][1] for k in ms_of}
+            shares = {k: kt[key[k]][0] for k in ms_of}
+            timing = ("inside a solve: CUDA events between the launch groups "
+                      "of a traced solve of the same system")
+        total = sum(kt[key[k]][0] for k in key)
+        in_solve_out = {
+            "iterations": in_solve["iters"],
+            "kernel_ms": round(total, 4),
+            "kernel_us_per_iteration": round(1e3 * total / max(1, in_solve["iters"]), 2),
+            "per_kind_ms": {k: round(kt[key[k]][0], 4) for k in key},
+            "per_kind_launch_groups": {k: kt[key[k]][1] for k in key},
+            "dropped": kt["dropped"]}
     dom = max(shares, key=shares.get)
     peak, peak_kind = measured_peaks()
     achieved = bytes_of[dom] / (ms_of[dom] * 1e-3) / 1e9
     return {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
+            "timing": timing, "in_solve": in_solve_out,
+            "isolated_launch_ms": {k: round(v, 5) for k, v in iso_ms.items()},
+            "isolated_per_kernel_frac": {
+                k: round(bytes_of[k] / (iso_ms[k] * 1e-3) / 1e9 / peak, 4)
+                for k in bytes_of},
             "sweep_form": {1: "line", 0: "stream"}.get(form, "none"),
             "factor_weight_bytes": wb,
             "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
@@ -489,8 +532,15 @@ def run_sequence(args):
     sz.setGuess(None)
     sz.solve()
     zero = dict(sz.stats.as_dict())
-    roof_m = kernel_roofline(pg, sm, n, nnz, dd=True, eqn=eqn, coarse=args.coarse)
-    roof_p = kernel_roofline(pg, sp, n, nnz, dd=False, eqn=eqn, coarse=args.coarse)
+    # kernel time inside real solves (after the timed region): step t0 again
+    # from the step-(t0-1) solution, traced, by the float-float and the FP64
+    # solver
+    in_m = traced_solve(sm, eqn, x_prev_host)
+    in_p = traced_solve(sp, eqn, x_prev_host)
+    roof_m = kernel_roofline(pg, sm, n, nnz, dd=True, eqn=eqn,
+                             coarse=args.coarse, in_solve=in_m)
+    roof_p = kernel_roofline(pg, sp, n, nnz, dd=False, eqn=eqn,
+                             coarse=args.coarse, in_solve=in_p)
     # DRAM traffic needs a profiler, and no number of this line is taken
     # under one: the per-launch dram__bytes of the same kernels are in the
     # ncu summaries under profiles/
@@ -659,11 +709,12 @@ def cylinder_summary(pg, torch, args):
         out[name] = {"ms": round(float(np.mean(ms[1:])), 3),
                      "iters": its[1:], "converged": bool(ok),
                      "sweep_form": {1: "line", 0: "stream"}.get(s.sweep_form())}
-        if name == "fp64":
-            r = kernel_roofline(pg, s, eqn.n, int(eqn.nnz), dd=False, eqn=eqn,
-                                coarse=args.coarse)
-            out["fp64"]["per_kernel_frac"] = r["per_kernel_frac"]
-            out["fp64"]["per_kernel_ms"] = r["per_kernel_ms"]
+        r = kernel_roofline(pg, s, eqn.n, int(eqn.nnz), dd=prec == pg.MIXED,
+                            eqn=eqn, coarse=args.coarse,
+                            in_solve=traced_solve(s, eqn, None))
+        out[name]["per_kernel_frac"] = r["per_kernel_frac"]
+        out[name]["per_kernel_ms"] = r["per_kernel_ms"]
+        out[name]["isolated_per_kernel_frac"] = r["isolated_per_kernel_frac"]
     return out
 
 
@@ -1031,8 +1082,9 @@ def run_single(args):
     # of the hot kernels (FP64 ones, or the float-float ones of the mixed
     # solver; both move 8-byte values and vector entries)
     a_nnz = int(eqn.nnz)
+    in_solve = traced_solve(solver, eqn, None)
     roofline = kernel_roofline(pg, solver, n, a_nnz, dd=prec == pg.MIXED,
-                               eqn=eqn, coarse=args.coarse)
+                               eqn=eqn, coarse=args.coarse, in_solve=in_solve)
     roofline["traffic"] = None  # needs a profiler: see the ncu summaries
     iters = max(1, stats[-1]["iters"])
 

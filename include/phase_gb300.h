@@ -447,6 +447,26 @@ int pg_solver_get_x(const pg_solver *s, double *x, int ptr_kind);
  * reference counterpart: measurement.) */
 int pg_solver_profile(pg_solver *s, int reps, double *ms);
 
+/* Kernel time inside a solve (no reference counterpart: measurement).
+ * With on != 0 the BiCGStab solves that follow launch their iteration
+ * chunks directly instead of replaying CUDA graphs, with a CUDA event on
+ * the library stream after every launch group; pg_solver_kernel_times then
+ * returns, for the last such solve, the device time ms[k] (milliseconds)
+ * and the number count[k] of groups of each kind k below, and in *dropped
+ * (may be NULL) the groups left untimed when the event pool (65,536) ran
+ * out.  Intervals that span a host wait (chunk boundaries) are not booked.
+ * Synchronises the library stream. */
+#define PG_KT_SPMV 0   /* SpMV with its fused dot products */
+#define PG_KT_SWEEP 1  /* preconditioner sweep (ILU(k) or Jacobi) */
+#define PG_KT_UPDATE 2 /* x / r update with its fused dot products */
+#define PG_KT_COARSE 3 /* coarse correction: the deflation stage before the
+                          sweep (input sums, y = A_c^-1 Z^T p, p - A Z y), or
+                          the additive correction after it */
+#define PG_KT_N 4
+int pg_solver_trace_kernels(pg_solver *s, int on);
+int pg_solver_kernel_times(pg_solver *s, double *ms, int64_t *count,
+                           int64_t *dropped);
+
 /* ---------------------------------------------------------------------
  * Batched solves: many independent pressure systems of uneven sizes
  * (e.g. one per immersed-boundary case) solved together.  The reference

@@ -122,6 +122,8 @@ PROTOTYPES = {
     "pg_solver_coarse_inverse": (_I, [_P, _P, ctypes.POINTER(_I)]),
     "pg_solver_set_row_coords": (_I, [_P, _P]),
     "pg_solver_profile": (_I, [_P, _I, _P]),
+    "pg_solver_trace_kernels": (_I, [_P, _I]),
+    "pg_solver_kernel_times": (_I, [_P, _P, _P, _P]),
     "pg_solver_apply_precond": (_I, [_P, _P, _P, _I]),
     "pg_batch_create": (_I, [_P, ctypes.POINTER(_P)]),
     "pg_batch_destroy": (_I, [_P]),
@@ -607,6 +609,26 @@ class SparseMatrixSolver:
         return dict(spmv=ms[0], precond=ms[1], update=ms[2], factor=ms[3],
                     precond_dd=ms[4], spmv_dd=ms[5], update_dd=ms[6],
                     coarse=ms[7], coarse_inverse=ms[8])
+
+    KERNEL_KINDS = ("spmv", "sweep", "update", "coarse")
+
+    def trace_kernels(self, on: bool = True):
+        """Time the kernels inside the following solves (their iteration
+        chunks launched directly, a CUDA event after every launch group)."""
+        _check(lib().pg_solver_trace_kernels(self._h, 1 if on else 0))
+
+    def kernel_times(self):
+        """Device time inside the last traced solve, per launch-group kind:
+        {kind: (total ms, groups)}, plus "dropped" (groups left untimed)."""
+        ms = np.zeros(len(self.KERNEL_KINDS))
+        cnt = np.zeros(len(self.KERNEL_KINDS), np.int64)
+        dropped = np.zeros(1, np.int64)
+        _check(lib().pg_solver_kernel_times(self._h, _ptr(ms), _ptr(cnt),
+                                            _ptr(dropped)))
+        out = {k: (float(ms[i]), int(cnt[i]))
+               for i, k in enumerate(self.KERNEL_KINDS)}
+        out["dropped"] = int(dropped[0])
+        return out
 
     def printStatus(self, msg: str):
         print(f"{msg} iterations = {self.nIters()}, error = {self.error():f}.")

@@ -33,6 +33,7 @@ namespace pg {
 namespace {
 
 constexpr int kCoarseBlock = 128;
+constexpr int kDefRows = 4;  // rows per thread in flight in k_def_pre
 constexpr int kCorrectBlock = 256;
 constexpr int kGjB = 32;     // pivots per block of the Gauss-Jordan inversion
 
@@ -463,12 +464,27 @@ k_def_pre(int mode, const int32_t *__restrict__ sub_ptr,
   __shared__ double red[kCoarseBlock];
   const int s = blockIdx.x;
   double acc = 0.;
-  for (int32_t i = sub_ptr[s] + threadIdx.x; i < sub_ptr[s + 1]; i += kCoarseBlock) {
-    const double val = pre_combine<double>(mode, mode ? r[i] : 0.,
-                                           mode != 2 ? pv[i] : 0.,
-                                           mode ? v[i] : 0., sc);
-    if (mode) pv[i] = val;
-    acc += val;
+  const int32_t e = sub_ptr[s + 1];
+  for (int32_t i0 = sub_ptr[s] + threadIdx.x; i0 < e; i0 += kDefRows * kCoarseBlock) {
+    // the group's loads first, then the rows in order
+    double ri[kDefRows], pi[kDefRows], vi[kDefRows];
+#pragma unroll
+    for (int u = 0; u < kDefRows; ++u) {
+      const int32_t i = i0 + u * kCoarseBlock;
+      const bool in = i < e;
+      ri[u] = in && mode ? r[i] : 0.;
+      pi[u] = in && mode != 2 ? pv[i] : 0.;
+      vi[u] = in && mode ? v[i] : 0.;
+    }
+#pragma unroll
+    for (int u = 0; u < kDefRows; ++u) {
+      const int32_t i = i0 + u * kCoarseBlock;
+      if (i < e) {
+        const double val = pre_combine<double>(mode, ri[u], pi[u], vi[u], sc);
+        if (mode) pv[i] = val;
+        acc += val;
+      }
+    }
   }
   const double t = block_sum(acc, red);
   if (threadIdx.x == 0) csum[s] = dd_from(t);
@@ -555,12 +571,27 @@ k_def_pre_dd(int mode, const int32_t *__restrict__ sub_ptr,
   const int s = blockIdx.x;
   const float2 zero = make_float2(0.f, 0.f);
   DdAcc acc = dd_acc(zero);
-  for (int32_t i = sub_ptr[s] + threadIdx.x; i < sub_ptr[s + 1]; i += kCoarseBlock) {
-    const float2 val = dd_pre_combine(mode, mode ? r[i] : zero,
-                                      mode != 2 ? pv[i] : zero,
-                                      mode ? v[i] : zero, sc);
-    if (mode) pv[i] = val;
-    dd_acc_add(acc, val);
+  const int32_t e = sub_ptr[s + 1];
+  for (int32_t i0 = sub_ptr[s] + threadIdx.x; i0 < e; i0 += kDefRows * kCoarseBlock) {
+    // the group's loads first, then the rows in order
+    float2 ri[kDefRows], pi[kDefRows], vi[kDefRows];
+#pragma unroll
+    for (int u = 0; u < kDefRows; ++u) {
+      const int32_t i = i0 + u * kCoarseBlock;
+      const bool in = i < e;
+      ri[u] = in && mode ? r[i] : zero;
+      pi[u] = in && mode != 2 ? pv[i] : zero;
+      vi[u] = in && mode ? v[i] : zero;
+    }
+#pragma unroll
+    for (int u = 0; u < kDefRows; ++u) {
+      const int32_t i = i0 + u * kCoarseBlock;
+      if (i < e) {
+        const float2 val = dd_pre_combine(mode, ri[u], pi[u], vi[u], sc);
+        if (mode) pv[i] = val;
+        dd_acc_add(acc, val);
+      }
+    }
   }
   const double t = block_sum(dd_acc_to_double(acc), red);
   if (threadIdx.x == 0) csum[s] = dd_from(t);

@@ -238,10 +238,12 @@ struct SolverDev {
   int n, nnz, n_sub;
   // permuted CSR
   const int32_t *prp, *pci;
-  // its sliced ELLPACK copy for the FP64 SpMVs (sell_val refreshed with the
-  // values; NULL: the CSR is used)
+  // its sliced ELLPACK copy for the SpMVs (32-row slices, column-major;
+  // sell_val refreshed with the values, sell_val_dd their float pairs for
+  // the mixed solver; NULL: the CSR is used)
   const int32_t *sell_ptr = nullptr, *sell_col = nullptr;
   const double *sell_val = nullptr;
+  const float2 *sell_val_dd = nullptr;
   // ILU(0) records (FP64)
   const SubMeta *meta64;
   uint8_t *rec64;

@@ -58,6 +58,7 @@ struct pg_solver {
   // sliced ELLPACK copy of the matrix for the FP64 SpMVs (PG_FP64 solvers)
   DevBuf<int32_t> sell_ptr, sell_col, sell_src;
   DevBuf<double> sell_val;
+  DevBuf<float2> sell_val_dd;  // PG_MIXED: float pairs of sell_val
   bool sell_on = false;
   DevBuf<SubMeta> meta64;
   DevBuf<uint8_t> rec64;
@@ -115,6 +116,16 @@ struct pg_solver {
   // [4], [5] as [0], [1] with the second coarse-inverse buffer
   cudaGraphExec_t chunk_graph[6] = {};
   int chunk_launches[6] = {};  // kernels in one replay of each graph
+  // pg_solver_trace_kernels: an event after every launch group of the
+  // Krylov loop (chunks launched directly, not replayed), each interval
+  // booked to the kind of the group that ends it
+  struct KernelTrace {
+    bool on = false;
+    std::vector<cudaEvent_t> ev;
+    std::vector<int8_t> kind;
+    size_t used = 0;
+    int64_t dropped = 0;
+  } kt;
   // two-level Schwarz coarse space (cfg.coarse): structure, the dense
   // coarse matrix / its inverse, elimination buffers, subdomain sums and the
   // graph of the K elimination steps
@@ -221,6 +232,7 @@ struct pg_solver {
     if (diff_host) cudaFreeHost(diff_host);
     for (auto &e : ev)
       if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : kt.ev) cudaEventDestroy(e);
   }
 
   SolverDev dev() const {
@@ -234,6 +246,7 @@ struct pg_solver {
       d.sell_ptr = sell_ptr.p;
       d.sell_col = sell_col.p;
       d.sell_val = sell_val.p;
+      d.sell_val_dd = sell_val_dd.p;
     }
     d.meta64 = meta64.p;
     d.rec64 = rec64.p;
@@ -343,13 +356,15 @@ int upload_analysis(pg_solver *s) {
   up(s->perm, a.perm);
   up(s->prp, a.prp);
   up(s->pci, a.pci);
-  s->sell_on = s->cfg.precision == PG_FP64 && !s->batch_mode &&
-               !a.sell_ptr.empty();
+  s->sell_on = (s->cfg.precision == PG_FP64 || s->cfg.precision == PG_MIXED) &&
+               !s->batch_mode && !a.sell_ptr.empty();
   if (s->sell_on) {
     up(s->sell_ptr, a.sell_ptr);
     up(s->sell_col, a.sell_col);
     up(s->sell_src, a.sell_src);
     if (e == cudaSuccess) e = s->sell_val.reserve(a.sell_col.size());
+    if (e == cudaSuccess && s->cfg.precision == PG_MIXED)
+      e = s->sell_val_dd.reserve(a.sell_col.size());
   }
   up(s->psrc, a.psrc);
   up(s->dup_dst, a.dup_dst);
@@ -525,12 +540,46 @@ bool trace_enabled() {
   return on != 0;
 }
 
-// Replays the captured chunk graph (capturing it on the second call).
+// Kernel trace (pg_solver_trace_kernels): records an event on st that
+// ends an interval of the given kind (PG_KT_*; -1 opens a new run of
+// intervals after a host wait).  Events come from a pool that grows by 256
+// up to kKtMaxEvents; past that the rest of the solve is not timed.
+constexpr size_t kKtMaxEvents = 1 << 16;
+void kt_mark(pg_solver *s, int kind, cudaStream_t st) {
+  auto &t = s->kt;
+  if (!t.on) return;
+  if (t.dropped) {
+    ++t.dropped;
+    return;
+  }
+  if (t.used == t.ev.size()) {
+    for (int i = 0; i < 256 && t.ev.size() < kKtMaxEvents; ++i) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) break;
+      t.ev.push_back(e);
+      t.kind.push_back(-1);
+    }
+    if (t.used == t.ev.size()) {
+      ++t.dropped;
+      return;
+    }
+  }
+  if (cudaEventRecord(t.ev[t.used], st) != cudaSuccess) {
+    ++t.dropped;
+    return;
+  }
+  t.kind[t.used++] = (int8_t)kind;
+}
+
+// Replays the captured chunk graph (capturing it on the second call); with
+// the kernel trace on, every chunk is launched directly.
 template <class F>
 int run_chunk(cudaGraphExec_t &gexec, int &n_launch, bool &direct_done,
-              F &&chunk) {
+              F &&chunk, bool direct = false) {
   cudaStream_t st = stream();
-  if (gexec) {
+  if (direct) {
+    chunk();
+  } else if (gexec) {
     PG_CUDA(cudaGraphLaunch(gexec, st));
     count_launches(n_launch);
   } else if (direct_done) {
@@ -586,27 +635,40 @@ int run_bicgstab(pg_solver *s, double tol, int max_iters, int *iters,
       // sweep adds y as it writes z
       launch_def_pre(cdev, mode, r, pv, v, s->sc.p, st);
       launch_def_in(cdev, d.n, pv, cdev.tmp, s->sc.p, st);
+      kt_mark(s, PG_KT_COARSE, st);
       if (s->cfg.precond == PG_PREC_ILU0 &&
-          launch_ilu0_apply_def(d3, cdev.tmp, z, s->sc.p, st))
+          launch_ilu0_apply_def(d3, cdev.tmp, z, s->sc.p, st)) {
+        kt_mark(s, PG_KT_SWEEP, st);
         return;
+      }
       launch_precond<double, double>(s->cfg.precond, 0, d0, jd, r, cdev.tmp,
                                      v, z, s->sc.p, st);
+      kt_mark(s, PG_KT_SWEEP, st);
       launch_coarse_add(cdev, z, s->sc.p, st);
+      kt_mark(s, PG_KT_COARSE, st);
       return;
     }
     launch_precond<double, double>(s->cfg.precond, mode, d, jd, r, pv, v, z,
                                    s->sc.p, st);
+    kt_mark(s, PG_KT_SWEEP, st);
     // the input (p or s) is in pv after the fused update; the streamed
     // ILU(0) sweep has summed it per subdomain already
-    if (cdev.K) launch_coarse_apply(cdev, pv, z, ilu_stream, s->sc.p, st);
+    if (cdev.K) {
+      launch_coarse_apply(cdev, pv, z, ilu_stream, s->sc.p, st);
+      kt_mark(s, PG_KT_COARSE, st);
+    }
   };
   auto chunk = [&]() {
+    kt_mark(s, -1, st);
     for (int c = 0; c < kChunk; ++c) {
       precond(1, p, ph);
       launch_spmv_v<double, double>(d, val, ph, v, rh, s->sc.p, w, st);
+      kt_mark(s, PG_KT_SPMV, st);
       precond(2, ss, sh);
       launch_spmv_t<double, double>(d, val, sh, t, ss, s->sc.p, w, st);
+      kt_mark(s, PG_KT_SPMV, st);
       launch_update<double>(d.n, x, r, ph, sh, ss, t, rh, s->sc.p, w, st);
+      kt_mark(s, PG_KT_UPDATE, st);
     }
   };
   auto read_scalars = [&]() -> int {
@@ -650,7 +712,9 @@ int run_bicgstab(pg_solver *s, double tol, int max_iters, int *iters,
   cudaGraphExec_t &gexec = s->chunk_graph[slot];
   bool direct_done = false;
   for (;;) {
-    if ((rc = run_chunk(gexec, s->chunk_launches[slot], direct_done, chunk))) return rc;
+    if ((rc = run_chunk(gexec, s->chunk_launches[slot], direct_done, chunk,
+                        s->kt.on)))
+      return rc;
     if ((rc = read_scalars())) return rc;
     const KScalars k = *s->sc_host;
     *iters = k.iter;
@@ -712,28 +776,41 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
       // A-DEF1 in float-float
       launch_def_pre_dd(cdev, mode, r, pv, v, s->sc.p, st);
       launch_def_in_dd(cdev, n, pv, cdev.tmp_dd, s->sc.p, st);
-      if (ilu && launch_ilu0_apply_def_dd(d3, cdev.tmp_dd, z, s->sc.p, st))
+      kt_mark(s, PG_KT_COARSE, st);
+      if (ilu && launch_ilu0_apply_def_dd(d3, cdev.tmp_dd, z, s->sc.p, st)) {
+        kt_mark(s, PG_KT_SWEEP, st);
         return;
+      }
       if (ilu)
         launch_ilu0_apply_dd(0, d0, r, cdev.tmp_dd, v, z, s->sc.p, st);
       else
         launch_dd_diag_apply(0, n, jd, r, cdev.tmp_dd, v, z, s->sc.p, st);
+      kt_mark(s, PG_KT_SWEEP, st);
       launch_coarse_add_dd(cdev, z, s->sc.p, st);
+      kt_mark(s, PG_KT_COARSE, st);
       return;
     }
     if (ilu)
       launch_ilu0_apply_dd(mode, d, r, pv, v, z, s->sc.p, st);
     else
       launch_dd_diag_apply(mode, n, jd, r, pv, v, z, s->sc.p, st);
-    if (cdev.K) launch_coarse_apply_dd(cdev, pv, z, ilu && d.dd_stream, s->sc.p, st);
+    kt_mark(s, PG_KT_SWEEP, st);
+    if (cdev.K) {
+      launch_coarse_apply_dd(cdev, pv, z, ilu && d.dd_stream, s->sc.p, st);
+      kt_mark(s, PG_KT_COARSE, st);
+    }
   };
   auto chunk = [&]() {
+    kt_mark(s, -1, st);
     for (int c = 0; c < kChunk; ++c) {
       precond(1, p, ph);
       launch_dd_spmv_v(d, val, ph, v, rh, s->sc.p, w, st);
+      kt_mark(s, PG_KT_SPMV, st);
       precond(2, ss, sh);
       launch_dd_spmv_t(d, val, sh, t, ss, s->sc.p, w, st);
+      kt_mark(s, PG_KT_SPMV, st);
       launch_dd_update(n, x, r, ph, sh, ss, t, rh, s->sc.p, w, st);
+      kt_mark(s, PG_KT_UPDATE, st);
     }
   };
   auto read_scalars = [&]() -> int {
@@ -783,7 +860,7 @@ int run_bicgstab_dd(pg_solver *s, double tol, int max_iters, int *iters,
   for (;;) {
     const int slot = cdev.K ? (s->ac_ready ? 5 : 1) : 3;
     if ((rc = run_chunk(s->chunk_graph[slot], s->chunk_launches[slot],
-                        direct_done, chunk)))
+                        direct_done, chunk, s->kt.on)))
       return rc;
     if ((rc = read_scalars())) return rc;
     const KScalars k = *s->sc_host;
@@ -1208,6 +1285,9 @@ int factor(pg_solver *s, cudaStream_t st) {
     if (dd) launch_dd_split(d.n, s->jdinv.p, 1.0, s->jdinv_dd.p, st);
   }
   if (dd) launch_dd_split(d.nnz, s->pvals.p, 1.0, s->pvals_dd.p, st);
+  if (dd && s->sell_on && s->sell_val_dd.p)
+    launch_dd_split((int64_t)s->a.sell_col.size(), s->sell_val.p, 1.0,
+                    s->sell_val_dd.p, st);
   PG_CUDA(cudaGetLastError());
   if (dd && s->cfg.precond == PG_PREC_ILU0 && s->dd_stream < 0)
     return choose_dd_sweep(s);  // library stream only (see start_factor)
@@ -1518,6 +1598,8 @@ extern "C" int pg_solver_solve(pg_solver *s, pg_solve_stats *stats) {
                "pg_solver_solve: matrix and rhs must be set first");
   cudaStream_t st = stream();
   const int64_t n = s->a.n;
+  s->kt.used = 0;
+  s->kt.dropped = 0;
   if (!s->have_x) PG_CUDA(cudaMemsetAsync(s->x.p, 0, n * sizeof(double), st));
   PG_CUDA(cudaEventRecord(s->ev[0], st));
   // the factorisation started at the hand-over, or now (unless the values
@@ -1639,6 +1721,35 @@ extern "C" int pg_solver_get_x(const pg_solver *s, double *x, int ptr_kind) {
 }
 
 extern "C" uint64_t pg_kernel_launches(void) { return launch_count(); }
+
+extern "C" int pg_solver_trace_kernels(pg_solver *s, int on) {
+  PG_CHECK_ARG(s, "pg_solver_trace_kernels: NULL solver");
+  s->kt.on = on != 0;
+  s->kt.used = 0;
+  s->kt.dropped = 0;
+  return PG_OK;
+}
+
+extern "C" int pg_solver_kernel_times(pg_solver *s, double *ms, int64_t *count,
+                                      int64_t *dropped) {
+  PG_CHECK_ARG(s && ms && count, "pg_solver_kernel_times: bad argument");
+  PG_CUDA(cudaStreamSynchronize(stream()));
+  for (int k = 0; k < PG_KT_N; ++k) {
+    ms[k] = 0.;
+    count[k] = 0;
+  }
+  const auto &t = s->kt;
+  for (size_t i = 1; i < t.used; ++i) {
+    const int k = t.kind[i];
+    if (k < 0 || k >= PG_KT_N) continue;
+    float f = 0.f;
+    PG_CUDA(cudaEventElapsedTime(&f, t.ev[i - 1], t.ev[i]));
+    ms[k] += f;
+    ++count[k];
+  }
+  if (dropped) *dropped = t.dropped;
+  return PG_OK;
+}
 
 extern "C" int pg_solver_profile(pg_solver *s, int reps, double *ms) {
   PG_CHECK_ARG(s && ms && reps > 0, "pg_solver_profile: bad argument");
