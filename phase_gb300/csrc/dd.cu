@@ -15,6 +15,7 @@
 #include "../../include/phase_gb300.h"
 #include "dd.cuh"
 #include "kernels.cuh"
+#include "tma.cuh"
 
 namespace pg {
 
@@ -85,6 +86,54 @@ __device__ bool grid_reduce_dd(DdAcc (&v)[ND], const RedWork &w,
 }
 
 __device__ __forceinline__ bool finite_d(double v) { return isfinite(v); }
+
+// The BiCGStab recurrences of the float-float kernels (last block,
+// thread 0): after the x / r update (tot = {<rhat, r>, <r, r>}), after
+// v = A phat (alpha from <rhat, v>), after t = A shat (omega)
+__device__ __forceinline__ void dd_update_scalars(KScalars *sc, const double (&tot)[2]) {
+  const double rho_new = tot[0], alv = sc->alpha, omv = sc->omega;
+  sc->rr = tot[1];
+  sc->iter += 1;
+  if (!finite_d(tot[0]) || !finite_d(tot[1])) {
+    sc->status = PG_NON_FINITE;
+    sc->done = 1;
+  } else {
+    if (omv != 0. && sc->rho != 0.)
+      sc->beta = (rho_new / sc->rho) * (alv / omv);
+    sc->beta_dd = dd_from(sc->beta);
+    sc->rho_prev = sc->rho;
+    sc->rho = rho_new;
+    if (tot[1] <= sc->tol2 * sc->bb) {
+      sc->status = PG_OK;
+      sc->done = 1;
+    } else if (sc->iter >= sc->max_iter) {
+      sc->status = PG_MAX_ITERS;
+      sc->done = 1;
+    } else if (rho_new == 0. || omv == 0.) {
+      sc->status = PG_BREAKDOWN;
+      sc->done = 1;
+    }
+  }
+}
+__device__ __forceinline__ void dd_spmv_v_scalars(KScalars *sc, double rv) {
+  sc->rv = rv;
+  if (!finite_d(rv)) {
+    sc->status = PG_NON_FINITE;
+    sc->done = 1;
+  } else if (rv == 0.) {
+    sc->status = PG_BREAKDOWN;
+    sc->done = 1;
+  } else {
+    sc->alpha = sc->rho / rv;
+    sc->alpha_dd = dd_from(sc->alpha);
+  }
+}
+__device__ __forceinline__ void dd_spmv_t_scalars(KScalars *sc, const double (&tot)[2]) {
+  sc->tt = tot[0];
+  sc->ts = tot[1];
+  sc->omega = tot[0] > 0. ? tot[1] / tot[0] : 0.;
+  sc->omega_dd = dd_from(sc->omega);
+}
 
 __device__ __forceinline__ float2 row_dot_dd(const int32_t *__restrict__ rp,
                                              const int32_t *__restrict__ ci,
@@ -185,19 +234,7 @@ k_dd_spmv_v(SolverDev d, const float2 *__restrict__ val,
     dd_acc_fma(acc[0], rh[i], vi);
   }
   double tot[1];
-  if (grid_reduce_dd<1>(acc, w, tot) && threadIdx.x == 0) {
-    sc->rv = tot[0];
-    if (!finite_d(tot[0])) {
-      sc->status = PG_NON_FINITE;
-      sc->done = 1;
-    } else if (tot[0] == 0.) {
-      sc->status = PG_BREAKDOWN;
-      sc->done = 1;
-    } else {
-      sc->alpha = sc->rho / tot[0];
-      sc->alpha_dd = dd_from(sc->alpha);
-    }
-  }
+  if (grid_reduce_dd<1>(acc, w, tot) && threadIdx.x == 0) dd_spmv_v_scalars(sc, tot[0]);
 }
 
 __global__ void __launch_bounds__(kVecBlock)
@@ -215,12 +252,7 @@ k_dd_spmv_t(SolverDev d, const float2 *__restrict__ val,
     dd_acc_fma(acc[1], ti, s[i]);
   }
   double tot[2];
-  if (grid_reduce_dd<2>(acc, w, tot) && threadIdx.x == 0) {
-    sc->tt = tot[0];
-    sc->ts = tot[1];
-    sc->omega = tot[0] > 0. ? tot[1] / tot[0] : 0.;
-    sc->omega_dd = dd_from(sc->omega);
-  }
+  if (grid_reduce_dd<2>(acc, w, tot) && threadIdx.x == 0) dd_spmv_t_scalars(sc, tot);
 }
 
 __global__ void __launch_bounds__(kVecBlock)
@@ -241,31 +273,83 @@ k_dd_update(int n, float2 *__restrict__ x, float2 *__restrict__ r,
     dd_acc_fma(acc[1], ri, ri);
   }
   double tot[2];
-  if (grid_reduce_dd<2>(acc, w, tot) && threadIdx.x == 0) {
-    const double rho_new = tot[0], alv = sc->alpha, omv = sc->omega;
-    sc->rr = tot[1];
-    sc->iter += 1;
-    if (!finite_d(tot[0]) || !finite_d(tot[1])) {
-      sc->status = PG_NON_FINITE;
-      sc->done = 1;
-    } else {
-      if (omv != 0. && sc->rho != 0.)
-        sc->beta = (rho_new / sc->rho) * (alv / omv);
-      sc->beta_dd = dd_from(sc->beta);
-      sc->rho_prev = sc->rho;
-      sc->rho = rho_new;
-      if (tot[1] <= sc->tol2 * sc->bb) {
-        sc->status = PG_OK;
-        sc->done = 1;
-      } else if (sc->iter >= sc->max_iter) {
-        sc->status = PG_MAX_ITERS;
-        sc->done = 1;
-      } else if (rho_new == 0. || omv == 0.) {
-        sc->status = PG_BREAKDOWN;
-        sc->done = 1;
+  if (grid_reduce_dd<2>(acc, w, tot) && threadIdx.x == 0) dd_update_scalars(sc, tot);
+}
+
+// ---- streamed x / r update (bulk copies through shared memory, tma.cuh;
+// the same per-element arithmetic as k_dd_update, each thread's sums in its
+// tiles' order).  The SpMVs stay thread-per-row: their x gathers, not the
+// matrix stream, set their time, and a tile ring's CTAs hide them worse. ----
+constexpr int kUpdStages = 4;   // tiles in flight per CTA, x / r update
+
+__global__ void __launch_bounds__(kTileN)
+k_dd_update_tma(int n, float2 *__restrict__ x, float2 *__restrict__ r,
+                const float2 *__restrict__ ph, const float2 *__restrict__ sh,
+                const float2 *__restrict__ s, const float2 *__restrict__ t,
+                const float2 *__restrict__ rh, KScalars *sc, RedWork w) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  __shared__ __align__(8) uint64_t bar[kUpdStages];
+  pdl_wait();
+  if (sc->done) return;
+  const float2 al = sc->alpha_dd, om = sc->omega_dd;
+  const int tid = threadIdx.x, G = gridDim.x, blk = blockIdx.x;
+  const int n_tiles = (n + kTileN - 1) / kTileN;
+  const int m = blk < n_tiles ? (n_tiles - 1 - blk) / G + 1 : 0;
+  constexpr int kStage = 6 * kTileN * 8;
+  const void *const src[6] = {x, ph, sh, s, t, rh};
+  if (tid == 0) {
+    for (int b = 0; b < kUpdStages; ++b) mbar_init(&bar[b], 1);
+    for (int k = 0; k < kUpdStages && k < m; ++k)
+      issue_vec_tile<6>(smem + k * kStage, src, n, blk + k * G, &bar[k]);
+  }
+  __syncthreads();
+  DdAcc acc[2] = {{0.f, 0.f}, {0.f, 0.f}};
+  int k = 0;
+  bool failed = false;
+  for (; k < m; ++k) {
+    const int b = k % kUpdStages;
+    const bool ok = mbar_wait_bounded(&bar[b], w.err, (uint32_t)((k / kUpdStages) & 1));
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    const int j = blk + k * G;
+    const int i = j * kTileN + tid;
+    if (i < n) {
+      const float2 *stg = reinterpret_cast<const float2 *>(smem + b * kStage);
+      float2 xv, pv, shv, sv, tv, rhv;
+      if (tid < tile_bulk_count(n, j)) {
+        xv = stg[tid];
+        pv = stg[kTileN + tid];
+        shv = stg[2 * kTileN + tid];
+        sv = stg[3 * kTileN + tid];
+        tv = stg[4 * kTileN + tid];
+        rhv = stg[5 * kTileN + tid];
+      } else {
+        xv = x[i];
+        pv = ph[i];
+        shv = sh[i];
+        sv = s[i];
+        tv = t[i];
+        rhv = rh[i];
       }
+      x[i] = dd_add(xv, dd_add(dd_mul(al, pv), dd_mul(om, shv)));
+      const float2 ri = dd_sub(sv, dd_mul(om, tv));
+      r[i] = ri;
+      dd_acc_fma(acc[0], rhv, ri);
+      dd_acc_fma(acc[1], ri, ri);
+    }
+    __syncthreads();  // stage b is free
+    if (tid == 0 && k + kUpdStages < m) {
+      fence_proxy_async();
+      issue_vec_tile<6>(smem + b * kStage, src, n, blk + (k + kUpdStages) * G, &bar[b]);
     }
   }
+  if (failed && tid == 0)  // the copies still in flight, before leaving
+    for (int k2 = k + 1; k2 < m && k2 < k + kUpdStages; ++k2)
+      mbar_wait_bounded(&bar[k2 % kUpdStages], nullptr, (uint32_t)((k2 / kUpdStages) & 1));
+  double tot[2];
+  if (grid_reduce_dd<2>(acc, w, tot) && threadIdx.x == 0) dd_update_scalars(sc, tot);
 }
 
 template <int MODE>
@@ -333,6 +417,22 @@ void launch_dd_update(int n, float2 *x, float2 *r, const float2 *ph,
                       const float2 *sh, const float2 *s, const float2 *t,
                       const float2 *rh, KScalars *sc, RedWork w,
                       cudaStream_t st) {
+  if (stream_enabled() && n > 0 && aligned16(x) && aligned16(r) &&
+      aligned16(ph) && aligned16(sh) && aligned16(s) && aligned16(t) &&
+      aligned16(rh)) {
+    constexpr size_t smem = kUpdStages * 6 * kTileN * 8;
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_dd_update_tma,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      attr = true;
+    }
+    const int g = stream_grid((const void *)k_dd_update_tma, smem,
+                              (n + kTileN - 1) / kTileN, w.grid);
+    launch_pdl(k_dd_update_tma, g, kTileN, smem, st, n, x, r, ph, sh, s, t, rh, sc, w);
+    count_launches(1);
+    return;
+  }
   launch_pdl(k_dd_update, w.grid, kVecBlock, 0, st, n, x, r, ph, sh, s, t, rh, sc, w);
   count_launches(1);
 }

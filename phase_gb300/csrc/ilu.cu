@@ -22,63 +22,11 @@
 #include "../../include/phase_gb300.h"
 #include "dd.cuh"
 #include "kernels.cuh"
+#include "tma.cuh"
 
 namespace pg {
 
 namespace {
-
-// ---- TMA / mbarrier helpers (sm_90+ PTX) ----
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(count)
-               : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
-                   smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void bulk_load(void *dst, const void *src,
-                                          uint32_t bytes, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
-      "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], "
-      "%2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-constexpr int kWaitLimit = 1 << 22;  // try_wait polls before giving up
-
-// Bounded wait on a single-use barrier.  On expiry the error flag is set and
-// the copy still in flight is waited for once more (bounded) so the CTA does
-// not exit under it.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, int *err,
-                                                  uint32_t parity = 0) {
-  for (int it = 0; it < kWaitLimit; ++it)
-    if (mbar_try_wait(bar, parity)) return true;
-  if (err) atomicExch(err, 1);
-  for (int it = 0; it < kWaitLimit; ++it)
-    if (mbar_try_wait(bar, parity)) break;
-  return false;
-}
-__device__ __forceinline__ void fence_proxy_async() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-__device__ __forceinline__ int al16(int b) { return (b + 15) & ~15; }
 
 // Row-wise IKJ ILU(0) (Saad, Iterative Methods for Sparse Linear Systems,
 // Alg. 10.4) on the diagonal block of one subdomain, in its record.  The CTA

@@ -22,6 +22,7 @@
 #include <type_traits>
 
 #include "kernels.cuh"
+#include "tma.cuh"
 
 namespace pg {
 
@@ -454,6 +455,54 @@ __device__ __forceinline__ VT row_dot_any(const SolverDev &d,
   return row_dot<VT, MT>(d.prp, d.pci, val, x, i);
 }
 
+// The BiCGStab recurrence after the x / r update (last block, thread 0):
+// tot = {<rhat, r>, <r, r>}
+__device__ __forceinline__ void update_scalars(KScalars *sc, const double (&tot)[2],
+                                               double al, double om) {
+  const double rho_new = tot[0];
+  sc->rr = tot[1];
+  sc->iter += 1;
+  if (!finite(tot[0]) || !finite(tot[1])) {
+    sc->status = PG_NON_FINITE;
+    sc->done = 1;
+  } else {
+    // rho_prev/rho advance on every exit, so a residual replacement after
+    // a stop can continue the recurrence
+    if (om != 0. && sc->rho != 0.) sc->beta = (rho_new / sc->rho) * (al / om);
+    sc->rho_prev = sc->rho;
+    sc->rho = rho_new;
+    if (tot[1] <= sc->tol2 * sc->bb) {
+      sc->status = PG_OK;
+      sc->done = 1;
+    } else if (sc->iter >= sc->max_iter) {
+      sc->status = PG_MAX_ITERS;
+      sc->done = 1;
+    } else if (rho_new == 0. || om == 0.) {
+      sc->status = PG_BREAKDOWN;
+      sc->done = 1;
+    }
+  }
+}
+// ... after the SpMV v = A phat: alpha from <rhat, v>
+__device__ __forceinline__ void spmv_v_scalars(KScalars *sc, double rv) {
+  sc->rv = rv;
+  if (!finite(rv)) {
+    sc->status = PG_NON_FINITE;
+    sc->done = 1;
+  } else if (rv == 0.) {
+    sc->status = PG_BREAKDOWN;
+    sc->done = 1;
+  } else {
+    sc->alpha = sc->rho / rv;
+  }
+}
+// ... after the SpMV t = A shat: omega from <t, t> and <t, s>
+__device__ __forceinline__ void spmv_t_scalars(KScalars *sc, const double (&tot)[2]) {
+  sc->tt = tot[0];
+  sc->ts = tot[1];
+  sc->omega = tot[0] > 0. ? tot[1] / tot[0] : 0.;
+}
+
 template <class VT, class MT>
 __global__ void __launch_bounds__(kVecBlock)
 k_spmv_v(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ ph,
@@ -469,18 +518,7 @@ k_spmv_v(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ ph,
     acc[0] += (double)rh[i] * (double)vi;
   }
   double tot[1];
-  if (grid_reduce<1>(acc, w, tot) && threadIdx.x == 0) {
-    sc->rv = tot[0];
-    if (!finite(tot[0])) {
-      sc->status = PG_NON_FINITE;
-      sc->done = 1;
-    } else if (tot[0] == 0.) {
-      sc->status = PG_BREAKDOWN;
-      sc->done = 1;
-    } else {
-      sc->alpha = sc->rho / tot[0];
-    }
-  }
+  if (grid_reduce<1>(acc, w, tot) && threadIdx.x == 0) spmv_v_scalars(sc, tot[0]);
 }
 
 template <class VT, class MT>
@@ -499,11 +537,7 @@ k_spmv_t(SolverDev d, const MT *__restrict__ val, const VT *__restrict__ sh,
     acc[1] += (double)ti * (double)s[i];
   }
   double tot[2];
-  if (grid_reduce<2>(acc, w, tot) && threadIdx.x == 0) {
-    sc->tt = tot[0];
-    sc->ts = tot[1];
-    sc->omega = tot[0] > 0. ? tot[1] / tot[0] : 0.;
-  }
+  if (grid_reduce<2>(acc, w, tot) && threadIdx.x == 0) spmv_t_scalars(sc, tot);
 }
 
 template <class VT>
@@ -526,30 +560,200 @@ k_update(int n, VT *__restrict__ x, VT *__restrict__ r,
     acc[1] += (double)ri * (double)ri;
   }
   double tot[2];
-  if (grid_reduce<2>(acc, w, tot) && threadIdx.x == 0) {
-    const double rho_new = tot[0];
-    sc->rr = tot[1];
-    sc->iter += 1;
-    if (!finite(tot[0]) || !finite(tot[1])) {
-      sc->status = PG_NON_FINITE;
-      sc->done = 1;
-    } else {
-      // rho_prev/rho advance on every exit, so a residual replacement after
-      // a stop can continue the recurrence
-      if (om != 0. && sc->rho != 0.) sc->beta = (rho_new / sc->rho) * (al / om);
-      sc->rho_prev = sc->rho;
-      sc->rho = rho_new;
-      if (tot[1] <= sc->tol2 * sc->bb) {
-        sc->status = PG_OK;
-        sc->done = 1;
-      } else if (sc->iter >= sc->max_iter) {
-        sc->status = PG_MAX_ITERS;
-        sc->done = 1;
-      } else if (rho_new == 0. || om == 0.) {
-        sc->status = PG_BREAKDOWN;
-        sc->done = 1;
+  if (grid_reduce<2>(acc, w, tot) && threadIdx.x == 0)
+    update_scalars(sc, tot, al, om);
+}
+
+// ---- streamed forms (the vectors and matrix tiles move through shared
+// memory by bulk copies, tma.cuh; the same sums as the kernels above, each
+// thread's in its tiles' order) ----
+constexpr int kUpdStages = 4;   // tiles in flight per CTA, x / r update
+constexpr int kSpmvStages = 3;  // tiles in flight per CTA, SpMV
+constexpr int kSellMaxW = 16;   // widest slice the streamed SpMV takes
+
+// x += alpha phat + omega shat; r = s - omega t; <rhat, r>, <r, r>
+__global__ void __launch_bounds__(kTileN)
+k_update_tma(int n, double *__restrict__ x, double *__restrict__ r,
+             const double *__restrict__ ph, const double *__restrict__ sh,
+             const double *__restrict__ s, const double *__restrict__ t,
+             const double *__restrict__ rh, KScalars *sc, RedWork w) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  __shared__ __align__(8) uint64_t bar[kUpdStages];
+  pdl_wait();
+  if (sc->done) return;
+  const double al = sc->alpha, om = sc->omega;
+  const int tid = threadIdx.x, G = gridDim.x, blk = blockIdx.x;
+  const int n_tiles = (n + kTileN - 1) / kTileN;
+  const int m = blk < n_tiles ? (n_tiles - 1 - blk) / G + 1 : 0;
+  constexpr int kStage = 6 * kTileN * 8;
+  const void *const src[6] = {x, ph, sh, s, t, rh};
+  if (tid == 0) {
+    for (int b = 0; b < kUpdStages; ++b) mbar_init(&bar[b], 1);
+    for (int k = 0; k < kUpdStages && k < m; ++k)
+      issue_vec_tile<6>(smem + k * kStage, src, n, blk + k * G, &bar[k]);
+  }
+  __syncthreads();
+  double acc[2] = {0., 0.};
+  int k = 0;
+  bool failed = false;
+  for (; k < m; ++k) {
+    const int b = k % kUpdStages;
+    const bool ok = mbar_wait_bounded(&bar[b], w.err, (uint32_t)((k / kUpdStages) & 1));
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    const int j = blk + k * G;
+    const int i = j * kTileN + tid;
+    if (i < n) {
+      const double *stg = reinterpret_cast<const double *>(smem + b * kStage);
+      double xv, pv, shv, sv, tv, rhv;
+      if (tid < tile_bulk_count(n, j)) {
+        xv = stg[tid];
+        pv = stg[kTileN + tid];
+        shv = stg[2 * kTileN + tid];
+        sv = stg[3 * kTileN + tid];
+        tv = stg[4 * kTileN + tid];
+        rhv = stg[5 * kTileN + tid];
+      } else {
+        xv = x[i];
+        pv = ph[i];
+        shv = sh[i];
+        sv = s[i];
+        tv = t[i];
+        rhv = rh[i];
+      }
+      x[i] = xv + al * pv + om * shv;
+      const double ri = sv - om * tv;
+      r[i] = ri;
+      acc[0] += rhv * ri;
+      acc[1] += ri * ri;
+    }
+    __syncthreads();  // stage b is free
+    if (tid == 0 && k + kUpdStages < m) {
+      fence_proxy_async();
+      issue_vec_tile<6>(smem + b * kStage, src, n, blk + (k + kUpdStages) * G, &bar[b]);
+    }
+  }
+  if (failed && tid == 0)  // the copies still in flight, before leaving
+    for (int k2 = k + 1; k2 < m && k2 < k + kUpdStages; ++k2)
+      mbar_wait_bounded(&bar[k2 % kUpdStages], nullptr, (uint32_t)((k2 / kUpdStages) & 1));
+  double tot[2];
+  if (grid_reduce<2>(acc, w, tot) && threadIdx.x == 0)
+    update_scalars(sc, tot, al, om);
+}
+
+// SpMV on the sliced ELLPACK copy with its fused dot products:
+// WHICH 0: out = v = A phat, <rhat, v> (dv = rhat); WHICH 1: out = t =
+// A shat, <t, t>, <t, s> (dv = s).  A row's products are summed in its
+// entry order, as row_dot_sell.
+template <int WHICH>
+__global__ void __launch_bounds__(kTileN)
+k_spmv_tma(SolverDev d, const double *__restrict__ xin,
+           double *__restrict__ out, const double *__restrict__ dv,
+           KScalars *sc, RedWork w) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  __shared__ __align__(8) uint64_t bar[kSpmvStages];
+  pdl_wait();
+  if (sc->done) return;
+  const int tid = threadIdx.x, G = gridDim.x, blk = blockIdx.x;
+  const int n = d.n, W = d.sell_w, ns = (n + 31) >> 5;
+  const int n_tiles = (n + kTileN - 1) / kTileN;
+  const int m = blk < n_tiles ? (n_tiles - 1 - blk) / G + 1 : 0;
+  const size_t stage = sell_stage_bytes(W, 1);
+  const void *const vsrc[1] = {dv};
+  // entry range [a, b) of the k-th tile (thread 0, for the issue)
+  auto range = [&](int k, int &a, int &b) {
+    const int s0 = 8 * (blk + k * G);
+    a = __ldg(d.sell_ptr + s0);
+    b = __ldg(d.sell_ptr + (s0 + 8 < ns ? s0 + 8 : ns));
+  };
+  // this thread's slice of the k-th tile: the tile's first entry and the
+  // slice's entry range
+  auto slice_of = [&](int k, int &ta, int &lo, int &hi) {
+    const int j = blk + k * G;
+    const int i = j * kTileN + tid;
+    ta = lo = hi = 0;
+    if (i < n) {
+      ta = __ldg(d.sell_ptr + 8 * j);
+      lo = __ldg(d.sell_ptr + (i >> 5));
+      hi = __ldg(d.sell_ptr + (i >> 5) + 1);
+    }
+  };
+  if (tid == 0) {
+    for (int b = 0; b < kSpmvStages; ++b) mbar_init(&bar[b], 1);
+    for (int k = 0; k < kSpmvStages && k < m; ++k) {
+      int a, b;
+      range(k, a, b);
+      issue_sell_tile<1>(smem + k * stage, W, d.sell_val, d.sell_col, a, b,
+                         vsrc, n, blk + k * G, &bar[k]);
+    }
+  }
+  int ta = 0, lo = 0, hi = 0;
+  if (m > 0) slice_of(0, ta, lo, hi);
+  __syncthreads();
+  double acc[2] = {0., 0.};
+  int k = 0;
+  bool failed = false;
+  for (; k < m; ++k) {
+    const int b = k % kSpmvStages;
+    // loads for the next issue and the next tile, in flight during this one
+    int na = 0, nb = 0;
+    if (tid == 0 && k + kSpmvStages < m) range(k + kSpmvStages, na, nb);
+    const int cta = ta, clo = lo, chi = hi;
+    if (k + 1 < m) slice_of(k + 1, ta, lo, hi);
+    const bool ok = mbar_wait_bounded(&bar[b], w.err, (uint32_t)((k / kSpmvStages) & 1));
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    const int j = blk + k * G;
+    const int i = j * kTileN + tid;
+    if (i < n) {
+      const uint8_t *stg = smem + b * stage;
+      const double *vals = reinterpret_cast<const double *>(stg);
+      const int32_t *cols = reinterpret_cast<const int32_t *>(stg + (size_t)kTileN * W * 8);
+      const double *dvec = reinterpret_cast<const double *>(stg + (size_t)kTileN * W * 12);
+      const int o = clo - cta + (tid & 31), wq = (chi - clo) >> 5;
+      double a = 0.;
+      if (wq <= 8) {
+        int32_t cc[8];
+        double xv[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) cc[q] = q < wq ? cols[o + 32 * q] : 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) xv[q] = q < wq ? __ldg(xin + cc[q]) : 0.;
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (q < wq) a += vals[o + 32 * q] * xv[q];
+      } else {
+        for (int q = 0; q < wq; ++q) a += vals[o + 32 * q] * __ldg(xin + cols[o + 32 * q]);
+      }
+      out[i] = a;
+      const double dvi = tid < tile_bulk_count(n, j) ? dvec[tid] : dv[i];
+      if (WHICH == 0) {
+        acc[0] += dvi * a;
+      } else {
+        acc[0] += a * a;
+        acc[1] += a * dvi;
       }
     }
+    __syncthreads();  // stage b is free
+    if (tid == 0 && k + kSpmvStages < m) {
+      fence_proxy_async();
+      issue_sell_tile<1>(smem + b * stage, W, d.sell_val, d.sell_col, na, nb,
+                         vsrc, n, blk + (k + kSpmvStages) * G, &bar[b]);
+    }
+  }
+  if (failed && tid == 0)
+    for (int k2 = k + 1; k2 < m && k2 < k + kSpmvStages; ++k2)
+      mbar_wait_bounded(&bar[k2 % kSpmvStages], nullptr, (uint32_t)((k2 / kSpmvStages) & 1));
+  if (WHICH == 0) {
+    double a1[1] = {acc[0]}, tot[1];
+    if (grid_reduce<1>(a1, w, tot) && threadIdx.x == 0) spmv_v_scalars(sc, tot[0]);
+  } else {
+    double tot[2];
+    if (grid_reduce<2>(acc, w, tot) && threadIdx.x == 0) spmv_t_scalars(sc, tot);
   }
 }
 
@@ -836,15 +1040,48 @@ void launch_unpermute_vec(int n, const int32_t *perm, const double *src,
   count_launches(1);
 }
 
+// The streamed SpMV when the sliced copy is there, narrow enough and the
+// vectors are 16-byte aligned (PG_STREAM=0 keeps the thread-per-row forms)
+bool stream_enabled() {
+  static const bool on = [] {
+    const char *e = std::getenv("PG_STREAM");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+template <int WHICH>
+bool launch_spmv_tma(const SolverDev &d, const double *xin, double *out,
+                     const double *dv, KScalars *sc, RedWork w, cudaStream_t st) {
+  if (!stream_enabled() || !d.sell_val || d.sell_w < 1 || d.sell_w > kSellMaxW ||
+      !aligned16(dv) || !aligned16(d.sell_val) || !aligned16(d.sell_col) || d.n < 1)
+    return false;
+  const size_t smem = kSpmvStages * sell_stage_bytes(d.sell_w, 1);
+  static size_t attr = 0;
+  if (attr < smem) {
+    cudaFuncSetAttribute(k_spmv_tma<WHICH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    attr = smem;
+  }
+  const int g = stream_grid((const void *)k_spmv_tma<WHICH>, smem,
+                            (d.n + kTileN - 1) / kTileN, w.grid);
+  launch_pdl(k_spmv_tma<WHICH>, g, kTileN, smem, st, d, xin, out, dv, sc, w);
+  count_launches(1);
+  return true;
+}
+
 template <class VT, class MT>
 void launch_spmv_v(const SolverDev &d, const MT *val, const VT *ph, VT *v,
                    const VT *rh, KScalars *sc, RedWork w, cudaStream_t st) {
+  if constexpr (std::is_same<VT, double>::value && std::is_same<MT, double>::value)
+    if (launch_spmv_tma<0>(d, ph, v, rh, sc, w, st)) return;
   launch_pdl(k_spmv_v<VT, MT>, w.grid, kVecBlock, 0, st, d, val, ph, v, rh, sc, w);
   count_launches(1);
 }
 template <class VT, class MT>
 void launch_spmv_t(const SolverDev &d, const MT *val, const VT *sh, VT *t,
                    const VT *s, KScalars *sc, RedWork w, cudaStream_t st) {
+  if constexpr (std::is_same<VT, double>::value && std::is_same<MT, double>::value)
+    if (launch_spmv_tma<1>(d, sh, t, s, sc, w, st)) return;
   launch_pdl(k_spmv_t<VT, MT>, w.grid, kVecBlock, 0, st, d, val, sh, t, s, sc, w);
   count_launches(1);
 }
@@ -852,6 +1089,24 @@ template <class VT>
 void launch_update(int n, VT *x, VT *r, const VT *ph, const VT *sh,
                    const VT *s, const VT *t, const VT *rh, KScalars *sc,
                    RedWork w, cudaStream_t st) {
+  if constexpr (std::is_same<VT, double>::value) {
+    if (stream_enabled() && n > 0 && aligned16(x) && aligned16(r) &&
+        aligned16(ph) && aligned16(sh) && aligned16(s) && aligned16(t) &&
+        aligned16(rh)) {
+      constexpr size_t smem = kUpdStages * 6 * kTileN * 8;
+      static bool attr = false;
+      if (!attr) {
+        cudaFuncSetAttribute(k_update_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        attr = true;
+      }
+      const int g = stream_grid((const void *)k_update_tma, smem,
+                                (n + kTileN - 1) / kTileN, w.grid);
+      launch_pdl(k_update_tma, g, kTileN, smem, st, n, x, r, ph, sh, s, t, rh, sc, w);
+      count_launches(1);
+      return;
+    }
+  }
   launch_pdl(k_update<VT>, w.grid, kVecBlock, 0, st, n, x, r, ph, sh, s, t, rh, sc, w);
   count_launches(1);
 }

@@ -17,9 +17,12 @@ uint64_t launch_count();
 // scheduled while the previous kernel of its stream is finishing (captured
 // CUDA graphs keep this as a programmatic edge): it calls pdl_wait() before
 // touching anything that kernel writes (the wait returns once that grid
-// has completed and its writes are visible; at once without PDL), and
-// pdl_trigger() so the next kernel may be scheduled in turn.  PG_PDL=0 in
-// the environment launches them in plain stream order.
+// has completed and its writes are visible; at once without PDL).  The
+// kernels leave the trigger for the next launch implicit (at exit): an
+// explicit pdl_trigger() at a kernel's start measured 12 % slower solves on
+// the 1M-row bubble, the next grid's waiting CTAs taking SM resources from
+// the running one.  PG_PDL=0 in the environment launches them in plain
+// stream order.
 __device__ __forceinline__ void pdl_wait() {
   asm volatile("griddepcontrol.wait;" ::: "memory");
 }
@@ -27,6 +30,9 @@ __device__ __forceinline__ void pdl_trigger() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 bool pdl_enabled();
+// streamed (bulk-copy) forms of the SpMVs and the x / r update
+// (PG_STREAM=0 in the environment keeps the thread-per-row forms)
+bool stream_enabled();
 template <typename... KArgs, typename... Args>
 inline void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block,
                        size_t smem, cudaStream_t st, Args... args) {
@@ -71,7 +77,8 @@ constexpr int kMaxDots = 3;      // fused dot products per kernel
 struct RedWork {
   double *partials;      // [kMaxDots][grid]
   unsigned int *ticket;  // one counter
-  int grid;
+  int grid;              // at least the grid of every kernel that reduces
+  int *err = nullptr;    // set when a bounded device wait runs out
 };
 
 // ---- assembly / field kernels (FP64, reference arithmetic) ----
@@ -238,12 +245,12 @@ struct SolverDev {
   int n, nnz, n_sub;
   // permuted CSR
   const int32_t *prp, *pci;
-  // its sliced ELLPACK copy for the SpMVs (32-row slices, column-major;
-  // sell_val refreshed with the values, sell_val_dd their float pairs for
-  // the mixed solver; NULL: the CSR is used)
+  // its sliced ELLPACK copy for the FP64 SpMVs (32-row slices,
+  // column-major; sell_val refreshed with the values; NULL: the CSR is
+  // used)
   const int32_t *sell_ptr = nullptr, *sell_col = nullptr;
   const double *sell_val = nullptr;
-  const float2 *sell_val_dd = nullptr;
+  int sell_w = 0;  // widest slice (entries per row)
   // ILU(0) records (FP64)
   const SubMeta *meta64;
   uint8_t *rec64;

@@ -58,8 +58,8 @@ struct pg_solver {
   // sliced ELLPACK copy of the matrix for the FP64 SpMVs (PG_FP64 solvers)
   DevBuf<int32_t> sell_ptr, sell_col, sell_src;
   DevBuf<double> sell_val;
-  DevBuf<float2> sell_val_dd;  // PG_MIXED: float pairs of sell_val
   bool sell_on = false;
+  int sell_w = 0;  // widest slice
   DevBuf<SubMeta> meta64;
   DevBuf<uint8_t> rec64;
   DevBuf<StreamMeta> smeta64;
@@ -246,7 +246,7 @@ struct pg_solver {
       d.sell_ptr = sell_ptr.p;
       d.sell_col = sell_col.p;
       d.sell_val = sell_val.p;
-      d.sell_val_dd = sell_val_dd.p;
+      d.sell_w = sell_w;
     }
     d.meta64 = meta64.p;
     d.rec64 = rec64.p;
@@ -297,7 +297,7 @@ struct pg_solver {
     d.n_lpack32 = line32 ? (int)a.lpack32_src.size() : 0;
     return d;
   }
-  RedWork red() const { return RedWork{partials.p, ticket.p, red_grid}; }
+  RedWork red() const { return RedWork{partials.p, ticket.p, red_grid, err.p}; }
 };
 
 namespace {
@@ -356,15 +356,16 @@ int upload_analysis(pg_solver *s) {
   up(s->perm, a.perm);
   up(s->prp, a.prp);
   up(s->pci, a.pci);
-  s->sell_on = (s->cfg.precision == PG_FP64 || s->cfg.precision == PG_MIXED) &&
-               !s->batch_mode && !a.sell_ptr.empty();
+  s->sell_on = s->cfg.precision == PG_FP64 && !s->batch_mode &&
+               !a.sell_ptr.empty();
   if (s->sell_on) {
     up(s->sell_ptr, a.sell_ptr);
     up(s->sell_col, a.sell_col);
     up(s->sell_src, a.sell_src);
     if (e == cudaSuccess) e = s->sell_val.reserve(a.sell_col.size());
-    if (e == cudaSuccess && s->cfg.precision == PG_MIXED)
-      e = s->sell_val_dd.reserve(a.sell_col.size());
+    s->sell_w = 0;
+    for (size_t sl = 0; sl + 1 < a.sell_ptr.size(); ++sl)
+      s->sell_w = std::max<int>(s->sell_w, (a.sell_ptr[sl + 1] - a.sell_ptr[sl]) / 32);
   }
   up(s->psrc, a.psrc);
   up(s->dup_dst, a.dup_dst);
@@ -1285,9 +1286,6 @@ int factor(pg_solver *s, cudaStream_t st) {
     if (dd) launch_dd_split(d.n, s->jdinv.p, 1.0, s->jdinv_dd.p, st);
   }
   if (dd) launch_dd_split(d.nnz, s->pvals.p, 1.0, s->pvals_dd.p, st);
-  if (dd && s->sell_on && s->sell_val_dd.p)
-    launch_dd_split((int64_t)s->a.sell_col.size(), s->sell_val.p, 1.0,
-                    s->sell_val_dd.p, st);
   PG_CUDA(cudaGetLastError());
   if (dd && s->cfg.precond == PG_PREC_ILU0 && s->dd_stream < 0)
     return choose_dd_sweep(s);  // library stream only (see start_factor)
