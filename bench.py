@@ -308,9 +308,12 @@ def kernel_roofline(pg, solver, n, nnz, dd, eqn=None, coarse=0, in_solve=None):
     b_spmv = 12 * nnz + 4 * (n + 1) + 3 * 8 * n          # A, x, rhat in; v out
     # factor weights (8 B, or 4 B for the mixed solver's FP32-stored factor;
     # the stream form adds a 2-byte column each, the line form's columns are
-    # implicit), 1/u_ii, r p v in, p z out
+    # implicit), 1/u_ii, and the vectors: r p v in, p z out when the sweep
+    # fuses the Krylov update; with the deflated coarse correction the
+    # deflation stage does that and the sweep reads p - A Z y and writes z
     wb = 4 if (dd and form == 1 and solver.cfg.mixed_sweep == 3) else 8
-    b_prec = (wb if form == 1 else wb + 2) * off_in + wb * n + 5 * 8 * n
+    vec_prec = 2 * 8 * n if coarse == 2 else 5 * 8 * n
+    b_prec = (wb if form == 1 else wb + 2) * off_in + wb * n + vec_prec
     b_upd = 9 * 8 * n                                    # x r ph sh s t rh in; x r out
     sfx = "_dd" if dd else ""
     ms_of = {"spmv": prof["spmv" + sfx], "ilu_apply": prof["precond" + sfx],
