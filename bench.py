@@ -101,7 +101,8 @@ def parse():
                     help="sequence mode: leave out the cylinder and batched "
                          "summaries")
     ap.add_argument("--mode", default="sequence",
-                    choices=["sequence", "single", "batch", "direct"])
+                    choices=["sequence", "single", "batch", "direct",
+                             "cylinder"])
     ap.add_argument("--systems", type=int, default=256,
                     help="batch mode: number of immersed-boundary systems")
     ap.add_argument("--t0", type=int, default=1801,
@@ -1287,13 +1288,24 @@ def run_direct(args):
     print(json.dumps({"direct": direct_summary(pg, args, nx_list=(args.nx,))}))
 
 
+def run_cylinder(args):
+    """--mode cylinder: the cylinder-channel pCorr system alone (the summary
+    of the default line), for profiling."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import phase_gb300 as pg
+    print(json.dumps({"cylinder": cylinder_summary(pg, torch, args)}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     else:
         {"sequence": run_sequence, "single": run_single,
-         "batch": run_batch, "direct": run_direct}[args.mode](args)
+         "batch": run_batch, "direct": run_direct,
+         "cylinder": run_cylinder}[args.mode](args)
 
 
 if __name__ == "__main__":
