@@ -74,3 +74,13 @@ def test_header_is_c99_and_links_from_c(built, tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "max_iters 500" in r.stdout
+
+
+def test_kernel_trace_entry_points_check_arguments(built):
+    # argument checks come before any CUDA call: no GPU needed
+    lib = built.lib()
+    assert lib.pg_solver_trace_kernels(None, 1) == built.PG_BAD_ARG
+    ms = np.zeros(4)
+    cnt = np.zeros(4, np.int64)
+    assert lib.pg_solver_kernel_times(None, ms.ctypes.data, cnt.ctypes.data,
+                                      None) == built.PG_BAD_ARG
