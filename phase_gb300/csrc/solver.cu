@@ -130,7 +130,7 @@ struct pg_solver {
   // coarse matrix / its inverse, elimination buffers, subdomain sums and the
   // graph of the K elimination steps
   bool coarse_on = false;
-  bool coarse_use = true;   // the drivers apply the coarse correction
+  bool coarse_use = true;   // the Krylov drivers apply the coarse correction
   bool batch_mode = false;  // inner solver of a pg_batch (its own coarse space)
   // the coarse matrix and its inverse are built on side2 beside the first
   // (one-level) iterations; ev_coarse marks them done
@@ -158,7 +158,7 @@ struct pg_solver {
   // current
   DevBuf<float> c_ac2;
   cudaGraphExec_t gj_graph2 = nullptr;
-  int ac_ready = 0;      // the buffer the drivers apply
+  int ac_ready = 0;      // the buffer the Krylov drivers apply
   int ac_next = -1;      // the buffer being inverted on side2 (-1: none)
   bool ac_valid = false; // ac_ready holds an inverse for this analysis
   float *ac_buf(int b) const { return b ? c_ac2.p : c_ac.p; }
